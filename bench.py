@@ -1,0 +1,346 @@
+"""Benchmark of the GB300 monodomain time step.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Workload: ORd (tissue myocyte) on the 20 x 7 x 3 mm slab at h = 0.1 mm
+(200 x 70 x 30 = 420,000 cells), dt = 5 us, implicit backward-Euler/BDF2
+diffusion with PCG (tol 1e-8), corner box stimulus 5e4 A/m^3 for 2 ms,
+Vm0 = -84 mV, starting at t = 0.  Synthetic (the reference publishes no
+dataset for this path).  A step is one runTime++/evolve over all cells.
+
+The headline `value` is the mixed-precision form's device-resident
+throughput in cell-steps/s; the FP64 plain form is timed on the same
+workload and the activation-time difference between the two runs is
+reported.  `e2e` repeats the mixed run through the C ABI with Vm copied in
+from and out to pinned host memory every step.  Under torchrun every rank
+runs an independent replica on its own GPU (the step has no cross-rank
+exchange at one GPU per replica).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "monodomain cell-steps/s, mixed vs FP64 on GB300 at ≤0.05 ms activation error"
+SIGMA = (0.1334, 0.0, 0.0, 0.0176, 0.0, 0.0176)
+BOX = [((0.0, 0.0, 0.0), (1.5e-3, 1.5e-3, 1.5e-3), 0.0, 2e-3, 5e4)]
+WORKLOAD = ("ORd myocyte monodomain slab 20x7x3 mm, h=0.1 mm (200x70x30 = 420000 cells), "
+            "dt=5e-6 s, implicit (backward ddt, PIMPLE residualControl 1e-6, PCG tol 1e-8), "
+            "corner stimulus 5e4 A/m^3 x 2 ms, from t=0")
+DIMS = (200, 70, 30)
+H = 1e-4
+DT = 5e-6
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return d, "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "sm_max_mhz": 2070.0}, "fallback"
+
+
+def opcounts():
+    return json.loads((ROOT / "cardiacfoam_gb300/csrc/models/opcounts.json").read_text())
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    def __init__(self, index: int):
+        self.proc = None
+        self.path = ROOT / "gpurun_out" / f"clocks_{os.getpid()}.csv"
+        self.index = index
+
+    def __enter__(self):
+        try:
+            self.path.parent.mkdir(exist_ok=True)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}",
+                 "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,"
+                 "clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+                 "clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.fh, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait()
+            self.fh.close()
+
+    def summary(self):
+        if not self.proc or not self.path.exists():
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        rows = [r.split(", ") for r in self.path.read_text().strip().splitlines() if r]
+        sm = [float(r[1]) for r in rows if len(r) >= 9 and r[1].strip().isdigit()]
+        mx = [float(r[2]) for r in rows if len(r) >= 9 and r[2].strip().isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows if len(r) >= 9
+                          for i in range(4) if r[5 + i].strip() == "Active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(sm)}
+
+
+def build_mesh():
+    from cardiacfoam_gb300.mesh import box_mesh
+    nx, ny, nz = DIMS
+    return box_mesh(nx, ny, nz, nx * H, ny * H, nz * H)
+
+
+def make_model(mesh, precision):
+    from cardiacfoam_gb300 import api
+    return api.Monodomain(mesh, "ORd", "myocyte", SIGMA, dt=DT, precision=precision, boxes=BOX,
+                          max_steps=10 ** 6)
+
+
+def timed_steps(md, k, flush):
+    """Run k steps, timing each with CUDA events on the context's stream;
+    L2 is flushed (256 MB write on another stream) between steps."""
+    import torch
+    stream = torch.cuda.ExternalStream(md.stream())
+    total = 0.0
+    for _ in range(k):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        md.step(DT)
+        e1.record(stream)
+        e1.synchronize()
+        total += e0.elapsed_time(e1)
+        flush.zero_()
+        torch.cuda.synchronize()
+    return total / 1e3
+
+
+def gpu_arm(args, rank, world):
+    import torch
+    from cardiacfoam_gb300 import build as gpu_build, lib
+    if rank == 0 or not (ROOT / "cardiacfoam_gb300/libcardiac_gpu.so").exists():
+        gpu_build.build()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.set_device(rank % max(torch.cuda.device_count(), 1))
+    dev = torch.cuda.current_device()
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")   # 256 MB > L2
+    mesh = build_mesh()
+    n = mesh.n_cells
+
+    # ---------------- mixed form (headline)
+    mixed = make_model(mesh, lib.PRECISION_MIXED)
+    for _ in range(args.warmup):
+        mixed.step(DT)
+    mixed.set_timing(True)
+    evals0 = mixed.rhs_evaluations()
+    if world > 1:
+        torch.distributed.barrier()
+    with ClockSampler(dev) as clk:
+        t_mixed = timed_steps(mixed, args.steps, flush)
+    if world > 1:
+        tt = torch.tensor([t_mixed], device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_mixed = float(tt.item())
+    ionic_ms, diff_ms, nsteps, launches = mixed.timings()
+    evals = mixed.rhs_evaluations() - evals0
+    act_mixed = mixed.activation()
+    clocks = clk.summary()
+
+    # ---------------- FP64 plain form on the same workload
+    k64 = max(1, min(args.steps, args.fp64_steps))
+    fp64 = make_model(mesh, lib.PRECISION_FP64)
+    for _ in range(args.warmup):
+        fp64.step(DT)
+    fp64.set_timing(True)
+    t_fp64 = timed_steps(fp64, k64, flush)
+    ionic64_ms, diff64_ms, _, _ = fp64.timings()
+    # activation-time difference over the cells both runs activated in the
+    # common simulated window
+    common = args.warmup + k64
+    mixed_b = make_model(mesh, lib.PRECISION_MIXED)
+    for _ in range(common):
+        mixed_b.step(DT)
+    a64, amx = fp64.activation(), mixed_b.activation()
+    both = (a64 > 0) & (amx > 0)
+    act_err_ms = float(np.max(np.abs(a64[both] - amx[both])) * 1e3) if both.any() else None
+    mismatch = int(np.sum((a64 > 0) != (amx > 0)))
+    del mixed_b
+
+    # ---------------- end to end through the C ABI with host copies
+    pin_in = torch.empty(n, dtype=torch.float64, pin_memory=True)
+    pin_out = torch.empty(n, dtype=torch.float64, pin_memory=True)
+    ke2e = max(1, min(args.steps, args.e2e_steps))
+    vm_host = pin_in.numpy()
+    vm_host[:] = mixed.vm()
+    vm_out = pin_out.numpy()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(ke2e):
+        mixed.set_field(lib.FIELD_VM, vm_host)
+        mixed.step(DT)
+        vm_out[:] = 0.0
+        from cardiacfoam_gb300 import lib as L
+        L.check(mixed._lib.cfg_monodomain_get_field(mixed.h, L.FIELD_VM, L.dptr(vm_out)))
+        vm_host, vm_out = vm_out, vm_host
+    t_e2e = time.perf_counter() - t0
+
+    # ---------------- roofline of the dominant kernel (ionic, mixed form)
+    pk, src = peaks()
+    ops = opcounts()["ORd"]
+    sm_mhz = pk.get("sm_max_mhz", 2070.0)
+    fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12        # TFLOP/s, FP32 FMA pipe
+    ionic_s = ionic_ms / 1e3
+    achieved = evals * (ops["flops"] + ops["transcendental"]) / ionic_s / 1e12
+    nnz = 2 * mesh.n_faces
+    return dict(n=n, t_mixed=t_mixed, t_fp64=t_fp64, k64=k64, ionic_ms=ionic_ms,
+                diff_ms=diff_ms, ionic64_ms=ionic64_ms, diff64_ms=diff64_ms, evals=evals,
+                launches=launches, clocks=clocks, act_err_ms=act_err_ms, act_mismatch=mismatch,
+                act_cells=int(both.sum()), t_e2e=t_e2e, ke2e=ke2e, achieved=achieved,
+                fp32_peak=fp32_peak, peaks=pk, peak_src=src, nnz=nnz,
+                n_active_mixed=int((act_mixed > 0).sum()))
+
+
+def cpu_baseline(nthreads=None, cells_x=40, steps=10):
+    """The oracle (restated reference numerics) on a bounded sample of the
+    workload: a 4 x 7 x 3 mm piece of the slab (40 x 70 x 30 cells) for a few
+    steps with OpenMP over the host's cores."""
+    from oracle import pyoracle as po
+    nthreads = nthreads or os.cpu_count() or 1
+    nx, ny, nz = cells_x, DIMS[1], DIMS[2]
+    mesh = po.Mesh(nx, ny, nz, nx * H, ny * H, nz * H)
+    d = po.tissue_desc("ORd", 4, SIGMA, implicit=True, precond_dic=True, pcg_tol=1e-8,
+                       boxes=BOX, ode=po.ode_settings(max_steps=10 ** 6))
+    T = po.Tissue(d, mesh)
+    T.step(DT, nthreads)           # first step outside the timing (allocation)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        T.step(DT, nthreads)
+    el = time.perf_counter() - t0
+    n = nx * ny * nz
+    return {"value": n * steps / el, "unit": "cell-steps/s", "cores": nthreads, "kind": "port",
+            "sample": f"CPU oracle (reference ionic code + restated OpenFOAM numerics, DIC-PCG) "
+                      f"on {nx}x{ny}x{nz} = {n} cells of the slab, {steps} steps after 1 "
+                      f"untimed step, {nthreads} threads"}
+
+
+def reference_arm(args, rank, world):
+    if rank != 0:
+        return None
+    from oracle import build as ob
+    ob.build()
+    from oracle import pyoracle as po
+    nthreads = os.cpu_count() or 1
+    nx, ny, nz = DIMS
+    mesh = po.Mesh(nx, ny, nz, nx * H, ny * H, nz * H)
+    d = po.tissue_desc("ORd", 4, SIGMA, implicit=True, precond_dic=True, pcg_tol=1e-8,
+                       boxes=BOX, ode=po.ode_settings(max_steps=10 ** 6))
+    T = po.Tissue(d, mesh)
+    k = max(1, min(args.steps, args.ref_steps))
+    for _ in range(min(args.warmup, 1)):
+        T.step(DT, nthreads)
+    t0 = time.perf_counter()
+    for _ in range(k):
+        T.step(DT, nthreads)
+    el = time.perf_counter() - t0
+    value = mesh.n * k / el
+    sample = (f"CPU oracle (reference ionic code + restated OpenFOAM numerics, DIC-PCG) on the "
+              f"full 420000-cell slab, {k} timed steps, {nthreads} threads")
+    return {"metric": METRIC, "impl": "reference", "value": value, "unit": "cell-steps/s",
+            "n_gpus": world, "steps": k, "warmup": min(args.warmup, 1),
+            "ms_per_step": el / k * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "cells": mesh.n, "precision": "fp64",
+                       "parallelism": "host threads"},
+            "cpu_baseline": {"value": value, "unit": "cell-steps/s", "cores": nthreads,
+                             "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": "cell-steps/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=60)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--fp64-steps", type=int, default=12)
+    ap.add_argument("--e2e-steps", type=int, default=20)
+    ap.add_argument("--ref-steps", type=int, default=10)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "gb300":
+        args.warmup = 3
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if world > 1:
+        import torch
+        backend = "nccl" if args.impl == "gb300" else "gloo"
+        torch.distributed.init_process_group(backend)
+    if args.impl == "reference":
+        out = reference_arm(args, rank, world)
+        if out is not None:
+            print(json.dumps(out), flush=True)
+        return
+    r = gpu_arm(args, rank, world)
+    if rank != 0:
+        return
+    n = r["n"]
+    value = n * args.steps * world / r["t_mixed"]
+    fp64_value = n * r["k64"] / r["t_fp64"]
+    e2e_value = n * r["ke2e"] / r["t_e2e"]
+    ionic_s = r["ionic_ms"] / 1e3
+    out = {
+        "metric": METRIC, "value": value, "unit": "cell-steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": r["t_mixed"] / args.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64 (mixed)",
+        "data": "synthetic (seeded geometry/stimulus of the ORd slab configuration)",
+        "config": {"workload": WORKLOAD, "cells": n, "dt_s": DT, "precision": "mixed",
+                   "l2": "flushed (256 MB write) between timed steps",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "fp64": {"value": fp64_value, "unit": "cell-steps/s", "steps": r["k64"],
+                 "ms_per_step": r["t_fp64"] / r["k64"] * 1e3,
+                 "ionic_ms_per_step": r["ionic64_ms"] / r["k64"],
+                 "diffusion_ms_per_step": r["diff64_ms"] / r["k64"]},
+        "speedup_vs_fp64": value / world / fp64_value,
+        "activation_error_ms": r["act_err_ms"], "activation_cells_compared": r["act_cells"],
+        "activation_flag_mismatches": r["act_mismatch"],
+        "phases_ms_per_step": {"ionic": r["ionic_ms"] / args.steps,
+                               "diffusion": r["diff_ms"] / args.steps},
+        "e2e": {"value": e2e_value, "unit": "cell-steps/s", "h2d_bytes_per_step": 8 * n,
+                "d2h_bytes_per_step": 8 * n, "steps": r["ke2e"],
+                "path": "cfg_monodomain_set_field(Vm) + cfg_monodomain_step + "
+                        "cfg_monodomain_get_field(Vm), pinned host buffers"},
+        "roofline": {"bound": "fp32", "kernel": "ionic_step_kernel<ORd, mixed>",
+                     "achieved": r["achieved"], "peak": r["fp32_peak"], "unit": "TFLOP/s",
+                     "frac": r["achieved"] / r["fp32_peak"], "traffic": None,
+                     "work": f"{r['evals']} RHS evaluations x "
+                             f"{opcounts()['ORd']['flops']:.0f} FLOP + "
+                             f"{opcounts()['ORd']['transcendental']:.0f} transcendental",
+                     "peak_source": f"152 SMs x 128 FP32 lanes x 2 x {r['peaks'].get('sm_max_mhz')} "
+                                    f"MHz (MEASURED_PEAKS.json sm_max_mhz, {r['peak_src']}); "
+                                    "no FP32 figure is measured"},
+        "gpu_launches": r["launches"],
+        "clocks": r["clocks"],
+    }
+    if not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline()
+    print(json.dumps(out), flush=True)
+
+
+if __name__ == "__main__":
+    main()

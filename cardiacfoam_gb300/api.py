@@ -1,0 +1,262 @@
+"""Python view of the C ABI, shaped like the reference's plugin interfaces.
+
+``IonicModel`` mirrors ``ionicModel::New(dict, nIntegrationPoints,
+initialDeltaT, solveVmWithinODESolver)`` and ``solveODE(t0, dt, Vm, Im)``
+(src/ionicModels/ionicModel/ionicModel.H:184-256); ``Monodomain`` mirrors a
+MyocardiumDomain driven by MonodomainSolver (myocardiumDomain.C:180-529).
+Both hold GPU-resident state; host arrays cross the boundary only in the
+calls that take or return them.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import lib as _L
+from .mesh import LduMesh
+
+TISSUE_FLAGS = {"epicardialCells": 1, "mCells": 2, "endocardialCells": 3, "myocyte": 4}
+
+
+def ode_desc(solver="RKF45", abs_tol=-1.0, rel_tol=-1.0, max_steps=-1) -> _L.OdeDesc:
+    d = _L.OdeDesc()
+    d.solver = solver.encode() if solver else None
+    d.abs_tol, d.rel_tol, d.max_steps = abs_tol, rel_tol, max_steps
+    d.safe_scale = d.min_scale = d.max_scale = d.alpha_increase = d.alpha_decrease = -1.0
+    return d
+
+
+def stimulus_desc(stim_start=0.0, stim_period_s1=0.0, stim_duration=0.0, stim_amplitude=0.0,
+                  nstim1=0, stim_period_s2=0.0, nstim2=0) -> _L.StimulusDesc:
+    return _L.StimulusDesc(stim_start, stim_period_s1, stim_duration, stim_amplitude, nstim1,
+                           stim_period_s2, nstim2)
+
+
+def ionic_desc(model: str, tissue: str, n_cells: int, initial_delta_t: float,
+               solve_vm_within_ode: bool = False, precision: int = _L.PRECISION_FP64,
+               ode: Optional[_L.OdeDesc] = None, stimulus: Optional[_L.StimulusDesc] = None,
+               tissue_per_cell: Optional[np.ndarray] = None,
+               scales: Optional[np.ndarray] = None, _keep: Optional[list] = None) -> _L.IonicDesc:
+    d = _L.IonicDesc()
+    d.ionic_model = model.encode()
+    d.tissue = tissue.encode() if tissue else None
+    d.n_cells = n_cells
+    d.initial_delta_t = initial_delta_t
+    d.solve_vm_within_ode = int(solve_vm_within_ode)
+    d.precision = precision
+    d.ode = ode if ode is not None else ode_desc()
+    d.stimulus = stimulus if stimulus is not None else stimulus_desc()
+    if tissue_per_cell is not None:
+        t = np.ascontiguousarray(tissue_per_cell, dtype=np.uint8)
+        d.tissue_per_cell = _L.uptr(t)
+        if _keep is not None:
+            _keep.append(t)
+    if scales is not None:
+        s = np.ascontiguousarray(scales, dtype=np.float64)
+        d.scales = _L.dptr(s)
+        if _keep is not None:
+            _keep.append(s)
+    return d
+
+
+class IonicModel:
+    """ionicModel::New + solveODE on the GPU."""
+
+    def __init__(self, model: str, tissue: str, n_cells: int, initial_delta_t: float,
+                 solve_vm_within_ode: bool = False, precision: int = _L.PRECISION_FP64,
+                 ode: Optional[_L.OdeDesc] = None, stimulus: Optional[_L.StimulusDesc] = None,
+                 tissue_per_cell=None, scales=None):
+        self._lib = _L.load()
+        keep: list = []
+        d = ionic_desc(model, tissue, n_cells, initial_delta_t, solve_vm_within_ode, precision,
+                       ode, stimulus, tissue_per_cell, scales, keep)
+        h = C.c_void_p()
+        _L.check(self._lib.cfg_ionic_create(C.byref(d), C.byref(h)))
+        self.h = h
+        self.n = n_cells
+        ns = C.c_int()
+        _L.check(self._lib.cfg_ionic_num_states(self.h, C.byref(ns)))
+        self.n_states = ns.value
+
+    def solveODE(self, t0: float, dt: float, vm: Optional[np.ndarray], im: np.ndarray):
+        vm_p = _L.dptr(vm) if vm is not None else None
+        _L.check(self._lib.cfg_ionic_solve(self.h, t0, dt, vm_p, _L.dptr(im)))
+
+    def state_names(self):
+        out = []
+        buf = C.create_string_buffer(128)
+        for i in range(self.n_states):
+            _L.check(self._lib.cfg_ionic_state_name(self.h, i, buf, 128))
+            out.append(buf.value.decode())
+        return out
+
+    def states(self) -> np.ndarray:
+        a = np.zeros((self.n_states, self.n))
+        _L.check(self._lib.cfg_ionic_get_states(self.h, _L.dptr(a)))
+        return a
+
+    def set_states(self, a: np.ndarray):
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        _L.check(self._lib.cfg_ionic_set_states(self.h, _L.dptr(a)))
+
+    def steps(self) -> np.ndarray:
+        a = np.zeros(self.n)
+        _L.check(self._lib.cfg_ionic_get_steps(self.h, _L.dptr(a)))
+        return a
+
+    def rhs_evaluations(self) -> int:
+        v = C.c_ulonglong()
+        _L.check(self._lib.cfg_ionic_rhs_evaluations(self.h, C.byref(v)))
+        return v.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            self._lib.cfg_ionic_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+
+def mesh_desc(mesh: LduMesh, face_coeff: Optional[np.ndarray] = None,
+              structured: bool = True) -> tuple:
+    keep = [mesh.owner, mesh.neighbour, mesh.volumes, mesh.centres, mesh.face_sf,
+            mesh.face_delta_coeffs]
+    d = _L.MeshDesc()
+    d.n_cells = mesh.n_cells
+    d.n_faces = mesh.n_faces
+    d.owner = _L.iptr(mesh.owner)
+    d.neighbour = _L.iptr(mesh.neighbour)
+    d.volumes = _L.dptr(mesh.volumes)
+    d.centres = _L.dptr(mesh.centres)
+    d.face_sf = _L.dptr(np.ascontiguousarray(mesh.face_sf))
+    d.face_delta_coeffs = _L.dptr(mesh.face_delta_coeffs)
+    if face_coeff is not None:
+        fc = np.ascontiguousarray(face_coeff, dtype=np.float64)
+        keep.append(fc)
+        d.face_coeff = _L.dptr(fc)
+    if structured:
+        for i in range(3):
+            d.structured[i] = mesh.structured[i]
+    return d, keep
+
+
+class Monodomain:
+    """MyocardiumDomain + MonodomainSolver on the GPU."""
+
+    def __init__(self, mesh: LduMesh, model="TNNP", tissue="epicardialCells",
+                 sigma=(0.1334, 0.0, 0.0, 0.0176, 0.0, 0.0176), chi=140000.0, cm=0.01,
+                 dt=1e-5, precision=_L.PRECISION_FP64, implicit=True, ddt_backward=True,
+                 pcg_tol=1e-8, pcg_rel_tol=0.0, pcg_max_iter=1000, n_outer=1000,
+                 outer_tol=1e-6, vm0=-0.084, boxes: Sequence = (), ode=None,
+                 tissue_per_cell=None, scales=None, stencil=True, max_steps=10 ** 6):
+        self._lib = _L.load()
+        self.mesh = mesh
+        keep: list = []
+        d = _L.MonodomainDesc()
+        d.ionic = ionic_desc(model, tissue, mesh.n_cells, dt, False, precision,
+                             ode if ode is not None else ode_desc(max_steps=max_steps),
+                             None, tissue_per_cell, scales, keep)
+        for i, s in enumerate(sigma):
+            d.conductivity[i] = s
+        d.chi, d.cm = chi, cm
+        d.implicit, d.ddt_backward = int(implicit), int(ddt_backward)
+        d.pcg_tol, d.pcg_rel_tol, d.pcg_max_iter = pcg_tol, pcg_rel_tol, pcg_max_iter
+        d.n_outer, d.outer_tol, d.vm0 = n_outer, outer_tol, vm0
+        d.n_boxes = len(boxes)
+        for b, (lo, hi, t0, dur, inten) in enumerate(boxes):
+            for k in range(3):
+                d.box_min[b][k] = lo[k]
+                d.box_max[b][k] = hi[k]
+            d.box_start[b], d.box_duration[b], d.box_intensity[b] = t0, dur, inten
+        md, keep2 = mesh_desc(mesh, structured=stencil)
+        h = C.c_void_p()
+        _L.check(self._lib.cfg_monodomain_create(C.byref(d), C.byref(md), C.byref(h)))
+        self.h = h
+        self.n = mesh.n_cells
+
+    @classmethod
+    def from_dict(cls, text: str, mesh: LduMesh, dt: float, precision=_L.PRECISION_FP64,
+                  stencil=True):
+        self = cls.__new__(cls)
+        self._lib = _L.load()
+        self.mesh = mesh
+        md, keep = mesh_desc(mesh, structured=stencil)
+        h = C.c_void_p()
+        _L.check(self._lib.cfg_monodomain_create_from_dict(text.encode(), C.byref(md), dt,
+                                                           precision, C.byref(h)))
+        self.h = h
+        self.n = mesh.n_cells
+        return self
+
+    def step(self, dt: float):
+        _L.check(self._lib.cfg_monodomain_step(self.h, dt))
+
+    def run(self, dt: float, n_steps: int):
+        _L.check(self._lib.cfg_monodomain_run(self.h, dt, n_steps))
+
+    def field(self, which: int) -> np.ndarray:
+        a = np.zeros(self.n)
+        _L.check(self._lib.cfg_monodomain_get_field(self.h, which, _L.dptr(a)))
+        return a
+
+    def set_field(self, which: int, a: np.ndarray):
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        _L.check(self._lib.cfg_monodomain_set_field(self.h, which, _L.dptr(a)))
+
+    def vm(self):
+        return self.field(_L.FIELD_VM)
+
+    def iion(self):
+        return self.field(_L.FIELD_IION)
+
+    def activation(self):
+        return self.field(_L.FIELD_ACTIVATION)
+
+    def source(self):
+        return self.field(_L.FIELD_SOURCE)
+
+    def time(self) -> float:
+        return self._lib.cfg_monodomain_time(self.h)
+
+    def stats(self):
+        s = _L.StepStats()
+        _L.check(self._lib.cfg_monodomain_last_stats(self.h, C.byref(s)))
+        k = min(s.n_solves, 16)
+        return (np.array(s.initial_residual[:k]), np.array(s.final_residual[:k]),
+                np.array(s.iterations[:k]))
+
+    def states(self) -> np.ndarray:
+        ion = self._lib.cfg_monodomain_ionic(self.h)
+        ns = C.c_int()
+        _L.check(self._lib.cfg_ionic_num_states(ion, C.byref(ns)))
+        a = np.zeros((ns.value, self.n))
+        _L.check(self._lib.cfg_ionic_get_states(ion, _L.dptr(a)))
+        return a
+
+    def rhs_evaluations(self) -> int:
+        ion = self._lib.cfg_monodomain_ionic(self.h)
+        v = C.c_ulonglong()
+        _L.check(self._lib.cfg_ionic_rhs_evaluations(ion, C.byref(v)))
+        return v.value
+
+    def set_timing(self, enable: bool = True):
+        _L.check(self._lib.cfg_monodomain_set_timing(self.h, int(enable)))
+
+    def timings(self):
+        """(ionic ms, diffusion ms, steps, kernel launches) since set_timing."""
+        a, b, n, k = C.c_double(), C.c_double(), C.c_longlong(), C.c_longlong()
+        _L.check(self._lib.cfg_monodomain_timings(self.h, C.byref(a), C.byref(b), C.byref(n),
+                                                  C.byref(k)))
+        return a.value, b.value, n.value, k.value
+
+    def stream(self) -> int:
+        return self._lib.cfg_monodomain_stream(self.h)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self._lib.cfg_monodomain_destroy(self.h)
+            self.h = None
+
+    __del__ = close

@@ -1,0 +1,100 @@
+"""Build libcardiac_gpu.so in-tree for sm_103a (GB300).
+
+Each ionic model is compiled twice from ``csrc/ionic_instance.cu``: the plain
+form with ``--fmad=false`` (FP64 rounding in the host's evaluation order) and
+the mixed form with FMA contraction.  Translation units are compiled in
+parallel; only changed ones are rebuilt.
+"""
+from __future__ import annotations
+
+import hashlib
+import os
+import shutil
+import subprocess
+from concurrent.futures import ThreadPoolExecutor
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+CSRC = PKG / "csrc"
+BUILD = PKG / "_build"
+LIB = PKG / "libcardiac_gpu.so"
+INCLUDE = PKG.parent / "include"
+
+MODELS = ["tnnp", "ord", "torord_dyncl", "alievpanfilov", "buenoorovio"]
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+COMMON = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
+          "-Xcompiler", "-ffp-contract=off", "-I", str(CSRC), "-I", str(INCLUDE)]
+
+
+def nvcc() -> str:
+    cand = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not Path(cand).exists():
+        raise RuntimeError("nvcc not found; the CUDA toolkit is required to build the library")
+    return cand
+
+
+def _units():
+    units = []
+    for m in MODELS:
+        for prec, flags in (("fp64", ["--fmad=false", "-DCFG_FP64=1"]),
+                            ("mixed", ["--fmad=true", "-DCFG_FP64=0"])):
+            units.append((f"ionic_{m}_{prec}", CSRC / "ionic_instance.cu",
+                          flags + [f"-DCFG_MODEL={m}"]))
+    units.append(("ionic_registry", CSRC / "ionic_registry.cu", []))
+    units.append(("ionic", CSRC / "ionic.cu", []))
+    units.append(("diffusion", CSRC / "diffusion.cu", []))
+    units.append(("monodomain", CSRC / "monodomain.cu", []))
+    units.append(("dictionary", CSRC / "dictionary.cpp", []))
+    return units
+
+
+def _deps_hash(src: Path, flags) -> str:
+    h = hashlib.sha256()
+    h.update(" ".join(ARCH + COMMON + list(flags)).encode())
+    for p in sorted(list(CSRC.rglob("*.cu")) + list(CSRC.rglob("*.cuh")) +
+                    list(CSRC.rglob("*.h")) + list(CSRC.rglob("*.cpp")) +
+                    list(INCLUDE.glob("*.h"))):
+        h.update(p.name.encode())
+        h.update(p.read_bytes())
+    return h.hexdigest()
+
+
+def build(force: bool = False, jobs: int | None = None, verbose: bool = False) -> Path:
+    BUILD.mkdir(exist_ok=True)
+    cc = nvcc()
+    units = _units()
+
+    def compile_unit(u):
+        name, src, flags = u
+        obj = BUILD / f"{name}.o"
+        stamp = BUILD / f"{name}.hash"
+        digest = _deps_hash(src, flags)
+        if not force and obj.exists() and stamp.exists() and stamp.read_text() == digest:
+            return name, False
+        cmd = [cc, *ARCH, *COMMON, *flags, "-c", str(src), "-o", str(obj)]
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"nvcc failed for {name}:\n{r.stderr[-6000:]}")
+        stamp.write_text(digest)
+        return name, True
+
+    jobs = jobs or max(1, min(len(units), os.cpu_count() or 1))
+    with ThreadPoolExecutor(max_workers=jobs) as ex:
+        results = list(ex.map(compile_unit, units))
+    rebuilt = any(r for _, r in results)
+    if rebuilt or force or not LIB.exists():
+        objs = [str(BUILD / f"{n}.o") for n, _, _ in units]
+        tmp = str(LIB) + ".tmp"
+        cmd = [cc, *ARCH, "-shared", "-o", tmp, *objs]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"link failed:\n{r.stderr[-4000:]}")
+        os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    import sys
+    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))

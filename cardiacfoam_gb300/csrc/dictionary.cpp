@@ -1,0 +1,309 @@
+// Reader for the subset of OpenFOAM dictionary syntax used by
+// constant/electroProperties, and cfg_monodomain_create_from_dict, which
+// applies the reference's keys and selection rules:
+//   myocardiumSolver <name>;  <name>Coeffs { ... }      (electroModel.C:142-200)
+//   conductivity [dims] (xx xy xz yy yz zz);            (monodomainSolver.C:86-95)
+//   chi / cm [dims] value;                              (myocardiumDomain.C:265-266)
+//   ionicModel, tissue, solver, absTol, relTol, maxSteps (ionicModel.C:76-94)
+//   solutionAlgorithm implicit|explicit                 (myocardiumDomain.C:271-277)
+//   externalStimulus { ... }                            (stimulusIO.C:305-400)
+#include <cctype>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "host_common.h"
+
+namespace cfg {
+namespace {
+
+struct Entry;
+using Dict = std::map<std::string, std::shared_ptr<Entry>>;
+
+struct Entry {
+    bool is_dict = false;
+    std::vector<std::string> tokens;   // value tokens, "(" ")" kept, [dims] dropped
+    Dict dict;
+};
+
+class Parser {
+public:
+    explicit Parser(const std::string& s) : s_(s) {}
+
+    bool parse(Dict& out, std::string& err)
+    {
+        try {
+            parse_body(out, false);
+        } catch (const std::string& e) {
+            err = e;
+            return false;
+        }
+        return true;
+    }
+
+private:
+    const std::string& s_;
+    size_t i_ = 0;
+
+    void skip()
+    {
+        for (;;) {
+            while (i_ < s_.size() && std::isspace((unsigned char)s_[i_])) ++i_;
+            if (s_.compare(i_, 2, "//") == 0) {
+                while (i_ < s_.size() && s_[i_] != '\n') ++i_;
+            } else if (s_.compare(i_, 2, "/*") == 0) {
+                size_t e = s_.find("*/", i_ + 2);
+                i_ = e == std::string::npos ? s_.size() : e + 2;
+            } else {
+                return;
+            }
+        }
+    }
+
+    std::string token()
+    {
+        skip();
+        if (i_ >= s_.size()) return "";
+        const char c = s_[i_];
+        if (std::strchr("(){}[];", c)) {
+            ++i_;
+            return std::string(1, c);
+        }
+        if (c == '"') {
+            size_t e = s_.find('"', i_ + 1);
+            if (e == std::string::npos) throw std::string("unterminated string");
+            std::string t = s_.substr(i_ + 1, e - i_ - 1);
+            i_ = e + 1;
+            return t;
+        }
+        size_t b = i_;
+        while (i_ < s_.size() && !std::isspace((unsigned char)s_[i_]) &&
+               !std::strchr("(){}[];", s_[i_]))
+            ++i_;
+        return s_.substr(b, i_ - b);
+    }
+
+    std::string peek()
+    {
+        size_t save = i_;
+        std::string t = token();
+        i_ = save;
+        return t;
+    }
+
+    void parse_body(Dict& d, bool nested)
+    {
+        for (;;) {
+            std::string key = token();
+            if (key.empty()) {
+                if (nested) throw std::string("missing '}'");
+                return;
+            }
+            if (key == "}") {
+                if (!nested) throw std::string("unexpected '}'");
+                return;
+            }
+            if (key == ";") continue;
+            if (key[0] == '#') {   // directives (#include, #inputMode) are not followed
+                while (!token().empty() && peek() != ";" && s_[i_ - 1] != '\n') {}
+                continue;
+            }
+            auto e = std::make_shared<Entry>();
+            if (peek() == "{") {
+                token();
+                e->is_dict = true;
+                parse_body(e->dict, true);
+            } else {
+                int depth = 0;
+                for (;;) {
+                    std::string t = token();
+                    if (t.empty()) throw std::string("missing ';' after " + key);
+                    if (t == "[") {   // dimension set: dropped
+                        while (true) {
+                            std::string u = token();
+                            if (u.empty()) throw std::string("missing ']'");
+                            if (u == "]") break;
+                        }
+                        continue;
+                    }
+                    if (t == "(") ++depth;
+                    if (t == ")") --depth;
+                    if (t == ";" && depth == 0) break;
+                    e->tokens.push_back(t);
+                }
+            }
+            d[key] = e;
+        }
+    }
+};
+
+const Entry* find(const Dict& d, const char* k)
+{
+    auto it = d.find(k);
+    return it == d.end() ? nullptr : it->second.get();
+}
+
+bool scalar(const Dict& d, const char* k, double& v)
+{
+    const Entry* e = find(d, k);
+    if (!e || e->is_dict || e->tokens.empty()) return false;
+    // "name value" (dimensionedScalar with a name) or "value"
+    const std::string& t = e->tokens.back();
+    char* end = nullptr;
+    v = std::strtod(t.c_str(), &end);
+    return end && *end == '\0';
+}
+
+bool word(const Dict& d, const char* k, std::string& v)
+{
+    const Entry* e = find(d, k);
+    if (!e || e->is_dict || e->tokens.empty()) return false;
+    v = e->tokens[0];
+    return true;
+}
+
+// numbers inside the (possibly nested) list of an entry
+std::vector<double> numbers(const Entry* e)
+{
+    std::vector<double> out;
+    if (!e) return out;
+    for (const std::string& t : e->tokens) {
+        if (t == "(" || t == ")") continue;
+        char* end = nullptr;
+        double v = std::strtod(t.c_str(), &end);
+        if (end && *end == '\0') out.push_back(v);
+    }
+    return out;
+}
+
+}  // namespace
+}  // namespace cfg
+
+using namespace cfg;
+
+extern "C" int cfg_monodomain_create_from_dict(const char* text, const cfg_mesh_desc* mesh,
+                                               double delta_t, int precision,
+                                               cfg_monodomain** out)
+{
+    clear_error();
+    if (!text || !mesh || !out) return fail(CFG_ERR_INVALID, "null argument");
+    Dict root;
+    std::string err;
+    std::string src(text);
+    if (!Parser(src).parse(root, err))
+        return fail(CFG_ERR_INVALID, "electroProperties: %s", err.c_str());
+    std::string solver;
+    if (!word(root, "myocardiumSolver", solver))
+        return fail(CFG_ERR_INVALID, "electroProperties: keyword myocardiumSolver is undefined");
+    if (solver != "monodomainSolver")
+        return fail(CFG_ERR_UNSUPPORTED, "myocardiumSolver %s: only monodomainSolver runs here",
+                    solver.c_str());
+    const Entry* ce = find(root, "monodomainSolverCoeffs");
+    if (!ce || !ce->is_dict)
+        return fail(CFG_ERR_INVALID, "electroProperties: monodomainSolverCoeffs is undefined");
+    const Dict& c = ce->dict;
+
+    cfg_monodomain_desc d{};
+    static thread_local std::string model, tissue, ode_solver;
+    if (!word(c, "ionicModel", model))
+        return fail(CFG_ERR_INVALID, "keyword ionicModel is undefined");
+    if (!word(c, "tissue", tissue)) tissue.clear();
+    d.ionic.ionic_model = model.c_str();
+    d.ionic.tissue = tissue.empty() ? nullptr : tissue.c_str();
+    d.ionic.n_cells = mesh->n_cells;
+    d.ionic.initial_delta_t = delta_t;   // runTime.deltaT (myocardiumDomainInterface.C:71-76)
+    d.ionic.solve_vm_within_ode = 0;
+    d.ionic.precision = precision;
+    d.ionic.ode.solver = word(c, "solver", ode_solver) ? ode_solver.c_str() : "RKF45";
+    double v;
+    d.ionic.ode.abs_tol = scalar(c, "absTol", v) ? v : -1;
+    d.ionic.ode.rel_tol = scalar(c, "relTol", v) ? v : -1;
+    d.ionic.ode.max_steps = scalar(c, "maxSteps", v) ? (long long)v : -1;
+    d.ionic.ode.safe_scale = scalar(c, "safeScale", v) ? v : -1;
+    d.ionic.ode.min_scale = scalar(c, "minScale", v) ? v : -1;
+    d.ionic.ode.max_scale = scalar(c, "maxScale", v) ? v : -1;
+    d.ionic.ode.alpha_increase = scalar(c, "alphaIncrease", v) ? v : -1;
+    d.ionic.ode.alpha_decrease = scalar(c, "alphaDecrease", v) ? v : -1;
+
+    std::vector<double> sig = numbers(find(c, "conductivity"));
+    if (sig.size() != 6)
+        return fail(CFG_ERR_INVALID, "conductivity must be a symmTensor (xx xy xz yy yz zz)");
+    for (int k = 0; k < 6; ++k) d.conductivity[k] = sig[size_t(k)];
+    if (!scalar(c, "chi", d.chi)) return fail(CFG_ERR_INVALID, "keyword chi is undefined");
+    if (!scalar(c, "cm", d.cm)) return fail(CFG_ERR_INVALID, "keyword cm is undefined");
+    std::string alg = "implicit";
+    word(c, "solutionAlgorithm", alg);
+    if (alg != "implicit" && alg != "explicit")
+        return fail(CFG_ERR_INVALID, "Unrecognised solution algorithm %s", alg.c_str());
+    d.implicit = alg == "implicit";
+    // fvSchemes / fvSolution of the tutorials (backward; PCG 1e-8 relTol 0;
+    // PIMPLE residualControl 1e-6); a "gpu" sub-dictionary may override them
+    d.ddt_backward = 1;
+    d.pcg_tol = 1e-8;
+    d.pcg_rel_tol = 0.0;
+    d.pcg_max_iter = 1000;
+    d.n_outer = 1000;
+    d.outer_tol = 1e-6;
+    d.vm0 = -0.084;
+    if (const Entry* g = find(c, "gpu"); g && g->is_dict) {
+        std::string ddt;
+        if (word(g->dict, "ddtScheme", ddt)) d.ddt_backward = ddt == "backward";
+        if (scalar(g->dict, "tolerance", v)) d.pcg_tol = v;
+        if (scalar(g->dict, "relTol", v)) d.pcg_rel_tol = v;
+        if (scalar(g->dict, "maxIter", v)) d.pcg_max_iter = int(v);
+        if (scalar(g->dict, "nOuterCorrectors", v)) d.n_outer = int(v);
+        if (scalar(g->dict, "residualControl", v)) d.outer_tol = v;
+    }
+    // externalStimulus (stimulusIO::loadExternalStimulusProtocol)
+    if (const Entry* se = find(c, "externalStimulus"); se && se->is_dict) {
+        const Dict& s = se->dict;
+        std::vector<double> mn, mx;
+        const bool lists = find(s, "stimulusLocationMinList") != nullptr;
+        if (lists != (find(s, "stimulusLocationMaxList") != nullptr))
+            return fail(CFG_ERR_INVALID, "Both stimulusLocationMinList and "
+                                         "stimulusLocationMaxList must be provided together.");
+        mn = numbers(find(s, lists ? "stimulusLocationMinList" : "stimulusLocationMin"));
+        mx = numbers(find(s, lists ? "stimulusLocationMaxList" : "stimulusLocationMax"));
+        if (mn.size() != mx.size() || mn.empty() || mn.size() % 3)
+            return fail(CFG_ERR_INVALID, "stimulus box corners are inconsistent");
+        const int nb = int(mn.size() / 3);
+        if (nb > 8) return fail(CFG_ERR_UNSUPPORTED, "at most 8 stimulus boxes");
+        d.n_boxes = nb;
+        auto per_box = [&](const char* list, const char* single, double* dst, bool required,
+                           double dflt) -> int {
+            std::vector<double> l = numbers(find(s, list));
+            if (!l.empty()) {
+                if (int(l.size()) != nb)
+                    return fail(CFG_ERR_INVALID, "%s has %d entries, expected %d", list,
+                                int(l.size()), nb);
+                for (int b = 0; b < nb; ++b) dst[b] = l[size_t(b)];
+                return CFG_OK;
+            }
+            double x = dflt;
+            if (!scalar(s, single, x) && required)
+                return fail(CFG_ERR_INVALID, "keyword %s is undefined", single);
+            for (int b = 0; b < nb; ++b) dst[b] = x;
+            return CFG_OK;
+        };
+        int rc;
+        if ((rc = per_box("stimulusStartTimeList", "stimulusStartTime", d.box_start, false, 0.0)))
+            return rc;
+        if ((rc = per_box("stimulusDurationList", "stimulusDuration", d.box_duration, true, 0.0)))
+            return rc;
+        if ((rc = per_box("stimulusIntensityList", "stimulusIntensity", d.box_intensity, true,
+                          0.0)))
+            return rc;
+        for (int b = 0; b < nb; ++b) {
+            if (d.box_duration[b] < 0)
+                return fail(CFG_ERR_INVALID, "stimulusDuration must be non-negative");
+            for (int k = 0; k < 3; ++k) {
+                d.box_min[b][k] = mn[size_t(3 * b + k)];
+                d.box_max[b][k] = mx[size_t(3 * b + k)];
+            }
+        }
+    }
+    return cfg_monodomain_create(&d, mesh, out);
+}

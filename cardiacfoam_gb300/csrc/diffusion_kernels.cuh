@@ -1,0 +1,232 @@
+// Diffusion half of the monodomain step on the GPU:
+//   chi*Cm*ddt(Vm) == laplacian(sigma, Vm) - chi*Cm*Iion + src
+// (MonodomainSolver::solveDiffusionImplicit/Explicit, monodomainSolver.C:103-150).
+//
+// Matrix: OpenFOAM's symmetric lduMatrix re-laid as ELL rows (column-major,
+// neighbours sorted ascending, per-row counts) so a row sum visits the
+// off-diagonals in the same order as lduMatrix::Amul's face loop; the
+// diagonal is rebuilt each solve from the ddt coefficient and the static
+// Laplacian row sum.
+//
+// PCG restates lduMatrix PCG (normFactor, L1 residual, convergence test)
+// with the diagonal preconditioner.  Scalars live in device memory; every
+// reduction writes per-block partials and the last block to finish sums them
+// in a fixed order, so results do not depend on scheduling.  Kernels of a
+// finished solve return at once, which lets a fixed launch sequence (or a
+// graph with conditional nodes) run a data-dependent number of iterations.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "../../include/cardiac_gpu.h"
+
+namespace cfg {
+
+constexpr int kDiffBlock = 256;
+constexpr int kMaxSolves = 16;
+
+struct PcgState {
+    // --- control (device-owned during a step)
+    int n_old;            // stored old-time levels of Vm (GeometricField::nOldTimes)
+    int corr;             // PIMPLE corrector of the current step (1-based)
+    int solve_active;     // current PCG solve still iterating
+    int outer_active;     // PIMPLE loop continues
+    int converged_outer;  // residualControl met; the running corrector is the final one
+    int iter;             // iterations of the current solve
+    int n_solves;
+    int status;           // CFG_ERR_* bits
+    // --- settings
+    double tol, rel_tol, outer_tol;
+    int max_iter, n_outer;
+    // --- scalars
+    double sum_x, avg, sum_absr, normf, init_res, res, wArA, wArAold, wApA, alpha, beta;
+    double t, t0;         // runTime value and step start
+    unsigned int arrive[4];
+    // --- statistics of the last step
+    int iters[kMaxSolves];
+    double init_r[kMaxSolves], final_r[kMaxSolves];
+};
+
+struct DiffusionArgs {
+    long long n;
+    int width;                 // ELL width
+    const int* ell_col;        // [width][n]
+    const double* ell_coef;    // [width][n] face coefficient (>0)
+    const unsigned char* ell_cnt;  // [n]
+    const double* lapdiag;     // [n] sum of -coef in row order
+    const double* vol;         // [n]
+    // stencil form (structured block, uniform coefficient per direction)
+    int sx, sy, sz;            // nx, ny, nz (0 = use ELL)
+    double cx, cy, cz;
+    // fields
+    double* vm;                // x
+    double* vm_old;
+    double* vm_oldold;
+    const double* iion;
+    double* act;
+    unsigned char* act_flag;
+    // boxes
+    const unsigned char* box_mask;  // [n] bit b: centre inside box b
+    int n_boxes;
+    double box_start[8], box_end[8], box_intensity[8];
+    // PCG work
+    double *diag, *rD, *b, *r, *z, *ax, *sumA, *pA, *pB, *ap;
+    double* partial;           // [4][nblocks]
+    int nblocks;
+    PcgState* st;
+    // step constants
+    double dt, chicm;
+    int ddt_backward;
+};
+
+// ------------------------------------------------------------------ helpers
+
+__device__ __forceinline__ double warp_sum(double v)
+{
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Block-level sums of up to 3 values into partial[k][blockIdx.x] (fixed order).
+template <int K>
+__device__ __forceinline__ void block_partials(const DiffusionArgs& a, double (&v)[K])
+{
+    __shared__ double sh[K][kDiffBlock / 32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        double s = warp_sum(v[k]);
+        if (lane == 0) sh[k][w] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            double s = 0.0;
+            for (int j = 0; j < kDiffBlock / 32; ++j) s += sh[k][j];
+            a.partial[k * a.nblocks + blockIdx.x] = s;
+        }
+    }
+}
+
+// True in exactly one block: the last to arrive.  Its threads then sum the
+// partials with sum_partials().
+__device__ __forceinline__ bool last_block(const DiffusionArgs& a, int slot)
+{
+    __shared__ bool is_last;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        unsigned prev = atomicAdd(&a.st->arrive[slot], 1u);
+        is_last = (prev == unsigned(a.nblocks) - 1);
+        if (is_last) a.st->arrive[slot] = 0;
+    }
+    __syncthreads();
+    if (is_last) __threadfence();
+    return is_last;
+}
+
+// Deterministic sum of partial[k][0..nblocks) by the calling block.
+__device__ __forceinline__ double sum_partials(const DiffusionArgs& a, int k)
+{
+    __shared__ double sh[kDiffBlock];
+    double s = 0.0;
+    for (int i = threadIdx.x; i < a.nblocks; i += kDiffBlock)
+        s += *((volatile double*)&a.partial[k * a.nblocks + i]);
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int h = kDiffBlock / 2; h > 0; h >>= 1) {
+        if (threadIdx.x < h) sh[threadIdx.x] += sh[threadIdx.x + h];
+        __syncthreads();
+    }
+    double r = sh[0];
+    __syncthreads();
+    return r;
+}
+
+// A.x for row c with A = diag - offdiag: diag*x, then each (-coef)*x_nb
+// added in column order (bitwise the same as lduMatrix::Amul).
+template <class F>
+__device__ __forceinline__ double row_amul(const DiffusionArgs& a, long long c, double d, F f)
+{
+    double acc = d * f(c);
+    if (a.sx) {
+        const long long nx = a.sx, nxy = (long long)a.sx * a.sy;
+        const long long i = c % nx, j = (c / nx) % a.sy, k = c / nxy;
+        if (k > 0) acc += (-a.cz) * f(c - nxy);
+        if (j > 0) acc += (-a.cy) * f(c - nx);
+        if (i > 0) acc += (-a.cx) * f(c - 1);
+        if (i + 1 < nx) acc += (-a.cx) * f(c + 1);
+        if (j + 1 < a.sy) acc += (-a.cy) * f(c + nx);
+        if (k + 1 < a.sz) acc += (-a.cz) * f(c + nxy);
+    } else {
+        const int cnt = a.ell_cnt[c];
+        for (int q = 0; q < cnt; ++q)
+            acc += (-a.ell_coef[(long long)q * a.n + c]) * f(a.ell_col[(long long)q * a.n + c]);
+    }
+    return acc;
+}
+
+// row sum of the matrix (lduMatrix::sumA): diag then each -coef
+__device__ __forceinline__ double row_sum(const DiffusionArgs& a, long long c, double d)
+{
+    return row_amul(a, c, d, [](long long) { return 1.0; });
+}
+
+// ddt coefficients (EulerDdtScheme / backwardDdtScheme with deltaT0 = GREAT
+// while fewer than two old-time levels exist)
+__device__ __forceinline__ void ddt_coeffs(const DiffusionArgs& a, int n_old, double& cft,
+                                           double& cft0, double& cft00)
+{
+    if (!a.ddt_backward) {
+        cft = 1.0; cft0 = 1.0; cft00 = 0.0;
+        return;
+    }
+    const double dt = a.dt;
+    const double dt0 = n_old < 2 ? 1e15 : dt;
+    cft = 1 + dt / (dt + dt0);
+    cft00 = dt * dt / (dt0 * (dt + dt0));
+    cft0 = cft + cft00;
+}
+
+// MyocardiumDomain::updateExternalStimulusCurrent for one cell
+__device__ __forceinline__ double box_source(const DiffusionArgs& a, long long c, double t0)
+{
+    double s = 0.0;
+    if (!a.box_mask) return s;
+    const unsigned m = a.box_mask[c];
+    for (int b = 0; b < a.n_boxes; ++b) {
+        if (t0 < a.box_start[b] || t0 > a.box_end[b]) continue;
+        if (m & (1u << b)) s += a.box_intensity[b];
+    }
+    return s;
+}
+
+// PIMPLE control after a solve ends (pimpleLoop::loop / criteriaSatisfied):
+// the next corrector runs unless the loop already converged; it is the
+// final one when this solve's initial residual met residualControl.
+__device__ __forceinline__ void end_solve(PcgState* st)
+{
+    int k = st->n_solves;
+    if (k < kMaxSolves) {
+        st->iters[k] = st->iter;
+        st->init_r[k] = st->init_res;
+        st->final_r[k] = st->res;
+    }
+    st->n_solves = k + 1;
+    st->solve_active = 0;
+    if (st->converged_outer || st->corr + 1 > st->n_outer) {
+        st->outer_active = 0;
+    } else {
+        if (st->init_res < st->outer_tol) st->converged_outer = 1;
+        st->outer_active = 1;
+    }
+    st->corr += 1;
+}
+
+__device__ __forceinline__ bool pcg_converged(const PcgState* st, double r)
+{
+    return r < st->tol || (st->rel_tol > 1e-20 && r < st->rel_tol * st->init_res);
+}
+
+}  // namespace cfg

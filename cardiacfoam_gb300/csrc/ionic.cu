@@ -1,0 +1,379 @@
+// cfg_ionic_*: the GPU ionic model behind the ionicModel plugin interface
+// (src/ionicModels/ionicModel/ionicModel.H:184-256).
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "host_common.h"
+#include "ionic_host.h"
+
+namespace cfg {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const char* fmt, ...)
+{
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return code;
+}
+
+void clear_error() { g_last_error.clear(); }
+
+int tissue_flag(const char* t)
+{
+    if (!t) return -1;
+    if (!std::strcmp(t, "epicardialCells")) return 1;
+    if (!std::strcmp(t, "mCells")) return 2;
+    if (!std::strcmp(t, "endocardialCells")) return 3;
+    if (!std::strcmp(t, "myocyte")) return 4;
+    return -1;
+}
+
+static const char* tissue_name(int f)
+{
+    switch (f) {
+    case 1: return "epicardialCells";
+    case 2: return "mCells";
+    case 3: return "endocardialCells";
+    case 4: return "myocyte";
+    default: return "unknown";
+    }
+}
+
+static bool supported(const IonicModelOps* m, int flag)
+{
+    for (const int* t = m->tissues; *t; ++t)
+        if (*t == flag) return true;
+    return false;
+}
+
+static std::string supported_list(const IonicModelOps* m)
+{
+    std::string s = "(";
+    for (const int* t = m->tissues; *t; ++t) {
+        if (t != m->tissues) s += ' ';
+        s += tissue_name(*t);
+    }
+    return s + ")";
+}
+
+OdeSettings make_ode(const cfg_ode_desc& d)
+{
+    OdeSettings s;
+    s.abs_tol = d.abs_tol >= 0 ? d.abs_tol : 1e-15;
+    s.rel_tol = d.rel_tol >= 0 ? d.rel_tol : 1e-4;
+    s.max_steps = d.max_steps > 0 ? d.max_steps : 10000;
+    s.safe_scale = d.safe_scale > 0 ? d.safe_scale : 0.9;
+    s.min_scale = d.min_scale > 0 ? d.min_scale : 0.2;
+    s.max_scale = d.max_scale > 0 ? d.max_scale : 10.0;
+    s.alpha_inc = d.alpha_increase > 0 ? d.alpha_increase : 0.2;
+    s.alpha_dec = d.alpha_decrease > 0 ? d.alpha_decrease : 0.25;
+    s.inc_threshold = std::pow(s.max_scale / s.safe_scale, -1.0 / s.alpha_inc);
+    return s;
+}
+
+int ionic_validate(const cfg_ionic_desc* d, const IonicModelOps** model, int* tissue)
+{
+    if (!d) return fail(CFG_ERR_INVALID, "null argument");
+    const IonicModelOps* m = find_ionic_model(d->ionic_model);
+    if (!m)
+        return fail(CFG_ERR_INVALID, "Unknown ionicModel type %s. Valid ionicModel types are: %s",
+                    d->ionic_model ? d->ionic_model : "(null)", ionic_model_names());
+    if (d->ode.solver && std::strcmp(d->ode.solver, "RKF45") != 0)
+        return fail(CFG_ERR_UNSUPPORTED, "ODE solver %s is not available on the GPU (RKF45 is)",
+                    d->ode.solver);
+    if (d->n_cells < 0) return fail(CFG_ERR_INVALID, "negative cell count");
+    if (d->precision != CFG_PRECISION_FP64 && d->precision != CFG_PRECISION_MIXED)
+        return fail(CFG_ERR_INVALID, "unknown precision %d", d->precision);
+    // ionicSelector::selectTissue (ionicSelector.C:32-53)
+    if (!d->tissue) return fail(CFG_ERR_INVALID, "Normal model requires 'tissue' entry");
+    const int flag = tissue_flag(d->tissue);
+    if (flag < 0 || !supported(m, flag))
+        return fail(CFG_ERR_INVALID, "Unsupported tissue '%s' allowed: %s", d->tissue,
+                    supported_list(m).c_str());
+    if (d->tissue_per_cell) {
+        for (long long c = 0; c < d->n_cells; ++c)
+            if (!supported(m, d->tissue_per_cell[c]))
+                return fail(CFG_ERR_INVALID, "cell %lld: unsupported tissue flag %d", c,
+                            int(d->tissue_per_cell[c]));
+    }
+    if (!(d->initial_delta_t > 0)) return fail(CFG_ERR_INVALID, "initialDeltaT must be positive");
+    *model = m;
+    *tissue = flag;
+    return CFG_OK;
+}
+
+int ionic_create(const cfg_ionic_desc* d, cudaStream_t stream, cfg_ionic** out)
+{
+    if (!out) return fail(CFG_ERR_INVALID, "null argument");
+    *out = nullptr;
+    const IonicModelOps* m = nullptr;
+    int flag = 0;
+    if (int rc = ionic_validate(d, &m, &flag)) return rc;
+    cfg_ionic* ion = new cfg_ionic();
+    ion->ops = m;
+    ion->n = d->n_cells;
+    ion->precision = d->precision;
+    ion->solve_vm = d->solve_vm_within_ode != 0;
+    ion->tissue = flag;
+    ion->ode = make_ode(d->ode);
+    const cfg_stimulus_desc& s = d->stimulus;
+    ion->stim = CfgStimulus{s.stim_start, s.stim_period_s1, s.stim_duration, s.stim_amplitude,
+                            s.nstim1, s.stim_period_s2, s.nstim2};
+    ion->stream = stream;
+    const long long n = ion->n;
+    const int p = ion->precision;
+    const int nw = m->n_wide[p], nn = m->ns - m->n_wide[p];
+    auto cleanup_fail = [&](int code) {
+        ionic_free(ion);
+        return code;
+    };
+    cudaError_t e = cudaSuccess;
+    if (!e) e = dmalloc(&ion->d_yw, size_t(nw) * n);
+    if (!e) e = dmalloc(&ion->d_yn, size_t(nn) * n);
+    if (!e) e = dmalloc(&ion->d_step, size_t(n));
+    if (!e) e = dmalloc(&ion->d_vm, size_t(n));
+    if (!e) e = dmalloc(&ion->d_im, size_t(n));
+    if (!e) e = dmalloc(&ion->d_status, 1);
+    if (!e) e = dmalloc(&ion->d_evals, 1);
+    if (!e) e = dmalloc(&ion->d_fail, 8);
+    if (!e) e = cudaMemsetAsync(ion->d_fail, 0, 8 * sizeof(double), stream);
+    if (!e && d->tissue_per_cell) {
+        e = dmalloc(&ion->d_tissue, size_t(n));
+        if (!e) e = cudaMemcpyAsync(ion->d_tissue, d->tissue_per_cell, size_t(n),
+                                    cudaMemcpyHostToDevice, stream);
+    }
+    if (!e && d->scales) {
+        e = dmalloc(&ion->d_scales, size_t(6) * n);
+        if (!e) e = cudaMemcpyAsync(ion->d_scales, d->scales, sizeof(double) * 6 * size_t(n),
+                                    cudaMemcpyHostToDevice, stream);
+    }
+    if (!e) e = cudaMemsetAsync(ion->d_status, 0, sizeof(int), stream);
+    if (!e) e = cudaMemsetAsync(ion->d_evals, 0, sizeof(unsigned long long), stream);
+    if (!e)
+        e = m->init[p](n, flag, ion->d_tissue, ion->d_scales, n, d->initial_delta_t, ion->d_yw,
+                       ion->d_yn, ion->d_step, stream);
+    if (!e) e = cudaStreamSynchronize(stream);
+    if (e) {
+        fail(CFG_ERR_CUDA, "ionic model set-up failed: %s", cudaGetErrorString(e));
+        return cleanup_fail(CFG_ERR_CUDA);
+    }
+    *out = ion;
+    return CFG_OK;
+}
+
+void ionic_free(cfg_ionic* ion)
+{
+    if (!ion) return;
+    dfree(ion->d_yw);
+    dfree(ion->d_yn);
+    dfree(ion->d_step);
+    dfree(ion->d_vm);
+    dfree(ion->d_im);
+    dfree(ion->d_status);
+    dfree(ion->d_evals);
+    dfree(ion->d_fail);
+    dfree(ion->d_tissue);
+    dfree(ion->d_scales);
+    if (ion->own_stream && ion->stream) cudaStreamDestroy(ion->stream);
+    delete ion;
+}
+
+IonicLaunch ionic_launch_args(const cfg_ionic* ion, double t0, double dt, const double* t_dev,
+                              const double* vm_dev, double* im_dev)
+{
+    IonicLaunch L{};
+    L.n = ion->n;
+    L.t0 = t0;
+    L.dt = dt;
+    L.t_dev = t_dev;
+    L.tissue = ion->tissue;
+    L.tissue_cell = ion->d_tissue;
+    L.scales = ion->d_scales;
+    L.scale_stride = ion->n;
+    L.stim = ion->stim;
+    L.ode = ion->ode;
+    L.vm = vm_dev;
+    L.im = im_dev;
+    L.yw = ion->d_yw;
+    L.yn = ion->d_yn;
+    L.step = ion->d_step;
+    L.status = ion->d_status;
+    L.rhs_evals = ion->d_evals;
+    L.fail_record = ion->d_fail;
+    return L;
+}
+
+cudaError_t ionic_enqueue(const cfg_ionic* ion, const IonicLaunch& L)
+{
+    return ion->ops->step[ion->precision][ion->solve_vm ? 1 : 0](L, ion->stream, ion->block);
+}
+
+int ionic_check_status(cfg_ionic* ion)
+{
+    int st = 0;
+    CFG_CUDA_TRY(cudaMemcpyAsync(&st, ion->d_status, sizeof(int), cudaMemcpyDeviceToHost,
+                                 ion->stream));
+    CFG_CUDA_TRY(cudaStreamSynchronize(ion->stream));
+    if (st & CFG_ERR_ODE_STEPS) {
+        double r[8] = {0};
+        cudaMemcpy(r, ion->d_fail, sizeof r, cudaMemcpyDeviceToHost);
+        const int worst = int(r[4]);
+        return fail(CFG_ERR_ODE_STEPS,
+                    "%s: cell %lld: %s (maximum %lld) at x = %.17g, dx = %.6g after %lld "
+                    "substeps; worst state %s = %.9g with normalised error %.6g",
+                    ion->ops->name, (long long)r[0],
+                    r[1] == 2 ? "stepsize underflow" : "Integration steps greater than maximum",
+                    (long long)ion->ode.max_steps, r[2], r[3], (long long)r[7],
+                    worst >= 0 && worst < ion->ops->ns ? ion->ops->state_names[worst] : "?",
+                    r[6], r[5]);
+    }
+    if (st & CFG_ERR_NONFINITE)
+        return fail(CFG_ERR_NONFINITE, "non-finite ionic current in %s", ion->ops->name);
+    return CFG_OK;
+}
+
+}  // namespace cfg
+
+using namespace cfg;
+
+extern "C" {
+
+const char* cfg_last_error(void) { return g_last_error.c_str(); }
+
+int cfg_ionic_create(const cfg_ionic_desc* desc, cfg_ionic** out)
+{
+    clear_error();
+    const IonicModelOps* m = nullptr;
+    int flag = 0;
+    if (!out) return fail(CFG_ERR_INVALID, "null argument");
+    *out = nullptr;
+    if (int rc = ionic_validate(desc, &m, &flag)) return rc;
+    cudaStream_t s = nullptr;
+    CFG_CUDA_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    int rc = ionic_create(desc, s, out);
+    if (rc) {
+        cudaStreamDestroy(s);
+        return rc;
+    }
+    (*out)->own_stream = true;
+    return CFG_OK;
+}
+
+int cfg_ionic_solve(cfg_ionic* ion, double t0, double dt, const double* vm, double* im)
+{
+    if (!ion) return fail(CFG_ERR_INVALID, "null ionic model");
+    const size_t bytes = sizeof(double) * size_t(ion->n);
+    if (!ion->solve_vm) {
+        if (!vm) return fail(CFG_ERR_INVALID, "null Vm");
+        CFG_CUDA_TRY(cudaMemcpyAsync(ion->d_vm, vm, bytes, cudaMemcpyHostToDevice, ion->stream));
+    }
+    IonicLaunch L = ionic_launch_args(ion, t0, dt, nullptr, ion->d_vm, ion->d_im);
+    CFG_CUDA_TRY(ionic_enqueue(ion, L));
+    if (im)
+        CFG_CUDA_TRY(cudaMemcpyAsync(im, ion->d_im, bytes, cudaMemcpyDeviceToHost, ion->stream));
+    return ionic_check_status(ion);
+}
+
+int cfg_ionic_solve_device(cfg_ionic* ion, double t0, double dt, const double* vm_dev,
+                           double* im_dev)
+{
+    if (!ion) return fail(CFG_ERR_INVALID, "null ionic model");
+    IonicLaunch L = ionic_launch_args(ion, t0, dt, nullptr, vm_dev, im_dev);
+    CFG_CUDA_TRY(ionic_enqueue(ion, L));
+    return CFG_OK;
+}
+
+int cfg_ionic_num_states(const cfg_ionic* ion, int* n)
+{
+    if (!ion || !n) return fail(CFG_ERR_INVALID, "null argument");
+    *n = ion->ops->ns;
+    return CFG_OK;
+}
+
+int cfg_ionic_state_name(const cfg_ionic* ion, int i, char* buf, size_t len)
+{
+    if (!ion || !buf || i < 0 || i >= ion->ops->ns) return fail(CFG_ERR_INVALID, "bad index");
+    std::snprintf(buf, len, "%s", ion->ops->state_names[i]);
+    return CFG_OK;
+}
+
+int cfg_ionic_get_states(cfg_ionic* ion, double* host)
+{
+    if (!ion || !host) return fail(CFG_ERR_INVALID, "null argument");
+    const long long n = ion->n;
+    const int p = ion->precision, ns = ion->ops->ns;
+    std::vector<float> tmp;
+    for (int i = 0; i < ns; ++i) {
+        const int w = ion->ops->wide_of[p * ns + i], s = ion->ops->slot_of[p * ns + i];
+        if (w) {
+            CFG_CUDA_TRY(cudaMemcpyAsync(host + size_t(i) * n, ion->d_yw + size_t(s) * n,
+                                         sizeof(double) * n, cudaMemcpyDeviceToHost, ion->stream));
+        } else {
+            tmp.resize(n);
+            CFG_CUDA_TRY(cudaMemcpyAsync(tmp.data(), ion->d_yn + size_t(s) * n, sizeof(float) * n,
+                                         cudaMemcpyDeviceToHost, ion->stream));
+            CFG_CUDA_TRY(cudaStreamSynchronize(ion->stream));
+            for (long long c = 0; c < n; ++c) host[size_t(i) * n + c] = tmp[c];
+        }
+    }
+    CFG_CUDA_TRY(cudaStreamSynchronize(ion->stream));
+    return CFG_OK;
+}
+
+int cfg_ionic_set_states(cfg_ionic* ion, const double* host)
+{
+    if (!ion || !host) return fail(CFG_ERR_INVALID, "null argument");
+    const long long n = ion->n;
+    const int p = ion->precision, ns = ion->ops->ns;
+    std::vector<float> tmp;
+    for (int i = 0; i < ns; ++i) {
+        const int w = ion->ops->wide_of[p * ns + i], s = ion->ops->slot_of[p * ns + i];
+        if (w) {
+            CFG_CUDA_TRY(cudaMemcpyAsync(ion->d_yw + size_t(s) * n, host + size_t(i) * n,
+                                         sizeof(double) * n, cudaMemcpyHostToDevice, ion->stream));
+        } else {
+            tmp.resize(n);
+            for (long long c = 0; c < n; ++c) tmp[c] = float(host[size_t(i) * n + c]);
+            CFG_CUDA_TRY(cudaMemcpyAsync(ion->d_yn + size_t(s) * n, tmp.data(), sizeof(float) * n,
+                                         cudaMemcpyHostToDevice, ion->stream));
+            CFG_CUDA_TRY(cudaStreamSynchronize(ion->stream));
+        }
+    }
+    CFG_CUDA_TRY(cudaStreamSynchronize(ion->stream));
+    return CFG_OK;
+}
+
+int cfg_ionic_get_steps(cfg_ionic* ion, double* host)
+{
+    if (!ion || !host) return fail(CFG_ERR_INVALID, "null argument");
+    CFG_CUDA_TRY(cudaMemcpyAsync(host, ion->d_step, sizeof(double) * size_t(ion->n),
+                                 cudaMemcpyDeviceToHost, ion->stream));
+    CFG_CUDA_TRY(cudaStreamSynchronize(ion->stream));
+    return CFG_OK;
+}
+
+int cfg_ionic_rhs_evaluations(const cfg_ionic* ion, unsigned long long* count)
+{
+    if (!ion || !count) return fail(CFG_ERR_INVALID, "null argument");
+    CFG_CUDA_TRY(cudaMemcpyAsync(count, ion->d_evals, sizeof(unsigned long long),
+                                 cudaMemcpyDeviceToHost, ion->stream));
+    CFG_CUDA_TRY(cudaStreamSynchronize(ion->stream));
+    return CFG_OK;
+}
+
+int cfg_ionic_destroy(cfg_ionic* ion)
+{
+    if (ion) {
+        cudaStreamSynchronize(ion->stream);
+        ionic_free(ion);
+    }
+    return CFG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,39 @@
+// Host representation of a GPU ionic model (one ionicModel instance).
+#pragma once
+
+#include "host_common.h"
+#include "ionic_registry.h"
+
+struct cfg_ionic {
+    const cfg::IonicModelOps* ops = nullptr;
+    long long n = 0;
+    int precision = CFG_PRECISION_FP64;
+    bool solve_vm = false;
+    int tissue = 0;
+    cfg::OdeSettings ode{};
+    cfg::CfgStimulus stim{};
+    double* d_yw = nullptr;        // wide (double) states, SoA
+    float* d_yn = nullptr;         // narrow (float) states, SoA (mixed form)
+    double* d_step = nullptr;      // per-cell persistent ODE step
+    double* d_vm = nullptr;        // staging for host-field solves
+    double* d_im = nullptr;
+    int* d_status = nullptr;
+    unsigned long long* d_evals = nullptr;
+    double* d_fail = nullptr;      // IonicFailure record of the first failing cell
+    unsigned char* d_tissue = nullptr;
+    double* d_scales = nullptr;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int block = 128;
+};
+
+namespace cfg {
+OdeSettings make_ode(const cfg_ode_desc& d);
+int ionic_validate(const cfg_ionic_desc* d, const IonicModelOps** model, int* tissue);
+int ionic_create(const cfg_ionic_desc* d, cudaStream_t stream, cfg_ionic** out);
+void ionic_free(cfg_ionic* ion);
+IonicLaunch ionic_launch_args(const cfg_ionic* ion, double t0, double dt, const double* t_dev,
+                              const double* vm_dev, double* im_dev);
+cudaError_t ionic_enqueue(const cfg_ionic* ion, const IonicLaunch& L);
+int ionic_check_status(cfg_ionic* ion);
+}  // namespace cfg

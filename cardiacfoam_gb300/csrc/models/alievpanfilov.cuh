@@ -1,0 +1,98 @@
+// Generated by cardiacfoam_gb300.cellml2cuda from src/ionicModels/AlievPanfilov/AlievPanfilov_1996.H.
+// The equations are the published cell model as cellML2foam wrote them;
+// regenerate with `python -m cardiacfoam_gb300.cellml2cuda` instead of editing.
+#pragma once
+#include "../ionic_common.cuh"
+
+namespace cfg { namespace alievpanfilov {
+
+constexpr int NS = 2;
+constexpr int NC = 8;
+constexpr int NA = 3;
+enum State { S_u, S_recovery_r };
+enum Constant { C_AC_Vp, C_AC_Vr, C_AC_Vth, C_AC_epsilon, C_AC_k, C_AC_mu1, C_AC_mu2, C_AC_a };
+// states kept in double in the mixed form (bit i = state i)
+constexpr unsigned long long WIDE_MASK = 0x3ull;
+constexpr double IION_SCALE = 100.0;
+constexpr double TIME_SCALE = 12.9;
+constexpr int VM_MAP = CFG_VM_ALIEV;
+constexpr int N_TISSUES = 1;
+static const int TISSUES[] = {4, 0};
+static const char* const STATE_NAMES[NS] = {"u", "recovery_r"};
+CFG_HD inline bool tissue_supported(int t) { return t == 4; }
+
+// per-cell conductance scales: index into the scale vector, or -1
+constexpr int SCALE_GNa = -1;
+constexpr int SCALE_GCaL = -1;
+constexpr int SCALE_GKr = -1;
+constexpr int SCALE_GKs = -1;
+constexpr int SCALE_GK1 = -1;
+constexpr int SCALE_Gto = -1;
+
+// Constants and initial states (initConsts).  `scale` may be null;
+// otherwise scale[SCALE_x] multiplies the named conductance right after
+// it is assigned, before constants derived from it are computed.
+CFG_HD __forceinline__ void init_consts(double* C, double* y, int tissue, const double* scale)
+{
+    (void)tissue; (void)scale;
+    C[C_AC_Vp] = 20.0;
+    C[C_AC_Vr] = (-80.0);
+    C[C_AC_Vth] = (-70.0);
+    C[C_AC_epsilon] = 0.01;
+    C[C_AC_k] = 8.0;
+    C[C_AC_mu1] = 0.2;
+    C[C_AC_mu2] = 0.3;
+    C[C_AC_a] = ((C[C_AC_Vth] - C[C_AC_Vr]) / (C[C_AC_Vp] - C[C_AC_Vr]));
+    y[S_u] = 0.05;
+    y[S_recovery_r] = 0.0;
+}
+
+// Right-hand side as used by derivatives(): dydt for every state that the
+// reference assigns (RATES of V only when SOLVE_VM).  Returns Iion.
+// Y(i) reads state i as R, K(i) reads constant i as R.
+template <class R, bool SOLVE_VM, class YS, class KS>
+__device__ __forceinline__ R rhs(double t, const YS& Y, const KS& K, R* dydt, int tissue, const CfgStimulus& stim)
+{
+    (void)tissue; (void)stim; (void)t;
+    R a_AV_eps = (K(C_AC_epsilon) + ((K(C_AC_mu1) * Y(S_recovery_r)) / (K(C_AC_mu2) + Y(S_u))));
+    dydt[S_recovery_r] = (a_AV_eps * ((-Y(S_recovery_r)) - ((K(C_AC_k) * Y(S_u)) * (Y(S_u) - (K(C_AC_a) + R(1.0))))));
+    R a_Iion_cm = ((((K(C_AC_k) * Y(S_u)) * (Y(S_u) - K(C_AC_a))) * (Y(S_u) - R(1.0))) + (Y(S_recovery_r) * Y(S_u)));
+    R a_Istim = R(cfg_stimulus_current<double>(t, stim));
+    if (SOLVE_VM) {
+        dydt[S_u] = ((-a_Iion_cm) - a_Istim);
+    }
+    return a_Iion_cm;
+}
+
+// Ionic current after the step (computeVariables at tEnd).
+template <class R, bool SOLVE_VM, class YS, class KS>
+__device__ __forceinline__ R iion(double t, const YS& Y, const KS& K, int tissue, const CfgStimulus& stim)
+{
+    (void)tissue; (void)stim; (void)t;
+    R dydt[NS];
+    R a_AV_eps = (K(C_AC_epsilon) + ((K(C_AC_mu1) * Y(S_recovery_r)) / (K(C_AC_mu2) + Y(S_u))));
+    dydt[S_recovery_r] = (a_AV_eps * ((-Y(S_recovery_r)) - ((K(C_AC_k) * Y(S_u)) * (Y(S_u) - (K(C_AC_a) + R(1.0))))));
+    R a_Iion_cm = ((((K(C_AC_k) * Y(S_u)) * (Y(S_u) - K(C_AC_a))) * (Y(S_u) - R(1.0))) + (Y(S_recovery_r) * Y(S_u)));
+    R a_Istim = R(cfg_stimulus_current<double>(t, stim));
+    if (SOLVE_VM) {
+        dydt[S_u] = ((-a_Iion_cm) - a_Istim);
+    }
+    (void)dydt;
+    return a_Iion_cm;
+}
+
+// traits bundle used by the kernel templates
+struct Model {
+    static constexpr int NS = alievpanfilov::NS, NC = alievpanfilov::NC;
+    static constexpr unsigned long long WIDE_MASK = alievpanfilov::WIDE_MASK;
+    static constexpr double IION_SCALE = alievpanfilov::IION_SCALE;
+    static constexpr double TIME_SCALE = alievpanfilov::TIME_SCALE;
+    static constexpr int VM_MAP = alievpanfilov::VM_MAP;
+    CFG_HD static __forceinline__ void init(double* C, double* y, int tissue, const double* scale) { init_consts(C, y, tissue, scale); }
+    template <class R, bool SV, class YS, class KS>
+    __device__ static __forceinline__ R rates(double t, const YS& Y, const KS& K, R* dydt, int tissue, const CfgStimulus& st) { return rhs<R, SV>(t, Y, K, dydt, tissue, st); }
+    template <class R, bool SV, class YS, class KS>
+    __device__ static __forceinline__ R current(double t, const YS& Y, const KS& K, int tissue, const CfgStimulus& st) { return iion<R, SV>(t, Y, K, tissue, st); }
+};
+
+} }  // namespace cfg::alievpanfilov

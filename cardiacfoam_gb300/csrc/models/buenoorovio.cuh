@@ -1,0 +1,142 @@
+// Generated by cardiacfoam_gb300.cellml2cuda from src/ionicModels/BuenoOrovio/BuenoOrovio_2008.H.
+// The equations are the published cell model as cellML2foam wrote them;
+// regenerate with `python -m cardiacfoam_gb300.cellml2cuda` instead of editing.
+#pragma once
+#include "../ionic_common.cuh"
+
+namespace cfg { namespace buenoorovio {
+
+constexpr int NS = 4;
+constexpr int NC = 28;
+constexpr int NA = 12;
+enum State { S_u, S_v, S_w, S_s };
+enum Constant { C_uO, C_uU, C_thetaV, C_thetaW, C_thetaVMinus, C_thetaO, C_tauV1Minus, C_tauV2Minus, C_tauVPlus, C_tauW1Minus, C_tauW2Minus, C_kWMinus, C_uWMinus, C_tauWPlus, C_tauFi, C_tauO1, C_tauO2, C_tauSo1, C_tauSo2, C_kSo, C_uSo, C_tauS1, C_tauS2, C_kS, C_uS, C_tauSi, C_tauWInfty, C_wInftyStar };
+// states kept in double in the mixed form (bit i = state i)
+constexpr unsigned long long WIDE_MASK = 0xfull;
+constexpr double IION_SCALE = 85.7;
+constexpr double TIME_SCALE = 1.0;
+constexpr int VM_MAP = CFG_VM_BUENO;
+constexpr int N_TISSUES = 3;
+static const int TISSUES[] = {3, 2, 1, 0};
+static const char* const STATE_NAMES[NS] = {"u", "v", "w", "s"};
+CFG_HD inline bool tissue_supported(int t) { return t == 3 || t == 2 || t == 1; }
+
+// per-cell conductance scales: index into the scale vector, or -1
+constexpr int SCALE_GNa = -1;
+constexpr int SCALE_GCaL = -1;
+constexpr int SCALE_GKr = -1;
+constexpr int SCALE_GKs = -1;
+constexpr int SCALE_GK1 = -1;
+constexpr int SCALE_Gto = -1;
+
+// Constants and initial states (initConsts).  `scale` may be null;
+// otherwise scale[SCALE_x] multiplies the named conductance right after
+// it is assigned, before constants derived from it are computed.
+CFG_HD __forceinline__ void init_consts(double* C, double* y, int tissue, const double* scale)
+{
+    (void)tissue; (void)scale;
+    C[C_uO] = 0;
+    C[C_uU] = ((tissue == 1) ? 1.55 : ((tissue == 2) ? 1.61 : 1.56));
+    C[C_thetaV] = 0.3;
+    C[C_thetaW] = 0.13;
+    C[C_thetaVMinus] = ((tissue == 1) ? 0.006 : ((tissue == 2) ? 0.1 : 0.2));
+    C[C_thetaO] = ((tissue == 2) ? 0.005 : 0.006);
+    C[C_tauV1Minus] = ((tissue == 1) ? 60 : ((tissue == 2) ? 80 : 75));
+    C[C_tauV2Minus] = ((tissue == 1) ? 1150 : ((tissue == 2) ? 1.4506 : 10));
+    C[C_tauVPlus] = 1.4506;
+    C[C_tauW1Minus] = ((tissue == 1) ? 60 : ((tissue == 2) ? 70 : 6));
+    C[C_tauW2Minus] = ((tissue == 1) ? 15 : ((tissue == 2) ? 8 : 140));
+    C[C_kWMinus] = ((tissue == 1) ? 65 : 200);
+    C[C_uWMinus] = ((tissue == 1) ? 0.03 : 0.016);
+    C[C_tauWPlus] = ((tissue == 1) ? 200 : 280);
+    C[C_tauFi] = ((tissue == 1) ? 0.11 : ((tissue == 2) ? 0.078 : 0.1));
+    C[C_tauO1] = ((tissue == 1) ? 400 : ((tissue == 2) ? 410 : 470));
+    C[C_tauO2] = ((tissue == 2) ? 7 : 6);
+    C[C_tauSo1] = ((tissue == 1) ? 30.0181 : ((tissue == 2) ? 91 : 40));
+    C[C_tauSo2] = ((tissue == 1) ? 0.9957 : ((tissue == 2) ? 0.8 : 1.2));
+    C[C_kSo] = ((tissue == 1) ? 2.0458 : ((tissue == 2) ? 2.1 : 2));
+    C[C_uSo] = ((tissue == 2) ? 0.6 : 0.65);
+    C[C_tauS1] = 2.7342;
+    C[C_tauS2] = ((tissue == 1) ? 16 : ((tissue == 2) ? 4 : 2));
+    C[C_kS] = 2.0994;
+    C[C_uS] = 0.9087;
+    C[C_tauSi] = ((tissue == 1) ? 1.8875 : ((tissue == 2) ? 3.3849 : 2.9013));
+    C[C_tauWInfty] = ((tissue == 1) ? 0.07 : ((tissue == 2) ? 0.01 : 0.0273));
+    C[C_wInftyStar] = ((tissue == 1) ? 0.94 : ((tissue == 2) ? 0.5 : 0.78));
+    y[S_u] = 0;
+    y[S_v] = 1.0;
+    y[S_w] = 1.0;
+    y[S_s] = 0.0;
+}
+
+// Right-hand side as used by derivatives(): dydt for every state that the
+// reference assigns (RATES of V only when SOLVE_VM).  Returns Iion.
+// Y(i) reads state i as R, K(i) reads constant i as R.
+template <class R, bool SOLVE_VM, class YS, class KS>
+__device__ __forceinline__ R rhs(double t, const YS& Y, const KS& K, R* dydt, int tissue, const CfgStimulus& stim)
+{
+    (void)tissue; (void)stim; (void)t;
+    R a_tauSo = (K(C_tauSo1) + (((K(C_tauSo2) - K(C_tauSo1)) * (R(1.0) + cfg_tanh((K(C_kSo) * (Y(S_u) - K(C_uSo)))))) / R(2.0)));
+    R a_tauO = (((R(1.0) - (((Y(S_u) - K(C_thetaO))) > R(0) ? 1 : 0)) * K(C_tauO1)) + ((((Y(S_u) - K(C_thetaO))) > R(0) ? 1 : 0) * K(C_tauO2)));
+    R a_Jfi = (((((-Y(S_v)) * (((Y(S_u) - K(C_thetaV))) > R(0) ? 1 : 0)) * (Y(S_u) - K(C_thetaV))) * (K(C_uU) - Y(S_u))) / K(C_tauFi));
+    R a_Jso = ((((Y(S_u) - K(C_uO)) * (R(1.0) - (((Y(S_u) - K(C_thetaW))) > R(0) ? 1 : 0))) / a_tauO) + ((((Y(S_u) - K(C_thetaW))) > R(0) ? 1 : 0) / a_tauSo));
+    R a_Jsi = ((((-(((Y(S_u) - K(C_thetaW))) > R(0) ? 1 : 0)) * Y(S_w)) * Y(S_s)) / K(C_tauSi));
+    R a_Jion = ((a_Jfi + a_Jso) + a_Jsi);
+    R a_tauVMinus = (((R(1.0) - (((Y(S_u) - K(C_thetaVMinus))) > R(0) ? 1 : 0)) * K(C_tauV1Minus)) + ((((Y(S_u) - K(C_thetaVMinus))) > R(0) ? 1 : 0) * K(C_tauV2Minus)));
+    R a_tauWMinus = (K(C_tauW1Minus) + (((K(C_tauW2Minus) - K(C_tauW1Minus)) * (R(1.0) + cfg_tanh((K(C_kWMinus) * (Y(S_u) - K(C_uWMinus)))))) / R(2.0)));
+    R a_tauS = (((R(1.0) - (((Y(S_u) - K(C_thetaW))) > R(0) ? 1 : 0)) * K(C_tauS1)) + ((((Y(S_u) - K(C_thetaW))) > R(0) ? 1 : 0) * K(C_tauS2)));
+    R a_vInfty = (((K(C_thetaVMinus) - Y(S_u))) > R(0) ? 1 : 0);
+    R a_wInfty = (((R(1.0) - (((Y(S_u) - K(C_thetaO))) > R(0) ? 1 : 0)) * (R(1.0) - (Y(S_u) / K(C_tauWInfty)))) + ((((Y(S_u) - K(C_thetaO))) > R(0) ? 1 : 0) * K(C_wInftyStar)));
+    dydt[S_v] = ((((R(1.0) - (((Y(S_u) - K(C_thetaV))) > R(0) ? 1 : 0)) * (a_vInfty - Y(S_v))) / a_tauVMinus) - (((((Y(S_u) - K(C_thetaV))) > R(0) ? 1 : 0) * Y(S_v)) / K(C_tauVPlus)));
+    dydt[S_w] = ((((R(1.0) - (((Y(S_u) - K(C_thetaW))) > R(0) ? 1 : 0)) * (a_wInfty - Y(S_w))) / a_tauWMinus) - (((((Y(S_u) - K(C_thetaW))) > R(0) ? 1 : 0) * Y(S_w)) / K(C_tauWPlus)));
+    dydt[S_s] = ((((R(1.0) + cfg_tanh((K(C_kS) * (Y(S_u) - K(C_uS))))) / R(2.0)) - Y(S_s)) / a_tauS);
+    R a_Istim = R(cfg_stimulus_current<double>(t, stim));
+    if (SOLVE_VM) {
+        dydt[S_u] = ((-a_Jion) - a_Istim);
+    }
+    return a_Jion;
+}
+
+// Ionic current after the step (computeVariables at tEnd).
+template <class R, bool SOLVE_VM, class YS, class KS>
+__device__ __forceinline__ R iion(double t, const YS& Y, const KS& K, int tissue, const CfgStimulus& stim)
+{
+    (void)tissue; (void)stim; (void)t;
+    R dydt[NS];
+    R a_tauSo = (K(C_tauSo1) + (((K(C_tauSo2) - K(C_tauSo1)) * (R(1.0) + cfg_tanh((K(C_kSo) * (Y(S_u) - K(C_uSo)))))) / R(2.0)));
+    R a_tauO = (((R(1.0) - (((Y(S_u) - K(C_thetaO))) > R(0) ? 1 : 0)) * K(C_tauO1)) + ((((Y(S_u) - K(C_thetaO))) > R(0) ? 1 : 0) * K(C_tauO2)));
+    R a_Jfi = (((((-Y(S_v)) * (((Y(S_u) - K(C_thetaV))) > R(0) ? 1 : 0)) * (Y(S_u) - K(C_thetaV))) * (K(C_uU) - Y(S_u))) / K(C_tauFi));
+    R a_Jso = ((((Y(S_u) - K(C_uO)) * (R(1.0) - (((Y(S_u) - K(C_thetaW))) > R(0) ? 1 : 0))) / a_tauO) + ((((Y(S_u) - K(C_thetaW))) > R(0) ? 1 : 0) / a_tauSo));
+    R a_Jsi = ((((-(((Y(S_u) - K(C_thetaW))) > R(0) ? 1 : 0)) * Y(S_w)) * Y(S_s)) / K(C_tauSi));
+    R a_Jion = ((a_Jfi + a_Jso) + a_Jsi);
+    R a_tauVMinus = (((R(1.0) - (((Y(S_u) - K(C_thetaVMinus))) > R(0) ? 1 : 0)) * K(C_tauV1Minus)) + ((((Y(S_u) - K(C_thetaVMinus))) > R(0) ? 1 : 0) * K(C_tauV2Minus)));
+    R a_tauWMinus = (K(C_tauW1Minus) + (((K(C_tauW2Minus) - K(C_tauW1Minus)) * (R(1.0) + cfg_tanh((K(C_kWMinus) * (Y(S_u) - K(C_uWMinus)))))) / R(2.0)));
+    R a_tauS = (((R(1.0) - (((Y(S_u) - K(C_thetaW))) > R(0) ? 1 : 0)) * K(C_tauS1)) + ((((Y(S_u) - K(C_thetaW))) > R(0) ? 1 : 0) * K(C_tauS2)));
+    R a_vInfty = (((K(C_thetaVMinus) - Y(S_u))) > R(0) ? 1 : 0);
+    R a_wInfty = (((R(1.0) - (((Y(S_u) - K(C_thetaO))) > R(0) ? 1 : 0)) * (R(1.0) - (Y(S_u) / K(C_tauWInfty)))) + ((((Y(S_u) - K(C_thetaO))) > R(0) ? 1 : 0) * K(C_wInftyStar)));
+    dydt[S_v] = ((((R(1.0) - (((Y(S_u) - K(C_thetaV))) > R(0) ? 1 : 0)) * (a_vInfty - Y(S_v))) / a_tauVMinus) - (((((Y(S_u) - K(C_thetaV))) > R(0) ? 1 : 0) * Y(S_v)) / K(C_tauVPlus)));
+    dydt[S_w] = ((((R(1.0) - (((Y(S_u) - K(C_thetaW))) > R(0) ? 1 : 0)) * (a_wInfty - Y(S_w))) / a_tauWMinus) - (((((Y(S_u) - K(C_thetaW))) > R(0) ? 1 : 0) * Y(S_w)) / K(C_tauWPlus)));
+    dydt[S_s] = ((((R(1.0) + cfg_tanh((K(C_kS) * (Y(S_u) - K(C_uS))))) / R(2.0)) - Y(S_s)) / a_tauS);
+    R a_Istim = R(cfg_stimulus_current<double>(t, stim));
+    if (SOLVE_VM) {
+        dydt[S_u] = ((-a_Jion) - a_Istim);
+    }
+    (void)dydt;
+    return a_Jion;
+}
+
+// traits bundle used by the kernel templates
+struct Model {
+    static constexpr int NS = buenoorovio::NS, NC = buenoorovio::NC;
+    static constexpr unsigned long long WIDE_MASK = buenoorovio::WIDE_MASK;
+    static constexpr double IION_SCALE = buenoorovio::IION_SCALE;
+    static constexpr double TIME_SCALE = buenoorovio::TIME_SCALE;
+    static constexpr int VM_MAP = buenoorovio::VM_MAP;
+    CFG_HD static __forceinline__ void init(double* C, double* y, int tissue, const double* scale) { init_consts(C, y, tissue, scale); }
+    template <class R, bool SV, class YS, class KS>
+    __device__ static __forceinline__ R rates(double t, const YS& Y, const KS& K, R* dydt, int tissue, const CfgStimulus& st) { return rhs<R, SV>(t, Y, K, dydt, tissue, st); }
+    template <class R, bool SV, class YS, class KS>
+    __device__ static __forceinline__ R current(double t, const YS& Y, const KS& K, int tissue, const CfgStimulus& st) { return iion<R, SV>(t, Y, K, tissue, st); }
+};
+
+} }  // namespace cfg::buenoorovio

@@ -1,0 +1,500 @@
+// cfg_monodomain_*: MyocardiumDomain + MonodomainSolver on one GPU
+// (src/electroModels/electroDomains/myocardiumDomain/myocardiumDomain.C:180-529,
+//  src/electroModels/myocardiumModels/monodomainSolver/monodomainSolver.C:39-150).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "diffusion_kernels.cuh"
+#include "host_common.h"
+#include "ionic_host.h"
+#include "monodomain_host.h"
+
+namespace cfg {
+
+__global__ void k_step_begin(DiffusionArgs a);
+__global__ void k_solve_begin(DiffusionArgs a);
+__global__ void k_solve_norm(DiffusionArgs a);
+__global__ void k_pcg_p(DiffusionArgs a);
+__global__ void k_pcg_update(DiffusionArgs a);
+__global__ void k_activation(DiffusionArgs a);
+__global__ void k_explicit(DiffusionArgs a);
+__global__ void k_explicit_finish(PcgState* st, int ddt_backward);
+
+static void md_free(cfg_monodomain* md)
+{
+    if (!md) return;
+    if (md->graph_exec) cudaGraphExecDestroy(md->graph_exec);
+    for (cudaEvent_t& e : md->ev)
+        if (e) cudaEventDestroy(e);
+    if (md->ion) ionic_free(md->ion);
+    dfree(md->d_col); dfree(md->d_coef); dfree(md->d_cnt); dfree(md->d_lapdiag);
+    dfree(md->d_vol); dfree(md->d_vm); dfree(md->d_vm_old); dfree(md->d_vm_oldold);
+    dfree(md->d_iion); dfree(md->d_act); dfree(md->d_act_flag); dfree(md->d_box);
+    dfree(md->d_diag); dfree(md->d_rD); dfree(md->d_b); dfree(md->d_r); dfree(md->d_z);
+    dfree(md->d_ax); dfree(md->d_sumA); dfree(md->d_pA); dfree(md->d_pB); dfree(md->d_ap);
+    dfree(md->d_partial); dfree(md->d_st);
+    if (md->h_st) cudaFreeHost(md->h_st);
+    if (md->stream) cudaStreamDestroy(md->stream);
+    delete md;
+}
+
+// lduAddressing -> ELL rows with neighbours in ascending order (the order in
+// which lduMatrix::Amul's face loop reaches a row for upper-triangular face
+// ordering); lapdiag = sum of -coef in that order (fvMatrix::negSumDiag).
+static int build_operator(cfg_monodomain* md, const cfg_mesh_desc* m, const double* sigma)
+{
+    const long long n = m->n_cells, nf = m->n_faces;
+    // face coefficients: given, or deltaCoeffs * (Sf.sigma.Sf)/|Sf| for the
+    // uniform conductivity (gaussLaplacianScheme, fvmLaplacianUncorrected)
+    std::vector<double> fc;
+    const double* coeff = m->face_coeff;
+    if (!coeff) {
+        if (!m->face_sf || !m->face_delta_coeffs)
+            return fail(CFG_ERR_INVALID, "mesh needs face_coeff or face_sf + face_delta_coeffs");
+        fc.resize(size_t(nf));
+        const double* s = sigma;
+        for (long long f = 0; f < nf; ++f) {
+            const double* S = m->face_sf + 3 * f;
+            const double magSf = std::sqrt(S[0] * S[0] + S[1] * S[1] + S[2] * S[2]);
+            const double g0 = S[0] * s[0] + S[1] * s[1] + S[2] * s[2];
+            const double g1 = S[0] * s[1] + S[1] * s[3] + S[2] * s[4];
+            const double g2 = S[0] * s[2] + S[1] * s[4] + S[2] * s[5];
+            const double sfgsn = (g0 * S[0] + g1 * S[1] + g2 * S[2]) / magSf;
+            fc[size_t(f)] = m->face_delta_coeffs[f] * sfgsn;
+        }
+        coeff = fc.data();
+    }
+    std::vector<std::vector<std::pair<int, double>>> rows(static_cast<size_t>(n));
+    for (long long f = 0; f < nf; ++f) {
+        const int l = m->owner[f], u = m->neighbour[f];
+        if (l < 0 || u < 0 || l >= n || u >= n || l == u)
+            return fail(CFG_ERR_INVALID, "face %lld has invalid owner/neighbour %d/%d", f, l, u);
+        rows[size_t(l)].push_back({u, coeff[f]});
+        rows[size_t(u)].push_back({l, coeff[f]});
+    }
+    int width = 0;
+    for (auto& r : rows) {
+        std::stable_sort(r.begin(), r.end(),
+                         [](const std::pair<int, double>& a, const std::pair<int, double>& b) {
+                             return a.first < b.first;
+                         });
+        width = std::max(width, int(r.size()));
+    }
+    if (width > 255) return fail(CFG_ERR_INVALID, "cell with more than 255 faces");
+    md->width = width;
+    std::vector<int> col(size_t(width) * n, 0);
+    std::vector<double> coef(size_t(width) * n, 0.0);
+    std::vector<unsigned char> cnt(static_cast<size_t>(n));
+    std::vector<double> lapdiag(static_cast<size_t>(n));
+    for (long long c = 0; c < n; ++c) {
+        const auto& r = rows[size_t(c)];
+        cnt[size_t(c)] = (unsigned char)r.size();
+        double s = 0.0;
+        for (size_t q = 0; q < r.size(); ++q) {
+            col[q * n + c] = r[q].first;
+            coef[q * n + c] = r[q].second;
+            s -= r[q].second;
+        }
+        lapdiag[size_t(c)] = s;
+    }
+    // structured block with one coefficient per direction: stencil form
+    md->sx = md->sy = md->sz = 0;
+    if (m->structured[0] > 0 && (long long)m->structured[0] * m->structured[1] * m->structured[2] == n) {
+        const long long nx = m->structured[0], ny = m->structured[1];
+        double cdir[3] = {0, 0, 0};
+        bool ok = true, seen[3] = {false, false, false};
+        for (long long f = 0; f < nf && ok; ++f) {
+            const long long l = m->owner[f], u = m->neighbour[f], d = u - l;
+            const int dir = d == 1 ? 0 : d == nx ? 1 : d == nx * ny ? 2 : -1;
+            if (dir < 0) { ok = false; break; }
+            if (!seen[dir]) { cdir[dir] = coeff[f]; seen[dir] = true; }
+            else if (std::fabs(coeff[f] - cdir[dir]) > 1e-12 * std::fabs(cdir[dir])) ok = false;
+        }
+        if (ok) {
+            md->sx = m->structured[0]; md->sy = m->structured[1]; md->sz = m->structured[2];
+            md->cx = cdir[0]; md->cy = cdir[1]; md->cz = cdir[2];
+        }
+    }
+    CFG_CUDA_TRY(dmalloc(&md->d_col, col.size()));
+    CFG_CUDA_TRY(dmalloc(&md->d_coef, coef.size()));
+    CFG_CUDA_TRY(dmalloc(&md->d_cnt, cnt.size()));
+    CFG_CUDA_TRY(dmalloc(&md->d_lapdiag, lapdiag.size()));
+    CFG_CUDA_TRY(cudaMemcpy(md->d_col, col.data(), col.size() * sizeof(int), cudaMemcpyHostToDevice));
+    CFG_CUDA_TRY(cudaMemcpy(md->d_coef, coef.data(), coef.size() * sizeof(double),
+                            cudaMemcpyHostToDevice));
+    CFG_CUDA_TRY(cudaMemcpy(md->d_cnt, cnt.data(), cnt.size(), cudaMemcpyHostToDevice));
+    CFG_CUDA_TRY(cudaMemcpy(md->d_lapdiag, lapdiag.data(), lapdiag.size() * sizeof(double),
+                            cudaMemcpyHostToDevice));
+    md->ell_bytes = col.size() * sizeof(int) + coef.size() * sizeof(double) + cnt.size();
+    md->nnz_offdiag = 2 * nf;
+    return CFG_OK;
+}
+
+static void fill_args(cfg_monodomain* md, double dt)
+{
+    DiffusionArgs& a = md->args;
+    a = DiffusionArgs{};
+    a.n = md->n;
+    a.width = md->width;
+    a.ell_col = md->d_col;
+    a.ell_coef = md->d_coef;
+    a.ell_cnt = md->d_cnt;
+    a.lapdiag = md->d_lapdiag;
+    a.vol = md->d_vol;
+    a.sx = md->use_stencil ? md->sx : 0;
+    a.sy = md->sy;
+    a.sz = md->sz;
+    a.cx = md->cx; a.cy = md->cy; a.cz = md->cz;
+    a.vm = md->d_vm;
+    a.vm_old = md->d_vm_old;
+    a.vm_oldold = md->d_vm_oldold;
+    a.iion = md->d_iion;
+    a.act = md->d_act;
+    a.act_flag = md->d_act_flag;
+    a.box_mask = md->d_box;
+    a.n_boxes = md->n_boxes;
+    for (int b = 0; b < md->n_boxes; ++b) {
+        a.box_start[b] = md->box_start[b];
+        a.box_end[b] = md->box_start[b] + md->box_duration[b];   // tStart + duration
+        a.box_intensity[b] = md->box_intensity[b];
+    }
+    a.diag = md->d_diag; a.rD = md->d_rD; a.b = md->d_b; a.r = md->d_r; a.z = md->d_z;
+    a.ax = md->d_ax; a.sumA = md->d_sumA; a.pA = md->d_pA; a.pB = md->d_pB; a.ap = md->d_ap;
+    a.partial = md->d_partial;
+    a.nblocks = int((md->n + kDiffBlock - 1) / kDiffBlock);
+    a.st = md->d_st;
+    a.dt = dt;
+    a.chicm = md->chicm;
+    a.ddt_backward = md->ddt_backward;
+}
+
+int monodomain_create(const cfg_monodomain_desc* d, const cfg_mesh_desc* m, cfg_monodomain** out)
+{
+    if (!d || !m || !out) return fail(CFG_ERR_INVALID, "null argument");
+    *out = nullptr;
+    if (m->n_cells <= 0) return fail(CFG_ERR_INVALID, "mesh has no cells");
+    if (d->ionic.n_cells != m->n_cells)
+        return fail(CFG_ERR_INVALID, "ionic model has %lld integration points, mesh %lld cells",
+                    d->ionic.n_cells, m->n_cells);
+    if (d->ionic.solve_vm_within_ode)
+        return fail(CFG_ERR_INVALID, "the tissue step needs solveVmWithinODESolver false");
+    if (!m->owner || !m->neighbour || !m->volumes || (d->n_boxes && !m->centres))
+        return fail(CFG_ERR_INVALID, "incomplete mesh description");
+    if (d->n_boxes < 0 || d->n_boxes > 8) return fail(CFG_ERR_INVALID, "at most 8 stimulus boxes");
+    if (!(d->chi > 0) || !(d->cm > 0)) return fail(CFG_ERR_INVALID, "chi and cm must be positive");
+    {
+        const IonicModelOps* im = nullptr;
+        int flag = 0;
+        if (int rc = ionic_validate(&d->ionic, &im, &flag)) return rc;
+    }
+
+    cfg_monodomain* md = new cfg_monodomain();
+    auto bail = [&](int rc) {
+        md_free(md);
+        return rc;
+    };
+    if (cudaStreamCreateWithFlags(&md->stream, cudaStreamNonBlocking) != cudaSuccess)
+        return bail(fail(CFG_ERR_CUDA, "stream creation failed"));
+    int rc = ionic_create(&d->ionic, md->stream, &md->ion);
+    if (rc) return bail(rc);
+    md->n = m->n_cells;
+    md->implicit = d->implicit != 0;
+    md->ddt_backward = d->ddt_backward != 0;
+    md->chicm = d->chi * d->cm;   // chi*Cm evaluated first (monodomainSolver.C:129)
+    md->n_boxes = d->n_boxes;
+    for (int b = 0; b < d->n_boxes; ++b) {
+        md->box_start[b] = d->box_start[b];
+        md->box_duration[b] = d->box_duration[b];
+        md->box_intensity[b] = d->box_intensity[b];
+        for (int k = 0; k < 3; ++k) {
+            md->box_min[b][k] = d->box_min[b][k];
+            md->box_max[b][k] = d->box_max[b][k];
+        }
+    }
+    if ((rc = build_operator(md, m, d->conductivity))) return bail(rc);
+    md->use_stencil = md->sx > 0;
+    const size_t n = size_t(md->n);
+    cudaError_t e = cudaSuccess;
+    double** vecs[] = {&md->d_vol, &md->d_vm, &md->d_vm_old, &md->d_vm_oldold, &md->d_iion,
+                       &md->d_act, &md->d_diag, &md->d_rD, &md->d_b, &md->d_r, &md->d_z,
+                       &md->d_ax, &md->d_sumA, &md->d_pA, &md->d_pB, &md->d_ap};
+    for (double** v : vecs)
+        if (!e) e = dmalloc(v, n);
+    const int nblocks = int((n + kDiffBlock - 1) / kDiffBlock);
+    if (!e) e = dmalloc(&md->d_partial, size_t(4) * nblocks);
+    if (!e) e = dmalloc(&md->d_act_flag, n);
+    if (!e) e = dmalloc(&md->d_st, 1);
+    if (!e) e = cudaMallocHost(reinterpret_cast<void**>(&md->h_st), sizeof(PcgState));
+    if (e) return bail(fail(CFG_ERR_CUDA, "device allocation failed: %s", cudaGetErrorString(e)));
+    // box membership (boundBox::contains is inclusive)
+    md->h_box.assign(n, 0);
+    for (size_t c = 0; c < n; ++c)
+        for (int b = 0; b < d->n_boxes; ++b) {
+            const double* p = m->centres + 3 * c;
+            bool in = true;
+            for (int k = 0; k < 3; ++k)
+                in = in && p[k] >= d->box_min[b][k] && p[k] <= d->box_max[b][k];
+            if (in) md->h_box[c] |= (unsigned char)(1u << b);
+        }
+    if (d->n_boxes) {
+        if (dmalloc(&md->d_box, n) != cudaSuccess)
+            return bail(fail(CFG_ERR_CUDA, "device allocation failed"));
+        cudaMemcpy(md->d_box, md->h_box.data(), n, cudaMemcpyHostToDevice);
+    }
+    std::vector<double> vm0(n, d->vm0);
+    e = cudaMemcpy(md->d_vol, m->volumes, n * sizeof(double), cudaMemcpyHostToDevice);
+    if (!e) e = cudaMemcpy(md->d_vm, vm0.data(), n * sizeof(double), cudaMemcpyHostToDevice);
+    if (!e) e = cudaMemcpy(md->d_vm_old, vm0.data(), n * sizeof(double), cudaMemcpyHostToDevice);
+    if (!e) e = cudaMemcpy(md->d_vm_oldold, vm0.data(), n * sizeof(double), cudaMemcpyHostToDevice);
+    if (!e) e = cudaMemset(md->d_iion, 0, n * sizeof(double));
+    if (!e) e = cudaMemset(md->d_act, 0, n * sizeof(double));
+    if (!e) e = cudaMemset(md->d_act_flag, 1, n);
+    if (!e) e = cudaMemset(md->d_partial, 0, sizeof(double) * 4 * nblocks);
+    PcgState st{};
+    st.n_old = 0;
+    st.tol = d->pcg_tol;
+    st.rel_tol = d->pcg_rel_tol;
+    st.max_iter = d->pcg_max_iter > 0 ? d->pcg_max_iter : 1000;
+    st.n_outer = d->n_outer > 0 ? d->n_outer : 1;
+    st.outer_tol = d->outer_tol;
+    if (!e) e = cudaMemcpy(md->d_st, &st, sizeof st, cudaMemcpyHostToDevice);
+    if (e) return bail(fail(CFG_ERR_CUDA, "device initialisation failed: %s", cudaGetErrorString(e)));
+    *out = md;
+    return CFG_OK;
+}
+
+static int read_state(cfg_monodomain* md)
+{
+    CFG_CUDA_TRY(cudaMemcpyAsync(md->h_st, md->d_st, sizeof(PcgState), cudaMemcpyDeviceToHost,
+                                 md->stream));
+    CFG_CUDA_TRY(cudaStreamSynchronize(md->stream));
+    return CFG_OK;
+}
+
+// Enqueue the work of one time step.  With `host_control` the PIMPLE and PCG
+// loops are driven from the host by reading the device state; otherwise a
+// fixed sequence is enqueued whose surplus kernels return at once.
+int enqueue_step(cfg_monodomain* md, double dt, bool host_control)
+{
+    long long launches = 0;
+    struct Count {
+        cfg_monodomain* m;
+        long long& n;
+        ~Count() { if (m->timing) m->timed_launches += n; }
+    } counter{md, launches};
+    fill_args(md, dt);
+    const DiffusionArgs& a = md->args;
+    const unsigned grid = unsigned(a.nblocks);
+    cudaStream_t s = md->stream;
+    k_step_begin<<<grid, kDiffBlock, 0, s>>>(a);
+    CFG_CUDA_TRY(cudaGetLastError());
+    if (md->timing) CFG_CUDA_TRY(cudaEventRecord(md->ev[0], s));
+    IonicLaunch L = ionic_launch_args(md->ion, 0.0, dt, &md->d_st->t0, md->d_vm, md->d_iion);
+    CFG_CUDA_TRY(ionic_enqueue(md->ion, L));
+    launches += 2;
+    if (md->timing) CFG_CUDA_TRY(cudaEventRecord(md->ev[1], s));
+    if (!md->implicit) {
+        k_explicit<<<grid, kDiffBlock, 0, s>>>(a);
+        k_explicit_finish<<<1, 1, 0, s>>>(md->d_st, md->ddt_backward);
+        launches += 2;
+        CFG_CUDA_TRY(cudaGetLastError());
+        if (md->timing) CFG_CUDA_TRY(cudaEventRecord(md->ev[2], s));
+        return CFG_OK;
+    }
+    if (host_control) {
+        for (int corr = 0; corr < 1000000; ++corr) {
+            k_solve_begin<<<grid, kDiffBlock, 0, s>>>(a);
+            k_solve_norm<<<grid, kDiffBlock, 0, s>>>(a);
+            launches += 2;
+            CFG_CUDA_TRY(cudaGetLastError());
+            int rc = read_state(md);
+            if (rc) return rc;
+            while (md->h_st->solve_active) {
+                for (int k = 0; k < md->iter_chunk; ++k) {
+                    k_pcg_p<<<grid, kDiffBlock, 0, s>>>(a);
+                    k_pcg_update<<<grid, kDiffBlock, 0, s>>>(a);
+                }
+                launches += 2 * md->iter_chunk;
+                CFG_CUDA_TRY(cudaGetLastError());
+                if ((rc = read_state(md))) return rc;
+            }
+            if (!md->h_st->outer_active) break;
+        }
+    } else {
+        for (int corr = 0; corr < md->graph_max_corr; ++corr) {
+            k_solve_begin<<<grid, kDiffBlock, 0, s>>>(a);
+            k_solve_norm<<<grid, kDiffBlock, 0, s>>>(a);
+            for (int k = 0; k < md->graph_max_iter; ++k) {
+                k_pcg_p<<<grid, kDiffBlock, 0, s>>>(a);
+                k_pcg_update<<<grid, kDiffBlock, 0, s>>>(a);
+            }
+        }
+        CFG_CUDA_TRY(cudaGetLastError());
+    }
+    k_activation<<<grid, kDiffBlock, 0, s>>>(a);
+    launches += 1;
+    CFG_CUDA_TRY(cudaGetLastError());
+    if (md->timing) CFG_CUDA_TRY(cudaEventRecord(md->ev[2], s));
+    return CFG_OK;
+}
+
+int check_step(cfg_monodomain* md)
+{
+    int rc = read_state(md);
+    if (rc) return rc;
+    if (md->timing) {
+        float a = 0, b = 0;
+        CFG_CUDA_TRY(cudaEventElapsedTime(&a, md->ev[0], md->ev[1]));
+        CFG_CUDA_TRY(cudaEventElapsedTime(&b, md->ev[1], md->ev[2]));
+        md->ionic_ms += a;
+        md->diffusion_ms += b;
+        md->timed_steps++;
+    }
+    if ((rc = ionic_check_status(md->ion))) return rc;
+    if (md->implicit && (md->h_st->outer_active || md->h_st->solve_active))
+        return fail(CFG_ERR_PCG, "PIMPLE/PCG loop did not finish within the launched sequence");
+    return CFG_OK;
+}
+
+}  // namespace cfg
+
+using namespace cfg;
+
+extern "C" {
+
+int cfg_monodomain_create(const cfg_monodomain_desc* desc, const cfg_mesh_desc* mesh,
+                          cfg_monodomain** out)
+{
+    clear_error();
+    return monodomain_create(desc, mesh, out);
+}
+
+int cfg_monodomain_step(cfg_monodomain* md, double dt)
+{
+    if (!md) return fail(CFG_ERR_INVALID, "null context");
+    if (!(dt > 0)) return fail(CFG_ERR_INVALID, "deltaT must be positive");
+    int rc = enqueue_step(md, dt, true);
+    if (rc) return rc;
+    md->t_host = md->t_host + dt;
+    md->steps++;
+    return check_step(md);
+}
+
+int cfg_monodomain_run(cfg_monodomain* md, double dt, long long n_steps)
+{
+    if (!md) return fail(CFG_ERR_INVALID, "null context");
+    for (long long i = 0; i < n_steps; ++i) {
+        int rc = cfg_monodomain_step(md, dt);
+        if (rc) return rc;
+    }
+    return CFG_OK;
+}
+
+int cfg_monodomain_get_field(cfg_monodomain* md, int field, double* host)
+{
+    if (!md || !host) return fail(CFG_ERR_INVALID, "null argument");
+    const size_t bytes = sizeof(double) * size_t(md->n);
+    const double* src = nullptr;
+    switch (field) {
+    case CFG_FIELD_VM: src = md->d_vm; break;
+    case CFG_FIELD_IION: src = md->d_iion; break;
+    case CFG_FIELD_ACTIVATION: src = md->d_act; break;
+    case CFG_FIELD_VM_OLD: src = md->d_vm_old; break;
+    case CFG_FIELD_SOURCE: {
+        // externalStimulusCurrent of the last step start
+        const double t0 = md->t_host - md->args.dt;
+        for (long long c = 0; c < md->n; ++c) {
+            double s = 0.0;
+            for (int b = 0; b < md->n_boxes; ++b) {
+                const double ts = md->box_start[b], te = ts + md->box_duration[b];
+                if (md->steps == 0 || t0 < ts || t0 > te) continue;
+                if (md->h_box[size_t(c)] & (1u << b)) s += md->box_intensity[b];
+            }
+            host[c] = s;
+        }
+        return CFG_OK;
+    }
+    default: return fail(CFG_ERR_INVALID, "unknown field %d", field);
+    }
+    CFG_CUDA_TRY(cudaMemcpyAsync(host, src, bytes, cudaMemcpyDeviceToHost, md->stream));
+    CFG_CUDA_TRY(cudaStreamSynchronize(md->stream));
+    return CFG_OK;
+}
+
+int cfg_monodomain_set_field(cfg_monodomain* md, int field, const double* host)
+{
+    if (!md || !host) return fail(CFG_ERR_INVALID, "null argument");
+    const size_t bytes = sizeof(double) * size_t(md->n);
+    if (field == CFG_FIELD_VM) {
+        CFG_CUDA_TRY(cudaMemcpyAsync(md->d_vm, host, bytes, cudaMemcpyHostToDevice, md->stream));
+        if (md->steps == 0) {
+            // no old-time level exists yet: the first access copies Vm
+            CFG_CUDA_TRY(cudaMemcpyAsync(md->d_vm_old, host, bytes, cudaMemcpyHostToDevice, md->stream));
+            CFG_CUDA_TRY(cudaMemcpyAsync(md->d_vm_oldold, host, bytes, cudaMemcpyHostToDevice, md->stream));
+        }
+    } else if (field == CFG_FIELD_ACTIVATION) {
+        CFG_CUDA_TRY(cudaMemcpyAsync(md->d_act, host, bytes, cudaMemcpyHostToDevice, md->stream));
+    } else {
+        return fail(CFG_ERR_INVALID, "field %d cannot be set", field);
+    }
+    CFG_CUDA_TRY(cudaStreamSynchronize(md->stream));
+    return CFG_OK;
+}
+
+double cfg_monodomain_time(const cfg_monodomain* md) { return md ? md->t_host : 0.0; }
+
+cfg_ionic* cfg_monodomain_ionic(cfg_monodomain* md) { return md ? md->ion : nullptr; }
+
+int cfg_monodomain_last_stats(const cfg_monodomain* md, cfg_step_stats* s)
+{
+    if (!md || !s) return fail(CFG_ERR_INVALID, "null argument");
+    cfg_monodomain* m = const_cast<cfg_monodomain*>(md);
+    int rc = read_state(m);
+    if (rc) return rc;
+    std::memset(s, 0, sizeof *s);
+    s->n_solves = m->h_st->n_solves;
+    for (int k = 0; k < std::min(s->n_solves, 16); ++k) {
+        s->iterations[k] = m->h_st->iters[k];
+        s->initial_residual[k] = m->h_st->init_r[k];
+        s->final_residual[k] = m->h_st->final_r[k];
+    }
+    return CFG_OK;
+}
+
+int cfg_monodomain_set_timing(cfg_monodomain* md, int enable)
+{
+    if (!md) return fail(CFG_ERR_INVALID, "null context");
+    for (cudaEvent_t& e : md->ev)
+        if (!e) CFG_CUDA_TRY(cudaEventCreate(&e));
+    md->timing = enable != 0;
+    md->ionic_ms = md->diffusion_ms = 0.0;
+    md->timed_steps = 0;
+    md->timed_launches = 0;
+    return CFG_OK;
+}
+
+int cfg_monodomain_timings(const cfg_monodomain* md, double* ionic_ms, double* diffusion_ms,
+                           long long* steps, long long* kernel_launches)
+{
+    if (!md) return fail(CFG_ERR_INVALID, "null context");
+    if (ionic_ms) *ionic_ms = md->ionic_ms;
+    if (diffusion_ms) *diffusion_ms = md->diffusion_ms;
+    if (steps) *steps = md->timed_steps;
+    if (kernel_launches) *kernel_launches = md->timed_launches;
+    return CFG_OK;
+}
+
+void* cfg_monodomain_stream(cfg_monodomain* md) { return md ? (void*)md->stream : nullptr; }
+
+int cfg_monodomain_destroy(cfg_monodomain* md)
+{
+    if (md) {
+        cudaStreamSynchronize(md->stream);
+        md_free(md);
+    }
+    return CFG_OK;
+}
+
+}  // extern "C"

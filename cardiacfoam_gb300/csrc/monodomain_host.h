@@ -1,0 +1,61 @@
+// Host representation of a GPU monodomain context.
+#pragma once
+
+#include <vector>
+
+#include "diffusion_kernels.cuh"
+#include "host_common.h"
+
+struct cfg_monodomain {
+    cfg_ionic* ion = nullptr;
+    long long n = 0;
+    int width = 0;
+    size_t ell_bytes = 0;
+    long long nnz_offdiag = 0;
+    // structured stencil form
+    int sx = 0, sy = 0, sz = 0;
+    double cx = 0, cy = 0, cz = 0;
+    bool use_stencil = false;
+    // settings
+    bool implicit = true, ddt_backward = true;
+    double chicm = 0;
+    int n_boxes = 0;
+    double box_min[8][3], box_max[8][3], box_start[8], box_duration[8], box_intensity[8];
+    std::vector<unsigned char> h_box;
+    // device operator and fields
+    int* d_col = nullptr;
+    double* d_coef = nullptr;
+    unsigned char* d_cnt = nullptr;
+    double* d_lapdiag = nullptr;
+    double* d_vol = nullptr;
+    double *d_vm = nullptr, *d_vm_old = nullptr, *d_vm_oldold = nullptr, *d_iion = nullptr;
+    double* d_act = nullptr;
+    unsigned char* d_act_flag = nullptr;
+    unsigned char* d_box = nullptr;
+    // PCG work
+    double *d_diag = nullptr, *d_rD = nullptr, *d_b = nullptr, *d_r = nullptr, *d_z = nullptr,
+           *d_ax = nullptr, *d_sumA = nullptr, *d_pA = nullptr, *d_pB = nullptr, *d_ap = nullptr;
+    double* d_partial = nullptr;
+    cfg::PcgState* d_st = nullptr;
+    cfg::PcgState* h_st = nullptr;   // pinned mirror
+    cfg::DiffusionArgs args{};
+    // control
+    cudaStream_t stream = nullptr;
+    int iter_chunk = 2;
+    int graph_max_corr = 4, graph_max_iter = 4;
+    cudaGraphExec_t graph_exec = nullptr;
+    double t_host = 0.0;
+    long long steps = 0;
+    // phase timing
+    bool timing = false;
+    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+    double ionic_ms = 0.0, diffusion_ms = 0.0;
+    long long timed_steps = 0;
+    long long timed_launches = 0;
+};
+
+namespace cfg {
+int monodomain_create(const cfg_monodomain_desc* d, const cfg_mesh_desc* m, cfg_monodomain** out);
+int enqueue_step(cfg_monodomain* md, double dt, bool host_control);
+int check_step(cfg_monodomain* md);
+}  // namespace cfg

@@ -1,0 +1,161 @@
+"""ctypes bindings of the C ABI in include/cardiac_gpu.h.
+
+The shared library is built in-tree by :func:`cardiacfoam_gb300.build.build`.
+There is no CPU fallback: every entry point runs on the GPU, and loading
+fails loudly when the library is missing.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+from typing import Optional
+
+import numpy as np
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = PKG / "libcardiac_gpu.so"
+
+CFG_OK = 0
+CFG_ERR_INVALID = 1
+CFG_ERR_CUDA = 2
+CFG_ERR_ODE_STEPS = 4
+CFG_ERR_NONFINITE = 8
+CFG_ERR_PCG = 16
+CFG_ERR_UNSUPPORTED = 32
+PRECISION_FP64 = 0
+PRECISION_MIXED = 1
+FIELD_VM, FIELD_IION, FIELD_ACTIVATION, FIELD_SOURCE, FIELD_VM_OLD = range(5)
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+_up = C.POINTER(C.c_ubyte)
+
+
+class CfgError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[{code}] {msg}")
+        self.code = code
+
+
+class OdeDesc(C.Structure):
+    _fields_ = [("solver", C.c_char_p), ("abs_tol", C.c_double), ("rel_tol", C.c_double),
+                ("max_steps", C.c_longlong), ("safe_scale", C.c_double),
+                ("min_scale", C.c_double), ("max_scale", C.c_double),
+                ("alpha_increase", C.c_double), ("alpha_decrease", C.c_double)]
+
+
+class StimulusDesc(C.Structure):
+    _fields_ = [("stim_start", C.c_double), ("stim_period_s1", C.c_double),
+                ("stim_duration", C.c_double), ("stim_amplitude", C.c_double),
+                ("nstim1", C.c_int), ("stim_period_s2", C.c_double), ("nstim2", C.c_int)]
+
+
+class IonicDesc(C.Structure):
+    _fields_ = [("ionic_model", C.c_char_p), ("tissue", C.c_char_p), ("n_cells", C.c_longlong),
+                ("initial_delta_t", C.c_double), ("solve_vm_within_ode", C.c_int),
+                ("precision", C.c_int), ("ode", OdeDesc), ("stimulus", StimulusDesc),
+                ("tissue_per_cell", _up), ("scales", _dp)]
+
+
+class MeshDesc(C.Structure):
+    _fields_ = [("n_cells", C.c_longlong), ("n_faces", C.c_longlong), ("owner", _ip),
+                ("neighbour", _ip), ("volumes", _dp), ("centres", _dp), ("face_coeff", _dp),
+                ("face_sf", _dp), ("face_delta_coeffs", _dp), ("structured", C.c_int * 3)]
+
+
+class MonodomainDesc(C.Structure):
+    _fields_ = [("ionic", IonicDesc), ("conductivity", C.c_double * 6), ("chi", C.c_double),
+                ("cm", C.c_double),
+                ("implicit", C.c_int), ("ddt_backward", C.c_int), ("pcg_tol", C.c_double),
+                ("pcg_rel_tol", C.c_double), ("pcg_max_iter", C.c_int), ("n_outer", C.c_int),
+                ("outer_tol", C.c_double), ("vm0", C.c_double), ("n_boxes", C.c_int),
+                ("box_min", (C.c_double * 3) * 8), ("box_max", (C.c_double * 3) * 8),
+                ("box_start", C.c_double * 8), ("box_duration", C.c_double * 8),
+                ("box_intensity", C.c_double * 8)]
+
+
+class StepStats(C.Structure):
+    _fields_ = [("n_solves", C.c_int), ("iterations", C.c_int * 16),
+                ("initial_residual", C.c_double * 16), ("final_residual", C.c_double * 16)]
+
+
+# every symbol declared in include/cardiac_gpu.h
+EXPORTS = [
+    "cfg_last_error", "cfg_ionic_create", "cfg_ionic_solve", "cfg_ionic_solve_device",
+    "cfg_ionic_num_states", "cfg_ionic_state_name", "cfg_ionic_get_states",
+    "cfg_ionic_set_states", "cfg_ionic_get_steps", "cfg_ionic_rhs_evaluations",
+    "cfg_ionic_destroy", "cfg_monodomain_create", "cfg_monodomain_create_from_dict",
+    "cfg_monodomain_step", "cfg_monodomain_run", "cfg_monodomain_get_field",
+    "cfg_monodomain_set_field", "cfg_monodomain_time", "cfg_monodomain_ionic",
+    "cfg_monodomain_last_stats", "cfg_monodomain_set_timing", "cfg_monodomain_timings",
+    "cfg_monodomain_stream", "cfg_monodomain_destroy",
+]
+
+_lib = None
+
+
+def load(path: Optional[os.PathLike] = None):
+    """Load libcardiac_gpu.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise RuntimeError(f"{p} is missing: build it with cardiacfoam_gb300.build.build() "
+                           "(the GPU path has no CPU fallback)")
+    L = C.CDLL(str(p))
+    L.cfg_last_error.restype = C.c_char_p
+    L.cfg_ionic_create.argtypes = [C.POINTER(IonicDesc), C.POINTER(C.c_void_p)]
+    L.cfg_ionic_solve.argtypes = [C.c_void_p, C.c_double, C.c_double, _dp, _dp]
+    L.cfg_ionic_solve_device.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_void_p,
+                                         C.c_void_p]
+    L.cfg_ionic_num_states.argtypes = [C.c_void_p, _ip]
+    L.cfg_ionic_state_name.argtypes = [C.c_void_p, C.c_int, C.c_char_p, C.c_size_t]
+    L.cfg_ionic_get_states.argtypes = [C.c_void_p, _dp]
+    L.cfg_ionic_set_states.argtypes = [C.c_void_p, _dp]
+    L.cfg_ionic_get_steps.argtypes = [C.c_void_p, _dp]
+    L.cfg_ionic_rhs_evaluations.argtypes = [C.c_void_p, C.POINTER(C.c_ulonglong)]
+    L.cfg_ionic_destroy.argtypes = [C.c_void_p]
+    L.cfg_monodomain_create.argtypes = [C.POINTER(MonodomainDesc), C.POINTER(MeshDesc),
+                                        C.POINTER(C.c_void_p)]
+    L.cfg_monodomain_create_from_dict.argtypes = [C.c_char_p, C.POINTER(MeshDesc), C.c_double,
+                                                  C.c_int, C.POINTER(C.c_void_p)]
+    L.cfg_monodomain_step.argtypes = [C.c_void_p, C.c_double]
+    L.cfg_monodomain_run.argtypes = [C.c_void_p, C.c_double, C.c_longlong]
+    L.cfg_monodomain_get_field.argtypes = [C.c_void_p, C.c_int, _dp]
+    L.cfg_monodomain_set_field.argtypes = [C.c_void_p, C.c_int, _dp]
+    L.cfg_monodomain_time.argtypes = [C.c_void_p]
+    L.cfg_monodomain_time.restype = C.c_double
+    L.cfg_monodomain_ionic.argtypes = [C.c_void_p]
+    L.cfg_monodomain_ionic.restype = C.c_void_p
+    L.cfg_monodomain_last_stats.argtypes = [C.c_void_p, C.POINTER(StepStats)]
+    L.cfg_monodomain_set_timing.argtypes = [C.c_void_p, C.c_int]
+    L.cfg_monodomain_timings.argtypes = [C.c_void_p, _dp, _dp, C.POINTER(C.c_longlong),
+                                         C.POINTER(C.c_longlong)]
+    L.cfg_monodomain_stream.argtypes = [C.c_void_p]
+    L.cfg_monodomain_stream.restype = C.c_void_p
+    L.cfg_monodomain_destroy.argtypes = [C.c_void_p]
+    if path is None:
+        _lib = L
+    return L
+
+
+def check(rc: int):
+    if rc != CFG_OK:
+        raise CfgError(rc, load().cfg_last_error().decode())
+
+
+def dptr(a: np.ndarray):
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(_dp)
+
+
+def iptr(a: np.ndarray):
+    assert a.dtype == np.int32 and a.flags.c_contiguous
+    return a.ctypes.data_as(_ip)
+
+
+def uptr(a: np.ndarray):
+    assert a.dtype == np.uint8 and a.flags.c_contiguous
+    return a.ctypes.data_as(_up)

@@ -1,0 +1,211 @@
+/*
+ * cardiac_gpu.h - C ABI of the GB300 monodomain time step.
+ *
+ * A plain-C boundary (pointers, sizes, status codes; no C++ or torch types)
+ * that cardiacFoam's own C++ can call from a thin adapter, so that the
+ * electroProperties dictionary and the runtime selection tables stay as they
+ * are.  Every function returns CFG_OK (0) or a CFG_ERR_* code; the message of
+ * the last failure on the calling thread is available from cfg_last_error().
+ * A context is not re-entrant: one host thread and one CUDA stream per
+ * context (the reference is single-threaded per MPI rank).
+ *
+ * Units follow the reference: PDE fields in SI (Vm [V], Im [V/s], time [s],
+ * sources [A/m^3]); ionic model state in the model's own units.
+ */
+#ifndef CARDIAC_GPU_H
+#define CARDIAC_GPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+#define CFG_OK 0
+#define CFG_ERR_INVALID 1       /* bad argument, unknown model/tissue/key */
+#define CFG_ERR_CUDA 2          /* a CUDA call failed */
+#define CFG_ERR_ODE_STEPS 4     /* RKF45 exceeded maxSteps (ODESolver FatalError) */
+#define CFG_ERR_NONFINITE 8     /* a NaN/Inf ionic current was produced */
+#define CFG_ERR_PCG 16          /* PCG reached maxIter without converging */
+#define CFG_ERR_UNSUPPORTED 32  /* combination not built (e.g. solver other than RKF45) */
+
+#define CFG_PRECISION_FP64 0    /* plain form: FP64 throughout */
+#define CFG_PRECISION_MIXED 1   /* FP32 currents/gates, FP64 Vm/concentrations/PCG */
+
+/* Message of the last failure on this thread ("" when none). */
+const char* cfg_last_error(void);
+
+/* ------------------------------------------------------------ ionic model */
+
+/* ODESolver dictionary keys (solver, absTol, relTol, maxSteps) plus the
+ * adaptiveSolver keys; a negative value selects OpenFOAM's default. */
+typedef struct cfg_ode_desc {
+    const char* solver;          /* "RKF45" (NULL = "RKF45") */
+    double abs_tol;              /* default 1e-15 */
+    double rel_tol;              /* default 1e-4 */
+    long long max_steps;         /* default 10000 */
+    double safe_scale, min_scale, max_scale, alpha_increase, alpha_decrease;
+} cfg_ode_desc;
+
+/* singleCellStimulus sub-dictionary (StimulusProtocol, stimulusIO.H:32-53) */
+typedef struct cfg_stimulus_desc {
+    double stim_start, stim_period_s1, stim_duration, stim_amplitude;
+    int nstim1;
+    double stim_period_s2;
+    int nstim2;
+} cfg_stimulus_desc;
+
+typedef struct cfg_ionic_desc {
+    const char* ionic_model;          /* ionicModel key: TNNP ORd ToRORd_dynCl
+                                         AlievPanfilov BuenoOrovio */
+    const char* tissue;               /* tissue key: epicardialCells mCells
+                                         endocardialCells myocyte */
+    long long n_cells;                /* nIntegrationPoints */
+    double initial_delta_t;           /* initialDeltaT [s]; the reference uses it
+                                         as the first ODE step in ms */
+    int solve_vm_within_ode;          /* solveVmWithinODESolver */
+    int precision;                    /* CFG_PRECISION_* */
+    cfg_ode_desc ode;
+    cfg_stimulus_desc stimulus;       /* used only when solve_vm_within_ode */
+    const unsigned char* tissue_per_cell;  /* optional host [n] tissue flags */
+    const double* scales;             /* optional host [6][n] per-cell factors on
+                                         GNa GCaL GKr GKs GK1 Gto */
+} cfg_ionic_desc;
+
+typedef struct cfg_ionic cfg_ionic;
+
+/* ionicModel::New(dict, nIntegrationPoints, initialDeltaT,
+ * solveVmWithinODESolver) - src/ionicModels/ionicModel/ionicModel.C:76-94,
+ * including the tissue check of ionicSelector::selectTissue
+ * (ionicSelector.C:32-53). */
+int cfg_ionic_create(const cfg_ionic_desc* desc, cfg_ionic** out);
+
+/* ionicModel::solveODE(t0, dt, Vm, Im) - ionicModel.H:250-256 (e.g.
+ * TNNP.C:114-179) on HOST fields: copies Vm in and Im out. */
+int cfg_ionic_solve(cfg_ionic* ion, double t0, double dt, const double* vm, double* im);
+
+/* The same on device pointers, enqueued on the context's stream. */
+int cfg_ionic_solve_device(cfg_ionic* ion, double t0, double dt, const double* vm_dev,
+                           double* im_dev);
+
+/* Number of states and their names (ioNumStates/ioStateNames,
+ * ionicModel.H:115-168). */
+int cfg_ionic_num_states(const cfg_ionic* ion, int* n_states);
+int cfg_ionic_state_name(const cfg_ionic* ion, int index, char* buf, size_t len);
+
+/* State export/import as [n_states][n_cells] doubles (exportStates /
+ * importFields, ionicModel.H:584-638). */
+int cfg_ionic_get_states(cfg_ionic* ion, double* host_states);
+int cfg_ionic_set_states(cfg_ionic* ion, const double* host_states);
+/* Per-cell persistent ODE step (ionicModel::step(), ionicModel.H:244-247). */
+int cfg_ionic_get_steps(cfg_ionic* ion, double* host_steps);
+/* RHS evaluations since creation (work counter for the roofline). */
+int cfg_ionic_rhs_evaluations(const cfg_ionic* ion, unsigned long long* count);
+int cfg_ionic_destroy(cfg_ionic* ion);
+
+/* -------------------------------------------------------- monodomain step */
+
+/* lduMesh view of the myocardium: OpenFOAM's lower/upper addressing of the
+ * internal faces (upper-triangular order), cell volumes and centres, and
+ * either per-face coefficients face_coeff = deltaCoeffs * (Sf.sigma_f.Sf)/|Sf|
+ * (upper() of fvm::laplacian(conductivity, Vm), gaussLaplacianScheme), or the
+ * face geometry (Sf and deltaCoeffs) from which the library forms them with
+ * the descriptor's uniform conductivity.  zeroGradient walls contribute
+ * nothing (myocardiumDomain.C:207). */
+typedef struct cfg_mesh_desc {
+    long long n_cells, n_faces;
+    const int* owner;            /* [n_faces] lower addressing */
+    const int* neighbour;        /* [n_faces] upper addressing */
+    const double* volumes;       /* [n_cells] */
+    const double* centres;       /* [n_cells][3] */
+    const double* face_coeff;    /* [n_faces], or NULL to use the geometry below */
+    const double* face_sf;       /* [n_faces][3] face area vectors, owner -> neighbour */
+    const double* face_delta_coeffs;  /* [n_faces] 1/|d_PN| */
+    int structured[3];           /* nx ny nz when the cells are a blockMesh block
+                                    (x fastest) with uniform coefficients per
+                                    direction; {0,0,0} for a general mesh */
+} cfg_mesh_desc;
+
+/* monodomainSolverCoeffs (tutorials/electroProperties.template) plus
+ * fvSchemes/fvSolution settings used by the step. */
+typedef struct cfg_monodomain_desc {
+    cfg_ionic_desc ionic;        /* n_cells must equal the mesh's */
+    double conductivity[6];      /* xx xy xz yy yz zz [S/m]; used when the mesh
+                                    gives geometry instead of face_coeff */
+    double chi;                  /* [1/m] */
+    double cm;                   /* [F/m^2] */
+    int implicit;                /* solutionAlgorithm implicit (1) / explicit (0) */
+    int ddt_backward;            /* ddtSchemes default backward (1) / Euler (0) */
+    double pcg_tol, pcg_rel_tol; /* solvers Vm tolerance / relTol */
+    int pcg_max_iter;            /* maxIter (default 1000) */
+    int n_outer;                 /* PIMPLE nOuterCorrectors */
+    double outer_tol;            /* PIMPLE residualControl Vm tolerance */
+    double vm0;                  /* initial Vm [V] (MyocardiumDomain default -0.084) */
+    int n_boxes;                 /* externalStimulus boxes (<= 8) */
+    double box_min[8][3], box_max[8][3];
+    double box_start[8], box_duration[8], box_intensity[8];
+} cfg_monodomain_desc;
+
+typedef struct cfg_monodomain cfg_monodomain;
+
+/* MyocardiumDomain + MonodomainSolver construction (myocardiumDomain.C:180-304,
+ * monodomainSolver.C:39-100) on the given mesh. */
+int cfg_monodomain_create(const cfg_monodomain_desc* desc, const cfg_mesh_desc* mesh,
+                          cfg_monodomain** out);
+
+/* The same from the text of a constant/electroProperties file: selects
+ * myocardiumSolver, reads <type>Coeffs (conductivity, chi, cm, ionicModel,
+ * tissue, solutionAlgorithm, solver, absTol, relTol, maxSteps,
+ * externalStimulus) as electroModel::New / myocardiumDomainInterface::New do
+ * (electroModel.C:142-200, myocardiumDomainInterface.C:54-96).  fv_settings
+ * may override ddt scheme / PCG tolerances (NULL = the tutorials' values);
+ * `precision` picks the GPU form. */
+int cfg_monodomain_create_from_dict(const char* electro_properties, const cfg_mesh_desc* mesh,
+                                    double delta_t, int precision, cfg_monodomain** out);
+
+/* One time step: runTime++ then electroModel::evolve with the staggered
+ * scheme (electroModel.C:297-330, myocardiumDomain.C:487-529): box stimulus,
+ * ionic solveODE, implicit (PIMPLE + PCG) or explicit diffusion, activation
+ * time. */
+int cfg_monodomain_step(cfg_monodomain* md, double dt);
+
+/* n_steps steps replayed from a captured CUDA graph (no host work per step
+ * beyond the launch). */
+int cfg_monodomain_run(cfg_monodomain* md, double dt, long long n_steps);
+
+#define CFG_FIELD_VM 0              /* Vm [V] */
+#define CFG_FIELD_IION 1            /* ionicCurrent [V/s] */
+#define CFG_FIELD_ACTIVATION 2      /* activationTime [s] */
+#define CFG_FIELD_SOURCE 3          /* externalStimulusCurrent [A/m^3] */
+#define CFG_FIELD_VM_OLD 4          /* Vm.oldTime() [V] */
+
+/* Host copies of the domain's fields (written at output times only). */
+int cfg_monodomain_get_field(cfg_monodomain* md, int field, double* host);
+int cfg_monodomain_set_field(cfg_monodomain* md, int field, const double* host);
+double cfg_monodomain_time(const cfg_monodomain* md);
+cfg_ionic* cfg_monodomain_ionic(cfg_monodomain* md);
+
+typedef struct cfg_step_stats {
+    int n_solves;                  /* PIMPLE correctors run in the last step */
+    int iterations[16];            /* PCG iterations per solve */
+    double initial_residual[16];
+    double final_residual[16];
+} cfg_step_stats;
+int cfg_monodomain_last_stats(const cfg_monodomain* md, cfg_step_stats* stats);
+
+/* Per-phase device time, the GPU counterpart of electroModel's
+ * electrophysicsAdvanceTimings (electroModel.H:81, staggered...C:50-75):
+ * when enabled, CUDA events on the context's stream bracket the ionic and
+ * the diffusion phase of every step and the milliseconds accumulate. */
+int cfg_monodomain_set_timing(cfg_monodomain* md, int enable);
+int cfg_monodomain_timings(const cfg_monodomain* md, double* ionic_ms, double* diffusion_ms,
+                           long long* steps, long long* kernel_launches);
+/* The CUDA stream (cudaStream_t) all work of the context is enqueued on. */
+void* cfg_monodomain_stream(cfg_monodomain* md);
+int cfg_monodomain_destroy(cfg_monodomain* md);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

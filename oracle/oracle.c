@@ -1,0 +1,893 @@
+/* CPU oracle for the monodomain time step - TEST INFRASTRUCTURE ONLY.
+ * See oracle.h for what each part restates and its parity status.
+ *
+ * Build with -ffp-contract=off: the reference is compiled without fused
+ * multiply-add contraction on x86-64, and the oracle must round the same way
+ * on the aarch64 host, where GCC would otherwise contract a*b+c.
+ */
+#include "oracle.h"
+
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#include "models/tnnp.h"
+#include "models/ord.h"
+#include "models/torord_dyncl.h"
+#include "models/alievpanfilov.h"
+#include "models/buenoorovio.h"
+
+void oracle_fatal(const char* what)
+{
+    fprintf(stderr, "oracle: fatal: %s\n", what);
+    abort();
+}
+
+/* ------------------------------------------------------------------------ */
+/* model table                                                              */
+
+typedef void (*init_fn)(double*, double*, int, const double*);
+typedef void (*supp_fn)(double*);
+typedef void (*rhs_fn)(double, const double*, double*, const double*, double*, int, int,
+                       const oracle_stimulus*);
+
+typedef struct {
+    const char* name;
+    int ns, na, nc;
+    init_fn init;
+    supp_fn supplement; /* constants initConsts leaves unset (ORd) */
+    rhs_fn rates;       /* body used by <Model>::derivatives */
+    rhs_fn variables;   /* body(ies) called after the ODE solve */
+    int iion;
+    double iion_scale;
+    double time_scale;  /* model time = 1000 t / time_scale */
+    int vm_map;         /* 0: mV, 1: Aliev-Panfilov u, 2: Bueno-Orovio u */
+} model_info;
+
+static const model_info MODELS[ORACLE_NMODELS] = {
+    {"TNNP", TNNP_NS, TNNP_NA, TNNP_NC, tnnp_init, tnnp_supplement, tnnp_rates, tnnp_variables,
+     TNNP_IION_INDEX, TNNP_IION_SCALE, TNNP_TIME_SCALE, 0},
+    {"ORd", ORD_NS, ORD_NA, ORD_NC, ord_init, ord_supplement, ord_rates, ord_variables,
+     ORD_IION_INDEX, ORD_IION_SCALE, ORD_TIME_SCALE, 0},
+    {"ToRORd_dynCl", TORORD_DYNCL_NS, TORORD_DYNCL_NA, TORORD_DYNCL_NC, torord_dyncl_init, torord_dyncl_supplement,
+     torord_dyncl_rates, torord_dyncl_variables, TORORD_DYNCL_IION_INDEX,
+     TORORD_DYNCL_IION_SCALE, TORORD_DYNCL_TIME_SCALE, 0},
+    {"AlievPanfilov", ALIEVPANFILOV_NS, ALIEVPANFILOV_NA, ALIEVPANFILOV_NC,
+     alievpanfilov_init, alievpanfilov_supplement, alievpanfilov_rates, alievpanfilov_variables,
+     ALIEVPANFILOV_IION_INDEX, ALIEVPANFILOV_IION_SCALE, ALIEVPANFILOV_TIME_SCALE, 1},
+    {"BuenoOrovio", BUENOOROVIO_NS, BUENOOROVIO_NA, BUENOOROVIO_NC, buenoorovio_init, buenoorovio_supplement,
+     buenoorovio_rates, buenoorovio_variables, BUENOOROVIO_IION_INDEX,
+     BUENOOROVIO_IION_SCALE, BUENOOROVIO_TIME_SCALE, 2},
+};
+
+int oracle_model_sizes(int model, int* ns, int* na, int* nc)
+{
+    if (model < 0 || model >= ORACLE_NMODELS) return -1;
+    *ns = MODELS[model].ns;
+    *na = MODELS[model].na;
+    *nc = MODELS[model].nc;
+    return 0;
+}
+
+void oracle_model_init(int model, int tissue, double* C, double* y, const double* scale)
+{
+    MODELS[model].init(C, y, tissue, scale);
+}
+
+void oracle_model_supplement(int model, double* C) { MODELS[model].supplement(C); }
+
+void oracle_model_rates(int model, double t, const double* C, const double* y, double* dydt,
+                        double* alg, int tissue, int solve_vm, const oracle_stimulus* stim)
+{
+    MODELS[model].rates(t, C, dydt, y, alg, tissue, solve_vm, stim);
+}
+
+void oracle_model_variables(int model, double t, const double* C, const double* y,
+                            double* rates, double* alg, int tissue, int solve_vm,
+                            const oracle_stimulus* stim)
+{
+    MODELS[model].variables(t, C, rates, y, alg, tissue, solve_vm, stim);
+}
+
+int oracle_model_iion_index(int model) { return MODELS[model].iion; }
+
+/* ------------------------------------------------------------------------ */
+/* OpenFOAM RKF45 (ODESolver + adaptiveSolver + RKF45), restated            */
+
+void oracle_ode_default(oracle_ode_settings* s)
+{
+    s->abs_tol = 1e-15;   /* SMALL */
+    s->rel_tol = 1e-4;
+    s->max_steps = 10000;
+    s->safe_scale = 0.9;
+    s->min_scale = 0.2;
+    s->max_scale = 10.0;
+    s->alpha_inc = 0.2;
+    s->alpha_dec = 0.25;
+}
+
+/* Fehlberg 4(5) tableau; the 5th-order solution is propagated and the
+ * difference to the embedded 4th-order one is the error estimate. */
+static const double c2 = 1.0 / 4.0, c3 = 3.0 / 8.0, c4 = 12.0 / 13.0, c5 = 1.0, c6 = 1.0 / 2.0;
+static const double a21 = 1.0 / 4.0;
+static const double a31 = 3.0 / 32.0, a32 = 9.0 / 32.0;
+static const double a41 = 1932.0 / 2197.0, a42 = -7200.0 / 2197.0, a43 = 7296.0 / 2197.0;
+static const double a51 = 439.0 / 216.0, a52 = -8.0, a53 = 3680.0 / 513.0,
+                    a54 = -845.0 / 4104.0;
+static const double a61 = -8.0 / 27.0, a62 = 2.0, a63 = -3544.0 / 2565.0,
+                    a64 = 1859.0 / 4104.0, a65 = -11.0 / 40.0;
+static const double b1 = 16.0 / 135.0, b3 = 6656.0 / 12825.0, b4 = 28561.0 / 56430.0,
+                    b5 = -9.0 / 50.0, b6 = 2.0 / 55.0;
+#define E1 (25.0 / 216.0 - b1)
+#define E3 (1408.0 / 2565.0 - b3)
+#define E4 (2197.0 / 4104.0 - b4)
+#define E5 (-1.0 / 5.0 - b5)
+#define E6 (-b6)
+
+struct oracle_ionic {
+    const model_info* m;
+    int model;
+    long n;
+    int tissue;
+    int solve_vm;
+    oracle_ode_settings ode;
+    oracle_stimulus stim;
+    int has_stim;
+    double* C;          /* constants: one row, or one row per cell when scaled */
+    int per_cell_consts;
+    double* y;          /* STATES, AoS */
+    double* alg;        /* ALGEBRAIC, AoS (persistent, as ALGEBRAIC_) */
+    double* rates;      /* RATES, AoS */
+    double* step;       /* per-cell persistent ODE step (ms), ionicModel::step_ */
+    long rhs_evals;
+};
+
+typedef struct {
+    /* one RKF45 solver object's work arrays (OpenFOAM allocates these once per
+     * solver; the k arrays keep entries a model never writes, i.e. RATES[V]
+     * in tissue mode, at their initial zero) */
+    double *dydx0, *k2, *k3, *k4, *k5, *k6, *ytmp, *yout, *err, *algtmp;
+    long evals;
+} rk_ws;
+
+static void ws_alloc(rk_ws* w, int ns, int na)
+{
+    double* p = (double*)calloc((size_t)(9 * ns + na), sizeof(double));
+    w->dydx0 = p;
+    w->k2 = p + ns;
+    w->k3 = p + 2 * ns;
+    w->k4 = p + 3 * ns;
+    w->k5 = p + 4 * ns;
+    w->k6 = p + 5 * ns;
+    w->ytmp = p + 6 * ns;
+    w->yout = p + 7 * ns;
+    w->err = p + 8 * ns;
+    w->algtmp = p + 9 * ns;
+    w->evals = 0;
+}
+
+static void ws_free(rk_ws* w) { free(w->dydx0); }
+
+/* <Model>::derivatives: fresh zeroed ALGEBRAIC scratch, RATES = dydt */
+static void derivs(const oracle_ionic* io, const double* C, rk_ws* w, double t, const double* y,
+                   double* dydt)
+{
+    memset(w->algtmp, 0, sizeof(double) * (size_t)io->m->na);
+    io->m->rates(t, C, dydt, y, w->algtmp, io->tissue, io->solve_vm,
+                 io->has_stim ? &io->stim : NULL);
+    w->evals++;
+}
+
+/* RKF45::solve(x0, y0, dydx0, dx, y): one trial step, returns the error norm */
+static double rkf45_trial(const oracle_ionic* io, const double* C, rk_ws* w, double x0,
+                          const double* y0, double dx, double* y)
+{
+    const int ns = io->m->ns;
+    int i;
+    for (i = 0; i < ns; i++) w->ytmp[i] = y0[i] + a21 * dx * w->dydx0[i];
+    derivs(io, C, w, x0 + c2 * dx, w->ytmp, w->k2);
+    for (i = 0; i < ns; i++) w->ytmp[i] = y0[i] + dx * (a31 * w->dydx0[i] + a32 * w->k2[i]);
+    derivs(io, C, w, x0 + c3 * dx, w->ytmp, w->k3);
+    for (i = 0; i < ns; i++)
+        w->ytmp[i] = y0[i] + dx * (a41 * w->dydx0[i] + a42 * w->k2[i] + a43 * w->k3[i]);
+    derivs(io, C, w, x0 + c4 * dx, w->ytmp, w->k4);
+    for (i = 0; i < ns; i++)
+        w->ytmp[i] = y0[i] + dx * (a51 * w->dydx0[i] + a52 * w->k2[i] + a53 * w->k3[i]
+                                   + a54 * w->k4[i]);
+    derivs(io, C, w, x0 + c5 * dx, w->ytmp, w->k5);
+    for (i = 0; i < ns; i++)
+        w->ytmp[i] = y0[i] + dx * (a61 * w->dydx0[i] + a62 * w->k2[i] + a63 * w->k3[i]
+                                   + a64 * w->k4[i] + a65 * w->k5[i]);
+    derivs(io, C, w, x0 + c6 * dx, w->ytmp, w->k6);
+    for (i = 0; i < ns; i++)
+        y[i] = y0[i] + dx * (b1 * w->dydx0[i] + b3 * w->k3[i] + b4 * w->k4[i] + b5 * w->k5[i]
+                             + b6 * w->k6[i]);
+    for (i = 0; i < ns; i++)
+        w->err[i] = dx * (E1 * w->dydx0[i] + E3 * w->k3[i] + E4 * w->k4[i] + E5 * w->k5[i]
+                          + E6 * w->k6[i]);
+    /* ODESolver::normalizeError */
+    double maxerr = 0.0;
+    for (i = 0; i < ns; i++) {
+        double a = fabs(y0[i]), b = fabs(y[i]);
+        double tol = io->ode.abs_tol + io->ode.rel_tol * (a > b ? a : b);
+        double e = fabs(w->err[i]) / tol;
+        if (e > maxerr) maxerr = e;
+    }
+    return maxerr;
+}
+
+/* adaptiveSolver::solve(odes, x, y, dxTry) */
+static int adaptive_step(const oracle_ionic* io, const double* C, rk_ws* w, double* x, double* y,
+                         double* dx_try)
+{
+    const oracle_ode_settings* s = &io->ode;
+    double dx = *dx_try, err = 0.0;
+    derivs(io, C, w, *x, y, w->dydx0);
+    do {
+        err = rkf45_trial(io, C, w, *x, y, dx, w->yout);
+        if (err > 1) {
+            double scale = s->safe_scale * pow(err, -s->alpha_dec);
+            if (scale < s->min_scale) scale = s->min_scale;
+            dx *= scale;
+            if (dx < 1e-300) return -1;   /* stepsize underflow */
+        }
+    } while (err > 1);
+    *x += dx;
+    memcpy(y, w->yout, sizeof(double) * (size_t)io->m->ns);
+    if (err > pow(s->max_scale / s->safe_scale, -1.0 / s->alpha_inc)) {
+        double scale = s->safe_scale * pow(err, -s->alpha_inc);
+        if (scale > s->max_scale) scale = s->max_scale;
+        *dx_try = scale * dx;
+    } else {
+        *dx_try = s->safe_scale * s->max_scale * dx;
+    }
+    return 0;
+}
+
+/* ODESolver::solve(xStart, xEnd, y, dxTry): returns accepted steps or -1 */
+static long ode_solve(const oracle_ionic* io, const double* C, rk_ws* w, double xs, double xe,
+                      double* y, double* dx_try)
+{
+    double step_dx = *dx_try;
+    int last = 0;
+    double x = xs;
+    long n;
+    for (n = 0; n < io->ode.max_steps; n++) {
+        double dx_try0 = step_dx;
+        if ((x + step_dx - xe) * (x + step_dx - xs) > 0) {
+            last = 1;
+            step_dx = xe - x;
+        }
+        if (adaptive_step(io, C, w, &x, y, &step_dx) != 0) return -1;
+        if ((x - xe) * (xe - xs) >= 0) {
+            if (n > 0 && last) step_dx = dx_try0;
+            *dx_try = step_dx;
+            return n + 1;
+        }
+    }
+    return -1;
+}
+
+oracle_ionic* oracle_ionic_new(int model, long n, int tissue, double initial_dt, int solve_vm,
+                               const oracle_ode_settings* ode, const oracle_stimulus* stim,
+                               const double* scales)
+{
+    if (model < 0 || model >= ORACLE_NMODELS || n < 0) return NULL;
+    oracle_ionic* io = (oracle_ionic*)calloc(1, sizeof(oracle_ionic));
+    const model_info* m = &MODELS[model];
+    io->m = m;
+    io->model = model;
+    io->n = n;
+    io->tissue = tissue;
+    io->solve_vm = solve_vm;
+    if (ode) io->ode = *ode; else oracle_ode_default(&io->ode);
+    if (stim) { io->stim = *stim; io->has_stim = 1; }
+    io->per_cell_consts = scales != NULL;
+    io->C = (double*)calloc((size_t)m->nc * (size_t)(scales ? (n > 0 ? n : 1) : 1),
+                            sizeof(double));
+    io->y = (double*)calloc((size_t)(n * m->ns + 1), sizeof(double));
+    io->alg = (double*)calloc((size_t)(n * m->na + 1), sizeof(double));
+    io->rates = (double*)calloc((size_t)(n * m->ns + 1), sizeof(double));
+    io->step = (double*)malloc(sizeof(double) * (size_t)(n + 1));
+    for (long c = 0; c < n; c++) {
+        /* the reference re-runs initConsts into the shared CONSTANTS for
+         * every cell (TNNP.C:64-76); per-cell scales need a row per cell */
+        double* Crow = io->C + (scales ? (size_t)c * (size_t)m->nc : 0);
+        m->init(Crow, io->y + (size_t)c * (size_t)m->ns, tissue, scales ? scales + 6 * c : NULL);
+        m->supplement(Crow);
+        io->step[c] = initial_dt;
+    }
+    if (n == 0) { m->init(io->C, io->y, tissue, NULL); m->supplement(io->C); }
+    return io;
+}
+
+void oracle_ionic_free(oracle_ionic* io)
+{
+    if (!io) return;
+    free(io->C);
+    free(io->y);
+    free(io->alg);
+    free(io->rates);
+    free(io->step);
+    free(io);
+}
+
+double* oracle_ionic_states(oracle_ionic* io) { return io->y; }
+double* oracle_ionic_steps(oracle_ionic* io) { return io->step; }
+long oracle_ionic_rhs_evals(oracle_ionic* io) { return io->rhs_evals; }
+
+static double vm_to_state0(int map, double vm)
+{
+    if (map == 1) return (vm * 1000.0 + 80) / 100;       /* AlievPanfilov.C:121 */
+    if (map == 2) return (vm * 1000.0 + 84) / 85.7;      /* BuenoOrovio.C:120 */
+    return vm * 1000.0;                                  /* TNNP.C:137 */
+}
+
+/* <Model>::solveODE for cells [c0, c1) with one solver work set */
+static long solve_range(oracle_ionic* io, rk_ws* w, long c0, long c1, double t0, double dt,
+                        const double* vm, double* im)
+{
+    const model_info* m = io->m;
+    const double ts = m->time_scale;
+    /* tStart/tEnd in model time: TNNP.C:122-123, AlievPanfilov.C:107-108 */
+    const double t_start = (ts == 1.0) ? t0 * 1000 : t0 * 1000.0 / ts;
+    const double t_end = (ts == 1.0) ? (t0 + dt) * 1000 : (t0 + dt) * 1000.0 / ts;
+    const double dt_model = (ts == 1.0) ? dt * 1000.0 : dt * 1000.0 / ts;
+    long total = 0;
+    for (long c = c0; c < c1; c++) {
+        double* y = io->y + (size_t)c * (size_t)m->ns;
+        double* alg = io->alg + (size_t)c * (size_t)m->na;
+        double* rates = io->rates + (size_t)c * (size_t)m->ns;
+        const double* C = io->C + (io->per_cell_consts ? (size_t)c * (size_t)m->nc : 0);
+        if (!io->solve_vm) y[0] = vm_to_state0(m->vm_map, vm[c]);
+        double* step = &io->step[c];
+        if (dt_model < *step) *step = dt_model;
+        long k = ode_solve(io, C, w, t_start, t_end, y, step);
+        if (k < 0) return -1;
+        total += k;
+        m->variables(t_end, C, rates, y, alg, io->tissue, io->solve_vm,
+                     io->has_stim ? &io->stim : NULL);
+        if (im) im[c] = alg[m->iion] * m->iion_scale;
+    }
+    return total;
+}
+
+long oracle_ionic_solve(oracle_ionic* io, double t0, double dt, const double* vm, double* im,
+                        int nthreads)
+{
+    long total = 0;
+    int failed = 0;
+    long evals = 0;
+#ifdef _OPENMP
+    if (nthreads > 1) {
+#pragma omp parallel num_threads(nthreads) reduction(+ : total, evals) reduction(| : failed)
+        {
+            rk_ws w;
+            ws_alloc(&w, io->m->ns, io->m->na);
+            int tid = omp_get_thread_num(), nt = omp_get_num_threads();
+            long chunk = (io->n + nt - 1) / nt;
+            long c0 = tid * chunk, c1 = c0 + chunk < io->n ? c0 + chunk : io->n;
+            if (c0 < c1) {
+                long k = solve_range(io, &w, c0, c1, t0, dt, vm, im);
+                if (k < 0) failed = 1; else total += k;
+            }
+            evals += w.evals;
+            ws_free(&w);
+        }
+        io->rhs_evals += evals;
+        return failed ? -1 : total;
+    }
+#else
+    (void)nthreads;
+#endif
+    rk_ws w;
+    ws_alloc(&w, io->m->ns, io->m->na);
+    total = solve_range(io, &w, 0, io->n, t0, dt, vm, im);
+    io->rhs_evals += w.evals;
+    ws_free(&w);
+    (void)failed;
+    return total;
+}
+
+/* ------------------------------------------------------------------------ */
+/* structured hex mesh as blockMesh builds one block: cells x-fastest;       */
+/* internal faces in upper-triangular order (per owner: +x, +y, +z)         */
+
+struct oracle_mesh {
+    int nx, ny, nz;
+    long n, nf;
+    double dx, dy, dz;
+    int* owner;
+    int* neigh;
+    double* centres;  /* 3n */
+    double* vol;      /* n */
+    double* sf;       /* 3nf face area vectors, owner -> neighbour */
+    double* delta;    /* nf: |d_PN| */
+};
+
+oracle_mesh* oracle_mesh_box(int nx, int ny, int nz, double lx, double ly, double lz)
+{
+    oracle_mesh* m = (oracle_mesh*)calloc(1, sizeof(oracle_mesh));
+    m->nx = nx; m->ny = ny; m->nz = nz;
+    m->n = (long)nx * ny * nz;
+    m->dx = lx / nx; m->dy = ly / ny; m->dz = lz / nz;
+    long nf = (long)(nx - 1) * ny * nz + (long)nx * (ny - 1) * nz + (long)nx * ny * (nz - 1);
+    m->nf = nf;
+    m->owner = (int*)malloc(sizeof(int) * (size_t)(nf + 1));
+    m->neigh = (int*)malloc(sizeof(int) * (size_t)(nf + 1));
+    m->sf = (double*)malloc(sizeof(double) * 3 * (size_t)(nf + 1));
+    m->delta = (double*)malloc(sizeof(double) * (size_t)(nf + 1));
+    m->centres = (double*)malloc(sizeof(double) * 3 * (size_t)m->n);
+    m->vol = (double*)malloc(sizeof(double) * (size_t)m->n);
+    /* points of a uniform block: x_i = i*lx/nx */
+    long f = 0;
+    for (int k = 0; k < nz; k++)
+        for (int j = 0; j < ny; j++)
+            for (int i = 0; i < nx; i++) {
+                long c = ((long)k * ny + j) * nx + i;
+                double x0 = lx * i / nx, x1 = lx * (i + 1) / nx;
+                double y0 = ly * j / ny, y1 = ly * (j + 1) / ny;
+                double z0 = lz * k / nz, z1 = lz * (k + 1) / nz;
+                m->centres[3 * c + 0] = 0.5 * (x0 + x1);
+                m->centres[3 * c + 1] = 0.5 * (y0 + y1);
+                m->centres[3 * c + 2] = 0.5 * (z0 + z1);
+                m->vol[c] = (x1 - x0) * (y1 - y0) * (z1 - z0);
+            }
+    for (long c = 0; c < m->n; c++) {
+        int i = (int)(c % nx), j = (int)((c / nx) % ny), k = (int)(c / ((long)nx * ny));
+        long nb[3] = {i + 1 < nx ? c + 1 : -1, j + 1 < ny ? c + nx : -1,
+                      k + 1 < nz ? c + (long)nx * ny : -1};
+        for (int d = 0; d < 3; d++) {
+            if (nb[d] < 0) continue;
+            m->owner[f] = (int)c;
+            m->neigh[f] = (int)nb[d];
+            double area = d == 0 ? (ly / ny) * (lz / nz) : d == 1 ? (lx / nx) * (lz / nz)
+                                                                 : (lx / nx) * (ly / ny);
+            m->sf[3 * f + 0] = d == 0 ? area : 0.0;
+            m->sf[3 * f + 1] = d == 1 ? area : 0.0;
+            m->sf[3 * f + 2] = d == 2 ? area : 0.0;
+            double dd = m->centres[3 * nb[d] + d] - m->centres[3 * c + d];
+            m->delta[f] = dd;
+            f++;
+        }
+    }
+    return m;
+}
+
+void oracle_mesh_free(oracle_mesh* m)
+{
+    if (!m) return;
+    free(m->owner); free(m->neigh); free(m->sf); free(m->delta);
+    free(m->centres); free(m->vol);
+    free(m);
+}
+
+long oracle_mesh_ncells(const oracle_mesh* m) { return m->n; }
+long oracle_mesh_nfaces(const oracle_mesh* m) { return m->nf; }
+
+void oracle_mesh_addressing(const oracle_mesh* m, int* owner, int* neighbour)
+{
+    memcpy(owner, m->owner, sizeof(int) * (size_t)m->nf);
+    memcpy(neighbour, m->neigh, sizeof(int) * (size_t)m->nf);
+}
+
+void oracle_mesh_centres(const oracle_mesh* m, double* c)
+{
+    memcpy(c, m->centres, sizeof(double) * 3 * (size_t)m->n);
+}
+
+/* ------------------------------------------------------------------------ */
+/* monodomain tissue                                                        */
+
+#define MAX_SOLVES 64
+
+struct oracle_tissue {
+    oracle_tissue_desc d;
+    const oracle_mesh* mesh;
+    oracle_ionic* ionic;
+    long n, nf;
+    double t;           /* runTime value */
+    long time_index;
+    double* vm;
+    double* vm_old;
+    double* vm_oldold;
+    int n_old;          /* stored old-time levels of Vm (GeometricField::nOldTimes) */
+    double* iion;
+    double* src;
+    double* act;
+    unsigned char* calc_act;
+    double* lap;        /* upper coefficient per face: deltaCoeff * (Sf.sigma.Sf)/|Sf| */
+    /* PCG work */
+    double *diag, *upper, *b, *rA, *wA, *pA, *rD, *tmp;
+    int n_solves;
+    double init_res[MAX_SOLVES], final_res[MAX_SOLVES];
+    int iters[MAX_SOLVES];
+};
+
+oracle_tissue* oracle_tissue_new(const oracle_tissue_desc* d, const oracle_mesh* mesh)
+{
+    oracle_tissue* T = (oracle_tissue*)calloc(1, sizeof(oracle_tissue));
+    T->d = *d;
+    T->mesh = mesh;
+    T->n = mesh->n;
+    T->nf = mesh->nf;
+    long n = T->n, nf = T->nf;
+    /* ionicModel::New(coeffs, nCells, runTime.deltaT): the initial ODE step is
+     * deltaT in seconds, used as milliseconds by the clamp (TNNP.C:141) */
+    T->ionic = NULL;
+    T->vm = (double*)malloc(sizeof(double) * (size_t)n);
+    T->vm_old = (double*)malloc(sizeof(double) * (size_t)n);
+    T->vm_oldold = (double*)malloc(sizeof(double) * (size_t)n);
+    T->iion = (double*)calloc((size_t)n, sizeof(double));
+    T->src = (double*)calloc((size_t)n, sizeof(double));
+    T->act = (double*)calloc((size_t)n, sizeof(double));
+    T->calc_act = (unsigned char*)malloc((size_t)n);
+    T->lap = (double*)malloc(sizeof(double) * (size_t)(nf + 1));
+    T->diag = (double*)malloc(sizeof(double) * (size_t)n);
+    T->upper = (double*)malloc(sizeof(double) * (size_t)(nf + 1));
+    T->b = (double*)malloc(sizeof(double) * (size_t)n);
+    T->rA = (double*)malloc(sizeof(double) * (size_t)n);
+    T->wA = (double*)malloc(sizeof(double) * (size_t)n);
+    T->pA = (double*)malloc(sizeof(double) * (size_t)n);
+    T->rD = (double*)malloc(sizeof(double) * (size_t)n);
+    T->tmp = (double*)malloc(sizeof(double) * (size_t)n);
+    for (long c = 0; c < n; c++) {
+        T->vm[c] = d->vm0;
+        T->calc_act[c] = 1;
+    }
+    /* uniform conductivity tensor (monodomainSolver.C:86-95); on a face,
+     * SfGammaSn = Sf.(sigma.Sf)/|Sf| and the implicit coefficient is
+     * deltaCoeffs * SfGammaSn (gaussLaplacianScheme, orthogonal mesh) */
+    const double* s = d->sigma;
+    for (long f = 0; f < nf; f++) {
+        const double* S = mesh->sf + 3 * f;
+        double magSf = sqrt(S[0] * S[0] + S[1] * S[1] + S[2] * S[2]);
+        double g0 = S[0] * s[0] + S[1] * s[1] + S[2] * s[2];
+        double g1 = S[0] * s[1] + S[1] * s[3] + S[2] * s[4];
+        double g2 = S[0] * s[2] + S[1] * s[4] + S[2] * s[5];
+        double sfgsn = (g0 * S[0] + g1 * S[1] + g2 * S[2]) / magSf;
+        double delta_coeff = 1.0 / mesh->delta[f];
+        T->lap[f] = delta_coeff * sfgsn;
+    }
+    return T;
+}
+
+void oracle_tissue_free(oracle_tissue* T)
+{
+    if (!T) return;
+    oracle_ionic_free(T->ionic);
+    free(T->vm); free(T->vm_old); free(T->vm_oldold); free(T->iion); free(T->src);
+    free(T->act); free(T->calc_act); free(T->lap); free(T->diag); free(T->upper);
+    free(T->b); free(T->rA); free(T->wA); free(T->pA); free(T->rD); free(T->tmp);
+    free(T);
+}
+
+double oracle_tissue_time(const oracle_tissue* T) { return T->t; }
+double* oracle_tissue_vm(oracle_tissue* T) { return T->vm; }
+double* oracle_tissue_iion(oracle_tissue* T) { return T->iion; }
+double* oracle_tissue_activation(oracle_tissue* T) { return T->act; }
+double* oracle_tissue_source(oracle_tissue* T) { return T->src; }
+oracle_ionic* oracle_tissue_ionic(oracle_tissue* T) { return T->ionic; }
+
+int oracle_tissue_last_solves(const oracle_tissue* T, double* ir, double* fr, int* it, int mx)
+{
+    int k = T->n_solves < mx ? T->n_solves : mx;
+    for (int i = 0; i < k; i++) {
+        ir[i] = T->init_res[i];
+        fr[i] = T->final_res[i];
+        it[i] = T->iters[i];
+    }
+    return T->n_solves;
+}
+
+/* lduMatrix::Amul for the symmetric matrix (diag, upper) */
+static void amul(const oracle_tissue* T, const double* x, double* y)
+{
+    const int* l = T->mesh->owner;
+    const int* u = T->mesh->neigh;
+    for (long c = 0; c < T->n; c++) y[c] = T->diag[c] * x[c];
+    for (long f = 0; f < T->nf; f++) {
+        y[u[f]] += T->upper[f] * x[l[f]];
+        y[l[f]] += T->upper[f] * x[u[f]];
+    }
+}
+
+/* lduMatrix::solver::normFactor */
+static double norm_factor(const oracle_tissue* T, const double* psi, const double* src,
+                          const double* Apsi)
+{
+    const int* l = T->mesh->owner;
+    const int* u = T->mesh->neigh;
+    double* sumA = T->tmp;
+    for (long c = 0; c < T->n; c++) sumA[c] = T->diag[c];
+    for (long f = 0; f < T->nf; f++) {
+        sumA[u[f]] += T->upper[f];
+        sumA[l[f]] += T->upper[f];
+    }
+    double avg = 0.0;
+    for (long c = 0; c < T->n; c++) avg += psi[c];
+    avg /= (double)T->n;
+    double nf = 0.0;
+    for (long c = 0; c < T->n; c++) {
+        double pa = sumA[c] * avg;
+        nf += fabs(Apsi[c] - pa) + fabs(src[c] - pa);
+    }
+    return nf + 1e-20;
+}
+
+static void precondition(const oracle_tissue* T, double* wA, const double* rA)
+{
+    const double* rD = T->rD;
+    for (long c = 0; c < T->n; c++) wA[c] = rD[c] * rA[c];
+    if (!T->d.precond_dic) return;
+    const int* l = T->mesh->owner;
+    const int* u = T->mesh->neigh;
+    for (long f = 0; f < T->nf; f++) wA[u[f]] -= rD[u[f]] * T->upper[f] * wA[l[f]];
+    for (long f = T->nf - 1; f >= 0; f--) wA[l[f]] -= rD[l[f]] * T->upper[f] * wA[u[f]];
+}
+
+/* PCG::solve (lduMatrix), returns iterations */
+static int pcg(oracle_tissue* T, double* psi, const double* src, double* init_res,
+               double* final_res)
+{
+    long n = T->n;
+    double *wA = T->wA, *rA = T->rA, *pA = T->pA;
+    amul(T, psi, wA);
+    for (long c = 0; c < n; c++) rA[c] = src[c] - wA[c];
+    double normf = norm_factor(T, psi, src, wA);
+    double s = 0.0;
+    for (long c = 0; c < n; c++) s += fabs(rA[c]);
+    double res = s / normf;
+    *init_res = res;
+    int it = 0;
+    const double tol = T->d.pcg_tol, rel = T->d.pcg_rel_tol;
+#define CONVERGED(r) ((r) < tol || (rel > 1e-20 && (r) < rel * (*init_res)))
+    if (!CONVERGED(res)) {
+        /* preconditioner set-up (DIC: calcReciprocalD; diagonal: 1/diag) */
+        for (long c = 0; c < n; c++) T->rD[c] = T->diag[c];
+        if (T->d.precond_dic) {
+            const int* l = T->mesh->owner;
+            const int* u = T->mesh->neigh;
+            for (long f = 0; f < T->nf; f++)
+                T->rD[u[f]] -= T->upper[f] * T->upper[f] / T->rD[l[f]];
+        }
+        for (long c = 0; c < n; c++) T->rD[c] = 1.0 / T->rD[c];
+        double wArA = 1e300, wArAold;
+        do {
+            wArAold = wArA;
+            precondition(T, wA, rA);
+            wArA = 0.0;
+            for (long c = 0; c < n; c++) wArA += wA[c] * rA[c];
+            if (it == 0) {
+                for (long c = 0; c < n; c++) pA[c] = wA[c];
+            } else {
+                double beta = wArA / wArAold;
+                for (long c = 0; c < n; c++) pA[c] = wA[c] + beta * pA[c];
+            }
+            amul(T, pA, wA);
+            double wApA = 0.0;
+            for (long c = 0; c < n; c++) wApA += wA[c] * pA[c];
+            if (fabs(wApA) / normf < 1e-300) break;   /* checkSingularity */
+            double alpha = wArA / wApA;
+            for (long c = 0; c < n; c++) {
+                psi[c] += alpha * pA[c];
+                rA[c] -= alpha * wA[c];
+            }
+            s = 0.0;
+            for (long c = 0; c < n; c++) s += fabs(rA[c]);
+            res = s / normf;
+        } while (++it < T->d.pcg_max_iter && !CONVERGED(res));
+    }
+#undef CONVERGED
+    *final_res = res;
+    return it;
+}
+
+/* MyocardiumDomain::updateExternalStimulusCurrent (myocardiumDomain.C:307-342) */
+static void update_stimulus(oracle_tissue* T, double t0)
+{
+    for (long c = 0; c < T->n; c++) T->src[c] = 0.0;
+    for (int b = 0; b < T->d.n_boxes; b++) {
+        double ts = T->d.box_start[b], te = ts + T->d.box_duration[b];
+        if (t0 < ts || t0 > te) continue;
+        for (long c = 0; c < T->n; c++) {
+            const double* p = T->mesh->centres + 3 * c;
+            if (p[0] >= T->d.box_min[b][0] && p[0] <= T->d.box_max[b][0] &&
+                p[1] >= T->d.box_min[b][1] && p[1] <= T->d.box_max[b][1] &&
+                p[2] >= T->d.box_min[b][2] && p[2] <= T->d.box_max[b][2])
+                T->src[c] += T->d.box_intensity[b];
+        }
+    }
+}
+
+/* ddt coefficients (EulerDdtScheme / backwardDdtScheme); backward uses
+ * deltaT0 = GREAT while fewer than two old-time levels are stored */
+static void ddt_coeffs(const oracle_tissue* T, double dt, double* cft, double* cft0,
+                       double* cft00)
+{
+    if (!T->d.ddt_backward) {
+        *cft = 1.0; *cft0 = 1.0; *cft00 = 0.0;
+        return;
+    }
+    double dt0 = T->n_old < 2 ? 1e15 : dt;
+    *cft = 1 + dt / (dt + dt0);
+    *cft00 = dt * dt / (dt0 * (dt + dt0));
+    *cft0 = *cft + *cft00;
+}
+
+/* one fvMatrix assembly + solve of chi*Cm*ddt(Vm) == laplacian - chi*Cm*Iion + src */
+static int solve_implicit(oracle_tissue* T, double dt)
+{
+    double cft, cft0, cft00;
+    /* fvm::ddt accesses Vm.oldTime() and Vm.oldTime().oldTime() (backward):
+     * the first access creates each level as a copy of the newer one */
+    int n_old_before = T->n_old;
+    ddt_coeffs(T, dt, &cft, &cft0, &cft00);
+    if (T->n_old < 1) { memcpy(T->vm_old, T->vm, sizeof(double) * (size_t)T->n); T->n_old = 1; }
+    if (T->d.ddt_backward && T->n_old < 2) {
+        memcpy(T->vm_oldold, T->vm_old, sizeof(double) * (size_t)T->n);
+        T->n_old = 2;
+    }
+    (void)n_old_before;
+    const double chicm = T->d.chi * T->d.cm;
+    const double rdt = 1.0 / dt;
+    const double* V = T->mesh->vol;
+    for (long c = 0; c < T->n; c++) {
+        double ddt_diag, ddt_src;
+        if (T->d.ddt_backward) {
+            ddt_diag = (cft * rdt) * V[c];
+            ddt_src = rdt * V[c] * (cft0 * T->vm_old[c] - cft00 * T->vm_oldold[c]);
+        } else {
+            ddt_diag = rdt * V[c];
+            ddt_src = rdt * T->vm_old[c] * V[c];
+        }
+        T->diag[c] = chicm * ddt_diag;
+        T->b[c] = chicm * ddt_src;
+    }
+    /* minus the Laplacian: upper = -coef, diag += sum coef (negSumDiag) */
+    const int* l = T->mesh->owner;
+    const int* u = T->mesh->neigh;
+    for (long f = 0; f < T->nf; f++) T->upper[f] = -T->lap[f];
+    {
+        double* lapdiag = T->tmp;
+        for (long c = 0; c < T->n; c++) lapdiag[c] = 0.0;
+        for (long f = 0; f < T->nf; f++) {
+            lapdiag[l[f]] -= T->lap[f];
+            lapdiag[u[f]] -= T->lap[f];
+        }
+        for (long c = 0; c < T->n; c++) T->diag[c] = T->diag[c] - lapdiag[c];
+    }
+    /* explicit sources: -(chi*Cm*Iion) + src, each times V */
+    for (long c = 0; c < T->n; c++) {
+        double su = -(chicm * T->iion[c]) * V[c];
+        su = su + T->src[c] * V[c];
+        T->b[c] = T->b[c] + su;
+    }
+    int k = T->n_solves;
+    if (k >= MAX_SOLVES) return -1;
+    int it = pcg(T, T->vm, T->b, &T->init_res[k], &T->final_res[k]);
+    T->iters[k] = it;
+    T->n_solves++;
+    return it;
+}
+
+/* explicit form: chi*Cm*ddt(Vm) == fvc::laplacian(sigma,Vm) - chi*Cm*Iion + src */
+static int solve_explicit(oracle_tissue* T, double dt)
+{
+    double cft, cft0, cft00;
+    ddt_coeffs(T, dt, &cft, &cft0, &cft00);
+    if (T->n_old < 1) { memcpy(T->vm_old, T->vm, sizeof(double) * (size_t)T->n); T->n_old = 1; }
+    if (T->d.ddt_backward && T->n_old < 2) {
+        memcpy(T->vm_oldold, T->vm_old, sizeof(double) * (size_t)T->n);
+        T->n_old = 2;
+    }
+    const double chicm = T->d.chi * T->d.cm;
+    const double rdt = 1.0 / dt;
+    const double* V = T->mesh->vol;
+    const int* l = T->mesh->owner;
+    const int* u = T->mesh->neigh;
+    double* div = T->tmp;
+    for (long c = 0; c < T->n; c++) div[c] = 0.0;
+    for (long f = 0; f < T->nf; f++) {
+        double flux = T->lap[f] * (T->vm[u[f]] - T->vm[l[f]]);
+        div[l[f]] += flux;
+        div[u[f]] -= flux;
+    }
+    for (long c = 0; c < T->n; c++) {
+        double diag, src;
+        if (T->d.ddt_backward) {
+            diag = chicm * ((cft * rdt) * V[c]);
+            src = chicm * (rdt * V[c] * (cft0 * T->vm_old[c] - cft00 * T->vm_oldold[c]));
+        } else {
+            diag = chicm * (rdt * V[c]);
+            src = chicm * (rdt * T->vm_old[c] * V[c]);
+        }
+        double lapc = div[c] / V[c];
+        double rhs = lapc - chicm * T->iion[c] + T->src[c];
+        src = src + rhs * V[c];
+        T->vm[c] = src / diag;
+    }
+    return 0;
+}
+
+/* MyocardiumDomain::updateActivationTime (myocardiumDomain.C:345-374) */
+static void update_activation(oracle_tissue* T, double dt)
+{
+    const double old_time = T->t - dt;
+    for (long c = 0; c < T->n; c++) {
+        if (T->calc_act[c] && T->vm[c] > 1e-15) {
+            T->calc_act[c] = 0;
+            double w = (0.0 - T->vm_old[c]) / (T->vm[c] - T->vm_old[c]);
+            T->act[c] = old_time + w * dt;
+        }
+    }
+}
+
+/* Advance by dt [s]: runTime++ then electroModel::evolve with the staggered
+ * advance scheme (stimulus -> ionic -> diffusion -> activation time). */
+int oracle_tissue_step(oracle_tissue* T, double dt, int nthreads)
+{
+    if (!T->ionic) {
+        T->ionic = oracle_ionic_new(T->d.model, T->n, T->d.tissue, dt, 0, &T->d.ode, NULL, NULL);
+        if (!T->ionic) return -1;
+    }
+    /* Time::operator++ : value += deltaT; store old-time levels of Vm */
+    T->t = T->t + dt;
+    T->time_index++;
+    if (T->n_old >= 1) {
+        if (T->n_old >= 2) memcpy(T->vm_oldold, T->vm_old, sizeof(double) * (size_t)T->n);
+        memcpy(T->vm_old, T->vm, sizeof(double) * (size_t)T->n);
+    }
+    const double t0 = T->t - dt;
+    update_stimulus(T, t0);
+    if (oracle_ionic_solve(T->ionic, t0, dt, T->vm, T->iion, nthreads) < 0) return -1;
+    T->n_solves = 0;
+    int total = 0;
+    if (T->d.implicit) {
+        /* pimpleControl loop: from the second corrector on, residualControl
+         * compares the initial residual of the latest Vm solve with the
+         * tolerance; once met, one final corrector still runs, then the loop
+         * ends (pimpleLoop::loop / criteriaSatisfied, restated) */
+        int converged = 0;
+        for (int corr = 1; corr <= T->d.n_outer && !converged; corr++) {
+            if (corr > 1 && T->init_res[T->n_solves - 1] < T->d.outer_tol) converged = 1;
+            int it = solve_implicit(T, dt);
+            if (it < 0) return -1;
+            total += it;
+        }
+    } else {
+        solve_explicit(T, dt);
+    }
+    if (T->n_old < 1) { memcpy(T->vm_old, T->vm, sizeof(double) * (size_t)T->n); T->n_old = 1; }
+    update_activation(T, dt);
+    return total;
+}
+
+/* ------------------------------------------------------------------------ */
+/* single cell                                                              */
+
+long oracle_single_cell(int model, int tissue, double dt, long n_steps,
+                        const oracle_ode_settings* ode, const oracle_stimulus* stim,
+                        const double* scales, double* vm_trace, double* final_states)
+{
+    oracle_ionic* io = oracle_ionic_new(model, 1, tissue, dt, 1, ode, stim, scales);
+    if (!io) return -1;
+    const model_info* m = io->m;
+    double t = 0.0, dummy_vm = 0.0, dummy_im = 0.0;
+    long total = 0;
+    for (long s = 0; s < n_steps; s++) {
+        t = t + dt;
+        long k = oracle_ionic_solve(io, t - dt, dt, &dummy_vm, &dummy_im, 1);
+        if (k < 0) { oracle_ionic_free(io); return -1; }
+        total += k;
+        double u = io->y[0];
+        double vm = m->vm_map == 1 ? u * 100 - 80 : m->vm_map == 2 ? u * 85.7 - 84.0 : u;
+        if (vm_trace) vm_trace[s] = vm;
+    }
+    if (final_states) memcpy(final_states, io->y, sizeof(double) * (size_t)m->ns);
+    oracle_ionic_free(io);
+    return total;
+}

@@ -1,0 +1,126 @@
+/* CPU oracle for the monodomain time step - TEST INFRASTRUCTURE ONLY.
+ *
+ * A plain-C restatement of the reference's algorithm for cardiacFoam's
+ * MonodomainSolver step, used by tests/, the smoke check and bench.py's CPU
+ * baseline leg as the checker; the product never links it.
+ *
+ *  - ionic update: <Model>::solveODE (e.g. src/ionicModels/TNNP/TNNP.C:114-179)
+ *    driving OpenFOAM's RKF45 ODESolver (restated from the published
+ *    Fehlberg 4(5) method and OpenFOAM's adaptiveSolver/ODESolver step control,
+ *    which live outside the reference tree);
+ *  - box stimulus and activation time: MyocardiumDomain
+ *    (src/electroModels/electroDomains/myocardiumDomain/myocardiumDomain.C:307-374);
+ *  - diffusion: MonodomainSolver::solveDiffusionImplicit/Explicit
+ *    (src/electroModels/myocardiumModels/monodomainSolver/monodomainSolver.C:103-150)
+ *    with OpenFOAM's Gauss-linear-corrected Laplacian, Euler/backward ddt,
+ *    lduMatrix PCG with DIC or diagonal preconditioning, and the PIMPLE
+ *    residual control of the tutorials' fvSolution - restated.
+ *
+ * Parity status: the ionic right-hand sides are pinned bit-for-bit against
+ * the reference's own generated headers (golden vectors under tests/golden);
+ * RKF45 is pinned by the reference's single-cell regression values; the
+ * implicit PCG path has no reference test and is "parity unpinned".
+ */
+#ifndef ORACLE_H
+#define ORACLE_H
+
+#include "oracle_common.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum { ORACLE_TNNP = 0, ORACLE_ORD = 1, ORACLE_TORORD = 2, ORACLE_ALIEV = 3,
+       ORACLE_BUENO = 4, ORACLE_NMODELS = 5 };
+
+/* --- model-level entry points (golden-vector pins) --------------------- */
+int oracle_model_sizes(int model, int* ns, int* na, int* nc);
+void oracle_model_init(int model, int tissue, double* C, double* y, const double* scale);
+/* constants the reference's initConsts leaves unset (ORd's Na/K pump and
+ * upScale); the ionic and tissue paths apply it after oracle_model_init */
+void oracle_model_supplement(int model, double* C);
+void oracle_model_rates(int model, double t, const double* C, const double* y,
+                        double* dydt, double* alg, int tissue, int solve_vm,
+                        const oracle_stimulus* stim);
+void oracle_model_variables(int model, double t, const double* C, const double* y,
+                            double* rates, double* alg, int tissue, int solve_vm,
+                            const oracle_stimulus* stim);
+int oracle_model_iion_index(int model);
+
+/* --- ODE solver settings (ODESolver/adaptiveSolver dictionary keys) ----- */
+typedef struct oracle_ode_settings {
+    double abs_tol, rel_tol;     /* absTol (default 1e-15), relTol (1e-4) */
+    long max_steps;              /* maxSteps (10000) */
+    double safe_scale, min_scale, max_scale, alpha_inc, alpha_dec;
+} oracle_ode_settings;
+void oracle_ode_default(oracle_ode_settings* s);
+
+/* --- ionic model over N cells (one ionicModel instance) ----------------- */
+typedef struct oracle_ionic oracle_ionic;
+oracle_ionic* oracle_ionic_new(int model, long n, int tissue, double initial_dt,
+                               int solve_vm, const oracle_ode_settings* ode,
+                               const oracle_stimulus* stim, const double* scales);
+void oracle_ionic_free(oracle_ionic*);
+/* ionicModel::solveODE(t0 [s], dt [s], Vm [V], Im [V/s]); returns the total
+ * number of accepted RKF45 substeps, or -1 on maxSteps overflow.  nthreads>1
+ * splits the independent cells over OpenMP threads. */
+long oracle_ionic_solve(oracle_ionic*, double t0, double dt, const double* vm,
+                        double* im, int nthreads);
+double* oracle_ionic_states(oracle_ionic*);   /* AoS: cell*ns + i */
+double* oracle_ionic_steps(oracle_ionic*);
+long oracle_ionic_rhs_evals(oracle_ionic*);
+
+/* --- structured hex mesh (blockMesh single block, x fastest) ------------ */
+typedef struct oracle_mesh oracle_mesh;
+oracle_mesh* oracle_mesh_box(int nx, int ny, int nz, double lx, double ly, double lz);
+void oracle_mesh_free(oracle_mesh*);
+long oracle_mesh_ncells(const oracle_mesh*);
+long oracle_mesh_nfaces(const oracle_mesh*);
+void oracle_mesh_addressing(const oracle_mesh*, int* owner, int* neighbour);
+void oracle_mesh_centres(const oracle_mesh*, double* c);
+
+/* --- monodomain tissue model -------------------------------------------- */
+typedef struct oracle_tissue_desc {
+    int model, tissue;
+    double sigma[6];                 /* xx xy xz yy yz zz [S/m] */
+    double chi, cm;                  /* [1/m], [F/m^2] */
+    int implicit;                    /* solutionAlgorithm implicit/explicit */
+    int ddt_backward;                /* ddtSchemes backward (1) or Euler (0) */
+    int precond_dic;                 /* 1 = DIC, 0 = diagonal */
+    double pcg_tol, pcg_rel_tol;     /* fvSolution solver tolerance / relTol */
+    int pcg_max_iter;                /* default 1000 */
+    int n_outer;                     /* PIMPLE nOuterCorrectors */
+    double outer_tol;                /* PIMPLE residualControl tolerance */
+    double vm0;                      /* initial Vm [V] (-0.084) */
+    int n_boxes;
+    double box_min[8][3], box_max[8][3];
+    double box_start[8], box_duration[8], box_intensity[8];   /* s, s, A/m^3 */
+    oracle_ode_settings ode;
+} oracle_tissue_desc;
+
+typedef struct oracle_tissue oracle_tissue;
+oracle_tissue* oracle_tissue_new(const oracle_tissue_desc*, const oracle_mesh*);
+void oracle_tissue_free(oracle_tissue*);
+/* One runTime++ / evolve(): returns PCG iterations of the step (all outer
+ * correctors), or -1 on failure.  `nthreads` parallelises the ionic loop. */
+int oracle_tissue_step(oracle_tissue*, double dt, int nthreads);
+double oracle_tissue_time(const oracle_tissue*);
+double* oracle_tissue_vm(oracle_tissue*);
+double* oracle_tissue_iion(oracle_tissue*);
+double* oracle_tissue_activation(oracle_tissue*);
+double* oracle_tissue_source(oracle_tissue*);
+oracle_ionic* oracle_tissue_ionic(oracle_tissue*);
+int oracle_tissue_last_solves(const oracle_tissue*, double* init_res, double* final_res,
+                              int* iters, int max_solves);
+
+/* --- single cell (SingleCellSolver::evolve) ------------------------------ */
+/* Runs n_steps of dt [s] from t=0 with Vm inside the ODE; writes the
+ * membrane potential in mV after each step into vm_trace (n_steps values). */
+long oracle_single_cell(int model, int tissue, double dt, long n_steps,
+                        const oracle_ode_settings* ode, const oracle_stimulus* stim,
+                        const double* scales, double* vm_trace, double* final_states);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

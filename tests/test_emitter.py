@@ -1,0 +1,58 @@
+"""cellML2foam-to-CUDA emitter: parser units and reproducibility."""
+import os
+from pathlib import Path
+
+import pytest
+
+from cardiacfoam_gb300.cellml2cuda import cexpr
+from cardiacfoam_gb300.cellml2cuda.emit import emit_c, emit_cuda
+from cardiacfoam_gb300.cellml2cuda.model import WRAPPERS, load_model, use_before_def
+
+ROOT = Path(__file__).resolve().parents[1]
+REF = Path(os.environ.get("CARDIACFOAM_REFERENCE", "/root/reference")) / "src" / "ionicModels"
+
+
+def test_parser_precedence():
+    e = cexpr.parse_expr("- 56.86 - STATES[V] / 2.0 * x")
+    assert isinstance(e, cexpr.Bin) and e.op == "-"
+    assert isinstance(e.l, cexpr.Unary)
+    c = cexpr.parse_expr("a < - 40.0 ? 1.0 : b == 2 ? 3 : 4")
+    assert isinstance(c, cexpr.Cond) and isinstance(c.b, cexpr.Cond)
+    p = cexpr.parse_expr("pow(STATES[Ca_i] / 0.000325, 8.00000)")
+    assert isinstance(p, cexpr.Call) and p.fn == "pow"
+    with pytest.raises(cexpr.ParseError):
+        cexpr.parse_expr("a ^ b")
+
+
+def test_generated_files_present():
+    for name in WRAPPERS:
+        key = name.lower()
+        assert (ROOT / "cardiacfoam_gb300" / "csrc" / "models" / f"{key}.cuh").exists()
+        assert (ROOT / "oracle" / "models" / f"{key}.h").exists()
+
+
+@pytest.mark.skipif(not REF.is_dir(), reason="reference checkout not available")
+@pytest.mark.parametrize("name", list(WRAPPERS))
+def test_regeneration_is_identical(name):
+    m = load_model(REF, name)
+    rel = f"src/ionicModels/{WRAPPERS[name]['dir']}/{WRAPPERS[name]['header']}"
+    key = name.lower()
+    assert emit_cuda(m, rel) == (ROOT / "cardiacfoam_gb300/csrc/models" / f"{key}.cuh").read_text()
+    assert emit_c(m, rel) == (ROOT / "oracle/models" / f"{key}.h").read_text()
+
+
+@pytest.mark.skipif(not REF.is_dir(), reason="reference checkout not available")
+def test_use_before_def_is_only_istim():
+    for name in WRAPPERS:
+        m = load_model(REF, name)
+        assert set(use_before_def(m.rates)) <= {"Istim"}
+
+
+@pytest.mark.skipif(not REF.is_dir(), reason="reference checkout not available")
+def test_supplement_covers_exactly_the_unassigned_constants():
+    from cardiacfoam_gb300.cellml2cuda.emit import SUPPLEMENT, supplement_for, unassigned_constants
+    for name in WRAPPERS:
+        m = load_model(REF, name)
+        sup = supplement_for(m)          # raises on any mismatch
+        assert [c for c, _ in sup] == [c for c, _ in SUPPLEMENT.get(name, [])]
+        assert (len(unassigned_constants(m)) > 0) == (name == "ORd")

@@ -1,0 +1,125 @@
+"""GPU monodomain step (cfg_monodomain_* through the C ABI) against the oracle."""
+import numpy as np
+import pytest
+
+from cardiacfoam_gb300 import api, lib
+from cardiacfoam_gb300.mesh import box_mesh
+
+SIGMA = (0.1334, 0.0, 0.0, 0.0176, 0.0, 0.0176)
+BOX = [((0.0, 0.0, 0.0), (1.5e-3, 1.5e-3, 1.5e-3), 0.0, 2e-3, 5e4)]
+
+
+def run_pair(oracle, model, tissue, nsteps, dt=1e-5, implicit=True, precond_dic=False,
+             precision=lib.PRECISION_FP64, dims=(20, 7, 3), h=1e-3, stencil=True,
+             pcg_tol=1e-8):
+    nx, ny, nz = dims
+    mesh = box_mesh(nx, ny, nz, nx * h, ny * h, nz * h)
+    g = api.Monodomain(mesh, model, tissue, SIGMA, dt=dt, precision=precision,
+                       implicit=implicit, boxes=BOX, stencil=stencil, pcg_tol=pcg_tol)
+    om = oracle.Mesh(nx, ny, nz, nx * h, ny * h, nz * h)
+    d = oracle.tissue_desc(model, api.TISSUE_FLAGS[tissue], SIGMA, implicit=implicit,
+                           precond_dic=precond_dic, boxes=BOX, pcg_tol=pcg_tol)
+    o = oracle.Tissue(d, om)
+    stats = []
+    for s in range(nsteps):
+        g.step(dt)
+        o.step(dt, 4)
+        if implicit:
+            stats.append((g.stats(), o.solves()))
+    return g, o, stats
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("model,tissue", [("TNNP", "epicardialCells"), ("ORd", "myocyte")])
+def test_implicit_fp64_matches_oracle_same_preconditioner(gpu_lib, oracle, model, tissue):
+    g, o, stats = run_pair(oracle, model, tissue, 300)
+    vg, vo = g.vm(), o.vm()
+    assert np.max(np.abs(vg - vo) / np.abs(vo)) < 1e-9
+    ag, ao = g.activation(), o.activation()
+    assert np.array_equal(ag > 0, ao > 0)
+    assert np.max(np.abs(ag - ao)) < 1e-9
+    for (gi, gf, git), (oi, of, oit) in stats:
+        assert len(git) == len(oit)
+        assert np.array_equal(git, oit)
+        # residuals agree to 1e-6 where they are resolved; below the PCG
+        # tolerance they are round-off of the converged field
+        big = np.maximum(np.abs(gi), np.abs(oi)) > 1e-9
+        assert np.allclose(gi[big], oi[big], rtol=1e-6)
+        assert np.all(gi[~big] < 1e-8) and np.all(oi[~big] < 1e-8)
+    assert abs(g.time() - o.time()) == 0.0
+
+
+@pytest.mark.gpu
+def test_implicit_fp64_against_dic_reference_solver(gpu_lib, oracle):
+    """The reference's own preconditioner (DIC) converges to the same field
+    within the PCG tolerance."""
+    g, o, _ = run_pair(oracle, "TNNP", "epicardialCells", 300, precond_dic=True)
+    vg, vo = g.vm(), o.vm()
+    assert np.max(np.abs(vg - vo) / np.abs(vo)) < 1e-6
+    ag, ao = g.activation(), o.activation()
+    assert np.array_equal(ag > 0, ao > 0)
+    assert np.max(np.abs(ag - ao)) <= 1e-5       # within one dt
+
+
+@pytest.mark.gpu
+def test_general_ell_operator_matches_stencil(gpu_lib, oracle):
+    g1, o, _ = run_pair(oracle, "TNNP", "epicardialCells", 100, stencil=False)
+    assert np.max(np.abs(g1.vm() - o.vm()) / np.abs(o.vm())) < 1e-9
+
+
+@pytest.mark.gpu
+def test_explicit_fp64_matches_oracle(gpu_lib, oracle):
+    g, o, _ = run_pair(oracle, "TNNP", "epicardialCells", 300, implicit=False)
+    vg, vo = g.vm(), o.vm()
+    assert np.max(np.abs(vg - vo) / np.abs(vo)) < 1e-9
+    assert np.max(np.abs(g.activation() - o.activation())) < 1e-9
+
+
+@pytest.mark.gpu
+def test_mixed_precision_activation_error(gpu_lib, oracle):
+    dims, h, dt, n = (20, 7, 3), 1e-3, 1e-5, 1500
+    mesh = box_mesh(*dims, dims[0] * h, dims[1] * h, dims[2] * h)
+    a = api.Monodomain(mesh, "TNNP", "epicardialCells", SIGMA, dt=dt, boxes=BOX)
+    b = api.Monodomain(mesh, "TNNP", "epicardialCells", SIGMA, dt=dt, boxes=BOX,
+                       precision=lib.PRECISION_MIXED)
+    for s in range(n):
+        a.step(dt)
+        b.step(dt)
+    aa, ab = a.activation(), b.activation()
+    assert np.array_equal(aa > 0, ab > 0)
+    assert np.max(np.abs(aa - ab)) <= 5e-5          # <= 0.05 ms
+
+
+@pytest.mark.gpu
+def test_dictionary_front_end_equals_direct(gpu_lib):
+    text = """
+myocardiumSolver  monodomainSolver;
+monodomainSolverCoeffs
+{
+    conductivity [-1 -3 3 0 0 2 0] (0.1334 0 0 0.0176 0 0.0176);
+    chi   [0 -1 0 0 0 0 0] 140000;
+    cm    [-1 -4 4 0 0 2 0] 0.01;
+    ionicModel    TNNP;
+    tissue    epicardialCells;
+    solutionAlgorithm implicit;
+    solver RKF45;
+    maxSteps 1000000000;
+    externalStimulus
+    {
+        stimulusLocationMin (0 0 0);
+        stimulusLocationMax (1.5e-3 1.5e-3 1.5e-3);
+        stimulusDuration [0 0 1 0 0 0 0] 2e-3;
+        stimulusIntensity [0 -3 0 0 0 1 0] 50000;
+        stimulusStartTime 0.0;
+    }
+}
+"""
+    dt = 1e-5
+    mesh = box_mesh(20, 7, 3, 0.02, 0.007, 0.003)
+    a = api.Monodomain.from_dict(text, mesh, dt)
+    b = api.Monodomain(mesh, "TNNP", "epicardialCells", SIGMA, dt=dt, boxes=BOX)
+    for _ in range(50):
+        a.step(dt)
+        b.step(dt)
+    assert np.array_equal(a.vm(), b.vm())
+    assert np.array_equal(a.source(), b.source())
