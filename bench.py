@@ -104,10 +104,16 @@ def build_mesh():
     return box_mesh(nx, ny, nz, nx * H, ny * H, nz * H)
 
 
+GRAPH = True
+
+
 def make_model(mesh, precision):
     from cardiacfoam_gb300 import api
-    return api.Monodomain(mesh, "ORd", "myocyte", SIGMA, dt=DT, precision=precision, boxes=BOX,
-                          max_steps=10 ** 6)
+    m = api.Monodomain(mesh, "ORd", "myocyte", SIGMA, dt=DT, precision=precision, boxes=BOX,
+                       max_steps=10 ** 6)
+    if not GRAPH:
+        m.set_graph(False)   # every kernel launched on its own (for per-kernel profiling)
+    return m
 
 
 def timed_steps(md, k, flush):
@@ -281,7 +287,11 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--ref-steps", type=int, default=10)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-graph", action="store_true",
+                    help="host-driven PIMPLE/PCG loops instead of the step graph")
     args = ap.parse_args()
+    global GRAPH
+    GRAPH = not args.no_graph
     if args.warmup < 3 and args.impl == "gb300":
         args.warmup = 3
     rank = int(os.environ.get("RANK", "0"))

@@ -241,6 +241,9 @@ class Monodomain:
         _L.check(self._lib.cfg_ionic_rhs_evaluations(ion, C.byref(v)))
         return v.value
 
+    def set_graph(self, enable: bool = True):
+        _L.check(self._lib.cfg_monodomain_set_graph(self.h, int(enable)))
+
     def set_timing(self, enable: bool = True):
         _L.check(self._lib.cfg_monodomain_set_timing(self.h, int(enable)))
 

@@ -21,6 +21,10 @@ LIB = PKG / "libcardiac_gpu.so"
 INCLUDE = PKG.parent / "include"
 
 MODELS = ["tnnp", "ord", "torord_dyncl", "alievpanfilov", "buenoorovio"]
+# per-model unroll factor of the per-state loops around the right-hand side
+# (measured on GB300: ORd fastest at 4, the others at 1)
+STATE_UNROLL = {"ord": 4}
+
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
           "-Xcompiler", "-ffp-contract=off", "-I", str(CSRC), "-I", str(INCLUDE)]
@@ -35,15 +39,25 @@ def nvcc() -> str:
 
 def _units():
     units = []
+    # register budget of the ionic kernels: resident 128-thread blocks per SM
+    mb = os.environ.get("CFG_IONIC_MIN_BLOCKS")
+    ionic_extra = [f"-DCFG_IONIC_MIN_BLOCKS={int(mb)}"] if mb else []
+    unroll = os.environ.get("CFG_IONIC_STATE_UNROLL")
+    if unroll:
+        ionic_extra.append(f"-DCFG_IONIC_STATE_UNROLL={int(unroll)}")
     for m in MODELS:
         for prec, flags in (("fp64", ["--fmad=false", "-DCFG_FP64=1"]),
-                            ("mixed", ["--fmad=true", "-DCFG_FP64=0"])):
+                            ("mixed", ["--use_fast_math", "-DCFG_FP64=0"])):
+            extra = list(ionic_extra)
+            if not unroll and m in STATE_UNROLL:
+                extra.append(f"-DCFG_IONIC_STATE_UNROLL={STATE_UNROLL[m]}")
             units.append((f"ionic_{m}_{prec}", CSRC / "ionic_instance.cu",
-                          flags + [f"-DCFG_MODEL={m}"]))
+                          flags + [f"-DCFG_MODEL={m}"] + extra))
     units.append(("ionic_registry", CSRC / "ionic_registry.cu", []))
     units.append(("ionic", CSRC / "ionic.cu", []))
     units.append(("diffusion", CSRC / "diffusion.cu", []))
     units.append(("monodomain", CSRC / "monodomain.cu", []))
+    units.append(("step_graph", CSRC / "step_graph.cu", []))
     units.append(("dictionary", CSRC / "dictionary.cpp", []))
     return units
 

@@ -227,8 +227,10 @@ class _CudaPrinter(_Printer):
             return f"(({self(a[0])}) > R(0) ? 1 : 0)" if self.mode != "init" \
                 else f"(({self(a[0])}) > 0.0 ? 1 : 0)"
         if c.fn == "computeIstim":
-            # stimulus timing stays in double in every precision
-            return "R(cfg_stimulus_current<double>(t, stim))"
+            # stimulus timing stays in double in every precision; tissue runs
+            # (SOLVE_VM false) have no single-cell stimulus: the reference
+            # refuses an active one (myocardiumDomain.C:377-394)
+            return "(SOLVE_VM ? R(cfg_stimulus_current<double>(t, stim)) : R(0))"
         if c.fn == "tissueSelect":
             return (f"((tissue == 3) ? {self(a[1])} : (tissue == 2) ? {self(a[2])} "
                     f": {self(a[3])})")
@@ -277,6 +279,31 @@ def _predeclare_conditional_algebraics(m: Model, stmts, out, indent):
     return sorted(inside)
 
 
+def constant_values(m: Model, tissue: int) -> List[float]:
+    """initConsts (plus the supplement) evaluated with IEEE double arithmetic
+    for one tissue flag; the order of operations is the header's, and exp/log/
+    pow/sqrt come from the C library as in the reference."""
+    from .opcount import _Eval
+    ev = _Eval(m, {}, {}, tissue)
+    ev.run(m.init, "init")
+    out = []
+    for c in m.constants:
+        v = ev.C.get(c, 0.0)
+        out.append(float(v))
+    for c, expr in supplement_for(m):
+        out[m.constants.index(c)] = float(eval(expr))
+    return out
+
+
+def _cxx_double(v: float) -> str:
+    if v != v:
+        return "__builtin_nan(\"\")"
+    if v in (float("inf"), float("-inf")):
+        return ("-" if v < 0 else "") + "__builtin_huge_val()"
+    r = repr(float(v))
+    return r if ("e" in r or "." in r or "inf" in r) else r + ".0"
+
+
 def emit_cuda(m: Model, src_rel: str) -> str:
     ns = ident(m.name)
     L: List[str] = []
@@ -306,6 +333,7 @@ def emit_cuda(m: Model, src_rel: str) -> str:
            for t in m.tissues]
     L.append("constexpr int N_TISSUES = %d;" % len(tis))
     L.append("static const int TISSUES[] = {" + ", ".join(str(t) for t in tis) + ", 0};")
+    L.append("using TissueSet = TissueList<" + ", ".join(str(t) for t in tis) + ">;")
     L.append("static const char* const STATE_NAMES[NS] = {" +
              ", ".join(f'"{s}"' for s in m.states) + "};")
     L.append("CFG_HD inline bool tissue_supported(int t) { return " +
@@ -341,6 +369,23 @@ def emit_cuda(m: Model, src_rel: str) -> str:
         for c, v in sup:
             L.append(f"    C[C_{c}] = {v};")
     L.append("}")
+    L.append("")
+    # per-tissue constant tables, folded into the kernels as immediates
+    L.append("// initConsts evaluated per tissue flag (IEEE double, the header's order of")
+    L.append("// operations): cval<T>(i) is constant i for tissue T.  Kernels for one uniform")
+    L.append("// tissue without per-cell scales read constants from here, so the compiler")
+    L.append("// folds them into the instructions.")
+    L.append("template <int T> CFG_HD constexpr double cval(int i);")
+    for t in tis:
+        vals = constant_values(m, t)
+        L.append(f"template <> CFG_HD constexpr double cval<{t}>(int i)")
+        L.append("{")
+        L.append("    switch (i) {")
+        for k, v in enumerate(vals):
+            L.append(f"    case {k}: return {_cxx_double(v)};")
+        L.append("    default: return 0.0;")
+        L.append("    }")
+        L.append("}")
     L.append("")
     # rhs
     early = use_before_def(m.rates)
@@ -390,6 +435,8 @@ def emit_cuda(m: Model, src_rel: str) -> str:
     L.append("    static constexpr int VM_MAP = " + ns + "::VM_MAP;")
     L.append("    CFG_HD static __forceinline__ void init(double* C, double* y, int tissue, "
              "const double* scale) { init_consts(C, y, tissue, scale); }")
+    L.append("    template <int T> CFG_HD static constexpr double constant(int i) "
+             "{ return cval<T>(i); }")
     L.append("    template <class R, bool SV, class YS, class KS>")
     L.append("    __device__ static __forceinline__ R rates(double t, const YS& Y, const KS& K, "
              "R* dydt, int tissue, const CfgStimulus& st) { return rhs<R, SV>(t, Y, K, dydt, "

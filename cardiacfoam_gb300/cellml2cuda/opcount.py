@@ -30,7 +30,7 @@ class _Eval:
     def ev(self, e):
         n = self.n
         if isinstance(e, Num):
-            return e.value
+            return int(e.text) if e.is_int_literal else e.value
         if isinstance(e, Ref):
             if e.array == "STATES":
                 return self.Y[e.name]

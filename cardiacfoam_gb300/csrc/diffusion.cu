@@ -1,5 +1,8 @@
 // Kernels of the diffusion half of the monodomain step (see
 // diffusion_kernels.cuh for the formulation and the reduction scheme).
+// Each thread owns one row; the ddt coefficients, the diagonal and its
+// reciprocal are precomputed per dt, so the per-step kernels carry no FP64
+// division (GB300's FP64 pipe, not HBM, would otherwise bound them).
 #include "diffusion_kernels.cuh"
 
 namespace cfg {
@@ -24,33 +27,45 @@ __global__ void k_step_begin(DiffusionArgs a)
         st->solve_active = 0;
         st->n_solves = 0;
         st->iter = 0;
+        st->step_iters = 0;
     }
 }
 
-// Start of one PIMPLE corrector: assemble the diagonal and the source of
+// Diagonal (chi*Cm*coefft*V/dt + sum of face coefficients), its reciprocal
+// and the row sums of both ddt coefficient sets; recomputed when dt changes.
+__global__ void k_prepare(DiffusionArgs a)
+{
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= a.n) return;
+    const double V = a.vol[c];
+    for (int v = 0; v < 2; ++v) {
+        const double ddt_diag = a.ddt_backward ? (a.cft[v] * a.rdt) * V : a.rdt * V;
+        const double d = a.chicm * ddt_diag - a.lapdiag[c];
+        a.diag2[v * a.n + c] = d;
+        a.rdiag2[v * a.n + c] = 1.0 / d;
+        a.sumA2[v * a.n + c] = row_sum(a, c, d);
+    }
+}
+
+// Start of one PIMPLE corrector: the source of
 //   chi*Cm*ddt(Vm) - laplacian(sigma,Vm) = -chi*Cm*Iion + src
-// (backward/Euler fvmDdt, fvmLaplacianUncorrected, fvMatrix sources), then
-// the residual r = b - A.x and the sums for lduMatrix::solver::normFactor.
+// (backward/Euler fvmDdt, fvMatrix sources, box stimulus), the residual
+// r = b - A.x and the sums for lduMatrix::solver::normFactor.
 __global__ void __launch_bounds__(kDiffBlock) k_solve_begin(DiffusionArgs a)
 {
     PcgState* st = a.st;
     if (!st->outer_active) return;
     const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    double v[2] = {0.0, 0.0};
+    const int v = ddt_variant(a, st->n_old);
+    double vals[2] = {0.0, 0.0};
     if (c < a.n) {
-        double cft, cft0, cft00;
-        ddt_coeffs(a, st->n_old, cft, cft0, cft00);
-        const double rdt = 1.0 / a.dt;
         const double V = a.vol[c];
-        double ddt_diag, ddt_src;
-        if (a.ddt_backward) {
-            ddt_diag = (cft * rdt) * V;
-            ddt_src = rdt * V * (cft0 * a.vm_old[c] - cft00 * a.vm_oldold[c]);
-        } else {
-            ddt_diag = rdt * V;
-            ddt_src = rdt * a.vm_old[c] * V;
-        }
-        const double d = a.chicm * ddt_diag - a.lapdiag[c];
+        double ddt_src;
+        if (a.ddt_backward)
+            ddt_src = a.rdt * V * (a.cft0[v] * a.vm_old[c] - a.cft00[v] * a.vm_oldold[c]);
+        else
+            ddt_src = a.rdt * a.vm_old[c] * V;
+        const double d = a.diag2[v * a.n + c];
         double bb = a.chicm * ddt_src;
         double su = -(a.chicm * a.iion[c]) * V;
         su = su + box_source(a, c, st->t0) * V;
@@ -58,15 +73,13 @@ __global__ void __launch_bounds__(kDiffBlock) k_solve_begin(DiffusionArgs a)
         const double* x = a.vm;
         const double ax = row_amul(a, c, d, [x](long long q) { return x[q]; });
         const double r = bb - ax;
-        a.diag[c] = d;
         a.b[c] = bb;
         a.ax[c] = ax;
         a.r[c] = r;
-        a.sumA[c] = row_sum(a, c, d);
-        v[0] = x[c];
-        v[1] = fabs(r);
+        vals[0] = x[c];
+        vals[1] = fabs(r);
     }
-    block_partials<2>(a, v);
+    block_partials<2>(a, vals);
     if (last_block(a, 0)) {
         const double sx = sum_partials(a, 0);
         const double sr = sum_partials(a, 1);
@@ -74,6 +87,7 @@ __global__ void __launch_bounds__(kDiffBlock) k_solve_begin(DiffusionArgs a)
             st->sum_x = sx;
             st->avg = sx / double(a.n);
             st->sum_absr = sr;
+            st->variant = v;
             // fvm::ddt created Vm.oldTime() (and its old time for backward)
             if (st->n_old < 1) st->n_old = 1;
             if (a.ddt_backward && st->n_old < 2) st->n_old = 2;
@@ -88,17 +102,16 @@ __global__ void __launch_bounds__(kDiffBlock) k_solve_norm(DiffusionArgs a)
     PcgState* st = a.st;
     if (!st->outer_active) return;
     const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    double v[2] = {0.0, 0.0};
+    const int v = st->variant;
+    double vals[2] = {0.0, 0.0};
     if (c < a.n) {
-        const double pa = a.sumA[c] * st->avg;
-        v[0] = fabs(a.ax[c] - pa) + fabs(a.b[c] - pa);
-        const double rd = 1.0 / a.diag[c];
-        const double z = rd * a.r[c];
-        a.rD[c] = rd;
+        const double pa = a.sumA2[v * a.n + c] * st->avg;
+        vals[0] = fabs(a.ax[c] - pa) + fabs(a.b[c] - pa);
+        const double z = a.rdiag2[v * a.n + c] * a.r[c];
         a.z[c] = z;
-        v[1] = z * a.r[c];
+        vals[1] = z * a.r[c];
     }
-    block_partials<2>(a, v);
+    block_partials<2>(a, vals);
     if (last_block(a, 1)) {
         const double nf = sum_partials(a, 0);
         const double zr = sum_partials(a, 1);
@@ -113,6 +126,7 @@ __global__ void __launch_bounds__(kDiffBlock) k_solve_norm(DiffusionArgs a)
             } else {
                 st->solve_active = 1;
             }
+            set_inner(a, st->solve_active);
         }
     }
 }
@@ -130,16 +144,16 @@ __global__ void __launch_bounds__(kDiffBlock) k_pcg_p(DiffusionArgs a)
     const double* pold = (it & 1) ? a.pA : a.pB;
     double* pnew = (it & 1) ? a.pB : a.pA;
     const double* z = a.z;
-    double v[1] = {0.0};
+    double vals[1] = {0.0};
     if (c < a.n) {
         auto p = [=](long long q) { return it == 0 ? z[q] : z[q] + beta * pold[q]; };
         const double pc = p(c);
-        const double ap = row_amul(a, c, a.diag[c], p);
+        const double ap = row_amul(a, c, a.diag2[st->variant * a.n + c], p);
         pnew[c] = pc;
         a.ap[c] = ap;
-        v[0] = ap * pc;
+        vals[0] = ap * pc;
     }
-    block_partials<1>(a, v);
+    block_partials<1>(a, vals);
     if (last_block(a, 2)) {
         const double wApA = sum_partials(a, 0);
         if (threadIdx.x == 0) {
@@ -157,36 +171,46 @@ __global__ void __launch_bounds__(kDiffBlock) k_pcg_p(DiffusionArgs a)
 __global__ void __launch_bounds__(kDiffBlock) k_pcg_update(DiffusionArgs a)
 {
     PcgState* st = a.st;
-    if (!st->solve_active) return;
+    if (!st->solve_active) {   // ended in k_pcg_p (singular)
+        if (blockIdx.x == 0 && threadIdx.x == 0) set_inner(a, 0);
+        return;
+    }
     const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const int it = st->iter;
     const double alpha = st->alpha;
     const double* p = (it & 1) ? a.pB : a.pA;
-    double v[2] = {0.0, 0.0};
+    double vals[2] = {0.0, 0.0};
     if (c < a.n) {
         a.vm[c] += alpha * p[c];
         const double r = a.r[c] - alpha * a.ap[c];
         a.r[c] = r;
-        const double z = a.rD[c] * r;
+        const double z = a.rdiag2[st->variant * a.n + c] * r;
         a.z[c] = z;
-        v[0] = fabs(r);
-        v[1] = z * r;
+        vals[0] = fabs(r);
+        vals[1] = z * r;
     }
-    block_partials<2>(a, v);
+    block_partials<2>(a, vals);
     if (last_block(a, 3)) {
         const double sr = sum_partials(a, 0);
         const double zr = sum_partials(a, 1);
         if (threadIdx.x == 0) {
             st->res = sr / st->normf;
             st->iter = it + 1;
+            st->step_iters += 1;
             if (pcg_converged(st, st->res) || st->iter >= st->max_iter) {
                 if (!pcg_converged(st, st->res)) st->status |= CFG_ERR_PCG;
                 end_solve(st);
+            } else if (st->step_iters >= a.iter_cap) {
+                // guard of the device-driven loops: give up the step
+                st->status |= CFG_ERR_PCG;
+                end_solve(st);
+                st->outer_active = 0;
             } else {
                 st->wArAold = st->wArA;
                 st->wArA = zr;
                 st->beta = st->wArA / st->wArAold;
             }
+            set_inner(a, st->solve_active);
         }
     }
 }
@@ -201,6 +225,9 @@ __device__ __forceinline__ void activation(const DiffusionArgs& a, long long c, 
         a.act[c] = old_time + w * a.dt;
     }
 }
+
+// End of a PIMPLE corrector in the step graph: whether another one runs.
+__global__ void k_outer_cond(DiffusionArgs a) { set_outer(a, a.st->outer_active); }
 
 __global__ void k_activation(DiffusionArgs a)
 {
@@ -219,9 +246,9 @@ __global__ void k_explicit(DiffusionArgs a)
     const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const int n_old = st->n_old;   // read before any block updates it below
     if (c < a.n) {
-        double cft, cft0, cft00;
-        ddt_coeffs(a, n_old, cft, cft0, cft00);
-        const double rdt = 1.0 / a.dt;
+        const int v = ddt_variant(a, n_old);
+        const double cft = a.cft[v], cft0 = a.cft0[v], cft00 = a.cft00[v];
+        const double rdt = a.rdt;
         const double V = a.vol[c];
         const double* x = a.vm_old;
         const double xc = x[c];

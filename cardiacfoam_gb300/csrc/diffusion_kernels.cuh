@@ -34,7 +34,9 @@ struct PcgState {
     int converged_outer;  // residualControl met; the running corrector is the final one
     int iter;             // iterations of the current solve
     int n_solves;
+    int variant;          // ddt coefficient set of the current corrector
     int status;           // CFG_ERR_* bits
+    long long step_iters; // PCG iterations of the current step (loop guard)
     // --- settings
     double tol, rel_tol, outer_tol;
     int max_iter, n_outer;
@@ -69,11 +71,24 @@ struct DiffusionArgs {
     const unsigned char* box_mask;  // [n] bit b: centre inside box b
     int n_boxes;
     double box_start[8], box_end[8], box_intensity[8];
+    // matrix diagonal, its reciprocal (diagonal preconditioner) and row sums
+    // for the two ddt coefficient sets: [0] while fewer than two old-time
+    // levels exist (backward falls back to deltaT0 = GREAT), [1] afterwards
+    double* diag2;             // [2][n]
+    double* rdiag2;            // [2][n]
+    double* sumA2;             // [2][n]
+    double cft[2], cft0[2], cft00[2];
+    double rdt;
     // PCG work
-    double *diag, *rD, *b, *r, *z, *ax, *sumA, *pA, *pB, *ap;
+    double *b, *r, *z, *ax, *pA, *pB, *ap;
     double* partial;           // [4][nblocks]
     int nblocks;
     PcgState* st;
+    // graph control: conditional handles of the PIMPLE and PCG while-nodes
+    // (set only when the kernels run inside the step graph)
+    int use_graph;
+    cudaGraphConditionalHandle h_outer, h_inner;
+    long long iter_cap;        // PCG iterations per step before the step is aborted
     // step constants
     double dt, chicm;
     int ddt_backward;
@@ -173,20 +188,11 @@ __device__ __forceinline__ double row_sum(const DiffusionArgs& a, long long c, d
     return row_amul(a, c, d, [](long long) { return 1.0; });
 }
 
-// ddt coefficients (EulerDdtScheme / backwardDdtScheme with deltaT0 = GREAT
-// while fewer than two old-time levels exist)
-__device__ __forceinline__ void ddt_coeffs(const DiffusionArgs& a, int n_old, double& cft,
-                                           double& cft0, double& cft00)
+// ddt coefficient set in use: backwardDdtScheme takes deltaT0 = GREAT while
+// fewer than two old-time levels exist (Euler has one set)
+__device__ __forceinline__ int ddt_variant(const DiffusionArgs& a, int n_old)
 {
-    if (!a.ddt_backward) {
-        cft = 1.0; cft0 = 1.0; cft00 = 0.0;
-        return;
-    }
-    const double dt = a.dt;
-    const double dt0 = n_old < 2 ? 1e15 : dt;
-    cft = 1 + dt / (dt + dt0);
-    cft00 = dt * dt / (dt0 * (dt + dt0));
-    cft0 = cft + cft00;
+    return (a.ddt_backward && n_old >= 2) ? 1 : 0;
 }
 
 // MyocardiumDomain::updateExternalStimulusCurrent for one cell
@@ -222,6 +228,16 @@ __device__ __forceinline__ void end_solve(PcgState* st)
         st->outer_active = 1;
     }
     st->corr += 1;
+}
+
+// Publish the loop conditions to the step graph's while-nodes.
+__device__ __forceinline__ void set_inner(const DiffusionArgs& a, int v)
+{
+    if (a.use_graph) cudaGraphSetConditional(a.h_inner, unsigned(v));
+}
+__device__ __forceinline__ void set_outer(const DiffusionArgs& a, int v)
+{
+    if (a.use_graph) cudaGraphSetConditional(a.h_outer, unsigned(v));
 }
 
 __device__ __forceinline__ bool pcg_converged(const PcgState* st, double r)

@@ -21,6 +21,10 @@
 
 namespace cfg {
 
+// compile-time list of tissue flags
+template <int... T>
+struct TissueList {};
+
 // ---------------------------------------------------------------- math
 // double: IEEE functions (the plain form); float: single-precision
 // functions (the mixed form).  Integer powers are products, so pow(x, 2.0)

@@ -20,13 +20,34 @@
 using M = cfg::CFG_MODEL::Model;
 static constexpr bool kFP64 = CFG_FP64 != 0;
 
+using cfg::TissueList;
+using Tissues = cfg::CFG_MODEL::TissueSet;
+
+template <int T0, int... TR>
+static bool launch_uniform(const cfg::IonicLaunch& p, cudaStream_t s, unsigned grid, int block,
+                           TissueList<T0, TR...>)
+{
+    if (p.tissue == T0) {
+        cfg::ionic_step_kernel<M, kFP64, false, T0><<<grid, block, 0, s>>>(p);
+        return true;
+    }
+    if constexpr (sizeof...(TR) > 0) return launch_uniform(p, s, grid, block, TissueList<TR...>{});
+    return false;
+}
+
 extern "C" cudaError_t CFG_CAT3(cfg_ionic_step_, CFG_MODEL, CFG_PREC_TAG)(
     const cfg::IonicLaunch& p, int solve_vm, cudaStream_t stream, int block)
 {
     if (p.n <= 0) return cudaSuccess;
     const unsigned grid = unsigned((p.n + block - 1) / block);
-    if (solve_vm) cfg::ionic_step_kernel<M, kFP64, true><<<grid, block, 0, stream>>>(p);
-    else cfg::ionic_step_kernel<M, kFP64, false><<<grid, block, 0, stream>>>(p);
+    const bool uniform = !p.tissue_cell && !p.scales;
+    if (solve_vm) {
+        cfg::ionic_step_kernel<M, kFP64, true, 0><<<grid, block, 0, stream>>>(p);
+    } else if (uniform && launch_uniform(p, stream, grid, block, Tissues{})) {
+        // tissue-specialised kernel launched
+    } else {
+        cfg::ionic_step_kernel<M, kFP64, false, 0><<<grid, block, 0, stream>>>(p);
+    }
     return cudaGetLastError();
 }
 

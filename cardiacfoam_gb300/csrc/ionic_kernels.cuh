@@ -24,7 +24,22 @@
 #include "ionic_common.cuh"
 #include "../../include/cardiac_gpu.h"
 
+// resident 128-thread blocks per SM the ionic kernels are compiled for
+// (register budget 65536 / (128 * blocks))
+#ifndef CFG_IONIC_MIN_BLOCKS
+#define CFG_IONIC_MIN_BLOCKS 2
+#endif
+// unroll factor of the per-state loops around the right-hand side (stage
+// sums, 5th-order update, error norm); 1 keeps the kernel's instruction
+// footprint close to one copy of the model body
+#ifndef CFG_IONIC_STATE_UNROLL
+#define CFG_IONIC_STATE_UNROLL 1
+#endif
+
+
 namespace cfg {
+
+constexpr int kStateUnroll = CFG_IONIC_STATE_UNROLL;
 
 struct IonicLaunch {
     long long n;                     // cells
@@ -62,10 +77,17 @@ struct ArrayView {
     CFG_D __forceinline__ R operator()(int i) const { return a[i]; }
 };
 
+// constants computed at run time (per-cell tissue or conductance scales)
 template <class R>
 struct ConstView {
     const double* c;
     CFG_D __forceinline__ R operator()(int i) const { return R(c[i]); }
+};
+
+// constants of one uniform tissue, known at compile time
+template <class R, class M, int T>
+struct ConstFold {
+    CFG_D __forceinline__ R operator()(int i) const { return R(M::template constant<T>(i)); }
 };
 
 template <unsigned long long MASK>
@@ -121,7 +143,8 @@ CFG_D __forceinline__ double exact_add(double a, double b) { return __dadd_rn(a,
 CFG_D __forceinline__ double exact_sub(double a, double b) { return __dsub_rn(a, b); }
 CFG_D __forceinline__ double exact_mul(double a, double b) { return __dmul_rn(a, b); }
 
-// Stage table of the Fehlberg tableau for the stage loop (row s: a_s,j)
+// Stage table of the Fehlberg tableau for the stage loop (row s: a_s,j),
+// in double for the plain form and float for the mixed form.
 static __constant__ double kRkfA[6][5] = {
     {0, 0, 0, 0, 0},
     {rkf::a21, 0, 0, 0, 0},
@@ -130,12 +153,47 @@ static __constant__ double kRkfA[6][5] = {
     {rkf::a51, rkf::a52, rkf::a53, rkf::a54, 0},
     {rkf::a61, rkf::a62, rkf::a63, rkf::a64, rkf::a65},
 };
+static __constant__ float kRkfAf[6][5] = {
+    {0, 0, 0, 0, 0},
+    {float(rkf::a21), 0, 0, 0, 0},
+    {float(rkf::a31), float(rkf::a32), 0, 0, 0},
+    {float(rkf::a41), float(rkf::a42), float(rkf::a43), 0, 0},
+    {float(rkf::a51), float(rkf::a52), float(rkf::a53), float(rkf::a54), 0},
+    {float(rkf::a61), float(rkf::a62), float(rkf::a63), float(rkf::a64), float(rkf::a65)},
+};
 static __constant__ double kRkfC[6] = {0.0, rkf::c2, rkf::c3, rkf::c4, rkf::c5, rkf::c6};
+
+template <class R>
+CFG_D __forceinline__ R tableau_a(int s, int j)
+{
+    if constexpr (sizeof(R) == sizeof(double)) return kRkfA[s][j];
+    else return kRkfAf[s][j];
+}
 
 // Mixed form: multiple of the FP32 unit round-off charged to each stage
 // derivative in the error test (model right-hand sides lose a few tens of
 // ulps through exp/log/division chains).
 constexpr double kFp32NoiseUlps = 64.0;
+
+
+// One right-hand-side evaluation.  Not inlined: the stage loop and the final
+// current evaluation share one copy of the (large) model body, which keeps
+// the kernel's instruction footprint to a single model instance.
+template <class M, bool SV, class R, class KS>
+__device__ __noinline__ R rhs_eval(double t, const R* y, const KS* K, R* dydt, int tissue,
+                                   const CfgStimulus* st)
+{
+    return M::template rates<R, SV>(t, ArrayView<R>{y}, *K, dydt, tissue, *st);
+}
+
+// Per-cell solver state: y holds every state in double (the plain form) or
+// only the slow (WIDE_MASK) states in double; yf holds every state in the
+// arithmetic type R, which is what the right-hand side reads.
+template <class M, class R>
+struct CellState {
+    double y[M::NS];
+    R yf[M::NS];
+};
 
 // ODESolver::solve(xStart, xEnd, y, dxTry) with adaptiveSolver::solve and
 // RKF45::solve inside.  The six right-hand-side evaluations of a trial step
@@ -143,20 +201,24 @@ constexpr double kFp32NoiseUlps = 64.0;
 // instantiated once.  FP64 stage sums are accumulated left to right exactly
 // as the host code writes them.  Returns accepted substeps, or -1 on
 // maxSteps overflow / step underflow.
-template <class M, bool SV, class R>
-CFG_D __forceinline__ long long rkf45_solve(double xs, double xe, double* y, double& dx_try,
-                                            R (*k)[M::NS], const double* C, int tissue,
-                                            const CfgStimulus& st, const OdeSettings& s,
-                                            unsigned& evals, IonicFailure* why = nullptr)
+template <class M, bool SV, class R, class KS>
+CFG_D __forceinline__ long long rkf45_solve(double xs, double xe, CellState<M, R>& cs,
+                                            double& dx_try, R (*k)[M::NS], const KS& K,
+                                            int tissue, const CfgStimulus& st,
+                                            const OdeSettings& s, unsigned& evals,
+                                            IonicFailure* why = nullptr)
 {
     using namespace rkf;
     constexpr int NS = M::NS;
     constexpr bool D = sizeof(R) == sizeof(double);
+    double* y = cs.y;
+    R* yf = cs.yf;
     double step_dx = dx_try;
     bool last = false;
     double x = xs;
-    double y5[NS];
     R yt[NS];
+    R y5f[NS];
+    double y5w[NS];
     for (long long n = 0; n < s.max_steps; ++n) {
         const double dx_try0 = step_dx;
         {
@@ -176,25 +238,24 @@ CFG_D __forceinline__ long long rkf45_solve(double xs, double xe, double* y, dou
 #pragma unroll 1
             for (int sg = s0; sg < 6; ++sg) {
                 if (sg == 0) {
-#pragma unroll
-                    for (int i = 0; i < NS; ++i) yt[i] = R(y[i]);
+#pragma unroll kStateUnroll
+                    for (int i = 0; i < NS; ++i) yt[i] = yf[i];
                 } else if (sg == 1) {
-#pragma unroll
+#pragma unroll kStateUnroll
                     for (int i = 0; i < NS; ++i) {
                         if constexpr (D) yt[i] = y[i] + a21 * dx * k[0][i];
-                        else yt[i] = R(y[i]) + R(a21) * h * k[0][i];
+                        else yt[i] = yf[i] + R(a21) * h * k[0][i];
                     }
                 } else {
-#pragma unroll
+#pragma unroll kStateUnroll
                     for (int i = 0; i < NS; ++i) {
-                        R acc = R(kRkfA[sg][0]) * k[0][i];
-                        for (int j = 1; j < sg; ++j) acc += R(kRkfA[sg][j]) * k[j][i];
+                        R acc = tableau_a<R>(sg, 0) * k[0][i];
+                        for (int j = 1; j < sg; ++j) acc += tableau_a<R>(sg, j) * k[j][i];
                         if constexpr (D) yt[i] = y[i] + dx * acc;
-                        else yt[i] = R(y[i]) + h * acc;
+                        else yt[i] = yf[i] + h * acc;
                     }
                 }
-                M::template rates<R, SV>(x + kRkfC[sg] * dx, ArrayView<R>{yt}, ConstView<R>{C},
-                                         k[sg], tissue, st);
+                rhs_eval<M, SV, R, KS>(x + kRkfC[sg] * dx, yt, &K, k[sg], tissue, &st);
                 evals += 1;
             }
             s0 = 1;
@@ -203,25 +264,30 @@ CFG_D __forceinline__ long long rkf45_solve(double xs, double xe, double* y, dou
             double maxerr = 0.0;
             R maxerr_r = R(0);
             worst = -1;
-#pragma unroll
+#pragma unroll kStateUnroll
             for (int i = 0; i < NS; ++i) {
                 if constexpr (D) {
-                    y5[i] = y[i] + dx * (b1 * k[0][i] + b3 * k[2][i] + b4 * k[3][i]
-                                         + b5 * k[4][i] + b6 * k[5][i]);
+                    y5w[i] = y[i] + dx * (b1 * k[0][i] + b3 * k[2][i] + b4 * k[3][i]
+                                          + b5 * k[4][i] + b6 * k[5][i]);
+                    y5f[i] = y5w[i];
                 } else {
                     R incr = h * (R(b1) * k[0][i] + R(b3) * k[2][i] + R(b4) * k[3][i]
                                   + R(b5) * k[4][i] + R(b6) * k[5][i]);
                     // slow states accumulate in FP64, gates in FP32
-                    if (is_wide<M::WIDE_MASK>(i)) y5[i] = y[i] + double(incr);
-                    else y5[i] = double(R(y[i]) + incr);
+                    if (is_wide<M::WIDE_MASK>(i)) {
+                        y5w[i] = y[i] + double(incr);
+                        y5f[i] = R(y5w[i]);
+                    } else {
+                        y5f[i] = yf[i] + incr;
+                    }
                 }
             }
-#pragma unroll
+#pragma unroll kStateUnroll
             for (int i = 0; i < NS; ++i) {
                 if constexpr (D) {
                     double e_i = dx * (e1 * k[0][i] + e3 * k[2][i] + e4 * k[3][i]
                                        + e5 * k[4][i] + e6 * k[5][i]);
-                    double a = fabs(y[i]), b = fabs(y5[i]);
+                    double a = fabs(y[i]), b = fabs(y5w[i]);
                     double tol = s.abs_tol + s.rel_tol * (a > b ? a : b);
                     double e = fabs(e_i) / tol;
                     if (e > maxerr) { maxerr = e; worst = i; }
@@ -236,7 +302,7 @@ CFG_D __forceinline__ long long rkf45_solve(double xs, double xe, double* y, dou
                               * (fabsf(R(e1) * k[0][i]) + fabsf(R(e3) * k[2][i])
                                  + fabsf(R(e4) * k[3][i]) + fabsf(R(e5) * k[4][i])
                                  + fabsf(R(e6) * k[5][i]));
-                    R a = fabsf(R(y[i])), b = fabsf(R(y5[i]));
+                    R a = fabsf(yf[i]), b = fabsf(y5f[i]);
                     R tol = R(s.abs_tol) + R(s.rel_tol) * (a > b ? a : b) + noise;
                     R e = fabsf(e_i) / tol;
                     if (e > maxerr_r) { maxerr_r = e; worst = i; }
@@ -244,7 +310,9 @@ CFG_D __forceinline__ long long rkf45_solve(double xs, double xe, double* y, dou
             }
             err = D ? maxerr : double(maxerr_r);
             if (!(err > 1)) break;
-            double scale = s.safe_scale * pow(err, -s.alpha_dec);
+            double scale;
+            if constexpr (D) scale = s.safe_scale * pow(err, -s.alpha_dec);
+            else scale = double(float(s.safe_scale) * powf(float(err), -float(s.alpha_dec)));
             if (scale < s.min_scale) scale = s.min_scale;
             dx *= scale;
             if (dx < 1e-300) {
@@ -254,10 +322,15 @@ CFG_D __forceinline__ long long rkf45_solve(double xs, double xe, double* y, dou
         }
         if (why) { why->x = x; why->dx = dx; why->err = err; why->worst = worst; why->steps = n; }
         x = exact_add(x, dx);
-#pragma unroll
-        for (int i = 0; i < NS; ++i) y[i] = y5[i];
+#pragma unroll kStateUnroll
+        for (int i = 0; i < NS; ++i) {
+            yf[i] = y5f[i];
+            if (D || is_wide<M::WIDE_MASK>(i)) y[i] = y5w[i];
+        }
         if (err > s.inc_threshold) {
-            double scale = s.safe_scale * pow(err, -s.alpha_inc);
+            double scale;
+            if constexpr (D) scale = s.safe_scale * pow(err, -s.alpha_inc);
+            else scale = double(float(s.safe_scale) * powf(float(err), -float(s.alpha_inc)));
             if (scale > s.max_scale) scale = s.max_scale;
             step_dx = scale * dx;
         } else {
@@ -278,8 +351,11 @@ CFG_D __forceinline__ long long rkf45_solve(double xs, double xe, double* y, dou
 }
 
 // Tissue / single-cell ionic update of one PDE step for all cells.
-template <class M, bool FP64, bool SV>
-__global__ void __launch_bounds__(128) ionic_step_kernel(IonicLaunch p)
+// TISSUE > 0: every cell has that tissue flag and no per-cell scales, and the
+// constants are compile-time values; TISSUE == 0: constants are evaluated per
+// cell (per-cell tissue flags or conductance scales).
+template <class M, bool FP64, bool SV, int TISSUE>
+__global__ void __launch_bounds__(128, CFG_IONIC_MIN_BLOCKS) ionic_step_kernel(IonicLaunch p)
 {
     using R = typename std::conditional<FP64, double, float>::type;
     using L = Layout<M, FP64>;
@@ -291,25 +367,20 @@ __global__ void __launch_bounds__(128) ionic_step_kernel(IonicLaunch p)
         double ts, te, dtm;
         model_times<M>(t0, p.dt, ts, te, dtm);
 
-        const int tissue = p.tissue_cell ? int(p.tissue_cell[c]) : p.tissue;
-        double C[M::NC] = {};   // the reference zero-fills CONSTANTS
-        double yinit[NS];
-        double sc[6];
-        const double* scp = nullptr;
-        if (p.scales) {
-#pragma unroll
-            for (int j = 0; j < 6; ++j) sc[j] = p.scales[j * p.scale_stride + c];
-            scp = sc;
-        }
-        M::init(C, yinit, tissue, scp);
-
-        double y[NS];
+        CellState<M, R> cs;
 #pragma unroll
         for (int i = 0; i < NS; ++i) {
-            if (FP64 || is_wide<M::WIDE_MASK>(i)) y[i] = p.yw[(long long)L::slot(i) * p.n + c];
-            else y[i] = double(p.yn[(long long)L::slot(i) * p.n + c]);
+            if (FP64 || is_wide<M::WIDE_MASK>(i)) {
+                cs.y[i] = p.yw[(long long)L::slot(i) * p.n + c];
+                cs.yf[i] = R(cs.y[i]);
+            } else {
+                cs.yf[i] = p.yn[(long long)L::slot(i) * p.n + c];
+            }
         }
-        if (!SV) y[0] = vm_to_state0<M::VM_MAP>(p.vm[c]);
+        if (!SV) {
+            cs.y[0] = vm_to_state0<M::VM_MAP>(p.vm[c]);
+            cs.yf[0] = R(cs.y[0]);
+        }
         double step = p.step[c];
         if (dtm < step) step = dtm;   // step = min(step, dt_model)
 
@@ -320,8 +391,35 @@ __global__ void __launch_bounds__(128) ionic_step_kernel(IonicLaunch p)
             for (int i = 0; i < NS; ++i) k[j][i] = R(0);
 
         IonicFailure why;
-        long long nsub = rkf45_solve<M, SV, R>(ts, te, y, step, k, C, tissue, p.stim, p.ode, evals,
-                                               &why);
+        long long nsub;
+        R iion;
+        int tissue = TISSUE;
+        if constexpr (TISSUE > 0) {
+            const ConstFold<R, M, TISSUE> K{};
+            nsub = rkf45_solve<M, SV, R>(ts, te, cs, step, k, K, TISSUE, p.stim, p.ode, evals,
+                                         &why);
+            // computeVariables at tEnd: the rates body computes the same Iion
+            iion = rhs_eval<M, SV, R, ConstFold<R, M, TISSUE>>(te, cs.yf, &K, k[0], TISSUE,
+                                                               &p.stim);
+        } else {
+            tissue = p.tissue_cell ? int(p.tissue_cell[c]) : p.tissue;
+            double C[M::NC] = {};   // the reference zero-fills CONSTANTS
+            double yinit[NS];
+            double sc[6];
+            const double* scp = nullptr;
+            if (p.scales) {
+#pragma unroll
+                for (int j = 0; j < 6; ++j) sc[j] = p.scales[j * p.scale_stride + c];
+                scp = sc;
+            }
+            M::init(C, yinit, tissue, scp);
+            const ConstView<R> K{C};
+            nsub = rkf45_solve<M, SV, R>(ts, te, cs, step, k, K, tissue, p.stim, p.ode, evals,
+                                         &why);
+            iion = rhs_eval<M, SV, R, ConstView<R>>(te, cs.yf, &K, k[0], tissue, &p.stim);
+        }
+        (void)tissue;
+        evals += 1;
         if (nsub < 0) {
             const int prev = atomicOr(p.status, CFG_ERR_ODE_STEPS);
             if (p.fail_record && !(prev & CFG_ERR_ODE_STEPS)) {
@@ -331,20 +429,14 @@ __global__ void __launch_bounds__(128) ionic_step_kernel(IonicLaunch p)
                 r[4] = why.worst; r[5] = why.err; r[6] = why.value; r[7] = double(why.steps);
             }
         }
-
-        R yr[NS];
-#pragma unroll
-        for (int i = 0; i < NS; ++i) yr[i] = R(y[i]);
-        R iion = M::template current<R, SV>(te, ArrayView<R>{yr}, ConstView<R>{C}, tissue, p.stim);
-        evals += 1;
-        double im = double(iion) * M::IION_SCALE;
+        const double im = double(iion) * M::IION_SCALE;
         if (!isfinite(im)) atomicOr(p.status, CFG_ERR_NONFINITE);
         if (p.im) p.im[c] = im;
 
 #pragma unroll
         for (int i = 0; i < NS; ++i) {
-            if (FP64 || is_wide<M::WIDE_MASK>(i)) p.yw[(long long)L::slot(i) * p.n + c] = y[i];
-            else p.yn[(long long)L::slot(i) * p.n + c] = float(y[i]);
+            if (FP64 || is_wide<M::WIDE_MASK>(i)) p.yw[(long long)L::slot(i) * p.n + c] = cs.y[i];
+            else p.yn[(long long)L::slot(i) * p.n + c] = cs.yf[i];
         }
         p.step[c] = step;
     }

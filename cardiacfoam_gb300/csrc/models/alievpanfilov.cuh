@@ -18,6 +18,7 @@ constexpr double TIME_SCALE = 12.9;
 constexpr int VM_MAP = CFG_VM_ALIEV;
 constexpr int N_TISSUES = 1;
 static const int TISSUES[] = {4, 0};
+using TissueSet = TissueList<4>;
 static const char* const STATE_NAMES[NS] = {"u", "recovery_r"};
 CFG_HD inline bool tissue_supported(int t) { return t == 4; }
 
@@ -47,6 +48,26 @@ CFG_HD __forceinline__ void init_consts(double* C, double* y, int tissue, const 
     y[S_recovery_r] = 0.0;
 }
 
+// initConsts evaluated per tissue flag (IEEE double, the header's order of
+// operations): cval<T>(i) is constant i for tissue T.  Kernels for one uniform
+// tissue without per-cell scales read constants from here, so the compiler
+// folds them into the instructions.
+template <int T> CFG_HD constexpr double cval(int i);
+template <> CFG_HD constexpr double cval<4>(int i)
+{
+    switch (i) {
+    case 0: return 20.0;
+    case 1: return -80.0;
+    case 2: return -70.0;
+    case 3: return 0.01;
+    case 4: return 8.0;
+    case 5: return 0.2;
+    case 6: return 0.3;
+    case 7: return 0.1;
+    default: return 0.0;
+    }
+}
+
 // Right-hand side as used by derivatives(): dydt for every state that the
 // reference assigns (RATES of V only when SOLVE_VM).  Returns Iion.
 // Y(i) reads state i as R, K(i) reads constant i as R.
@@ -57,7 +78,7 @@ __device__ __forceinline__ R rhs(double t, const YS& Y, const KS& K, R* dydt, in
     R a_AV_eps = (K(C_AC_epsilon) + ((K(C_AC_mu1) * Y(S_recovery_r)) / (K(C_AC_mu2) + Y(S_u))));
     dydt[S_recovery_r] = (a_AV_eps * ((-Y(S_recovery_r)) - ((K(C_AC_k) * Y(S_u)) * (Y(S_u) - (K(C_AC_a) + R(1.0))))));
     R a_Iion_cm = ((((K(C_AC_k) * Y(S_u)) * (Y(S_u) - K(C_AC_a))) * (Y(S_u) - R(1.0))) + (Y(S_recovery_r) * Y(S_u)));
-    R a_Istim = R(cfg_stimulus_current<double>(t, stim));
+    R a_Istim = (SOLVE_VM ? R(cfg_stimulus_current<double>(t, stim)) : R(0));
     if (SOLVE_VM) {
         dydt[S_u] = ((-a_Iion_cm) - a_Istim);
     }
@@ -73,7 +94,7 @@ __device__ __forceinline__ R iion(double t, const YS& Y, const KS& K, int tissue
     R a_AV_eps = (K(C_AC_epsilon) + ((K(C_AC_mu1) * Y(S_recovery_r)) / (K(C_AC_mu2) + Y(S_u))));
     dydt[S_recovery_r] = (a_AV_eps * ((-Y(S_recovery_r)) - ((K(C_AC_k) * Y(S_u)) * (Y(S_u) - (K(C_AC_a) + R(1.0))))));
     R a_Iion_cm = ((((K(C_AC_k) * Y(S_u)) * (Y(S_u) - K(C_AC_a))) * (Y(S_u) - R(1.0))) + (Y(S_recovery_r) * Y(S_u)));
-    R a_Istim = R(cfg_stimulus_current<double>(t, stim));
+    R a_Istim = (SOLVE_VM ? R(cfg_stimulus_current<double>(t, stim)) : R(0));
     if (SOLVE_VM) {
         dydt[S_u] = ((-a_Iion_cm) - a_Istim);
     }
@@ -89,6 +110,7 @@ struct Model {
     static constexpr double TIME_SCALE = alievpanfilov::TIME_SCALE;
     static constexpr int VM_MAP = alievpanfilov::VM_MAP;
     CFG_HD static __forceinline__ void init(double* C, double* y, int tissue, const double* scale) { init_consts(C, y, tissue, scale); }
+    template <int T> CFG_HD static constexpr double constant(int i) { return cval<T>(i); }
     template <class R, bool SV, class YS, class KS>
     __device__ static __forceinline__ R rates(double t, const YS& Y, const KS& K, R* dydt, int tissue, const CfgStimulus& st) { return rhs<R, SV>(t, Y, K, dydt, tissue, st); }
     template <class R, bool SV, class YS, class KS>

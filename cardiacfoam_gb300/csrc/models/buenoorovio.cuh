@@ -18,6 +18,7 @@ constexpr double TIME_SCALE = 1.0;
 constexpr int VM_MAP = CFG_VM_BUENO;
 constexpr int N_TISSUES = 3;
 static const int TISSUES[] = {3, 2, 1, 0};
+using TissueSet = TissueList<3, 2, 1>;
 static const char* const STATE_NAMES[NS] = {"u", "v", "w", "s"};
 CFG_HD inline bool tissue_supported(int t) { return t == 3 || t == 2 || t == 1; }
 
@@ -69,6 +70,114 @@ CFG_HD __forceinline__ void init_consts(double* C, double* y, int tissue, const 
     y[S_s] = 0.0;
 }
 
+// initConsts evaluated per tissue flag (IEEE double, the header's order of
+// operations): cval<T>(i) is constant i for tissue T.  Kernels for one uniform
+// tissue without per-cell scales read constants from here, so the compiler
+// folds them into the instructions.
+template <int T> CFG_HD constexpr double cval(int i);
+template <> CFG_HD constexpr double cval<3>(int i)
+{
+    switch (i) {
+    case 0: return 0.0;
+    case 1: return 1.56;
+    case 2: return 0.3;
+    case 3: return 0.13;
+    case 4: return 0.2;
+    case 5: return 0.006;
+    case 6: return 75.0;
+    case 7: return 10.0;
+    case 8: return 1.4506;
+    case 9: return 6.0;
+    case 10: return 140.0;
+    case 11: return 200.0;
+    case 12: return 0.016;
+    case 13: return 280.0;
+    case 14: return 0.1;
+    case 15: return 470.0;
+    case 16: return 6.0;
+    case 17: return 40.0;
+    case 18: return 1.2;
+    case 19: return 2.0;
+    case 20: return 0.65;
+    case 21: return 2.7342;
+    case 22: return 2.0;
+    case 23: return 2.0994;
+    case 24: return 0.9087;
+    case 25: return 2.9013;
+    case 26: return 0.0273;
+    case 27: return 0.78;
+    default: return 0.0;
+    }
+}
+template <> CFG_HD constexpr double cval<2>(int i)
+{
+    switch (i) {
+    case 0: return 0.0;
+    case 1: return 1.61;
+    case 2: return 0.3;
+    case 3: return 0.13;
+    case 4: return 0.1;
+    case 5: return 0.005;
+    case 6: return 80.0;
+    case 7: return 1.4506;
+    case 8: return 1.4506;
+    case 9: return 70.0;
+    case 10: return 8.0;
+    case 11: return 200.0;
+    case 12: return 0.016;
+    case 13: return 280.0;
+    case 14: return 0.078;
+    case 15: return 410.0;
+    case 16: return 7.0;
+    case 17: return 91.0;
+    case 18: return 0.8;
+    case 19: return 2.1;
+    case 20: return 0.6;
+    case 21: return 2.7342;
+    case 22: return 4.0;
+    case 23: return 2.0994;
+    case 24: return 0.9087;
+    case 25: return 3.3849;
+    case 26: return 0.01;
+    case 27: return 0.5;
+    default: return 0.0;
+    }
+}
+template <> CFG_HD constexpr double cval<1>(int i)
+{
+    switch (i) {
+    case 0: return 0.0;
+    case 1: return 1.55;
+    case 2: return 0.3;
+    case 3: return 0.13;
+    case 4: return 0.006;
+    case 5: return 0.006;
+    case 6: return 60.0;
+    case 7: return 1150.0;
+    case 8: return 1.4506;
+    case 9: return 60.0;
+    case 10: return 15.0;
+    case 11: return 65.0;
+    case 12: return 0.03;
+    case 13: return 200.0;
+    case 14: return 0.11;
+    case 15: return 400.0;
+    case 16: return 6.0;
+    case 17: return 30.0181;
+    case 18: return 0.9957;
+    case 19: return 2.0458;
+    case 20: return 0.65;
+    case 21: return 2.7342;
+    case 22: return 16.0;
+    case 23: return 2.0994;
+    case 24: return 0.9087;
+    case 25: return 1.8875;
+    case 26: return 0.07;
+    case 27: return 0.94;
+    default: return 0.0;
+    }
+}
+
 // Right-hand side as used by derivatives(): dydt for every state that the
 // reference assigns (RATES of V only when SOLVE_VM).  Returns Iion.
 // Y(i) reads state i as R, K(i) reads constant i as R.
@@ -90,7 +199,7 @@ __device__ __forceinline__ R rhs(double t, const YS& Y, const KS& K, R* dydt, in
     dydt[S_v] = ((((R(1.0) - (((Y(S_u) - K(C_thetaV))) > R(0) ? 1 : 0)) * (a_vInfty - Y(S_v))) / a_tauVMinus) - (((((Y(S_u) - K(C_thetaV))) > R(0) ? 1 : 0) * Y(S_v)) / K(C_tauVPlus)));
     dydt[S_w] = ((((R(1.0) - (((Y(S_u) - K(C_thetaW))) > R(0) ? 1 : 0)) * (a_wInfty - Y(S_w))) / a_tauWMinus) - (((((Y(S_u) - K(C_thetaW))) > R(0) ? 1 : 0) * Y(S_w)) / K(C_tauWPlus)));
     dydt[S_s] = ((((R(1.0) + cfg_tanh((K(C_kS) * (Y(S_u) - K(C_uS))))) / R(2.0)) - Y(S_s)) / a_tauS);
-    R a_Istim = R(cfg_stimulus_current<double>(t, stim));
+    R a_Istim = (SOLVE_VM ? R(cfg_stimulus_current<double>(t, stim)) : R(0));
     if (SOLVE_VM) {
         dydt[S_u] = ((-a_Jion) - a_Istim);
     }
@@ -117,7 +226,7 @@ __device__ __forceinline__ R iion(double t, const YS& Y, const KS& K, int tissue
     dydt[S_v] = ((((R(1.0) - (((Y(S_u) - K(C_thetaV))) > R(0) ? 1 : 0)) * (a_vInfty - Y(S_v))) / a_tauVMinus) - (((((Y(S_u) - K(C_thetaV))) > R(0) ? 1 : 0) * Y(S_v)) / K(C_tauVPlus)));
     dydt[S_w] = ((((R(1.0) - (((Y(S_u) - K(C_thetaW))) > R(0) ? 1 : 0)) * (a_wInfty - Y(S_w))) / a_tauWMinus) - (((((Y(S_u) - K(C_thetaW))) > R(0) ? 1 : 0) * Y(S_w)) / K(C_tauWPlus)));
     dydt[S_s] = ((((R(1.0) + cfg_tanh((K(C_kS) * (Y(S_u) - K(C_uS))))) / R(2.0)) - Y(S_s)) / a_tauS);
-    R a_Istim = R(cfg_stimulus_current<double>(t, stim));
+    R a_Istim = (SOLVE_VM ? R(cfg_stimulus_current<double>(t, stim)) : R(0));
     if (SOLVE_VM) {
         dydt[S_u] = ((-a_Jion) - a_Istim);
     }
@@ -133,6 +242,7 @@ struct Model {
     static constexpr double TIME_SCALE = buenoorovio::TIME_SCALE;
     static constexpr int VM_MAP = buenoorovio::VM_MAP;
     CFG_HD static __forceinline__ void init(double* C, double* y, int tissue, const double* scale) { init_consts(C, y, tissue, scale); }
+    template <int T> CFG_HD static constexpr double constant(int i) { return cval<T>(i); }
     template <class R, bool SV, class YS, class KS>
     __device__ static __forceinline__ R rates(double t, const YS& Y, const KS& K, R* dydt, int tissue, const CfgStimulus& st) { return rhs<R, SV>(t, Y, K, dydt, tissue, st); }
     template <class R, bool SV, class YS, class KS>

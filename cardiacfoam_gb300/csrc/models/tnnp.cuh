@@ -18,6 +18,7 @@ constexpr double TIME_SCALE = 1.0;
 constexpr int VM_MAP = CFG_VM_MV;
 constexpr int N_TISSUES = 3;
 static const int TISSUES[] = {3, 2, 1, 0};
+using TissueSet = TissueList<3, 2, 1>;
 static const char* const STATE_NAMES[NS] = {"V", "K_i", "Na_i", "Ca_i", "Xr1", "Xr2", "Xs", "m", "h", "j", "d", "f", "fCa", "s", "r", "Ca_SR", "g"};
 CFG_HD inline bool tissue_supported(int t) { return t == 3 || t == 2 || t == 1; }
 
@@ -102,6 +103,156 @@ CFG_HD __forceinline__ void init_consts(double* C, double* y, int tissue, const 
     C[C_tau_fCa] = 2.00000;
 }
 
+// initConsts evaluated per tissue flag (IEEE double, the header's order of
+// operations): cval<T>(i) is constant i for tissue T.  Kernels for one uniform
+// tissue without per-cell scales read constants from here, so the compiler
+// folds them into the instructions.
+template <int T> CFG_HD constexpr double cval(int i);
+template <> CFG_HD constexpr double cval<3>(int i)
+{
+    switch (i) {
+    case 0: return 8.314;
+    case 1: return 310.0;
+    case 2: return 96.485;
+    case 3: return 185.0;
+    case 4: return 16404.0;
+    case 5: return 0.03;
+    case 6: return 5.4;
+    case 7: return 140.0;
+    case 8: return 2.0;
+    case 9: return 5.405;
+    case 10: return 0.096;
+    case 11: return 0.245;
+    case 12: return 14.838;
+    case 13: return 0.00029;
+    case 14: return 0.175;
+    case 15: return 0.000592;
+    case 16: return 0.073;
+    case 17: return 1.362;
+    case 18: return 1.0;
+    case 19: return 40.0;
+    case 20: return 1000.0;
+    case 21: return 0.1;
+    case 22: return 2.5;
+    case 23: return 0.35;
+    case 24: return 1.38;
+    case 25: return 87.5;
+    case 26: return 0.825;
+    case 27: return 0.0005;
+    case 28: return 0.0146;
+    case 29: return 2.0;
+    case 30: return 0.016464;
+    case 31: return 0.25;
+    case 32: return 0.008232;
+    case 33: return 0.00025;
+    case 34: return 8e-05;
+    case 35: return 0.000425;
+    case 36: return 0.15;
+    case 37: return 0.001;
+    case 38: return 10.0;
+    case 39: return 0.3;
+    case 40: return 1094.0;
+    case 41: return 2.0;
+    default: return 0.0;
+    }
+}
+template <> CFG_HD constexpr double cval<2>(int i)
+{
+    switch (i) {
+    case 0: return 8.314;
+    case 1: return 310.0;
+    case 2: return 96.485;
+    case 3: return 185.0;
+    case 4: return 16404.0;
+    case 5: return 0.03;
+    case 6: return 5.4;
+    case 7: return 140.0;
+    case 8: return 2.0;
+    case 9: return 5.405;
+    case 10: return 0.096;
+    case 11: return 0.062;
+    case 12: return 14.838;
+    case 13: return 0.00029;
+    case 14: return 0.175;
+    case 15: return 0.000592;
+    case 16: return 0.294;
+    case 17: return 1.362;
+    case 18: return 1.0;
+    case 19: return 40.0;
+    case 20: return 1000.0;
+    case 21: return 0.1;
+    case 22: return 2.5;
+    case 23: return 0.35;
+    case 24: return 1.38;
+    case 25: return 87.5;
+    case 26: return 0.825;
+    case 27: return 0.0005;
+    case 28: return 0.0146;
+    case 29: return 2.0;
+    case 30: return 0.016464;
+    case 31: return 0.25;
+    case 32: return 0.008232;
+    case 33: return 0.00025;
+    case 34: return 8e-05;
+    case 35: return 0.000425;
+    case 36: return 0.15;
+    case 37: return 0.001;
+    case 38: return 10.0;
+    case 39: return 0.3;
+    case 40: return 1094.0;
+    case 41: return 2.0;
+    default: return 0.0;
+    }
+}
+template <> CFG_HD constexpr double cval<1>(int i)
+{
+    switch (i) {
+    case 0: return 8.314;
+    case 1: return 310.0;
+    case 2: return 96.485;
+    case 3: return 185.0;
+    case 4: return 16404.0;
+    case 5: return 0.03;
+    case 6: return 5.4;
+    case 7: return 140.0;
+    case 8: return 2.0;
+    case 9: return 5.405;
+    case 10: return 0.096;
+    case 11: return 0.245;
+    case 12: return 14.838;
+    case 13: return 0.00029;
+    case 14: return 0.175;
+    case 15: return 0.000592;
+    case 16: return 0.294;
+    case 17: return 1.362;
+    case 18: return 1.0;
+    case 19: return 40.0;
+    case 20: return 1000.0;
+    case 21: return 0.1;
+    case 22: return 2.5;
+    case 23: return 0.35;
+    case 24: return 1.38;
+    case 25: return 87.5;
+    case 26: return 0.825;
+    case 27: return 0.0005;
+    case 28: return 0.0146;
+    case 29: return 2.0;
+    case 30: return 0.016464;
+    case 31: return 0.25;
+    case 32: return 0.008232;
+    case 33: return 0.00025;
+    case 34: return 8e-05;
+    case 35: return 0.000425;
+    case 36: return 0.15;
+    case 37: return 0.001;
+    case 38: return 10.0;
+    case 39: return 0.3;
+    case 40: return 1094.0;
+    case 41: return 2.0;
+    default: return 0.0;
+    }
+}
+
 // Right-hand side as used by derivatives(): dydt for every state that the
 // reference assigns (RATES of V only when SOLVE_VM).  Returns Iion.
 // Y(i) reads state i as R, K(i) reads constant i as R.
@@ -184,7 +335,7 @@ __device__ __forceinline__ R rhs(double t, const YS& Y, const KS& K, R* dydt, in
     R a_i_p_K = ((K(C_g_pK) * (Y(S_V) - a_E_K)) / (R(1.00000) + cfg_exp(((R(25.0000) - Y(S_V)) / R(5.98000)))));
     R a_i_p_Ca = ((K(C_g_pCa) * Y(S_Ca_i)) / (Y(S_Ca_i) + K(C_K_pCa)));
     R a_Iion_cm = (((((((((((a_i_K1 + a_i_to) + a_i_Kr) + a_i_Ks) + a_i_CaL) + a_i_NaK) + a_i_Na) + a_i_b_Na) + a_i_NaCa) + a_i_b_Ca) + a_i_p_K) + a_i_p_Ca);
-    R a_Istim = R(cfg_stimulus_current<double>(t, stim));
+    R a_Istim = (SOLVE_VM ? R(cfg_stimulus_current<double>(t, stim)) : R(0));
     dydt[S_V] = R(0.0);
     if (SOLVE_VM) {
         dydt[S_V] = ((-a_Iion_cm) - a_Istim);
@@ -277,7 +428,7 @@ __device__ __forceinline__ R iion(double t, const YS& Y, const KS& K, int tissue
     R a_ddt_Ca_sr_total = ((K(C_V_c) / K(C_V_sr)) * (a_i_up - (a_i_rel + a_i_leak)));
     R a_f_JCa_sr_free = (R(1.00000) / (R(1.00000) + ((K(C_Buf_sr) * K(C_K_buf_sr)) / cfg_ipow<2>((Y(S_Ca_SR) + K(C_K_buf_sr))))));
     R a_Iion_cm = (((((((((((a_i_K1 + a_i_to) + a_i_Kr) + a_i_Ks) + a_i_CaL) + a_i_NaK) + a_i_Na) + a_i_b_Na) + a_i_NaCa) + a_i_b_Ca) + a_i_p_K) + a_i_p_Ca);
-    R a_Istim = R(cfg_stimulus_current<double>(t, stim));
+    R a_Istim = (SOLVE_VM ? R(cfg_stimulus_current<double>(t, stim)) : R(0));
     a_m_inf = (R(1.00000) / cfg_ipow<2>((R(1.00000) + cfg_exp((((-R(56.8600)) - Y(S_V)) / R(9.03000))))));
     a_alpha_m = (R(1.00000) / (R(1.00000) + cfg_exp((((-R(60.0000)) - Y(S_V)) / R(5.00000)))));
     a_beta_m = ((R(0.100000) / (R(1.00000) + cfg_exp(((Y(S_V) + R(35.0000)) / R(5.00000))))) + (R(0.100000) / (R(1.00000) + cfg_exp(((Y(S_V) - R(50.0000)) / R(200.000))))));
@@ -353,7 +504,7 @@ __device__ __forceinline__ R iion(double t, const YS& Y, const KS& K, int tissue
     a_i_p_K = ((K(C_g_pK) * (Y(S_V) - a_E_K)) / (R(1.00000) + cfg_exp(((R(25.0000) - Y(S_V)) / R(5.98000)))));
     a_i_p_Ca = ((K(C_g_pCa) * Y(S_Ca_i)) / (Y(S_Ca_i) + K(C_K_pCa)));
     a_Iion_cm = (((((((((((a_i_K1 + a_i_to) + a_i_Kr) + a_i_Ks) + a_i_CaL) + a_i_NaK) + a_i_Na) + a_i_b_Na) + a_i_NaCa) + a_i_b_Ca) + a_i_p_K) + a_i_p_Ca);
-    a_Istim = R(cfg_stimulus_current<double>(t, stim));
+    a_Istim = (SOLVE_VM ? R(cfg_stimulus_current<double>(t, stim)) : R(0));
     dydt[S_V] = R(0.0);
     if (SOLVE_VM) {
         dydt[S_V] = ((-a_Iion_cm) - a_Istim);
@@ -380,6 +531,7 @@ struct Model {
     static constexpr double TIME_SCALE = tnnp::TIME_SCALE;
     static constexpr int VM_MAP = tnnp::VM_MAP;
     CFG_HD static __forceinline__ void init(double* C, double* y, int tissue, const double* scale) { init_consts(C, y, tissue, scale); }
+    template <int T> CFG_HD static constexpr double constant(int i) { return cval<T>(i); }
     template <class R, bool SV, class YS, class KS>
     __device__ static __forceinline__ R rates(double t, const YS& Y, const KS& K, R* dydt, int tissue, const CfgStimulus& st) { return rhs<R, SV>(t, Y, K, dydt, tissue, st); }
     template <class R, bool SV, class YS, class KS>

@@ -13,6 +13,7 @@
 
 namespace cfg {
 
+__global__ void k_prepare(DiffusionArgs a);
 __global__ void k_step_begin(DiffusionArgs a);
 __global__ void k_solve_begin(DiffusionArgs a);
 __global__ void k_solve_norm(DiffusionArgs a);
@@ -32,8 +33,8 @@ static void md_free(cfg_monodomain* md)
     dfree(md->d_col); dfree(md->d_coef); dfree(md->d_cnt); dfree(md->d_lapdiag);
     dfree(md->d_vol); dfree(md->d_vm); dfree(md->d_vm_old); dfree(md->d_vm_oldold);
     dfree(md->d_iion); dfree(md->d_act); dfree(md->d_act_flag); dfree(md->d_box);
-    dfree(md->d_diag); dfree(md->d_rD); dfree(md->d_b); dfree(md->d_r); dfree(md->d_z);
-    dfree(md->d_ax); dfree(md->d_sumA); dfree(md->d_pA); dfree(md->d_pB); dfree(md->d_ap);
+    dfree(md->d_diag2); dfree(md->d_rdiag2); dfree(md->d_sumA2); dfree(md->d_b); dfree(md->d_r);
+    dfree(md->d_z); dfree(md->d_ax); dfree(md->d_pA); dfree(md->d_pB); dfree(md->d_ap);
     dfree(md->d_partial); dfree(md->d_st);
     if (md->h_st) cudaFreeHost(md->h_st);
     if (md->stream) cudaStreamDestroy(md->stream);
@@ -160,15 +161,33 @@ static void fill_args(cfg_monodomain* md, double dt)
         a.box_end[b] = md->box_start[b] + md->box_duration[b];   // tStart + duration
         a.box_intensity[b] = md->box_intensity[b];
     }
-    a.diag = md->d_diag; a.rD = md->d_rD; a.b = md->d_b; a.r = md->d_r; a.z = md->d_z;
-    a.ax = md->d_ax; a.sumA = md->d_sumA; a.pA = md->d_pA; a.pB = md->d_pB; a.ap = md->d_ap;
+    a.diag2 = md->d_diag2; a.rdiag2 = md->d_rdiag2; a.sumA2 = md->d_sumA2;
+    a.b = md->d_b; a.r = md->d_r; a.z = md->d_z; a.ax = md->d_ax; a.pA = md->d_pA;
+    a.pB = md->d_pB; a.ap = md->d_ap;
     a.partial = md->d_partial;
     a.nblocks = int((md->n + kDiffBlock - 1) / kDiffBlock);
     a.st = md->d_st;
     a.dt = dt;
     a.chicm = md->chicm;
     a.ddt_backward = md->ddt_backward;
+    a.use_graph = 0;
+    a.iter_cap = md->iter_cap;
+    // ddt coefficients (EulerDdtScheme; backwardDdtScheme with deltaT0 =
+    // GREAT while fewer than two old-time levels exist, then deltaT0 = dt)
+    a.rdt = 1.0 / dt;
+    for (int v = 0; v < 2; ++v) {
+        if (!md->ddt_backward) {
+            a.cft[v] = 1.0; a.cft0[v] = 1.0; a.cft00[v] = 0.0;
+            continue;
+        }
+        const double dt0 = v == 0 ? 1e15 : dt;
+        a.cft[v] = 1 + dt / (dt + dt0);
+        a.cft00[v] = dt * dt / (dt0 * (dt + dt0));
+        a.cft0[v] = a.cft[v] + a.cft00[v];
+    }
 }
+
+void fill_args_public(cfg_monodomain* md, double dt) { fill_args(md, dt); }
 
 int monodomain_create(const cfg_monodomain_desc* d, const cfg_mesh_desc* m, cfg_monodomain** out)
 {
@@ -218,10 +237,13 @@ int monodomain_create(const cfg_monodomain_desc* d, const cfg_mesh_desc* m, cfg_
     const size_t n = size_t(md->n);
     cudaError_t e = cudaSuccess;
     double** vecs[] = {&md->d_vol, &md->d_vm, &md->d_vm_old, &md->d_vm_oldold, &md->d_iion,
-                       &md->d_act, &md->d_diag, &md->d_rD, &md->d_b, &md->d_r, &md->d_z,
-                       &md->d_ax, &md->d_sumA, &md->d_pA, &md->d_pB, &md->d_ap};
+                       &md->d_act, &md->d_b, &md->d_r, &md->d_z, &md->d_ax, &md->d_pA,
+                       &md->d_pB, &md->d_ap};
     for (double** v : vecs)
         if (!e) e = dmalloc(v, n);
+    if (!e) e = dmalloc(&md->d_diag2, 2 * n);
+    if (!e) e = dmalloc(&md->d_rdiag2, 2 * n);
+    if (!e) e = dmalloc(&md->d_sumA2, 2 * n);
     const int nblocks = int((n + kDiffBlock - 1) / kDiffBlock);
     if (!e) e = dmalloc(&md->d_partial, size_t(4) * nblocks);
     if (!e) e = dmalloc(&md->d_act_flag, n);
@@ -288,6 +310,12 @@ int enqueue_step(cfg_monodomain* md, double dt, bool host_control)
     const DiffusionArgs& a = md->args;
     const unsigned grid = unsigned(a.nblocks);
     cudaStream_t s = md->stream;
+    if (dt != md->prepared_dt) {
+        k_prepare<<<grid, kDiffBlock, 0, s>>>(a);
+        CFG_CUDA_TRY(cudaGetLastError());
+        md->prepared_dt = dt;
+        launches += 1;
+    }
     k_step_begin<<<grid, kDiffBlock, 0, s>>>(a);
     CFG_CUDA_TRY(cudaGetLastError());
     if (md->timing) CFG_CUDA_TRY(cudaEventRecord(md->ev[0], s));
@@ -371,24 +399,72 @@ int cfg_monodomain_create(const cfg_monodomain_desc* desc, const cfg_mesh_desc* 
     return monodomain_create(desc, mesh, out);
 }
 
+// Enqueue one step from the step graph (built on first use and whenever dt
+// or the timing switch changes).
+static int enqueue_graph_step(cfg_monodomain* md, double dt)
+{
+    if (dt != md->prepared_dt) {
+        fill_args(md, dt);
+        const unsigned grid = unsigned(md->args.nblocks);
+        k_prepare<<<grid, kDiffBlock, 0, md->stream>>>(md->args);
+        CFG_CUDA_TRY(cudaGetLastError());
+        md->prepared_dt = dt;
+    }
+    if (!md->graph_exec || md->graph_dt != dt || md->graph_timing != md->timing) {
+        int rc = build_step_graph(md, dt);
+        if (rc) return rc;
+    }
+    CFG_CUDA_TRY(cudaGraphLaunch(md->graph_exec, md->stream));
+    return CFG_OK;
+}
+
+// kernels a graph step launched, from the step's solver statistics
+static long long graph_step_launches(const cfg_monodomain* md)
+{
+    if (!md->implicit) return 4;
+    long long n = 3;   // step_begin, ionic, activation
+    for (int k = 0; k < md->h_st->n_solves && k < kMaxSolves; ++k)
+        n += 3 + 2LL * md->h_st->iters[k];
+    return n;
+}
+
 int cfg_monodomain_step(cfg_monodomain* md, double dt)
 {
     if (!md) return fail(CFG_ERR_INVALID, "null context");
     if (!(dt > 0)) return fail(CFG_ERR_INVALID, "deltaT must be positive");
-    int rc = enqueue_step(md, dt, true);
+    int rc = md->use_graph ? enqueue_graph_step(md, dt) : enqueue_step(md, dt, true);
     if (rc) return rc;
     md->t_host = md->t_host + dt;
     md->steps++;
-    return check_step(md);
+    rc = check_step(md);
+    if (!rc && md->use_graph && md->timing) md->timed_launches += graph_step_launches(md);
+    return rc;
 }
 
 int cfg_monodomain_run(cfg_monodomain* md, double dt, long long n_steps)
 {
     if (!md) return fail(CFG_ERR_INVALID, "null context");
-    for (long long i = 0; i < n_steps; ++i) {
-        int rc = cfg_monodomain_step(md, dt);
-        if (rc) return rc;
+    if (!(dt > 0)) return fail(CFG_ERR_INVALID, "deltaT must be positive");
+    if (!md->use_graph || md->timing) {
+        for (long long i = 0; i < n_steps; ++i) {
+            int rc = cfg_monodomain_step(md, dt);
+            if (rc) return rc;
+        }
+        return CFG_OK;
     }
+    for (long long i = 0; i < n_steps; ++i) {
+        int rc = enqueue_graph_step(md, dt);
+        if (rc) return rc;
+        md->t_host = md->t_host + dt;
+        md->steps++;
+    }
+    return n_steps > 0 ? check_step(md) : CFG_OK;
+}
+
+int cfg_monodomain_set_graph(cfg_monodomain* md, int enable)
+{
+    if (!md) return fail(CFG_ERR_INVALID, "null context");
+    md->use_graph = enable != 0;
     return CFG_OK;
 }
 

@@ -32,9 +32,11 @@ struct cfg_monodomain {
     double* d_act = nullptr;
     unsigned char* d_act_flag = nullptr;
     unsigned char* d_box = nullptr;
-    // PCG work
-    double *d_diag = nullptr, *d_rD = nullptr, *d_b = nullptr, *d_r = nullptr, *d_z = nullptr,
-           *d_ax = nullptr, *d_sumA = nullptr, *d_pA = nullptr, *d_pB = nullptr, *d_ap = nullptr;
+    // operator per ddt coefficient set, and PCG work
+    double *d_diag2 = nullptr, *d_rdiag2 = nullptr, *d_sumA2 = nullptr;
+    double prepared_dt = 0.0;
+    double *d_b = nullptr, *d_r = nullptr, *d_z = nullptr, *d_ax = nullptr, *d_pA = nullptr,
+           *d_pB = nullptr, *d_ap = nullptr;
     double* d_partial = nullptr;
     cfg::PcgState* d_st = nullptr;
     cfg::PcgState* h_st = nullptr;   // pinned mirror
@@ -43,7 +45,13 @@ struct cfg_monodomain {
     cudaStream_t stream = nullptr;
     int iter_chunk = 2;
     int graph_max_corr = 4, graph_max_iter = 4;
+    // step graph (device-driven PIMPLE/PCG loops), rebuilt when dt or the
+    // timing switch change
     cudaGraphExec_t graph_exec = nullptr;
+    double graph_dt = 0.0;
+    bool graph_timing = false;
+    bool use_graph = true;
+    long long iter_cap = 100000;   // PCG iterations per step before the step aborts
     double t_host = 0.0;
     long long steps = 0;
     // phase timing
@@ -58,4 +66,6 @@ namespace cfg {
 int monodomain_create(const cfg_monodomain_desc* d, const cfg_mesh_desc* m, cfg_monodomain** out);
 int enqueue_step(cfg_monodomain* md, double dt, bool host_control);
 int check_step(cfg_monodomain* md);
+int build_step_graph(cfg_monodomain* md, double dt);
+void fill_args_public(cfg_monodomain* md, double dt);
 }  // namespace cfg

@@ -86,7 +86,7 @@ EXPORTS = [
     "cfg_ionic_num_states", "cfg_ionic_state_name", "cfg_ionic_get_states",
     "cfg_ionic_set_states", "cfg_ionic_get_steps", "cfg_ionic_rhs_evaluations",
     "cfg_ionic_destroy", "cfg_monodomain_create", "cfg_monodomain_create_from_dict",
-    "cfg_monodomain_step", "cfg_monodomain_run", "cfg_monodomain_get_field",
+    "cfg_monodomain_step", "cfg_monodomain_run", "cfg_monodomain_set_graph", "cfg_monodomain_get_field",
     "cfg_monodomain_set_field", "cfg_monodomain_time", "cfg_monodomain_ionic",
     "cfg_monodomain_last_stats", "cfg_monodomain_set_timing", "cfg_monodomain_timings",
     "cfg_monodomain_stream", "cfg_monodomain_destroy",
@@ -123,6 +123,7 @@ def load(path: Optional[os.PathLike] = None):
                                                   C.c_int, C.POINTER(C.c_void_p)]
     L.cfg_monodomain_step.argtypes = [C.c_void_p, C.c_double]
     L.cfg_monodomain_run.argtypes = [C.c_void_p, C.c_double, C.c_longlong]
+    L.cfg_monodomain_set_graph.argtypes = [C.c_void_p, C.c_int]
     L.cfg_monodomain_get_field.argtypes = [C.c_void_p, C.c_int, _dp]
     L.cfg_monodomain_set_field.argtypes = [C.c_void_p, C.c_int, _dp]
     L.cfg_monodomain_time.argtypes = [C.c_void_p]

@@ -170,9 +170,15 @@ int cfg_monodomain_create_from_dict(const char* electro_properties, const cfg_me
  * time. */
 int cfg_monodomain_step(cfg_monodomain* md, double dt);
 
-/* n_steps steps replayed from a captured CUDA graph (no host work per step
- * beyond the launch). */
+/* n_steps steps replayed from the step's CUDA graph, whose PIMPLE and PCG
+ * loops are conditional nodes driven by device-side solver state: no host
+ * work per step beyond the launch, one status check at the end. */
 int cfg_monodomain_run(cfg_monodomain* md, double dt, long long n_steps);
+
+/* Use the step graph (1, default) or drive the PIMPLE/PCG loops from the
+ * host, reading the solver state after every solve start and iteration pair
+ * (0; for debugging; same results). */
+int cfg_monodomain_set_graph(cfg_monodomain* md, int enable);
 
 #define CFG_FIELD_VM 0              /* Vm [V] */
 #define CFG_FIELD_IION 1            /* ionicCurrent [V/s] */

@@ -123,3 +123,30 @@ monodomainSolverCoeffs
         b.step(dt)
     assert np.array_equal(a.vm(), b.vm())
     assert np.array_equal(a.source(), b.source())
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("implicit", [True, False])
+def test_step_graph_equals_host_control(gpu_lib, implicit):
+    """The step graph (device-driven PIMPLE/PCG loops) gives the same fields
+    and solver statistics as host-driven control, and run(n) equals n steps."""
+    dt, nsteps = 1e-5, 120
+    mesh = box_mesh(20, 7, 3, 0.02, 0.007, 0.003)
+    runs = []
+    for mode in ("graph", "host", "run"):
+        m = api.Monodomain(mesh, "TNNP", "epicardialCells", SIGMA, dt=dt, boxes=BOX,
+                           implicit=implicit)
+        if mode == "host":
+            m.set_graph(False)
+        if mode == "run":
+            m.run(dt, nsteps)
+        else:
+            for _ in range(nsteps):
+                m.step(dt)
+        runs.append((m.vm(), m.activation(), m.stats(), m.time()))
+    (v0, a0, s0, t0), (v1, a1, s1, t1), (v2, a2, s2, t2) = runs
+    assert np.array_equal(v0, v1) and np.array_equal(v0, v2)
+    assert np.array_equal(a0, a1) and np.array_equal(a0, a2)
+    if implicit:
+        assert np.array_equal(s0[2], s1[2]) and np.array_equal(s0[2], s2[2])
+    assert t0 == t1 == t2
