@@ -166,7 +166,9 @@ def gpu_arm(args, rank, world):
     act_mixed = mixed.activation()
     clocks = clk.summary()
 
-    # ---------------- FP64 plain form on the same workload
+    # ---------------- FP64 plain form on the same workload; both forms then
+    # run to the end of an accuracy window and their activation times are
+    # compared over the cells both activated
     k64 = max(1, min(args.steps, args.fp64_steps))
     fp64 = make_model(mesh, lib.PRECISION_FP64)
     for _ in range(args.warmup):
@@ -174,17 +176,17 @@ def gpu_arm(args, rank, world):
     fp64.set_timing(True)
     t_fp64 = timed_steps(fp64, k64, flush)
     ionic64_ms, diff64_ms, _, _ = fp64.timings()
-    # activation-time difference over the cells both runs activated in the
-    # common simulated window
-    common = args.warmup + k64
+    fp64.set_timing(False)
+    window = max(args.accuracy_steps, args.warmup + k64)
+    fp64.run(DT, window - args.warmup - k64)
     mixed_b = make_model(mesh, lib.PRECISION_MIXED)
-    for _ in range(common):
-        mixed_b.step(DT)
+    mixed_b.run(DT, window)
     a64, amx = fp64.activation(), mixed_b.activation()
     both = (a64 > 0) & (amx > 0)
     act_err_ms = float(np.max(np.abs(a64[both] - amx[both])) * 1e3) if both.any() else None
     mismatch = int(np.sum((a64 > 0) != (amx > 0)))
-    del mixed_b
+    vm_err = float(np.max(np.abs(fp64.vm() - mixed_b.vm())))
+    del mixed_b, fp64
 
     # ---------------- end to end through the C ABI with host copies
     pin_in = torch.empty(n, dtype=torch.float64, pin_memory=True)
@@ -215,7 +217,7 @@ def gpu_arm(args, rank, world):
     return dict(n=n, t_mixed=t_mixed, t_fp64=t_fp64, k64=k64, ionic_ms=ionic_ms,
                 diff_ms=diff_ms, ionic64_ms=ionic64_ms, diff64_ms=diff64_ms, evals=evals,
                 launches=launches, clocks=clocks, act_err_ms=act_err_ms, act_mismatch=mismatch,
-                act_cells=int(both.sum()), t_e2e=t_e2e, ke2e=ke2e, achieved=achieved,
+                act_cells=int(both.sum()), vm_err=vm_err, window=window, t_e2e=t_e2e, ke2e=ke2e, achieved=achieved,
                 fp32_peak=fp32_peak, peaks=pk, peak_src=src, nnz=nnz,
                 n_active_mixed=int((act_mixed > 0).sum()))
 
@@ -286,6 +288,8 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=12)
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--ref-steps", type=int, default=10)
+    ap.add_argument("--accuracy-steps", type=int, default=300,
+                    help="steps both forms run before activation times are compared")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-graph", action="store_true",
                     help="host-driven PIMPLE/PCG loops instead of the step graph")
@@ -328,6 +332,7 @@ def main():
                  "diffusion_ms_per_step": r["diff64_ms"] / r["k64"]},
         "speedup_vs_fp64": value / world / fp64_value,
         "activation_error_ms": r["act_err_ms"], "activation_cells_compared": r["act_cells"],
+        "accuracy_window_steps": r["window"], "vm_linf_error_V": r["vm_err"],
         "activation_flag_mismatches": r["act_mismatch"],
         "phases_ms_per_step": {"ionic": r["ionic_ms"] / args.steps,
                                "diffusion": r["diff_ms"] / args.steps},

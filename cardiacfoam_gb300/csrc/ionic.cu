@@ -103,6 +103,20 @@ int ionic_validate(const cfg_ionic_desc* d, const IonicModelOps** model, int* ti
                             int(d->tissue_per_cell[c]));
     }
     if (!(d->initial_delta_t > 0)) return fail(CFG_ERR_INVALID, "initialDeltaT must be positive");
+    // MyocardiumDomain::validateNoIonicStimulusInMonodomain (myocardiumDomain.C:377-394)
+    // with stimulusIO::hasActiveStimulus (stimulusIO.C:288-303)
+    {
+        const cfg_stimulus_desc& s = d->stimulus;
+        const double small = 1e-15;
+        const bool s1 = s.stim_period_s1 > small && s.nstim1 > 0 && s.stim_duration > small &&
+                        std::fabs(s.stim_amplitude) > small;
+        const bool s2 = s.stim_period_s2 > small && s.nstim2 > 0 && s.stim_duration > small &&
+                        std::fabs(s.stim_amplitude) > small;
+        if (!d->solve_vm_within_ode && (s1 || s2))
+            return fail(CFG_ERR_INVALID,
+                        "Detected active ionic-model stimulus protocol while using a "
+                        "reaction-diffusion myocardium domain; use externalStimulus instead");
+    }
     *model = m;
     *tissue = flag;
     return CFG_OK;
