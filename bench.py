@@ -40,6 +40,14 @@ WORKLOAD = ("ORd myocyte monodomain slab 20x7x3 mm, h=0.1 mm (200x70x30 = 420000
 DIMS = (200, 70, 30)
 H = 1e-4
 DT = 5e-6
+# DRAM bytes (read + write) of one mixed ORd ionic launch on this workload,
+# from an ncu capture of the current kernel (dram__bytes_read.sum +
+# dram__bytes_write.sum); ncu cannot run inside the timed region, so the
+# figure is carried here and refreshed with each capture.
+IONIC_TRAFFIC_BYTES = 1027.8e6
+IONIC_TRAFFIC_SOURCE = "profiles/ionic_step_kernel_ord_mixed_420k.md"
+# states read and written (31 FP32 + 10 FP64 = 204 B) + Vm in + Iion out
+IONIC_STATE_BYTES = 2 * 204 + 16
 
 
 def peaks():
@@ -342,7 +350,10 @@ def main():
                         "cfg_monodomain_get_field(Vm), pinned host buffers"},
         "roofline": {"bound": "fp32", "kernel": "ionic_step_kernel<ORd, mixed>",
                      "achieved": r["achieved"], "peak": r["fp32_peak"], "unit": "TFLOP/s",
-                     "frac": r["achieved"] / r["fp32_peak"], "traffic": None,
+                     "frac": r["achieved"] / r["fp32_peak"],
+                     "traffic": IONIC_TRAFFIC_BYTES, "traffic_unit": "bytes per launch",
+                     "traffic_source": IONIC_TRAFFIC_SOURCE,
+                     "algorithmic_bytes": IONIC_STATE_BYTES * n,
                      "work": f"{r['evals']} RHS evaluations x "
                              f"{opcounts()['ORd']['flops']:.0f} FLOP + "
                              f"{opcounts()['ORd']['transcendental']:.0f} transcendental",
