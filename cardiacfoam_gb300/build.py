@@ -58,6 +58,7 @@ def _units():
     units.append(("diffusion", CSRC / "diffusion.cu", []))
     units.append(("monodomain", CSRC / "monodomain.cu", []))
     units.append(("step_graph", CSRC / "step_graph.cu", []))
+    units.append(("noalloc", CSRC / "noalloc.cu", []))
     units.append(("dictionary", CSRC / "dictionary.cpp", []))
     return units
 

@@ -80,6 +80,21 @@ class StepStats(C.Structure):
                 ("initial_residual", C.c_double * 16), ("final_residual", C.c_double * 16)]
 
 
+class BoxDiffusionDesc(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int),
+                ("cell_volume", C.c_double), ("face_coeff", C.c_double * 3),
+                ("chi", C.c_double), ("cm", C.c_double), ("ddt_backward", C.c_int),
+                ("pcg_tol", C.c_double), ("pcg_rel_tol", C.c_double),
+                ("pcg_max_iter", C.c_int)]
+
+
+class SolveResult(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("converged", C.c_int),
+                ("initial_residual", C.c_double), ("final_residual", C.c_double)]
+
+
+NOALLOC_MAX_CELLS = 65536
+
 # every symbol declared in include/cardiac_gpu.h
 EXPORTS = [
     "cfg_last_error", "cfg_ionic_create", "cfg_ionic_solve", "cfg_ionic_solve_device",
@@ -89,7 +104,7 @@ EXPORTS = [
     "cfg_monodomain_step", "cfg_monodomain_run", "cfg_monodomain_set_graph", "cfg_monodomain_get_field",
     "cfg_monodomain_set_field", "cfg_monodomain_time", "cfg_monodomain_ionic",
     "cfg_monodomain_last_stats", "cfg_monodomain_set_timing", "cfg_monodomain_timings",
-    "cfg_monodomain_stream", "cfg_monodomain_destroy",
+    "cfg_monodomain_stream", "cfg_monodomain_destroy", "cfg_box_diffusion_solve_noalloc",
 ]
 
 _lib = None
@@ -137,6 +152,10 @@ def load(path: Optional[os.PathLike] = None):
     L.cfg_monodomain_stream.argtypes = [C.c_void_p]
     L.cfg_monodomain_stream.restype = C.c_void_p
     L.cfg_monodomain_destroy.argtypes = [C.c_void_p]
+    L.cfg_box_diffusion_solve_noalloc.argtypes = [C.POINTER(BoxDiffusionDesc), C.c_double,
+                                                  C.c_void_p, C.c_void_p, C.c_void_p,
+                                                  C.c_void_p, C.c_void_p,
+                                                  C.POINTER(SolveResult)]
     if path is None:
         _lib = L
     return L

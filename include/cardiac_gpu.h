@@ -211,6 +211,51 @@ int cfg_monodomain_timings(const cfg_monodomain* md, double* ionic_ms, double* d
 void* cfg_monodomain_stream(cfg_monodomain* md);
 int cfg_monodomain_destroy(cfg_monodomain* md);
 
+/* ------------------------------------ diffusion solve without allocation
+ * No counterpart in the reference.  For callers that cannot call cudaMalloc
+ * when they need a solve (a host application that owns all device memory
+ * through its own pool, or one that cannot take the device-wide
+ * synchronisation of cudaFree/cudaMalloc in the middle of a step): one
+ * implicit diffusion corrector of the monodomain equation
+ *   chi*Cm*ddt(Vm) - laplacian(sigma, Vm) = -chi*Cm*Iion
+ * on a structured box (x fastest, uniform cells, one face coefficient per
+ * direction), solved with the monodomain step's own PCG kernels, and no
+ * device memory allocated: the temporaries live in one static device array
+ * of CFG_NOALLOC_SCRATCH_BYTES, held on every GPU that loads the library
+ * until the process exits.  Boxes above CFG_NOALLOC_MAX_CELLS cells are
+ * rejected with CFG_ERR_INVALID.
+ *
+ * vm_old, vm_oldold (backward ddt only; may be NULL for Euler), iion are
+ * read; vm holds the initial guess on entry and the solution on return;
+ * all are device pointers of nx*ny*nz doubles.  stream is a cudaStream_t
+ * (NULL: the legacy default stream); the call returns after the solve
+ * finished.  The first call on a device looks up the array's address with
+ * that device current: make it before any stream capture on the device.
+ * Every call shares the array: calls that overlap on the GPU race. */
+#define CFG_NOALLOC_MAX_CELLS 65536
+#define CFG_NOALLOC_SCRATCH_BYTES 7880704   /* 15 vectors of 64 Ki doubles + state */
+
+typedef struct cfg_box_diffusion_desc {
+    int nx, ny, nz;                /* cells per direction */
+    double cell_volume;            /* [m^3] */
+    double face_coeff[3];          /* deltaCoeffs*(Sf.sigma.Sf)/|Sf| of x, y, z faces */
+    double chi, cm;                /* surface-to-volume ratio, membrane capacitance */
+    int ddt_backward;              /* 0: Euler, 1: backward with both old levels */
+    double pcg_tol, pcg_rel_tol;
+    int pcg_max_iter;
+} cfg_box_diffusion_desc;
+
+typedef struct cfg_solve_result {
+    int iterations;
+    int converged;                 /* 0 when maxIter ended the solve */
+    double initial_residual, final_residual;
+} cfg_solve_result;
+
+int cfg_box_diffusion_solve_noalloc(const cfg_box_diffusion_desc* desc, double delta_t,
+                                    const double* vm_old, const double* vm_oldold,
+                                    const double* iion, double* vm, void* stream,
+                                    cfg_solve_result* result);
+
 #ifdef __cplusplus
 }
 #endif
