@@ -326,8 +326,18 @@ int cfg_ionic_get_states(cfg_ionic* ion, double* host)
     for (int i = 0; i < ns; ++i) {
         const int w = ion->ops->wide_of[p * ns + i], s = ion->ops->slot_of[p * ns + i];
         if (w) {
-            CFG_CUDA_TRY(cudaMemcpyAsync(host + size_t(i) * n, ion->d_yw + size_t(s) * n,
-                                         sizeof(double) * n, cudaMemcpyDeviceToHost, ion->stream));
+            double* dst = host + size_t(i) * n;
+            CFG_CUDA_TRY(cudaMemcpyAsync(dst, ion->d_yw + size_t(s) * n, sizeof(double) * n,
+                                         cudaMemcpyDeviceToHost, ion->stream));
+            if (p == CFG_PRECISION_MIXED) {
+                // each slot holds the FP32 pair (hi, lo) of the state
+                CFG_CUDA_TRY(cudaStreamSynchronize(ion->stream));
+                for (long long c = 0; c < n; ++c) {
+                    float hl[2];
+                    std::memcpy(hl, dst + c, sizeof hl);
+                    dst[c] = double(hl[0]) + double(hl[1]);
+                }
+            }
         } else {
             tmp.resize(n);
             CFG_CUDA_TRY(cudaMemcpyAsync(tmp.data(), ion->d_yn + size_t(s) * n, sizeof(float) * n,
@@ -348,7 +358,17 @@ int cfg_ionic_set_states(cfg_ionic* ion, const double* host)
     std::vector<float> tmp;
     for (int i = 0; i < ns; ++i) {
         const int w = ion->ops->wide_of[p * ns + i], s = ion->ops->slot_of[p * ns + i];
-        if (w) {
+        if (w && p == CFG_PRECISION_MIXED) {
+            std::vector<double> pairs(static_cast<size_t>(n));
+            for (long long c = 0; c < n; ++c) {
+                const double v = host[size_t(i) * n + c];
+                const float hl[2] = {float(v), float(v - double(float(v)))};
+                std::memcpy(&pairs[size_t(c)], hl, sizeof hl);
+            }
+            CFG_CUDA_TRY(cudaMemcpyAsync(ion->d_yw + size_t(s) * n, pairs.data(),
+                                         sizeof(double) * n, cudaMemcpyHostToDevice, ion->stream));
+            CFG_CUDA_TRY(cudaStreamSynchronize(ion->stream));
+        } else if (w) {
             CFG_CUDA_TRY(cudaMemcpyAsync(ion->d_yw + size_t(s) * n, host + size_t(i) * n,
                                          sizeof(double) * n, cudaMemcpyHostToDevice, ion->stream));
         } else {

@@ -12,7 +12,7 @@ struct cfg_ionic {
     int tissue = 0;
     cfg::OdeSettings ode{};
     cfg::CfgStimulus stim{};
-    double* d_yw = nullptr;        // wide (double) states, SoA
+    double* d_yw = nullptr;        // wide states, SoA: FP64, or FP32 (hi, lo) pairs (mixed)
     float* d_yn = nullptr;         // narrow (float) states, SoA (mixed form)
     double* d_step = nullptr;      // per-cell persistent ODE step
     double* d_vm = nullptr;        // staging for host-field solves

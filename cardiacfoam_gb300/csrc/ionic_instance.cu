@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include "ionic_kernels.cuh"
+#include "ionic_mixed.cuh"
 
 #define CFG_STR2(x) #x
 #define CFG_STR(x) CFG_STR2(x)
@@ -23,15 +24,57 @@ static constexpr bool kFP64 = CFG_FP64 != 0;
 using cfg::TissueList;
 using Tissues = cfg::CFG_MODEL::TissueSet;
 
+// The plain form runs ionic_step_kernel (one cell per thread, stage arrays
+// per thread); the mixed form runs ionic_mixed_kernel (stage data in shared
+// memory, block size fixed by the model's slice length).
+template <bool SV, int T>
+static void launch_one(const cfg::IonicLaunch& p, cudaStream_t s, int block)
+{
+    if constexpr (kFP64) {
+        const unsigned grid = unsigned((p.n + block - 1) / block);
+        cfg::ionic_step_kernel<M, true, SV, T><<<grid, block, 0, s>>>(p);
+    } else {
+        using S = cfg::mixed::Slice<M>;
+        const unsigned grid = unsigned((p.n + S::block - 1) / S::block);
+        cfg::ionic_mixed_kernel<M, SV, T><<<grid, S::block, S::smem_bytes, s>>>(p);
+    }
+}
+
+// Opt the mixed kernels into their dynamic shared memory (above the 48 KB
+// default) on the current device; runs when a model is created, before any
+// launch can be captured into a graph.
+template <bool SV, int T>
+static cudaError_t prepare_one()
+{
+    if constexpr (kFP64) {
+        return cudaSuccess;
+    } else {
+        return cudaFuncSetAttribute(&cfg::ionic_mixed_kernel<M, SV, T>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    cfg::mixed::Slice<M>::smem_bytes);
+    }
+}
+
+template <int... TS>
+static cudaError_t prepare_all(TissueList<TS...>)
+{
+    cudaError_t e = prepare_one<true, 0>();
+    if (e == cudaSuccess) e = prepare_one<false, 0>();
+    cudaError_t r[] = {cudaSuccess, prepare_one<false, TS>()...};
+    for (cudaError_t x : r)
+        if (e == cudaSuccess) e = x;
+    return e;
+}
+
 template <int T0, int... TR>
-static bool launch_uniform(const cfg::IonicLaunch& p, cudaStream_t s, unsigned grid, int block,
+static bool launch_uniform(const cfg::IonicLaunch& p, cudaStream_t s, int block,
                            TissueList<T0, TR...>)
 {
     if (p.tissue == T0) {
-        cfg::ionic_step_kernel<M, kFP64, false, T0><<<grid, block, 0, s>>>(p);
+        launch_one<false, T0>(p, s, block);
         return true;
     }
-    if constexpr (sizeof...(TR) > 0) return launch_uniform(p, s, grid, block, TissueList<TR...>{});
+    if constexpr (sizeof...(TR) > 0) return launch_uniform(p, s, block, TissueList<TR...>{});
     return false;
 }
 
@@ -39,14 +82,13 @@ extern "C" cudaError_t CFG_CAT3(cfg_ionic_step_, CFG_MODEL, CFG_PREC_TAG)(
     const cfg::IonicLaunch& p, int solve_vm, cudaStream_t stream, int block)
 {
     if (p.n <= 0) return cudaSuccess;
-    const unsigned grid = unsigned((p.n + block - 1) / block);
     const bool uniform = !p.tissue_cell && !p.scales;
     if (solve_vm) {
-        cfg::ionic_step_kernel<M, kFP64, true, 0><<<grid, block, 0, stream>>>(p);
-    } else if (uniform && launch_uniform(p, stream, grid, block, Tissues{})) {
+        launch_one<true, 0>(p, stream, block);
+    } else if (uniform && launch_uniform(p, stream, block, Tissues{})) {
         // tissue-specialised kernel launched
     } else {
-        cfg::ionic_step_kernel<M, kFP64, false, 0><<<grid, block, 0, stream>>>(p);
+        launch_one<false, 0>(p, stream, block);
     }
     return cudaGetLastError();
 }
@@ -56,6 +98,7 @@ extern "C" cudaError_t CFG_CAT3(cfg_ionic_init_, CFG_MODEL, CFG_PREC_TAG)(
     long long stride, double init_step, double* yw, float* yn, double* step,
     cudaStream_t stream)
 {
+    if (cudaError_t e = prepare_all(Tissues{})) return e;
     if (n <= 0) return cudaSuccess;
     const int block = 128;
     const unsigned grid = unsigned((n + block - 1) / block);

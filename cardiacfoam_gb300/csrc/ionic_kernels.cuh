@@ -350,7 +350,8 @@ CFG_D __forceinline__ long long rkf45_solve(double xs, double xe, CellState<M, R
     return -1;
 }
 
-// Tissue / single-cell ionic update of one PDE step for all cells.
+// Tissue / single-cell ionic update of one PDE step for all cells (the plain
+// FP64 form; the mixed form runs ionic_mixed_kernel).
 // TISSUE > 0: every cell has that tissue flag and no per-cell scales, and the
 // constants are compile-time values; TISSUE == 0: constants are evaluated per
 // cell (per-cell tissue flags or conductance scales).
@@ -468,8 +469,16 @@ __global__ void ionic_init_kernel(long long n, int tissue, const unsigned char* 
     M::init(C, y, t, scp);
 #pragma unroll
     for (int i = 0; i < M::NS; ++i) {
-        if (FP64 || is_wide<M::WIDE_MASK>(i)) yw[(long long)L::slot(i) * n + c] = y[i];
-        else yn[(long long)L::slot(i) * n + c] = float(y[i]);
+        if (FP64) {
+            yw[(long long)L::slot(i) * n + c] = y[i];
+        } else if (is_wide<M::WIDE_MASK>(i)) {
+            // mixed form: the slot holds the FP32 pair (hi, lo) of the state
+            const float hi = float(y[i]);
+            reinterpret_cast<float2*>(yw)[(long long)L::slot(i) * n + c] =
+                make_float2(hi, float(y[i] - double(hi)));
+        } else {
+            yn[(long long)L::slot(i) * n + c] = float(y[i]);
+        }
     }
     step[c] = init_step;
 }

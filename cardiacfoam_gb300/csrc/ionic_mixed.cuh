@@ -1,0 +1,399 @@
+// Mixed-precision ionic step with the RKF45 stage data in shared memory.
+//
+// The six stage derivatives, the stage input and the state of one cell
+// (~1.2 KB for ORd) do not fit in registers; as per-thread local arrays they
+// overflow the L1 at useful occupancy and round-trip through L2/DRAM.  Here
+// each thread owns a slice of dynamic shared memory instead:
+//
+//   Y[NSP]   states in FP32 (the high part for the slow states)
+//   T[NSP]   stage input
+//   K[5][NSP] stage slots: k1..k5, then (after the stage-6 input is formed)
+//            P = sum b_j k_j (j<6), E = sum e_j k_j (j<6), k6, and the FP32
+//            round-off bound of E
+//   LO[NW]   low parts of the slow (WIDE_MASK) states
+//
+// The slice length is odd, so the 32 threads of a warp touching the same
+// element hit 32 different banks.
+//
+// Arithmetic: right-hand sides, stage sums, error norm and step control in
+// FP32 (with step control relative to the start of the PDE step, which keeps
+// its FP32 resolution); slow states as unevaluated FP32 sums hi + lo
+// (Knuth two-sum), which keeps ~48 bits for concentrations whose increments
+// are below the FP32 resolution of their values; in global memory each slow
+// state is that (hi, lo) pair in the 8 bytes of its slot.  FP64 is left only
+// for the PDE fields (Vm in, Iion out) and the persistent step, a handful of
+// operations per cell: GB300 issues FP64 at 1/64 of the FP32 rate, so FP64
+// inside the RKF45 loop, or on every state, would cost as much as the model
+// body itself.
+#pragma once
+
+#include "ionic_kernels.cuh"
+
+namespace cfg {
+
+namespace mixed {
+
+// dynamic shared memory per SM available to blocks (228 KB) and the
+// per-block reservation
+constexpr int kSmemPerSm = 233472;
+constexpr int kSmemReserve = 1024;
+
+constexpr int blocks_per_sm(int block, int len)
+{
+    return kSmemPerSm / (block * len * 4 + kSmemReserve);
+}
+
+template <class M>
+struct Slice {
+    static constexpr int NSP = M::NS | 1;   // odd stride for each array
+    static constexpr int NW = Layout<M, false>::n_wide();
+    static constexpr int raw = 7 * NSP + NW;
+    static constexpr int len = raw | 1;       // odd slice length: conflict-free
+    // 64 threads per block unless 32 keeps more threads resident per SM
+    static constexpr int block =
+        32 * blocks_per_sm(32, len) > 64 * blocks_per_sm(64, len) ? 32 : 64;
+    static constexpr int fit = blocks_per_sm(block, len);
+    static constexpr int min_blocks = fit < 1 ? 1 : (fit > 16 ? 16 : fit);
+    static constexpr int smem_bytes = block * len * 4;
+};
+
+constexpr float fa21 = float(rkf::a21);
+constexpr float fa31 = float(rkf::a31), fa32 = float(rkf::a32);
+constexpr float fa41 = float(rkf::a41), fa42 = float(rkf::a42), fa43 = float(rkf::a43);
+constexpr float fa51 = float(rkf::a51), fa52 = float(rkf::a52), fa53 = float(rkf::a53),
+                fa54 = float(rkf::a54);
+constexpr float fa61 = float(rkf::a61), fa62 = float(rkf::a62), fa63 = float(rkf::a63),
+                fa64 = float(rkf::a64), fa65 = float(rkf::a65);
+constexpr float fb1 = float(rkf::b1), fb3 = float(rkf::b3), fb4 = float(rkf::b4),
+                fb5 = float(rkf::b5), fb6 = float(rkf::b6);
+constexpr float fe1 = float(rkf::e1), fe3 = float(rkf::e3), fe4 = float(rkf::e4),
+                fe5 = float(rkf::e5), fe6 = float(rkf::e6);
+CFG_D __forceinline__ float stage_c(int s)
+{
+    switch (s) {
+    case 1: return float(rkf::c2);
+    case 2: return float(rkf::c3);
+    case 3: return float(rkf::c4);
+    case 4: return float(rkf::c5);
+    case 5: return float(rkf::c6);
+    default: return 0.0f;
+    }
+}
+
+// hi + lo += d, renormalised (two-sum of hi and d, low parts added after)
+CFG_D __forceinline__ void add_wide(float& hi, float& lo, float d)
+{
+    const float s = hi + d;
+    const float bp = s - hi;
+    const float err = (hi - (s - bp)) + (d - bp);
+    const float l = lo + err;
+    const float h = s + l;
+    lo = l - (h - s);
+    hi = h;
+}
+
+// Stage input T = Y + h * sum_j a_sj k_j for stages 2..5 (s = 1..4).
+template <class M>
+CFG_D __forceinline__ void stage_input(int s, float h, const float* Y, float* T, const float* K)
+{
+    constexpr int NS = M::NS, P = Slice<M>::NSP;
+    switch (s) {
+    case 1:
+#pragma unroll 4
+        for (int i = 0; i < NS; ++i) T[i] = Y[i] + h * (fa21 * K[i]);
+        break;
+    case 2:
+#pragma unroll 4
+        for (int i = 0; i < NS; ++i) {
+            float acc = fa31 * K[i];
+            acc += fa32 * K[P + i];
+            T[i] = Y[i] + h * acc;
+        }
+        break;
+    case 3:
+#pragma unroll 4
+        for (int i = 0; i < NS; ++i) {
+            float acc = fa41 * K[i];
+            acc += fa42 * K[P + i];
+            acc += fa43 * K[2 * P + i];
+            T[i] = Y[i] + h * acc;
+        }
+        break;
+    default:
+#pragma unroll 4
+        for (int i = 0; i < NS; ++i) {
+            float acc = fa51 * K[i];
+            acc += fa52 * K[P + i];
+            acc += fa53 * K[2 * P + i];
+            acc += fa54 * K[3 * P + i];
+            T[i] = Y[i] + h * acc;
+        }
+        break;
+    }
+}
+
+// Stage-6 input, and P, E and the round-off bound of E into slots 1, 2, 4
+// (k2 and the old k3..k5 are not needed afterwards: b2 = e2 = 0).
+template <class M>
+CFG_D __forceinline__ void stage6_input(float h, const float* Y, float* T, float* K)
+{
+    constexpr int NS = M::NS, P = Slice<M>::NSP;
+#pragma unroll 4
+    for (int i = 0; i < NS; ++i) {
+        const float k1 = K[i], k2 = K[P + i], k3 = K[2 * P + i], k4 = K[3 * P + i],
+                    k5 = K[4 * P + i];
+        float acc = fa61 * k1;
+        acc += fa62 * k2;
+        acc += fa63 * k3;
+        acc += fa64 * k4;
+        acc += fa65 * k5;
+        T[i] = Y[i] + h * acc;
+        K[P + i] = fb1 * k1 + fb3 * k3 + fb4 * k4 + fb5 * k5;
+        K[2 * P + i] = fe1 * k1 + fe3 * k3 + fe4 * k4 + fe5 * k5;
+        K[4 * P + i] = fabsf(fe1 * k1) + fabsf(fe3 * k3) + fabsf(fe4 * k4) + fabsf(fe5 * k5);
+    }
+}
+
+// ODESolver::solve over [xs, xs + D] (RKF45 inside adaptiveSolver::solve),
+// then the right-hand side at the end of the interval for the current.
+// Returns accepted substeps, or -1 on maxSteps overflow / step underflow.
+template <class M, bool SV, class KS>
+CFG_D __forceinline__ long long solve(double xs, double xe, float D, float* Y, float* T, float* K, float* LO,
+                                      float& dx_try, const KS& Kc, int tissue,
+                                      const CfgStimulus& st, const OdeSettings& s,
+                                      unsigned& evals, IonicFailure& why, float& iion)
+{
+    constexpr int NS = M::NS, P = Slice<M>::NSP;
+    const float abs_tol = float(s.abs_tol), rel_tol = float(s.rel_tol);
+    const float safe = float(s.safe_scale), min_scale = float(s.min_scale),
+                max_scale = float(s.max_scale), a_inc = float(s.alpha_inc),
+                a_dec = float(s.alpha_dec), inc_thr = float(s.inc_threshold);
+    constexpr float noise_ulps = float(kFp32NoiseUlps * 1.1920929e-07);
+
+    float u = 0.0f;            // x - xs
+    float u_prev = 0.0f;
+    float step_dx = dx_try;
+    float dx = 0.0f, dx_try0 = 0.0f;
+    bool last = false, to_end = false;
+    long long n = 0;           // substep (ODESolver::solve loop index)
+    int sg = 0;                // next evaluation: stage 0..5, 6 = current at xs + D
+    bool begin = true;
+    float err = 0.0f;
+    int worst = -1;
+    for (;;) {
+        if (begin) {
+            if (n >= s.max_steps) {
+                // the last accepted substep, as ODESolver reports it
+                why.reason = 1;
+                why.x = xs + double(u_prev); why.dx = dx; why.err = err; why.worst = worst;
+                why.value = worst >= 0 ? double(Y[worst]) : 0.0;
+                why.steps = n - 1;
+                return -1;
+            }
+            begin = false;
+            dx_try0 = step_dx;
+            to_end = false;
+            if (u + step_dx > D) {
+                last = true;
+                step_dx = D - u;
+            }
+            if (u + step_dx >= D) to_end = true;
+            dx = step_dx;
+            sg = 0;
+        }
+        const float h = dx;
+        const float* in = Y;
+        float* out;
+        if (sg == 0) {
+            out = K;
+        } else if (sg < 5) {
+            stage_input<M>(sg, h, Y, T, K);
+            in = T;
+            out = K + sg * P;
+        } else if (sg == 5) {
+            stage6_input<M>(h, Y, T, K);
+            in = T;
+            out = K + 3 * P;
+        } else {
+            out = T;
+        }
+        double t = 0.0;
+        if constexpr (SV) t = sg == 6 ? xe : xs + double(u) + double(stage_c(sg) * h);
+        const float r = M::template rates<float, SV>(t, ArrayView<float>{in}, Kc, out, tissue, st);
+        ++evals;
+        if (sg == 6) {
+            iion = r;
+            return n;
+        }
+        if (sg < 5) {
+            ++sg;
+            continue;
+        }
+        // --- RKF45::solve error estimate and ODESolver::normalizeError
+        float maxerr = 0.0f;
+        worst = -1;
+#pragma unroll 4
+        for (int i = 0; i < NS; ++i) {
+            const float k6 = K[3 * P + i];
+            const float y0 = Y[i];
+            const float y5 = y0 + h * (K[P + i] + fb6 * k6);
+            const float e_i = h * (K[2 * P + i] + fe6 * k6);
+            const float noise = noise_ulps * h * (K[4 * P + i] + fabsf(fe6 * k6));
+            const float a = fabsf(y0), b = fabsf(y5);
+            const float tol = abs_tol + rel_tol * (a > b ? a : b) + noise;
+            const float e = fabsf(e_i) / tol;
+            if (e > maxerr) { maxerr = e; worst = i; }
+        }
+        err = maxerr;
+        if (err > 1.0f) {
+            float scale = safe * __powf(err, -a_dec);
+            if (scale < min_scale) scale = min_scale;
+            dx *= scale;
+            if (!(dx >= 1e-37f)) {
+                why.reason = 2;
+                why.x = xs + double(u); why.dx = dx; why.err = err; why.worst = worst;
+                why.value = worst >= 0 ? double(Y[worst]) : 0.0;
+                why.steps = n;
+                return -1;
+            }
+            sg = 1;   // k1 = f(y) is reused
+            continue;
+        }
+        // --- accept: y = y5 (slow states as hi + lo)
+        int w = 0;
+#pragma unroll 4
+        for (int i = 0; i < NS; ++i) {
+            const float incr = h * (K[P + i] + fb6 * K[3 * P + i]);
+            if (is_wide<M::WIDE_MASK>(i)) {
+                float hi = Y[i], lo = LO[w];
+                add_wide(hi, lo, incr);
+                Y[i] = hi;
+                LO[w] = lo;
+                ++w;
+            } else {
+                Y[i] = Y[i] + incr;
+            }
+        }
+        u_prev = u;
+        u = (to_end && dx == step_dx) ? D : u + dx;
+        if (err > inc_thr) {
+            float scale = safe * __powf(err, -a_inc);
+            if (scale > max_scale) scale = max_scale;
+            step_dx = scale * dx;
+        } else {
+            step_dx = safe * max_scale * dx;
+        }
+        if (u >= D) {
+            if (n > 0 && last) step_dx = dx_try0;
+            dx_try = step_dx;
+            ++n;
+            sg = 6;
+            continue;
+        }
+        ++n;
+        begin = true;
+    }
+}
+
+}  // namespace mixed
+
+// Mixed-form tissue / single-cell step with shared-memory stage data.
+// TISSUE > 0: uniform tissue with compile-time constants; TISSUE == 0:
+// constants per cell (per-cell tissue flags or conductance scales).
+template <class M, bool SV, int TISSUE>
+__global__ void __launch_bounds__(mixed::Slice<M>::block, mixed::Slice<M>::min_blocks)
+ionic_mixed_kernel(IonicLaunch p)
+{
+    using S = mixed::Slice<M>;
+    using L = Layout<M, false>;
+    constexpr int NS = M::NS, P = S::NSP;
+    extern __shared__ float cfg_mixed_smem[];
+    float* Y = cfg_mixed_smem + threadIdx.x * S::len;
+    float* T = Y + P;
+    float* K = T + P;
+    float* LO = K + 5 * P;
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned evals = 0;
+    if (c < p.n) {
+        const double t0 = p.t_dev ? p.t_dev[0] : p.t0;
+        double ts, te, dtm;
+        model_times<M>(t0, p.dt, ts, te, dtm);
+        // derivatives the model does not assign (Vm in tissue mode) stay zero
+        // in every stage slot, as in a zero-filled dydt array
+        for (int i = 0; i < 6 * P; ++i) T[i] = 0.0f;
+        const float2* yw2 = reinterpret_cast<const float2*>(p.yw);
+        int w = 0;
+#pragma unroll
+        for (int i = 0; i < NS; ++i) {
+            if (is_wide<M::WIDE_MASK>(i)) {
+                const float2 v = yw2[(long long)L::slot(i) * p.n + c];
+                Y[i] = v.x;
+                LO[w++] = v.y;
+            } else {
+                Y[i] = p.yn[(long long)L::slot(i) * p.n + c];
+            }
+        }
+        if constexpr (!SV) {
+            // Vm from the PDE field, split into hi + lo
+            const double v = vm_to_state0<M::VM_MAP>(p.vm[c]);
+            const float hi = float(v);
+            Y[0] = hi;
+            if (is_wide<M::WIDE_MASK>(0)) LO[0] = float(v - double(hi));
+        }
+        // step = min(step, dt_model); rounding to FP32 keeps the order
+        float dx_try = fminf(float(p.step[c]), float(dtm));
+
+        IonicFailure why;
+        long long nsub;
+        float iion = 0.0f;
+        if constexpr (TISSUE > 0) {
+            const ConstFold<float, M, TISSUE> Kc{};
+            nsub = mixed::solve<M, SV>(ts, te, float(dtm), Y, T, K, LO, dx_try, Kc, TISSUE, p.stim,
+                                       p.ode, evals, why, iion);
+        } else {
+            const int tissue = p.tissue_cell ? int(p.tissue_cell[c]) : p.tissue;
+            double C[M::NC] = {};   // the reference zero-fills CONSTANTS
+            double yinit[NS];
+            double sc[6];
+            const double* scp = nullptr;
+            if (p.scales) {
+#pragma unroll
+                for (int j = 0; j < 6; ++j) sc[j] = p.scales[j * p.scale_stride + c];
+                scp = sc;
+            }
+            M::init(C, yinit, tissue, scp);
+            const ConstView<float> Kc{C};
+            nsub = mixed::solve<M, SV>(ts, te, float(dtm), Y, T, K, LO, dx_try, Kc, tissue, p.stim,
+                                       p.ode, evals, why, iion);
+        }
+        if (nsub < 0) {
+            const int prev = atomicOr(p.status, CFG_ERR_ODE_STEPS);
+            if (p.fail_record && !(prev & CFG_ERR_ODE_STEPS)) {
+                double* r = p.fail_record;
+                r[0] = double(c); r[1] = why.reason; r[2] = why.x; r[3] = why.dx;
+                r[4] = why.worst; r[5] = why.err; r[6] = why.value; r[7] = double(why.steps);
+            }
+        }
+        const double im = double(iion) * M::IION_SCALE;
+        if (!isfinite(im)) atomicOr(p.status, CFG_ERR_NONFINITE);
+        if (p.im) p.im[c] = im;
+        float2* yw2o = reinterpret_cast<float2*>(p.yw);
+        w = 0;
+#pragma unroll
+        for (int i = 0; i < NS; ++i) {
+            if (is_wide<M::WIDE_MASK>(i)) {
+                yw2o[(long long)L::slot(i) * p.n + c] = make_float2(Y[i], LO[w++]);
+            } else {
+                p.yn[(long long)L::slot(i) * p.n + c] = Y[i];
+            }
+        }
+        p.step[c] = double(dx_try);
+    }
+    if (p.rhs_evals) {
+        unsigned long long v = evals;
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if ((threadIdx.x & 31) == 0 && v) atomicAdd(p.rhs_evals, v);
+    }
+}
+
+}  // namespace cfg
