@@ -244,6 +244,11 @@ class Monodomain:
     def set_graph(self, enable: bool = True):
         _L.check(self._lib.cfg_monodomain_set_graph(self.h, int(enable)))
 
+    def set_persistent(self, enable: bool = True):
+        """One persistent diffusion kernel per step (default) or the kernel
+        sequence per PCG iteration."""
+        _L.check(self._lib.cfg_monodomain_set_persistent(self.h, int(enable)))
+
     def set_timing(self, enable: bool = True):
         _L.check(self._lib.cfg_monodomain_set_timing(self.h, int(enable)))
 

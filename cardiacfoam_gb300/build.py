@@ -57,6 +57,7 @@ def _units():
     units.append(("ionic", CSRC / "ionic.cu", []))
     units.append(("diffusion", CSRC / "diffusion.cu", []))
     units.append(("monodomain", CSRC / "monodomain.cu", []))
+    units.append(("diffusion_coop", CSRC / "diffusion_coop.cu", []))
     units.append(("step_graph", CSRC / "step_graph.cu", []))
     units.append(("noalloc", CSRC / "noalloc.cu", []))
     units.append(("dictionary", CSRC / "dictionary.cpp", []))

@@ -28,6 +28,8 @@ __global__ void k_step_begin(DiffusionArgs a)
         st->n_solves = 0;
         st->iter = 0;
         st->step_iters = 0;
+        st->bar_count = 0;
+        st->bar_abort = 0;
     }
 }
 
@@ -212,17 +214,6 @@ __global__ void __launch_bounds__(kDiffBlock) k_pcg_update(DiffusionArgs a)
             }
             set_inner(a, st->solve_active);
         }
-    }
-}
-
-// MyocardiumDomain::updateActivationTime (myocardiumDomain.C:345-374)
-__device__ __forceinline__ void activation(const DiffusionArgs& a, long long c, double vnew,
-                                           double vold, double old_time)
-{
-    if (a.act_flag[c] && vnew > 1e-15) {
-        a.act_flag[c] = 0;
-        const double w = (0.0 - vold) / (vnew - vold);
-        a.act[c] = old_time + w * a.dt;
     }
 }
 

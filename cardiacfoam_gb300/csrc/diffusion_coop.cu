@@ -1,0 +1,423 @@
+// Implicit diffusion of one monodomain step as ONE persistent kernel: every
+// PIMPLE corrector and every PCG iteration of the step runs inside a single
+// cooperative launch whose blocks meet at grid barriers, instead of two to
+// four kernel launches per iteration.
+//
+// The numerics are those of the per-kernel path (diffusion.cu): the same
+// right-hand side, lduMatrix::Amul order, normFactor, L1 residual,
+// convergence test and PIMPLE residual control.  Two things change:
+//   * each thread owns a fixed set of rows for the whole step, so its own
+//     entries of x, r, p, b, A.x and A.p are only ever touched by it; z and
+//     x (read at the neighbours) and the reduction partials cross blocks,
+//     and those are read through L2 (ld.global.cg), which is coherent;
+//   * A.p is updated as A.z + beta A.p, so one halo exchange (of z) serves
+//     both the new direction and its product, and an iteration needs two
+//     grid barriers; reductions are per thread over its rows, then per
+//     block, then summed by every block in the same fixed order.  GB300
+//     executes FP64 at 1/64 of the FP32 rate, so the FP64 instruction count
+//     per row (15 per PCG iteration here) and the barriers set the speed of
+//     the solve, not HBM: its vectors stay in L2.
+//
+// Grid barriers are cooperative-launch safe (all blocks co-resident) and
+// bounded: a block that waits longer than ~1 s sets an abort flag, every
+// block leaves at its next barrier, and the step reports CFG_ERR_PCG.
+#include <cuda_runtime.h>
+
+#include "diffusion_kernels.cuh"
+
+namespace cfg {
+
+namespace {
+
+constexpr int kCoopBlock = 512;
+constexpr int kCoopWarps = kCoopBlock / 32;
+constexpr long long kSpinLimit = 1LL << 25;   // x >= 32 ns per spin: about a second
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned* p)
+{
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ int ld_relaxed_int(const int* p)
+{
+    int v;
+    asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Grid-wide barrier on a monotonic arrival counter (reset every step):
+// each block adds one arrival and waits until all gridDim.x arrivals of this
+// barrier are in; `epoch` counts the arrivals expected so far.  Returns false
+// when the step was aborted (a block waited too long); then every block
+// leaves at its next barrier.
+__device__ __forceinline__ bool grid_barrier(PcgState* st, unsigned& epoch)
+{
+    __shared__ int ok;
+    epoch += gridDim.x;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        atomicAdd(&st->bar_count, 1u);
+        int good = 1;
+        long long spins = 0;
+        while (ld_acquire(&st->bar_count) < epoch) {
+            if (ld_relaxed_int(&st->bar_abort)) { good = 0; break; }
+            if (++spins > kSpinLimit) {
+                atomicExch(&st->bar_abort, 1);
+                good = 0;
+                break;
+            }
+            if (spins > 32) __nanosleep(32);
+        }
+        if (ld_relaxed_int(&st->bar_abort)) good = 0;
+        __threadfence();
+        ok = good;
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+// Block sums of K per-thread values into partial[set][k][blockIdx.x].
+template <int K>
+__device__ __forceinline__ void block_sums(double* partial, int set, double (&v)[K])
+{
+    __shared__ double sh[K][kCoopWarps];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        double s = v[k];
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+        if (lane == 0) sh[k][w] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x < 32 * K && (threadIdx.x & 31) == 0) {
+        const int k = threadIdx.x >> 5;
+        double s = 0.0;
+        for (int j = 0; j < kCoopWarps; ++j) s += sh[k][j];
+        __stcg(&partial[(size_t(set) * 2 + k) * gridDim.x + blockIdx.x], s);
+    }
+}
+
+// Sum of partial[set][k][0..gridDim.x) in a fixed order; every block gets
+// the same value.  Called after a grid barrier, by all threads.
+template <int K>
+__device__ __forceinline__ void grid_sums(const double* partial, int set, double (&out)[K])
+{
+    __shared__ double sh[K];
+    if (threadIdx.x < 32) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            const double* src = partial + (size_t(set) * 2 + k) * gridDim.x;
+            double s = 0.0;
+            for (unsigned i = threadIdx.x; i < gridDim.x; i += 32) s += __ldcg(&src[i]);
+            for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+            if (threadIdx.x == 0) sh[k] = s;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < K; ++k) out[k] = sh[k];
+    __syncthreads();
+}
+
+// x / d for 0 <= x < 2^31 by multiply-high (round-up method): avoids the
+// 64-bit integer division of a cell index in every stencil row.
+struct FastDiv {
+    unsigned m, s;
+};
+
+__device__ __forceinline__ unsigned fdiv(unsigned x, FastDiv f)
+{
+    return (__umulhi(x, f.m) + x) >> f.s;
+}
+
+}  // namespace
+
+struct CoopArgs {
+    FastDiv div_nx, div_ny;   // stencil form only
+};
+
+// A.q for row c (diag*q_c, then each -coef*q_nb in column order), q read
+// through L2.  Stencil neighbours come from (i, j, k) = row decomposition.
+__device__ __forceinline__ double amul_cg(const DiffusionArgs& a, const CoopArgs& ca,
+                                          unsigned c, double d, const double* q)
+{
+    double acc = d * __ldcg(&q[c]);
+    if (a.sx) {
+        const unsigned nx = unsigned(a.sx), nxy = nx * unsigned(a.sy);
+        const unsigned line = fdiv(c, ca.div_nx), i = c - line * nx;
+        const unsigned k = fdiv(line, ca.div_ny), j = line - k * unsigned(a.sy);
+        if (k > 0) acc += (-a.cz) * __ldcg(&q[c - nxy]);
+        if (j > 0) acc += (-a.cy) * __ldcg(&q[c - nx]);
+        if (i > 0) acc += (-a.cx) * __ldcg(&q[c - 1]);
+        if (i + 1 < nx) acc += (-a.cx) * __ldcg(&q[c + 1]);
+        if (j + 1 < unsigned(a.sy)) acc += (-a.cy) * __ldcg(&q[c + nx]);
+        if (k + 1 < unsigned(a.sz)) acc += (-a.cz) * __ldcg(&q[c + nxy]);
+    } else {
+        const int cnt = a.ell_cnt[c];
+        for (int e = 0; e < cnt; ++e)
+            acc += (-a.ell_coef[(long long)e * a.n + c]) *
+                   __ldcg(&q[a.ell_col[(long long)e * a.n + c]]);
+    }
+    return acc;
+}
+
+// The whole implicit diffusion of one step (all correctors, all PCG
+// iterations) and the activation-time update.  Launched cooperatively with
+// every block resident; rows are strided over the grid, two per loop trip so
+// that two independent FP64 chains are in flight per thread.
+//
+// PCG iteration with two grid barriers (lduMatrix PCG in exact arithmetic):
+//   halo pass:   w = A.z (z of the neighbours through L2), p = z + beta p,
+//                A.p = w + beta A.p (linearity of A), sum p.A.p  | barrier
+//   update pass: x += alpha p, r -= alpha A.p, z = D^-1 r (published for
+//                the next halo pass), sums |r| and z.r           | barrier
+__global__ void __launch_bounds__(kCoopBlock, 1) k_implicit_coop(DiffusionArgs a, CoopArgs ca)
+{
+    PcgState* st = a.st;
+    const unsigned n = unsigned(a.n);
+    const unsigned stride = gridDim.x * blockDim.x;
+    const unsigned first = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool lead = blockIdx.x == 0 && threadIdx.x == 0;
+    // values every block reads before block 0 may update them
+    int n_old = st->n_old;
+    const double t_step = st->t, t0 = st->t0;
+    const double tol = st->tol, rel_tol = st->rel_tol, outer_tol = st->outer_tol;
+    const int max_iter = st->max_iter, n_outer = st->n_outer;
+    double* __restrict__ x = a.vm;
+    double* __restrict__ b = a.b;
+    double* __restrict__ ax = a.ax;
+    double* __restrict__ r = a.r;
+    double* __restrict__ z = a.z;     // published: read by neighbours
+    double* __restrict__ p = a.pA;    // own rows only
+    double* __restrict__ ap = a.ap;   // own rows only
+    unsigned epoch = 0;               // arrivals expected at the next barrier
+    int set = 0;                      // partial buffer of the next reduction
+    int n_solves = 0, status = 0;
+    bool converged_outer = false, abort_step = false;
+    long long step_iters = 0;
+    double last_init = 0.0, last_res = 0.0;
+    int last_iter = 0, last_v = 0;
+
+    for (int corr = 1;; ++corr) {
+        const int v = ddt_variant(a, n_old);
+        const double* __restrict__ diag = a.diag2 + size_t(v) * n;
+        const double* __restrict__ rdiag = a.rdiag2 + size_t(v) * n;
+        const double* __restrict__ sumA = a.sumA2 + size_t(v) * n;
+        const double cft0 = a.cft0[v], cft00 = a.cft00[v];
+        // --- source, A.x, r = b - A.x; sums of x and |r|
+        double s1[2] = {0.0, 0.0};
+        auto rhs_row = [&](unsigned c) {
+            const double V = a.vol[c];
+            double ddt_src;
+            if (a.ddt_backward)
+                ddt_src = a.rdt * V * (cft0 * a.vm_old[c] - cft00 * a.vm_oldold[c]);
+            else
+                ddt_src = a.rdt * a.vm_old[c] * V;
+            double bb = a.chicm * ddt_src;
+            double su = -(a.chicm * a.iion[c]) * V;
+            su = su + box_source(a, c, t0) * V;
+            return bb + su;
+        };
+        for (unsigned c = first; c < n; c += 2 * stride) {
+            const unsigned c2 = c + stride;
+            const bool two = c2 < n;
+            const double b0 = rhs_row(c), b1 = two ? rhs_row(c2) : 0.0;
+            const double a0 = amul_cg(a, ca, c, diag[c], x);
+            const double a1 = two ? amul_cg(a, ca, c2, diag[c2], x) : 0.0;
+            const double r0 = b0 - a0, r1 = b1 - a1;
+            b[c] = b0; ax[c] = a0; r[c] = r0;
+            s1[0] += x[c];
+            s1[1] += fabs(r0);
+            if (two) {
+                b[c2] = b1; ax[c2] = a1; r[c2] = r1;
+                s1[0] += x[c2];
+                s1[1] += fabs(r1);
+            }
+        }
+        block_sums<2>(a.partial, set, s1);
+        if (!grid_barrier(st, epoch)) { abort_step = true; break; }
+        double g1[2];
+        grid_sums<2>(a.partial, set, g1);
+        set ^= 1;
+        const double avg = g1[0] / double(n);
+        // fvm::ddt created the old time levels
+        if (n_old < 1) n_old = 1;
+        if (a.ddt_backward && n_old < 2) n_old = 2;
+        // --- normFactor, z = D^-1 r (published), z.r
+        double s2[2] = {0.0, 0.0};
+        for (unsigned c = first; c < n; c += stride) {
+            const double pa = sumA[c] * avg;
+            s2[0] += fabs(ax[c] - pa) + fabs(b[c] - pa);
+            const double zc = rdiag[c] * r[c];
+            __stcg(&z[c], zc);
+            s2[1] += zc * r[c];
+        }
+        block_sums<2>(a.partial, set, s2);
+        if (!grid_barrier(st, epoch)) { abort_step = true; break; }
+        double g2[2];
+        grid_sums<2>(a.partial, set, g2);
+        set ^= 1;
+        const double normf = g2[0] + 1e-20;
+        const double init_res = g1[1] / normf;
+        double res = init_res;
+        double wArA = g2[1], beta = 0.0;
+        int iter = 0;
+        bool aborted = false;
+        const auto conv = [&](double rr) {
+            return rr < tol || (rel_tol > 1e-20 && rr < rel_tol * init_res);
+        };
+        if (!conv(res)) {
+            for (;;) {
+                // --- halo pass: w = A.z, p = z + beta p, A.p = w + beta A.p
+                double s3[1] = {0.0};
+                const bool first_it = iter == 0;
+                for (unsigned c = first; c < n; c += 2 * stride) {
+                    const unsigned c2 = c + stride;
+                    const bool two = c2 < n;
+                    const double w0 = amul_cg(a, ca, c, diag[c], z);
+                    const double w1 = two ? amul_cg(a, ca, c2, diag[c2], z) : 0.0;
+                    const double z0 = __ldcg(&z[c]);
+                    const double z1 = two ? __ldcg(&z[c2]) : 0.0;
+                    double p0, p1, q0, q1;
+                    if (first_it) {
+                        p0 = z0; p1 = z1; q0 = w0; q1 = w1;
+                    } else {
+                        p0 = z0 + beta * p[c];
+                        q0 = w0 + beta * ap[c];
+                        p1 = two ? z1 + beta * p[c2] : 0.0;
+                        q1 = two ? w1 + beta * ap[c2] : 0.0;
+                    }
+                    p[c] = p0; ap[c] = q0;
+                    s3[0] += q0 * p0;
+                    if (two) {
+                        p[c2] = p1; ap[c2] = q1;
+                        s3[0] += q1 * p1;
+                    }
+                }
+                block_sums<1>(a.partial, set, s3);
+                if (!grid_barrier(st, epoch)) { aborted = true; break; }
+                double g3[1];
+                grid_sums<1>(a.partial, set, g3);
+                set ^= 1;
+                const double wApA = g3[0];
+                if (fabs(wApA) / normf < 1e-300) break;   // checkSingularity
+                const double alpha = wArA / wApA;
+                // --- update pass: x, r, z; |r| and z.r
+                double s4[2] = {0.0, 0.0};
+                for (unsigned c = first; c < n; c += 2 * stride) {
+                    const unsigned c2 = c + stride;
+                    const bool two = c2 < n;
+                    const double x0 = x[c] + alpha * p[c];
+                    const double r0 = r[c] - alpha * ap[c];
+                    const double z0 = rdiag[c] * r0;
+                    x[c] = x0; r[c] = r0;
+                    __stcg(&z[c], z0);
+                    s4[0] += fabs(r0);
+                    s4[1] += z0 * r0;
+                    if (two) {
+                        const double x1 = x[c2] + alpha * p[c2];
+                        const double r1 = r[c2] - alpha * ap[c2];
+                        const double z1 = rdiag[c2] * r1;
+                        x[c2] = x1; r[c2] = r1;
+                        __stcg(&z[c2], z1);
+                        s4[0] += fabs(r1);
+                        s4[1] += z1 * r1;
+                    }
+                }
+                block_sums<2>(a.partial, set, s4);
+                if (!grid_barrier(st, epoch)) { aborted = true; break; }
+                double g4[2];
+                grid_sums<2>(a.partial, set, g4);
+                set ^= 1;
+                res = g4[0] / normf;
+                ++iter;
+                ++step_iters;
+                if (conv(res) || iter >= max_iter) {
+                    if (!conv(res)) status |= CFG_ERR_PCG;
+                    break;
+                }
+                if (step_iters >= a.iter_cap) {
+                    // guard of the in-kernel loops: give up the step
+                    status |= CFG_ERR_PCG;
+                    aborted = true;
+                    break;
+                }
+                const double wArAold = wArA;
+                wArA = g4[1];
+                beta = wArA / wArAold;
+            }
+        }
+        if (lead && n_solves < kMaxSolves) {
+            st->iters[n_solves] = iter;
+            st->init_r[n_solves] = init_res;
+            st->final_r[n_solves] = res;
+        }
+        ++n_solves;
+        last_init = init_res; last_res = res; last_iter = iter; last_v = v;
+        if (aborted) { abort_step = true; break; }
+        // pimpleLoop: the corrector after a converged one is the last
+        if (converged_outer || corr + 1 > n_outer) break;
+        if (init_res < outer_tol) converged_outer = true;
+        // the next corrector reads other blocks' rows of x only through
+        // amul_cg (L2), after the last barrier of this one
+    }
+    // --- activation time (MyocardiumDomain::updateActivationTime)
+    if (abort_step) status |= CFG_ERR_PCG;
+    else
+        for (unsigned c = first; c < n; c += stride)
+            activation(a, c, x[c], a.vm_old[c], t_step - a.dt);
+    if (lead) {
+        st->n_old = n_old;
+        st->n_solves = n_solves;
+        st->iter = last_iter;
+        st->init_res = last_init;
+        st->res = last_res;
+        st->variant = last_v;
+        st->step_iters = step_iters;
+        st->corr = n_solves + 1;
+        st->solve_active = 0;
+        st->outer_active = 0;
+        st->converged_outer = converged_outer ? 1 : 0;
+    }
+    if (status && threadIdx.x == 0) atomicOr(&st->status, status);
+}
+
+// Host helpers: fast-division constants and the cooperative launch.
+static FastDiv make_fastdiv(unsigned d)
+{
+    unsigned s = 0;
+    while ((1ull << s) < d) ++s;
+    const unsigned long long m = ((1ull << 32) * ((1ull << s) - d)) / d + 1;
+    return FastDiv{unsigned(m), s};
+}
+
+int coop_grid_blocks(long long n)
+{
+    int dev = 0, sms = 0, per_sm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_implicit_coop, kCoopBlock, 0) !=
+        cudaSuccess)
+        return 0;
+    long long want = (n + kCoopBlock - 1) / kCoopBlock;
+    long long cap = (long long)sms * per_sm;
+    return int(want < cap ? want : cap);
+}
+
+cudaError_t launch_implicit_coop(const DiffusionArgs& a, int blocks, cudaStream_t s)
+{
+    CoopArgs ca{};
+    if (a.sx) {
+        ca.div_nx = make_fastdiv(unsigned(a.sx));
+        ca.div_ny = make_fastdiv(unsigned(a.sy));
+    }
+    DiffusionArgs args = a;
+    void* params[] = {&args, &ca};
+    return cudaLaunchCooperativeKernel(reinterpret_cast<void*>(k_implicit_coop), dim3(blocks),
+                                       dim3(kCoopBlock), params, 0, s);
+}
+
+}  // namespace cfg

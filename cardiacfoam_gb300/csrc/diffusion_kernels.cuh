@@ -44,6 +44,9 @@ struct PcgState {
     double sum_x, avg, sum_absr, normf, init_res, res, wArA, wArAold, wApA, alpha, beta;
     double t, t0;         // runTime value and step start
     unsigned int arrive[4];
+    // grid barrier of the persistent diffusion kernel (reset every step)
+    unsigned int bar_count;
+    int bar_abort;
     // --- statistics of the last step
     int iters[kMaxSolves];
     double init_r[kMaxSolves], final_r[kMaxSolves];
@@ -238,6 +241,17 @@ __device__ __forceinline__ void set_inner(const DiffusionArgs& a, int v)
 __device__ __forceinline__ void set_outer(const DiffusionArgs& a, int v)
 {
     if (a.use_graph) cudaGraphSetConditional(a.h_outer, unsigned(v));
+}
+
+// MyocardiumDomain::updateActivationTime (myocardiumDomain.C:345-374)
+__device__ __forceinline__ void activation(const DiffusionArgs& a, long long c, double vnew,
+                                           double vold, double old_time)
+{
+    if (a.act_flag[c] && vnew > 1e-15) {
+        a.act_flag[c] = 0;
+        const double w = (0.0 - vold) / (vnew - vold);
+        a.act[c] = old_time + w * a.dt;
+    }
 }
 
 __device__ __forceinline__ bool pcg_converged(const PcgState* st, double r)

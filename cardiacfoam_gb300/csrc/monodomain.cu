@@ -283,6 +283,16 @@ int monodomain_create(const cfg_monodomain_desc* d, const cfg_mesh_desc* m, cfg_
     st.outer_tol = d->outer_tol;
     if (!e) e = cudaMemcpy(md->d_st, &st, sizeof st, cudaMemcpyHostToDevice);
     if (e) return bail(fail(CFG_ERR_CUDA, "device initialisation failed: %s", cudaGetErrorString(e)));
+    // persistent diffusion kernel: grid of co-resident blocks, if the device
+    // supports cooperative launches
+    {
+        int dev = 0, coop = 0;
+        if (cudaGetDevice(&dev) == cudaSuccess &&
+            cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) == cudaSuccess && coop)
+            md->coop_blocks = coop_grid_blocks(n);
+        md->persistent = md->coop_blocks > 0;
+        cudaGetLastError();
+    }
     *out = md;
     return CFG_OK;
 }
@@ -328,6 +338,12 @@ int enqueue_step(cfg_monodomain* md, double dt, bool host_control)
         k_explicit_finish<<<1, 1, 0, s>>>(md->d_st, md->ddt_backward);
         launches += 2;
         CFG_CUDA_TRY(cudaGetLastError());
+        if (md->timing) CFG_CUDA_TRY(cudaEventRecord(md->ev[2], s));
+        return CFG_OK;
+    }
+    if (md->persistent) {
+        CFG_CUDA_TRY(launch_implicit_coop(a, md->coop_blocks, s));
+        launches += 1;
         if (md->timing) CFG_CUDA_TRY(cudaEventRecord(md->ev[2], s));
         return CFG_OK;
     }
@@ -381,6 +397,8 @@ int check_step(cfg_monodomain* md)
         md->timed_steps++;
     }
     if ((rc = ionic_check_status(md->ion))) return rc;
+    if (md->h_st->bar_abort)
+        return fail(CFG_ERR_PCG, "diffusion kernel aborted: a grid barrier timed out");
     if (md->implicit && (md->h_st->outer_active || md->h_st->solve_active))
         return fail(CFG_ERR_PCG, "PIMPLE/PCG loop did not finish within the launched sequence");
     return CFG_OK;
@@ -410,7 +428,8 @@ static int enqueue_graph_step(cfg_monodomain* md, double dt)
         CFG_CUDA_TRY(cudaGetLastError());
         md->prepared_dt = dt;
     }
-    if (!md->graph_exec || md->graph_dt != dt || md->graph_timing != md->timing) {
+    if (!md->graph_exec || md->graph_dt != dt || md->graph_timing != md->timing ||
+        md->graph_persistent != md->persistent) {
         int rc = build_step_graph(md, dt);
         if (rc) return rc;
     }
@@ -422,6 +441,7 @@ static int enqueue_graph_step(cfg_monodomain* md, double dt)
 static long long graph_step_launches(const cfg_monodomain* md)
 {
     if (!md->implicit) return 4;
+    if (md->persistent) return 3;   // step_begin, ionic, persistent diffusion
     long long n = 3;   // step_begin, ionic, activation
     for (int k = 0; k < md->h_st->n_solves && k < kMaxSolves; ++k)
         n += 3 + 2LL * md->h_st->iters[k];
@@ -465,6 +485,15 @@ int cfg_monodomain_set_graph(cfg_monodomain* md, int enable)
 {
     if (!md) return fail(CFG_ERR_INVALID, "null context");
     md->use_graph = enable != 0;
+    return CFG_OK;
+}
+
+int cfg_monodomain_set_persistent(cfg_monodomain* md, int enable)
+{
+    if (!md) return fail(CFG_ERR_INVALID, "null context");
+    if (enable && md->coop_blocks <= 0)
+        return fail(CFG_ERR_UNSUPPORTED, "cooperative launch is not available on this device");
+    md->persistent = enable != 0;
     return CFG_OK;
 }
 

@@ -51,6 +51,11 @@ struct cfg_monodomain {
     double graph_dt = 0.0;
     bool graph_timing = false;
     bool use_graph = true;
+    // implicit diffusion as one persistent cooperative kernel per step
+    // (cooperative launch needed; otherwise the per-kernel sequence)
+    bool persistent = true;
+    int coop_blocks = 0;
+    bool graph_persistent = false;
     long long iter_cap = 100000;   // PCG iterations per step before the step aborts
     double t_host = 0.0;
     long long steps = 0;
@@ -68,4 +73,6 @@ int enqueue_step(cfg_monodomain* md, double dt, bool host_control);
 int check_step(cfg_monodomain* md);
 int build_step_graph(cfg_monodomain* md, double dt);
 void fill_args_public(cfg_monodomain* md, double dt);
+int coop_grid_blocks(long long n);
+cudaError_t launch_implicit_coop(const DiffusionArgs& a, int blocks, cudaStream_t s);
 }  // namespace cfg

@@ -77,12 +77,52 @@ cudaError_t capture_ionic(cfg_monodomain* md, double dt, cudaGraph_t* out)
         }                                                                                     \
     } while (0)
 
+// Step graph of the persistent form, captured from the stream:
+//   k_step_begin -> ionic step -> persistent implicit diffusion
+// (the corrector and PCG loops run inside the last kernel).  The timing
+// events are recorded as external event nodes, so the host can read them.
+static int build_persistent_graph(cfg_monodomain* md, double dt)
+{
+    fill_args_public(md, dt);
+    DiffusionArgs a = md->args;
+    cudaStream_t s = md->stream;
+    cudaGraph_t g = nullptr;
+    CFG_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    cudaError_t le = cudaSuccess;
+    k_step_begin<<<unsigned(a.nblocks), kDiffBlock, 0, s>>>(a);
+    le = cudaGetLastError();
+    if (!le && md->timing) le = cudaEventRecordWithFlags(md->ev[0], s, cudaEventRecordExternal);
+    if (!le) {
+        IonicLaunch L = ionic_launch_args(md->ion, 0.0, dt, &md->d_st->t0, md->d_vm, md->d_iion);
+        le = ionic_enqueue(md->ion, L);
+    }
+    if (!le && md->timing) le = cudaEventRecordWithFlags(md->ev[1], s, cudaEventRecordExternal);
+    if (!le) le = launch_implicit_coop(a, md->coop_blocks, s);
+    if (!le && md->timing) le = cudaEventRecordWithFlags(md->ev[2], s, cudaEventRecordExternal);
+    const cudaError_t ce = cudaStreamEndCapture(s, &g);
+    if (le || ce) {
+        if (g) cudaGraphDestroy(g);
+        return fail(CFG_ERR_CUDA, "step graph capture failed: %s",
+                    cudaGetErrorString(le ? le : ce));
+    }
+    cudaGraphExec_t exec = nullptr;
+    const cudaError_t ie = cudaGraphInstantiate(&exec, g, 0);
+    cudaGraphDestroy(g);
+    if (ie) return fail(CFG_ERR_CUDA, "step graph instantiation failed: %s", cudaGetErrorString(ie));
+    md->graph_exec = exec;
+    md->graph_dt = dt;
+    md->graph_timing = md->timing;
+    md->graph_persistent = true;
+    return CFG_OK;
+}
+
 int build_step_graph(cfg_monodomain* md, double dt)
 {
     if (md->graph_exec) {
         cudaGraphExecDestroy(md->graph_exec);
         md->graph_exec = nullptr;
     }
+    if (md->implicit && md->persistent) return build_persistent_graph(md, dt);
     fill_args_public(md, dt);
     DiffusionArgs a = md->args;
     a.use_graph = 1;
@@ -165,6 +205,7 @@ int build_step_graph(cfg_monodomain* md, double dt)
     md->graph_exec = exec;
     md->graph_dt = dt;
     md->graph_timing = timing;
+    md->graph_persistent = md->persistent;
     return CFG_OK;
 }
 

@@ -105,6 +105,7 @@ EXPORTS = [
     "cfg_monodomain_set_field", "cfg_monodomain_time", "cfg_monodomain_ionic",
     "cfg_monodomain_last_stats", "cfg_monodomain_set_timing", "cfg_monodomain_timings",
     "cfg_monodomain_stream", "cfg_monodomain_destroy", "cfg_box_diffusion_solve_noalloc",
+    "cfg_monodomain_set_persistent",
 ]
 
 _lib = None
@@ -152,6 +153,7 @@ def load(path: Optional[os.PathLike] = None):
     L.cfg_monodomain_stream.argtypes = [C.c_void_p]
     L.cfg_monodomain_stream.restype = C.c_void_p
     L.cfg_monodomain_destroy.argtypes = [C.c_void_p]
+    L.cfg_monodomain_set_persistent.argtypes = [C.c_void_p, C.c_int]
     L.cfg_box_diffusion_solve_noalloc.argtypes = [C.POINTER(BoxDiffusionDesc), C.c_double,
                                                   C.c_void_p, C.c_void_p, C.c_void_p,
                                                   C.c_void_p, C.c_void_p,

@@ -207,6 +207,13 @@ int cfg_monodomain_last_stats(const cfg_monodomain* md, cfg_step_stats* stats);
 int cfg_monodomain_set_timing(cfg_monodomain* md, int enable);
 int cfg_monodomain_timings(const cfg_monodomain* md, double* ionic_ms, double* diffusion_ms,
                            long long* steps, long long* kernel_launches);
+/* Implicit diffusion as one persistent cooperative kernel per step (all
+ * PIMPLE correctors and PCG iterations inside one launch; the default where
+ * the device supports cooperative launches), or as a kernel sequence per
+ * iteration (enable = 0).  Same numerics up to the order of the reduction
+ * sums.  MonodomainSolver::solveDiffusionImplicit (monodomainSolver.C:112-150)
+ * is what either form computes. */
+int cfg_monodomain_set_persistent(cfg_monodomain* md, int enable);
 /* The CUDA stream (cudaStream_t) all work of the context is enqueued on. */
 void* cfg_monodomain_stream(cfg_monodomain* md);
 int cfg_monodomain_destroy(cfg_monodomain* md);

@@ -150,3 +150,28 @@ def test_step_graph_equals_host_control(gpu_lib, implicit):
     if implicit:
         assert np.array_equal(s0[2], s1[2]) and np.array_equal(s0[2], s2[2])
     assert t0 == t1 == t2
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("stencil", [True, False], ids=["stencil", "ell"])
+def test_persistent_diffusion_equals_kernel_sequence(gpu_lib, stencil):
+    """One persistent cooperative kernel per step (all correctors and PCG
+    iterations in one launch) against the kernel sequence per iteration:
+    the same solve up to the order of the reduction sums."""
+    dt, nsteps = 1e-5, 150
+    mesh = box_mesh(20, 7, 3, 0.02, 0.007, 0.003)
+    runs = []
+    for persistent in (True, False):
+        m = api.Monodomain(mesh, "TNNP", "epicardialCells", SIGMA, dt=dt, boxes=BOX,
+                           stencil=stencil)
+        m.set_persistent(persistent)
+        iters = 0
+        for _ in range(nsteps):
+            m.step(dt)
+            iters += int(np.sum(m.stats()[2]))
+        runs.append((m.vm(), m.activation(), iters))
+    (v0, a0, i0), (v1, a1, i1) = runs
+    assert np.max(np.abs(v0 - v1)) <= 1e-7 * np.max(np.abs(v1))
+    assert np.array_equal(a0 > 0, a1 > 0)
+    assert np.max(np.abs(a0 - a1)) <= 1e-8
+    assert abs(i0 - i1) <= max(2, nsteps // 50)
