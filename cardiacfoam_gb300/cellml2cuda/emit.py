@@ -27,7 +27,7 @@ import re
 from typing import Dict, List
 
 from .cexpr import Bin, Call, Cond, Node, Num, Ref, Unary, Var
-from .model import Assign, Fatal, If, Model, iter_assigns, use_before_def
+from .model import Assign, Fatal, If, Model, iter_assigns, refs, use_before_def
 
 # states stored and accumulated in double precision in the mixed form: the
 # membrane potential and every ion concentration / CaMK occupancy (slow states
@@ -56,6 +56,40 @@ SCALABLE = {
     "BuenoOrovio": {},
 }
 SCALE_ORDER = ["GNa", "GCaL", "GKr", "GKs", "GK1", "Gto"]
+
+# intracellular calcium state of each model (peak Ca of a beat)
+CALCIUM_STATE = {"TNNP": "Ca_i", "ORd": "Ca_i", "ToRORd_dynCl": "Cai"}
+
+
+def scale_dependent_constants(m: "Model") -> List[str]:
+    """Constants whose value depends on a per-cell scale (the scaled ones and
+    every constant initConsts computes from them) and that the right-hand
+    side or the current evaluation reads, in constant-index order."""
+    dep = set(SCALABLE[m.name].values())
+    changed = True
+    while changed:
+        changed = False
+        for st in iter_assigns(m.init):
+            t = st.target
+            if t.array == "CONSTANTS" and t.name not in dep and any(
+                    r.array == "CONSTANTS" and r.name in dep for r in refs(st.expr)):
+                dep.add(t.name)
+                changed = True
+    used = set()
+
+    def visit(body):
+        for st in body:
+            exprs = [st.expr] if isinstance(st, Assign) else \
+                [st.cond] if isinstance(st, If) else []
+            for e in exprs:
+                used.update(r.name for r in refs(e) if r.array == "CONSTANTS")
+            if isinstance(st, If):
+                visit(st.then)
+                visit(st.orelse)
+
+    visit(m.rates)
+    visit(m.variables)
+    return [c for c in m.constants if c in dep and c in used]
 
 # Constants a model's right-hand side reads but its initConsts never assigns.
 # The reference zero-fills CONSTANTS, so ORd_2011.H evaluates the Na/K pump
@@ -181,6 +215,7 @@ class _CudaPrinter(_Printer):
         self.early = set(early)
         self.mode = mode            # "init" | "rhs"
         self.defined = set()
+        self.states_read = set()    # states the body reads (loaded once, up front)
 
     def num(self, n: Num) -> str:
         if n.is_int_literal:
@@ -191,7 +226,10 @@ class _CudaPrinter(_Printer):
 
     def ref(self, r: Ref) -> str:
         if r.array == "STATES":
-            return f"y[S_{r.name}]" if self.mode == "init" else f"Y(S_{r.name})"
+            if self.mode == "init":
+                return f"y[S_{r.name}]"
+            self.states_read.add(r.name)
+            return f"y_{r.name}"
         if r.array == "CONSTANTS":
             return f"C[C_{r.name}]" if self.mode == "init" else f"K(C_{r.name})"
         if r.array == "ALGEBRAIC":
@@ -263,6 +301,14 @@ def _cuda_body(m: Model, stmts, pr: _CudaPrinter, indent: str, out: List[str]):
             out.append(f"{indent}}}")
         elif isinstance(st, Fatal):
             out.append(f"{indent}/* unsupported configuration in the reference */")
+
+
+def _state_loads(m: Model, pr: "_CudaPrinter") -> List[str]:
+    """Every state the body reads, loaded once before any derivative is
+    written: the stores to dydt then cannot force reloads (the compiler must
+    assume dydt may alias the state array), and the loads can be scheduled
+    early."""
+    return [f"    const R y_{s} = Y(S_{s});" for s in m.states if s in pr.states_read]
 
 
 def _predeclare_conditional_algebraics(m: Model, stmts, out, indent):
@@ -345,6 +391,33 @@ def emit_cuda(m: Model, src_rel: str) -> str:
     for k in SCALE_ORDER:
         L.append(f"constexpr int SCALE_{k} = {SCALE_ORDER.index(k) if k in sc else -1};")
     L.append("")
+    # constants that depend on the scales
+    sd = scale_dependent_constants(m)
+    L.append("// Constants that depend on the per-cell conductance scales and that the")
+    L.append("// right-hand side reads: the scaled conductances and every constant")
+    L.append("// initConsts derives from them.  sd_slot(i) is constant i's index in a")
+    L.append("// cell's vector of them, or -1 (then the constant is the tissue's).")
+    L.append(f"constexpr int NSD = {len(sd)};")
+    L.append("CFG_HD constexpr int sd_const(int k)")
+    L.append("{")
+    L.append("    switch (k) {")
+    for k, c in enumerate(sd):
+        L.append(f"    case {k}: return C_{c};")
+    L.append("    default: return -1;")
+    L.append("    }")
+    L.append("}")
+    L.append("CFG_HD constexpr int sd_slot(int i)")
+    L.append("{")
+    L.append("    switch (i) {")
+    for k, c in enumerate(sd):
+        L.append(f"    case C_{c}: return {k};")
+    L.append("    default: return -1;")
+    L.append("    }")
+    L.append("}")
+    ca = CALCIUM_STATE.get(m.name)
+    L.append("// intracellular calcium state (peak Ca of a beat), or -1")
+    L.append(f"constexpr int CA_STATE = {('S_' + ca) if ca else -1};")
+    L.append("")
     # init
     L.append("// Constants and initial states (initConsts).  `scale` may be null;")
     L.append("// otherwise scale[SCALE_x] multiplies the named conductance right after")
@@ -391,7 +464,8 @@ def emit_cuda(m: Model, src_rel: str) -> str:
     early = use_before_def(m.rates)
     L.append("// Right-hand side as used by derivatives(): dydt for every state that the")
     L.append("// reference assigns (RATES of V only when SOLVE_VM).  Returns Iion.")
-    L.append("// Y(i) reads state i as R, K(i) reads constant i as R.")
+    L.append("// Y(i) reads state i as R (each state once, before any dydt store),")
+    L.append("// K(i) reads constant i as R.")
     L.append("template <class R, bool SOLVE_VM, class YS, class KS>")
     L.append("__device__ __forceinline__ R rhs(double t, const YS& Y, const KS& K, R* dydt, "
              "int tissue, const CfgStimulus& stim)")
@@ -403,6 +477,7 @@ def emit_cuda(m: Model, src_rel: str) -> str:
         body.append(f"    R a_{name} = R(0);")
         pr.defined.add(name)
     _cuda_body(m, m.rates, pr, "    ", body)
+    L.extend(_state_loads(m, pr))
     L.extend(body)
     L.append(f"    return a_{m.iion_name};")
     L.append("}")
@@ -421,6 +496,7 @@ def emit_cuda(m: Model, src_rel: str) -> str:
         body.append(f"    R a_{name} = R(0);")
         pr.defined.add(name)
     _cuda_body(m, m.variables, pr, "    ", body)
+    L.extend(_state_loads(m, pr))
     L.extend(body)
     L.append("    (void)dydt;")
     L.append(f"    return a_{m.iion_name};")
@@ -437,6 +513,9 @@ def emit_cuda(m: Model, src_rel: str) -> str:
              "const double* scale) { init_consts(C, y, tissue, scale); }")
     L.append("    template <int T> CFG_HD static constexpr double constant(int i) "
              "{ return cval<T>(i); }")
+    L.append("    static constexpr int NSD = " + ns + "::NSD, CA_STATE = " + ns + "::CA_STATE;")
+    L.append("    CFG_HD static constexpr int sd_slot(int i) { return " + ns + "::sd_slot(i); }")
+    L.append("    CFG_HD static constexpr int sd_const(int k) { return " + ns + "::sd_const(k); }")
     L.append("    template <class R, bool SV, class YS, class KS>")
     L.append("    __device__ static __forceinline__ R rates(double t, const YS& Y, const KS& K, "
              "R* dydt, int tissue, const CfgStimulus& st) { return rhs<R, SV>(t, Y, K, dydt, "

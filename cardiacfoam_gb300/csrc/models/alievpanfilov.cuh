@@ -30,6 +30,26 @@ constexpr int SCALE_GKs = -1;
 constexpr int SCALE_GK1 = -1;
 constexpr int SCALE_Gto = -1;
 
+// Constants that depend on the per-cell conductance scales and that the
+// right-hand side reads: the scaled conductances and every constant
+// initConsts derives from them.  sd_slot(i) is constant i's index in a
+// cell's vector of them, or -1 (then the constant is the tissue's).
+constexpr int NSD = 0;
+CFG_HD constexpr int sd_const(int k)
+{
+    switch (k) {
+    default: return -1;
+    }
+}
+CFG_HD constexpr int sd_slot(int i)
+{
+    switch (i) {
+    default: return -1;
+    }
+}
+// intracellular calcium state (peak Ca of a beat), or -1
+constexpr int CA_STATE = -1;
+
 // Constants and initial states (initConsts).  `scale` may be null;
 // otherwise scale[SCALE_x] multiplies the named conductance right after
 // it is assigned, before constants derived from it are computed.
@@ -70,14 +90,17 @@ template <> CFG_HD constexpr double cval<4>(int i)
 
 // Right-hand side as used by derivatives(): dydt for every state that the
 // reference assigns (RATES of V only when SOLVE_VM).  Returns Iion.
-// Y(i) reads state i as R, K(i) reads constant i as R.
+// Y(i) reads state i as R (each state once, before any dydt store),
+// K(i) reads constant i as R.
 template <class R, bool SOLVE_VM, class YS, class KS>
 __device__ __forceinline__ R rhs(double t, const YS& Y, const KS& K, R* dydt, int tissue, const CfgStimulus& stim)
 {
     (void)tissue; (void)stim; (void)t;
-    R a_AV_eps = (K(C_AC_epsilon) + ((K(C_AC_mu1) * Y(S_recovery_r)) / (K(C_AC_mu2) + Y(S_u))));
-    dydt[S_recovery_r] = (a_AV_eps * ((-Y(S_recovery_r)) - ((K(C_AC_k) * Y(S_u)) * (Y(S_u) - (K(C_AC_a) + R(1.0))))));
-    R a_Iion_cm = ((((K(C_AC_k) * Y(S_u)) * (Y(S_u) - K(C_AC_a))) * (Y(S_u) - R(1.0))) + (Y(S_recovery_r) * Y(S_u)));
+    const R y_u = Y(S_u);
+    const R y_recovery_r = Y(S_recovery_r);
+    R a_AV_eps = (K(C_AC_epsilon) + ((K(C_AC_mu1) * y_recovery_r) / (K(C_AC_mu2) + y_u)));
+    dydt[S_recovery_r] = (a_AV_eps * ((-y_recovery_r) - ((K(C_AC_k) * y_u) * (y_u - (K(C_AC_a) + R(1.0))))));
+    R a_Iion_cm = ((((K(C_AC_k) * y_u) * (y_u - K(C_AC_a))) * (y_u - R(1.0))) + (y_recovery_r * y_u));
     R a_Istim = (SOLVE_VM ? R(cfg_stimulus_current<double>(t, stim)) : R(0));
     if (SOLVE_VM) {
         dydt[S_u] = ((-a_Iion_cm) - a_Istim);
@@ -91,9 +114,11 @@ __device__ __forceinline__ R iion(double t, const YS& Y, const KS& K, int tissue
 {
     (void)tissue; (void)stim; (void)t;
     R dydt[NS];
-    R a_AV_eps = (K(C_AC_epsilon) + ((K(C_AC_mu1) * Y(S_recovery_r)) / (K(C_AC_mu2) + Y(S_u))));
-    dydt[S_recovery_r] = (a_AV_eps * ((-Y(S_recovery_r)) - ((K(C_AC_k) * Y(S_u)) * (Y(S_u) - (K(C_AC_a) + R(1.0))))));
-    R a_Iion_cm = ((((K(C_AC_k) * Y(S_u)) * (Y(S_u) - K(C_AC_a))) * (Y(S_u) - R(1.0))) + (Y(S_recovery_r) * Y(S_u)));
+    const R y_u = Y(S_u);
+    const R y_recovery_r = Y(S_recovery_r);
+    R a_AV_eps = (K(C_AC_epsilon) + ((K(C_AC_mu1) * y_recovery_r) / (K(C_AC_mu2) + y_u)));
+    dydt[S_recovery_r] = (a_AV_eps * ((-y_recovery_r) - ((K(C_AC_k) * y_u) * (y_u - (K(C_AC_a) + R(1.0))))));
+    R a_Iion_cm = ((((K(C_AC_k) * y_u) * (y_u - K(C_AC_a))) * (y_u - R(1.0))) + (y_recovery_r * y_u));
     R a_Istim = (SOLVE_VM ? R(cfg_stimulus_current<double>(t, stim)) : R(0));
     if (SOLVE_VM) {
         dydt[S_u] = ((-a_Iion_cm) - a_Istim);
@@ -111,6 +136,9 @@ struct Model {
     static constexpr int VM_MAP = alievpanfilov::VM_MAP;
     CFG_HD static __forceinline__ void init(double* C, double* y, int tissue, const double* scale) { init_consts(C, y, tissue, scale); }
     template <int T> CFG_HD static constexpr double constant(int i) { return cval<T>(i); }
+    static constexpr int NSD = alievpanfilov::NSD, CA_STATE = alievpanfilov::CA_STATE;
+    CFG_HD static constexpr int sd_slot(int i) { return alievpanfilov::sd_slot(i); }
+    CFG_HD static constexpr int sd_const(int k) { return alievpanfilov::sd_const(k); }
     template <class R, bool SV, class YS, class KS>
     __device__ static __forceinline__ R rates(double t, const YS& Y, const KS& K, R* dydt, int tissue, const CfgStimulus& st) { return rhs<R, SV>(t, Y, K, dydt, tissue, st); }
     template <class R, bool SV, class YS, class KS>

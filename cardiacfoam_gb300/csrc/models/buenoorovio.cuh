@@ -30,6 +30,26 @@ constexpr int SCALE_GKs = -1;
 constexpr int SCALE_GK1 = -1;
 constexpr int SCALE_Gto = -1;
 
+// Constants that depend on the per-cell conductance scales and that the
+// right-hand side reads: the scaled conductances and every constant
+// initConsts derives from them.  sd_slot(i) is constant i's index in a
+// cell's vector of them, or -1 (then the constant is the tissue's).
+constexpr int NSD = 0;
+CFG_HD constexpr int sd_const(int k)
+{
+    switch (k) {
+    default: return -1;
+    }
+}
+CFG_HD constexpr int sd_slot(int i)
+{
+    switch (i) {
+    default: return -1;
+    }
+}
+// intracellular calcium state (peak Ca of a beat), or -1
+constexpr int CA_STATE = -1;
+
 // Constants and initial states (initConsts).  `scale` may be null;
 // otherwise scale[SCALE_x] multiplies the named conductance right after
 // it is assigned, before constants derived from it are computed.
@@ -180,25 +200,30 @@ template <> CFG_HD constexpr double cval<1>(int i)
 
 // Right-hand side as used by derivatives(): dydt for every state that the
 // reference assigns (RATES of V only when SOLVE_VM).  Returns Iion.
-// Y(i) reads state i as R, K(i) reads constant i as R.
+// Y(i) reads state i as R (each state once, before any dydt store),
+// K(i) reads constant i as R.
 template <class R, bool SOLVE_VM, class YS, class KS>
 __device__ __forceinline__ R rhs(double t, const YS& Y, const KS& K, R* dydt, int tissue, const CfgStimulus& stim)
 {
     (void)tissue; (void)stim; (void)t;
-    R a_tauSo = (K(C_tauSo1) + (((K(C_tauSo2) - K(C_tauSo1)) * (R(1.0) + cfg_tanh((K(C_kSo) * (Y(S_u) - K(C_uSo)))))) / R(2.0)));
-    R a_tauO = (((R(1.0) - (((Y(S_u) - K(C_thetaO))) > R(0) ? 1 : 0)) * K(C_tauO1)) + ((((Y(S_u) - K(C_thetaO))) > R(0) ? 1 : 0) * K(C_tauO2)));
-    R a_Jfi = (((((-Y(S_v)) * (((Y(S_u) - K(C_thetaV))) > R(0) ? 1 : 0)) * (Y(S_u) - K(C_thetaV))) * (K(C_uU) - Y(S_u))) / K(C_tauFi));
-    R a_Jso = ((((Y(S_u) - K(C_uO)) * (R(1.0) - (((Y(S_u) - K(C_thetaW))) > R(0) ? 1 : 0))) / a_tauO) + ((((Y(S_u) - K(C_thetaW))) > R(0) ? 1 : 0) / a_tauSo));
-    R a_Jsi = ((((-(((Y(S_u) - K(C_thetaW))) > R(0) ? 1 : 0)) * Y(S_w)) * Y(S_s)) / K(C_tauSi));
+    const R y_u = Y(S_u);
+    const R y_v = Y(S_v);
+    const R y_w = Y(S_w);
+    const R y_s = Y(S_s);
+    R a_tauSo = (K(C_tauSo1) + (((K(C_tauSo2) - K(C_tauSo1)) * (R(1.0) + cfg_tanh((K(C_kSo) * (y_u - K(C_uSo)))))) / R(2.0)));
+    R a_tauO = (((R(1.0) - (((y_u - K(C_thetaO))) > R(0) ? 1 : 0)) * K(C_tauO1)) + ((((y_u - K(C_thetaO))) > R(0) ? 1 : 0) * K(C_tauO2)));
+    R a_Jfi = (((((-y_v) * (((y_u - K(C_thetaV))) > R(0) ? 1 : 0)) * (y_u - K(C_thetaV))) * (K(C_uU) - y_u)) / K(C_tauFi));
+    R a_Jso = ((((y_u - K(C_uO)) * (R(1.0) - (((y_u - K(C_thetaW))) > R(0) ? 1 : 0))) / a_tauO) + ((((y_u - K(C_thetaW))) > R(0) ? 1 : 0) / a_tauSo));
+    R a_Jsi = ((((-(((y_u - K(C_thetaW))) > R(0) ? 1 : 0)) * y_w) * y_s) / K(C_tauSi));
     R a_Jion = ((a_Jfi + a_Jso) + a_Jsi);
-    R a_tauVMinus = (((R(1.0) - (((Y(S_u) - K(C_thetaVMinus))) > R(0) ? 1 : 0)) * K(C_tauV1Minus)) + ((((Y(S_u) - K(C_thetaVMinus))) > R(0) ? 1 : 0) * K(C_tauV2Minus)));
-    R a_tauWMinus = (K(C_tauW1Minus) + (((K(C_tauW2Minus) - K(C_tauW1Minus)) * (R(1.0) + cfg_tanh((K(C_kWMinus) * (Y(S_u) - K(C_uWMinus)))))) / R(2.0)));
-    R a_tauS = (((R(1.0) - (((Y(S_u) - K(C_thetaW))) > R(0) ? 1 : 0)) * K(C_tauS1)) + ((((Y(S_u) - K(C_thetaW))) > R(0) ? 1 : 0) * K(C_tauS2)));
-    R a_vInfty = (((K(C_thetaVMinus) - Y(S_u))) > R(0) ? 1 : 0);
-    R a_wInfty = (((R(1.0) - (((Y(S_u) - K(C_thetaO))) > R(0) ? 1 : 0)) * (R(1.0) - (Y(S_u) / K(C_tauWInfty)))) + ((((Y(S_u) - K(C_thetaO))) > R(0) ? 1 : 0) * K(C_wInftyStar)));
-    dydt[S_v] = ((((R(1.0) - (((Y(S_u) - K(C_thetaV))) > R(0) ? 1 : 0)) * (a_vInfty - Y(S_v))) / a_tauVMinus) - (((((Y(S_u) - K(C_thetaV))) > R(0) ? 1 : 0) * Y(S_v)) / K(C_tauVPlus)));
-    dydt[S_w] = ((((R(1.0) - (((Y(S_u) - K(C_thetaW))) > R(0) ? 1 : 0)) * (a_wInfty - Y(S_w))) / a_tauWMinus) - (((((Y(S_u) - K(C_thetaW))) > R(0) ? 1 : 0) * Y(S_w)) / K(C_tauWPlus)));
-    dydt[S_s] = ((((R(1.0) + cfg_tanh((K(C_kS) * (Y(S_u) - K(C_uS))))) / R(2.0)) - Y(S_s)) / a_tauS);
+    R a_tauVMinus = (((R(1.0) - (((y_u - K(C_thetaVMinus))) > R(0) ? 1 : 0)) * K(C_tauV1Minus)) + ((((y_u - K(C_thetaVMinus))) > R(0) ? 1 : 0) * K(C_tauV2Minus)));
+    R a_tauWMinus = (K(C_tauW1Minus) + (((K(C_tauW2Minus) - K(C_tauW1Minus)) * (R(1.0) + cfg_tanh((K(C_kWMinus) * (y_u - K(C_uWMinus)))))) / R(2.0)));
+    R a_tauS = (((R(1.0) - (((y_u - K(C_thetaW))) > R(0) ? 1 : 0)) * K(C_tauS1)) + ((((y_u - K(C_thetaW))) > R(0) ? 1 : 0) * K(C_tauS2)));
+    R a_vInfty = (((K(C_thetaVMinus) - y_u)) > R(0) ? 1 : 0);
+    R a_wInfty = (((R(1.0) - (((y_u - K(C_thetaO))) > R(0) ? 1 : 0)) * (R(1.0) - (y_u / K(C_tauWInfty)))) + ((((y_u - K(C_thetaO))) > R(0) ? 1 : 0) * K(C_wInftyStar)));
+    dydt[S_v] = ((((R(1.0) - (((y_u - K(C_thetaV))) > R(0) ? 1 : 0)) * (a_vInfty - y_v)) / a_tauVMinus) - (((((y_u - K(C_thetaV))) > R(0) ? 1 : 0) * y_v) / K(C_tauVPlus)));
+    dydt[S_w] = ((((R(1.0) - (((y_u - K(C_thetaW))) > R(0) ? 1 : 0)) * (a_wInfty - y_w)) / a_tauWMinus) - (((((y_u - K(C_thetaW))) > R(0) ? 1 : 0) * y_w) / K(C_tauWPlus)));
+    dydt[S_s] = ((((R(1.0) + cfg_tanh((K(C_kS) * (y_u - K(C_uS))))) / R(2.0)) - y_s) / a_tauS);
     R a_Istim = (SOLVE_VM ? R(cfg_stimulus_current<double>(t, stim)) : R(0));
     if (SOLVE_VM) {
         dydt[S_u] = ((-a_Jion) - a_Istim);
@@ -212,20 +237,24 @@ __device__ __forceinline__ R iion(double t, const YS& Y, const KS& K, int tissue
 {
     (void)tissue; (void)stim; (void)t;
     R dydt[NS];
-    R a_tauSo = (K(C_tauSo1) + (((K(C_tauSo2) - K(C_tauSo1)) * (R(1.0) + cfg_tanh((K(C_kSo) * (Y(S_u) - K(C_uSo)))))) / R(2.0)));
-    R a_tauO = (((R(1.0) - (((Y(S_u) - K(C_thetaO))) > R(0) ? 1 : 0)) * K(C_tauO1)) + ((((Y(S_u) - K(C_thetaO))) > R(0) ? 1 : 0) * K(C_tauO2)));
-    R a_Jfi = (((((-Y(S_v)) * (((Y(S_u) - K(C_thetaV))) > R(0) ? 1 : 0)) * (Y(S_u) - K(C_thetaV))) * (K(C_uU) - Y(S_u))) / K(C_tauFi));
-    R a_Jso = ((((Y(S_u) - K(C_uO)) * (R(1.0) - (((Y(S_u) - K(C_thetaW))) > R(0) ? 1 : 0))) / a_tauO) + ((((Y(S_u) - K(C_thetaW))) > R(0) ? 1 : 0) / a_tauSo));
-    R a_Jsi = ((((-(((Y(S_u) - K(C_thetaW))) > R(0) ? 1 : 0)) * Y(S_w)) * Y(S_s)) / K(C_tauSi));
+    const R y_u = Y(S_u);
+    const R y_v = Y(S_v);
+    const R y_w = Y(S_w);
+    const R y_s = Y(S_s);
+    R a_tauSo = (K(C_tauSo1) + (((K(C_tauSo2) - K(C_tauSo1)) * (R(1.0) + cfg_tanh((K(C_kSo) * (y_u - K(C_uSo)))))) / R(2.0)));
+    R a_tauO = (((R(1.0) - (((y_u - K(C_thetaO))) > R(0) ? 1 : 0)) * K(C_tauO1)) + ((((y_u - K(C_thetaO))) > R(0) ? 1 : 0) * K(C_tauO2)));
+    R a_Jfi = (((((-y_v) * (((y_u - K(C_thetaV))) > R(0) ? 1 : 0)) * (y_u - K(C_thetaV))) * (K(C_uU) - y_u)) / K(C_tauFi));
+    R a_Jso = ((((y_u - K(C_uO)) * (R(1.0) - (((y_u - K(C_thetaW))) > R(0) ? 1 : 0))) / a_tauO) + ((((y_u - K(C_thetaW))) > R(0) ? 1 : 0) / a_tauSo));
+    R a_Jsi = ((((-(((y_u - K(C_thetaW))) > R(0) ? 1 : 0)) * y_w) * y_s) / K(C_tauSi));
     R a_Jion = ((a_Jfi + a_Jso) + a_Jsi);
-    R a_tauVMinus = (((R(1.0) - (((Y(S_u) - K(C_thetaVMinus))) > R(0) ? 1 : 0)) * K(C_tauV1Minus)) + ((((Y(S_u) - K(C_thetaVMinus))) > R(0) ? 1 : 0) * K(C_tauV2Minus)));
-    R a_tauWMinus = (K(C_tauW1Minus) + (((K(C_tauW2Minus) - K(C_tauW1Minus)) * (R(1.0) + cfg_tanh((K(C_kWMinus) * (Y(S_u) - K(C_uWMinus)))))) / R(2.0)));
-    R a_tauS = (((R(1.0) - (((Y(S_u) - K(C_thetaW))) > R(0) ? 1 : 0)) * K(C_tauS1)) + ((((Y(S_u) - K(C_thetaW))) > R(0) ? 1 : 0) * K(C_tauS2)));
-    R a_vInfty = (((K(C_thetaVMinus) - Y(S_u))) > R(0) ? 1 : 0);
-    R a_wInfty = (((R(1.0) - (((Y(S_u) - K(C_thetaO))) > R(0) ? 1 : 0)) * (R(1.0) - (Y(S_u) / K(C_tauWInfty)))) + ((((Y(S_u) - K(C_thetaO))) > R(0) ? 1 : 0) * K(C_wInftyStar)));
-    dydt[S_v] = ((((R(1.0) - (((Y(S_u) - K(C_thetaV))) > R(0) ? 1 : 0)) * (a_vInfty - Y(S_v))) / a_tauVMinus) - (((((Y(S_u) - K(C_thetaV))) > R(0) ? 1 : 0) * Y(S_v)) / K(C_tauVPlus)));
-    dydt[S_w] = ((((R(1.0) - (((Y(S_u) - K(C_thetaW))) > R(0) ? 1 : 0)) * (a_wInfty - Y(S_w))) / a_tauWMinus) - (((((Y(S_u) - K(C_thetaW))) > R(0) ? 1 : 0) * Y(S_w)) / K(C_tauWPlus)));
-    dydt[S_s] = ((((R(1.0) + cfg_tanh((K(C_kS) * (Y(S_u) - K(C_uS))))) / R(2.0)) - Y(S_s)) / a_tauS);
+    R a_tauVMinus = (((R(1.0) - (((y_u - K(C_thetaVMinus))) > R(0) ? 1 : 0)) * K(C_tauV1Minus)) + ((((y_u - K(C_thetaVMinus))) > R(0) ? 1 : 0) * K(C_tauV2Minus)));
+    R a_tauWMinus = (K(C_tauW1Minus) + (((K(C_tauW2Minus) - K(C_tauW1Minus)) * (R(1.0) + cfg_tanh((K(C_kWMinus) * (y_u - K(C_uWMinus)))))) / R(2.0)));
+    R a_tauS = (((R(1.0) - (((y_u - K(C_thetaW))) > R(0) ? 1 : 0)) * K(C_tauS1)) + ((((y_u - K(C_thetaW))) > R(0) ? 1 : 0) * K(C_tauS2)));
+    R a_vInfty = (((K(C_thetaVMinus) - y_u)) > R(0) ? 1 : 0);
+    R a_wInfty = (((R(1.0) - (((y_u - K(C_thetaO))) > R(0) ? 1 : 0)) * (R(1.0) - (y_u / K(C_tauWInfty)))) + ((((y_u - K(C_thetaO))) > R(0) ? 1 : 0) * K(C_wInftyStar)));
+    dydt[S_v] = ((((R(1.0) - (((y_u - K(C_thetaV))) > R(0) ? 1 : 0)) * (a_vInfty - y_v)) / a_tauVMinus) - (((((y_u - K(C_thetaV))) > R(0) ? 1 : 0) * y_v) / K(C_tauVPlus)));
+    dydt[S_w] = ((((R(1.0) - (((y_u - K(C_thetaW))) > R(0) ? 1 : 0)) * (a_wInfty - y_w)) / a_tauWMinus) - (((((y_u - K(C_thetaW))) > R(0) ? 1 : 0) * y_w) / K(C_tauWPlus)));
+    dydt[S_s] = ((((R(1.0) + cfg_tanh((K(C_kS) * (y_u - K(C_uS))))) / R(2.0)) - y_s) / a_tauS);
     R a_Istim = (SOLVE_VM ? R(cfg_stimulus_current<double>(t, stim)) : R(0));
     if (SOLVE_VM) {
         dydt[S_u] = ((-a_Jion) - a_Istim);
@@ -243,6 +272,9 @@ struct Model {
     static constexpr int VM_MAP = buenoorovio::VM_MAP;
     CFG_HD static __forceinline__ void init(double* C, double* y, int tissue, const double* scale) { init_consts(C, y, tissue, scale); }
     template <int T> CFG_HD static constexpr double constant(int i) { return cval<T>(i); }
+    static constexpr int NSD = buenoorovio::NSD, CA_STATE = buenoorovio::CA_STATE;
+    CFG_HD static constexpr int sd_slot(int i) { return buenoorovio::sd_slot(i); }
+    CFG_HD static constexpr int sd_const(int k) { return buenoorovio::sd_const(k); }
     template <class R, bool SV, class YS, class KS>
     __device__ static __forceinline__ R rates(double t, const YS& Y, const KS& K, R* dydt, int tissue, const CfgStimulus& st) { return rhs<R, SV>(t, Y, K, dydt, tissue, st); }
     template <class R, bool SV, class YS, class KS>

@@ -30,6 +30,38 @@ constexpr int SCALE_GKs = 3;
 constexpr int SCALE_GK1 = 4;
 constexpr int SCALE_Gto = 5;
 
+// Constants that depend on the per-cell conductance scales and that the
+// right-hand side reads: the scaled conductances and every constant
+// initConsts derives from them.  sd_slot(i) is constant i's index in a
+// cell's vector of them, or -1 (then the constant is the tissue's).
+constexpr int NSD = 6;
+CFG_HD constexpr int sd_const(int k)
+{
+    switch (k) {
+    case 0: return C_g_K1;
+    case 1: return C_g_Kr;
+    case 2: return C_g_Ks;
+    case 3: return C_g_Na;
+    case 4: return C_g_CaL;
+    case 5: return C_g_to;
+    default: return -1;
+    }
+}
+CFG_HD constexpr int sd_slot(int i)
+{
+    switch (i) {
+    case C_g_K1: return 0;
+    case C_g_Kr: return 1;
+    case C_g_Ks: return 2;
+    case C_g_Na: return 3;
+    case C_g_CaL: return 4;
+    case C_g_to: return 5;
+    default: return -1;
+    }
+}
+// intracellular calcium state (peak Ca of a beat), or -1
+constexpr int CA_STATE = S_Ca_i;
+
 // Constants and initial states (initConsts).  `scale` may be null;
 // otherwise scale[SCALE_x] multiplies the named conductance right after
 // it is assigned, before constants derived from it are computed.
@@ -255,85 +287,103 @@ template <> CFG_HD constexpr double cval<1>(int i)
 
 // Right-hand side as used by derivatives(): dydt for every state that the
 // reference assigns (RATES of V only when SOLVE_VM).  Returns Iion.
-// Y(i) reads state i as R, K(i) reads constant i as R.
+// Y(i) reads state i as R (each state once, before any dydt store),
+// K(i) reads constant i as R.
 template <class R, bool SOLVE_VM, class YS, class KS>
 __device__ __forceinline__ R rhs(double t, const YS& Y, const KS& K, R* dydt, int tissue, const CfgStimulus& stim)
 {
     (void)tissue; (void)stim; (void)t;
-    R a_m_inf = (R(1.00000) / cfg_ipow<2>((R(1.00000) + cfg_exp((((-R(56.8600)) - Y(S_V)) / R(9.03000))))));
-    R a_alpha_m = (R(1.00000) / (R(1.00000) + cfg_exp((((-R(60.0000)) - Y(S_V)) / R(5.00000)))));
-    R a_beta_m = ((R(0.100000) / (R(1.00000) + cfg_exp(((Y(S_V) + R(35.0000)) / R(5.00000))))) + (R(0.100000) / (R(1.00000) + cfg_exp(((Y(S_V) - R(50.0000)) / R(200.000))))));
+    const R y_V = Y(S_V);
+    const R y_K_i = Y(S_K_i);
+    const R y_Na_i = Y(S_Na_i);
+    const R y_Ca_i = Y(S_Ca_i);
+    const R y_Xr1 = Y(S_Xr1);
+    const R y_Xr2 = Y(S_Xr2);
+    const R y_Xs = Y(S_Xs);
+    const R y_m = Y(S_m);
+    const R y_h = Y(S_h);
+    const R y_j = Y(S_j);
+    const R y_d = Y(S_d);
+    const R y_f = Y(S_f);
+    const R y_fCa = Y(S_fCa);
+    const R y_s = Y(S_s);
+    const R y_r = Y(S_r);
+    const R y_Ca_SR = Y(S_Ca_SR);
+    const R y_g = Y(S_g);
+    R a_m_inf = (R(1.00000) / cfg_ipow<2>((R(1.00000) + cfg_exp((((-R(56.8600)) - y_V) / R(9.03000))))));
+    R a_alpha_m = (R(1.00000) / (R(1.00000) + cfg_exp((((-R(60.0000)) - y_V) / R(5.00000)))));
+    R a_beta_m = ((R(0.100000) / (R(1.00000) + cfg_exp(((y_V + R(35.0000)) / R(5.00000))))) + (R(0.100000) / (R(1.00000) + cfg_exp(((y_V - R(50.0000)) / R(200.000))))));
     R a_tau_m = ((R(1.00000) * a_alpha_m) * a_beta_m);
-    dydt[S_m] = ((a_m_inf - Y(S_m)) / a_tau_m);
-    R a_h_inf = (R(1.00000) / cfg_ipow<2>((R(1.00000) + cfg_exp(((Y(S_V) + R(71.5500)) / R(7.43000))))));
-    R a_alpha_h = ((Y(S_V) < (-R(40.0000))) ? (R(0.0570000) * cfg_exp(((-(Y(S_V) + R(80.0000))) / R(6.80000)))) : R(0.00000));
-    R a_beta_h = ((Y(S_V) < (-R(40.0000))) ? ((R(2.70000) * cfg_exp((R(0.0790000) * Y(S_V)))) + (R(310000.) * cfg_exp((R(0.348500) * Y(S_V))))) : (R(0.770000) / (R(0.130000) * (R(1.00000) + cfg_exp(((Y(S_V) + R(10.6600)) / (-R(11.1000))))))));
+    dydt[S_m] = ((a_m_inf - y_m) / a_tau_m);
+    R a_h_inf = (R(1.00000) / cfg_ipow<2>((R(1.00000) + cfg_exp(((y_V + R(71.5500)) / R(7.43000))))));
+    R a_alpha_h = ((y_V < (-R(40.0000))) ? (R(0.0570000) * cfg_exp(((-(y_V + R(80.0000))) / R(6.80000)))) : R(0.00000));
+    R a_beta_h = ((y_V < (-R(40.0000))) ? ((R(2.70000) * cfg_exp((R(0.0790000) * y_V))) + (R(310000.) * cfg_exp((R(0.348500) * y_V)))) : (R(0.770000) / (R(0.130000) * (R(1.00000) + cfg_exp(((y_V + R(10.6600)) / (-R(11.1000))))))));
     R a_tau_h = (R(1.00000) / (a_alpha_h + a_beta_h));
-    dydt[S_h] = ((a_h_inf - Y(S_h)) / a_tau_h);
-    R a_j_inf = (R(1.00000) / cfg_ipow<2>((R(1.00000) + cfg_exp(((Y(S_V) + R(71.5500)) / R(7.43000))))));
-    R a_alpha_j = ((Y(S_V) < (-R(40.0000))) ? ((((((-R(25428.0)) * cfg_exp((R(0.244400) * Y(S_V)))) - (R(6.94800e-06) * cfg_exp(((-R(0.0439100)) * Y(S_V))))) * (Y(S_V) + R(37.7800))) / R(1.00000)) / (R(1.00000) + cfg_exp((R(0.311000) * (Y(S_V) + R(79.2300)))))) : R(0.00000));
-    R a_beta_j = ((Y(S_V) < (-R(40.0000))) ? ((R(0.0242400) * cfg_exp(((-R(0.0105200)) * Y(S_V)))) / (R(1.00000) + cfg_exp(((-R(0.137800)) * (Y(S_V) + R(40.1400)))))) : ((R(0.600000) * cfg_exp((R(0.0570000) * Y(S_V)))) / (R(1.00000) + cfg_exp(((-R(0.100000)) * (Y(S_V) + R(32.0000)))))));
+    dydt[S_h] = ((a_h_inf - y_h) / a_tau_h);
+    R a_j_inf = (R(1.00000) / cfg_ipow<2>((R(1.00000) + cfg_exp(((y_V + R(71.5500)) / R(7.43000))))));
+    R a_alpha_j = ((y_V < (-R(40.0000))) ? ((((((-R(25428.0)) * cfg_exp((R(0.244400) * y_V))) - (R(6.94800e-06) * cfg_exp(((-R(0.0439100)) * y_V)))) * (y_V + R(37.7800))) / R(1.00000)) / (R(1.00000) + cfg_exp((R(0.311000) * (y_V + R(79.2300)))))) : R(0.00000));
+    R a_beta_j = ((y_V < (-R(40.0000))) ? ((R(0.0242400) * cfg_exp(((-R(0.0105200)) * y_V))) / (R(1.00000) + cfg_exp(((-R(0.137800)) * (y_V + R(40.1400)))))) : ((R(0.600000) * cfg_exp((R(0.0570000) * y_V))) / (R(1.00000) + cfg_exp(((-R(0.100000)) * (y_V + R(32.0000)))))));
     R a_tau_j = (R(1.00000) / (a_alpha_j + a_beta_j));
-    dydt[S_j] = ((a_j_inf - Y(S_j)) / a_tau_j);
-    R a_d_inf = (R(1.00000) / (R(1.00000) + cfg_exp((((-R(5.00000)) - Y(S_V)) / R(7.50000)))));
-    R a_alpha_d = ((R(1.40000) / (R(1.00000) + cfg_exp((((-R(35.0000)) - Y(S_V)) / R(13.0000))))) + R(0.250000));
-    R a_gama_fCa = (R(1.40000) / (R(1.00000) + cfg_exp(((Y(S_V) + R(5.00000)) / R(5.00000)))));
-    R a_gamma_d = (R(1.00000) / (R(1.00000) + cfg_exp(((R(50.0000) - Y(S_V)) / R(20.0000)))));
+    dydt[S_j] = ((a_j_inf - y_j) / a_tau_j);
+    R a_d_inf = (R(1.00000) / (R(1.00000) + cfg_exp((((-R(5.00000)) - y_V) / R(7.50000)))));
+    R a_alpha_d = ((R(1.40000) / (R(1.00000) + cfg_exp((((-R(35.0000)) - y_V) / R(13.0000))))) + R(0.250000));
+    R a_gama_fCa = (R(1.40000) / (R(1.00000) + cfg_exp(((y_V + R(5.00000)) / R(5.00000)))));
+    R a_gamma_d = (R(1.00000) / (R(1.00000) + cfg_exp(((R(50.0000) - y_V) / R(20.0000)))));
     R a_tau_d = (((R(1.00000) * a_alpha_d) * a_gama_fCa) + a_gamma_d);
-    dydt[S_d] = ((a_d_inf - Y(S_d)) / a_tau_d);
-    R a_f_inf = (R(1.00000) / (R(1.00000) + cfg_exp(((Y(S_V) + R(20.0000)) / R(7.00000)))));
-    R a_tau_f = (((R(1125.00) * cfg_exp(((-cfg_ipow<2>((Y(S_V) + R(27.0000)))) / R(240.000)))) + R(80.0000)) + (R(165.000) / (R(1.00000) + cfg_exp(((R(25.0000) - Y(S_V)) / R(10.0000))))));
-    dydt[S_f] = ((a_f_inf - Y(S_f)) / a_tau_f);
-    R a_alpha_fCa = (R(1.00000) / (R(1.00000) + cfg_ipow<8>((Y(S_Ca_i) / R(0.000325000)))));
-    R a_beta_fCa = (R(0.100000) / (R(1.00000) + cfg_exp(((Y(S_Ca_i) - R(0.000500000)) / R(0.000100000)))));
-    R a_beta_d = (R(0.200000) / (R(1.00000) + cfg_exp(((Y(S_Ca_i) - R(0.000750000)) / R(0.000800000)))));
+    dydt[S_d] = ((a_d_inf - y_d) / a_tau_d);
+    R a_f_inf = (R(1.00000) / (R(1.00000) + cfg_exp(((y_V + R(20.0000)) / R(7.00000)))));
+    R a_tau_f = (((R(1125.00) * cfg_exp(((-cfg_ipow<2>((y_V + R(27.0000)))) / R(240.000)))) + R(80.0000)) + (R(165.000) / (R(1.00000) + cfg_exp(((R(25.0000) - y_V) / R(10.0000))))));
+    dydt[S_f] = ((a_f_inf - y_f) / a_tau_f);
+    R a_alpha_fCa = (R(1.00000) / (R(1.00000) + cfg_ipow<8>((y_Ca_i / R(0.000325000)))));
+    R a_beta_fCa = (R(0.100000) / (R(1.00000) + cfg_exp(((y_Ca_i - R(0.000500000)) / R(0.000100000)))));
+    R a_beta_d = (R(0.200000) / (R(1.00000) + cfg_exp(((y_Ca_i - R(0.000750000)) / R(0.000800000)))));
     R a_fCa_inf = ((((a_alpha_fCa + a_beta_fCa) + a_beta_d) + R(0.230000)) / R(1.46000));
-    R a_d_fCa = ((a_fCa_inf - Y(S_fCa)) / K(C_tau_fCa));
-    dydt[S_fCa] = (((a_fCa_inf > Y(S_fCa)) && (Y(S_V) > (-R(60.0000)))) ? R(0.00000) : a_d_fCa);
-    R a_s_inf = ((tissue == 1) ? (R(1.00000) / (R(1.00000) + cfg_exp(((Y(S_V) + R(20.0000)) / R(5.00000))))) : (R(1.10000) / (R(1.00000) + cfg_exp(((Y(S_V) + R(28.0000)) / R(6.00000))))));
-    R a_tau_s = ((tissue == 1) ? (((R(85.0000) * cfg_exp(((-cfg_ipow<2>((Y(S_V) + R(45.0000)))) / R(320.000)))) + (R(5.00000) / (R(1.00000) + cfg_exp(((Y(S_V) - R(20.0000)) / R(5.00000)))))) + R(3.00000)) : ((R(1000.0000) * cfg_exp(((-cfg_ipow<2>((Y(S_V) + R(67.0000)))) / R(1000.000)))) + R(8.00000)));
-    dydt[S_s] = ((a_s_inf - Y(S_s)) / a_tau_s);
-    R a_r_inf = (R(1.00000) / (R(1.00000) + cfg_exp(((R(20.0000) - Y(S_V)) / R(6.00000)))));
-    R a_tau_r = ((R(9.50000) * cfg_exp(((-cfg_ipow<2>((Y(S_V) + R(40.0000)))) / R(1800.00)))) + R(0.800000));
-    dydt[S_r] = ((a_r_inf - Y(S_r)) / a_tau_r);
-    R a_xr1_inf = (R(1.00000) / (R(1.00000) + cfg_exp((((-R(26.0000)) - Y(S_V)) / R(7.00000)))));
-    R a_alpha_xr1 = (R(450.000) / (R(1.00000) + cfg_exp((((-R(45.0000)) - Y(S_V)) / R(10.0000)))));
-    R a_beta_xr1 = (R(6.00000) / (R(1.00000) + cfg_exp(((Y(S_V) + R(30.0000)) / R(11.5000)))));
+    R a_d_fCa = ((a_fCa_inf - y_fCa) / K(C_tau_fCa));
+    dydt[S_fCa] = (((a_fCa_inf > y_fCa) && (y_V > (-R(60.0000)))) ? R(0.00000) : a_d_fCa);
+    R a_s_inf = ((tissue == 1) ? (R(1.00000) / (R(1.00000) + cfg_exp(((y_V + R(20.0000)) / R(5.00000))))) : (R(1.10000) / (R(1.00000) + cfg_exp(((y_V + R(28.0000)) / R(6.00000))))));
+    R a_tau_s = ((tissue == 1) ? (((R(85.0000) * cfg_exp(((-cfg_ipow<2>((y_V + R(45.0000)))) / R(320.000)))) + (R(5.00000) / (R(1.00000) + cfg_exp(((y_V - R(20.0000)) / R(5.00000)))))) + R(3.00000)) : ((R(1000.0000) * cfg_exp(((-cfg_ipow<2>((y_V + R(67.0000)))) / R(1000.000)))) + R(8.00000)));
+    dydt[S_s] = ((a_s_inf - y_s) / a_tau_s);
+    R a_r_inf = (R(1.00000) / (R(1.00000) + cfg_exp(((R(20.0000) - y_V) / R(6.00000)))));
+    R a_tau_r = ((R(9.50000) * cfg_exp(((-cfg_ipow<2>((y_V + R(40.0000)))) / R(1800.00)))) + R(0.800000));
+    dydt[S_r] = ((a_r_inf - y_r) / a_tau_r);
+    R a_xr1_inf = (R(1.00000) / (R(1.00000) + cfg_exp((((-R(26.0000)) - y_V) / R(7.00000)))));
+    R a_alpha_xr1 = (R(450.000) / (R(1.00000) + cfg_exp((((-R(45.0000)) - y_V) / R(10.0000)))));
+    R a_beta_xr1 = (R(6.00000) / (R(1.00000) + cfg_exp(((y_V + R(30.0000)) / R(11.5000)))));
     R a_tau_xr1 = ((R(1.00000) * a_alpha_xr1) * a_beta_xr1);
-    dydt[S_Xr1] = ((a_xr1_inf - Y(S_Xr1)) / a_tau_xr1);
-    R a_xr2_inf = (R(1.00000) / (R(1.00000) + cfg_exp(((Y(S_V) + R(88.0000)) / R(24.0000)))));
-    R a_alpha_xr2 = (R(3.00000) / (R(1.00000) + cfg_exp((((-R(60.0000)) - Y(S_V)) / R(20.0000)))));
-    R a_beta_xr2 = (R(1.12000) / (R(1.00000) + cfg_exp(((Y(S_V) - R(60.0000)) / R(20.0000)))));
+    dydt[S_Xr1] = ((a_xr1_inf - y_Xr1) / a_tau_xr1);
+    R a_xr2_inf = (R(1.00000) / (R(1.00000) + cfg_exp(((y_V + R(88.0000)) / R(24.0000)))));
+    R a_alpha_xr2 = (R(3.00000) / (R(1.00000) + cfg_exp((((-R(60.0000)) - y_V) / R(20.0000)))));
+    R a_beta_xr2 = (R(1.12000) / (R(1.00000) + cfg_exp(((y_V - R(60.0000)) / R(20.0000)))));
     R a_tau_xr2 = ((R(1.00000) * a_alpha_xr2) * a_beta_xr2);
-    dydt[S_Xr2] = ((a_xr2_inf - Y(S_Xr2)) / a_tau_xr2);
-    R a_xs_inf = (R(1.00000) / (R(1.00000) + cfg_exp((((-R(5.00000)) - Y(S_V)) / R(14.0000)))));
-    R a_alpha_xs = (R(1100.00) / cfg_sqrt((R(1.00000) + cfg_exp((((-R(10.0000)) - Y(S_V)) / R(6.00000))))));
-    R a_beta_xs = (R(1.00000) / (R(1.00000) + cfg_exp(((Y(S_V) - R(60.0000)) / R(20.0000)))));
+    dydt[S_Xr2] = ((a_xr2_inf - y_Xr2) / a_tau_xr2);
+    R a_xs_inf = (R(1.00000) / (R(1.00000) + cfg_exp((((-R(5.00000)) - y_V) / R(14.0000)))));
+    R a_alpha_xs = (R(1100.00) / cfg_sqrt((R(1.00000) + cfg_exp((((-R(10.0000)) - y_V) / R(6.00000))))));
+    R a_beta_xs = (R(1.00000) / (R(1.00000) + cfg_exp(((y_V - R(60.0000)) / R(20.0000)))));
     R a_tau_xs = ((R(1.00000) * a_alpha_xs) * a_beta_xs);
-    dydt[S_Xs] = ((a_xs_inf - Y(S_Xs)) / a_tau_xs);
-    R a_g_inf = ((Y(S_Ca_i) < R(0.000350000)) ? (R(1.00000) / (R(1.00000) + cfg_ipow<6>((Y(S_Ca_i) / R(0.000350000))))) : (R(1.00000) / (R(1.00000) + cfg_ipow<16>((Y(S_Ca_i) / R(0.000350000))))));
-    R a_d_g = ((a_g_inf - Y(S_g)) / K(C_tau_g));
-    dydt[S_g] = (((a_g_inf > Y(S_g)) && (Y(S_V) > (-R(60.0000)))) ? R(0.00000) : a_d_g);
-    R a_i_NaK = (((((K(C_P_NaK) * K(C_K_o)) / (K(C_K_o) + K(C_K_mk))) * Y(S_Na_i)) / (Y(S_Na_i) + K(C_K_mNa))) / ((R(1.00000) + (R(0.124500) * cfg_exp(((((-R(0.100000)) * Y(S_V)) * K(C_F)) / (K(C_R) * K(C_T)))))) + (R(0.0353000) * cfg_exp((((-Y(S_V)) * K(C_F)) / (K(C_R) * K(C_T)))))));
-    R a_E_Na = (((K(C_R) * K(C_T)) / K(C_F)) * cfg_log((K(C_Na_o) / Y(S_Na_i))));
-    R a_i_Na = ((((K(C_g_Na) * cfg_ipow<3>(Y(S_m))) * Y(S_h)) * Y(S_j)) * (Y(S_V) - a_E_Na));
-    R a_i_b_Na = (K(C_g_bNa) * (Y(S_V) - a_E_Na));
-    R a_i_NaCa = ((K(C_K_NaCa) * (((cfg_exp((((K(C_gamma_NCX) * Y(S_V)) * K(C_F)) / (K(C_R) * K(C_T)))) * cfg_ipow<3>(Y(S_Na_i))) * K(C_Ca_o)) - (((cfg_exp(((((K(C_gamma_NCX) - R(1.00000)) * Y(S_V)) * K(C_F)) / (K(C_R) * K(C_T)))) * cfg_ipow<3>(K(C_Na_o))) * Y(S_Ca_i)) * K(C_alpha_NCX)))) / (((cfg_ipow<3>(K(C_Km_Nai)) + cfg_ipow<3>(K(C_Na_o))) * (K(C_Km_Ca) + K(C_Ca_o))) * (R(1.00000) + (K(C_K_sat) * cfg_exp(((((K(C_gamma_NCX) - R(1.00000)) * Y(S_V)) * K(C_F)) / (K(C_R) * K(C_T))))))));
+    dydt[S_Xs] = ((a_xs_inf - y_Xs) / a_tau_xs);
+    R a_g_inf = ((y_Ca_i < R(0.000350000)) ? (R(1.00000) / (R(1.00000) + cfg_ipow<6>((y_Ca_i / R(0.000350000))))) : (R(1.00000) / (R(1.00000) + cfg_ipow<16>((y_Ca_i / R(0.000350000))))));
+    R a_d_g = ((a_g_inf - y_g) / K(C_tau_g));
+    dydt[S_g] = (((a_g_inf > y_g) && (y_V > (-R(60.0000)))) ? R(0.00000) : a_d_g);
+    R a_i_NaK = (((((K(C_P_NaK) * K(C_K_o)) / (K(C_K_o) + K(C_K_mk))) * y_Na_i) / (y_Na_i + K(C_K_mNa))) / ((R(1.00000) + (R(0.124500) * cfg_exp(((((-R(0.100000)) * y_V) * K(C_F)) / (K(C_R) * K(C_T)))))) + (R(0.0353000) * cfg_exp((((-y_V) * K(C_F)) / (K(C_R) * K(C_T)))))));
+    R a_E_Na = (((K(C_R) * K(C_T)) / K(C_F)) * cfg_log((K(C_Na_o) / y_Na_i)));
+    R a_i_Na = ((((K(C_g_Na) * cfg_ipow<3>(y_m)) * y_h) * y_j) * (y_V - a_E_Na));
+    R a_i_b_Na = (K(C_g_bNa) * (y_V - a_E_Na));
+    R a_i_NaCa = ((K(C_K_NaCa) * (((cfg_exp((((K(C_gamma_NCX) * y_V) * K(C_F)) / (K(C_R) * K(C_T)))) * cfg_ipow<3>(y_Na_i)) * K(C_Ca_o)) - (((cfg_exp(((((K(C_gamma_NCX) - R(1.00000)) * y_V) * K(C_F)) / (K(C_R) * K(C_T)))) * cfg_ipow<3>(K(C_Na_o))) * y_Ca_i) * K(C_alpha_NCX)))) / (((cfg_ipow<3>(K(C_Km_Nai)) + cfg_ipow<3>(K(C_Na_o))) * (K(C_Km_Ca) + K(C_Ca_o))) * (R(1.00000) + (K(C_K_sat) * cfg_exp(((((K(C_gamma_NCX) - R(1.00000)) * y_V) * K(C_F)) / (K(C_R) * K(C_T))))))));
     dydt[S_Na_i] = (((-(((a_i_Na + a_i_b_Na) + (R(3.00000) * a_i_NaK)) + (R(3.00000) * a_i_NaCa))) * K(C_Cm)) / (K(C_V_c) * K(C_F)));
-    R a_E_K = (((K(C_R) * K(C_T)) / K(C_F)) * cfg_log((K(C_K_o) / Y(S_K_i))));
-    R a_alpha_K1 = (R(0.100000) / (R(1.00000) + cfg_exp((R(0.0600000) * ((Y(S_V) - a_E_K) - R(200.000))))));
-    R a_beta_K1 = (((R(3.00000) * cfg_exp((R(0.000200000) * ((Y(S_V) - a_E_K) + R(100.000))))) + (R(1.00000) * cfg_exp((R(0.100000) * ((Y(S_V) - a_E_K) - R(10.0000)))))) / (R(1.00000) + cfg_exp(((-R(0.500000)) * (Y(S_V) - a_E_K)))));
+    R a_E_K = (((K(C_R) * K(C_T)) / K(C_F)) * cfg_log((K(C_K_o) / y_K_i)));
+    R a_alpha_K1 = (R(0.100000) / (R(1.00000) + cfg_exp((R(0.0600000) * ((y_V - a_E_K) - R(200.000))))));
+    R a_beta_K1 = (((R(3.00000) * cfg_exp((R(0.000200000) * ((y_V - a_E_K) + R(100.000))))) + (R(1.00000) * cfg_exp((R(0.100000) * ((y_V - a_E_K) - R(10.0000)))))) / (R(1.00000) + cfg_exp(((-R(0.500000)) * (y_V - a_E_K)))));
     R a_xK1_inf = (a_alpha_K1 / (a_alpha_K1 + a_beta_K1));
-    R a_i_K1 = (((K(C_g_K1) * a_xK1_inf) * cfg_sqrt((K(C_K_o) / R(5.40000)))) * (Y(S_V) - a_E_K));
-    R a_i_to = (((K(C_g_to) * Y(S_r)) * Y(S_s)) * (Y(S_V) - a_E_K));
-    R a_i_Kr = ((((K(C_g_Kr) * cfg_sqrt((K(C_K_o) / R(5.40000)))) * Y(S_Xr1)) * Y(S_Xr2)) * (Y(S_V) - a_E_K));
-    R a_E_Ks = (((K(C_R) * K(C_T)) / K(C_F)) * cfg_log(((K(C_K_o) + (K(C_P_kna) * K(C_Na_o))) / (Y(S_K_i) + (K(C_P_kna) * Y(S_Na_i))))));
-    R a_i_Ks = ((K(C_g_Ks) * cfg_ipow<2>(Y(S_Xs))) * (Y(S_V) - a_E_Ks));
-    R a_i_CaL = (((((((((K(C_g_CaL) * Y(S_d)) * Y(S_f)) * Y(S_fCa)) * R(4.00000)) * Y(S_V)) * cfg_ipow<2>(K(C_F))) / (K(C_R) * K(C_T))) * ((Y(S_Ca_i) * cfg_exp((((R(2.00000) * Y(S_V)) * K(C_F)) / (K(C_R) * K(C_T))))) - (R(0.341000) * K(C_Ca_o)))) / (cfg_exp((((R(2.00000) * Y(S_V)) * K(C_F)) / (K(C_R) * K(C_T)))) - R(1.00000)));
-    R a_E_Ca = ((((R(0.500000) * K(C_R)) * K(C_T)) / K(C_F)) * cfg_log((K(C_Ca_o) / Y(S_Ca_i))));
-    R a_i_b_Ca = (K(C_g_bCa) * (Y(S_V) - a_E_Ca));
-    R a_i_p_K = ((K(C_g_pK) * (Y(S_V) - a_E_K)) / (R(1.00000) + cfg_exp(((R(25.0000) - Y(S_V)) / R(5.98000)))));
-    R a_i_p_Ca = ((K(C_g_pCa) * Y(S_Ca_i)) / (Y(S_Ca_i) + K(C_K_pCa)));
+    R a_i_K1 = (((K(C_g_K1) * a_xK1_inf) * cfg_sqrt((K(C_K_o) / R(5.40000)))) * (y_V - a_E_K));
+    R a_i_to = (((K(C_g_to) * y_r) * y_s) * (y_V - a_E_K));
+    R a_i_Kr = ((((K(C_g_Kr) * cfg_sqrt((K(C_K_o) / R(5.40000)))) * y_Xr1) * y_Xr2) * (y_V - a_E_K));
+    R a_E_Ks = (((K(C_R) * K(C_T)) / K(C_F)) * cfg_log(((K(C_K_o) + (K(C_P_kna) * K(C_Na_o))) / (y_K_i + (K(C_P_kna) * y_Na_i)))));
+    R a_i_Ks = ((K(C_g_Ks) * cfg_ipow<2>(y_Xs)) * (y_V - a_E_Ks));
+    R a_i_CaL = (((((((((K(C_g_CaL) * y_d) * y_f) * y_fCa) * R(4.00000)) * y_V) * cfg_ipow<2>(K(C_F))) / (K(C_R) * K(C_T))) * ((y_Ca_i * cfg_exp((((R(2.00000) * y_V) * K(C_F)) / (K(C_R) * K(C_T))))) - (R(0.341000) * K(C_Ca_o)))) / (cfg_exp((((R(2.00000) * y_V) * K(C_F)) / (K(C_R) * K(C_T)))) - R(1.00000)));
+    R a_E_Ca = ((((R(0.500000) * K(C_R)) * K(C_T)) / K(C_F)) * cfg_log((K(C_Ca_o) / y_Ca_i)));
+    R a_i_b_Ca = (K(C_g_bCa) * (y_V - a_E_Ca));
+    R a_i_p_K = ((K(C_g_pK) * (y_V - a_E_K)) / (R(1.00000) + cfg_exp(((R(25.0000) - y_V) / R(5.98000)))));
+    R a_i_p_Ca = ((K(C_g_pCa) * y_Ca_i) / (y_Ca_i + K(C_K_pCa)));
     R a_Iion_cm = (((((((((((a_i_K1 + a_i_to) + a_i_Kr) + a_i_Ks) + a_i_CaL) + a_i_NaK) + a_i_Na) + a_i_b_Na) + a_i_NaCa) + a_i_b_Ca) + a_i_p_K) + a_i_p_Ca);
     R a_Istim = (SOLVE_VM ? R(cfg_stimulus_current<double>(t, stim)) : R(0));
     dydt[S_V] = R(0.0);
@@ -341,14 +391,14 @@ __device__ __forceinline__ R rhs(double t, const YS& Y, const KS& K, R* dydt, in
         dydt[S_V] = ((-a_Iion_cm) - a_Istim);
     }
     dydt[S_K_i] = (((-((((((a_i_K1 + a_i_to) + a_i_Kr) + a_i_Ks) + a_i_p_K) + a_Istim) - (R(2.00000) * a_i_NaK))) * K(C_Cm)) / (K(C_V_c) * K(C_F)));
-    R a_i_rel = (((((K(C_a_rel) * cfg_ipow<2>(Y(S_Ca_SR))) / (cfg_ipow<2>(K(C_b_rel)) + cfg_ipow<2>(Y(S_Ca_SR)))) + K(C_c_rel)) * Y(S_d)) * Y(S_g));
-    R a_i_up = (K(C_Vmax_up) / (R(1.00000) + (cfg_ipow<2>(K(C_K_up)) / cfg_ipow<2>(Y(S_Ca_i)))));
-    R a_i_leak = (K(C_V_leak) * (Y(S_Ca_SR) - Y(S_Ca_i)));
+    R a_i_rel = (((((K(C_a_rel) * cfg_ipow<2>(y_Ca_SR)) / (cfg_ipow<2>(K(C_b_rel)) + cfg_ipow<2>(y_Ca_SR))) + K(C_c_rel)) * y_d) * y_g);
+    R a_i_up = (K(C_Vmax_up) / (R(1.00000) + (cfg_ipow<2>(K(C_K_up)) / cfg_ipow<2>(y_Ca_i))));
+    R a_i_leak = (K(C_V_leak) * (y_Ca_SR - y_Ca_i));
     R a_ddt_Ca_i_total = ((((((-(((a_i_CaL + a_i_b_Ca) + a_i_p_Ca) - (R(2.00000) * a_i_NaCa))) / ((R(2.00000) * K(C_V_c)) * K(C_F))) * K(C_Cm)) + a_i_leak) - a_i_up) + a_i_rel);
-    R a_f_JCa_i_free = (R(1.00000) / (R(1.00000) + ((K(C_Buf_c) * K(C_K_buf_c)) / cfg_ipow<2>((Y(S_Ca_i) + K(C_K_buf_c))))));
+    R a_f_JCa_i_free = (R(1.00000) / (R(1.00000) + ((K(C_Buf_c) * K(C_K_buf_c)) / cfg_ipow<2>((y_Ca_i + K(C_K_buf_c))))));
     dydt[S_Ca_i] = (a_ddt_Ca_i_total * a_f_JCa_i_free);
     R a_ddt_Ca_sr_total = ((K(C_V_c) / K(C_V_sr)) * (a_i_up - (a_i_rel + a_i_leak)));
-    R a_f_JCa_sr_free = (R(1.00000) / (R(1.00000) + ((K(C_Buf_sr) * K(C_K_buf_sr)) / cfg_ipow<2>((Y(S_Ca_SR) + K(C_K_buf_sr))))));
+    R a_f_JCa_sr_free = (R(1.00000) / (R(1.00000) + ((K(C_Buf_sr) * K(C_K_buf_sr)) / cfg_ipow<2>((y_Ca_SR + K(C_K_buf_sr))))));
     dydt[S_Ca_SR] = (a_ddt_Ca_sr_total * a_f_JCa_sr_free);
     return a_Iion_cm;
 }
@@ -359,150 +409,167 @@ __device__ __forceinline__ R iion(double t, const YS& Y, const KS& K, int tissue
 {
     (void)tissue; (void)stim; (void)t;
     R dydt[NS];
-    R a_f_inf = (R(1.00000) / (R(1.00000) + cfg_exp(((Y(S_V) + R(20.0000)) / R(7.00000)))));
-    R a_tau_f = (((R(1125.00) * cfg_exp(((-cfg_ipow<2>((Y(S_V) + R(27.0000)))) / R(240.000)))) + R(80.0000)) + (R(165.000) / (R(1.00000) + cfg_exp(((R(25.0000) - Y(S_V)) / R(10.0000))))));
-    R a_s_inf = ((tissue == 1) ? (R(1.00000) / (R(1.00000) + cfg_exp(((Y(S_V) + R(20.0000)) / R(5.00000))))) : (R(1.10000) / (R(1.00000) + cfg_exp(((Y(S_V) + R(28.0000)) / R(6.00000))))));
-    R a_tau_s = ((tissue == 1) ? (((R(85.0000) * cfg_exp(((-cfg_ipow<2>((Y(S_V) + R(45.0000)))) / R(320.000)))) + (R(5.00000) / (R(1.00000) + cfg_exp(((Y(S_V) - R(20.0000)) / R(5.00000)))))) + R(3.00000)) : ((R(1000.0000) * cfg_exp(((-cfg_ipow<2>((Y(S_V) + R(67.0000)))) / R(1000.000)))) + R(8.00000)));
-    R a_r_inf = (R(1.00000) / (R(1.00000) + cfg_exp(((R(20.0000) - Y(S_V)) / R(6.00000)))));
-    R a_tau_r = ((R(9.50000) * cfg_exp(((-cfg_ipow<2>((Y(S_V) + R(40.0000)))) / R(1800.00)))) + R(0.800000));
-    R a_g_inf = ((Y(S_Ca_i) < R(0.000350000)) ? (R(1.00000) / (R(1.00000) + cfg_ipow<6>((Y(S_Ca_i) / R(0.000350000))))) : (R(1.00000) / (R(1.00000) + cfg_ipow<16>((Y(S_Ca_i) / R(0.000350000))))));
-    R a_d_g = ((a_g_inf - Y(S_g)) / K(C_tau_g));
-    R a_xr1_inf = (R(1.00000) / (R(1.00000) + cfg_exp((((-R(26.0000)) - Y(S_V)) / R(7.00000)))));
-    R a_alpha_xr1 = (R(450.000) / (R(1.00000) + cfg_exp((((-R(45.0000)) - Y(S_V)) / R(10.0000)))));
-    R a_beta_xr1 = (R(6.00000) / (R(1.00000) + cfg_exp(((Y(S_V) + R(30.0000)) / R(11.5000)))));
+    const R y_V = Y(S_V);
+    const R y_K_i = Y(S_K_i);
+    const R y_Na_i = Y(S_Na_i);
+    const R y_Ca_i = Y(S_Ca_i);
+    const R y_Xr1 = Y(S_Xr1);
+    const R y_Xr2 = Y(S_Xr2);
+    const R y_Xs = Y(S_Xs);
+    const R y_m = Y(S_m);
+    const R y_h = Y(S_h);
+    const R y_j = Y(S_j);
+    const R y_d = Y(S_d);
+    const R y_f = Y(S_f);
+    const R y_fCa = Y(S_fCa);
+    const R y_s = Y(S_s);
+    const R y_r = Y(S_r);
+    const R y_Ca_SR = Y(S_Ca_SR);
+    const R y_g = Y(S_g);
+    R a_f_inf = (R(1.00000) / (R(1.00000) + cfg_exp(((y_V + R(20.0000)) / R(7.00000)))));
+    R a_tau_f = (((R(1125.00) * cfg_exp(((-cfg_ipow<2>((y_V + R(27.0000)))) / R(240.000)))) + R(80.0000)) + (R(165.000) / (R(1.00000) + cfg_exp(((R(25.0000) - y_V) / R(10.0000))))));
+    R a_s_inf = ((tissue == 1) ? (R(1.00000) / (R(1.00000) + cfg_exp(((y_V + R(20.0000)) / R(5.00000))))) : (R(1.10000) / (R(1.00000) + cfg_exp(((y_V + R(28.0000)) / R(6.00000))))));
+    R a_tau_s = ((tissue == 1) ? (((R(85.0000) * cfg_exp(((-cfg_ipow<2>((y_V + R(45.0000)))) / R(320.000)))) + (R(5.00000) / (R(1.00000) + cfg_exp(((y_V - R(20.0000)) / R(5.00000)))))) + R(3.00000)) : ((R(1000.0000) * cfg_exp(((-cfg_ipow<2>((y_V + R(67.0000)))) / R(1000.000)))) + R(8.00000)));
+    R a_r_inf = (R(1.00000) / (R(1.00000) + cfg_exp(((R(20.0000) - y_V) / R(6.00000)))));
+    R a_tau_r = ((R(9.50000) * cfg_exp(((-cfg_ipow<2>((y_V + R(40.0000)))) / R(1800.00)))) + R(0.800000));
+    R a_g_inf = ((y_Ca_i < R(0.000350000)) ? (R(1.00000) / (R(1.00000) + cfg_ipow<6>((y_Ca_i / R(0.000350000))))) : (R(1.00000) / (R(1.00000) + cfg_ipow<16>((y_Ca_i / R(0.000350000))))));
+    R a_d_g = ((a_g_inf - y_g) / K(C_tau_g));
+    R a_xr1_inf = (R(1.00000) / (R(1.00000) + cfg_exp((((-R(26.0000)) - y_V) / R(7.00000)))));
+    R a_alpha_xr1 = (R(450.000) / (R(1.00000) + cfg_exp((((-R(45.0000)) - y_V) / R(10.0000)))));
+    R a_beta_xr1 = (R(6.00000) / (R(1.00000) + cfg_exp(((y_V + R(30.0000)) / R(11.5000)))));
     R a_tau_xr1 = ((R(1.00000) * a_alpha_xr1) * a_beta_xr1);
-    R a_xr2_inf = (R(1.00000) / (R(1.00000) + cfg_exp(((Y(S_V) + R(88.0000)) / R(24.0000)))));
-    R a_alpha_xr2 = (R(3.00000) / (R(1.00000) + cfg_exp((((-R(60.0000)) - Y(S_V)) / R(20.0000)))));
-    R a_beta_xr2 = (R(1.12000) / (R(1.00000) + cfg_exp(((Y(S_V) - R(60.0000)) / R(20.0000)))));
+    R a_xr2_inf = (R(1.00000) / (R(1.00000) + cfg_exp(((y_V + R(88.0000)) / R(24.0000)))));
+    R a_alpha_xr2 = (R(3.00000) / (R(1.00000) + cfg_exp((((-R(60.0000)) - y_V) / R(20.0000)))));
+    R a_beta_xr2 = (R(1.12000) / (R(1.00000) + cfg_exp(((y_V - R(60.0000)) / R(20.0000)))));
     R a_tau_xr2 = ((R(1.00000) * a_alpha_xr2) * a_beta_xr2);
-    R a_xs_inf = (R(1.00000) / (R(1.00000) + cfg_exp((((-R(5.00000)) - Y(S_V)) / R(14.0000)))));
-    R a_alpha_xs = (R(1100.00) / cfg_sqrt((R(1.00000) + cfg_exp((((-R(10.0000)) - Y(S_V)) / R(6.00000))))));
-    R a_beta_xs = (R(1.00000) / (R(1.00000) + cfg_exp(((Y(S_V) - R(60.0000)) / R(20.0000)))));
+    R a_xs_inf = (R(1.00000) / (R(1.00000) + cfg_exp((((-R(5.00000)) - y_V) / R(14.0000)))));
+    R a_alpha_xs = (R(1100.00) / cfg_sqrt((R(1.00000) + cfg_exp((((-R(10.0000)) - y_V) / R(6.00000))))));
+    R a_beta_xs = (R(1.00000) / (R(1.00000) + cfg_exp(((y_V - R(60.0000)) / R(20.0000)))));
     R a_tau_xs = ((R(1.00000) * a_alpha_xs) * a_beta_xs);
-    R a_m_inf = (R(1.00000) / cfg_ipow<2>((R(1.00000) + cfg_exp((((-R(56.8600)) - Y(S_V)) / R(9.03000))))));
-    R a_alpha_m = (R(1.00000) / (R(1.00000) + cfg_exp((((-R(60.0000)) - Y(S_V)) / R(5.00000)))));
-    R a_beta_m = ((R(0.100000) / (R(1.00000) + cfg_exp(((Y(S_V) + R(35.0000)) / R(5.00000))))) + (R(0.100000) / (R(1.00000) + cfg_exp(((Y(S_V) - R(50.0000)) / R(200.000))))));
+    R a_m_inf = (R(1.00000) / cfg_ipow<2>((R(1.00000) + cfg_exp((((-R(56.8600)) - y_V) / R(9.03000))))));
+    R a_alpha_m = (R(1.00000) / (R(1.00000) + cfg_exp((((-R(60.0000)) - y_V) / R(5.00000)))));
+    R a_beta_m = ((R(0.100000) / (R(1.00000) + cfg_exp(((y_V + R(35.0000)) / R(5.00000))))) + (R(0.100000) / (R(1.00000) + cfg_exp(((y_V - R(50.0000)) / R(200.000))))));
     R a_tau_m = ((R(1.00000) * a_alpha_m) * a_beta_m);
-    R a_h_inf = (R(1.00000) / cfg_ipow<2>((R(1.00000) + cfg_exp(((Y(S_V) + R(71.5500)) / R(7.43000))))));
-    R a_alpha_h = ((Y(S_V) < (-R(40.0000))) ? (R(0.0570000) * cfg_exp(((-(Y(S_V) + R(80.0000))) / R(6.80000)))) : R(0.00000));
-    R a_beta_h = ((Y(S_V) < (-R(40.0000))) ? ((R(2.70000) * cfg_exp((R(0.0790000) * Y(S_V)))) + (R(310000.) * cfg_exp((R(0.348500) * Y(S_V))))) : (R(0.770000) / (R(0.130000) * (R(1.00000) + cfg_exp(((Y(S_V) + R(10.6600)) / (-R(11.1000))))))));
+    R a_h_inf = (R(1.00000) / cfg_ipow<2>((R(1.00000) + cfg_exp(((y_V + R(71.5500)) / R(7.43000))))));
+    R a_alpha_h = ((y_V < (-R(40.0000))) ? (R(0.0570000) * cfg_exp(((-(y_V + R(80.0000))) / R(6.80000)))) : R(0.00000));
+    R a_beta_h = ((y_V < (-R(40.0000))) ? ((R(2.70000) * cfg_exp((R(0.0790000) * y_V))) + (R(310000.) * cfg_exp((R(0.348500) * y_V)))) : (R(0.770000) / (R(0.130000) * (R(1.00000) + cfg_exp(((y_V + R(10.6600)) / (-R(11.1000))))))));
     R a_tau_h = (R(1.00000) / (a_alpha_h + a_beta_h));
-    R a_j_inf = (R(1.00000) / cfg_ipow<2>((R(1.00000) + cfg_exp(((Y(S_V) + R(71.5500)) / R(7.43000))))));
-    R a_alpha_j = ((Y(S_V) < (-R(40.0000))) ? ((((((-R(25428.0)) * cfg_exp((R(0.244400) * Y(S_V)))) - (R(6.94800e-06) * cfg_exp(((-R(0.0439100)) * Y(S_V))))) * (Y(S_V) + R(37.7800))) / R(1.00000)) / (R(1.00000) + cfg_exp((R(0.311000) * (Y(S_V) + R(79.2300)))))) : R(0.00000));
-    R a_beta_j = ((Y(S_V) < (-R(40.0000))) ? ((R(0.0242400) * cfg_exp(((-R(0.0105200)) * Y(S_V)))) / (R(1.00000) + cfg_exp(((-R(0.137800)) * (Y(S_V) + R(40.1400)))))) : ((R(0.600000) * cfg_exp((R(0.0570000) * Y(S_V)))) / (R(1.00000) + cfg_exp(((-R(0.100000)) * (Y(S_V) + R(32.0000)))))));
+    R a_j_inf = (R(1.00000) / cfg_ipow<2>((R(1.00000) + cfg_exp(((y_V + R(71.5500)) / R(7.43000))))));
+    R a_alpha_j = ((y_V < (-R(40.0000))) ? ((((((-R(25428.0)) * cfg_exp((R(0.244400) * y_V))) - (R(6.94800e-06) * cfg_exp(((-R(0.0439100)) * y_V)))) * (y_V + R(37.7800))) / R(1.00000)) / (R(1.00000) + cfg_exp((R(0.311000) * (y_V + R(79.2300)))))) : R(0.00000));
+    R a_beta_j = ((y_V < (-R(40.0000))) ? ((R(0.0242400) * cfg_exp(((-R(0.0105200)) * y_V))) / (R(1.00000) + cfg_exp(((-R(0.137800)) * (y_V + R(40.1400)))))) : ((R(0.600000) * cfg_exp((R(0.0570000) * y_V))) / (R(1.00000) + cfg_exp(((-R(0.100000)) * (y_V + R(32.0000)))))));
     R a_tau_j = (R(1.00000) / (a_alpha_j + a_beta_j));
-    R a_d_inf = (R(1.00000) / (R(1.00000) + cfg_exp((((-R(5.00000)) - Y(S_V)) / R(7.50000)))));
-    R a_alpha_d = ((R(1.40000) / (R(1.00000) + cfg_exp((((-R(35.0000)) - Y(S_V)) / R(13.0000))))) + R(0.250000));
-    R a_gama_fCa = (R(1.40000) / (R(1.00000) + cfg_exp(((Y(S_V) + R(5.00000)) / R(5.00000)))));
-    R a_gamma_d = (R(1.00000) / (R(1.00000) + cfg_exp(((R(50.0000) - Y(S_V)) / R(20.0000)))));
+    R a_d_inf = (R(1.00000) / (R(1.00000) + cfg_exp((((-R(5.00000)) - y_V) / R(7.50000)))));
+    R a_alpha_d = ((R(1.40000) / (R(1.00000) + cfg_exp((((-R(35.0000)) - y_V) / R(13.0000))))) + R(0.250000));
+    R a_gama_fCa = (R(1.40000) / (R(1.00000) + cfg_exp(((y_V + R(5.00000)) / R(5.00000)))));
+    R a_gamma_d = (R(1.00000) / (R(1.00000) + cfg_exp(((R(50.0000) - y_V) / R(20.0000)))));
     R a_tau_d = (((R(1.00000) * a_alpha_d) * a_gama_fCa) + a_gamma_d);
-    R a_alpha_fCa = (R(1.00000) / (R(1.00000) + cfg_ipow<8>((Y(S_Ca_i) / R(0.000325000)))));
-    R a_beta_fCa = (R(0.100000) / (R(1.00000) + cfg_exp(((Y(S_Ca_i) - R(0.000500000)) / R(0.000100000)))));
-    R a_beta_d = (R(0.200000) / (R(1.00000) + cfg_exp(((Y(S_Ca_i) - R(0.000750000)) / R(0.000800000)))));
+    R a_alpha_fCa = (R(1.00000) / (R(1.00000) + cfg_ipow<8>((y_Ca_i / R(0.000325000)))));
+    R a_beta_fCa = (R(0.100000) / (R(1.00000) + cfg_exp(((y_Ca_i - R(0.000500000)) / R(0.000100000)))));
+    R a_beta_d = (R(0.200000) / (R(1.00000) + cfg_exp(((y_Ca_i - R(0.000750000)) / R(0.000800000)))));
     R a_fCa_inf = ((((a_alpha_fCa + a_beta_fCa) + a_beta_d) + R(0.230000)) / R(1.46000));
-    R a_d_fCa = ((a_fCa_inf - Y(S_fCa)) / K(C_tau_fCa));
-    R a_i_NaK = (((((K(C_P_NaK) * K(C_K_o)) / (K(C_K_o) + K(C_K_mk))) * Y(S_Na_i)) / (Y(S_Na_i) + K(C_K_mNa))) / ((R(1.00000) + (R(0.124500) * cfg_exp(((((-R(0.100000)) * Y(S_V)) * K(C_F)) / (K(C_R) * K(C_T)))))) + (R(0.0353000) * cfg_exp((((-Y(S_V)) * K(C_F)) / (K(C_R) * K(C_T)))))));
-    R a_E_Na = (((K(C_R) * K(C_T)) / K(C_F)) * cfg_log((K(C_Na_o) / Y(S_Na_i))));
-    R a_i_Na = ((((K(C_g_Na) * cfg_ipow<3>(Y(S_m))) * Y(S_h)) * Y(S_j)) * (Y(S_V) - a_E_Na));
-    R a_i_b_Na = (K(C_g_bNa) * (Y(S_V) - a_E_Na));
-    R a_i_NaCa = ((K(C_K_NaCa) * (((cfg_exp((((K(C_gamma_NCX) * Y(S_V)) * K(C_F)) / (K(C_R) * K(C_T)))) * cfg_ipow<3>(Y(S_Na_i))) * K(C_Ca_o)) - (((cfg_exp(((((K(C_gamma_NCX) - R(1.00000)) * Y(S_V)) * K(C_F)) / (K(C_R) * K(C_T)))) * cfg_ipow<3>(K(C_Na_o))) * Y(S_Ca_i)) * K(C_alpha_NCX)))) / (((cfg_ipow<3>(K(C_Km_Nai)) + cfg_ipow<3>(K(C_Na_o))) * (K(C_Km_Ca) + K(C_Ca_o))) * (R(1.00000) + (K(C_K_sat) * cfg_exp(((((K(C_gamma_NCX) - R(1.00000)) * Y(S_V)) * K(C_F)) / (K(C_R) * K(C_T))))))));
-    R a_E_K = (((K(C_R) * K(C_T)) / K(C_F)) * cfg_log((K(C_K_o) / Y(S_K_i))));
-    R a_alpha_K1 = (R(0.100000) / (R(1.00000) + cfg_exp((R(0.0600000) * ((Y(S_V) - a_E_K) - R(200.000))))));
-    R a_beta_K1 = (((R(3.00000) * cfg_exp((R(0.000200000) * ((Y(S_V) - a_E_K) + R(100.000))))) + (R(1.00000) * cfg_exp((R(0.100000) * ((Y(S_V) - a_E_K) - R(10.0000)))))) / (R(1.00000) + cfg_exp(((-R(0.500000)) * (Y(S_V) - a_E_K)))));
+    R a_d_fCa = ((a_fCa_inf - y_fCa) / K(C_tau_fCa));
+    R a_i_NaK = (((((K(C_P_NaK) * K(C_K_o)) / (K(C_K_o) + K(C_K_mk))) * y_Na_i) / (y_Na_i + K(C_K_mNa))) / ((R(1.00000) + (R(0.124500) * cfg_exp(((((-R(0.100000)) * y_V) * K(C_F)) / (K(C_R) * K(C_T)))))) + (R(0.0353000) * cfg_exp((((-y_V) * K(C_F)) / (K(C_R) * K(C_T)))))));
+    R a_E_Na = (((K(C_R) * K(C_T)) / K(C_F)) * cfg_log((K(C_Na_o) / y_Na_i)));
+    R a_i_Na = ((((K(C_g_Na) * cfg_ipow<3>(y_m)) * y_h) * y_j) * (y_V - a_E_Na));
+    R a_i_b_Na = (K(C_g_bNa) * (y_V - a_E_Na));
+    R a_i_NaCa = ((K(C_K_NaCa) * (((cfg_exp((((K(C_gamma_NCX) * y_V) * K(C_F)) / (K(C_R) * K(C_T)))) * cfg_ipow<3>(y_Na_i)) * K(C_Ca_o)) - (((cfg_exp(((((K(C_gamma_NCX) - R(1.00000)) * y_V) * K(C_F)) / (K(C_R) * K(C_T)))) * cfg_ipow<3>(K(C_Na_o))) * y_Ca_i) * K(C_alpha_NCX)))) / (((cfg_ipow<3>(K(C_Km_Nai)) + cfg_ipow<3>(K(C_Na_o))) * (K(C_Km_Ca) + K(C_Ca_o))) * (R(1.00000) + (K(C_K_sat) * cfg_exp(((((K(C_gamma_NCX) - R(1.00000)) * y_V) * K(C_F)) / (K(C_R) * K(C_T))))))));
+    R a_E_K = (((K(C_R) * K(C_T)) / K(C_F)) * cfg_log((K(C_K_o) / y_K_i)));
+    R a_alpha_K1 = (R(0.100000) / (R(1.00000) + cfg_exp((R(0.0600000) * ((y_V - a_E_K) - R(200.000))))));
+    R a_beta_K1 = (((R(3.00000) * cfg_exp((R(0.000200000) * ((y_V - a_E_K) + R(100.000))))) + (R(1.00000) * cfg_exp((R(0.100000) * ((y_V - a_E_K) - R(10.0000)))))) / (R(1.00000) + cfg_exp(((-R(0.500000)) * (y_V - a_E_K)))));
     R a_xK1_inf = (a_alpha_K1 / (a_alpha_K1 + a_beta_K1));
-    R a_i_K1 = (((K(C_g_K1) * a_xK1_inf) * cfg_sqrt((K(C_K_o) / R(5.40000)))) * (Y(S_V) - a_E_K));
-    R a_i_to = (((K(C_g_to) * Y(S_r)) * Y(S_s)) * (Y(S_V) - a_E_K));
-    R a_i_Kr = ((((K(C_g_Kr) * cfg_sqrt((K(C_K_o) / R(5.40000)))) * Y(S_Xr1)) * Y(S_Xr2)) * (Y(S_V) - a_E_K));
-    R a_E_Ks = (((K(C_R) * K(C_T)) / K(C_F)) * cfg_log(((K(C_K_o) + (K(C_P_kna) * K(C_Na_o))) / (Y(S_K_i) + (K(C_P_kna) * Y(S_Na_i))))));
-    R a_i_Ks = ((K(C_g_Ks) * cfg_ipow<2>(Y(S_Xs))) * (Y(S_V) - a_E_Ks));
-    R a_i_CaL = (((((((((K(C_g_CaL) * Y(S_d)) * Y(S_f)) * Y(S_fCa)) * R(4.00000)) * Y(S_V)) * cfg_ipow<2>(K(C_F))) / (K(C_R) * K(C_T))) * ((Y(S_Ca_i) * cfg_exp((((R(2.00000) * Y(S_V)) * K(C_F)) / (K(C_R) * K(C_T))))) - (R(0.341000) * K(C_Ca_o)))) / (cfg_exp((((R(2.00000) * Y(S_V)) * K(C_F)) / (K(C_R) * K(C_T)))) - R(1.00000)));
-    R a_E_Ca = ((((R(0.500000) * K(C_R)) * K(C_T)) / K(C_F)) * cfg_log((K(C_Ca_o) / Y(S_Ca_i))));
-    R a_i_b_Ca = (K(C_g_bCa) * (Y(S_V) - a_E_Ca));
-    R a_i_p_K = ((K(C_g_pK) * (Y(S_V) - a_E_K)) / (R(1.00000) + cfg_exp(((R(25.0000) - Y(S_V)) / R(5.98000)))));
-    R a_i_p_Ca = ((K(C_g_pCa) * Y(S_Ca_i)) / (Y(S_Ca_i) + K(C_K_pCa)));
-    R a_i_rel = (((((K(C_a_rel) * cfg_ipow<2>(Y(S_Ca_SR))) / (cfg_ipow<2>(K(C_b_rel)) + cfg_ipow<2>(Y(S_Ca_SR)))) + K(C_c_rel)) * Y(S_d)) * Y(S_g));
-    R a_i_up = (K(C_Vmax_up) / (R(1.00000) + (cfg_ipow<2>(K(C_K_up)) / cfg_ipow<2>(Y(S_Ca_i)))));
-    R a_i_leak = (K(C_V_leak) * (Y(S_Ca_SR) - Y(S_Ca_i)));
+    R a_i_K1 = (((K(C_g_K1) * a_xK1_inf) * cfg_sqrt((K(C_K_o) / R(5.40000)))) * (y_V - a_E_K));
+    R a_i_to = (((K(C_g_to) * y_r) * y_s) * (y_V - a_E_K));
+    R a_i_Kr = ((((K(C_g_Kr) * cfg_sqrt((K(C_K_o) / R(5.40000)))) * y_Xr1) * y_Xr2) * (y_V - a_E_K));
+    R a_E_Ks = (((K(C_R) * K(C_T)) / K(C_F)) * cfg_log(((K(C_K_o) + (K(C_P_kna) * K(C_Na_o))) / (y_K_i + (K(C_P_kna) * y_Na_i)))));
+    R a_i_Ks = ((K(C_g_Ks) * cfg_ipow<2>(y_Xs)) * (y_V - a_E_Ks));
+    R a_i_CaL = (((((((((K(C_g_CaL) * y_d) * y_f) * y_fCa) * R(4.00000)) * y_V) * cfg_ipow<2>(K(C_F))) / (K(C_R) * K(C_T))) * ((y_Ca_i * cfg_exp((((R(2.00000) * y_V) * K(C_F)) / (K(C_R) * K(C_T))))) - (R(0.341000) * K(C_Ca_o)))) / (cfg_exp((((R(2.00000) * y_V) * K(C_F)) / (K(C_R) * K(C_T)))) - R(1.00000)));
+    R a_E_Ca = ((((R(0.500000) * K(C_R)) * K(C_T)) / K(C_F)) * cfg_log((K(C_Ca_o) / y_Ca_i)));
+    R a_i_b_Ca = (K(C_g_bCa) * (y_V - a_E_Ca));
+    R a_i_p_K = ((K(C_g_pK) * (y_V - a_E_K)) / (R(1.00000) + cfg_exp(((R(25.0000) - y_V) / R(5.98000)))));
+    R a_i_p_Ca = ((K(C_g_pCa) * y_Ca_i) / (y_Ca_i + K(C_K_pCa)));
+    R a_i_rel = (((((K(C_a_rel) * cfg_ipow<2>(y_Ca_SR)) / (cfg_ipow<2>(K(C_b_rel)) + cfg_ipow<2>(y_Ca_SR))) + K(C_c_rel)) * y_d) * y_g);
+    R a_i_up = (K(C_Vmax_up) / (R(1.00000) + (cfg_ipow<2>(K(C_K_up)) / cfg_ipow<2>(y_Ca_i))));
+    R a_i_leak = (K(C_V_leak) * (y_Ca_SR - y_Ca_i));
     R a_ddt_Ca_i_total = ((((((-(((a_i_CaL + a_i_b_Ca) + a_i_p_Ca) - (R(2.00000) * a_i_NaCa))) / ((R(2.00000) * K(C_V_c)) * K(C_F))) * K(C_Cm)) + a_i_leak) - a_i_up) + a_i_rel);
-    R a_f_JCa_i_free = (R(1.00000) / (R(1.00000) + ((K(C_Buf_c) * K(C_K_buf_c)) / cfg_ipow<2>((Y(S_Ca_i) + K(C_K_buf_c))))));
+    R a_f_JCa_i_free = (R(1.00000) / (R(1.00000) + ((K(C_Buf_c) * K(C_K_buf_c)) / cfg_ipow<2>((y_Ca_i + K(C_K_buf_c))))));
     R a_ddt_Ca_sr_total = ((K(C_V_c) / K(C_V_sr)) * (a_i_up - (a_i_rel + a_i_leak)));
-    R a_f_JCa_sr_free = (R(1.00000) / (R(1.00000) + ((K(C_Buf_sr) * K(C_K_buf_sr)) / cfg_ipow<2>((Y(S_Ca_SR) + K(C_K_buf_sr))))));
+    R a_f_JCa_sr_free = (R(1.00000) / (R(1.00000) + ((K(C_Buf_sr) * K(C_K_buf_sr)) / cfg_ipow<2>((y_Ca_SR + K(C_K_buf_sr))))));
     R a_Iion_cm = (((((((((((a_i_K1 + a_i_to) + a_i_Kr) + a_i_Ks) + a_i_CaL) + a_i_NaK) + a_i_Na) + a_i_b_Na) + a_i_NaCa) + a_i_b_Ca) + a_i_p_K) + a_i_p_Ca);
     R a_Istim = (SOLVE_VM ? R(cfg_stimulus_current<double>(t, stim)) : R(0));
-    a_m_inf = (R(1.00000) / cfg_ipow<2>((R(1.00000) + cfg_exp((((-R(56.8600)) - Y(S_V)) / R(9.03000))))));
-    a_alpha_m = (R(1.00000) / (R(1.00000) + cfg_exp((((-R(60.0000)) - Y(S_V)) / R(5.00000)))));
-    a_beta_m = ((R(0.100000) / (R(1.00000) + cfg_exp(((Y(S_V) + R(35.0000)) / R(5.00000))))) + (R(0.100000) / (R(1.00000) + cfg_exp(((Y(S_V) - R(50.0000)) / R(200.000))))));
+    a_m_inf = (R(1.00000) / cfg_ipow<2>((R(1.00000) + cfg_exp((((-R(56.8600)) - y_V) / R(9.03000))))));
+    a_alpha_m = (R(1.00000) / (R(1.00000) + cfg_exp((((-R(60.0000)) - y_V) / R(5.00000)))));
+    a_beta_m = ((R(0.100000) / (R(1.00000) + cfg_exp(((y_V + R(35.0000)) / R(5.00000))))) + (R(0.100000) / (R(1.00000) + cfg_exp(((y_V - R(50.0000)) / R(200.000))))));
     a_tau_m = ((R(1.00000) * a_alpha_m) * a_beta_m);
-    dydt[S_m] = ((a_m_inf - Y(S_m)) / a_tau_m);
-    a_h_inf = (R(1.00000) / cfg_ipow<2>((R(1.00000) + cfg_exp(((Y(S_V) + R(71.5500)) / R(7.43000))))));
-    a_alpha_h = ((Y(S_V) < (-R(40.0000))) ? (R(0.0570000) * cfg_exp(((-(Y(S_V) + R(80.0000))) / R(6.80000)))) : R(0.00000));
-    a_beta_h = ((Y(S_V) < (-R(40.0000))) ? ((R(2.70000) * cfg_exp((R(0.0790000) * Y(S_V)))) + (R(310000.) * cfg_exp((R(0.348500) * Y(S_V))))) : (R(0.770000) / (R(0.130000) * (R(1.00000) + cfg_exp(((Y(S_V) + R(10.6600)) / (-R(11.1000))))))));
+    dydt[S_m] = ((a_m_inf - y_m) / a_tau_m);
+    a_h_inf = (R(1.00000) / cfg_ipow<2>((R(1.00000) + cfg_exp(((y_V + R(71.5500)) / R(7.43000))))));
+    a_alpha_h = ((y_V < (-R(40.0000))) ? (R(0.0570000) * cfg_exp(((-(y_V + R(80.0000))) / R(6.80000)))) : R(0.00000));
+    a_beta_h = ((y_V < (-R(40.0000))) ? ((R(2.70000) * cfg_exp((R(0.0790000) * y_V))) + (R(310000.) * cfg_exp((R(0.348500) * y_V)))) : (R(0.770000) / (R(0.130000) * (R(1.00000) + cfg_exp(((y_V + R(10.6600)) / (-R(11.1000))))))));
     a_tau_h = (R(1.00000) / (a_alpha_h + a_beta_h));
-    dydt[S_h] = ((a_h_inf - Y(S_h)) / a_tau_h);
-    a_j_inf = (R(1.00000) / cfg_ipow<2>((R(1.00000) + cfg_exp(((Y(S_V) + R(71.5500)) / R(7.43000))))));
-    a_alpha_j = ((Y(S_V) < (-R(40.0000))) ? ((((((-R(25428.0)) * cfg_exp((R(0.244400) * Y(S_V)))) - (R(6.94800e-06) * cfg_exp(((-R(0.0439100)) * Y(S_V))))) * (Y(S_V) + R(37.7800))) / R(1.00000)) / (R(1.00000) + cfg_exp((R(0.311000) * (Y(S_V) + R(79.2300)))))) : R(0.00000));
-    a_beta_j = ((Y(S_V) < (-R(40.0000))) ? ((R(0.0242400) * cfg_exp(((-R(0.0105200)) * Y(S_V)))) / (R(1.00000) + cfg_exp(((-R(0.137800)) * (Y(S_V) + R(40.1400)))))) : ((R(0.600000) * cfg_exp((R(0.0570000) * Y(S_V)))) / (R(1.00000) + cfg_exp(((-R(0.100000)) * (Y(S_V) + R(32.0000)))))));
+    dydt[S_h] = ((a_h_inf - y_h) / a_tau_h);
+    a_j_inf = (R(1.00000) / cfg_ipow<2>((R(1.00000) + cfg_exp(((y_V + R(71.5500)) / R(7.43000))))));
+    a_alpha_j = ((y_V < (-R(40.0000))) ? ((((((-R(25428.0)) * cfg_exp((R(0.244400) * y_V))) - (R(6.94800e-06) * cfg_exp(((-R(0.0439100)) * y_V)))) * (y_V + R(37.7800))) / R(1.00000)) / (R(1.00000) + cfg_exp((R(0.311000) * (y_V + R(79.2300)))))) : R(0.00000));
+    a_beta_j = ((y_V < (-R(40.0000))) ? ((R(0.0242400) * cfg_exp(((-R(0.0105200)) * y_V))) / (R(1.00000) + cfg_exp(((-R(0.137800)) * (y_V + R(40.1400)))))) : ((R(0.600000) * cfg_exp((R(0.0570000) * y_V))) / (R(1.00000) + cfg_exp(((-R(0.100000)) * (y_V + R(32.0000)))))));
     a_tau_j = (R(1.00000) / (a_alpha_j + a_beta_j));
-    dydt[S_j] = ((a_j_inf - Y(S_j)) / a_tau_j);
-    a_d_inf = (R(1.00000) / (R(1.00000) + cfg_exp((((-R(5.00000)) - Y(S_V)) / R(7.50000)))));
-    a_alpha_d = ((R(1.40000) / (R(1.00000) + cfg_exp((((-R(35.0000)) - Y(S_V)) / R(13.0000))))) + R(0.250000));
-    a_gama_fCa = (R(1.40000) / (R(1.00000) + cfg_exp(((Y(S_V) + R(5.00000)) / R(5.00000)))));
-    a_gamma_d = (R(1.00000) / (R(1.00000) + cfg_exp(((R(50.0000) - Y(S_V)) / R(20.0000)))));
+    dydt[S_j] = ((a_j_inf - y_j) / a_tau_j);
+    a_d_inf = (R(1.00000) / (R(1.00000) + cfg_exp((((-R(5.00000)) - y_V) / R(7.50000)))));
+    a_alpha_d = ((R(1.40000) / (R(1.00000) + cfg_exp((((-R(35.0000)) - y_V) / R(13.0000))))) + R(0.250000));
+    a_gama_fCa = (R(1.40000) / (R(1.00000) + cfg_exp(((y_V + R(5.00000)) / R(5.00000)))));
+    a_gamma_d = (R(1.00000) / (R(1.00000) + cfg_exp(((R(50.0000) - y_V) / R(20.0000)))));
     a_tau_d = (((R(1.00000) * a_alpha_d) * a_gama_fCa) + a_gamma_d);
-    dydt[S_d] = ((a_d_inf - Y(S_d)) / a_tau_d);
-    a_f_inf = (R(1.00000) / (R(1.00000) + cfg_exp(((Y(S_V) + R(20.0000)) / R(7.00000)))));
-    a_tau_f = (((R(1125.00) * cfg_exp(((-cfg_ipow<2>((Y(S_V) + R(27.0000)))) / R(240.000)))) + R(80.0000)) + (R(165.000) / (R(1.00000) + cfg_exp(((R(25.0000) - Y(S_V)) / R(10.0000))))));
-    dydt[S_f] = ((a_f_inf - Y(S_f)) / a_tau_f);
-    a_alpha_fCa = (R(1.00000) / (R(1.00000) + cfg_ipow<8>((Y(S_Ca_i) / R(0.000325000)))));
-    a_beta_fCa = (R(0.100000) / (R(1.00000) + cfg_exp(((Y(S_Ca_i) - R(0.000500000)) / R(0.000100000)))));
-    a_beta_d = (R(0.200000) / (R(1.00000) + cfg_exp(((Y(S_Ca_i) - R(0.000750000)) / R(0.000800000)))));
+    dydt[S_d] = ((a_d_inf - y_d) / a_tau_d);
+    a_f_inf = (R(1.00000) / (R(1.00000) + cfg_exp(((y_V + R(20.0000)) / R(7.00000)))));
+    a_tau_f = (((R(1125.00) * cfg_exp(((-cfg_ipow<2>((y_V + R(27.0000)))) / R(240.000)))) + R(80.0000)) + (R(165.000) / (R(1.00000) + cfg_exp(((R(25.0000) - y_V) / R(10.0000))))));
+    dydt[S_f] = ((a_f_inf - y_f) / a_tau_f);
+    a_alpha_fCa = (R(1.00000) / (R(1.00000) + cfg_ipow<8>((y_Ca_i / R(0.000325000)))));
+    a_beta_fCa = (R(0.100000) / (R(1.00000) + cfg_exp(((y_Ca_i - R(0.000500000)) / R(0.000100000)))));
+    a_beta_d = (R(0.200000) / (R(1.00000) + cfg_exp(((y_Ca_i - R(0.000750000)) / R(0.000800000)))));
     a_fCa_inf = ((((a_alpha_fCa + a_beta_fCa) + a_beta_d) + R(0.230000)) / R(1.46000));
-    a_d_fCa = ((a_fCa_inf - Y(S_fCa)) / K(C_tau_fCa));
-    dydt[S_fCa] = (((a_fCa_inf > Y(S_fCa)) && (Y(S_V) > (-R(60.0000)))) ? R(0.00000) : a_d_fCa);
-    a_s_inf = ((tissue == 1) ? (R(1.00000) / (R(1.00000) + cfg_exp(((Y(S_V) + R(20.0000)) / R(5.00000))))) : (R(1.10000) / (R(1.00000) + cfg_exp(((Y(S_V) + R(28.0000)) / R(6.00000))))));
-    a_tau_s = ((tissue == 1) ? (((R(85.0000) * cfg_exp(((-cfg_ipow<2>((Y(S_V) + R(45.0000)))) / R(320.000)))) + (R(5.00000) / (R(1.00000) + cfg_exp(((Y(S_V) - R(20.0000)) / R(5.00000)))))) + R(3.00000)) : ((R(1000.0000) * cfg_exp(((-cfg_ipow<2>((Y(S_V) + R(67.0000)))) / R(1000.000)))) + R(8.00000)));
-    dydt[S_s] = ((a_s_inf - Y(S_s)) / a_tau_s);
-    a_r_inf = (R(1.00000) / (R(1.00000) + cfg_exp(((R(20.0000) - Y(S_V)) / R(6.00000)))));
-    a_tau_r = ((R(9.50000) * cfg_exp(((-cfg_ipow<2>((Y(S_V) + R(40.0000)))) / R(1800.00)))) + R(0.800000));
-    dydt[S_r] = ((a_r_inf - Y(S_r)) / a_tau_r);
-    a_xr1_inf = (R(1.00000) / (R(1.00000) + cfg_exp((((-R(26.0000)) - Y(S_V)) / R(7.00000)))));
-    a_alpha_xr1 = (R(450.000) / (R(1.00000) + cfg_exp((((-R(45.0000)) - Y(S_V)) / R(10.0000)))));
-    a_beta_xr1 = (R(6.00000) / (R(1.00000) + cfg_exp(((Y(S_V) + R(30.0000)) / R(11.5000)))));
+    a_d_fCa = ((a_fCa_inf - y_fCa) / K(C_tau_fCa));
+    dydt[S_fCa] = (((a_fCa_inf > y_fCa) && (y_V > (-R(60.0000)))) ? R(0.00000) : a_d_fCa);
+    a_s_inf = ((tissue == 1) ? (R(1.00000) / (R(1.00000) + cfg_exp(((y_V + R(20.0000)) / R(5.00000))))) : (R(1.10000) / (R(1.00000) + cfg_exp(((y_V + R(28.0000)) / R(6.00000))))));
+    a_tau_s = ((tissue == 1) ? (((R(85.0000) * cfg_exp(((-cfg_ipow<2>((y_V + R(45.0000)))) / R(320.000)))) + (R(5.00000) / (R(1.00000) + cfg_exp(((y_V - R(20.0000)) / R(5.00000)))))) + R(3.00000)) : ((R(1000.0000) * cfg_exp(((-cfg_ipow<2>((y_V + R(67.0000)))) / R(1000.000)))) + R(8.00000)));
+    dydt[S_s] = ((a_s_inf - y_s) / a_tau_s);
+    a_r_inf = (R(1.00000) / (R(1.00000) + cfg_exp(((R(20.0000) - y_V) / R(6.00000)))));
+    a_tau_r = ((R(9.50000) * cfg_exp(((-cfg_ipow<2>((y_V + R(40.0000)))) / R(1800.00)))) + R(0.800000));
+    dydt[S_r] = ((a_r_inf - y_r) / a_tau_r);
+    a_xr1_inf = (R(1.00000) / (R(1.00000) + cfg_exp((((-R(26.0000)) - y_V) / R(7.00000)))));
+    a_alpha_xr1 = (R(450.000) / (R(1.00000) + cfg_exp((((-R(45.0000)) - y_V) / R(10.0000)))));
+    a_beta_xr1 = (R(6.00000) / (R(1.00000) + cfg_exp(((y_V + R(30.0000)) / R(11.5000)))));
     a_tau_xr1 = ((R(1.00000) * a_alpha_xr1) * a_beta_xr1);
-    dydt[S_Xr1] = ((a_xr1_inf - Y(S_Xr1)) / a_tau_xr1);
-    a_xr2_inf = (R(1.00000) / (R(1.00000) + cfg_exp(((Y(S_V) + R(88.0000)) / R(24.0000)))));
-    a_alpha_xr2 = (R(3.00000) / (R(1.00000) + cfg_exp((((-R(60.0000)) - Y(S_V)) / R(20.0000)))));
-    a_beta_xr2 = (R(1.12000) / (R(1.00000) + cfg_exp(((Y(S_V) - R(60.0000)) / R(20.0000)))));
+    dydt[S_Xr1] = ((a_xr1_inf - y_Xr1) / a_tau_xr1);
+    a_xr2_inf = (R(1.00000) / (R(1.00000) + cfg_exp(((y_V + R(88.0000)) / R(24.0000)))));
+    a_alpha_xr2 = (R(3.00000) / (R(1.00000) + cfg_exp((((-R(60.0000)) - y_V) / R(20.0000)))));
+    a_beta_xr2 = (R(1.12000) / (R(1.00000) + cfg_exp(((y_V - R(60.0000)) / R(20.0000)))));
     a_tau_xr2 = ((R(1.00000) * a_alpha_xr2) * a_beta_xr2);
-    dydt[S_Xr2] = ((a_xr2_inf - Y(S_Xr2)) / a_tau_xr2);
-    a_xs_inf = (R(1.00000) / (R(1.00000) + cfg_exp((((-R(5.00000)) - Y(S_V)) / R(14.0000)))));
-    a_alpha_xs = (R(1100.00) / cfg_sqrt((R(1.00000) + cfg_exp((((-R(10.0000)) - Y(S_V)) / R(6.00000))))));
-    a_beta_xs = (R(1.00000) / (R(1.00000) + cfg_exp(((Y(S_V) - R(60.0000)) / R(20.0000)))));
+    dydt[S_Xr2] = ((a_xr2_inf - y_Xr2) / a_tau_xr2);
+    a_xs_inf = (R(1.00000) / (R(1.00000) + cfg_exp((((-R(5.00000)) - y_V) / R(14.0000)))));
+    a_alpha_xs = (R(1100.00) / cfg_sqrt((R(1.00000) + cfg_exp((((-R(10.0000)) - y_V) / R(6.00000))))));
+    a_beta_xs = (R(1.00000) / (R(1.00000) + cfg_exp(((y_V - R(60.0000)) / R(20.0000)))));
     a_tau_xs = ((R(1.00000) * a_alpha_xs) * a_beta_xs);
-    dydt[S_Xs] = ((a_xs_inf - Y(S_Xs)) / a_tau_xs);
-    a_g_inf = ((Y(S_Ca_i) < R(0.000350000)) ? (R(1.00000) / (R(1.00000) + cfg_ipow<6>((Y(S_Ca_i) / R(0.000350000))))) : (R(1.00000) / (R(1.00000) + cfg_ipow<16>((Y(S_Ca_i) / R(0.000350000))))));
-    a_d_g = ((a_g_inf - Y(S_g)) / K(C_tau_g));
-    dydt[S_g] = (((a_g_inf > Y(S_g)) && (Y(S_V) > (-R(60.0000)))) ? R(0.00000) : a_d_g);
-    a_i_NaK = (((((K(C_P_NaK) * K(C_K_o)) / (K(C_K_o) + K(C_K_mk))) * Y(S_Na_i)) / (Y(S_Na_i) + K(C_K_mNa))) / ((R(1.00000) + (R(0.124500) * cfg_exp(((((-R(0.100000)) * Y(S_V)) * K(C_F)) / (K(C_R) * K(C_T)))))) + (R(0.0353000) * cfg_exp((((-Y(S_V)) * K(C_F)) / (K(C_R) * K(C_T)))))));
-    a_E_Na = (((K(C_R) * K(C_T)) / K(C_F)) * cfg_log((K(C_Na_o) / Y(S_Na_i))));
-    a_i_Na = ((((K(C_g_Na) * cfg_ipow<3>(Y(S_m))) * Y(S_h)) * Y(S_j)) * (Y(S_V) - a_E_Na));
-    a_i_b_Na = (K(C_g_bNa) * (Y(S_V) - a_E_Na));
-    a_i_NaCa = ((K(C_K_NaCa) * (((cfg_exp((((K(C_gamma_NCX) * Y(S_V)) * K(C_F)) / (K(C_R) * K(C_T)))) * cfg_ipow<3>(Y(S_Na_i))) * K(C_Ca_o)) - (((cfg_exp(((((K(C_gamma_NCX) - R(1.00000)) * Y(S_V)) * K(C_F)) / (K(C_R) * K(C_T)))) * cfg_ipow<3>(K(C_Na_o))) * Y(S_Ca_i)) * K(C_alpha_NCX)))) / (((cfg_ipow<3>(K(C_Km_Nai)) + cfg_ipow<3>(K(C_Na_o))) * (K(C_Km_Ca) + K(C_Ca_o))) * (R(1.00000) + (K(C_K_sat) * cfg_exp(((((K(C_gamma_NCX) - R(1.00000)) * Y(S_V)) * K(C_F)) / (K(C_R) * K(C_T))))))));
+    dydt[S_Xs] = ((a_xs_inf - y_Xs) / a_tau_xs);
+    a_g_inf = ((y_Ca_i < R(0.000350000)) ? (R(1.00000) / (R(1.00000) + cfg_ipow<6>((y_Ca_i / R(0.000350000))))) : (R(1.00000) / (R(1.00000) + cfg_ipow<16>((y_Ca_i / R(0.000350000))))));
+    a_d_g = ((a_g_inf - y_g) / K(C_tau_g));
+    dydt[S_g] = (((a_g_inf > y_g) && (y_V > (-R(60.0000)))) ? R(0.00000) : a_d_g);
+    a_i_NaK = (((((K(C_P_NaK) * K(C_K_o)) / (K(C_K_o) + K(C_K_mk))) * y_Na_i) / (y_Na_i + K(C_K_mNa))) / ((R(1.00000) + (R(0.124500) * cfg_exp(((((-R(0.100000)) * y_V) * K(C_F)) / (K(C_R) * K(C_T)))))) + (R(0.0353000) * cfg_exp((((-y_V) * K(C_F)) / (K(C_R) * K(C_T)))))));
+    a_E_Na = (((K(C_R) * K(C_T)) / K(C_F)) * cfg_log((K(C_Na_o) / y_Na_i)));
+    a_i_Na = ((((K(C_g_Na) * cfg_ipow<3>(y_m)) * y_h) * y_j) * (y_V - a_E_Na));
+    a_i_b_Na = (K(C_g_bNa) * (y_V - a_E_Na));
+    a_i_NaCa = ((K(C_K_NaCa) * (((cfg_exp((((K(C_gamma_NCX) * y_V) * K(C_F)) / (K(C_R) * K(C_T)))) * cfg_ipow<3>(y_Na_i)) * K(C_Ca_o)) - (((cfg_exp(((((K(C_gamma_NCX) - R(1.00000)) * y_V) * K(C_F)) / (K(C_R) * K(C_T)))) * cfg_ipow<3>(K(C_Na_o))) * y_Ca_i) * K(C_alpha_NCX)))) / (((cfg_ipow<3>(K(C_Km_Nai)) + cfg_ipow<3>(K(C_Na_o))) * (K(C_Km_Ca) + K(C_Ca_o))) * (R(1.00000) + (K(C_K_sat) * cfg_exp(((((K(C_gamma_NCX) - R(1.00000)) * y_V) * K(C_F)) / (K(C_R) * K(C_T))))))));
     dydt[S_Na_i] = (((-(((a_i_Na + a_i_b_Na) + (R(3.00000) * a_i_NaK)) + (R(3.00000) * a_i_NaCa))) * K(C_Cm)) / (K(C_V_c) * K(C_F)));
-    a_E_K = (((K(C_R) * K(C_T)) / K(C_F)) * cfg_log((K(C_K_o) / Y(S_K_i))));
-    a_alpha_K1 = (R(0.100000) / (R(1.00000) + cfg_exp((R(0.0600000) * ((Y(S_V) - a_E_K) - R(200.000))))));
-    a_beta_K1 = (((R(3.00000) * cfg_exp((R(0.000200000) * ((Y(S_V) - a_E_K) + R(100.000))))) + (R(1.00000) * cfg_exp((R(0.100000) * ((Y(S_V) - a_E_K) - R(10.0000)))))) / (R(1.00000) + cfg_exp(((-R(0.500000)) * (Y(S_V) - a_E_K)))));
+    a_E_K = (((K(C_R) * K(C_T)) / K(C_F)) * cfg_log((K(C_K_o) / y_K_i)));
+    a_alpha_K1 = (R(0.100000) / (R(1.00000) + cfg_exp((R(0.0600000) * ((y_V - a_E_K) - R(200.000))))));
+    a_beta_K1 = (((R(3.00000) * cfg_exp((R(0.000200000) * ((y_V - a_E_K) + R(100.000))))) + (R(1.00000) * cfg_exp((R(0.100000) * ((y_V - a_E_K) - R(10.0000)))))) / (R(1.00000) + cfg_exp(((-R(0.500000)) * (y_V - a_E_K)))));
     a_xK1_inf = (a_alpha_K1 / (a_alpha_K1 + a_beta_K1));
-    a_i_K1 = (((K(C_g_K1) * a_xK1_inf) * cfg_sqrt((K(C_K_o) / R(5.40000)))) * (Y(S_V) - a_E_K));
-    a_i_to = (((K(C_g_to) * Y(S_r)) * Y(S_s)) * (Y(S_V) - a_E_K));
-    a_i_Kr = ((((K(C_g_Kr) * cfg_sqrt((K(C_K_o) / R(5.40000)))) * Y(S_Xr1)) * Y(S_Xr2)) * (Y(S_V) - a_E_K));
-    a_E_Ks = (((K(C_R) * K(C_T)) / K(C_F)) * cfg_log(((K(C_K_o) + (K(C_P_kna) * K(C_Na_o))) / (Y(S_K_i) + (K(C_P_kna) * Y(S_Na_i))))));
-    a_i_Ks = ((K(C_g_Ks) * cfg_ipow<2>(Y(S_Xs))) * (Y(S_V) - a_E_Ks));
-    a_i_CaL = (((((((((K(C_g_CaL) * Y(S_d)) * Y(S_f)) * Y(S_fCa)) * R(4.00000)) * Y(S_V)) * cfg_ipow<2>(K(C_F))) / (K(C_R) * K(C_T))) * ((Y(S_Ca_i) * cfg_exp((((R(2.00000) * Y(S_V)) * K(C_F)) / (K(C_R) * K(C_T))))) - (R(0.341000) * K(C_Ca_o)))) / (cfg_exp((((R(2.00000) * Y(S_V)) * K(C_F)) / (K(C_R) * K(C_T)))) - R(1.00000)));
-    a_E_Ca = ((((R(0.500000) * K(C_R)) * K(C_T)) / K(C_F)) * cfg_log((K(C_Ca_o) / Y(S_Ca_i))));
-    a_i_b_Ca = (K(C_g_bCa) * (Y(S_V) - a_E_Ca));
-    a_i_p_K = ((K(C_g_pK) * (Y(S_V) - a_E_K)) / (R(1.00000) + cfg_exp(((R(25.0000) - Y(S_V)) / R(5.98000)))));
-    a_i_p_Ca = ((K(C_g_pCa) * Y(S_Ca_i)) / (Y(S_Ca_i) + K(C_K_pCa)));
+    a_i_K1 = (((K(C_g_K1) * a_xK1_inf) * cfg_sqrt((K(C_K_o) / R(5.40000)))) * (y_V - a_E_K));
+    a_i_to = (((K(C_g_to) * y_r) * y_s) * (y_V - a_E_K));
+    a_i_Kr = ((((K(C_g_Kr) * cfg_sqrt((K(C_K_o) / R(5.40000)))) * y_Xr1) * y_Xr2) * (y_V - a_E_K));
+    a_E_Ks = (((K(C_R) * K(C_T)) / K(C_F)) * cfg_log(((K(C_K_o) + (K(C_P_kna) * K(C_Na_o))) / (y_K_i + (K(C_P_kna) * y_Na_i)))));
+    a_i_Ks = ((K(C_g_Ks) * cfg_ipow<2>(y_Xs)) * (y_V - a_E_Ks));
+    a_i_CaL = (((((((((K(C_g_CaL) * y_d) * y_f) * y_fCa) * R(4.00000)) * y_V) * cfg_ipow<2>(K(C_F))) / (K(C_R) * K(C_T))) * ((y_Ca_i * cfg_exp((((R(2.00000) * y_V) * K(C_F)) / (K(C_R) * K(C_T))))) - (R(0.341000) * K(C_Ca_o)))) / (cfg_exp((((R(2.00000) * y_V) * K(C_F)) / (K(C_R) * K(C_T)))) - R(1.00000)));
+    a_E_Ca = ((((R(0.500000) * K(C_R)) * K(C_T)) / K(C_F)) * cfg_log((K(C_Ca_o) / y_Ca_i)));
+    a_i_b_Ca = (K(C_g_bCa) * (y_V - a_E_Ca));
+    a_i_p_K = ((K(C_g_pK) * (y_V - a_E_K)) / (R(1.00000) + cfg_exp(((R(25.0000) - y_V) / R(5.98000)))));
+    a_i_p_Ca = ((K(C_g_pCa) * y_Ca_i) / (y_Ca_i + K(C_K_pCa)));
     a_Iion_cm = (((((((((((a_i_K1 + a_i_to) + a_i_Kr) + a_i_Ks) + a_i_CaL) + a_i_NaK) + a_i_Na) + a_i_b_Na) + a_i_NaCa) + a_i_b_Ca) + a_i_p_K) + a_i_p_Ca);
     a_Istim = (SOLVE_VM ? R(cfg_stimulus_current<double>(t, stim)) : R(0));
     dydt[S_V] = R(0.0);
@@ -510,14 +577,14 @@ __device__ __forceinline__ R iion(double t, const YS& Y, const KS& K, int tissue
         dydt[S_V] = ((-a_Iion_cm) - a_Istim);
     }
     dydt[S_K_i] = (((-((((((a_i_K1 + a_i_to) + a_i_Kr) + a_i_Ks) + a_i_p_K) + a_Istim) - (R(2.00000) * a_i_NaK))) * K(C_Cm)) / (K(C_V_c) * K(C_F)));
-    a_i_rel = (((((K(C_a_rel) * cfg_ipow<2>(Y(S_Ca_SR))) / (cfg_ipow<2>(K(C_b_rel)) + cfg_ipow<2>(Y(S_Ca_SR)))) + K(C_c_rel)) * Y(S_d)) * Y(S_g));
-    a_i_up = (K(C_Vmax_up) / (R(1.00000) + (cfg_ipow<2>(K(C_K_up)) / cfg_ipow<2>(Y(S_Ca_i)))));
-    a_i_leak = (K(C_V_leak) * (Y(S_Ca_SR) - Y(S_Ca_i)));
+    a_i_rel = (((((K(C_a_rel) * cfg_ipow<2>(y_Ca_SR)) / (cfg_ipow<2>(K(C_b_rel)) + cfg_ipow<2>(y_Ca_SR))) + K(C_c_rel)) * y_d) * y_g);
+    a_i_up = (K(C_Vmax_up) / (R(1.00000) + (cfg_ipow<2>(K(C_K_up)) / cfg_ipow<2>(y_Ca_i))));
+    a_i_leak = (K(C_V_leak) * (y_Ca_SR - y_Ca_i));
     a_ddt_Ca_i_total = ((((((-(((a_i_CaL + a_i_b_Ca) + a_i_p_Ca) - (R(2.00000) * a_i_NaCa))) / ((R(2.00000) * K(C_V_c)) * K(C_F))) * K(C_Cm)) + a_i_leak) - a_i_up) + a_i_rel);
-    a_f_JCa_i_free = (R(1.00000) / (R(1.00000) + ((K(C_Buf_c) * K(C_K_buf_c)) / cfg_ipow<2>((Y(S_Ca_i) + K(C_K_buf_c))))));
+    a_f_JCa_i_free = (R(1.00000) / (R(1.00000) + ((K(C_Buf_c) * K(C_K_buf_c)) / cfg_ipow<2>((y_Ca_i + K(C_K_buf_c))))));
     dydt[S_Ca_i] = (a_ddt_Ca_i_total * a_f_JCa_i_free);
     a_ddt_Ca_sr_total = ((K(C_V_c) / K(C_V_sr)) * (a_i_up - (a_i_rel + a_i_leak)));
-    a_f_JCa_sr_free = (R(1.00000) / (R(1.00000) + ((K(C_Buf_sr) * K(C_K_buf_sr)) / cfg_ipow<2>((Y(S_Ca_SR) + K(C_K_buf_sr))))));
+    a_f_JCa_sr_free = (R(1.00000) / (R(1.00000) + ((K(C_Buf_sr) * K(C_K_buf_sr)) / cfg_ipow<2>((y_Ca_SR + K(C_K_buf_sr))))));
     dydt[S_Ca_SR] = (a_ddt_Ca_sr_total * a_f_JCa_sr_free);
     (void)dydt;
     return a_Iion_cm;
@@ -532,6 +599,9 @@ struct Model {
     static constexpr int VM_MAP = tnnp::VM_MAP;
     CFG_HD static __forceinline__ void init(double* C, double* y, int tissue, const double* scale) { init_consts(C, y, tissue, scale); }
     template <int T> CFG_HD static constexpr double constant(int i) { return cval<T>(i); }
+    static constexpr int NSD = tnnp::NSD, CA_STATE = tnnp::CA_STATE;
+    CFG_HD static constexpr int sd_slot(int i) { return tnnp::sd_slot(i); }
+    CFG_HD static constexpr int sd_const(int k) { return tnnp::sd_const(k); }
     template <class R, bool SV, class YS, class KS>
     __device__ static __forceinline__ R rates(double t, const YS& Y, const KS& K, R* dydt, int tissue, const CfgStimulus& st) { return rhs<R, SV>(t, Y, K, dydt, tissue, st); }
     template <class R, bool SV, class YS, class KS>
