@@ -209,7 +209,23 @@ class _Printer:
 # CUDA
 
 
+def _is_one(e) -> bool:
+    try:
+        return isinstance(e, Num) and float(e.text) == 1.0
+    except ValueError:
+        return False
+
+
 class _CudaPrinter(_Printer):
+    def __call__(self, e: Node) -> str:
+        # exp(x) - 1 (the GHK flux denominators) through cfg_expm1: the FP64
+        # overload evaluates exactly exp(x) - 1.0, the FP32 one is expm1f,
+        # which does not cancel to 0 as x -> 0 (Vm crossing 0 mV)
+        if (self.mode == "rhs" and isinstance(e, Bin) and e.op == "-" and _is_one(e.r)
+                and isinstance(e.l, Call) and e.l.fn == "exp"):
+            return f"cfg_expm1({self(e.l.args[0])})"
+        return super().__call__(e)
+
     def __init__(self, m: Model, early: List[str], mode: str):
         super().__init__(m)
         self.early = set(early)

@@ -42,6 +42,11 @@ CFG_HD __forceinline__ float cfg_fabs(float x) { return fabsf(x); }
 CFG_HD __forceinline__ double cfg_floor(double x) { return floor(x); }
 CFG_HD __forceinline__ float cfg_floor(float x) { return floorf(x); }
 CFG_HD __forceinline__ double cfg_pow(double x, double y) { return pow(x, y); }
+// exp(x) - 1 of the generated GHK fluxes: in double exactly the reference's
+// two operations; in float expm1f, which keeps its relative accuracy as
+// x -> 0 where expf(x) - 1 cancels to 0 (and the flux to 0/0)
+CFG_HD __forceinline__ double cfg_expm1(double x) { return exp(x) - 1.0; }
+CFG_HD __forceinline__ float cfg_expm1(float x) { return expm1f(x); }
 CFG_HD __forceinline__ float cfg_pow(float x, float y) { return powf(x, y); }
 
 template <int N, class R>

@@ -231,6 +231,7 @@ CFG_D __forceinline__ long long solve(double xs, double xe, float D, float* Y, f
         }
         // --- RKF45::solve error estimate and ODESolver::normalizeError
         float maxerr = 0.0f;
+        bool finite = true;
         worst = -1;
 #pragma unroll 4
         for (int i = 0; i < NS; ++i) {
@@ -243,11 +244,15 @@ CFG_D __forceinline__ long long solve(double xs, double xe, float D, float* Y, f
             const float tol = abs_tol + rel_tol * (a > b ? a : b) + noise;
             const float e = fabsf(e_i) / tol;
             if (e > maxerr) { maxerr = e; worst = i; }
+            if (!(e == e)) { finite = false; worst = i; }
         }
-        err = maxerr;
-        if (err > 1.0f) {
-            float scale = safe * __powf(err, -a_dec);
-            if (scale < min_scale) scale = min_scale;
+        err = finite ? maxerr : __int_as_float(0x7fc00000);
+        // A trial stage can overflow FP32 (exp of an overshooting voltage):
+        // a non-finite error norm rejects the step with the smallest scale,
+        // where the FP64 form would see a large but finite error.
+        if (!(err <= 1.0f)) {
+            float scale = err == err ? safe * __powf(err, -a_dec) : min_scale;
+            if (!(scale >= min_scale)) scale = min_scale;
             dx *= scale;
             if (!(dx >= 1e-37f)) {
                 why.reason = 2;
