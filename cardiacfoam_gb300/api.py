@@ -268,3 +268,80 @@ class Monodomain:
             self.h = None
 
     __del__ = close
+
+
+# NUM_STATES of the compiled models
+STATE_COUNTS = {"TNNP": 17, "ORd": 41, "ToRORd_dynCl": 45, "AlievPanfilov": 2, "BuenoOrovio": 4}
+
+
+class BatchCells:
+    """SingleCellSolver for many independent cells (per-cell conductance
+    scales, S1/S2 protocol and end time) in one persistent, work-stealing
+    launch, with APD90 and peak Ca of each cell's last beat computed on the
+    device.  ``stimuli`` is a sequence of ``stimulus_desc`` (model time
+    units), ``end_time`` an array [s]."""
+
+    def __init__(self, model: str, tissue: str, dt: float, stimuli: Sequence,
+                 end_time: np.ndarray, precision: int = _L.PRECISION_FP64,
+                 scales: Optional[np.ndarray] = None, ode=None, trace_cells: int = 0,
+                 trace_samples: int = 0, chunk: int = 0):
+        self._lib = _L.load()
+        n = len(end_time)
+        self.n = n
+        self.model = model
+        self._stim = (_L.StimulusDesc * n)(*stimuli)
+        self._end = np.ascontiguousarray(end_time, dtype=np.float64)
+        self._scales = None if scales is None else np.ascontiguousarray(scales, dtype=np.float64)
+        d = _L.BatchDesc()
+        d.ionic_model = model.encode()
+        d.tissue = tissue.encode()
+        d.n_cells = n
+        d.delta_t = dt
+        d.precision = precision
+        d.ode = ode if ode is not None else ode_desc()
+        d.stimulus = C.cast(self._stim, C.c_void_p)
+        d.end_time = self._end.ctypes.data
+        d.scales = None if self._scales is None else self._scales.ctypes.data
+        d.trace_cells, d.trace_samples, d.chunk = trace_cells, trace_samples, chunk
+        self.trace_cells, self.trace_samples = trace_cells, trace_samples
+        h = C.c_void_p()
+        _L.check(self._lib.cfg_batch_create(C.byref(d), C.byref(h)))
+        self.h = h
+
+    def run(self):
+        _L.check(self._lib.cfg_batch_run(self.h))
+
+    def results(self):
+        """(beats detected, last-beat APD90 [ms], its upstroke time [s], its peak Ca)."""
+        nb = np.zeros(self.n, dtype=np.int32)
+        apd, tup, ca = np.zeros(self.n), np.zeros(self.n), np.zeros(self.n)
+        _L.check(self._lib.cfg_batch_results(self.h, nb.ctypes.data, apd.ctypes.data,
+                                             tup.ctypes.data, ca.ctypes.data))
+        return nb, apd, tup, ca
+
+    def trace(self) -> np.ndarray:
+        """[trace_cells, 2, trace_samples]: Vm [mV] and Ca from t = 0."""
+        a = np.zeros((self.trace_cells, 2, self.trace_samples))
+        _L.check(self._lib.cfg_batch_trace(self.h, _L.dptr(a)))
+        return a
+
+    def states(self) -> np.ndarray:
+        a = np.zeros((STATE_COUNTS[self.model], self.n))
+        _L.check(self._lib.cfg_batch_get_states(self.h, _L.dptr(a)))
+        return a
+
+    def stats(self):
+        """(RHS evaluations, solver steps, launches)."""
+        e, s, l = C.c_ulonglong(), C.c_longlong(), C.c_longlong()
+        _L.check(self._lib.cfg_batch_stats(self.h, C.byref(e), C.byref(s), C.byref(l)))
+        return e.value, s.value, l.value
+
+    def stream(self) -> int:
+        return self._lib.cfg_batch_stream(self.h)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self._lib.cfg_batch_destroy(self.h)
+            self.h = None
+
+    __del__ = close

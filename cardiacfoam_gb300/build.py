@@ -55,6 +55,7 @@ def _units():
                           flags + [f"-DCFG_MODEL={m}"] + extra))
     units.append(("ionic_registry", CSRC / "ionic_registry.cu", []))
     units.append(("ionic", CSRC / "ionic.cu", []))
+    units.append(("batch", CSRC / "batch.cu", []))
     units.append(("diffusion", CSRC / "diffusion.cu", []))
     units.append(("monodomain", CSRC / "monodomain.cu", []))
     units.append(("diffusion_coop", CSRC / "diffusion_coop.cu", []))

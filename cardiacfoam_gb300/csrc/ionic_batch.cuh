@@ -1,0 +1,440 @@
+// Batched single cells: SingleCellSolver::evolve (singleCellSolver.C:179-230)
+// for many independently parameterised cells (conductance scales, S1/S2
+// protocol, run length) in one persistent launch, with the restitution
+// post-processing (APD90 and peak Ca per beat, postProcessing_restCurves.py)
+// done on the fly.
+//
+// Work stealing: every thread takes the next cell from a queue counter,
+// advances it by up to `chunk` solver steps, stores it and takes another;
+// finished cells are skipped.  The host relaunches until no cell is left,
+// so uneven run lengths do not idle the GPU and no launch runs for long.
+//
+// Per-cell scales change only a handful of constants (the scaled
+// conductances and what initConsts derives from them); those come from a
+// per-cell vector, every other constant is the tissue's compile-time value.
+#pragma once
+
+#include "ionic_kernels.cuh"
+#include "ionic_mixed.cuh"
+
+namespace cfg {
+
+// Beat detection settings (postProcessing_restCurves.py:14-17): upstroke at
+// dV/dt = 5000 mV/s, baseline = minimum over the 2 ms before it, peak and
+// repolarisation searched up to 2 s after it or to the next upstroke.
+struct ApdParams {
+    double dvdt_threshold;   // mV/s
+    double baseline;         // s
+    double peak_search;      // s
+    int ring;                // samples kept for the baseline window
+};
+
+// Streaming state of the beat detector of one cell.  Samples are the
+// solver's trace (time [s], Vm [mV], Ca); sample m is processed into the beat
+// windows when sample m+1 arrives, because the central dV/dt at m needs it.
+struct ApdTracker {
+    long long m;             // samples seen
+    double t1, v1, ca1;      // sample m-1
+    double t2, v2;           // sample m-2
+    double d1;               // dV/dt at sample m-2
+    int open;                // a beat window is open
+    int crossed;             // repolarisation found after the current peak
+    double t_up, v_base, v_peak, t_rep, ca_peak;
+    double tw, vw;           // previous sample inside the window
+    int n_beats;
+    double last_t_up, last_apd, last_ca;   // last finished beat (apd [s], NaN if none)
+};
+
+CFG_HD inline ApdParams apd_defaults(double dt)
+{
+    ApdParams p;
+    p.dvdt_threshold = 5000.0;
+    p.baseline = 0.002;
+    p.peak_search = 2.0;
+    p.ring = int(p.baseline / dt) + 3;
+    return p;
+}
+
+CFG_D __forceinline__ double cfg_nan() { return __longlong_as_double(0x7ff8000000000000ll); }
+CFG_D __forceinline__ double cfg_neg_inf() { return __longlong_as_double(0xfff0000000000000ll); }
+
+// One sample of the open window: peak, first downward crossing of v90 after
+// the peak (linear interpolation), peak Ca.
+CFG_D __forceinline__ void apd_include(ApdTracker& a, double t, double v, double ca)
+{
+    if (v > a.v_peak) {
+        a.v_peak = v;
+        a.t_rep = cfg_nan();
+        a.crossed = 0;
+    } else if (!a.crossed) {
+        const double v90 = a.v_base + 0.1 * (a.v_peak - a.v_base);
+        if (a.vw > v90 && v90 >= v) {
+            const double frac = (v90 - a.vw) / (v - a.vw);
+            a.t_rep = a.tw + frac * (t - a.tw);
+            a.crossed = 1;
+        }
+    }
+    if (ca > a.ca_peak) a.ca_peak = ca;
+    a.tw = t;
+    a.vw = v;
+}
+
+CFG_D __forceinline__ void apd_finish(ApdTracker& a)
+{
+    a.n_beats += 1;
+    a.last_t_up = a.t_up;
+    a.last_apd = a.crossed ? a.t_rep - a.t_up : cfg_nan();
+    a.last_ca = a.ca_peak;
+    a.open = 0;
+}
+
+// Sample m (t, v, ca).  ring_t/ring_v: this cell's ring of the last
+// `ring` samples, stride `rs` between entries.
+CFG_D inline void apd_sample(ApdTracker& a, const ApdParams& P, double t, double v, double ca,
+                             double* ring_t, double* ring_v, long long rs)
+{
+    const long long slot = (a.m % P.ring) * rs;
+    ring_t[slot] = t;
+    ring_v[slot] = v;
+    if (a.m >= 2) {
+        const double d = (v - a.v2) / (t - a.t2);          // dV/dt at sample m-1
+        const double dprev = a.m == 2 ? d : a.d1;           // sample 0 copies sample 1
+        const double thr = P.dvdt_threshold;
+        bool cand = dprev < thr && thr <= d;
+        double tup = 0.0;
+        if (cand) {
+            const double frac = (thr - dprev) / (d - dprev);
+            cand = frac >= 0.0 && frac <= 1.0;
+            tup = a.t2 + frac * (a.t1 - a.t2);
+        }
+        if (cand) {
+            if (a.open) {
+                if (a.t1 <= tup) apd_include(a, a.t1, a.v1, a.ca1);
+                apd_finish(a);
+            }
+            // baseline: minimum over tup - baseline <= t < tup
+            double vb = 0.0;
+            bool any = false;
+            const long long k0 = a.m + 1 > P.ring ? a.m + 1 - P.ring : 0;
+            for (long long k = k0; k <= a.m; ++k) {
+                const long long s = (k % P.ring) * rs;
+                const double tk = ring_t[s];
+                if (tk >= tup - P.baseline && tk < tup) {
+                    const double vk = ring_v[s];
+                    if (!any || vk < vb) vb = vk;
+                    any = true;
+                }
+            }
+            if (any) {
+                a.open = 1;
+                a.t_up = tup;
+                a.v_base = vb;
+                a.v_peak = cfg_neg_inf();
+                a.t_rep = cfg_nan();
+                a.crossed = 0;
+                a.ca_peak = cfg_neg_inf();
+                apd_include(a, a.t1, a.v1, a.ca1);
+            }
+        } else if (a.open) {
+            if (a.t1 <= a.t_up + P.peak_search) apd_include(a, a.t1, a.v1, a.ca1);
+            else apd_finish(a);
+        }
+        a.d1 = d;
+    }
+    a.t2 = a.t1;
+    a.v2 = a.v1;
+    a.t1 = t;
+    a.v1 = v;
+    a.ca1 = ca;
+    a.m += 1;
+}
+
+// End of the trace: the last sample (no upstroke can start there, dV/dt at
+// the end copies its neighbour) and the open beat.
+CFG_D inline void apd_end(ApdTracker& a, const ApdParams& P)
+{
+    if (a.m >= 2 && a.open) {
+        if (a.t1 <= a.t_up + P.peak_search) apd_include(a, a.t1, a.v1, a.ca1);
+        else apd_finish(a);
+    }
+    if (a.open) apd_finish(a);
+}
+
+// Constants of a uniform tissue with the scale-dependent ones per cell.
+template <class R, class M, int T>
+struct ScaledFold {
+    const R* dep;   // [NSD] this cell's scale-dependent constants
+    CFG_D __forceinline__ R operator()(int i) const
+    {
+        return M::sd_slot(i) >= 0 ? dep[M::sd_slot(i)] : R(M::template constant<T>(i));
+    }
+};
+
+struct BatchLaunch {
+    long long n;
+    double dt;                      // SingleCellSolver deltaT [s]
+    long long chunk;                // solver steps per claim
+    OdeSettings ode;
+    const CfgStimulus* stim;        // [n]
+    const long long* n_steps;       // [n] solver steps of each cell
+    long long* done;                // [n] steps taken
+    double* t;                      // [n] time [s]
+    double* yw;                     // wide states [NW][n] (FP64, or (hi, lo) pairs)
+    float* yn;                      // narrow states [NN][n] (mixed form)
+    double* step;                   // [n] persistent ODE step [model time]
+    double* dep;                    // [NSD][n] scale-dependent constants
+    ApdTracker* apd;                // [n]
+    double* ring_t;                 // [ring][n]
+    double* ring_v;
+    ApdParams apdp;
+    double* trace;                  // [trace_cells][2][trace_cap]: Vm [mV], Ca
+    long long trace_cells, trace_cap;
+    unsigned long long* queue;      // next cell to claim (zeroed before a launch)
+    long long* active;              // cells not finished
+    int* status;
+    unsigned long long* rhs_evals;
+    double* fail_record;
+};
+
+template <class M>
+CFG_D __forceinline__ double state0_to_mv(double u)
+{
+    if constexpr (M::VM_MAP == CFG_VM_ALIEV) return u * 100.0 - 80.0;
+    else if constexpr (M::VM_MAP == CFG_VM_BUENO) return u * 85.7 - 84.0;
+    else return u;
+}
+
+// sample of the cell after a step, its trace entry and the beat detector
+template <class M>
+CFG_D __forceinline__ void batch_sample(const BatchLaunch& p, long long c, long long k,
+                                        ApdTracker& a, double t, double v0, double ca)
+{
+    const double v = state0_to_mv<M>(v0);
+    apd_sample(a, p.apdp, t, v, ca, p.ring_t + c, p.ring_v + c, p.n);
+    if (c < p.trace_cells && k < p.trace_cap) {
+        p.trace[(c * 2 + 0) * p.trace_cap + k] = v;
+        p.trace[(c * 2 + 1) * p.trace_cap + k] = ca;
+    }
+}
+
+CFG_D __forceinline__ void batch_fail(const BatchLaunch& p, long long c, const IonicFailure& why)
+{
+    const int prev = atomicOr(p.status, CFG_ERR_ODE_STEPS);
+    if (p.fail_record && !(prev & CFG_ERR_ODE_STEPS)) {
+        double* r = p.fail_record;
+        r[0] = double(c); r[1] = why.reason; r[2] = why.x; r[3] = why.dx;
+        r[4] = why.worst; r[5] = why.err; r[6] = why.value; r[7] = double(why.steps);
+    }
+}
+
+// Initial states (initConsts with the cell's scales), its scale-dependent
+// constants, and sample 0 of the trace.
+template <class M, bool FP64>
+__global__ void batch_init_kernel(BatchLaunch p, const double* scales, int tissue,
+                                  double init_step)
+{
+    using L = Layout<M, FP64>;
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= p.n) return;
+    double C[M::NC] = {};
+    double y[M::NS];
+    double sc[6];
+    const double* scp = nullptr;
+    if (scales) {
+        for (int j = 0; j < 6; ++j) sc[j] = scales[j * p.n + c];
+        scp = sc;
+    }
+    M::init(C, y, tissue, scp);
+    for (int k = 0; k < M::NSD; ++k) p.dep[k * p.n + c] = C[M::sd_const(k)];
+#pragma unroll
+    for (int i = 0; i < M::NS; ++i) {
+        if (FP64) {
+            p.yw[(long long)L::slot(i) * p.n + c] = y[i];
+        } else if (is_wide<M::WIDE_MASK>(i)) {
+            const float hi = float(y[i]);
+            reinterpret_cast<float2*>(p.yw)[(long long)L::slot(i) * p.n + c] =
+                make_float2(hi, float(y[i] - double(hi)));
+        } else {
+            p.yn[(long long)L::slot(i) * p.n + c] = float(y[i]);
+        }
+    }
+    p.step[c] = init_step;
+    p.t[c] = 0.0;
+    p.done[c] = 0;
+    ApdTracker a{};
+    a.last_apd = cfg_nan();
+    a.last_ca = cfg_nan();
+    a.last_t_up = cfg_nan();
+    batch_sample<M>(p, c, 0, a, 0.0, y[0], M::CA_STATE >= 0 ? y[M::CA_STATE] : 0.0);
+    p.apd[c] = a;
+}
+
+// FP64 plain form: per-thread stage arrays, as the tissue kernel.
+template <class M, int T>
+__global__ void __launch_bounds__(128) batch_fp64_kernel(BatchLaunch p)
+{
+    using L = Layout<M, true>;
+    constexpr int NS = M::NS;
+    unsigned evals = 0;
+    double k6[6][NS];
+    for (;;) {
+        const long long c = (long long)atomicAdd(p.queue, 1ull);
+        if (c >= p.n) break;
+        long long k = p.done[c];
+        const long long total = p.n_steps[c];
+        if (k >= total) continue;
+        // derivatives a model does not assign stay zero, as in a zeroed dydt
+        for (int j = 0; j < 6; ++j)
+            for (int i = 0; i < NS; ++i) k6[j][i] = 0.0;
+        CellState<M, double> cs;
+#pragma unroll
+        for (int i = 0; i < NS; ++i) {
+            cs.y[i] = p.yw[(long long)L::slot(i) * p.n + c];
+            cs.yf[i] = cs.y[i];
+        }
+        double dep[M::NSD > 0 ? M::NSD : 1];
+#pragma unroll
+        for (int j = 0; j < M::NSD; ++j) dep[j] = p.dep[j * p.n + c];
+        const ScaledFold<double, M, T> Kc{dep};
+        const CfgStimulus stim = p.stim[c];
+        ApdTracker a = p.apd[c];
+        double t = p.t[c];
+        double step = p.step[c];
+        const long long k_end = total < k + p.chunk ? total : k + p.chunk;
+        bool failed = false;
+        for (; k < k_end; ++k) {
+            const double t_new = t + p.dt;   // runTime++
+            double ts, te, dtm;
+            model_times<M>(t_new - p.dt, p.dt, ts, te, dtm);
+            if (dtm < step) step = dtm;
+            IonicFailure why;
+            const long long nsub =
+                rkf45_solve<M, true, double>(ts, te, cs, step, k6, Kc, T, stim, p.ode, evals, &why);
+            if (nsub < 0) {
+                batch_fail(p, c, why);
+                failed = true;
+                break;
+            }
+            t = t_new;
+            batch_sample<M>(p, c, k + 1, a, t, cs.y[0],
+                            M::CA_STATE >= 0 ? cs.y[M::CA_STATE] : 0.0);
+        }
+#pragma unroll
+        for (int i = 0; i < NS; ++i) p.yw[(long long)L::slot(i) * p.n + c] = cs.y[i];
+        p.step[c] = step;
+        p.t[c] = t;
+        if (failed) k = total;
+        p.done[c] = k;
+        if (k >= total) {
+            apd_end(a, p.apdp);
+            atomicAdd((unsigned long long*)p.active, (unsigned long long)-1ll);
+        }
+        p.apd[c] = a;
+    }
+    if (p.rhs_evals) {
+        unsigned long long v = evals;
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if ((threadIdx.x & 31) == 0 && v) atomicAdd(p.rhs_evals, v);
+    }
+}
+
+// Mixed form: stage data in shared memory, FP32 arithmetic, slow states as
+// (hi, lo) pairs (see ionic_mixed.cuh).
+template <class M, int T>
+__global__ void __launch_bounds__(mixed::Slice<M>::block, mixed::Slice<M>::min_blocks)
+batch_mixed_kernel(BatchLaunch p)
+{
+    using S = mixed::Slice<M>;
+    using L = Layout<M, false>;
+    constexpr int NS = M::NS, P = S::NSP;
+    extern __shared__ float cfg_batch_smem[];
+    float* Y = cfg_batch_smem + threadIdx.x * S::len;
+    float* Tm = Y + P;
+    float* K = Tm + P;
+    float* LO = K + 5 * P;
+    unsigned evals = 0;
+    for (;;) {
+        const long long c = (long long)atomicAdd(p.queue, 1ull);
+        if (c >= p.n) break;
+        long long k = p.done[c];
+        const long long total = p.n_steps[c];
+        if (k >= total) continue;
+        for (int i = 0; i < 6 * P; ++i) Tm[i] = 0.0f;
+        const float2* yw2 = reinterpret_cast<const float2*>(p.yw);
+        int w = 0;
+#pragma unroll
+        for (int i = 0; i < NS; ++i) {
+            if (is_wide<M::WIDE_MASK>(i)) {
+                const float2 v = yw2[(long long)L::slot(i) * p.n + c];
+                Y[i] = v.x;
+                LO[w++] = v.y;
+            } else {
+                Y[i] = p.yn[(long long)L::slot(i) * p.n + c];
+            }
+        }
+        float dep[M::NSD > 0 ? M::NSD : 1];
+#pragma unroll
+        for (int j = 0; j < M::NSD; ++j) dep[j] = float(p.dep[j * p.n + c]);
+        const ScaledFold<float, M, T> Kc{dep};
+        const CfgStimulus stim = p.stim[c];
+        ApdTracker a = p.apd[c];
+        double t = p.t[c];
+        float dx_try = float(p.step[c]);
+        const long long k_end = total < k + p.chunk ? total : k + p.chunk;
+        bool failed = false;
+        for (; k < k_end; ++k) {
+            const double t_new = t + p.dt;
+            double ts, te, dtm;
+            model_times<M>(t_new - p.dt, p.dt, ts, te, dtm);
+            dx_try = fminf(dx_try, float(dtm));
+            IonicFailure why;
+            float iion;
+            const long long nsub = mixed::solve<M, true>(ts, te, float(dtm), Y, Tm, K, LO,
+                                                         dx_try, Kc, T, stim, p.ode, evals,
+                                                         why, iion);
+            if (nsub < 0) {
+                batch_fail(p, c, why);
+                failed = true;
+                break;
+            }
+            t = t_new;
+            const double v0 = is_wide<M::WIDE_MASK>(0) ? double(Y[0]) + double(LO[0])
+                                                       : double(Y[0]);
+            double ca = 0.0;
+            if constexpr (M::CA_STATE >= 0) {
+                if (is_wide<M::WIDE_MASK>(M::CA_STATE)) {
+                    constexpr int wc = Layout<M, false>::slot(M::CA_STATE);
+                    ca = double(Y[M::CA_STATE]) + double(LO[wc]);
+                } else {
+                    ca = double(Y[M::CA_STATE]);
+                }
+            }
+            batch_sample<M>(p, c, k + 1, a, t, v0, ca);
+        }
+        float2* yw2o = reinterpret_cast<float2*>(p.yw);
+        w = 0;
+#pragma unroll
+        for (int i = 0; i < NS; ++i) {
+            if (is_wide<M::WIDE_MASK>(i))
+                yw2o[(long long)L::slot(i) * p.n + c] = make_float2(Y[i], LO[w++]);
+            else
+                p.yn[(long long)L::slot(i) * p.n + c] = Y[i];
+        }
+        p.step[c] = double(dx_try);
+        p.t[c] = t;
+        if (failed) k = total;
+        p.done[c] = k;
+        if (k >= total) {
+            apd_end(a, p.apdp);
+            atomicAdd((unsigned long long*)p.active, (unsigned long long)-1ll);
+        }
+        p.apd[c] = a;
+    }
+    if (p.rhs_evals) {
+        unsigned long long v = evals;
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if ((threadIdx.x & 31) == 0 && v) atomicAdd(p.rhs_evals, v);
+    }
+}
+
+}  // namespace cfg

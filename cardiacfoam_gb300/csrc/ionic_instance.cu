@@ -5,6 +5,7 @@
 
 #include "ionic_kernels.cuh"
 #include "ionic_mixed.cuh"
+#include "ionic_batch.cuh"
 
 #define CFG_STR2(x) #x
 #define CFG_STR(x) CFG_STR2(x)
@@ -115,3 +116,86 @@ extern "C" void CFG_CAT3(cfg_ionic_host_init_, CFG_MODEL, )(double* C, double* y
     M::init(C, y, tissue, scale);
 }
 #endif
+
+// ---------------------------------------------------------------- batched single cells
+
+template <int T>
+static void* batch_kernel_ptr()
+{
+    if constexpr (kFP64) return reinterpret_cast<void*>(&cfg::batch_fp64_kernel<M, T>);
+    else return reinterpret_cast<void*>(&cfg::batch_mixed_kernel<M, T>);
+}
+
+template <int T>
+static cudaError_t batch_launch(const cfg::BatchLaunch& p, cudaStream_t s)
+{
+    int block, smem;
+    if constexpr (kFP64) {
+        block = 128;
+        smem = 0;
+    } else {
+        block = cfg::mixed::Slice<M>::block;
+        smem = cfg::mixed::Slice<M>::smem_bytes;
+    }
+    // persistent grid: every block resident, cells handed out by the queue
+    static int per_sm = 0, sms = 0;
+    if (!per_sm) {
+        int dev = 0;
+        cudaError_t e = cudaGetDevice(&dev);
+        if (!e) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (!e) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel_ptr<T>(),
+                                                                  block, smem);
+        if (e) return e;
+        if (per_sm < 1) per_sm = 1;
+    }
+    const long long want = (p.n + block - 1) / block;
+    const long long cap = (long long)sms * per_sm;
+    const unsigned grid = unsigned(want < cap ? want : cap);
+    if constexpr (kFP64) cfg::batch_fp64_kernel<M, T><<<grid, block, 0, s>>>(p);
+    else cfg::batch_mixed_kernel<M, T><<<grid, block, smem, s>>>(p);
+    return cudaGetLastError();
+}
+
+template <int T0, int... TR>
+static cudaError_t batch_dispatch(const cfg::BatchLaunch& p, int tissue, cudaStream_t s,
+                                  TissueList<T0, TR...>)
+{
+    if (tissue == T0) return batch_launch<T0>(p, s);
+    if constexpr (sizeof...(TR) > 0) return batch_dispatch(p, tissue, s, TissueList<TR...>{});
+    return cudaErrorInvalidValue;
+}
+
+template <int... TS>
+static cudaError_t batch_prepare(TissueList<TS...>)
+{
+    if constexpr (kFP64) {
+        return cudaSuccess;
+    } else {
+        cudaError_t r[] = {cudaSuccess,
+                           cudaFuncSetAttribute(&cfg::batch_mixed_kernel<M, TS>,
+                                                cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                cfg::mixed::Slice<M>::smem_bytes)...};
+        for (cudaError_t x : r)
+            if (x) return x;
+        return cudaSuccess;
+    }
+}
+
+extern "C" cudaError_t CFG_CAT3(cfg_batch_init_, CFG_MODEL, CFG_PREC_TAG)(
+    const cfg::BatchLaunch& p, const double* scales, int tissue, double init_step,
+    cudaStream_t stream)
+{
+    if (cudaError_t e = batch_prepare(Tissues{})) return e;
+    if (p.n <= 0) return cudaSuccess;
+    const int block = 128;
+    const unsigned grid = unsigned((p.n + block - 1) / block);
+    cfg::batch_init_kernel<M, kFP64><<<grid, block, 0, stream>>>(p, scales, tissue, init_step);
+    return cudaGetLastError();
+}
+
+extern "C" cudaError_t CFG_CAT3(cfg_batch_step_, CFG_MODEL, CFG_PREC_TAG)(
+    const cfg::BatchLaunch& p, int tissue, cudaStream_t stream)
+{
+    if (p.n <= 0) return cudaSuccess;
+    return batch_dispatch(p, tissue, stream, Tissues{});
+}

@@ -21,7 +21,15 @@
                                                        const double*, long long, double,      \
                                                        double*, float*, double*,              \
                                                        cudaStream_t);                         \
-    extern "C" void cfg_ionic_host_init_##ns(double*, double*, int, const double*);
+    extern "C" void cfg_ionic_host_init_##ns(double*, double*, int, const double*);          \
+    extern "C" cudaError_t cfg_batch_init_##ns##_fp64(const cfg::BatchLaunch&, const double*, \
+                                                      int, double, cudaStream_t);             \
+    extern "C" cudaError_t cfg_batch_init_##ns##_mixed(const cfg::BatchLaunch&, const double*,\
+                                                       int, double, cudaStream_t);            \
+    extern "C" cudaError_t cfg_batch_step_##ns##_fp64(const cfg::BatchLaunch&, int,           \
+                                                      cudaStream_t);                          \
+    extern "C" cudaError_t cfg_batch_step_##ns##_mixed(const cfg::BatchLaunch&, int,          \
+                                                       cudaStream_t);
 
 CFG_DECLARE_MODEL(tnnp)
 CFG_DECLARE_MODEL(ord)
@@ -75,6 +83,12 @@ struct Tables {
         o.init[0] = cfg_ionic_init_##NSP##_fp64;                                                 \
         o.init[1] = cfg_ionic_init_##NSP##_mixed;                                                \
         o.host_init = cfg_ionic_host_init_##NSP;                                                 \
+        o.batch_init[0] = cfg_batch_init_##NSP##_fp64;                                           \
+        o.batch_init[1] = cfg_batch_init_##NSP##_mixed;                                          \
+        o.batch_step[0] = cfg_batch_step_##NSP##_fp64;                                           \
+        o.batch_step[1] = cfg_batch_step_##NSP##_mixed;                                          \
+        o.nsd = NSP::NSD;                                                                        \
+        o.ca_state = NSP::CA_STATE;                                                              \
         return o;                                                                               \
     }()
 

@@ -5,6 +5,7 @@
 
 #include <cuda_runtime.h>
 
+#include "ionic_batch.cuh"
 #include "ionic_kernels.cuh"
 
 namespace cfg {
@@ -27,6 +28,13 @@ struct IonicModelOps {
     // host evaluation of initConsts (for checks and initial state export)
     void (*host_init)(double* C, double* y, int tissue, const double* scale);
     int nc;
+    // batched single cells: initial states + trace sample 0, and one
+    // work-stealing launch, per precision
+    cudaError_t (*batch_init[2])(const BatchLaunch&, const double* scales, int tissue,
+                                 double init_step, cudaStream_t);
+    cudaError_t (*batch_step[2])(const BatchLaunch&, int tissue, cudaStream_t);
+    int nsd;                     // scale-dependent constants per cell
+    int ca_state;                // intracellular calcium state, or -1
 };
 
 const IonicModelOps* find_ionic_model(const char* name);

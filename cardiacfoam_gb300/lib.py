@@ -95,6 +95,14 @@ class SolveResult(C.Structure):
 
 NOALLOC_MAX_CELLS = 65536
 
+
+class BatchDesc(C.Structure):
+    _fields_ = [("ionic_model", C.c_char_p), ("tissue", C.c_char_p), ("n_cells", C.c_longlong),
+                ("delta_t", C.c_double), ("precision", C.c_int), ("ode", OdeDesc),
+                ("stimulus", C.c_void_p), ("end_time", C.c_void_p), ("scales", C.c_void_p),
+                ("trace_cells", C.c_longlong), ("trace_samples", C.c_longlong),
+                ("chunk", C.c_longlong)]
+
 # every symbol declared in include/cardiac_gpu.h
 EXPORTS = [
     "cfg_last_error", "cfg_ionic_create", "cfg_ionic_solve", "cfg_ionic_solve_device",
@@ -105,7 +113,9 @@ EXPORTS = [
     "cfg_monodomain_set_field", "cfg_monodomain_time", "cfg_monodomain_ionic",
     "cfg_monodomain_last_stats", "cfg_monodomain_set_timing", "cfg_monodomain_timings",
     "cfg_monodomain_stream", "cfg_monodomain_destroy", "cfg_box_diffusion_solve_noalloc",
-    "cfg_monodomain_set_persistent",
+    "cfg_monodomain_set_persistent", "cfg_batch_create", "cfg_batch_run", "cfg_batch_results",
+    "cfg_batch_trace", "cfg_batch_get_states", "cfg_batch_stats", "cfg_batch_stream",
+    "cfg_batch_destroy",
 ]
 
 _lib = None
@@ -154,6 +164,16 @@ def load(path: Optional[os.PathLike] = None):
     L.cfg_monodomain_stream.restype = C.c_void_p
     L.cfg_monodomain_destroy.argtypes = [C.c_void_p]
     L.cfg_monodomain_set_persistent.argtypes = [C.c_void_p, C.c_int]
+    L.cfg_batch_create.argtypes = [C.POINTER(BatchDesc), C.POINTER(C.c_void_p)]
+    L.cfg_batch_run.argtypes = [C.c_void_p]
+    L.cfg_batch_results.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    L.cfg_batch_trace.argtypes = [C.c_void_p, _dp]
+    L.cfg_batch_get_states.argtypes = [C.c_void_p, _dp]
+    L.cfg_batch_stats.argtypes = [C.c_void_p, C.POINTER(C.c_ulonglong), C.POINTER(C.c_longlong),
+                                  C.POINTER(C.c_longlong)]
+    L.cfg_batch_stream.argtypes = [C.c_void_p]
+    L.cfg_batch_stream.restype = C.c_void_p
+    L.cfg_batch_destroy.argtypes = [C.c_void_p]
     L.cfg_box_diffusion_solve_noalloc.argtypes = [C.POINTER(BoxDiffusionDesc), C.c_double,
                                                   C.c_void_p, C.c_void_p, C.c_void_p,
                                                   C.c_void_p, C.c_void_p,

@@ -218,6 +218,53 @@ int cfg_monodomain_set_persistent(cfg_monodomain* md, int enable);
 void* cfg_monodomain_stream(cfg_monodomain* md);
 int cfg_monodomain_destroy(cfg_monodomain* md);
 
+/* ------------------------------------------------ batched single cells
+ * SingleCellSolver (singleCellSolver.C:45-230: runTime++; solveODE(t - dt,
+ * dt) with Vm inside the ODE) for many independent cells in one persistent,
+ * work-stealing launch: each cell has its own conductance scales, S1/S2
+ * protocol (singleCellStimulus, stimulusIO.H:32-53) and end time.  The
+ * restitution post-processing of the traces (postProcessing_restCurves.py:
+ * upstroke where dV/dt crosses 5000 mV/s, baseline = minimum over the 2 ms
+ * before it, APD90 at 90 % repolarisation, windows up to 2 s or the next
+ * upstroke) runs on the device while the cells are stepped, together with
+ * the peak intracellular Ca of each beat. */
+typedef struct cfg_batch_desc {
+    const char* ionic_model;           /* ionicModel key */
+    const char* tissue;                /* tissue key (one for all cells) */
+    long long n_cells;
+    double delta_t;                    /* deltaT [s]: solver step, and first ODE step */
+    int precision;                     /* CFG_PRECISION_* */
+    cfg_ode_desc ode;
+    const cfg_stimulus_desc* stimulus; /* host [n_cells] protocols, model time units */
+    const double* end_time;            /* host [n_cells] endTime [s] */
+    const double* scales;              /* optional host [6][n_cells] factors on
+                                          GNa GCaL GKr GKs GK1 Gto */
+    long long trace_cells;             /* keep the Vm and Ca traces of cells
+                                          [0, trace_cells) */
+    long long trace_samples;           /* samples kept per traced cell, from t = 0 */
+    long long chunk;                   /* solver steps per claim (0: 2000) */
+} cfg_batch_desc;
+
+typedef struct cfg_batch cfg_batch;
+
+int cfg_batch_create(const cfg_batch_desc* desc, cfg_batch** out);
+/* Advance every cell to its end time; returns after the last launch. */
+int cfg_batch_run(cfg_batch* b);
+/* Per cell: beats detected, last beat's APD90 [ms] (NaN when it did not
+ * repolarise inside its window), upstroke time [s] and peak Ca. */
+int cfg_batch_results(cfg_batch* b, int* n_beats, double* apd90_ms, double* t_up,
+                      double* peak_ca);
+/* Traces as [trace_cells][2][trace_samples]: Vm [mV] then Ca. */
+int cfg_batch_trace(cfg_batch* b, double* host);
+/* Final states as [n_states][n_cells]. */
+int cfg_batch_get_states(cfg_batch* b, double* host_states);
+/* RHS evaluations, solver steps taken and kernel launches since creation. */
+int cfg_batch_stats(const cfg_batch* b, unsigned long long* rhs_evaluations,
+                    long long* solver_steps, long long* launches);
+/* The CUDA stream (cudaStream_t) the batch runs on. */
+void* cfg_batch_stream(cfg_batch* b);
+int cfg_batch_destroy(cfg_batch* b);
+
 /* ------------------------------------ diffusion solve without allocation
  * No counterpart in the reference.  For callers that cannot call cudaMalloc
  * when they need a solve (a host application that owns all device memory

@@ -873,6 +873,17 @@ long oracle_single_cell(int model, int tissue, double dt, long n_steps,
                         const oracle_ode_settings* ode, const oracle_stimulus* stim,
                         const double* scales, double* vm_trace, double* final_states)
 {
+    return oracle_single_cell_traces(model, tissue, dt, n_steps, ode, stim, scales, vm_trace,
+                                     -1, NULL, final_states);
+}
+
+/* The same, also tracing state `state_b` (e.g. intracellular Ca) after each
+ * step when b_trace is given. */
+long oracle_single_cell_traces(int model, int tissue, double dt, long n_steps,
+                               const oracle_ode_settings* ode, const oracle_stimulus* stim,
+                               const double* scales, double* vm_trace, int state_b,
+                               double* b_trace, double* final_states)
+{
     oracle_ionic* io = oracle_ionic_new(model, 1, tissue, dt, 1, ode, stim, scales);
     if (!io) return -1;
     const model_info* m = io->m;
@@ -886,6 +897,7 @@ long oracle_single_cell(int model, int tissue, double dt, long n_steps,
         double u = io->y[0];
         double vm = m->vm_map == 1 ? u * 100 - 80 : m->vm_map == 2 ? u * 85.7 - 84.0 : u;
         if (vm_trace) vm_trace[s] = vm;
+        if (b_trace && state_b >= 0) b_trace[s] = io->y[state_b];
     }
     if (final_states) memcpy(final_states, io->y, sizeof(double) * (size_t)m->ns);
     oracle_ionic_free(io);

@@ -119,6 +119,10 @@ int oracle_tissue_last_solves(const oracle_tissue*, double* init_res, double* fi
 long oracle_single_cell(int model, int tissue, double dt, long n_steps,
                         const oracle_ode_settings* ode, const oracle_stimulus* stim,
                         const double* scales, double* vm_trace, double* final_states);
+long oracle_single_cell_traces(int model, int tissue, double dt, long n_steps,
+                               const oracle_ode_settings* ode, const oracle_stimulus* stim,
+                               const double* scales, double* vm_trace, int state_b,
+                               double* b_trace, double* final_states);
 
 #ifdef __cplusplus
 }

@@ -100,6 +100,10 @@ def lib():
                                          C.POINTER(OdeSettings), C.POINTER(Stimulus), _dp,
                                          _dp, _dp]
         L.oracle_single_cell.restype = C.c_long
+        L.oracle_single_cell_traces.argtypes = [C.c_int, C.c_int, C.c_double, C.c_long,
+                                                C.POINTER(OdeSettings), C.POINTER(Stimulus),
+                                                _dp, _dp, C.c_int, _dp, _dp]
+        L.oracle_single_cell_traces.restype = C.c_long
         _lib = L
     return _lib
 
@@ -317,6 +321,24 @@ def single_cell(model: str, tissue: int, dt: float, n_steps: int, ode=None, stim
     if k < 0:
         raise RuntimeError("oracle single cell failed")
     return trace, final, k
+
+
+def single_cell_traces(model: str, tissue: int, dt: float, n_steps: int, state_b: int,
+                       ode=None, stim=None, scales=None):
+    """single_cell plus the trace of state `state_b` after each step."""
+    ns = sizes(model)[0]
+    trace = np.zeros(n_steps)
+    btrace = np.zeros(n_steps)
+    final = np.zeros(ns)
+    sc = None if scales is None else np.ascontiguousarray(scales, dtype=np.float64)
+    k = lib().oracle_single_cell_traces(MODELS[model], tissue, dt, n_steps,
+                                        C.byref(ode) if ode else None,
+                                        C.byref(stim) if stim else None,
+                                        ptr(sc) if sc is not None else None, ptr(trace),
+                                        state_b, ptr(btrace), ptr(final))
+    if k < 0:
+        raise RuntimeError("oracle single cell failed")
+    return trace, btrace, final, k
 
 
 # --- the reference's own model code, compiled verbatim (pinning only) -----
