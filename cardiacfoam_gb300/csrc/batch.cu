@@ -79,7 +79,7 @@ int batch_create(const cfg_batch_desc* d, cfg_batch** out)
     const long long n = d->n_cells;
     std::vector<CfgStimulus> stim(static_cast<size_t>(n));
     std::vector<long long> steps(static_cast<size_t>(n));
-    long long total = 0;
+    long long total = 0, with_work = 0;
     for (long long c = 0; c < n; ++c) {
         const cfg_stimulus_desc& s = d->stimulus[c];
         stim[size_t(c)] = CfgStimulus{s.stim_start, s.stim_period_s1, s.stim_duration,
@@ -88,6 +88,7 @@ int batch_create(const cfg_batch_desc* d, cfg_batch** out)
             return fail(CFG_ERR_INVALID, "cell %lld: negative end time", c);
         steps[size_t(c)] = (long long)std::llround(d->end_time[c] / d->delta_t);
         total += steps[size_t(c)];
+        with_work += steps[size_t(c)] > 0 ? 1 : 0;
     }
 
     cfg_batch* b = new cfg_batch;
@@ -125,7 +126,7 @@ int batch_create(const cfg_batch_desc* d, cfg_batch** out)
     if (!e) e = cudaMemcpy(b->d_n_steps, steps.data(), sizeof(long long) * n, cudaMemcpyHostToDevice);
     if (!e && d->scales)
         e = cudaMemcpy(b->d_scales, d->scales, sizeof(double) * 6 * n, cudaMemcpyHostToDevice);
-    const long long active = n;
+    const long long active = with_work;   // zero-length cells are done at set-up
     if (!e) e = cudaMemcpy(b->d_active, &active, sizeof active, cudaMemcpyHostToDevice);
     if (!e) e = cudaMemset(b->d_evals, 0, sizeof(unsigned long long));
     if (!e) e = cudaMemset(b->d_status, 0, sizeof(int));

@@ -266,6 +266,7 @@ __global__ void batch_init_kernel(BatchLaunch p, const double* scales, int tissu
     a.last_ca = cfg_nan();
     a.last_t_up = cfg_nan();
     batch_sample<M>(p, c, 0, a, 0.0, y[0], M::CA_STATE >= 0 ? y[M::CA_STATE] : 0.0);
+    if (p.n_steps[c] <= 0) apd_end(a, p.apdp);   // nothing to integrate
     p.apd[c] = a;
 }
 
