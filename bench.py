@@ -287,6 +287,69 @@ def reference_arm(args, rank, world):
                     "d2h_bytes_per_step": 0}}
 
 
+def batch_population(n, seed=2024):
+    """Batched single cells of the ToRORd_dynCl population: per-cell
+    log-uniform scales in [0.5, 2] on GNa GCaL GKr GKs GK1 Gto, S1 cycle
+    length U[300, 1000] ms, beat count U{5..50}, stimulus 53 uA/uF for 1 ms."""
+    from cardiacfoam_gb300 import api
+    rng = np.random.default_rng(seed)
+    scales = np.exp(rng.uniform(np.log(0.5), np.log(2.0), (6, n)))
+    cl = rng.uniform(300.0, 1000.0, n)
+    beats = rng.integers(5, 51, n)
+    stimuli = [api.stimulus_desc(10.0, float(cl[c]), 1.0, 53.0, int(beats[c])) for c in range(n)]
+    return stimuli, scales, cl, beats
+
+
+def batch_arm(args):
+    """Batched single cells: throughput of the persistent work-stealing
+    kernels on a bounded window of the 65,536-cell population (dt 0.01 ms),
+    and the mixed form's APD90 / peak-Ca error against FP64 over one full
+    beat of a subset (dt 0.1 ms: a lone FP64 thread integrates ToRORd_dynCl at
+    GB300's FP64 rate, so full beats at 0.01 ms would take minutes)."""
+    from cardiacfoam_gb300 import api, lib
+    n, dt = args.batch_cells, 1e-5
+    stimuli, scales, cl, beats = batch_population(n)
+    out = {"workload": f"{n} ToRORd_dynCl endocardialCells single cells, per-cell scales, "
+                       f"S1 CL U[300,1000] ms x U{{5..50}} beats, stimulus 53 uA/uF x 1 ms, "
+                       f"dt 0.01 ms", "unit": "cell-steps/s"}
+    for name, prec, window in (("mixed", lib.PRECISION_MIXED, args.batch_window),
+                               ("fp64", lib.PRECISION_FP64, args.batch_window_fp64)):
+        end = np.full(n, window * dt)
+        b = api.BatchCells("ToRORd_dynCl", "endocardialCells", dt, stimuli, end,
+                           precision=prec, scales=scales, ode=api.ode_desc(max_steps=10 ** 6),
+                           chunk=window)
+        t0 = time.perf_counter()
+        b.run()
+        el = time.perf_counter() - t0
+        evals, steps, launches = b.stats()
+        out[name] = {"value": steps / el, "steps_per_cell": window, "seconds": el,
+                     "rhs_evaluations": evals, "launches": launches}
+        b.close()
+    out["speedup_mixed_vs_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
+    # accuracy over one beat of a subset
+    m, dt_acc = args.batch_accuracy_cells, 1e-4
+    stim1 = [api.stimulus_desc(10.0, float(cl[c]), 1.0, 53.0, 1) for c in range(m)]
+    end = np.full(m, 0.01 + 0.5)        # one beat and 500 ms to repolarise
+    res = []
+    for prec in (lib.PRECISION_FP64, lib.PRECISION_MIXED):
+        b = api.BatchCells("ToRORd_dynCl", "endocardialCells", dt_acc, stim1, end,
+                           precision=prec, scales=scales[:, :m].copy(),
+                           ode=api.ode_desc(max_steps=10 ** 6))
+        b.run()
+        res.append(b.results())
+        b.close()
+    (nb0, apd0, _, ca0), (nb1, apd1, _, ca1) = res
+    ok = ~np.isnan(apd0) & ~np.isnan(apd1)
+    out["accuracy"] = {
+        "cells": m, "dt_s": dt_acc, "beats": 1, "window_s": 0.5,
+        "apd90_max_abs_error_ms": float(np.max(np.abs(apd0[ok] - apd1[ok]))) if ok.any() else None,
+        "apd90_cells_compared": int(ok.sum()),
+        "apd90_fp64_range_ms": [float(np.nanmin(apd0)), float(np.nanmax(apd0))],
+        "peak_ca_max_rel_error": float(np.max(np.abs(ca1 - ca0) / np.abs(ca0))),
+        "beat_count_mismatches": int(np.sum(nb0 != nb1))}
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -299,6 +362,12 @@ def main():
     ap.add_argument("--accuracy-steps", type=int, default=300,
                     help="steps both forms run before activation times are compared")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched single cells")
+    ap.add_argument("--batch-cells", type=int, default=65536)
+    ap.add_argument("--batch-window", type=int, default=2000,
+                    help="solver steps per cell timed for the mixed batch")
+    ap.add_argument("--batch-window-fp64", type=int, default=100)
+    ap.add_argument("--batch-accuracy-cells", type=int, default=256)
     ap.add_argument("--no-graph", action="store_true",
                     help="host-driven PIMPLE/PCG loops instead of the step graph")
     args = ap.parse_args()
@@ -363,6 +432,8 @@ def main():
         "gpu_launches": r["launches"],
         "clocks": r["clocks"],
     }
+    if not args.no_batch:
+        out["batched_single_cells"] = batch_arm(args)
     if not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline()
     print(json.dumps(out), flush=True)
