@@ -44,9 +44,9 @@ DT = 5e-6
 # from an ncu capture of the current kernel (dram__bytes_read.sum +
 # dram__bytes_write.sum); ncu cannot run inside the timed region, so the
 # figure is carried here and refreshed with each capture.
-IONIC_TRAFFIC_BYTES = 1027.8e6
-IONIC_TRAFFIC_SOURCE = "profiles/ionic_step_kernel_ord_mixed_420k.md"
-# states read and written (31 FP32 + 10 FP64 = 204 B) + Vm in + Iion out
+IONIC_TRAFFIC_BYTES = 124.2e6
+IONIC_TRAFFIC_SOURCE = "profiles/ionic_mixed_kernel_ord_420k.md"
+# states read and written (31 FP32 + 10 FP32 hi/lo pairs = 204 B) + Vm in + Iion out
 IONIC_STATE_BYTES = 2 * 204 + 16
 
 
@@ -417,7 +417,7 @@ def main():
                 "d2h_bytes_per_step": 8 * n, "steps": r["ke2e"],
                 "path": "cfg_monodomain_set_field(Vm) + cfg_monodomain_step + "
                         "cfg_monodomain_get_field(Vm), pinned host buffers"},
-        "roofline": {"bound": "fp32", "kernel": "ionic_step_kernel<ORd, mixed>",
+        "roofline": {"bound": "fp32", "kernel": "ionic_mixed_kernel<ORd, tissue 4>",
                      "achieved": r["achieved"], "peak": r["fp32_peak"], "unit": "TFLOP/s",
                      "frac": r["achieved"] / r["fp32_peak"],
                      "traffic": IONIC_TRAFFIC_BYTES, "traffic_unit": "bytes per launch",
