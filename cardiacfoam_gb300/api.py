@@ -17,7 +17,8 @@ import numpy as np
 from . import lib as _L
 from .mesh import LduMesh
 
-TISSUE_FLAGS = {"epicardialCells": 1, "mCells": 2, "endocardialCells": 3, "myocyte": 4}
+TISSUE_FLAGS = {"epicardialCells": 1, "mCells": 2, "endocardialCells": 3, "myocyte": 4,
+                "1D": 11, "2D": 12, "3D": 13}
 
 
 def ode_desc(solver="RKF45", abs_tol=-1.0, rel_tol=-1.0, max_steps=-1) -> _L.OdeDesc:
@@ -235,6 +236,12 @@ class Monodomain:
         _L.check(self._lib.cfg_ionic_get_states(ion, _L.dptr(a)))
         return a
 
+    def set_states(self, a: np.ndarray):
+        """Ionic states as [n_states][n_cells] (importFields)."""
+        ion = self._lib.cfg_monodomain_ionic(self.h)
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        _L.check(self._lib.cfg_ionic_set_states(ion, _L.dptr(a)))
+
     def rhs_evaluations(self) -> int:
         ion = self._lib.cfg_monodomain_ionic(self.h)
         v = C.c_ulonglong()
@@ -271,7 +278,8 @@ class Monodomain:
 
 
 # NUM_STATES of the compiled models
-STATE_COUNTS = {"TNNP": 17, "ORd": 41, "ToRORd_dynCl": 45, "AlievPanfilov": 2, "BuenoOrovio": 4}
+STATE_COUNTS = {"TNNP": 17, "ORd": 41, "ToRORd_dynCl": 45, "AlievPanfilov": 2, "BuenoOrovio": 4,
+                "monodomainFDAManufactured": 4}
 
 
 class BatchCells:

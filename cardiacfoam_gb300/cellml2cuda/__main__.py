@@ -10,7 +10,7 @@ from pathlib import Path
 
 import json
 
-from .emit import emit_c, emit_cuda, ident
+from .emit import TISSUE_FLAGS, emit_c, emit_cuda, ident
 from .model import WRAPPERS, load_model
 from .opcount import count_rhs
 
@@ -30,8 +30,7 @@ def main(argv=None):
     counts = {}
     for name in args.models:
         m = load_model(args.ionic_models, name)
-        tissue = {"myocyte": 4, "epicardialCells": 1, "endocardialCells": 3,
-                  "mCells": 2}[m.tissues[0]]
+        tissue = TISSUE_FLAGS[m.tissues[0]]
         counts[name] = count_rhs(m, tissue)
         rel = f"src/ionicModels/{WRAPPERS[name]['dir']}/{WRAPPERS[name]['header']}"
         (cu_dir / f"{ident(name)}.cuh").write_text(emit_cuda(m, rel))

@@ -40,6 +40,7 @@ WIDE_STATES = {
                      "Cajsr", "Cai", "Cli", "Clss"],
     "AlievPanfilov": ["u", "recovery_r"],
     "BuenoOrovio": ["u", "v", "w", "s"],
+    "monodomainFDAManufactured": ["V", "u1", "u2", "u3"],
 }
 
 # constants a batched run may scale per cell (log-uniform factors); the
@@ -54,8 +55,14 @@ SCALABLE = {
                      "GKs": "AC_GKs_b", "GK1": "AC_GK1_b", "Gto": "AC_Gto_b"},
     "AlievPanfilov": {},
     "BuenoOrovio": {},
+    "monodomainFDAManufactured": {},
 }
 SCALE_ORDER = ["GNa", "GCaL", "GKr", "GKs", "GK1", "Gto"]
+
+# tissue keys and their flags; the manufactured-solution model selects its
+# constants by mesh dimension instead (flags 11-13: dimension = flag - 10)
+TISSUE_FLAGS = {"epicardialCells": 1, "mCells": 2, "endocardialCells": 3, "myocyte": 4,
+                "1D": 11, "2D": 12, "3D": 13}
 
 # intracellular calcium state of each model (peak Ca of a beat)
 CALCIUM_STATE = {"TNNP": "Ca_i", "ORd": "Ca_i", "ToRORd_dynCl": "Cai"}
@@ -260,6 +267,8 @@ class _CudaPrinter(_Printer):
     def var(self, v: Var) -> str:
         if v.name == "tissueFlag":
             return "tissue"
+        if v.name == "dimension":
+            return "(tissue - 10)"
         if v.name == "solveVmWithinODESolver":
             return "SOLVE_VM"
         if v.name == "VOI":
@@ -391,8 +400,7 @@ def emit_cuda(m: Model, src_rel: str) -> str:
     L.append(f"constexpr double IION_SCALE = {m.iion_scale!r};")
     L.append(f"constexpr double TIME_SCALE = {m.time_scale!r};")
     L.append(f'constexpr int VM_MAP = CFG_VM_{m.vm_to_state.upper()};')
-    tis = [{"epicardialCells": 1, "mCells": 2, "endocardialCells": 3, "myocyte": 4}[t]
-           for t in m.tissues]
+    tis = [TISSUE_FLAGS[t] for t in m.tissues]
     L.append("constexpr int N_TISSUES = %d;" % len(tis))
     L.append("static const int TISSUES[] = {" + ", ".join(str(t) for t in tis) + ", 0};")
     L.append("using TissueSet = TissueList<" + ", ".join(str(t) for t in tis) + ">;")
@@ -564,7 +572,7 @@ class _CPrinter(_Printer):
         return f"{arr}[{self.pre}_{kind}_{r.name}]"
 
     def var(self, v: Var) -> str:
-        return {"tissueFlag": "tissueFlag", "VOI": "VOI",
+        return {"tissueFlag": "tissueFlag", "VOI": "VOI", "dimension": "(tissueFlag - 10)",
                 "solveVmWithinODESolver": "solveVm"}[v.name]
 
     def call(self, c: Call) -> str:

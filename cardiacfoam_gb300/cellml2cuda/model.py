@@ -291,6 +291,18 @@ WRAPPERS = {
                         tissues=["endocardialCells", "mCells", "epicardialCells"],
                         vm_to_state="bueno", iion_name="Jion", iion_scale=85.7,
                         time_scale=1.0),
+    # monodomainFDAManufactured.C:54-72 (dimension selects the constants),
+    # 88-132 (solveODE: S[V] = Vm, model time = t [s], h = min(h, deltaT),
+    # Im = Iion / Cm with Cm = 2).  The verification model of the
+    # manufactured-solution convergence study.
+    "monodomainFDAManufactured": dict(
+        dir="monodomainFDAManufactured", header="monodomainFDAManufactured_2014.H",
+        names="monodomainFDAManufactured_2014Names.H", prefix="monodomainFDAManufactured",
+        init_fn="monodomainFDAManufacturedInitConsts",
+        rates_fn="monodomainFDAManufacturedComputeVariables",
+        variables_fns=["monodomainFDAManufacturedComputeVariables"],
+        tissues=["1D", "2D", "3D"],
+        vm_to_state="identity", iion_name="Iion", iion_scale=0.5, time_scale=1000.0),
 }
 
 
@@ -302,7 +314,7 @@ def load_model(ionic_models_dir: Union[str, Path], name: str) -> Model:
     states = _enum_names(names_txt, "STATES_INDEX", "STATE_INDEX")
     algebraic = _enum_names(names_txt, "ALGEBRAIC_INDEX")
     constants = _enum_names(names_txt, "CONSTANTS_INDEX", "CONSTANT_INDEX")
-    init = _parse_function(hdr_txt, w["prefix"] + "initConsts")
+    init = _parse_function(hdr_txt, w.get("init_fn", w["prefix"] + "initConsts"))
     rates = _parse_function(hdr_txt, w["rates_fn"])
     variables = []
     for fn in w["variables_fns"]:

@@ -33,14 +33,15 @@ class _Eval:
             return int(e.text) if e.is_int_literal else e.value
         if isinstance(e, Ref):
             if e.array == "STATES":
-                return self.Y[e.name]
+                return self.Y.get(e.name, 0.5)   # states initConsts leaves unset
             if e.array == "CONSTANTS":
                 return self.C.get(e.name, 0.0)
             if e.array == "ALGEBRAIC":
                 return self.A.get(e.name, 0.0)
             return self.R.get(e.name, 0.0)
         if isinstance(e, Var):
-            return {"tissueFlag": self.tissue, "VOI": 0.0, "solveVmWithinODESolver": 0}[e.name]
+            return {"tissueFlag": self.tissue, "dimension": self.tissue - 10, "VOI": 0.0,
+                "solveVmWithinODESolver": 0}[e.name]
         if isinstance(e, Unary):
             v = self.ev(e.e)
             return -v if e.op == "-" else (v if e.op == "+" else float(not v))

@@ -31,6 +31,10 @@ int tissue_flag(const char* t)
     if (!std::strcmp(t, "mCells")) return 2;
     if (!std::strcmp(t, "endocardialCells")) return 3;
     if (!std::strcmp(t, "myocyte")) return 4;
+    // the manufactured-solution model's `dimension` key
+    if (!std::strcmp(t, "1D")) return 11;
+    if (!std::strcmp(t, "2D")) return 12;
+    if (!std::strcmp(t, "3D")) return 13;
     return -1;
 }
 
@@ -41,6 +45,9 @@ static const char* tissue_name(int f)
     case 2: return "mCells";
     case 3: return "endocardialCells";
     case 4: return "myocyte";
+    case 11: return "1D";
+    case 12: return "2D";
+    case 13: return "3D";
     default: return "unknown";
     }
 }

@@ -201,6 +201,7 @@ CFG_D __forceinline__ double state0_to_mv(double u)
 {
     if constexpr (M::VM_MAP == CFG_VM_ALIEV) return u * 100.0 - 80.0;
     else if constexpr (M::VM_MAP == CFG_VM_BUENO) return u * 85.7 - 84.0;
+    else if constexpr (M::VM_MAP == CFG_VM_IDENTITY) return u;
     else return u;
 }
 
@@ -237,7 +238,7 @@ __global__ void batch_init_kernel(BatchLaunch p, const double* scales, int tissu
     const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= p.n) return;
     double C[M::NC] = {};
-    double y[M::NS];
+    double y[M::NS] = {};   // states initConsts leaves unset are zero
     double sc[6];
     const double* scp = nullptr;
     if (scales) {

@@ -18,6 +18,7 @@
 #define CFG_VM_MV 0      // mV (TNNP.C:137, ORd.C:125, ToRORd_dynCl.C:125)
 #define CFG_VM_ALIEV 1   // (1000 Vm + 80) / 100 (AlievPanfilov.C:121)
 #define CFG_VM_BUENO 2   // (1000 Vm + 84) / 85.7 (BuenoOrovio.C:120)
+#define CFG_VM_IDENTITY 3  // Vm itself (monodomainFDAManufactured.C:108)
 
 namespace cfg {
 

@@ -118,6 +118,7 @@ CFG_D __forceinline__ double vm_to_state0(double vm)
 {
     if constexpr (MAP == CFG_VM_ALIEV) return (vm * 1000.0 + 80) / 100;
     else if constexpr (MAP == CFG_VM_BUENO) return (vm * 1000.0 + 84) / 85.7;
+    else if constexpr (MAP == CFG_VM_IDENTITY) return vm;
     else return vm * 1000.0;
 }
 
@@ -125,7 +126,12 @@ CFG_D __forceinline__ double vm_to_state0(double vm)
 template <class M>
 CFG_D __forceinline__ void model_times(double t0, double dt, double& ts, double& te, double& dtm)
 {
-    if constexpr (M::TIME_SCALE == 1.0) {
+    if constexpr (M::TIME_SCALE == 1000.0) {
+        // model time in seconds (monodomainFDAManufactured.C:96-97)
+        ts = t0;
+        te = t0 + dt;
+        dtm = dt;
+    } else if constexpr (M::TIME_SCALE == 1.0) {
         ts = t0 * 1000;
         te = (t0 + dt) * 1000;
         dtm = dt * 1000.0;
@@ -191,7 +197,7 @@ __device__ __noinline__ R rhs_eval(double t, const R* y, const KS* K, R* dydt, i
 // arithmetic type R, which is what the right-hand side reads.
 template <class M, class R>
 struct CellState {
-    double y[M::NS];
+    double y[M::NS] = {};   // states initConsts leaves unset are zero
     R yf[M::NS];
 };
 
@@ -405,7 +411,7 @@ __global__ void __launch_bounds__(128, CFG_IONIC_MIN_BLOCKS) ionic_step_kernel(I
         } else {
             tissue = p.tissue_cell ? int(p.tissue_cell[c]) : p.tissue;
             double C[M::NC] = {};   // the reference zero-fills CONSTANTS
-            double yinit[NS];
+            double yinit[NS] = {};
             double sc[6];
             const double* scp = nullptr;
             if (p.scales) {
@@ -459,7 +465,7 @@ __global__ void ionic_init_kernel(long long n, int tissue, const unsigned char* 
     if (c >= n) return;
     const int t = tissue_cell ? int(tissue_cell[c]) : tissue;
     double C[M::NC] = {};
-    double y[M::NS];
+    double y[M::NS] = {};   // states initConsts leaves unset are zero
     double sc[6];
     const double* scp = nullptr;
     if (scales) {

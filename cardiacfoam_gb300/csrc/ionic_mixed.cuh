@@ -358,7 +358,7 @@ ionic_mixed_kernel(IonicLaunch p)
         } else {
             const int tissue = p.tissue_cell ? int(p.tissue_cell[c]) : p.tissue;
             double C[M::NC] = {};   // the reference zero-fills CONSTANTS
-            double yinit[NS];
+            double yinit[NS] = {};
             double sc[6];
             const double* scp = nullptr;
             if (p.scales) {

@@ -8,6 +8,7 @@
 #include "models/ord.cuh"
 #include "models/tnnp.cuh"
 #include "models/torord_dyncl.cuh"
+#include "models/monodomainfdamanufactured.cuh"
 
 #define CFG_DECLARE_MODEL(ns)                                                                  \
     extern "C" cudaError_t cfg_ionic_step_##ns##_fp64(const cfg::IonicLaunch&, int,           \
@@ -36,6 +37,7 @@ CFG_DECLARE_MODEL(ord)
 CFG_DECLARE_MODEL(torord_dyncl)
 CFG_DECLARE_MODEL(alievpanfilov)
 CFG_DECLARE_MODEL(buenoorovio)
+CFG_DECLARE_MODEL(monodomainfdamanufactured)
 
 namespace cfg {
 namespace {
@@ -100,6 +102,7 @@ const IonicModelOps* table()
         CFG_MODEL_ENTRY("ToRORd_dynCl", torord_dyncl),
         CFG_MODEL_ENTRY("AlievPanfilov", alievpanfilov),
         CFG_MODEL_ENTRY("BuenoOrovio", buenoorovio),
+        CFG_MODEL_ENTRY("monodomainFDAManufactured", monodomainfdamanufactured),
         IonicModelOps{},
     };
     return models;

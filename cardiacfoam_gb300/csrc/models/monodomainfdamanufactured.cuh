@@ -1,0 +1,166 @@
+// Generated by cardiacfoam_gb300.cellml2cuda from src/ionicModels/monodomainFDAManufactured/monodomainFDAManufactured_2014.H.
+// The equations are the published cell model as cellML2foam wrote them;
+// regenerate with `python -m cardiacfoam_gb300.cellml2cuda` instead of editing.
+#pragma once
+#include "../ionic_common.cuh"
+
+namespace cfg { namespace monodomainfdamanufactured {
+
+constexpr int NS = 4;
+constexpr int NC = 3;
+constexpr int NA = 1;
+enum State { S_V, S_u1, S_u2, S_u3 };
+enum Constant { C_Cm, C_Beta, C_Chi };
+// states kept in double in the mixed form (bit i = state i)
+constexpr unsigned long long WIDE_MASK = 0xfull;
+constexpr double IION_SCALE = 0.5;
+constexpr double TIME_SCALE = 1000.0;
+constexpr int VM_MAP = CFG_VM_IDENTITY;
+constexpr int N_TISSUES = 3;
+static const int TISSUES[] = {11, 12, 13, 0};
+using TissueSet = TissueList<11, 12, 13>;
+static const char* const STATE_NAMES[NS] = {"V", "u1", "u2", "u3"};
+CFG_HD inline bool tissue_supported(int t) { return t == 11 || t == 12 || t == 13; }
+
+// per-cell conductance scales: index into the scale vector, or -1
+constexpr int SCALE_GNa = -1;
+constexpr int SCALE_GCaL = -1;
+constexpr int SCALE_GKr = -1;
+constexpr int SCALE_GKs = -1;
+constexpr int SCALE_GK1 = -1;
+constexpr int SCALE_Gto = -1;
+
+// Constants that depend on the per-cell conductance scales and that the
+// right-hand side reads: the scaled conductances and every constant
+// initConsts derives from them.  sd_slot(i) is constant i's index in a
+// cell's vector of them, or -1 (then the constant is the tissue's).
+constexpr int NSD = 0;
+CFG_HD constexpr int sd_const(int k)
+{
+    switch (k) {
+    default: return -1;
+    }
+}
+CFG_HD constexpr int sd_slot(int i)
+{
+    switch (i) {
+    default: return -1;
+    }
+}
+// intracellular calcium state (peak Ca of a beat), or -1
+constexpr int CA_STATE = -1;
+
+// Constants and initial states (initConsts).  `scale` may be null;
+// otherwise scale[SCALE_x] multiplies the named conductance right after
+// it is assigned, before constants derived from it are computed.
+CFG_HD __forceinline__ void init_consts(double* C, double* y, int tissue, const double* scale)
+{
+    (void)tissue; (void)scale;
+    C[C_Cm] = 2.0;
+    C[C_Chi] = 3.0;
+    if (((tissue - 10) == 1)) {
+        C[C_Beta] = (-1.1);
+    } else {
+        if (((tissue - 10) == 2)) {
+            C[C_Beta] = (-5.9);
+        } else {
+            if (((tissue - 10) == 3)) {
+                C[C_Beta] = (-8.6);
+            } else {
+                /* unsupported configuration in the reference */
+            }
+        }
+    }
+}
+
+// initConsts evaluated per tissue flag (IEEE double, the header's order of
+// operations): cval<T>(i) is constant i for tissue T.  Kernels for one uniform
+// tissue without per-cell scales read constants from here, so the compiler
+// folds them into the instructions.
+template <int T> CFG_HD constexpr double cval(int i);
+template <> CFG_HD constexpr double cval<11>(int i)
+{
+    switch (i) {
+    case 0: return 2.0;
+    case 1: return -1.1;
+    case 2: return 3.0;
+    default: return 0.0;
+    }
+}
+template <> CFG_HD constexpr double cval<12>(int i)
+{
+    switch (i) {
+    case 0: return 2.0;
+    case 1: return -5.9;
+    case 2: return 3.0;
+    default: return 0.0;
+    }
+}
+template <> CFG_HD constexpr double cval<13>(int i)
+{
+    switch (i) {
+    case 0: return 2.0;
+    case 1: return -8.6;
+    case 2: return 3.0;
+    default: return 0.0;
+    }
+}
+
+// Right-hand side as used by derivatives(): dydt for every state that the
+// reference assigns (RATES of V only when SOLVE_VM).  Returns Iion.
+// Y(i) reads state i as R (each state once, before any dydt store),
+// K(i) reads constant i as R.
+template <class R, bool SOLVE_VM, class YS, class KS>
+__device__ __forceinline__ R rhs(double t, const YS& Y, const KS& K, R* dydt, int tissue, const CfgStimulus& stim)
+{
+    (void)tissue; (void)stim; (void)t;
+    const R y_V = Y(S_V);
+    const R y_u1 = Y(S_u1);
+    const R y_u2 = Y(S_u2);
+    const R y_u3 = Y(S_u3);
+    dydt[S_V] = R(0.0);
+    dydt[S_u1] = ((cfg_ipow<2>(((y_u1 + y_u3) - y_V)) * cfg_ipow<2>(y_u2)) + (((R(0.5) * ((y_u1 + y_u3) - y_V)) * cfg_ipow<2>(y_u2)) * (y_V - y_u3)));
+    dydt[S_u2] = ((-((y_u1 + y_u3) - y_V)) * cfg_ipow<3>(y_u2));
+    dydt[S_u3] = 0;
+    R a_Iion = ((((((-R(0.5)) * K(C_Cm)) * ((y_u1 + y_u3) - y_V)) * cfg_ipow<2>(y_u2)) * (y_V - y_u3)) + ((K(C_Beta) * (y_V - y_u3)) / K(C_Chi)));
+    return a_Iion;
+}
+
+// Ionic current after the step (computeVariables at tEnd).
+template <class R, bool SOLVE_VM, class YS, class KS>
+__device__ __forceinline__ R iion(double t, const YS& Y, const KS& K, int tissue, const CfgStimulus& stim)
+{
+    (void)tissue; (void)stim; (void)t;
+    R dydt[NS];
+    const R y_V = Y(S_V);
+    const R y_u1 = Y(S_u1);
+    const R y_u2 = Y(S_u2);
+    const R y_u3 = Y(S_u3);
+    dydt[S_V] = R(0.0);
+    dydt[S_u1] = ((cfg_ipow<2>(((y_u1 + y_u3) - y_V)) * cfg_ipow<2>(y_u2)) + (((R(0.5) * ((y_u1 + y_u3) - y_V)) * cfg_ipow<2>(y_u2)) * (y_V - y_u3)));
+    dydt[S_u2] = ((-((y_u1 + y_u3) - y_V)) * cfg_ipow<3>(y_u2));
+    dydt[S_u3] = 0;
+    R a_Iion = ((((((-R(0.5)) * K(C_Cm)) * ((y_u1 + y_u3) - y_V)) * cfg_ipow<2>(y_u2)) * (y_V - y_u3)) + ((K(C_Beta) * (y_V - y_u3)) / K(C_Chi)));
+    (void)dydt;
+    return a_Iion;
+}
+
+// traits bundle used by the kernel templates
+struct Model {
+    static constexpr int NS = monodomainfdamanufactured::NS, NC = monodomainfdamanufactured::NC;
+    static constexpr unsigned long long WIDE_MASK = monodomainfdamanufactured::WIDE_MASK;
+    static constexpr double IION_SCALE = monodomainfdamanufactured::IION_SCALE;
+    static constexpr double TIME_SCALE = monodomainfdamanufactured::TIME_SCALE;
+    static constexpr int VM_MAP = monodomainfdamanufactured::VM_MAP;
+    CFG_HD static __forceinline__ void init(double* C, double* y, int tissue, const double* scale) { init_consts(C, y, tissue, scale); }
+    template <int T> CFG_HD static constexpr double constant(int i) { return cval<T>(i); }
+    static constexpr int NSD = monodomainfdamanufactured::NSD, CA_STATE = monodomainfdamanufactured::CA_STATE;
+    CFG_HD static constexpr int sd_slot(int i) { return monodomainfdamanufactured::sd_slot(i); }
+    CFG_HD static constexpr int sd_const(int k) { return monodomainfdamanufactured::sd_const(k); }
+    template <class R, bool SV, class YS, class KS>
+    __device__ static __forceinline__ R rates(double t, const YS& Y, const KS& K, R* dydt, int tissue, const CfgStimulus& st) { return rhs<R, SV>(t, Y, K, dydt, tissue, st); }
+    template <class R, bool SV, class YS, class KS>
+    __device__ static __forceinline__ R current(double t, const YS& Y, const KS& K, int tissue, const CfgStimulus& st) { return iion<R, SV>(t, Y, K, tissue, st); }
+};
+
+} }  // namespace cfg::monodomainfdamanufactured

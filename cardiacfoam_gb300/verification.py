@@ -1,0 +1,98 @@
+"""Manufactured-solution verification of the monodomain step (the GPU
+counterpart of the reference's ``manufacturedFDAMonodomainVerifier``).
+
+The monodomainFDAManufactured ionic model and the exact solution
+
+    V  = sqrt(1 + t) F(x),   F = cos(pi x) [cos(2 pi y) [cos(3 pi z)]]
+    u1 = (1 + t) G(x) + sqrt(1 + t) F(x),  G = 1 + x [y^2 [z^3]]
+    u2 = G(x)^(-1/2) / (1 + t),  u3 = 0
+
+(src/verificationModels/monodomainVerification/manufacturedFDAReference.H:33-167)
+solve chi Cm dV/dt = div(sigma grad V) - chi Cm Im with zero-gradient walls
+on the unit cube (1D: 1 x 0.1 x 0.1, 2D: 1 x 1 x 0.1), chi = 3, Cm = 2 and
+the tutorial's anisotropic conductivity
+(tutorials/manufacturedSolutions/monodomainPseudoECG/constant/electroProperties).
+Errors are the verifier's L1 (mean), L2 (RMS) and L-infinity norms over the
+cells (manufacturedFDAMonodomainVerifier.C:139-169); the convergence rate
+between two meshes is log(e1/e2)/log(h1/h2) with h = 1/N
+(setupManufacturedFDA/post_processing_manufactured.py:119-124), the time step
+shrinking with h^2 as in the tutorial's sweep (10/20/40/80 cells at
+dt = 8.92857e-3 / 2.24215e-3 / 5.60538e-4 / 1.40174e-4 s, to t = 0.2 s).
+"""
+from __future__ import annotations
+
+import math
+from typing import Dict, Tuple
+
+import numpy as np
+
+from . import api
+from . import lib as _L
+from .mesh import box_mesh
+
+SIGMA = (0.111453302, 0.0, 0.0, 0.121585420, 0.0, 0.030396355)
+CHI, CM = 3.0, 2.0
+END_TIME = 0.2
+SWEEP = {10: 0.00892857, 20: 0.00224215, 40: 0.000560538, 80: 0.000140174}
+
+
+def manufactured_fields(centres: np.ndarray, t: float, dim: int):
+    """Exact V, u1, u2, u3 at the cell centres (computeF/G/V/U,
+    manufacturedFDAReference.H:33-135)."""
+    x, y, z = centres[:, 0], centres[:, 1], centres[:, 2]
+    pi = math.pi
+    if dim == 1:
+        F, G = np.cos(pi * x), 1.0 + x
+    elif dim == 2:
+        F, G = np.cos(pi * x) * np.cos(2.0 * pi * y), 1.0 + x * y ** 2
+    else:
+        F = np.cos(pi * x) * np.cos(2.0 * pi * y) * np.cos(3.0 * pi * z)
+        G = 1.0 + x * y ** 2 * z ** 3
+    s = math.sqrt(1.0 + t)
+    V = s * F
+    u1 = (1.0 + t) * G + s * F
+    u2 = (1.0 / (1.0 + t)) * G ** -0.5
+    return V, u1, u2, np.zeros_like(V)
+
+
+def norms(num: np.ndarray, exact: np.ndarray) -> Tuple[float, float, float]:
+    """(L1 mean, L2 RMS, L-infinity) of num - exact."""
+    d = np.abs(num - exact)
+    return float(d.sum() / d.size), float(math.sqrt((d * d).sum() / d.size)), float(d.max())
+
+
+def rate(e1: float, e2: float, n1: int, n2: int) -> float:
+    """Observed order between meshes of n1 and n2 cells per direction."""
+    return math.log(e1 / e2) / math.log((1.0 / n1) / (1.0 / n2))
+
+
+def mesh_for(dim: int, n: int):
+    """The tutorial's blockMesh: n cells per resolved direction, 0.1 thick
+    (one cell) in the others."""
+    nx, ny, nz = n, (n if dim >= 2 else 1), (n if dim == 3 else 1)
+    return box_mesh(nx, ny, nz, 1.0, 1.0 if dim >= 2 else 0.1, 1.0 if dim == 3 else 0.1)
+
+
+def run(dim: int, n: int, dt: float | None = None, end_time: float = END_TIME,
+        precision: int = _L.PRECISION_FP64, pcg_tol: float = 1e-12) -> Dict:
+    """One manufactured case on the GPU: implicit backward ddt, two PIMPLE
+    correctors (the tutorial's fvSolution), PCG to `pcg_tol`.  Returns the
+    error norms of V, u1 and u2 at the end time."""
+    dt = SWEEP[n] if dt is None else dt
+    mesh = mesh_for(dim, n)
+    md = api.Monodomain(mesh, model="monodomainFDAManufactured", tissue=f"{dim}D", sigma=SIGMA,
+                        chi=CHI, cm=CM, dt=dt, precision=precision, implicit=True,
+                        ddt_backward=True, pcg_tol=pcg_tol, pcg_rel_tol=0.0,
+                        pcg_max_iter=2000, n_outer=2, outer_tol=0.0)
+    V, u1, u2, u3 = manufactured_fields(mesh.centres, 0.0, dim)
+    md.set_field(_L.FIELD_VM, V)
+    md.set_states(np.stack([V, u1, u2, u3]))
+    steps = int(round(end_time / dt))
+    md.run(dt, steps)
+    t = md.time()
+    Ve, u1e, u2e, _ = manufactured_fields(mesh.centres, t, dim)
+    st = md.states()
+    out = {"dim": dim, "n": n, "dt": dt, "steps": steps, "t": t,
+           "V": norms(md.vm(), Ve), "u1": norms(st[1], u1e), "u2": norms(st[2], u2e)}
+    md.close()
+    return out

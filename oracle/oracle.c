@@ -19,6 +19,7 @@
 #include "models/torord_dyncl.h"
 #include "models/alievpanfilov.h"
 #include "models/buenoorovio.h"
+#include "models/monodomainfdamanufactured.h"
 
 void oracle_fatal(const char* what)
 {
@@ -44,7 +45,7 @@ typedef struct {
     int iion;
     double iion_scale;
     double time_scale;  /* model time = 1000 t / time_scale */
-    int vm_map;         /* 0: mV, 1: Aliev-Panfilov u, 2: Bueno-Orovio u */
+    int vm_map;         /* 0: mV, 1: Aliev-Panfilov u, 2: Bueno-Orovio u, 3: Vm */
 } model_info;
 
 static const model_info MODELS[ORACLE_NMODELS] = {
@@ -61,6 +62,11 @@ static const model_info MODELS[ORACLE_NMODELS] = {
     {"BuenoOrovio", BUENOOROVIO_NS, BUENOOROVIO_NA, BUENOOROVIO_NC, buenoorovio_init, buenoorovio_supplement,
      buenoorovio_rates, buenoorovio_variables, BUENOOROVIO_IION_INDEX,
      BUENOOROVIO_IION_SCALE, BUENOOROVIO_TIME_SCALE, 2},
+    {"monodomainFDAManufactured", MONODOMAINFDAMANUFACTURED_NS, MONODOMAINFDAMANUFACTURED_NA,
+     MONODOMAINFDAMANUFACTURED_NC, monodomainfdamanufactured_init,
+     monodomainfdamanufactured_supplement, monodomainfdamanufactured_rates,
+     monodomainfdamanufactured_variables, MONODOMAINFDAMANUFACTURED_IION_INDEX,
+     MONODOMAINFDAMANUFACTURED_IION_SCALE, MONODOMAINFDAMANUFACTURED_TIME_SCALE, 3},
 };
 
 int oracle_model_sizes(int model, int* ns, int* na, int* nc)
@@ -323,6 +329,7 @@ static double vm_to_state0(int map, double vm)
 {
     if (map == 1) return (vm * 1000.0 + 80) / 100;       /* AlievPanfilov.C:121 */
     if (map == 2) return (vm * 1000.0 + 84) / 85.7;      /* BuenoOrovio.C:120 */
+    if (map == 3) return vm;                             /* monodomainFDAManufactured.C:108 */
     return vm * 1000.0;                                  /* TNNP.C:137 */
 }
 
@@ -333,9 +340,11 @@ static long solve_range(oracle_ionic* io, rk_ws* w, long c0, long c1, double t0,
     const model_info* m = io->m;
     const double ts = m->time_scale;
     /* tStart/tEnd in model time: TNNP.C:122-123, AlievPanfilov.C:107-108 */
-    const double t_start = (ts == 1.0) ? t0 * 1000 : t0 * 1000.0 / ts;
-    const double t_end = (ts == 1.0) ? (t0 + dt) * 1000 : (t0 + dt) * 1000.0 / ts;
-    const double dt_model = (ts == 1.0) ? dt * 1000.0 : dt * 1000.0 / ts;
+    /* model time in seconds: monodomainFDAManufactured.C:96-97, 109 */
+    const double t_start = (ts == 1000.0) ? t0 : (ts == 1.0) ? t0 * 1000 : t0 * 1000.0 / ts;
+    const double t_end = (ts == 1000.0) ? t0 + dt
+                       : (ts == 1.0) ? (t0 + dt) * 1000 : (t0 + dt) * 1000.0 / ts;
+    const double dt_model = (ts == 1000.0) ? dt : (ts == 1.0) ? dt * 1000.0 : dt * 1000.0 / ts;
     long total = 0;
     for (long c = c0; c < c1; c++) {
         double* y = io->y + (size_t)c * (size_t)m->ns;
@@ -826,14 +835,21 @@ static void update_activation(oracle_tissue* T, double dt)
     }
 }
 
+/* The ionic model of the tissue, constructed with initialDeltaT = dt as
+ * the domain constructs it; done by the first step when not called before
+ * (e.g. to import states first). */
+int oracle_tissue_init_ionic(oracle_tissue* T, double dt)
+{
+    if (!T->ionic)
+        T->ionic = oracle_ionic_new(T->d.model, T->n, T->d.tissue, dt, 0, &T->d.ode, NULL, NULL);
+    return T->ionic ? 0 : -1;
+}
+
 /* Advance by dt [s]: runTime++ then electroModel::evolve with the staggered
  * advance scheme (stimulus -> ionic -> diffusion -> activation time). */
 int oracle_tissue_step(oracle_tissue* T, double dt, int nthreads)
 {
-    if (!T->ionic) {
-        T->ionic = oracle_ionic_new(T->d.model, T->n, T->d.tissue, dt, 0, &T->d.ode, NULL, NULL);
-        if (!T->ionic) return -1;
-    }
+    if (oracle_tissue_init_ionic(T, dt)) return -1;
     /* Time::operator++ : value += deltaT; store old-time levels of Vm */
     T->t = T->t + dt;
     T->time_index++;

@@ -31,7 +31,7 @@ extern "C" {
 #endif
 
 enum { ORACLE_TNNP = 0, ORACLE_ORD = 1, ORACLE_TORORD = 2, ORACLE_ALIEV = 3,
-       ORACLE_BUENO = 4, ORACLE_NMODELS = 5 };
+       ORACLE_BUENO = 4, ORACLE_MMS = 5, ORACLE_NMODELS = 6 };
 
 /* --- model-level entry points (golden-vector pins) --------------------- */
 int oracle_model_sizes(int model, int* ns, int* na, int* nc);
@@ -103,6 +103,7 @@ oracle_tissue* oracle_tissue_new(const oracle_tissue_desc*, const oracle_mesh*);
 void oracle_tissue_free(oracle_tissue*);
 /* One runTime++ / evolve(): returns PCG iterations of the step (all outer
  * correctors), or -1 on failure.  `nthreads` parallelises the ionic loop. */
+int oracle_tissue_init_ionic(oracle_tissue* T, double dt);
 int oracle_tissue_step(oracle_tissue*, double dt, int nthreads);
 double oracle_tissue_time(const oracle_tissue*);
 double* oracle_tissue_vm(oracle_tissue*);

@@ -14,8 +14,10 @@ import numpy as np
 
 from . import build as _build
 
-MODELS = {"TNNP": 0, "ORd": 1, "ToRORd_dynCl": 2, "AlievPanfilov": 3, "BuenoOrovio": 4}
-TISSUES = {"epicardialCells": 1, "mCells": 2, "endocardialCells": 3, "myocyte": 4}
+MODELS = {"TNNP": 0, "ORd": 1, "ToRORd_dynCl": 2, "AlievPanfilov": 3, "BuenoOrovio": 4,
+          "monodomainFDAManufactured": 5}
+TISSUES = {"epicardialCells": 1, "mCells": 2, "endocardialCells": 3, "myocyte": 4,
+           "1D": 11, "2D": 12, "3D": 13}
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
@@ -93,6 +95,7 @@ def lib():
         for f in ("vm", "iion", "activation", "source"):
             getattr(L, f"oracle_tissue_{f}").argtypes = [C.c_void_p]
             getattr(L, f"oracle_tissue_{f}").restype = _dp
+        L.oracle_tissue_init_ionic.argtypes = [C.c_void_p, C.c_double]
         L.oracle_tissue_ionic.argtypes = [C.c_void_p]
         L.oracle_tissue_ionic.restype = C.c_void_p
         L.oracle_tissue_last_solves.argtypes = [C.c_void_p, _dp, _dp, _ip, C.c_int]
@@ -275,6 +278,20 @@ class Tissue:
 
     def vm(self):
         return self._arr("vm")
+
+    def set_vm(self, a):
+        p = lib().oracle_tissue_vm(self.h)
+        np.ctypeslib.as_array(p, shape=(self.n,))[:] = a
+
+    def set_states(self, a, dt):
+        """Ionic states as [n_states][n_cells]; constructs the ionic model
+        with initialDeltaT = dt if no step has run yet."""
+        if lib().oracle_tissue_init_ionic(self.h, dt):
+            raise RuntimeError("oracle ionic model construction failed")
+        p = lib().oracle_tissue_ionic(self.h)
+        ns = sizes(list(MODELS)[self.desc.model])[0]
+        sp = lib().oracle_ionic_states(p)
+        np.ctypeslib.as_array(sp, shape=(self.n, ns))[:] = np.asarray(a).T
 
     def iion(self):
         return self._arr("iion")
