@@ -93,6 +93,24 @@ class IonicModel:
             out.append(buf.value.decode())
         return out
 
+    def sweep_currents(self) -> list:
+        """availableSweepCurrents."""
+        buf = C.create_string_buffer(8192)
+        _L.check(self._lib.cfg_ionic_sweep_currents(self.h, buf, len(buf)))
+        return buf.value.decode().split()
+
+    def sweep_current(self, current: str, v_min: float, v_max: float, n_points: int):
+        """sweepCurrent: (header column names, [n_points, columns] table)."""
+        nc = C.c_int()
+        hdr = C.create_string_buffer(8192)
+        _L.check(self._lib.cfg_ionic_sweep_current(self.h, current.encode(), v_min, v_max,
+                                                   n_points, None, C.byref(nc), hdr, len(hdr)))
+        out = np.zeros((n_points, nc.value))
+        _L.check(self._lib.cfg_ionic_sweep_current(self.h, current.encode(), v_min, v_max,
+                                                   n_points, out.ctypes.data, C.byref(nc),
+                                                   None, 0))
+        return hdr.value.decode().split(","), out
+
     def states(self) -> np.ndarray:
         a = np.zeros((self.n_states, self.n))
         _L.check(self._lib.cfg_ionic_get_states(self.h, _L.dptr(a)))

@@ -526,6 +526,42 @@ def emit_cuda(m: Model, src_rel: str) -> str:
     L.append(f"    return a_{m.iion_name};")
     L.append("}")
     L.append("")
+    # every algebraic of the sweep body (sweepCurrent)
+    L.append("// computeVariables with every algebraic stored: A[k] is ALGEBRAIC[k] (0 for")
+    L.append("// the ones the body does not assign), dydt the RATES it assigns.")
+    L.append("template <class R, bool SOLVE_VM, class YS, class KS>")
+    L.append("__device__ __forceinline__ void variables_all(double t, const YS& Y, const KS& K, "
+             "R* A, R* dydt, int tissue, const CfgStimulus& stim)")
+    L.append("{")
+    L.append("    (void)tissue; (void)stim; (void)t;")
+    pr = _CudaPrinter(m, use_before_def(m.sweep_body), "rhs")
+    body = []
+    for name in _predeclare_conditional_algebraics(m, m.sweep_body, body, "    "):
+        body.append(f"    R a_{name} = R(0);")
+        pr.defined.add(name)
+    _cuda_body(m, m.sweep_body, pr, "    ", body)
+    L.extend(_state_loads(m, pr))
+    L.extend(body)
+    for k, a in enumerate(m.algebraic):
+        if a in pr.defined:
+            L.append(f"    A[{k}] = a_{a};")
+    L.append("}")
+    L.append("")
+    # the reference's name tables and sweepCurrent dependency map
+    def strtab(name, items, n):
+        items = list(items) + [""] * max(0, n - len(items))
+        L.append(f"static const char* const {name}[{max(1, n)}] = {{" +
+                 (", ".join(f'"{x}"' for x in items[:n]) if n else '""') + "};")
+    L.append("// STATES_NAMES / ALGEBRAIC_NAMES as the header spells them; matched by")
+    L.append("// position, entries the header leaves out are empty")
+    strtab("STATE_STRINGS", m.state_strings, len(m.states))
+    strtab("ALG_STRINGS", m.alg_strings, len(m.algebraic))
+    L.append("// <Model>DependencyMap(): current -> comma-separated variables, null-ended")
+    L.append("static const char* const SWEEP_CURRENTS[] = {" +
+             "".join(f'"{k}", ' for k, _ in m.sweep_deps) + "nullptr};")
+    L.append("static const char* const SWEEP_DEPS[] = {" +
+             "".join('"' + ",".join(v) + '", ' for _, v in m.sweep_deps) + "nullptr};")
+    L.append("")
     L.append("// traits bundle used by the kernel templates")
     L.append("struct Model {")
     L.append("    static constexpr int NS = " + ns + "::NS, NC = " + ns + "::NC;")
@@ -539,6 +575,11 @@ def emit_cuda(m: Model, src_rel: str) -> str:
              "{ return cval<T>(i); }")
     L.append("    static constexpr int NSD = " + ns + "::NSD, CA_STATE = " + ns + "::CA_STATE;")
     L.append("    CFG_HD static constexpr int sd_slot(int i) { return " + ns + "::sd_slot(i); }")
+    L.append("    static constexpr int NA = " + ns + "::NA;")
+    L.append("    template <class R, bool SV, class YS, class KS>")
+    L.append("    __device__ static __forceinline__ void all_variables(double t, const YS& Y, "
+             "const KS& K, R* A, R* dydt, int tissue, const CfgStimulus& st) "
+             "{ variables_all<R, SV>(t, Y, K, A, dydt, tissue, st); }")
     L.append("    CFG_HD static constexpr int sd_const(int k) { return " + ns + "::sd_const(k); }")
     L.append("    template <class R, bool SV, class YS, class KS>")
     L.append("    __device__ static __forceinline__ R rates(double t, const YS& Y, const KS& K, "

@@ -66,6 +66,15 @@ class Model:
     iion_scale: float = 1.0         # Im = scale * ALGEBRAIC[iion]
     time_scale: float = 1.0         # model time = t[s] * 1000 / time_scale
     extra_args: List[str] = field(default_factory=list)
+    # the header's string tables (ALGEBRAIC_NAMES may differ from the enum:
+    # entries are matched by position, as ionicModelIO does) and the
+    # <Model>DependencyMap() of sweepCurrent: (current, [variable names])
+    state_strings: List[str] = field(default_factory=list)
+    alg_strings: List[str] = field(default_factory=list)
+    sweep_deps: List = field(default_factory=list)
+    # the body sweepCurrent evaluates (the first variables function only,
+    # e.g. TNNP.C:250-261 calls TNNPcomputeVariables without computeRates)
+    sweep_body: List[Stmt] = field(default_factory=list)
 
     def state_index(self, n: str) -> int:
         return self.states.index(n)
@@ -306,6 +315,24 @@ WRAPPERS = {
 }
 
 
+def _string_table(text: str, table: str) -> List[str]:
+    m = re.search(r"(\w*)" + table + r"\s*\[[^\]]*\]\s*=\s*\{(.*?)\};", text, re.S)
+    return re.findall(r'"([^"]*)"', m.group(2)) if m else []
+
+
+def _dependency_map(text: str):
+    """Entries of <Model>DependencyMap(): {"INa", wordList({"i_Na", ...})}."""
+    body, _ = _function_body(text, next(iter(re.findall(r"\b(\w+DependencyMap)\s*\(\s*\)",
+                                                         text)), "NoDependencyMap"))
+    if body is None:
+        return []
+    out = []
+    for key, items in re.findall(r'\{\s*"(\w+)"\s*,\s*Foam::wordList\s*\(\s*\{([^}]*)\}\s*\)\s*\}',
+                                 body):
+        out.append((key, re.findall(r'"([^"]*)"', items)))
+    return out
+
+
 def load_model(ionic_models_dir: Union[str, Path], name: str) -> Model:
     w = WRAPPERS[name]
     d = Path(ionic_models_dir) / w["dir"]
@@ -326,6 +353,11 @@ def load_model(ionic_models_dir: Union[str, Path], name: str) -> Model:
               tissues=list(w["tissues"]), vm_to_state=w["vm_to_state"],
               iion_name=w["iion_name"], iion_scale=w["iion_scale"],
               time_scale=w["time_scale"])
+    raw = (d / w["header"]).read_text()
+    m.state_strings = _string_table(raw, "STATES_NAMES")
+    m.alg_strings = _string_table(raw, "ALGEBRAIC_NAMES")
+    m.sweep_deps = _dependency_map(_strip_comments(raw))
+    m.sweep_body = _parse_function(hdr_txt, w["variables_fns"][0])
     _check_names(m)
     return m
 

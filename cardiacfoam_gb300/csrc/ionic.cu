@@ -418,3 +418,186 @@ int cfg_ionic_destroy(cfg_ionic* ion)
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------- sweepCurrent
+
+namespace cfg {
+namespace {
+
+// ionicVariableCompatibility::canonicalName (ionicVariableCompatibility.C:37-59):
+// lower case, separators dropped, an "av" prefix stripped
+std::string canonical_name(const char* raw)
+{
+    std::string out;
+    for (const char* p = raw; *p; ++p) {
+        char c = *p;
+        if (c >= 'A' && c <= 'Z') c = char(c - 'A' + 'a');
+        if (c == '_' || c == '-' || c == ' ') continue;
+        out.push_back(c);
+    }
+    if (out.size() > 2 && out[0] == 'a' && out[1] == 'v') return out.substr(2);
+    return out;
+}
+
+bool same_name(const std::string& name, const char* table_entry)
+{
+    return name == table_entry || canonical_name(name.c_str()) == canonical_name(table_entry);
+}
+
+// resolveVariable (ionicVariableCompatibility.C:215-275): Vm, a state, an
+// algebraic, or RATES_<state> (prefix case-insensitive).  The column is an
+// index into a sweep row [states | algebraic | rates].
+bool resolve_column(const IonicModelOps* m, const std::string& name, int* col)
+{
+    if (name == "Vm" || canonical_name(name.c_str()) == "vm") {
+        *col = 0;
+        return true;
+    }
+    for (int s = 0; s < m->ns; ++s)
+        if (same_name(name, m->state_strings[s])) { *col = s; return true; }
+    for (int a = 0; a < m->na; ++a)
+        if (m->alg_strings[a][0] && same_name(name, m->alg_strings[a])) { *col = m->ns + a; return true; }
+    static const char prefix[] = "RATES_";
+    if (name.size() > 6) {
+        bool ok = true;
+        for (int i = 0; i < 6; ++i) {
+            char c = name[size_t(i)];
+            if (c >= 'A' && c <= 'Z') c = char(c - 'A' + 'a');
+            char q = prefix[i];
+            if (q >= 'A' && q <= 'Z') q = char(q - 'A' + 'a');
+            ok = ok && c == q;
+        }
+        if (ok) {
+            const std::string st = name.substr(6);
+            for (int s = 0; s < m->ns; ++s)
+                if (same_name(st, m->state_strings[s])) { *col = m->ns + m->na + s; return true; }
+        }
+    }
+    return false;
+}
+
+std::vector<std::string> split_commas(const char* s)
+{
+    std::vector<std::string> out;
+    std::string cur;
+    for (const char* p = s; *p; ++p) {
+        if (*p == ',') { out.push_back(cur); cur.clear(); }
+        else cur.push_back(*p);
+    }
+    if (!cur.empty()) out.push_back(cur);
+    return out;
+}
+
+}  // namespace
+}  // namespace cfg
+
+extern "C" {
+
+int cfg_ionic_sweep_currents(const cfg_ionic* ion, char* buf, size_t len)
+{
+    if (!ion || !buf || !len) return fail(CFG_ERR_INVALID, "null argument");
+    std::string s;
+    for (const char* const* c = ion->ops->sweep_currents; *c; ++c) {
+        if (!s.empty()) s += ' ';
+        s += *c;
+    }
+    std::snprintf(buf, len, "%s", s.c_str());
+    return CFG_OK;
+}
+
+int cfg_ionic_sweep_current(cfg_ionic* ion, const char* current, double v_min, double v_max,
+                            int n_points, double* out, int* n_columns, char* header,
+                            size_t header_len)
+{
+    if (!ion || !current) return fail(CFG_ERR_INVALID, "null argument");
+    const IonicModelOps* m = ion->ops;
+    const char* deps = nullptr;
+    std::string avail;
+    for (int k = 0; m->sweep_currents[k]; ++k) {
+        if (!std::strcmp(m->sweep_currents[k], current)) deps = m->sweep_deps[k];
+        avail += std::string(avail.empty() ? "" : " ") + m->sweep_currents[k];
+    }
+    if (!deps)
+        return fail(CFG_ERR_INVALID, "Unknown current: %s\nAvailable currents: (%s)", current,
+                    avail.c_str());
+    const std::vector<std::string> names = split_commas(deps);
+    std::vector<int> cols(names.size());
+    for (size_t k = 0; k < names.size(); ++k)
+        if (!resolve_column(m, names[k], &cols[k]))
+            return fail(CFG_ERR_INVALID, "Unknown debug variable: %s. Expected Vm, one of the "
+                        "STATE names, one of the ALGEBRAIC names, or a rate name of the form "
+                        "RATES_<stateName>.", names[k].c_str());
+    const int nc = 1 + int(names.size());
+    if (n_columns) *n_columns = nc;
+    if (header && header_len) {
+        std::string h = "V";
+        for (const std::string& s : names) h += "," + s;
+        std::snprintf(header, header_len, "%s", h.c_str());
+    }
+    if (!out) return CFG_OK;
+    if (n_points < 2) return fail(CFG_ERR_INVALID, "a sweep needs at least 2 points");
+
+    // states of integration point 0 and the model's constants
+    const long long n = ion->n;
+    const int p = ion->precision, ns = m->ns;
+    std::vector<double> y0(static_cast<size_t>(ns));
+    for (int i = 0; i < ns; ++i) {
+        const int w = m->wide_of[p * ns + i], s = m->slot_of[p * ns + i];
+        if (w) {
+            double v = 0.0;
+            CFG_CUDA_TRY(cudaMemcpy(&v, ion->d_yw + size_t(s) * n, sizeof v, cudaMemcpyDeviceToHost));
+            if (p == CFG_PRECISION_MIXED) {
+                float hl[2];
+                std::memcpy(hl, &v, sizeof hl);
+                v = double(hl[0]) + double(hl[1]);
+            }
+            y0[size_t(i)] = v;
+        } else {
+            float v = 0.0f;
+            CFG_CUDA_TRY(cudaMemcpy(&v, ion->d_yn + size_t(s) * n, sizeof v, cudaMemcpyDeviceToHost));
+            y0[size_t(i)] = v;
+        }
+    }
+    int tissue = ion->tissue;
+    if (ion->d_tissue) {
+        unsigned char t = 0;
+        CFG_CUDA_TRY(cudaMemcpy(&t, ion->d_tissue, 1, cudaMemcpyDeviceToHost));
+        tissue = t;
+    }
+    double sc[6];
+    const double* scp = nullptr;
+    if (ion->d_scales) {
+        for (int j = 0; j < 6; ++j)
+            CFG_CUDA_TRY(cudaMemcpy(&sc[j], ion->d_scales + size_t(j) * n, sizeof(double),
+                                    cudaMemcpyDeviceToHost));
+        scp = sc;
+    }
+    std::vector<double> C(static_cast<size_t>(m->nc), 0.0), yinit(static_cast<size_t>(ns), 0.0);
+    m->host_init(C.data(), yinit.data(), tissue, scp);
+    const int width = 2 * ns + m->na;
+    double *d_y = nullptr, *d_c = nullptr, *d_out = nullptr;
+    cudaError_t e = dmalloc(&d_y, size_t(ns));
+    if (!e) e = dmalloc(&d_c, size_t(m->nc));
+    if (!e) e = dmalloc(&d_out, size_t(n_points) * width);
+    if (!e) e = cudaMemcpy(d_y, y0.data(), sizeof(double) * ns, cudaMemcpyHostToDevice);
+    if (!e) e = cudaMemcpy(d_c, C.data(), sizeof(double) * m->nc, cudaMemcpyHostToDevice);
+    if (!e) e = m->sweep(d_y, d_c, tissue, ion->solve_vm ? 1 : 0, ion->stim, v_min, v_max,
+                         n_points, d_out, ion->stream);
+    std::vector<double> rows(size_t(n_points) * width);
+    if (!e) e = cudaMemcpyAsync(rows.data(), d_out, sizeof(double) * rows.size(),
+                                cudaMemcpyDeviceToHost, ion->stream);
+    if (!e) e = cudaStreamSynchronize(ion->stream);
+    dfree(d_y);
+    dfree(d_c);
+    dfree(d_out);
+    if (e) return fail(CFG_ERR_CUDA, "sweep failed: %s", cudaGetErrorString(e));
+    for (int i = 0; i < n_points; ++i) {
+        const double* row = &rows[size_t(i) * width];
+        double* o = out + size_t(i) * nc;
+        o[0] = row[0];
+        for (size_t k = 0; k < cols.size(); ++k) o[1 + k] = row[cols[k]];
+    }
+    return CFG_OK;
+}
+
+}  // extern "C"

@@ -30,7 +30,10 @@
     extern "C" cudaError_t cfg_batch_step_##ns##_fp64(const cfg::BatchLaunch&, int,           \
                                                       cudaStream_t);                          \
     extern "C" cudaError_t cfg_batch_step_##ns##_mixed(const cfg::BatchLaunch&, int,          \
-                                                       cudaStream_t);
+                                                       cudaStream_t);                         \
+    extern "C" cudaError_t cfg_ionic_sweep_##ns(const double*, const double*, int, int,        \
+                                                const cfg::CfgStimulus&, double, double, int,  \
+                                                double*, cudaStream_t);
 
 CFG_DECLARE_MODEL(tnnp)
 CFG_DECLARE_MODEL(ord)
@@ -91,6 +94,12 @@ struct Tables {
         o.batch_step[1] = cfg_batch_step_##NSP##_mixed;                                          \
         o.nsd = NSP::NSD;                                                                        \
         o.ca_state = NSP::CA_STATE;                                                              \
+        o.na = NSP::NA;                                                                          \
+        o.state_strings = NSP::STATE_STRINGS;                                                    \
+        o.alg_strings = NSP::ALG_STRINGS;                                                        \
+        o.sweep_currents = NSP::SWEEP_CURRENTS;                                                  \
+        o.sweep_deps = NSP::SWEEP_DEPS;                                                          \
+        o.sweep = cfg_ionic_sweep_##NSP;                                                         \
         return o;                                                                               \
     }()
 

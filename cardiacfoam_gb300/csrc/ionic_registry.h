@@ -35,6 +35,16 @@ struct IonicModelOps {
     cudaError_t (*batch_step[2])(const BatchLaunch&, int tissue, cudaStream_t);
     int nsd;                     // scale-dependent constants per cell
     int ca_state;                // intracellular calcium state, or -1
+    // sweepCurrent: the header's name tables, its dependency map (current ->
+    // comma-separated variables, null-ended) and the FP64 sweep launch
+    int na;                      // NUM_ALGEBRAIC
+    const char* const* state_strings;
+    const char* const* alg_strings;
+    const char* const* sweep_currents;
+    const char* const* sweep_deps;
+    cudaError_t (*sweep)(const double* y0, const double* C, int tissue, int solve_vm,
+                         const CfgStimulus& stim, double vmin, double vmax, int npts,
+                         double* out, cudaStream_t);
 };
 
 const IonicModelOps* find_ionic_model(const char* name);

@@ -127,6 +127,34 @@ __device__ __forceinline__ R iion(double t, const YS& Y, const KS& K, int tissue
     return a_Iion_cm;
 }
 
+// computeVariables with every algebraic stored: A[k] is ALGEBRAIC[k] (0 for
+// the ones the body does not assign), dydt the RATES it assigns.
+template <class R, bool SOLVE_VM, class YS, class KS>
+__device__ __forceinline__ void variables_all(double t, const YS& Y, const KS& K, R* A, R* dydt, int tissue, const CfgStimulus& stim)
+{
+    (void)tissue; (void)stim; (void)t;
+    const R y_u = Y(S_u);
+    const R y_recovery_r = Y(S_recovery_r);
+    R a_AV_eps = (K(C_AC_epsilon) + ((K(C_AC_mu1) * y_recovery_r) / (K(C_AC_mu2) + y_u)));
+    dydt[S_recovery_r] = (a_AV_eps * ((-y_recovery_r) - ((K(C_AC_k) * y_u) * (y_u - (K(C_AC_a) + R(1.0))))));
+    R a_Iion_cm = ((((K(C_AC_k) * y_u) * (y_u - K(C_AC_a))) * (y_u - R(1.0))) + (y_recovery_r * y_u));
+    R a_Istim = (SOLVE_VM ? R(cfg_stimulus_current<double>(t, stim)) : R(0));
+    if (SOLVE_VM) {
+        dydt[S_u] = ((-a_Iion_cm) - a_Istim);
+    }
+    A[0] = a_AV_eps;
+    A[1] = a_Istim;
+    A[2] = a_Iion_cm;
+}
+
+// STATES_NAMES / ALGEBRAIC_NAMES as the header spells them; matched by
+// position, entries the header leaves out are empty
+static const char* const STATE_STRINGS[2] = {"u", "recovery_r"};
+static const char* const ALG_STRINGS[3] = {"AV_eps", "Istim", "Iion_cm"};
+// <Model>DependencyMap(): current -> comma-separated variables, null-ended
+static const char* const SWEEP_CURRENTS[] = {"Iion", "I_ion", "Iion_cm", "u", "recovery_r", nullptr};
+static const char* const SWEEP_DEPS[] = {"Iion_cm,u,recovery_r,AV_eps", "Iion_cm,u,recovery_r,AV_eps", "Iion_cm,u,recovery_r,AV_eps", "u,RATES_u", "recovery_r,AV_eps,RATES_recovery_r", nullptr};
+
 // traits bundle used by the kernel templates
 struct Model {
     static constexpr int NS = alievpanfilov::NS, NC = alievpanfilov::NC;
@@ -138,6 +166,9 @@ struct Model {
     template <int T> CFG_HD static constexpr double constant(int i) { return cval<T>(i); }
     static constexpr int NSD = alievpanfilov::NSD, CA_STATE = alievpanfilov::CA_STATE;
     CFG_HD static constexpr int sd_slot(int i) { return alievpanfilov::sd_slot(i); }
+    static constexpr int NA = alievpanfilov::NA;
+    template <class R, bool SV, class YS, class KS>
+    __device__ static __forceinline__ void all_variables(double t, const YS& Y, const KS& K, R* A, R* dydt, int tissue, const CfgStimulus& st) { variables_all<R, SV>(t, Y, K, A, dydt, tissue, st); }
     CFG_HD static constexpr int sd_const(int k) { return alievpanfilov::sd_const(k); }
     template <class R, bool SV, class YS, class KS>
     __device__ static __forceinline__ R rates(double t, const YS& Y, const KS& K, R* dydt, int tissue, const CfgStimulus& st) { return rhs<R, SV>(t, Y, K, dydt, tissue, st); }

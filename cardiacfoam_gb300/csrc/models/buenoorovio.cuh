@@ -263,6 +263,56 @@ __device__ __forceinline__ R iion(double t, const YS& Y, const KS& K, int tissue
     return a_Jion;
 }
 
+// computeVariables with every algebraic stored: A[k] is ALGEBRAIC[k] (0 for
+// the ones the body does not assign), dydt the RATES it assigns.
+template <class R, bool SOLVE_VM, class YS, class KS>
+__device__ __forceinline__ void variables_all(double t, const YS& Y, const KS& K, R* A, R* dydt, int tissue, const CfgStimulus& stim)
+{
+    (void)tissue; (void)stim; (void)t;
+    const R y_u = Y(S_u);
+    const R y_v = Y(S_v);
+    const R y_w = Y(S_w);
+    const R y_s = Y(S_s);
+    R a_tauSo = (K(C_tauSo1) + (((K(C_tauSo2) - K(C_tauSo1)) * (R(1.0) + cfg_tanh((K(C_kSo) * (y_u - K(C_uSo)))))) / R(2.0)));
+    R a_tauO = (((R(1.0) - (((y_u - K(C_thetaO))) > R(0) ? 1 : 0)) * K(C_tauO1)) + ((((y_u - K(C_thetaO))) > R(0) ? 1 : 0) * K(C_tauO2)));
+    R a_Jfi = (((((-y_v) * (((y_u - K(C_thetaV))) > R(0) ? 1 : 0)) * (y_u - K(C_thetaV))) * (K(C_uU) - y_u)) / K(C_tauFi));
+    R a_Jso = ((((y_u - K(C_uO)) * (R(1.0) - (((y_u - K(C_thetaW))) > R(0) ? 1 : 0))) / a_tauO) + ((((y_u - K(C_thetaW))) > R(0) ? 1 : 0) / a_tauSo));
+    R a_Jsi = ((((-(((y_u - K(C_thetaW))) > R(0) ? 1 : 0)) * y_w) * y_s) / K(C_tauSi));
+    R a_Jion = ((a_Jfi + a_Jso) + a_Jsi);
+    R a_tauVMinus = (((R(1.0) - (((y_u - K(C_thetaVMinus))) > R(0) ? 1 : 0)) * K(C_tauV1Minus)) + ((((y_u - K(C_thetaVMinus))) > R(0) ? 1 : 0) * K(C_tauV2Minus)));
+    R a_tauWMinus = (K(C_tauW1Minus) + (((K(C_tauW2Minus) - K(C_tauW1Minus)) * (R(1.0) + cfg_tanh((K(C_kWMinus) * (y_u - K(C_uWMinus)))))) / R(2.0)));
+    R a_tauS = (((R(1.0) - (((y_u - K(C_thetaW))) > R(0) ? 1 : 0)) * K(C_tauS1)) + ((((y_u - K(C_thetaW))) > R(0) ? 1 : 0) * K(C_tauS2)));
+    R a_vInfty = (((K(C_thetaVMinus) - y_u)) > R(0) ? 1 : 0);
+    R a_wInfty = (((R(1.0) - (((y_u - K(C_thetaO))) > R(0) ? 1 : 0)) * (R(1.0) - (y_u / K(C_tauWInfty)))) + ((((y_u - K(C_thetaO))) > R(0) ? 1 : 0) * K(C_wInftyStar)));
+    dydt[S_v] = ((((R(1.0) - (((y_u - K(C_thetaV))) > R(0) ? 1 : 0)) * (a_vInfty - y_v)) / a_tauVMinus) - (((((y_u - K(C_thetaV))) > R(0) ? 1 : 0) * y_v) / K(C_tauVPlus)));
+    dydt[S_w] = ((((R(1.0) - (((y_u - K(C_thetaW))) > R(0) ? 1 : 0)) * (a_wInfty - y_w)) / a_tauWMinus) - (((((y_u - K(C_thetaW))) > R(0) ? 1 : 0) * y_w) / K(C_tauWPlus)));
+    dydt[S_s] = ((((R(1.0) + cfg_tanh((K(C_kS) * (y_u - K(C_uS))))) / R(2.0)) - y_s) / a_tauS);
+    R a_Istim = (SOLVE_VM ? R(cfg_stimulus_current<double>(t, stim)) : R(0));
+    if (SOLVE_VM) {
+        dydt[S_u] = ((-a_Jion) - a_Istim);
+    }
+    A[0] = a_Jfi;
+    A[1] = a_Jso;
+    A[2] = a_Jsi;
+    A[3] = a_Jion;
+    A[4] = a_Istim;
+    A[5] = a_tauSo;
+    A[6] = a_tauO;
+    A[7] = a_tauVMinus;
+    A[8] = a_tauWMinus;
+    A[9] = a_tauS;
+    A[10] = a_vInfty;
+    A[11] = a_wInfty;
+}
+
+// STATES_NAMES / ALGEBRAIC_NAMES as the header spells them; matched by
+// position, entries the header leaves out are empty
+static const char* const STATE_STRINGS[4] = {"u", "v", "w", "s"};
+static const char* const ALG_STRINGS[12] = {"Jfi", "Jso", "Jsi", "Jion", "Istim", "tauSo", "tauO", "tauVMinus", "tauWMinus", "tauS", "vInfty", "wInfty"};
+// <Model>DependencyMap(): current -> comma-separated variables, null-ended
+static const char* const SWEEP_CURRENTS[] = {"Jfi", "Jso", "Jsi", "Jion", "v", "w", "s", "I_fi", "I_so", "I_si", "Iion", "I_ion", "Iion_cm", nullptr};
+static const char* const SWEEP_DEPS[] = {"Jfi,v,RATES_v", "Jso,tauO,tauSo", "Jsi,w,s,RATES_s", "Jfi,Jso,Jsi,Jion", "v,vInfty,tauVMinus,RATES_v", "w,wInfty,tauWMinus,RATES_w", "s,tauS,RATES_s", "Jfi,v,RATES_v", "Jso,tauO,tauSo", "Jsi,w,s,RATES_s", "Jfi,Jso,Jsi,Jion", "Jfi,Jso,Jsi,Jion", "Jfi,Jso,Jsi,Jion", nullptr};
+
 // traits bundle used by the kernel templates
 struct Model {
     static constexpr int NS = buenoorovio::NS, NC = buenoorovio::NC;
@@ -274,6 +324,9 @@ struct Model {
     template <int T> CFG_HD static constexpr double constant(int i) { return cval<T>(i); }
     static constexpr int NSD = buenoorovio::NSD, CA_STATE = buenoorovio::CA_STATE;
     CFG_HD static constexpr int sd_slot(int i) { return buenoorovio::sd_slot(i); }
+    static constexpr int NA = buenoorovio::NA;
+    template <class R, bool SV, class YS, class KS>
+    __device__ static __forceinline__ void all_variables(double t, const YS& Y, const KS& K, R* A, R* dydt, int tissue, const CfgStimulus& st) { variables_all<R, SV>(t, Y, K, A, dydt, tissue, st); }
     CFG_HD static constexpr int sd_const(int k) { return buenoorovio::sd_const(k); }
     template <class R, bool SV, class YS, class KS>
     __device__ static __forceinline__ R rates(double t, const YS& Y, const KS& K, R* dydt, int tissue, const CfgStimulus& st) { return rhs<R, SV>(t, Y, K, dydt, tissue, st); }

@@ -145,6 +145,32 @@ __device__ __forceinline__ R iion(double t, const YS& Y, const KS& K, int tissue
     return a_Iion;
 }
 
+// computeVariables with every algebraic stored: A[k] is ALGEBRAIC[k] (0 for
+// the ones the body does not assign), dydt the RATES it assigns.
+template <class R, bool SOLVE_VM, class YS, class KS>
+__device__ __forceinline__ void variables_all(double t, const YS& Y, const KS& K, R* A, R* dydt, int tissue, const CfgStimulus& stim)
+{
+    (void)tissue; (void)stim; (void)t;
+    const R y_V = Y(S_V);
+    const R y_u1 = Y(S_u1);
+    const R y_u2 = Y(S_u2);
+    const R y_u3 = Y(S_u3);
+    dydt[S_V] = R(0.0);
+    dydt[S_u1] = ((cfg_ipow<2>(((y_u1 + y_u3) - y_V)) * cfg_ipow<2>(y_u2)) + (((R(0.5) * ((y_u1 + y_u3) - y_V)) * cfg_ipow<2>(y_u2)) * (y_V - y_u3)));
+    dydt[S_u2] = ((-((y_u1 + y_u3) - y_V)) * cfg_ipow<3>(y_u2));
+    dydt[S_u3] = 0;
+    R a_Iion = ((((((-R(0.5)) * K(C_Cm)) * ((y_u1 + y_u3) - y_V)) * cfg_ipow<2>(y_u2)) * (y_V - y_u3)) + ((K(C_Beta) * (y_V - y_u3)) / K(C_Chi)));
+    A[0] = a_Iion;
+}
+
+// STATES_NAMES / ALGEBRAIC_NAMES as the header spells them; matched by
+// position, entries the header leaves out are empty
+static const char* const STATE_STRINGS[4] = {"V", "u1", "u2", "u3"};
+static const char* const ALG_STRINGS[1] = {"Iion"};
+// <Model>DependencyMap(): current -> comma-separated variables, null-ended
+static const char* const SWEEP_CURRENTS[] = {nullptr};
+static const char* const SWEEP_DEPS[] = {nullptr};
+
 // traits bundle used by the kernel templates
 struct Model {
     static constexpr int NS = monodomainfdamanufactured::NS, NC = monodomainfdamanufactured::NC;
@@ -156,6 +182,9 @@ struct Model {
     template <int T> CFG_HD static constexpr double constant(int i) { return cval<T>(i); }
     static constexpr int NSD = monodomainfdamanufactured::NSD, CA_STATE = monodomainfdamanufactured::CA_STATE;
     CFG_HD static constexpr int sd_slot(int i) { return monodomainfdamanufactured::sd_slot(i); }
+    static constexpr int NA = monodomainfdamanufactured::NA;
+    template <class R, bool SV, class YS, class KS>
+    __device__ static __forceinline__ void all_variables(double t, const YS& Y, const KS& K, R* A, R* dydt, int tissue, const CfgStimulus& st) { variables_all<R, SV>(t, Y, K, A, dydt, tissue, st); }
     CFG_HD static constexpr int sd_const(int k) { return monodomainfdamanufactured::sd_const(k); }
     template <class R, bool SV, class YS, class KS>
     __device__ static __forceinline__ R rates(double t, const YS& Y, const KS& K, R* dydt, int tissue, const CfgStimulus& st) { return rhs<R, SV>(t, Y, K, dydt, tissue, st); }

@@ -108,7 +108,7 @@ EXPORTS = [
     "cfg_last_error", "cfg_ionic_create", "cfg_ionic_solve", "cfg_ionic_solve_device",
     "cfg_ionic_num_states", "cfg_ionic_state_name", "cfg_ionic_get_states",
     "cfg_ionic_set_states", "cfg_ionic_get_steps", "cfg_ionic_rhs_evaluations",
-    "cfg_ionic_destroy", "cfg_monodomain_create", "cfg_monodomain_create_from_dict",
+    "cfg_ionic_destroy", "cfg_ionic_sweep_currents", "cfg_ionic_sweep_current", "cfg_monodomain_create", "cfg_monodomain_create_from_dict",
     "cfg_monodomain_step", "cfg_monodomain_run", "cfg_monodomain_set_graph", "cfg_monodomain_get_field",
     "cfg_monodomain_set_field", "cfg_monodomain_time", "cfg_monodomain_ionic",
     "cfg_monodomain_last_stats", "cfg_monodomain_set_timing", "cfg_monodomain_timings",
@@ -143,6 +143,9 @@ def load(path: Optional[os.PathLike] = None):
     L.cfg_ionic_get_steps.argtypes = [C.c_void_p, _dp]
     L.cfg_ionic_rhs_evaluations.argtypes = [C.c_void_p, C.POINTER(C.c_ulonglong)]
     L.cfg_ionic_destroy.argtypes = [C.c_void_p]
+    L.cfg_ionic_sweep_currents.argtypes = [C.c_void_p, C.c_char_p, C.c_size_t]
+    L.cfg_ionic_sweep_current.argtypes = [C.c_void_p, C.c_char_p, C.c_double, C.c_double, C.c_int,
+                                          C.c_void_p, _ip, C.c_char_p, C.c_size_t]
     L.cfg_monodomain_create.argtypes = [C.POINTER(MonodomainDesc), C.POINTER(MeshDesc),
                                         C.POINTER(C.c_void_p)]
     L.cfg_monodomain_create_from_dict.argtypes = [C.c_char_p, C.POINTER(MeshDesc), C.c_double,

@@ -104,6 +104,21 @@ int cfg_ionic_get_steps(cfg_ionic* ion, double* host_steps);
 int cfg_ionic_rhs_evaluations(const cfg_ionic* ion, unsigned long long* count);
 int cfg_ionic_destroy(cfg_ionic* ion);
 
+/* availableSweepCurrents (e.g. TNNP.C:274-277): the keys of the model's
+ * dependency map, space-separated. */
+int cfg_ionic_sweep_currents(const cfg_ionic* ion, char* buf, size_t len);
+/* sweepCurrent(currentName, Vmin, Vmax, nPts, file) (ionicModel.H:742-759,
+ * e.g. TNNP.C:208-272): the states of integration point 0 with state 0
+ * clamped to Vmin + (Vmax - Vmin) i / (nPts - 1) (model units), the model's
+ * variables at VOI = 0, and the current's dependency columns resolved as
+ * ionicModelIO does (Vm, STATE names, ALGEBRAIC names, RATES_<state>).
+ * out: host [n_points][n_columns], column 0 = V; header: "V,<deps...>" as the
+ * reference writes it.  With out = NULL only n_columns and header are set.
+ * Evaluated in FP64 on the device, one thread per voltage. */
+int cfg_ionic_sweep_current(cfg_ionic* ion, const char* current, double v_min, double v_max,
+                            int n_points, double* out, int* n_columns, char* header,
+                            size_t header_len);
+
 /* -------------------------------------------------------- monodomain step */
 
 /* lduMesh view of the myocardium: OpenFOAM's lower/upper addressing of the
