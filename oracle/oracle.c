@@ -138,6 +138,7 @@ struct oracle_ionic {
     int model;
     long n;
     int tissue;
+    unsigned char* tissue_cell;   /* per-cell tissue flags, or NULL */
     int solve_vm;
     oracle_ode_settings ode;
     oracle_stimulus stim;
@@ -157,6 +158,7 @@ typedef struct {
      * in tissue mode, at their initial zero) */
     double *dydx0, *k2, *k3, *k4, *k5, *k6, *ytmp, *yout, *err, *algtmp;
     long evals;
+    int tissue;         /* tissue flag of the cell being integrated */
 } rk_ws;
 
 static void ws_alloc(rk_ws* w, int ns, int na)
@@ -173,6 +175,7 @@ static void ws_alloc(rk_ws* w, int ns, int na)
     w->err = p + 8 * ns;
     w->algtmp = p + 9 * ns;
     w->evals = 0;
+    w->tissue = 0;
 }
 
 static void ws_free(rk_ws* w) { free(w->dydx0); }
@@ -182,7 +185,7 @@ static void derivs(const oracle_ionic* io, const double* C, rk_ws* w, double t, 
                    double* dydt)
 {
     memset(w->algtmp, 0, sizeof(double) * (size_t)io->m->na);
-    io->m->rates(t, C, dydt, y, w->algtmp, io->tissue, io->solve_vm,
+    io->m->rates(t, C, dydt, y, w->algtmp, w->tissue, io->solve_vm,
                  io->has_stim ? &io->stim : NULL);
     w->evals++;
 }
@@ -281,6 +284,16 @@ oracle_ionic* oracle_ionic_new(int model, long n, int tissue, double initial_dt,
                                const oracle_ode_settings* ode, const oracle_stimulus* stim,
                                const double* scales)
 {
+    return oracle_ionic_new_cells(model, n, tissue, NULL, initial_dt, solve_vm, ode, stim, scales);
+}
+
+/* The same with a tissue flag per cell (tissue_cell, or NULL for `tissue`
+ * everywhere); per-cell flags give each cell its own constants. */
+oracle_ionic* oracle_ionic_new_cells(int model, long n, int tissue,
+                                     const unsigned char* tissue_cell, double initial_dt,
+                                     int solve_vm, const oracle_ode_settings* ode,
+                                     const oracle_stimulus* stim, const double* scales)
+{
     if (model < 0 || model >= ORACLE_NMODELS || n < 0) return NULL;
     oracle_ionic* io = (oracle_ionic*)calloc(1, sizeof(oracle_ionic));
     const model_info* m = &MODELS[model];
@@ -291,8 +304,12 @@ oracle_ionic* oracle_ionic_new(int model, long n, int tissue, double initial_dt,
     io->solve_vm = solve_vm;
     if (ode) io->ode = *ode; else oracle_ode_default(&io->ode);
     if (stim) { io->stim = *stim; io->has_stim = 1; }
-    io->per_cell_consts = scales != NULL;
-    io->C = (double*)calloc((size_t)m->nc * (size_t)(scales ? (n > 0 ? n : 1) : 1),
+    io->per_cell_consts = scales != NULL || tissue_cell != NULL;
+    if (tissue_cell) {
+        io->tissue_cell = (unsigned char*)malloc((size_t)(n > 0 ? n : 1));
+        memcpy(io->tissue_cell, tissue_cell, (size_t)n);
+    }
+    io->C = (double*)calloc((size_t)m->nc * (size_t)(io->per_cell_consts ? (n > 0 ? n : 1) : 1),
                             sizeof(double));
     io->y = (double*)calloc((size_t)(n * m->ns + 1), sizeof(double));
     io->alg = (double*)calloc((size_t)(n * m->na + 1), sizeof(double));
@@ -301,8 +318,9 @@ oracle_ionic* oracle_ionic_new(int model, long n, int tissue, double initial_dt,
     for (long c = 0; c < n; c++) {
         /* the reference re-runs initConsts into the shared CONSTANTS for
          * every cell (TNNP.C:64-76); per-cell scales need a row per cell */
-        double* Crow = io->C + (scales ? (size_t)c * (size_t)m->nc : 0);
-        m->init(Crow, io->y + (size_t)c * (size_t)m->ns, tissue, scales ? scales + 6 * c : NULL);
+        double* Crow = io->C + (io->per_cell_consts ? (size_t)c * (size_t)m->nc : 0);
+        const int tc = tissue_cell ? (int)tissue_cell[c] : tissue;
+        m->init(Crow, io->y + (size_t)c * (size_t)m->ns, tc, scales ? scales + 6 * c : NULL);
         m->supplement(Crow);
         io->step[c] = initial_dt;
     }
@@ -318,6 +336,7 @@ void oracle_ionic_free(oracle_ionic* io)
     free(io->alg);
     free(io->rates);
     free(io->step);
+    free(io->tissue_cell);
     free(io);
 }
 
@@ -351,13 +370,14 @@ static long solve_range(oracle_ionic* io, rk_ws* w, long c0, long c1, double t0,
         double* alg = io->alg + (size_t)c * (size_t)m->na;
         double* rates = io->rates + (size_t)c * (size_t)m->ns;
         const double* C = io->C + (io->per_cell_consts ? (size_t)c * (size_t)m->nc : 0);
+        w->tissue = io->tissue_cell ? (int)io->tissue_cell[c] : io->tissue;
         if (!io->solve_vm) y[0] = vm_to_state0(m->vm_map, vm[c]);
         double* step = &io->step[c];
         if (dt_model < *step) *step = dt_model;
         long k = ode_solve(io, C, w, t_start, t_end, y, step);
         if (k < 0) return -1;
         total += k;
-        m->variables(t_end, C, rates, y, alg, io->tissue, io->solve_vm,
+        m->variables(t_end, C, rates, y, alg, w->tissue, io->solve_vm,
                      io->has_stim ? &io->stim : NULL);
         if (im) im[c] = alg[m->iion] * m->iion_scale;
     }
@@ -415,6 +435,12 @@ struct oracle_mesh {
     double* vol;      /* n */
     double* sf;       /* 3nf face area vectors, owner -> neighbour */
     double* delta;    /* nf: |d_PN| */
+    /* full geometry of a general mesh (NULL/0 for the structured box) */
+    double* cf;       /* 3nf face centres */
+    long nb;          /* boundary faces (all zeroGradient for Vm) */
+    int* bcell;       /* nb owner cells */
+    double* bsf;      /* 3nb outward area vectors */
+    double* bcf;      /* 3nb face centres */
 };
 
 oracle_mesh* oracle_mesh_box(int nx, int ny, int nz, double lx, double ly, double lz)
@@ -466,11 +492,52 @@ oracle_mesh* oracle_mesh_box(int nx, int ny, int nz, double lx, double ly, doubl
     return m;
 }
 
+static void* dup_array(const void* src, size_t bytes)
+{
+    void* p = malloc(bytes ? bytes : 1);
+    if (bytes) memcpy(p, src, bytes);
+    return p;
+}
+
+/* A general (unstructured) mesh from its lduAddressing and geometry as
+ * fvMesh holds them: cell centres and volumes, internal faces (owner <
+ * neighbour, upper-triangular order) with area vectors owner -> neighbour
+ * and centres, and the boundary faces with their cells, outward area
+ * vectors and centres. */
+oracle_mesh* oracle_mesh_general(long n, long nf, const int* owner, const int* neigh,
+                                 const double* centres, const double* vol,
+                                 const double* face_centres, const double* face_sf, long nb,
+                                 const int* bcell, const double* bsf, const double* bcf)
+{
+    oracle_mesh* m = (oracle_mesh*)calloc(1, sizeof(oracle_mesh));
+    m->n = n;
+    m->nf = nf;
+    m->nb = nb;
+    m->owner = (int*)dup_array(owner, sizeof(int) * (size_t)nf);
+    m->neigh = (int*)dup_array(neigh, sizeof(int) * (size_t)nf);
+    m->centres = (double*)dup_array(centres, sizeof(double) * 3 * (size_t)n);
+    m->vol = (double*)dup_array(vol, sizeof(double) * (size_t)n);
+    m->cf = (double*)dup_array(face_centres, sizeof(double) * 3 * (size_t)nf);
+    m->sf = (double*)dup_array(face_sf, sizeof(double) * 3 * (size_t)nf);
+    m->bcell = (int*)dup_array(bcell, sizeof(int) * (size_t)nb);
+    m->bsf = (double*)dup_array(bsf, sizeof(double) * 3 * (size_t)nb);
+    m->bcf = (double*)dup_array(bcf, sizeof(double) * 3 * (size_t)nb);
+    m->delta = (double*)malloc(sizeof(double) * (size_t)(nf + 1));
+    for (long f = 0; f < nf; f++) {
+        const double* P = m->centres + 3 * (size_t)owner[f];
+        const double* N = m->centres + 3 * (size_t)neigh[f];
+        double d0 = N[0] - P[0], d1 = N[1] - P[1], d2 = N[2] - P[2];
+        m->delta[f] = sqrt(d0 * d0 + d1 * d1 + d2 * d2);
+    }
+    return m;
+}
+
 void oracle_mesh_free(oracle_mesh* m)
 {
     if (!m) return;
     free(m->owner); free(m->neigh); free(m->sf); free(m->delta);
     free(m->centres); free(m->vol);
+    free(m->cf); free(m->bcell); free(m->bsf); free(m->bcf);
     free(m);
 }
 
@@ -509,12 +576,249 @@ struct oracle_tissue {
     double* act;
     unsigned char* calc_act;
     double* lap;        /* upper coefficient per face: deltaCoeff * (Sf.sigma.Sf)/|Sf| */
+    double* sigma_cell; /* [n][6] conductivity per cell, or NULL (uniform) */
+    unsigned char* tissue_cell;   /* [n] tissue flag per cell, or NULL */
+    /* general mesh: gaussLaplacianScheme with corrected snGrad */
+    int corrected_mesh; /* face centres given: explicit corrections are on */
+    double *w, *dcoef, *corrv, *sfgsn, *sfgcorr, *bsfgcorr, *bn, *lsp, *lsn, *grad, *fflux;
     /* PCG work */
     double *diag, *upper, *b, *rA, *wA, *pA, *rD, *tmp;
     int n_solves;
     double init_res[MAX_SOLVES], final_res[MAX_SOLVES];
     int iters[MAX_SOLVES];
 };
+
+/* Conductivity of cell c as a full tensor, row-major (the symmTensor &
+ * tensor(I) of monodomainSolver.C:86-95 for the uniform case). */
+static void cell_sigma(const oracle_tissue* T, long c, double s[9])
+{
+    const double* v = T->sigma_cell ? T->sigma_cell + 6 * (size_t)c : T->d.sigma;
+    s[0] = v[0]; s[1] = v[1]; s[2] = v[2];
+    s[3] = v[1]; s[4] = v[3]; s[5] = v[4];
+    s[6] = v[2]; s[7] = v[4]; s[8] = v[5];
+}
+
+/* vector & tensor: out_j = sum_i S_i G_ij */
+static void vec_dot_tensor(const double* S, const double* G, double* out)
+{
+    out[0] = S[0] * G[0] + S[1] * G[3] + S[2] * G[6];
+    out[1] = S[0] * G[1] + S[1] * G[4] + S[2] * G[7];
+    out[2] = S[0] * G[2] + S[1] * G[5] + S[2] * G[8];
+}
+
+static double dot3(const double* a, const double* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+
+/* SfGamma, SfGammaSn and SfGammaCorr of one face (gaussLaplacianScheme::
+ * fvmLaplacian for a tensor Gamma, OpenFOAM v2312). */
+static double face_gamma(const double* S, const double* G, double* corr)
+{
+    const double magSf = sqrt(dot3(S, S));
+    const double Sn[3] = {S[0] / magSf, S[1] / magSf, S[2] / magSf};
+    double SfG[3];
+    vec_dot_tensor(S, G, SfG);
+    const double sfgsn = dot3(SfG, Sn);
+    for (int k = 0; k < 3; k++) corr[k] = SfG[k] - sfgsn * Sn[k];
+    return sfgsn;
+}
+
+/* The uncorrected coefficients (orthogonal structured box, uniform sigma)
+ * or, for a general mesh, every geometric quantity of OpenFOAM's
+ * Gauss-linear-corrected Laplacian and of the cell gradient its explicit
+ * part needs:
+ *   weights      w = |Sf.(N - Cf)| / (|Sf.(Cf - P)| + |Sf.(N - Cf)|)
+ *                (surfaceInterpolation::makeWeights)
+ *   deltaCoeffs  1/max(Sn.d, 0.05|d|)  (makeNonOrthDeltaCoeffs)
+ *   corrVecs     Sn - d*deltaCoeff     (makeNonOrthCorrectionVectors;
+ *                zero on boundary faces)
+ *   Gamma_f      w (Gamma_P - Gamma_N) + Gamma_N  (linear interpolation)
+ *   leastSquares vectors (leastSquaresVectors::calcLeastSquaresVectors):
+ *                dd = sum over faces of d d/|d|^2 with boundary d the
+ *                patch-normal delta n (n.(Cf - C)); P: invDd_P.d/|d|^2,
+ *                N: -invDd_N.d/|d|^2. */
+static void assemble_laplacian(oracle_tissue* T)
+{
+    const oracle_mesh* M = T->mesh;
+    const long nf = T->nf;
+    if (!T->corrected_mesh) {
+        /* uniform conductivity tensor (monodomainSolver.C:86-95); on a face,
+         * SfGammaSn = Sf.(sigma.Sf)/|Sf| and the implicit coefficient is
+         * deltaCoeffs * SfGammaSn (gaussLaplacianScheme, orthogonal mesh) */
+        const double* s = T->d.sigma;
+        for (long f = 0; f < nf; f++) {
+            const double* S = M->sf + 3 * f;
+            double magSf = sqrt(S[0] * S[0] + S[1] * S[1] + S[2] * S[2]);
+            double g0 = S[0] * s[0] + S[1] * s[1] + S[2] * s[2];
+            double g1 = S[0] * s[1] + S[1] * s[3] + S[2] * s[4];
+            double g2 = S[0] * s[2] + S[1] * s[4] + S[2] * s[5];
+            double sfgsn = (g0 * S[0] + g1 * S[1] + g2 * S[2]) / magSf;
+            double delta_coeff = 1.0 / M->delta[f];
+            T->lap[f] = delta_coeff * sfgsn;
+        }
+        return;
+    }
+    double* dd = (double*)calloc(6 * (size_t)T->n, sizeof(double));
+    for (long f = 0; f < nf; f++) {
+        const long P = M->owner[f], N = M->neigh[f];
+        const double* S = M->sf + 3 * f;
+        const double* Cf = M->cf + 3 * f;
+        const double* CP = M->centres + 3 * P;
+        const double* CN = M->centres + 3 * N;
+        const double magSf = sqrt(dot3(S, S));
+        const double Sn[3] = {S[0] / magSf, S[1] / magSf, S[2] / magSf};
+        const double fo[3] = {Cf[0] - CP[0], Cf[1] - CP[1], Cf[2] - CP[2]};
+        const double nf3[3] = {CN[0] - Cf[0], CN[1] - Cf[1], CN[2] - Cf[2]};
+        const double SfdOwn = fabs(dot3(S, fo)), SfdNei = fabs(dot3(S, nf3));
+        const double w = SfdNei / (SfdOwn + SfdNei);
+        T->w[f] = w;
+        const double d[3] = {CN[0] - CP[0], CN[1] - CP[1], CN[2] - CP[2]};
+        const double magd = sqrt(dot3(d, d));
+        const double sd = dot3(Sn, d);
+        const double dc = 1.0 / (sd > 0.05 * magd ? sd : 0.05 * magd);
+        T->dcoef[f] = dc;
+        for (int k = 0; k < 3; k++) T->corrv[3 * f + k] = Sn[k] - d[k] * dc;
+        double GP[9], GN[9], G[9];
+        cell_sigma(T, P, GP);
+        cell_sigma(T, N, GN);
+        for (int k = 0; k < 9; k++) G[k] = w * (GP[k] - GN[k]) + GN[k];
+        T->sfgsn[f] = face_gamma(S, G, T->sfgcorr + 3 * f);
+        T->lap[f] = dc * T->sfgsn[f];
+        /* leastSquares dd */
+        const double md2 = dot3(d, d);
+        double* a = dd + 6 * P;
+        double* b = dd + 6 * N;
+        const double wdd[6] = {d[0] * d[0] / md2, d[0] * d[1] / md2, d[0] * d[2] / md2,
+                               d[1] * d[1] / md2, d[1] * d[2] / md2, d[2] * d[2] / md2};
+        for (int k = 0; k < 6; k++) { a[k] += wdd[k]; b[k] += wdd[k]; }
+    }
+    for (long bf = 0; bf < M->nb; bf++) {
+        const long P = M->bcell[bf];
+        const double* S = M->bsf + 3 * bf;
+        const double magSf = sqrt(dot3(S, S));
+        double* n = T->bn + 3 * bf;
+        for (int k = 0; k < 3; k++) n[k] = S[k] / magSf;
+        double G[9];
+        cell_sigma(T, P, G);
+        (void)face_gamma(S, G, T->bsfgcorr + 3 * bf);
+        const double* Cf = M->bcf + 3 * bf;
+        const double* CP = M->centres + 3 * P;
+        const double r[3] = {Cf[0] - CP[0], Cf[1] - CP[1], Cf[2] - CP[2]};
+        const double nr = dot3(n, r);
+        const double d[3] = {n[0] * nr, n[1] * nr, n[2] * nr};
+        const double md2 = dot3(d, d);
+        double* a = dd + 6 * P;
+        a[0] += d[0] * d[0] / md2; a[1] += d[0] * d[1] / md2; a[2] += d[0] * d[2] / md2;
+        a[3] += d[1] * d[1] / md2; a[4] += d[1] * d[2] / md2; a[5] += d[2] * d[2] / md2;
+    }
+    /* invert dd (symmetric 3x3, cofactors over the determinant) */
+    for (long c = 0; c < T->n; c++) {
+        double* a = dd + 6 * c;
+        const double xx = a[0], xy = a[1], xz = a[2], yy = a[3], yz = a[4], zz = a[5];
+        const double det = xx * (yy * zz - yz * yz) - xy * (xy * zz - xz * yz) +
+                           xz * (xy * yz - yy * xz);
+        a[0] = (yy * zz - yz * yz) / det;
+        a[1] = (xz * yz - xy * zz) / det;
+        a[2] = (xy * yz - xz * yy) / det;
+        a[3] = (xx * zz - xz * xz) / det;
+        a[4] = (xy * xz - xx * yz) / det;
+        a[5] = (xx * yy - xy * xy) / det;
+    }
+    for (long f = 0; f < nf; f++) {
+        const long P = M->owner[f], N = M->neigh[f];
+        const double* CP = M->centres + 3 * P;
+        const double* CN = M->centres + 3 * N;
+        const double d[3] = {CN[0] - CP[0], CN[1] - CP[1], CN[2] - CP[2]};
+        const double k = 1.0 / dot3(d, d);
+        const double* a = dd + 6 * P;
+        const double* b = dd + 6 * N;
+        T->lsp[3 * f + 0] = k * (a[0] * d[0] + a[1] * d[1] + a[2] * d[2]);
+        T->lsp[3 * f + 1] = k * (a[1] * d[0] + a[3] * d[1] + a[4] * d[2]);
+        T->lsp[3 * f + 2] = k * (a[2] * d[0] + a[4] * d[1] + a[5] * d[2]);
+        T->lsn[3 * f + 0] = -k * (b[0] * d[0] + b[1] * d[1] + b[2] * d[2]);
+        T->lsn[3 * f + 1] = -k * (b[1] * d[0] + b[3] * d[1] + b[4] * d[2]);
+        T->lsn[3 * f + 2] = -k * (b[2] * d[0] + b[4] * d[1] + b[5] * d[2]);
+    }
+    free(dd);
+}
+
+/* Cell gradient of phi: leastSquaresGrad::calcGrad (the boundary terms
+ * carry phi_b - phi_P = 0 on zeroGradient walls) or gaussGrad (face values
+ * by linear interpolation, boundary value phi_P, divided by V). */
+static void cell_gradient(oracle_tissue* T, const double* phi, double* g)
+{
+    const oracle_mesh* M = T->mesh;
+    memset(g, 0, sizeof(double) * 3 * (size_t)T->n);
+    if (!T->d.grad_gauss) {
+        for (long f = 0; f < T->nf; f++) {
+            const long P = M->owner[f], N = M->neigh[f];
+            const double dv = phi[N] - phi[P];
+            for (int k = 0; k < 3; k++) {
+                g[3 * P + k] += T->lsp[3 * f + k] * dv;
+                g[3 * N + k] -= T->lsn[3 * f + k] * dv;
+            }
+        }
+        return;
+    }
+    for (long f = 0; f < T->nf; f++) {
+        const long P = M->owner[f], N = M->neigh[f];
+        const double pf = T->w[f] * (phi[P] - phi[N]) + phi[N];
+        for (int k = 0; k < 3; k++) {
+            g[3 * P + k] += M->sf[3 * f + k] * pf;
+            g[3 * N + k] -= M->sf[3 * f + k] * pf;
+        }
+    }
+    for (long bf = 0; bf < M->nb; bf++) {
+        const long P = M->bcell[bf];
+        for (int k = 0; k < 3; k++) g[3 * P + k] += M->bsf[3 * bf + k] * phi[P];
+    }
+    for (long c = 0; c < T->n; c++)
+        for (int k = 0; k < 3; k++) g[3 * c + k] /= M->vol[c];
+}
+
+/* Boundary value of the gradient on a zeroGradient wall
+ * (gaussGrad::correctBoundaryConditions): g + n (snGrad - n.g), snGrad = 0. */
+static void boundary_gradient(const double* gP, const double* n, double* gb)
+{
+    const double ng = dot3(n, gP);
+    for (int k = 0; k < 3; k++) gb[k] = gP[k] + n[k] * (0.0 - ng);
+}
+
+/* Face flux at one internal face of the explicit correction
+ * (gammaSnGradCorr + SfGammaSn * correctedSnGrad::correction): the gradient
+ * linearly interpolated to the face (dotInterpolate). */
+static double correction_flux(const oracle_tissue* T, long f, const double* g)
+{
+    const oracle_mesh* M = T->mesh;
+    const long P = M->owner[f], N = M->neigh[f];
+    const double w = T->w[f];
+    double gf[3];
+    for (int k = 0; k < 3; k++) gf[k] = w * (g[3 * P + k] - g[3 * N + k]) + g[3 * N + k];
+    double flux = dot3(T->sfgcorr + 3 * f, gf);
+    if (!T->d.uncorrected) flux += T->sfgsn[f] * dot3(T->corrv + 3 * f, gf);
+    return flux;
+}
+
+/* fvc::div of the explicit correction fluxes times V (surfaceIntegrate):
+ * the Laplacian's fvMatrix source is minus this. */
+static void correction_div_v(oracle_tissue* T, const double* vf, double* out)
+{
+    const oracle_mesh* M = T->mesh;
+    double* g = T->grad;
+    cell_gradient(T, vf, g);
+    double* div = T->fflux;
+    memset(div, 0, sizeof(double) * (size_t)T->n);
+    for (long f = 0; f < T->nf; f++) {
+        const double flux = correction_flux(T, f, g);
+        div[M->owner[f]] += flux;
+        div[M->neigh[f]] -= flux;
+    }
+    for (long bf = 0; bf < M->nb; bf++) {
+        const long P = M->bcell[bf];
+        double gb[3];
+        boundary_gradient(g + 3 * P, T->bn + 3 * bf, gb);
+        div[P] += dot3(T->bsfgcorr + 3 * bf, gb);
+    }
+    for (long c = 0; c < T->n; c++) out[c] = M->vol[c] * (div[c] / M->vol[c]);
+}
 
 oracle_tissue* oracle_tissue_new(const oracle_tissue_desc* d, const oracle_mesh* mesh)
 {
@@ -547,21 +851,41 @@ oracle_tissue* oracle_tissue_new(const oracle_tissue_desc* d, const oracle_mesh*
         T->vm[c] = d->vm0;
         T->calc_act[c] = 1;
     }
-    /* uniform conductivity tensor (monodomainSolver.C:86-95); on a face,
-     * SfGammaSn = Sf.(sigma.Sf)/|Sf| and the implicit coefficient is
-     * deltaCoeffs * SfGammaSn (gaussLaplacianScheme, orthogonal mesh) */
-    const double* s = d->sigma;
-    for (long f = 0; f < nf; f++) {
-        const double* S = mesh->sf + 3 * f;
-        double magSf = sqrt(S[0] * S[0] + S[1] * S[1] + S[2] * S[2]);
-        double g0 = S[0] * s[0] + S[1] * s[1] + S[2] * s[2];
-        double g1 = S[0] * s[1] + S[1] * s[3] + S[2] * s[4];
-        double g2 = S[0] * s[2] + S[1] * s[4] + S[2] * s[5];
-        double sfgsn = (g0 * S[0] + g1 * S[1] + g2 * S[2]) / magSf;
-        double delta_coeff = 1.0 / mesh->delta[f];
-        T->lap[f] = delta_coeff * sfgsn;
+    if (mesh->cf) {
+        T->corrected_mesh = 1;
+        T->w = (double*)malloc(sizeof(double) * (size_t)(nf + 1));
+        T->dcoef = (double*)malloc(sizeof(double) * (size_t)(nf + 1));
+        T->corrv = (double*)malloc(sizeof(double) * 3 * (size_t)(nf + 1));
+        T->sfgsn = (double*)malloc(sizeof(double) * (size_t)(nf + 1));
+        T->sfgcorr = (double*)malloc(sizeof(double) * 3 * (size_t)(nf + 1));
+        T->bsfgcorr = (double*)malloc(sizeof(double) * 3 * (size_t)(mesh->nb + 1));
+        T->bn = (double*)malloc(sizeof(double) * 3 * (size_t)(mesh->nb + 1));
+        T->lsp = (double*)malloc(sizeof(double) * 3 * (size_t)(nf + 1));
+        T->lsn = (double*)malloc(sizeof(double) * 3 * (size_t)(nf + 1));
+        T->grad = (double*)malloc(sizeof(double) * 3 * (size_t)n);
+        T->fflux = (double*)malloc(sizeof(double) * (size_t)n);
     }
+    assemble_laplacian(T);
     return T;
+}
+
+/* Per-cell conductivity [n][6] (xx xy xz yy yz zz), as read from a
+ * 0/conductivity volTensorField (monodomainSolver.C:48-100); boundary faces
+ * take their cell's value.  Re-assembles the Laplacian. */
+void oracle_tissue_set_conductivity(oracle_tissue* T, const double* sigma6)
+{
+    if (!T->sigma_cell) T->sigma_cell = (double*)malloc(sizeof(double) * 6 * (size_t)T->n);
+    memcpy(T->sigma_cell, sigma6, sizeof(double) * 6 * (size_t)T->n);
+    assemble_laplacian(T);
+}
+
+/* Tissue flag per cell for the ionic model (before its first step). */
+int oracle_tissue_set_cell_tissue(oracle_tissue* T, const unsigned char* flags)
+{
+    if (T->ionic) return -1;
+    if (!T->tissue_cell) T->tissue_cell = (unsigned char*)malloc((size_t)T->n);
+    memcpy(T->tissue_cell, flags, (size_t)T->n);
+    return 0;
 }
 
 void oracle_tissue_free(oracle_tissue* T)
@@ -571,6 +895,9 @@ void oracle_tissue_free(oracle_tissue* T)
     free(T->vm); free(T->vm_old); free(T->vm_oldold); free(T->iion); free(T->src);
     free(T->act); free(T->calc_act); free(T->lap); free(T->diag); free(T->upper);
     free(T->b); free(T->rA); free(T->wA); free(T->pA); free(T->rD); free(T->tmp);
+    free(T->sigma_cell); free(T->tissue_cell);
+    free(T->w); free(T->dcoef); free(T->corrv); free(T->sfgsn); free(T->sfgcorr);
+    free(T->bsfgcorr); free(T->bn); free(T->lsp); free(T->lsn); free(T->grad); free(T->fflux);
     free(T);
 }
 
@@ -775,6 +1102,14 @@ static int solve_implicit(oracle_tissue* T, double dt)
         su = su + T->src[c] * V[c];
         T->b[c] = T->b[c] + su;
     }
+    /* general mesh: the Laplacian's explicit correction of the current Vm
+     * (fvm.source() -= V*fvc::div(faceFluxCorrection), on the other side
+     * of ==) */
+    if (T->corrected_mesh) {
+        double* cv = T->tmp;
+        correction_div_v(T, T->vm, cv);
+        for (long c = 0; c < T->n; c++) T->b[c] = T->b[c] + cv[c];
+    }
     int k = T->n_solves;
     if (k >= MAX_SOLVES) return -1;
     int it = pcg(T, T->vm, T->b, &T->init_res[k], &T->final_res[k]);
@@ -800,10 +1135,34 @@ static int solve_explicit(oracle_tissue* T, double dt)
     const int* u = T->mesh->neigh;
     double* div = T->tmp;
     for (long c = 0; c < T->n; c++) div[c] = 0.0;
-    for (long f = 0; f < T->nf; f++) {
-        double flux = T->lap[f] * (T->vm[u[f]] - T->vm[l[f]]);
-        div[l[f]] += flux;
-        div[u[f]] -= flux;
+    if (T->corrected_mesh) {
+        /* fvc::laplacian = fvc::div(SfGammaSn*snGrad(Vm) + gammaSnGradCorr)
+         * with snGrad = deltaCoeffs*(Vm_N - Vm_P) + correction */
+        double* g = T->grad;
+        cell_gradient(T, T->vm, g);
+        for (long f = 0; f < T->nf; f++) {
+            const long P = l[f], N = u[f];
+            const double w = T->w[f];
+            double gf[3];
+            for (int k = 0; k < 3; k++) gf[k] = w * (g[3 * P + k] - g[3 * N + k]) + g[3 * N + k];
+            double sn = T->dcoef[f] * (T->vm[N] - T->vm[P]);
+            if (!T->d.uncorrected) sn = sn + dot3(T->corrv + 3 * f, gf);
+            const double flux = T->sfgsn[f] * sn + dot3(T->sfgcorr + 3 * f, gf);
+            div[P] += flux;
+            div[N] -= flux;
+        }
+        for (long bf = 0; bf < T->mesh->nb; bf++) {
+            const long P = T->mesh->bcell[bf];
+            double gb[3];
+            boundary_gradient(g + 3 * P, T->bn + 3 * bf, gb);
+            div[P] += dot3(T->bsfgcorr + 3 * bf, gb);
+        }
+    } else {
+        for (long f = 0; f < T->nf; f++) {
+            double flux = T->lap[f] * (T->vm[u[f]] - T->vm[l[f]]);
+            div[l[f]] += flux;
+            div[u[f]] -= flux;
+        }
     }
     for (long c = 0; c < T->n; c++) {
         double diag, src;
@@ -819,6 +1178,55 @@ static int solve_explicit(oracle_tissue* T, double dt)
         src = src + rhs * V[c];
         T->vm[c] = src / diag;
     }
+    return 0;
+}
+
+/* fvc::laplacian(sigma, phi) per cell (the explicit form's operator),
+ * for checks of the discretisation on given fields. */
+void oracle_tissue_laplacian(oracle_tissue* T, const double* phi, double* out)
+{
+    double* save = T->vm;
+    T->vm = (double*)phi;
+    const int* l = T->mesh->owner;
+    const int* u = T->mesh->neigh;
+    double* div = out;
+    for (long c = 0; c < T->n; c++) div[c] = 0.0;
+    if (T->corrected_mesh) {
+        double* g = T->grad;
+        cell_gradient(T, phi, g);
+        for (long f = 0; f < T->nf; f++) {
+            const long P = l[f], N = u[f];
+            const double w = T->w[f];
+            double gf[3];
+            for (int k = 0; k < 3; k++) gf[k] = w * (g[3 * P + k] - g[3 * N + k]) + g[3 * N + k];
+            double sn = T->dcoef[f] * (phi[N] - phi[P]);
+            if (!T->d.uncorrected) sn = sn + dot3(T->corrv + 3 * f, gf);
+            const double flux = T->sfgsn[f] * sn + dot3(T->sfgcorr + 3 * f, gf);
+            div[P] += flux;
+            div[N] -= flux;
+        }
+        for (long bf = 0; bf < T->mesh->nb; bf++) {
+            const long P = T->mesh->bcell[bf];
+            double gb[3];
+            boundary_gradient(g + 3 * P, T->bn + 3 * bf, gb);
+            div[P] += dot3(T->bsfgcorr + 3 * bf, gb);
+        }
+    } else {
+        for (long f = 0; f < T->nf; f++) {
+            const double flux = T->lap[f] * (phi[u[f]] - phi[l[f]]);
+            div[l[f]] += flux;
+            div[u[f]] -= flux;
+        }
+    }
+    for (long c = 0; c < T->n; c++) div[c] /= T->mesh->vol[c];
+    T->vm = save;
+}
+
+/* Cell gradient of phi with the tissue's gradient scheme (general mesh). */
+int oracle_tissue_gradient(oracle_tissue* T, const double* phi, double* g)
+{
+    if (!T->corrected_mesh) return -1;
+    cell_gradient(T, phi, g);
     return 0;
 }
 
@@ -841,7 +1249,8 @@ static void update_activation(oracle_tissue* T, double dt)
 int oracle_tissue_init_ionic(oracle_tissue* T, double dt)
 {
     if (!T->ionic)
-        T->ionic = oracle_ionic_new(T->d.model, T->n, T->d.tissue, dt, 0, &T->d.ode, NULL, NULL);
+        T->ionic = oracle_ionic_new_cells(T->d.model, T->n, T->d.tissue, T->tissue_cell, dt, 0,
+                                          &T->d.ode, NULL, NULL);
     return T->ionic ? 0 : -1;
 }
 

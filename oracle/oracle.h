@@ -19,7 +19,9 @@
  * Parity status: the ionic right-hand sides are pinned bit-for-bit against
  * the reference's own generated headers (golden vectors under tests/golden);
  * RKF45 is pinned by the reference's single-cell regression values; the
- * implicit PCG path has no reference test and is "parity unpinned".
+ * implicit PCG path has no reference test and is "parity unpinned"; so is
+ * the corrected Laplacian on general meshes, restated from OpenFOAM v2312's
+ * finiteVolume library (absent from the reference tree).
  */
 #ifndef ORACLE_H
 #define ORACLE_H
@@ -60,6 +62,11 @@ typedef struct oracle_ionic oracle_ionic;
 oracle_ionic* oracle_ionic_new(int model, long n, int tissue, double initial_dt,
                                int solve_vm, const oracle_ode_settings* ode,
                                const oracle_stimulus* stim, const double* scales);
+/* per-cell tissue flags (NULL: `tissue` for every cell) */
+oracle_ionic* oracle_ionic_new_cells(int model, long n, int tissue,
+                                     const unsigned char* tissue_cell, double initial_dt,
+                                     int solve_vm, const oracle_ode_settings* ode,
+                                     const oracle_stimulus* stim, const double* scales);
 void oracle_ionic_free(oracle_ionic*);
 /* ionicModel::solveODE(t0 [s], dt [s], Vm [V], Im [V/s]); returns the total
  * number of accepted RKF45 substeps, or -1 on maxSteps overflow.  nthreads>1
@@ -78,6 +85,11 @@ long oracle_mesh_ncells(const oracle_mesh*);
 long oracle_mesh_nfaces(const oracle_mesh*);
 void oracle_mesh_addressing(const oracle_mesh*, int* owner, int* neighbour);
 void oracle_mesh_centres(const oracle_mesh*, double* c);
+/* --- general mesh: lduAddressing plus the geometry of fvMesh ----------- */
+oracle_mesh* oracle_mesh_general(long n, long nf, const int* owner, const int* neigh,
+                                 const double* centres, const double* vol,
+                                 const double* face_centres, const double* face_sf, long nb,
+                                 const int* bcell, const double* bsf, const double* bcf);
 
 /* --- monodomain tissue model -------------------------------------------- */
 typedef struct oracle_tissue_desc {
@@ -96,6 +108,11 @@ typedef struct oracle_tissue_desc {
     double box_min[8][3], box_max[8][3];
     double box_start[8], box_duration[8], box_intensity[8];   /* s, s, A/m^3 */
     oracle_ode_settings ode;
+    /* general meshes (fvSchemes): gradSchemes default leastSquares (0) or
+     * Gauss linear (1); laplacianSchemes Gauss linear corrected (0) or
+     * uncorrected (1) */
+    int grad_gauss;
+    int uncorrected;
 } oracle_tissue_desc;
 
 typedef struct oracle_tissue oracle_tissue;
@@ -113,6 +130,13 @@ double* oracle_tissue_source(oracle_tissue*);
 oracle_ionic* oracle_tissue_ionic(oracle_tissue*);
 int oracle_tissue_last_solves(const oracle_tissue*, double* init_res, double* final_res,
                               int* iters, int max_solves);
+/* per-cell conductivity [n][6] (xx xy xz yy yz zz); re-assembles */
+void oracle_tissue_set_conductivity(oracle_tissue*, const double* sigma6);
+/* per-cell tissue flags for the ionic model, before the first step */
+int oracle_tissue_set_cell_tissue(oracle_tissue*, const unsigned char* flags);
+/* fvc::laplacian(sigma, phi) [per volume] and the cell gradient of phi */
+void oracle_tissue_laplacian(oracle_tissue*, const double* phi, double* out);
+int oracle_tissue_gradient(oracle_tissue*, const double* phi, double* g);
 
 /* --- single cell (SingleCellSolver::evolve) ------------------------------ */
 /* Runs n_steps of dt [s] from t=0 with Vm inside the ODE; writes the

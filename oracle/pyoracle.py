@@ -45,7 +45,8 @@ class TissueDesc(C.Structure):
                 ("vm0", C.c_double), ("n_boxes", C.c_int),
                 ("box_min", (C.c_double * 3) * 8), ("box_max", (C.c_double * 3) * 8),
                 ("box_start", C.c_double * 8), ("box_duration", C.c_double * 8),
-                ("box_intensity", C.c_double * 8), ("ode", OdeSettings)]
+                ("box_intensity", C.c_double * 8), ("ode", OdeSettings),
+                ("grad_gauss", C.c_int), ("uncorrected", C.c_int)]
 
 
 _lib = None
@@ -86,6 +87,13 @@ def lib():
         L.oracle_mesh_nfaces.restype = C.c_long
         L.oracle_mesh_addressing.argtypes = [C.c_void_p, _ip, _ip]
         L.oracle_mesh_centres.argtypes = [C.c_void_p, _dp]
+        L.oracle_mesh_general.argtypes = [C.c_long, C.c_long, _ip, _ip, _dp, _dp, _dp, _dp,
+                                          C.c_long, _ip, _dp, _dp]
+        L.oracle_mesh_general.restype = C.c_void_p
+        L.oracle_tissue_set_conductivity.argtypes = [C.c_void_p, _dp]
+        L.oracle_tissue_set_cell_tissue.argtypes = [C.c_void_p, C.POINTER(C.c_ubyte)]
+        L.oracle_tissue_laplacian.argtypes = [C.c_void_p, _dp, _dp]
+        L.oracle_tissue_gradient.argtypes = [C.c_void_p, _dp, _dp]
         L.oracle_tissue_new.argtypes = [C.POINTER(TissueDesc), C.c_void_p]
         L.oracle_tissue_new.restype = C.c_void_p
         L.oracle_tissue_free.argtypes = [C.c_void_p]
@@ -211,12 +219,31 @@ class Ionic:
 
 
 class Mesh:
-    """blockMesh-style single block of nx*ny*nz hexes over [0,lx]x[0,ly]x[0,lz]."""
+    """blockMesh-style single block of nx*ny*nz hexes over [0,lx]x[0,ly]x[0,lz],
+    or (``Mesh.general``) any mesh given by its lduAddressing and geometry."""
 
     def __init__(self, nx, ny, nz, lx, ly, lz):
         self.h = lib().oracle_mesh_box(nx, ny, nz, lx, ly, lz)
         self.n = lib().oracle_mesh_ncells(self.h)
         self.nf = lib().oracle_mesh_nfaces(self.h)
+
+    @classmethod
+    def general(cls, m):
+        """From an object with n_cells, owner, neighbour, centres, volumes,
+        face_centres, face_sf, boundary_cell, boundary_sf, boundary_centres."""
+        self = cls.__new__(cls)
+        keep = [np.ascontiguousarray(a, dtype=t) for a, t in (
+            (m.owner, np.int32), (m.neighbour, np.int32), (m.centres, np.float64),
+            (m.volumes, np.float64), (m.face_centres, np.float64), (m.face_sf, np.float64),
+            (m.boundary_cell, np.int32), (m.boundary_sf, np.float64),
+            (m.boundary_centres, np.float64))]
+        o, nb, c, v, fc, sf, bc, bsf, bcf = keep
+        self.h = lib().oracle_mesh_general(m.n_cells, o.size, iptr(o), iptr(nb), ptr(c), ptr(v),
+                                           ptr(fc), ptr(sf), bc.size, iptr(bc), ptr(bsf),
+                                           ptr(bcf))
+        self.n = m.n_cells
+        self.nf = o.size
+        return self
 
     def addressing(self):
         o = np.zeros(self.nf, np.int32)
@@ -239,7 +266,8 @@ def tissue_desc(model="TNNP", tissue=1, sigma=(0.1334177215, 0, 0, 0.01760617761
                                                 0.01760617761),
                 chi=140000.0, cm=0.01, implicit=True, ddt_backward=True, precond_dic=True,
                 pcg_tol=1e-8, pcg_rel_tol=0.0, pcg_max_iter=1000, n_outer=1000,
-                outer_tol=1e-6, vm0=-0.084, boxes: Sequence = (), ode=None) -> TissueDesc:
+                outer_tol=1e-6, vm0=-0.084, boxes: Sequence = (), ode=None,
+                grad_gauss=False, uncorrected=False) -> TissueDesc:
     d = TissueDesc()
     d.model = MODELS[model] if isinstance(model, str) else model
     d.tissue = tissue
@@ -256,6 +284,7 @@ def tissue_desc(model="TNNP", tissue=1, sigma=(0.1334177215, 0, 0, 0.01760617761
             d.box_max[b][k] = hi[k]
         d.box_start[b], d.box_duration[b], d.box_intensity[b] = t0, dur, inten
     d.ode = ode if ode is not None else ode_settings(max_steps=1000000000)
+    d.grad_gauss, d.uncorrected = int(grad_gauss), int(uncorrected)
     return d
 
 
@@ -319,6 +348,30 @@ class Tissue:
         ns = sizes(list(MODELS)[self.desc.model])[0]
         sp = lib().oracle_ionic_states(p)
         return np.ctypeslib.as_array(sp, shape=(self.n, ns)).copy()
+
+    def set_conductivity(self, sigma6: np.ndarray):
+        """Per-cell conductivity [n][6] (xx xy xz yy yz zz)."""
+        a = np.ascontiguousarray(sigma6, dtype=np.float64).reshape(self.n, 6)
+        lib().oracle_tissue_set_conductivity(self.h, ptr(a))
+
+    def set_cell_tissue(self, flags: np.ndarray):
+        a = np.ascontiguousarray(flags, dtype=np.uint8)
+        if lib().oracle_tissue_set_cell_tissue(self.h, a.ctypes.data_as(C.POINTER(C.c_ubyte))):
+            raise RuntimeError("cell tissue flags must be set before the first step")
+
+    def laplacian(self, phi: np.ndarray) -> np.ndarray:
+        """fvc::laplacian(sigma, phi) per cell."""
+        p = np.ascontiguousarray(phi, dtype=np.float64)
+        out = np.zeros(self.n)
+        lib().oracle_tissue_laplacian(self.h, ptr(p), ptr(out))
+        return out
+
+    def gradient(self, phi: np.ndarray) -> np.ndarray:
+        p = np.ascontiguousarray(phi, dtype=np.float64)
+        g = np.zeros((self.n, 3))
+        if lib().oracle_tissue_gradient(self.h, ptr(p), ptr(g)):
+            raise RuntimeError("the cell gradient needs a general mesh")
+        return g
 
     def __del__(self):
         if getattr(self, "h", None):
