@@ -158,6 +158,17 @@ def mesh_desc(mesh: LduMesh, face_coeff: Optional[np.ndarray] = None,
     if structured:
         for i in range(3):
             d.structured[i] = mesh.structured[i]
+    if mesh.has_geometry:
+        geo = [np.ascontiguousarray(mesh.face_centres, dtype=np.float64),
+               np.ascontiguousarray(mesh.boundary_cell, dtype=np.int32),
+               np.ascontiguousarray(mesh.boundary_sf, dtype=np.float64),
+               np.ascontiguousarray(mesh.boundary_centres, dtype=np.float64)]
+        keep.extend(geo)
+        d.face_centres = _L.dptr(geo[0])
+        d.n_boundary_faces = mesh.n_boundary_faces
+        d.boundary_cell = _L.iptr(geo[1])
+        d.boundary_sf = _L.dptr(geo[2])
+        d.boundary_centres = _L.dptr(geo[3])
     return d, keep
 
 
@@ -169,7 +180,9 @@ class Monodomain:
                  dt=1e-5, precision=_L.PRECISION_FP64, implicit=True, ddt_backward=True,
                  pcg_tol=1e-8, pcg_rel_tol=0.0, pcg_max_iter=1000, n_outer=1000,
                  outer_tol=1e-6, vm0=-0.084, boxes: Sequence = (), ode=None,
-                 tissue_per_cell=None, scales=None, stencil=True, max_steps=10 ** 6):
+                 tissue_per_cell=None, scales=None, stencil=True, max_steps=10 ** 6,
+                 conductivity_per_cell=None, grad_scheme=_L.GRAD_LEAST_SQUARES,
+                 laplacian_uncorrected=False):
         self._lib = _L.load()
         self.mesh = mesh
         keep: list = []
@@ -189,6 +202,14 @@ class Monodomain:
                 d.box_min[b][k] = lo[k]
                 d.box_max[b][k] = hi[k]
             d.box_start[b], d.box_duration[b], d.box_intensity[b] = t0, dur, inten
+        if conductivity_per_cell is not None:
+            sig = np.ascontiguousarray(conductivity_per_cell, dtype=np.float64).reshape(-1, 6)
+            if sig.shape[0] != mesh.n_cells:
+                raise ValueError("conductivity_per_cell needs one row of 6 per cell")
+            keep.append(sig)
+            d.conductivity_per_cell = _L.dptr(sig)
+        d.grad_scheme = int(grad_scheme)
+        d.laplacian_uncorrected = int(laplacian_uncorrected)
         md, keep2 = mesh_desc(mesh, structured=stencil)
         h = C.c_void_p()
         _L.check(self._lib.cfg_monodomain_create(C.byref(d), C.byref(md), C.byref(h)))

@@ -63,6 +63,7 @@ def _units():
     units.append(("step_graph", CSRC / "step_graph.cu", []))
     units.append(("noalloc", CSRC / "noalloc.cu", []))
     units.append(("dictionary", CSRC / "dictionary.cpp", []))
+    units.append(("geometry", CSRC / "geometry.cpp", []))
     return units
 
 

@@ -72,6 +72,11 @@ __global__ void __launch_bounds__(kDiffBlock) k_solve_begin(DiffusionArgs a)
         double su = -(a.chicm * a.iion[c]) * V;
         su = su + box_source(a, c, st->t0) * V;
         bb = bb + su;
+        if (a.nc_gw) {
+            const double* gr = a.grad;
+            const long long n = a.n;
+            bb = bb + nc_correction(a, c, [gr, n](long long q, int k) { return gr[k * n + q]; });
+        }
         const double* x = a.vm;
         const double ax = row_amul(a, c, d, [x](long long q) { return x[q]; });
         const double r = bb - ax;
@@ -96,6 +101,29 @@ __global__ void __launch_bounds__(kDiffBlock) k_solve_begin(DiffusionArgs a)
         }
     }
 }
+
+// Cell gradient of Vm on a general mesh, for the explicit correction of the
+// Laplacian: of the current iterate at the start of each PIMPLE corrector
+// (k_grad_iterate), or of the start-of-step Vm, which vm_old holds, before
+// the explicit form (k_grad_start).
+__device__ __forceinline__ void grad_row(const DiffusionArgs& a, const double* x)
+{
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= a.n) return;
+    double g[3];
+    nc_gradient(a, c, [x](long long q) { return x[q]; }, g);
+    a.grad[c] = g[0];
+    a.grad[a.n + c] = g[1];
+    a.grad[2 * a.n + c] = g[2];
+}
+
+__global__ void __launch_bounds__(kDiffBlock) k_grad_iterate(DiffusionArgs a)
+{
+    if (!a.st->outer_active) return;
+    grad_row(a, a.vm);
+}
+
+__global__ void __launch_bounds__(kDiffBlock) k_grad_start(DiffusionArgs a) { grad_row(a, a.vm_old); }
 
 // normFactor, the initial residual, and the preconditioned residual of
 // iteration 0 (z = D^-1 r, z.r).
@@ -262,6 +290,11 @@ __global__ void k_explicit(DiffusionArgs a)
                 const double coef = a.ell_coef[(long long)q * a.n + c];
                 if (nb < c) div -= coef * (xc - x[nb]);
                 else div += coef * (x[nb] - xc);
+            }
+            if (a.nc_gw) {
+                const double* gr = a.grad;
+                const long long n = a.n;
+                div += nc_correction(a, c, [gr, n](long long q, int k) { return gr[k * n + q]; });
             }
         }
         double diag, src;

@@ -18,6 +18,10 @@
 //     per row (15 per PCG iteration here) and the barriers set the speed of
 //     the solve, not HBM: its vectors stay in L2.
 //
+// On a general mesh every corrector first forms the cell gradient of the
+// iterate (one more barrier) for the explicit correction of the Laplacian
+// in the source.
+//
 // Grid barriers are cooperative-launch safe (all blocks co-resident) and
 // bounded: a block that waits longer than ~1 s sets an abort flag, every
 // block leaves at its next barrier, and the step reports CFG_ERR_PCG.
@@ -207,6 +211,19 @@ __global__ void __launch_bounds__(kCoopBlock, 1) k_implicit_coop(DiffusionArgs a
         const double* __restrict__ rdiag = a.rdiag2 + size_t(v) * n;
         const double* __restrict__ sumA = a.sumA2 + size_t(v) * n;
         const double cft0 = a.cft0[v], cft00 = a.cft00[v];
+        // --- general mesh: gradient of the current iterate for the
+        // Laplacian's explicit correction, published for the neighbours
+        double* __restrict__ grad = a.grad;
+        if (a.nc_gw) {
+            for (unsigned c = first; c < n; c += stride) {
+                double g[3];
+                nc_gradient(a, c, [x](long long q) { return __ldcg(&x[q]); }, g);
+                __stcg(&grad[c], g[0]);
+                __stcg(&grad[size_t(n) + c], g[1]);
+                __stcg(&grad[2 * size_t(n) + c], g[2]);
+            }
+            if (!grid_barrier(st, epoch)) { abort_step = true; break; }
+        }
         // --- source, A.x, r = b - A.x; sums of x and |r|
         double s1[2] = {0.0, 0.0};
         auto rhs_row = [&](unsigned c) {
@@ -219,7 +236,12 @@ __global__ void __launch_bounds__(kCoopBlock, 1) k_implicit_coop(DiffusionArgs a
             double bb = a.chicm * ddt_src;
             double su = -(a.chicm * a.iion[c]) * V;
             su = su + box_source(a, c, t0) * V;
-            return bb + su;
+            double rhs = bb + su;
+            if (a.nc_gw)
+                rhs = rhs + nc_correction(a, c, [grad, n](long long q, int k) {
+                          return __ldcg(&grad[size_t(k) * n + size_t(q)]);
+                      });
+            return rhs;
         };
         for (unsigned c = first; c < n; c += 2 * stride) {
             const unsigned c2 = c + stride;

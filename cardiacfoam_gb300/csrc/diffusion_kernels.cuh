@@ -60,6 +60,15 @@ struct DiffusionArgs {
     const unsigned char* ell_cnt;  // [n]
     const double* lapdiag;     // [n] sum of -coef in row order
     const double* vol;         // [n]
+    // explicit correction of the Laplacian on a general mesh (null: none):
+    // per ELL slot the gradient weight of (x_nb - x_c), the correction
+    // vector signed for the row (+ for the face's owner) and the row cell's
+    // interpolation weight; per cell the wall factor and the gradient
+    const double* nc_gw;       // [3][width][n]
+    const double* nc_k;        // [3][width][n]
+    const double* nc_om;       // [width][n]
+    const double* nc_bk;       // [3][n]
+    double* grad;              // [3][n]
     // stencil form (structured block, uniform coefficient per direction)
     int sx, sy, sz;            // nx, ny, nz (0 = use ELL)
     double cx, cy, cz;
@@ -183,6 +192,49 @@ __device__ __forceinline__ double row_amul(const DiffusionArgs& a, long long c, 
             acc += (-a.ell_coef[(long long)q * a.n + c]) * f(a.ell_col[(long long)q * a.n + c]);
     }
     return acc;
+}
+
+// Cell gradient of x at row c on a general mesh: sum over the row's slots
+// of gw_e (x_nb - x_c) (leastSquares or Gauss linear weights).
+template <class F>
+__device__ __forceinline__ void nc_gradient(const DiffusionArgs& a, long long c, F x, double (&g)[3])
+{
+    const long long n = a.n, wn = (long long)a.width * n;
+    const double xc = x(c);
+    g[0] = g[1] = g[2] = 0.0;
+    const int cnt = a.ell_cnt[c];
+    for (int e = 0; e < cnt; ++e) {
+        const long long i = (long long)e * n + c;
+        const double dv = x(a.ell_col[i]) - xc;
+        g[0] += a.nc_gw[i] * dv;
+        g[1] += a.nc_gw[wn + i] * dv;
+        g[2] += a.nc_gw[2 * wn + i] * dv;
+    }
+}
+
+// fvc::div of the explicit correction fluxes times V at row c: each face's
+// flux k.(w (g_P - g_N) + g_N) with the sign of the row (faces in column
+// order, the order of the face loop), then the wall term bk.g_c.  g(q, k)
+// reads component k of cell q's gradient.
+template <class G>
+__device__ __forceinline__ double nc_correction(const DiffusionArgs& a, long long c, G g)
+{
+    const long long n = a.n, wn = (long long)a.width * n;
+    const double g0 = g(c, 0), g1 = g(c, 1), g2 = g(c, 2);
+    double s = 0.0;
+    const int cnt = a.ell_cnt[c];
+    for (int e = 0; e < cnt; ++e) {
+        const long long i = (long long)e * n + c;
+        const long long nb = a.ell_col[i];
+        const double om = a.nc_om[i];
+        const double n0 = g(nb, 0), n1 = g(nb, 1), n2 = g(nb, 2);
+        const double f0 = om * (g0 - n0) + n0;
+        const double f1 = om * (g1 - n1) + n1;
+        const double f2 = om * (g2 - n2) + n2;
+        s += a.nc_k[i] * f0 + a.nc_k[wn + i] * f1 + a.nc_k[2 * wn + i] * f2;
+    }
+    s += a.nc_bk[c] * g0 + a.nc_bk[n + c] * g1 + a.nc_bk[2 * n + c] * g2;
+    return s;
 }
 
 // row sum of the matrix (lduMatrix::sumA): diag then each -coef

@@ -7,6 +7,7 @@
 #include <vector>
 
 #include "diffusion_kernels.cuh"
+#include "geometry.h"
 #include "host_common.h"
 #include "ionic_host.h"
 #include "monodomain_host.h"
@@ -22,6 +23,8 @@ __global__ void k_pcg_update(DiffusionArgs a);
 __global__ void k_activation(DiffusionArgs a);
 __global__ void k_explicit(DiffusionArgs a);
 __global__ void k_explicit_finish(PcgState* st, int ddt_backward);
+__global__ void k_grad_iterate(DiffusionArgs a);
+__global__ void k_grad_start(DiffusionArgs a);
 
 static void md_free(cfg_monodomain* md)
 {
@@ -36,6 +39,8 @@ static void md_free(cfg_monodomain* md)
     dfree(md->d_diag2); dfree(md->d_rdiag2); dfree(md->d_sumA2); dfree(md->d_b); dfree(md->d_r);
     dfree(md->d_z); dfree(md->d_ax); dfree(md->d_pA); dfree(md->d_pB); dfree(md->d_ap);
     dfree(md->d_partial); dfree(md->d_st);
+    dfree(md->d_nc_gw); dfree(md->d_nc_k); dfree(md->d_nc_om); dfree(md->d_nc_bk);
+    dfree(md->d_grad);
     if (md->h_st) cudaFreeHost(md->h_st);
     if (md->stream) cudaStreamDestroy(md->stream);
     delete md;
@@ -44,14 +49,35 @@ static void md_free(cfg_monodomain* md)
 // lduAddressing -> ELL rows with neighbours in ascending order (the order in
 // which lduMatrix::Amul's face loop reaches a row for upper-triangular face
 // ordering); lapdiag = sum of -coef in that order (fvMatrix::negSumDiag).
-static int build_operator(cfg_monodomain* md, const cfg_mesh_desc* m, const double* sigma)
+// On a general mesh (face centres given) the coefficients and the factors of
+// the explicit correction come from the corrected assembly, laid out per ELL
+// slot: gradient weight, signed correction vector and the row cell's
+// interpolation weight of the slot's face.
+static int build_operator(cfg_monodomain* md, const cfg_mesh_desc* m, const cfg_monodomain_desc* d)
 {
     const long long n = m->n_cells, nf = m->n_faces;
-    // face coefficients: given, or deltaCoeffs * (Sf.sigma.Sf)/|Sf| for the
-    // uniform conductivity (gaussLaplacianScheme, fvmLaplacianUncorrected)
+    const double* sigma = d->conductivity;
+    const bool general = m->face_centres != nullptr;
+    if (d->conductivity_per_cell && !general)
+        return fail(CFG_ERR_INVALID, "a per-cell conductivity needs the mesh's face_centres");
+    if (general && m->face_coeff)
+        return fail(CFG_ERR_INVALID, "give face_coeff or the full geometry, not both");
+    for (long long f = 0; f < nf; ++f) {
+        const int l = m->owner[f], u = m->neighbour[f];
+        if (l < 0 || u < 0 || l >= n || u >= n || l == u)
+            return fail(CFG_ERR_INVALID, "face %lld has invalid owner/neighbour %d/%d", f, l, u);
+    }
+    CorrectedOperator op;
     std::vector<double> fc;
     const double* coeff = m->face_coeff;
-    if (!coeff) {
+    if (general) {
+        if (int rc = assemble_corrected(m, sigma, d->conductivity_per_cell, d->grad_scheme,
+                                        d->laplacian_uncorrected, op))
+            return rc;
+        coeff = op.coeff.data();
+    } else if (!coeff) {
+        // face coefficients: deltaCoeffs * (Sf.sigma.Sf)/|Sf| for the uniform
+        // conductivity (gaussLaplacianScheme, fvmLaplacianUncorrected)
         if (!m->face_sf || !m->face_delta_coeffs)
             return fail(CFG_ERR_INVALID, "mesh needs face_coeff or face_sf + face_delta_coeffs");
         fc.resize(size_t(nf));
@@ -67,42 +93,63 @@ static int build_operator(cfg_monodomain* md, const cfg_mesh_desc* m, const doub
         }
         coeff = fc.data();
     }
-    std::vector<std::vector<std::pair<int, double>>> rows(static_cast<size_t>(n));
+    // row entries: (column, face, the row cell owns the face)
+    struct Entry {
+        int col;
+        long long face;
+        bool own;
+    };
+    std::vector<std::vector<Entry>> rows(static_cast<size_t>(n));
     for (long long f = 0; f < nf; ++f) {
         const int l = m->owner[f], u = m->neighbour[f];
-        if (l < 0 || u < 0 || l >= n || u >= n || l == u)
-            return fail(CFG_ERR_INVALID, "face %lld has invalid owner/neighbour %d/%d", f, l, u);
-        rows[size_t(l)].push_back({u, coeff[f]});
-        rows[size_t(u)].push_back({l, coeff[f]});
+        rows[size_t(l)].push_back({u, f, true});
+        rows[size_t(u)].push_back({l, f, false});
     }
     int width = 0;
     for (auto& r : rows) {
         std::stable_sort(r.begin(), r.end(),
-                         [](const std::pair<int, double>& a, const std::pair<int, double>& b) {
-                             return a.first < b.first;
-                         });
+                         [](const Entry& a, const Entry& b) { return a.col < b.col; });
         width = std::max(width, int(r.size()));
     }
     if (width > 255) return fail(CFG_ERR_INVALID, "cell with more than 255 faces");
     md->width = width;
-    std::vector<int> col(size_t(width) * n, 0);
-    std::vector<double> coef(size_t(width) * n, 0.0);
+    const size_t slots = size_t(width) * size_t(n);
+    std::vector<int> col(slots, 0);
+    std::vector<double> coef(slots, 0.0);
     std::vector<unsigned char> cnt(static_cast<size_t>(n));
     std::vector<double> lapdiag(static_cast<size_t>(n));
+    std::vector<double> gw, kc, om;
+    if (general) {
+        gw.assign(3 * slots, 0.0);
+        kc.assign(3 * slots, 0.0);
+        om.assign(slots, 0.0);
+    }
     for (long long c = 0; c < n; ++c) {
         const auto& r = rows[size_t(c)];
         cnt[size_t(c)] = (unsigned char)r.size();
         double s = 0.0;
         for (size_t q = 0; q < r.size(); ++q) {
-            col[q * n + c] = r[q].first;
-            coef[q * n + c] = r[q].second;
-            s -= r[q].second;
+            const size_t i = q * size_t(n) + size_t(c);
+            const long long f = r[q].face;
+            col[i] = r[q].col;
+            coef[i] = coeff[f];
+            s -= coeff[f];
+            if (general) {
+                const double* g = r[q].own ? op.g_own.data() : op.g_nei.data();
+                const double sg = r[q].own ? 1.0 : -1.0;
+                for (int k = 0; k < 3; ++k) {
+                    gw[size_t(k) * slots + i] = g[3 * f + k];
+                    kc[size_t(k) * slots + i] = sg * op.k[size_t(3 * f + k)];
+                }
+                om[i] = r[q].own ? op.w[size_t(f)] : 1.0 - op.w[size_t(f)];
+            }
         }
         lapdiag[size_t(c)] = s;
     }
     // structured block with one coefficient per direction: stencil form
     md->sx = md->sy = md->sz = 0;
-    if (m->structured[0] > 0 && (long long)m->structured[0] * m->structured[1] * m->structured[2] == n) {
+    if (!general && m->structured[0] > 0 &&
+        (long long)m->structured[0] * m->structured[1] * m->structured[2] == n) {
         const long long nx = m->structured[0], ny = m->structured[1];
         double cdir[3] = {0, 0, 0};
         bool ok = true, seen[3] = {false, false, false};
@@ -130,6 +177,27 @@ static int build_operator(cfg_monodomain* md, const cfg_mesh_desc* m, const doub
                             cudaMemcpyHostToDevice));
     md->ell_bytes = col.size() * sizeof(int) + coef.size() * sizeof(double) + cnt.size();
     md->nnz_offdiag = 2 * nf;
+    md->corrected = general;
+    if (general) {
+        std::vector<double> bk(size_t(3) * size_t(n));
+        for (long long c = 0; c < n; ++c)
+            for (int k = 0; k < 3; ++k) bk[size_t(k) * size_t(n) + size_t(c)] = op.bk[size_t(3 * c + k)];
+        CFG_CUDA_TRY(dmalloc(&md->d_nc_gw, gw.size()));
+        CFG_CUDA_TRY(dmalloc(&md->d_nc_k, kc.size()));
+        CFG_CUDA_TRY(dmalloc(&md->d_nc_om, om.size()));
+        CFG_CUDA_TRY(dmalloc(&md->d_nc_bk, bk.size()));
+        CFG_CUDA_TRY(dmalloc(&md->d_grad, size_t(3) * size_t(n)));
+        CFG_CUDA_TRY(cudaMemcpy(md->d_nc_gw, gw.data(), gw.size() * sizeof(double),
+                                cudaMemcpyHostToDevice));
+        CFG_CUDA_TRY(cudaMemcpy(md->d_nc_k, kc.data(), kc.size() * sizeof(double),
+                                cudaMemcpyHostToDevice));
+        CFG_CUDA_TRY(cudaMemcpy(md->d_nc_om, om.data(), om.size() * sizeof(double),
+                                cudaMemcpyHostToDevice));
+        CFG_CUDA_TRY(cudaMemcpy(md->d_nc_bk, bk.data(), bk.size() * sizeof(double),
+                                cudaMemcpyHostToDevice));
+        CFG_CUDA_TRY(cudaMemset(md->d_grad, 0, sizeof(double) * 3 * size_t(n)));
+        md->ell_bytes += (gw.size() + kc.size() + om.size()) * sizeof(double);
+    }
     return CFG_OK;
 }
 
@@ -144,6 +212,11 @@ static void fill_args(cfg_monodomain* md, double dt)
     a.ell_cnt = md->d_cnt;
     a.lapdiag = md->d_lapdiag;
     a.vol = md->d_vol;
+    a.nc_gw = md->d_nc_gw;
+    a.nc_k = md->d_nc_k;
+    a.nc_om = md->d_nc_om;
+    a.nc_bk = md->d_nc_bk;
+    a.grad = md->d_grad;
     a.sx = md->use_stencil ? md->sx : 0;
     a.sy = md->sy;
     a.sz = md->sz;
@@ -232,7 +305,7 @@ int monodomain_create(const cfg_monodomain_desc* d, const cfg_mesh_desc* m, cfg_
             md->box_max[b][k] = d->box_max[b][k];
         }
     }
-    if ((rc = build_operator(md, m, d->conductivity))) return bail(rc);
+    if ((rc = build_operator(md, m, d))) return bail(rc);
     md->use_stencil = md->sx > 0;
     const size_t n = size_t(md->n);
     cudaError_t e = cudaSuccess;
@@ -334,6 +407,10 @@ int enqueue_step(cfg_monodomain* md, double dt, bool host_control)
     launches += 2;
     if (md->timing) CFG_CUDA_TRY(cudaEventRecord(md->ev[1], s));
     if (!md->implicit) {
+        if (md->corrected) {
+            k_grad_start<<<grid, kDiffBlock, 0, s>>>(a);
+            launches += 1;
+        }
         k_explicit<<<grid, kDiffBlock, 0, s>>>(a);
         k_explicit_finish<<<1, 1, 0, s>>>(md->d_st, md->ddt_backward);
         launches += 2;
@@ -349,6 +426,10 @@ int enqueue_step(cfg_monodomain* md, double dt, bool host_control)
     }
     if (host_control) {
         for (int corr = 0; corr < 1000000; ++corr) {
+            if (md->corrected) {
+                k_grad_iterate<<<grid, kDiffBlock, 0, s>>>(a);
+                launches += 1;
+            }
             k_solve_begin<<<grid, kDiffBlock, 0, s>>>(a);
             k_solve_norm<<<grid, kDiffBlock, 0, s>>>(a);
             launches += 2;
@@ -368,6 +449,7 @@ int enqueue_step(cfg_monodomain* md, double dt, bool host_control)
         }
     } else {
         for (int corr = 0; corr < md->graph_max_corr; ++corr) {
+            if (md->corrected) k_grad_iterate<<<grid, kDiffBlock, 0, s>>>(a);
             k_solve_begin<<<grid, kDiffBlock, 0, s>>>(a);
             k_solve_norm<<<grid, kDiffBlock, 0, s>>>(a);
             for (int k = 0; k < md->graph_max_iter; ++k) {

@@ -4,9 +4,12 @@
 // round trip:
 //
 //   k_step_begin -> ionic step -> WHILE(outer) {
-//       k_solve_begin -> k_solve_norm -> WHILE(inner) { k_pcg_p -> k_pcg_update }
-//       -> k_outer_cond }
+//       [k_grad_iterate] -> k_solve_begin -> k_solve_norm
+//       -> WHILE(inner) { k_pcg_p -> k_pcg_update } -> k_outer_cond }
 //   -> k_activation
+//
+// (k_grad_iterate only on general meshes, for the Laplacian's explicit
+// correction.)
 //
 // Both loops are bounded: PCG stops at maxIter, the corrector loop at
 // nOuterCorrectors, and a per-step iteration cap ends the step with an error.
@@ -26,6 +29,8 @@ __global__ void k_outer_cond(DiffusionArgs a);
 __global__ void k_activation(DiffusionArgs a);
 __global__ void k_explicit(DiffusionArgs a);
 __global__ void k_explicit_finish(PcgState* st, int ddt_backward);
+__global__ void k_grad_iterate(DiffusionArgs a);
+__global__ void k_grad_start(DiffusionArgs a);
 
 namespace {
 
@@ -151,6 +156,11 @@ int build_step_graph(cfg_monodomain* md, double dt)
     }
     if (!md->implicit) {
         cudaGraphNode_t n_ex, n_fin;
+        if (md->corrected) {
+            cudaGraphNode_t n_g;
+            CFG_G(b.kernel(k_grad_start, &n_g, &prev, 1));
+            prev = n_g;
+        }
         CFG_G(b.kernel(k_explicit, &n_ex, &prev, 1));
         cudaKernelNodeParams p{};
         PcgState* st = md->d_st;
@@ -177,7 +187,13 @@ int build_step_graph(cfg_monodomain* md, double dt)
         CFG_G(cudaGraphConditionalHandleCreate(&a.h_inner, body, 0, 0));
         Builder bb{body, &a, unsigned(a.nblocks)};
         cudaGraphNode_t n_sb, n_sn, n_inner, n_oc;
-        CFG_G(bb.kernel(k_solve_begin, &n_sb, nullptr, 0));
+        if (md->corrected) {
+            cudaGraphNode_t n_g;
+            CFG_G(bb.kernel(k_grad_iterate, &n_g, nullptr, 0));
+            CFG_G(bb.kernel(k_solve_begin, &n_sb, &n_g, 1));
+        } else {
+            CFG_G(bb.kernel(k_solve_begin, &n_sb, nullptr, 0));
+        }
         CFG_G(bb.kernel(k_solve_norm, &n_sn, &n_sb, 1));
         cudaGraphNodeParams ip{};
         ip.type = cudaGraphNodeTypeConditional;

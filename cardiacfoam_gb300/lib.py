@@ -58,10 +58,15 @@ class IonicDesc(C.Structure):
                 ("tissue_per_cell", _up), ("scales", _dp)]
 
 
+GRAD_LEAST_SQUARES, GRAD_GAUSS_LINEAR = 0, 1
+
+
 class MeshDesc(C.Structure):
     _fields_ = [("n_cells", C.c_longlong), ("n_faces", C.c_longlong), ("owner", _ip),
                 ("neighbour", _ip), ("volumes", _dp), ("centres", _dp), ("face_coeff", _dp),
-                ("face_sf", _dp), ("face_delta_coeffs", _dp), ("structured", C.c_int * 3)]
+                ("face_sf", _dp), ("face_delta_coeffs", _dp), ("structured", C.c_int * 3),
+                ("face_centres", _dp), ("n_boundary_faces", C.c_longlong),
+                ("boundary_cell", _ip), ("boundary_sf", _dp), ("boundary_centres", _dp)]
 
 
 class MonodomainDesc(C.Structure):
@@ -72,7 +77,8 @@ class MonodomainDesc(C.Structure):
                 ("outer_tol", C.c_double), ("vm0", C.c_double), ("n_boxes", C.c_int),
                 ("box_min", (C.c_double * 3) * 8), ("box_max", (C.c_double * 3) * 8),
                 ("box_start", C.c_double * 8), ("box_duration", C.c_double * 8),
-                ("box_intensity", C.c_double * 8)]
+                ("box_intensity", C.c_double * 8), ("conductivity_per_cell", _dp),
+                ("grad_scheme", C.c_int), ("laplacian_uncorrected", C.c_int)]
 
 
 class StepStats(C.Structure):

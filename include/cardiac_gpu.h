@@ -127,7 +127,21 @@ int cfg_ionic_sweep_current(cfg_ionic* ion, const char* current, double v_min, d
  * (upper() of fvm::laplacian(conductivity, Vm), gaussLaplacianScheme), or the
  * face geometry (Sf and deltaCoeffs) from which the library forms them with
  * the descriptor's uniform conductivity.  zeroGradient walls contribute
- * nothing (myocardiumDomain.C:207). */
+ * nothing to the matrix (myocardiumDomain.C:207).
+ *
+ * General (non-orthogonal) meshes give the full geometry instead: with
+ * face_centres and the boundary faces the library assembles OpenFOAM's
+ * "Gauss linear corrected" Laplacian of a tensor conductivity
+ * (gaussLaplacianScheme::fvmLaplacian, finiteVolume of OpenFOAM v2312, the
+ * version line the reference builds against): linear interpolation weights,
+ * non-orthogonal deltaCoeffs 1/max(n.d, 0.05|d|) in the matrix, and in the
+ * source, re-evaluated every PIMPLE corrector, the explicit face fluxes
+ * SfGammaCorr.grad_f (conductivity not aligned with the face normal) plus
+ * SfGammaSn corrVec.grad_f (non-orthogonal correction), grad the cell
+ * gradient of Vm (leastSquares or Gauss linear) linearly interpolated to the
+ * face; on the walls SfGammaCorr.grad_b with grad_b the zeroGradient wall
+ * value of the gradient.  Replaces fvm::laplacian(conductivity_, Vm) of
+ * monodomainSolver.C:129-136 on such meshes. */
 typedef struct cfg_mesh_desc {
     long long n_cells, n_faces;
     const int* owner;            /* [n_faces] lower addressing */
@@ -140,7 +154,16 @@ typedef struct cfg_mesh_desc {
     int structured[3];           /* nx ny nz when the cells are a blockMesh block
                                     (x fastest) with uniform coefficients per
                                     direction; {0,0,0} for a general mesh */
+    /* full geometry of a general mesh (all NULL/0 otherwise) */
+    const double* face_centres;  /* [n_faces][3] */
+    long long n_boundary_faces;
+    const int* boundary_cell;    /* [n_boundary_faces] cell of each wall face */
+    const double* boundary_sf;   /* [n_boundary_faces][3] outward area vectors */
+    const double* boundary_centres;  /* [n_boundary_faces][3] */
 } cfg_mesh_desc;
+
+#define CFG_GRAD_LEAST_SQUARES 0    /* gradSchemes default leastSquares (tutorials) */
+#define CFG_GRAD_GAUSS_LINEAR 1     /* gradSchemes default Gauss linear */
 
 /* monodomainSolverCoeffs (tutorials/electroProperties.template) plus
  * fvSchemes/fvSolution settings used by the step. */
@@ -160,6 +183,15 @@ typedef struct cfg_monodomain_desc {
     int n_boxes;                 /* externalStimulus boxes (<= 8) */
     double box_min[8][3], box_max[8][3];
     double box_start[8], box_duration[8], box_intensity[8];
+    /* general meshes only (the mesh gives face_centres): */
+    const double* conductivity_per_cell;  /* optional host [n_cells][6] xx xy xz yy
+                                             yz zz, a 0/conductivity volTensorField
+                                             (monodomainSolver.C:48-100); wall faces
+                                             take their cell's value */
+    int grad_scheme;             /* CFG_GRAD_* of the explicit correction */
+    int laplacian_uncorrected;   /* laplacianSchemes Gauss linear uncorrected (1):
+                                    drops the non-orthogonal part of the
+                                    correction, keeps the tangential one */
 } cfg_monodomain_desc;
 
 typedef struct cfg_monodomain cfg_monodomain;
