@@ -124,7 +124,7 @@ def make_model(mesh, precision):
     return m
 
 
-def timed_steps(md, k, flush):
+def timed_steps(md, k, flush, dt=DT):
     """Run k steps, timing each with CUDA events on the context's stream;
     L2 is flushed (256 MB write on another stream) between steps."""
     import torch
@@ -133,7 +133,7 @@ def timed_steps(md, k, flush):
     for _ in range(k):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        md.step(DT)
+        md.step(dt)
         e1.record(stream)
         e1.synchronize()
         total += e0.elapsed_time(e1)
@@ -228,6 +228,95 @@ def gpu_arm(args, rank, world):
                 act_cells=int(both.sum()), vm_err=vm_err, window=window, t_e2e=t_e2e, ke2e=ke2e, achieved=achieved,
                 fp32_peak=fp32_peak, peaks=pk, peak_src=src, nnz=nnz,
                 n_active_mixed=int((act_mixed > 0).sum()))
+
+
+LV_DT = 1e-5
+LV_INTENSITY = 5e4       # A/m^3, for 2 ms
+
+
+def lv_arm(args, flush):
+    """The left-ventricle configuration: a truncated prolate-ellipsoid shell
+    of about 4.0 M tetrahedra with rule-based fibres (per-cell conductivity
+    tensors) and TNNP endo/M/epi cells, apical stimulus, the Laplacian with
+    its explicit non-orthogonal and tangential corrections; mixed form in
+    the step graph, timed over a bounded number of steps of the 400 ms run,
+    FP64 form timed on the same steps, and activation times of both forms
+    compared after an accuracy window."""
+    import torch
+    from cardiacfoam_gb300 import api, lib, lv
+    t0 = time.perf_counter()
+    dims = lv.config_sizes()
+    L = lv.left_ventricle(*dims)
+    t_mesh = time.perf_counter() - t0
+    lo, hi = L.apex_box(2e-3)
+    boxes = [(lo, hi, 0.0, 2e-3, LV_INTENSITY)]
+
+    def make(precision):
+        return api.Monodomain(L.mesh, "TNNP", "epicardialCells", dt=LV_DT, precision=precision,
+                              boxes=boxes, tissue_per_cell=L.tissue,
+                              conductivity_per_cell=L.conductivity, stencil=False,
+                              max_steps=10 ** 6)
+
+    t0 = time.perf_counter()
+    mixed = make(lib.PRECISION_MIXED)
+    t_setup = time.perf_counter() - t0
+    for _ in range(args.warmup):
+        mixed.step(LV_DT)
+    mixed.set_timing(True)
+    t_mixed = timed_steps(mixed, args.lv_steps, flush, LV_DT)
+    ionic_ms, diff_ms, nsteps, launches = mixed.timings()
+    mixed.set_timing(False)
+    iters, corrs = [], []
+    for _ in range(5):
+        mixed.step(LV_DT)
+        it = mixed.stats()[2]
+        iters.append(int(it.sum()))
+        corrs.append(int(it.size))
+    fp64 = make(lib.PRECISION_FP64)
+    for _ in range(1):
+        fp64.step(LV_DT)
+    fp64.set_timing(True)
+    k64 = max(1, min(args.lv_steps, args.lv_fp64_steps))
+    t_fp64 = timed_steps(fp64, k64, flush, LV_DT)
+    ionic64_ms, diff64_ms, _, _ = fp64.timings()
+    fp64.set_timing(False)
+    window = args.lv_accuracy_steps
+    fp64.run(LV_DT, window - 1 - k64)
+    mixed_b = make(lib.PRECISION_MIXED)
+    mixed_b.run(LV_DT, window)
+    a64, amx = fp64.activation(), mixed_b.activation()
+    both = (a64 > 0) & (amx > 0)
+    n = L.mesh.n_cells
+    out = {
+        "workload": (f"TNNP endo/M/epi by transmural fraction (0-0.3/0.3-0.6/0.6-1) on a "
+                     f"truncated prolate-ellipsoid LV shell (endo 25x25x60 mm, wall 10 mm, base "
+                     f"z=0): {dims[0]} x ({dims[1]}^2 + 4x{dims[1]}x{dims[2]}) hexahedra x 6 = "
+                     f"{n} tetrahedra; fibres +60 (endo) to -60 deg (epi), sigma_l 0.1334, "
+                     f"sigma_t 0.0176 S/m per cell; apical 2 mm cube stimulus 5e4 A/m^3 x 2 ms; "
+                     f"dt 1e-5 s; implicit backward ddt, Gauss linear corrected Laplacian "
+                     f"(leastSquares gradient), PIMPLE residualControl 1e-6, PCG tol 1e-8"),
+        "cells": n, "faces": L.mesh.n_faces, "wall_faces": L.mesh.n_boundary_faces,
+        "mesh_seconds": t_mesh, "setup_seconds": t_setup,
+        "mixed": {"value": n * args.lv_steps / t_mixed, "unit": "cell-steps/s",
+                  "steps": args.lv_steps, "ms_per_step": t_mixed / args.lv_steps * 1e3,
+                  "ionic_ms_per_step": ionic_ms / max(nsteps, 1),
+                  "diffusion_ms_per_step": diff_ms / max(nsteps, 1),
+                  "gpu_launches": launches,
+                  "pcg_iterations_per_step": iters, "pimple_correctors_per_step": corrs},
+        "fp64": {"value": n * k64 / t_fp64, "unit": "cell-steps/s", "steps": k64,
+                 "ms_per_step": t_fp64 / k64 * 1e3,
+                 "ionic_ms_per_step": ionic64_ms / k64, "diffusion_ms_per_step": diff64_ms / k64},
+        "speedup_mixed_vs_fp64": (n * args.lv_steps / t_mixed) / (n * k64 / t_fp64),
+        "accuracy": {"window_steps": window, "activated_cells": int(both.sum()),
+                     "activation_flag_mismatches": int(np.sum((a64 > 0) != (amx > 0))),
+                     "activation_error_ms": float(np.max(np.abs(a64[both] - amx[both])) * 1e3)
+                     if both.any() else None,
+                     "vm_linf_error_V": float(np.max(np.abs(fp64.vm() - mixed_b.vm())))},
+        "l2": "flushed (256 MB write) between timed steps",
+    }
+    del mixed, mixed_b, fp64
+    torch.cuda.synchronize()
+    return out
 
 
 def cpu_baseline(nthreads=None, cells_x=40, steps=10):
@@ -386,6 +475,10 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched single cells")
     ap.add_argument("--no-mms", action="store_true", help="skip the manufactured-solution sweep")
+    ap.add_argument("--no-lv", action="store_true", help="skip the left-ventricle configuration")
+    ap.add_argument("--lv-steps", type=int, default=20)
+    ap.add_argument("--lv-fp64-steps", type=int, default=3)
+    ap.add_argument("--lv-accuracy-steps", type=int, default=250)
     ap.add_argument("--batch-cells", type=int, default=65536)
     ap.add_argument("--batch-window", type=int, default=2000,
                     help="solver steps per cell timed for the mixed batch")
@@ -455,6 +548,11 @@ def main():
         "gpu_launches": r["launches"],
         "clocks": r["clocks"],
     }
+    if not args.no_lv:
+        import torch
+        flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+        out["left_ventricle"] = lv_arm(args, flush)
+        del flush
     if not args.no_batch:
         out["batched_single_cells"] = batch_arm(args)
     if not args.no_mms:
