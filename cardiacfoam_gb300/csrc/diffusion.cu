@@ -72,11 +72,7 @@ __global__ void __launch_bounds__(kDiffBlock) k_solve_begin(DiffusionArgs a)
         double su = -(a.chicm * a.iion[c]) * V;
         su = su + box_source(a, c, st->t0) * V;
         bb = bb + su;
-        if (a.nc_gw) {
-            const double* gr = a.grad;
-            const long long n = a.n;
-            bb = bb + nc_correction(a, c, [gr, n](long long q, int k) { return gr[k * n + q]; });
-        }
+        if (a.nc_gw) bb = bb + nc_correction_plain(a, c);
         const double* x = a.vm;
         const double ax = row_amul(a, c, d, [x](long long q) { return x[q]; });
         const double r = bb - ax;
@@ -110,11 +106,7 @@ __device__ __forceinline__ void grad_row(const DiffusionArgs& a, const double* x
 {
     const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= a.n) return;
-    double g[3];
-    nc_gradient(a, c, [x](long long q) { return x[q]; }, g);
-    a.grad[c] = g[0];
-    a.grad[a.n + c] = g[1];
-    a.grad[2 * a.n + c] = g[2];
+    nc_gradient_plain(a, c, x);
 }
 
 __global__ void __launch_bounds__(kDiffBlock) k_grad_iterate(DiffusionArgs a)
@@ -291,11 +283,7 @@ __global__ void k_explicit(DiffusionArgs a)
                 if (nb < c) div -= coef * (xc - x[nb]);
                 else div += coef * (x[nb] - xc);
             }
-            if (a.nc_gw) {
-                const double* gr = a.grad;
-                const long long n = a.n;
-                div += nc_correction(a, c, [gr, n](long long q, int k) { return gr[k * n + q]; });
-            }
+            if (a.nc_gw) div += nc_correction_plain(a, c);
         }
         double diag, src;
         if (a.ddt_backward) {

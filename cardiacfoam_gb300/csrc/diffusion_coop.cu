@@ -178,6 +178,7 @@ __device__ __forceinline__ double amul_cg(const DiffusionArgs& a, const CoopArgs
 //                A.p = w + beta A.p (linearity of A), sum p.A.p  | barrier
 //   update pass: x += alpha p, r -= alpha A.p, z = D^-1 r (published for
 //                the next halo pass), sums |r| and z.r           | barrier
+template <class CR>
 __global__ void __launch_bounds__(kCoopBlock, 1) k_implicit_coop(DiffusionArgs a, CoopArgs ca)
 {
     PcgState* st = a.st;
@@ -204,6 +205,7 @@ __global__ void __launch_bounds__(kCoopBlock, 1) k_implicit_coop(DiffusionArgs a
     long long step_iters = 0;
     double last_init = 0.0, last_res = 0.0;
     int last_iter = 0, last_v = 0;
+    int bsrc_variant = -1;            // ddt coefficient set of the kept source
 
     for (int corr = 1;; ++corr) {
         const int v = ddt_variant(a, n_old);
@@ -213,32 +215,43 @@ __global__ void __launch_bounds__(kCoopBlock, 1) k_implicit_coop(DiffusionArgs a
         const double cft0 = a.cft0[v], cft00 = a.cft00[v];
         // --- general mesh: gradient of the current iterate for the
         // Laplacian's explicit correction, published for the neighbours
-        double* __restrict__ grad = a.grad;
+        CR* __restrict__ grad = static_cast<CR*>(a.grad);
         if (a.nc_gw) {
             for (unsigned c = first; c < n; c += stride) {
-                double g[3];
-                nc_gradient(a, c, [x](long long q) { return __ldcg(&x[q]); }, g);
+                CR g[3];
+                nc_gradient<CR>(a, c, [x](long long q) { return __ldcg(&x[q]); }, g);
                 __stcg(&grad[c], g[0]);
                 __stcg(&grad[size_t(n) + c], g[1]);
                 __stcg(&grad[2 * size_t(n) + c], g[2]);
             }
             if (!grid_barrier(st, epoch)) { abort_step = true; break; }
         }
-        // --- source, A.x, r = b - A.x; sums of x and |r|
+        // --- source, A.x, r = b - A.x; sums of x and |r|.  The ddt, ionic
+        // and stimulus parts of the source change between correctors only
+        // with the ddt coefficient set (the first step creates the old-time
+        // levels in its first corrector): kept in bsrc for the others.
         double s1[2] = {0.0, 0.0};
+        const bool fresh = corr == 1 || v != bsrc_variant;
+        bsrc_variant = v;
         auto rhs_row = [&](unsigned c) {
-            const double V = a.vol[c];
-            double ddt_src;
-            if (a.ddt_backward)
-                ddt_src = a.rdt * V * (cft0 * a.vm_old[c] - cft00 * a.vm_oldold[c]);
-            else
-                ddt_src = a.rdt * a.vm_old[c] * V;
-            double bb = a.chicm * ddt_src;
-            double su = -(a.chicm * a.iion[c]) * V;
-            su = su + box_source(a, c, t0) * V;
-            double rhs = bb + su;
+            double rhs;
+            if (fresh) {
+                const double V = a.vol[c];
+                double ddt_src;
+                if (a.ddt_backward)
+                    ddt_src = a.rdt * V * (cft0 * a.vm_old[c] - cft00 * a.vm_oldold[c]);
+                else
+                    ddt_src = a.rdt * a.vm_old[c] * V;
+                double bb = a.chicm * ddt_src;
+                double su = -(a.chicm * a.iion[c]) * V;
+                su = su + box_source(a, c, t0) * V;
+                rhs = bb + su;
+                a.bsrc[c] = rhs;
+            } else {
+                rhs = a.bsrc[c];
+            }
             if (a.nc_gw)
-                rhs = rhs + nc_correction(a, c, [grad, n](long long q, int k) {
+                rhs = rhs + nc_correction<CR>(a, c, [grad, n](long long q, int k) {
                           return __ldcg(&grad[size_t(k) * n + size_t(q)]);
                       });
             return rhs;
@@ -421,9 +434,13 @@ int coop_grid_blocks(long long n)
     int dev = 0, sms = 0, per_sm = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return 0;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_implicit_coop, kCoopBlock, 0) !=
-        cudaSuccess)
+    int per_sm_f = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_implicit_coop<double>, kCoopBlock,
+                                                      0) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_f, k_implicit_coop<float>, kCoopBlock,
+                                                      0) != cudaSuccess)
         return 0;
+    per_sm = per_sm < per_sm_f ? per_sm : per_sm_f;
     long long want = (n + kCoopBlock - 1) / kCoopBlock;
     long long cap = (long long)sms * per_sm;
     return int(want < cap ? want : cap);
@@ -438,8 +455,9 @@ cudaError_t launch_implicit_coop(const DiffusionArgs& a, int blocks, cudaStream_
     }
     DiffusionArgs args = a;
     void* params[] = {&args, &ca};
-    return cudaLaunchCooperativeKernel(reinterpret_cast<void*>(k_implicit_coop), dim3(blocks),
-                                       dim3(kCoopBlock), params, 0, s);
+    void* fn = a.nc_fp32 ? reinterpret_cast<void*>(k_implicit_coop<float>)
+                         : reinterpret_cast<void*>(k_implicit_coop<double>);
+    return cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(kCoopBlock), params, 0, s);
 }
 
 }  // namespace cfg

@@ -63,12 +63,17 @@ struct DiffusionArgs {
     // explicit correction of the Laplacian on a general mesh (null: none):
     // per ELL slot the gradient weight of (x_nb - x_c), the correction
     // vector signed for the row (+ for the face's owner) and the row cell's
-    // interpolation weight; per cell the wall factor and the gradient
-    const double* nc_gw;       // [3][width][n]
-    const double* nc_k;        // [3][width][n]
-    const double* nc_om;       // [width][n]
-    const double* nc_bk;       // [3][n]
-    double* grad;              // [3][n]
+    // interpolation weight; per cell the wall factor and the gradient.
+    // Arrays of double, or of float when nc_fp32 (the mixed form).
+    const void* nc_gw;         // [3][width][n]
+    const void* nc_k;          // [3][width][n]
+    const void* nc_om;         // [width][n]
+    const void* nc_bk;         // [3][n]
+    void* grad;                // [3][n]
+    int nc_fp32;
+    // corrector-independent part of the source (ddt, -chi*Cm*Iion, stimulus),
+    // kept by the persistent kernel from the first corrector of a step
+    double* bsrc;              // [n]
     // stencil form (structured block, uniform coefficient per direction)
     int sx, sy, sz;            // nx, ny, nz (0 = use ELL)
     double cx, cy, cz;
@@ -195,20 +200,22 @@ __device__ __forceinline__ double row_amul(const DiffusionArgs& a, long long c, 
 }
 
 // Cell gradient of x at row c on a general mesh: sum over the row's slots
-// of gw_e (x_nb - x_c) (leastSquares or Gauss linear weights).
-template <class F>
-__device__ __forceinline__ void nc_gradient(const DiffusionArgs& a, long long c, F x, double (&g)[3])
+// of gw_e (x_nb - x_c) (leastSquares or Gauss linear weights), in R (the
+// differences are taken in FP64).
+template <class R, class F>
+__device__ __forceinline__ void nc_gradient(const DiffusionArgs& a, long long c, F x, R (&g)[3])
 {
+    const R* gw = static_cast<const R*>(a.nc_gw);
     const long long n = a.n, wn = (long long)a.width * n;
     const double xc = x(c);
-    g[0] = g[1] = g[2] = 0.0;
+    g[0] = g[1] = g[2] = R(0);
     const int cnt = a.ell_cnt[c];
     for (int e = 0; e < cnt; ++e) {
         const long long i = (long long)e * n + c;
-        const double dv = x(a.ell_col[i]) - xc;
-        g[0] += a.nc_gw[i] * dv;
-        g[1] += a.nc_gw[wn + i] * dv;
-        g[2] += a.nc_gw[2 * wn + i] * dv;
+        const R dv = R(x(a.ell_col[i]) - xc);
+        g[0] += gw[i] * dv;
+        g[1] += gw[wn + i] * dv;
+        g[2] += gw[2 * wn + i] * dv;
     }
 }
 
@@ -216,25 +223,58 @@ __device__ __forceinline__ void nc_gradient(const DiffusionArgs& a, long long c,
 // flux k.(w (g_P - g_N) + g_N) with the sign of the row (faces in column
 // order, the order of the face loop), then the wall term bk.g_c.  g(q, k)
 // reads component k of cell q's gradient.
-template <class G>
+template <class R, class G>
 __device__ __forceinline__ double nc_correction(const DiffusionArgs& a, long long c, G g)
 {
+    const R* kc = static_cast<const R*>(a.nc_k);
+    const R* omv = static_cast<const R*>(a.nc_om);
+    const R* bk = static_cast<const R*>(a.nc_bk);
     const long long n = a.n, wn = (long long)a.width * n;
-    const double g0 = g(c, 0), g1 = g(c, 1), g2 = g(c, 2);
-    double s = 0.0;
+    const R g0 = g(c, 0), g1 = g(c, 1), g2 = g(c, 2);
+    R s = R(0);
     const int cnt = a.ell_cnt[c];
     for (int e = 0; e < cnt; ++e) {
         const long long i = (long long)e * n + c;
         const long long nb = a.ell_col[i];
-        const double om = a.nc_om[i];
-        const double n0 = g(nb, 0), n1 = g(nb, 1), n2 = g(nb, 2);
-        const double f0 = om * (g0 - n0) + n0;
-        const double f1 = om * (g1 - n1) + n1;
-        const double f2 = om * (g2 - n2) + n2;
-        s += a.nc_k[i] * f0 + a.nc_k[wn + i] * f1 + a.nc_k[2 * wn + i] * f2;
+        const R om = omv[i];
+        const R n0 = g(nb, 0), n1 = g(nb, 1), n2 = g(nb, 2);
+        const R f0 = om * (g0 - n0) + n0;
+        const R f1 = om * (g1 - n1) + n1;
+        const R f2 = om * (g2 - n2) + n2;
+        s += kc[i] * f0 + kc[wn + i] * f1 + kc[2 * wn + i] * f2;
     }
-    s += a.nc_bk[c] * g0 + a.nc_bk[n + c] * g1 + a.nc_bk[2 * n + c] * g2;
-    return s;
+    s += bk[c] * g0 + bk[n + c] * g1 + bk[2 * n + c] * g2;
+    return double(s);
+}
+
+// The correction at row c from the gradient array (plain loads).
+__device__ __forceinline__ double nc_correction_plain(const DiffusionArgs& a, long long c)
+{
+    const long long n = a.n;
+    if (a.nc_fp32) {
+        const float* gr = static_cast<const float*>(a.grad);
+        return nc_correction<float>(a, c, [gr, n](long long q, int k) { return gr[k * n + q]; });
+    }
+    const double* gr = static_cast<const double*>(a.grad);
+    return nc_correction<double>(a, c, [gr, n](long long q, int k) { return gr[k * n + q]; });
+}
+
+// The gradient of x at row c into the gradient array (plain loads/stores).
+__device__ __forceinline__ void nc_gradient_plain(const DiffusionArgs& a, long long c,
+                                                  const double* x)
+{
+    const long long n = a.n;
+    if (a.nc_fp32) {
+        float g[3];
+        nc_gradient<float>(a, c, [x](long long q) { return x[q]; }, g);
+        float* gr = static_cast<float*>(a.grad);
+        gr[c] = g[0]; gr[n + c] = g[1]; gr[2 * n + c] = g[2];
+    } else {
+        double g[3];
+        nc_gradient<double>(a, c, [x](long long q) { return x[q]; }, g);
+        double* gr = static_cast<double*>(a.grad);
+        gr[c] = g[0]; gr[n + c] = g[1]; gr[2 * n + c] = g[2];
+    }
 }
 
 // row sum of the matrix (lduMatrix::sumA): diag then each -coef

@@ -1,5 +1,6 @@
 // cfg_ionic_*: the GPU ionic model behind the ionicModel plugin interface
 // (src/ionicModels/ionicModel/ionicModel.H:184-256).
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -164,9 +165,43 @@ int ionic_create(const cfg_ionic_desc* d, cudaStream_t stream, cfg_ionic** out)
     if (!e) e = dmalloc(&ion->d_evals, 1);
     if (!e) e = dmalloc(&ion->d_fail, 8);
     if (!e) e = cudaMemsetAsync(ion->d_fail, 0, 8 * sizeof(double), stream);
-    if (!e && d->tissue_per_cell) {
+    std::vector<unsigned char> slot_tissue;
+    if (d->tissue_per_cell && !d->scales && !ion->solve_vm) {
+        // group the cells by tissue flag (stable), one specialised launch per group
+        long long count[256] = {0};
+        for (long long c = 0; c < n; ++c) count[d->tissue_per_cell[c]]++;
+        int distinct = 0, only = 0;
+        for (int t = 0; t < 256; ++t)
+            if (count[t]) { ++distinct; only = t; }
+        if (distinct == 1) {
+            ion->tissue = only;   // one tissue after all: the uniform launch
+        } else if (distinct > 1) {
+            long long start[256], at = 0;
+            for (int t = 0; t < 256; ++t) {
+                start[t] = at;
+                if (count[t]) ion->groups.push_back({at, count[t], t});
+                at += count[t];
+            }
+            ion->h_perm.resize(size_t(n));
+            slot_tissue.resize(size_t(n));
+            for (long long c = 0; c < n; ++c) {
+                const int t = d->tissue_per_cell[c];
+                ion->h_perm[size_t(start[t])] = int(c);
+                slot_tissue[size_t(start[t])] = (unsigned char)t;
+                start[t]++;
+            }
+        }
+    } else if (d->tissue_per_cell) {
+        slot_tissue.assign(d->tissue_per_cell, d->tissue_per_cell + n);
+    }
+    if (!e && !slot_tissue.empty()) {
         e = dmalloc(&ion->d_tissue, size_t(n));
-        if (!e) e = cudaMemcpyAsync(ion->d_tissue, d->tissue_per_cell, size_t(n),
+        if (!e) e = cudaMemcpyAsync(ion->d_tissue, slot_tissue.data(), size_t(n),
+                                    cudaMemcpyHostToDevice, stream);
+    }
+    if (!e && !ion->h_perm.empty()) {
+        e = dmalloc(&ion->d_perm, size_t(n));
+        if (!e) e = cudaMemcpyAsync(ion->d_perm, ion->h_perm.data(), sizeof(int) * size_t(n),
                                     cudaMemcpyHostToDevice, stream);
     }
     if (!e && d->scales) {
@@ -201,6 +236,7 @@ void ionic_free(cfg_ionic* ion)
     dfree(ion->d_fail);
     dfree(ion->d_tissue);
     dfree(ion->d_scales);
+    dfree(ion->d_perm);
     if (ion->own_stream && ion->stream) cudaStreamDestroy(ion->stream);
     delete ion;
 }
@@ -210,6 +246,9 @@ IonicLaunch ionic_launch_args(const cfg_ionic* ion, double t0, double dt, const 
 {
     IonicLaunch L{};
     L.n = ion->n;
+    L.first = 0;
+    L.count = ion->n;
+    L.perm = ion->d_perm;
     L.t0 = t0;
     L.dt = dt;
     L.t_dev = t_dev;
@@ -232,7 +271,44 @@ IonicLaunch ionic_launch_args(const cfg_ionic* ion, double t0, double dt, const 
 
 cudaError_t ionic_enqueue(const cfg_ionic* ion, const IonicLaunch& L)
 {
-    return ion->ops->step[ion->precision][ion->solve_vm ? 1 : 0](L, ion->stream, ion->block);
+    const auto step = ion->ops->step[ion->precision][ion->solve_vm ? 1 : 0];
+    if (ion->groups.empty()) return step(L, ion->stream, ion->block);
+    for (const cfg_ionic::Group& g : ion->groups) {
+        IonicLaunch G = L;
+        G.first = g.first;
+        G.count = g.count;
+        G.tissue = g.tissue;
+        G.tissue_cell = nullptr;
+        if (cudaError_t e = step(G, ion->stream, ion->block)) return e;
+    }
+    return cudaSuccess;
+}
+
+// Reorder n values per row between the state slots and the cells.
+template <class T>
+static void slots_to_cells(const cfg_ionic* ion, T* a)
+{
+    if (ion->h_perm.empty()) return;
+    std::vector<T> tmp(a, a + ion->n);
+    for (long long k = 0; k < ion->n; ++k) a[ion->h_perm[size_t(k)]] = tmp[size_t(k)];
+}
+
+template <class T>
+static void cells_to_slots(const cfg_ionic* ion, const T* a, T* out)
+{
+    if (ion->h_perm.empty()) {
+        std::copy(a, a + ion->n, out);
+        return;
+    }
+    for (long long k = 0; k < ion->n; ++k) out[k] = a[ion->h_perm[size_t(k)]];
+}
+
+// state slot of integration point 0
+static long long slot_of_cell0(const cfg_ionic* ion)
+{
+    for (size_t k = 0; k < ion->h_perm.size(); ++k)
+        if (ion->h_perm[k] == 0) return (long long)k;
+    return 0;
 }
 
 int ionic_check_status(cfg_ionic* ion)
@@ -336,21 +412,23 @@ int cfg_ionic_get_states(cfg_ionic* ion, double* host)
             double* dst = host + size_t(i) * n;
             CFG_CUDA_TRY(cudaMemcpyAsync(dst, ion->d_yw + size_t(s) * n, sizeof(double) * n,
                                          cudaMemcpyDeviceToHost, ion->stream));
+            CFG_CUDA_TRY(cudaStreamSynchronize(ion->stream));
             if (p == CFG_PRECISION_MIXED) {
                 // each slot holds the FP32 pair (hi, lo) of the state
-                CFG_CUDA_TRY(cudaStreamSynchronize(ion->stream));
                 for (long long c = 0; c < n; ++c) {
                     float hl[2];
                     std::memcpy(hl, dst + c, sizeof hl);
                     dst[c] = double(hl[0]) + double(hl[1]);
                 }
             }
+            slots_to_cells(ion, dst);
         } else {
             tmp.resize(n);
             CFG_CUDA_TRY(cudaMemcpyAsync(tmp.data(), ion->d_yn + size_t(s) * n, sizeof(float) * n,
                                          cudaMemcpyDeviceToHost, ion->stream));
             CFG_CUDA_TRY(cudaStreamSynchronize(ion->stream));
             for (long long c = 0; c < n; ++c) host[size_t(i) * n + c] = tmp[c];
+            slots_to_cells(ion, host + size_t(i) * n);
         }
     }
     CFG_CUDA_TRY(cudaStreamSynchronize(ion->stream));
@@ -363,12 +441,14 @@ int cfg_ionic_set_states(cfg_ionic* ion, const double* host)
     const long long n = ion->n;
     const int p = ion->precision, ns = ion->ops->ns;
     std::vector<float> tmp;
+    std::vector<double> row(static_cast<size_t>(n));
     for (int i = 0; i < ns; ++i) {
         const int w = ion->ops->wide_of[p * ns + i], s = ion->ops->slot_of[p * ns + i];
+        cells_to_slots(ion, host + size_t(i) * n, row.data());
         if (w && p == CFG_PRECISION_MIXED) {
             std::vector<double> pairs(static_cast<size_t>(n));
             for (long long c = 0; c < n; ++c) {
-                const double v = host[size_t(i) * n + c];
+                const double v = row[size_t(c)];
                 const float hl[2] = {float(v), float(v - double(float(v)))};
                 std::memcpy(&pairs[size_t(c)], hl, sizeof hl);
             }
@@ -376,11 +456,12 @@ int cfg_ionic_set_states(cfg_ionic* ion, const double* host)
                                          sizeof(double) * n, cudaMemcpyHostToDevice, ion->stream));
             CFG_CUDA_TRY(cudaStreamSynchronize(ion->stream));
         } else if (w) {
-            CFG_CUDA_TRY(cudaMemcpyAsync(ion->d_yw + size_t(s) * n, host + size_t(i) * n,
+            CFG_CUDA_TRY(cudaMemcpyAsync(ion->d_yw + size_t(s) * n, row.data(),
                                          sizeof(double) * n, cudaMemcpyHostToDevice, ion->stream));
+            CFG_CUDA_TRY(cudaStreamSynchronize(ion->stream));
         } else {
             tmp.resize(n);
-            for (long long c = 0; c < n; ++c) tmp[c] = float(host[size_t(i) * n + c]);
+            for (long long c = 0; c < n; ++c) tmp[c] = float(row[size_t(c)]);
             CFG_CUDA_TRY(cudaMemcpyAsync(ion->d_yn + size_t(s) * n, tmp.data(), sizeof(float) * n,
                                          cudaMemcpyHostToDevice, ion->stream));
             CFG_CUDA_TRY(cudaStreamSynchronize(ion->stream));
@@ -396,6 +477,7 @@ int cfg_ionic_get_steps(cfg_ionic* ion, double* host)
     CFG_CUDA_TRY(cudaMemcpyAsync(host, ion->d_step, sizeof(double) * size_t(ion->n),
                                  cudaMemcpyDeviceToHost, ion->stream));
     CFG_CUDA_TRY(cudaStreamSynchronize(ion->stream));
+    slots_to_cells(ion, host);
     return CFG_OK;
 }
 
@@ -539,13 +621,15 @@ int cfg_ionic_sweep_current(cfg_ionic* ion, const char* current, double v_min, d
 
     // states of integration point 0 and the model's constants
     const long long n = ion->n;
+    const long long k0 = slot_of_cell0(ion);
     const int p = ion->precision, ns = m->ns;
     std::vector<double> y0(static_cast<size_t>(ns));
     for (int i = 0; i < ns; ++i) {
         const int w = m->wide_of[p * ns + i], s = m->slot_of[p * ns + i];
         if (w) {
             double v = 0.0;
-            CFG_CUDA_TRY(cudaMemcpy(&v, ion->d_yw + size_t(s) * n, sizeof v, cudaMemcpyDeviceToHost));
+            CFG_CUDA_TRY(cudaMemcpy(&v, ion->d_yw + size_t(s) * n + k0, sizeof v,
+                                    cudaMemcpyDeviceToHost));
             if (p == CFG_PRECISION_MIXED) {
                 float hl[2];
                 std::memcpy(hl, &v, sizeof hl);
@@ -554,14 +638,15 @@ int cfg_ionic_sweep_current(cfg_ionic* ion, const char* current, double v_min, d
             y0[size_t(i)] = v;
         } else {
             float v = 0.0f;
-            CFG_CUDA_TRY(cudaMemcpy(&v, ion->d_yn + size_t(s) * n, sizeof v, cudaMemcpyDeviceToHost));
+            CFG_CUDA_TRY(cudaMemcpy(&v, ion->d_yn + size_t(s) * n + k0, sizeof v,
+                                    cudaMemcpyDeviceToHost));
             y0[size_t(i)] = v;
         }
     }
     int tissue = ion->tissue;
     if (ion->d_tissue) {
         unsigned char t = 0;
-        CFG_CUDA_TRY(cudaMemcpy(&t, ion->d_tissue, 1, cudaMemcpyDeviceToHost));
+        CFG_CUDA_TRY(cudaMemcpy(&t, ion->d_tissue + k0, 1, cudaMemcpyDeviceToHost));
         tissue = t;
     }
     double sc[6];

@@ -1,6 +1,8 @@
 // Host representation of a GPU ionic model (one ionicModel instance).
 #pragma once
 
+#include <vector>
+
 #include "host_common.h"
 #include "ionic_registry.h"
 
@@ -20,8 +22,18 @@ struct cfg_ionic {
     int* d_status = nullptr;
     unsigned long long* d_evals = nullptr;
     double* d_fail = nullptr;      // IonicFailure record of the first failing cell
-    unsigned char* d_tissue = nullptr;
+    unsigned char* d_tissue = nullptr;   // per state slot
     double* d_scales = nullptr;
+    // Per-cell tissue flags without conductance scales: the states are kept
+    // grouped by tissue (slot k holds cell perm[k]) and each group runs the
+    // kernel specialised for its tissue.
+    struct Group {
+        long long first, count;
+        int tissue;
+    };
+    std::vector<Group> groups;
+    std::vector<int> h_perm;
+    int* d_perm = nullptr;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     int block = 128;

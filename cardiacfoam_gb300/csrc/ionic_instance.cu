@@ -32,11 +32,11 @@ template <bool SV, int T>
 static void launch_one(const cfg::IonicLaunch& p, cudaStream_t s, int block)
 {
     if constexpr (kFP64) {
-        const unsigned grid = unsigned((p.n + block - 1) / block);
+        const unsigned grid = unsigned((p.count + block - 1) / block);
         cfg::ionic_step_kernel<M, true, SV, T><<<grid, block, 0, s>>>(p);
     } else {
         using S = cfg::mixed::Slice<M>;
-        const unsigned grid = unsigned((p.n + S::block - 1) / S::block);
+        const unsigned grid = unsigned((p.count + S::block - 1) / S::block);
         cfg::ionic_mixed_kernel<M, SV, T><<<grid, S::block, S::smem_bytes, s>>>(p);
     }
 }
@@ -82,7 +82,7 @@ static bool launch_uniform(const cfg::IonicLaunch& p, cudaStream_t s, int block,
 extern "C" cudaError_t CFG_CAT3(cfg_ionic_step_, CFG_MODEL, CFG_PREC_TAG)(
     const cfg::IonicLaunch& p, int solve_vm, cudaStream_t stream, int block)
 {
-    if (p.n <= 0) return cudaSuccess;
+    if (p.n <= 0 || p.count <= 0) return cudaSuccess;
     const bool uniform = !p.tissue_cell && !p.scales;
     if (solve_vm) {
         launch_one<true, 0>(p, stream, block);

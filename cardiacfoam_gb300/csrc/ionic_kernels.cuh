@@ -42,7 +42,9 @@ namespace cfg {
 constexpr int kStateUnroll = CFG_IONIC_STATE_UNROLL;
 
 struct IonicLaunch {
-    long long n;                     // cells
+    long long n;                     // cells (and the stride of the state arrays)
+    long long first, count;          // state slots [first, first + count) of this launch
+    const int* perm;                 // [n] cell of each state slot, or null (slot = cell)
     double t0, dt;                   // PDE step [s] (used when t_dev is null)
     const double* t_dev;             // device time of the step start [s], or null
     int tissue;                      // uniform tissue flag (when tissue_cell is null)
@@ -367,9 +369,10 @@ __global__ void __launch_bounds__(128, CFG_IONIC_MIN_BLOCKS) ionic_step_kernel(I
     using R = typename std::conditional<FP64, double, float>::type;
     using L = Layout<M, FP64>;
     constexpr int NS = M::NS;
-    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long c = p.first + (long long)blockIdx.x * blockDim.x + threadIdx.x;
     unsigned evals = 0;
-    if (c < p.n) {
+    if (c < p.first + p.count) {
+        const long long cell = p.perm ? p.perm[c] : c;
         const double t0 = p.t_dev ? p.t_dev[0] : p.t0;
         double ts, te, dtm;
         model_times<M>(t0, p.dt, ts, te, dtm);
@@ -385,7 +388,7 @@ __global__ void __launch_bounds__(128, CFG_IONIC_MIN_BLOCKS) ionic_step_kernel(I
             }
         }
         if (!SV) {
-            cs.y[0] = vm_to_state0<M::VM_MAP>(p.vm[c]);
+            cs.y[0] = vm_to_state0<M::VM_MAP>(p.vm[cell]);
             cs.yf[0] = R(cs.y[0]);
         }
         double step = p.step[c];
@@ -432,13 +435,13 @@ __global__ void __launch_bounds__(128, CFG_IONIC_MIN_BLOCKS) ionic_step_kernel(I
             if (p.fail_record && !(prev & CFG_ERR_ODE_STEPS)) {
                 // the thread that raised the flag first writes the record
                 double* r = p.fail_record;
-                r[0] = double(c); r[1] = why.reason; r[2] = why.x; r[3] = why.dx;
+                r[0] = double(cell); r[1] = why.reason; r[2] = why.x; r[3] = why.dx;
                 r[4] = why.worst; r[5] = why.err; r[6] = why.value; r[7] = double(why.steps);
             }
         }
         const double im = double(iion) * M::IION_SCALE;
         if (!isfinite(im)) atomicOr(p.status, CFG_ERR_NONFINITE);
-        if (p.im) p.im[c] = im;
+        if (p.im) p.im[cell] = im;
 
 #pragma unroll
         for (int i = 0; i < NS; ++i) {

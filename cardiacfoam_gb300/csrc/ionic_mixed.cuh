@@ -317,9 +317,10 @@ ionic_mixed_kernel(IonicLaunch p)
     float* T = Y + P;
     float* K = T + P;
     float* LO = K + 5 * P;
-    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long c = p.first + (long long)blockIdx.x * blockDim.x + threadIdx.x;
     unsigned evals = 0;
-    if (c < p.n) {
+    if (c < p.first + p.count) {
+        const long long cell = p.perm ? p.perm[c] : c;
         const double t0 = p.t_dev ? p.t_dev[0] : p.t0;
         double ts, te, dtm;
         model_times<M>(t0, p.dt, ts, te, dtm);
@@ -340,7 +341,7 @@ ionic_mixed_kernel(IonicLaunch p)
         }
         if constexpr (!SV) {
             // Vm from the PDE field, split into hi + lo
-            const double v = vm_to_state0<M::VM_MAP>(p.vm[c]);
+            const double v = vm_to_state0<M::VM_MAP>(p.vm[cell]);
             const float hi = float(v);
             Y[0] = hi;
             if (is_wide<M::WIDE_MASK>(0)) LO[0] = float(v - double(hi));
@@ -375,13 +376,13 @@ ionic_mixed_kernel(IonicLaunch p)
             const int prev = atomicOr(p.status, CFG_ERR_ODE_STEPS);
             if (p.fail_record && !(prev & CFG_ERR_ODE_STEPS)) {
                 double* r = p.fail_record;
-                r[0] = double(c); r[1] = why.reason; r[2] = why.x; r[3] = why.dx;
+                r[0] = double(cell); r[1] = why.reason; r[2] = why.x; r[3] = why.dx;
                 r[4] = why.worst; r[5] = why.err; r[6] = why.value; r[7] = double(why.steps);
             }
         }
         const double im = double(iion) * M::IION_SCALE;
         if (!isfinite(im)) atomicOr(p.status, CFG_ERR_NONFINITE);
-        if (p.im) p.im[c] = im;
+        if (p.im) p.im[cell] = im;
         float2* yw2o = reinterpret_cast<float2*>(p.yw);
         w = 0;
 #pragma unroll

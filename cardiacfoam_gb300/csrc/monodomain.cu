@@ -39,8 +39,11 @@ static void md_free(cfg_monodomain* md)
     dfree(md->d_diag2); dfree(md->d_rdiag2); dfree(md->d_sumA2); dfree(md->d_b); dfree(md->d_r);
     dfree(md->d_z); dfree(md->d_ax); dfree(md->d_pA); dfree(md->d_pB); dfree(md->d_ap);
     dfree(md->d_partial); dfree(md->d_st);
-    dfree(md->d_nc_gw); dfree(md->d_nc_k); dfree(md->d_nc_om); dfree(md->d_nc_bk);
-    dfree(md->d_grad);
+    for (void** p : {&md->d_nc_gw, &md->d_nc_k, &md->d_nc_om, &md->d_nc_bk, &md->d_grad}) {
+        if (*p) cudaFree(*p);
+        *p = nullptr;
+    }
+    dfree(md->d_bsrc);
     if (md->h_st) cudaFreeHost(md->h_st);
     if (md->stream) cudaStreamDestroy(md->stream);
     delete md;
@@ -182,21 +185,28 @@ static int build_operator(cfg_monodomain* md, const cfg_mesh_desc* m, const cfg_
         std::vector<double> bk(size_t(3) * size_t(n));
         for (long long c = 0; c < n; ++c)
             for (int k = 0; k < 3; ++k) bk[size_t(k) * size_t(n) + size_t(c)] = op.bk[size_t(3 * c + k)];
-        CFG_CUDA_TRY(dmalloc(&md->d_nc_gw, gw.size()));
-        CFG_CUDA_TRY(dmalloc(&md->d_nc_k, kc.size()));
-        CFG_CUDA_TRY(dmalloc(&md->d_nc_om, om.size()));
-        CFG_CUDA_TRY(dmalloc(&md->d_nc_bk, bk.size()));
-        CFG_CUDA_TRY(dmalloc(&md->d_grad, size_t(3) * size_t(n)));
-        CFG_CUDA_TRY(cudaMemcpy(md->d_nc_gw, gw.data(), gw.size() * sizeof(double),
-                                cudaMemcpyHostToDevice));
-        CFG_CUDA_TRY(cudaMemcpy(md->d_nc_k, kc.data(), kc.size() * sizeof(double),
-                                cudaMemcpyHostToDevice));
-        CFG_CUDA_TRY(cudaMemcpy(md->d_nc_om, om.data(), om.size() * sizeof(double),
-                                cudaMemcpyHostToDevice));
-        CFG_CUDA_TRY(cudaMemcpy(md->d_nc_bk, bk.data(), bk.size() * sizeof(double),
-                                cudaMemcpyHostToDevice));
-        CFG_CUDA_TRY(cudaMemset(md->d_grad, 0, sizeof(double) * 3 * size_t(n)));
-        md->ell_bytes += (gw.size() + kc.size() + om.size()) * sizeof(double);
+        // the mixed form evaluates the correction (a small explicit source)
+        // in FP32 from FP64 differences of Vm
+        md->nc_fp32 = d->ionic.precision == CFG_PRECISION_MIXED;
+        auto upload = [&](void** dst, const std::vector<double>& v) -> cudaError_t {
+            if (md->nc_fp32) {
+                std::vector<float> f(v.begin(), v.end());
+                cudaError_t e = cudaMalloc(dst, f.size() * sizeof(float));
+                if (!e) e = cudaMemcpy(*dst, f.data(), f.size() * sizeof(float), cudaMemcpyHostToDevice);
+                return e;
+            }
+            cudaError_t e = cudaMalloc(dst, v.size() * sizeof(double));
+            if (!e) e = cudaMemcpy(*dst, v.data(), v.size() * sizeof(double), cudaMemcpyHostToDevice);
+            return e;
+        };
+        const size_t esz = md->nc_fp32 ? sizeof(float) : sizeof(double);
+        CFG_CUDA_TRY(upload(&md->d_nc_gw, gw));
+        CFG_CUDA_TRY(upload(&md->d_nc_k, kc));
+        CFG_CUDA_TRY(upload(&md->d_nc_om, om));
+        CFG_CUDA_TRY(upload(&md->d_nc_bk, bk));
+        CFG_CUDA_TRY(cudaMalloc(&md->d_grad, esz * 3 * size_t(n)));
+        CFG_CUDA_TRY(cudaMemset(md->d_grad, 0, esz * 3 * size_t(n)));
+        md->ell_bytes += (gw.size() + kc.size() + om.size()) * esz;
     }
     return CFG_OK;
 }
@@ -217,6 +227,8 @@ static void fill_args(cfg_monodomain* md, double dt)
     a.nc_om = md->d_nc_om;
     a.nc_bk = md->d_nc_bk;
     a.grad = md->d_grad;
+    a.nc_fp32 = md->nc_fp32 ? 1 : 0;
+    a.bsrc = md->d_bsrc;
     a.sx = md->use_stencil ? md->sx : 0;
     a.sy = md->sy;
     a.sz = md->sz;
@@ -311,7 +323,7 @@ int monodomain_create(const cfg_monodomain_desc* d, const cfg_mesh_desc* m, cfg_
     cudaError_t e = cudaSuccess;
     double** vecs[] = {&md->d_vol, &md->d_vm, &md->d_vm_old, &md->d_vm_oldold, &md->d_iion,
                        &md->d_act, &md->d_b, &md->d_r, &md->d_z, &md->d_ax, &md->d_pA,
-                       &md->d_pB, &md->d_ap};
+                       &md->d_pB, &md->d_ap, &md->d_bsrc};
     for (double** v : vecs)
         if (!e) e = dmalloc(v, n);
     if (!e) e = dmalloc(&md->d_diag2, 2 * n);

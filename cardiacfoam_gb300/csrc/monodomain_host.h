@@ -30,8 +30,10 @@ struct cfg_monodomain {
     double* d_vol = nullptr;
     // explicit correction of the Laplacian on a general mesh
     bool corrected = false;
-    double *d_nc_gw = nullptr, *d_nc_k = nullptr, *d_nc_om = nullptr, *d_nc_bk = nullptr;
-    double* d_grad = nullptr;
+    bool nc_fp32 = false;         // correction arrays in float (mixed form)
+    void *d_nc_gw = nullptr, *d_nc_k = nullptr, *d_nc_om = nullptr, *d_nc_bk = nullptr;
+    void* d_grad = nullptr;
+    double* d_bsrc = nullptr;     // corrector-independent source of the persistent kernel
     double *d_vm = nullptr, *d_vm_old = nullptr, *d_vm_oldold = nullptr, *d_iion = nullptr;
     double* d_act = nullptr;
     unsigned char* d_act_flag = nullptr;
