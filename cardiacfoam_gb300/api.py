@@ -392,3 +392,75 @@ class BatchCells:
             self.h = None
 
     __del__ = close
+
+
+class AdjointProblem:
+    """Probe-voltage misfit of the differentiable monodomain step and its
+    gradient (cfg_adjoint_*): per-cell log-scales of TNNP g_Na and g_K1 and
+    the conductivities sigma_l, sigma_t along/across the fibre direction."""
+
+    def __init__(self, mesh: LduMesh, n_steps: int, dt: float, probes: Sequence[int],
+                 sample_every: int, checkpoint_every: int = 200, substeps: int = 5,
+                 tissue="epicardialCells", chi=140000.0, cm=0.01, vm0=-0.084,
+                 fibre=(1.0, 0.0, 0.0), boxes: Sequence = (), pcg_tol=1e-13,
+                 pcg_max_iter=10000):
+        self._lib = _L.load()
+        self.mesh = mesh
+        self.n = mesh.n_cells
+        self.n_steps = n_steps
+        self.dt = dt
+        self.probes = np.ascontiguousarray(probes, dtype=np.int32)
+        self.n_samples = n_steps // sample_every
+        d = _L.AdjointDesc()
+        d.ionic_model = b"TNNP"
+        d.tissue = tissue.encode()
+        d.delta_t = dt
+        d.n_steps = n_steps
+        d.substeps = substeps
+        d.checkpoint_every = checkpoint_every
+        d.sample_every = sample_every
+        d.n_probes = self.probes.size
+        d.probes = _L.iptr(self.probes)
+        d.chi, d.cm, d.vm0 = chi, cm, vm0
+        for k in range(3):
+            d.fibre[k] = fibre[k]
+        d.n_boxes = len(boxes)
+        for b, (lo, hi, t0, dur, inten) in enumerate(boxes):
+            for k in range(3):
+                d.box_min[b][k] = lo[k]
+                d.box_max[b][k] = hi[k]
+            d.box_start[b], d.box_duration[b], d.box_intensity[b] = t0, dur, inten
+        d.pcg_tol, d.pcg_max_iter = pcg_tol, pcg_max_iter
+        md, self._keep = mesh_desc(mesh, structured=False)
+        h = C.c_void_p()
+        _L.check(self._lib.cfg_adjoint_create(C.byref(d), C.byref(md), C.byref(h)))
+        self.h = h
+
+    def set_target(self, target: np.ndarray):
+        t = np.ascontiguousarray(target, dtype=np.float64).reshape(self.n_samples,
+                                                                   self.probes.size)
+        _L.check(self._lib.cfg_adjoint_set_target(self.h, _L.dptr(t)))
+
+    def forward(self, log_gna: np.ndarray, log_gk1: np.ndarray, sigma_l: float,
+                sigma_t: float):
+        """(J, probe trace [n_samples][n_probes])."""
+        a = np.ascontiguousarray(log_gna, dtype=np.float64)
+        b = np.ascontiguousarray(log_gk1, dtype=np.float64)
+        loss = np.zeros(1)
+        trace = np.zeros((self.n_samples, self.probes.size))
+        _L.check(self._lib.cfg_adjoint_forward(self.h, _L.dptr(a), _L.dptr(b), float(sigma_l),
+                                               float(sigma_t), _L.dptr(loss), _L.dptr(trace)))
+        return float(loss[0]), trace
+
+    def backward(self):
+        """(dJ/dlog_gna [n], dJ/dlog_gk1 [n], dJ/d(sigma_l, sigma_t) [2])."""
+        ga, gb, gs = np.zeros(self.n), np.zeros(self.n), np.zeros(2)
+        _L.check(self._lib.cfg_adjoint_backward(self.h, _L.dptr(ga), _L.dptr(gb), _L.dptr(gs)))
+        return ga, gb, gs
+
+    def close(self):
+        if getattr(self, "h", None):
+            self._lib.cfg_adjoint_destroy(self.h)
+            self.h = None
+
+    __del__ = close

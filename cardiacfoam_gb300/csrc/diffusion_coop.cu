@@ -28,103 +28,25 @@
 #include <cuda_runtime.h>
 
 #include "diffusion_kernels.cuh"
+#include "grid_sync.cuh"
 
 namespace cfg {
 
 namespace {
 
 constexpr int kCoopBlock = 512;
-constexpr int kCoopWarps = kCoopBlock / 32;
-constexpr long long kSpinLimit = 1LL << 25;   // x >= 32 ns per spin: about a second
-
-__device__ __forceinline__ unsigned ld_acquire(const unsigned* p)
-{
-    unsigned v;
-    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    return v;
-}
-
-__device__ __forceinline__ int ld_relaxed_int(const int* p)
-{
-    int v;
-    asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    return v;
-}
-
-// Grid-wide barrier on a monotonic arrival counter (reset every step):
-// each block adds one arrival and waits until all gridDim.x arrivals of this
-// barrier are in; `epoch` counts the arrivals expected so far.  Returns false
-// when the step was aborted (a block waited too long); then every block
-// leaves at its next barrier.
 __device__ __forceinline__ bool grid_barrier(PcgState* st, unsigned& epoch)
 {
-    __shared__ int ok;
-    epoch += gridDim.x;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        __threadfence();
-        atomicAdd(&st->bar_count, 1u);
-        int good = 1;
-        long long spins = 0;
-        while (ld_acquire(&st->bar_count) < epoch) {
-            if (ld_relaxed_int(&st->bar_abort)) { good = 0; break; }
-            if (++spins > kSpinLimit) {
-                atomicExch(&st->bar_abort, 1);
-                good = 0;
-                break;
-            }
-            if (spins > 32) __nanosleep(32);
-        }
-        if (ld_relaxed_int(&st->bar_abort)) good = 0;
-        __threadfence();
-        ok = good;
-    }
-    __syncthreads();
-    return ok != 0;
+    return gsync::grid_barrier(&st->bar_count, &st->bar_abort, epoch);
 }
 
-// Block sums of K per-thread values into partial[set][k][blockIdx.x].
 template <int K>
 __device__ __forceinline__ void block_sums(double* partial, int set, double (&v)[K])
 {
-    __shared__ double sh[K][kCoopWarps];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-        double s = v[k];
-        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-        if (lane == 0) sh[k][w] = s;
-    }
-    __syncthreads();
-    if (threadIdx.x < 32 * K && (threadIdx.x & 31) == 0) {
-        const int k = threadIdx.x >> 5;
-        double s = 0.0;
-        for (int j = 0; j < kCoopWarps; ++j) s += sh[k][j];
-        __stcg(&partial[(size_t(set) * 2 + k) * gridDim.x + blockIdx.x], s);
-    }
+    gsync::block_sums<kCoopBlock, K>(partial, set, v);
 }
 
-// Sum of partial[set][k][0..gridDim.x) in a fixed order; every block gets
-// the same value.  Called after a grid barrier, by all threads.
-template <int K>
-__device__ __forceinline__ void grid_sums(const double* partial, int set, double (&out)[K])
-{
-    __shared__ double sh[K];
-    if (threadIdx.x < 32) {
-#pragma unroll
-        for (int k = 0; k < K; ++k) {
-            const double* src = partial + (size_t(set) * 2 + k) * gridDim.x;
-            double s = 0.0;
-            for (unsigned i = threadIdx.x; i < gridDim.x; i += 32) s += __ldcg(&src[i]);
-            for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-            if (threadIdx.x == 0) sh[k] = s;
-        }
-    }
-    __syncthreads();
-#pragma unroll
-    for (int k = 0; k < K; ++k) out[k] = sh[k];
-    __syncthreads();
-}
+using gsync::grid_sums;
 
 // x / d for 0 <= x < 2^31 by multiply-high (round-up method): avoids the
 // 64-bit integer division of a cell index in every stencil row.

@@ -1,0 +1,105 @@
+// Grid-wide synchronisation and deterministic reductions for persistent
+// cooperative kernels (every block resident).  A barrier counts arrivals on a
+// monotonic counter that the caller resets before the launch, and its spin
+// is bounded: a block that waits longer than about a second sets an abort
+// flag and every block leaves at its next barrier.
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace cfg {
+namespace gsync {
+
+constexpr long long kSpinLimit = 1LL << 25;   // x >= 32 ns per spin: about a second
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned* p)
+{
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ int ld_relaxed_int(const int* p)
+{
+    int v;
+    asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Each block adds one arrival and waits until all gridDim.x arrivals of this
+// barrier are in; `epoch` counts the arrivals expected so far.  Returns false
+// when the launch was aborted (some block waited too long).
+__device__ __forceinline__ bool grid_barrier(unsigned* count, int* abort, unsigned& epoch)
+{
+    __shared__ int ok;
+    epoch += gridDim.x;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        atomicAdd(count, 1u);
+        int good = 1;
+        long long spins = 0;
+        while (ld_acquire(count) < epoch) {
+            if (ld_relaxed_int(abort)) { good = 0; break; }
+            if (++spins > kSpinLimit) {
+                atomicExch(abort, 1);
+                good = 0;
+                break;
+            }
+            if (spins > 32) __nanosleep(32);
+        }
+        if (ld_relaxed_int(abort)) good = 0;
+        __threadfence();
+        ok = good;
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+// Block sums of K per-thread values into partial[set][k][blockIdx.x]
+// (sets of two slots, alternated between consecutive reductions).
+template <int kBlock, int K>
+__device__ __forceinline__ void block_sums(double* partial, int set, double (&v)[K])
+{
+    constexpr int kWarps = kBlock / 32;
+    __shared__ double sh[K][kWarps];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        double s = v[k];
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+        if (lane == 0) sh[k][w] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x < 32 * K && (threadIdx.x & 31) == 0) {
+        const int k = threadIdx.x >> 5;
+        double s = 0.0;
+        for (int j = 0; j < kWarps; ++j) s += sh[k][j];
+        __stcg(&partial[(size_t(set) * 2 + k) * gridDim.x + blockIdx.x], s);
+    }
+}
+
+// Sum of partial[set][k][0..gridDim.x) in a fixed order; every block gets
+// the same value.  Called after a grid barrier, by all threads.
+template <int K>
+__device__ __forceinline__ void grid_sums(const double* partial, int set, double (&out)[K])
+{
+    __shared__ double sh[K];
+    if (threadIdx.x < 32) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            const double* src = partial + (size_t(set) * 2 + k) * gridDim.x;
+            double s = 0.0;
+            for (unsigned i = threadIdx.x; i < gridDim.x; i += 32) s += __ldcg(&src[i]);
+            for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+            if (threadIdx.x == 0) sh[k] = s;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < K; ++k) out[k] = sh[k];
+    __syncthreads();
+}
+
+}  // namespace gsync
+}  // namespace cfg

@@ -109,6 +109,18 @@ class BatchDesc(C.Structure):
                 ("trace_cells", C.c_longlong), ("trace_samples", C.c_longlong),
                 ("chunk", C.c_longlong)]
 
+class AdjointDesc(C.Structure):
+    _fields_ = [("ionic_model", C.c_char_p), ("tissue", C.c_char_p), ("delta_t", C.c_double),
+                ("n_steps", C.c_longlong), ("substeps", C.c_int), ("checkpoint_every", C.c_int),
+                ("sample_every", C.c_int), ("n_probes", C.c_int), ("probes", _ip),
+                ("chi", C.c_double), ("cm", C.c_double), ("vm0", C.c_double),
+                ("fibre", C.c_double * 3), ("n_boxes", C.c_int),
+                ("box_min", (C.c_double * 3) * 8), ("box_max", (C.c_double * 3) * 8),
+                ("box_start", C.c_double * 8), ("box_duration", C.c_double * 8),
+                ("box_intensity", C.c_double * 8), ("pcg_tol", C.c_double),
+                ("pcg_max_iter", C.c_int)]
+
+
 # every symbol declared in include/cardiac_gpu.h
 EXPORTS = [
     "cfg_last_error", "cfg_ionic_create", "cfg_ionic_solve", "cfg_ionic_solve_device",
@@ -121,7 +133,8 @@ EXPORTS = [
     "cfg_monodomain_stream", "cfg_monodomain_destroy", "cfg_box_diffusion_solve_noalloc",
     "cfg_monodomain_set_persistent", "cfg_batch_create", "cfg_batch_run", "cfg_batch_results",
     "cfg_batch_trace", "cfg_batch_get_states", "cfg_batch_stats", "cfg_batch_stream",
-    "cfg_batch_destroy",
+    "cfg_batch_destroy", "cfg_adjoint_create", "cfg_adjoint_set_target", "cfg_adjoint_forward",
+    "cfg_adjoint_backward", "cfg_adjoint_destroy",
 ]
 
 _lib = None
@@ -183,6 +196,12 @@ def load(path: Optional[os.PathLike] = None):
     L.cfg_batch_stream.argtypes = [C.c_void_p]
     L.cfg_batch_stream.restype = C.c_void_p
     L.cfg_batch_destroy.argtypes = [C.c_void_p]
+    L.cfg_adjoint_create.argtypes = [C.POINTER(AdjointDesc), C.POINTER(MeshDesc),
+                                     C.POINTER(C.c_void_p)]
+    L.cfg_adjoint_set_target.argtypes = [C.c_void_p, _dp]
+    L.cfg_adjoint_forward.argtypes = [C.c_void_p, _dp, _dp, C.c_double, C.c_double, _dp, _dp]
+    L.cfg_adjoint_backward.argtypes = [C.c_void_p, _dp, _dp, _dp]
+    L.cfg_adjoint_destroy.argtypes = [C.c_void_p]
     L.cfg_box_diffusion_solve_noalloc.argtypes = [C.POINTER(BoxDiffusionDesc), C.c_double,
                                                   C.c_void_p, C.c_void_p, C.c_void_p,
                                                   C.c_void_p, C.c_void_p,

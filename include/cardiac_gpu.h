@@ -312,6 +312,55 @@ int cfg_batch_stats(const cfg_batch* b, unsigned long long* rhs_evaluations,
 void* cfg_batch_stream(cfg_batch* b);
 int cfg_batch_destroy(cfg_batch* b);
 
+/* ------------------------------------------------------ adjoint step
+ *
+ * No reference counterpart: the differentiable form of the monodomain step
+ * and its adjoint, for gradients of a probe-voltage misfit
+ *   J = sum over sampled steps and probe cells of (Vm - target)^2
+ * with respect to per-cell log-scale fields of two conductances (TNNP g_Na
+ * and g_K1: g = g0 exp(theta)) and the conductivities sigma_l, sigma_t of
+ * sigma = sigma_t I + (sigma_l - sigma_t) f f (f the fibre direction).
+ * The forward runs the ionic update with a fixed number of RKF45 substeps
+ * per PDE step (no step-size control, so J is a smooth function of the
+ * parameters), implicit Euler diffusion with one PCG solve per step on an
+ * orthogonal mesh (no explicit correction), and keeps a checkpoint every
+ * checkpoint_every steps; the backward recomputes each window from its
+ * checkpoint and runs the adjoint kernels back through it.  FP64. */
+typedef struct cfg_adjoint_desc {
+    const char* ionic_model;     /* "TNNP" */
+    const char* tissue;          /* tissue key */
+    double delta_t;              /* PDE step [s] */
+    long long n_steps;
+    int substeps;                /* RKF45 substeps per PDE step (1..16) */
+    int checkpoint_every;        /* steps between checkpoints */
+    int sample_every;            /* steps between probe samples */
+    int n_probes;
+    const int* probes;           /* [n_probes] probe cells */
+    double chi, cm, vm0;
+    double fibre[3];             /* fibre direction of sigma_l */
+    int n_boxes;
+    double box_min[8][3], box_max[8][3];
+    double box_start[8], box_duration[8], box_intensity[8];
+    double pcg_tol;              /* ||r||_2 <= pcg_tol ||b||_2 for both solves */
+    int pcg_max_iter;
+} cfg_adjoint_desc;
+
+typedef struct cfg_adjoint cfg_adjoint;
+
+int cfg_adjoint_create(const cfg_adjoint_desc* desc, const cfg_mesh_desc* mesh,
+                       cfg_adjoint** out);
+/* target[n_steps / sample_every][n_probes] of the misfit */
+int cfg_adjoint_set_target(cfg_adjoint* adj, const double* target);
+/* Forward run from the model's initial states and Vm0: J and (optional)
+ * the probe trace [n_samples][n_probes]. */
+int cfg_adjoint_forward(cfg_adjoint* adj, const double* log_gna, const double* log_gk1,
+                        double sigma_l, double sigma_t, double* loss, double* probe_trace);
+/* dJ/dlog_gna [n], dJ/dlog_gk1 [n], dJ/d(sigma_l, sigma_t) [2] at the
+ * parameters of the last forward run. */
+int cfg_adjoint_backward(cfg_adjoint* adj, double* grad_log_gna, double* grad_log_gk1,
+                         double* grad_sigma);
+int cfg_adjoint_destroy(cfg_adjoint* adj);
+
 /* ------------------------------------ diffusion solve without allocation
  * No counterpart in the reference.  For callers that cannot call cudaMalloc
  * when they need a solve (a host application that owns all device memory
