@@ -244,8 +244,9 @@ def lv_arm(args, flush):
     compared after an accuracy window."""
     import torch
     from cardiacfoam_gb300 import api, lib, lv
+    ops = opcounts()["TNNP"]
     t0 = time.perf_counter()
-    dims = lv.config_sizes()
+    dims = tuple(int(v) for v in args.lv_dims.split(",")) if args.lv_dims else lv.config_sizes()
     L = lv.left_ventricle(*dims)
     t_mesh = time.perf_counter() - t0
     lo, hi = L.apex_box(2e-3)
@@ -263,8 +264,10 @@ def lv_arm(args, flush):
     for _ in range(args.warmup):
         mixed.step(LV_DT)
     mixed.set_timing(True)
+    evals0 = mixed.rhs_evaluations()
     t_mixed = timed_steps(mixed, args.lv_steps, flush, LV_DT)
     ionic_ms, diff_ms, nsteps, launches = mixed.timings()
+    evals = mixed.rhs_evaluations() - evals0
     mixed.set_timing(False)
     iters, corrs = [], []
     for _ in range(5):
@@ -280,7 +283,7 @@ def lv_arm(args, flush):
     t_fp64 = timed_steps(fp64, k64, flush, LV_DT)
     ionic64_ms, diff64_ms, _, _ = fp64.timings()
     fp64.set_timing(False)
-    window = args.lv_accuracy_steps
+    window = max(args.lv_accuracy_steps, 1 + k64)
     fp64.run(LV_DT, window - 1 - k64)
     mixed_b = make(lib.PRECISION_MIXED)
     mixed_b.run(LV_DT, window)
@@ -302,6 +305,9 @@ def lv_arm(args, flush):
                   "ionic_ms_per_step": ionic_ms / max(nsteps, 1),
                   "diffusion_ms_per_step": diff_ms / max(nsteps, 1),
                   "gpu_launches": launches,
+                  "rhs_evaluations_per_cell_step": evals / (n * args.lv_steps),
+                  "ionic_fp32_tflops": evals * (ops["flops"] + ops["transcendental"]) /
+                                       (ionic_ms / 1e3) / 1e12 if ionic_ms > 0 else None,
                   "pcg_iterations_per_step": iters, "pimple_correctors_per_step": corrs},
         "fp64": {"value": n * k64 / t_fp64, "unit": "cell-steps/s", "steps": k64,
                  "ms_per_step": t_fp64 / k64 * 1e3,
@@ -316,6 +322,113 @@ def lv_arm(args, flush):
     }
     del mixed, mixed_b, fp64
     torch.cuda.synchronize()
+    return out
+
+
+def adjoint_arm(args):
+    """The adjoint configuration: a 128 x 128 TNNP sheet (h = 0.25 mm),
+    sigma_l = sigma_t = 0.1334 S/m at the evaluation point, corner stimulus,
+    200 ms at dt 0.01 ms (5 fixed RKF45 substeps per step), per-cell log-scale
+    fields of g_Na and g_K1 from a seeded smooth Gaussian random field
+    (correlation 5 mm, std 0.2), 64 seeded probes sampled every 1 ms against a
+    target run from a second seeded field, checkpoints every 200 steps.
+
+    The mixed form's gradient is timed over the full 200 ms.  On a window of
+    `--adjoint-check-steps` steps the FP64 form gives the reference gradient
+    (mixed against it), and the FP64 gradient is checked against central
+    differences of the FP64 forward at eps = 1e-6 and 1e-8 on seeded random
+    directions."""
+    from cardiacfoam_gb300 import api, lib
+    from cardiacfoam_gb300.fields import gaussian_random_field
+    from cardiacfoam_gb300.mesh import box_mesh
+    nx = ny = 128
+    h = 2.5e-4
+    dt = 1e-5
+    mesh = box_mesh(nx, ny, 1, nx * h, ny * h, h)
+    rng = np.random.default_rng(2024)
+    probes = rng.choice(mesh.n_cells, 64, replace=False)
+    boxes = [((0.0, 0.0, 0.0), (1.5e-3, 1.5e-3, h), 0.0, 2e-3, 5e4)]
+    sig = (0.1334, 0.1334)
+
+    def fields(seed):
+        return (gaussian_random_field((ny, nx), h, 5e-3, 0.2, seed).ravel(),
+                gaussian_random_field((ny, nx), h, 5e-3, 0.2, seed + 1).ravel())
+
+    def problem(steps, precision):
+        return api.AdjointProblem(mesh, steps, dt, probes, 100, checkpoint_every=200,
+                                  substeps=5, boxes=boxes, precision=precision)
+
+    a, b = fields(1)
+    n = mesh.n_cells
+    out = {"workload": (f"TNNP epicardial sheet 128x128 (h 0.25 mm), dt 0.01 ms with 5 fixed "
+                        f"RKF45 substeps, implicit Euler diffusion, PCG to 1e-13, GRF log-scales "
+                        f"of g_Na and g_K1 (corr 5 mm, std 0.2), 64 probes every 1 ms against a "
+                        f"second seeded field, checkpoints every 200 steps"),
+           "cells": n}
+    # full run, mixed form
+    steps = args.adjoint_steps
+    pm = problem(steps, lib.PRECISION_MIXED)
+    _, target = pm.forward(*fields(7), *sig)
+    pm.set_target(target)
+    t0 = time.perf_counter()
+    J, _ = pm.forward(a, b, *sig)
+    t_f = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    gm = pm.backward()
+    t_b = time.perf_counter() - t0
+    pm.close()
+    out["mixed"] = {"steps": steps, "loss": J, "forward_seconds": t_f,
+                    "gradient_seconds": t_f + t_b,
+                    "forward_cell_steps_per_s": n * steps / t_f,
+                    "gradient_cell_steps_per_s": n * steps / (t_f + t_b)}
+    # check window: FP64 reference gradient and central differences
+    ks = args.adjoint_check_steps
+    res = {}
+    for name, prec in (("fp64", lib.PRECISION_FP64), ("mixed", lib.PRECISION_MIXED)):
+        p = problem(ks, prec)
+        _, tgt = p.forward(*fields(7), *sig)
+        p.set_target(tgt)
+        t0 = time.perf_counter()
+        Jc, _ = p.forward(a, b, *sig)
+        tf = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        g = p.backward()
+        tb = time.perf_counter() - t0
+        res[name] = (p, Jc, g, tf, tb)
+    p64, J64, g64, tf64, tb64 = res["fp64"]
+    _, Jmx, gmx, tfm, tbm = res["mixed"]
+    res["mixed"][0].close()
+    rel = lambda x, y: float(np.linalg.norm(x - y) / np.linalg.norm(y))
+    checks = []
+    r = np.random.default_rng(100)
+    for d in range(args.adjoint_fd_directions):
+        va, vb = r.standard_normal(a.size), r.standard_normal(b.size)
+        vs = r.standard_normal(2) * np.array(sig)
+        ad = float(g64[0] @ va + g64[1] @ vb + g64[2] @ vs)
+        adm = float(gmx[0] @ va + gmx[1] @ vb + gmx[2] @ vs)
+        row = {"adjoint_fp64": ad, "adjoint_mixed": adm}
+        for eps in (1e-6, 1e-8):
+            jp, _ = p64.forward(a + eps * va, b + eps * vb, sig[0] + eps * vs[0], sig[1] + eps * vs[1])
+            jm, _ = p64.forward(a - eps * va, b - eps * vb, sig[0] - eps * vs[0], sig[1] - eps * vs[1])
+            fd = (jp - jm) / (2 * eps)
+            row[f"fd_eps_{eps:g}"] = fd
+            row[f"rel_err_eps_{eps:g}"] = abs(ad - fd) / max(abs(fd), 1e-300)
+        row["mixed_vs_fp64_rel"] = abs(adm - ad) / max(abs(ad), 1e-300)
+        checks.append(row)
+    p64.close()
+    out["check_window"] = {
+        "steps": ks, "fp64_loss": J64, "mixed_loss": Jmx,
+        "fp64_gradient_seconds": tf64 + tb64, "mixed_gradient_seconds": tfm + tbm,
+        "mixed_vs_fp64_gradient_rel_l2": {"log_gna": rel(gmx[0], g64[0]),
+                                          "log_gk1": rel(gmx[1], g64[1]),
+                                          "sigma": rel(gmx[2], g64[2])},
+        "directions": checks,
+        "note": ("TNNP's h and j gate rates are piecewise in Vm with a jump at -40 mV; a "
+                 "perturbation that moves a stage evaluation across it changes J by a "
+                 "step, which a central difference divides by 2 eps.  The adjoint is the "
+                 "derivative of the smooth branches; the smaller eps makes such "
+                 "crossings unlikely."),
+    }
     return out
 
 
@@ -476,6 +589,15 @@ def main():
     ap.add_argument("--no-batch", action="store_true", help="skip the batched single cells")
     ap.add_argument("--no-mms", action="store_true", help="skip the manufactured-solution sweep")
     ap.add_argument("--no-lv", action="store_true", help="skip the left-ventricle configuration")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint configuration")
+    ap.add_argument("--adjoint-only", action="store_true")
+    ap.add_argument("--adjoint-steps", type=int, default=20000)
+    ap.add_argument("--adjoint-fd-directions", type=int, default=2)
+    ap.add_argument("--adjoint-check-steps", type=int, default=2000)
+    ap.add_argument("--lv-only", action="store_true",
+                    help="run only the left-ventricle configuration (profiling)")
+    ap.add_argument("--lv-dims", default="",
+                    help="nt,m,nr of the LV mesh (default: the 4.0 M-tet configuration)")
     ap.add_argument("--lv-steps", type=int, default=20)
     ap.add_argument("--lv-fp64-steps", type=int, default=3)
     ap.add_argument("--lv-accuracy-steps", type=int, default=250)
@@ -501,6 +623,18 @@ def main():
         out = reference_arm(args, rank, world)
         if out is not None:
             print(json.dumps(out), flush=True)
+        return
+    if args.adjoint_only:
+        from cardiacfoam_gb300 import build as gpu_build
+        gpu_build.build()
+        print(json.dumps({"adjoint": adjoint_arm(args)}), flush=True)
+        return
+    if args.lv_only:
+        import torch
+        from cardiacfoam_gb300 import build as gpu_build
+        gpu_build.build()
+        flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+        print(json.dumps({"left_ventricle": lv_arm(args, flush)}), flush=True)
         return
     r = gpu_arm(args, rank, world)
     if rank != 0:
@@ -555,6 +689,8 @@ def main():
         del flush
     if not args.no_batch:
         out["batched_single_cells"] = batch_arm(args)
+    if not args.no_adjoint:
+        out["adjoint"] = adjoint_arm(args)
     if not args.no_mms:
         out["manufactured_solution"] = mms_arm()
     if not args.no_cpu_baseline:

@@ -403,7 +403,7 @@ class AdjointProblem:
                  sample_every: int, checkpoint_every: int = 200, substeps: int = 5,
                  tissue="epicardialCells", chi=140000.0, cm=0.01, vm0=-0.084,
                  fibre=(1.0, 0.0, 0.0), boxes: Sequence = (), pcg_tol=1e-13,
-                 pcg_max_iter=10000):
+                 pcg_max_iter=10000, precision=_L.PRECISION_FP64):
         self._lib = _L.load()
         self.mesh = mesh
         self.n = mesh.n_cells
@@ -431,6 +431,7 @@ class AdjointProblem:
                 d.box_max[b][k] = hi[k]
             d.box_start[b], d.box_duration[b], d.box_intensity[b] = t0, dur, inten
         d.pcg_tol, d.pcg_max_iter = pcg_tol, pcg_max_iter
+        d.precision = precision
         md, self._keep = mesh_desc(mesh, structured=False)
         h = C.c_void_p()
         _L.check(self._lib.cfg_adjoint_create(C.byref(d), C.byref(md), C.byref(h)))

@@ -16,6 +16,7 @@ down its expression tree with the derivative rule of each operator:
     sqrt a, tanh a    g / (2 v), g (1 - v^2)
     pow(a, n)         g n a^(n-1) (and g v log a for a non-constant exponent)
     fabs a            g sign(a);  floor, heaviside, comparisons: 0
+    exp(x) - 1        evaluated as cfg_expm1(x), adjoint g (v + 1)
 
 Algebraics read before their assignment are the zeroed scratch of
 ``derivatives()`` (constant 0).  The single-cell stimulus does not exist in
@@ -37,6 +38,15 @@ from .emit import SCALABLE, SCALE_ORDER, _int_exponent, _is_half, ident
 from .model import Assign, Fatal, If, Model, use_before_def
 
 _CMP = ("==", "!=", "<", ">", "<=", ">=", "&&", "||")
+
+
+def _expm1_arg(e: Node):
+    """x of exp(x) - 1 (the GHK flux denominators), else None: evaluated as
+    cfg_expm1(x), which in FP32 does not cancel to 0 as x -> 0."""
+    if isinstance(e, Bin) and e.op == "-" and isinstance(e.r, Num) and \
+            float(e.r.text.rstrip("fF")) == 1.0 and isinstance(e.l, Call) and e.l.fn == "exp":
+        return e.l.args[0]
+    return None
 
 
 def tissue_mode_body(stmts) -> List[Assign]:
@@ -121,6 +131,13 @@ class _Gen:
         lf = self.leaf(e)
         if lf is not None:
             return lf
+        x = _expm1_arg(e)
+        if x is not None:
+            a = self.fwd(x, out, ind)
+            v = self.tmp()
+            out.append(f"{ind}{v} = cfg_expm1({a});")
+            self.value[id(e)] = v
+            return v
         if isinstance(e, Unary):
             if e.op == "!":
                 raise ValueError("logical not in an arithmetic position")
@@ -207,6 +224,10 @@ class _Gen:
                 out.append(f"{ind}{self.alg_ref[id(e)]} += {g};")
             return
         val = lambda x: self.value.get(id(x)) or self.leaf(x)
+        x = _expm1_arg(e)
+        if x is not None:
+            self.push(x, f"({g} * ({self.value[id(e)]} + R(1)))", out, ind)
+            return
         if isinstance(e, Unary):
             if e.op == "+":
                 self.acc(e.e, g, out, ind)

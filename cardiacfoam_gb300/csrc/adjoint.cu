@@ -1,4 +1,6 @@
-// Differentiable monodomain steps and their adjoint (FP64).
+// Differentiable monodomain steps and their adjoint: FP64, or with the
+// ionic right-hand side and its derivative in FP32 (mixed form; states,
+// adjoint accumulations, PCG and the conductivity derivative stay FP64).
 //
 // Forward step n -> n+1 on an orthogonal mesh (implicit Euler ddt, one
 // linear solve per step):
@@ -51,11 +53,12 @@ constexpr double vm_map_slope()
                                       : MAP == CFG_VM_IDENTITY ? 1.0 : 1000.0;
 }
 
-// constants of cell c from the [NC][n] table
+// constants of cell c from the [NC][n] table, read as R
+template <class R>
 struct ColView {
     const double* c;
     long long n, cell;
-    CFG_D __forceinline__ double operator()(int i) const { return c[(long long)i * n + cell]; }
+    CFG_D __forceinline__ R operator()(int i) const { return R(c[(long long)i * n + cell]); }
 };
 
 struct IonicArgs {
@@ -74,108 +77,137 @@ struct IonicArgs {
     double* pbar;               // [6][n] += adjoint of the scalable conductances
 };
 
-// The six stages of one RKF45 substep from y: k[s] = f(Y_s).
-__device__ __forceinline__ void stages(double t, double h, const double* y, const ColView& K,
-                                       int tissue, double (*k)[NS], double (*Y)[NS])
+// RKF45 tableau as arrays
+struct Tableau {
+    double a[6][5], b[6], c[6];
+};
+__device__ __forceinline__ Tableau tableau()
 {
     using namespace rkf;
+    return Tableau{{{0, 0, 0, 0, 0},
+                    {a21, 0, 0, 0, 0},
+                    {a31, a32, 0, 0, 0},
+                    {a41, a42, a43, 0, 0},
+                    {a51, a52, a53, a54, 0},
+                    {a61, a62, a63, a64, a65}},
+                   {b1, 0.0, b3, b4, b5, b6},
+                   {0.0, c2, c3, c4, c5, c6}};
+}
+
+// The six stages of one RKF45 substep from the (double) state y: stage
+// inputs Y_s = y + h sum_j a_sj k_j accumulated in double and handed to the
+// right-hand side in R; k_s = f(Y_s) in R.
+template <class R>
+__device__ __forceinline__ void stages(double t, double h, const double* y,
+                                       const ColView<R>& K, int tissue, R (*k)[NS],
+                                       R (*Y)[NS])
+{
+    const Tableau T = tableau();
     const CfgStimulus none{};
-    const double a[6][5] = {{0, 0, 0, 0, 0},
-                            {a21, 0, 0, 0, 0},
-                            {a31, a32, 0, 0, 0},
-                            {a41, a42, a43, 0, 0},
-                            {a51, a52, a53, a54, 0},
-                            {a61, a62, a63, a64, a65}};
-    const double c[6] = {0.0, c2, c3, c4, c5, c6};
     for (int s = 0; s < 6; ++s) {
         for (int i = 0; i < NS; ++i) {
             double acc = 0.0;
-            for (int j = 0; j < s; ++j) acc += a[s][j] * k[j][i];
-            Y[s][i] = y[i] + h * acc;
-            k[s][i] = 0.0;            // RATES of V stay zero in tissue mode
+            for (int j = 0; j < s; ++j) acc += T.a[s][j] * double(k[j][i]);
+            Y[s][i] = R(y[i] + h * acc);
+            k[s][i] = R(0);           // RATES of V stay zero in tissue mode
         }
-        M::rates<double, false>(t + c[s] * h, ArrayView<double>{Y[s]}, K, k[s], tissue, none);
+        M::rates<R, false>(t + T.c[s] * h, ArrayView<R>{Y[s]}, K, k[s], tissue, none);
     }
 }
 
-__device__ __forceinline__ void substep(double h, double* y, const double (*k)[NS])
+// y += h sum_s b_s k_s, in double
+template <class R>
+__device__ __forceinline__ void substep(double h, double* y, const R (*k)[NS])
 {
-    using namespace rkf;
-    for (int i = 0; i < NS; ++i)
-        y[i] += h * (b1 * k[0][i] + b3 * k[2][i] + b4 * k[3][i] + b5 * k[4][i] + b6 * k[5][i]);
+    const Tableau T = tableau();
+    for (int i = 0; i < NS; ++i) {
+        double acc = 0.0;
+        for (int s = 0; s < 6; ++s) acc += T.b[s] * double(k[s][i]);
+        y[i] += h * acc;
+    }
 }
 
+// Forward ionic update of one PDE step with fixed substeps.  R = double is
+// the FP64 form; R = float evaluates the right-hand side in FP32 and keeps
+// the states and their accumulation in FP64.
+template <class R>
 __global__ void __launch_bounds__(kBlock) k_ionic_forward(IonicArgs a)
 {
     const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= a.n) return;
-    const ColView K{a.consts, a.n, c};
+    const ColView<R> K{a.consts, a.n, c};
     double y[NS];
     for (int i = 0; i < NS; ++i) y[i] = a.y[(long long)i * a.n + c];
     y[0] = vm_to_state0<M::VM_MAP>(a.vm[c]);
-    double k[6][NS], Y[6][NS];
+    R k[6][NS], Y[6][NS];
     const double h = a.dtm / a.substeps;
     for (int j = 0; j < a.substeps; ++j) {
-        stages(a.t0 + j * h, h, y, K, a.tissue, k, Y);
-        substep(h, y, k);
+        stages<R>(a.t0 + j * h, h, y, K, a.tissue, k, Y);
+        substep<R>(h, y, k);
     }
-    double d[NS] = {};
+    R yr[NS], d[NS];
+    for (int i = 0; i < NS; ++i) {
+        yr[i] = R(y[i]);
+        d[i] = R(0);
+    }
     const CfgStimulus none{};
-    const double iion = M::rates<double, false>(a.t0 + a.dtm, ArrayView<double>{y}, K, d,
-                                                a.tissue, none);
-    a.im[c] = iion * M::IION_SCALE;
+    const R iion = M::rates<R, false>(a.t0 + a.dtm, ArrayView<R>{yr}, K, d, a.tissue, none);
+    a.im[c] = double(iion) * M::IION_SCALE;
     for (int i = 0; i < NS; ++i) a.y[(long long)i * a.n + c] = y[i];
 }
 
+// Reverse of one PDE step of the ionic update (the same arithmetic as the
+// forward recomputed, then the stages backwards through rhs_vjp<R>); the
+// adjoints accumulate in double.
+template <class R>
 __global__ void __launch_bounds__(kBlock) k_ionic_reverse(IonicArgs a)
 {
-    using namespace rkf;
     const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= a.n) return;
-    const ColView K{a.consts, a.n, c};
+    const Tableau T = tableau();
+    const ColView<R> K{a.consts, a.n, c};
     const double h = a.dtm / a.substeps;
     // forward again, keeping the start of every substep
     double ys[kMaxSub + 1][NS];
     for (int i = 0; i < NS; ++i) ys[0][i] = a.y_start[(long long)i * a.n + c];
     ys[0][0] = vm_to_state0<M::VM_MAP>(a.vm[c]);
-    double k[6][NS], Y[6][NS];
+    R k[6][NS], Y[6][NS];
     for (int j = 0; j < a.substeps; ++j) {
         for (int i = 0; i < NS; ++i) ys[j + 1][i] = ys[j][i];
-        stages(a.t0 + j * h, h, ys[j], K, a.tissue, k, Y);
-        substep(h, ys[j + 1], k);
+        stages<R>(a.t0 + j * h, h, ys[j], K, a.tissue, k, Y);
+        substep<R>(h, ys[j + 1], k);
     }
     double pb[6] = {0, 0, 0, 0, 0, 0};
     double yb[NS];
     for (int i = 0; i < NS; ++i) yb[i] = a.ybar[(long long)i * a.n + c];
     yb[0] = 0.0;                      // the next step overwrites state 0 with Vm
+    R Yb[NS], dbR[NS], pbR[6], yr[NS];
+    auto vjp = [&](double t, const R* y, const R* dbar, R ibar) {
+        for (int i = 0; i < NS; ++i) Yb[i] = R(0);
+        for (int q = 0; q < 6; ++q) pbR[q] = R(0);
+        tnnp::rhs_vjp<R>(t, y, K, a.tissue, dbar, ibar, Yb, pbR);
+        for (int q = 0; q < 6; ++q) pb[q] += double(pbR[q]);
+    };
     // the current at the end of the step
-    {
-        const double zero[NS] = {};
-        tnnp::rhs_vjp<double>(a.t0 + a.dtm, ys[a.substeps], K, a.tissue, zero,
-                              a.imbar[c] * M::IION_SCALE, yb, pb);
+    for (int i = 0; i < NS; ++i) {
+        yr[i] = R(ys[a.substeps][i]);
+        dbR[i] = R(0);
     }
-    const double bw[6] = {b1, 0.0, b3, b4, b5, b6};
-    const double aw[6][5] = {{0, 0, 0, 0, 0},
-                             {a21, 0, 0, 0, 0},
-                             {a31, a32, 0, 0, 0},
-                             {a41, a42, a43, 0, 0},
-                             {a51, a52, a53, a54, 0},
-                             {a61, a62, a63, a64, a65}};
-    const double cs[6] = {0.0, c2, c3, c4, c5, c6};
-    double kb[6][NS], Yb[NS];
+    vjp(a.t0 + a.dtm, yr, dbR, R(a.imbar[c] * M::IION_SCALE));
+    for (int i = 0; i < NS; ++i) yb[i] += double(Yb[i]);
+    double kb[6][NS];
     for (int j = a.substeps - 1; j >= 0; --j) {
-        stages(a.t0 + j * h, h, ys[j], K, a.tissue, k, Y);
+        stages<R>(a.t0 + j * h, h, ys[j], K, a.tissue, k, Y);
         for (int s = 0; s < 6; ++s)
-            for (int i = 0; i < NS; ++i) kb[s][i] = h * bw[s] * yb[i];
+            for (int i = 0; i < NS; ++i) kb[s][i] = h * T.b[s] * yb[i];
         // yb stays as the adjoint of the substep's start (identity part)
         for (int s = 5; s >= 0; --s) {
-            for (int i = 0; i < NS; ++i) Yb[i] = 0.0;
-            kb[s][0] = 0.0;               // RATES of V are not part of the map
-            tnnp::rhs_vjp<double>(a.t0 + j * h + cs[s] * h, Y[s], K, a.tissue, kb[s], 0.0, Yb,
-                                  pb);
-            for (int i = 0; i < NS; ++i) yb[i] += Yb[i];
+            for (int i = 0; i < NS; ++i) dbR[i] = R(kb[s][i]);
+            dbR[0] = R(0);                // RATES of V are not part of the map
+            vjp(a.t0 + j * h + T.c[s] * h, Y[s], dbR, R(0));
+            for (int i = 0; i < NS; ++i) yb[i] += double(Yb[i]);
             for (int l = 0; l < s; ++l)
-                for (int i = 0; i < NS; ++i) kb[l][i] += h * aw[s][l] * Yb[i];
+                for (int i = 0; i < NS; ++i) kb[l][i] += h * T.a[s][l] * double(Yb[i]);
         }
     }
     a.vbar[c] += yb[0] * vm_map_slope<M::VM_MAP>();
@@ -445,6 +477,7 @@ struct cfg_adjoint {
     double box_start[8], box_end[8], box_intensity[8];
     double sigma[2] = {0, 0};
     int pcg_blocks = 0;
+    bool fp32 = false;          // FP32 right-hand side and its derivative (mixed form)
     cudaStream_t stream = nullptr;
     // device
     int* d_col = nullptr;
@@ -563,7 +596,10 @@ int forward_step(cfg_adjoint* a, long long step)
     cudaStream_t s = a->stream;
     const size_t bytes = sizeof(double) * size_t(a->n);
     CFG_CUDA_TRY(cudaMemcpyAsync(a->d_vm_old, a->d_vm, bytes, cudaMemcpyDeviceToDevice, s));
-    k_ionic_forward<<<grid_of(a->n, kBlock), kBlock, 0, s>>>(ionic_args(a, step));
+    if (a->fp32)
+        k_ionic_forward<float><<<grid_of(a->n, kBlock), kBlock, 0, s>>>(ionic_args(a, step));
+    else
+        k_ionic_forward<double><<<grid_of(a->n, kBlock), kBlock, 0, s>>>(ionic_args(a, step));
     k_rhs<<<grid_of(a->n, kBlock), kBlock, 0, s>>>(step_args(a, step));
     CFG_CUDA_TRY(cudaGetLastError());
     return solve(a, a->d_b, a->d_vm);     // the previous Vm is the initial guess
@@ -667,6 +703,7 @@ int cfg_adjoint_create(const cfg_adjoint_desc* d, const cfg_mesh_desc* m, cfg_ad
     a->chicm = d->chi * d->cm;
     a->vm0 = d->vm0;
     a->pcg_tol = d->pcg_tol > 0 ? d->pcg_tol : 1e-13;
+    a->fp32 = d->precision == CFG_PRECISION_MIXED;
     a->pcg_max_iter = d->pcg_max_iter > 0 ? d->pcg_max_iter : 10000;
     a->n_boxes = d->n_boxes;
     for (int q = 0; q < d->n_boxes; ++q) {
@@ -890,7 +927,8 @@ int cfg_adjoint_backward(cfg_adjoint* a, double* grad_log_gna, double* grad_log_
             ia.imbar = a->d_imbar;
             ia.vbar = a->d_vbar;
             ia.pbar = a->d_pbar;
-            k_ionic_reverse<<<g, kBlock, 0, s>>>(ia);
+            if (a->fp32) k_ionic_reverse<float><<<g, kBlock, 0, s>>>(ia);
+            else k_ionic_reverse<double><<<g, kBlock, 0, s>>>(ia);
             CFG_CUDA_TRY(cudaGetLastError());
         }
         if (int rc = check(a)) return rc;

@@ -118,7 +118,7 @@ class AdjointDesc(C.Structure):
                 ("box_min", (C.c_double * 3) * 8), ("box_max", (C.c_double * 3) * 8),
                 ("box_start", C.c_double * 8), ("box_duration", C.c_double * 8),
                 ("box_intensity", C.c_double * 8), ("pcg_tol", C.c_double),
-                ("pcg_max_iter", C.c_int)]
+                ("pcg_max_iter", C.c_int), ("precision", C.c_int)]
 
 
 # every symbol declared in include/cardiac_gpu.h

@@ -325,7 +325,7 @@ int cfg_batch_destroy(cfg_batch* b);
  * parameters), implicit Euler diffusion with one PCG solve per step on an
  * orthogonal mesh (no explicit correction), and keeps a checkpoint every
  * checkpoint_every steps; the backward recomputes each window from its
- * checkpoint and runs the adjoint kernels back through it.  FP64. */
+ * checkpoint and runs the adjoint kernels back through it. */
 typedef struct cfg_adjoint_desc {
     const char* ionic_model;     /* "TNNP" */
     const char* tissue;          /* tissue key */
@@ -343,6 +343,9 @@ typedef struct cfg_adjoint_desc {
     double box_start[8], box_duration[8], box_intensity[8];
     double pcg_tol;              /* ||r||_2 <= pcg_tol ||b||_2 for both solves */
     int pcg_max_iter;
+    int precision;               /* CFG_PRECISION_FP64, or _MIXED: the ionic right-hand
+                                    side and its derivative in FP32, states and
+                                    adjoint accumulations in FP64 */
 } cfg_adjoint_desc;
 
 typedef struct cfg_adjoint cfg_adjoint;

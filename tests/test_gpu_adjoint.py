@@ -5,7 +5,7 @@ the forward run, checkpoint-invariant, and through torch.autograd."""
 import numpy as np
 import pytest
 
-from cardiacfoam_gb300 import api
+from cardiacfoam_gb300 import api, lib
 from cardiacfoam_gb300.fields import gaussian_random_field
 from cardiacfoam_gb300.mesh import box_mesh
 
@@ -14,13 +14,15 @@ NX = NY = 24
 DT = 1e-5
 
 
-def _problem(n_steps=400, checkpoint_every=50, sample_every=20, seed=3):
+def _problem(n_steps=400, checkpoint_every=50, sample_every=20, seed=3,
+             precision=lib.PRECISION_FP64):
     mesh = box_mesh(NX, NY, 1, NX * H, NY * H, H)
     rng = np.random.default_rng(seed)
     probes = rng.choice(mesh.n_cells, 8, replace=False)
     boxes = [((0.0, 0.0, 0.0), (1.5e-3, 1.5e-3, H), 0.0, 2e-3, 5e4)]
     return api.AdjointProblem(mesh, n_steps, DT, probes, sample_every,
-                              checkpoint_every=checkpoint_every, substeps=5, boxes=boxes)
+                              checkpoint_every=checkpoint_every, substeps=5, boxes=boxes,
+                              precision=precision)
 
 
 def _fields(seed):
@@ -110,3 +112,29 @@ def test_torch_autograd_function(setup):
     assert np.allclose(ta.grad.numpy(), 3.0 * ga, rtol=0, atol=0)
     assert np.allclose(tb.grad.numpy(), 3.0 * gb, rtol=0, atol=0)
     assert np.allclose(ts.grad.numpy(), 3.0 * gs, rtol=0, atol=0)
+
+
+@pytest.mark.gpu
+def test_mixed_gradient_against_fp64_reference(gpu_lib, setup):
+    """The mixed form (FP32 right-hand side and derivative, FP64 states,
+    adjoint accumulation and solves) against the FP64 reference gradient."""
+    p64, a, b, (sl, st) = setup
+    _, target = p64.forward(*_fields(11), 0.15, 0.03)
+    p64.set_target(target)
+    J64, _ = p64.forward(a, b, sl, st)
+    g64 = p64.backward()
+    pm = _problem(precision=lib.PRECISION_MIXED)
+    pm.set_target(target)
+    Jm, _ = pm.forward(a, b, sl, st)
+    gm = pm.backward()
+    pm.close()
+    assert abs(Jm - J64) <= 1e-3 * J64
+    for x, y in zip(gm[:2], g64[:2]):
+        assert np.linalg.norm(x - y) <= 1e-2 * np.linalg.norm(y)
+    assert np.all(np.abs(gm[2] - g64[2]) <= 1e-2 * np.abs(g64[2]))
+    rng = np.random.default_rng(9)
+    for _ in range(4):
+        va, vb, vs = rng.standard_normal(a.size), rng.standard_normal(b.size), rng.standard_normal(2)
+        d64 = g64[0] @ va + g64[1] @ vb + g64[2] @ vs
+        dm = gm[0] @ va + gm[1] @ vb + gm[2] @ vs
+        assert abs(dm - d64) <= 1e-2 * abs(d64), (dm, d64)
