@@ -159,6 +159,8 @@ def gpu_arm(args, rank, world):
     mixed = make_model(mesh, lib.PRECISION_MIXED)
     for _ in range(args.warmup):
         mixed.step(DT)
+    tune_mixed = mixed.autotune() if not args.no_autotune else None
+    mixed.step(DT)                 # rebuilds the step graph with the chosen shape
     mixed.set_timing(True)
     evals0 = mixed.rhs_evaluations()
     if world > 1:
@@ -181,12 +183,14 @@ def gpu_arm(args, rank, world):
     fp64 = make_model(mesh, lib.PRECISION_FP64)
     for _ in range(args.warmup):
         fp64.step(DT)
+    tune_fp64 = fp64.autotune() if not args.no_autotune else None
+    fp64.step(DT)
     fp64.set_timing(True)
     t_fp64 = timed_steps(fp64, k64, flush)
     ionic64_ms, diff64_ms, _, _ = fp64.timings()
     fp64.set_timing(False)
-    window = max(args.accuracy_steps, args.warmup + k64)
-    fp64.run(DT, window - args.warmup - k64)
+    window = max(args.accuracy_steps, args.warmup + 1 + k64)
+    fp64.run(DT, window - args.warmup - 1 - k64)
     mixed_b = make_model(mesh, lib.PRECISION_MIXED)
     mixed_b.run(DT, window)
     a64, amx = fp64.activation(), mixed_b.activation()
@@ -227,7 +231,8 @@ def gpu_arm(args, rank, world):
                 launches=launches, clocks=clocks, act_err_ms=act_err_ms, act_mismatch=mismatch,
                 act_cells=int(both.sum()), vm_err=vm_err, window=window, t_e2e=t_e2e, ke2e=ke2e, achieved=achieved,
                 fp32_peak=fp32_peak, peaks=pk, peak_src=src, nnz=nnz,
-                n_active_mixed=int((act_mixed > 0).sum()))
+                n_active_mixed=int((act_mixed > 0).sum()),
+                autotune={"mixed": tune_mixed, "fp64": tune_fp64})
 
 
 LV_DT = 1e-5
@@ -263,6 +268,8 @@ def lv_arm(args, flush):
     t_setup = time.perf_counter() - t0
     for _ in range(args.warmup):
         mixed.step(LV_DT)
+    tune = mixed.autotune() if not args.no_autotune else None
+    mixed.step(LV_DT)
     mixed.set_timing(True)
     evals0 = mixed.rhs_evaluations()
     t_mixed = timed_steps(mixed, args.lv_steps, flush, LV_DT)
@@ -287,6 +294,8 @@ def lv_arm(args, flush):
     fp64.run(LV_DT, window - 1 - k64)
     mixed_b = make(lib.PRECISION_MIXED)
     mixed_b.run(LV_DT, window)
+    # (the window counts the warm-up and tuning steps of the mixed context
+    # only through mixed_b, which starts from t = 0 like fp64)
     a64, amx = fp64.activation(), mixed_b.activation()
     both = (a64 > 0) & (amx > 0)
     n = L.mesh.n_cells
@@ -299,6 +308,8 @@ def lv_arm(args, flush):
                      f"dt 1e-5 s; implicit backward ddt, Gauss linear corrected Laplacian "
                      f"(leastSquares gradient), PIMPLE residualControl 1e-6, PCG tol 1e-8"),
         "cells": n, "faces": L.mesh.n_faces, "wall_faces": L.mesh.n_boundary_faces,
+        "autotune": None if tune is None else {"block": tune[0], "cells_per_thread": tune[1],
+                                               "ionic_ms": tune[2]},
         "mesh_seconds": t_mesh, "setup_seconds": t_setup,
         "mixed": {"value": n * args.lv_steps / t_mixed, "unit": "cell-steps/s",
                   "steps": args.lv_steps, "ms_per_step": t_mixed / args.lv_steps * 1e3,
@@ -590,6 +601,8 @@ def main():
     ap.add_argument("--no-mms", action="store_true", help="skip the manufactured-solution sweep")
     ap.add_argument("--no-lv", action="store_true", help="skip the left-ventricle configuration")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint configuration")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="keep the ionic kernels' default launch shape")
     ap.add_argument("--adjoint-only", action="store_true")
     ap.add_argument("--adjoint-steps", type=int, default=20000)
     ap.add_argument("--adjoint-fd-directions", type=int, default=2)
@@ -681,6 +694,9 @@ def main():
                                     "no FP32 figure is measured"},
         "gpu_launches": r["launches"],
         "clocks": r["clocks"],
+        "autotune": {k: (None if v is None else {"block": v[0], "cells_per_thread": v[1],
+                                                 "ionic_ms": v[2]})
+                     for k, v in r["autotune"].items()},
     }
     if not args.no_lv:
         import torch

@@ -130,6 +130,16 @@ class IonicModel:
         _L.check(self._lib.cfg_ionic_rhs_evaluations(self.h, C.byref(v)))
         return v.value
 
+    def set_launch(self, block: int, cells_per_thread: int):
+        _L.check(self._lib.cfg_ionic_set_launch(self.h, block, cells_per_thread))
+
+    def autotune(self, t0: float, dt: float):
+        """(block, cells per thread, ms per step) chosen by timing."""
+        b, c, ms = C.c_int(), C.c_int(), C.c_float()
+        _L.check(self._lib.cfg_ionic_autotune(self.h, t0, dt, None, C.byref(b), C.byref(c),
+                                              C.byref(ms)))
+        return b.value, c.value, ms.value
+
     def close(self):
         if getattr(self, "h", None):
             self._lib.cfg_ionic_destroy(self.h)
@@ -297,6 +307,13 @@ class Monodomain:
 
     def set_timing(self, enable: bool = True):
         _L.check(self._lib.cfg_monodomain_set_timing(self.h, int(enable)))
+
+    def autotune(self):
+        """Pick the ionic kernel's launch shape by timing; (block, cells per
+        thread, ms per ionic step)."""
+        b, c, ms = C.c_int(), C.c_int(), C.c_float()
+        _L.check(self._lib.cfg_monodomain_autotune(self.h, C.byref(b), C.byref(c), C.byref(ms)))
+        return b.value, c.value, ms.value
 
     def timings(self):
         """(ionic ms, diffusion ms, steps, kernel launches) since set_timing."""

@@ -249,6 +249,7 @@ IonicLaunch ionic_launch_args(const cfg_ionic* ion, double t0, double dt, const 
     L.first = 0;
     L.count = ion->n;
     L.perm = ion->d_perm;
+    L.cells_per_thread = ion->cells_per_thread;
     L.t0 = t0;
     L.dt = dt;
     L.t_dev = t_dev;
@@ -282,6 +283,93 @@ cudaError_t ionic_enqueue(const cfg_ionic* ion, const IonicLaunch& L)
         if (cudaError_t e = step(G, ion->stream, ion->block)) return e;
     }
     return cudaSuccess;
+}
+
+// Time every (block, cells per thread) candidate of the step kernel on
+// scratch copies of the states (the context's states are not touched) and
+// keep the fastest.  Each slot's arithmetic does not depend on the launch
+// shape, so the choice changes the speed only.
+int ionic_autotune(cfg_ionic* ion, double t0, double dt, const double* t_dev, const double* vm_dev,
+                   int repeats, int* block_out, int* cpt_out, float* ms_out)
+{
+    const int p = ion->precision;
+    const long long n = ion->n;
+    const int nw = ion->ops->n_wide[p], nn = ion->ops->ns - nw;
+    const int max_b = ion->ops->max_block[p]();
+    std::vector<int> blocks;
+    for (int b = 32; b <= max_b; b *= 2) blocks.push_back(b);
+    const int cpts[] = {1, 2, 4};
+    double *yw = nullptr, *step = nullptr, *im = nullptr;
+    float* yn = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaStream_t s = ion->stream;
+    auto cleanup = [&]() {
+        if (yw) cudaFree(yw);
+        if (yn) cudaFree(yn);
+        if (step) cudaFree(step);
+        if (im) cudaFree(im);
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+    };
+    cudaError_t e = dmalloc(&yw, size_t(nw) * n);
+    if (!e) e = dmalloc(&yn, size_t(nn) * n);
+    if (!e) e = dmalloc(&step, size_t(n));
+    if (!e) e = dmalloc(&im, size_t(n));
+    if (!e) e = cudaEventCreate(&e0);
+    if (!e) e = cudaEventCreate(&e1);
+    if (e) {
+        cleanup();
+        return fail(CFG_ERR_CUDA, "autotune set-up failed: %s", cudaGetErrorString(e));
+    }
+    const int saved_b = ion->block, saved_c = ion->cells_per_thread;
+    float best = 1e30f;
+    int best_b = saved_b, best_c = saved_c;
+    for (int b : blocks)
+        for (int c : cpts) {
+            ion->block = b;
+            ion->cells_per_thread = c;
+            float total = 0.0f;
+            for (int r = 0; r <= repeats && !e; ++r) {
+                // the same starting states for every launch
+                e = cudaMemcpyAsync(yw, ion->d_yw, sizeof(double) * size_t(nw) * n,
+                                    cudaMemcpyDeviceToDevice, s);
+                if (!e && nn)
+                    e = cudaMemcpyAsync(yn, ion->d_yn, sizeof(float) * size_t(nn) * n,
+                                        cudaMemcpyDeviceToDevice, s);
+                if (!e) e = cudaMemcpyAsync(step, ion->d_step, sizeof(double) * n,
+                                            cudaMemcpyDeviceToDevice, s);
+                IonicLaunch L = ionic_launch_args(ion, t0, dt, t_dev, vm_dev, im);
+                L.yw = yw;
+                L.yn = yn;
+                L.step = step;
+                L.rhs_evals = nullptr;
+                L.fail_record = nullptr;
+                if (!e) e = cudaEventRecord(e0, s);
+                if (!e) e = ionic_enqueue(ion, L);
+                if (!e) e = cudaEventRecord(e1, s);
+                if (!e) e = cudaEventSynchronize(e1);
+                float ms = 0.0f;
+                if (!e) e = cudaEventElapsedTime(&ms, e0, e1);
+                if (r > 0) total += ms;        // the first launch warms up
+            }
+            if (e) break;
+            if (total < best) {
+                best = total;
+                best_b = b;
+                best_c = c;
+            }
+        }
+    ion->block = e ? saved_b : best_b;
+    ion->cells_per_thread = e ? saved_c : best_c;
+    // a failing candidate must not leave an error status behind
+    cudaMemsetAsync(ion->d_status, 0, sizeof(int), s);
+    cudaStreamSynchronize(s);
+    cleanup();
+    if (e) return fail(CFG_ERR_CUDA, "autotune failed: %s", cudaGetErrorString(e));
+    if (block_out) *block_out = best_b;
+    if (cpt_out) *cpt_out = best_c;
+    if (ms_out) *ms_out = best / float(repeats > 0 ? repeats : 1);
+    return CFG_OK;
 }
 
 // Reorder n values per row between the state slots and the cells.
@@ -488,6 +576,34 @@ int cfg_ionic_rhs_evaluations(const cfg_ionic* ion, unsigned long long* count)
                                  cudaMemcpyDeviceToHost, ion->stream));
     CFG_CUDA_TRY(cudaStreamSynchronize(ion->stream));
     return CFG_OK;
+}
+
+int cfg_ionic_set_launch(cfg_ionic* ion, int block, int cells_per_thread)
+{
+    if (!ion) return fail(CFG_ERR_INVALID, "null ionic model");
+    const int max_b = ion->ops->max_block[ion->precision]();
+    if (block < 0 || block > max_b || block % 32 != 0 || cells_per_thread < 1)
+        return fail(CFG_ERR_INVALID, "launch shape %d x %d: block must be a multiple of 32 up to %d",
+                    block, cells_per_thread, max_b);
+    ion->block = block;
+    ion->cells_per_thread = cells_per_thread;
+    return CFG_OK;
+}
+
+int cfg_ionic_autotune(cfg_ionic* ion, double t0, double dt, const double* vm_dev,
+                       int* block, int* cells_per_thread, float* ms_per_step)
+{
+    if (!ion) return fail(CFG_ERR_INVALID, "null ionic model");
+    clear_error();
+    const double* vm = vm_dev;
+    if (!ion->solve_vm && !vm) {
+        // the context's Vm staging buffer at the resting value
+        std::vector<double> v(size_t(ion->n), -0.084);
+        CFG_CUDA_TRY(cudaMemcpy(ion->d_vm, v.data(), sizeof(double) * v.size(),
+                                cudaMemcpyHostToDevice));
+        vm = ion->d_vm;
+    }
+    return ionic_autotune(ion, t0, dt, nullptr, vm, 3, block, cells_per_thread, ms_per_step);
 }
 
 int cfg_ionic_destroy(cfg_ionic* ion)

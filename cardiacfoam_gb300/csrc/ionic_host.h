@@ -36,7 +36,10 @@ struct cfg_ionic {
     int* d_perm = nullptr;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
-    int block = 128;
+    // launch shape of the step kernel (cfg_ionic_autotune): threads per
+    // block (0 = the kernel's largest) and cells per thread
+    int block = 0;
+    int cells_per_thread = 1;
 };
 
 namespace cfg {
@@ -48,4 +51,6 @@ IonicLaunch ionic_launch_args(const cfg_ionic* ion, double t0, double dt, const 
                               const double* vm_dev, double* im_dev);
 cudaError_t ionic_enqueue(const cfg_ionic* ion, const IonicLaunch& L);
 int ionic_check_status(cfg_ionic* ion);
+int ionic_autotune(cfg_ionic* ion, double t0, double dt, const double* t_dev, const double* vm_dev,
+                   int repeats, int* block, int* cells_per_thread, float* ms);
 }  // namespace cfg

@@ -28,17 +28,30 @@ using Tissues = cfg::CFG_MODEL::TissueSet;
 // The plain form runs ionic_step_kernel (one cell per thread, stage arrays
 // per thread); the mixed form runs ionic_mixed_kernel (stage data in shared
 // memory, block size fixed by the model's slice length).
+// `block` threads per block (the plain form: at most 128; the mixed form:
+// at most the model's slice block, 0 = that block) and p.cells_per_thread
+// slots per thread; every slot's arithmetic is independent of both, so the
+// results are too.
 template <bool SV, int T>
 static void launch_one(const cfg::IonicLaunch& p, cudaStream_t s, int block)
 {
+    const long long cpt = p.cells_per_thread > 0 ? p.cells_per_thread : 1;
     if constexpr (kFP64) {
-        const unsigned grid = unsigned((p.count + block - 1) / block);
-        cfg::ionic_step_kernel<M, true, SV, T><<<grid, block, 0, s>>>(p);
+        const int b = (block > 0 && block <= 128) ? block : 128;
+        const unsigned grid = unsigned((p.count + b * cpt - 1) / (b * cpt));
+        cfg::ionic_step_kernel<M, true, SV, T><<<grid, b, 0, s>>>(p);
     } else {
         using S = cfg::mixed::Slice<M>;
-        const unsigned grid = unsigned((p.count + S::block - 1) / S::block);
-        cfg::ionic_mixed_kernel<M, SV, T><<<grid, S::block, S::smem_bytes, s>>>(p);
+        const int b = (block > 0 && block <= S::block && block % 32 == 0) ? block : S::block;
+        const unsigned grid = unsigned((p.count + b * cpt - 1) / (b * cpt));
+        cfg::ionic_mixed_kernel<M, SV, T><<<grid, b, size_t(b) * S::len * 4, s>>>(p);
     }
+}
+
+extern "C" int CFG_CAT3(cfg_ionic_max_block_, CFG_MODEL, CFG_PREC_TAG)()
+{
+    if constexpr (kFP64) return 128;
+    else return cfg::mixed::Slice<M>::block;
 }
 
 // Opt the mixed kernels into their dynamic shared memory (above the 48 KB

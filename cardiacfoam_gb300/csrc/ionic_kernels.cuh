@@ -45,6 +45,7 @@ struct IonicLaunch {
     long long n;                     // cells (and the stride of the state arrays)
     long long first, count;          // state slots [first, first + count) of this launch
     const int* perm;                 // [n] cell of each state slot, or null (slot = cell)
+    int cells_per_thread;            // slots per thread (grid-stride), chosen by the launcher
     double t0, dt;                   // PDE step [s] (used when t_dev is null)
     const double* t_dev;             // device time of the step start [s], or null
     int tissue;                      // uniform tissue flag (when tissue_cell is null)
@@ -369,9 +370,10 @@ __global__ void __launch_bounds__(128, CFG_IONIC_MIN_BLOCKS) ionic_step_kernel(I
     using R = typename std::conditional<FP64, double, float>::type;
     using L = Layout<M, FP64>;
     constexpr int NS = M::NS;
-    const long long c = p.first + (long long)blockIdx.x * blockDim.x + threadIdx.x;
     unsigned evals = 0;
-    if (c < p.first + p.count) {
+    const long long end = p.first + p.count;
+    for (long long c = p.first + (long long)blockIdx.x * blockDim.x + threadIdx.x; c < end;
+         c += (long long)gridDim.x * blockDim.x) {
         const long long cell = p.perm ? p.perm[c] : c;
         const double t0 = p.t_dev ? p.t_dev[0] : p.t0;
         double ts, te, dtm;

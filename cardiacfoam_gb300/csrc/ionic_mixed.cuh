@@ -317,9 +317,10 @@ ionic_mixed_kernel(IonicLaunch p)
     float* T = Y + P;
     float* K = T + P;
     float* LO = K + 5 * P;
-    const long long c = p.first + (long long)blockIdx.x * blockDim.x + threadIdx.x;
     unsigned evals = 0;
-    if (c < p.first + p.count) {
+    const long long end = p.first + p.count;
+    for (long long c = p.first + (long long)blockIdx.x * blockDim.x + threadIdx.x; c < end;
+         c += (long long)gridDim.x * blockDim.x) {
         const long long cell = p.perm ? p.perm[c] : c;
         const double t0 = p.t_dev ? p.t_dev[0] : p.t0;
         double ts, te, dtm;

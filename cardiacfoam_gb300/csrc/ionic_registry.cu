@@ -33,7 +33,9 @@
                                                        cudaStream_t);                         \
     extern "C" cudaError_t cfg_ionic_sweep_##ns(const double*, const double*, int, int,        \
                                                 const cfg::CfgStimulus&, double, double, int,  \
-                                                double*, cudaStream_t);
+                                                double*, cudaStream_t);                       \
+    extern "C" int cfg_ionic_max_block_##ns##_fp64();                                         \
+    extern "C" int cfg_ionic_max_block_##ns##_mixed();
 
 CFG_DECLARE_MODEL(tnnp)
 CFG_DECLARE_MODEL(ord)
@@ -100,6 +102,8 @@ struct Tables {
         o.sweep_currents = NSP::SWEEP_CURRENTS;                                                  \
         o.sweep_deps = NSP::SWEEP_DEPS;                                                          \
         o.sweep = cfg_ionic_sweep_##NSP;                                                         \
+        o.max_block[0] = cfg_ionic_max_block_##NSP##_fp64;                                       \
+        o.max_block[1] = cfg_ionic_max_block_##NSP##_mixed;                                      \
         return o;                                                                               \
     }()
 

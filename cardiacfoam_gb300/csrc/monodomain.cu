@@ -582,6 +582,24 @@ int cfg_monodomain_set_graph(cfg_monodomain* md, int enable)
     return CFG_OK;
 }
 
+int cfg_monodomain_autotune(cfg_monodomain* md, int* block, int* cells_per_thread,
+                            float* ionic_ms)
+{
+    if (!md) return fail(CFG_ERR_INVALID, "null context");
+    clear_error();
+    CFG_CUDA_TRY(cudaStreamSynchronize(md->stream));
+    const double dt = md->graph_dt > 0 ? md->graph_dt : (md->prepared_dt > 0 ? md->prepared_dt : 1e-5);
+    int rc = ionic_autotune(md->ion, md->t_host, dt, nullptr, md->d_vm, 3, block,
+                            cells_per_thread, ionic_ms);
+    if (rc) return rc;
+    // the launch shape is part of the captured step graph
+    if (md->graph_exec) {
+        cudaGraphExecDestroy(md->graph_exec);
+        md->graph_exec = nullptr;
+    }
+    return CFG_OK;
+}
+
 int cfg_monodomain_set_persistent(cfg_monodomain* md, int enable)
 {
     if (!md) return fail(CFG_ERR_INVALID, "null context");

@@ -134,7 +134,8 @@ EXPORTS = [
     "cfg_monodomain_set_persistent", "cfg_batch_create", "cfg_batch_run", "cfg_batch_results",
     "cfg_batch_trace", "cfg_batch_get_states", "cfg_batch_stats", "cfg_batch_stream",
     "cfg_batch_destroy", "cfg_adjoint_create", "cfg_adjoint_set_target", "cfg_adjoint_forward",
-    "cfg_adjoint_backward", "cfg_adjoint_destroy",
+    "cfg_adjoint_backward", "cfg_adjoint_destroy", "cfg_ionic_autotune", "cfg_monodomain_autotune",
+    "cfg_ionic_set_launch",
 ]
 
 _lib = None
@@ -202,6 +203,10 @@ def load(path: Optional[os.PathLike] = None):
     L.cfg_adjoint_forward.argtypes = [C.c_void_p, _dp, _dp, C.c_double, C.c_double, _dp, _dp]
     L.cfg_adjoint_backward.argtypes = [C.c_void_p, _dp, _dp, _dp]
     L.cfg_adjoint_destroy.argtypes = [C.c_void_p]
+    L.cfg_ionic_autotune.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_void_p, _ip, _ip,
+                                     C.POINTER(C.c_float)]
+    L.cfg_monodomain_autotune.argtypes = [C.c_void_p, _ip, _ip, C.POINTER(C.c_float)]
+    L.cfg_ionic_set_launch.argtypes = [C.c_void_p, C.c_int, C.c_int]
     L.cfg_box_diffusion_solve_noalloc.argtypes = [C.POINTER(BoxDiffusionDesc), C.c_double,
                                                   C.c_void_p, C.c_void_p, C.c_void_p,
                                                   C.c_void_p, C.c_void_p,

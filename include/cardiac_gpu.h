@@ -89,6 +89,16 @@ int cfg_ionic_solve(cfg_ionic* ion, double t0, double dt, const double* vm, doub
 int cfg_ionic_solve_device(cfg_ionic* ion, double t0, double dt, const double* vm_dev,
                            double* im_dev);
 
+/* Autotuner (no reference counterpart): times every launch shape of the
+ * step kernel - threads per block (32 .. the kernel's largest) x cells per
+ * thread (1, 2, 4) - on scratch copies of the states with the given Vm
+ * (device pointer; NULL = resting Vm) and keeps the fastest for this
+ * context.  The results of a step do not depend on the launch shape. */
+int cfg_ionic_autotune(cfg_ionic* ion, double t0, double dt, const double* vm_dev,
+                       int* block, int* cells_per_thread, float* ms_per_step);
+/* The same launch shape set directly (block 0 = the kernel's largest). */
+int cfg_ionic_set_launch(cfg_ionic* ion, int block, int cells_per_thread);
+
 /* Number of states and their names (ioNumStates/ioStateNames,
  * ionicModel.H:115-168). */
 int cfg_ionic_num_states(const cfg_ionic* ion, int* n_states);
@@ -216,6 +226,13 @@ int cfg_monodomain_create_from_dict(const char* electro_properties, const cfg_me
  * ionic solveODE, implicit (PIMPLE + PCG) or explicit diffusion, activation
  * time. */
 int cfg_monodomain_step(cfg_monodomain* md, double dt);
+
+/* The autotuner on the context's ionic model with its current Vm and
+ * time (see cfg_ionic_autotune); the step graph is rebuilt at the next step.
+ * The ELL width of the operator is the mesh's longest row (exact: tets 4,
+ * hexahedra 6), so there is nothing to choose there. */
+int cfg_monodomain_autotune(cfg_monodomain* md, int* block, int* cells_per_thread,
+                            float* ionic_ms);
 
 /* n_steps steps replayed from the step's CUDA graph, whose PIMPLE and PCG
  * loops are conditional nodes driven by device-side solver state: no host
