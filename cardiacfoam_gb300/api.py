@@ -130,6 +130,19 @@ class IonicModel:
         _L.check(self._lib.cfg_ionic_rhs_evaluations(self.h, C.byref(v)))
         return v.value
 
+    def trace_header(self, columns: Optional[str] = None) -> str:
+        buf = C.create_string_buffer(1 << 16)
+        _L.check(self._lib.cfg_ionic_trace_header(self.h, columns.encode() if columns else None,
+                                                  buf, len(buf)))
+        return buf.value.decode()
+
+    def trace_row(self, cell: int, t: float, columns: Optional[str] = None) -> str:
+        buf = C.create_string_buffer(1 << 16)
+        _L.check(self._lib.cfg_ionic_trace_row(self.h, cell, t,
+                                               columns.encode() if columns else None, buf,
+                                               len(buf)))
+        return buf.value.decode()
+
     def set_launch(self, block: int, cells_per_thread: int):
         _L.check(self._lib.cfg_ionic_set_launch(self.h, block, cells_per_thread))
 
@@ -307,6 +320,12 @@ class Monodomain:
 
     def set_timing(self, enable: bool = True):
         _L.check(self._lib.cfg_monodomain_set_timing(self.h, int(enable)))
+
+    def write(self, case_dir, patches=(("walls", "zeroGradient"),), precision=6):
+        """Vm and activationTime as OpenFOAM ASCII volScalarFields in
+        <case_dir>/<timeName>/."""
+        from .io import write_monodomain_fields
+        return write_monodomain_fields(self, case_dir, patches, precision)
 
     def autotune(self):
         """Pick the ionic kernel's launch shape by timing; (block, cells per

@@ -686,6 +686,126 @@ std::vector<std::string> split_commas(const char* s)
     return out;
 }
 
+// The states (FP64; the mixed form's pairs summed), constants and tissue of
+// integration point `cell`.
+int cell_snapshot(cfg_ionic* ion, long long cell, std::vector<double>& y0, std::vector<double>& C,
+                  int* tissue_out)
+{
+    const IonicModelOps* m = ion->ops;
+    const long long n = ion->n;
+    long long k0 = cell;
+    if (!ion->h_perm.empty())
+        for (size_t k = 0; k < ion->h_perm.size(); ++k)
+            if (ion->h_perm[k] == cell) { k0 = (long long)k; break; }
+    const int p = ion->precision, ns = m->ns;
+    y0.assign(size_t(ns), 0.0);
+    for (int i = 0; i < ns; ++i) {
+        const int w = m->wide_of[p * ns + i], s = m->slot_of[p * ns + i];
+        if (w) {
+            double v = 0.0;
+            CFG_CUDA_TRY(cudaMemcpy(&v, ion->d_yw + size_t(s) * n + k0, sizeof v,
+                                    cudaMemcpyDeviceToHost));
+            if (p == CFG_PRECISION_MIXED) {
+                float hl[2];
+                std::memcpy(hl, &v, sizeof hl);
+                v = double(hl[0]) + double(hl[1]);
+            }
+            y0[size_t(i)] = v;
+        } else {
+            float v = 0.0f;
+            CFG_CUDA_TRY(cudaMemcpy(&v, ion->d_yn + size_t(s) * n + k0, sizeof v,
+                                    cudaMemcpyDeviceToHost));
+            y0[size_t(i)] = v;
+        }
+    }
+    int tissue = ion->tissue;
+    if (ion->d_tissue) {
+        unsigned char t = 0;
+        CFG_CUDA_TRY(cudaMemcpy(&t, ion->d_tissue + k0, 1, cudaMemcpyDeviceToHost));
+        tissue = t;
+    }
+    double sc[6];
+    const double* scp = nullptr;
+    if (ion->d_scales) {
+        for (int j = 0; j < 6; ++j)
+            CFG_CUDA_TRY(cudaMemcpy(&sc[j], ion->d_scales + size_t(j) * n + k0, sizeof(double),
+                                    cudaMemcpyDeviceToHost));
+        scp = sc;
+    }
+    C.assign(size_t(m->nc), 0.0);
+    std::vector<double> yinit(size_t(ns), 0.0);
+    m->host_init(C.data(), yinit.data(), tissue, scp);
+    *tissue_out = tissue;
+    return CFG_OK;
+}
+
+// [states | algebraic | rates] of one cell at model time t (clamp = 0) or of
+// a clamped-voltage sweep (clamp = 1, n_points rows).
+int evaluate_rows(cfg_ionic* ion, const std::vector<double>& y0, const std::vector<double>& C,
+                  int tissue, double vmin, double vmax, int n_points, double t, int clamp,
+                  std::vector<double>& rows)
+{
+    const IonicModelOps* m = ion->ops;
+    const int width = 2 * m->ns + m->na;
+    double *d_y = nullptr, *d_c = nullptr, *d_out = nullptr;
+    cudaError_t e = dmalloc(&d_y, y0.size());
+    if (!e) e = dmalloc(&d_c, C.size());
+    if (!e) e = dmalloc(&d_out, size_t(n_points) * width);
+    if (!e) e = cudaMemcpy(d_y, y0.data(), sizeof(double) * y0.size(), cudaMemcpyHostToDevice);
+    if (!e) e = cudaMemcpy(d_c, C.data(), sizeof(double) * C.size(), cudaMemcpyHostToDevice);
+    if (!e) e = m->sweep(d_y, d_c, tissue, ion->solve_vm ? 1 : 0, ion->stim, vmin, vmax, n_points,
+                         t, clamp, d_out, ion->stream);
+    rows.assign(size_t(n_points) * width, 0.0);
+    if (!e) e = cudaMemcpyAsync(rows.data(), d_out, sizeof(double) * rows.size(),
+                                cudaMemcpyDeviceToHost, ion->stream);
+    if (!e) e = cudaStreamSynchronize(ion->stream);
+    dfree(d_y);
+    dfree(d_c);
+    dfree(d_out);
+    if (e) return fail(CFG_ERR_CUDA, "variable evaluation failed: %s", cudaGetErrorString(e));
+    return CFG_OK;
+}
+
+// ionicModelIO's write plan: Vm (transformed state 0), the other states,
+// the algebraics, RATES_<state> (fullPlan, ionicModelIO.C:169-232), or the
+// requested names that resolve (exportedFieldNamesRef: unknown names are
+// ignored).  Column -1 is Vm.
+std::vector<std::pair<std::string, int>> trace_plan(const IonicModelOps* m, const char* columns)
+{
+    std::vector<std::pair<std::string, int>> plan;
+    if (!columns || !*columns) {
+        plan.push_back({"Vm", -1});
+        for (int s = 1; s < m->ns; ++s) plan.push_back({m->state_strings[s], s});
+        for (int a = 0; a < m->na; ++a) plan.push_back({m->alg_strings[a], m->ns + a});
+        for (int s = 0; s < m->ns; ++s)
+            plan.push_back({std::string("RATES_") + m->state_strings[s], m->ns + m->na + s});
+        return plan;
+    }
+    std::string cur;
+    auto flush = [&]() {
+        if (cur.empty()) return;
+        int col = 0;
+        if (cur == "Vm" || canonical_name(cur.c_str()) == "vm") plan.push_back({cur, -1});
+        else if (resolve_column(m, cur, &col)) plan.push_back({cur, col});
+        cur.clear();
+    };
+    for (const char* p = columns; *p; ++p) {
+        if (*p == ' ' || *p == ',' || *p == '\t' || *p == '(' || *p == ')') flush();
+        else cur.push_back(*p);
+    }
+    flush();
+    return plan;
+}
+
+// getter of the transformed membrane potential (AlievPanfilov.H:78-81,
+// BuenoOrovio.H:78-81; otherwise state 0)
+double transformed_vm(int vm_map, double s0)
+{
+    if (vm_map == CFG_VM_ALIEV) return s0 * 100 - 80;
+    if (vm_map == CFG_VM_BUENO) return s0 * 85.7 - 84.0;
+    return s0;
+}
+
 }  // namespace
 }  // namespace cfg
 
@@ -736,68 +856,56 @@ int cfg_ionic_sweep_current(cfg_ionic* ion, const char* current, double v_min, d
     if (n_points < 2) return fail(CFG_ERR_INVALID, "a sweep needs at least 2 points");
 
     // states of integration point 0 and the model's constants
-    const long long n = ion->n;
-    const long long k0 = slot_of_cell0(ion);
-    const int p = ion->precision, ns = m->ns;
-    std::vector<double> y0(static_cast<size_t>(ns));
-    for (int i = 0; i < ns; ++i) {
-        const int w = m->wide_of[p * ns + i], s = m->slot_of[p * ns + i];
-        if (w) {
-            double v = 0.0;
-            CFG_CUDA_TRY(cudaMemcpy(&v, ion->d_yw + size_t(s) * n + k0, sizeof v,
-                                    cudaMemcpyDeviceToHost));
-            if (p == CFG_PRECISION_MIXED) {
-                float hl[2];
-                std::memcpy(hl, &v, sizeof hl);
-                v = double(hl[0]) + double(hl[1]);
-            }
-            y0[size_t(i)] = v;
-        } else {
-            float v = 0.0f;
-            CFG_CUDA_TRY(cudaMemcpy(&v, ion->d_yn + size_t(s) * n + k0, sizeof v,
-                                    cudaMemcpyDeviceToHost));
-            y0[size_t(i)] = v;
-        }
-    }
-    int tissue = ion->tissue;
-    if (ion->d_tissue) {
-        unsigned char t = 0;
-        CFG_CUDA_TRY(cudaMemcpy(&t, ion->d_tissue + k0, 1, cudaMemcpyDeviceToHost));
-        tissue = t;
-    }
-    double sc[6];
-    const double* scp = nullptr;
-    if (ion->d_scales) {
-        for (int j = 0; j < 6; ++j)
-            CFG_CUDA_TRY(cudaMemcpy(&sc[j], ion->d_scales + size_t(j) * n, sizeof(double),
-                                    cudaMemcpyDeviceToHost));
-        scp = sc;
-    }
-    std::vector<double> C(static_cast<size_t>(m->nc), 0.0), yinit(static_cast<size_t>(ns), 0.0);
-    m->host_init(C.data(), yinit.data(), tissue, scp);
-    const int width = 2 * ns + m->na;
-    double *d_y = nullptr, *d_c = nullptr, *d_out = nullptr;
-    cudaError_t e = dmalloc(&d_y, size_t(ns));
-    if (!e) e = dmalloc(&d_c, size_t(m->nc));
-    if (!e) e = dmalloc(&d_out, size_t(n_points) * width);
-    if (!e) e = cudaMemcpy(d_y, y0.data(), sizeof(double) * ns, cudaMemcpyHostToDevice);
-    if (!e) e = cudaMemcpy(d_c, C.data(), sizeof(double) * m->nc, cudaMemcpyHostToDevice);
-    if (!e) e = m->sweep(d_y, d_c, tissue, ion->solve_vm ? 1 : 0, ion->stim, v_min, v_max,
-                         n_points, d_out, ion->stream);
-    std::vector<double> rows(size_t(n_points) * width);
-    if (!e) e = cudaMemcpyAsync(rows.data(), d_out, sizeof(double) * rows.size(),
-                                cudaMemcpyDeviceToHost, ion->stream);
-    if (!e) e = cudaStreamSynchronize(ion->stream);
-    dfree(d_y);
-    dfree(d_c);
-    dfree(d_out);
-    if (e) return fail(CFG_ERR_CUDA, "sweep failed: %s", cudaGetErrorString(e));
+    std::vector<double> y0, C, rows;
+    int tissue = 0;
+    if (int rc = cell_snapshot(ion, 0, y0, C, &tissue)) return rc;
+    if (int rc = evaluate_rows(ion, y0, C, tissue, v_min, v_max, n_points, 0.0, 1, rows)) return rc;
+    const int width = 2 * m->ns + m->na;
     for (int i = 0; i < n_points; ++i) {
         const double* row = &rows[size_t(i) * width];
         double* o = out + size_t(i) * nc;
         o[0] = row[0];
         for (size_t k = 0; k < cols.size(); ++k) o[1 + k] = row[cols[k]];
     }
+    return CFG_OK;
+}
+
+int cfg_ionic_trace_header(const cfg_ionic* ion, const char* columns, char* buf, size_t len)
+{
+    if (!ion || !buf || !len) return fail(CFG_ERR_INVALID, "null argument");
+    std::string h = "time";
+    for (const auto& c : trace_plan(ion->ops, columns)) h += " " + c.first;
+    h += "\n";
+    if (h.size() + 1 > len) return fail(CFG_ERR_INVALID, "trace header needs %zu bytes", h.size() + 1);
+    std::memcpy(buf, h.c_str(), h.size() + 1);
+    return CFG_OK;
+}
+
+int cfg_ionic_trace_row(cfg_ionic* ion, long long cell, double t, const char* columns, char* buf,
+                        size_t len)
+{
+    if (!ion || !buf || !len) return fail(CFG_ERR_INVALID, "null argument");
+    if (cell < 0 || cell >= ion->n) return fail(CFG_ERR_INVALID, "cell %lld outside the model", cell);
+    const IonicModelOps* m = ion->ops;
+    std::vector<double> y0, C, rows;
+    int tissue = 0;
+    if (int rc = cell_snapshot(ion, cell, y0, C, &tissue)) return rc;
+    // the variables of the last solveODE: computeVariables at tEnd, model time
+    const double tm = m->time_scale == 1000.0 ? t : t * 1000.0 / m->time_scale;
+    if (int rc = evaluate_rows(ion, y0, C, tissue, 0.0, 0.0, 1, tm, 0, rows)) return rc;
+    // OFstream with std::ios::fixed and precision 7 (singleCellSolver.C:117-118)
+    std::string r;
+    char tmp[64];
+    std::snprintf(tmp, sizeof tmp, "%.7f", t);
+    r += tmp;
+    for (const auto& c : trace_plan(m, columns)) {
+        const double v = c.second < 0 ? transformed_vm(m->vm_map, rows[0]) : rows[size_t(c.second)];
+        std::snprintf(tmp, sizeof tmp, " %.7f", v);
+        r += tmp;
+    }
+    r += "\n";
+    if (r.size() + 1 > len) return fail(CFG_ERR_INVALID, "trace row needs %zu bytes", r.size() + 1);
+    std::memcpy(buf, r.c_str(), r.size() + 1);
     return CFG_OK;
 }
 

@@ -219,21 +219,25 @@ extern "C" cudaError_t CFG_CAT3(cfg_batch_step_, CFG_MODEL, CFG_PREC_TAG)(
 // state 0 clamped to V = vmin + (vmax - vmin) i / (npts - 1), the first
 // variables function at VOI = 0, one thread per voltage.  Row i of `out` is
 // [states | algebraic | rates] (2 NS + NA doubles).
+// With clamp = 0 the states are taken as they are (one row: the variables
+// of a cell at model time t, as a trace row of ionicModelIO::write holds).
 template <bool SV>
 __global__ void sweep_kernel(const double* y0, const double* C, int tissue, cfg::CfgStimulus stim,
-                             double vmin, double vmax, int npts, double* out)
+                             double vmin, double vmax, int npts, double t, int clamp, double* out)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= npts) return;
     constexpr int NS = M::NS, NA = M::NA;
     double y[NS];
     for (int k = 0; k < NS; ++k) y[k] = y0[k];
-    const double denom = double(npts - 1);
-    y[0] = vmin + (vmax - vmin) * double(i) / denom;
+    if (clamp) {
+        const double denom = double(npts - 1);
+        y[0] = vmin + (vmax - vmin) * double(i) / denom;
+    }
     double A[NA > 0 ? NA : 1] = {};
     double R[NS] = {};
     const cfg::ConstView<double> K{C};
-    M::template all_variables<double, SV>(0.0, cfg::ArrayView<double>{y}, K, A, R, tissue, stim);
+    M::template all_variables<double, SV>(t, cfg::ArrayView<double>{y}, K, A, R, tissue, stim);
     double* row = out + (long long)i * (2 * NS + NA);
     for (int k = 0; k < NS; ++k) row[k] = y[k];
     for (int k = 0; k < NA; ++k) row[NS + k] = A[k];
@@ -242,13 +246,17 @@ __global__ void sweep_kernel(const double* y0, const double* C, int tissue, cfg:
 
 extern "C" cudaError_t CFG_CAT3(cfg_ionic_sweep_, CFG_MODEL, )(
     const double* y0, const double* C, int tissue, int solve_vm, const cfg::CfgStimulus& stim,
-    double vmin, double vmax, int npts, double* out, cudaStream_t s)
+    double vmin, double vmax, int npts, double t, int clamp, double* out, cudaStream_t s)
 {
     if (npts <= 0) return cudaSuccess;
     const int block = 64;
     const unsigned grid = unsigned((npts + block - 1) / block);
-    if (solve_vm) sweep_kernel<true><<<grid, block, 0, s>>>(y0, C, tissue, stim, vmin, vmax, npts, out);
-    else sweep_kernel<false><<<grid, block, 0, s>>>(y0, C, tissue, stim, vmin, vmax, npts, out);
+    if (solve_vm)
+        sweep_kernel<true><<<grid, block, 0, s>>>(y0, C, tissue, stim, vmin, vmax, npts, t, clamp,
+                                                  out);
+    else
+        sweep_kernel<false><<<grid, block, 0, s>>>(y0, C, tissue, stim, vmin, vmax, npts, t, clamp,
+                                                   out);
     return cudaGetLastError();
 }
 #endif

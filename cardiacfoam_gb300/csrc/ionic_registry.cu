@@ -33,7 +33,7 @@
                                                        cudaStream_t);                         \
     extern "C" cudaError_t cfg_ionic_sweep_##ns(const double*, const double*, int, int,        \
                                                 const cfg::CfgStimulus&, double, double, int,  \
-                                                double*, cudaStream_t);                       \
+                                                double, int, double*, cudaStream_t);          \
     extern "C" int cfg_ionic_max_block_##ns##_fp64();                                         \
     extern "C" int cfg_ionic_max_block_##ns##_mixed();
 

@@ -44,7 +44,7 @@ struct IonicModelOps {
     const char* const* sweep_deps;
     cudaError_t (*sweep)(const double* y0, const double* C, int tissue, int solve_vm,
                          const CfgStimulus& stim, double vmin, double vmax, int npts,
-                         double* out, cudaStream_t);
+                         double t, int clamp, double* out, cudaStream_t);
     int (*max_block[2])();       // largest block the step kernel takes, per precision
 };
 

@@ -1,0 +1,115 @@
+"""Output in the reference's formats.
+
+* OpenFOAM ASCII ``volScalarField`` files of the myocardium fields at write
+  times (what ``runTime.write()`` produces for ``Vm`` and ``activationTime``
+  in ``MyocardiumDomain``: ``<case>/<timeName>/<field>``), so a GPU run can be
+  diffed against an OpenFOAM case or read by its post-processing.
+* The single-cell trace of ``SingleCellSolver`` (``ionicModelIO::write``):
+  ``postProcessing/<model>_<tissue>_<protocol>.txt`` with a ``time <names>``
+  header and fixed 7-decimal rows; the rows are formatted by the library
+  (``cfg_ionic_trace_row``).
+"""
+from __future__ import annotations
+
+import os
+from pathlib import Path
+from typing import Iterable, Optional, Sequence, Tuple
+
+import numpy as np
+
+DIM_VM = "[1 2 -3 0 0 -1 0]"          # V = kg m^2 s^-3 A^-1
+DIM_TIME = "[0 0 1 0 0 0 0]"
+
+
+def time_name(t: float, precision: int = 6) -> str:
+    """Time::timeName: the value in general format with `precision`
+    significant digits (controlDict timePrecision, default 6)."""
+    return f"{t:.{precision}g}"
+
+
+def _scalar(v: float, precision: int) -> str:
+    return f"{v:.{precision}g}"
+
+
+def write_vol_scalar_field(path, name: str, values: np.ndarray, dimensions: str,
+                           location: str, patches: Sequence[Tuple[str, str]] = (("walls",
+                                                                                  "zeroGradient"),),
+                           precision: int = 6):
+    """One ASCII volScalarField file (uniform when every value is equal);
+    each patch gets `type <t>;` (zeroGradient for the myocardium fields,
+    myocardiumDomain.C:207)."""
+    v = np.asarray(values, dtype=np.float64).ravel()
+    L = ["/*--------------------------------*- C++ -*----------------------------------*\\",
+         "  written by cardiacfoam_gb300",
+         "\\*---------------------------------------------------------------------------*/",
+         "FoamFile", "{", "    version     2.0;", "    format      ascii;",
+         "    class       volScalarField;", f'    location    "{location}";',
+         f"    object      {name};", "}",
+         "// * * * * * * * * * * * * * * * * * * * * * * * * * * * * * * * * * * * * * //",
+         "", f"dimensions      {dimensions};", ""]
+    if v.size and np.all(v == v[0]):
+        L.append(f"internalField   uniform {_scalar(v[0], precision)};")
+    else:
+        L.append("internalField   nonuniform List<scalar> ")
+        L.append(str(v.size))
+        L.append("(")
+        L.extend(_scalar(x, precision) for x in v)
+        L.append(")")
+        L.append(";")
+    L += ["", "boundaryField", "{"]
+    for pname, ptype in patches:
+        L += [f"    {pname}", "    {", f"        type            {ptype};", "    }"]
+    L += ["}", "", "", "// " + "*" * 73 + " //", ""]
+    Path(path).parent.mkdir(parents=True, exist_ok=True)
+    Path(path).write_text("\n".join(L))
+
+
+def write_monodomain_fields(md, case_dir, patches=(("walls", "zeroGradient"),),
+                            precision: int = 6, time_precision: int = 6):
+    """Vm and activationTime of a Monodomain context at its current time."""
+    t = md.time()
+    tn = time_name(t, time_precision)
+    d = Path(case_dir) / tn
+    write_vol_scalar_field(d / "Vm", "Vm", md.vm(), DIM_VM, tn, patches, precision)
+    write_vol_scalar_field(d / "activationTime", "activationTime", md.activation(), DIM_TIME,
+                           tn, patches, precision)
+    return d
+
+
+def protocol_suffix(stim_period_s1: float, nstim1: int, stim_period_s2: float = 0.0,
+                    nstim2: int = 0) -> str:
+    """stimulusIO::protocolSuffix (stimulusIO.C:392-423): noStim, S1_<s1> or
+    S1_<s1>_S2_<s2> (Foam::name: general format, 6 digits)."""
+    small = 1e-15
+    if stim_period_s1 <= small or nstim1 <= 0:
+        return "noStim"
+    out = f"S1_{stim_period_s1:.6g}"
+    if nstim2 > 0:
+        out += f"_S2_{stim_period_s2:.6g}"
+    return out
+
+
+def trace_file_name(model: str, tissue: str, stim) -> str:
+    """<ionicModel type>_<tissueName>_<protocol>.txt (singleCellSolver.C:100-112)."""
+    return f"{model}_{tissue}_{protocol_suffix(stim.stim_period_s1, stim.nstim1, stim.stim_period_s2, stim.nstim2)}.txt"
+
+
+class SingleCellTrace:
+    """SingleCellSolver's output file for an IonicModel: the header on
+    creation, one row per write(t) for integration point `cell`."""
+
+    def __init__(self, ionic, path, columns: Optional[Iterable[str]] = None, cell: int = 0):
+        self.ionic = ionic
+        self.cell = cell
+        self.columns = " ".join(columns) if columns else None
+        Path(path).parent.mkdir(parents=True, exist_ok=True)
+        self.fh = open(path, "w")
+        self.fh.write(ionic.trace_header(self.columns))
+
+    def write(self, t: float):
+        self.fh.write(self.ionic.trace_row(self.cell, t, self.columns))
+
+    def close(self):
+        if self.fh:
+            self.fh.close()
+            self.fh = None

@@ -135,7 +135,7 @@ EXPORTS = [
     "cfg_batch_trace", "cfg_batch_get_states", "cfg_batch_stats", "cfg_batch_stream",
     "cfg_batch_destroy", "cfg_adjoint_create", "cfg_adjoint_set_target", "cfg_adjoint_forward",
     "cfg_adjoint_backward", "cfg_adjoint_destroy", "cfg_ionic_autotune", "cfg_monodomain_autotune",
-    "cfg_ionic_set_launch",
+    "cfg_ionic_set_launch", "cfg_ionic_trace_header", "cfg_ionic_trace_row",
 ]
 
 _lib = None
@@ -207,6 +207,9 @@ def load(path: Optional[os.PathLike] = None):
                                      C.POINTER(C.c_float)]
     L.cfg_monodomain_autotune.argtypes = [C.c_void_p, _ip, _ip, C.POINTER(C.c_float)]
     L.cfg_ionic_set_launch.argtypes = [C.c_void_p, C.c_int, C.c_int]
+    L.cfg_ionic_trace_header.argtypes = [C.c_void_p, C.c_char_p, C.c_char_p, C.c_size_t]
+    L.cfg_ionic_trace_row.argtypes = [C.c_void_p, C.c_longlong, C.c_double, C.c_char_p,
+                                      C.c_char_p, C.c_size_t]
     L.cfg_box_diffusion_solve_noalloc.argtypes = [C.POINTER(BoxDiffusionDesc), C.c_double,
                                                   C.c_void_p, C.c_void_p, C.c_void_p,
                                                   C.c_void_p, C.c_void_p,

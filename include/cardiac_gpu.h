@@ -129,6 +129,19 @@ int cfg_ionic_sweep_current(cfg_ionic* ion, const char* current, double v_min, d
                             int n_points, double* out, int* n_columns, char* header,
                             size_t header_len);
 
+/* The single-cell trace (ionicModelIO::writeHeader / write,
+ * genericWriter/ionicModelIO.C:28-86,169-232, as SingleCellSolver writes it,
+ * singleCellSolver.C:100-118,226-229): "time" and the column names, then per
+ * call one row for integration point `cell` at time t [s]: t and the values,
+ * fixed with 7 decimals.  columns = NULL or "" writes every variable (Vm -
+ * transformed for AlievPanfilov and BuenoOrovio -, the other states, the
+ * algebraics, RATES_<state>); otherwise the variableExport names (separated
+ * by spaces or commas) resolved as ionicModelIO does, unknown ones ignored.
+ * The algebraics and rates are those of the model's variables at t. */
+int cfg_ionic_trace_header(const cfg_ionic* ion, const char* columns, char* buf, size_t len);
+int cfg_ionic_trace_row(cfg_ionic* ion, long long cell, double t, const char* columns, char* buf,
+                        size_t len);
+
 /* -------------------------------------------------------- monodomain step */
 
 /* lduMesh view of the myocardium: OpenFOAM's lower/upper addressing of the

@@ -52,3 +52,39 @@ def test_sweep_unknown_current(gpu_lib):
         ion.sweep_current("NoSuchCurrent", -90, 60, 10)
     assert "Unknown current: NoSuchCurrent" in str(e.value)
     assert "INa" in str(e.value)
+
+
+@pytest.mark.gpu
+def test_single_cell_trace_against_reference_file(gpu_lib, tmp_path):
+    """SingleCellSolver's trace of AlievPanfilov written through
+    cfg_ionic_trace_row equals the reference's own trace file (time and Vm,
+    7 decimals) within one unit of the last printed digit."""
+    from cardiacfoam_gb300 import io
+    g = np.load(GOLDEN / "aliev_panfilov_singlecell.npz")
+    ref = g["vm_1e7"][:400] * 1e-7
+    dt = 5e-5
+    stim = api.stimulus_desc(20, 1000, 1, 0.4, 3)
+    m = api.IonicModel("AlievPanfilov", "myocyte", 1, dt, solve_vm_within_ode=True,
+                       ode=api.ode_desc(abs_tol=1e-6, rel_tol=1e-4, max_steps=10 ** 6),
+                       stimulus=stim)
+    path = tmp_path / io.trace_file_name("AlievPanfilov", "myocyte", stim)
+    tr = io.SingleCellTrace(m, path, columns=["Vm"])
+    im = np.zeros(1)
+    t = 0.0
+    for k in range(ref.size):
+        t = t + dt                       # runTime accumulates deltaT
+        m.solveODE(t - dt, dt, None, im)
+        tr.write(t)
+    tr.close()
+    lines = path.read_text().splitlines()
+    assert lines[0] == "time Vm"
+    rows = np.array([[float(x) for x in l.split()] for l in lines[1:]])
+    assert np.allclose(rows[:, 0], (np.arange(ref.size) + 1) * dt, atol=5e-8)
+    assert np.max(np.abs(rows[:, 1] - ref)) <= 2.01e-7
+    # every variable: Vm, the other states, the algebraics, RATES_<state>
+    header = m.trace_header()
+    names = header.split()
+    assert names[0] == "time" and names[1] == "Vm" and names[-1].startswith("RATES_")
+    row = m.trace_row(0, t).split()
+    assert len(row) == len(names)
+    m.close()
