@@ -67,6 +67,7 @@ struct CoopArgs {
 
 // A.q for row c (diag*q_c, then each -coef*q_nb in column order), q read
 // through L2.  Stencil neighbours come from (i, j, k) = row decomposition.
+template <int W>
 __device__ __forceinline__ double amul_cg(const DiffusionArgs& a, const CoopArgs& ca,
                                           unsigned c, double d, const double* q)
 {
@@ -81,6 +82,12 @@ __device__ __forceinline__ double amul_cg(const DiffusionArgs& a, const CoopArgs
         if (i + 1 < nx) acc += (-a.cx) * __ldcg(&q[c + 1]);
         if (j + 1 < unsigned(a.sy)) acc += (-a.cy) * __ldcg(&q[c + nx]);
         if (k + 1 < unsigned(a.sz)) acc += (-a.cz) * __ldcg(&q[c + nxy]);
+    } else if constexpr (W > 0) {
+        // padded slots: coefficient 0 and column 0, an exact zero term
+#pragma unroll
+        for (int e = 0; e < W; ++e)
+            acc += (-ld_stream(&a.ell_coef[(long long)e * a.n + c])) *
+                   __ldcg(&q[ld_stream(&a.ell_col[(long long)e * a.n + c])]);
     } else {
         const int cnt = a.ell_cnt[c];
         for (int e = 0; e < cnt; ++e)
@@ -100,7 +107,7 @@ __device__ __forceinline__ double amul_cg(const DiffusionArgs& a, const CoopArgs
 //                A.p = w + beta A.p (linearity of A), sum p.A.p  | barrier
 //   update pass: x += alpha p, r -= alpha A.p, z = D^-1 r (published for
 //                the next halo pass), sums |r| and z.r           | barrier
-template <class CR>
+template <class CR, int W>
 __global__ void __launch_bounds__(kCoopBlock, 1) k_implicit_coop(DiffusionArgs a, CoopArgs ca)
 {
     PcgState* st = a.st;
@@ -141,7 +148,7 @@ __global__ void __launch_bounds__(kCoopBlock, 1) k_implicit_coop(DiffusionArgs a
         if (a.nc_gw) {
             for (unsigned c = first; c < n; c += stride) {
                 CR g[3];
-                nc_gradient<CR>(a, c, [x](long long q) { return __ldcg(&x[q]); }, g);
+                nc_gradient<CR, W>(a, c, [x](long long q) { return __ldcg(&x[q]); }, g);
                 __stcg(&grad[c], g[0]);
                 __stcg(&grad[size_t(n) + c], g[1]);
                 __stcg(&grad[2 * size_t(n) + c], g[2]);
@@ -173,7 +180,7 @@ __global__ void __launch_bounds__(kCoopBlock, 1) k_implicit_coop(DiffusionArgs a
                 rhs = a.bsrc[c];
             }
             if (a.nc_gw)
-                rhs = rhs + nc_correction<CR>(a, c, [grad, n](long long q, int k) {
+                rhs = rhs + nc_correction<CR, W>(a, c, [grad, n](long long q, int k) {
                           return __ldcg(&grad[size_t(k) * n + size_t(q)]);
                       });
             return rhs;
@@ -182,8 +189,8 @@ __global__ void __launch_bounds__(kCoopBlock, 1) k_implicit_coop(DiffusionArgs a
             const unsigned c2 = c + stride;
             const bool two = c2 < n;
             const double b0 = rhs_row(c), b1 = two ? rhs_row(c2) : 0.0;
-            const double a0 = amul_cg(a, ca, c, diag[c], x);
-            const double a1 = two ? amul_cg(a, ca, c2, diag[c2], x) : 0.0;
+            const double a0 = amul_cg<W>(a, ca, c, diag[c], x);
+            const double a1 = two ? amul_cg<W>(a, ca, c2, diag[c2], x) : 0.0;
             const double r0 = b0 - a0, r1 = b1 - a1;
             b[c] = b0; ax[c] = a0; r[c] = r0;
             s1[0] += x[c];
@@ -234,8 +241,8 @@ __global__ void __launch_bounds__(kCoopBlock, 1) k_implicit_coop(DiffusionArgs a
                 for (unsigned c = first; c < n; c += 2 * stride) {
                     const unsigned c2 = c + stride;
                     const bool two = c2 < n;
-                    const double w0 = amul_cg(a, ca, c, diag[c], z);
-                    const double w1 = two ? amul_cg(a, ca, c2, diag[c2], z) : 0.0;
+                    const double w0 = amul_cg<W>(a, ca, c, diag[c], z);
+                    const double w1 = two ? amul_cg<W>(a, ca, c2, diag[c2], z) : 0.0;
                     const double z0 = __ldcg(&z[c]);
                     const double z1 = two ? __ldcg(&z[c2]) : 0.0;
                     double p0, p1, q0, q1;
@@ -356,13 +363,16 @@ int coop_grid_blocks(long long n)
     int dev = 0, sms = 0, per_sm = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return 0;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
-    int per_sm_f = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_implicit_coop<double>, kCoopBlock,
-                                                      0) != cudaSuccess ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_f, k_implicit_coop<float>, kCoopBlock,
-                                                      0) != cudaSuccess)
-        return 0;
-    per_sm = per_sm < per_sm_f ? per_sm : per_sm_f;
+    per_sm = 1 << 30;
+    const void* fns[] = {(const void*)k_implicit_coop<double, 0>, (const void*)k_implicit_coop<float, 0>,
+                         (const void*)k_implicit_coop<double, 4>, (const void*)k_implicit_coop<float, 4>,
+                         (const void*)k_implicit_coop<double, 6>, (const void*)k_implicit_coop<float, 6>};
+    for (const void* f : fns) {
+        int k = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&k, f, kCoopBlock, 0) != cudaSuccess)
+            return 0;
+        per_sm = per_sm < k ? per_sm : k;
+    }
     long long want = (n + kCoopBlock - 1) / kCoopBlock;
     long long cap = (long long)sms * per_sm;
     return int(want < cap ? want : cap);
@@ -377,8 +387,16 @@ cudaError_t launch_implicit_coop(const DiffusionArgs& a, int blocks, cudaStream_
     }
     DiffusionArgs args = a;
     void* params[] = {&args, &ca};
-    void* fn = a.nc_fp32 ? reinterpret_cast<void*>(k_implicit_coop<float>)
-                         : reinterpret_cast<void*>(k_implicit_coop<double>);
+    // rows of a general mesh visited over the full ELL width when it is 4
+    // (tetrahedra) or 6 (hexahedra)
+    const int w = (!a.sx && (a.width == 4 || a.width == 6)) ? a.width : 0;
+    void* fn = nullptr;
+    if (a.nc_fp32)
+        fn = w == 4 ? (void*)k_implicit_coop<float, 4> : w == 6 ? (void*)k_implicit_coop<float, 6>
+                                                                : (void*)k_implicit_coop<float, 0>;
+    else
+        fn = w == 4 ? (void*)k_implicit_coop<double, 4> : w == 6 ? (void*)k_implicit_coop<double, 6>
+                                                                 : (void*)k_implicit_coop<double, 0>;
     return cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(kCoopBlock), params, 0, s);
 }
 

@@ -202,20 +202,33 @@ __device__ __forceinline__ double row_amul(const DiffusionArgs& a, long long c, 
 // Cell gradient of x at row c on a general mesh: sum over the row's slots
 // of gw_e (x_nb - x_c) (leastSquares or Gauss linear weights), in R (the
 // differences are taken in FP64).
-template <class R, class F>
+// Streaming loads of the operator's per-slot arrays: read once per pass and
+// larger than L2 on big meshes, so they are loaded evict-first and leave L2
+// to the vectors whose entries the neighbours gather.
+template <class T>
+__device__ __forceinline__ T ld_stream(const T* p)
+{
+    return __ldcs(p);
+}
+
+// W > 0: every row is visited over W slots (the ELL width); padded slots
+// hold zero weights and coefficients, so they add exact zeros, and the
+// fixed trip count lets all of a row's loads be issued together.
+template <class R, int W = 0, class F>
 __device__ __forceinline__ void nc_gradient(const DiffusionArgs& a, long long c, F x, R (&g)[3])
 {
     const R* gw = static_cast<const R*>(a.nc_gw);
     const long long n = a.n, wn = (long long)a.width * n;
     const double xc = x(c);
     g[0] = g[1] = g[2] = R(0);
-    const int cnt = a.ell_cnt[c];
-    for (int e = 0; e < cnt; ++e) {
+    const int cnt = W > 0 ? W : a.ell_cnt[c];
+#pragma unroll
+    for (int e = 0; e < (W > 0 ? W : cnt); ++e) {
         const long long i = (long long)e * n + c;
-        const R dv = R(x(a.ell_col[i]) - xc);
-        g[0] += gw[i] * dv;
-        g[1] += gw[wn + i] * dv;
-        g[2] += gw[2 * wn + i] * dv;
+        const R dv = R(x(ld_stream(&a.ell_col[i])) - xc);
+        g[0] += ld_stream(&gw[i]) * dv;
+        g[1] += ld_stream(&gw[wn + i]) * dv;
+        g[2] += ld_stream(&gw[2 * wn + i]) * dv;
     }
 }
 
@@ -223,7 +236,7 @@ __device__ __forceinline__ void nc_gradient(const DiffusionArgs& a, long long c,
 // flux k.(w (g_P - g_N) + g_N) with the sign of the row (faces in column
 // order, the order of the face loop), then the wall term bk.g_c.  g(q, k)
 // reads component k of cell q's gradient.
-template <class R, class G>
+template <class R, int W = 0, class G>
 __device__ __forceinline__ double nc_correction(const DiffusionArgs& a, long long c, G g)
 {
     const R* kc = static_cast<const R*>(a.nc_k);
@@ -232,18 +245,19 @@ __device__ __forceinline__ double nc_correction(const DiffusionArgs& a, long lon
     const long long n = a.n, wn = (long long)a.width * n;
     const R g0 = g(c, 0), g1 = g(c, 1), g2 = g(c, 2);
     R s = R(0);
-    const int cnt = a.ell_cnt[c];
-    for (int e = 0; e < cnt; ++e) {
+    const int cnt = W > 0 ? W : a.ell_cnt[c];
+#pragma unroll
+    for (int e = 0; e < (W > 0 ? W : cnt); ++e) {
         const long long i = (long long)e * n + c;
-        const long long nb = a.ell_col[i];
-        const R om = omv[i];
+        const long long nb = ld_stream(&a.ell_col[i]);
+        const R om = ld_stream(&omv[i]);
         const R n0 = g(nb, 0), n1 = g(nb, 1), n2 = g(nb, 2);
         const R f0 = om * (g0 - n0) + n0;
         const R f1 = om * (g1 - n1) + n1;
         const R f2 = om * (g2 - n2) + n2;
-        s += kc[i] * f0 + kc[wn + i] * f1 + kc[2 * wn + i] * f2;
+        s += ld_stream(&kc[i]) * f0 + ld_stream(&kc[wn + i]) * f1 + ld_stream(&kc[2 * wn + i]) * f2;
     }
-    s += bk[c] * g0 + bk[n + c] * g1 + bk[2 * n + c] * g2;
+    s += ld_stream(&bk[c]) * g0 + ld_stream(&bk[n + c]) * g1 + ld_stream(&bk[2 * n + c]) * g2;
     return double(s);
 }
 
