@@ -730,16 +730,16 @@ def main():
         out["cpu_baseline"] = cpu_baseline()
         one = cpu_baseline(nthreads=1, cells_x=10, steps=5)
         out["cpu_baseline"]["single_thread"] = {k: one[k] for k in ("value", "cores", "sample")}
+        import platform
+        cpu = platform.processor() or platform.machine()
         try:
-            import platform
-            cpu = platform.processor() or platform.machine()
             with open("/proc/cpuinfo") as fh:
                 for line in fh:
                     if line.lower().startswith(("model name", "cpu part")):
                         cpu = line.split(":", 1)[1].strip()
                         break
         except OSError:
-            cpu = platform.machine()
+            pass
         out["cpu_baseline"]["cpu"] = f"{cpu}, nproc {os.cpu_count()}"
     print(json.dumps(out), flush=True)
 
