@@ -351,8 +351,7 @@ batch_mixed_kernel(BatchLaunch p)
     constexpr int NS = M::NS, P = S::NSP;
     extern __shared__ float cfg_batch_smem[];
     float* Y = cfg_batch_smem + threadIdx.x * S::len;
-    float* Tm = Y + P;
-    float* K = Tm + P;
+    float* K = Y + P;
     float* LO = K + 5 * P;
     unsigned evals = 0;
     for (;;) {
@@ -361,7 +360,7 @@ batch_mixed_kernel(BatchLaunch p)
         long long k = p.done[c];
         const long long total = p.n_steps[c];
         if (k >= total) continue;
-        for (int i = 0; i < 6 * P; ++i) Tm[i] = 0.0f;
+        for (int i = 0; i < 5 * P; ++i) K[i] = 0.0f;
         const float2* yw2 = reinterpret_cast<const float2*>(p.yw);
         int w = 0;
 #pragma unroll
@@ -391,7 +390,7 @@ batch_mixed_kernel(BatchLaunch p)
             dx_try = fminf(dx_try, float(dtm));
             IonicFailure why;
             float iion;
-            const long long nsub = mixed::solve<M, true>(ts, te, float(dtm), Y, Tm, K, LO,
+            const long long nsub = mixed::solve<M, true>(ts, te, float(dtm), Y, K, LO,
                                                          dx_try, Kc, T, stim, p.ode, evals,
                                                          why, iion);
             if (nsub < 0) {

@@ -47,7 +47,7 @@ template <class M>
 struct Slice {
     static constexpr int NSP = M::NS | 1;   // odd stride for each array
     static constexpr int NW = Layout<M, false>::n_wide();
-    static constexpr int raw = 7 * NSP + NW;
+    static constexpr int raw = 6 * NSP + NW;   // Y, five stage slots, low parts
     static constexpr int len = raw | 1;       // odd slice length: conflict-free
     // 64 threads per block unless 32 keeps more threads resident per SM
     static constexpr int block =
@@ -92,7 +92,9 @@ CFG_D __forceinline__ void add_wide(float& hi, float& lo, float d)
     hi = h;
 }
 
-// Stage input T = Y + h * sum_j a_sj k_j for stages 2..5 (s = 1..4).
+// Stage input T = Y + h * sum_j a_sj k_j for stages 2..5 (s = 1..4); T is
+// the stage's own slot K + s P, where its derivative is then evaluated in
+// place.
 template <class M>
 CFG_D __forceinline__ void stage_input(int s, float h, const float* Y, float* T, const float* K)
 {
@@ -132,8 +134,9 @@ CFG_D __forceinline__ void stage_input(int s, float h, const float* Y, float* T,
     }
 }
 
-// Stage-6 input, and P, E and the round-off bound of E into slots 1, 2, 4
-// (k2 and the old k3..k5 are not needed afterwards: b2 = e2 = 0).
+// Stage-6 input into slot 3 (k4's, read first), and P, E and the round-off
+// bound of E into slots 1, 2, 4 (k2 and the old k3..k5 are not needed
+// afterwards: b2 = e2 = 0).
 template <class M>
 CFG_D __forceinline__ void stage6_input(float h, const float* Y, float* T, float* K)
 {
@@ -157,8 +160,12 @@ CFG_D __forceinline__ void stage6_input(float h, const float* Y, float* T, float
 // ODESolver::solve over [xs, xs + D] (RKF45 inside adaptiveSolver::solve),
 // then the right-hand side at the end of the interval for the current.
 // Returns accepted substeps, or -1 on maxSteps overflow / step underflow.
+// Every stage's derivative is evaluated in place, in the slot that holds the
+// stage input (the generated right-hand side reads every state before it
+// writes a derivative); in tissue mode the slot's state-0 entry, which the
+// model leaves unassigned or sets to zero, is then zeroed.
 template <class M, bool SV, class KS>
-CFG_D __forceinline__ long long solve(double xs, double xe, float D, float* Y, float* T, float* K, float* LO,
+CFG_D __forceinline__ long long solve(double xs, double xe, float D, float* Y, float* K, float* LO,
                                       float& dx_try, const KS& Kc, int tissue,
                                       const CfgStimulus& st, const OdeSettings& s,
                                       unsigned& evals, IonicFailure& why, float& iion)
@@ -207,19 +214,20 @@ CFG_D __forceinline__ long long solve(double xs, double xe, float D, float* Y, f
         if (sg == 0) {
             out = K;
         } else if (sg < 5) {
-            stage_input<M>(sg, h, Y, T, K);
-            in = T;
             out = K + sg * P;
+            stage_input<M>(sg, h, Y, out, K);
+            in = out;
         } else if (sg == 5) {
-            stage6_input<M>(h, Y, T, K);
-            in = T;
             out = K + 3 * P;
+            stage6_input<M>(h, Y, out, K);
+            in = out;
         } else {
-            out = T;
+            out = K + P;      // the current at the end: any free slot
         }
         double t = 0.0;
         if constexpr (SV) t = sg == 6 ? xe : xs + double(u) + double(stage_c(sg) * h);
         const float r = M::template rates<float, SV>(t, ArrayView<float>{in}, Kc, out, tissue, st);
+        if constexpr (!SV) out[0] = 0.0f;
         ++evals;
         if (sg == 6) {
             iion = r;
@@ -314,8 +322,7 @@ ionic_mixed_kernel(IonicLaunch p)
     constexpr int NS = M::NS, P = S::NSP;
     extern __shared__ float cfg_mixed_smem[];
     float* Y = cfg_mixed_smem + threadIdx.x * S::len;
-    float* T = Y + P;
-    float* K = T + P;
+    float* K = Y + P;
     float* LO = K + 5 * P;
     unsigned evals = 0;
     const long long end = p.first + p.count;
@@ -325,9 +332,9 @@ ionic_mixed_kernel(IonicLaunch p)
         const double t0 = p.t_dev ? p.t_dev[0] : p.t0;
         double ts, te, dtm;
         model_times<M>(t0, p.dt, ts, te, dtm);
-        // derivatives the model does not assign (Vm in tissue mode) stay zero
+        // derivatives the model does not assign (Vm in tissue mode) are zero
         // in every stage slot, as in a zero-filled dydt array
-        for (int i = 0; i < 6 * P; ++i) T[i] = 0.0f;
+        for (int i = 0; i < 5 * P; ++i) K[i] = 0.0f;
         const float2* yw2 = reinterpret_cast<const float2*>(p.yw);
         int w = 0;
 #pragma unroll
@@ -355,7 +362,7 @@ ionic_mixed_kernel(IonicLaunch p)
         float iion = 0.0f;
         if constexpr (TISSUE > 0) {
             const ConstFold<float, M, TISSUE> Kc{};
-            nsub = mixed::solve<M, SV>(ts, te, float(dtm), Y, T, K, LO, dx_try, Kc, TISSUE, p.stim,
+            nsub = mixed::solve<M, SV>(ts, te, float(dtm), Y, K, LO, dx_try, Kc, TISSUE, p.stim,
                                        p.ode, evals, why, iion);
         } else {
             const int tissue = p.tissue_cell ? int(p.tissue_cell[c]) : p.tissue;
@@ -370,7 +377,7 @@ ionic_mixed_kernel(IonicLaunch p)
             }
             M::init(C, yinit, tissue, scp);
             const ConstView<float> Kc{C};
-            nsub = mixed::solve<M, SV>(ts, te, float(dtm), Y, T, K, LO, dx_try, Kc, tissue, p.stim,
+            nsub = mixed::solve<M, SV>(ts, te, float(dtm), Y, K, LO, dx_try, Kc, tissue, p.stim,
                                        p.ode, evals, why, iion);
         }
         if (nsub < 0) {
