@@ -25,6 +25,10 @@ MODELS = ["tnnp", "ord", "torord_dyncl", "alievpanfilov", "buenoorovio",
 # per-model unroll factor of the per-state loops around the right-hand side
 # (measured on GB300: ORd fastest at 4, the others at 1)
 STATE_UNROLL = {"ord": 4}
+# resident blocks of 64 per SM the mixed kernel is built for, where the
+# model's registers (right-hand side plus the state held in registers) and
+# not its shared-memory slice set the limit: TNNP at 8 (128 registers)
+MIXED_MIN_BLOCKS = {"tnnp": 8}
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
@@ -52,6 +56,8 @@ def _units():
             extra = list(ionic_extra)
             if not unroll and m in STATE_UNROLL:
                 extra.append(f"-DCFG_IONIC_STATE_UNROLL={STATE_UNROLL[m]}")
+            if prec == "mixed" and m in MIXED_MIN_BLOCKS:
+                extra.append(f"-DCFG_MIXED_MIN_BLOCKS={MIXED_MIN_BLOCKS[m]}")
             units.append((f"ionic_{m}_{prec}", CSRC / "ionic_instance.cu",
                           flags + [f"-DCFG_MODEL={m}"] + extra))
     units.append(("ionic_registry", CSRC / "ionic_registry.cu", []))

@@ -350,9 +350,9 @@ batch_mixed_kernel(BatchLaunch p)
     using L = Layout<M, false>;
     constexpr int NS = M::NS, P = S::NSP;
     extern __shared__ float cfg_batch_smem[];
-    float* Y = cfg_batch_smem + threadIdx.x * S::len;
-    float* K = Y + P;
-    float* LO = K + 5 * P;
+    float* K = cfg_batch_smem + threadIdx.x * S::len;
+    float Y[NS];
+    float LO[S::NWA];
     unsigned evals = 0;
     for (;;) {
         const long long c = (long long)atomicAdd(p.queue, 1ull);

@@ -43,17 +43,27 @@ constexpr int blocks_per_sm(int block, int len)
     return kSmemPerSm / (block * len * 4 + kSmemReserve);
 }
 
+// Per thread: the five stage slots in shared memory (the state Y and the
+// low parts of the slow states live in registers).
 template <class M>
 struct Slice {
     static constexpr int NSP = M::NS | 1;   // odd stride for each array
     static constexpr int NW = Layout<M, false>::n_wide();
-    static constexpr int raw = 6 * NSP + NW;   // Y, five stage slots, low parts
+    static constexpr int NWA = NW > 0 ? NW : 1;
+    static constexpr int raw = 5 * NSP;     // five stage slots
     static constexpr int len = raw | 1;       // odd slice length: conflict-free
     // 64 threads per block unless 32 keeps more threads resident per SM
     static constexpr int block =
         32 * blocks_per_sm(32, len) > 64 * blocks_per_sm(64, len) ? 32 : 64;
     static constexpr int fit = blocks_per_sm(block, len);
-    static constexpr int min_blocks = fit < 1 ? 1 : (fit > 16 ? 16 : fit);
+#ifdef CFG_MIXED_MIN_BLOCKS
+    // register budget of the model (its right-hand side plus the state in
+    // registers) when that, not shared memory, limits the resident blocks
+    static constexpr int want = fit < CFG_MIXED_MIN_BLOCKS ? fit : CFG_MIXED_MIN_BLOCKS;
+#else
+    static constexpr int want = fit;
+#endif
+    static constexpr int min_blocks = want < 1 ? 1 : (want > 16 ? 16 : want);
     static constexpr int smem_bytes = block * len * 4;
 };
 
@@ -96,16 +106,17 @@ CFG_D __forceinline__ void add_wide(float& hi, float& lo, float d)
 // the stage's own slot K + s P, where its derivative is then evaluated in
 // place.
 template <class M>
-CFG_D __forceinline__ void stage_input(int s, float h, const float* Y, float* T, const float* K)
+CFG_D __forceinline__ void stage_input(int s, float h, const float (&Y)[M::NS], float* T,
+                                       const float* K)
 {
     constexpr int NS = M::NS, P = Slice<M>::NSP;
     switch (s) {
     case 1:
-#pragma unroll 4
+#pragma unroll
         for (int i = 0; i < NS; ++i) T[i] = Y[i] + h * (fa21 * K[i]);
         break;
     case 2:
-#pragma unroll 4
+#pragma unroll
         for (int i = 0; i < NS; ++i) {
             float acc = fa31 * K[i];
             acc += fa32 * K[P + i];
@@ -113,7 +124,7 @@ CFG_D __forceinline__ void stage_input(int s, float h, const float* Y, float* T,
         }
         break;
     case 3:
-#pragma unroll 4
+#pragma unroll
         for (int i = 0; i < NS; ++i) {
             float acc = fa41 * K[i];
             acc += fa42 * K[P + i];
@@ -122,7 +133,7 @@ CFG_D __forceinline__ void stage_input(int s, float h, const float* Y, float* T,
         }
         break;
     default:
-#pragma unroll 4
+#pragma unroll
         for (int i = 0; i < NS; ++i) {
             float acc = fa51 * K[i];
             acc += fa52 * K[P + i];
@@ -138,10 +149,10 @@ CFG_D __forceinline__ void stage_input(int s, float h, const float* Y, float* T,
 // bound of E into slots 1, 2, 4 (k2 and the old k3..k5 are not needed
 // afterwards: b2 = e2 = 0).
 template <class M>
-CFG_D __forceinline__ void stage6_input(float h, const float* Y, float* T, float* K)
+CFG_D __forceinline__ void stage6_input(float h, const float (&Y)[M::NS], float* T, float* K)
 {
     constexpr int NS = M::NS, P = Slice<M>::NSP;
-#pragma unroll 4
+#pragma unroll
     for (int i = 0; i < NS; ++i) {
         const float k1 = K[i], k2 = K[P + i], k3 = K[2 * P + i], k4 = K[3 * P + i],
                     k5 = K[4 * P + i];
@@ -164,8 +175,21 @@ CFG_D __forceinline__ void stage6_input(float h, const float* Y, float* T, float
 // stage input (the generated right-hand side reads every state before it
 // writes a derivative); in tissue mode the slot's state-0 entry, which the
 // model leaves unassigned or sets to zero, is then zeroed.
+// State i of Y at a run-time index (for failure records), without indexing
+// the register array at run time.
+template <int NS>
+CFG_D __forceinline__ double state_at(const float (&Y)[NS], int i)
+{
+    float v = 0.0f;
+#pragma unroll
+    for (int k = 0; k < NS; ++k)
+        if (k == i) v = Y[k];
+    return double(v);
+}
+
 template <class M, bool SV, class KS>
-CFG_D __forceinline__ long long solve(double xs, double xe, float D, float* Y, float* K, float* LO,
+CFG_D __forceinline__ long long solve(double xs, double xe, float D, float (&Y)[M::NS], float* K,
+                                      float (&LO)[Slice<M>::NWA],
                                       float& dx_try, const KS& Kc, int tissue,
                                       const CfgStimulus& st, const OdeSettings& s,
                                       unsigned& evals, IonicFailure& why, float& iion)
@@ -193,7 +217,7 @@ CFG_D __forceinline__ long long solve(double xs, double xe, float D, float* Y, f
                 // the last accepted substep, as ODESolver reports it
                 why.reason = 1;
                 why.x = xs + double(u_prev); why.dx = dx; why.err = err; why.worst = worst;
-                why.value = worst >= 0 ? double(Y[worst]) : 0.0;
+                why.value = worst >= 0 ? state_at(Y, worst) : 0.0;
                 why.steps = n - 1;
                 return -1;
             }
@@ -209,21 +233,25 @@ CFG_D __forceinline__ long long solve(double xs, double xe, float D, float* Y, f
             sg = 0;
         }
         const float h = dx;
-        const float* in = Y;
         float* out;
         if (sg == 0) {
+            // k1 = f(y), evaluated in slot 0 from a copy of y
             out = K;
+#pragma unroll
+            for (int i = 0; i < NS; ++i) out[i] = Y[i];
         } else if (sg < 5) {
             out = K + sg * P;
             stage_input<M>(sg, h, Y, out, K);
-            in = out;
         } else if (sg == 5) {
             out = K + 3 * P;
             stage6_input<M>(h, Y, out, K);
-            in = out;
         } else {
-            out = K + P;      // the current at the end: any free slot
+            // the current at the end, from y in a free slot
+            out = K + P;
+#pragma unroll
+            for (int i = 0; i < NS; ++i) out[i] = Y[i];
         }
+        const float* in = out;
         double t = 0.0;
         if constexpr (SV) t = sg == 6 ? xe : xs + double(u) + double(stage_c(sg) * h);
         const float r = M::template rates<float, SV>(t, ArrayView<float>{in}, Kc, out, tissue, st);
@@ -241,7 +269,7 @@ CFG_D __forceinline__ long long solve(double xs, double xe, float D, float* Y, f
         float maxerr = 0.0f;
         bool finite = true;
         worst = -1;
-#pragma unroll 4
+#pragma unroll
         for (int i = 0; i < NS; ++i) {
             const float k6 = K[3 * P + i];
             const float y0 = Y[i];
@@ -265,7 +293,7 @@ CFG_D __forceinline__ long long solve(double xs, double xe, float D, float* Y, f
             if (!(dx >= 1e-37f)) {
                 why.reason = 2;
                 why.x = xs + double(u); why.dx = dx; why.err = err; why.worst = worst;
-                why.value = worst >= 0 ? double(Y[worst]) : 0.0;
+                why.value = worst >= 0 ? state_at(Y, worst) : 0.0;
                 why.steps = n;
                 return -1;
             }
@@ -274,7 +302,7 @@ CFG_D __forceinline__ long long solve(double xs, double xe, float D, float* Y, f
         }
         // --- accept: y = y5 (slow states as hi + lo)
         int w = 0;
-#pragma unroll 4
+#pragma unroll
         for (int i = 0; i < NS; ++i) {
             const float incr = h * (K[P + i] + fb6 * K[3 * P + i]);
             if (is_wide<M::WIDE_MASK>(i)) {
@@ -321,9 +349,9 @@ ionic_mixed_kernel(IonicLaunch p)
     using L = Layout<M, false>;
     constexpr int NS = M::NS, P = S::NSP;
     extern __shared__ float cfg_mixed_smem[];
-    float* Y = cfg_mixed_smem + threadIdx.x * S::len;
-    float* K = Y + P;
-    float* LO = K + 5 * P;
+    float* K = cfg_mixed_smem + threadIdx.x * S::len;
+    float Y[NS];
+    float LO[S::NWA];
     unsigned evals = 0;
     const long long end = p.first + p.count;
     for (long long c = p.first + (long long)blockIdx.x * blockDim.x + threadIdx.x; c < end;
