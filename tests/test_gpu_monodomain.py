@@ -175,3 +175,25 @@ def test_persistent_diffusion_equals_kernel_sequence(gpu_lib, stencil):
     assert np.array_equal(a0 > 0, a1 > 0)
     assert np.max(np.abs(a0 - a1)) <= 1e-8
     assert abs(i0 - i1) <= max(2, nsteps // 50)
+
+
+@pytest.mark.gpu
+def test_fields_written_as_openfoam_volscalarfields(gpu_lib, tmp_path):
+    """Vm and activationTime of a context written at its current time and
+    read back from the ASCII files."""
+    mesh = box_mesh(20, 7, 3, 0.02, 0.007, 0.003)
+    m = api.Monodomain(mesh, "TNNP", "epicardialCells", SIGMA, dt=1e-5, boxes=BOX)
+    m.run(1e-5, 50)
+    d = m.write(tmp_path, patches=[("walls", "zeroGradient")])
+    assert d.name == "0.0005"
+    for name, ref in (("Vm", m.vm()), ("activationTime", m.activation())):
+        text = (d / name).read_text()
+        assert f"object      {name};" in text
+        if "nonuniform" in text:
+            body = text.split("nonuniform List<scalar>")[1].split("(", 1)[1].split(")", 1)[0]
+            vals = np.array([float(x) for x in body.split()])
+        else:
+            vals = np.full(ref.size, float(text.split("uniform")[1].split(";")[0]))
+        assert vals.size == ref.size
+        assert np.allclose(vals, ref, rtol=1e-5, atol=1e-12)
+    m.close()
