@@ -256,6 +256,44 @@ LV_DT = 1e-5
 LV_INTENSITY = 5e4       # A/m^3, for 2 ms
 
 
+def ecg_timing(args, L, md, launches: int = 50):
+    """The pseudo-ECG at the LV's five electrodes (PseudoECGSolver::compute,
+    folded into one lead row per electrode): `launches` evaluations recorded
+    back to back on the context's stream between CUDA events.  One evaluation
+    reads the rows and Vm once, (electrodes + 1) x 8 bytes per cell, more
+    than L2 holds at this size."""
+    import torch
+    from cardiacfoam_gb300 import api
+    el = L.ecg_electrodes()
+    t0 = time.perf_counter()
+    pe = api.PseudoECG(L.mesh, el, conductivity_per_cell=L.conductivity, max_rows=launches + 3)
+    t_setup = time.perf_counter() - t0
+    s = torch.cuda.ExternalStream(md.stream())
+    for _ in range(3):
+        pe.record(md)
+    pe.reset()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(s)
+    for _ in range(launches):
+        pe.record(md)
+    e1.record(s)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / launches
+    _, values = pe.series()
+    pe.close()
+    n = L.mesh.n_cells
+    nbytes = n * 8 * (len(el) + 1)
+    pk, src = peaks()
+    peak = pk["hbm_gbs"]
+    gbs = nbytes / (ms * 1e-3) / 1e9
+    return {"electrodes": len(el), "setup_seconds": t_setup, "launches": launches,
+            "us_per_evaluation": ms * 1e3, "bytes_per_evaluation": nbytes,
+            "achieved_gbs": gbs, "hbm_peak_gbs": peak, "peak_src": src,
+            "frac_of_hbm_peak": gbs / peak,
+            "values_at_t": [float(v) for v in values[-1]]}
+
+
 def lv_arm(args, flush):
     """The left-ventricle configuration: a truncated prolate-ellipsoid shell
     of about 4.0 M tetrahedra with rule-based fibres (per-cell conductivity
@@ -293,6 +331,7 @@ def lv_arm(args, flush):
     ionic_ms, diff_ms, nsteps, launches = mixed.timings()
     evals = mixed.rhs_evaluations() - evals0
     mixed.set_timing(False)
+    ecg = ecg_timing(args, L, mixed)
     iters, corrs = [], []
     for _ in range(5):
         mixed.step(LV_DT)
@@ -346,6 +385,7 @@ def lv_arm(args, flush):
                      "activation_error_ms": float(np.max(np.abs(a64[both] - amx[both])) * 1e3)
                      if both.any() else None,
                      "vm_linf_error_V": float(np.max(np.abs(fp64.vm() - mixed_b.vm())))},
+        "pseudo_ecg": ecg,
         "l2": "flushed (256 MB write) between timed steps",
     }
     del mixed, mixed_b, fp64

@@ -430,6 +430,115 @@ class BatchCells:
     __del__ = close
 
 
+def ecg_electrodes(text: str, domain: Optional[str] = None):
+    """(names, positions [n][3]) of an ecgDomains entry of an electroProperties
+    text (ECGDomain::readElectrodes, ecgDomain.C:45-80), in the dictionary's
+    order; the first ecgDomains entry when domain is None."""
+    lib = _L.load()
+    n = C.c_int()
+    dom = domain.encode() if domain else None
+    rc = lib.cfg_pseudo_ecg_electrodes_from_dict(text.encode(), dom, None, 0, None, 0,
+                                                 C.byref(n))
+    k = n.value
+    if rc != _L.CFG_OK and k == 0:   # with k > 0 the first call only found no room
+        _L.check(rc)
+    pos = np.zeros((max(k, 1), 3))
+    buf = C.create_string_buffer(len(text) + 1)
+    _L.check(lib.cfg_pseudo_ecg_electrodes_from_dict(text.encode(), dom, buf, len(buf),
+                                                     _L.dptr(pos), k, C.byref(n)))
+    names = buf.value.decode().split()
+    return names, pos[:k].copy()
+
+
+class PseudoECG:
+    """ECGDomain with the pseudoECG solver on the GPU (cfg_pseudo_ecg_*,
+    pseudoECGSolver.C:34-87): phi at each electrode of the domain's Vm.
+
+    The mesh needs its full geometry (LduMesh.has_geometry); conductivity is
+    the monodomain's (uniform or per cell) and grad_scheme its gradSchemes
+    default.  ``record`` after each step keeps the time series on the device
+    (up to ``max_rows`` rows) without waiting for the GPU."""
+
+    def __init__(self, mesh: LduMesh, electrodes, names: Optional[Sequence[str]] = None,
+                 sigma=(0.1334, 0.0, 0.0, 0.0176, 0.0, 0.0176), conductivity_per_cell=None,
+                 grad_scheme=_L.GRAD_LEAST_SQUARES, max_rows: int = 0):
+        self._lib = _L.load()
+        if not mesh.has_geometry:
+            raise ValueError("the pseudo-ECG needs a mesh with its full geometry")
+        self.electrodes = np.ascontiguousarray(electrodes, dtype=np.float64).reshape(-1, 3)
+        self.n_electrodes = self.electrodes.shape[0]
+        self.names = list(names) if names is not None else [f"E{i + 1}" for i in
+                                                            range(self.n_electrodes)]
+        if len(self.names) != self.n_electrodes:
+            raise ValueError("one name per electrode")
+        self.n = mesh.n_cells
+        self.max_rows = int(max_rows)
+        d = _L.PseudoEcgDesc()
+        for i, v in enumerate(sigma):
+            d.conductivity[i] = v
+        keep = [self.electrodes]
+        if conductivity_per_cell is not None:
+            sig = np.ascontiguousarray(conductivity_per_cell, dtype=np.float64).reshape(-1, 6)
+            if sig.shape[0] != mesh.n_cells:
+                raise ValueError("conductivity_per_cell needs one row of 6 per cell")
+            keep.append(sig)
+            d.conductivity_per_cell = _L.dptr(sig)
+        d.grad_scheme = int(grad_scheme)
+        d.n_electrodes = self.n_electrodes
+        d.electrodes = _L.dptr(self.electrodes)
+        d.max_rows = self.max_rows
+        md, keep2 = mesh_desc(mesh, structured=False)
+        h = C.c_void_p()
+        _L.check(self._lib.cfg_pseudo_ecg_create(C.byref(d), C.byref(md), C.byref(h)))
+        self.h = h
+
+    @classmethod
+    def from_dict(cls, text: str, mesh: LduMesh, domain: Optional[str] = None, **kw):
+        """Electrodes of the electroProperties' ecgDomains entry."""
+        names, pos = ecg_electrodes(text, domain)
+        return cls(mesh, pos, names=names, **kw)
+
+    def compute(self, source) -> np.ndarray:
+        """phi [n_electrodes] of a Monodomain's Vm, or of a CUDA tensor of
+        n_cells doubles (on torch's current stream)."""
+        out = np.zeros(self.n_electrodes)
+        if isinstance(source, Monodomain):
+            _L.check(self._lib.cfg_pseudo_ecg_compute_monodomain(self.h, source.h,
+                                                                 _L.dptr(out)))
+            return out
+        import torch
+        if not (source.is_cuda and source.dtype == torch.float64 and source.is_contiguous()
+                and source.numel() == self.n):
+            raise ValueError("a contiguous CUDA float64 tensor of n_cells values")
+        stream = torch.cuda.current_stream(source.device).cuda_stream
+        _L.check(self._lib.cfg_pseudo_ecg_compute(self.h, C.c_void_p(source.data_ptr()),
+                                                  C.c_void_p(stream), _L.dptr(out)))
+        return out
+
+    def record(self, md: "Monodomain"):
+        _L.check(self._lib.cfg_pseudo_ecg_record(self.h, md.h))
+
+    def series(self):
+        """(times [rows], values [rows][n_electrodes]) recorded so far."""
+        n = C.c_longlong()
+        _L.check(self._lib.cfg_pseudo_ecg_series(self.h, None, None, 0, C.byref(n)))
+        t = np.zeros(max(n.value, 1))
+        v = np.zeros((max(n.value, 1), self.n_electrodes))
+        _L.check(self._lib.cfg_pseudo_ecg_series(self.h, _L.dptr(t), _L.dptr(v), n.value,
+                                                 C.byref(n)))
+        return t[:n.value].copy(), v[:n.value].copy()
+
+    def reset(self):
+        _L.check(self._lib.cfg_pseudo_ecg_reset(self.h))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self._lib.cfg_pseudo_ecg_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+
 class AdjointProblem:
     """Probe-voltage misfit of the differentiable monodomain step and its
     gradient (cfg_adjoint_*): per-cell log-scales of TNNP g_Na and g_K1 and

@@ -70,6 +70,7 @@ def _units():
     units.append(("noalloc", CSRC / "noalloc.cu", []))
     units.append(("dictionary", CSRC / "dictionary.cpp", []))
     units.append(("geometry", CSRC / "geometry.cpp", []))
+    units.append(("ecg", CSRC / "ecg.cu", []))
     units.append(("adjoint", CSRC / "adjoint.cu", ["--use_fast_math"]))
     return units
 

@@ -27,6 +27,7 @@ struct Entry {
     bool is_dict = false;
     std::vector<std::string> tokens;   // value tokens, "(" ")" kept, [dims] dropped
     Dict dict;
+    std::vector<std::string> order;    // keys of dict in the order they first appear
 };
 
 class Parser {
@@ -94,7 +95,7 @@ private:
         return t;
     }
 
-    void parse_body(Dict& d, bool nested)
+    void parse_body(Dict& d, bool nested, std::vector<std::string>* order = nullptr)
     {
         for (;;) {
             std::string key = token();
@@ -115,7 +116,7 @@ private:
             if (peek() == "{") {
                 token();
                 e->is_dict = true;
-                parse_body(e->dict, true);
+                parse_body(e->dict, true, &e->order);
             } else {
                 int depth = 0;
                 for (;;) {
@@ -135,6 +136,7 @@ private:
                     e->tokens.push_back(t);
                 }
             }
+            if (order && d.find(key) == d.end()) order->push_back(key);
             d[key] = e;
         }
     }
@@ -306,4 +308,60 @@ extern "C" int cfg_monodomain_create_from_dict(const char* text, const cfg_mesh_
         }
     }
     return cfg_monodomain_create(&d, mesh, out);
+}
+
+// ECGDomain::readElectrodes (ecgDomain.C:45-80) of the ecgDomains entry in
+// <myocardiumSolver>Coeffs, with the solver selection of ECGSolver::New.
+extern "C" int cfg_pseudo_ecg_electrodes_from_dict(const char* text, const char* domain,
+                                                   char* names, size_t len, double* positions,
+                                                   int max, int* n_electrodes)
+{
+    clear_error();
+    if (!text || !n_electrodes) return fail(CFG_ERR_INVALID, "null argument");
+    *n_electrodes = 0;
+    Dict root;
+    std::string err;
+    std::string src(text);
+    if (!Parser(src).parse(root, err))
+        return fail(CFG_ERR_INVALID, "electroProperties: %s", err.c_str());
+    std::string solver;
+    const Dict* coeffs = &root;
+    if (word(root, "myocardiumSolver", solver)) {
+        const Entry* ce = find(root, (solver + "Coeffs").c_str());
+        if (ce && ce->is_dict) coeffs = &ce->dict;
+    }
+    const Entry* ed = find(*coeffs, "ecgDomains");
+    if (!ed || !ed->is_dict || ed->order.empty())
+        return fail(CFG_ERR_INVALID, "electroProperties: no ecgDomains");
+    const std::string want = domain ? domain : "";
+    const std::string name = want.empty() ? ed->order.front() : want;
+    const Entry* de = find(ed->dict, name.c_str());
+    if (!de || !de->is_dict) return fail(CFG_ERR_INVALID, "ecgDomains: no domain %s", name.c_str());
+    std::string ecg_solver;
+    if (!word(de->dict, "ecgSolver", ecg_solver))
+        return fail(CFG_ERR_INVALID, "ecgDomains.%s: keyword ecgSolver is undefined", name.c_str());
+    if (ecg_solver != "pseudoECG")
+        return fail(CFG_ERR_UNSUPPORTED, "ecgSolver %s is not built (pseudoECG is)",
+                    ecg_solver.c_str());
+    const Entry* pe = find(de->dict, "electrodePositions");
+    if (!pe || !pe->is_dict) return CFG_OK;   // no electrodes: an empty list
+    std::string joined;
+    int k = 0;
+    for (const std::string& key : pe->order) {
+        std::vector<double> p = numbers(find(pe->dict, key.c_str()));
+        if (p.size() != 3)
+            return fail(CFG_ERR_INVALID, "electrode %s: expected (x y z)", key.c_str());
+        if (k < max && positions)
+            for (int i = 0; i < 3; ++i) positions[3 * k + i] = p[size_t(i)];
+        if (!joined.empty()) joined += ' ';
+        joined += key;
+        ++k;
+    }
+    *n_electrodes = k;
+    if (k > max) return fail(CFG_ERR_INVALID, "%d electrodes, room for %d", k, max);
+    if (names) {
+        if (joined.size() + 1 > len) return fail(CFG_ERR_INVALID, "electrode names exceed %zu bytes", len);
+        std::memcpy(names, joined.c_str(), joined.size() + 1);
+    }
+    return CFG_OK;
 }

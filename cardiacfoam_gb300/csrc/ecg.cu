@@ -1,0 +1,313 @@
+// Pseudo-ECG (PseudoECGSolver::compute, pseudoECGSolver.C:34-87) on the GPU.
+//
+//   phi(P_e) = sum_c ((sigma_c grad(Vm)_c) V_c) . r_ec / |r_ec|^3,  r_ec = C_c - P_e
+//
+// The gradient is linear in Vm (fvc::grad with zeroGradient walls) and the
+// mesh, the conductivity and the electrodes do not change during a run, so
+// phi is a fixed linear functional of Vm.  Creation folds the gradient
+// scheme's per-face weights and each cell's dipole geometry
+// z_ec = V_c sigma_c r_ec / |r_ec|^3 into one lead row L[e][0..n) per
+// electrode; an evaluation is phi_e = sum_c L[e][c] Vm_c, one streaming
+// pass over the rows (8 bytes per cell and electrode) and over Vm, bound by
+// HBM bandwidth.  Block partial sums are combined in block order by the
+// last block to finish, so the values do not depend on scheduling.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "geometry.h"
+#include "host_common.h"
+#include "monodomain_host.h"
+
+namespace {
+
+constexpr int kEcgBlock = 256;
+constexpr int kEcgChunk = 8;      // electrodes accumulated per pass over the cells
+constexpr int kEcgBlocksPerSm = 8;
+
+struct EcgArgs {
+    const double* lead;   // [n_el][n]
+    const double* vm;     // [n]
+    long long n;
+    int n_el;
+    double* partial;      // [gridDim.x][n_el]
+    unsigned* ticket;
+    double* out;          // [n_el]
+};
+
+__device__ __forceinline__ double warp_sum(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__global__ void __launch_bounds__(kEcgBlock) k_pseudo_ecg(EcgArgs a)
+{
+    __shared__ double red[kEcgBlock / 32][kEcgChunk];
+    __shared__ bool last;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const long long stride = (long long)gridDim.x * kEcgBlock;
+    const long long first = (long long)blockIdx.x * kEcgBlock + threadIdx.x;
+    for (int e0 = 0; e0 < a.n_el; e0 += kEcgChunk) {
+        const int ne = min(kEcgChunk, a.n_el - e0);
+        const double* lead = a.lead + (long long)e0 * a.n;
+        double acc[kEcgChunk];
+#pragma unroll
+        for (int j = 0; j < kEcgChunk; ++j) acc[j] = 0.0;
+        for (long long c = first; c < a.n; c += stride) {
+            const double v = __ldcs(&a.vm[c]);
+#pragma unroll
+            for (int j = 0; j < kEcgChunk; ++j)
+                if (j < ne) acc[j] = fma(__ldcs(&lead[(long long)j * a.n + c]), v, acc[j]);
+        }
+#pragma unroll
+        for (int j = 0; j < kEcgChunk; ++j) acc[j] = warp_sum(acc[j]);
+        if (lane == 0)
+#pragma unroll
+            for (int j = 0; j < kEcgChunk; ++j) red[warp][j] = acc[j];
+        __syncthreads();
+        if (threadIdx.x < ne) {
+            double s = 0.0;
+#pragma unroll
+            for (int w = 0; w < kEcgBlock / 32; ++w) s += red[w][threadIdx.x];
+            a.partial[(long long)blockIdx.x * a.n_el + e0 + threadIdx.x] = s;
+        }
+        __syncthreads();
+    }
+    __threadfence();
+    if (threadIdx.x == 0) last = atomicAdd(a.ticket, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    for (int e = warp; e < a.n_el; e += kEcgBlock / 32) {
+        double s = 0.0;
+        for (int b = lane; b < (int)gridDim.x; b += 32) s += __ldcg(&a.partial[(long long)b * a.n_el + e]);
+        s = warp_sum(s);
+        if (lane == 0) a.out[e] = s;
+    }
+    if (threadIdx.x == 0) *a.ticket = 0u;
+}
+
+}  // namespace
+
+struct cfg_pseudo_ecg {
+    long long n = 0;
+    int n_el = 0;
+    int blocks = 0;
+    double* d_lead = nullptr;
+    double* d_partial = nullptr;
+    unsigned* d_ticket = nullptr;
+    double* d_values = nullptr;     // compute()
+    double* h_values = nullptr;     // pinned mirror
+    double* d_series = nullptr;     // [max_rows][n_el]
+    long long max_rows = 0, rows = 0;
+    std::vector<double> times;
+    cudaStream_t last_stream = nullptr;   // stream of the last launch
+    bool launched = false;
+};
+
+using namespace cfg;
+
+namespace {
+
+// Lead rows L[e][c] of the pseudo-ECG: for each face the owner's gradient
+// gains g_own (phi_N - phi_P) and the neighbour's g_nei (phi_P - phi_N)
+// (the difference form of leastSquaresGrad / gaussGrad with zeroGradient
+// walls, built by assemble_corrected), so z_eP.g_own moves to N from P and
+// z_eN.g_nei to P from N.
+int fold_lead(const cfg_mesh_desc* m, const cfg_pseudo_ecg_desc* d, const CorrectedOperator& op,
+              std::vector<double>& lead)
+{
+    const long long n = m->n_cells, nf = m->n_faces;
+    const int ne = d->n_electrodes;
+    lead.assign(size_t(ne) * size_t(n), 0.0);
+    std::vector<double> z(size_t(3) * size_t(n));
+    for (int e = 0; e < ne; ++e) {
+        const double* P = d->electrodes + 3 * e;
+        for (long long c = 0; c < n; ++c) {
+            const double* C = m->centres + 3 * c;
+            const double r[3] = {C[0] - P[0], C[1] - P[1], C[2] - P[2]};
+            const double mag = std::sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+            double* zc = z.data() + 3 * c;
+            if (!(mag > 1e-300)) {   // VSMALL
+                zc[0] = zc[1] = zc[2] = 0.0;
+                continue;
+            }
+            const double* s = d->conductivity_per_cell ? d->conductivity_per_cell + 6 * c
+                                                       : d->conductivity;
+            const double k = m->volumes[c] / (mag * mag * mag);
+            // (sigma g) . r = g . (sigma r) for the symmetric sigma
+            zc[0] = k * (s[0] * r[0] + s[1] * r[1] + s[2] * r[2]);
+            zc[1] = k * (s[1] * r[0] + s[3] * r[1] + s[4] * r[2]);
+            zc[2] = k * (s[2] * r[0] + s[4] * r[1] + s[5] * r[2]);
+        }
+        double* L = lead.data() + size_t(e) * size_t(n);
+        for (long long f = 0; f < nf; ++f) {
+            const long long own = m->owner[f], nei = m->neighbour[f];
+            const double* go = op.g_own.data() + 3 * f;
+            const double* gn = op.g_nei.data() + 3 * f;
+            const double* zp = z.data() + 3 * own;
+            const double* zn = z.data() + 3 * nei;
+            const double a = zp[0] * go[0] + zp[1] * go[1] + zp[2] * go[2];
+            const double b = zn[0] * gn[0] + zn[1] * gn[1] + zn[2] * gn[2];
+            L[nei] += a - b;
+            L[own] += b - a;
+        }
+    }
+    return CFG_OK;
+}
+
+// The partial sums and the ticket are the object's own: a launch on another
+// stream than the last one waits for that one first.
+int launch(cfg_pseudo_ecg* ecg, const double* vm, cudaStream_t s, double* out)
+{
+    if (ecg->launched && s != ecg->last_stream)
+        CFG_CUDA_TRY(cudaStreamSynchronize(ecg->last_stream));
+    EcgArgs a{ecg->d_lead, vm, ecg->n, ecg->n_el, ecg->d_partial, ecg->d_ticket, out};
+    k_pseudo_ecg<<<ecg->blocks, kEcgBlock, 0, s>>>(a);
+    CFG_CUDA_TRY(cudaGetLastError());
+    ecg->last_stream = s;
+    ecg->launched = true;
+    return CFG_OK;
+}
+
+}  // namespace
+
+extern "C" int cfg_pseudo_ecg_create(const cfg_pseudo_ecg_desc* d, const cfg_mesh_desc* m,
+                                     cfg_pseudo_ecg** out)
+{
+    clear_error();
+    if (!d || !m || !out) return fail(CFG_ERR_INVALID, "null argument");
+    *out = nullptr;
+    if (!m->face_centres || !m->centres || !m->volumes || !m->face_sf)
+        return fail(CFG_ERR_INVALID, "the pseudo-ECG needs the mesh's full geometry");
+    if (d->n_electrodes <= 0 || !d->electrodes)
+        return fail(CFG_ERR_INVALID, "no electrodes");
+    if (d->max_rows < 0) return fail(CFG_ERR_INVALID, "max_rows must be non-negative");
+    if (d->grad_scheme != CFG_GRAD_LEAST_SQUARES && d->grad_scheme != CFG_GRAD_GAUSS_LINEAR)
+        return fail(CFG_ERR_INVALID, "unknown gradient scheme %d", d->grad_scheme);
+    const long long n = m->n_cells;
+    for (long long f = 0; f < m->n_faces; ++f) {
+        const int l = m->owner[f], u = m->neighbour[f];
+        if (l < 0 || u < 0 || l >= n || u >= n || l == u)
+            return fail(CFG_ERR_INVALID, "face %lld has invalid owner/neighbour %d/%d", f, l, u);
+    }
+    const size_t lead_bytes = size_t(d->n_electrodes) * size_t(n) * sizeof(double);
+    size_t free_b = 0, total_b = 0;
+    CFG_CUDA_TRY(cudaMemGetInfo(&free_b, &total_b));
+    if (lead_bytes > free_b / 2)
+        return fail(CFG_ERR_INVALID, "the lead rows (%zu bytes) exceed half the free device memory",
+                    lead_bytes);
+    CorrectedOperator op;
+    if (int rc = assemble_corrected(m, d->conductivity, d->conductivity_per_cell, d->grad_scheme,
+                                    0, op))
+        return rc;
+    std::vector<double> lead;
+    if (int rc = fold_lead(m, d, op, lead)) return rc;
+
+    auto* ecg = new cfg_pseudo_ecg();
+    ecg->n = n;
+    ecg->n_el = d->n_electrodes;
+    // one wave of resident blocks, grid-striding over the cells
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pseudo_ecg, kEcgBlock, 0);
+    per_sm = std::max(1, std::min(per_sm, kEcgBlocksPerSm));
+    const long long need = (n + kEcgBlock - 1) / kEcgBlock;
+    ecg->blocks = int(std::max(1LL, std::min<long long>(need, (long long)std::max(sms, 1) * per_sm)));
+    auto bail = [&](int rc) {
+        cfg_pseudo_ecg_destroy(ecg);
+        return rc;
+    };
+    cudaError_t e = dmalloc(&ecg->d_lead, lead.size());
+    if (!e) e = cudaMemcpy(ecg->d_lead, lead.data(), lead_bytes, cudaMemcpyHostToDevice);
+    if (!e) e = dmalloc(&ecg->d_partial, size_t(ecg->blocks) * size_t(ecg->n_el));
+    if (!e) e = dmalloc(&ecg->d_ticket, 1);
+    if (!e) e = cudaMemset(ecg->d_ticket, 0, sizeof(unsigned));
+    if (!e) e = dmalloc(&ecg->d_values, size_t(ecg->n_el));
+    if (!e) e = cudaMallocHost(reinterpret_cast<void**>(&ecg->h_values),
+                               size_t(ecg->n_el) * sizeof(double));
+    if (!e && d->max_rows > 0) e = dmalloc(&ecg->d_series, size_t(d->max_rows) * size_t(ecg->n_el));
+    if (e) return bail(fail(CFG_ERR_CUDA, "pseudo-ECG allocation: %s", cudaGetErrorString(e)));
+    ecg->max_rows = d->max_rows;
+    ecg->times.reserve(size_t(d->max_rows));
+    *out = ecg;
+    return CFG_OK;
+}
+
+extern "C" int cfg_pseudo_ecg_compute(cfg_pseudo_ecg* ecg, const double* vm, void* stream,
+                                      double* values)
+{
+    if (!ecg || !vm || !values) return fail(CFG_ERR_INVALID, "null argument");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (int rc = launch(ecg, vm, s, ecg->d_values)) return rc;
+    CFG_CUDA_TRY(cudaMemcpyAsync(ecg->h_values, ecg->d_values, size_t(ecg->n_el) * sizeof(double),
+                                 cudaMemcpyDeviceToHost, s));
+    CFG_CUDA_TRY(cudaStreamSynchronize(s));
+    std::memcpy(values, ecg->h_values, size_t(ecg->n_el) * sizeof(double));
+    return CFG_OK;
+}
+
+extern "C" int cfg_pseudo_ecg_compute_monodomain(cfg_pseudo_ecg* ecg, cfg_monodomain* md,
+                                                 double* values)
+{
+    if (!ecg || !md) return fail(CFG_ERR_INVALID, "null argument");
+    if (md->n != ecg->n) return fail(CFG_ERR_INVALID, "the context has %lld cells, the ECG %lld",
+                                     md->n, ecg->n);
+    return cfg_pseudo_ecg_compute(ecg, md->d_vm, md->stream, values);
+}
+
+extern "C" int cfg_pseudo_ecg_record(cfg_pseudo_ecg* ecg, cfg_monodomain* md)
+{
+    if (!ecg || !md) return fail(CFG_ERR_INVALID, "null argument");
+    if (md->n != ecg->n) return fail(CFG_ERR_INVALID, "the context has %lld cells, the ECG %lld",
+                                     md->n, ecg->n);
+    if (ecg->rows >= ecg->max_rows)
+        return fail(CFG_ERR_INVALID, "the pseudo-ECG series is full (%lld rows)", ecg->max_rows);
+    if (int rc = launch(ecg, md->d_vm, md->stream, ecg->d_series + ecg->rows * ecg->n_el)) return rc;
+    ecg->times.push_back(md->t_host);
+    ecg->rows++;
+    return CFG_OK;
+}
+
+extern "C" int cfg_pseudo_ecg_series(cfg_pseudo_ecg* ecg, double* times, double* values,
+                                     long long max_rows, long long* n_rows)
+{
+    if (!ecg) return fail(CFG_ERR_INVALID, "null argument");
+    if (n_rows) *n_rows = ecg->rows;
+    const long long k = std::min(max_rows, ecg->rows);
+    if (k <= 0) return CFG_OK;
+    if (ecg->launched) CFG_CUDA_TRY(cudaStreamSynchronize(ecg->last_stream));
+    if (values)
+        CFG_CUDA_TRY(cudaMemcpy(values, ecg->d_series, size_t(k) * size_t(ecg->n_el) * sizeof(double),
+                                cudaMemcpyDeviceToHost));
+    if (times) std::memcpy(times, ecg->times.data(), size_t(k) * sizeof(double));
+    return CFG_OK;
+}
+
+extern "C" int cfg_pseudo_ecg_reset(cfg_pseudo_ecg* ecg)
+{
+    if (!ecg) return fail(CFG_ERR_INVALID, "null argument");
+    ecg->rows = 0;
+    ecg->times.clear();
+    return CFG_OK;
+}
+
+extern "C" int cfg_pseudo_ecg_destroy(cfg_pseudo_ecg* ecg)
+{
+    if (!ecg) return CFG_OK;
+    if (ecg->launched) cudaStreamSynchronize(ecg->last_stream);
+    dfree(ecg->d_lead);
+    dfree(ecg->d_partial);
+    dfree(ecg->d_ticket);
+    dfree(ecg->d_values);
+    dfree(ecg->d_series);
+    if (ecg->h_values) cudaFreeHost(ecg->h_values);
+    delete ecg;
+    return CFG_OK;
+}

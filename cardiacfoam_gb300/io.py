@@ -8,6 +8,9 @@
   ``postProcessing/<model>_<tissue>_<protocol>.txt`` with a ``time <names>``
   header and fixed 7-decimal rows; the rows are formatted by the library
   (``cfg_ionic_trace_row``).
+* The pseudo-ECG time series of ``ECGDomain`` (``ecgModelIO::openTimeSeries``
+  / ``writeRow``): ``postProcessing/pseudoECG.dat`` with a ``# time <names>``
+  header and rows in scientific notation with 8 decimals.
 """
 from __future__ import annotations
 
@@ -113,3 +116,30 @@ class SingleCellTrace:
         if self.fh:
             self.fh.close()
             self.fh = None
+
+
+def ecg_header(names: Sequence[str]) -> str:
+    """ecgModelIO::openTimeSeries (ecgModelIO.C:30-50): '# time' and the
+    electrode names, two spaces apart."""
+    return "# time" + "".join("  " + n for n in names) + "\n"
+
+
+def ecg_row(t: float, values: Sequence[float]) -> str:
+    """ecgModelIO::writeRow (ecgModelIO.C:53-66) on the scientific,
+    precision-8 stream."""
+    return f"{t:.8e}" + "".join(f"  {v:.8e}" for v in values) + "\n"
+
+
+def write_pseudo_ecg(case_dir, names: Sequence[str], times: Sequence[float], values,
+                     file_name: str = "pseudoECG.dat") -> Path:
+    """<case>/postProcessing/pseudoECG.dat with the given rows (ECGDomain
+    writes the rows of output times, ecgDomain.C:163-180)."""
+    out = Path(case_dir) / "postProcessing"
+    out.mkdir(parents=True, exist_ok=True)
+    path = out / file_name
+    v = np.asarray(values, dtype=np.float64).reshape(len(times), len(names))
+    with open(path, "w") as fh:
+        fh.write(ecg_header(names))
+        for t, row in zip(times, v):
+            fh.write(ecg_row(float(t), row))
+    return path

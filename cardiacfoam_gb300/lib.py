@@ -122,6 +122,12 @@ class AdjointDesc(C.Structure):
 
 
 # every symbol declared in include/cardiac_gpu.h
+class PseudoEcgDesc(C.Structure):
+    _fields_ = [("conductivity", C.c_double * 6), ("conductivity_per_cell", _dp),
+                ("grad_scheme", C.c_int), ("n_electrodes", C.c_int), ("electrodes", _dp),
+                ("max_rows", C.c_longlong)]
+
+
 EXPORTS = [
     "cfg_last_error", "cfg_ionic_create", "cfg_ionic_solve", "cfg_ionic_solve_device",
     "cfg_ionic_num_states", "cfg_ionic_state_name", "cfg_ionic_get_states",
@@ -136,6 +142,9 @@ EXPORTS = [
     "cfg_batch_destroy", "cfg_adjoint_create", "cfg_adjoint_set_target", "cfg_adjoint_forward",
     "cfg_adjoint_backward", "cfg_adjoint_destroy", "cfg_ionic_autotune", "cfg_monodomain_autotune",
     "cfg_ionic_set_launch", "cfg_ionic_trace_header", "cfg_ionic_trace_row",
+    "cfg_pseudo_ecg_create", "cfg_pseudo_ecg_compute", "cfg_pseudo_ecg_compute_monodomain",
+    "cfg_pseudo_ecg_record", "cfg_pseudo_ecg_series", "cfg_pseudo_ecg_reset",
+    "cfg_pseudo_ecg_destroy", "cfg_pseudo_ecg_electrodes_from_dict",
 ]
 
 _lib = None
@@ -210,6 +219,17 @@ def load(path: Optional[os.PathLike] = None):
     L.cfg_ionic_trace_header.argtypes = [C.c_void_p, C.c_char_p, C.c_char_p, C.c_size_t]
     L.cfg_ionic_trace_row.argtypes = [C.c_void_p, C.c_longlong, C.c_double, C.c_char_p,
                                       C.c_char_p, C.c_size_t]
+    L.cfg_pseudo_ecg_create.argtypes = [C.POINTER(PseudoEcgDesc), C.POINTER(MeshDesc),
+                                        C.POINTER(C.c_void_p)]
+    L.cfg_pseudo_ecg_compute.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, _dp]
+    L.cfg_pseudo_ecg_compute_monodomain.argtypes = [C.c_void_p, C.c_void_p, _dp]
+    L.cfg_pseudo_ecg_record.argtypes = [C.c_void_p, C.c_void_p]
+    L.cfg_pseudo_ecg_series.argtypes = [C.c_void_p, _dp, _dp, C.c_longlong,
+                                        C.POINTER(C.c_longlong)]
+    L.cfg_pseudo_ecg_reset.argtypes = [C.c_void_p]
+    L.cfg_pseudo_ecg_destroy.argtypes = [C.c_void_p]
+    L.cfg_pseudo_ecg_electrodes_from_dict.argtypes = [C.c_char_p, C.c_char_p, C.c_char_p,
+                                                      C.c_size_t, _dp, C.c_int, _ip]
     L.cfg_box_diffusion_solve_noalloc.argtypes = [C.POINTER(BoxDiffusionDesc), C.c_double,
                                                   C.c_void_p, C.c_void_p, C.c_void_p,
                                                   C.c_void_p, C.c_void_p,

@@ -62,6 +62,13 @@ class LeftVentricle:
         h = 0.5 * size
         return (-h, -h, z0), (h, h, z0 + size)
 
+    def ecg_electrodes(self) -> np.ndarray:
+        """Five pseudo-ECG electrodes around the shell [m]: below the apex,
+        above the base, and three to the sides at 1.5 to 2 outer radii."""
+        a, c = ENDO_A + WALL, ENDO_C + WALL
+        return np.array([[0.0, 0.0, -1.5 * c], [0.0, 0.0, 0.6 * c], [2.0 * a, 0.0, -0.4 * c],
+                         [0.0, -1.8 * a, -0.5 * c], [1.2 * a, 1.2 * a, -0.2 * c]])
+
 
 def _meridian(n: int = 200001):
     """Polar angle as a function of arc length on the mid-wall meridian."""

@@ -28,7 +28,7 @@ import numpy as np
 
 from . import api
 from . import lib as _L
-from .mesh import box_mesh
+from .mesh import box_mesh, with_box_geometry
 
 SIGMA = (0.111453302, 0.0, 0.0, 0.121585420, 0.0, 0.030396355)
 CHI, CM = 3.0, 2.0
@@ -73,11 +73,83 @@ def mesh_for(dim: int, n: int):
     return box_mesh(nx, ny, nz, 1.0, 1.0 if dim >= 2 else 0.1, 1.0 if dim == 3 else 0.1)
 
 
+# the tutorial's electrodes (monodomainPseudoECG/constant/electroProperties)
+ECG_ELECTRODES = (("E1", (-0.5, 0.5, 0.5)), ("E2", (1.5, 0.5, 0.5)), ("E3", (1.2, 0.23, 0.61)),
+                  ("E4", (1.35, 0.74, 0.28)), ("E5", (1.55, 0.41, 0.83)))
+
+
+def gauss_legendre(order: int):
+    """Nodes and weights of the order-point Gauss-Legendre rule on [-1, 1]
+    (pseudoECGManufacturedQuadratureRule, manufacturedFDAReference.H:220-292,
+    finds the same roots of P_order by Newton's method)."""
+    if order <= 0:
+        raise ValueError("quadrature order must be positive")
+    return np.polynomial.legendre.leggauss(order)
+
+
+def pseudo_ecg_spatial_reference(electrodes, dim: int, order: int = 96,
+                                 sigma=SIGMA) -> np.ndarray:
+    """Integral over the unit line/square/cube of (sigma grad F) . r / |r|^3,
+    r = x - P (the in-plane distance in 1D/2D), by the tensor Gauss-Legendre
+    rule mapped to [0, 1] (computeManufacturedPseudoECGSpatialReference,
+    manufacturedFDAReference.H:393-472); points with |r|^2 <= VSMALL add 0."""
+    nodes, weights = gauss_legendre(order)
+    x = 0.5 * (nodes + 1.0)
+    pi = math.pi
+    s = np.array([[sigma[0], sigma[1], sigma[2]], [sigma[1], sigma[3], sigma[4]],
+                  [sigma[2], sigma[4], sigma[5]]])
+    out = []
+    for P in np.asarray(electrodes, dtype=np.float64).reshape(-1, 3):
+        if dim == 1:
+            X = x
+            g = np.stack([-pi * np.sin(pi * X), 0 * X, 0 * X])
+            W = weights
+            r = np.stack([X - P[0], 0 * X, 0 * X])
+        elif dim == 2:
+            X, Y = np.meshgrid(x, x, indexing="ij")
+            g = np.stack([-pi * np.sin(pi * X) * np.cos(2 * pi * Y),
+                          -2 * pi * np.cos(pi * X) * np.sin(2 * pi * Y), 0 * X])
+            W = np.multiply.outer(weights, weights)
+            r = np.stack([X - P[0], Y - P[1], 0 * X])
+        else:
+            X, Y, Z = np.meshgrid(x, x, x, indexing="ij")
+            cx, cy, cz = np.cos(pi * X), np.cos(2 * pi * Y), np.cos(3 * pi * Z)
+            g = np.stack([-pi * np.sin(pi * X) * cy * cz,
+                          -2 * pi * cx * np.sin(2 * pi * Y) * cz,
+                          -3 * pi * cx * cy * np.sin(3 * pi * Z)])
+            W = np.multiply.outer(np.multiply.outer(weights, weights), weights)
+            r = np.stack([X - P[0], Y - P[1], Z - P[2]])
+        sg = np.einsum("ij,j...->i...", s, g)
+        r2 = (r * r).sum(axis=0)
+        f = np.where(r2 > 1e-300, (sg * r).sum(axis=0) / np.where(r2 > 1e-300, r2, 1.0) ** 1.5,
+                     0.0)
+        out.append(0.5 ** dim * float((W * f).sum()))
+    return np.array(out)
+
+
+def pseudo_ecg_reference(t: float, electrodes, dim: int, order: int = 96) -> np.ndarray:
+    """sqrt(1 + t) times the spatial reference (computeManufacturedPseudoECGReference,
+    manufacturedFDAReference.H:495-512)."""
+    return math.sqrt(1.0 + t) * pseudo_ecg_spatial_reference(electrodes, dim, order)
+
+
+def geometry_mesh_for(dim: int, n: int):
+    """mesh_for with the face centres and walls the pseudo-ECG gradient needs."""
+    return with_box_geometry(mesh_for(dim, n), 1.0, 1.0 if dim >= 2 else 0.1,
+                             1.0 if dim == 3 else 0.1)
+
+
 def run(dim: int, n: int, dt: float | None = None, end_time: float = END_TIME,
-        precision: int = _L.PRECISION_FP64, pcg_tol: float = 1e-12) -> Dict:
+        precision: int = _L.PRECISION_FP64, pcg_tol: float = 1e-12, ecg: bool = False,
+        ecg_order: int = 96) -> Dict:
     """One manufactured case on the GPU: implicit backward ddt, two PIMPLE
     correctors (the tutorial's fvSolution), PCG to `pcg_tol`.  Returns the
-    error norms of V, u1 and u2 at the end time."""
+    error norms of V, u1 and u2 at the end time; with ``ecg`` also the
+    pseudo-ECG at the tutorial's electrodes after every step (Gauss linear
+    gradient, the tutorial's gradSchemes) against the quadrature reference,
+    as pseudoECGManufacturedVerifier::updateStatistics accumulates them
+    (pseudoECGManufacturedVerifier.C:257-300): per electrode the L1 (mean),
+    L2 (RMS) and L-infinity of the error over the samples."""
     dt = SWEEP[n] if dt is None else dt
     mesh = mesh_for(dim, n)
     md = api.Monodomain(mesh, model="monodomainFDAManufactured", tissue=f"{dim}D", sigma=SIGMA,
@@ -88,11 +160,29 @@ def run(dim: int, n: int, dt: float | None = None, end_time: float = END_TIME,
     md.set_field(_L.FIELD_VM, V)
     md.set_states(np.stack([V, u1, u2, u3]))
     steps = int(round(end_time / dt))
-    md.run(dt, steps)
+    pe = None
+    if ecg:
+        pe = api.PseudoECG(geometry_mesh_for(dim, n), [p for _, p in ECG_ELECTRODES],
+                           names=[k for k, _ in ECG_ELECTRODES], sigma=SIGMA,
+                           grad_scheme=_L.GRAD_GAUSS_LINEAR, max_rows=steps)
+        for _ in range(steps):
+            md.step(dt)
+            pe.record(md)
+    else:
+        md.run(dt, steps)
     t = md.time()
     Ve, u1e, u2e, _ = manufactured_fields(mesh.centres, t, dim)
     st = md.states()
     out = {"dim": dim, "n": n, "dt": dt, "steps": steps, "t": t,
            "V": norms(md.vm(), Ve), "u1": norms(st[1], u1e), "u2": norms(st[2], u2e)}
+    if pe is not None:
+        times, values = pe.series()
+        spatial = pseudo_ecg_spatial_reference([p for _, p in ECG_ELECTRODES], dim, ecg_order)
+        ref = np.sqrt(1.0 + times)[:, None] * spatial[None, :]
+        err = np.abs(values - ref)
+        out["ecg"] = {"times": times, "values": values, "reference": ref,
+                      "L1": err.mean(axis=0), "L2": np.sqrt((err * err).mean(axis=0)),
+                      "Linf": err.max(axis=0)}
+        pe.close()
     md.close()
     return out

@@ -394,6 +394,59 @@ int cfg_adjoint_backward(cfg_adjoint* adj, double* grad_log_gna, double* grad_lo
                          double* grad_sigma);
 int cfg_adjoint_destroy(cfg_adjoint* adj);
 
+/* ----------------------------------------------------------- pseudo-ECG
+ * ECGDomain with the pseudoECG solver (ecgDomain.C:84-160,
+ * pseudoECGSolver.C:34-87): at each electrode P
+ *   phi(P) = sum over cells c of ((sigma_c & grad(Vm)_c) V_c) & r / |r|^3,
+ *   r = C_c - P, cells with |r| <= VSMALL skipped,
+ * grad the mesh's gradSchemes default (leastSquares or Gauss linear) with
+ * zeroGradient walls.  The mesh, the conductivity and the electrodes are
+ * fixed for the object's life, so phi is a fixed linear functional of Vm:
+ * creation folds the gradient weights and the dipole geometry into one row
+ * of n_cells coefficients per electrode (8 bytes per cell and electrode in
+ * device memory) and every evaluation is one pass over those rows and Vm.
+ * The mesh needs its full geometry (face_centres, walls). */
+typedef struct cfg_pseudo_ecg_desc {
+    double conductivity[6];              /* xx xy xz yy yz zz, used when ... */
+    const double* conductivity_per_cell; /* ... this is NULL; else host [n_cells][6] */
+    int grad_scheme;                     /* CFG_GRAD_* */
+    int n_electrodes;
+    const double* electrodes;            /* host [n_electrodes][3] positions [m] */
+    long long max_rows;                  /* rows of the device time series (0: none) */
+} cfg_pseudo_ecg_desc;
+
+typedef struct cfg_pseudo_ecg cfg_pseudo_ecg;
+
+int cfg_pseudo_ecg_create(const cfg_pseudo_ecg_desc* desc, const cfg_mesh_desc* mesh,
+                          cfg_pseudo_ecg** out);
+/* phi at every electrode of the device field vm [n_cells] into host
+ * values [n_electrodes]; stream is a cudaStream_t (NULL: the legacy default
+ * stream) and the call returns when the values are on the host. */
+int cfg_pseudo_ecg_compute(cfg_pseudo_ecg* ecg, const double* vm, void* stream, double* values);
+/* The same for a monodomain context's Vm on its stream. */
+int cfg_pseudo_ecg_compute_monodomain(cfg_pseudo_ecg* ecg, cfg_monodomain* md, double* values);
+/* ECGDomain::evolve (ecgDomain.C:163-180) after a monodomain step: phi of
+ * the context's Vm appended to the device time series with the context's
+ * time, enqueued on its stream without waiting (CFG_ERR_INVALID when the
+ * series is full). */
+int cfg_pseudo_ecg_record(cfg_pseudo_ecg* ecg, cfg_monodomain* md);
+/* The recorded rows: times [rows], values [rows][n_electrodes] (host; up to
+ * max_rows of them); *n_rows the number recorded.  reset empties the series. */
+int cfg_pseudo_ecg_series(cfg_pseudo_ecg* ecg, double* times, double* values,
+                          long long max_rows, long long* n_rows);
+int cfg_pseudo_ecg_reset(cfg_pseudo_ecg* ecg);
+int cfg_pseudo_ecg_destroy(cfg_pseudo_ecg* ecg);
+
+/* Electrodes of an ecgDomains entry of constant/electroProperties
+ * (<type>Coeffs.ecgDomains.<domain>: ecgSolver pseudoECG; electrodePositions
+ * { name (x y z); ... }, ecgDomain.C:45-80): names space-separated into
+ * names[len] in the dictionary's order, positions into [max][3].  domain
+ * NULL or "" takes the first ecgDomains entry.  An ecgSolver other than
+ * pseudoECG is CFG_ERR_UNSUPPORTED. */
+int cfg_pseudo_ecg_electrodes_from_dict(const char* electro_properties, const char* domain,
+                                        char* names, size_t len, double* positions, int max,
+                                        int* n_electrodes);
+
 /* ------------------------------------ diffusion solve without allocation
  * No counterpart in the reference.  For callers that cannot call cudaMalloc
  * when they need a solve (a host application that owns all device memory

@@ -1230,6 +1230,35 @@ int oracle_tissue_gradient(oracle_tissue* T, const double* phi, double* g)
     return 0;
 }
 
+/* PseudoECGSolver::compute (pseudoECGSolver.C:34-87): for each electrode P,
+ * sum over cells of ((sigma_c . grad(Vm)_c) V_c) . r / |r|^3 with r = C_c - P
+ * (cells at |r| <= VSMALL skipped), grad the tissue's gradient scheme. */
+int oracle_tissue_pseudo_ecg(oracle_tissue* T, const double* vm, int n_el, const double* el,
+                             double* out)
+{
+    if (!T->corrected_mesh) return -1;
+    double* g = (double*)malloc(sizeof(double) * 3 * (size_t)T->n);
+    cell_gradient(T, vm, g);
+    const oracle_mesh* M = T->mesh;
+    for (int e = 0; e < n_el; e++) out[e] = 0.0;
+    for (long c = 0; c < T->n; c++) {
+        double S[9];
+        cell_sigma(T, c, S);
+        const double* gc = g + 3 * c;
+        double dip[3];
+        for (int i = 0; i < 3; i++)
+            dip[i] = (S[3 * i] * gc[0] + S[3 * i + 1] * gc[1] + S[3 * i + 2] * gc[2]) * M->vol[c];
+        const double* C = M->centres + 3 * c;
+        for (int e = 0; e < n_el; e++) {
+            const double r[3] = {C[0] - el[3 * e], C[1] - el[3 * e + 1], C[2] - el[3 * e + 2]};
+            const double m = sqrt(dot3(r, r));
+            if (m > 1e-300) out[e] += dot3(dip, r) / (m * m * m);
+        }
+    }
+    free(g);
+    return 0;
+}
+
 /* MyocardiumDomain::updateActivationTime (myocardiumDomain.C:345-374) */
 static void update_activation(oracle_tissue* T, double dt)
 {

@@ -137,6 +137,9 @@ int oracle_tissue_set_cell_tissue(oracle_tissue*, const unsigned char* flags);
 /* fvc::laplacian(sigma, phi) [per volume] and the cell gradient of phi */
 void oracle_tissue_laplacian(oracle_tissue*, const double* phi, double* out);
 int oracle_tissue_gradient(oracle_tissue*, const double* phi, double* g);
+/* the pseudo-ECG of a Vm field at n_el electrodes [n_el][3] (general mesh) */
+int oracle_tissue_pseudo_ecg(oracle_tissue*, const double* vm, int n_el, const double* el,
+                             double* out);
 
 /* --- single cell (SingleCellSolver::evolve) ------------------------------ */
 /* Runs n_steps of dt [s] from t=0 with Vm inside the ODE; writes the

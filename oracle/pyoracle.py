@@ -94,6 +94,7 @@ def lib():
         L.oracle_tissue_set_cell_tissue.argtypes = [C.c_void_p, C.POINTER(C.c_ubyte)]
         L.oracle_tissue_laplacian.argtypes = [C.c_void_p, _dp, _dp]
         L.oracle_tissue_gradient.argtypes = [C.c_void_p, _dp, _dp]
+        L.oracle_tissue_pseudo_ecg.argtypes = [C.c_void_p, _dp, C.c_int, _dp, _dp]
         L.oracle_tissue_new.argtypes = [C.POINTER(TissueDesc), C.c_void_p]
         L.oracle_tissue_new.restype = C.c_void_p
         L.oracle_tissue_free.argtypes = [C.c_void_p]
@@ -364,6 +365,15 @@ class Tissue:
         p = np.ascontiguousarray(phi, dtype=np.float64)
         out = np.zeros(self.n)
         lib().oracle_tissue_laplacian(self.h, ptr(p), ptr(out))
+        return out
+
+    def pseudo_ecg(self, vm: np.ndarray, electrodes) -> np.ndarray:
+        """PseudoECGSolver::compute of the field vm at the electrodes [n][3]."""
+        v = np.ascontiguousarray(vm, dtype=np.float64)
+        el = np.ascontiguousarray(electrodes, dtype=np.float64).reshape(-1, 3)
+        out = np.zeros(el.shape[0])
+        if lib().oracle_tissue_pseudo_ecg(self.h, ptr(v), el.shape[0], ptr(el), ptr(out)):
+            raise RuntimeError("the pseudo-ECG needs a general mesh")
         return out
 
     def gradient(self, phi: np.ndarray) -> np.ndarray:
