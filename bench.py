@@ -256,27 +256,31 @@ LV_DT = 1e-5
 LV_INTENSITY = 5e4       # A/m^3, for 2 ms
 
 
-def ecg_timing(args, L, md, launches: int = 50):
+def ecg_timing(L, source, launches: int = 50):
     """The pseudo-ECG at the LV's five electrodes (PseudoECGSolver::compute,
     folded into one lead row per electrode): `launches` evaluations recorded
-    back to back on the context's stream between CUDA events.  One evaluation
-    reads the rows and Vm once, (electrodes + 1) x 8 bytes per cell, more
-    than L2 holds at this size."""
+    back to back between CUDA events on the stream they run on (a
+    Monodomain's, or torch's current stream for a CUDA tensor of Vm).  One
+    evaluation reads the rows and Vm once, (electrodes + 1) x 8 bytes per
+    cell: 191 MB on the 4.0 M-tet LV, more than L2 holds."""
     import torch
     from cardiacfoam_gb300 import api
     el = L.ecg_electrodes()
     t0 = time.perf_counter()
     pe = api.PseudoECG(L.mesh, el, conductivity_per_cell=L.conductivity, max_rows=launches + 3)
     t_setup = time.perf_counter() - t0
-    s = torch.cuda.ExternalStream(md.stream())
+    if isinstance(source, api.Monodomain):
+        s = torch.cuda.ExternalStream(source.stream())
+    else:
+        s = torch.cuda.current_stream()
     for _ in range(3):
-        pe.record(md)
+        pe.record(source)
     pe.reset()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
     e0.record(s)
     for _ in range(launches):
-        pe.record(md)
+        pe.record(source)
     e1.record(s)
     e1.synchronize()
     ms = e0.elapsed_time(e1) / launches
@@ -287,11 +291,23 @@ def ecg_timing(args, L, md, launches: int = 50):
     pk, src = peaks()
     peak = pk["hbm_gbs"]
     gbs = nbytes / (ms * 1e-3) / 1e9
-    return {"electrodes": len(el), "setup_seconds": t_setup, "launches": launches,
+    return {"electrodes": len(el), "cells": n, "setup_seconds": t_setup, "launches": launches,
             "us_per_evaluation": ms * 1e3, "bytes_per_evaluation": nbytes,
             "achieved_gbs": gbs, "hbm_peak_gbs": peak, "peak_src": src,
             "frac_of_hbm_peak": gbs / peak,
             "values_at_t": [float(v) for v in values[-1]]}
+
+
+def ecg_arm(args):
+    """The pseudo-ECG kernel alone on the LV mesh, on a seeded random Vm field
+    (uniform in [-90, 40] mV; the pass reads the same bytes for any values)."""
+    import torch
+    from cardiacfoam_gb300 import lv
+    dims = tuple(int(v) for v in args.lv_dims.split(",")) if args.lv_dims else lv.config_sizes()
+    L = lv.left_ventricle(*dims)
+    g = torch.Generator(device="cuda").manual_seed(7)
+    vm = torch.rand(L.mesh.n_cells, dtype=torch.float64, device="cuda", generator=g) * 0.13 - 0.09
+    return ecg_timing(L, vm, launches=args.ecg_launches)
 
 
 def lv_arm(args, flush):
@@ -331,7 +347,7 @@ def lv_arm(args, flush):
     ionic_ms, diff_ms, nsteps, launches = mixed.timings()
     evals = mixed.rhs_evaluations() - evals0
     mixed.set_timing(False)
-    ecg = ecg_timing(args, L, mixed)
+    ecg = ecg_timing(L, mixed)
     iters, corrs = [], []
     for _ in range(5):
         mixed.step(LV_DT)
@@ -664,6 +680,9 @@ def main():
     ap.add_argument("--adjoint-steps", type=int, default=20000)
     ap.add_argument("--adjoint-fd-directions", type=int, default=2)
     ap.add_argument("--adjoint-check-steps", type=int, default=2000)
+    ap.add_argument("--ecg-only", action="store_true",
+                    help="time the pseudo-ECG kernel alone on the LV mesh (--lv-dims)")
+    ap.add_argument("--ecg-launches", type=int, default=50)
     ap.add_argument("--lv-only", action="store_true",
                     help="run only the left-ventricle configuration (profiling)")
     ap.add_argument("--lv-dims", default="",
@@ -698,6 +717,11 @@ def main():
         from cardiacfoam_gb300 import build as gpu_build
         gpu_build.build()
         print(json.dumps({"adjoint": adjoint_arm(args)}), flush=True)
+        return
+    if args.ecg_only:
+        from cardiacfoam_gb300 import build as gpu_build
+        gpu_build.build()
+        print(json.dumps({"pseudo_ecg": ecg_arm(args)}), flush=True)
         return
     if args.lv_only:
         import torch

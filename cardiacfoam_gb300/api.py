@@ -432,7 +432,7 @@ class BatchCells:
 
 def ecg_electrodes(text: str, domain: Optional[str] = None):
     """(names, positions [n][3]) of an ecgDomains entry of an electroProperties
-    text (ECGDomain::readElectrodes, ecgDomain.C:45-80), in the dictionary's
+    text (ECGDomain::readElectrodes, ecgDomain.C:53-82), in the dictionary's
     order; the first ecgDomains entry when domain is None."""
     lib = _L.load()
     n = C.c_int()
@@ -498,6 +498,14 @@ class PseudoECG:
         names, pos = ecg_electrodes(text, domain)
         return cls(mesh, pos, names=names, **kw)
 
+    def _device_field(self, x):
+        import torch
+        if not (isinstance(x, torch.Tensor) and x.is_cuda and x.dtype == torch.float64
+                and x.is_contiguous() and x.numel() == self.n):
+            raise ValueError("a contiguous CUDA float64 tensor of n_cells values")
+        return (C.c_void_p(x.data_ptr()),
+                C.c_void_p(torch.cuda.current_stream(x.device).cuda_stream))
+
     def compute(self, source) -> np.ndarray:
         """phi [n_electrodes] of a Monodomain's Vm, or of a CUDA tensor of
         n_cells doubles (on torch's current stream)."""
@@ -506,17 +514,19 @@ class PseudoECG:
             _L.check(self._lib.cfg_pseudo_ecg_compute_monodomain(self.h, source.h,
                                                                  _L.dptr(out)))
             return out
-        import torch
-        if not (source.is_cuda and source.dtype == torch.float64 and source.is_contiguous()
-                and source.numel() == self.n):
-            raise ValueError("a contiguous CUDA float64 tensor of n_cells values")
-        stream = torch.cuda.current_stream(source.device).cuda_stream
-        _L.check(self._lib.cfg_pseudo_ecg_compute(self.h, C.c_void_p(source.data_ptr()),
-                                                  C.c_void_p(stream), _L.dptr(out)))
+        vm, stream = self._device_field(source)
+        _L.check(self._lib.cfg_pseudo_ecg_compute(self.h, vm, stream, _L.dptr(out)))
         return out
 
-    def record(self, md: "Monodomain"):
-        _L.check(self._lib.cfg_pseudo_ecg_record(self.h, md.h))
+    def record(self, source, t: Optional[float] = None):
+        """Append phi of a Monodomain's Vm (at its time), or of a CUDA tensor
+        at time t, to the device series without waiting."""
+        if isinstance(source, Monodomain):
+            _L.check(self._lib.cfg_pseudo_ecg_record(self.h, source.h))
+            return
+        vm, stream = self._device_field(source)
+        _L.check(self._lib.cfg_pseudo_ecg_record_field(self.h, vm, stream,
+                                                       float(0.0 if t is None else t)))
 
     def series(self):
         """(times [rows], values [rows][n_electrodes]) recorded so far."""

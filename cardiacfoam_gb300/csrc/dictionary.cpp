@@ -310,7 +310,7 @@ extern "C" int cfg_monodomain_create_from_dict(const char* text, const cfg_mesh_
     return cfg_monodomain_create(&d, mesh, out);
 }
 
-// ECGDomain::readElectrodes (ecgDomain.C:45-80) of the ecgDomains entry in
+// ECGDomain::readElectrodes (ecgDomain.C:53-82) of the ecgDomains entry in
 // <myocardiumSolver>Coeffs, with the solver selection of ECGSolver::New.
 extern "C" int cfg_pseudo_ecg_electrodes_from_dict(const char* text, const char* domain,
                                                    char* names, size_t len, double* positions,

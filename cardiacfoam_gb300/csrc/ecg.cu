@@ -13,7 +13,9 @@
 // last block to finish, so the values do not depend on scheduling.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
+#include <cstdint>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -25,16 +27,16 @@
 namespace {
 
 constexpr int kEcgBlock = 256;
-constexpr int kEcgChunk = 8;      // electrodes accumulated per pass over the cells
+constexpr int kEcgChunk = 8;      // electrodes of one launch
 constexpr int kEcgBlocksPerSm = 8;
 
 struct EcgArgs {
-    const double* lead;   // [n_el][n]
+    const double* lead;   // [n_el][ld], rows padded with zeros to an even length
     const double* vm;     // [n]
-    long long n;
-    int n_el;
+    long long n, ld;
+    int n_el, e0;         // all electrodes; the first of this launch
     double* partial;      // [gridDim.x][n_el]
-    unsigned* ticket;
+    unsigned* ticket;     // this launch's
     double* out;          // [n_el]
 };
 
@@ -45,62 +47,157 @@ __device__ __forceinline__ double warp_sum(double v)
     return v;
 }
 
+// phi_e += L[e][c] Vm_c for the NE electrodes from e0 over a grid-stride
+// loop; VEC: two cells per 16-byte load (Vm 16-byte aligned), two strides
+// per trip with every load issued before the first multiply-add.
+template <int NE, bool VEC>
 __global__ void __launch_bounds__(kEcgBlock) k_pseudo_ecg(EcgArgs a)
 {
-    __shared__ double red[kEcgBlock / 32][kEcgChunk];
+    __shared__ double red[kEcgBlock / 32][NE];
     __shared__ bool last;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const double* lead = a.lead + (long long)a.e0 * a.ld;
     const long long stride = (long long)gridDim.x * kEcgBlock;
-    const long long first = (long long)blockIdx.x * kEcgBlock + threadIdx.x;
-    for (int e0 = 0; e0 < a.n_el; e0 += kEcgChunk) {
-        const int ne = min(kEcgChunk, a.n_el - e0);
-        const double* lead = a.lead + (long long)e0 * a.n;
-        double acc[kEcgChunk];
+    long long i = (long long)blockIdx.x * kEcgBlock + threadIdx.x;
+    double acc[NE];
 #pragma unroll
-        for (int j = 0; j < kEcgChunk; ++j) acc[j] = 0.0;
-        for (long long c = first; c < a.n; c += stride) {
-            const double v = __ldcs(&a.vm[c]);
+    for (int j = 0; j < NE; ++j) acc[j] = 0.0;
+    if (VEC) {
+        const long long nv = a.n >> 1;
+        const double2* v2 = reinterpret_cast<const double2*>(a.vm);
+        for (; i + stride < nv; i += 2 * stride) {
+            const double2 x0 = __ldcs(v2 + i), x1 = __ldcs(v2 + i + stride);
+            double2 l0[NE], l1[NE];
 #pragma unroll
-            for (int j = 0; j < kEcgChunk; ++j)
-                if (j < ne) acc[j] = fma(__ldcs(&lead[(long long)j * a.n + c]), v, acc[j]);
+            for (int j = 0; j < NE; ++j) {
+                const double2* row = reinterpret_cast<const double2*>(lead + j * a.ld);
+                l0[j] = __ldcs(row + i);
+                l1[j] = __ldcs(row + i + stride);
+            }
+#pragma unroll
+            for (int j = 0; j < NE; ++j) {
+                acc[j] = fma(l0[j].x, x0.x, acc[j]);
+                acc[j] = fma(l0[j].y, x0.y, acc[j]);
+                acc[j] = fma(l1[j].x, x1.x, acc[j]);
+                acc[j] = fma(l1[j].y, x1.y, acc[j]);
+            }
         }
+        if (i < nv) {
+            const double2 x0 = __ldcs(v2 + i);
 #pragma unroll
-        for (int j = 0; j < kEcgChunk; ++j) acc[j] = warp_sum(acc[j]);
-        if (lane == 0)
-#pragma unroll
-            for (int j = 0; j < kEcgChunk; ++j) red[warp][j] = acc[j];
-        __syncthreads();
-        if (threadIdx.x < ne) {
-            double s = 0.0;
-#pragma unroll
-            for (int w = 0; w < kEcgBlock / 32; ++w) s += red[w][threadIdx.x];
-            a.partial[(long long)blockIdx.x * a.n_el + e0 + threadIdx.x] = s;
+            for (int j = 0; j < NE; ++j) {
+                const double2 l0 = __ldcs(reinterpret_cast<const double2*>(lead + j * a.ld) + i);
+                acc[j] = fma(l0.x, x0.x, acc[j]);
+                acc[j] = fma(l0.y, x0.y, acc[j]);
+            }
         }
-        __syncthreads();
+        if ((a.n & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
+            const long long c = a.n - 1;
+#pragma unroll
+            for (int j = 0; j < NE; ++j) acc[j] = fma(lead[j * a.ld + c], a.vm[c], acc[j]);
+        }
+    } else {
+        for (; i + stride < a.n; i += 2 * stride) {
+            const double x0 = __ldcs(a.vm + i), x1 = __ldcs(a.vm + i + stride);
+            double l0[NE], l1[NE];
+#pragma unroll
+            for (int j = 0; j < NE; ++j) {
+                l0[j] = __ldcs(lead + j * a.ld + i);
+                l1[j] = __ldcs(lead + j * a.ld + i + stride);
+            }
+#pragma unroll
+            for (int j = 0; j < NE; ++j) {
+                acc[j] = fma(l0[j], x0, acc[j]);
+                acc[j] = fma(l1[j], x1, acc[j]);
+            }
+        }
+        if (i < a.n) {
+            const double x0 = __ldcs(a.vm + i);
+#pragma unroll
+            for (int j = 0; j < NE; ++j) acc[j] = fma(__ldcs(lead + j * a.ld + i), x0, acc[j]);
+        }
     }
+#pragma unroll
+    for (int j = 0; j < NE; ++j) acc[j] = warp_sum(acc[j]);
+    if (lane == 0)
+#pragma unroll
+        for (int j = 0; j < NE; ++j) red[warp][j] = acc[j];
+    __syncthreads();
+    if (threadIdx.x < NE) {
+        double s = 0.0;
+#pragma unroll
+        for (int w = 0; w < kEcgBlock / 32; ++w) s += red[w][threadIdx.x];
+        a.partial[(long long)blockIdx.x * a.n_el + a.e0 + threadIdx.x] = s;
+    }
+    // the last block to finish adds the blocks' sums in block order
     __threadfence();
+    __syncthreads();
     if (threadIdx.x == 0) last = atomicAdd(a.ticket, 1u) == gridDim.x - 1;
     __syncthreads();
     if (!last) return;
     __threadfence();
-    for (int e = warp; e < a.n_el; e += kEcgBlock / 32) {
+    for (int e = warp; e < NE; e += kEcgBlock / 32) {
         double s = 0.0;
-        for (int b = lane; b < (int)gridDim.x; b += 32) s += __ldcg(&a.partial[(long long)b * a.n_el + e]);
+        for (int b = lane; b < (int)gridDim.x; b += 32)
+            s += __ldcg(&a.partial[(long long)b * a.n_el + a.e0 + e]);
         s = warp_sum(s);
-        if (lane == 0) a.out[e] = s;
+        if (lane == 0) a.out[a.e0 + e] = s;
     }
     if (threadIdx.x == 0) *a.ticket = 0u;
+}
+
+template <int NE>
+void launch_chunk(const EcgArgs& a, bool vec, int blocks, cudaStream_t s)
+{
+    if (vec) k_pseudo_ecg<NE, true><<<blocks, kEcgBlock, 0, s>>>(a);
+    else k_pseudo_ecg<NE, false><<<blocks, kEcgBlock, 0, s>>>(a);
+}
+
+template <int NE>
+int resident_blocks()
+{
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pseudo_ecg<NE, true>, kEcgBlock, 0);
+    return per_sm;
+}
+
+int resident_blocks_any(int ne)
+{
+    switch (ne) {
+    case 1: return resident_blocks<1>();
+    case 2: return resident_blocks<2>();
+    case 3: return resident_blocks<3>();
+    case 4: return resident_blocks<4>();
+    case 5: return resident_blocks<5>();
+    case 6: return resident_blocks<6>();
+    case 7: return resident_blocks<7>();
+    default: return resident_blocks<8>();
+    }
+}
+
+void launch_any(const EcgArgs& a, int ne, bool vec, int blocks, cudaStream_t s)
+{
+    switch (ne) {
+    case 1: launch_chunk<1>(a, vec, blocks, s); break;
+    case 2: launch_chunk<2>(a, vec, blocks, s); break;
+    case 3: launch_chunk<3>(a, vec, blocks, s); break;
+    case 4: launch_chunk<4>(a, vec, blocks, s); break;
+    case 5: launch_chunk<5>(a, vec, blocks, s); break;
+    case 6: launch_chunk<6>(a, vec, blocks, s); break;
+    case 7: launch_chunk<7>(a, vec, blocks, s); break;
+    default: launch_chunk<8>(a, vec, blocks, s); break;
+    }
 }
 
 }  // namespace
 
 struct cfg_pseudo_ecg {
-    long long n = 0;
+    long long n = 0, ld = 0;
     int n_el = 0;
-    int blocks = 0;
+    std::vector<int> blocks;        // grid of each launch
     double* d_lead = nullptr;
     double* d_partial = nullptr;
-    unsigned* d_ticket = nullptr;
+    unsigned* d_ticket = nullptr;   // one per launch of kEcgChunk electrodes
     double* d_values = nullptr;     // compute()
     double* h_values = nullptr;     // pinned mirror
     double* d_series = nullptr;     // [max_rows][n_el]
@@ -120,11 +217,11 @@ namespace {
 // walls, built by assemble_corrected), so z_eP.g_own moves to N from P and
 // z_eN.g_nei to P from N.
 int fold_lead(const cfg_mesh_desc* m, const cfg_pseudo_ecg_desc* d, const CorrectedOperator& op,
-              std::vector<double>& lead)
+              long long ld, std::vector<double>& lead)
 {
     const long long n = m->n_cells, nf = m->n_faces;
     const int ne = d->n_electrodes;
-    lead.assign(size_t(ne) * size_t(n), 0.0);
+    lead.assign(size_t(ne) * size_t(ld), 0.0);
     std::vector<double> z(size_t(3) * size_t(n));
     for (int e = 0; e < ne; ++e) {
         const double* P = d->electrodes + 3 * e;
@@ -145,7 +242,7 @@ int fold_lead(const cfg_mesh_desc* m, const cfg_pseudo_ecg_desc* d, const Correc
             zc[1] = k * (s[1] * r[0] + s[3] * r[1] + s[4] * r[2]);
             zc[2] = k * (s[2] * r[0] + s[4] * r[1] + s[5] * r[2]);
         }
-        double* L = lead.data() + size_t(e) * size_t(n);
+        double* L = lead.data() + size_t(e) * size_t(ld);
         for (long long f = 0; f < nf; ++f) {
             const long long own = m->owner[f], nei = m->neighbour[f];
             const double* go = op.g_own.data() + 3 * f;
@@ -167,9 +264,13 @@ int launch(cfg_pseudo_ecg* ecg, const double* vm, cudaStream_t s, double* out)
 {
     if (ecg->launched && s != ecg->last_stream)
         CFG_CUDA_TRY(cudaStreamSynchronize(ecg->last_stream));
-    EcgArgs a{ecg->d_lead, vm, ecg->n, ecg->n_el, ecg->d_partial, ecg->d_ticket, out};
-    k_pseudo_ecg<<<ecg->blocks, kEcgBlock, 0, s>>>(a);
-    CFG_CUDA_TRY(cudaGetLastError());
+    const bool vec = (reinterpret_cast<uintptr_t>(vm) & 15) == 0;
+    for (int e0 = 0, k = 0; e0 < ecg->n_el; e0 += kEcgChunk, ++k) {
+        EcgArgs a{ecg->d_lead, vm, ecg->n, ecg->ld, ecg->n_el, e0, ecg->d_partial,
+                  ecg->d_ticket + k, out};
+        launch_any(a, std::min(kEcgChunk, ecg->n_el - e0), vec, ecg->blocks[size_t(k)], s);
+        CFG_CUDA_TRY(cudaGetLastError());
+    }
     ecg->last_stream = s;
     ecg->launched = true;
     return CFG_OK;
@@ -196,7 +297,8 @@ extern "C" int cfg_pseudo_ecg_create(const cfg_pseudo_ecg_desc* d, const cfg_mes
         if (l < 0 || u < 0 || l >= n || u >= n || l == u)
             return fail(CFG_ERR_INVALID, "face %lld has invalid owner/neighbour %d/%d", f, l, u);
     }
-    const size_t lead_bytes = size_t(d->n_electrodes) * size_t(n) * sizeof(double);
+    const long long ld = n + (n & 1);
+    const size_t lead_bytes = size_t(d->n_electrodes) * size_t(ld) * sizeof(double);
     size_t free_b = 0, total_b = 0;
     CFG_CUDA_TRY(cudaMemGetInfo(&free_b, &total_b));
     if (lead_bytes > free_b / 2)
@@ -207,28 +309,35 @@ extern "C" int cfg_pseudo_ecg_create(const cfg_pseudo_ecg_desc* d, const cfg_mes
                                     0, op))
         return rc;
     std::vector<double> lead;
-    if (int rc = fold_lead(m, d, op, lead)) return rc;
+    if (int rc = fold_lead(m, d, op, ld, lead)) return rc;
 
     auto* ecg = new cfg_pseudo_ecg();
     ecg->n = n;
+    ecg->ld = ld;
     ecg->n_el = d->n_electrodes;
-    // one wave of resident blocks, grid-striding over the cells
-    int dev = 0, sms = 0, per_sm = 0;
+    // per launch one wave of resident blocks, grid-striding over the cells
+    int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pseudo_ecg, kEcgBlock, 0);
-    per_sm = std::max(1, std::min(per_sm, kEcgBlocksPerSm));
-    const long long need = (n + kEcgBlock - 1) / kEcgBlock;
-    ecg->blocks = int(std::max(1LL, std::min<long long>(need, (long long)std::max(sms, 1) * per_sm)));
+    const long long need = (n / 2 + kEcgBlock - 1) / kEcgBlock;
+    for (int e0 = 0; e0 < ecg->n_el; e0 += kEcgChunk) {
+        const int per_sm = std::max(1, std::min(resident_blocks_any(std::min(kEcgChunk,
+                                                                             ecg->n_el - e0)),
+                                                kEcgBlocksPerSm));
+        ecg->blocks.push_back(int(std::max(1LL, std::min<long long>(
+                                                    need, (long long)std::max(sms, 1) * per_sm))));
+    }
+    const int max_blocks = *std::max_element(ecg->blocks.begin(), ecg->blocks.end());
     auto bail = [&](int rc) {
         cfg_pseudo_ecg_destroy(ecg);
         return rc;
     };
     cudaError_t e = dmalloc(&ecg->d_lead, lead.size());
     if (!e) e = cudaMemcpy(ecg->d_lead, lead.data(), lead_bytes, cudaMemcpyHostToDevice);
-    if (!e) e = dmalloc(&ecg->d_partial, size_t(ecg->blocks) * size_t(ecg->n_el));
-    if (!e) e = dmalloc(&ecg->d_ticket, 1);
-    if (!e) e = cudaMemset(ecg->d_ticket, 0, sizeof(unsigned));
+    if (!e) e = dmalloc(&ecg->d_partial, size_t(max_blocks) * size_t(ecg->n_el));
+    const int chunks = (ecg->n_el + kEcgChunk - 1) / kEcgChunk;
+    if (!e) e = dmalloc(&ecg->d_ticket, size_t(chunks));
+    if (!e) e = cudaMemset(ecg->d_ticket, 0, sizeof(unsigned) * size_t(chunks));
     if (!e) e = dmalloc(&ecg->d_values, size_t(ecg->n_el));
     if (!e) e = cudaMallocHost(reinterpret_cast<void**>(&ecg->h_values),
                                size_t(ecg->n_el) * sizeof(double));
@@ -262,17 +371,26 @@ extern "C" int cfg_pseudo_ecg_compute_monodomain(cfg_pseudo_ecg* ecg, cfg_monodo
     return cfg_pseudo_ecg_compute(ecg, md->d_vm, md->stream, values);
 }
 
+extern "C" int cfg_pseudo_ecg_record_field(cfg_pseudo_ecg* ecg, const double* vm, void* stream,
+                                           double t)
+{
+    if (!ecg || !vm) return fail(CFG_ERR_INVALID, "null argument");
+    if (ecg->rows >= ecg->max_rows)
+        return fail(CFG_ERR_INVALID, "the pseudo-ECG series is full (%lld rows)", ecg->max_rows);
+    if (int rc = launch(ecg, vm, static_cast<cudaStream_t>(stream),
+                        ecg->d_series + ecg->rows * ecg->n_el))
+        return rc;
+    ecg->times.push_back(t);
+    ecg->rows++;
+    return CFG_OK;
+}
+
 extern "C" int cfg_pseudo_ecg_record(cfg_pseudo_ecg* ecg, cfg_monodomain* md)
 {
     if (!ecg || !md) return fail(CFG_ERR_INVALID, "null argument");
     if (md->n != ecg->n) return fail(CFG_ERR_INVALID, "the context has %lld cells, the ECG %lld",
                                      md->n, ecg->n);
-    if (ecg->rows >= ecg->max_rows)
-        return fail(CFG_ERR_INVALID, "the pseudo-ECG series is full (%lld rows)", ecg->max_rows);
-    if (int rc = launch(ecg, md->d_vm, md->stream, ecg->d_series + ecg->rows * ecg->n_el)) return rc;
-    ecg->times.push_back(md->t_host);
-    ecg->rows++;
-    return CFG_OK;
+    return cfg_pseudo_ecg_record_field(ecg, md->d_vm, md->stream, md->t_host);
 }
 
 extern "C" int cfg_pseudo_ecg_series(cfg_pseudo_ecg* ecg, double* times, double* values,

@@ -119,13 +119,13 @@ class SingleCellTrace:
 
 
 def ecg_header(names: Sequence[str]) -> str:
-    """ecgModelIO::openTimeSeries (ecgModelIO.C:30-50): '# time' and the
+    """ecgModelIO::openTimeSeries (ecgModelIO.C:30-52): '# time' and the
     electrode names, two spaces apart."""
     return "# time" + "".join("  " + n for n in names) + "\n"
 
 
 def ecg_row(t: float, values: Sequence[float]) -> str:
-    """ecgModelIO::writeRow (ecgModelIO.C:53-66) on the scientific,
+    """ecgModelIO::writeRow (ecgModelIO.C:55-68) on the scientific,
     precision-8 stream."""
     return f"{t:.8e}" + "".join(f"  {v:.8e}" for v in values) + "\n"
 
@@ -133,7 +133,7 @@ def ecg_row(t: float, values: Sequence[float]) -> str:
 def write_pseudo_ecg(case_dir, names: Sequence[str], times: Sequence[float], values,
                      file_name: str = "pseudoECG.dat") -> Path:
     """<case>/postProcessing/pseudoECG.dat with the given rows (ECGDomain
-    writes the rows of output times, ecgDomain.C:163-180)."""
+    writes the rows of output times, ecgDomain.C:167-190)."""
     out = Path(case_dir) / "postProcessing"
     out.mkdir(parents=True, exist_ok=True)
     path = out / file_name

@@ -143,7 +143,7 @@ EXPORTS = [
     "cfg_adjoint_backward", "cfg_adjoint_destroy", "cfg_ionic_autotune", "cfg_monodomain_autotune",
     "cfg_ionic_set_launch", "cfg_ionic_trace_header", "cfg_ionic_trace_row",
     "cfg_pseudo_ecg_create", "cfg_pseudo_ecg_compute", "cfg_pseudo_ecg_compute_monodomain",
-    "cfg_pseudo_ecg_record", "cfg_pseudo_ecg_series", "cfg_pseudo_ecg_reset",
+    "cfg_pseudo_ecg_record", "cfg_pseudo_ecg_record_field", "cfg_pseudo_ecg_series", "cfg_pseudo_ecg_reset",
     "cfg_pseudo_ecg_destroy", "cfg_pseudo_ecg_electrodes_from_dict",
 ]
 
@@ -224,6 +224,7 @@ def load(path: Optional[os.PathLike] = None):
     L.cfg_pseudo_ecg_compute.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, _dp]
     L.cfg_pseudo_ecg_compute_monodomain.argtypes = [C.c_void_p, C.c_void_p, _dp]
     L.cfg_pseudo_ecg_record.argtypes = [C.c_void_p, C.c_void_p]
+    L.cfg_pseudo_ecg_record_field.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double]
     L.cfg_pseudo_ecg_series.argtypes = [C.c_void_p, _dp, _dp, C.c_longlong,
                                         C.POINTER(C.c_longlong)]
     L.cfg_pseudo_ecg_reset.argtypes = [C.c_void_p]

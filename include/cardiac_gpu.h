@@ -395,7 +395,7 @@ int cfg_adjoint_backward(cfg_adjoint* adj, double* grad_log_gna, double* grad_lo
 int cfg_adjoint_destroy(cfg_adjoint* adj);
 
 /* ----------------------------------------------------------- pseudo-ECG
- * ECGDomain with the pseudoECG solver (ecgDomain.C:84-160,
+ * ECGDomain with the pseudoECG solver (ecgDomain.C:119-159,
  * pseudoECGSolver.C:34-87): at each electrode P
  *   phi(P) = sum over cells c of ((sigma_c & grad(Vm)_c) V_c) & r / |r|^3,
  *   r = C_c - P, cells with |r| <= VSMALL skipped,
@@ -425,11 +425,13 @@ int cfg_pseudo_ecg_create(const cfg_pseudo_ecg_desc* desc, const cfg_mesh_desc* 
 int cfg_pseudo_ecg_compute(cfg_pseudo_ecg* ecg, const double* vm, void* stream, double* values);
 /* The same for a monodomain context's Vm on its stream. */
 int cfg_pseudo_ecg_compute_monodomain(cfg_pseudo_ecg* ecg, cfg_monodomain* md, double* values);
-/* ECGDomain::evolve (ecgDomain.C:163-180) after a monodomain step: phi of
+/* ECGDomain::evolve (ecgDomain.C:167-190) after a monodomain step: phi of
  * the context's Vm appended to the device time series with the context's
  * time, enqueued on its stream without waiting (CFG_ERR_INVALID when the
  * series is full). */
 int cfg_pseudo_ecg_record(cfg_pseudo_ecg* ecg, cfg_monodomain* md);
+/* The same for a device field vm [n_cells] at time t, enqueued on stream. */
+int cfg_pseudo_ecg_record_field(cfg_pseudo_ecg* ecg, const double* vm, void* stream, double t);
 /* The recorded rows: times [rows], values [rows][n_electrodes] (host; up to
  * max_rows of them); *n_rows the number recorded.  reset empties the series. */
 int cfg_pseudo_ecg_series(cfg_pseudo_ecg* ecg, double* times, double* values,
@@ -439,7 +441,7 @@ int cfg_pseudo_ecg_destroy(cfg_pseudo_ecg* ecg);
 
 /* Electrodes of an ecgDomains entry of constant/electroProperties
  * (<type>Coeffs.ecgDomains.<domain>: ecgSolver pseudoECG; electrodePositions
- * { name (x y z); ... }, ecgDomain.C:45-80): names space-separated into
+ * { name (x y z); ... }, ecgDomain.C:53-82): names space-separated into
  * names[len] in the dictionary's order, positions into [max][3].  domain
  * NULL or "" takes the first ecgDomains entry.  An ecgSolver other than
  * pseudoECG is CFG_ERR_UNSUPPORTED. */

@@ -122,10 +122,12 @@ def test_manufactured_run_records_the_ecg(gpu_lib):
 
 @pytest.mark.gpu
 def test_many_electrodes_and_a_centre_electrode(gpu_lib, oracle):
-    """19 electrodes (three passes of the kernel's electrode chunk), one of
-    them exactly on a cell centre (that cell is skipped)."""
+    """19 electrodes (three launches of up to 8), one of them exactly on a
+    cell centre (that cell is skipped), an odd cell count (the tail of the
+    paired loads) and a misaligned Vm."""
     torch = pytest.importorskip("torch")
-    m = V.geometry_mesh_for(3, 12)
+    m = V.geometry_mesh_for(3, 11)
+    assert m.n_cells % 2 == 1
     rng = np.random.default_rng(8)
     el = np.vstack([m.centres[[5, 300]], rng.uniform(-1.0, 2.0, (17, 3))])
     vm = rng.standard_normal(m.n_cells) * 0.02 - 0.08
@@ -138,6 +140,11 @@ def test_many_electrodes_and_a_centre_electrode(gpu_lib, oracle):
     o.set_conductivity(np.tile(np.asarray(V.SIGMA), (m.n_cells, 1)))
     want = o.pseudo_ecg(vm, el)
     assert np.all(np.abs(got - want) <= 1e-10 * np.abs(want).max())
+    # Vm at an address that is not 16-byte aligned: the one-cell-per-load path
+    xs = torch.tensor(np.r_[0.0, vm], device="cuda")[1:]
+    assert xs.data_ptr() % 16 == 8
+    got1 = pe.compute(xs)
+    assert np.all(np.abs(got1 - want) <= 1e-10 * np.abs(want).max())
     pe.close()
 
 
