@@ -257,6 +257,17 @@ LV_INTENSITY = 5e4       # A/m^3, for 2 ms
 
 
 def ecg_timing(L, source, launches: int = 50):
+    """Both arithmetic forms of the pseudo-ECG (float pairs, the default, and
+    FP64 multiply-adds), each timed as below."""
+    from cardiacfoam_gb300 import lib
+    out = {"float_pairs": ecg_timing_one(L, source, launches, lib.ECG_FLOAT_PAIRS),
+           "fp64": ecg_timing_one(L, source, launches, lib.ECG_FP64)}
+    a, b = out["float_pairs"].pop("_values"), out["fp64"].pop("_values")
+    out["pairs_vs_fp64_max_rel"] = float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
+    return out
+
+
+def ecg_timing_one(L, source, launches: int, arithmetic):
     """The pseudo-ECG at the LV's five electrodes (PseudoECGSolver::compute,
     folded into one lead row per electrode): `launches` evaluations recorded
     back to back between CUDA events on the stream they run on (a
@@ -267,7 +278,8 @@ def ecg_timing(L, source, launches: int = 50):
     from cardiacfoam_gb300 import api
     el = L.ecg_electrodes()
     t0 = time.perf_counter()
-    pe = api.PseudoECG(L.mesh, el, conductivity_per_cell=L.conductivity, max_rows=launches + 3)
+    pe = api.PseudoECG(L.mesh, el, conductivity_per_cell=L.conductivity, max_rows=launches + 3,
+                       arithmetic=arithmetic)
     t_setup = time.perf_counter() - t0
     if isinstance(source, api.Monodomain):
         s = torch.cuda.ExternalStream(source.stream())
@@ -295,7 +307,7 @@ def ecg_timing(L, source, launches: int = 50):
             "us_per_evaluation": ms * 1e3, "bytes_per_evaluation": nbytes,
             "achieved_gbs": gbs, "hbm_peak_gbs": peak, "peak_src": src,
             "frac_of_hbm_peak": gbs / peak,
-            "values_at_t": [float(v) for v in values[-1]]}
+            "values_at_t": [float(v) for v in values[-1]], "_values": values[-1]}
 
 
 def ecg_arm(args):

@@ -457,11 +457,15 @@ class PseudoECG:
     The mesh needs its full geometry (LduMesh.has_geometry); conductivity is
     the monodomain's (uniform or per cell) and grad_scheme its gradSchemes
     default.  ``record`` after each step keeps the time series on the device
-    (up to ``max_rows`` rows) without waiting for the GPU."""
+    (up to ``max_rows`` rows) without waiting for the GPU.  ``arithmetic``:
+    ECG_FLOAT_PAIRS (default; 48-bit significands on the FP32 pipe, within
+    1e-12 of the FP64 sum relative to the largest electrode value on the
+    tests' fields) or ECG_FP64 (bound by GB300's FP64 pipe)."""
 
     def __init__(self, mesh: LduMesh, electrodes, names: Optional[Sequence[str]] = None,
                  sigma=(0.1334, 0.0, 0.0, 0.0176, 0.0, 0.0176), conductivity_per_cell=None,
-                 grad_scheme=_L.GRAD_LEAST_SQUARES, max_rows: int = 0):
+                 grad_scheme=_L.GRAD_LEAST_SQUARES, max_rows: int = 0,
+                 arithmetic=_L.ECG_FLOAT_PAIRS):
         self._lib = _L.load()
         if not mesh.has_geometry:
             raise ValueError("the pseudo-ECG needs a mesh with its full geometry")
@@ -487,6 +491,7 @@ class PseudoECG:
         d.n_electrodes = self.n_electrodes
         d.electrodes = _L.dptr(self.electrodes)
         d.max_rows = self.max_rows
+        d.arithmetic = int(arithmetic)
         md, keep2 = mesh_desc(mesh, structured=False)
         h = C.c_void_p()
         _L.check(self._lib.cfg_pseudo_ecg_create(C.byref(d), C.byref(md), C.byref(h)))

@@ -18,6 +18,7 @@
 #include <cstdint>
 #include <cstring>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "geometry.h"
@@ -31,9 +32,10 @@ constexpr int kEcgChunk = 8;      // electrodes of one launch
 constexpr int kEcgBlocksPerSm = 8;
 
 struct EcgArgs {
-    const double* lead;   // [n_el][ld], rows padded with zeros to an even length
+    const void* lead;     // [n_el][ld] doubles, or (hi, lo) float pairs of the scaled rows
+    const double* scale;  // pairs: the power of two each row was scaled by
     const double* vm;     // [n]
-    long long n, ld;
+    long long n, ld;      // rows padded with zeros to an even length
     int n_el, e0;         // all electrodes; the first of this launch
     double* partial;      // [gridDim.x][n_el]
     unsigned* ticket;     // this launch's
@@ -47,59 +49,149 @@ __device__ __forceinline__ double warp_sum(double v)
     return v;
 }
 
+// v = hi + lo with |v - hi - lo| <= 2^-48 |v|: hi takes the leading 24
+// significant bits of the double (truncated), lo the remaining 29 rounded to
+// 24, both assembled from the bit pattern with integer operations (the FP64
+// pipe is not used).  |v| below 2^-126 reads as zero, beyond the float range
+// as the rounded float.
+__device__ __forceinline__ void split_fp64(double v, float& hi, float& lo)
+{
+    const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(v));
+    const unsigned hw = unsigned(b >> 32), lw = unsigned(b);
+    const unsigned sign = hw & 0x80000000u;
+    const int e = int((hw >> 20) & 0x7ffu);
+    const int ef = e - 896;                // biased float exponent of 2^(e - 1023)
+    if (ef <= 0) {
+        hi = lo = 0.0f;
+        return;
+    }
+    if (ef >= 255) {
+        hi = __double2float_rn(v);
+        lo = 0.0f;
+        return;
+    }
+    hi = __uint_as_float(sign | (unsigned(ef) << 23) | ((hw & 0xfffffu) << 3) | (lw >> 29));
+    const int es = e - 948;                // biased float exponent of 2^(e - 1075)
+    const float rem = es > 0 ? __fmul_rn(__uint2float_rn(lw & 0x1fffffffu),
+                                         __uint_as_float(unsigned(es) << 23))
+                             : 0.0f;
+    lo = __uint_as_float(__float_as_uint(rem) | sign);
+}
+
+// Accumulators: FP64 multiply-add, or a float pair (ch + cl) fed by the
+// error-free product of two float pairs (Dekker's product with fmaf for the
+// rounding error, the low-order cross terms added into it) and Knuth's
+// two-sum; the rounded operations are the _rn intrinsics so that no
+// multiply-add contraction changes them.
+template <bool PAIR>
+struct Acc;
+
+template <>
+struct Acc<false> {
+    double a = 0.0;
+    __device__ __forceinline__ void add(double l, double v) { a = fma(l, v, a); }
+    __device__ __forceinline__ double value() const { return a; }
+};
+
+template <>
+struct Acc<true> {
+    float h = 0.0f, l = 0.0f;
+    __device__ __forceinline__ void add(float2 a, float bh, float bl)
+    {
+        const float p = __fmul_rn(a.x, bh);
+        float e = fmaf(a.x, bh, -p);
+        e = fmaf(a.x, bl, e);
+        e = fmaf(a.y, bh, e);
+        const float s = __fadd_rn(h, p);
+        const float z = __fsub_rn(s, h);
+        const float t = __fadd_rn(__fsub_rn(h, __fsub_rn(s, z)), __fsub_rn(p, z));
+        l = __fadd_rn(l, __fadd_rn(t, e));
+        h = s;
+    }
+    __device__ __forceinline__ void renormalize()
+    {
+        const float s = __fadd_rn(h, l);
+        l = __fsub_rn(l, __fsub_rn(s, h));
+        h = s;
+    }
+    __device__ __forceinline__ double value() const { return double(h) + double(l); }
+};
+
 // phi_e += L[e][c] Vm_c for the NE electrodes from e0 over a grid-stride
 // loop; VEC: two cells per 16-byte load (Vm 16-byte aligned), two strides
-// per trip with every load issued before the first multiply-add.
-template <int NE, bool VEC>
+// per trip with every load issued before the first multiply-add; PAIR: the
+// float-pair arithmetic on the scaled rows.
+template <int NE, bool VEC, bool PAIR>
 __global__ void __launch_bounds__(kEcgBlock) k_pseudo_ecg(EcgArgs a)
 {
     __shared__ double red[kEcgBlock / 32][NE];
     __shared__ bool last;
+    using Entry = typename std::conditional<PAIR, float2, double>::type;
+    using Entry2 = typename std::conditional<PAIR, float4, double2>::type;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const double* lead = a.lead + (long long)a.e0 * a.ld;
+    const Entry* lead = static_cast<const Entry*>(a.lead) + (long long)a.e0 * a.ld;
     const long long stride = (long long)gridDim.x * kEcgBlock;
     long long i = (long long)blockIdx.x * kEcgBlock + threadIdx.x;
-    double acc[NE];
+    Acc<PAIR> acc[NE];
+    // one cell: entry l of a row, Vm value v
+    auto term = [&](int j, Entry l, double v) {
+        if constexpr (PAIR) {
+            float vh, vl;
+            split_fp64(v, vh, vl);
+            acc[j].add(l, vh, vl);
+        } else {
+            acc[j].add(l, v);
+        }
+    };
+    auto term2 = [&](int j, Entry2 l, double2 v) {
+        if constexpr (PAIR) {
+            term(j, make_float2(l.x, l.y), v.x);
+            term(j, make_float2(l.z, l.w), v.y);
+        } else {
+            term(j, l.x, v.x);
+            term(j, l.y, v.y);
+        }
+    };
+    auto renormalize = [&]() {
+        if constexpr (PAIR) {
 #pragma unroll
-    for (int j = 0; j < NE; ++j) acc[j] = 0.0;
+            for (int j = 0; j < NE; ++j) acc[j].renormalize();
+        }
+    };
     if (VEC) {
         const long long nv = a.n >> 1;
         const double2* v2 = reinterpret_cast<const double2*>(a.vm);
         for (; i + stride < nv; i += 2 * stride) {
             const double2 x0 = __ldcs(v2 + i), x1 = __ldcs(v2 + i + stride);
-            double2 l0[NE], l1[NE];
+            Entry2 l0[NE], l1[NE];
 #pragma unroll
             for (int j = 0; j < NE; ++j) {
-                const double2* row = reinterpret_cast<const double2*>(lead + j * a.ld);
+                const Entry2* row = reinterpret_cast<const Entry2*>(lead + j * a.ld);
                 l0[j] = __ldcs(row + i);
                 l1[j] = __ldcs(row + i + stride);
             }
 #pragma unroll
             for (int j = 0; j < NE; ++j) {
-                acc[j] = fma(l0[j].x, x0.x, acc[j]);
-                acc[j] = fma(l0[j].y, x0.y, acc[j]);
-                acc[j] = fma(l1[j].x, x1.x, acc[j]);
-                acc[j] = fma(l1[j].y, x1.y, acc[j]);
+                term2(j, l0[j], x0);
+                term2(j, l1[j], x1);
             }
+            renormalize();
         }
         if (i < nv) {
             const double2 x0 = __ldcs(v2 + i);
 #pragma unroll
-            for (int j = 0; j < NE; ++j) {
-                const double2 l0 = __ldcs(reinterpret_cast<const double2*>(lead + j * a.ld) + i);
-                acc[j] = fma(l0.x, x0.x, acc[j]);
-                acc[j] = fma(l0.y, x0.y, acc[j]);
-            }
+            for (int j = 0; j < NE; ++j)
+                term2(j, __ldcs(reinterpret_cast<const Entry2*>(lead + j * a.ld) + i), x0);
         }
         if ((a.n & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
             const long long c = a.n - 1;
 #pragma unroll
-            for (int j = 0; j < NE; ++j) acc[j] = fma(lead[j * a.ld + c], a.vm[c], acc[j]);
+            for (int j = 0; j < NE; ++j) term(j, lead[j * a.ld + c], a.vm[c]);
         }
     } else {
         for (; i + stride < a.n; i += 2 * stride) {
             const double x0 = __ldcs(a.vm + i), x1 = __ldcs(a.vm + i + stride);
-            double l0[NE], l1[NE];
+            Entry l0[NE], l1[NE];
 #pragma unroll
             for (int j = 0; j < NE; ++j) {
                 l0[j] = __ldcs(lead + j * a.ld + i);
@@ -107,21 +199,23 @@ __global__ void __launch_bounds__(kEcgBlock) k_pseudo_ecg(EcgArgs a)
             }
 #pragma unroll
             for (int j = 0; j < NE; ++j) {
-                acc[j] = fma(l0[j], x0, acc[j]);
-                acc[j] = fma(l1[j], x1, acc[j]);
+                term(j, l0[j], x0);
+                term(j, l1[j], x1);
             }
+            renormalize();
         }
         if (i < a.n) {
             const double x0 = __ldcs(a.vm + i);
 #pragma unroll
-            for (int j = 0; j < NE; ++j) acc[j] = fma(__ldcs(lead + j * a.ld + i), x0, acc[j]);
+            for (int j = 0; j < NE; ++j) term(j, __ldcs(lead + j * a.ld + i), x0);
         }
     }
+    double sum[NE];
 #pragma unroll
-    for (int j = 0; j < NE; ++j) acc[j] = warp_sum(acc[j]);
+    for (int j = 0; j < NE; ++j) sum[j] = warp_sum(acc[j].value());
     if (lane == 0)
 #pragma unroll
-        for (int j = 0; j < NE; ++j) red[warp][j] = acc[j];
+        for (int j = 0; j < NE; ++j) red[warp][j] = sum[j];
     __syncthreads();
     if (threadIdx.x < NE) {
         double s = 0.0;
@@ -141,51 +235,61 @@ __global__ void __launch_bounds__(kEcgBlock) k_pseudo_ecg(EcgArgs a)
         for (int b = lane; b < (int)gridDim.x; b += 32)
             s += __ldcg(&a.partial[(long long)b * a.n_el + a.e0 + e]);
         s = warp_sum(s);
-        if (lane == 0) a.out[a.e0 + e] = s;
+        if (lane == 0) a.out[a.e0 + e] = PAIR ? s / a.scale[a.e0 + e] : s;
     }
     if (threadIdx.x == 0) *a.ticket = 0u;
 }
 
 template <int NE>
-void launch_chunk(const EcgArgs& a, bool vec, int blocks, cudaStream_t s)
+void launch_chunk(const EcgArgs& a, bool vec, bool pair, int blocks, cudaStream_t s)
 {
-    if (vec) k_pseudo_ecg<NE, true><<<blocks, kEcgBlock, 0, s>>>(a);
-    else k_pseudo_ecg<NE, false><<<blocks, kEcgBlock, 0, s>>>(a);
-}
-
-template <int NE>
-int resident_blocks()
-{
-    int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pseudo_ecg<NE, true>, kEcgBlock, 0);
-    return per_sm;
-}
-
-int resident_blocks_any(int ne)
-{
-    switch (ne) {
-    case 1: return resident_blocks<1>();
-    case 2: return resident_blocks<2>();
-    case 3: return resident_blocks<3>();
-    case 4: return resident_blocks<4>();
-    case 5: return resident_blocks<5>();
-    case 6: return resident_blocks<6>();
-    case 7: return resident_blocks<7>();
-    default: return resident_blocks<8>();
+    if (pair) {
+        if (vec) k_pseudo_ecg<NE, true, true><<<blocks, kEcgBlock, 0, s>>>(a);
+        else k_pseudo_ecg<NE, false, true><<<blocks, kEcgBlock, 0, s>>>(a);
+    } else {
+        if (vec) k_pseudo_ecg<NE, true, false><<<blocks, kEcgBlock, 0, s>>>(a);
+        else k_pseudo_ecg<NE, false, false><<<blocks, kEcgBlock, 0, s>>>(a);
     }
 }
 
-void launch_any(const EcgArgs& a, int ne, bool vec, int blocks, cudaStream_t s)
+template <int NE>
+int resident_blocks(bool pair)
+{
+    int per_sm = 0;
+    if (pair)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pseudo_ecg<NE, true, true>,
+                                                      kEcgBlock, 0);
+    else
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pseudo_ecg<NE, true, false>,
+                                                      kEcgBlock, 0);
+    return per_sm;
+}
+
+int resident_blocks_any(int ne, bool pair)
 {
     switch (ne) {
-    case 1: launch_chunk<1>(a, vec, blocks, s); break;
-    case 2: launch_chunk<2>(a, vec, blocks, s); break;
-    case 3: launch_chunk<3>(a, vec, blocks, s); break;
-    case 4: launch_chunk<4>(a, vec, blocks, s); break;
-    case 5: launch_chunk<5>(a, vec, blocks, s); break;
-    case 6: launch_chunk<6>(a, vec, blocks, s); break;
-    case 7: launch_chunk<7>(a, vec, blocks, s); break;
-    default: launch_chunk<8>(a, vec, blocks, s); break;
+    case 1: return resident_blocks<1>(pair);
+    case 2: return resident_blocks<2>(pair);
+    case 3: return resident_blocks<3>(pair);
+    case 4: return resident_blocks<4>(pair);
+    case 5: return resident_blocks<5>(pair);
+    case 6: return resident_blocks<6>(pair);
+    case 7: return resident_blocks<7>(pair);
+    default: return resident_blocks<8>(pair);
+    }
+}
+
+void launch_any(const EcgArgs& a, int ne, bool vec, bool pair, int blocks, cudaStream_t s)
+{
+    switch (ne) {
+    case 1: launch_chunk<1>(a, vec, pair, blocks, s); break;
+    case 2: launch_chunk<2>(a, vec, pair, blocks, s); break;
+    case 3: launch_chunk<3>(a, vec, pair, blocks, s); break;
+    case 4: launch_chunk<4>(a, vec, pair, blocks, s); break;
+    case 5: launch_chunk<5>(a, vec, pair, blocks, s); break;
+    case 6: launch_chunk<6>(a, vec, pair, blocks, s); break;
+    case 7: launch_chunk<7>(a, vec, pair, blocks, s); break;
+    default: launch_chunk<8>(a, vec, pair, blocks, s); break;
     }
 }
 
@@ -195,7 +299,9 @@ struct cfg_pseudo_ecg {
     long long n = 0, ld = 0;
     int n_el = 0;
     std::vector<int> blocks;        // grid of each launch
-    double* d_lead = nullptr;
+    bool pair = false;              // float-pair arithmetic on scaled rows
+    void* d_lead = nullptr;         // [n_el][ld] doubles or float pairs
+    double* d_scale = nullptr;      // [n_el] row scales (pairs)
     double* d_partial = nullptr;
     unsigned* d_ticket = nullptr;   // one per launch of kEcgChunk electrodes
     double* d_values = nullptr;     // compute()
@@ -266,9 +372,10 @@ int launch(cfg_pseudo_ecg* ecg, const double* vm, cudaStream_t s, double* out)
         CFG_CUDA_TRY(cudaStreamSynchronize(ecg->last_stream));
     const bool vec = (reinterpret_cast<uintptr_t>(vm) & 15) == 0;
     for (int e0 = 0, k = 0; e0 < ecg->n_el; e0 += kEcgChunk, ++k) {
-        EcgArgs a{ecg->d_lead, vm, ecg->n, ecg->ld, ecg->n_el, e0, ecg->d_partial,
-                  ecg->d_ticket + k, out};
-        launch_any(a, std::min(kEcgChunk, ecg->n_el - e0), vec, ecg->blocks[size_t(k)], s);
+        EcgArgs a{ecg->d_lead, ecg->d_scale, vm, ecg->n, ecg->ld, ecg->n_el, e0,
+                  ecg->d_partial, ecg->d_ticket + k, out};
+        launch_any(a, std::min(kEcgChunk, ecg->n_el - e0), vec, ecg->pair,
+                   ecg->blocks[size_t(k)], s);
         CFG_CUDA_TRY(cudaGetLastError());
     }
     ecg->last_stream = s;
@@ -291,6 +398,8 @@ extern "C" int cfg_pseudo_ecg_create(const cfg_pseudo_ecg_desc* d, const cfg_mes
     if (d->max_rows < 0) return fail(CFG_ERR_INVALID, "max_rows must be non-negative");
     if (d->grad_scheme != CFG_GRAD_LEAST_SQUARES && d->grad_scheme != CFG_GRAD_GAUSS_LINEAR)
         return fail(CFG_ERR_INVALID, "unknown gradient scheme %d", d->grad_scheme);
+    if (d->arithmetic != CFG_ECG_FP64 && d->arithmetic != CFG_ECG_FLOAT_PAIRS)
+        return fail(CFG_ERR_INVALID, "unknown arithmetic %d", d->arithmetic);
     const long long n = m->n_cells;
     for (long long f = 0; f < m->n_faces; ++f) {
         const int l = m->owner[f], u = m->neighbour[f];
@@ -315,6 +424,7 @@ extern "C" int cfg_pseudo_ecg_create(const cfg_pseudo_ecg_desc* d, const cfg_mes
     ecg->n = n;
     ecg->ld = ld;
     ecg->n_el = d->n_electrodes;
+    ecg->pair = d->arithmetic == CFG_ECG_FLOAT_PAIRS;
     // per launch one wave of resident blocks, grid-striding over the cells
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
@@ -322,7 +432,8 @@ extern "C" int cfg_pseudo_ecg_create(const cfg_pseudo_ecg_desc* d, const cfg_mes
     const long long need = (n / 2 + kEcgBlock - 1) / kEcgBlock;
     for (int e0 = 0; e0 < ecg->n_el; e0 += kEcgChunk) {
         const int per_sm = std::max(1, std::min(resident_blocks_any(std::min(kEcgChunk,
-                                                                             ecg->n_el - e0)),
+                                                                             ecg->n_el - e0),
+                                                                    ecg->pair),
                                                 kEcgBlocksPerSm));
         ecg->blocks.push_back(int(std::max(1LL, std::min<long long>(
                                                     need, (long long)std::max(sms, 1) * per_sm))));
@@ -332,8 +443,33 @@ extern "C" int cfg_pseudo_ecg_create(const cfg_pseudo_ecg_desc* d, const cfg_mes
         cfg_pseudo_ecg_destroy(ecg);
         return rc;
     };
-    cudaError_t e = dmalloc(&ecg->d_lead, lead.size());
-    if (!e) e = cudaMemcpy(ecg->d_lead, lead.data(), lead_bytes, cudaMemcpyHostToDevice);
+    cudaError_t e = cudaMalloc(&ecg->d_lead, lead_bytes);
+    if (!e && ecg->pair) {
+        // each row scaled by a power of two to a largest magnitude in [0.5, 1)
+        // (exact), then split into the nearest float and the float nearest
+        // to the rest
+        std::vector<float2> pairs(lead.size());
+        std::vector<double> scale(size_t(ecg->n_el), 1.0);
+        for (int r = 0; r < ecg->n_el; ++r) {
+            const double* row = lead.data() + size_t(r) * size_t(ld);
+            double mx = 0.0;
+            for (long long c = 0; c < ld; ++c) mx = std::max(mx, std::fabs(row[c]));
+            int ex = 0;
+            if (mx > 0.0) std::frexp(mx, &ex);
+            scale[size_t(r)] = std::ldexp(1.0, -ex);
+            for (long long c = 0; c < ld; ++c) {
+                const double v = row[c] * scale[size_t(r)];
+                const float h = float(v);
+                pairs[size_t(r) * size_t(ld) + size_t(c)] = make_float2(h, float(v - double(h)));
+            }
+        }
+        e = cudaMemcpy(ecg->d_lead, pairs.data(), lead_bytes, cudaMemcpyHostToDevice);
+        if (!e) e = dmalloc(&ecg->d_scale, scale.size());
+        if (!e) e = cudaMemcpy(ecg->d_scale, scale.data(), scale.size() * sizeof(double),
+                               cudaMemcpyHostToDevice);
+    } else if (!e) {
+        e = cudaMemcpy(ecg->d_lead, lead.data(), lead_bytes, cudaMemcpyHostToDevice);
+    }
     if (!e) e = dmalloc(&ecg->d_partial, size_t(max_blocks) * size_t(ecg->n_el));
     const int chunks = (ecg->n_el + kEcgChunk - 1) / kEcgChunk;
     if (!e) e = dmalloc(&ecg->d_ticket, size_t(chunks));
@@ -420,7 +556,8 @@ extern "C" int cfg_pseudo_ecg_destroy(cfg_pseudo_ecg* ecg)
 {
     if (!ecg) return CFG_OK;
     if (ecg->launched) cudaStreamSynchronize(ecg->last_stream);
-    dfree(ecg->d_lead);
+    if (ecg->d_lead) cudaFree(ecg->d_lead);
+    dfree(ecg->d_scale);
     dfree(ecg->d_partial);
     dfree(ecg->d_ticket);
     dfree(ecg->d_values);

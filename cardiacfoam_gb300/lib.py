@@ -59,6 +59,7 @@ class IonicDesc(C.Structure):
 
 
 GRAD_LEAST_SQUARES, GRAD_GAUSS_LINEAR = 0, 1
+ECG_FP64, ECG_FLOAT_PAIRS = 0, 1
 
 
 class MeshDesc(C.Structure):
@@ -125,7 +126,7 @@ class AdjointDesc(C.Structure):
 class PseudoEcgDesc(C.Structure):
     _fields_ = [("conductivity", C.c_double * 6), ("conductivity_per_cell", _dp),
                 ("grad_scheme", C.c_int), ("n_electrodes", C.c_int), ("electrodes", _dp),
-                ("max_rows", C.c_longlong)]
+                ("max_rows", C.c_longlong), ("arithmetic", C.c_int)]
 
 
 EXPORTS = [

@@ -406,6 +406,11 @@ int cfg_adjoint_destroy(cfg_adjoint* adj);
  * of n_cells coefficients per electrode (8 bytes per cell and electrode in
  * device memory) and every evaluation is one pass over those rows and Vm.
  * The mesh needs its full geometry (face_centres, walls). */
+#define CFG_ECG_FP64 0          /* FP64 multiply-add per cell and electrode */
+#define CFG_ECG_FLOAT_PAIRS 1   /* float pairs: rows and Vm each carried to 48
+                                   significant bits, error-free products and
+                                   two-sum accumulation on the FP32 pipe; same
+                                   bytes, a sixth of the FP64 operations' time */
 typedef struct cfg_pseudo_ecg_desc {
     double conductivity[6];              /* xx xy xz yy yz zz, used when ... */
     const double* conductivity_per_cell; /* ... this is NULL; else host [n_cells][6] */
@@ -413,6 +418,7 @@ typedef struct cfg_pseudo_ecg_desc {
     int n_electrodes;
     const double* electrodes;            /* host [n_electrodes][3] positions [m] */
     long long max_rows;                  /* rows of the device time series (0: none) */
+    int arithmetic;                      /* CFG_ECG_* */
 } cfg_pseudo_ecg_desc;
 
 typedef struct cfg_pseudo_ecg cfg_pseudo_ecg;

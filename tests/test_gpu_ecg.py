@@ -27,17 +27,23 @@ def _tol(ref):
     return 1e-10 * np.max(np.abs(ref))
 
 
+ARITHMETIC = pytest.mark.parametrize("arith", [lib.ECG_FLOAT_PAIRS, lib.ECG_FP64],
+                                     ids=["float-pairs", "fp64"])
+
+
 @pytest.mark.gpu
+@ARITHMETIC
 @pytest.mark.parametrize("grad", [lib.GRAD_LEAST_SQUARES, lib.GRAD_GAUSS_LINEAR],
                          ids=["least-squares", "gauss-linear"])
-def test_lv_matches_oracle(gpu_lib, oracle, small_lv, grad):
+def test_lv_matches_oracle(gpu_lib, oracle, small_lv, grad, arith):
     L = small_lv
     lo, hi = L.apex_box(8e-3)
     md = api.Monodomain(L.mesh, "TNNP", "epicardialCells", dt=DT, boxes=[(lo, hi, 0.0, 2e-3, 5e4)],
                         tissue_per_cell=L.tissue, conductivity_per_cell=L.conductivity,
                         grad_scheme=grad, stencil=False)
     el = _lv_electrodes(L)
-    pe = api.PseudoECG(L.mesh, el, conductivity_per_cell=L.conductivity, grad_scheme=grad)
+    pe = api.PseudoECG(L.mesh, el, conductivity_per_cell=L.conductivity, grad_scheme=grad,
+                       arithmetic=arith)
     d = oracle.tissue_desc("TNNP", 1, grad_gauss=grad == lib.GRAD_GAUSS_LINEAR)
     o = oracle.Tissue(d, oracle.Mesh.general(L.mesh))
     o.set_conductivity(L.conductivity)
@@ -121,7 +127,8 @@ def test_manufactured_run_records_the_ecg(gpu_lib):
 
 
 @pytest.mark.gpu
-def test_many_electrodes_and_a_centre_electrode(gpu_lib, oracle):
+@ARITHMETIC
+def test_many_electrodes_and_a_centre_electrode(gpu_lib, oracle, arith):
     """19 electrodes (three launches of up to 8), one of them exactly on a
     cell centre (that cell is skipped), an odd cell count (the tail of the
     paired loads) and a misaligned Vm."""
@@ -131,7 +138,7 @@ def test_many_electrodes_and_a_centre_electrode(gpu_lib, oracle):
     rng = np.random.default_rng(8)
     el = np.vstack([m.centres[[5, 300]], rng.uniform(-1.0, 2.0, (17, 3))])
     vm = rng.standard_normal(m.n_cells) * 0.02 - 0.08
-    pe = api.PseudoECG(m, el, sigma=V.SIGMA, grad_scheme=lib.GRAD_GAUSS_LINEAR)
+    pe = api.PseudoECG(m, el, sigma=V.SIGMA, grad_scheme=lib.GRAD_GAUSS_LINEAR, arithmetic=arith)
     x = torch.tensor(vm, device="cuda")
     got = pe.compute(x)
     assert np.array_equal(got, pe.compute(x))
@@ -164,3 +171,28 @@ def test_invalid_arguments(gpu_lib, small_lv):
         pe.compute(md)                                        # other cell count
     md.close()
     pe.close()
+
+
+@pytest.mark.gpu
+def test_float_pairs_against_fp64(gpu_lib, small_lv):
+    """The two arithmetic forms on the same Vm: within 1e-12 of the largest
+    electrode value, including a Vm with exact zeros and a uniform Vm (whose
+    pseudo-ECG vanishes up to the rows' round-off)."""
+    torch = pytest.importorskip("torch")
+    L = small_lv
+    el = _lv_electrodes(L)
+    a = api.PseudoECG(L.mesh, el, conductivity_per_cell=L.conductivity,
+                      arithmetic=lib.ECG_FLOAT_PAIRS)
+    b = api.PseudoECG(L.mesh, el, conductivity_per_cell=L.conductivity, arithmetic=lib.ECG_FP64)
+    rng = np.random.default_rng(3)
+    vm = -0.084 + 0.12 * (L.mesh.centres[:, 2] > -0.03) + 1e-3 * rng.standard_normal(L.mesh.n_cells)
+    vm[::7] = 0.0
+    x = torch.tensor(vm, device="cuda")
+    pa, pb = a.compute(x), b.compute(x)
+    assert np.max(np.abs(pa - pb)) <= 1e-12 * np.max(np.abs(pb))
+    flat = torch.full((L.mesh.n_cells,), -0.084, dtype=torch.float64, device="cuda")
+    scale = np.max(np.abs(pb))
+    assert np.max(np.abs(a.compute(flat))) <= 1e-12 * scale
+    assert np.max(np.abs(b.compute(flat))) <= 1e-12 * scale
+    a.close()
+    b.close()
