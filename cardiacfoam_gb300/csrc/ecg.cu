@@ -91,6 +91,12 @@ struct Acc<false> {
     double a = 0.0;
     __device__ __forceinline__ void add(double l, double v) { a = fma(l, v, a); }
     __device__ __forceinline__ double value() const { return a; }
+    static __device__ __forceinline__ Acc nan()
+    {
+        Acc r;
+        r.a = __longlong_as_double(0x7ff8000000000000LL);
+        return r;
+    }
 };
 
 template <>
@@ -115,101 +121,22 @@ struct Acc<true> {
         h = s;
     }
     __device__ __forceinline__ double value() const { return double(h) + double(l); }
+    static __device__ __forceinline__ Acc nan()
+    {
+        Acc r;
+        r.h = __uint_as_float(0x7fc00000u);
+        return r;
+    }
 };
 
-// phi_e += L[e][c] Vm_c for the NE electrodes from e0 over a grid-stride
-// loop; VEC: two cells per 16-byte load (Vm 16-byte aligned), two strides
-// per trip with every load issued before the first multiply-add; PAIR: the
-// float-pair arithmetic on the scaled rows.
-template <int NE, bool VEC, bool PAIR>
-__global__ void __launch_bounds__(kEcgBlock) k_pseudo_ecg(EcgArgs a)
+// Adds the block's sums to the partial sums and, in the last block to
+// finish, the blocks' sums in block order into out (divided by the row
+// scale for pairs).
+template <int NE, bool PAIR>
+__device__ __forceinline__ void finish(const EcgArgs& a, const Acc<PAIR> (&acc)[NE],
+                                       double (&red)[kEcgBlock / 32][NE], bool& last)
 {
-    __shared__ double red[kEcgBlock / 32][NE];
-    __shared__ bool last;
-    using Entry = typename std::conditional<PAIR, float2, double>::type;
-    using Entry2 = typename std::conditional<PAIR, float4, double2>::type;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const Entry* lead = static_cast<const Entry*>(a.lead) + (long long)a.e0 * a.ld;
-    const long long stride = (long long)gridDim.x * kEcgBlock;
-    long long i = (long long)blockIdx.x * kEcgBlock + threadIdx.x;
-    Acc<PAIR> acc[NE];
-    // one cell: entry l of a row, Vm value v
-    auto term = [&](int j, Entry l, double v) {
-        if constexpr (PAIR) {
-            float vh, vl;
-            split_fp64(v, vh, vl);
-            acc[j].add(l, vh, vl);
-        } else {
-            acc[j].add(l, v);
-        }
-    };
-    auto term2 = [&](int j, Entry2 l, double2 v) {
-        if constexpr (PAIR) {
-            term(j, make_float2(l.x, l.y), v.x);
-            term(j, make_float2(l.z, l.w), v.y);
-        } else {
-            term(j, l.x, v.x);
-            term(j, l.y, v.y);
-        }
-    };
-    auto renormalize = [&]() {
-        if constexpr (PAIR) {
-#pragma unroll
-            for (int j = 0; j < NE; ++j) acc[j].renormalize();
-        }
-    };
-    if (VEC) {
-        const long long nv = a.n >> 1;
-        const double2* v2 = reinterpret_cast<const double2*>(a.vm);
-        for (; i + stride < nv; i += 2 * stride) {
-            const double2 x0 = __ldcs(v2 + i), x1 = __ldcs(v2 + i + stride);
-            Entry2 l0[NE], l1[NE];
-#pragma unroll
-            for (int j = 0; j < NE; ++j) {
-                const Entry2* row = reinterpret_cast<const Entry2*>(lead + j * a.ld);
-                l0[j] = __ldcs(row + i);
-                l1[j] = __ldcs(row + i + stride);
-            }
-#pragma unroll
-            for (int j = 0; j < NE; ++j) {
-                term2(j, l0[j], x0);
-                term2(j, l1[j], x1);
-            }
-            renormalize();
-        }
-        if (i < nv) {
-            const double2 x0 = __ldcs(v2 + i);
-#pragma unroll
-            for (int j = 0; j < NE; ++j)
-                term2(j, __ldcs(reinterpret_cast<const Entry2*>(lead + j * a.ld) + i), x0);
-        }
-        if ((a.n & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
-            const long long c = a.n - 1;
-#pragma unroll
-            for (int j = 0; j < NE; ++j) term(j, lead[j * a.ld + c], a.vm[c]);
-        }
-    } else {
-        for (; i + stride < a.n; i += 2 * stride) {
-            const double x0 = __ldcs(a.vm + i), x1 = __ldcs(a.vm + i + stride);
-            Entry l0[NE], l1[NE];
-#pragma unroll
-            for (int j = 0; j < NE; ++j) {
-                l0[j] = __ldcs(lead + j * a.ld + i);
-                l1[j] = __ldcs(lead + j * a.ld + i + stride);
-            }
-#pragma unroll
-            for (int j = 0; j < NE; ++j) {
-                term(j, l0[j], x0);
-                term(j, l1[j], x1);
-            }
-            renormalize();
-        }
-        if (i < a.n) {
-            const double x0 = __ldcs(a.vm + i);
-#pragma unroll
-            for (int j = 0; j < NE; ++j) term(j, __ldcs(lead + j * a.ld + i), x0);
-        }
-    }
     double sum[NE];
 #pragma unroll
     for (int j = 0; j < NE; ++j) sum[j] = warp_sum(acc[j].value());
@@ -223,7 +150,6 @@ __global__ void __launch_bounds__(kEcgBlock) k_pseudo_ecg(EcgArgs a)
         for (int w = 0; w < kEcgBlock / 32; ++w) s += red[w][threadIdx.x];
         a.partial[(long long)blockIdx.x * a.n_el + a.e0 + threadIdx.x] = s;
     }
-    // the last block to finish adds the blocks' sums in block order
     __threadfence();
     __syncthreads();
     if (threadIdx.x == 0) last = atomicAdd(a.ticket, 1u) == gridDim.x - 1;
@@ -240,15 +166,225 @@ __global__ void __launch_bounds__(kEcgBlock) k_pseudo_ecg(EcgArgs a)
     if (threadIdx.x == 0) *a.ticket = 0u;
 }
 
-template <int NE>
-void launch_chunk(const EcgArgs& a, bool vec, bool pair, int blocks, cudaStream_t s)
+// One cell's terms: entry l of each row, Vm value v.
+template <int NE, bool PAIR, class Entry>
+__device__ __forceinline__ void cell_terms(Acc<PAIR> (&acc)[NE], const Entry* lead, long long ld,
+                                           long long c, double v)
 {
-    if (pair) {
-        if (vec) k_pseudo_ecg<NE, true, true><<<blocks, kEcgBlock, 0, s>>>(a);
-        else k_pseudo_ecg<NE, false, true><<<blocks, kEcgBlock, 0, s>>>(a);
+    if constexpr (PAIR) {
+        float vh, vl;
+        split_fp64(v, vh, vl);
+#pragma unroll
+        for (int j = 0; j < NE; ++j) acc[j].add(lead[j * ld + c], vh, vl);
     } else {
-        if (vec) k_pseudo_ecg<NE, true, false><<<blocks, kEcgBlock, 0, s>>>(a);
-        else k_pseudo_ecg<NE, false, false><<<blocks, kEcgBlock, 0, s>>>(a);
+#pragma unroll
+        for (int j = 0; j < NE; ++j) acc[j].add(lead[j * ld + c], v);
+    }
+}
+
+template <int NE, bool PAIR>
+__device__ __forceinline__ void renormalize(Acc<PAIR> (&acc)[NE])
+{
+    if constexpr (PAIR) {
+#pragma unroll
+        for (int j = 0; j < NE; ++j) acc[j].renormalize();
+    }
+}
+
+// Grid-stride form, one cell per load: for a Vm that is not 16-byte aligned.
+template <int NE, bool PAIR>
+__global__ void __launch_bounds__(kEcgBlock) k_pseudo_ecg(EcgArgs a)
+{
+    __shared__ double red[kEcgBlock / 32][NE];
+    __shared__ bool last;
+    using Entry = typename std::conditional<PAIR, float2, double>::type;
+    const Entry* lead = static_cast<const Entry*>(a.lead) + (long long)a.e0 * a.ld;
+    const long long stride = (long long)gridDim.x * kEcgBlock;
+    Acc<PAIR> acc[NE];
+    for (long long c = (long long)blockIdx.x * kEcgBlock + threadIdx.x; c < a.n; c += stride) {
+        cell_terms<NE, PAIR>(acc, lead, a.ld, c, a.vm[c]);
+        renormalize<NE, PAIR>(acc);
+    }
+    finish<NE, PAIR>(a, acc, red, last);
+}
+
+// ---------------------------------------------------------------- staged
+// Persistent form, one block per SM over a contiguous range of tiles of
+// kTile cells: thread 0 moves each tile of Vm and of the NE rows into a ring
+// of shared-memory stages with bulk asynchronous copies (cp.async.bulk,
+// completion counted on the stage's mbarrier), keeping up to `stages` tiles
+// in flight while the block consumes the oldest.  Every wait is bounded: a
+// wait that runs out sets *error, the block waits (bounded) for the copies
+// it issued, and its sums become NaN.
+constexpr int kTile = 1024;
+constexpr int kMaxStages = 8;
+constexpr long long kWaitCycles = 1LL << 31;    // about a second
+
+__device__ __forceinline__ unsigned smem_u32(const void* p)
+{
+    return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(unsigned bar, unsigned count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(unsigned bar, unsigned bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ void bulk_copy(unsigned dst, const void* src, unsigned bytes,
+                                          unsigned bar)
+{
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+        ::"r"(dst), "l"(src), "r"(bytes), "r"(bar)
+        : "memory");
+}
+
+__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity)
+{
+    const long long t0 = clock64();
+    for (;;) {
+        unsigned ok;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(ok)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (ok) return true;
+        if (clock64() - t0 > kWaitCycles) return false;
+    }
+}
+
+template <int NE>
+constexpr unsigned stage_bytes()
+{
+    return unsigned(NE + 1) * kTile * 8u;
+}
+
+template <int NE, bool PAIR>
+__global__ void __launch_bounds__(kEcgBlock, 1) k_pseudo_ecg_staged(EcgArgs a, int stages,
+                                                                  unsigned* error)
+{
+    extern __shared__ __align__(128) unsigned char stage_mem[];
+    __shared__ __align__(8) unsigned long long full[kMaxStages];
+    __shared__ double red[kEcgBlock / 32][NE];
+    __shared__ bool last;
+    __shared__ int failed;
+    using Entry = typename std::conditional<PAIR, float2, double>::type;
+    constexpr unsigned kRow = kTile * 8u;
+    const long long n_even = a.n & ~1LL;
+    const long long tiles = (n_even + kTile - 1) / kTile;
+    const long long per = (tiles + gridDim.x - 1) / gridDim.x;
+    const long long t_begin = min(tiles, (long long)blockIdx.x * per);
+    const long long t_end = min(tiles, t_begin + per);
+    const char* lead = static_cast<const char*>(a.lead) + (long long)a.e0 * a.ld * 8;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < stages; ++s) mbar_init(smem_u32(&full[s]), 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        failed = 0;
+    }
+    __syncthreads();
+    long long issued = 0;    // thread 0: tiles whose copies were issued
+    auto issue = [&](long long t, int s) {
+        const long long c0 = t * kTile;
+        const unsigned bytes = unsigned(min((long long)kTile, n_even - c0) * 8);
+        const unsigned bar = smem_u32(&full[s]);
+        const unsigned dst = smem_u32(stage_mem + (size_t)s * stage_bytes<NE>());
+        mbar_expect_tx(bar, bytes * unsigned(NE + 1));
+        bulk_copy(dst, a.vm + c0, bytes, bar);
+#pragma unroll
+        for (int j = 0; j < NE; ++j)
+            bulk_copy(dst + unsigned(j + 1) * kRow, lead + ((long long)j * a.ld + c0) * 8, bytes, bar);
+        ++issued;
+    };
+    if (threadIdx.x == 0)
+        for (int k = 0; k < stages && t_begin + k < t_end; ++k) issue(t_begin + k, k);
+    Acc<PAIR> acc[NE];
+    long long k = 0;
+    for (long long t = t_begin; t < t_end; ++t, ++k) {
+        const int s = int(k % stages);
+        if (!mbar_wait(smem_u32(&full[s]), unsigned((k / stages) & 1))) atomicOr(&failed, 1);
+        __syncthreads();
+        if (failed) break;
+        const unsigned char* st = stage_mem + (size_t)s * stage_bytes<NE>();
+        const double* vs = reinterpret_cast<const double*>(st);
+        const Entry* rows = reinterpret_cast<const Entry*>(st + kRow);
+        const int m = int(min((long long)kTile, n_even - t * kTile));
+#pragma unroll
+        for (int q = 0; q < kTile / kEcgBlock; ++q) {
+            const int i = threadIdx.x + q * kEcgBlock;
+            if (i < m) cell_terms<NE, PAIR>(acc, rows, kTile, i, vs[i]);
+        }
+        renormalize<NE, PAIR>(acc);
+        __syncthreads();    // stage s read by every thread: refill it
+        if (threadIdx.x == 0 && t + stages < t_end) issue(t + stages, s);
+    }
+    if (failed) {
+        if (threadIdx.x == 0) {
+            // let the copies still in flight land before the block leaves
+            for (long long q = k; q < issued; ++q)
+                mbar_wait(smem_u32(&full[int(q % stages)]), unsigned((q / stages) & 1));
+            atomicOr(error, 1u);
+        }
+#pragma unroll
+        for (int j = 0; j < NE; ++j) acc[j] = Acc<PAIR>::nan();
+    }
+    // the odd last cell
+    if ((a.n & 1) && blockIdx.x == 0 && threadIdx.x == 0)
+        cell_terms<NE, PAIR>(acc, reinterpret_cast<const Entry*>(lead), a.ld, a.n - 1,
+                             a.vm[a.n - 1]);
+    finish<NE, PAIR>(a, acc, red, last);
+}
+
+template <int NE, bool PAIR>
+int stages_for()
+{
+    return std::max(2, std::min(kMaxStages, int((208u * 1024u) / stage_bytes<NE>())));
+}
+
+template <int NE, bool PAIR>
+cudaError_t launch_typed(const EcgArgs& a, bool staged, int blocks, unsigned* error, cudaStream_t s)
+{
+    if (staged) {
+        const int st = stages_for<NE, PAIR>();
+        const size_t smem = size_t(st) * stage_bytes<NE>();
+        cudaError_t e = cudaFuncSetAttribute(k_pseudo_ecg_staged<NE, PAIR>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+        if (e) return e;
+        k_pseudo_ecg_staged<NE, PAIR><<<blocks, kEcgBlock, smem, s>>>(a, st, error);
+    } else {
+        k_pseudo_ecg<NE, PAIR><<<blocks, kEcgBlock, 0, s>>>(a);
+    }
+    return cudaGetLastError();
+}
+
+template <int NE>
+cudaError_t launch_chunk(const EcgArgs& a, bool staged, bool pair, int blocks, unsigned* error,
+                         cudaStream_t s)
+{
+    return pair ? launch_typed<NE, true>(a, staged, blocks, error, s)
+                : launch_typed<NE, false>(a, staged, blocks, error, s);
+}
+
+cudaError_t launch_any(const EcgArgs& a, int ne, bool staged, bool pair, int blocks,
+                       unsigned* error, cudaStream_t s)
+{
+    switch (ne) {
+    case 1: return launch_chunk<1>(a, staged, pair, blocks, error, s);
+    case 2: return launch_chunk<2>(a, staged, pair, blocks, error, s);
+    case 3: return launch_chunk<3>(a, staged, pair, blocks, error, s);
+    case 4: return launch_chunk<4>(a, staged, pair, blocks, error, s);
+    case 5: return launch_chunk<5>(a, staged, pair, blocks, error, s);
+    case 6: return launch_chunk<6>(a, staged, pair, blocks, error, s);
+    case 7: return launch_chunk<7>(a, staged, pair, blocks, error, s);
+    default: return launch_chunk<8>(a, staged, pair, blocks, error, s);
     }
 }
 
@@ -257,11 +393,10 @@ int resident_blocks(bool pair)
 {
     int per_sm = 0;
     if (pair)
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pseudo_ecg<NE, true, true>,
-                                                      kEcgBlock, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pseudo_ecg<NE, true>, kEcgBlock, 0);
     else
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pseudo_ecg<NE, true, false>,
-                                                      kEcgBlock, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pseudo_ecg<NE, false>, kEcgBlock,
+                                                      0);
     return per_sm;
 }
 
@@ -279,26 +414,15 @@ int resident_blocks_any(int ne, bool pair)
     }
 }
 
-void launch_any(const EcgArgs& a, int ne, bool vec, bool pair, int blocks, cudaStream_t s)
-{
-    switch (ne) {
-    case 1: launch_chunk<1>(a, vec, pair, blocks, s); break;
-    case 2: launch_chunk<2>(a, vec, pair, blocks, s); break;
-    case 3: launch_chunk<3>(a, vec, pair, blocks, s); break;
-    case 4: launch_chunk<4>(a, vec, pair, blocks, s); break;
-    case 5: launch_chunk<5>(a, vec, pair, blocks, s); break;
-    case 6: launch_chunk<6>(a, vec, pair, blocks, s); break;
-    case 7: launch_chunk<7>(a, vec, pair, blocks, s); break;
-    default: launch_chunk<8>(a, vec, pair, blocks, s); break;
-    }
-}
-
 }  // namespace
 
 struct cfg_pseudo_ecg {
     long long n = 0, ld = 0;
     int n_el = 0;
-    std::vector<int> blocks;        // grid of each launch
+    std::vector<int> blocks;        // grid of each grid-stride launch
+    int staged_blocks = 0;          // grid of the staged form
+    unsigned* d_error = nullptr;    // set by a staged launch whose copy wait ran out
+    unsigned* h_error = nullptr;    // pinned mirror
     bool pair = false;              // float-pair arithmetic on scaled rows
     void* d_lead = nullptr;         // [n_el][ld] doubles or float pairs
     double* d_scale = nullptr;      // [n_el] row scales (pairs)
@@ -370,16 +494,31 @@ int launch(cfg_pseudo_ecg* ecg, const double* vm, cudaStream_t s, double* out)
 {
     if (ecg->launched && s != ecg->last_stream)
         CFG_CUDA_TRY(cudaStreamSynchronize(ecg->last_stream));
-    const bool vec = (reinterpret_cast<uintptr_t>(vm) & 15) == 0;
+    // the staged form copies whole 16-byte units of Vm
+    const bool staged = (reinterpret_cast<uintptr_t>(vm) & 15) == 0;
     for (int e0 = 0, k = 0; e0 < ecg->n_el; e0 += kEcgChunk, ++k) {
         EcgArgs a{ecg->d_lead, ecg->d_scale, vm, ecg->n, ecg->ld, ecg->n_el, e0,
                   ecg->d_partial, ecg->d_ticket + k, out};
-        launch_any(a, std::min(kEcgChunk, ecg->n_el - e0), vec, ecg->pair,
-                   ecg->blocks[size_t(k)], s);
-        CFG_CUDA_TRY(cudaGetLastError());
+        const int blocks = staged ? ecg->staged_blocks : ecg->blocks[size_t(k)];
+        CFG_CUDA_TRY(launch_any(a, std::min(kEcgChunk, ecg->n_el - e0), staged, ecg->pair,
+                                blocks, ecg->d_error, s));
     }
     ecg->last_stream = s;
     ecg->launched = true;
+    return CFG_OK;
+}
+
+// Waits for the stream and reports a staged launch whose copy wait ran out
+// (the flag is cleared).
+int check_error(cfg_pseudo_ecg* ecg, cudaStream_t s)
+{
+    CFG_CUDA_TRY(cudaMemcpyAsync(ecg->h_error, ecg->d_error, sizeof(unsigned),
+                                 cudaMemcpyDeviceToHost, s));
+    CFG_CUDA_TRY(cudaStreamSynchronize(s));
+    if (*ecg->h_error) {
+        CFG_CUDA_TRY(cudaMemset(ecg->d_error, 0, sizeof(unsigned)));
+        return fail(CFG_ERR_CUDA, "a pseudo-ECG tile copy did not complete within its wait limit");
+    }
     return CFG_OK;
 }
 
@@ -425,11 +564,14 @@ extern "C" int cfg_pseudo_ecg_create(const cfg_pseudo_ecg_desc* d, const cfg_mes
     ecg->ld = ld;
     ecg->n_el = d->n_electrodes;
     ecg->pair = d->arithmetic == CFG_ECG_FLOAT_PAIRS;
-    // per launch one wave of resident blocks, grid-striding over the cells
+    // staged form: one block per SM (at most one per tile); grid-stride form:
+    // per launch one wave of resident blocks
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const long long need = (n / 2 + kEcgBlock - 1) / kEcgBlock;
+    ecg->staged_blocks = int(std::max(1LL, std::min<long long>(std::max(sms, 1),
+                                                               ((n & ~1LL) + kTile - 1) / kTile)));
+    const long long need = (n + kEcgBlock - 1) / kEcgBlock;
     for (int e0 = 0; e0 < ecg->n_el; e0 += kEcgChunk) {
         const int per_sm = std::max(1, std::min(resident_blocks_any(std::min(kEcgChunk,
                                                                              ecg->n_el - e0),
@@ -438,7 +580,8 @@ extern "C" int cfg_pseudo_ecg_create(const cfg_pseudo_ecg_desc* d, const cfg_mes
         ecg->blocks.push_back(int(std::max(1LL, std::min<long long>(
                                                     need, (long long)std::max(sms, 1) * per_sm))));
     }
-    const int max_blocks = *std::max_element(ecg->blocks.begin(), ecg->blocks.end());
+    const int max_blocks = std::max(ecg->staged_blocks,
+                                    *std::max_element(ecg->blocks.begin(), ecg->blocks.end()));
     auto bail = [&](int rc) {
         cfg_pseudo_ecg_destroy(ecg);
         return rc;
@@ -474,9 +617,12 @@ extern "C" int cfg_pseudo_ecg_create(const cfg_pseudo_ecg_desc* d, const cfg_mes
     const int chunks = (ecg->n_el + kEcgChunk - 1) / kEcgChunk;
     if (!e) e = dmalloc(&ecg->d_ticket, size_t(chunks));
     if (!e) e = cudaMemset(ecg->d_ticket, 0, sizeof(unsigned) * size_t(chunks));
+    if (!e) e = dmalloc(&ecg->d_error, 1);
+    if (!e) e = cudaMemset(ecg->d_error, 0, sizeof(unsigned));
     if (!e) e = dmalloc(&ecg->d_values, size_t(ecg->n_el));
     if (!e) e = cudaMallocHost(reinterpret_cast<void**>(&ecg->h_values),
                                size_t(ecg->n_el) * sizeof(double));
+    if (!e) e = cudaMallocHost(reinterpret_cast<void**>(&ecg->h_error), sizeof(unsigned));
     if (!e && d->max_rows > 0) e = dmalloc(&ecg->d_series, size_t(d->max_rows) * size_t(ecg->n_el));
     if (e) return bail(fail(CFG_ERR_CUDA, "pseudo-ECG allocation: %s", cudaGetErrorString(e)));
     ecg->max_rows = d->max_rows;
@@ -493,7 +639,7 @@ extern "C" int cfg_pseudo_ecg_compute(cfg_pseudo_ecg* ecg, const double* vm, voi
     if (int rc = launch(ecg, vm, s, ecg->d_values)) return rc;
     CFG_CUDA_TRY(cudaMemcpyAsync(ecg->h_values, ecg->d_values, size_t(ecg->n_el) * sizeof(double),
                                  cudaMemcpyDeviceToHost, s));
-    CFG_CUDA_TRY(cudaStreamSynchronize(s));
+    if (int rc = check_error(ecg, s)) return rc;
     std::memcpy(values, ecg->h_values, size_t(ecg->n_el) * sizeof(double));
     return CFG_OK;
 }
@@ -536,7 +682,8 @@ extern "C" int cfg_pseudo_ecg_series(cfg_pseudo_ecg* ecg, double* times, double*
     if (n_rows) *n_rows = ecg->rows;
     const long long k = std::min(max_rows, ecg->rows);
     if (k <= 0) return CFG_OK;
-    if (ecg->launched) CFG_CUDA_TRY(cudaStreamSynchronize(ecg->last_stream));
+    if (ecg->launched)
+        if (int rc = check_error(ecg, ecg->last_stream)) return rc;
     if (values)
         CFG_CUDA_TRY(cudaMemcpy(values, ecg->d_series, size_t(k) * size_t(ecg->n_el) * sizeof(double),
                                 cudaMemcpyDeviceToHost));
@@ -560,9 +707,11 @@ extern "C" int cfg_pseudo_ecg_destroy(cfg_pseudo_ecg* ecg)
     dfree(ecg->d_scale);
     dfree(ecg->d_partial);
     dfree(ecg->d_ticket);
+    dfree(ecg->d_error);
     dfree(ecg->d_values);
     dfree(ecg->d_series);
     if (ecg->h_values) cudaFreeHost(ecg->h_values);
+    if (ecg->h_error) cudaFreeHost(ecg->h_error);
     delete ecg;
     return CFG_OK;
 }
