@@ -70,7 +70,10 @@ def _units():
     units.append(("noalloc", CSRC / "noalloc.cu", []))
     units.append(("dictionary", CSRC / "dictionary.cpp", []))
     units.append(("geometry", CSRC / "geometry.cpp", []))
-    units.append(("ecg", CSRC / "ecg.cu", []))
+    # staged pseudo-ECG launch shape: cells per tile, blocks per SM
+    ecg_extra = [f"-D{k}={int(os.environ[k])}" for k in ("CFG_ECG_TILE", "CFG_ECG_STAGED_PER_SM")
+                 if os.environ.get(k)]
+    units.append(("ecg", CSRC / "ecg.cu", ecg_extra))
     units.append(("adjoint", CSRC / "adjoint.cu", ["--use_fast_math"]))
     return units
 

@@ -30,12 +30,22 @@ namespace {
 constexpr int kEcgBlock = 256;
 constexpr int kEcgChunk = 8;      // electrodes of one launch
 constexpr int kEcgBlocksPerSm = 8;
+#ifndef CFG_ECG_TILE
+#define CFG_ECG_TILE 1024
+#endif
+#ifndef CFG_ECG_STAGED_PER_SM
+#define CFG_ECG_STAGED_PER_SM 1
+#endif
+constexpr int kTile = CFG_ECG_TILE;             // cells per tile (a multiple of 2 * kEcgBlock)
+constexpr int kStagedPerSm = CFG_ECG_STAGED_PER_SM;
+constexpr int kMaxStages = 8;
+static_assert(kTile % (2 * kEcgBlock) == 0, "a tile is whole pairs of cells per thread");
 
 struct EcgArgs {
-    const void* lead;     // [n_el][ld] doubles, or (hi, lo) float pairs of the scaled rows
+    const void* lead;     // tile-blocked rows (below): doubles, or (hi, lo) float pairs
     const double* scale;  // pairs: the power of two each row was scaled by
     const double* vm;     // [n]
-    long long n, ld;      // rows padded with zeros to an even length
+    long long n, ld;      // cells; row length padded with zeros to whole tiles
     int n_el, e0;         // all electrodes; the first of this launch
     double* partial;      // [gridDim.x][n_el]
     unsigned* ticket;     // this launch's
@@ -167,18 +177,23 @@ __device__ __forceinline__ void finish(const EcgArgs& a, const Acc<PAIR> (&acc)[
 }
 
 // One cell's terms: entry l of each row, Vm value v.
+// Rows of one launch's NE electrodes are stored tile-blocked: tile t of
+// kTile cells holds row 0's kTile entries, then row 1's, ..., so that a tile
+// of all NE rows is one contiguous block (one bulk copy).  Entry (j, c) is at
+// (c / kTile) NE kTile + j kTile + c % kTile.
 template <int NE, bool PAIR, class Entry>
-__device__ __forceinline__ void cell_terms(Acc<PAIR> (&acc)[NE], const Entry* lead, long long ld,
-                                           long long c, double v)
+__device__ __forceinline__ void cell_terms(Acc<PAIR> (&acc)[NE], const Entry* lead, long long c,
+                                           double v)
 {
+    const Entry* e = lead + (c / kTile) * NE * kTile + c % kTile;
     if constexpr (PAIR) {
         float vh, vl;
         split_fp64(v, vh, vl);
 #pragma unroll
-        for (int j = 0; j < NE; ++j) acc[j].add(lead[j * ld + c], vh, vl);
+        for (int j = 0; j < NE; ++j) acc[j].add(e[j * kTile], vh, vl);
     } else {
 #pragma unroll
-        for (int j = 0; j < NE; ++j) acc[j].add(lead[j * ld + c], v);
+        for (int j = 0; j < NE; ++j) acc[j].add(e[j * kTile], v);
     }
 }
 
@@ -202,7 +217,7 @@ __global__ void __launch_bounds__(kEcgBlock) k_pseudo_ecg(EcgArgs a)
     const long long stride = (long long)gridDim.x * kEcgBlock;
     Acc<PAIR> acc[NE];
     for (long long c = (long long)blockIdx.x * kEcgBlock + threadIdx.x; c < a.n; c += stride) {
-        cell_terms<NE, PAIR>(acc, lead, a.ld, c, a.vm[c]);
+        cell_terms<NE, PAIR>(acc, lead, c, a.vm[c]);
         renormalize<NE, PAIR>(acc);
     }
     finish<NE, PAIR>(a, acc, red, last);
@@ -216,8 +231,6 @@ __global__ void __launch_bounds__(kEcgBlock) k_pseudo_ecg(EcgArgs a)
 // in flight while the block consumes the oldest.  Every wait is bounded: a
 // wait that runs out sets *error, the block waits (bounded) for the copies
 // it issued, and its sums become NaN.
-constexpr int kTile = 1024;
-constexpr int kMaxStages = 8;
 constexpr long long kWaitCycles = 1LL << 31;    // about a second
 
 __device__ __forceinline__ unsigned smem_u32(const void* p)
@@ -269,7 +282,7 @@ constexpr unsigned stage_bytes()
 }
 
 template <int NE, bool PAIR>
-__global__ void __launch_bounds__(kEcgBlock, 1) k_pseudo_ecg_staged(EcgArgs a, int stages,
+__global__ void __launch_bounds__(kEcgBlock, kStagedPerSm) k_pseudo_ecg_staged(EcgArgs a, int stages,
                                                                   unsigned* error)
 {
     extern __shared__ __align__(128) unsigned char stage_mem[];
@@ -297,11 +310,9 @@ __global__ void __launch_bounds__(kEcgBlock, 1) k_pseudo_ecg_staged(EcgArgs a, i
         const unsigned bytes = unsigned(min((long long)kTile, n_even - c0) * 8);
         const unsigned bar = smem_u32(&full[s]);
         const unsigned dst = smem_u32(stage_mem + (size_t)s * stage_bytes<NE>());
-        mbar_expect_tx(bar, bytes * unsigned(NE + 1));
+        mbar_expect_tx(bar, bytes + unsigned(NE) * kRow);
         bulk_copy(dst, a.vm + c0, bytes, bar);
-#pragma unroll
-        for (int j = 0; j < NE; ++j)
-            bulk_copy(dst + unsigned(j + 1) * kRow, lead + ((long long)j * a.ld + c0) * 8, bytes, bar);
+        bulk_copy(dst + kRow, lead + t * NE * (long long)kRow, unsigned(NE) * kRow, bar);
         ++issued;
     };
     if (threadIdx.x == 0)
@@ -320,7 +331,7 @@ __global__ void __launch_bounds__(kEcgBlock, 1) k_pseudo_ecg_staged(EcgArgs a, i
 #pragma unroll
         for (int q = 0; q < kTile / kEcgBlock; ++q) {
             const int i = threadIdx.x + q * kEcgBlock;
-            if (i < m) cell_terms<NE, PAIR>(acc, rows, kTile, i, vs[i]);
+            if (i < m) cell_terms<NE, PAIR>(acc, rows, i, vs[i]);
         }
         renormalize<NE, PAIR>(acc);
         __syncthreads();    // stage s read by every thread: refill it
@@ -338,15 +349,14 @@ __global__ void __launch_bounds__(kEcgBlock, 1) k_pseudo_ecg_staged(EcgArgs a, i
     }
     // the odd last cell
     if ((a.n & 1) && blockIdx.x == 0 && threadIdx.x == 0)
-        cell_terms<NE, PAIR>(acc, reinterpret_cast<const Entry*>(lead), a.ld, a.n - 1,
-                             a.vm[a.n - 1]);
+        cell_terms<NE, PAIR>(acc, reinterpret_cast<const Entry*>(lead), a.n - 1, a.vm[a.n - 1]);
     finish<NE, PAIR>(a, acc, red, last);
 }
 
 template <int NE, bool PAIR>
 int stages_for()
 {
-    return std::max(2, std::min(kMaxStages, int((208u * 1024u) / stage_bytes<NE>())));
+    return std::max(2, std::min(kMaxStages, int((208u * 1024u / kStagedPerSm) / stage_bytes<NE>())));
 }
 
 template <int NE, bool PAIR>
@@ -424,7 +434,7 @@ struct cfg_pseudo_ecg {
     unsigned* d_error = nullptr;    // set by a staged launch whose copy wait ran out
     unsigned* h_error = nullptr;    // pinned mirror
     bool pair = false;              // float-pair arithmetic on scaled rows
-    void* d_lead = nullptr;         // [n_el][ld] doubles or float pairs
+    void* d_lead = nullptr;         // tile-blocked rows per launch, doubles or float pairs
     double* d_scale = nullptr;      // [n_el] row scales (pairs)
     double* d_partial = nullptr;
     unsigned* d_ticket = nullptr;   // one per launch of kEcgChunk electrodes
@@ -447,11 +457,11 @@ namespace {
 // walls, built by assemble_corrected), so z_eP.g_own moves to N from P and
 // z_eN.g_nei to P from N.
 int fold_lead(const cfg_mesh_desc* m, const cfg_pseudo_ecg_desc* d, const CorrectedOperator& op,
-              long long ld, std::vector<double>& lead)
+              std::vector<double>& lead)
 {
     const long long n = m->n_cells, nf = m->n_faces;
     const int ne = d->n_electrodes;
-    lead.assign(size_t(ne) * size_t(ld), 0.0);
+    lead.assign(size_t(ne) * size_t(n), 0.0);
     std::vector<double> z(size_t(3) * size_t(n));
     for (int e = 0; e < ne; ++e) {
         const double* P = d->electrodes + 3 * e;
@@ -472,7 +482,7 @@ int fold_lead(const cfg_mesh_desc* m, const cfg_pseudo_ecg_desc* d, const Correc
             zc[1] = k * (s[1] * r[0] + s[3] * r[1] + s[4] * r[2]);
             zc[2] = k * (s[2] * r[0] + s[4] * r[1] + s[5] * r[2]);
         }
-        double* L = lead.data() + size_t(e) * size_t(ld);
+        double* L = lead.data() + size_t(e) * size_t(n);
         for (long long f = 0; f < nf; ++f) {
             const long long own = m->owner[f], nei = m->neighbour[f];
             const double* go = op.g_own.data() + 3 * f;
@@ -545,7 +555,8 @@ extern "C" int cfg_pseudo_ecg_create(const cfg_pseudo_ecg_desc* d, const cfg_mes
         if (l < 0 || u < 0 || l >= n || u >= n || l == u)
             return fail(CFG_ERR_INVALID, "face %lld has invalid owner/neighbour %d/%d", f, l, u);
     }
-    const long long ld = n + (n & 1);
+    if (n <= 0) return fail(CFG_ERR_INVALID, "the mesh has no cells");
+    const long long ld = (n + kTile - 1) / kTile * kTile;
     const size_t lead_bytes = size_t(d->n_electrodes) * size_t(ld) * sizeof(double);
     size_t free_b = 0, total_b = 0;
     CFG_CUDA_TRY(cudaMemGetInfo(&free_b, &total_b));
@@ -557,7 +568,7 @@ extern "C" int cfg_pseudo_ecg_create(const cfg_pseudo_ecg_desc* d, const cfg_mes
                                     0, op))
         return rc;
     std::vector<double> lead;
-    if (int rc = fold_lead(m, d, op, ld, lead)) return rc;
+    if (int rc = fold_lead(m, d, op, lead)) return rc;
 
     auto* ecg = new cfg_pseudo_ecg();
     ecg->n = n;
@@ -569,7 +580,7 @@ extern "C" int cfg_pseudo_ecg_create(const cfg_pseudo_ecg_desc* d, const cfg_mes
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    ecg->staged_blocks = int(std::max(1LL, std::min<long long>(std::max(sms, 1),
+    ecg->staged_blocks = int(std::max(1LL, std::min<long long>(std::max(sms, 1) * kStagedPerSm,
                                                                ((n & ~1LL) + kTile - 1) / kTile)));
     const long long need = (n + kEcgBlock - 1) / kEcgBlock;
     for (int e0 = 0; e0 < ecg->n_el; e0 += kEcgChunk) {
@@ -587,31 +598,48 @@ extern "C" int cfg_pseudo_ecg_create(const cfg_pseudo_ecg_desc* d, const cfg_mes
         return rc;
     };
     cudaError_t e = cudaMalloc(&ecg->d_lead, lead_bytes);
-    if (!e && ecg->pair) {
-        // each row scaled by a power of two to a largest magnitude in [0.5, 1)
-        // (exact), then split into the nearest float and the float nearest
-        // to the rest
-        std::vector<float2> pairs(lead.size());
-        std::vector<double> scale(size_t(ecg->n_el), 1.0);
+    // pairs: each row scaled by a power of two to a largest magnitude in
+    // [0.5, 1) (exact), then split into the nearest float and the float
+    // nearest to the rest
+    std::vector<double> scale(size_t(ecg->n_el), 1.0);
+    if (ecg->pair)
         for (int r = 0; r < ecg->n_el; ++r) {
-            const double* row = lead.data() + size_t(r) * size_t(ld);
+            const double* row = lead.data() + size_t(r) * size_t(n);
             double mx = 0.0;
-            for (long long c = 0; c < ld; ++c) mx = std::max(mx, std::fabs(row[c]));
+            for (long long c = 0; c < n; ++c) mx = std::max(mx, std::fabs(row[c]));
             int ex = 0;
             if (mx > 0.0) std::frexp(mx, &ex);
             scale[size_t(r)] = std::ldexp(1.0, -ex);
-            for (long long c = 0; c < ld; ++c) {
-                const double v = row[c] * scale[size_t(r)];
-                const float h = float(v);
-                pairs[size_t(r) * size_t(ld) + size_t(c)] = make_float2(h, float(v - double(h)));
-            }
         }
+    // tile-blocked order per launch of up to kEcgChunk electrodes, zero padded
+    auto blocked = [&](auto put) {
+        for (int e0 = 0; e0 < ecg->n_el; e0 += kEcgChunk) {
+            const int ne = std::min(kEcgChunk, ecg->n_el - e0);
+            for (long long t = 0; t < ld / kTile; ++t)
+                for (int j = 0; j < ne; ++j)
+                    for (long long i = 0; i < kTile; ++i) {
+                        const long long c = t * kTile + i;
+                        const size_t at = size_t(e0) * size_t(ld) +
+                                          size_t((t * ne + j) * kTile + i);
+                        put(at, e0 + j, c < n ? lead[size_t(e0 + j) * size_t(n) + size_t(c)] : 0.0);
+                    }
+        }
+    };
+    if (!e && ecg->pair) {
+        std::vector<float2> pairs(size_t(ecg->n_el) * size_t(ld));
+        blocked([&](size_t at, int r, double x) {
+            const double v = x * scale[size_t(r)];
+            const float h = float(v);
+            pairs[at] = make_float2(h, float(v - double(h)));
+        });
         e = cudaMemcpy(ecg->d_lead, pairs.data(), lead_bytes, cudaMemcpyHostToDevice);
         if (!e) e = dmalloc(&ecg->d_scale, scale.size());
         if (!e) e = cudaMemcpy(ecg->d_scale, scale.data(), scale.size() * sizeof(double),
                                cudaMemcpyHostToDevice);
     } else if (!e) {
-        e = cudaMemcpy(ecg->d_lead, lead.data(), lead_bytes, cudaMemcpyHostToDevice);
+        std::vector<double> rows(size_t(ecg->n_el) * size_t(ld));
+        blocked([&](size_t at, int, double x) { rows[at] = x; });
+        e = cudaMemcpy(ecg->d_lead, rows.data(), lead_bytes, cudaMemcpyHostToDevice);
     }
     if (!e) e = dmalloc(&ecg->d_partial, size_t(max_blocks) * size_t(ecg->n_el));
     const int chunks = (ecg->n_el + kEcgChunk - 1) / kEcgChunk;
