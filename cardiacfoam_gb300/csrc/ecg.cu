@@ -31,15 +31,21 @@ constexpr int kEcgBlock = 256;
 constexpr int kEcgChunk = 8;      // electrodes of one launch
 constexpr int kEcgBlocksPerSm = 8;
 #ifndef CFG_ECG_TILE
-#define CFG_ECG_TILE 1024
+#define CFG_ECG_TILE 2048
 #endif
 #ifndef CFG_ECG_STAGED_PER_SM
 #define CFG_ECG_STAGED_PER_SM 1
 #endif
 constexpr int kTile = CFG_ECG_TILE;             // cells per tile (a multiple of 2 * kEcgBlock)
+// Tile of a launch of ne electrodes: kTile while two stages of Vm and ne rows
+// fit in 216 KB of shared memory, else half of it.
+constexpr int tile_of(int ne)
+{
+    return 2 * (ne + 1) * kTile * 8 <= 216 * 1024 ? kTile : kTile / 2;
+}
 constexpr int kStagedPerSm = CFG_ECG_STAGED_PER_SM;
 constexpr int kMaxStages = 8;
-static_assert(kTile % (2 * kEcgBlock) == 0, "a tile is whole pairs of cells per thread");
+static_assert(kTile % (4 * kEcgBlock) == 0, "a tile is whole pairs of cells per thread");
 
 struct EcgArgs {
     const void* lead;     // tile-blocked rows (below): doubles, or (hi, lo) float pairs
@@ -178,22 +184,23 @@ __device__ __forceinline__ void finish(const EcgArgs& a, const Acc<PAIR> (&acc)[
 
 // One cell's terms: entry l of each row, Vm value v.
 // Rows of one launch's NE electrodes are stored tile-blocked: tile t of
-// kTile cells holds row 0's kTile entries, then row 1's, ..., so that a tile
-// of all NE rows is one contiguous block (one bulk copy).  Entry (j, c) is at
-// (c / kTile) NE kTile + j kTile + c % kTile.
+// T = tile_of(NE) cells holds row 0's T entries, then row 1's, ..., so that
+// a tile of all NE rows is one contiguous block (one bulk copy).  Entry
+// (j, c) is at (c / T) NE T + j T + c % T.
 template <int NE, bool PAIR, class Entry>
 __device__ __forceinline__ void cell_terms(Acc<PAIR> (&acc)[NE], const Entry* lead, long long c,
                                            double v)
 {
-    const Entry* e = lead + (c / kTile) * NE * kTile + c % kTile;
+    constexpr int T = tile_of(NE);
+    const Entry* e = lead + (c / T) * NE * T + c % T;
     if constexpr (PAIR) {
         float vh, vl;
         split_fp64(v, vh, vl);
 #pragma unroll
-        for (int j = 0; j < NE; ++j) acc[j].add(e[j * kTile], vh, vl);
+        for (int j = 0; j < NE; ++j) acc[j].add(e[j * T], vh, vl);
     } else {
 #pragma unroll
-        for (int j = 0; j < NE; ++j) acc[j].add(e[j * kTile], v);
+        for (int j = 0; j < NE; ++j) acc[j].add(e[j * T], v);
     }
 }
 
@@ -225,7 +232,7 @@ __global__ void __launch_bounds__(kEcgBlock) k_pseudo_ecg(EcgArgs a)
 
 // ---------------------------------------------------------------- staged
 // Persistent form, one block per SM over a contiguous range of tiles of
-// kTile cells: thread 0 moves each tile of Vm and of the NE rows into a ring
+// tile_of(NE) cells: thread 0 moves each tile of Vm and of the NE rows into a ring
 // of shared-memory stages with bulk asynchronous copies (cp.async.bulk,
 // completion counted on the stage's mbarrier), keeping up to `stages` tiles
 // in flight while the block consumes the oldest.  Every wait is bounded: a
@@ -278,7 +285,7 @@ __device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity)
 template <int NE>
 constexpr unsigned stage_bytes()
 {
-    return unsigned(NE + 1) * kTile * 8u;
+    return unsigned(NE + 1) * unsigned(tile_of(NE)) * 8u;
 }
 
 template <int NE, bool PAIR>
@@ -291,9 +298,10 @@ __global__ void __launch_bounds__(kEcgBlock, kStagedPerSm) k_pseudo_ecg_staged(E
     __shared__ bool last;
     __shared__ int failed;
     using Entry = typename std::conditional<PAIR, float2, double>::type;
-    constexpr unsigned kRow = kTile * 8u;
+    constexpr int T = tile_of(NE);
+    constexpr unsigned kRow = T * 8u;
     const long long n_even = a.n & ~1LL;
-    const long long tiles = (n_even + kTile - 1) / kTile;
+    const long long tiles = (n_even + T - 1) / T;
     const long long per = (tiles + gridDim.x - 1) / gridDim.x;
     const long long t_begin = min(tiles, (long long)blockIdx.x * per);
     const long long t_end = min(tiles, t_begin + per);
@@ -306,8 +314,8 @@ __global__ void __launch_bounds__(kEcgBlock, kStagedPerSm) k_pseudo_ecg_staged(E
     __syncthreads();
     long long issued = 0;    // thread 0: tiles whose copies were issued
     auto issue = [&](long long t, int s) {
-        const long long c0 = t * kTile;
-        const unsigned bytes = unsigned(min((long long)kTile, n_even - c0) * 8);
+        const long long c0 = t * T;
+        const unsigned bytes = unsigned(min((long long)T, n_even - c0) * 8);
         const unsigned bar = smem_u32(&full[s]);
         const unsigned dst = smem_u32(stage_mem + (size_t)s * stage_bytes<NE>());
         mbar_expect_tx(bar, bytes + unsigned(NE) * kRow);
@@ -327,9 +335,9 @@ __global__ void __launch_bounds__(kEcgBlock, kStagedPerSm) k_pseudo_ecg_staged(E
         const unsigned char* st = stage_mem + (size_t)s * stage_bytes<NE>();
         const double* vs = reinterpret_cast<const double*>(st);
         const Entry* rows = reinterpret_cast<const Entry*>(st + kRow);
-        const int m = int(min((long long)kTile, n_even - t * kTile));
+        const int m = int(min((long long)T, n_even - t * T));
 #pragma unroll
-        for (int q = 0; q < kTile / kEcgBlock; ++q) {
+        for (int q = 0; q < T / kEcgBlock; ++q) {
             const int i = threadIdx.x + q * kEcgBlock;
             if (i < m) cell_terms<NE, PAIR>(acc, rows, i, vs[i]);
         }
@@ -356,7 +364,7 @@ __global__ void __launch_bounds__(kEcgBlock, kStagedPerSm) k_pseudo_ecg_staged(E
 template <int NE, bool PAIR>
 int stages_for()
 {
-    return std::max(2, std::min(kMaxStages, int((208u * 1024u / kStagedPerSm) / stage_bytes<NE>())));
+    return std::max(2, std::min(kMaxStages, int((216u * 1024u / kStagedPerSm) / stage_bytes<NE>())));
 }
 
 template <int NE, bool PAIR>
@@ -430,7 +438,7 @@ struct cfg_pseudo_ecg {
     long long n = 0, ld = 0;
     int n_el = 0;
     std::vector<int> blocks;        // grid of each grid-stride launch
-    int staged_blocks = 0;          // grid of the staged form
+    std::vector<int> staged_blocks; // grid of each staged launch
     unsigned* d_error = nullptr;    // set by a staged launch whose copy wait ran out
     unsigned* h_error = nullptr;    // pinned mirror
     bool pair = false;              // float-pair arithmetic on scaled rows
@@ -509,7 +517,7 @@ int launch(cfg_pseudo_ecg* ecg, const double* vm, cudaStream_t s, double* out)
     for (int e0 = 0, k = 0; e0 < ecg->n_el; e0 += kEcgChunk, ++k) {
         EcgArgs a{ecg->d_lead, ecg->d_scale, vm, ecg->n, ecg->ld, ecg->n_el, e0,
                   ecg->d_partial, ecg->d_ticket + k, out};
-        const int blocks = staged ? ecg->staged_blocks : ecg->blocks[size_t(k)];
+        const int blocks = staged ? ecg->staged_blocks[size_t(k)] : ecg->blocks[size_t(k)];
         CFG_CUDA_TRY(launch_any(a, std::min(kEcgChunk, ecg->n_el - e0), staged, ecg->pair,
                                 blocks, ecg->d_error, s));
     }
@@ -556,7 +564,7 @@ extern "C" int cfg_pseudo_ecg_create(const cfg_pseudo_ecg_desc* d, const cfg_mes
             return fail(CFG_ERR_INVALID, "face %lld has invalid owner/neighbour %d/%d", f, l, u);
     }
     if (n <= 0) return fail(CFG_ERR_INVALID, "the mesh has no cells");
-    const long long ld = (n + kTile - 1) / kTile * kTile;
+    const long long ld = (n + kTile - 1) / kTile * kTile;   // whole tiles of either size
     const size_t lead_bytes = size_t(d->n_electrodes) * size_t(ld) * sizeof(double);
     size_t free_b = 0, total_b = 0;
     CFG_CUDA_TRY(cudaMemGetInfo(&free_b, &total_b));
@@ -580,8 +588,11 @@ extern "C" int cfg_pseudo_ecg_create(const cfg_pseudo_ecg_desc* d, const cfg_mes
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    ecg->staged_blocks = int(std::max(1LL, std::min<long long>(std::max(sms, 1) * kStagedPerSm,
-                                                               ((n & ~1LL) + kTile - 1) / kTile)));
+    for (int e0 = 0; e0 < ecg->n_el; e0 += kEcgChunk) {
+        const long long T = tile_of(std::min(kEcgChunk, ecg->n_el - e0));
+        ecg->staged_blocks.push_back(int(std::max(
+            1LL, std::min<long long>(std::max(sms, 1) * kStagedPerSm, ((n & ~1LL) + T - 1) / T))));
+    }
     const long long need = (n + kEcgBlock - 1) / kEcgBlock;
     for (int e0 = 0; e0 < ecg->n_el; e0 += kEcgChunk) {
         const int per_sm = std::max(1, std::min(resident_blocks_any(std::min(kEcgChunk,
@@ -591,8 +602,9 @@ extern "C" int cfg_pseudo_ecg_create(const cfg_pseudo_ecg_desc* d, const cfg_mes
         ecg->blocks.push_back(int(std::max(1LL, std::min<long long>(
                                                     need, (long long)std::max(sms, 1) * per_sm))));
     }
-    const int max_blocks = std::max(ecg->staged_blocks,
-                                    *std::max_element(ecg->blocks.begin(), ecg->blocks.end()));
+    const int max_blocks = std::max(
+        *std::max_element(ecg->staged_blocks.begin(), ecg->staged_blocks.end()),
+        *std::max_element(ecg->blocks.begin(), ecg->blocks.end()));
     auto bail = [&](int rc) {
         cfg_pseudo_ecg_destroy(ecg);
         return rc;
@@ -615,12 +627,13 @@ extern "C" int cfg_pseudo_ecg_create(const cfg_pseudo_ecg_desc* d, const cfg_mes
     auto blocked = [&](auto put) {
         for (int e0 = 0; e0 < ecg->n_el; e0 += kEcgChunk) {
             const int ne = std::min(kEcgChunk, ecg->n_el - e0);
-            for (long long t = 0; t < ld / kTile; ++t)
+            const long long T = tile_of(ne);
+            for (long long t = 0; t < ld / T; ++t)
                 for (int j = 0; j < ne; ++j)
-                    for (long long i = 0; i < kTile; ++i) {
-                        const long long c = t * kTile + i;
+                    for (long long i = 0; i < T; ++i) {
+                        const long long c = t * T + i;
                         const size_t at = size_t(e0) * size_t(ld) +
-                                          size_t((t * ne + j) * kTile + i);
+                                          size_t((t * ne + j) * T + i);
                         put(at, e0 + j, c < n ? lead[size_t(e0 + j) * size_t(n) + size_t(c)] : 0.0);
                     }
         }
