@@ -354,7 +354,7 @@ class Monodomain:
 
 # NUM_STATES of the compiled models
 STATE_COUNTS = {"TNNP": 17, "ORd": 41, "ToRORd_dynCl": 45, "AlievPanfilov": 2, "BuenoOrovio": 4,
-                "monodomainFDAManufactured": 4}
+                "monodomainFDAManufactured": 4, "bidomainFDAManufactured": 4}
 
 
 class BatchCells:

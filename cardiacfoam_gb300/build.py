@@ -21,7 +21,7 @@ LIB = PKG / "libcardiac_gpu.so"
 INCLUDE = PKG.parent / "include"
 
 MODELS = ["tnnp", "ord", "torord_dyncl", "alievpanfilov", "buenoorovio",
-          "monodomainfdamanufactured"]
+          "monodomainfdamanufactured", "bidomainfdamanufactured"]
 # per-model unroll factor of the per-state loops around the right-hand side
 # (measured on GB300: ORd fastest at 4, the others at 1)
 STATE_UNROLL = {"ord": 4}

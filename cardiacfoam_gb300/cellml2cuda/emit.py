@@ -41,6 +41,7 @@ WIDE_STATES = {
     "AlievPanfilov": ["u", "recovery_r"],
     "BuenoOrovio": ["u", "v", "w", "s"],
     "monodomainFDAManufactured": ["V", "u1", "u2", "u3"],
+    "bidomainFDAManufactured": ["BidomainV", "BidomainU1", "BidomainU2", "BidomainU3"],
 }
 
 # constants a batched run may scale per cell (log-uniform factors); the
@@ -56,6 +57,7 @@ SCALABLE = {
     "AlievPanfilov": {},
     "BuenoOrovio": {},
     "monodomainFDAManufactured": {},
+    "bidomainFDAManufactured": {},
 }
 SCALE_ORDER = ["GNa", "GCaL", "GKr", "GKs", "GK1", "Gto"]
 

@@ -124,7 +124,7 @@ def _strip_comments(src: str) -> str:
 
 def _enum_names(text: str, *enum_names: str) -> List[str]:
     for en in enum_names:
-        m = re.search(r"enum\s+" + en + r"\s*\{(.*?)\}", text, re.S)
+        m = re.search(r"enum\s+(?:\w+_)?" + en + r"\s*\{(.*?)\}", text, re.S)
         if m:
             names = []
             for item in m.group(1).split(","):
@@ -132,7 +132,7 @@ def _enum_names(text: str, *enum_names: str) -> List[str]:
                 if not item:
                     continue
                 nm = item.split("=")[0].strip()
-                if nm.startswith("NUM_"):
+                if nm.startswith("NUM_") or "_NUM_" in nm:
                     continue
                 names.append(nm)
             return names
@@ -312,7 +312,28 @@ WRAPPERS = {
         variables_fns=["monodomainFDAManufacturedComputeVariables"],
         tissues=["1D", "2D", "3D"],
         vm_to_state="identity", iion_name="Iion", iion_scale=0.5, time_scale=1000.0),
+    # bidomainFDAManufactured.C:47-60 (k from manufacturedBidomain.k, default
+    # 1/sqrt(2); the tutorial's value is compiled in), 77 (initConsts with k),
+    # solveODE as monodomainFDAManufactured.  initConsts keeps the dimension's
+    # Beta in a local before scaling it by (1 - k); the rewrite keeps it in
+    # the Beta constant instead, with the same arithmetic (and the casts to
+    # void that mark unused parameters go).
+    "bidomainFDAManufactured": dict(
+        dir="bidomainFDAManufactured", header="bidomainFDAManufactured_2014.H",
+        names="bidomainFDAManufactured_2014Names.H", prefix="bidomainFDAManufactured",
+        init_fn="bidomainFDAManufacturedInitConsts",
+        rates_fn="bidomainFDAManufacturedComputeVariables",
+        variables_fns=["bidomainFDAManufacturedComputeVariables"],
+        tissues=["1D", "2D", "3D"],
+        vm_to_state="identity", iion_name="BidomainIion", iion_scale=0.5, time_scale=1000.0,
+        rewrite=[("CONSTANTS[BidomainBeta] = betaBase*(1.0 - k);",
+                  "CONSTANTS[BidomainBeta] = CONSTANTS[BidomainBeta]*(1.0 - 0.7071067811865476);"),
+                 ("double betaBase = 0.0;", "CONSTANTS[BidomainBeta] = 0.0;"),
+                 ("betaBase = ", "CONSTANTS[BidomainBeta] = "),
+                 ("(void)VOI;", ""), ("(void)dimension;", ""),
+                 ("(void)solveVmWithinODESolver;", "")]),
 }
+BIDOMAIN_K = 0.7071067811865476   # manufacturedBidomain.k of the bidomain tutorial
 
 
 def _string_table(text: str, table: str) -> List[str]:
@@ -338,6 +359,10 @@ def load_model(ionic_models_dir: Union[str, Path], name: str) -> Model:
     d = Path(ionic_models_dir) / w["dir"]
     names_txt = _strip_comments((d / w["names"]).read_text())
     hdr_txt = _strip_comments((d / w["header"]).read_text())
+    for a, b in w.get("rewrite", []):
+        if a not in hdr_txt:
+            raise ParseError(f"{name}: rewrite target {a!r} not found")
+        hdr_txt = hdr_txt.replace(a, b)
     states = _enum_names(names_txt, "STATES_INDEX", "STATE_INDEX")
     algebraic = _enum_names(names_txt, "ALGEBRAIC_INDEX")
     constants = _enum_names(names_txt, "CONSTANTS_INDEX", "CONSTANT_INDEX")

@@ -9,6 +9,7 @@
 #include "models/tnnp.cuh"
 #include "models/torord_dyncl.cuh"
 #include "models/monodomainfdamanufactured.cuh"
+#include "models/bidomainfdamanufactured.cuh"
 
 #define CFG_DECLARE_MODEL(ns)                                                                  \
     extern "C" cudaError_t cfg_ionic_step_##ns##_fp64(const cfg::IonicLaunch&, int,           \
@@ -43,6 +44,7 @@ CFG_DECLARE_MODEL(torord_dyncl)
 CFG_DECLARE_MODEL(alievpanfilov)
 CFG_DECLARE_MODEL(buenoorovio)
 CFG_DECLARE_MODEL(monodomainfdamanufactured)
+CFG_DECLARE_MODEL(bidomainfdamanufactured)
 
 namespace cfg {
 namespace {
@@ -116,6 +118,7 @@ const IonicModelOps* table()
         CFG_MODEL_ENTRY("AlievPanfilov", alievpanfilov),
         CFG_MODEL_ENTRY("BuenoOrovio", buenoorovio),
         CFG_MODEL_ENTRY("monodomainFDAManufactured", monodomainfdamanufactured),
+        CFG_MODEL_ENTRY("bidomainFDAManufactured", bidomainfdamanufactured),
         IonicModelOps{},
     };
     return models;

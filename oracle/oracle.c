@@ -20,6 +20,7 @@
 #include "models/alievpanfilov.h"
 #include "models/buenoorovio.h"
 #include "models/monodomainfdamanufactured.h"
+#include "models/bidomainfdamanufactured.h"
 
 void oracle_fatal(const char* what)
 {
@@ -67,6 +68,11 @@ static const model_info MODELS[ORACLE_NMODELS] = {
      monodomainfdamanufactured_supplement, monodomainfdamanufactured_rates,
      monodomainfdamanufactured_variables, MONODOMAINFDAMANUFACTURED_IION_INDEX,
      MONODOMAINFDAMANUFACTURED_IION_SCALE, MONODOMAINFDAMANUFACTURED_TIME_SCALE, 3},
+    {"bidomainFDAManufactured", BIDOMAINFDAMANUFACTURED_NS, BIDOMAINFDAMANUFACTURED_NA,
+     BIDOMAINFDAMANUFACTURED_NC, bidomainfdamanufactured_init,
+     bidomainfdamanufactured_supplement, bidomainfdamanufactured_rates,
+     bidomainfdamanufactured_variables, BIDOMAINFDAMANUFACTURED_IION_INDEX,
+     BIDOMAINFDAMANUFACTURED_IION_SCALE, BIDOMAINFDAMANUFACTURED_TIME_SCALE, 3},
 };
 
 int oracle_model_sizes(int model, int* ns, int* na, int* nc)
@@ -580,6 +586,7 @@ struct oracle_tissue {
     unsigned char* tissue_cell;   /* [n] tissue flag per cell, or NULL */
     /* general mesh: gaussLaplacianScheme with corrected snGrad */
     int corrected_mesh; /* face centres given: explicit corrections are on */
+    const double* extra_src;  /* bidomain: V fvc::div(Gi & grad(phiE)) added to the source */
     double *w, *dcoef, *corrv, *sfgsn, *sfgcorr, *bsfgcorr, *bn, *lsp, *lsn, *grad, *fflux;
     /* PCG work */
     double *diag, *upper, *b, *rA, *wA, *pA, *rD, *tmp;
@@ -1110,6 +1117,8 @@ static int solve_implicit(oracle_tissue* T, double dt)
         correction_div_v(T, T->vm, cv);
         for (long c = 0; c < T->n; c++) T->b[c] = T->b[c] + cv[c];
     }
+    if (T->extra_src)
+        for (long c = 0; c < T->n; c++) T->b[c] = T->b[c] + T->extra_src[c];
     int k = T->n_solves;
     if (k >= MAX_SOLVES) return -1;
     int it = pcg(T, T->vm, T->b, &T->init_res[k], &T->final_res[k]);
@@ -1314,6 +1323,209 @@ int oracle_tissue_step(oracle_tissue* T, double dt, int nthreads)
         }
     } else {
         solve_explicit(T, dt);
+    }
+    if (T->n_old < 1) { memcpy(T->vm_old, T->vm, sizeof(double) * (size_t)T->n); T->n_old = 1; }
+    update_activation(T, dt);
+    return total;
+}
+
+/* ------------------------------------------------------------------------ */
+/* bidomain                                                                 */
+
+/* BidomainSolver (bidomainSolver.C:36-263) on a general mesh: the tissue Ti
+ * carries Vm, the ionic model, the stimulus, the activation time and the
+ * Laplacian of the intracellular conductivity Gi; Te carries the Laplacian of
+ * Gi + Ge for phiE. */
+struct oracle_bidomain {
+    oracle_tissue* Ti;
+    oracle_tissue* Te;
+    double *phie, *phii, *dv, *ue, *src;
+    long ref;
+    double ref_value;
+    double phie_tol, phie_rel_tol;
+    int phie_max_iter;
+    int n_solves;
+    double init_res[MAX_SOLVES], final_res[MAX_SOLVES];
+    int iters[MAX_SOLVES];
+};
+
+/* V fvc::div(G & fvc::grad(x)) with Gauss linear divergence: the cell
+ * vectors G g linearly interpolated to the faces, the wall values
+ * G (g - n (n.g)) (gaussGrad::correctBoundaryConditions on zeroGradient
+ * walls; a per-cell G takes its cell's value on the wall). */
+static void div_gamma_grad_v(oracle_tissue* T, const double* x, double* out, double* u)
+{
+    const oracle_mesh* M = T->mesh;
+    double* g = T->grad;
+    cell_gradient(T, x, g);
+    for (long c = 0; c < T->n; c++) {
+        double S[9];
+        cell_sigma(T, c, S);
+        const double* gc = g + 3 * c;
+        for (int i = 0; i < 3; i++)
+            u[3 * c + i] = S[3 * i] * gc[0] + S[3 * i + 1] * gc[1] + S[3 * i + 2] * gc[2];
+    }
+    double* div = T->fflux;
+    memset(div, 0, sizeof(double) * (size_t)T->n);
+    for (long f = 0; f < T->nf; f++) {
+        const long P = M->owner[f], N = M->neigh[f];
+        double uf[3];
+        for (int k = 0; k < 3; k++) uf[k] = T->w[f] * (u[3 * P + k] - u[3 * N + k]) + u[3 * N + k];
+        const double flux = dot3(M->sf + 3 * f, uf);
+        div[P] += flux;
+        div[N] -= flux;
+    }
+    for (long bf = 0; bf < M->nb; bf++) {
+        const long P = M->bcell[bf];
+        double gb[3], S[9], ub[3];
+        boundary_gradient(g + 3 * P, T->bn + 3 * bf, gb);
+        cell_sigma(T, P, S);
+        for (int i = 0; i < 3; i++) ub[i] = S[3 * i] * gb[0] + S[3 * i + 1] * gb[1] + S[3 * i + 2] * gb[2];
+        div[P] += dot3(M->bsf + 3 * bf, ub);
+    }
+    for (long c = 0; c < T->n; c++) out[c] = M->vol[c] * (div[c] / M->vol[c]);
+}
+
+/* polyMesh::findCell restated for the reference point: the cell whose centre
+ * is nearest (the first in cell order on ties). */
+static long nearest_cell(const oracle_mesh* M, const double* p)
+{
+    long best = -1;
+    double bd = 0.0;
+    for (long c = 0; c < M->n; c++) {
+        const double* C = M->centres + 3 * c;
+        const double d = (C[0] - p[0]) * (C[0] - p[0]) + (C[1] - p[1]) * (C[1] - p[1]) +
+                         (C[2] - p[2]) * (C[2] - p[2]);
+        if (best < 0 || d < bd) { best = c; bd = d; }
+    }
+    return best;
+}
+
+oracle_bidomain* oracle_bidomain_new(const oracle_tissue_desc* d, const double* sigma_e,
+                                     const oracle_mesh* mesh, const double* ref_point,
+                                     double ref_value, double phie_tol, double phie_rel_tol,
+                                     int phie_max_iter)
+{
+    if (!mesh->cf) return NULL;
+    oracle_bidomain* B = (oracle_bidomain*)calloc(1, sizeof(oracle_bidomain));
+    B->Ti = oracle_tissue_new(d, mesh);
+    oracle_tissue_desc de = *d;
+    for (int k = 0; k < 6; k++) de.sigma[k] = d->sigma[k] + sigma_e[k];
+    B->Te = oracle_tissue_new(&de, mesh);
+    long n = mesh->n;
+    B->phie = (double*)calloc((size_t)n, sizeof(double));
+    B->phii = (double*)calloc((size_t)n, sizeof(double));
+    B->dv = (double*)malloc(sizeof(double) * (size_t)n);
+    B->src = (double*)malloc(sizeof(double) * (size_t)n);
+    B->ue = (double*)malloc(sizeof(double) * 3 * (size_t)n);
+    B->ref = nearest_cell(mesh, ref_point);
+    B->ref_value = ref_value;
+    B->phie_tol = phie_tol;
+    B->phie_rel_tol = phie_rel_tol;
+    B->phie_max_iter = phie_max_iter;
+    return B;
+}
+
+void oracle_bidomain_free(oracle_bidomain* B)
+{
+    if (!B) return;
+    oracle_tissue_free(B->Ti);
+    oracle_tissue_free(B->Te);
+    free(B->phie); free(B->phii); free(B->dv); free(B->src); free(B->ue);
+    free(B);
+}
+
+oracle_tissue* oracle_bidomain_tissue(oracle_bidomain* B) { return B->Ti; }
+double* oracle_bidomain_phie(oracle_bidomain* B) { return B->phie; }
+double* oracle_bidomain_phii(oracle_bidomain* B) { return B->phii; }
+long oracle_bidomain_ref_cell(const oracle_bidomain* B) { return B->ref; }
+
+int oracle_bidomain_last_solves(const oracle_bidomain* B, double* ir, double* fr, int* it, int mx)
+{
+    int k = B->n_solves < mx ? B->n_solves : mx;
+    for (int i = 0; i < k; i++) {
+        ir[i] = B->init_res[i];
+        fr[i] = B->final_res[i];
+        it[i] = B->iters[i];
+    }
+    return B->n_solves;
+}
+
+/* fvm::laplacian(Gi + Ge, phiE) == -fvc::div(Gi & fvc::grad(Vm)) with
+ * setReference(refCell, phiEReferenceValue, true)
+ * (bidomainSolver.C:222-233; fvMatrix::setReference: source += diag value,
+ * diag += diag), solved in its own (negative definite) form by PCG. */
+static int solve_phie(oracle_bidomain* B)
+{
+    oracle_tissue* Te = B->Te;
+    oracle_tissue* Ti = B->Ti;
+    const int* l = Te->mesh->owner;
+    const int* u = Te->mesh->neigh;
+    for (long c = 0; c < Te->n; c++) Te->diag[c] = 0.0;
+    for (long f = 0; f < Te->nf; f++) {
+        Te->upper[f] = Te->lap[f];
+        Te->diag[l[f]] -= Te->lap[f];
+        Te->diag[u[f]] -= Te->lap[f];
+    }
+    div_gamma_grad_v(Ti, Ti->vm, B->dv, B->ue);
+    for (long c = 0; c < Te->n; c++) B->src[c] = -B->dv[c];
+    /* the Laplacian's explicit correction of the current phiE (general
+     * meshes): fvm.source() -= V fvc::div(faceFluxCorrection) */
+    if (Te->corrected_mesh) {
+        double* cv = Te->tmp;
+        correction_div_v(Te, B->phie, cv);
+        for (long c = 0; c < Te->n; c++) B->src[c] = B->src[c] - cv[c];
+    }
+    if (B->ref >= 0) {
+        B->src[B->ref] += Te->diag[B->ref] * B->ref_value;
+        Te->diag[B->ref] += Te->diag[B->ref];
+    }
+    const double tol = Te->d.pcg_tol, rel = Te->d.pcg_rel_tol;
+    const int mx = Te->d.pcg_max_iter;
+    Te->d.pcg_tol = B->phie_tol;
+    Te->d.pcg_rel_tol = B->phie_rel_tol;
+    Te->d.pcg_max_iter = B->phie_max_iter;
+    int k = B->n_solves;
+    if (k >= MAX_SOLVES) return -1;
+    int it = pcg(Te, B->phie, B->src, &B->init_res[k], &B->final_res[k]);
+    B->iters[k] = it;
+    B->n_solves++;
+    Te->d.pcg_tol = tol; Te->d.pcg_rel_tol = rel; Te->d.pcg_max_iter = mx;
+    return it;
+}
+
+/* One runTime++ / evolve() of the bidomain domain: stimulus, ionic, then
+ * per PIMPLE corrector the phiE solve and the Vm solve
+ *   chi Cm ddt(Vm) == laplacian(Gi, Vm) + fvc::div(Gi & grad(phiE)) - chi Cm Iion + src
+ * (bidomainSolver.C:215-261), phiI = Vm + phiE, activation time. */
+int oracle_bidomain_step(oracle_bidomain* B, double dt, int nthreads)
+{
+    oracle_tissue* T = B->Ti;
+    if (oracle_tissue_init_ionic(T, dt)) return -1;
+    T->t = T->t + dt;
+    T->time_index++;
+    if (T->n_old >= 1) {
+        if (T->n_old >= 2) memcpy(T->vm_oldold, T->vm_old, sizeof(double) * (size_t)T->n);
+        memcpy(T->vm_old, T->vm, sizeof(double) * (size_t)T->n);
+    }
+    const double t0 = T->t - dt;
+    update_stimulus(T, t0);
+    if (oracle_ionic_solve(T->ionic, t0, dt, T->vm, T->iion, nthreads) < 0) return -1;
+    T->n_solves = 0;
+    B->n_solves = 0;
+    int total = 0, converged = 0;
+    for (int corr = 1; corr <= T->d.n_outer && !converged; corr++) {
+        if (corr > 1 && T->init_res[T->n_solves - 1] < T->d.outer_tol) converged = 1;
+        int it = solve_phie(B);
+        if (it < 0) return -1;
+        total += it;
+        div_gamma_grad_v(T, B->phie, B->dv, B->ue);
+        T->extra_src = B->dv;
+        it = solve_implicit(T, dt);
+        T->extra_src = NULL;
+        if (it < 0) return -1;
+        total += it;
+        for (long c = 0; c < T->n; c++) B->phii[c] = T->vm[c] + B->phie[c];
     }
     if (T->n_old < 1) { memcpy(T->vm_old, T->vm, sizeof(double) * (size_t)T->n); T->n_old = 1; }
     update_activation(T, dt);

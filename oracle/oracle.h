@@ -33,7 +33,7 @@ extern "C" {
 #endif
 
 enum { ORACLE_TNNP = 0, ORACLE_ORD = 1, ORACLE_TORORD = 2, ORACLE_ALIEV = 3,
-       ORACLE_BUENO = 4, ORACLE_MMS = 5, ORACLE_NMODELS = 6 };
+       ORACLE_BUENO = 4, ORACLE_MMS = 5, ORACLE_BIDOMAIN_MMS = 6, ORACLE_NMODELS = 7 };
 
 /* --- model-level entry points (golden-vector pins) --------------------- */
 int oracle_model_sizes(int model, int* ns, int* na, int* nc);
@@ -137,6 +137,21 @@ int oracle_tissue_set_cell_tissue(oracle_tissue*, const unsigned char* flags);
 /* fvc::laplacian(sigma, phi) [per volume] and the cell gradient of phi */
 void oracle_tissue_laplacian(oracle_tissue*, const double* phi, double* out);
 int oracle_tissue_gradient(oracle_tissue*, const double* phi, double* g);
+/* bidomain (BidomainSolver) on a general mesh: d carries Gi, the Vm solver
+ * settings, the ionic model and the stimulus; sigma_e is Ge */
+typedef struct oracle_bidomain oracle_bidomain;
+oracle_bidomain* oracle_bidomain_new(const oracle_tissue_desc* d, const double* sigma_e,
+                                     const oracle_mesh* mesh, const double* ref_point,
+                                     double ref_value, double phie_tol, double phie_rel_tol,
+                                     int phie_max_iter);
+void oracle_bidomain_free(oracle_bidomain*);
+int oracle_bidomain_step(oracle_bidomain*, double dt, int nthreads);
+oracle_tissue* oracle_bidomain_tissue(oracle_bidomain*);
+double* oracle_bidomain_phie(oracle_bidomain*);
+double* oracle_bidomain_phii(oracle_bidomain*);
+long oracle_bidomain_ref_cell(const oracle_bidomain*);
+int oracle_bidomain_last_solves(const oracle_bidomain*, double* init_res, double* final_res,
+                                int* iters, int max_solves);
 /* the pseudo-ECG of a Vm field at n_el electrodes [n_el][3] (general mesh) */
 int oracle_tissue_pseudo_ecg(oracle_tissue*, const double* vm, int n_el, const double* el,
                              double* out);

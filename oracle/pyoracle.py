@@ -15,7 +15,7 @@ import numpy as np
 from . import build as _build
 
 MODELS = {"TNNP": 0, "ORd": 1, "ToRORd_dynCl": 2, "AlievPanfilov": 3, "BuenoOrovio": 4,
-          "monodomainFDAManufactured": 5}
+          "monodomainFDAManufactured": 5, "bidomainFDAManufactured": 6}
 TISSUES = {"epicardialCells": 1, "mCells": 2, "endocardialCells": 3, "myocyte": 4,
            "1D": 11, "2D": 12, "3D": 13}
 
@@ -95,6 +95,19 @@ def lib():
         L.oracle_tissue_laplacian.argtypes = [C.c_void_p, _dp, _dp]
         L.oracle_tissue_gradient.argtypes = [C.c_void_p, _dp, _dp]
         L.oracle_tissue_pseudo_ecg.argtypes = [C.c_void_p, _dp, C.c_int, _dp, _dp]
+        L.oracle_bidomain_new.argtypes = [C.POINTER(TissueDesc), _dp, C.c_void_p, _dp,
+                                          C.c_double, C.c_double, C.c_double, C.c_int]
+        L.oracle_bidomain_new.restype = C.c_void_p
+        L.oracle_bidomain_free.argtypes = [C.c_void_p]
+        L.oracle_bidomain_step.argtypes = [C.c_void_p, C.c_double, C.c_int]
+        L.oracle_bidomain_tissue.argtypes = [C.c_void_p]
+        L.oracle_bidomain_tissue.restype = C.c_void_p
+        for f in ("phie", "phii"):
+            getattr(L, f"oracle_bidomain_{f}").argtypes = [C.c_void_p]
+            getattr(L, f"oracle_bidomain_{f}").restype = _dp
+        L.oracle_bidomain_ref_cell.argtypes = [C.c_void_p]
+        L.oracle_bidomain_ref_cell.restype = C.c_long
+        L.oracle_bidomain_last_solves.argtypes = [C.c_void_p, _dp, _dp, _ip, C.c_int]
         L.oracle_tissue_new.argtypes = [C.POINTER(TissueDesc), C.c_void_p]
         L.oracle_tissue_new.restype = C.c_void_p
         L.oracle_tissue_free.argtypes = [C.c_void_p]
@@ -443,3 +456,55 @@ def ref_lib():
                                                        C.c_int, _dp]
         _ref = L
     return _ref
+
+
+class _BorrowedTissue(Tissue):
+    """The Vm side of a Bidomain (owned by it)."""
+
+    def __init__(self, h, desc, mesh):
+        self.h, self.desc, self.mesh, self.n = h, desc, mesh, mesh.n
+
+    def __del__(self):
+        pass
+
+
+class Bidomain:
+    """BidomainSolver restated (oracle_bidomain_*): desc carries Gi and the
+    Vm solver settings; sigma_e is Ge; phiE's PCG has its own tolerances."""
+
+    def __init__(self, desc: TissueDesc, sigma_e, mesh: Mesh, ref_point, ref_value=0.0,
+                 phie_tol=1e-15, phie_rel_tol=0.0, phie_max_iter=1000):
+        self.mesh = mesh
+        self.n = mesh.n
+        se = np.ascontiguousarray(sigma_e, dtype=np.float64)
+        rp = np.ascontiguousarray(ref_point, dtype=np.float64)
+        self.h = lib().oracle_bidomain_new(C.byref(desc), ptr(se), mesh.h, ptr(rp), ref_value,
+                                           phie_tol, phie_rel_tol, phie_max_iter)
+        if not self.h:
+            raise RuntimeError("the oracle bidomain needs a general mesh")
+        self.tissue = _BorrowedTissue(lib().oracle_bidomain_tissue(self.h), desc, mesh)
+
+    def step(self, dt, nthreads=1) -> int:
+        it = lib().oracle_bidomain_step(self.h, dt, nthreads)
+        if it < 0:
+            raise RuntimeError("oracle bidomain step failed")
+        return it
+
+    def phie(self):
+        return np.ctypeslib.as_array(lib().oracle_bidomain_phie(self.h), shape=(self.n,)).copy()
+
+    def phii(self):
+        return np.ctypeslib.as_array(lib().oracle_bidomain_phii(self.h), shape=(self.n,)).copy()
+
+    def ref_cell(self) -> int:
+        return int(lib().oracle_bidomain_ref_cell(self.h))
+
+    def phie_solves(self):
+        ir, fr, it = np.zeros(64), np.zeros(64), np.zeros(64, np.int32)
+        k = lib().oracle_bidomain_last_solves(self.h, ptr(ir), ptr(fr), iptr(it), 64)
+        return ir[:k], fr[:k], it[:k]
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().oracle_bidomain_free(self.h)
+            self.h = None
