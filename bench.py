@@ -256,6 +256,82 @@ LV_DT = 1e-5
 LV_INTENSITY = 5e4       # A/m^3, for 2 ms
 
 
+def bidomain_arm(args):
+    """The bidomain tutorial's manufactured case (bidomainSolver,
+    bidomainFDAManufactured, 3D unit cube at 40 cells per direction, dt of the
+    tutorial's sweep, two PIMPLE correctors, PCG tolerance 1e-12 for Vm and
+    phiE): GPU steps timed with CUDA events after warm-up, the oracle (DIC, one
+    thread) on a bounded sample of the same steps, and the two compared
+    after that sample."""
+    import torch
+    from cardiacfoam_gb300 import api, lib
+    from cardiacfoam_gb300 import verification as V
+    from oracle import pyoracle
+    dim, n = 3, args.bidomain_cells
+    dt = V.SWEEP.get(n, 0.2 / (10 * n * n / 4))
+    mesh = V.geometry_mesh_for(dim, n)
+
+    def gpu():
+        bd = api.Bidomain(mesh, model="bidomainFDAManufactured", tissue=f"{dim}D",
+                          sigma_i=V.BIDOMAIN_SIGMA_I, sigma_e=V.BIDOMAIN_SIGMA_E, chi=V.CHI,
+                          cm=V.CM, dt=dt, pcg_tol=1e-12, phie_tol=1e-12, phie_max_iter=4000,
+                          n_outer=2, ref_point=V.BIDOMAIN_REF_POINT,
+                          grad_scheme=lib.GRAD_GAUSS_LINEAR)
+        vm, pe, _, u1, u2, u3 = V.bidomain_fields(mesh.centres, 0.0, dim)
+        bd.set_field(lib.FIELD_VM, vm)
+        bd.set_field(lib.FIELD_PHIE, pe)
+        bd.set_states(np.stack([vm, u1, u2, u3]))
+        return bd
+
+    bd = gpu()
+    ks = args.bidomain_sample
+    bd.run(dt, ks)
+    g_vm, g_pe = bd.vm(), bd.phie()
+    bd.run(dt, 3)
+    s = torch.cuda.ExternalStream(bd.stream())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    its_v, its_e = [], []
+    torch.cuda.synchronize()
+    e0.record(s)
+    for _ in range(args.bidomain_steps):
+        bd.step(dt)
+        (_, _, iv), (_, _, ie) = bd.stats()
+        its_v.append(int(iv.sum()))
+        its_e.append(int(ie.sum()))
+    e1.record(s)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / args.bidomain_steps
+    bd.close()
+    # oracle sample: the same first steps from the same state
+    d = pyoracle.tissue_desc("bidomainFDAManufactured", 10 + dim, V.BIDOMAIN_SIGMA_I, chi=V.CHI,
+                             cm=V.CM, implicit=True, precond_dic=True, pcg_tol=1e-12,
+                             pcg_rel_tol=0.0, pcg_max_iter=2000, n_outer=2, outer_tol=0.0,
+                             grad_gauss=True)
+    B = pyoracle.Bidomain(d, V.BIDOMAIN_SIGMA_E, pyoracle.Mesh.general(mesh),
+                          V.BIDOMAIN_REF_POINT, 0.0, 1e-12, 0.0, 4000)
+    vm, pe, _, u1, u2, u3 = V.bidomain_fields(mesh.centres, 0.0, dim)
+    B.tissue.set_vm(vm)
+    B.tissue.set_states(np.stack([vm, u1, u2, u3]), dt)
+    B.set_phie(pe)
+    t0 = time.perf_counter()
+    for _ in range(ks):
+        B.step(dt)
+    t_cpu = time.perf_counter() - t0
+    cells = mesh.n_cells
+    return {"workload": (f"bidomain tutorial manufactured case, 3D unit cube {n}^3 = {cells} "
+                         f"cells, dt {dt} s, Gi/Ge of the tutorial, backward ddt, 2 PIMPLE "
+                         f"correctors, PCG 1e-12 (Vm, phiE), Gauss linear gradients"),
+            "value": cells / (ms * 1e-3), "unit": "cell-steps/s", "ms_per_step": ms,
+            "steps": args.bidomain_steps,
+            "pcg_iterations_per_step": {"vm": its_v, "phie": its_e},
+            "cpu_oracle": {"value": cells * ks / t_cpu, "unit": "cell-steps/s", "cores": 1,
+                           "kind": "port", "sample": f"the first {ks} steps, DIC preconditioner"},
+            "gpu_vs_oracle_after_sample": {
+                "vm_max_rel": float(np.max(np.abs(g_vm - B.tissue.vm())) /
+                                    np.max(np.abs(B.tissue.vm()))),
+                "phie_max_rel": float(np.max(np.abs(g_pe - B.phie())) / np.max(np.abs(B.phie())))}}
+
+
 def ecg_timing(L, source, launches: int = 50):
     """Both arithmetic forms of the pseudo-ECG (float pairs, the default, and
     FP64 multiply-adds), each timed as below."""
@@ -692,6 +768,11 @@ def main():
     ap.add_argument("--adjoint-steps", type=int, default=20000)
     ap.add_argument("--adjoint-fd-directions", type=int, default=2)
     ap.add_argument("--adjoint-check-steps", type=int, default=2000)
+    ap.add_argument("--no-bidomain", action="store_true", help="skip the bidomain case")
+    ap.add_argument("--bidomain-only", action="store_true")
+    ap.add_argument("--bidomain-cells", type=int, default=40)
+    ap.add_argument("--bidomain-steps", type=int, default=20)
+    ap.add_argument("--bidomain-sample", type=int, default=3)
     ap.add_argument("--ecg-only", action="store_true",
                     help="time the pseudo-ECG kernel alone on the LV mesh (--lv-dims)")
     ap.add_argument("--ecg-launches", type=int, default=50)
@@ -729,6 +810,11 @@ def main():
         from cardiacfoam_gb300 import build as gpu_build
         gpu_build.build()
         print(json.dumps({"adjoint": adjoint_arm(args)}), flush=True)
+        return
+    if args.bidomain_only:
+        from cardiacfoam_gb300 import build as gpu_build
+        gpu_build.build()
+        print(json.dumps({"bidomain": bidomain_arm(args)}), flush=True)
         return
     if args.ecg_only:
         from cardiacfoam_gb300 import build as gpu_build
@@ -802,6 +888,8 @@ def main():
         out["adjoint"] = adjoint_arm(args)
     if not args.no_mms:
         out["manufactured_solution"] = mms_arm()
+    if not args.no_bidomain:
+        out["bidomain"] = bidomain_arm(args)
     if not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline()
         one = cpu_baseline(nthreads=1, cells_x=10, steps=5)

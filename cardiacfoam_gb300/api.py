@@ -430,6 +430,125 @@ class BatchCells:
     __del__ = close
 
 
+class Bidomain:
+    """MyocardiumDomain with the bidomainSolver on the GPU (cfg_bidomain_*,
+    bidomainSolver.C:36-263): Vm, phiE and phiI, FP64 diffusion.  The mesh
+    needs its full geometry; sigma_i / sigma_e are the uniform intra- and
+    extracellular conductivity tensors (xx xy xz yy yz zz)."""
+
+    def __init__(self, mesh: LduMesh, model="TNNP", tissue="epicardialCells",
+                 sigma_i=(0.17, 0.0, 0.0, 0.019, 0.0, 0.019),
+                 sigma_e=(0.62, 0.0, 0.0, 0.24, 0.0, 0.24), chi=140000.0, cm=0.01, dt=1e-5,
+                 precision=_L.PRECISION_FP64, ddt_backward=True, pcg_tol=1e-8, pcg_rel_tol=0.0,
+                 pcg_max_iter=1000, phie_tol=1e-8, phie_rel_tol=0.0, phie_max_iter=1000,
+                 n_outer=1, outer_tol=0.0, vm0=-0.084, ref_point=(0.0, 0.0, 0.0),
+                 ref_value=0.0, boxes: Sequence = (), ode=None, max_steps=10 ** 6,
+                 grad_scheme=_L.GRAD_LEAST_SQUARES):
+        self._lib = _L.load()
+        if not mesh.has_geometry:
+            raise ValueError("the bidomain step needs a mesh with its full geometry")
+        self.mesh = mesh
+        self.n = mesh.n_cells
+        keep: list = []
+        d = _L.BidomainDesc()
+        d.ionic = ionic_desc(model, tissue, mesh.n_cells, dt, False, precision,
+                             ode if ode is not None else ode_desc(max_steps=max_steps),
+                             None, None, None, keep)
+        for i in range(6):
+            d.conductivity_i[i] = sigma_i[i]
+            d.conductivity_e[i] = sigma_e[i]
+        d.chi, d.cm = chi, cm
+        d.ddt_backward = int(ddt_backward)
+        d.pcg_tol, d.pcg_rel_tol, d.pcg_max_iter = pcg_tol, pcg_rel_tol, pcg_max_iter
+        d.phie_tol, d.phie_rel_tol, d.phie_max_iter = phie_tol, phie_rel_tol, phie_max_iter
+        d.n_outer, d.outer_tol, d.vm0 = n_outer, outer_tol, vm0
+        for k in range(3):
+            d.ref_point[k] = ref_point[k]
+        d.ref_value = ref_value
+        d.n_boxes = len(boxes)
+        for b, (lo, hi, t0, dur, inten) in enumerate(boxes):
+            for k in range(3):
+                d.box_min[b][k] = lo[k]
+                d.box_max[b][k] = hi[k]
+            d.box_start[b], d.box_duration[b], d.box_intensity[b] = t0, dur, inten
+        d.grad_scheme = int(grad_scheme)
+        md, keep2 = mesh_desc(mesh, structured=False)
+        h = C.c_void_p()
+        _L.check(self._lib.cfg_bidomain_create(C.byref(d), C.byref(md), C.byref(h)))
+        self.h = h
+
+    def step(self, dt: float):
+        _L.check(self._lib.cfg_bidomain_step(self.h, dt))
+
+    def run(self, dt: float, n_steps: int):
+        _L.check(self._lib.cfg_bidomain_run(self.h, dt, n_steps))
+
+    def field(self, which: int) -> np.ndarray:
+        a = np.zeros(self.n)
+        _L.check(self._lib.cfg_bidomain_get_field(self.h, which, _L.dptr(a)))
+        return a
+
+    def set_field(self, which: int, a: np.ndarray):
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        _L.check(self._lib.cfg_bidomain_set_field(self.h, which, _L.dptr(a)))
+
+    def vm(self):
+        return self.field(_L.FIELD_VM)
+
+    def phie(self):
+        return self.field(_L.FIELD_PHIE)
+
+    def phii(self):
+        return self.field(_L.FIELD_PHII)
+
+    def iion(self):
+        return self.field(_L.FIELD_IION)
+
+    def activation(self):
+        return self.field(_L.FIELD_ACTIVATION)
+
+    def time(self) -> float:
+        return self._lib.cfg_bidomain_time(self.h)
+
+    def reference_cell(self) -> int:
+        return int(self._lib.cfg_bidomain_reference_cell(self.h))
+
+    def stats(self):
+        """((init, final, iterations) of the Vm solves, the same of the phiE
+        solves) of the last step."""
+        a, b = _L.StepStats(), _L.StepStats()
+        _L.check(self._lib.cfg_bidomain_last_stats(self.h, C.byref(a), C.byref(b)))
+        out = []
+        for s in (a, b):
+            k = min(s.n_solves, 16)
+            out.append((np.array(s.initial_residual[:k]), np.array(s.final_residual[:k]),
+                        np.array(s.iterations[:k])))
+        return tuple(out)
+
+    def states(self) -> np.ndarray:
+        ion = self._lib.cfg_bidomain_ionic(self.h)
+        ns = C.c_int()
+        _L.check(self._lib.cfg_ionic_num_states(ion, C.byref(ns)))
+        a = np.zeros((ns.value, self.n))
+        _L.check(self._lib.cfg_ionic_get_states(ion, _L.dptr(a)))
+        return a
+
+    def set_states(self, a: np.ndarray):
+        ion = self._lib.cfg_bidomain_ionic(self.h)
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        _L.check(self._lib.cfg_ionic_set_states(ion, _L.dptr(a)))
+
+    def stream(self) -> int:
+        return self._lib.cfg_bidomain_stream(self.h)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self._lib.cfg_bidomain_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+
 def ecg_electrodes(text: str, domain: Optional[str] = None):
     """(names, positions [n][3]) of an ecgDomains entry of an electroProperties
     text (ECGDomain::readElectrodes, ecgDomain.C:53-82), in the dictionary's

@@ -74,6 +74,7 @@ def _units():
     ecg_extra = [f"-D{k}={int(os.environ[k])}" for k in ("CFG_ECG_TILE", "CFG_ECG_STAGED_PER_SM")
                  if os.environ.get(k)]
     units.append(("ecg", CSRC / "ecg.cu", ecg_extra))
+    units.append(("bidomain", CSRC / "bidomain.cu", []))
     units.append(("adjoint", CSRC / "adjoint.cu", ["--use_fast_math"]))
     return units
 

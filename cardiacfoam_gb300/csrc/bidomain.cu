@@ -1,0 +1,822 @@
+// Bidomain step (BidomainSolver, bidomainSolver.C:36-263, in
+// MyocardiumDomain's staggered advance) on the GPU, FP64 diffusion.
+//
+// Per step: box stimulus, the ionic update (cfg_ionic, either form), then per
+// PIMPLE corrector
+//   phiE:  laplacian(Gi + Ge, phiE) == -div(Gi & grad(Vm)), setReference
+//   Vm:    chi Cm ddt(Vm) == laplacian(Gi, Vm) + div(Gi & grad(phiE))
+//                            - chi Cm Iion + src
+//   phiI = Vm + phiE,
+// and the activation time.  The two Laplacians are solved by diagonal-
+// preconditioned CG with lduMatrix's normFactor and L1 residual, the phiE one
+// in its negated (positive definite) form; the explicit divergence of
+// Gi & grad(x) is Gauss linear over the faces with gaussGrad's zeroGradient
+// wall values.  Operators are per-row ELL slots (column, the two Laplacian
+// coefficients, gradient weights, face area vector and interpolation
+// weight).  Meshes whose Laplacians need explicit non-orthogonal or
+// tangential corrections are rejected (CFG_ERR_UNSUPPORTED).
+//
+// The PCG runs as a kernel sequence with its scalars on the device: the host
+// enqueues iterations in chunks and reads one flag per chunk; iterations
+// after convergence return at once.  Reductions are per block, then summed in
+// block order by one block, so results are reproducible bit for bit.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "geometry.h"
+#include "host_common.h"
+#include "ionic_host.h"
+
+namespace {
+
+constexpr int kBlock = 256;
+constexpr int kChunk = 16;          // PCG iterations enqueued per host check
+constexpr int kMaxSolves = 16;
+
+struct BdOp {
+    long long n;
+    int width;
+    const int* col;             // [slot][cell]
+    const unsigned char* cnt;   // [cell]
+    const double* coef_i;       // [slot][cell] Laplacian coefficient of Gi
+    const double* coef_e;       // [slot][cell] of Gi + Ge
+    const double* gw;           // [3][slot][cell] gradient weight of (x_nb - x_c)
+    const double* sf;           // [3][slot][cell] face area vector (owner -> neighbour)
+    const double* w;            // [slot][cell] the face's owner interpolation weight
+    const unsigned char* own;   // [slot][cell] 1: the row cell owns the face
+    const double* bw;           // [3][cell] wall factor of the divergence
+    const double* vol;
+    double G[6];                // Gi: xx xy xz yy yz zz
+};
+
+struct PcgScalars {
+    double avg, normf, init_res, res, wArA, wApA, alpha, beta, abs_r;
+    double tol, rel;
+    int iter, max_iter, done, status;
+};
+
+__device__ __forceinline__ double block_sum(double v, double* sh)
+{
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) sh[warp] = v;
+    __syncthreads();
+    double s = 0.0;
+    if (threadIdx.x == 0)
+        for (int k = 0; k < kBlock / 32; ++k) s += sh[k];
+    return s;   // valid in thread 0
+}
+
+template <int K>
+__device__ __forceinline__ void write_partials(double (&v)[K], double* partial)
+{
+    __shared__ double sh[kBlock / 32];
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        const double s = block_sum(v[k], sh);
+        if (threadIdx.x == 0) partial[(long long)k * gridDim.x + blockIdx.x] = s;
+    }
+}
+
+// (M q)_c for M = diag - off-diagonal coefficients (lduMatrix::Amul order:
+// diagonal, then the row's slots in column order)
+__device__ __forceinline__ double amul(const BdOp& op, const double* coef, const double* diag,
+                                      const double* q, long long c)
+{
+    double acc = diag[c] * q[c];
+    const int k = op.cnt[c];
+    for (int e = 0; e < k; ++e) {
+        const long long i = (long long)e * op.n + c;
+        acc += (-coef[i]) * q[op.col[i]];
+    }
+    return acc;
+}
+
+__device__ __forceinline__ double row_sum(const BdOp& op, const double* coef, const double* diag,
+                                         long long c)
+{
+    double acc = diag[c];
+    const int k = op.cnt[c];
+    for (int e = 0; e < k; ++e) acc += -coef[(long long)e * op.n + c];
+    return acc;
+}
+
+__global__ void k_gradient(BdOp op, const double* __restrict__ x, double* __restrict__ g)
+{
+    const long long c = (long long)blockIdx.x * kBlock + threadIdx.x;
+    if (c >= op.n) return;
+    const long long wn = (long long)op.width * op.n;
+    const double xc = x[c];
+    double g0 = 0.0, g1 = 0.0, g2 = 0.0;
+    for (int e = 0; e < op.cnt[c]; ++e) {
+        const long long i = (long long)e * op.n + c;
+        const double dv = x[op.col[i]] - xc;
+        g0 += op.gw[i] * dv;
+        g1 += op.gw[wn + i] * dv;
+        g2 += op.gw[2 * wn + i] * dv;
+    }
+    g[c] = g0;
+    g[op.n + c] = g1;
+    g[2 * op.n + c] = g2;
+}
+
+__device__ __forceinline__ void gamma_g(const double* G, double g0, double g1, double g2,
+                                        double* u)
+{
+    u[0] = G[0] * g0 + G[1] * g1 + G[2] * g2;
+    u[1] = G[1] * g0 + G[3] * g1 + G[4] * g2;
+    u[2] = G[2] * g0 + G[4] * g1 + G[5] * g2;
+}
+
+// out_c = V_c (sum over faces of Sf . (G grad x)_f + walls) / V_c * ... as
+// fvc::div returns it per volume and the equation multiplies by V
+__global__ void k_div_gamma_grad(BdOp op, const double* __restrict__ g, double* __restrict__ out)
+{
+    const long long c = (long long)blockIdx.x * kBlock + threadIdx.x;
+    if (c >= op.n) return;
+    const long long n = op.n, wn = (long long)op.width * n;
+    double uc[3];
+    gamma_g(op.G, g[c], g[n + c], g[2 * n + c], uc);
+    double div = 0.0;
+    for (int e = 0; e < op.cnt[c]; ++e) {
+        const long long i = (long long)e * n + c;
+        const long long nb = op.col[i];
+        double un[3];
+        gamma_g(op.G, g[nb], g[n + nb], g[2 * n + nb], un);
+        const double w = op.w[i];
+        double uf[3];
+        if (op.own[i]) {
+            for (int k = 0; k < 3; ++k) uf[k] = w * (uc[k] - un[k]) + un[k];
+        } else {
+            for (int k = 0; k < 3; ++k) uf[k] = w * (un[k] - uc[k]) + uc[k];
+        }
+        const double flux = op.sf[i] * uf[0] + op.sf[wn + i] * uf[1] + op.sf[2 * wn + i] * uf[2];
+        div += op.own[i] ? flux : -flux;
+    }
+    div += op.bw[c] * g[c] + op.bw[n + c] * g[n + c] + op.bw[2 * n + c] * g[2 * n + c];
+    const double V = op.vol[c];
+    out[c] = V * (div / V);
+}
+
+struct StimArgs {
+    int n_boxes;
+    double lo[8][3], hi[8][3], start[8], dur[8], amp[8];
+};
+
+__global__ void k_stimulus(long long n, const double* __restrict__ centres, StimArgs s, double t0,
+                           double* __restrict__ src)
+{
+    const long long c = (long long)blockIdx.x * kBlock + threadIdx.x;
+    if (c >= n) return;
+    const double* p = centres + 3 * c;
+    double v = 0.0;
+    for (int b = 0; b < s.n_boxes; ++b) {
+        if (t0 < s.start[b] || t0 > s.start[b] + s.dur[b]) continue;
+        if (p[0] >= s.lo[b][0] && p[0] <= s.hi[b][0] && p[1] >= s.lo[b][1] && p[1] <= s.hi[b][1] &&
+            p[2] >= s.lo[b][2] && p[2] <= s.hi[b][2])
+            v += s.amp[b];
+    }
+    src[c] = v;
+}
+
+// phiE right-hand side and diagonal of the negated system: b = V div(Gi grad Vm)
+// (= -source), diag = sum of the coefficients; at the reference cell the
+// diagonal doubles and b gains the diagonal times the reference value
+__global__ void k_phie_system(BdOp op, const double* __restrict__ dv, long long ref,
+                              double ref_value, double* __restrict__ diag, double* __restrict__ b)
+{
+    const long long c = (long long)blockIdx.x * kBlock + threadIdx.x;
+    if (c >= op.n) return;
+    double d = 0.0;
+    for (int e = 0; e < op.cnt[c]; ++e) d -= op.coef_e[(long long)e * op.n + c];
+    // the reference form's diagonal is d (negative); setReference: source +=
+    // d * value, d += d; negated here
+    double bb = -(-dv[c]);
+    if (c == ref) {
+        bb = -((-dv[c]) + d * ref_value);
+        d = d + d;
+    }
+    diag[c] = -d;
+    b[c] = bb;
+}
+
+struct VmArgs {
+    double chicm, rdt, cft, cft0, cft00;
+    int backward;
+};
+
+// Vm system: diag = chi Cm ddt diagonal + sum of the Gi coefficients; b as
+// the reference assembles the source (ddt, -chi Cm Iion V, + src V) plus the
+// explicit V div(Gi grad phiE)
+__global__ void k_vm_system(BdOp op, VmArgs a, const double* __restrict__ vm_old,
+                            const double* __restrict__ vm_oldold, const double* __restrict__ iion,
+                            const double* __restrict__ src, const double* __restrict__ dp,
+                            double* __restrict__ diag, double* __restrict__ b)
+{
+    const long long c = (long long)blockIdx.x * kBlock + threadIdx.x;
+    if (c >= op.n) return;
+    const double V = op.vol[c];
+    double ddt_diag, ddt_src;
+    if (a.backward) {
+        ddt_diag = (a.cft * a.rdt) * V;
+        ddt_src = a.rdt * V * (a.cft0 * vm_old[c] - a.cft00 * vm_oldold[c]);
+    } else {
+        ddt_diag = a.rdt * V;
+        ddt_src = a.rdt * vm_old[c] * V;
+    }
+    double lapdiag = 0.0;
+    for (int e = 0; e < op.cnt[c]; ++e) lapdiag -= op.coef_i[(long long)e * op.n + c];
+    diag[c] = a.chicm * ddt_diag - lapdiag;
+    double bb = a.chicm * ddt_src;
+    double su = -(a.chicm * iion[c]) * V;
+    su = su + src[c] * V;
+    bb = bb + su;
+    b[c] = bb + dp[c];
+}
+
+// --- PCG kernels (device scalars in PcgScalars) ---------------------------
+
+__global__ void k_pcg_begin(BdOp op, const double* coef, const double* __restrict__ diag,
+                            const double* __restrict__ x, const double* __restrict__ b,
+                            double* __restrict__ ax, double* __restrict__ r, double* partial)
+{
+    const long long c = (long long)blockIdx.x * kBlock + threadIdx.x;
+    double v[2] = {0.0, 0.0};
+    if (c < op.n) {
+        const double a = amul(op, coef, diag, x, c);
+        const double rr = b[c] - a;
+        ax[c] = a;
+        r[c] = rr;
+        v[0] = x[c];
+        v[1] = fabs(rr);
+    }
+    write_partials<2>(v, partial);
+}
+
+__global__ void k_pcg_norm(BdOp op, const double* coef, const double* __restrict__ diag,
+                           const double* __restrict__ ax, const double* __restrict__ b,
+                           const double* __restrict__ r, double* __restrict__ z,
+                           const PcgScalars* st, double* partial)
+{
+    const long long c = (long long)blockIdx.x * kBlock + threadIdx.x;
+    double v[2] = {0.0, 0.0};
+    if (c < op.n) {
+        const double pa = row_sum(op, coef, diag, c) * st->avg;
+        v[0] = fabs(ax[c] - pa) + fabs(b[c] - pa);
+        const double zc = r[c] / diag[c];
+        z[c] = zc;
+        v[1] = zc * r[c];
+    }
+    write_partials<2>(v, partial);
+}
+
+// w = M z, p = z + beta p, M p = w + beta M p (linearity), sum p.Mp
+__global__ void k_pcg_direction(BdOp op, const double* coef, const double* __restrict__ diag,
+                                const double* __restrict__ z, double* __restrict__ p,
+                                double* __restrict__ ap, const PcgScalars* st, double* partial)
+{
+    if (st->done) return;
+    const long long c = (long long)blockIdx.x * kBlock + threadIdx.x;
+    double v[1] = {0.0};
+    if (c < op.n) {
+        const double w = amul(op, coef, diag, z, c);
+        double pc, qc;
+        if (st->iter == 0) {
+            pc = z[c];
+            qc = w;
+        } else {
+            pc = z[c] + st->beta * p[c];
+            qc = w + st->beta * ap[c];
+        }
+        p[c] = pc;
+        ap[c] = qc;
+        v[0] = qc * pc;
+    }
+    write_partials<1>(v, partial);
+}
+
+__global__ void k_pcg_update(long long n, const double* __restrict__ diag, double* __restrict__ x,
+                             double* __restrict__ r, double* __restrict__ z,
+                             const double* __restrict__ p, const double* __restrict__ ap,
+                             const PcgScalars* st, double* partial)
+{
+    if (st->done) return;
+    const long long c = (long long)blockIdx.x * kBlock + threadIdx.x;
+    double v[2] = {0.0, 0.0};
+    if (c < n) {
+        const double a = st->alpha;
+        x[c] = x[c] + a * p[c];
+        const double rr = r[c] - a * ap[c];
+        r[c] = rr;
+        const double zc = rr / diag[c];
+        z[c] = zc;
+        v[0] = fabs(rr);
+        v[1] = zc * rr;
+    }
+    write_partials<2>(v, partial);
+}
+
+// One block: the blocks' partial sums in block order, then the stage's
+// scalar update.  stage 0: begin; 1: norm; 2: direction; 3: update.
+__global__ void k_pcg_reduce(const double* partial, int nblocks, int nsums, int stage,
+                             long long n, PcgScalars* st)
+{
+    __shared__ double sh[kBlock / 32];
+    if (stage >= 2 && st->done) return;
+    double s[2] = {0.0, 0.0};
+    for (int k = 0; k < nsums; ++k) {
+        double v = 0.0;
+        for (int b = threadIdx.x; b < nblocks; b += kBlock) v += partial[(long long)k * nblocks + b];
+        s[k] = block_sum(v, sh);
+    }
+    if (threadIdx.x != 0) return;
+    const auto conv = [&](double rr) {
+        return rr < st->tol || (st->rel > 1e-20 && rr < st->rel * st->init_res);
+    };
+    if (stage == 0) {
+        st->avg = s[0] / double(n);
+        st->abs_r = s[1];
+    } else if (stage == 1) {
+        st->normf = s[0] + 1e-20;
+        st->init_res = st->abs_r / st->normf;
+        st->res = st->init_res;
+        st->wArA = s[1];
+        st->iter = 0;
+        st->status = 0;
+        st->done = conv(st->init_res) ? 1 : 0;
+    } else if (stage == 2) {
+        st->wApA = s[0];
+        if (fabs(st->wApA) / st->normf < 1e-300) st->done = 1;   // checkSingularity
+        else st->alpha = st->wArA / st->wApA;
+    } else {
+        st->res = s[0] / st->normf;
+        st->iter = st->iter + 1;
+        if (conv(st->res) || st->iter >= st->max_iter) {
+            if (!conv(st->res)) st->status = 1;
+            st->done = 1;
+        } else {
+            st->beta = s[1] / st->wArA;
+            st->wArA = s[1];
+        }
+    }
+}
+
+__global__ void k_phii(long long n, const double* vm, const double* phie, double* phii)
+{
+    const long long c = (long long)blockIdx.x * kBlock + threadIdx.x;
+    if (c < n) phii[c] = vm[c] + phie[c];
+}
+
+// MyocardiumDomain::updateActivationTime
+__global__ void k_activation(long long n, const double* vm, const double* vm_old, double old_time,
+                             double dt, unsigned char* calc, double* act)
+{
+    const long long c = (long long)blockIdx.x * kBlock + threadIdx.x;
+    if (c >= n) return;
+    if (calc[c] && vm[c] > 1e-15) {
+        calc[c] = 0;
+        const double w = (0.0 - vm_old[c]) / (vm[c] - vm_old[c]);
+        act[c] = old_time + w * dt;
+    }
+}
+
+}  // namespace
+
+struct cfg_bidomain {
+    cfg_ionic* ion = nullptr;
+    cudaStream_t stream = nullptr;
+    long long n = 0;
+    int blocks = 0;
+    BdOp op{};
+    // operator storage
+    int* d_col = nullptr;
+    unsigned char *d_cnt = nullptr, *d_own = nullptr;
+    double *d_coef_i = nullptr, *d_coef_e = nullptr, *d_gw = nullptr, *d_sf = nullptr,
+           *d_w = nullptr, *d_bw = nullptr, *d_vol = nullptr, *d_centres = nullptr;
+    // fields
+    double *d_vm = nullptr, *d_vm_old = nullptr, *d_vm_oldold = nullptr, *d_iion = nullptr,
+           *d_src = nullptr, *d_act = nullptr, *d_phie = nullptr, *d_phii = nullptr;
+    unsigned char* d_calc = nullptr;
+    // work
+    double *d_grad = nullptr, *d_dv = nullptr, *d_diag = nullptr, *d_b = nullptr, *d_r = nullptr,
+           *d_z = nullptr, *d_p = nullptr, *d_ap = nullptr, *d_ax = nullptr, *d_partial = nullptr;
+    PcgScalars* d_st = nullptr;
+    PcgScalars* h_st = nullptr;     // pinned
+    // settings
+    double chicm = 0.0;
+    bool backward = true;
+    double vm_tol = 1e-8, vm_rel = 0.0, e_tol = 1e-8, e_rel = 0.0;
+    int vm_max = 1000, e_max = 1000, n_outer = 1;
+    double outer_tol = 0.0;
+    long long ref = -1;
+    double ref_value = 0.0;
+    StimArgs stim{};
+    // state
+    double t = 0.0;
+    int n_old = 0;
+    cfg_step_stats vm_stats{}, e_stats{};
+};
+
+using namespace cfg;
+
+namespace {
+
+int pcg_solve(cfg_bidomain* bd, const double* coef, double* x, double tol, double rel, int max_iter,
+              cfg_step_stats& stats)
+{
+    cudaStream_t s = bd->stream;
+    const BdOp& op = bd->op;
+    const int nb = bd->blocks;
+    PcgScalars init{};
+    init.tol = tol;
+    init.rel = rel;
+    init.max_iter = max_iter;
+    *bd->h_st = init;
+    CFG_CUDA_TRY(cudaMemcpyAsync(bd->d_st, bd->h_st, sizeof(PcgScalars), cudaMemcpyHostToDevice, s));
+    k_pcg_begin<<<nb, kBlock, 0, s>>>(op, coef, bd->d_diag, x, bd->d_b, bd->d_ax, bd->d_r,
+                                      bd->d_partial);
+    k_pcg_reduce<<<1, kBlock, 0, s>>>(bd->d_partial, nb, 2, 0, op.n, bd->d_st);
+    k_pcg_norm<<<nb, kBlock, 0, s>>>(op, coef, bd->d_diag, bd->d_ax, bd->d_b, bd->d_r, bd->d_z,
+                                     bd->d_st, bd->d_partial);
+    k_pcg_reduce<<<1, kBlock, 0, s>>>(bd->d_partial, nb, 2, 1, op.n, bd->d_st);
+    CFG_CUDA_TRY(cudaGetLastError());
+    for (int it = 0;; it += kChunk) {
+        CFG_CUDA_TRY(cudaMemcpyAsync(bd->h_st, bd->d_st, sizeof(PcgScalars), cudaMemcpyDeviceToHost, s));
+        CFG_CUDA_TRY(cudaStreamSynchronize(s));
+        if (bd->h_st->done) break;
+        if (it > max_iter + kChunk) return fail(CFG_ERR_PCG, "bidomain PCG did not finish");
+        for (int k = 0; k < kChunk; ++k) {
+            k_pcg_direction<<<nb, kBlock, 0, s>>>(op, coef, bd->d_diag, bd->d_z, bd->d_p, bd->d_ap,
+                                                  bd->d_st, bd->d_partial);
+            k_pcg_reduce<<<1, kBlock, 0, s>>>(bd->d_partial, nb, 1, 2, op.n, bd->d_st);
+            k_pcg_update<<<nb, kBlock, 0, s>>>(op.n, bd->d_diag, x, bd->d_r, bd->d_z, bd->d_p,
+                                               bd->d_ap, bd->d_st, bd->d_partial);
+            k_pcg_reduce<<<1, kBlock, 0, s>>>(bd->d_partial, nb, 2, 3, op.n, bd->d_st);
+        }
+        CFG_CUDA_TRY(cudaGetLastError());
+    }
+    const PcgScalars& st = *bd->h_st;
+    const int k = stats.n_solves;
+    if (k < kMaxSolves) {
+        stats.iterations[k] = st.iter;
+        stats.initial_residual[k] = st.init_res;
+        stats.final_residual[k] = st.res;
+    }
+    stats.n_solves = k + 1;
+    if (st.status) return fail(CFG_ERR_PCG, "bidomain PCG reached maxIter (%d) at residual %g",
+                               max_iter, st.res);
+    return CFG_OK;
+}
+
+void div_gamma_grad(cfg_bidomain* bd, const double* x, double* out)
+{
+    k_gradient<<<bd->blocks, kBlock, 0, bd->stream>>>(bd->op, x, bd->d_grad);
+    k_div_gamma_grad<<<bd->blocks, kBlock, 0, bd->stream>>>(bd->op, bd->d_grad, out);
+}
+
+}  // namespace
+
+extern "C" int cfg_bidomain_destroy(cfg_bidomain* bd)
+{
+    if (!bd) return CFG_OK;
+    if (bd->stream) cudaStreamSynchronize(bd->stream);
+    for (double** p : {&bd->d_coef_i, &bd->d_coef_e, &bd->d_gw, &bd->d_sf, &bd->d_w, &bd->d_bw,
+                       &bd->d_vol, &bd->d_centres, &bd->d_vm, &bd->d_vm_old, &bd->d_vm_oldold,
+                       &bd->d_iion, &bd->d_src, &bd->d_act, &bd->d_phie, &bd->d_phii,
+                       &bd->d_grad, &bd->d_dv, &bd->d_diag, &bd->d_b, &bd->d_r, &bd->d_z,
+                       &bd->d_p, &bd->d_ap, &bd->d_ax, &bd->d_partial})
+        dfree(*p);
+    dfree(bd->d_col);
+    dfree(bd->d_cnt);
+    dfree(bd->d_own);
+    dfree(bd->d_calc);
+    dfree(bd->d_st);
+    if (bd->h_st) cudaFreeHost(bd->h_st);
+    if (bd->ion) cfg_ionic_destroy(bd->ion);
+    if (bd->stream) cudaStreamDestroy(bd->stream);
+    delete bd;
+    return CFG_OK;
+}
+
+extern "C" int cfg_bidomain_create(const cfg_bidomain_desc* d, const cfg_mesh_desc* m,
+                                   cfg_bidomain** out)
+{
+    clear_error();
+    if (!d || !m || !out) return fail(CFG_ERR_INVALID, "null argument");
+    *out = nullptr;
+    const long long n = m->n_cells, nf = m->n_faces;
+    if (n <= 0) return fail(CFG_ERR_INVALID, "the mesh has no cells");
+    if (d->ionic.n_cells != n)
+        return fail(CFG_ERR_INVALID, "ionic n_cells %lld != mesh cells %lld", d->ionic.n_cells, n);
+    if (!m->face_centres)
+        return fail(CFG_ERR_INVALID, "the bidomain step needs the mesh's full geometry");
+    if (d->n_outer < 1) return fail(CFG_ERR_INVALID, "nOuterCorrectors must be at least 1");
+    if (d->n_boxes < 0 || d->n_boxes > 8) return fail(CFG_ERR_INVALID, "0 to 8 stimulus boxes");
+    for (long long f = 0; f < nf; ++f) {
+        const int l = m->owner[f], u = m->neighbour[f];
+        if (l < 0 || u < 0 || l >= n || u >= n || l == u)
+            return fail(CFG_ERR_INVALID, "face %lld has invalid owner/neighbour %d/%d", f, l, u);
+    }
+    double ge[6];
+    for (int k = 0; k < 6; ++k) ge[k] = d->conductivity_i[k] + d->conductivity_e[k];
+    CorrectedOperator oi, oe;
+    if (int rc = assemble_corrected(m, d->conductivity_i, nullptr, d->grad_scheme, 0, oi)) return rc;
+    if (int rc = assemble_corrected(m, ge, nullptr, d->grad_scheme, 0, oe)) return rc;
+    // no explicit Laplacian correction may be needed: the non-orthogonal and
+    // tangential parts (k per face, the wall factor per cell) must vanish
+    double gmax = 0.0;
+    for (int k = 0; k < 6; ++k) gmax = std::max(gmax, std::fabs(ge[k]));
+    for (long long f = 0; f < nf; ++f) {
+        const double* S = m->face_sf + 3 * f;
+        const double scale = gmax * std::sqrt(S[0] * S[0] + S[1] * S[1] + S[2] * S[2]);
+        for (const CorrectedOperator* o : {&oi, &oe})
+            for (int k = 0; k < 3; ++k)
+                if (std::fabs(o->k[size_t(3 * f + k)]) > 1e-12 * scale)
+                    return fail(CFG_ERR_UNSUPPORTED,
+                                "face %lld needs an explicit Laplacian correction (non-orthogonal "
+                                "face or a conductivity not aligned with it): not built for the "
+                                "bidomain step", f);
+    }
+    for (long long c = 0; c < n; ++c)
+        for (const CorrectedOperator* o : {&oi, &oe})
+            for (int k = 0; k < 3; ++k)
+                if (std::fabs(o->bk[size_t(3 * c + k)]) > 1e-12 * gmax * std::cbrt(m->volumes[c]) *
+                                                               std::cbrt(m->volumes[c]))
+                    return fail(CFG_ERR_UNSUPPORTED,
+                                "cell %lld needs a wall correction of the Laplacian: not built for "
+                                "the bidomain step", c);
+    // ELL rows: (column, face, own) sorted by column
+    struct Entry {
+        int col;
+        long long face;
+        bool own;
+    };
+    std::vector<std::vector<Entry>> rows(static_cast<size_t>(n));
+    for (long long f = 0; f < nf; ++f) {
+        rows[size_t(m->owner[f])].push_back({m->neighbour[f], f, true});
+        rows[size_t(m->neighbour[f])].push_back({m->owner[f], f, false});
+    }
+    int width = 0;
+    for (auto& r : rows) {
+        std::stable_sort(r.begin(), r.end(), [](const Entry& a, const Entry& b) { return a.col < b.col; });
+        width = std::max(width, int(r.size()));
+    }
+    if (width > 255) return fail(CFG_ERR_INVALID, "cell with more than 255 faces");
+    width = std::max(width, 1);
+    const size_t slots = size_t(width) * size_t(n);
+    std::vector<int> col(slots, 0);
+    std::vector<unsigned char> cnt(static_cast<size_t>(n)), own(slots, 0);
+    std::vector<double> ci(slots, 0.0), ce(slots, 0.0), gw(3 * slots, 0.0), sf(3 * slots, 0.0),
+        wv(slots, 0.0), bw(3 * size_t(n), 0.0);
+    for (long long c = 0; c < n; ++c) {
+        const auto& r = rows[size_t(c)];
+        cnt[size_t(c)] = (unsigned char)r.size();
+        for (size_t q = 0; q < r.size(); ++q) {
+            const size_t i = q * size_t(n) + size_t(c);
+            const long long f = r[q].face;
+            col[i] = r[q].col;
+            own[i] = r[q].own ? 1 : 0;
+            ci[i] = oi.coeff[size_t(f)];
+            ce[i] = oe.coeff[size_t(f)];
+            wv[i] = oi.w[size_t(f)];
+            const double* g = r[q].own ? oi.g_own.data() : oi.g_nei.data();
+            for (int k = 0; k < 3; ++k) {
+                gw[size_t(k) * slots + i] = g[3 * f + k];
+                sf[size_t(k) * slots + i] = m->face_sf[3 * f + k];
+            }
+        }
+    }
+    // wall factor of the divergence: sum over the cell's wall faces of
+    // Gi Sf - ((Gi Sf).n) n, so that Sf . Gi (g - n (n.g)) = bw . g
+    const double* G = d->conductivity_i;
+    for (long long b = 0; b < m->n_boundary_faces; ++b) {
+        const double* S = m->boundary_sf + 3 * b;
+        const double mag = std::sqrt(S[0] * S[0] + S[1] * S[1] + S[2] * S[2]);
+        const double nn[3] = {S[0] / mag, S[1] / mag, S[2] / mag};
+        const double gs[3] = {G[0] * S[0] + G[1] * S[1] + G[2] * S[2],
+                              G[1] * S[0] + G[3] * S[1] + G[4] * S[2],
+                              G[2] * S[0] + G[4] * S[1] + G[5] * S[2]};
+        const double gn = gs[0] * nn[0] + gs[1] * nn[1] + gs[2] * nn[2];
+        const long long c = m->boundary_cell[b];
+        for (int k = 0; k < 3; ++k) bw[size_t(k) * size_t(n) + size_t(c)] += gs[k] - gn * nn[k];
+    }
+    // the reference cell: nearest centre, the first in cell order on ties
+    long long ref = 0;
+    double best = -1.0;
+    for (long long c = 0; c < n; ++c) {
+        const double* C = m->centres + 3 * c;
+        const double dd = (C[0] - d->ref_point[0]) * (C[0] - d->ref_point[0]) +
+                          (C[1] - d->ref_point[1]) * (C[1] - d->ref_point[1]) +
+                          (C[2] - d->ref_point[2]) * (C[2] - d->ref_point[2]);
+        if (best < 0.0 || dd < best) { best = dd; ref = c; }
+    }
+
+    auto* bd = new cfg_bidomain();
+    auto bail = [&](int rc) {
+        cfg_bidomain_destroy(bd);
+        return rc;
+    };
+    cudaError_t e = cudaStreamCreateWithFlags(&bd->stream, cudaStreamNonBlocking);
+    if (e) return bail(fail(CFG_ERR_CUDA, "stream: %s", cudaGetErrorString(e)));
+    if (int rc = ionic_create(&d->ionic, bd->stream, &bd->ion)) return bail(rc);
+    bd->n = n;
+    bd->blocks = int((n + kBlock - 1) / kBlock);
+    bd->chicm = d->chi * d->cm;
+    bd->backward = d->ddt_backward != 0;
+    bd->vm_tol = d->pcg_tol; bd->vm_rel = d->pcg_rel_tol; bd->vm_max = d->pcg_max_iter;
+    bd->e_tol = d->phie_tol; bd->e_rel = d->phie_rel_tol; bd->e_max = d->phie_max_iter;
+    bd->n_outer = d->n_outer;
+    bd->outer_tol = d->outer_tol;
+    bd->ref = ref;
+    bd->ref_value = d->ref_value;
+    bd->stim.n_boxes = d->n_boxes;
+    for (int b = 0; b < d->n_boxes; ++b) {
+        for (int k = 0; k < 3; ++k) {
+            bd->stim.lo[b][k] = d->box_min[b][k];
+            bd->stim.hi[b][k] = d->box_max[b][k];
+        }
+        bd->stim.start[b] = d->box_start[b];
+        bd->stim.dur[b] = d->box_duration[b];
+        bd->stim.amp[b] = d->box_intensity[b];
+    }
+    auto up = [&](auto** dst, const auto& v) -> cudaError_t {
+        cudaError_t err = dmalloc(dst, v.size());
+        if (!err) err = cudaMemcpy(*dst, v.data(), v.size() * sizeof(v[0]), cudaMemcpyHostToDevice);
+        return err;
+    };
+    std::vector<double> vol(m->volumes, m->volumes + n), cen(m->centres, m->centres + 3 * n);
+    if (!e) e = up(&bd->d_col, col);
+    if (!e) e = up(&bd->d_cnt, cnt);
+    if (!e) e = up(&bd->d_own, own);
+    if (!e) e = up(&bd->d_coef_i, ci);
+    if (!e) e = up(&bd->d_coef_e, ce);
+    if (!e) e = up(&bd->d_gw, gw);
+    if (!e) e = up(&bd->d_sf, sf);
+    if (!e) e = up(&bd->d_w, wv);
+    if (!e) e = up(&bd->d_bw, bw);
+    if (!e) e = up(&bd->d_vol, vol);
+    if (!e) e = up(&bd->d_centres, cen);
+    for (double** p : {&bd->d_vm, &bd->d_vm_old, &bd->d_vm_oldold, &bd->d_iion, &bd->d_src,
+                       &bd->d_act, &bd->d_phie, &bd->d_phii, &bd->d_dv, &bd->d_diag, &bd->d_b,
+                       &bd->d_r, &bd->d_z, &bd->d_p, &bd->d_ap, &bd->d_ax})
+        if (!e) e = dmalloc(p, size_t(n));
+    if (!e) e = dmalloc(&bd->d_grad, 3 * size_t(n));
+    if (!e) e = dmalloc(&bd->d_partial, 2 * size_t(bd->blocks));
+    if (!e) e = dmalloc(&bd->d_calc, size_t(n));
+    if (!e) e = dmalloc(&bd->d_st, 1);
+    if (!e) e = cudaMallocHost(reinterpret_cast<void**>(&bd->h_st), sizeof(PcgScalars));
+    if (e) return bail(fail(CFG_ERR_CUDA, "bidomain allocation: %s", cudaGetErrorString(e)));
+    std::vector<double> v0(size_t(n), d->vm0), zero(size_t(n), 0.0);
+    e = cudaMemcpy(bd->d_vm, v0.data(), size_t(n) * sizeof(double), cudaMemcpyHostToDevice);
+    for (double* p : {bd->d_iion, bd->d_src, bd->d_act, bd->d_phie, bd->d_phii, bd->d_p, bd->d_ap})
+        if (!e) e = cudaMemcpy(p, zero.data(), size_t(n) * sizeof(double), cudaMemcpyHostToDevice);
+    if (!e) e = cudaMemset(bd->d_calc, 1, size_t(n));
+    if (e) return bail(fail(CFG_ERR_CUDA, "bidomain initialisation: %s", cudaGetErrorString(e)));
+    BdOp& op = bd->op;
+    op.n = n;
+    op.width = width;
+    op.col = bd->d_col;
+    op.cnt = bd->d_cnt;
+    op.coef_i = bd->d_coef_i;
+    op.coef_e = bd->d_coef_e;
+    op.gw = bd->d_gw;
+    op.sf = bd->d_sf;
+    op.w = bd->d_w;
+    op.own = bd->d_own;
+    op.bw = bd->d_bw;
+    op.vol = bd->d_vol;
+    for (int k = 0; k < 6; ++k) op.G[k] = d->conductivity_i[k];
+    *out = bd;
+    return CFG_OK;
+}
+
+extern "C" int cfg_bidomain_step(cfg_bidomain* bd, double dt)
+{
+    if (!bd) return fail(CFG_ERR_INVALID, "null context");
+    if (!(dt > 0)) return fail(CFG_ERR_INVALID, "deltaT must be positive");
+    cudaStream_t s = bd->stream;
+    const long long n = bd->n;
+    const size_t bytes = size_t(n) * sizeof(double);
+    const int nb = bd->blocks;
+    // Time::operator++ and the old-time levels of Vm
+    bd->t = bd->t + dt;
+    if (bd->n_old >= 1) {
+        if (bd->n_old >= 2)
+            CFG_CUDA_TRY(cudaMemcpyAsync(bd->d_vm_oldold, bd->d_vm_old, bytes, cudaMemcpyDeviceToDevice, s));
+        CFG_CUDA_TRY(cudaMemcpyAsync(bd->d_vm_old, bd->d_vm, bytes, cudaMemcpyDeviceToDevice, s));
+    }
+    const double t0 = bd->t - dt;
+    k_stimulus<<<nb, kBlock, 0, s>>>(n, bd->d_centres, bd->stim, t0, bd->d_src);
+    if (int rc = cfg_ionic_solve_device(bd->ion, t0, dt, bd->d_vm, bd->d_iion)) return rc;
+    bd->vm_stats = cfg_step_stats{};
+    bd->e_stats = cfg_step_stats{};
+    bool converged = false;
+    for (int corr = 1; corr <= bd->n_outer && !converged; ++corr) {
+        if (corr > 1 && bd->vm_stats.n_solves > 0 &&
+            bd->vm_stats.initial_residual[std::min(bd->vm_stats.n_solves, kMaxSolves) - 1] <
+                bd->outer_tol)
+            converged = true;
+        // phiE
+        div_gamma_grad(bd, bd->d_vm, bd->d_dv);
+        k_phie_system<<<nb, kBlock, 0, s>>>(bd->op, bd->d_dv, bd->ref, bd->ref_value, bd->d_diag,
+                                            bd->d_b);
+        if (int rc = pcg_solve(bd, bd->op.coef_e, bd->d_phie, bd->e_tol, bd->e_rel, bd->e_max,
+                               bd->e_stats))
+            return rc;
+        // Vm: fvm::ddt creates the old-time levels on first access
+        double cft = 1.0, cft0 = 1.0, cft00 = 0.0;
+        if (bd->backward) {
+            const double dt0 = bd->n_old < 2 ? 1e15 : dt;
+            cft = 1 + dt / (dt + dt0);
+            cft00 = dt * dt / (dt0 * (dt + dt0));
+            cft0 = cft + cft00;
+        }
+        if (bd->n_old < 1) {
+            CFG_CUDA_TRY(cudaMemcpyAsync(bd->d_vm_old, bd->d_vm, bytes, cudaMemcpyDeviceToDevice, s));
+            bd->n_old = 1;
+        }
+        if (bd->backward && bd->n_old < 2) {
+            CFG_CUDA_TRY(cudaMemcpyAsync(bd->d_vm_oldold, bd->d_vm_old, bytes, cudaMemcpyDeviceToDevice, s));
+            bd->n_old = 2;
+        }
+        div_gamma_grad(bd, bd->d_phie, bd->d_dv);
+        VmArgs va{bd->chicm, 1.0 / dt, cft, cft0, cft00, bd->backward ? 1 : 0};
+        k_vm_system<<<nb, kBlock, 0, s>>>(bd->op, va, bd->d_vm_old, bd->d_vm_oldold, bd->d_iion,
+                                          bd->d_src, bd->d_dv, bd->d_diag, bd->d_b);
+        if (int rc = pcg_solve(bd, bd->op.coef_i, bd->d_vm, bd->vm_tol, bd->vm_rel, bd->vm_max,
+                               bd->vm_stats))
+            return rc;
+        k_phii<<<nb, kBlock, 0, s>>>(n, bd->d_vm, bd->d_phie, bd->d_phii);
+    }
+    if (bd->n_old < 1) {
+        CFG_CUDA_TRY(cudaMemcpyAsync(bd->d_vm_old, bd->d_vm, bytes, cudaMemcpyDeviceToDevice, s));
+        bd->n_old = 1;
+    }
+    k_activation<<<nb, kBlock, 0, s>>>(n, bd->d_vm, bd->d_vm_old, bd->t - dt, dt, bd->d_calc,
+                                       bd->d_act);
+    CFG_CUDA_TRY(cudaGetLastError());
+    if (int rc = ionic_check_status(bd->ion)) return rc;
+    return CFG_OK;
+}
+
+extern "C" int cfg_bidomain_run(cfg_bidomain* bd, double dt, long long n_steps)
+{
+    for (long long i = 0; i < n_steps; ++i)
+        if (int rc = cfg_bidomain_step(bd, dt)) return rc;
+    return CFG_OK;
+}
+
+static double* bidomain_field(cfg_bidomain* bd, int field)
+{
+    switch (field) {
+    case CFG_FIELD_VM: return bd->d_vm;
+    case CFG_FIELD_IION: return bd->d_iion;
+    case CFG_FIELD_ACTIVATION: return bd->d_act;
+    case CFG_FIELD_SOURCE: return bd->d_src;
+    case CFG_FIELD_VM_OLD: return bd->d_vm_old;
+    case CFG_FIELD_PHIE: return bd->d_phie;
+    case CFG_FIELD_PHII: return bd->d_phii;
+    default: return nullptr;
+    }
+}
+
+extern "C" int cfg_bidomain_get_field(cfg_bidomain* bd, int field, double* host)
+{
+    if (!bd || !host) return fail(CFG_ERR_INVALID, "null argument");
+    double* p = bidomain_field(bd, field);
+    if (!p) return fail(CFG_ERR_INVALID, "unknown field %d", field);
+    CFG_CUDA_TRY(cudaMemcpyAsync(host, p, size_t(bd->n) * sizeof(double), cudaMemcpyDeviceToHost,
+                                 bd->stream));
+    CFG_CUDA_TRY(cudaStreamSynchronize(bd->stream));
+    return CFG_OK;
+}
+
+extern "C" int cfg_bidomain_set_field(cfg_bidomain* bd, int field, const double* host)
+{
+    if (!bd || !host) return fail(CFG_ERR_INVALID, "null argument");
+    double* p = bidomain_field(bd, field);
+    if (!p) return fail(CFG_ERR_INVALID, "unknown field %d", field);
+    CFG_CUDA_TRY(cudaMemcpyAsync(p, host, size_t(bd->n) * sizeof(double), cudaMemcpyHostToDevice,
+                                 bd->stream));
+    CFG_CUDA_TRY(cudaStreamSynchronize(bd->stream));
+    return CFG_OK;
+}
+
+extern "C" int cfg_bidomain_last_stats(const cfg_bidomain* bd, cfg_step_stats* vm,
+                                       cfg_step_stats* phie)
+{
+    if (!bd) return fail(CFG_ERR_INVALID, "null context");
+    if (vm) *vm = bd->vm_stats;
+    if (phie) *phie = bd->e_stats;
+    return CFG_OK;
+}
+
+extern "C" double cfg_bidomain_time(const cfg_bidomain* bd) { return bd ? bd->t : 0.0; }
+extern "C" long long cfg_bidomain_reference_cell(const cfg_bidomain* bd) { return bd ? bd->ref : -1; }
+extern "C" cfg_ionic* cfg_bidomain_ionic(cfg_bidomain* bd) { return bd ? bd->ion : nullptr; }
+extern "C" void* cfg_bidomain_stream(cfg_bidomain* bd) { return bd ? bd->stream : nullptr; }

@@ -25,7 +25,7 @@ CFG_ERR_PCG = 16
 CFG_ERR_UNSUPPORTED = 32
 PRECISION_FP64 = 0
 PRECISION_MIXED = 1
-FIELD_VM, FIELD_IION, FIELD_ACTIVATION, FIELD_SOURCE, FIELD_VM_OLD = range(5)
+FIELD_VM, FIELD_IION, FIELD_ACTIVATION, FIELD_SOURCE, FIELD_VM_OLD, FIELD_PHIE, FIELD_PHII = range(7)
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
@@ -123,6 +123,19 @@ class AdjointDesc(C.Structure):
 
 
 # every symbol declared in include/cardiac_gpu.h
+class BidomainDesc(C.Structure):
+    _fields_ = [("ionic", IonicDesc), ("conductivity_i", C.c_double * 6),
+                ("conductivity_e", C.c_double * 6), ("chi", C.c_double), ("cm", C.c_double),
+                ("ddt_backward", C.c_int), ("pcg_tol", C.c_double), ("pcg_rel_tol", C.c_double),
+                ("pcg_max_iter", C.c_int), ("phie_tol", C.c_double),
+                ("phie_rel_tol", C.c_double), ("phie_max_iter", C.c_int), ("n_outer", C.c_int),
+                ("outer_tol", C.c_double), ("vm0", C.c_double), ("ref_point", C.c_double * 3),
+                ("ref_value", C.c_double), ("n_boxes", C.c_int),
+                ("box_min", (C.c_double * 3) * 8), ("box_max", (C.c_double * 3) * 8),
+                ("box_start", C.c_double * 8), ("box_duration", C.c_double * 8),
+                ("box_intensity", C.c_double * 8), ("grad_scheme", C.c_int)]
+
+
 class PseudoEcgDesc(C.Structure):
     _fields_ = [("conductivity", C.c_double * 6), ("conductivity_per_cell", _dp),
                 ("grad_scheme", C.c_int), ("n_electrodes", C.c_int), ("electrodes", _dp),
@@ -146,6 +159,10 @@ EXPORTS = [
     "cfg_pseudo_ecg_create", "cfg_pseudo_ecg_compute", "cfg_pseudo_ecg_compute_monodomain",
     "cfg_pseudo_ecg_record", "cfg_pseudo_ecg_record_field", "cfg_pseudo_ecg_series", "cfg_pseudo_ecg_reset",
     "cfg_pseudo_ecg_destroy", "cfg_pseudo_ecg_electrodes_from_dict",
+    "cfg_bidomain_create", "cfg_bidomain_step", "cfg_bidomain_run", "cfg_bidomain_get_field",
+    "cfg_bidomain_set_field", "cfg_bidomain_last_stats", "cfg_bidomain_time",
+    "cfg_bidomain_reference_cell", "cfg_bidomain_ionic", "cfg_bidomain_stream",
+    "cfg_bidomain_destroy",
 ]
 
 _lib = None
@@ -232,6 +249,22 @@ def load(path: Optional[os.PathLike] = None):
     L.cfg_pseudo_ecg_destroy.argtypes = [C.c_void_p]
     L.cfg_pseudo_ecg_electrodes_from_dict.argtypes = [C.c_char_p, C.c_char_p, C.c_char_p,
                                                       C.c_size_t, _dp, C.c_int, _ip]
+    L.cfg_bidomain_create.argtypes = [C.POINTER(BidomainDesc), C.POINTER(MeshDesc),
+                                      C.POINTER(C.c_void_p)]
+    L.cfg_bidomain_step.argtypes = [C.c_void_p, C.c_double]
+    L.cfg_bidomain_run.argtypes = [C.c_void_p, C.c_double, C.c_longlong]
+    L.cfg_bidomain_get_field.argtypes = [C.c_void_p, C.c_int, _dp]
+    L.cfg_bidomain_set_field.argtypes = [C.c_void_p, C.c_int, _dp]
+    L.cfg_bidomain_last_stats.argtypes = [C.c_void_p, C.POINTER(StepStats), C.POINTER(StepStats)]
+    L.cfg_bidomain_time.argtypes = [C.c_void_p]
+    L.cfg_bidomain_time.restype = C.c_double
+    L.cfg_bidomain_reference_cell.argtypes = [C.c_void_p]
+    L.cfg_bidomain_reference_cell.restype = C.c_longlong
+    L.cfg_bidomain_ionic.argtypes = [C.c_void_p]
+    L.cfg_bidomain_ionic.restype = C.c_void_p
+    L.cfg_bidomain_stream.argtypes = [C.c_void_p]
+    L.cfg_bidomain_stream.restype = C.c_void_p
+    L.cfg_bidomain_destroy.argtypes = [C.c_void_p]
     L.cfg_box_diffusion_solve_noalloc.argtypes = [C.POINTER(BoxDiffusionDesc), C.c_double,
                                                   C.c_void_p, C.c_void_p, C.c_void_p,
                                                   C.c_void_p, C.c_void_p,

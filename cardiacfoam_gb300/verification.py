@@ -186,3 +186,65 @@ def run(dim: int, n: int, dt: float | None = None, end_time: float = END_TIME,
         pe.close()
     md.close()
     return out
+
+
+# --------------------------------------------------------------------- bidomain
+# tutorials/manufacturedSolutions/bidomain/constant/electroProperties
+BIDOMAIN_SIGMA_I = SIGMA
+BIDOMAIN_SIGMA_E = (0.046165469, 0.0, 0.0, 0.050362330, 0.0, 0.012590582)
+BIDOMAIN_K = 0.7071067811865476
+BIDOMAIN_REF_POINT = (0.125, 0.05, 0.05)
+
+
+def bidomain_shift(t: float, dim: int, k: float = BIDOMAIN_K, ref_point=BIDOMAIN_REF_POINT,
+                   ref_value: float = 0.0) -> float:
+    """manufacturedFDABidomainShift (manufacturedFDABidomainReference.H:28-45):
+    phiE's constant, so that the exact phiE equals ref_value at ref_point."""
+    F = manufactured_fields(np.array([ref_point], dtype=np.float64), 0.0, dim)[0][0]
+    return ref_value + k * math.sqrt(1.0 + t) * F
+
+
+def bidomain_fields(centres: np.ndarray, t: float, dim: int, k: float = BIDOMAIN_K,
+                    ref_point=BIDOMAIN_REF_POINT, ref_value: float = 0.0):
+    """Exact V, phiE = -k sqrt(1 + t) F + shift, phiI = V + phiE, u1, u2, u3
+    (computeManufacturedBidomainPhiE/PhiI, manufacturedFDABidomainReference.H:
+    47-100; V and u as the monodomain case)."""
+    V, u1, u2, u3 = manufactured_fields(centres, t, dim)
+    F = manufactured_fields(centres, 0.0, dim)[0]
+    phie = (-k * math.sqrt(1.0 + t)) * F + bidomain_shift(t, dim, k, ref_point, ref_value)
+    return V, phie, V + phie, u1, u2, u3
+
+
+def run_bidomain(dim: int, n: int, dt: float | None = None, end_time: float = END_TIME,
+                 precision: int = _L.PRECISION_FP64, pcg_tol: float = 1e-12,
+                 phie_tol: float = 1e-12, steps: int | None = None) -> Dict:
+    """The bidomain tutorial's manufactured case on the GPU (bidomainSolver,
+    bidomainFDAManufactured, Gi and Ge of the tutorial, phiERefPoint
+    (0.125 0.05 0.05), backward ddt, two PIMPLE correctors, Gauss linear
+    gradients): norms of V, phiE, phiI, u1 and u2 at the end, as
+    manufacturedFDABidomainVerifier computes them.  The tutorial's PCG
+    tolerance is 1e-15 for both fields; at 1e-12 the solves converge instead
+    of running to maxIter, and the discretisation error is orders of
+    magnitude larger."""
+    dt = SWEEP[n] if dt is None else dt
+    mesh = geometry_mesh_for(dim, n)
+    bd = api.Bidomain(mesh, model="bidomainFDAManufactured", tissue=f"{dim}D",
+                      sigma_i=BIDOMAIN_SIGMA_I, sigma_e=BIDOMAIN_SIGMA_E, chi=CHI, cm=CM, dt=dt,
+                      precision=precision, ddt_backward=True, pcg_tol=pcg_tol, pcg_rel_tol=0.0,
+                      pcg_max_iter=2000, phie_tol=phie_tol, phie_rel_tol=0.0,
+                      phie_max_iter=4000, n_outer=2, outer_tol=0.0,
+                      ref_point=BIDOMAIN_REF_POINT, grad_scheme=_L.GRAD_GAUSS_LINEAR)
+    V, phie, _, u1, u2, u3 = bidomain_fields(mesh.centres, 0.0, dim)
+    bd.set_field(_L.FIELD_VM, V)
+    bd.set_field(_L.FIELD_PHIE, phie)
+    bd.set_states(np.stack([V, u1, u2, u3]))
+    steps = int(round(end_time / dt)) if steps is None else steps
+    bd.run(dt, steps)
+    t = bd.time()
+    Ve, pe, pie, u1e, u2e, _ = bidomain_fields(mesh.centres, t, dim)
+    st = bd.states()
+    out = {"dim": dim, "n": n, "dt": dt, "steps": steps, "t": t,
+           "V": norms(bd.vm(), Ve), "phiE": norms(bd.phie(), pe), "phiI": norms(bd.phii(), pie),
+           "u1": norms(st[1], u1e), "u2": norms(st[2], u2e)}
+    bd.close()
+    return out

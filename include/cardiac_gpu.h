@@ -262,6 +262,8 @@ int cfg_monodomain_set_graph(cfg_monodomain* md, int enable);
 #define CFG_FIELD_ACTIVATION 2      /* activationTime [s] */
 #define CFG_FIELD_SOURCE 3          /* externalStimulusCurrent [A/m^3] */
 #define CFG_FIELD_VM_OLD 4          /* Vm.oldTime() [V] */
+#define CFG_FIELD_PHIE 5            /* bidomain: extracellular potential phiE [V] */
+#define CFG_FIELD_PHII 6            /* bidomain: intracellular potential phiI = Vm + phiE [V] */
 
 /* Host copies of the domain's fields (written at output times only). */
 int cfg_monodomain_get_field(cfg_monodomain* md, int field, double* host);
@@ -393,6 +395,61 @@ int cfg_adjoint_forward(cfg_adjoint* adj, const double* log_gna, const double* l
 int cfg_adjoint_backward(cfg_adjoint* adj, double* grad_log_gna, double* grad_log_gk1,
                          double* grad_sigma);
 int cfg_adjoint_destroy(cfg_adjoint* adj);
+
+/* ------------------------------------------------------------- bidomain
+ * MyocardiumDomain with myocardiumSolver bidomainSolver (bidomainSolver.C:
+ * 36-263): per PIMPLE corrector
+ *   fvm::laplacian(Gi + Ge, phiE) == -fvc::div(Gi & fvc::grad(Vm)),
+ *     setReference(the cell at phiERefPoint, phiEReferenceValue, true);
+ *   chi Cm fvm::ddt(Vm) == fvm::laplacian(Gi, Vm) + fvc::div(Gi & fvc::grad(phiE))
+ *     - chi Cm Iion + src;
+ *   phiI = Vm + phiE,
+ * after the box stimulus and the ionic update of the step, then the
+ * activation time.  Diffusion in FP64 with diagonal-preconditioned PCG (the
+ * reference's lduMatrix convergence test); gradients by gradSchemes default,
+ * divergence Gauss linear.  Uniform conductivity tensors; the mesh needs its
+ * full geometry, and meshes whose Laplacians need explicit non-orthogonal or
+ * tangential corrections are CFG_ERR_UNSUPPORTED.  The reference cell is the
+ * cell whose centre is nearest to ref_point (the first on ties). */
+typedef struct cfg_bidomain_desc {
+    cfg_ionic_desc ionic;            /* n_cells must equal the mesh's */
+    double conductivity_i[6];        /* conductivityIntracellular xx xy xz yy yz zz */
+    double conductivity_e[6];        /* conductivityExtracellular */
+    double chi, cm;
+    int ddt_backward;                /* ddt(Vm) backward (1) / Euler (0) */
+    double pcg_tol, pcg_rel_tol;     /* Vm solver */
+    int pcg_max_iter;
+    double phie_tol, phie_rel_tol;   /* phiE solver */
+    int phie_max_iter;
+    int n_outer;                     /* PIMPLE nOuterCorrectors */
+    double outer_tol;                /* residualControl on Vm (0: none) */
+    double vm0;                      /* initial Vm [V] */
+    double ref_point[3];             /* phiERefPoint */
+    double ref_value;                /* phiEReferenceValue */
+    int n_boxes;
+    double box_min[8][3], box_max[8][3];
+    double box_start[8], box_duration[8], box_intensity[8];
+    int grad_scheme;                 /* CFG_GRAD_* */
+} cfg_bidomain_desc;
+
+typedef struct cfg_bidomain cfg_bidomain;
+
+int cfg_bidomain_create(const cfg_bidomain_desc* desc, const cfg_mesh_desc* mesh,
+                        cfg_bidomain** out);
+/* One time step (runTime++ then the staggered advance, as
+ * cfg_monodomain_step). */
+int cfg_bidomain_step(cfg_bidomain* bd, double dt);
+int cfg_bidomain_run(cfg_bidomain* bd, double dt, long long n_steps);
+/* CFG_FIELD_VM, _IION, _ACTIVATION, _SOURCE, _VM_OLD, _PHIE, _PHII */
+int cfg_bidomain_get_field(cfg_bidomain* bd, int field, double* host);
+int cfg_bidomain_set_field(cfg_bidomain* bd, int field, const double* host);
+/* The last step's Vm and phiE solves (one of each per corrector). */
+int cfg_bidomain_last_stats(const cfg_bidomain* bd, cfg_step_stats* vm, cfg_step_stats* phie);
+double cfg_bidomain_time(const cfg_bidomain* bd);
+long long cfg_bidomain_reference_cell(const cfg_bidomain* bd);
+cfg_ionic* cfg_bidomain_ionic(cfg_bidomain* bd);
+void* cfg_bidomain_stream(cfg_bidomain* bd);
+int cfg_bidomain_destroy(cfg_bidomain* bd);
 
 /* ----------------------------------------------------------- pseudo-ECG
  * ECGDomain with the pseudoECG solver (ecgDomain.C:119-159,

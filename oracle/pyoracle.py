@@ -496,6 +496,9 @@ class Bidomain:
     def phii(self):
         return np.ctypeslib.as_array(lib().oracle_bidomain_phii(self.h), shape=(self.n,)).copy()
 
+    def set_phie(self, a):
+        np.ctypeslib.as_array(lib().oracle_bidomain_phie(self.h), shape=(self.n,))[:] = a
+
     def ref_cell(self) -> int:
         return int(lib().oracle_bidomain_ref_cell(self.h))
 
