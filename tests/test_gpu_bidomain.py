@@ -93,9 +93,12 @@ def test_tnnp_slab_matches_oracle(gpu_lib, oracle):
 @pytest.mark.gpu
 def test_manufactured_convergence(gpu_lib):
     """The tutorial's 3D case at 10 and 20 cells to t = 0.2 s: Vm and phiE
-    (up to its reference constant) at second order."""
+    (up to its reference constant) converge towards second order (the
+    oracle's rates on the same meshes: L1/L2/Linf of Vm 1.69/1.74/1.65, phiE
+    1.76, still pre-asymptotic at 10 cells; 1D reaches 1.99)."""
     r = [V.run_bidomain(3, n) for n in (10, 20)]
-    assert V.rate(r[0]["V"][2], r[1]["V"][2], 10, 20) > 1.8
+    assert V.rate(r[0]["V"][1], r[1]["V"][1], 10, 20) > 1.6
+    assert V.rate(r[0]["V"][2], r[1]["V"][2], 10, 20) > 1.6
     errs = []
     for n in (10, 20):
         mesh, bd = _gpu_mms(3, n, V.SWEEP[n])
@@ -104,7 +107,7 @@ def test_manufactured_convergence(gpu_lib):
         e = bd.phie() - pe
         errs.append(np.max(np.abs(e - e.mean())))
         bd.close()
-    assert V.rate(errs[0], errs[1], 10, 20) > 1.8
+    assert V.rate(errs[0], errs[1], 10, 20) > 1.6
 
 
 @pytest.mark.gpu
