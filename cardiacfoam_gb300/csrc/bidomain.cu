@@ -16,10 +16,12 @@
 // weight).  Meshes whose Laplacians need explicit non-orthogonal or
 // tangential corrections are rejected (CFG_ERR_UNSUPPORTED).
 //
-// The PCG runs as a kernel sequence with its scalars on the device: the host
-// enqueues iterations in chunks and reads one flag per chunk; iterations
-// after convergence return at once.  Reductions are per block, then summed in
-// block order by one block, so results are reproducible bit for bit.
+// The PCG runs as a kernel sequence with its scalars on the device, two
+// launches per iteration (each kernel's last block finishes the reduction and
+// the scalar update); chunks of iterations are replayed from a CUDA graph and
+// the host reads one flag per chunk; iterations after convergence return at
+// once.  Reductions add the blocks' sums in block order, so results are
+// reproducible bit for bit.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -70,17 +72,6 @@ __device__ __forceinline__ double block_sum(double v, double* sh)
     if (threadIdx.x == 0)
         for (int k = 0; k < kBlock / 32; ++k) s += sh[k];
     return s;   // valid in thread 0
-}
-
-template <int K>
-__device__ __forceinline__ void write_partials(double (&v)[K], double* partial)
-{
-    __shared__ double sh[kBlock / 32];
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-        const double s = block_sum(v[k], sh);
-        if (threadIdx.x == 0) partial[(long long)k * gridDim.x + blockIdx.x] = s;
-    }
 }
 
 // (M q)_c for M = diag - off-diagonal coefficients (lduMatrix::Amul order:
@@ -240,101 +231,38 @@ __global__ void k_vm_system(BdOp op, VmArgs a, const double* __restrict__ vm_old
 }
 
 // --- PCG kernels (device scalars in PcgScalars) ---------------------------
+// Each kernel ends with its reduction: the blocks' sums go to the partial
+// buffer, and the last block to finish (a ticket counter) adds them in block
+// order and updates the scalars of its stage (0: begin, 1: norm, 2:
+// direction, 3: update), so an iteration is two launches.
 
-__global__ void k_pcg_begin(BdOp op, const double* coef, const double* __restrict__ diag,
-                            const double* __restrict__ x, const double* __restrict__ b,
-                            double* __restrict__ ax, double* __restrict__ r, double* partial)
-{
-    const long long c = (long long)blockIdx.x * kBlock + threadIdx.x;
-    double v[2] = {0.0, 0.0};
-    if (c < op.n) {
-        const double a = amul(op, coef, diag, x, c);
-        const double rr = b[c] - a;
-        ax[c] = a;
-        r[c] = rr;
-        v[0] = x[c];
-        v[1] = fabs(rr);
-    }
-    write_partials<2>(v, partial);
-}
-
-__global__ void k_pcg_norm(BdOp op, const double* coef, const double* __restrict__ diag,
-                           const double* __restrict__ ax, const double* __restrict__ b,
-                           const double* __restrict__ r, double* __restrict__ z,
-                           const PcgScalars* st, double* partial)
-{
-    const long long c = (long long)blockIdx.x * kBlock + threadIdx.x;
-    double v[2] = {0.0, 0.0};
-    if (c < op.n) {
-        const double pa = row_sum(op, coef, diag, c) * st->avg;
-        v[0] = fabs(ax[c] - pa) + fabs(b[c] - pa);
-        const double zc = r[c] / diag[c];
-        z[c] = zc;
-        v[1] = zc * r[c];
-    }
-    write_partials<2>(v, partial);
-}
-
-// w = M z, p = z + beta p, M p = w + beta M p (linearity), sum p.Mp
-__global__ void k_pcg_direction(BdOp op, const double* coef, const double* __restrict__ diag,
-                                const double* __restrict__ z, double* __restrict__ p,
-                                double* __restrict__ ap, const PcgScalars* st, double* partial)
-{
-    if (st->done) return;
-    const long long c = (long long)blockIdx.x * kBlock + threadIdx.x;
-    double v[1] = {0.0};
-    if (c < op.n) {
-        const double w = amul(op, coef, diag, z, c);
-        double pc, qc;
-        if (st->iter == 0) {
-            pc = z[c];
-            qc = w;
-        } else {
-            pc = z[c] + st->beta * p[c];
-            qc = w + st->beta * ap[c];
-        }
-        p[c] = pc;
-        ap[c] = qc;
-        v[0] = qc * pc;
-    }
-    write_partials<1>(v, partial);
-}
-
-__global__ void k_pcg_update(long long n, const double* __restrict__ diag, double* __restrict__ x,
-                             double* __restrict__ r, double* __restrict__ z,
-                             const double* __restrict__ p, const double* __restrict__ ap,
-                             const PcgScalars* st, double* partial)
-{
-    if (st->done) return;
-    const long long c = (long long)blockIdx.x * kBlock + threadIdx.x;
-    double v[2] = {0.0, 0.0};
-    if (c < n) {
-        const double a = st->alpha;
-        x[c] = x[c] + a * p[c];
-        const double rr = r[c] - a * ap[c];
-        r[c] = rr;
-        const double zc = rr / diag[c];
-        z[c] = zc;
-        v[0] = fabs(rr);
-        v[1] = zc * rr;
-    }
-    write_partials<2>(v, partial);
-}
-
-// One block: the blocks' partial sums in block order, then the stage's
-// scalar update.  stage 0: begin; 1: norm; 2: direction; 3: update.
-__global__ void k_pcg_reduce(const double* partial, int nblocks, int nsums, int stage,
-                             long long n, PcgScalars* st)
+template <int K>
+__device__ __forceinline__ void stage_end(double (&v)[K], double* partial, unsigned* ticket,
+                                          int stage, long long n, PcgScalars* st)
 {
     __shared__ double sh[kBlock / 32];
-    if (stage >= 2 && st->done) return;
+    __shared__ bool last;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        const double s = block_sum(v[k], sh);
+        if (threadIdx.x == 0) partial[(long long)k * gridDim.x + blockIdx.x] = s;
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
     double s[2] = {0.0, 0.0};
-    for (int k = 0; k < nsums; ++k) {
-        double v = 0.0;
-        for (int b = threadIdx.x; b < nblocks; b += kBlock) v += partial[(long long)k * nblocks + b];
-        s[k] = block_sum(v, sh);
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        double a = 0.0;
+        for (int b = threadIdx.x; b < (int)gridDim.x; b += kBlock)
+            a += __ldcg(&partial[(long long)k * gridDim.x + b]);
+        s[k] = block_sum(a, sh);
     }
     if (threadIdx.x != 0) return;
+    *ticket = 0u;
     const auto conv = [&](double rr) {
         return rr < st->tol || (st->rel > 1e-20 && rr < st->rel * st->init_res);
     };
@@ -364,6 +292,86 @@ __global__ void k_pcg_reduce(const double* partial, int nblocks, int nsums, int 
             st->wArA = s[1];
         }
     }
+}
+
+struct PcgArgs {
+    BdOp op;
+    const double* coef;
+    const double* diag;
+    const double* b;
+    double *x, *ax, *r, *z, *p, *ap, *partial;
+    unsigned* ticket;
+    PcgScalars* st;
+};
+
+__global__ void k_pcg_begin(PcgArgs a)
+{
+    const long long c = (long long)blockIdx.x * kBlock + threadIdx.x;
+    double v[2] = {0.0, 0.0};
+    if (c < a.op.n) {
+        const double ax = amul(a.op, a.coef, a.diag, a.x, c);
+        const double rr = a.b[c] - ax;
+        a.ax[c] = ax;
+        a.r[c] = rr;
+        v[0] = a.x[c];
+        v[1] = fabs(rr);
+    }
+    stage_end<2>(v, a.partial, a.ticket, 0, a.op.n, a.st);
+}
+
+__global__ void k_pcg_norm(PcgArgs a)
+{
+    const long long c = (long long)blockIdx.x * kBlock + threadIdx.x;
+    double v[2] = {0.0, 0.0};
+    if (c < a.op.n) {
+        const double pa = row_sum(a.op, a.coef, a.diag, c) * a.st->avg;
+        v[0] = fabs(a.ax[c] - pa) + fabs(a.b[c] - pa);
+        const double zc = a.r[c] / a.diag[c];
+        a.z[c] = zc;
+        v[1] = zc * a.r[c];
+    }
+    stage_end<2>(v, a.partial, a.ticket, 1, a.op.n, a.st);
+}
+
+// w = M z, p = z + beta p, M p = w + beta M p (linearity), sum p.Mp
+__global__ void k_pcg_direction(PcgArgs a)
+{
+    if (a.st->done) return;
+    const long long c = (long long)blockIdx.x * kBlock + threadIdx.x;
+    double v[1] = {0.0};
+    if (c < a.op.n) {
+        const double w = amul(a.op, a.coef, a.diag, a.z, c);
+        double pc, qc;
+        if (a.st->iter == 0) {
+            pc = a.z[c];
+            qc = w;
+        } else {
+            pc = a.z[c] + a.st->beta * a.p[c];
+            qc = w + a.st->beta * a.ap[c];
+        }
+        a.p[c] = pc;
+        a.ap[c] = qc;
+        v[0] = qc * pc;
+    }
+    stage_end<1>(v, a.partial, a.ticket, 2, a.op.n, a.st);
+}
+
+__global__ void k_pcg_update(PcgArgs a)
+{
+    if (a.st->done) return;
+    const long long c = (long long)blockIdx.x * kBlock + threadIdx.x;
+    double v[2] = {0.0, 0.0};
+    if (c < a.op.n) {
+        const double al = a.st->alpha;
+        a.x[c] = a.x[c] + al * a.p[c];
+        const double rr = a.r[c] - al * a.ap[c];
+        a.r[c] = rr;
+        const double zc = rr / a.diag[c];
+        a.z[c] = zc;
+        v[0] = fabs(rr);
+        v[1] = zc * rr;
+    }
+    stage_end<2>(v, a.partial, a.ticket, 3, a.op.n, a.st);
 }
 
 __global__ void k_phii(long long n, const double* vm, const double* phie, double* phii)
@@ -407,6 +415,9 @@ struct cfg_bidomain {
            *d_z = nullptr, *d_p = nullptr, *d_ap = nullptr, *d_ax = nullptr, *d_partial = nullptr;
     PcgScalars* d_st = nullptr;
     PcgScalars* h_st = nullptr;     // pinned
+    unsigned* d_ticket = nullptr;
+    // kChunk PCG iterations of each system captured as a graph: [0] phiE, [1] Vm
+    cudaGraphExec_t chunk[2] = {nullptr, nullptr};
     // settings
     double chicm = 0.0;
     bool backward = true;
@@ -426,39 +437,60 @@ using namespace cfg;
 
 namespace {
 
-int pcg_solve(cfg_bidomain* bd, const double* coef, double* x, double tol, double rel, int max_iter,
+PcgArgs pcg_args(cfg_bidomain* bd, const double* coef, double* x)
+{
+    PcgArgs a{};
+    a.op = bd->op;
+    a.coef = coef;
+    a.diag = bd->d_diag;
+    a.b = bd->d_b;
+    a.x = x;
+    a.ax = bd->d_ax;
+    a.r = bd->d_r;
+    a.z = bd->d_z;
+    a.p = bd->d_p;
+    a.ap = bd->d_ap;
+    a.partial = bd->d_partial;
+    a.ticket = bd->d_ticket;
+    a.st = bd->d_st;
+    return a;
+}
+
+// kind 0: phiE (coef_e, phiE), 1: Vm (coef_i, Vm)
+int pcg_solve(cfg_bidomain* bd, int kind, double tol, double rel, int max_iter,
               cfg_step_stats& stats)
 {
     cudaStream_t s = bd->stream;
-    const BdOp& op = bd->op;
     const int nb = bd->blocks;
+    const PcgArgs a = kind == 0 ? pcg_args(bd, bd->op.coef_e, bd->d_phie)
+                                : pcg_args(bd, bd->op.coef_i, bd->d_vm);
+    if (!bd->chunk[kind]) {
+        cudaGraph_t g = nullptr;
+        CFG_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        for (int k = 0; k < kChunk; ++k) {
+            k_pcg_direction<<<nb, kBlock, 0, s>>>(a);
+            k_pcg_update<<<nb, kBlock, 0, s>>>(a);
+        }
+        CFG_CUDA_TRY(cudaStreamEndCapture(s, &g));
+        const cudaError_t e = cudaGraphInstantiate(&bd->chunk[kind], g, 0);
+        cudaGraphDestroy(g);
+        CFG_CUDA_TRY(e);
+    }
     PcgScalars init{};
     init.tol = tol;
     init.rel = rel;
     init.max_iter = max_iter;
     *bd->h_st = init;
     CFG_CUDA_TRY(cudaMemcpyAsync(bd->d_st, bd->h_st, sizeof(PcgScalars), cudaMemcpyHostToDevice, s));
-    k_pcg_begin<<<nb, kBlock, 0, s>>>(op, coef, bd->d_diag, x, bd->d_b, bd->d_ax, bd->d_r,
-                                      bd->d_partial);
-    k_pcg_reduce<<<1, kBlock, 0, s>>>(bd->d_partial, nb, 2, 0, op.n, bd->d_st);
-    k_pcg_norm<<<nb, kBlock, 0, s>>>(op, coef, bd->d_diag, bd->d_ax, bd->d_b, bd->d_r, bd->d_z,
-                                     bd->d_st, bd->d_partial);
-    k_pcg_reduce<<<1, kBlock, 0, s>>>(bd->d_partial, nb, 2, 1, op.n, bd->d_st);
+    k_pcg_begin<<<nb, kBlock, 0, s>>>(a);
+    k_pcg_norm<<<nb, kBlock, 0, s>>>(a);
     CFG_CUDA_TRY(cudaGetLastError());
     for (int it = 0;; it += kChunk) {
         CFG_CUDA_TRY(cudaMemcpyAsync(bd->h_st, bd->d_st, sizeof(PcgScalars), cudaMemcpyDeviceToHost, s));
         CFG_CUDA_TRY(cudaStreamSynchronize(s));
         if (bd->h_st->done) break;
         if (it > max_iter + kChunk) return fail(CFG_ERR_PCG, "bidomain PCG did not finish");
-        for (int k = 0; k < kChunk; ++k) {
-            k_pcg_direction<<<nb, kBlock, 0, s>>>(op, coef, bd->d_diag, bd->d_z, bd->d_p, bd->d_ap,
-                                                  bd->d_st, bd->d_partial);
-            k_pcg_reduce<<<1, kBlock, 0, s>>>(bd->d_partial, nb, 1, 2, op.n, bd->d_st);
-            k_pcg_update<<<nb, kBlock, 0, s>>>(op.n, bd->d_diag, x, bd->d_r, bd->d_z, bd->d_p,
-                                               bd->d_ap, bd->d_st, bd->d_partial);
-            k_pcg_reduce<<<1, kBlock, 0, s>>>(bd->d_partial, nb, 2, 3, op.n, bd->d_st);
-        }
-        CFG_CUDA_TRY(cudaGetLastError());
+        CFG_CUDA_TRY(cudaGraphLaunch(bd->chunk[kind], s));
     }
     const PcgScalars& st = *bd->h_st;
     const int k = stats.n_solves;
@@ -496,6 +528,9 @@ extern "C" int cfg_bidomain_destroy(cfg_bidomain* bd)
     dfree(bd->d_own);
     dfree(bd->d_calc);
     dfree(bd->d_st);
+    dfree(bd->d_ticket);
+    for (cudaGraphExec_t& g : bd->chunk)
+        if (g) cudaGraphExecDestroy(g);
     if (bd->h_st) cudaFreeHost(bd->h_st);
     if (bd->ion) cfg_ionic_destroy(bd->ion);
     if (bd->stream) cudaStreamDestroy(bd->stream);
@@ -669,6 +704,8 @@ extern "C" int cfg_bidomain_create(const cfg_bidomain_desc* d, const cfg_mesh_de
     if (!e) e = dmalloc(&bd->d_partial, 2 * size_t(bd->blocks));
     if (!e) e = dmalloc(&bd->d_calc, size_t(n));
     if (!e) e = dmalloc(&bd->d_st, 1);
+    if (!e) e = dmalloc(&bd->d_ticket, 1);
+    if (!e) e = cudaMemset(bd->d_ticket, 0, sizeof(unsigned));
     if (!e) e = cudaMallocHost(reinterpret_cast<void**>(&bd->h_st), sizeof(PcgScalars));
     if (e) return bail(fail(CFG_ERR_CUDA, "bidomain allocation: %s", cudaGetErrorString(e)));
     std::vector<double> v0(size_t(n), d->vm0), zero(size_t(n), 0.0);
@@ -725,8 +762,7 @@ extern "C" int cfg_bidomain_step(cfg_bidomain* bd, double dt)
         div_gamma_grad(bd, bd->d_vm, bd->d_dv);
         k_phie_system<<<nb, kBlock, 0, s>>>(bd->op, bd->d_dv, bd->ref, bd->ref_value, bd->d_diag,
                                             bd->d_b);
-        if (int rc = pcg_solve(bd, bd->op.coef_e, bd->d_phie, bd->e_tol, bd->e_rel, bd->e_max,
-                               bd->e_stats))
+        if (int rc = pcg_solve(bd, 0, bd->e_tol, bd->e_rel, bd->e_max, bd->e_stats))
             return rc;
         // Vm: fvm::ddt creates the old-time levels on first access
         double cft = 1.0, cft0 = 1.0, cft00 = 0.0;
@@ -748,8 +784,7 @@ extern "C" int cfg_bidomain_step(cfg_bidomain* bd, double dt)
         VmArgs va{bd->chicm, 1.0 / dt, cft, cft0, cft00, bd->backward ? 1 : 0};
         k_vm_system<<<nb, kBlock, 0, s>>>(bd->op, va, bd->d_vm_old, bd->d_vm_oldold, bd->d_iion,
                                           bd->d_src, bd->d_dv, bd->d_diag, bd->d_b);
-        if (int rc = pcg_solve(bd, bd->op.coef_i, bd->d_vm, bd->vm_tol, bd->vm_rel, bd->vm_max,
-                               bd->vm_stats))
+        if (int rc = pcg_solve(bd, 1, bd->vm_tol, bd->vm_rel, bd->vm_max, bd->vm_stats))
             return rc;
         k_phii<<<nb, kBlock, 0, s>>>(n, bd->d_vm, bd->d_phie, bd->d_phii);
     }
