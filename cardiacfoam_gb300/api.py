@@ -477,6 +477,23 @@ class Bidomain:
         _L.check(self._lib.cfg_bidomain_create(C.byref(d), C.byref(md), C.byref(h)))
         self.h = h
 
+    @classmethod
+    def from_dict(cls, text: str, mesh: LduMesh, dt: float, precision=_L.PRECISION_FP64):
+        """From the text of a constant/electroProperties file with
+        myocardiumSolver bidomainSolver (cfg_bidomain_create_from_dict)."""
+        if not mesh.has_geometry:
+            raise ValueError("the bidomain step needs a mesh with its full geometry")
+        self = cls.__new__(cls)
+        self._lib = _L.load()
+        self.mesh = mesh
+        self.n = mesh.n_cells
+        md, keep = mesh_desc(mesh, structured=False)
+        h = C.c_void_p()
+        _L.check(self._lib.cfg_bidomain_create_from_dict(text.encode(), C.byref(md), dt,
+                                                         precision, C.byref(h)))
+        self.h = h
+        return self
+
     def step(self, dt: float):
         _L.check(self._lib.cfg_bidomain_step(self.h, dt))
 

@@ -181,85 +181,40 @@ std::vector<double> numbers(const Entry* e)
     return out;
 }
 
-}  // namespace
-}  // namespace cfg
-
-using namespace cfg;
-
-extern "C" int cfg_monodomain_create_from_dict(const char* text, const cfg_mesh_desc* mesh,
-                                               double delta_t, int precision,
-                                               cfg_monodomain** out)
+// ionicModel, tissue and the ODE solver keys of <type>Coeffs
+// (ionicModel.C:76-94); the strings live in thread-local storage until the
+// next call on the thread.
+int parse_ionic(const Dict& c, long long n_cells, double delta_t, int precision,
+                cfg_ionic_desc& io)
 {
-    clear_error();
-    if (!text || !mesh || !out) return fail(CFG_ERR_INVALID, "null argument");
-    Dict root;
-    std::string err;
-    std::string src(text);
-    if (!Parser(src).parse(root, err))
-        return fail(CFG_ERR_INVALID, "electroProperties: %s", err.c_str());
-    std::string solver;
-    if (!word(root, "myocardiumSolver", solver))
-        return fail(CFG_ERR_INVALID, "electroProperties: keyword myocardiumSolver is undefined");
-    if (solver != "monodomainSolver")
-        return fail(CFG_ERR_UNSUPPORTED, "myocardiumSolver %s: only monodomainSolver runs here",
-                    solver.c_str());
-    const Entry* ce = find(root, "monodomainSolverCoeffs");
-    if (!ce || !ce->is_dict)
-        return fail(CFG_ERR_INVALID, "electroProperties: monodomainSolverCoeffs is undefined");
-    const Dict& c = ce->dict;
-
-    cfg_monodomain_desc d{};
     static thread_local std::string model, tissue, ode_solver;
     if (!word(c, "ionicModel", model))
         return fail(CFG_ERR_INVALID, "keyword ionicModel is undefined");
     if (!word(c, "tissue", tissue)) tissue.clear();
-    d.ionic.ionic_model = model.c_str();
-    d.ionic.tissue = tissue.empty() ? nullptr : tissue.c_str();
-    d.ionic.n_cells = mesh->n_cells;
-    d.ionic.initial_delta_t = delta_t;   // runTime.deltaT (myocardiumDomainInterface.C:71-76)
-    d.ionic.solve_vm_within_ode = 0;
-    d.ionic.precision = precision;
-    d.ionic.ode.solver = word(c, "solver", ode_solver) ? ode_solver.c_str() : "RKF45";
+    io.ionic_model = model.c_str();
+    io.tissue = tissue.empty() ? nullptr : tissue.c_str();
+    io.n_cells = n_cells;
+    io.initial_delta_t = delta_t;   // runTime.deltaT (myocardiumDomainInterface.C:71-76)
+    io.solve_vm_within_ode = 0;
+    io.precision = precision;
+    io.ode.solver = word(c, "solver", ode_solver) ? ode_solver.c_str() : "RKF45";
     double v;
-    d.ionic.ode.abs_tol = scalar(c, "absTol", v) ? v : -1;
-    d.ionic.ode.rel_tol = scalar(c, "relTol", v) ? v : -1;
-    d.ionic.ode.max_steps = scalar(c, "maxSteps", v) ? (long long)v : -1;
-    d.ionic.ode.safe_scale = scalar(c, "safeScale", v) ? v : -1;
-    d.ionic.ode.min_scale = scalar(c, "minScale", v) ? v : -1;
-    d.ionic.ode.max_scale = scalar(c, "maxScale", v) ? v : -1;
-    d.ionic.ode.alpha_increase = scalar(c, "alphaIncrease", v) ? v : -1;
-    d.ionic.ode.alpha_decrease = scalar(c, "alphaDecrease", v) ? v : -1;
+    io.ode.abs_tol = scalar(c, "absTol", v) ? v : -1;
+    io.ode.rel_tol = scalar(c, "relTol", v) ? v : -1;
+    io.ode.max_steps = scalar(c, "maxSteps", v) ? (long long)v : -1;
+    io.ode.safe_scale = scalar(c, "safeScale", v) ? v : -1;
+    io.ode.min_scale = scalar(c, "minScale", v) ? v : -1;
+    io.ode.max_scale = scalar(c, "maxScale", v) ? v : -1;
+    io.ode.alpha_increase = scalar(c, "alphaIncrease", v) ? v : -1;
+    io.ode.alpha_decrease = scalar(c, "alphaDecrease", v) ? v : -1;
+    return CFG_OK;
+}
 
-    std::vector<double> sig = numbers(find(c, "conductivity"));
-    if (sig.size() != 6)
-        return fail(CFG_ERR_INVALID, "conductivity must be a symmTensor (xx xy xz yy yz zz)");
-    for (int k = 0; k < 6; ++k) d.conductivity[k] = sig[size_t(k)];
-    if (!scalar(c, "chi", d.chi)) return fail(CFG_ERR_INVALID, "keyword chi is undefined");
-    if (!scalar(c, "cm", d.cm)) return fail(CFG_ERR_INVALID, "keyword cm is undefined");
-    std::string alg = "implicit";
-    word(c, "solutionAlgorithm", alg);
-    if (alg != "implicit" && alg != "explicit")
-        return fail(CFG_ERR_INVALID, "Unrecognised solution algorithm %s", alg.c_str());
-    d.implicit = alg == "implicit";
-    // fvSchemes / fvSolution of the tutorials (backward; PCG 1e-8 relTol 0;
-    // PIMPLE residualControl 1e-6); a "gpu" sub-dictionary may override them
-    d.ddt_backward = 1;
-    d.pcg_tol = 1e-8;
-    d.pcg_rel_tol = 0.0;
-    d.pcg_max_iter = 1000;
-    d.n_outer = 1000;
-    d.outer_tol = 1e-6;
-    d.vm0 = -0.084;
-    if (const Entry* g = find(c, "gpu"); g && g->is_dict) {
-        std::string ddt;
-        if (word(g->dict, "ddtScheme", ddt)) d.ddt_backward = ddt == "backward";
-        if (scalar(g->dict, "tolerance", v)) d.pcg_tol = v;
-        if (scalar(g->dict, "relTol", v)) d.pcg_rel_tol = v;
-        if (scalar(g->dict, "maxIter", v)) d.pcg_max_iter = int(v);
-        if (scalar(g->dict, "nOuterCorrectors", v)) d.n_outer = int(v);
-        if (scalar(g->dict, "residualControl", v)) d.outer_tol = v;
-    }
-    // externalStimulus (stimulusIO::loadExternalStimulusProtocol)
+// externalStimulus (stimulusIO::loadExternalStimulusProtocol) into the box
+// fields of a monodomain or bidomain description
+template <class D>
+int parse_stimulus(const Dict& c, D& d)
+{
     if (const Entry* se = find(c, "externalStimulus"); se && se->is_dict) {
         const Dict& s = se->dict;
         std::vector<double> mn, mx;
@@ -307,7 +262,153 @@ extern "C" int cfg_monodomain_create_from_dict(const char* text, const cfg_mesh_
             }
         }
     }
+    return CFG_OK;
+}
+
+}  // namespace
+}  // namespace cfg
+
+using namespace cfg;
+
+extern "C" int cfg_monodomain_create_from_dict(const char* text, const cfg_mesh_desc* mesh,
+                                               double delta_t, int precision,
+                                               cfg_monodomain** out)
+{
+    clear_error();
+    if (!text || !mesh || !out) return fail(CFG_ERR_INVALID, "null argument");
+    Dict root;
+    std::string err;
+    std::string src(text);
+    if (!Parser(src).parse(root, err))
+        return fail(CFG_ERR_INVALID, "electroProperties: %s", err.c_str());
+    std::string solver;
+    if (!word(root, "myocardiumSolver", solver))
+        return fail(CFG_ERR_INVALID, "electroProperties: keyword myocardiumSolver is undefined");
+    if (solver != "monodomainSolver")
+        return fail(CFG_ERR_UNSUPPORTED,
+                    "myocardiumSolver %s: the monodomain context runs monodomainSolver%s",
+                    solver.c_str(),
+                    solver == "bidomainSolver" ? " (bidomainSolver: cfg_bidomain_create_from_dict)"
+                                               : "");
+    const Entry* ce = find(root, "monodomainSolverCoeffs");
+    if (!ce || !ce->is_dict)
+        return fail(CFG_ERR_INVALID, "electroProperties: monodomainSolverCoeffs is undefined");
+    const Dict& c = ce->dict;
+
+    cfg_monodomain_desc d{};
+    if (int rc = parse_ionic(c, mesh->n_cells, delta_t, precision, d.ionic)) return rc;
+    double v;
+
+    std::vector<double> sig = numbers(find(c, "conductivity"));
+    if (sig.size() != 6)
+        return fail(CFG_ERR_INVALID, "conductivity must be a symmTensor (xx xy xz yy yz zz)");
+    for (int k = 0; k < 6; ++k) d.conductivity[k] = sig[size_t(k)];
+    if (!scalar(c, "chi", d.chi)) return fail(CFG_ERR_INVALID, "keyword chi is undefined");
+    if (!scalar(c, "cm", d.cm)) return fail(CFG_ERR_INVALID, "keyword cm is undefined");
+    std::string alg = "implicit";
+    word(c, "solutionAlgorithm", alg);
+    if (alg != "implicit" && alg != "explicit")
+        return fail(CFG_ERR_INVALID, "Unrecognised solution algorithm %s", alg.c_str());
+    d.implicit = alg == "implicit";
+    // fvSchemes / fvSolution of the tutorials (backward; PCG 1e-8 relTol 0;
+    // PIMPLE residualControl 1e-6); a "gpu" sub-dictionary may override them
+    d.ddt_backward = 1;
+    d.pcg_tol = 1e-8;
+    d.pcg_rel_tol = 0.0;
+    d.pcg_max_iter = 1000;
+    d.n_outer = 1000;
+    d.outer_tol = 1e-6;
+    d.vm0 = -0.084;
+    if (const Entry* g = find(c, "gpu"); g && g->is_dict) {
+        std::string ddt;
+        if (word(g->dict, "ddtScheme", ddt)) d.ddt_backward = ddt == "backward";
+        if (scalar(g->dict, "tolerance", v)) d.pcg_tol = v;
+        if (scalar(g->dict, "relTol", v)) d.pcg_rel_tol = v;
+        if (scalar(g->dict, "maxIter", v)) d.pcg_max_iter = int(v);
+        if (scalar(g->dict, "nOuterCorrectors", v)) d.n_outer = int(v);
+        if (scalar(g->dict, "residualControl", v)) d.outer_tol = v;
+    }
+    if (int rc = parse_stimulus(c, d)) return rc;
     return cfg_monodomain_create(&d, mesh, out);
+}
+
+// The same for myocardiumSolver bidomainSolver: bidomainSolverCoeffs'
+// conductivityIntracellular / conductivityExtracellular (symmTensors),
+// phiERefPoint (required) and phiEReferenceValue (default 0)
+// (bidomainSolver.C:36-127), chi, cm, the ionic model and externalStimulus as
+// for the monodomain.  Solver settings follow the bidomain tutorial's
+// fvSolution and fvSchemes (relTol 0, maxIter 1000 for Vm and phiE;
+// nOuterCorrectors 2 without residualControl; backward ddt; Gauss linear
+// gradients) except the PCG tolerance: 1e-12 instead of the tutorial's 1e-15,
+// which double precision rarely reaches within maxIter (a solve that ends at
+// maxIter is an error here).  A "gpu" sub-dictionary overrides any of them.
+extern "C" int cfg_bidomain_create_from_dict(const char* text, const cfg_mesh_desc* mesh,
+                                             double delta_t, int precision, cfg_bidomain** out)
+{
+    clear_error();
+    if (!text || !mesh || !out) return fail(CFG_ERR_INVALID, "null argument");
+    Dict root;
+    std::string err;
+    std::string src(text);
+    if (!Parser(src).parse(root, err))
+        return fail(CFG_ERR_INVALID, "electroProperties: %s", err.c_str());
+    std::string solver;
+    if (!word(root, "myocardiumSolver", solver))
+        return fail(CFG_ERR_INVALID, "electroProperties: keyword myocardiumSolver is undefined");
+    if (solver != "bidomainSolver")
+        return fail(CFG_ERR_UNSUPPORTED, "myocardiumSolver %s: the bidomain context runs "
+                                         "bidomainSolver", solver.c_str());
+    const Entry* ce = find(root, "bidomainSolverCoeffs");
+    if (!ce || !ce->is_dict)
+        return fail(CFG_ERR_INVALID, "electroProperties: bidomainSolverCoeffs is undefined");
+    const Dict& c = ce->dict;
+    cfg_bidomain_desc d{};
+    if (int rc = parse_ionic(c, mesh->n_cells, delta_t, precision, d.ionic)) return rc;
+    for (int t = 0; t < 2; ++t) {
+        const char* key = t == 0 ? "conductivityIntracellular" : "conductivityExtracellular";
+        std::vector<double> sig = numbers(find(c, key));
+        if (sig.size() != 6)
+            return fail(CFG_ERR_INVALID, "%s must be a symmTensor (xx xy xz yy yz zz)", key);
+        for (int k = 0; k < 6; ++k)
+            (t == 0 ? d.conductivity_i : d.conductivity_e)[k] = sig[size_t(k)];
+    }
+    if (!scalar(c, "chi", d.chi)) return fail(CFG_ERR_INVALID, "keyword chi is undefined");
+    if (!scalar(c, "cm", d.cm)) return fail(CFG_ERR_INVALID, "keyword cm is undefined");
+    std::string alg = "implicit";
+    word(c, "solutionAlgorithm", alg);
+    if (alg == "explicit")
+        return fail(CFG_ERR_UNSUPPORTED, "the explicit bidomain algorithm is not built");
+    if (alg != "implicit")
+        return fail(CFG_ERR_INVALID, "Unrecognised solution algorithm %s", alg.c_str());
+    std::vector<double> rp = numbers(find(c, "phiERefPoint"));
+    if (rp.size() != 3) return fail(CFG_ERR_INVALID, "keyword phiERefPoint is undefined");
+    for (int k = 0; k < 3; ++k) d.ref_point[k] = rp[size_t(k)];
+    double v;
+    d.ref_value = scalar(c, "phiEReferenceValue", v) ? v : 0.0;
+    d.ddt_backward = 1;
+    d.pcg_tol = d.phie_tol = 1e-12;
+    d.pcg_rel_tol = d.phie_rel_tol = 0.0;
+    d.pcg_max_iter = d.phie_max_iter = 1000;
+    d.n_outer = 2;
+    d.outer_tol = 0.0;
+    d.vm0 = -0.084;
+    d.grad_scheme = CFG_GRAD_GAUSS_LINEAR;
+    if (const Entry* g = find(c, "gpu"); g && g->is_dict) {
+        std::string w;
+        if (word(g->dict, "ddtScheme", w)) d.ddt_backward = w == "backward";
+        if (word(g->dict, "gradScheme", w))
+            d.grad_scheme = w == "leastSquares" ? CFG_GRAD_LEAST_SQUARES : CFG_GRAD_GAUSS_LINEAR;
+        if (scalar(g->dict, "tolerance", v)) d.pcg_tol = v;
+        if (scalar(g->dict, "relTol", v)) d.pcg_rel_tol = v;
+        if (scalar(g->dict, "maxIter", v)) d.pcg_max_iter = int(v);
+        if (scalar(g->dict, "phiETolerance", v)) d.phie_tol = v;
+        if (scalar(g->dict, "phiERelTol", v)) d.phie_rel_tol = v;
+        if (scalar(g->dict, "phiEMaxIter", v)) d.phie_max_iter = int(v);
+        if (scalar(g->dict, "nOuterCorrectors", v)) d.n_outer = int(v);
+        if (scalar(g->dict, "residualControl", v)) d.outer_tol = v;
+    }
+    if (int rc = parse_stimulus(c, d)) return rc;
+    return cfg_bidomain_create(&d, mesh, out);
 }
 
 // ECGDomain::readElectrodes (ecgDomain.C:53-82) of the ecgDomains entry in

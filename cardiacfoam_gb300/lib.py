@@ -159,7 +159,7 @@ EXPORTS = [
     "cfg_pseudo_ecg_create", "cfg_pseudo_ecg_compute", "cfg_pseudo_ecg_compute_monodomain",
     "cfg_pseudo_ecg_record", "cfg_pseudo_ecg_record_field", "cfg_pseudo_ecg_series", "cfg_pseudo_ecg_reset",
     "cfg_pseudo_ecg_destroy", "cfg_pseudo_ecg_electrodes_from_dict",
-    "cfg_bidomain_create", "cfg_bidomain_step", "cfg_bidomain_run", "cfg_bidomain_get_field",
+    "cfg_bidomain_create", "cfg_bidomain_create_from_dict", "cfg_bidomain_step", "cfg_bidomain_run", "cfg_bidomain_get_field",
     "cfg_bidomain_set_field", "cfg_bidomain_last_stats", "cfg_bidomain_time",
     "cfg_bidomain_reference_cell", "cfg_bidomain_ionic", "cfg_bidomain_stream",
     "cfg_bidomain_destroy",
@@ -251,6 +251,8 @@ def load(path: Optional[os.PathLike] = None):
                                                       C.c_size_t, _dp, C.c_int, _ip]
     L.cfg_bidomain_create.argtypes = [C.POINTER(BidomainDesc), C.POINTER(MeshDesc),
                                       C.POINTER(C.c_void_p)]
+    L.cfg_bidomain_create_from_dict.argtypes = [C.c_char_p, C.POINTER(MeshDesc), C.c_double,
+                                                C.c_int, C.POINTER(C.c_void_p)]
     L.cfg_bidomain_step.argtypes = [C.c_void_p, C.c_double]
     L.cfg_bidomain_run.argtypes = [C.c_void_p, C.c_double, C.c_longlong]
     L.cfg_bidomain_get_field.argtypes = [C.c_void_p, C.c_int, _dp]

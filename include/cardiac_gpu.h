@@ -436,6 +436,20 @@ typedef struct cfg_bidomain cfg_bidomain;
 
 int cfg_bidomain_create(const cfg_bidomain_desc* desc, const cfg_mesh_desc* mesh,
                         cfg_bidomain** out);
+/* The same from the text of a constant/electroProperties file with
+ * myocardiumSolver bidomainSolver: bidomainSolverCoeffs' conductivityIntracellular,
+ * conductivityExtracellular, phiERefPoint, phiEReferenceValue, chi, cm, the ionic
+ * model keys and externalStimulus (bidomainSolver.C:36-127, as
+ * cfg_monodomain_create_from_dict for the rest).  Solver settings are the
+ * bidomain tutorial's (relTol 0 / maxIter 1000 for Vm and phiE,
+ * nOuterCorrectors 2, backward ddt, Gauss linear gradients) with PCG
+ * tolerance 1e-12 instead of its 1e-15 (rarely reached in double precision
+ * within maxIter, which is an error here); a "gpu"
+ * sub-dictionary may override them (tolerance, relTol, maxIter, phiETolerance,
+ * phiERelTol, phiEMaxIter, nOuterCorrectors, residualControl, ddtScheme,
+ * gradScheme). */
+int cfg_bidomain_create_from_dict(const char* electro_properties, const cfg_mesh_desc* mesh,
+                                  double delta_t, int precision, cfg_bidomain** out);
 /* One time step (runTime++ then the staggered advance, as
  * cfg_monodomain_step). */
 int cfg_bidomain_step(cfg_bidomain* bd, double dt);

@@ -62,3 +62,55 @@ def test_2d_phie_shape_converges(oracle):
         e = B.phie() - pe
         errs.append(np.max(np.abs(e - e.mean())))
     assert V.rate(errs[0], errs[1], 10, 20) > 1.7
+
+
+BIDOMAIN_DICT = """
+myocardiumSolver  %s;
+bidomainSolverCoeffs
+{
+    conductivityIntracellular [-1 -3 3 0 0 2 0] (0.17 0 0 0.019 0 0.019);
+    conductivityExtracellular [-1 -3 3 0 0 2 0] %s;
+    chi  [0 -1 0 0 0 0 0] 140000;
+    cm   [-1 -4 4 0 0 2 0] 0.01;
+    ionicModel TNNP;
+    tissue epicardialCells;
+    solutionAlgorithm %s;
+    maxSteps 1000000;
+    %s
+    externalStimulus
+    {
+        stimulusLocationMin (0 0 0);
+        stimulusLocationMax (1e-3 4e-3 5e-4);
+        stimulusDuration [0 0 1 0 0 0 0] 1e-3;
+        stimulusIntensity [0 -3 0 0 0 1 0] 1e5;
+    }
+}
+"""
+GOOD = ("bidomainSolver", "(0.62 0 0 0.24 0 0.24)", "implicit", "phiERefPoint (0 0 0);")
+
+
+def _from_dict(gpu_lib, text, mesh):
+    import ctypes as C
+    from cardiacfoam_gb300 import api
+    md, keep = api.mesh_desc(mesh, structured=False)
+    h = C.c_void_p()
+    return gpu_lib.cfg_bidomain_create_from_dict(text.encode(), C.byref(md), 2e-5, 0, C.byref(h))
+
+
+def test_bidomain_dictionary_errors(gpu_lib):
+    """Errors of cfg_bidomain_create_from_dict found while reading the
+    dictionary or the mesh, before any device work."""
+    from cardiacfoam_gb300 import lib
+    from cardiacfoam_gb300.mesh import box_mesh, with_box_geometry
+    geo = with_box_geometry(box_mesh(4, 2, 1, 1e-3, 5e-4, 2.5e-4), 1e-3, 5e-4, 2.5e-4)
+    bad = [(("monodomainSolver",) + GOOD[1:], lib.CFG_ERR_UNSUPPORTED),
+           ((GOOD[0], GOOD[1], "explicit", GOOD[3]), lib.CFG_ERR_UNSUPPORTED),
+           ((GOOD[0], GOOD[1], "sideways", GOOD[3]), lib.CFG_ERR_INVALID),
+           ((GOOD[0], "(0.62 0 0 0.24)", GOOD[2], GOOD[3]), lib.CFG_ERR_INVALID),
+           (GOOD[:3] + ("",), lib.CFG_ERR_INVALID)]
+    for args, code in bad:
+        assert _from_dict(gpu_lib, BIDOMAIN_DICT % args, geo) == code, args
+    # a mesh without its geometry is refused before the device is touched
+    assert _from_dict(gpu_lib, BIDOMAIN_DICT % GOOD, box_mesh(4, 2, 1, 1e-3, 5e-4, 2.5e-4)) == \
+        lib.CFG_ERR_INVALID
+    assert "geometry" in lib.load().cfg_last_error().decode()

@@ -118,3 +118,50 @@ def test_rejects_meshes_that_need_corrections(gpu_lib):
     assert e.value.code == lib.CFG_ERR_UNSUPPORTED
     with pytest.raises(ValueError):
         api.Bidomain(box_mesh(4, 4, 4, 1e-3, 1e-3, 1e-3), "TNNP", "epicardialCells")
+
+
+ELECTRO_PROPERTIES = """
+myocardiumSolver  bidomainSolver;
+bidomainSolverCoeffs
+{
+    conductivityIntracellular [-1 -3 3 0 0 2 0] (0.17 0 0 0.019 0 0.019);
+    conductivityExtracellular [-1 -3 3 0 0 2 0] (0.62 0 0 0.24 0 0.24);
+    chi  [0 -1 0 0 0 0 0] 140000;
+    cm   [-1 -4 4 0 0 2 0] 0.01;
+    ionicModel TNNP;
+    tissue epicardialCells;
+    solutionAlgorithm implicit;
+    maxSteps 1000000;
+    phiERefPoint (0 0 0);
+    externalStimulus
+    {
+        stimulusLocationMin (0 0 0);
+        stimulusLocationMax (1e-3 4e-3 5e-4);
+        stimulusDuration [0 0 1 0 0 0 0] 1e-3;
+        stimulusIntensity [0 -3 0 0 0 1 0] 1e5;
+    }
+}
+"""
+
+
+@pytest.mark.gpu
+def test_from_dict_equals_the_description(gpu_lib):
+    """cfg_bidomain_create_from_dict builds the same context as the
+    description with the dictionary's values and the documented defaults
+    (PCG 1e-12, maxIter 1000, two correctors, Gauss linear gradients)."""
+    h, dt = 2.5e-4, 2e-5
+    mesh = with_box_geometry(box_mesh(24, 8, 2, 24 * h, 8 * h, 2 * h), 24 * h, 8 * h, 2 * h)
+    a = api.Bidomain.from_dict(ELECTRO_PROPERTIES, mesh, dt)
+    b = api.Bidomain(mesh, "TNNP", "epicardialCells", sigma_i=(0.17, 0, 0, 0.019, 0, 0.019),
+                     sigma_e=(0.62, 0, 0, 0.24, 0, 0.24), chi=140000.0, cm=0.01, dt=dt,
+                     pcg_tol=1e-12, phie_tol=1e-12, n_outer=2, ref_point=(0.0, 0.0, 0.0),
+                     boxes=[((0.0, 0.0, 0.0), (1e-3, 4e-3, 5e-4), 0.0, 1e-3, 1e5)],
+                     grad_scheme=lib.GRAD_GAUSS_LINEAR, max_steps=10 ** 6)
+    for _ in range(30):
+        a.step(dt)
+        b.step(dt)
+    assert np.array_equal(a.vm(), b.vm())
+    assert np.array_equal(a.phie(), b.phie())
+    assert np.max(a.vm()) > -0.084
+    a.close()
+    b.close()
