@@ -26,7 +26,6 @@
 
 #include <algorithm>
 #include <cmath>
-#include <cstring>
 #include <vector>
 
 #include "geometry.h"
@@ -124,8 +123,9 @@ __device__ __forceinline__ void gamma_g(const double* G, double g0, double g1, d
     u[2] = G[2] * g0 + G[4] * g1 + G[5] * g2;
 }
 
-// out_c = V_c (sum over faces of Sf . (G grad x)_f + walls) / V_c * ... as
-// fvc::div returns it per volume and the equation multiplies by V
+// out_c = V_c * (D_c / V_c), D_c the sum over the cell's faces of
+// Sf . (G grad x)_f (outward) plus the walls: fvc::div per volume, times V as
+// the equation's source takes it
 __global__ void k_div_gamma_grad(BdOp op, const double* __restrict__ g, double* __restrict__ out)
 {
     const long long c = (long long)blockIdx.x * kBlock + threadIdx.x;
