@@ -114,3 +114,26 @@ def test_bidomain_dictionary_errors(gpu_lib):
     assert _from_dict(gpu_lib, BIDOMAIN_DICT % GOOD, box_mesh(4, 2, 1, 1e-3, 5e-4, 2.5e-4)) == \
         lib.CFG_ERR_INVALID
     assert "geometry" in lib.load().cfg_last_error().decode()
+
+
+def test_bidomain_model_constants(oracle):
+    """bidomainFDAManufactured's initConsts (bidomainFDAManufactured_2014.H)
+    as emitted: Cm 2, Chi 3, Beta = betaBase(dimension) (1 - k) with the
+    tutorial's k, everything else as the monodomain manufactured model; the
+    right-hand sides agree with the monodomain model's once Beta is equal."""
+    k = V.BIDOMAIN_K
+    rng = np.random.default_rng(5)
+    for dim, base in ((1, -1.1), (2, -5.9), (3, -8.6)):
+        c, _ = oracle.model_init("bidomainFDAManufactured", 10 + dim)
+        assert c[0] == 2.0 and c[2] == 3.0
+        assert c[1] == base * (1.0 - k)
+        cm, _ = oracle.model_init("monodomainFDAManufactured", 10 + dim)
+        y = rng.uniform(0.5, 1.5, 4)
+        out = []
+        for cc, model in ((c, "bidomainFDAManufactured"), (cm, "monodomainFDAManufactured")):
+            dydt, alg = np.zeros(4), np.zeros(1)
+            oracle.lib().oracle_model_variables(oracle.MODELS[model], 0.0, oracle.ptr(cc),
+                                                oracle.ptr(dydt), oracle.ptr(y), oracle.ptr(alg),
+                                                10 + dim, 0, None)
+            out.append((dydt.copy(), alg.copy()))
+        assert np.array_equal(out[0][0], out[1][0])   # the rates do not involve Beta
