@@ -137,3 +137,31 @@ def test_bidomain_model_constants(oracle):
                                                 10 + dim, 0, None)
             out.append((dydt.copy(), alg.copy()))
         assert np.array_equal(out[0][0], out[1][0])   # the rates do not involve Beta
+
+
+def test_create_rejects_bad_arguments(gpu_lib):
+    """cfg_bidomain_create's argument checks, made before any device work."""
+    import ctypes as C
+    from cardiacfoam_gb300 import api, lib
+    from cardiacfoam_gb300.mesh import box_mesh
+    geo = V.geometry_mesh_for(3, 4)
+
+    def create(mesh, n_cells=None, n_outer=2, boxes=0):
+        keep = []
+        d = lib.BidomainDesc()
+        d.ionic = api.ionic_desc("TNNP", "epicardialCells",
+                                 mesh.n_cells if n_cells is None else n_cells, 1e-5, False,
+                                 lib.PRECISION_FP64, api.ode_desc(), None, None, None, keep)
+        d.n_outer, d.n_boxes = n_outer, boxes
+        md, k2 = api.mesh_desc(mesh, structured=False)
+        h = C.c_void_p()
+        return gpu_lib.cfg_bidomain_create(C.byref(d), C.byref(md), C.byref(h))
+
+    assert create(box_mesh(4, 4, 4, 1.0, 1.0, 1.0)) == lib.CFG_ERR_INVALID    # no geometry
+    assert create(geo, n_cells=7) == lib.CFG_ERR_INVALID
+    assert create(geo, n_outer=0) == lib.CFG_ERR_INVALID
+    assert create(geo, boxes=9) == lib.CFG_ERR_INVALID
+    # tetrahedra need the explicit Laplacian corrections: not built
+    from cardiacfoam_gb300 import lv
+    assert create(lv.left_ventricle(3, 6, 8).mesh) == lib.CFG_ERR_UNSUPPORTED
+    assert "correction" in lib.load().cfg_last_error().decode()

@@ -122,3 +122,28 @@ def test_ecg_time_series_format(tmp_path):
     assert path.read_text() == ("# time  E1  E2\n"
                                 "0.00000000e+00  1.50000000e-03  -2.25000000e+00\n"
                                 "1.00000000e-01  0.00000000e+00  1.23456789e+05\n")
+
+
+def test_create_rejects_bad_arguments(gpu_lib):
+    """cfg_pseudo_ecg_create's argument checks, made before any device work."""
+    import ctypes as C
+    from cardiacfoam_gb300 import api, lib
+    from cardiacfoam_gb300.mesh import box_mesh
+    geo = V.geometry_mesh_for(3, 4)
+    el = np.ascontiguousarray(ELECTRODES, dtype=np.float64)
+
+    def create(mesh, n_el=5, grad=lib.GRAD_GAUSS_LINEAR, arith=lib.ECG_FLOAT_PAIRS, rows=0):
+        d = lib.PseudoEcgDesc()
+        for i, v in enumerate(V.SIGMA):
+            d.conductivity[i] = v
+        d.grad_scheme, d.n_electrodes, d.max_rows, d.arithmetic = grad, n_el, rows, arith
+        d.electrodes = lib.dptr(el)
+        md, keep = api.mesh_desc(mesh, structured=False)
+        h = C.c_void_p()
+        return gpu_lib.cfg_pseudo_ecg_create(C.byref(d), C.byref(md), C.byref(h))
+
+    assert create(box_mesh(4, 4, 4, 1.0, 1.0, 1.0)) == lib.CFG_ERR_INVALID    # no geometry
+    assert create(geo, n_el=0) == lib.CFG_ERR_INVALID
+    assert create(geo, grad=7) == lib.CFG_ERR_INVALID
+    assert create(geo, arith=9) == lib.CFG_ERR_INVALID
+    assert create(geo, rows=-1) == lib.CFG_ERR_INVALID
