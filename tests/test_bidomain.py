@@ -153,6 +153,9 @@ def test_create_rejects_bad_arguments(gpu_lib):
                                  mesh.n_cells if n_cells is None else n_cells, 1e-5, False,
                                  lib.PRECISION_FP64, api.ode_desc(), None, None, None, keep)
         d.n_outer, d.n_boxes = n_outer, boxes
+        for i in range(6):
+            d.conductivity_i[i] = (0.17, 0, 0, 0.019, 0, 0.019)[i]
+            d.conductivity_e[i] = (0.62, 0, 0, 0.24, 0, 0.24)[i]
         md, k2 = api.mesh_desc(mesh, structured=False)
         h = C.c_void_p()
         return gpu_lib.cfg_bidomain_create(C.byref(d), C.byref(md), C.byref(h))
