@@ -566,6 +566,8 @@ extern "C" int cfg_bidomain_create(const cfg_bidomain_desc* d, const cfg_mesh_de
     // tangential parts (k per face, the wall factor per cell) must vanish
     double gmax = 0.0;
     for (int k = 0; k < 6; ++k) gmax = std::max(gmax, std::fabs(ge[k]));
+    if (!(gmax > 0.0))
+        return fail(CFG_ERR_INVALID, "the bulk conductivity Gi + Ge is zero (phiE is undefined)");
     for (long long f = 0; f < nf; ++f) {
         const double* S = m->face_sf + 3 * f;
         const double scale = gmax * std::sqrt(S[0] * S[0] + S[1] * S[1] + S[2] * S[2]);

@@ -146,7 +146,7 @@ def test_create_rejects_bad_arguments(gpu_lib):
     from cardiacfoam_gb300.mesh import box_mesh
     geo = V.geometry_mesh_for(3, 4)
 
-    def create(mesh, n_cells=None, n_outer=2, boxes=0):
+    def create(mesh, n_cells=None, n_outer=2, boxes=0, zero_sigma=False):
         keep = []
         d = lib.BidomainDesc()
         d.ionic = api.ionic_desc("TNNP", "epicardialCells",
@@ -154,8 +154,9 @@ def test_create_rejects_bad_arguments(gpu_lib):
                                  lib.PRECISION_FP64, api.ode_desc(), None, None, None, keep)
         d.n_outer, d.n_boxes = n_outer, boxes
         for i in range(6):
-            d.conductivity_i[i] = (0.17, 0, 0, 0.019, 0, 0.019)[i]
-            d.conductivity_e[i] = (0.62, 0, 0, 0.24, 0, 0.24)[i]
+            if not zero_sigma:
+                d.conductivity_i[i] = (0.17, 0, 0, 0.019, 0, 0.019)[i]
+                d.conductivity_e[i] = (0.62, 0, 0, 0.24, 0, 0.24)[i]
         md, k2 = api.mesh_desc(mesh, structured=False)
         h = C.c_void_p()
         return gpu_lib.cfg_bidomain_create(C.byref(d), C.byref(md), C.byref(h))
@@ -164,6 +165,7 @@ def test_create_rejects_bad_arguments(gpu_lib):
     assert create(geo, n_cells=7) == lib.CFG_ERR_INVALID
     assert create(geo, n_outer=0) == lib.CFG_ERR_INVALID
     assert create(geo, boxes=9) == lib.CFG_ERR_INVALID
+    assert create(geo, zero_sigma=True) == lib.CFG_ERR_INVALID
     # tetrahedra need the explicit Laplacian corrections: not built
     from cardiacfoam_gb300 import lv
     assert create(lv.left_ventricle(3, 6, 8).mesh) == lib.CFG_ERR_UNSUPPORTED
