@@ -647,23 +647,37 @@ class PseudoECG:
         return (C.c_void_p(x.data_ptr()),
                 C.c_void_p(torch.cuda.current_stream(x.device).cuda_stream))
 
+    def _bidomain_vm(self, bd: "Bidomain"):
+        if bd.n != self.n:
+            raise ValueError("the bidomain context has another cell count")
+        return (C.c_void_p(self._lib.cfg_bidomain_device_field(bd.h, _L.FIELD_VM)),
+                C.c_void_p(bd.stream()))
+
     def compute(self, source) -> np.ndarray:
-        """phi [n_electrodes] of a Monodomain's Vm, or of a CUDA tensor of
-        n_cells doubles (on torch's current stream)."""
+        """phi [n_electrodes] of a Monodomain's or a Bidomain's Vm, or of a CUDA
+        tensor of n_cells doubles (on torch's current stream)."""
         out = np.zeros(self.n_electrodes)
         if isinstance(source, Monodomain):
             _L.check(self._lib.cfg_pseudo_ecg_compute_monodomain(self.h, source.h,
                                                                  _L.dptr(out)))
+            return out
+        if isinstance(source, Bidomain):
+            vm, stream = self._bidomain_vm(source)
+            _L.check(self._lib.cfg_pseudo_ecg_compute(self.h, vm, stream, _L.dptr(out)))
             return out
         vm, stream = self._device_field(source)
         _L.check(self._lib.cfg_pseudo_ecg_compute(self.h, vm, stream, _L.dptr(out)))
         return out
 
     def record(self, source, t: Optional[float] = None):
-        """Append phi of a Monodomain's Vm (at its time), or of a CUDA tensor
-        at time t, to the device series without waiting."""
+        """Append phi of a Monodomain's or a Bidomain's Vm (at its time), or of
+        a CUDA tensor at time t, to the device series without waiting."""
         if isinstance(source, Monodomain):
             _L.check(self._lib.cfg_pseudo_ecg_record(self.h, source.h))
+            return
+        if isinstance(source, Bidomain):
+            vm, stream = self._bidomain_vm(source)
+            _L.check(self._lib.cfg_pseudo_ecg_record_field(self.h, vm, stream, source.time()))
             return
         vm, stream = self._device_field(source)
         _L.check(self._lib.cfg_pseudo_ecg_record_field(self.h, vm, stream,

@@ -844,6 +844,11 @@ extern "C" int cfg_bidomain_set_field(cfg_bidomain* bd, int field, const double*
     return CFG_OK;
 }
 
+extern "C" const double* cfg_bidomain_device_field(cfg_bidomain* bd, int field)
+{
+    return bd ? bidomain_field(bd, field) : nullptr;
+}
+
 extern "C" int cfg_bidomain_last_stats(const cfg_bidomain* bd, cfg_step_stats* vm,
                                        cfg_step_stats* phie)
 {

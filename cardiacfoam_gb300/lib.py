@@ -160,7 +160,8 @@ EXPORTS = [
     "cfg_pseudo_ecg_record", "cfg_pseudo_ecg_record_field", "cfg_pseudo_ecg_series", "cfg_pseudo_ecg_reset",
     "cfg_pseudo_ecg_destroy", "cfg_pseudo_ecg_electrodes_from_dict",
     "cfg_bidomain_create", "cfg_bidomain_create_from_dict", "cfg_bidomain_step", "cfg_bidomain_run", "cfg_bidomain_get_field",
-    "cfg_bidomain_set_field", "cfg_bidomain_last_stats", "cfg_bidomain_time",
+    "cfg_bidomain_set_field", "cfg_bidomain_device_field", "cfg_bidomain_last_stats",
+    "cfg_bidomain_time",
     "cfg_bidomain_reference_cell", "cfg_bidomain_ionic", "cfg_bidomain_stream",
     "cfg_bidomain_destroy",
 ]
@@ -257,6 +258,8 @@ def load(path: Optional[os.PathLike] = None):
     L.cfg_bidomain_run.argtypes = [C.c_void_p, C.c_double, C.c_longlong]
     L.cfg_bidomain_get_field.argtypes = [C.c_void_p, C.c_int, _dp]
     L.cfg_bidomain_set_field.argtypes = [C.c_void_p, C.c_int, _dp]
+    L.cfg_bidomain_device_field.argtypes = [C.c_void_p, C.c_int]
+    L.cfg_bidomain_device_field.restype = C.c_void_p
     L.cfg_bidomain_last_stats.argtypes = [C.c_void_p, C.POINTER(StepStats), C.POINTER(StepStats)]
     L.cfg_bidomain_time.argtypes = [C.c_void_p]
     L.cfg_bidomain_time.restype = C.c_double

@@ -457,6 +457,9 @@ int cfg_bidomain_run(cfg_bidomain* bd, double dt, long long n_steps);
 /* CFG_FIELD_VM, _IION, _ACTIVATION, _SOURCE, _VM_OLD, _PHIE, _PHII */
 int cfg_bidomain_get_field(cfg_bidomain* bd, int field, double* host);
 int cfg_bidomain_set_field(cfg_bidomain* bd, int field, const double* host);
+/* Device address of a field (CFG_FIELD_*; NULL for an unknown one), valid
+ * until cfg_bidomain_destroy; work on it belongs on cfg_bidomain_stream. */
+const double* cfg_bidomain_device_field(cfg_bidomain* bd, int field);
 /* The last step's Vm and phiE solves (one of each per corrector). */
 int cfg_bidomain_last_stats(const cfg_bidomain* bd, cfg_step_stats* vm, cfg_step_stats* phie);
 double cfg_bidomain_time(const cfg_bidomain* bd);

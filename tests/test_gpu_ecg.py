@@ -196,3 +196,37 @@ def test_float_pairs_against_fp64(gpu_lib, small_lv):
     assert np.max(np.abs(b.compute(flat))) <= 1e-12 * scale
     a.close()
     b.close()
+
+
+@pytest.mark.gpu
+def test_bidomain_source(gpu_lib, oracle):
+    """ECGDomain over a bidomain state (conductivity Gi, the context's Vm): the
+    pseudo-ECG read from the Bidomain context equals the one of the same Vm
+    as a tensor, and the oracle's on its own bidomain run."""
+    torch = pytest.importorskip("torch")
+    from cardiacfoam_gb300.mesh import box_mesh, with_box_geometry
+    h, dt = 2.5e-4, 2e-5
+    mesh = with_box_geometry(box_mesh(24, 8, 2, 24 * h, 8 * h, 2 * h), 24 * h, 8 * h, 2 * h)
+    box = [((0.0, 0.0, 0.0), (1.0e-3, 2 * h * 8, 2 * h), 0.0, 1e-3, 1e5)]
+    gi, ge = (0.17, 0.0, 0.0, 0.019, 0.0, 0.019), (0.62, 0.0, 0.0, 0.24, 0.0, 0.24)
+    bd = api.Bidomain(mesh, "TNNP", "epicardialCells", sigma_i=gi, sigma_e=ge, dt=dt,
+                      pcg_tol=1e-10, phie_tol=1e-10, n_outer=2, ref_point=(0.0, 0.0, 0.0),
+                      boxes=box)
+    d = oracle.tissue_desc("TNNP", 1, gi, implicit=True, precond_dic=False, pcg_tol=1e-10,
+                           pcg_rel_tol=0.0, n_outer=2, outer_tol=0.0, boxes=box)
+    B = oracle.Bidomain(d, ge, oracle.Mesh.general(mesh), (0.0, 0.0, 0.0), 0.0, 1e-10, 0.0, 1000)
+    el = np.array([[-2e-3, 1e-3, 2.5e-4], [8e-3, 1e-3, 2.5e-4], [3e-3, -4e-3, 1e-3]])
+    pe = api.PseudoECG(mesh, el, sigma=gi, max_rows=4)
+    for _ in range(100):
+        bd.step(dt)
+        B.step(dt)
+    got = pe.compute(bd)
+    same = pe.compute(torch.tensor(bd.vm(), device="cuda"))
+    assert np.array_equal(got, same)
+    want = B.tissue.pseudo_ecg(B.tissue.vm(), el)
+    assert np.all(np.abs(got - want) <= 1e-7 * np.max(np.abs(want)))
+    pe.record(bd)
+    t, v = pe.series()
+    assert t[0] == bd.time() and np.array_equal(v[0], got)
+    pe.close()
+    bd.close()
