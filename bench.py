@@ -9,9 +9,11 @@ Vm0 = -84 mV, starting at t = 0.  Synthetic (the reference publishes no
 dataset for this path).  A step is one runTime++/evolve over all cells.
 
 The headline `value` is the mixed-precision form's device-resident
-throughput in cell-steps/s; the FP64 plain form is timed on the same
-workload and the activation-time difference between the two runs is
-reported.  `e2e` repeats the mixed run through the C ABI with Vm copied in
+throughput in cell-steps/s over K steps of the wavefront window (from
+t = 10 ms, step 2000: the front inside the slab, cells in the upstroke taking
+many RKF45 substeps); the rest-state window right after the warm-up is
+reported beside it.  The FP64 plain form is timed in the same window and
+both forms are compared at its end (activation times, Vm).  `e2e` repeats the mixed run through the C ABI with Vm copied in
 from and out to pinned host memory every step.  Under torchrun every rank
 runs an independent replica on its own GPU (the step has no cross-rank
 exchange at one GPU per replica).
@@ -23,6 +25,7 @@ import json
 import os
 import subprocess
 import sys
+import tempfile
 import time
 from pathlib import Path
 
@@ -36,7 +39,8 @@ SIGMA = (0.1334, 0.0, 0.0, 0.0176, 0.0, 0.0176)
 BOX = [((0.0, 0.0, 0.0), (1.5e-3, 1.5e-3, 1.5e-3), 0.0, 2e-3, 5e4)]
 WORKLOAD = ("ORd myocyte monodomain slab 20x7x3 mm, h=0.1 mm (200x70x30 = 420000 cells), "
             "dt=5e-6 s, implicit (backward ddt, PIMPLE residualControl 1e-6, PCG tol 1e-8), "
-            "corner stimulus 5e4 A/m^3 x 2 ms, from t=0")
+            "corner stimulus 5e4 A/m^3 x 2 ms, from t=0; timed window from t=10 ms "
+            "(step 2000, the wavefront inside the slab)")
 DIMS = (200, 70, 30)
 H = 1e-4
 DT = 5e-6
@@ -67,12 +71,11 @@ class ClockSampler:
 
     def __init__(self, index: int):
         self.proc = None
-        self.path = ROOT / "gpurun_out" / f"clocks_{os.getpid()}.csv"
+        self.path = Path(tempfile.gettempdir()) / f"cfg_bench_clocks_{os.getpid()}.csv"
         self.index = index
 
     def __enter__(self):
         try:
-            self.path.parent.mkdir(exist_ok=True)
             self.fh = open(self.path, "w")
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.index}",
@@ -163,6 +166,14 @@ def timed_steps(md, k, flush, dt=DT):
 
 
 def gpu_arm(args, rank, world):
+    """The headline: the mixed form timed over K steps of the wavefront
+    window (steps window_start .. window_start + K, t = 10 ms by default, the
+    front inside the slab), after W warm-up steps and an untimed advance to
+    the window.  The rest-state window right after the warm-up (t ~ 0.05 ms,
+    one RKF45 substep per cell) is timed too and reported beside it.  The FP64
+    form runs to the same window, is timed there, and both forms are compared
+    at the window's end (activation times over every cell both activated,
+    Vm L-inf)."""
     import torch
     from cardiacfoam_gb300 import build as gpu_build, lib
     if rank == 0 or not (ROOT / "cardiacfoam_gb300/libcardiac_gpu.so").exists():
@@ -174,6 +185,7 @@ def gpu_arm(args, rank, world):
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")   # 256 MB > L2
     mesh = build_mesh()
     n = mesh.n_cells
+    K = args.steps
 
     # ---------------- mixed form (headline)
     mixed = make_model(mesh, lib.PRECISION_MIXED)
@@ -181,46 +193,61 @@ def gpu_arm(args, rank, world):
         mixed.step(DT)
     tune_mixed = mixed.autotune() if not args.no_autotune else None
     mixed.step(DT)                 # rebuilds the step graph with the chosen shape
+    # rest-state window (secondary figure)
+    mixed.set_timing(True)
+    e0 = mixed.rhs_evaluations()
+    t_rest = timed_steps(mixed, K, flush)
+    rest_ionic_ms, rest_diff_ms, _, _ = mixed.timings()
+    rest_evals = mixed.rhs_evaluations() - e0
+    mixed.set_timing(False)
+    # untimed advance to the wavefront window
+    done = args.warmup + 1 + K
+    window_start = max(args.window_start, done)
+    mixed.run(DT, window_start - done)
     mixed.set_timing(True)
     evals0 = mixed.rhs_evaluations()
     if world > 1:
         torch.distributed.barrier()
     with ClockSampler(dev) as clk:
-        t_mixed = timed_steps(mixed, args.steps, flush)
+        t_mixed = timed_steps(mixed, K, flush)
     t_mixed = max_over_ranks(t_mixed, world)
     ionic_ms, diff_ms, nsteps, launches = mixed.timings()
     evals = mixed.rhs_evaluations() - evals0
-    act_mixed = mixed.activation()
+    mixed.set_timing(False)
     clocks = clk.summary()
+    total_steps = window_start + K
 
-    # ---------------- FP64 plain form on the same workload; both forms then
-    # run to the end of an accuracy window and their activation times are
-    # compared over the cells both activated
-    k64 = max(1, min(args.steps, args.fp64_steps))
+    # ---------------- FP64 plain form: to the same window, timed there, then
+    # on to the mixed context's step for the comparison
+    k64 = max(1, min(K, args.fp64_steps))
     fp64 = make_model(mesh, lib.PRECISION_FP64)
     for _ in range(args.warmup):
         fp64.step(DT)
     tune_fp64 = fp64.autotune() if not args.no_autotune else None
-    fp64.step(DT)
+    fp64.run(DT, window_start - args.warmup)
     fp64.set_timing(True)
     t_fp64 = timed_steps(fp64, k64, flush)
     ionic64_ms, diff64_ms, _, _ = fp64.timings()
     fp64.set_timing(False)
-    window = max(args.accuracy_steps, args.warmup + 1 + k64)
-    fp64.run(DT, window - args.warmup - 1 - k64)
-    mixed_b = make_model(mesh, lib.PRECISION_MIXED)
-    mixed_b.run(DT, window)
-    a64, amx = fp64.activation(), mixed_b.activation()
+    fp64.run(DT, total_steps - window_start - k64)
+    a64, amx = fp64.activation(), mixed.activation()
     both = (a64 > 0) & (amx > 0)
     act_err_ms = float(np.max(np.abs(a64[both] - amx[both])) * 1e3) if both.any() else None
     mismatch = int(np.sum((a64 > 0) != (amx > 0)))
-    vm_err = float(np.max(np.abs(fp64.vm() - mixed_b.vm())))
-    del mixed_b, fp64
+    vm_err = float(np.max(np.abs(fp64.vm() - mixed.vm())))
+    in_box = np.zeros(n, dtype=bool)
+    lo, hi = BOX[0][0], BOX[0][1]
+    c = mesh.centres
+    in_box[:] = np.all((c >= np.array(lo)) & (c <= np.array(hi)), axis=1)
+    propagated = int(np.sum(both & ~in_box))
+    fp64_time = fp64.time()
+    del fp64
 
-    # ---------------- end to end through the C ABI with host copies
+    # ---------------- end to end through the C ABI with host copies, in the
+    # wavefront window
     pin_in = torch.empty(n, dtype=torch.float64, pin_memory=True)
     pin_out = torch.empty(n, dtype=torch.float64, pin_memory=True)
-    ke2e = max(1, min(args.steps, args.e2e_steps))
+    ke2e = max(1, min(K, args.e2e_steps))
     vm_host = pin_in.numpy()
     vm_host[:] = mixed.vm()
     vm_out = pin_out.numpy()
@@ -230,8 +257,7 @@ def gpu_arm(args, rank, world):
         mixed.set_field(lib.FIELD_VM, vm_host)
         mixed.step(DT)
         vm_out[:] = 0.0
-        from cardiacfoam_gb300 import lib as L
-        L.check(mixed._lib.cfg_monodomain_get_field(mixed.h, L.FIELD_VM, L.dptr(vm_out)))
+        lib.check(mixed._lib.cfg_monodomain_get_field(mixed.h, lib.FIELD_VM, lib.dptr(vm_out)))
         vm_host, vm_out = vm_out, vm_host
     t_e2e = time.perf_counter() - t0
 
@@ -246,9 +272,13 @@ def gpu_arm(args, rank, world):
     return dict(n=n, t_mixed=t_mixed, t_fp64=t_fp64, k64=k64, ionic_ms=ionic_ms,
                 diff_ms=diff_ms, ionic64_ms=ionic64_ms, diff64_ms=diff64_ms, evals=evals,
                 launches=launches, clocks=clocks, act_err_ms=act_err_ms, act_mismatch=mismatch,
-                act_cells=int(both.sum()), vm_err=vm_err, window=window, t_e2e=t_e2e, ke2e=ke2e, achieved=achieved,
+                act_cells=int(both.sum()), act_cells_outside_box=propagated, vm_err=vm_err,
+                window_start=window_start, compared_at_step=total_steps,
+                compared_at_time=fp64_time, t_e2e=t_e2e, ke2e=ke2e, achieved=achieved,
                 fp32_peak=fp32_peak, peaks=pk, peak_src=src, nnz=nnz,
-                n_active_mixed=int((act_mixed > 0).sum()),
+                n_active_mixed=int((amx > 0).sum()),
+                rest={"t": t_rest, "ionic_ms": rest_ionic_ms, "diff_ms": rest_diff_ms,
+                      "evals": rest_evals, "start_step": args.warmup + 1},
                 autotune={"mixed": tune_mixed, "fp64": tune_fp64})
 
 
@@ -604,18 +634,20 @@ def adjoint_arm(args):
     return out
 
 
-def cpu_baseline(nthreads=None, cells_x=40, steps=10):
+def cpu_baseline(nthreads=None, cells=(30, 30, 30), window_start=2000, steps=10):
     """The oracle (restated reference numerics) on a bounded sample of the
-    workload: a 4 x 7 x 3 mm piece of the slab (40 x 70 x 30 cells) for a few
-    steps with OpenMP over the host's cores."""
+    workload: a 3 x 3 x 3 mm corner piece of the slab (30 x 30 x 30 cells,
+    holding the stimulus box), advanced untimed to the timed window's start,
+    then `steps` steps timed with OpenMP over the host's cores."""
     from oracle import pyoracle as po
     nthreads = nthreads or os.cpu_count() or 1
-    nx, ny, nz = cells_x, DIMS[1], DIMS[2]
+    nx, ny, nz = cells
     mesh = po.Mesh(nx, ny, nz, nx * H, ny * H, nz * H)
     d = po.tissue_desc("ORd", 4, SIGMA, implicit=True, precond_dic=True, pcg_tol=1e-8,
                        boxes=BOX, ode=po.ode_settings(max_steps=10 ** 6))
     T = po.Tissue(d, mesh)
-    T.step(DT, nthreads)           # first step outside the timing (allocation)
+    for _ in range(window_start):
+        T.step(DT, nthreads)
     t0 = time.perf_counter()
     for _ in range(steps):
         T.step(DT, nthreads)
@@ -623,11 +655,16 @@ def cpu_baseline(nthreads=None, cells_x=40, steps=10):
     n = nx * ny * nz
     return {"value": n * steps / el, "unit": "cell-steps/s", "cores": nthreads, "kind": "port",
             "sample": f"CPU oracle (reference ionic code + restated OpenFOAM numerics, DIC-PCG) "
-                      f"on {nx}x{ny}x{nz} = {n} cells of the slab, {steps} steps after 1 "
-                      f"untimed step, {nthreads} threads"}
+                      f"on a {nx}x{ny}x{nz} = {n}-cell corner piece of the slab, advanced "
+                      f"untimed to step {window_start}, then {steps} steps timed, {nthreads} "
+                      f"threads"}
 
 
 def reference_arm(args, rank, world):
+    """The reference arm: the CPU oracle (reference ionic code + restated
+    OpenFOAM numerics, DIC-PCG) on the full slab with every host thread,
+    advanced untimed to the GPU arm's timed window (W warm-up steps end at
+    its start), then exactly K steps timed."""
     if rank != 0:
         return None
     from oracle import build as ob
@@ -639,22 +676,30 @@ def reference_arm(args, rank, world):
     d = po.tissue_desc("ORd", 4, SIGMA, implicit=True, precond_dic=True, pcg_tol=1e-8,
                        boxes=BOX, ode=po.ode_settings(max_steps=10 ** 6))
     T = po.Tissue(d, mesh)
-    k = max(1, min(args.steps, args.ref_steps))
-    for _ in range(min(args.warmup, 1)):
+    k, w = args.steps, args.warmup
+    window_start = max(args.window_start, w)
+    t_ff = time.perf_counter()
+    for _ in range(window_start - w):
         T.step(DT, nthreads)
+    for _ in range(w):
+        T.step(DT, nthreads)
+    t_ff = time.perf_counter() - t_ff
     t0 = time.perf_counter()
     for _ in range(k):
         T.step(DT, nthreads)
     el = time.perf_counter() - t0
     value = mesh.n * k / el
     sample = (f"CPU oracle (reference ionic code + restated OpenFOAM numerics, DIC-PCG) on the "
-              f"full 420000-cell slab, {k} timed steps, {nthreads} threads")
+              f"full 420000-cell slab: advanced untimed to step {window_start} (t = "
+              f"{window_start * DT * 1e3:g} ms, the last {w} of those steps as warm-up), then "
+              f"{k} timed steps, {nthreads} threads")
     return {"metric": METRIC, "impl": "reference", "value": value, "unit": "cell-steps/s",
-            "n_gpus": world, "steps": k, "warmup": min(args.warmup, 1),
+            "n_gpus": world, "steps": k, "warmup": w,
             "ms_per_step": el / k * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": WORKLOAD, "cells": mesh.n, "precision": "fp64",
-                       "parallelism": "host threads"},
+                       "parallelism": "host threads", "window_start_step": window_start},
+            "untimed_advance_seconds": t_ff,
             "cpu_baseline": {"value": value, "unit": "cell-steps/s", "cores": nthreads,
                              "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": "cell-steps/s", "h2d_bytes_per_step": 0,
@@ -754,9 +799,10 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--fp64-steps", type=int, default=12)
     ap.add_argument("--e2e-steps", type=int, default=20)
-    ap.add_argument("--ref-steps", type=int, default=10)
-    ap.add_argument("--accuracy-steps", type=int, default=300,
-                    help="steps both forms run before activation times are compared")
+    ap.add_argument("--window-start", type=int, default=2000,
+                    help="step at which the timed window starts (2000 x 5 us = 10 ms: the "
+                         "wavefront inside the slab); the FP64 and mixed forms are compared "
+                         "at the window's end")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched single cells")
     ap.add_argument("--no-mms", action="store_true", help="skip the manufactured-solution sweep")
@@ -850,9 +896,23 @@ def main():
                  "ionic_ms_per_step": r["ionic64_ms"] / r["k64"],
                  "diffusion_ms_per_step": r["diff64_ms"] / r["k64"]},
         "speedup_vs_fp64": value / world / fp64_value,
-        "activation_error_ms": r["act_err_ms"], "activation_cells_compared": r["act_cells"],
-        "accuracy_window_steps": r["window"], "vm_linf_error_V": r["vm_err"],
-        "activation_flag_mismatches": r["act_mismatch"],
+        "timed_window": {"start_step": r["window_start"], "start_time_s": r["window_start"] * DT,
+                         "steps": args.steps,
+                         "rhs_evaluations_per_cell_step": r["evals"] / (n * args.steps)},
+        "rest_window": {"start_step": r["rest"]["start_step"], "steps": args.steps,
+                        "value": n * args.steps / r["rest"]["t"], "unit": "cell-steps/s",
+                        "ms_per_step": r["rest"]["t"] / args.steps * 1e3,
+                        "phases_ms_per_step": {"ionic": r["rest"]["ionic_ms"] / args.steps,
+                                               "diffusion": r["rest"]["diff_ms"] / args.steps},
+                        "rhs_evaluations_per_cell_step":
+                            r["rest"]["evals"] / (n * args.steps)},
+        "accuracy": {"compared_at_step": r["compared_at_step"],
+                     "compared_at_time_s": r["compared_at_time"],
+                     "activation_error_ms": r["act_err_ms"],
+                     "activated_cells_compared": r["act_cells"],
+                     "activated_cells_outside_stimulus_box": r["act_cells_outside_box"],
+                     "activation_flag_mismatches": r["act_mismatch"],
+                     "vm_linf_error_V": r["vm_err"]},
         "phases_ms_per_step": {"ionic": r["ionic_ms"] / args.steps,
                                "diffusion": r["diff_ms"] / args.steps},
         "e2e": {"value": e2e_value, "unit": "cell-steps/s", "h2d_bytes_per_step": 8 * n,
@@ -891,8 +951,9 @@ def main():
     if not args.no_bidomain:
         out["bidomain"] = bidomain_arm(args)
     if not args.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_baseline()
-        one = cpu_baseline(nthreads=1, cells_x=10, steps=5)
+        out["cpu_baseline"] = cpu_baseline(window_start=args.window_start)
+        one = cpu_baseline(nthreads=1, cells=(10, 10, 10), window_start=args.window_start,
+                           steps=5)
         out["cpu_baseline"]["single_thread"] = {k: one[k] for k in ("value", "cores", "sample")}
         import platform
         cpu = platform.processor() or platform.machine()

@@ -283,6 +283,19 @@ class Monodomain:
     def time(self) -> float:
         return self._lib.cfg_monodomain_time(self.h)
 
+    def delta_t(self) -> float:
+        """The context's time step (the explicit algorithm's Courant limit
+        when created from an explicit electroProperties)."""
+        v = C.c_double()
+        _L.check(self._lib.cfg_monodomain_delta_t(self.h, C.byref(v)))
+        return v.value
+
+    def suggest_explicit_delta_t(self, max_co: float = 0.1) -> float:
+        """MyocardiumDomain::suggestExplicitDeltaT(maxCo)."""
+        v = C.c_double()
+        _L.check(self._lib.cfg_monodomain_suggest_explicit_delta_t(self.h, max_co, C.byref(v)))
+        return v.value
+
     def stats(self):
         s = _L.StepStats()
         _L.check(self._lib.cfg_monodomain_last_stats(self.h, C.byref(s)))

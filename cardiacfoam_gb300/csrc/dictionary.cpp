@@ -6,6 +6,7 @@
 //   chi / cm [dims] value;                              (myocardiumDomain.C:265-266)
 //   ionicModel, tissue, solver, absTol, relTol, maxSteps (ionicModel.C:76-94)
 //   solutionAlgorithm implicit|explicit                 (myocardiumDomain.C:271-277)
+//   explicit: deltaT = maxCo min(dx^2/Df)                (electroModel.C:238-257)
 //   externalStimulus { ... }                            (stimulusIO.C:305-400)
 #include <cctype>
 #include <cstdlib>
@@ -328,8 +329,26 @@ extern "C" int cfg_monodomain_create_from_dict(const char* text, const cfg_mesh_
         if (scalar(g->dict, "nOuterCorrectors", v)) d.n_outer = int(v);
         if (scalar(g->dict, "residualControl", v)) d.outer_tol = v;
     }
+    // controlDict's maxCo (default 0.1, electroModel.C:238-257) for the
+    // explicit algorithm's time step; the gpu sub-dictionary may carry it
+    double max_co = 0.1;
+    if (const Entry* g = find(c, "gpu"); g && g->is_dict && scalar(g->dict, "maxCo", v))
+        max_co = v;
     if (int rc = parse_stimulus(c, d)) return rc;
-    return cfg_monodomain_create(&d, mesh, out);
+    if (int rc = cfg_monodomain_create(&d, mesh, out)) return rc;
+    if (!d.implicit) {
+        // electroModel::setDeltaT: the explicit algorithm replaces deltaT once
+        // with MyocardiumDomain::suggestExplicitDeltaT(maxCo)
+        double dt = 0.0;
+        int rc = cfg_monodomain_suggest_explicit_delta_t(*out, max_co, &dt);
+        if (!rc) rc = cfg_monodomain_set_delta_t(*out, dt);
+        if (rc) {
+            cfg_monodomain_destroy(*out);
+            *out = nullptr;
+            return rc;
+        }
+    }
+    return CFG_OK;
 }
 
 // The same for myocardiumSolver bidomainSolver: bidomainSolverCoeffs'

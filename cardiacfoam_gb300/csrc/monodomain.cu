@@ -96,6 +96,51 @@ static int build_operator(cfg_monodomain* md, const cfg_mesh_desc* m, const cfg_
         }
         coeff = fc.data();
     }
+    // MyocardiumDomain::suggestExplicitDeltaT at maxCo = 1
+    // (myocardiumDomain.C:532-550): min over internal faces of dx^2/Df with
+    // dx = 1/deltaCoeffs = |C_N - C_P| and Df = n.(n.sigma_f)/(chi Cm), sigma_f
+    // the linear interpolate of the cells' conductivity.  From pre-assembled
+    // face coefficients (orthogonal faces: coeff = |Sf| n.sigma_f.n/|d|) the
+    // normal conductivity is coeff |d|/|Sf|.
+    md->explicit_dt_unit = -1.0;
+    if (m->face_sf && m->centres && nf > 0) {
+        const double chicm = d->chi * d->cm;
+        double best = 0.0;
+        bool any = false;
+        for (long long f = 0; f < nf; ++f) {
+            const double* S = m->face_sf + 3 * f;
+            const double magSf = std::sqrt(S[0] * S[0] + S[1] * S[1] + S[2] * S[2]);
+            const double* cp = m->centres + 3 * size_t(m->owner[f]);
+            const double* cn = m->centres + 3 * size_t(m->neighbour[f]);
+            const double dd[3] = {cn[0] - cp[0], cn[1] - cp[1], cn[2] - cp[2]};
+            const double dx = std::sqrt(dd[0] * dd[0] + dd[1] * dd[1] + dd[2] * dd[2]);
+            double nsn;
+            if (m->face_coeff && !general) {
+                nsn = m->face_coeff[f] * dx / magSf;
+            } else {
+                double sf[6];
+                if (d->conductivity_per_cell) {
+                    const double w = op.w[size_t(f)];
+                    const double* a = d->conductivity_per_cell + 6 * size_t(m->owner[f]);
+                    const double* b = d->conductivity_per_cell + 6 * size_t(m->neighbour[f]);
+                    for (int k = 0; k < 6; ++k) sf[k] = w * a[k] + (1.0 - w) * b[k];
+                } else {
+                    for (int k = 0; k < 6; ++k) sf[k] = sigma[k];
+                }
+                const double nx = S[0] / magSf, ny = S[1] / magSf, nz = S[2] / magSf;
+                const double g0 = nx * sf[0] + ny * sf[1] + nz * sf[2];
+                const double g1 = nx * sf[1] + ny * sf[3] + nz * sf[4];
+                const double g2 = nx * sf[2] + ny * sf[4] + nz * sf[5];
+                nsn = nx * g0 + ny * g1 + nz * g2;
+            }
+            const double Df = nsn / chicm;
+            if (!(Df > 0)) continue;
+            const double v = dx * dx / Df;
+            if (!any || v < best) best = v;
+            any = true;
+        }
+        if (any) md->explicit_dt_unit = best;
+    }
     // row entries: (column, face, the row cell owns the face)
     struct Entry {
         int col;
@@ -307,6 +352,7 @@ int monodomain_create(const cfg_monodomain_desc* d, const cfg_mesh_desc* m, cfg_
     md->implicit = d->implicit != 0;
     md->ddt_backward = d->ddt_backward != 0;
     md->chicm = d->chi * d->cm;   // chi*Cm evaluated first (monodomainSolver.C:129)
+    md->delta_t = d->ionic.initial_delta_t;
     md->n_boxes = d->n_boxes;
     for (int b = 0; b < d->n_boxes; ++b) {
         md->box_start[b] = d->box_start[b];
@@ -545,6 +591,7 @@ static long long graph_step_launches(const cfg_monodomain* md)
 int cfg_monodomain_step(cfg_monodomain* md, double dt)
 {
     if (!md) return fail(CFG_ERR_INVALID, "null context");
+    if (dt == 0.0) dt = md->delta_t;   // the context's own time step
     if (!(dt > 0)) return fail(CFG_ERR_INVALID, "deltaT must be positive");
     int rc = md->use_graph ? enqueue_graph_step(md, dt) : enqueue_step(md, dt, true);
     if (rc) return rc;
@@ -558,6 +605,7 @@ int cfg_monodomain_step(cfg_monodomain* md, double dt)
 int cfg_monodomain_run(cfg_monodomain* md, double dt, long long n_steps)
 {
     if (!md) return fail(CFG_ERR_INVALID, "null context");
+    if (dt == 0.0) dt = md->delta_t;
     if (!(dt > 0)) return fail(CFG_ERR_INVALID, "deltaT must be positive");
     if (!md->use_graph || md->timing) {
         for (long long i = 0; i < n_steps; ++i) {
@@ -661,6 +709,32 @@ int cfg_monodomain_set_field(cfg_monodomain* md, int field, const double* host)
 }
 
 double cfg_monodomain_time(const cfg_monodomain* md) { return md ? md->t_host : 0.0; }
+
+int cfg_monodomain_suggest_explicit_delta_t(const cfg_monodomain* md, double max_co, double* dt)
+{
+    if (!md || !dt) return fail(CFG_ERR_INVALID, "null argument");
+    if (!(max_co > 0)) return fail(CFG_ERR_INVALID, "maxCo must be positive");
+    if (!(md->explicit_dt_unit > 0))
+        return fail(CFG_ERR_INVALID, "the explicit time-step rule needs the mesh's face_sf and "
+                                     "centres and a positive normal conductivity");
+    *dt = max_co * md->explicit_dt_unit;
+    return CFG_OK;
+}
+
+int cfg_monodomain_delta_t(const cfg_monodomain* md, double* dt)
+{
+    if (!md || !dt) return fail(CFG_ERR_INVALID, "null argument");
+    *dt = md->delta_t;
+    return CFG_OK;
+}
+
+int cfg_monodomain_set_delta_t(cfg_monodomain* md, double dt)
+{
+    if (!md) return fail(CFG_ERR_INVALID, "null context");
+    if (!(dt > 0)) return fail(CFG_ERR_INVALID, "deltaT must be positive");
+    md->delta_t = dt;
+    return CFG_OK;
+}
 
 cfg_ionic* cfg_monodomain_ionic(cfg_monodomain* md) { return md ? md->ion : nullptr; }
 

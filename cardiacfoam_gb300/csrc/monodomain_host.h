@@ -65,6 +65,10 @@ struct cfg_monodomain {
     long long iter_cap = 100000;   // PCG iterations per step before the step aborts
     double t_host = 0.0;
     long long steps = 0;
+    // time step a caller may leave to the context (cfg_monodomain_step with
+    // dt = 0), and the explicit algorithm's Courant limit at maxCo = 1
+    double delta_t = 0.0;
+    double explicit_dt_unit = -1.0;
     // phase timing
     bool timing = false;
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};

@@ -234,10 +234,26 @@ int cfg_monodomain_create(const cfg_monodomain_desc* desc, const cfg_mesh_desc* 
 int cfg_monodomain_create_from_dict(const char* electro_properties, const cfg_mesh_desc* mesh,
                                     double delta_t, int precision, cfg_monodomain** out);
 
+/* MyocardiumDomain::suggestExplicitDeltaT(maxCo) (myocardiumDomain.C:532-550):
+ * maxCo * min over internal faces of dx^2/Df, dx = 1/deltaCoeffs = |C_N - C_P|,
+ * Df = n.(n.sigma_f)/(chi Cm) with sigma_f the linear interpolate of the
+ * conductivity (needs the mesh's face_sf and centres). */
+int cfg_monodomain_suggest_explicit_delta_t(const cfg_monodomain* md, double max_co, double* dt);
+
+/* The context's time step: delta_t of the description, or, for an explicit
+ * electroProperties read by cfg_monodomain_create_from_dict, the value
+ * electroModel::setDeltaT sets once (electroModel.C:238-257):
+ * suggestExplicitDeltaT(maxCo) with maxCo from the Coeffs' gpu sub-dictionary
+ * (the reference reads it from controlDict), default 0.1.  A caller passes
+ * dt = 0 to cfg_monodomain_step / cfg_monodomain_run to step with it, as
+ * runTime does after setDeltaT. */
+int cfg_monodomain_delta_t(const cfg_monodomain* md, double* dt);
+int cfg_monodomain_set_delta_t(cfg_monodomain* md, double dt);
+
 /* One time step: runTime++ then electroModel::evolve with the staggered
  * scheme (electroModel.C:297-330, myocardiumDomain.C:487-529): box stimulus,
  * ionic solveODE, implicit (PIMPLE + PCG) or explicit diffusion, activation
- * time. */
+ * time.  dt = 0 steps with the context's time step (cfg_monodomain_delta_t). */
 int cfg_monodomain_step(cfg_monodomain* md, double dt);
 
 /* The autotuner on the context's ionic model with its current Vm and

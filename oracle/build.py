@@ -15,7 +15,17 @@ from pathlib import Path
 HERE = Path(__file__).resolve().parent
 LIB = HERE / "_build" / "liboracle.so"
 REF_LIB = HERE / "_ref" / "libref_models.so"
-REFERENCE_DIR = Path(os.environ.get("CARDIACFOAM_REFERENCE", "/root/reference"))
+
+
+def reference_dir() -> Path | None:
+    """The cardiacFoam checkout this recipe reads: $CARDIACFOAM_REFERENCE, else
+    the build container's read-only mount.  None where neither exists (the
+    GPU host, a user's machine): then nothing that needs the reference runs."""
+    env = os.environ.get("CARDIACFOAM_REFERENCE")
+    for cand in ([Path(env)] if env else []) + [Path("/root/reference")]:
+        if (cand / "src" / "ionicModels").is_dir():
+            return cand
+    return None
 
 
 def _sources():
@@ -36,9 +46,10 @@ def build(force: bool = False) -> Path:
     return LIB
 
 
-def build_ref(reference: Path = REFERENCE_DIR) -> Path | None:
+def build_ref(reference: Path | None = None) -> Path | None:
     """Compile the reference's generated model headers, if the reference exists."""
-    if not (reference / "src" / "ionicModels").is_dir():
+    reference = reference or reference_dir()
+    if reference is None or not (reference / "src" / "ionicModels").is_dir():
         return None
     subprocess.run(["sh", str(HERE / "ref" / "build_ref.sh"), str(reference)], check=True,
                    stdout=subprocess.DEVNULL)

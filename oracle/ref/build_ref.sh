@@ -1,10 +1,10 @@
 #!/bin/sh
 # Builds oracle/_ref/libref_models.so from the reference's generated ionic
 # model headers, compiled verbatim where they lie in the reference tree.
-# Usage: oracle/ref/build_ref.sh [<cardiacFoam checkout>]   (default /root/reference)
+# Usage: oracle/ref/build_ref.sh <cardiacFoam checkout>   (oracle/build.py passes it)
 # Test infrastructure only: it pins the oracle's model code; nothing ships it.
 set -e
-REF=${1:-/root/reference}
+REF=${1:?usage: build_ref.sh <cardiacFoam checkout>}
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/../_ref"
 IM="$REF/src/ionicModels"

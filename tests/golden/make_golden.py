@@ -1,7 +1,7 @@
 """Generate the golden fixtures in this directory from the reference.
 
-Run in a checkout where cardiacFoam is available (default /root/reference,
-or $CARDIACFOAM_REFERENCE):
+Run where a cardiacFoam checkout is available ($CARDIACFOAM_REFERENCE, or the
+location oracle/build.py knows):
 
     python tests/golden/make_golden.py
 
@@ -19,7 +19,6 @@ or $CARDIACFOAM_REFERENCE):
   tutorials/regressionTests/NiedererEtAl2012/NiedererEtAl2012.reference:8-13.
 """
 import json
-import os
 import sys
 from pathlib import Path
 
@@ -31,7 +30,11 @@ sys.path.insert(0, str(ROOT))
 
 from oracle import pyoracle as po  # noqa: E402
 
-REF = Path(os.environ.get("CARDIACFOAM_REFERENCE", "/root/reference"))
+from oracle.build import reference_dir  # noqa: E402
+
+REF = reference_dir()
+if REF is None:
+    sys.exit("no cardiacFoam checkout found: set CARDIACFOAM_REFERENCE")
 KEYS = {"TNNP": "tnnp", "ORd": "ord", "ToRORd_dynCl": "torord_dyncl",
         "AlievPanfilov": "alievpanfilov", "BuenoOrovio": "buenoorovio"}
 TISSUES = {"TNNP": [1, 2, 3], "ORd": [4], "ToRORd_dynCl": [1, 2, 3], "AlievPanfilov": [4],

@@ -1,5 +1,4 @@
 """cellML2foam-to-CUDA emitter: parser units and reproducibility."""
-import os
 from pathlib import Path
 
 import pytest
@@ -7,9 +6,11 @@ import pytest
 from cardiacfoam_gb300.cellml2cuda import cexpr
 from cardiacfoam_gb300.cellml2cuda.emit import emit_c, emit_cuda
 from cardiacfoam_gb300.cellml2cuda.model import WRAPPERS, load_model, use_before_def
+from oracle.build import reference_dir
 
 ROOT = Path(__file__).resolve().parents[1]
-REF = Path(os.environ.get("CARDIACFOAM_REFERENCE", "/root/reference")) / "src" / "ionicModels"
+_REF = reference_dir()
+REF = (_REF / "src" / "ionicModels") if _REF is not None else None
 
 
 def test_parser_precedence():
@@ -31,7 +32,7 @@ def test_generated_files_present():
         assert (ROOT / "oracle" / "models" / f"{key}.h").exists()
 
 
-@pytest.mark.skipif(not REF.is_dir(), reason="reference checkout not available")
+@pytest.mark.skipif(REF is None, reason="no cardiacFoam checkout: set CARDIACFOAM_REFERENCE")
 @pytest.mark.parametrize("name", list(WRAPPERS))
 def test_regeneration_is_identical(name):
     m = load_model(REF, name)
@@ -41,14 +42,14 @@ def test_regeneration_is_identical(name):
     assert emit_c(m, rel) == (ROOT / "oracle/models" / f"{key}.h").read_text()
 
 
-@pytest.mark.skipif(not REF.is_dir(), reason="reference checkout not available")
+@pytest.mark.skipif(REF is None, reason="no cardiacFoam checkout: set CARDIACFOAM_REFERENCE")
 def test_use_before_def_is_only_istim():
     for name in WRAPPERS:
         m = load_model(REF, name)
         assert set(use_before_def(m.rates)) <= {"Istim"}
 
 
-@pytest.mark.skipif(not REF.is_dir(), reason="reference checkout not available")
+@pytest.mark.skipif(REF is None, reason="no cardiacFoam checkout: set CARDIACFOAM_REFERENCE")
 def test_supplement_covers_exactly_the_unassigned_constants():
     from cardiacfoam_gb300.cellml2cuda.emit import SUPPLEMENT, supplement_for, unassigned_constants
     for name in WRAPPERS:

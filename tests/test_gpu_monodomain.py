@@ -197,3 +197,55 @@ def test_fields_written_as_openfoam_volscalarfields(gpu_lib, tmp_path):
         assert vals.size == ref.size
         assert np.allclose(vals, ref, rtol=1e-5, atol=1e-12)
     m.close()
+
+
+NIEDERER_DICT = """
+myocardiumSolver  monodomainSolver;
+monodomainSolverCoeffs
+{
+    conductivity [-1 -3 3 0 0 2 0] (0.1334177215 0 0 0.01760617761 0 0.01760617761);
+    chi   [0 -1 0 0 0 0 0] 140000;
+    cm    [-1 -4 4 0 0 2 0] 0.01;
+    ionicModel    BuenoOrovio;
+    tissue    epicardialCells;
+    solutionAlgorithm    explicit;
+    solver RKF45;
+    maxSteps 1000000000;
+    externalStimulus
+    {
+        stimulusLocationMin (0 0 5.5e-3);
+        stimulusLocationMax (1.5e-3 1.5e-3 7e-3);
+        stimulusDuration [0 0 1 0 0 0 0] 2e-3;
+        stimulusIntensity [0 -3 0 0 0 1 0] 50000;
+        stimulusStartTime 0.0;
+    }
+}
+"""
+
+
+@pytest.mark.gpu
+def test_explicit_delta_t_rule_on_the_niederer_slab(gpu_lib):
+    """electroModel::setDeltaT for the explicit algorithm: deltaT becomes
+    maxCo * min(dx^2/Df) (myocardiumDomain.C:532-550), computed here as the
+    regression test's restatement does, and steps taken with dt = 0 use it."""
+    nx, ny, nz, lx, ly, lz = 100, 15, 35, 0.02, 0.003, 0.007
+    mesh = box_mesh(nx, ny, nz, lx, ly, lz)
+    sig = (0.1334177215, 0.01760617761, 0.01760617761)
+    chicm = 140000 * 0.01
+    dxs = (lx / nx, ly / ny, lz / nz)
+    expect = 0.1 * min(dxs[d] ** 2 / (sig[d] / chicm) for d in range(3))
+    m = api.Monodomain.from_dict(NIEDERER_DICT, mesh, 5e-5)
+    assert abs(m.delta_t() - expect) <= 1e-14 * expect
+    assert abs(m.suggest_explicit_delta_t(0.2) - 2 * expect) <= 1e-14 * expect
+    m.step(0.0)
+    m.run(0.0, 4)
+    assert abs(m.time() - 5 * expect) <= 1e-15
+    # the controlDict's maxCo through the gpu sub-dictionary
+    text = NIEDERER_DICT.replace("solver RKF45;", "solver RKF45;\n    gpu { maxCo 0.05; }")
+    m2 = api.Monodomain.from_dict(text, mesh, 5e-5)
+    assert abs(m2.delta_t() - 0.5 * expect) <= 1e-14 * expect
+    # an implicit dictionary keeps the caller's deltaT
+    m3 = api.Monodomain.from_dict(NIEDERER_DICT.replace("explicit;", "implicit;"), mesh, 5e-5)
+    assert m3.delta_t() == 5e-5
+    for x in (m, m2, m3):
+        x.close()
