@@ -646,7 +646,8 @@ def cpu_baseline(nthreads=None, cells=(30, 30, 30), window_start=2000, steps=10)
     d = po.tissue_desc("ORd", 4, SIGMA, implicit=True, precond_dic=True, pcg_tol=1e-8,
                        boxes=BOX, ode=po.ode_settings(max_steps=10 ** 6))
     T = po.Tissue(d, mesh)
-    for _ in range(window_start):
+    T.step(DT, nthreads)           # first step outside the timing (allocation)
+    for _ in range(window_start - 1):
         T.step(DT, nthreads)
     t0 = time.perf_counter()
     for _ in range(steps):
@@ -656,8 +657,8 @@ def cpu_baseline(nthreads=None, cells=(30, 30, 30), window_start=2000, steps=10)
     return {"value": n * steps / el, "unit": "cell-steps/s", "cores": nthreads, "kind": "port",
             "sample": f"CPU oracle (reference ionic code + restated OpenFOAM numerics, DIC-PCG) "
                       f"on a {nx}x{ny}x{nz} = {n}-cell corner piece of the slab, advanced "
-                      f"untimed to step {window_start}, then {steps} steps timed, {nthreads} "
-                      f"threads"}
+                      f"untimed to step {max(window_start, 1)}, then {steps} steps timed, "
+                      f"{nthreads} threads"}
 
 
 def reference_arm(args, rank, world):
@@ -952,8 +953,9 @@ def main():
         out["bidomain"] = bidomain_arm(args)
     if not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(window_start=args.window_start)
-        one = cpu_baseline(nthreads=1, cells=(10, 10, 10), window_start=args.window_start,
-                           steps=5)
+        # one thread: a 10 x 70 x 30 piece timed from t = 0 (the advance to the
+        # wavefront window would take minutes on one core)
+        one = cpu_baseline(nthreads=1, cells=(10, 70, 30), window_start=0, steps=5)
         out["cpu_baseline"]["single_thread"] = {k: one[k] for k in ("value", "cores", "sample")}
         import platform
         cpu = platform.processor() or platform.machine()

@@ -334,6 +334,11 @@ class Monodomain:
     def set_timing(self, enable: bool = True):
         _L.check(self._lib.cfg_monodomain_set_timing(self.h, int(enable)))
 
+    def set_wait_limit(self, spins: int = -1):
+        """Bound on each grid-barrier wait of the persistent diffusion
+        kernel (spins; negative = the default, about a second)."""
+        _L.check(self._lib.cfg_monodomain_set_wait_limit(self.h, int(spins)))
+
     def write(self, case_dir, patches=(("walls", "zeroGradient"),), precision=6):
         """Vm and activationTime as OpenFOAM ASCII volScalarFields in
         <case_dir>/<timeName>/."""
@@ -456,7 +461,7 @@ class Bidomain:
                  pcg_max_iter=1000, phie_tol=1e-8, phie_rel_tol=0.0, phie_max_iter=1000,
                  n_outer=1, outer_tol=0.0, vm0=-0.084, ref_point=(0.0, 0.0, 0.0),
                  ref_value=0.0, boxes: Sequence = (), ode=None, max_steps=10 ** 6,
-                 grad_scheme=_L.GRAD_LEAST_SQUARES):
+                 grad_scheme=_L.GRAD_LEAST_SQUARES, implicit=True):
         self._lib = _L.load()
         if not mesh.has_geometry:
             raise ValueError("the bidomain step needs a mesh with its full geometry")
@@ -470,8 +475,11 @@ class Bidomain:
         for i in range(6):
             d.conductivity_i[i] = sigma_i[i]
             d.conductivity_e[i] = sigma_e[i]
+        # ECGDomain::conductivity() of a bidomain source is Gi (bidomainSolver.H:76-78)
+        self.sigma_i = tuple(float(v) for v in sigma_i)
         d.chi, d.cm = chi, cm
         d.ddt_backward = int(ddt_backward)
+        d.explicit_algorithm = int(not implicit)
         d.pcg_tol, d.pcg_rel_tol, d.pcg_max_iter = pcg_tol, pcg_rel_tol, pcg_max_iter
         d.phie_tol, d.phie_rel_tol, d.phie_max_iter = phie_tol, phie_rel_tol, phie_max_iter
         d.n_outer, d.outer_tol, d.vm0 = n_outer, outer_tol, vm0
@@ -626,6 +634,8 @@ class PseudoECG:
             raise ValueError("one name per electrode")
         self.n = mesh.n_cells
         self.max_rows = int(max_rows)
+        self.sigma = tuple(float(v) for v in sigma)
+        self.per_cell = conductivity_per_cell is not None
         d = _L.PseudoEcgDesc()
         for i, v in enumerate(sigma):
             d.conductivity[i] = v
@@ -663,6 +673,11 @@ class PseudoECG:
     def _bidomain_vm(self, bd: "Bidomain"):
         if bd.n != self.n:
             raise ValueError("the bidomain context has another cell count")
+        # the lead rows fold in the conductivity: for a bidomain source it must
+        # be the intracellular Gi, as ECGDomain::conductivity() gives it
+        if self.per_cell or self.sigma != bd.sigma_i:
+            raise ValueError("a pseudo-ECG of a bidomain context needs that context's "
+                             "intracellular conductivity sigma_i")
         return (C.c_void_p(self._lib.cfg_bidomain_device_field(bd.h, _L.FIELD_VM)),
                 C.c_void_p(bd.stream()))
 
@@ -708,6 +723,11 @@ class PseudoECG:
 
     def reset(self):
         _L.check(self._lib.cfg_pseudo_ecg_reset(self.h))
+
+    def set_wait_limit(self, cycles: int = -1):
+        """Bound on each tile-copy wait of the staged kernel (clock cycles;
+        negative = the default, about a second)."""
+        _L.check(self._lib.cfg_pseudo_ecg_set_wait_limit(self.h, int(cycles)))
 
     def close(self):
         if getattr(self, "h", None):

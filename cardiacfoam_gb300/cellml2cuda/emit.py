@@ -330,6 +330,112 @@ def _cuda_body(m: Model, stmts, pr: _CudaPrinter, indent: str, out: List[str]):
             out.append(f"{indent}/* unsupported configuration in the reference */")
 
 
+class _TissuePrinter(_CudaPrinter):
+    """The right-hand side of tissue mode with the membrane-potential-only
+    algebraics read from the per-cell values H (see hoist.py); a read before
+    such an algebraic's assignment is the zeroed scratch, as in the body."""
+
+    def __init__(self, m: Model, early: List[str], invariant, needed):
+        super().__init__(m, early, "rhs")
+        self.invariant = set(invariant)
+        self.needed = list(needed)
+        self.hoisted_defined = set()
+
+    def ref(self, r: Ref) -> str:
+        if r.array == "ALGEBRAIC" and r.name in self.invariant:
+            if r.name not in self.hoisted_defined:
+                return "R(0)"
+            return f"H(H_{r.name})"
+        return super().ref(r)
+
+
+def _cuda_body_tissue(m: Model, stmts, pr: _TissuePrinter, indent: str, out: List[str]):
+    """The body without the invariant assignments (whose values H holds)."""
+    inv = pr.invariant
+    for st in stmts:
+        if isinstance(st, Assign):
+            if st.target.array == "ALGEBRAIC" and st.target.name in inv:
+                pr.hoisted_defined.add(st.target.name)
+                continue
+            _cuda_body(m, [st], pr, indent, out)
+        elif isinstance(st, If):
+            assigns = list(iter_assigns([st]))
+            if all(a.target.array == "ALGEBRAIC" and a.target.name in inv for a in assigns):
+                pr.hoisted_defined.update(a.target.name for a in assigns)
+                continue
+            out.append(f"{indent}if ({pr(st.cond)}) {{")
+            _cuda_body_tissue(m, st.then, pr, indent + "    ", out)
+            if st.orelse:
+                out.append(f"{indent}}} else {{")
+                _cuda_body_tissue(m, st.orelse, pr, indent + "    ", out)
+            out.append(f"{indent}}}")
+        elif isinstance(st, Fatal):
+            out.append(f"{indent}/* unsupported configuration in the reference */")
+
+
+def _emit_tissue_rhs(m: Model, L: List[str]):
+    """hoist() and rhs_tissue(): the right-hand side of tissue mode split into
+    its membrane-potential-only part, evaluated once per cell and PDE step,
+    and the rest, evaluated at every RKF45 stage."""
+    from .hoist import analyse, invariant_statements
+    h = analyse(m, m.rates)
+    vm = m.states[0]
+    L.append("// Tissue mode (solveVmWithinODESolver false): the PDE owns the membrane")
+    L.append("// potential, so state 0 is the same at every RKF45 stage of a PDE step and")
+    L.append("// the algebraics computed from it and constants alone are too.  hoist()")
+    L.append("// evaluates the ones the rest of the body reads, once per cell and step,")
+    L.append("// into H[NH]; rhs_tissue() is the body without them, reading H(H_x) (the")
+    L.append("// same expressions in the same order: bitwise the values of rhs()).")
+    L.append(f"constexpr int NH = {len(h.needed)};")
+    if h.needed:
+        L.append("enum Hoisted { " + ", ".join(f"H_{a}" for a in h.needed) + " };")
+    L.append("template <class R, class KS>")
+    L.append(f"__device__ __forceinline__ void hoist(R y_{vm}, const KS& K, int tissue, R* H)")
+    L.append("{")
+    L.append(f"    (void)tissue; (void)K; (void)H; (void)y_{vm};")
+    if h.needed:
+        stmts = invariant_statements(m.rates, h.invariant)
+        pr = _CudaPrinter(m, [], "rhs")
+        body: List[str] = []
+        for name in _predeclare_conditional_algebraics(m, stmts, body, "    "):
+            body.append(f"    R a_{name} = R(0);")
+            pr.defined.add(name)
+        _cuda_body(m, stmts, pr, "    ", body)
+        if set(pr.states_read) - {vm}:
+            raise ValueError(f"{m.name}: hoisted statements read {pr.states_read}")
+        L.extend(body)
+        for a in h.needed:
+            L.append(f"    H[H_{a}] = a_{a};")
+    L.append("}")
+    L.append("template <class R, class YS, class KS, class HS>")
+    L.append("__device__ __forceinline__ R rhs_tissue(double t, const YS& Y, const KS& K, "
+             "const HS& H, R* dydt, int tissue, const CfgStimulus& stim)")
+    L.append("{")
+    if not h.needed:
+        L.append("    (void)H;")
+        L.append("    return rhs<R, false>(t, Y, K, dydt, tissue, stim);")
+        L.append("}")
+        return h
+    L.append("    constexpr bool SOLVE_VM = false;")
+    L.append("    (void)tissue; (void)stim; (void)t; (void)H;")
+    pr = _TissuePrinter(m, use_before_def(m.rates), h.invariant, h.needed)
+    body = []
+    for name in _predeclare_conditional_algebraics(m, m.rates, body, "    "):
+        if name in h.invariant:
+            continue
+        body.append(f"    R a_{name} = R(0);")
+        pr.defined.add(name)
+    _cuda_body_tissue(m, m.rates, pr, "    ", body)
+    L.extend(_state_loads(m, pr))
+    L.extend(body)
+    if m.iion_name in h.invariant:
+        L.append(f"    return H(H_{m.iion_name});")
+    else:
+        L.append(f"    return a_{m.iion_name};")
+    L.append("}")
+    return h
+
+
 def _state_loads(m: Model, pr: "_CudaPrinter") -> List[str]:
     """Every state the body reads, loaded once before any derivative is
     written: the stores to dydt then cannot force reloads (the compiler must
@@ -508,6 +614,8 @@ def emit_cuda(m: Model, src_rel: str) -> str:
     L.append(f"    return a_{m.iion_name};")
     L.append("}")
     L.append("")
+    _emit_tissue_rhs(m, L)
+    L.append("")
     # iion at end of step (the variables body); last Iion assignment wins
     L.append("// Ionic current after the step (computeVariables at tEnd).")
     L.append("template <class R, bool SOLVE_VM, class YS, class KS>")
@@ -576,6 +684,14 @@ def emit_cuda(m: Model, src_rel: str) -> str:
     L.append("    template <int T> CFG_HD static constexpr double constant(int i) "
              "{ return cval<T>(i); }")
     L.append("    static constexpr int NSD = " + ns + "::NSD, CA_STATE = " + ns + "::CA_STATE;")
+    L.append("    static constexpr int NH = " + ns + "::NH;")
+    L.append("    template <class R, class KS>")
+    L.append("    __device__ static __forceinline__ void hoist_vm(R v, const KS& K, int tissue, "
+             "R* H) { hoist<R>(v, K, tissue, H); }")
+    L.append("    template <class R, class YS, class KS, class HS>")
+    L.append("    __device__ static __forceinline__ R rates_tissue(double t, const YS& Y, "
+             "const KS& K, const HS& H, R* dydt, int tissue, const CfgStimulus& st) "
+             "{ return rhs_tissue<R>(t, Y, K, H, dydt, tissue, st); }")
     L.append("    CFG_HD static constexpr int sd_slot(int i) { return " + ns + "::sd_slot(i); }")
     L.append("    static constexpr int NA = " + ns + "::NA;")
     L.append("    template <class R, bool SV, class YS, class KS>")

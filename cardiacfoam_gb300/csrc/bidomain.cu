@@ -16,12 +16,18 @@
 // weight).  Meshes whose Laplacians need explicit non-orthogonal or
 // tangential corrections are rejected (CFG_ERR_UNSUPPORTED).
 //
-// The PCG runs as a kernel sequence with its scalars on the device, two
-// launches per iteration (each kernel's last block finishes the reduction and
-// the scalar update); chunks of iterations are replayed from a CUDA graph and
-// the host reads one flag per chunk; iterations after convergence return at
-// once.  Reductions add the blocks' sums in block order, so results are
-// reproducible bit for bit.
+// Each PCG solve is one persistent cooperative launch (every block resident,
+// rows strided over the grid) with two grid barriers per iteration: the
+// direction pass forms p = z + beta p_old and applies A to it, reading the
+// neighbours' z and previous p through L2 and forming their p the same way
+// (lduMatrix's PCG applies A to the new direction; p is double-buffered so
+// that no row is overwritten while a neighbour reads it), then the update
+// pass x += alpha p, r -= alpha A p, z = D^-1 r.  Block sums are added in
+// block order by every block, so the scalars are identical everywhere and
+// results reproducible bit for bit.  Barrier waits are bounded (the step then
+// reports CFG_ERR_PCG).  Where cooperative launch is not available the same
+// iteration runs as a kernel sequence with its scalars on the device, two
+// launches per iteration, replayed in chunks from a CUDA graph.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -29,6 +35,7 @@
 #include <vector>
 
 #include "geometry.h"
+#include "grid_sync.cuh"
 #include "host_common.h"
 #include "ionic_host.h"
 
@@ -230,6 +237,40 @@ __global__ void k_vm_system(BdOp op, VmArgs a, const double* __restrict__ vm_old
     b[c] = bb + dp[c];
 }
 
+// Explicit algorithm: chi Cm ddt(Vm) == V div(Gi grad(Vm + phiE)) - chi Cm
+// Iion V + src V with the diagonal matrix of fvm::ddt, solved as source over
+// diagonal; dv holds V div(Gi grad(Vm + phiE))
+__global__ void k_vm_explicit(BdOp op, VmArgs a, const double* __restrict__ vm_old,
+                              const double* __restrict__ vm_oldold,
+                              const double* __restrict__ iion, const double* __restrict__ src,
+                              const double* __restrict__ dv, double* __restrict__ vm)
+{
+    const long long c = (long long)blockIdx.x * kBlock + threadIdx.x;
+    if (c >= op.n) return;
+    const double V = op.vol[c];
+    double ddt_diag, ddt_src;
+    if (a.backward) {
+        ddt_diag = (a.cft * a.rdt) * V;
+        ddt_src = a.rdt * V * (a.cft0 * vm_old[c] - a.cft00 * vm_oldold[c]);
+    } else {
+        ddt_diag = a.rdt * V;
+        ddt_src = a.rdt * vm_old[c] * V;
+    }
+    const double diag = a.chicm * ddt_diag;
+    double bb = a.chicm * ddt_src;
+    double su = -(a.chicm * iion[c]) * V;
+    su = su + src[c] * V;
+    bb = bb + su;
+    vm[c] = (bb + dv[c]) / diag;
+}
+
+// x = u + v (Vm + phiE for the explicit divergence)
+__global__ void k_add(long long n, const double* u, const double* v, double* x)
+{
+    const long long c = (long long)blockIdx.x * kBlock + threadIdx.x;
+    if (c < n) x[c] = u[c] + v[c];
+}
+
 // --- PCG kernels (device scalars in PcgScalars) ---------------------------
 // Each kernel ends with its reduction: the blocks' sums go to the partial
 // buffer, and the last block to finish (a ticket counter) adds them in block
@@ -374,6 +415,144 @@ __global__ void k_pcg_update(PcgArgs a)
     stage_end<2>(v, a.partial, a.ticket, 3, a.op.n, a.st);
 }
 
+// --- the persistent solve --------------------------------------------------
+constexpr int kCoopBlock = 512;
+
+struct CoopPcgArgs {
+    PcgArgs a;
+    double* p_alt;            // second direction buffer
+    double* partial;          // [2 sets][2][gridDim.x]
+    unsigned* bar_count;      // grid barrier (zeroed before the launch)
+    int* bar_abort;
+    long long spin_limit;
+};
+
+// The direction of row q: z + beta p_old (z at the first iteration), the
+// same operations wherever a row's direction is formed.
+__device__ __forceinline__ double direction(const double* z, const double* p_old, double beta,
+                                            bool first, long long q)
+{
+    const double zq = __ldcg(&z[q]);
+    return first ? zq : __fma_rn(beta, __ldcg(&p_old[q]), zq);
+}
+
+__global__ void __launch_bounds__(kCoopBlock, 1) k_pcg_coop(CoopPcgArgs ca)
+{
+    using namespace cfg::gsync;
+    const PcgArgs& a = ca.a;
+    const BdOp& op = a.op;
+    PcgScalars* st = a.st;
+    const long long n = op.n;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const long long first = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const double tol = st->tol, rel = st->rel;
+    const int max_iter = st->max_iter;
+    unsigned epoch = 0;
+    int set = 0;
+    bool aborted = false;
+    double init_res = 0.0, res = 0.0;
+    int iter = 0, status = 0;
+    const auto conv = [&](double rr) { return rr < tol || (rel > 1e-20 && rr < rel * init_res); };
+    do {
+        // --- A x, r = b - A x; sums of x and |r|
+        double s1[2] = {0.0, 0.0};
+        for (long long c = first; c < n; c += stride) {
+            const double ax = amul(op, a.coef, a.diag, a.x, c);
+            const double rr = a.b[c] - ax;
+            a.ax[c] = ax;
+            a.r[c] = rr;
+            s1[0] += a.x[c];
+            s1[1] += fabs(rr);
+        }
+        block_sums<kCoopBlock, 2>(ca.partial, set, s1);
+        if (!grid_barrier(ca.bar_count, ca.bar_abort, epoch, ca.spin_limit)) { aborted = true; break; }
+        double g1[2];
+        grid_sums<2>(ca.partial, set, g1);
+        set ^= 1;
+        const double avg = g1[0] / double(n);
+        // --- normFactor; z = D^-1 r (published), z.r
+        double s2[2] = {0.0, 0.0};
+        for (long long c = first; c < n; c += stride) {
+            const double pa = row_sum(op, a.coef, a.diag, c) * avg;
+            s2[0] += fabs(a.ax[c] - pa) + fabs(a.b[c] - pa);
+            const double rr = a.r[c];
+            const double zc = rr / a.diag[c];
+            __stcg(&a.z[c], zc);
+            s2[1] += zc * rr;
+        }
+        block_sums<kCoopBlock, 2>(ca.partial, set, s2);
+        if (!grid_barrier(ca.bar_count, ca.bar_abort, epoch, ca.spin_limit)) { aborted = true; break; }
+        double g2[2];
+        grid_sums<2>(ca.partial, set, g2);
+        set ^= 1;
+        const double normf = g2[0] + 1e-20;
+        init_res = g1[1] / normf;
+        res = init_res;
+        double wArA = g2[1], beta = 0.0;
+        double* p_old = a.p;
+        double* p_new = ca.p_alt;
+        while (!conv(res)) {
+            // --- direction pass: p = z + beta p_old, A p, sum p.A p
+            const bool first_it = iter == 0;
+            double s3[1] = {0.0};
+            for (long long c = first; c < n; c += stride) {
+                const double pc = direction(a.z, p_old, beta, first_it, c);
+                double acc = a.diag[c] * pc;
+                const int k = op.cnt[c];
+                for (int e = 0; e < k; ++e) {
+                    const long long i = (long long)e * n + c;
+                    acc += (-a.coef[i]) * direction(a.z, p_old, beta, first_it, op.col[i]);
+                }
+                __stcg(&p_new[c], pc);
+                a.ap[c] = acc;
+                s3[0] += acc * pc;
+            }
+            block_sums<kCoopBlock, 1>(ca.partial, set, s3);
+            if (!grid_barrier(ca.bar_count, ca.bar_abort, epoch, ca.spin_limit)) { aborted = true; break; }
+            double g3[1];
+            grid_sums<1>(ca.partial, set, g3);
+            set ^= 1;
+            const double wApA = g3[0];
+            if (fabs(wApA) / normf < 1e-300) break;   // checkSingularity
+            const double alpha = wArA / wApA;
+            // --- update pass: x, r, z; |r| and z.r
+            double s4[2] = {0.0, 0.0};
+            for (long long c = first; c < n; c += stride) {
+                a.x[c] = a.x[c] + alpha * __ldcg(&p_new[c]);
+                const double rr = a.r[c] - alpha * a.ap[c];
+                a.r[c] = rr;
+                const double zc = rr / a.diag[c];
+                __stcg(&a.z[c], zc);
+                s4[0] += fabs(rr);
+                s4[1] += zc * rr;
+            }
+            block_sums<kCoopBlock, 2>(ca.partial, set, s4);
+            if (!grid_barrier(ca.bar_count, ca.bar_abort, epoch, ca.spin_limit)) { aborted = true; break; }
+            double g4[2];
+            grid_sums<2>(ca.partial, set, g4);
+            set ^= 1;
+            res = g4[0] / normf;
+            ++iter;
+            if (conv(res) || iter >= max_iter) {
+                if (!conv(res)) status = 1;
+                break;
+            }
+            beta = g4[1] / wArA;
+            wArA = g4[1];
+            double* t = p_old;
+            p_old = p_new;
+            p_new = t;
+        }
+    } while (false);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        st->iter = iter;
+        st->init_res = init_res;
+        st->res = res;
+        st->status = aborted ? 2 : status;
+        st->done = 1;
+    }
+}
+
 __global__ void k_phii(long long n, const double* vm, const double* phie, double* phii)
 {
     const long long c = (long long)blockIdx.x * kBlock + threadIdx.x;
@@ -416,6 +595,13 @@ struct cfg_bidomain {
     PcgScalars* d_st = nullptr;
     PcgScalars* h_st = nullptr;     // pinned
     unsigned* d_ticket = nullptr;
+    // the persistent solve: grid (0: not available), second direction buffer,
+    // its reduction partials and grid barrier
+    int coop_blocks = 0;
+    double *d_p_alt = nullptr, *d_coop_partial = nullptr;
+    unsigned* d_bar = nullptr;
+    int* d_abort = nullptr;
+    long long spin_limit = cfg::gsync::kSpinLimit;
     // kChunk PCG iterations of each system captured as a graph: [0] phiE, [1] Vm
     cudaGraphExec_t chunk[2] = {nullptr, nullptr};
     // settings
@@ -424,6 +610,7 @@ struct cfg_bidomain {
     double vm_tol = 1e-8, vm_rel = 0.0, e_tol = 1e-8, e_rel = 0.0;
     int vm_max = 1000, e_max = 1000, n_outer = 1;
     double outer_tol = 0.0;
+    bool explicit_alg = false;
     long long ref = -1;
     double ref_value = 0.0;
     StimArgs stim{};
@@ -464,6 +651,39 @@ int pcg_solve(cfg_bidomain* bd, int kind, double tol, double rel, int max_iter,
     const int nb = bd->blocks;
     const PcgArgs a = kind == 0 ? pcg_args(bd, bd->op.coef_e, bd->d_phie)
                                 : pcg_args(bd, bd->op.coef_i, bd->d_vm);
+    if (bd->coop_blocks > 0) {
+        PcgScalars init{};
+        init.tol = tol;
+        init.rel = rel;
+        init.max_iter = max_iter;
+        *bd->h_st = init;
+        CFG_CUDA_TRY(cudaMemcpyAsync(bd->d_st, bd->h_st, sizeof(PcgScalars),
+                                     cudaMemcpyHostToDevice, s));
+        CFG_CUDA_TRY(cudaMemsetAsync(bd->d_bar, 0, sizeof(unsigned), s));
+        CFG_CUDA_TRY(cudaMemsetAsync(bd->d_abort, 0, sizeof(int), s));
+        CoopPcgArgs ca{a, bd->d_p_alt, bd->d_coop_partial, bd->d_bar, bd->d_abort,
+                       bd->spin_limit};
+        void* params[] = {&ca};
+        CFG_CUDA_TRY(cudaLaunchCooperativeKernel((void*)k_pcg_coop, dim3(bd->coop_blocks),
+                                                 dim3(kCoopBlock), params, 0, s));
+        CFG_CUDA_TRY(cudaMemcpyAsync(bd->h_st, bd->d_st, sizeof(PcgScalars),
+                                     cudaMemcpyDeviceToHost, s));
+        CFG_CUDA_TRY(cudaStreamSynchronize(s));
+        const PcgScalars& st = *bd->h_st;
+        const int k = stats.n_solves;
+        if (k < kMaxSolves) {
+            stats.iterations[k] = st.iter;
+            stats.initial_residual[k] = st.init_res;
+            stats.final_residual[k] = st.res;
+        }
+        stats.n_solves = k + 1;
+        if (st.status == 2)
+            return fail(CFG_ERR_PCG, "bidomain PCG aborted: a grid barrier timed out");
+        if (st.status)
+            return fail(CFG_ERR_PCG, "bidomain PCG reached maxIter (%d) at residual %g",
+                        max_iter, st.res);
+        return CFG_OK;
+    }
     if (!bd->chunk[kind]) {
         cudaGraph_t g = nullptr;
         CFG_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
@@ -521,8 +741,11 @@ extern "C" int cfg_bidomain_destroy(cfg_bidomain* bd)
                        &bd->d_vol, &bd->d_centres, &bd->d_vm, &bd->d_vm_old, &bd->d_vm_oldold,
                        &bd->d_iion, &bd->d_src, &bd->d_act, &bd->d_phie, &bd->d_phii,
                        &bd->d_grad, &bd->d_dv, &bd->d_diag, &bd->d_b, &bd->d_r, &bd->d_z,
-                       &bd->d_p, &bd->d_ap, &bd->d_ax, &bd->d_partial})
+                       &bd->d_p, &bd->d_ap, &bd->d_ax, &bd->d_partial, &bd->d_p_alt,
+                       &bd->d_coop_partial})
         dfree(*p);
+    dfree(bd->d_bar);
+    dfree(bd->d_abort);
     dfree(bd->d_col);
     dfree(bd->d_cnt);
     dfree(bd->d_own);
@@ -669,6 +892,7 @@ extern "C" int cfg_bidomain_create(const cfg_bidomain_desc* d, const cfg_mesh_de
     bd->e_tol = d->phie_tol; bd->e_rel = d->phie_rel_tol; bd->e_max = d->phie_max_iter;
     bd->n_outer = d->n_outer;
     bd->outer_tol = d->outer_tol;
+    bd->explicit_alg = d->explicit_algorithm != 0;
     bd->ref = ref;
     bd->ref_value = d->ref_value;
     bd->stim.n_boxes = d->n_boxes;
@@ -709,6 +933,30 @@ extern "C" int cfg_bidomain_create(const cfg_bidomain_desc* d, const cfg_mesh_de
     if (!e) e = dmalloc(&bd->d_ticket, 1);
     if (!e) e = cudaMemset(bd->d_ticket, 0, sizeof(unsigned));
     if (!e) e = cudaMallocHost(reinterpret_cast<void**>(&bd->h_st), sizeof(PcgScalars));
+    // the persistent solve: one block of kCoopBlock per resident slot, at most
+    // one row per thread
+    {
+        int dev = 0, coop = 0, sms = 0, per_sm = 0;
+        if (!e && cudaGetDevice(&dev) == cudaSuccess &&
+            cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) == cudaSuccess &&
+            coop &&
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess &&
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pcg_coop, kCoopBlock, 0) ==
+                cudaSuccess &&
+            per_sm > 0) {
+            const long long want = (n + kCoopBlock - 1) / kCoopBlock;
+            const long long cap = (long long)sms * per_sm;
+            bd->coop_blocks = int(want < cap ? want : cap);
+        }
+        cudaGetLastError();
+    }
+    if (!e && bd->coop_blocks > 0) {
+        e = dmalloc(&bd->d_p_alt, size_t(n));
+        if (!e) e = cudaMemset(bd->d_p_alt, 0, size_t(n) * sizeof(double));
+        if (!e) e = dmalloc(&bd->d_coop_partial, 4 * size_t(bd->coop_blocks));
+        if (!e) e = dmalloc(&bd->d_bar, 1);
+        if (!e) e = dmalloc(&bd->d_abort, 1);
+    }
     if (e) return bail(fail(CFG_ERR_CUDA, "bidomain allocation: %s", cudaGetErrorString(e)));
     std::vector<double> v0(size_t(n), d->vm0), zero(size_t(n), 0.0);
     e = cudaMemcpy(bd->d_vm, v0.data(), size_t(n) * sizeof(double), cudaMemcpyHostToDevice);
@@ -754,6 +1002,41 @@ extern "C" int cfg_bidomain_step(cfg_bidomain* bd, double dt)
     if (int rc = cfg_ionic_solve_device(bd->ion, t0, dt, bd->d_vm, bd->d_iion)) return rc;
     bd->vm_stats = cfg_step_stats{};
     bd->e_stats = cfg_step_stats{};
+    if (bd->explicit_alg) {
+        // BidomainSolver::solveDiffusionExplicit (bidomainSolver.C:183-213)
+        div_gamma_grad(bd, bd->d_vm, bd->d_dv);
+        k_phie_system<<<nb, kBlock, 0, s>>>(bd->op, bd->d_dv, bd->ref, bd->ref_value, bd->d_diag,
+                                            bd->d_b);
+        if (int rc = pcg_solve(bd, 0, bd->e_tol, bd->e_rel, bd->e_max, bd->e_stats))
+            return rc;
+        double cft = 1.0, cft0 = 1.0, cft00 = 0.0;
+        if (bd->backward) {
+            const double dt0 = bd->n_old < 2 ? 1e15 : dt;
+            cft = 1 + dt / (dt + dt0);
+            cft00 = dt * dt / (dt0 * (dt + dt0));
+            cft0 = cft + cft00;
+        }
+        if (bd->n_old < 1) {
+            CFG_CUDA_TRY(cudaMemcpyAsync(bd->d_vm_old, bd->d_vm, bytes, cudaMemcpyDeviceToDevice, s));
+            bd->n_old = 1;
+        }
+        if (bd->backward && bd->n_old < 2) {
+            CFG_CUDA_TRY(cudaMemcpyAsync(bd->d_vm_oldold, bd->d_vm_old, bytes, cudaMemcpyDeviceToDevice, s));
+            bd->n_old = 2;
+        }
+        // fvc::div(Gi & fvc::grad(Vm + phiE)) of the fields before the update
+        k_add<<<nb, kBlock, 0, s>>>(n, bd->d_vm, bd->d_phie, bd->d_phii);
+        div_gamma_grad(bd, bd->d_phii, bd->d_dv);
+        VmArgs va{bd->chicm, 1.0 / dt, cft, cft0, cft00, bd->backward ? 1 : 0};
+        k_vm_explicit<<<nb, kBlock, 0, s>>>(bd->op, va, bd->d_vm_old, bd->d_vm_oldold, bd->d_iion,
+                                            bd->d_src, bd->d_dv, bd->d_vm);
+        k_phii<<<nb, kBlock, 0, s>>>(n, bd->d_vm, bd->d_phie, bd->d_phii);
+        k_activation<<<nb, kBlock, 0, s>>>(n, bd->d_vm, bd->d_vm_old, bd->t - dt, dt, bd->d_calc,
+                                           bd->d_act);
+        CFG_CUDA_TRY(cudaGetLastError());
+        if (int rc = ionic_check_status(bd->ion)) return rc;
+        return CFG_OK;
+    }
     bool converged = false;
     for (int corr = 1; corr <= bd->n_outer && !converged; ++corr) {
         if (corr > 1 && bd->vm_stats.n_solves > 0 &&

@@ -395,10 +395,9 @@ extern "C" int cfg_bidomain_create_from_dict(const char* text, const cfg_mesh_de
     if (!scalar(c, "cm", d.cm)) return fail(CFG_ERR_INVALID, "keyword cm is undefined");
     std::string alg = "implicit";
     word(c, "solutionAlgorithm", alg);
-    if (alg == "explicit")
-        return fail(CFG_ERR_UNSUPPORTED, "the explicit bidomain algorithm is not built");
-    if (alg != "implicit")
+    if (alg != "implicit" && alg != "explicit")
         return fail(CFG_ERR_INVALID, "Unrecognised solution algorithm %s", alg.c_str());
+    d.explicit_algorithm = alg == "explicit";
     std::vector<double> rp = numbers(find(c, "phiERefPoint"));
     if (rp.size() != 3) return fail(CFG_ERR_INVALID, "keyword phiERefPoint is undefined");
     for (int k = 0; k < 3; ++k) d.ref_point[k] = rp[size_t(k)];

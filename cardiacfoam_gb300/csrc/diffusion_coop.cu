@@ -23,8 +23,9 @@
 // in the source.
 //
 // Grid barriers are cooperative-launch safe (all blocks co-resident) and
-// bounded: a block that waits longer than ~1 s sets an abort flag, every
-// block leaves at its next barrier, and the step reports CFG_ERR_PCG.
+// bounded: a block that waits longer than the context's spin limit (~1 s by
+// default) sets an abort flag, every block leaves at its next barrier, and
+// the step reports CFG_ERR_PCG.
 #include <cuda_runtime.h>
 
 #include "diffusion_kernels.cuh"
@@ -35,9 +36,9 @@ namespace cfg {
 namespace {
 
 constexpr int kCoopBlock = 512;
-__device__ __forceinline__ bool grid_barrier(PcgState* st, unsigned& epoch)
+__device__ __forceinline__ bool grid_barrier(PcgState* st, unsigned& epoch, long long spin_limit)
 {
-    return gsync::grid_barrier(&st->bar_count, &st->bar_abort, epoch);
+    return gsync::grid_barrier(&st->bar_count, &st->bar_abort, epoch, spin_limit);
 }
 
 template <int K>
@@ -153,7 +154,7 @@ __global__ void __launch_bounds__(kCoopBlock, 1) k_implicit_coop(DiffusionArgs a
                 __stcg(&grad[size_t(n) + c], g[1]);
                 __stcg(&grad[2 * size_t(n) + c], g[2]);
             }
-            if (!grid_barrier(st, epoch)) { abort_step = true; break; }
+            if (!grid_barrier(st, epoch, a.spin_limit)) { abort_step = true; break; }
         }
         // --- source, A.x, r = b - A.x; sums of x and |r|.  The ddt, ionic
         // and stimulus parts of the source change between correctors only
@@ -202,7 +203,7 @@ __global__ void __launch_bounds__(kCoopBlock, 1) k_implicit_coop(DiffusionArgs a
             }
         }
         block_sums<2>(a.partial, set, s1);
-        if (!grid_barrier(st, epoch)) { abort_step = true; break; }
+        if (!grid_barrier(st, epoch, a.spin_limit)) { abort_step = true; break; }
         double g1[2];
         grid_sums<2>(a.partial, set, g1);
         set ^= 1;
@@ -220,7 +221,7 @@ __global__ void __launch_bounds__(kCoopBlock, 1) k_implicit_coop(DiffusionArgs a
             s2[1] += zc * r[c];
         }
         block_sums<2>(a.partial, set, s2);
-        if (!grid_barrier(st, epoch)) { abort_step = true; break; }
+        if (!grid_barrier(st, epoch, a.spin_limit)) { abort_step = true; break; }
         double g2[2];
         grid_sums<2>(a.partial, set, g2);
         set ^= 1;
@@ -262,7 +263,7 @@ __global__ void __launch_bounds__(kCoopBlock, 1) k_implicit_coop(DiffusionArgs a
                     }
                 }
                 block_sums<1>(a.partial, set, s3);
-                if (!grid_barrier(st, epoch)) { aborted = true; break; }
+                if (!grid_barrier(st, epoch, a.spin_limit)) { aborted = true; break; }
                 double g3[1];
                 grid_sums<1>(a.partial, set, g3);
                 set ^= 1;
@@ -292,7 +293,7 @@ __global__ void __launch_bounds__(kCoopBlock, 1) k_implicit_coop(DiffusionArgs a
                     }
                 }
                 block_sums<2>(a.partial, set, s4);
-                if (!grid_barrier(st, epoch)) { aborted = true; break; }
+                if (!grid_barrier(st, epoch, a.spin_limit)) { aborted = true; break; }
                 double g4[2];
                 grid_sums<2>(a.partial, set, g4);
                 set ^= 1;

@@ -106,6 +106,7 @@ struct DiffusionArgs {
     int use_graph;
     cudaGraphConditionalHandle h_outer, h_inner;
     long long iter_cap;        // PCG iterations per step before the step is aborted
+    long long spin_limit;      // spins a block waits at a grid barrier before it aborts
     // step constants
     double dt, chicm;
     int ddt_backward;

@@ -56,6 +56,7 @@ struct EcgArgs {
     double* partial;      // [gridDim.x][n_el]
     unsigned* ticket;     // this launch's
     double* out;          // [n_el]
+    long long wait_cycles;  // staged form: clock cycles a copy wait may take
 };
 
 __device__ __forceinline__ double warp_sum(double v)
@@ -236,8 +237,10 @@ __global__ void __launch_bounds__(kEcgBlock) k_pseudo_ecg(EcgArgs a)
 // of shared-memory stages with bulk asynchronous copies (cp.async.bulk,
 // completion counted on the stage's mbarrier), keeping up to `stages` tiles
 // in flight while the block consumes the oldest.  Every wait is bounded: a
-// wait that runs out sets *error, the block waits (bounded) for the copies
-// it issued, and its sums become NaN.
+// wait that runs out (after EcgArgs::wait_cycles, by default kWaitCycles)
+// sets *error, the block waits for the copies it issued (bounded by
+// kWaitCycles whatever the launch's limit, so that no copy lands in the
+// shared memory of a block that has left), and its sums become NaN.
 constexpr long long kWaitCycles = 1LL << 31;    // about a second
 
 __device__ __forceinline__ unsigned smem_u32(const void* p)
@@ -265,7 +268,7 @@ __device__ __forceinline__ void bulk_copy(unsigned dst, const void* src, unsigne
         : "memory");
 }
 
-__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity)
+__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity, long long limit)
 {
     const long long t0 = clock64();
     for (;;) {
@@ -278,7 +281,7 @@ __device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity)
             : "r"(bar), "r"(parity)
             : "memory");
         if (ok) return true;
-        if (clock64() - t0 > kWaitCycles) return false;
+        if (clock64() - t0 > limit) return false;
     }
 }
 
@@ -329,7 +332,8 @@ __global__ void __launch_bounds__(kEcgBlock, kStagedPerSm) k_pseudo_ecg_staged(E
     long long k = 0;
     for (long long t = t_begin; t < t_end; ++t, ++k) {
         const int s = int(k % stages);
-        if (!mbar_wait(smem_u32(&full[s]), unsigned((k / stages) & 1))) atomicOr(&failed, 1);
+        if (!mbar_wait(smem_u32(&full[s]), unsigned((k / stages) & 1), a.wait_cycles))
+            atomicOr(&failed, 1);
         __syncthreads();
         if (failed) break;
         const unsigned char* st = stage_mem + (size_t)s * stage_bytes<NE>();
@@ -349,7 +353,8 @@ __global__ void __launch_bounds__(kEcgBlock, kStagedPerSm) k_pseudo_ecg_staged(E
         if (threadIdx.x == 0) {
             // let the copies still in flight land before the block leaves
             for (long long q = k; q < issued; ++q)
-                mbar_wait(smem_u32(&full[int(q % stages)]), unsigned((q / stages) & 1));
+                mbar_wait(smem_u32(&full[int(q % stages)]), unsigned((q / stages) & 1),
+                          kWaitCycles);
             atomicOr(error, 1u);
         }
 #pragma unroll
@@ -453,6 +458,7 @@ struct cfg_pseudo_ecg {
     std::vector<double> times;
     cudaStream_t last_stream = nullptr;   // stream of the last launch
     bool launched = false;
+    long long wait_cycles = kWaitCycles;   // limit of the staged form's copy waits
 };
 
 using namespace cfg;
@@ -516,7 +522,7 @@ int launch(cfg_pseudo_ecg* ecg, const double* vm, cudaStream_t s, double* out)
     const bool staged = (reinterpret_cast<uintptr_t>(vm) & 15) == 0;
     for (int e0 = 0, k = 0; e0 < ecg->n_el; e0 += kEcgChunk, ++k) {
         EcgArgs a{ecg->d_lead, ecg->d_scale, vm, ecg->n, ecg->ld, ecg->n_el, e0,
-                  ecg->d_partial, ecg->d_ticket + k, out};
+                  ecg->d_partial, ecg->d_ticket + k, out, ecg->wait_cycles};
         const int blocks = staged ? ecg->staged_blocks[size_t(k)] : ecg->blocks[size_t(k)];
         CFG_CUDA_TRY(launch_any(a, std::min(kEcgChunk, ecg->n_el - e0), staged, ecg->pair,
                                 blocks, ecg->d_error, s));
@@ -729,6 +735,13 @@ extern "C" int cfg_pseudo_ecg_series(cfg_pseudo_ecg* ecg, double* times, double*
         CFG_CUDA_TRY(cudaMemcpy(values, ecg->d_series, size_t(k) * size_t(ecg->n_el) * sizeof(double),
                                 cudaMemcpyDeviceToHost));
     if (times) std::memcpy(times, ecg->times.data(), size_t(k) * sizeof(double));
+    return CFG_OK;
+}
+
+extern "C" int cfg_pseudo_ecg_set_wait_limit(cfg_pseudo_ecg* ecg, long long cycles)
+{
+    if (!ecg) return fail(CFG_ERR_INVALID, "null argument");
+    ecg->wait_cycles = cycles < 0 ? kWaitCycles : cycles;
     return CFG_OK;
 }
 

@@ -1,8 +1,9 @@
 // Grid-wide synchronisation and deterministic reductions for persistent
 // cooperative kernels (every block resident).  A barrier counts arrivals on a
 // monotonic counter that the caller resets before the launch, and its spin
-// is bounded: a block that waits longer than about a second sets an abort
-// flag and every block leaves at its next barrier.
+// is bounded: a block that waits longer than the spin limit (by default
+// about a second) sets an abort flag and every block leaves at its next
+// barrier.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -28,8 +29,10 @@ __device__ __forceinline__ int ld_relaxed_int(const int* p)
 
 // Each block adds one arrival and waits until all gridDim.x arrivals of this
 // barrier are in; `epoch` counts the arrivals expected so far.  Returns false
-// when the launch was aborted (some block waited too long).
-__device__ __forceinline__ bool grid_barrier(unsigned* count, int* abort, unsigned& epoch)
+// when the launch was aborted (some block waited more than `spin_limit`
+// spins).
+__device__ __forceinline__ bool grid_barrier(unsigned* count, int* abort, unsigned& epoch,
+                                             long long spin_limit = kSpinLimit)
 {
     __shared__ int ok;
     epoch += gridDim.x;
@@ -41,7 +44,7 @@ __device__ __forceinline__ bool grid_barrier(unsigned* count, int* abort, unsign
         long long spins = 0;
         while (ld_acquire(count) < epoch) {
             if (ld_relaxed_int(abort)) { good = 0; break; }
-            if (++spins > kSpinLimit) {
+            if (++spins > spin_limit) {
                 atomicExch(abort, 1);
                 good = 0;
                 break;

@@ -187,13 +187,26 @@ constexpr double kFp32NoiseUlps = 64.0;
 
 // One right-hand-side evaluation.  Not inlined: the stage loop and the final
 // current evaluation share one copy of the (large) model body, which keeps
-// the kernel's instruction footprint to a single model instance.
+// the kernel's instruction footprint to a single model instance.  In tissue
+// mode (SV false) the model's membrane-potential-only values come from H,
+// evaluated once per cell and PDE step by M::hoist_vm.
 template <class M, bool SV, class R, class KS>
-__device__ __noinline__ R rhs_eval(double t, const R* y, const KS* K, R* dydt, int tissue,
-                                   const CfgStimulus* st)
+__device__ __noinline__ R rhs_eval(double t, const R* y, const KS* K, const R* H, R* dydt,
+                                   int tissue, const CfgStimulus* st)
 {
-    return M::template rates<R, SV>(t, ArrayView<R>{y}, *K, dydt, tissue, *st);
+    if constexpr (!SV && M::NH > 0)
+        return M::template rates_tissue<R>(t, ArrayView<R>{y}, *K, ArrayView<R>{H}, dydt, tissue,
+                                           *st);
+    else
+        return M::template rates<R, SV>(t, ArrayView<R>{y}, *K, dydt, tissue, *st);
 }
+
+// Storage of the per-cell membrane-potential-only values (at least one
+// element, so that models without any still compile).
+template <class M, class R>
+struct Hoisted {
+    R v[M::NH > 0 ? M::NH : 1];
+};
 
 // Per-cell solver state: y holds every state in double (the plain form) or
 // only the slow (WIDE_MASK) states in double; yf holds every state in the
@@ -215,7 +228,8 @@ CFG_D __forceinline__ long long rkf45_solve(double xs, double xe, CellState<M, R
                                             double& dx_try, R (*k)[M::NS], const KS& K,
                                             int tissue, const CfgStimulus& st,
                                             const OdeSettings& s, unsigned& evals,
-                                            IonicFailure* why = nullptr)
+                                            IonicFailure* why = nullptr,
+                                            const R* H = nullptr)
 {
     using namespace rkf;
     constexpr int NS = M::NS;
@@ -264,7 +278,7 @@ CFG_D __forceinline__ long long rkf45_solve(double xs, double xe, CellState<M, R
                         else yt[i] = yf[i] + h * acc;
                     }
                 }
-                rhs_eval<M, SV, R, KS>(x + kRkfC[sg] * dx, yt, &K, k[sg], tissue, &st);
+                rhs_eval<M, SV, R, KS>(x + kRkfC[sg] * dx, yt, &K, H, k[sg], tissue, &st);
                 evals += 1;
             }
             s0 = 1;
@@ -406,12 +420,14 @@ __global__ void __launch_bounds__(128, CFG_IONIC_MIN_BLOCKS) ionic_step_kernel(I
         long long nsub;
         R iion;
         int tissue = TISSUE;
+        Hoisted<M, R> H;
         if constexpr (TISSUE > 0) {
             const ConstFold<R, M, TISSUE> K{};
+            if constexpr (!SV) M::template hoist_vm<R>(cs.yf[0], K, TISSUE, H.v);
             nsub = rkf45_solve<M, SV, R>(ts, te, cs, step, k, K, TISSUE, p.stim, p.ode, evals,
-                                         &why);
+                                         &why, H.v);
             // computeVariables at tEnd: the rates body computes the same Iion
-            iion = rhs_eval<M, SV, R, ConstFold<R, M, TISSUE>>(te, cs.yf, &K, k[0], TISSUE,
+            iion = rhs_eval<M, SV, R, ConstFold<R, M, TISSUE>>(te, cs.yf, &K, H.v, k[0], TISSUE,
                                                                &p.stim);
         } else {
             tissue = p.tissue_cell ? int(p.tissue_cell[c]) : p.tissue;
@@ -426,9 +442,10 @@ __global__ void __launch_bounds__(128, CFG_IONIC_MIN_BLOCKS) ionic_step_kernel(I
             }
             M::init(C, yinit, tissue, scp);
             const ConstView<R> K{C};
+            if constexpr (!SV) M::template hoist_vm<R>(cs.yf[0], K, tissue, H.v);
             nsub = rkf45_solve<M, SV, R>(ts, te, cs, step, k, K, tissue, p.stim, p.ode, evals,
-                                         &why);
-            iion = rhs_eval<M, SV, R, ConstView<R>>(te, cs.yf, &K, k[0], tissue, &p.stim);
+                                         &why, H.v);
+            iion = rhs_eval<M, SV, R, ConstView<R>>(te, cs.yf, &K, H.v, k[0], tissue, &p.stim);
         }
         (void)tissue;
         evals += 1;

@@ -192,7 +192,8 @@ CFG_D __forceinline__ long long solve(double xs, double xe, float D, float (&Y)[
                                       float (&LO)[Slice<M>::NWA],
                                       float& dx_try, const KS& Kc, int tissue,
                                       const CfgStimulus& st, const OdeSettings& s,
-                                      unsigned& evals, IonicFailure& why, float& iion)
+                                      unsigned& evals, IonicFailure& why, float& iion,
+                                      const float* H = nullptr)
 {
     constexpr int NS = M::NS, P = Slice<M>::NSP;
     const float abs_tol = float(s.abs_tol), rel_tol = float(s.rel_tol);
@@ -254,7 +255,12 @@ CFG_D __forceinline__ long long solve(double xs, double xe, float D, float (&Y)[
         const float* in = out;
         double t = 0.0;
         if constexpr (SV) t = sg == 6 ? xe : xs + double(u) + double(stage_c(sg) * h);
-        const float r = M::template rates<float, SV>(t, ArrayView<float>{in}, Kc, out, tissue, st);
+        float r;
+        if constexpr (!SV && M::NH > 0)
+            r = M::template rates_tissue<float>(t, ArrayView<float>{in}, Kc, ArrayView<float>{H},
+                                                out, tissue, st);
+        else
+            r = M::template rates<float, SV>(t, ArrayView<float>{in}, Kc, out, tissue, st);
         if constexpr (!SV) out[0] = 0.0f;
         ++evals;
         if (sg == 6) {
@@ -388,10 +394,13 @@ ionic_mixed_kernel(IonicLaunch p)
         IonicFailure why;
         long long nsub;
         float iion = 0.0f;
+        // tissue mode: the membrane-potential-only values, once per cell and step
+        Hoisted<M, float> H;
         if constexpr (TISSUE > 0) {
             const ConstFold<float, M, TISSUE> Kc{};
+            if constexpr (!SV) M::template hoist_vm<float>(Y[0], Kc, TISSUE, H.v);
             nsub = mixed::solve<M, SV>(ts, te, float(dtm), Y, K, LO, dx_try, Kc, TISSUE, p.stim,
-                                       p.ode, evals, why, iion);
+                                       p.ode, evals, why, iion, H.v);
         } else {
             const int tissue = p.tissue_cell ? int(p.tissue_cell[c]) : p.tissue;
             double C[M::NC] = {};   // the reference zero-fills CONSTANTS
@@ -405,8 +414,9 @@ ionic_mixed_kernel(IonicLaunch p)
             }
             M::init(C, yinit, tissue, scp);
             const ConstView<float> Kc{C};
+            if constexpr (!SV) M::template hoist_vm<float>(Y[0], Kc, tissue, H.v);
             nsub = mixed::solve<M, SV>(ts, te, float(dtm), Y, K, LO, dx_try, Kc, tissue, p.stim,
-                                       p.ode, evals, why, iion);
+                                       p.ode, evals, why, iion, H.v);
         }
         if (nsub < 0) {
             const int prev = atomicOr(p.status, CFG_ERR_ODE_STEPS);

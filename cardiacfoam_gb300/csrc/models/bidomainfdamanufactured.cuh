@@ -128,6 +128,25 @@ __device__ __forceinline__ R rhs(double t, const YS& Y, const KS& K, R* dydt, in
     return a_BidomainIion;
 }
 
+// Tissue mode (solveVmWithinODESolver false): the PDE owns the membrane
+// potential, so state 0 is the same at every RKF45 stage of a PDE step and
+// the algebraics computed from it and constants alone are too.  hoist()
+// evaluates the ones the rest of the body reads, once per cell and step,
+// into H[NH]; rhs_tissue() is the body without them, reading H(H_x) (the
+// same expressions in the same order: bitwise the values of rhs()).
+constexpr int NH = 0;
+template <class R, class KS>
+__device__ __forceinline__ void hoist(R y_BidomainV, const KS& K, int tissue, R* H)
+{
+    (void)tissue; (void)K; (void)H; (void)y_BidomainV;
+}
+template <class R, class YS, class KS, class HS>
+__device__ __forceinline__ R rhs_tissue(double t, const YS& Y, const KS& K, const HS& H, R* dydt, int tissue, const CfgStimulus& stim)
+{
+    (void)H;
+    return rhs<R, false>(t, Y, K, dydt, tissue, stim);
+}
+
 // Ionic current after the step (computeVariables at tEnd).
 template <class R, bool SOLVE_VM, class YS, class KS>
 __device__ __forceinline__ R iion(double t, const YS& Y, const KS& K, int tissue, const CfgStimulus& stim)
@@ -183,6 +202,11 @@ struct Model {
     CFG_HD static __forceinline__ void init(double* C, double* y, int tissue, const double* scale) { init_consts(C, y, tissue, scale); }
     template <int T> CFG_HD static constexpr double constant(int i) { return cval<T>(i); }
     static constexpr int NSD = bidomainfdamanufactured::NSD, CA_STATE = bidomainfdamanufactured::CA_STATE;
+    static constexpr int NH = bidomainfdamanufactured::NH;
+    template <class R, class KS>
+    __device__ static __forceinline__ void hoist_vm(R v, const KS& K, int tissue, R* H) { hoist<R>(v, K, tissue, H); }
+    template <class R, class YS, class KS, class HS>
+    __device__ static __forceinline__ R rates_tissue(double t, const YS& Y, const KS& K, const HS& H, R* dydt, int tissue, const CfgStimulus& st) { return rhs_tissue<R>(t, Y, K, H, dydt, tissue, st); }
     CFG_HD static constexpr int sd_slot(int i) { return bidomainfdamanufactured::sd_slot(i); }
     static constexpr int NA = bidomainfdamanufactured::NA;
     template <class R, bool SV, class YS, class KS>

@@ -231,6 +231,55 @@ __device__ __forceinline__ R rhs(double t, const YS& Y, const KS& K, R* dydt, in
     return a_Jion;
 }
 
+// Tissue mode (solveVmWithinODESolver false): the PDE owns the membrane
+// potential, so state 0 is the same at every RKF45 stage of a PDE step and
+// the algebraics computed from it and constants alone are too.  hoist()
+// evaluates the ones the rest of the body reads, once per cell and step,
+// into H[NH]; rhs_tissue() is the body without them, reading H(H_x) (the
+// same expressions in the same order: bitwise the values of rhs()).
+constexpr int NH = 6;
+enum Hoisted { H_Jso, H_vInfty, H_tauVMinus, H_wInfty, H_tauWMinus, H_tauS };
+template <class R, class KS>
+__device__ __forceinline__ void hoist(R y_u, const KS& K, int tissue, R* H)
+{
+    (void)tissue; (void)K; (void)H; (void)y_u;
+    R a_tauSo = (K(C_tauSo1) + (((K(C_tauSo2) - K(C_tauSo1)) * (R(1.0) + cfg_tanh((K(C_kSo) * (y_u - K(C_uSo)))))) / R(2.0)));
+    R a_tauO = (((R(1.0) - (((y_u - K(C_thetaO))) > R(0) ? 1 : 0)) * K(C_tauO1)) + ((((y_u - K(C_thetaO))) > R(0) ? 1 : 0) * K(C_tauO2)));
+    R a_Jso = ((((y_u - K(C_uO)) * (R(1.0) - (((y_u - K(C_thetaW))) > R(0) ? 1 : 0))) / a_tauO) + ((((y_u - K(C_thetaW))) > R(0) ? 1 : 0) / a_tauSo));
+    R a_tauVMinus = (((R(1.0) - (((y_u - K(C_thetaVMinus))) > R(0) ? 1 : 0)) * K(C_tauV1Minus)) + ((((y_u - K(C_thetaVMinus))) > R(0) ? 1 : 0) * K(C_tauV2Minus)));
+    R a_tauWMinus = (K(C_tauW1Minus) + (((K(C_tauW2Minus) - K(C_tauW1Minus)) * (R(1.0) + cfg_tanh((K(C_kWMinus) * (y_u - K(C_uWMinus)))))) / R(2.0)));
+    R a_tauS = (((R(1.0) - (((y_u - K(C_thetaW))) > R(0) ? 1 : 0)) * K(C_tauS1)) + ((((y_u - K(C_thetaW))) > R(0) ? 1 : 0) * K(C_tauS2)));
+    R a_vInfty = (((K(C_thetaVMinus) - y_u)) > R(0) ? 1 : 0);
+    R a_wInfty = (((R(1.0) - (((y_u - K(C_thetaO))) > R(0) ? 1 : 0)) * (R(1.0) - (y_u / K(C_tauWInfty)))) + ((((y_u - K(C_thetaO))) > R(0) ? 1 : 0) * K(C_wInftyStar)));
+    H[H_Jso] = a_Jso;
+    H[H_vInfty] = a_vInfty;
+    H[H_tauVMinus] = a_tauVMinus;
+    H[H_wInfty] = a_wInfty;
+    H[H_tauWMinus] = a_tauWMinus;
+    H[H_tauS] = a_tauS;
+}
+template <class R, class YS, class KS, class HS>
+__device__ __forceinline__ R rhs_tissue(double t, const YS& Y, const KS& K, const HS& H, R* dydt, int tissue, const CfgStimulus& stim)
+{
+    constexpr bool SOLVE_VM = false;
+    (void)tissue; (void)stim; (void)t; (void)H;
+    const R y_u = Y(S_u);
+    const R y_v = Y(S_v);
+    const R y_w = Y(S_w);
+    const R y_s = Y(S_s);
+    R a_Jfi = (((((-y_v) * (((y_u - K(C_thetaV))) > R(0) ? 1 : 0)) * (y_u - K(C_thetaV))) * (K(C_uU) - y_u)) / K(C_tauFi));
+    R a_Jsi = ((((-(((y_u - K(C_thetaW))) > R(0) ? 1 : 0)) * y_w) * y_s) / K(C_tauSi));
+    R a_Jion = ((a_Jfi + H(H_Jso)) + a_Jsi);
+    dydt[S_v] = ((((R(1.0) - (((y_u - K(C_thetaV))) > R(0) ? 1 : 0)) * (H(H_vInfty) - y_v)) / H(H_tauVMinus)) - (((((y_u - K(C_thetaV))) > R(0) ? 1 : 0) * y_v) / K(C_tauVPlus)));
+    dydt[S_w] = ((((R(1.0) - (((y_u - K(C_thetaW))) > R(0) ? 1 : 0)) * (H(H_wInfty) - y_w)) / H(H_tauWMinus)) - (((((y_u - K(C_thetaW))) > R(0) ? 1 : 0) * y_w) / K(C_tauWPlus)));
+    dydt[S_s] = ((((R(1.0) + cfg_tanh((K(C_kS) * (y_u - K(C_uS))))) / R(2.0)) - y_s) / H(H_tauS));
+    R a_Istim = (SOLVE_VM ? R(cfg_stimulus_current<double>(t, stim)) : R(0));
+    if (SOLVE_VM) {
+        dydt[S_u] = ((-a_Jion) - a_Istim);
+    }
+    return a_Jion;
+}
+
 // Ionic current after the step (computeVariables at tEnd).
 template <class R, bool SOLVE_VM, class YS, class KS>
 __device__ __forceinline__ R iion(double t, const YS& Y, const KS& K, int tissue, const CfgStimulus& stim)
@@ -323,6 +372,11 @@ struct Model {
     CFG_HD static __forceinline__ void init(double* C, double* y, int tissue, const double* scale) { init_consts(C, y, tissue, scale); }
     template <int T> CFG_HD static constexpr double constant(int i) { return cval<T>(i); }
     static constexpr int NSD = buenoorovio::NSD, CA_STATE = buenoorovio::CA_STATE;
+    static constexpr int NH = buenoorovio::NH;
+    template <class R, class KS>
+    __device__ static __forceinline__ void hoist_vm(R v, const KS& K, int tissue, R* H) { hoist<R>(v, K, tissue, H); }
+    template <class R, class YS, class KS, class HS>
+    __device__ static __forceinline__ R rates_tissue(double t, const YS& Y, const KS& K, const HS& H, R* dydt, int tissue, const CfgStimulus& st) { return rhs_tissue<R>(t, Y, K, H, dydt, tissue, st); }
     CFG_HD static constexpr int sd_slot(int i) { return buenoorovio::sd_slot(i); }
     static constexpr int NA = buenoorovio::NA;
     template <class R, bool SV, class YS, class KS>

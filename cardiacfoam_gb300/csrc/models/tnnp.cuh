@@ -403,6 +403,154 @@ __device__ __forceinline__ R rhs(double t, const YS& Y, const KS& K, R* dydt, in
     return a_Iion_cm;
 }
 
+// Tissue mode (solveVmWithinODESolver false): the PDE owns the membrane
+// potential, so state 0 is the same at every RKF45 stage of a PDE step and
+// the algebraics computed from it and constants alone are too.  hoist()
+// evaluates the ones the rest of the body reads, once per cell and step,
+// into H[NH]; rhs_tissue() is the body without them, reading H(H_x) (the
+// same expressions in the same order: bitwise the values of rhs()).
+constexpr int NH = 20;
+enum Hoisted { H_m_inf, H_tau_m, H_h_inf, H_tau_h, H_j_inf, H_tau_j, H_d_inf, H_tau_d, H_f_inf, H_tau_f, H_s_inf, H_tau_s, H_r_inf, H_tau_r, H_xr1_inf, H_tau_xr1, H_xr2_inf, H_tau_xr2, H_xs_inf, H_tau_xs };
+template <class R, class KS>
+__device__ __forceinline__ void hoist(R y_V, const KS& K, int tissue, R* H)
+{
+    (void)tissue; (void)K; (void)H; (void)y_V;
+    R a_m_inf = (R(1.00000) / cfg_ipow<2>((R(1.00000) + cfg_exp((((-R(56.8600)) - y_V) / R(9.03000))))));
+    R a_alpha_m = (R(1.00000) / (R(1.00000) + cfg_exp((((-R(60.0000)) - y_V) / R(5.00000)))));
+    R a_beta_m = ((R(0.100000) / (R(1.00000) + cfg_exp(((y_V + R(35.0000)) / R(5.00000))))) + (R(0.100000) / (R(1.00000) + cfg_exp(((y_V - R(50.0000)) / R(200.000))))));
+    R a_tau_m = ((R(1.00000) * a_alpha_m) * a_beta_m);
+    R a_h_inf = (R(1.00000) / cfg_ipow<2>((R(1.00000) + cfg_exp(((y_V + R(71.5500)) / R(7.43000))))));
+    R a_alpha_h = ((y_V < (-R(40.0000))) ? (R(0.0570000) * cfg_exp(((-(y_V + R(80.0000))) / R(6.80000)))) : R(0.00000));
+    R a_beta_h = ((y_V < (-R(40.0000))) ? ((R(2.70000) * cfg_exp((R(0.0790000) * y_V))) + (R(310000.) * cfg_exp((R(0.348500) * y_V)))) : (R(0.770000) / (R(0.130000) * (R(1.00000) + cfg_exp(((y_V + R(10.6600)) / (-R(11.1000))))))));
+    R a_tau_h = (R(1.00000) / (a_alpha_h + a_beta_h));
+    R a_j_inf = (R(1.00000) / cfg_ipow<2>((R(1.00000) + cfg_exp(((y_V + R(71.5500)) / R(7.43000))))));
+    R a_alpha_j = ((y_V < (-R(40.0000))) ? ((((((-R(25428.0)) * cfg_exp((R(0.244400) * y_V))) - (R(6.94800e-06) * cfg_exp(((-R(0.0439100)) * y_V)))) * (y_V + R(37.7800))) / R(1.00000)) / (R(1.00000) + cfg_exp((R(0.311000) * (y_V + R(79.2300)))))) : R(0.00000));
+    R a_beta_j = ((y_V < (-R(40.0000))) ? ((R(0.0242400) * cfg_exp(((-R(0.0105200)) * y_V))) / (R(1.00000) + cfg_exp(((-R(0.137800)) * (y_V + R(40.1400)))))) : ((R(0.600000) * cfg_exp((R(0.0570000) * y_V))) / (R(1.00000) + cfg_exp(((-R(0.100000)) * (y_V + R(32.0000)))))));
+    R a_tau_j = (R(1.00000) / (a_alpha_j + a_beta_j));
+    R a_d_inf = (R(1.00000) / (R(1.00000) + cfg_exp((((-R(5.00000)) - y_V) / R(7.50000)))));
+    R a_alpha_d = ((R(1.40000) / (R(1.00000) + cfg_exp((((-R(35.0000)) - y_V) / R(13.0000))))) + R(0.250000));
+    R a_gama_fCa = (R(1.40000) / (R(1.00000) + cfg_exp(((y_V + R(5.00000)) / R(5.00000)))));
+    R a_gamma_d = (R(1.00000) / (R(1.00000) + cfg_exp(((R(50.0000) - y_V) / R(20.0000)))));
+    R a_tau_d = (((R(1.00000) * a_alpha_d) * a_gama_fCa) + a_gamma_d);
+    R a_f_inf = (R(1.00000) / (R(1.00000) + cfg_exp(((y_V + R(20.0000)) / R(7.00000)))));
+    R a_tau_f = (((R(1125.00) * cfg_exp(((-cfg_ipow<2>((y_V + R(27.0000)))) / R(240.000)))) + R(80.0000)) + (R(165.000) / (R(1.00000) + cfg_exp(((R(25.0000) - y_V) / R(10.0000))))));
+    R a_s_inf = ((tissue == 1) ? (R(1.00000) / (R(1.00000) + cfg_exp(((y_V + R(20.0000)) / R(5.00000))))) : (R(1.10000) / (R(1.00000) + cfg_exp(((y_V + R(28.0000)) / R(6.00000))))));
+    R a_tau_s = ((tissue == 1) ? (((R(85.0000) * cfg_exp(((-cfg_ipow<2>((y_V + R(45.0000)))) / R(320.000)))) + (R(5.00000) / (R(1.00000) + cfg_exp(((y_V - R(20.0000)) / R(5.00000)))))) + R(3.00000)) : ((R(1000.0000) * cfg_exp(((-cfg_ipow<2>((y_V + R(67.0000)))) / R(1000.000)))) + R(8.00000)));
+    R a_r_inf = (R(1.00000) / (R(1.00000) + cfg_exp(((R(20.0000) - y_V) / R(6.00000)))));
+    R a_tau_r = ((R(9.50000) * cfg_exp(((-cfg_ipow<2>((y_V + R(40.0000)))) / R(1800.00)))) + R(0.800000));
+    R a_xr1_inf = (R(1.00000) / (R(1.00000) + cfg_exp((((-R(26.0000)) - y_V) / R(7.00000)))));
+    R a_alpha_xr1 = (R(450.000) / (R(1.00000) + cfg_exp((((-R(45.0000)) - y_V) / R(10.0000)))));
+    R a_beta_xr1 = (R(6.00000) / (R(1.00000) + cfg_exp(((y_V + R(30.0000)) / R(11.5000)))));
+    R a_tau_xr1 = ((R(1.00000) * a_alpha_xr1) * a_beta_xr1);
+    R a_xr2_inf = (R(1.00000) / (R(1.00000) + cfg_exp(((y_V + R(88.0000)) / R(24.0000)))));
+    R a_alpha_xr2 = (R(3.00000) / (R(1.00000) + cfg_exp((((-R(60.0000)) - y_V) / R(20.0000)))));
+    R a_beta_xr2 = (R(1.12000) / (R(1.00000) + cfg_exp(((y_V - R(60.0000)) / R(20.0000)))));
+    R a_tau_xr2 = ((R(1.00000) * a_alpha_xr2) * a_beta_xr2);
+    R a_xs_inf = (R(1.00000) / (R(1.00000) + cfg_exp((((-R(5.00000)) - y_V) / R(14.0000)))));
+    R a_alpha_xs = (R(1100.00) / cfg_sqrt((R(1.00000) + cfg_exp((((-R(10.0000)) - y_V) / R(6.00000))))));
+    R a_beta_xs = (R(1.00000) / (R(1.00000) + cfg_exp(((y_V - R(60.0000)) / R(20.0000)))));
+    R a_tau_xs = ((R(1.00000) * a_alpha_xs) * a_beta_xs);
+    H[H_m_inf] = a_m_inf;
+    H[H_tau_m] = a_tau_m;
+    H[H_h_inf] = a_h_inf;
+    H[H_tau_h] = a_tau_h;
+    H[H_j_inf] = a_j_inf;
+    H[H_tau_j] = a_tau_j;
+    H[H_d_inf] = a_d_inf;
+    H[H_tau_d] = a_tau_d;
+    H[H_f_inf] = a_f_inf;
+    H[H_tau_f] = a_tau_f;
+    H[H_s_inf] = a_s_inf;
+    H[H_tau_s] = a_tau_s;
+    H[H_r_inf] = a_r_inf;
+    H[H_tau_r] = a_tau_r;
+    H[H_xr1_inf] = a_xr1_inf;
+    H[H_tau_xr1] = a_tau_xr1;
+    H[H_xr2_inf] = a_xr2_inf;
+    H[H_tau_xr2] = a_tau_xr2;
+    H[H_xs_inf] = a_xs_inf;
+    H[H_tau_xs] = a_tau_xs;
+}
+template <class R, class YS, class KS, class HS>
+__device__ __forceinline__ R rhs_tissue(double t, const YS& Y, const KS& K, const HS& H, R* dydt, int tissue, const CfgStimulus& stim)
+{
+    constexpr bool SOLVE_VM = false;
+    (void)tissue; (void)stim; (void)t; (void)H;
+    const R y_V = Y(S_V);
+    const R y_K_i = Y(S_K_i);
+    const R y_Na_i = Y(S_Na_i);
+    const R y_Ca_i = Y(S_Ca_i);
+    const R y_Xr1 = Y(S_Xr1);
+    const R y_Xr2 = Y(S_Xr2);
+    const R y_Xs = Y(S_Xs);
+    const R y_m = Y(S_m);
+    const R y_h = Y(S_h);
+    const R y_j = Y(S_j);
+    const R y_d = Y(S_d);
+    const R y_f = Y(S_f);
+    const R y_fCa = Y(S_fCa);
+    const R y_s = Y(S_s);
+    const R y_r = Y(S_r);
+    const R y_Ca_SR = Y(S_Ca_SR);
+    const R y_g = Y(S_g);
+    dydt[S_m] = ((H(H_m_inf) - y_m) / H(H_tau_m));
+    dydt[S_h] = ((H(H_h_inf) - y_h) / H(H_tau_h));
+    dydt[S_j] = ((H(H_j_inf) - y_j) / H(H_tau_j));
+    dydt[S_d] = ((H(H_d_inf) - y_d) / H(H_tau_d));
+    dydt[S_f] = ((H(H_f_inf) - y_f) / H(H_tau_f));
+    R a_alpha_fCa = (R(1.00000) / (R(1.00000) + cfg_ipow<8>((y_Ca_i / R(0.000325000)))));
+    R a_beta_fCa = (R(0.100000) / (R(1.00000) + cfg_exp(((y_Ca_i - R(0.000500000)) / R(0.000100000)))));
+    R a_beta_d = (R(0.200000) / (R(1.00000) + cfg_exp(((y_Ca_i - R(0.000750000)) / R(0.000800000)))));
+    R a_fCa_inf = ((((a_alpha_fCa + a_beta_fCa) + a_beta_d) + R(0.230000)) / R(1.46000));
+    R a_d_fCa = ((a_fCa_inf - y_fCa) / K(C_tau_fCa));
+    dydt[S_fCa] = (((a_fCa_inf > y_fCa) && (y_V > (-R(60.0000)))) ? R(0.00000) : a_d_fCa);
+    dydt[S_s] = ((H(H_s_inf) - y_s) / H(H_tau_s));
+    dydt[S_r] = ((H(H_r_inf) - y_r) / H(H_tau_r));
+    dydt[S_Xr1] = ((H(H_xr1_inf) - y_Xr1) / H(H_tau_xr1));
+    dydt[S_Xr2] = ((H(H_xr2_inf) - y_Xr2) / H(H_tau_xr2));
+    dydt[S_Xs] = ((H(H_xs_inf) - y_Xs) / H(H_tau_xs));
+    R a_g_inf = ((y_Ca_i < R(0.000350000)) ? (R(1.00000) / (R(1.00000) + cfg_ipow<6>((y_Ca_i / R(0.000350000))))) : (R(1.00000) / (R(1.00000) + cfg_ipow<16>((y_Ca_i / R(0.000350000))))));
+    R a_d_g = ((a_g_inf - y_g) / K(C_tau_g));
+    dydt[S_g] = (((a_g_inf > y_g) && (y_V > (-R(60.0000)))) ? R(0.00000) : a_d_g);
+    R a_i_NaK = (((((K(C_P_NaK) * K(C_K_o)) / (K(C_K_o) + K(C_K_mk))) * y_Na_i) / (y_Na_i + K(C_K_mNa))) / ((R(1.00000) + (R(0.124500) * cfg_exp(((((-R(0.100000)) * y_V) * K(C_F)) / (K(C_R) * K(C_T)))))) + (R(0.0353000) * cfg_exp((((-y_V) * K(C_F)) / (K(C_R) * K(C_T)))))));
+    R a_E_Na = (((K(C_R) * K(C_T)) / K(C_F)) * cfg_log((K(C_Na_o) / y_Na_i)));
+    R a_i_Na = ((((K(C_g_Na) * cfg_ipow<3>(y_m)) * y_h) * y_j) * (y_V - a_E_Na));
+    R a_i_b_Na = (K(C_g_bNa) * (y_V - a_E_Na));
+    R a_i_NaCa = ((K(C_K_NaCa) * (((cfg_exp((((K(C_gamma_NCX) * y_V) * K(C_F)) / (K(C_R) * K(C_T)))) * cfg_ipow<3>(y_Na_i)) * K(C_Ca_o)) - (((cfg_exp(((((K(C_gamma_NCX) - R(1.00000)) * y_V) * K(C_F)) / (K(C_R) * K(C_T)))) * cfg_ipow<3>(K(C_Na_o))) * y_Ca_i) * K(C_alpha_NCX)))) / (((cfg_ipow<3>(K(C_Km_Nai)) + cfg_ipow<3>(K(C_Na_o))) * (K(C_Km_Ca) + K(C_Ca_o))) * (R(1.00000) + (K(C_K_sat) * cfg_exp(((((K(C_gamma_NCX) - R(1.00000)) * y_V) * K(C_F)) / (K(C_R) * K(C_T))))))));
+    dydt[S_Na_i] = (((-(((a_i_Na + a_i_b_Na) + (R(3.00000) * a_i_NaK)) + (R(3.00000) * a_i_NaCa))) * K(C_Cm)) / (K(C_V_c) * K(C_F)));
+    R a_E_K = (((K(C_R) * K(C_T)) / K(C_F)) * cfg_log((K(C_K_o) / y_K_i)));
+    R a_alpha_K1 = (R(0.100000) / (R(1.00000) + cfg_exp((R(0.0600000) * ((y_V - a_E_K) - R(200.000))))));
+    R a_beta_K1 = (((R(3.00000) * cfg_exp((R(0.000200000) * ((y_V - a_E_K) + R(100.000))))) + (R(1.00000) * cfg_exp((R(0.100000) * ((y_V - a_E_K) - R(10.0000)))))) / (R(1.00000) + cfg_exp(((-R(0.500000)) * (y_V - a_E_K)))));
+    R a_xK1_inf = (a_alpha_K1 / (a_alpha_K1 + a_beta_K1));
+    R a_i_K1 = (((K(C_g_K1) * a_xK1_inf) * cfg_sqrt((K(C_K_o) / R(5.40000)))) * (y_V - a_E_K));
+    R a_i_to = (((K(C_g_to) * y_r) * y_s) * (y_V - a_E_K));
+    R a_i_Kr = ((((K(C_g_Kr) * cfg_sqrt((K(C_K_o) / R(5.40000)))) * y_Xr1) * y_Xr2) * (y_V - a_E_K));
+    R a_E_Ks = (((K(C_R) * K(C_T)) / K(C_F)) * cfg_log(((K(C_K_o) + (K(C_P_kna) * K(C_Na_o))) / (y_K_i + (K(C_P_kna) * y_Na_i)))));
+    R a_i_Ks = ((K(C_g_Ks) * cfg_ipow<2>(y_Xs)) * (y_V - a_E_Ks));
+    R a_i_CaL = (((((((((K(C_g_CaL) * y_d) * y_f) * y_fCa) * R(4.00000)) * y_V) * cfg_ipow<2>(K(C_F))) / (K(C_R) * K(C_T))) * ((y_Ca_i * cfg_exp((((R(2.00000) * y_V) * K(C_F)) / (K(C_R) * K(C_T))))) - (R(0.341000) * K(C_Ca_o)))) / cfg_expm1((((R(2.00000) * y_V) * K(C_F)) / (K(C_R) * K(C_T)))));
+    R a_E_Ca = ((((R(0.500000) * K(C_R)) * K(C_T)) / K(C_F)) * cfg_log((K(C_Ca_o) / y_Ca_i)));
+    R a_i_b_Ca = (K(C_g_bCa) * (y_V - a_E_Ca));
+    R a_i_p_K = ((K(C_g_pK) * (y_V - a_E_K)) / (R(1.00000) + cfg_exp(((R(25.0000) - y_V) / R(5.98000)))));
+    R a_i_p_Ca = ((K(C_g_pCa) * y_Ca_i) / (y_Ca_i + K(C_K_pCa)));
+    R a_Iion_cm = (((((((((((a_i_K1 + a_i_to) + a_i_Kr) + a_i_Ks) + a_i_CaL) + a_i_NaK) + a_i_Na) + a_i_b_Na) + a_i_NaCa) + a_i_b_Ca) + a_i_p_K) + a_i_p_Ca);
+    R a_Istim = (SOLVE_VM ? R(cfg_stimulus_current<double>(t, stim)) : R(0));
+    dydt[S_V] = R(0.0);
+    if (SOLVE_VM) {
+        dydt[S_V] = ((-a_Iion_cm) - a_Istim);
+    }
+    dydt[S_K_i] = (((-((((((a_i_K1 + a_i_to) + a_i_Kr) + a_i_Ks) + a_i_p_K) + a_Istim) - (R(2.00000) * a_i_NaK))) * K(C_Cm)) / (K(C_V_c) * K(C_F)));
+    R a_i_rel = (((((K(C_a_rel) * cfg_ipow<2>(y_Ca_SR)) / (cfg_ipow<2>(K(C_b_rel)) + cfg_ipow<2>(y_Ca_SR))) + K(C_c_rel)) * y_d) * y_g);
+    R a_i_up = (K(C_Vmax_up) / (R(1.00000) + (cfg_ipow<2>(K(C_K_up)) / cfg_ipow<2>(y_Ca_i))));
+    R a_i_leak = (K(C_V_leak) * (y_Ca_SR - y_Ca_i));
+    R a_ddt_Ca_i_total = ((((((-(((a_i_CaL + a_i_b_Ca) + a_i_p_Ca) - (R(2.00000) * a_i_NaCa))) / ((R(2.00000) * K(C_V_c)) * K(C_F))) * K(C_Cm)) + a_i_leak) - a_i_up) + a_i_rel);
+    R a_f_JCa_i_free = (R(1.00000) / (R(1.00000) + ((K(C_Buf_c) * K(C_K_buf_c)) / cfg_ipow<2>((y_Ca_i + K(C_K_buf_c))))));
+    dydt[S_Ca_i] = (a_ddt_Ca_i_total * a_f_JCa_i_free);
+    R a_ddt_Ca_sr_total = ((K(C_V_c) / K(C_V_sr)) * (a_i_up - (a_i_rel + a_i_leak)));
+    R a_f_JCa_sr_free = (R(1.00000) / (R(1.00000) + ((K(C_Buf_sr) * K(C_K_buf_sr)) / cfg_ipow<2>((y_Ca_SR + K(C_K_buf_sr))))));
+    dydt[S_Ca_SR] = (a_ddt_Ca_sr_total * a_f_JCa_sr_free);
+    return a_Iion_cm;
+}
+
 // Ionic current after the step (computeVariables at tEnd).
 template <class R, bool SOLVE_VM, class YS, class KS>
 __device__ __forceinline__ R iion(double t, const YS& Y, const KS& K, int tissue, const CfgStimulus& stim)
@@ -773,6 +921,11 @@ struct Model {
     CFG_HD static __forceinline__ void init(double* C, double* y, int tissue, const double* scale) { init_consts(C, y, tissue, scale); }
     template <int T> CFG_HD static constexpr double constant(int i) { return cval<T>(i); }
     static constexpr int NSD = tnnp::NSD, CA_STATE = tnnp::CA_STATE;
+    static constexpr int NH = tnnp::NH;
+    template <class R, class KS>
+    __device__ static __forceinline__ void hoist_vm(R v, const KS& K, int tissue, R* H) { hoist<R>(v, K, tissue, H); }
+    template <class R, class YS, class KS, class HS>
+    __device__ static __forceinline__ R rates_tissue(double t, const YS& Y, const KS& K, const HS& H, R* dydt, int tissue, const CfgStimulus& st) { return rhs_tissue<R>(t, Y, K, H, dydt, tissue, st); }
     CFG_HD static constexpr int sd_slot(int i) { return tnnp::sd_slot(i); }
     static constexpr int NA = tnnp::NA;
     template <class R, bool SV, class YS, class KS>

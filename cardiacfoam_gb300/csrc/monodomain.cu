@@ -302,6 +302,7 @@ static void fill_args(cfg_monodomain* md, double dt)
     a.ddt_backward = md->ddt_backward;
     a.use_graph = 0;
     a.iter_cap = md->iter_cap;
+    a.spin_limit = md->spin_limit;
     // ddt coefficients (EulerDdtScheme; backwardDdtScheme with deltaT0 =
     // GREAT while fewer than two old-time levels exist, then deltaT0 = dt)
     a.rdt = 1.0 / dt;
@@ -641,6 +642,18 @@ int cfg_monodomain_autotune(cfg_monodomain* md, int* block, int* cells_per_threa
                             cells_per_thread, ionic_ms);
     if (rc) return rc;
     // the launch shape is part of the captured step graph
+    if (md->graph_exec) {
+        cudaGraphExecDestroy(md->graph_exec);
+        md->graph_exec = nullptr;
+    }
+    return CFG_OK;
+}
+
+int cfg_monodomain_set_wait_limit(cfg_monodomain* md, long long spins)
+{
+    if (!md) return fail(CFG_ERR_INVALID, "null context");
+    md->spin_limit = spins < 0 ? gsync::kSpinLimit : spins;
+    // the limit is an argument of the kernels captured in the step graph
     if (md->graph_exec) {
         cudaGraphExecDestroy(md->graph_exec);
         md->graph_exec = nullptr;

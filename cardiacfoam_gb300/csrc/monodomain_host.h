@@ -4,6 +4,7 @@
 #include <vector>
 
 #include "diffusion_kernels.cuh"
+#include "grid_sync.cuh"
 #include "host_common.h"
 
 struct cfg_monodomain {
@@ -63,6 +64,7 @@ struct cfg_monodomain {
     int coop_blocks = 0;
     bool graph_persistent = false;
     long long iter_cap = 100000;   // PCG iterations per step before the step aborts
+    long long spin_limit = cfg::gsync::kSpinLimit;   // grid-barrier spins before the step aborts
     double t_host = 0.0;
     long long steps = 0;
     // time step a caller may leave to the context (cfg_monodomain_step with

@@ -25,7 +25,10 @@
 //
 // The first call on a device resolves the array's device address with
 // cudaGetSymbolAddress (with that device current) and caches it; make that
-// first call before any stream capture is begun on the device.
+// first call before any stream capture is begun on the device.  The cached
+// address is that of the device's primary context at the first call: a
+// cudaDeviceReset (or another reset of the primary context) invalidates it,
+// and the entry point is not to be called after one in the same process.
 #include <mutex>
 
 #include "diffusion_kernels.cuh"

@@ -133,7 +133,8 @@ class BidomainDesc(C.Structure):
                 ("ref_value", C.c_double), ("n_boxes", C.c_int),
                 ("box_min", (C.c_double * 3) * 8), ("box_max", (C.c_double * 3) * 8),
                 ("box_start", C.c_double * 8), ("box_duration", C.c_double * 8),
-                ("box_intensity", C.c_double * 8), ("grad_scheme", C.c_int)]
+                ("box_intensity", C.c_double * 8), ("grad_scheme", C.c_int),
+                ("explicit_algorithm", C.c_int)]
 
 
 class PseudoEcgDesc(C.Structure):
@@ -152,7 +153,8 @@ EXPORTS = [
     "cfg_monodomain_last_stats", "cfg_monodomain_set_timing", "cfg_monodomain_timings",
     "cfg_monodomain_stream", "cfg_monodomain_destroy", "cfg_box_diffusion_solve_noalloc",
     "cfg_monodomain_set_persistent", "cfg_monodomain_suggest_explicit_delta_t",
-    "cfg_monodomain_delta_t", "cfg_monodomain_set_delta_t", "cfg_batch_create", "cfg_batch_run", "cfg_batch_results",
+    "cfg_monodomain_delta_t", "cfg_monodomain_set_delta_t", "cfg_monodomain_set_wait_limit",
+    "cfg_pseudo_ecg_set_wait_limit", "cfg_batch_create", "cfg_batch_run", "cfg_batch_results",
     "cfg_batch_trace", "cfg_batch_get_states", "cfg_batch_stats", "cfg_batch_stream",
     "cfg_batch_destroy", "cfg_adjoint_create", "cfg_adjoint_set_target", "cfg_adjoint_forward",
     "cfg_adjoint_backward", "cfg_adjoint_destroy", "cfg_ionic_autotune", "cfg_monodomain_autotune",
@@ -219,6 +221,8 @@ def load(path: Optional[os.PathLike] = None):
     L.cfg_monodomain_suggest_explicit_delta_t.argtypes = [C.c_void_p, C.c_double, _dp]
     L.cfg_monodomain_delta_t.argtypes = [C.c_void_p, _dp]
     L.cfg_monodomain_set_delta_t.argtypes = [C.c_void_p, C.c_double]
+    L.cfg_monodomain_set_wait_limit.argtypes = [C.c_void_p, C.c_longlong]
+    L.cfg_pseudo_ecg_set_wait_limit.argtypes = [C.c_void_p, C.c_longlong]
     L.cfg_batch_create.argtypes = [C.POINTER(BatchDesc), C.POINTER(C.c_void_p)]
     L.cfg_batch_run.argtypes = [C.c_void_p]
     L.cfg_batch_results.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]

@@ -309,6 +309,14 @@ int cfg_monodomain_timings(const cfg_monodomain* md, double* ionic_ms, double* d
  * sums.  MonodomainSolver::solveDiffusionImplicit (monodomainSolver.C:112-150)
  * is what either form computes. */
 int cfg_monodomain_set_persistent(cfg_monodomain* md, int enable);
+/* Bound on each grid-barrier wait of the persistent diffusion kernel, in
+ * spins of at least 32 ns (default 2^25, about a second; a negative value
+ * restores it).  A block that waits longer makes every block leave at its
+ * next barrier and the step returns CFG_ERR_PCG ("a grid barrier timed out");
+ * the context's fields are then those of a partial step.  No counterpart in
+ * the reference (its solver runs on the host); an application sets it to
+ * shorten the watchdog of a step. */
+int cfg_monodomain_set_wait_limit(cfg_monodomain* md, long long spins);
 /* The CUDA stream (cudaStream_t) all work of the context is enqueued on. */
 void* cfg_monodomain_stream(cfg_monodomain* md);
 int cfg_monodomain_destroy(cfg_monodomain* md);
@@ -446,6 +454,11 @@ typedef struct cfg_bidomain_desc {
     double box_min[8][3], box_max[8][3];
     double box_start[8], box_duration[8], box_intensity[8];
     int grad_scheme;                 /* CFG_GRAD_* */
+    int explicit_algorithm;          /* solutionAlgorithm explicit (1): phiE solved as in
+                                        the implicit form, then Vm from
+                                        chi Cm ddt(Vm) == div(Gi grad(Vm + phiE))
+                                        - chi Cm Iion + src with the diagonal ddt matrix
+                                        (bidomainSolver.C:183-213), no PIMPLE loop */
 } cfg_bidomain_desc;
 
 typedef struct cfg_bidomain cfg_bidomain;
@@ -533,6 +546,12 @@ int cfg_pseudo_ecg_record_field(cfg_pseudo_ecg* ecg, const double* vm, void* str
 int cfg_pseudo_ecg_series(cfg_pseudo_ecg* ecg, double* times, double* values,
                           long long max_rows, long long* n_rows);
 int cfg_pseudo_ecg_reset(cfg_pseudo_ecg* ecg);
+/* Bound on each wait of the staged pseudo-ECG kernel for its tile copies, in
+ * clock cycles (default 2^31, about a second; a negative value restores it).
+ * A wait that runs out makes that evaluation's values NaN and the call that
+ * reads them (compute, series) return CFG_ERR_CUDA, after which the flag is
+ * cleared and the object is usable again.  No counterpart in the reference. */
+int cfg_pseudo_ecg_set_wait_limit(cfg_pseudo_ecg* ecg, long long cycles);
 int cfg_pseudo_ecg_destroy(cfg_pseudo_ecg* ecg);
 
 /* Electrodes of an ecgDomains entry of constant/electroProperties
@@ -564,8 +583,12 @@ int cfg_pseudo_ecg_electrodes_from_dict(const char* electro_properties, const ch
  * all are device pointers of nx*ny*nz doubles.  stream is a cudaStream_t
  * (NULL: the legacy default stream); the call returns after the solve
  * finished.  The first call on a device looks up the array's address with
- * that device current: make it before any stream capture on the device.
- * Every call shares the array: calls that overlap on the GPU race. */
+ * that device current and keeps it for the process: make it before any
+ * stream capture on the device.  The address belongs to the device's
+ * primary context as it was at that call; after cudaDeviceReset (or any
+ * reset of the primary context) the entry point must not be called again in
+ * the same process.  Every call shares the array: calls that overlap on the
+ * GPU race. */
 #define CFG_NOALLOC_MAX_CELLS 65536
 #define CFG_NOALLOC_SCRATCH_BYTES 7880704   /* 15 vectors of 64 Ki doubles + state */
 

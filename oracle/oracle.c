@@ -1514,6 +1514,44 @@ int oracle_bidomain_step(oracle_bidomain* B, double dt, int nthreads)
     T->n_solves = 0;
     B->n_solves = 0;
     int total = 0, converged = 0;
+    if (!T->d.implicit) {
+        /* BidomainSolver::solveDiffusionExplicit (bidomainSolver.C:183-213):
+         * the phiE solve, then chi*Cm*ddt(Vm) == fvc::div(Gi & fvc::grad(Vm +
+         * phiE)) - chi*Cm*Iion + src with the diagonal ddt matrix, solved as
+         * source over diagonal */
+        int it = solve_phie(B);
+        if (it < 0) return -1;
+        double cft, cft0, cft00;
+        ddt_coeffs(T, dt, &cft, &cft0, &cft00);
+        if (T->n_old < 1) { memcpy(T->vm_old, T->vm, sizeof(double) * (size_t)T->n); T->n_old = 1; }
+        if (T->d.ddt_backward && T->n_old < 2) {
+            memcpy(T->vm_oldold, T->vm_old, sizeof(double) * (size_t)T->n);
+            T->n_old = 2;
+        }
+        for (long c = 0; c < T->n; c++) B->phii[c] = T->vm[c] + B->phie[c];
+        div_gamma_grad_v(T, B->phii, B->dv, B->ue);
+        const double chicm = T->d.chi * T->d.cm;
+        const double rdt = 1.0 / dt;
+        const double* V = T->mesh->vol;
+        for (long c = 0; c < T->n; c++) {
+            double ddt_diag, ddt_src;
+            if (T->d.ddt_backward) {
+                ddt_diag = (cft * rdt) * V[c];
+                ddt_src = rdt * V[c] * (cft0 * T->vm_old[c] - cft00 * T->vm_oldold[c]);
+            } else {
+                ddt_diag = rdt * V[c];
+                ddt_src = rdt * T->vm_old[c] * V[c];
+            }
+            double bb = chicm * ddt_src;
+            double su = -(chicm * T->iion[c]) * V[c];
+            su = su + T->src[c] * V[c];
+            bb = bb + su;
+            T->vm[c] = (bb + B->dv[c]) / (chicm * ddt_diag);
+        }
+        for (long c = 0; c < T->n; c++) B->phii[c] = T->vm[c] + B->phie[c];
+        update_activation(T, dt);
+        return it;
+    }
     for (int corr = 1; corr <= T->d.n_outer && !converged; corr++) {
         if (corr > 1 && T->init_res[T->n_solves - 1] < T->d.outer_tol) converged = 1;
         int it = solve_phie(B);

@@ -104,7 +104,6 @@ def test_bidomain_dictionary_errors(gpu_lib):
     from cardiacfoam_gb300.mesh import box_mesh, with_box_geometry
     geo = with_box_geometry(box_mesh(4, 2, 1, 1e-3, 5e-4, 2.5e-4), 1e-3, 5e-4, 2.5e-4)
     bad = [(("monodomainSolver",) + GOOD[1:], lib.CFG_ERR_UNSUPPORTED),
-           ((GOOD[0], GOOD[1], "explicit", GOOD[3]), lib.CFG_ERR_UNSUPPORTED),
            ((GOOD[0], GOOD[1], "sideways", GOOD[3]), lib.CFG_ERR_INVALID),
            ((GOOD[0], "(0.62 0 0 0.24)", GOOD[2], GOOD[3]), lib.CFG_ERR_INVALID),
            (GOOD[:3] + ("",), lib.CFG_ERR_INVALID)]

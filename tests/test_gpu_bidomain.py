@@ -165,3 +165,34 @@ def test_from_dict_equals_the_description(gpu_lib):
     assert np.max(a.vm()) > -0.084
     a.close()
     b.close()
+
+
+@pytest.mark.gpu
+def test_explicit_algorithm_matches_oracle(gpu_lib, oracle):
+    """solutionAlgorithm explicit (bidomainSolver.C:183-213): the phiE solve,
+    then Vm from the diagonal ddt matrix with div(Gi grad(Vm + phiE)), on the
+    propagating TNNP slab against the oracle's restatement; and from the
+    dictionary front end."""
+    h, dt = 2.5e-4, 5e-6
+    mesh = with_box_geometry(box_mesh(24, 8, 2, 24 * h, 8 * h, 2 * h), 24 * h, 8 * h, 2 * h)
+    box = [((0.0, 0.0, 0.0), (1.0e-3, 2 * h * 8, 2 * h), 0.0, 1e-3, 1e5)]
+    gi, ge = (0.17, 0.0, 0.0, 0.019, 0.0, 0.019), (0.62, 0.0, 0.0, 0.24, 0.0, 0.24)
+    bd = api.Bidomain(mesh, "TNNP", "epicardialCells", sigma_i=gi, sigma_e=ge, dt=dt,
+                      phie_tol=1e-10, ref_point=(0.0, 0.0, 0.0), boxes=box, implicit=False)
+    d = oracle.tissue_desc("TNNP", 1, gi, implicit=False, precond_dic=False, pcg_tol=1e-10,
+                           pcg_rel_tol=0.0, n_outer=1, outer_tol=0.0, boxes=box)
+    B = oracle.Bidomain(d, ge, oracle.Mesh.general(mesh), (0.0, 0.0, 0.0), 0.0, 1e-10, 0.0, 1000)
+    for _ in range(400):
+        bd.step(dt)
+        B.step(dt)
+        (_, _, it_v), (_, _, it_e) = bd.stats()
+        assert it_v.size == 0 or np.all(it_v == 0)
+        assert np.max(np.abs(it_e - B.phie_solves()[2])) <= 1
+    vg, vo = bd.vm(), B.tissue.vm()
+    assert np.max(np.abs(vg - vo)) <= 1e-9 * np.max(np.abs(vo))
+    assert _close(bd.phie(), B.phie(), 1e-9)
+    assert _close(bd.phii(), B.phii(), 1e-9)
+    ag, ao = bd.activation(), B.tissue.activation()
+    assert np.array_equal(ag > 0, ao > 0) and (ag > 0).sum() > 20
+    assert np.max(np.abs(ag - ao)) < 1e-9
+    bd.close()

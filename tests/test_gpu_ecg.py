@@ -229,4 +229,9 @@ def test_bidomain_source(gpu_lib, oracle):
     t, v = pe.series()
     assert t[0] == bd.time() and np.array_equal(v[0], got)
     pe.close()
+    # lead rows folded with another conductivity than the context's Gi
+    wrong = api.PseudoECG(mesh, el, sigma=ge)
+    with pytest.raises(ValueError):
+        wrong.compute(bd)
+    wrong.close()
     bd.close()

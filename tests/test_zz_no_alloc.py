@@ -105,3 +105,42 @@ def test_noalloc_matches_monodomain_step(gpu_lib, backward):
         assert res.converged == 1
         assert abs(res.iterations - int(iters[0])) <= 1, (res.iterations, iters)
     md.close()
+
+
+@pytest.mark.gpu
+def test_noalloc_leaves_device_memory_unchanged(gpu_lib):
+    """After a first call (which sets up the array's address), further calls
+    change neither the free device memory (cudaMemGetInfo) nor the memory
+    torch has reserved: the entry point allocates nothing."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    mesh = _box()
+    d = _desc(mesh, True)
+    dev = torch.device("cuda", 0)
+    n = mesh.n_cells
+    c = mesh.centres
+    r2 = ((c - c.mean(axis=0)) ** 2).sum(axis=1)
+    v0 = torch.from_numpy(-0.084 + 0.06 * np.exp(-r2 / (2 * (4 * H) ** 2))).to(dev)
+    vo, voo = v0.clone(), v0.clone()
+    ii = torch.zeros(n, dtype=torch.float64, device=dev)
+    vm = v0.clone()
+
+    def call():
+        res = lib.SolveResult()
+        rc = gpu_lib.cfg_box_diffusion_solve_noalloc(
+            C.byref(d), DT, C.c_void_p(vo.data_ptr()), C.c_void_p(voo.data_ptr()),
+            C.c_void_p(ii.data_ptr()), C.c_void_p(vm.data_ptr()), None, C.byref(res))
+        assert rc == lib.CFG_OK, gpu_lib.cfg_last_error().decode()
+        assert res.converged == 1
+
+    call()
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info(dev)
+    reserved0 = torch.cuda.memory_reserved(dev)
+    for _ in range(3):
+        call()
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info(dev)
+    assert free1 == free0
+    assert torch.cuda.memory_reserved(dev) == reserved0
