@@ -770,6 +770,133 @@ def batch_arm(args):
     return out
 
 
+def full_run_arm(args):
+    """The headline slab's whole run: both forms from t = 0 through
+    `--full-run-steps` steps (20,000 x 5 us = 100 ms, the configuration's
+    length), compared at the end over every cell either form activated:
+    activation times, Vm L-inf, flag mismatches; the mixed form's time per
+    step over the whole run."""
+    import torch
+    from cardiacfoam_gb300 import build as gpu_build, lib
+    gpu_build.build()
+    mesh = build_mesh()
+    n = mesh.n_cells
+    steps = args.full_run_steps
+    out = {"workload": WORKLOAD.split("; timed window")[0], "cells": n, "steps": steps,
+           "simulated_ms": steps * DT * 1e3}
+    runs = {}
+    for name, prec in (("mixed", lib.PRECISION_MIXED), ("fp64", lib.PRECISION_FP64)):
+        m = make_model(mesh, prec)
+        s = torch.cuda.ExternalStream(m.stream())
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(s)
+        m.run(DT, steps)
+        e1.record(s)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        runs[name] = (m.activation(), m.vm())
+        out[name] = {"seconds": ms / 1e3, "ms_per_step": ms / steps,
+                     "cell_steps_per_s": n * steps / (ms / 1e3),
+                     "rhs_evaluations_per_cell_step": m.rhs_evaluations() / (n * steps)}
+        m.close()
+    (a64, v64), (amx, vmx) = runs["fp64"], runs["mixed"]
+    both = (a64 > 0) & (amx > 0)
+    c = mesh.centres
+    in_box = np.all((c >= np.array(BOX[0][0])) & (c <= np.array(BOX[0][1])), axis=1)
+    out["accuracy"] = {
+        "activated_fp64": int((a64 > 0).sum()), "activated_mixed": int((amx > 0).sum()),
+        "activated_both": int(both.sum()),
+        "activated_both_outside_stimulus_box": int((both & ~in_box).sum()),
+        "activation_flag_mismatches": int(((a64 > 0) != (amx > 0)).sum()),
+        "activation_error_ms_max": float(np.max(np.abs(a64[both] - amx[both])) * 1e3),
+        "activation_error_ms_p99": float(np.percentile(np.abs(a64[both] - amx[both]), 99) * 1e3),
+        "latest_activation_ms": float(np.max(a64) * 1e3),
+        "vm_linf_error_V": float(np.max(np.abs(v64 - vmx)))}
+    out["speedup_mixed_vs_fp64"] = out["fp64"]["seconds"] / out["mixed"]["seconds"]
+    return out
+
+
+def tissue_apd_arm(args):
+    """APD90 of a tissue run in both forms: ORd myocyte on the slab at
+    h = 0.5 mm (40 x 14 x 6 = 3,360 cells), dt 5 us, corner stimulus, 400 ms
+    (one full beat and its repolarisation), per-cell beat detection on Vm
+    every 0.1 ms (cfg_monodomain_track_apd); mixed against FP64: APD90,
+    activation times and Vm at the end."""
+    from cardiacfoam_gb300 import build as gpu_build, lib, api
+    from cardiacfoam_gb300.mesh import box_mesh
+    gpu_build.build()
+    nx, ny, nz, h = 40, 14, 6, 5e-4
+    mesh = box_mesh(nx, ny, nz, nx * h, ny * h, nz * h)
+    steps, every = args.tissue_apd_steps, 20
+    res = {}
+    for name, prec in (("fp64", lib.PRECISION_FP64), ("mixed", lib.PRECISION_MIXED)):
+        m = api.Monodomain(mesh, "ORd", "myocyte", SIGMA, dt=DT, precision=prec, boxes=BOX,
+                           max_steps=10 ** 6)
+        m.track_apd(every)
+        t0 = time.perf_counter()
+        m.run(DT, steps)
+        nb, apd, tup = m.apd_results()
+        res[name] = {"seconds": time.perf_counter() - t0, "beats": nb, "apd": apd,
+                     "act": m.activation(), "vm": m.vm()}
+        m.close()
+    f, x = res["fp64"], res["mixed"]
+    ok = ~np.isnan(f["apd"]) & ~np.isnan(x["apd"])
+    both = (f["act"] > 0) & (x["act"] > 0)
+    return {"workload": (f"ORd myocyte slab 20x7x3 mm at h 0.5 mm ({mesh.n_cells} cells), dt 5 us, "
+                         f"{steps * DT * 1e3:g} ms, corner stimulus 5e4 A/m^3 x 2 ms; per-cell "
+                         f"APD90 from Vm sampled every {every * DT * 1e3:g} ms"),
+            "fp64_seconds": f["seconds"], "mixed_seconds": x["seconds"],
+            "apd90_cells_compared": int(ok.sum()),
+            "apd90_fp64_range_ms": [float(np.nanmin(f["apd"])), float(np.nanmax(f["apd"]))],
+            "apd90_max_abs_error_ms": float(np.max(np.abs(f["apd"][ok] - x["apd"][ok])))
+            if ok.any() else None,
+            "beat_count_mismatches": int(np.sum(f["beats"] != x["beats"])),
+            "activation_error_ms": float(np.max(np.abs(f["act"][both] - x["act"][both])) * 1e3)
+            if both.any() else None,
+            "activated_cells": int(both.sum()),
+            "vm_linf_error_V": float(np.max(np.abs(f["vm"] - x["vm"])))}
+
+
+def batch_apd_arm(args):
+    """Last-beat APD90 and peak Ca of the batched ToRORd_dynCl population at
+    the configuration's own dt (0.01 ms) over each cell's whole protocol, in
+    both forms, for the `--batch-apd-cells` cells of the 65,536 with the
+    shortest protocols (beats x cycle length): a lone FP64 thread integrates
+    ToRORd_dynCl at GB300's FP64 rate, so the whole population in FP64 would
+    take hours."""
+    from cardiacfoam_gb300 import build as gpu_build, api, lib
+    gpu_build.build()
+    n_all, dt = args.batch_cells, 1e-5
+    stimuli, scales, cl, beats = batch_population(n_all)
+    length = (10.0 + cl * beats) * 1e-3 + 0.5           # s: the protocol and 500 ms after it
+    pick = np.argsort(length, kind="stable")[:args.batch_apd_cells]
+    st = [stimuli[int(c)] for c in pick]
+    end = length[pick].copy()
+    res = {}
+    for name, prec in (("fp64", lib.PRECISION_FP64), ("mixed", lib.PRECISION_MIXED)):
+        b = api.BatchCells("ToRORd_dynCl", "endocardialCells", dt, st, end, precision=prec,
+                           scales=scales[:, pick].copy(), ode=api.ode_desc(max_steps=10 ** 6))
+        t0 = time.perf_counter()
+        b.run()
+        res[name] = (time.perf_counter() - t0,) + tuple(b.results())
+        b.close()
+    (t64, nb0, apd0, _, ca0), (tmx, nb1, apd1, _, ca1) = res["fp64"], res["mixed"]
+    ok = ~np.isnan(apd0) & ~np.isnan(apd1)
+    return {"workload": (f"the {pick.size} ToRORd_dynCl endocardialCells cells of the {n_all}-cell "
+                         f"population with the shortest protocols (per-cell scales, S1 CL "
+                         f"U[300,1000] ms x U{{5..50}} beats from 10 ms, stimulus 53 uA/uF x 1 ms, "
+                         f"+500 ms), dt 0.01 ms, whole protocols"),
+            "simulated_s_per_cell": [float(end.min()), float(end.max())],
+            "beats_per_cell": [int(beats[pick].min()), int(beats[pick].max())],
+            "fp64_seconds": t64, "mixed_seconds": tmx,
+            "apd90_cells_compared": int(ok.sum()),
+            "apd90_fp64_range_ms": [float(np.nanmin(apd0)), float(np.nanmax(apd0))],
+            "apd90_max_abs_error_ms": float(np.max(np.abs(apd0[ok] - apd1[ok]))) if ok.any() else None,
+            "peak_ca_max_rel_error": float(np.nanmax(np.abs(ca1 - ca0) / np.abs(ca0))),
+            "beat_count_mismatches": int(np.sum(nb0 != nb1))}
+
+
 def mms_arm():
     """Manufactured-solution convergence of the FP64 step on GPU: the 3D
     monodomainFDAManufactured case over the tutorial's sweep (10/20/40/80
@@ -837,6 +964,15 @@ def main():
     ap.add_argument("--batch-accuracy-cells", type=int, default=256)
     ap.add_argument("--no-graph", action="store_true",
                     help="host-driven PIMPLE/PCG loops instead of the step graph")
+    ap.add_argument("--full-run", action="store_true",
+                    help="only the whole 100 ms run of both forms and their comparison")
+    ap.add_argument("--full-run-steps", type=int, default=20000)
+    ap.add_argument("--tissue-apd", action="store_true",
+                    help="only the tissue APD90 comparison of both forms (reduced ORd slab)")
+    ap.add_argument("--tissue-apd-steps", type=int, default=80000)
+    ap.add_argument("--batch-apd", action="store_true",
+                    help="only the batched cells' APD90 over whole protocols, both forms")
+    ap.add_argument("--batch-apd-cells", type=int, default=304)
     args = ap.parse_args()
     global GRAPH
     GRAPH = not args.no_graph
@@ -852,6 +988,15 @@ def main():
         out = reference_arm(args, rank, world)
         if out is not None:
             print(json.dumps(out), flush=True)
+        return
+    if args.full_run:
+        print(json.dumps({"full_run": full_run_arm(args)}), flush=True)
+        return
+    if args.tissue_apd:
+        print(json.dumps({"tissue_apd": tissue_apd_arm(args)}), flush=True)
+        return
+    if args.batch_apd:
+        print(json.dumps({"batch_apd": batch_apd_arm(args)}), flush=True)
         return
     if args.adjoint_only:
         from cardiacfoam_gb300 import build as gpu_build

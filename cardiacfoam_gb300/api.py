@@ -334,6 +334,19 @@ class Monodomain:
     def set_timing(self, enable: bool = True):
         _L.check(self._lib.cfg_monodomain_set_timing(self.h, int(enable)))
 
+    def track_apd(self, every_steps: int):
+        """Per-cell beat detection on Vm after every `every_steps`-th step
+        (0 stops it)."""
+        _L.check(self._lib.cfg_monodomain_track_apd(self.h, int(every_steps)))
+
+    def apd_results(self):
+        """(beats, last-beat APD90 [ms], its upstroke time [s]) per cell."""
+        nb = np.zeros(self.n, dtype=np.int32)
+        apd, tup = np.zeros(self.n), np.zeros(self.n)
+        _L.check(self._lib.cfg_monodomain_apd_results(self.h, nb.ctypes.data, _L.dptr(apd),
+                                                      _L.dptr(tup)))
+        return nb, apd, tup
+
     def set_wait_limit(self, spins: int = -1):
         """Bound on each grid-barrier wait of the persistent diffusion
         kernel (spins; negative = the default, about a second)."""

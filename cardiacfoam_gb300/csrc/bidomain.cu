@@ -436,6 +436,36 @@ __device__ __forceinline__ double direction(const double* z, const double* p_old
     return first ? zq : __fma_rn(beta, __ldcg(&p_old[q]), zq);
 }
 
+// acc plus, over the row's slots in slot (column) order, -coef * f(column):
+// lduMatrix::Amul's order after the diagonal term.  W > 0: every row is
+// visited over the full ELL width (padded slots have column 0 and
+// coefficient 0, an exact zero term), so all of a row's loads are issued
+// together; W == 0: the row's own count.
+template <int W, class F>
+__device__ __forceinline__ double offdiag(const BdOp& op, const double* coef, long long c, F f,
+                                          double acc)
+{
+    if constexpr (W > 0) {
+        double v[W], k[W];
+#pragma unroll
+        for (int e = 0; e < W; ++e) {
+            const long long i = (long long)e * op.n + c;
+            k[e] = coef[i];
+            v[e] = f(op.col[i]);
+        }
+#pragma unroll
+        for (int e = 0; e < W; ++e) acc += (-k[e]) * v[e];
+    } else {
+        const int k = op.cnt[c];
+        for (int e = 0; e < k; ++e) {
+            const long long i = (long long)e * op.n + c;
+            acc += (-coef[i]) * f(op.col[i]);
+        }
+    }
+    return acc;
+}
+
+template <int W>
 __global__ void __launch_bounds__(kCoopBlock, 1) k_pcg_coop(CoopPcgArgs ca)
 {
     using namespace cfg::gsync;
@@ -457,7 +487,9 @@ __global__ void __launch_bounds__(kCoopBlock, 1) k_pcg_coop(CoopPcgArgs ca)
         // --- A x, r = b - A x; sums of x and |r|
         double s1[2] = {0.0, 0.0};
         for (long long c = first; c < n; c += stride) {
-            const double ax = amul(op, a.coef, a.diag, a.x, c);
+            const double* xx = a.x;
+            const double ax = offdiag<W>(op, a.coef, c, [xx](long long q) { return xx[q]; },
+                                         a.diag[c] * xx[c]);
             const double rr = a.b[c] - ax;
             a.ax[c] = ax;
             a.r[c] = rr;
@@ -497,12 +529,11 @@ __global__ void __launch_bounds__(kCoopBlock, 1) k_pcg_coop(CoopPcgArgs ca)
             double s3[1] = {0.0};
             for (long long c = first; c < n; c += stride) {
                 const double pc = direction(a.z, p_old, beta, first_it, c);
-                double acc = a.diag[c] * pc;
-                const int k = op.cnt[c];
-                for (int e = 0; e < k; ++e) {
-                    const long long i = (long long)e * n + c;
-                    acc += (-a.coef[i]) * direction(a.z, p_old, beta, first_it, op.col[i]);
-                }
+                const double* zz = a.z;
+                const double* po = p_old;
+                const double acc = offdiag<W>(op, a.coef, c, [zz, po, beta, first_it](long long q) {
+                    return direction(zz, po, beta, first_it, q);
+                }, a.diag[c] * pc);
                 __stcg(&p_new[c], pc);
                 a.ap[c] = acc;
                 s3[0] += acc * pc;
@@ -664,8 +695,11 @@ int pcg_solve(cfg_bidomain* bd, int kind, double tol, double rel, int max_iter,
         CoopPcgArgs ca{a, bd->d_p_alt, bd->d_coop_partial, bd->d_bar, bd->d_abort,
                        bd->spin_limit};
         void* params[] = {&ca};
-        CFG_CUDA_TRY(cudaLaunchCooperativeKernel((void*)k_pcg_coop, dim3(bd->coop_blocks),
-                                                 dim3(kCoopBlock), params, 0, s));
+        const void* fn = bd->op.width == 6 ? (const void*)k_pcg_coop<6>
+                       : bd->op.width == 4 ? (const void*)k_pcg_coop<4>
+                                           : (const void*)k_pcg_coop<0>;
+        CFG_CUDA_TRY(cudaLaunchCooperativeKernel(fn, dim3(bd->coop_blocks), dim3(kCoopBlock),
+                                                 params, 0, s));
         CFG_CUDA_TRY(cudaMemcpyAsync(bd->h_st, bd->d_st, sizeof(PcgScalars),
                                      cudaMemcpyDeviceToHost, s));
         CFG_CUDA_TRY(cudaStreamSynchronize(s));
@@ -941,9 +975,15 @@ extern "C" int cfg_bidomain_create(const cfg_bidomain_desc* d, const cfg_mesh_de
             cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) == cudaSuccess &&
             coop &&
             cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess &&
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pcg_coop, kCoopBlock, 0) ==
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pcg_coop<0>, kCoopBlock, 0) ==
                 cudaSuccess &&
             per_sm > 0) {
+            for (const void* f : {(const void*)k_pcg_coop<4>, (const void*)k_pcg_coop<6>}) {
+                int k = 0;
+                if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&k, f, kCoopBlock, 0) ==
+                    cudaSuccess)
+                    per_sm = std::min(per_sm, k);
+            }
             const long long want = (n + kCoopBlock - 1) / kCoopBlock;
             const long long cap = (long long)sms * per_sm;
             bd->coop_blocks = int(want < cap ? want : cap);

@@ -273,9 +273,11 @@ __device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity, long lo
     const long long t0 = clock64();
     for (;;) {
         unsigned ok;
+        // test_wait does not suspend the thread, so the clock limit alone
+        // bounds the wait (a limit of zero gives up unless the copy landed)
         asm volatile(
             "{\n\t.reg .pred p;\n\t"
-            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
             "selp.u32 %0, 1, 0, p;\n\t}"
             : "=r"(ok)
             : "r"(bar), "r"(parity)
@@ -456,7 +458,9 @@ struct cfg_pseudo_ecg {
     double* d_series = nullptr;     // [max_rows][n_el]
     long long max_rows = 0, rows = 0;
     std::vector<double> times;
-    cudaStream_t last_stream = nullptr;   // stream of the last launch
+    cudaStream_t last_stream = nullptr;   // stream of the last launch (the caller's)
+    cudaEvent_t done = nullptr;           // recorded after each launch: the object's
+                                          // own handle on its work, whatever the stream
     bool launched = false;
     long long wait_cycles = kWaitCycles;   // limit of the staged form's copy waits
 };
@@ -516,8 +520,7 @@ int fold_lead(const cfg_mesh_desc* m, const cfg_pseudo_ecg_desc* d, const Correc
 // stream than the last one waits for that one first.
 int launch(cfg_pseudo_ecg* ecg, const double* vm, cudaStream_t s, double* out)
 {
-    if (ecg->launched && s != ecg->last_stream)
-        CFG_CUDA_TRY(cudaStreamSynchronize(ecg->last_stream));
+    if (ecg->launched && s != ecg->last_stream) CFG_CUDA_TRY(cudaStreamWaitEvent(s, ecg->done, 0));
     // the staged form copies whole 16-byte units of Vm
     const bool staged = (reinterpret_cast<uintptr_t>(vm) & 15) == 0;
     for (int e0 = 0, k = 0; e0 < ecg->n_el; e0 += kEcgChunk, ++k) {
@@ -527,18 +530,18 @@ int launch(cfg_pseudo_ecg* ecg, const double* vm, cudaStream_t s, double* out)
         CFG_CUDA_TRY(launch_any(a, std::min(kEcgChunk, ecg->n_el - e0), staged, ecg->pair,
                                 blocks, ecg->d_error, s));
     }
+    CFG_CUDA_TRY(cudaEventRecord(ecg->done, s));
     ecg->last_stream = s;
     ecg->launched = true;
     return CFG_OK;
 }
 
-// Waits for the stream and reports a staged launch whose copy wait ran out
-// (the flag is cleared).
-int check_error(cfg_pseudo_ecg* ecg, cudaStream_t s)
+// Waits for the object's last launch and reports a staged launch whose copy
+// wait ran out (the flag is cleared).
+int check_error(cfg_pseudo_ecg* ecg)
 {
-    CFG_CUDA_TRY(cudaMemcpyAsync(ecg->h_error, ecg->d_error, sizeof(unsigned),
-                                 cudaMemcpyDeviceToHost, s));
-    CFG_CUDA_TRY(cudaStreamSynchronize(s));
+    CFG_CUDA_TRY(cudaEventSynchronize(ecg->done));
+    CFG_CUDA_TRY(cudaMemcpy(ecg->h_error, ecg->d_error, sizeof(unsigned), cudaMemcpyDeviceToHost));
     if (*ecg->h_error) {
         CFG_CUDA_TRY(cudaMemset(ecg->d_error, 0, sizeof(unsigned)));
         return fail(CFG_ERR_CUDA, "a pseudo-ECG tile copy did not complete within its wait limit");
@@ -664,6 +667,7 @@ extern "C" int cfg_pseudo_ecg_create(const cfg_pseudo_ecg_desc* d, const cfg_mes
     const int chunks = (ecg->n_el + kEcgChunk - 1) / kEcgChunk;
     if (!e) e = dmalloc(&ecg->d_ticket, size_t(chunks));
     if (!e) e = cudaMemset(ecg->d_ticket, 0, sizeof(unsigned) * size_t(chunks));
+    if (!e) e = cudaEventCreateWithFlags(&ecg->done, cudaEventDisableTiming);
     if (!e) e = dmalloc(&ecg->d_error, 1);
     if (!e) e = cudaMemset(ecg->d_error, 0, sizeof(unsigned));
     if (!e) e = dmalloc(&ecg->d_values, size_t(ecg->n_el));
@@ -686,7 +690,8 @@ extern "C" int cfg_pseudo_ecg_compute(cfg_pseudo_ecg* ecg, const double* vm, voi
     if (int rc = launch(ecg, vm, s, ecg->d_values)) return rc;
     CFG_CUDA_TRY(cudaMemcpyAsync(ecg->h_values, ecg->d_values, size_t(ecg->n_el) * sizeof(double),
                                  cudaMemcpyDeviceToHost, s));
-    if (int rc = check_error(ecg, s)) return rc;
+    CFG_CUDA_TRY(cudaEventRecord(ecg->done, s));   // after the copy of the values
+    if (int rc = check_error(ecg)) return rc;
     std::memcpy(values, ecg->h_values, size_t(ecg->n_el) * sizeof(double));
     return CFG_OK;
 }
@@ -730,7 +735,7 @@ extern "C" int cfg_pseudo_ecg_series(cfg_pseudo_ecg* ecg, double* times, double*
     const long long k = std::min(max_rows, ecg->rows);
     if (k <= 0) return CFG_OK;
     if (ecg->launched)
-        if (int rc = check_error(ecg, ecg->last_stream)) return rc;
+        if (int rc = check_error(ecg)) return rc;
     if (values)
         CFG_CUDA_TRY(cudaMemcpy(values, ecg->d_series, size_t(k) * size_t(ecg->n_el) * sizeof(double),
                                 cudaMemcpyDeviceToHost));
@@ -756,7 +761,10 @@ extern "C" int cfg_pseudo_ecg_reset(cfg_pseudo_ecg* ecg)
 extern "C" int cfg_pseudo_ecg_destroy(cfg_pseudo_ecg* ecg)
 {
     if (!ecg) return CFG_OK;
-    if (ecg->launched) cudaStreamSynchronize(ecg->last_stream);
+    // the last launch ran on a caller's stream, which may be gone by now: wait
+    // on the object's own event instead
+    if (ecg->launched) cudaEventSynchronize(ecg->done);
+    if (ecg->done) cudaEventDestroy(ecg->done);
     if (ecg->d_lead) cudaFree(ecg->d_lead);
     dfree(ecg->d_scale);
     dfree(ecg->d_partial);

@@ -49,7 +49,9 @@ __device__ __forceinline__ bool grid_barrier(unsigned* count, int* abort, unsign
                 good = 0;
                 break;
             }
-            if (spins > 32) __nanosleep(32);
+            // short waits spin; long ones back off (a waiting block then
+            // polls L2 less often)
+            if (spins > 4096) __nanosleep(64);
         }
         if (ld_relaxed_int(abort)) good = 0;
         __threadfence();

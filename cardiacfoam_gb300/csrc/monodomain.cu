@@ -28,6 +28,9 @@ __global__ void k_grad_start(DiffusionArgs a);
 
 static void md_free(cfg_monodomain* md)
 {
+    dfree(md->d_apd);
+    dfree(md->d_apd_ring_t);
+    dfree(md->d_apd_ring_v);
     if (!md) return;
     if (md->graph_exec) cudaGraphExecDestroy(md->graph_exec);
     for (cudaEvent_t& e : md->ev)
@@ -549,7 +552,119 @@ int check_step(cfg_monodomain* md)
 
 using namespace cfg;
 
+// --- per-cell APD tracking on the tissue's Vm ---------------------------------
+__global__ void k_apd_init(long long n, ApdTracker* apd)
+{
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    ApdTracker a{};
+    a.last_apd = cfg_nan();
+    a.last_ca = cfg_nan();
+    a.last_t_up = cfg_nan();
+    apd[c] = a;
+}
+
+// one sample (t, Vm in mV) of every cell; no calcium trace in the tissue
+__global__ void k_apd_sample(long long n, double t, const double* __restrict__ vm,
+                             ApdTracker* apd, ApdParams P, double* ring_t, double* ring_v)
+{
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    ApdTracker a = apd[c];
+    apd_sample(a, P, t, 1000.0 * vm[c], cfg_nan(), ring_t + c, ring_v + c, n);
+    apd[c] = a;
+}
+
+// the trace ending at the last sample: beats and the last beat's APD90, on a
+// copy of each tracker (the live one keeps running)
+__global__ void k_apd_results(long long n, const ApdTracker* apd, ApdParams P, int* beats,
+                              double* apd90, double* t_up)
+{
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    ApdTracker a = apd[c];
+    apd_end(a, P);
+    beats[c] = a.n_beats;
+    apd90[c] = a.last_apd * 1000.0;
+    t_up[c] = a.last_t_up;
+}
+
+static int apd_after_step(cfg_monodomain* md)
+{
+    if (md->apd_every <= 0) return CFG_OK;
+    if (++md->apd_steps % md->apd_every) return CFG_OK;
+    const unsigned grid = unsigned((md->n + 255) / 256);
+    k_apd_sample<<<grid, 256, 0, md->stream>>>(md->n, md->t_host, md->d_vm, md->d_apd, md->apdp,
+                                               md->d_apd_ring_t, md->d_apd_ring_v);
+    CFG_CUDA_TRY(cudaGetLastError());
+    return CFG_OK;
+}
+
 extern "C" {
+
+int cfg_monodomain_track_apd(cfg_monodomain* md, int every_steps)
+{
+    if (!md) return fail(CFG_ERR_INVALID, "null context");
+    dfree(md->d_apd);
+    dfree(md->d_apd_ring_t);
+    dfree(md->d_apd_ring_v);
+    md->d_apd = nullptr;
+    md->d_apd_ring_t = md->d_apd_ring_v = nullptr;
+    md->apd_every = 0;
+    if (every_steps <= 0) return CFG_OK;
+    if (!(md->delta_t > 0)) return fail(CFG_ERR_INVALID, "the context has no time step");
+    const ApdParams P = apd_defaults(md->delta_t * every_steps);
+    if (P.ring > 4096)
+        return fail(CFG_ERR_INVALID, "sampling every %d steps of %g s keeps %d samples for the "
+                                     "2 ms baseline window (at most 4096)", every_steps,
+                    md->delta_t, P.ring);
+    const size_t n = size_t(md->n);
+    cudaError_t e = dmalloc(&md->d_apd, n);
+    if (!e) e = dmalloc(&md->d_apd_ring_t, size_t(P.ring) * n);
+    if (!e) e = dmalloc(&md->d_apd_ring_v, size_t(P.ring) * n);
+    if (e) {
+        dfree(md->d_apd); dfree(md->d_apd_ring_t); dfree(md->d_apd_ring_v);
+        md->d_apd = nullptr;
+        md->d_apd_ring_t = md->d_apd_ring_v = nullptr;
+        return fail(CFG_ERR_CUDA, "device allocation failed: %s", cudaGetErrorString(e));
+    }
+    md->apdp = P;
+    md->apd_every = every_steps;
+    md->apd_steps = 0;
+    const unsigned grid = unsigned((md->n + 255) / 256);
+    k_apd_init<<<grid, 256, 0, md->stream>>>(md->n, md->d_apd);
+    // sample 0: the field as it is now
+    k_apd_sample<<<grid, 256, 0, md->stream>>>(md->n, md->t_host, md->d_vm, md->d_apd, md->apdp,
+                                               md->d_apd_ring_t, md->d_apd_ring_v);
+    CFG_CUDA_TRY(cudaGetLastError());
+    return CFG_OK;
+}
+
+int cfg_monodomain_apd_results(cfg_monodomain* md, int* n_beats, double* apd90_ms, double* t_up)
+{
+    if (!md || !n_beats || !apd90_ms || !t_up) return fail(CFG_ERR_INVALID, "null argument");
+    if (md->apd_every <= 0) return fail(CFG_ERR_INVALID, "APD tracking is not enabled");
+    const size_t n = size_t(md->n);
+    int* d_b = nullptr;
+    double *d_a = nullptr, *d_t = nullptr;
+    cudaError_t e = dmalloc(&d_b, n);
+    if (!e) e = dmalloc(&d_a, n);
+    if (!e) e = dmalloc(&d_t, n);
+    if (!e) {
+        const unsigned grid = unsigned((md->n + 255) / 256);
+        k_apd_results<<<grid, 256, 0, md->stream>>>(md->n, md->d_apd, md->apdp, d_b, d_a, d_t);
+        e = cudaGetLastError();
+    }
+    if (!e) e = cudaMemcpyAsync(n_beats, d_b, n * sizeof(int), cudaMemcpyDeviceToHost, md->stream);
+    if (!e) e = cudaMemcpyAsync(apd90_ms, d_a, n * sizeof(double), cudaMemcpyDeviceToHost, md->stream);
+    if (!e) e = cudaMemcpyAsync(t_up, d_t, n * sizeof(double), cudaMemcpyDeviceToHost, md->stream);
+    if (!e) e = cudaStreamSynchronize(md->stream);
+    dfree(d_b);
+    dfree(d_a);
+    dfree(d_t);
+    if (e) return fail(CFG_ERR_CUDA, "APD results: %s", cudaGetErrorString(e));
+    return CFG_OK;
+}
 
 int cfg_monodomain_create(const cfg_monodomain_desc* desc, const cfg_mesh_desc* mesh,
                           cfg_monodomain** out)
@@ -598,6 +713,7 @@ int cfg_monodomain_step(cfg_monodomain* md, double dt)
     if (rc) return rc;
     md->t_host = md->t_host + dt;
     md->steps++;
+    if ((rc = apd_after_step(md))) return rc;
     rc = check_step(md);
     if (!rc && md->use_graph && md->timing) md->timed_launches += graph_step_launches(md);
     return rc;
@@ -620,6 +736,7 @@ int cfg_monodomain_run(cfg_monodomain* md, double dt, long long n_steps)
         if (rc) return rc;
         md->t_host = md->t_host + dt;
         md->steps++;
+        if ((rc = apd_after_step(md))) return rc;
     }
     return n_steps > 0 ? check_step(md) : CFG_OK;
 }

@@ -3,6 +3,7 @@
 
 #include <vector>
 
+#include "apd.cuh"
 #include "diffusion_kernels.cuh"
 #include "grid_sync.cuh"
 #include "host_common.h"
@@ -67,6 +68,13 @@ struct cfg_monodomain {
     long long spin_limit = cfg::gsync::kSpinLimit;   // grid-barrier spins before the step aborts
     double t_host = 0.0;
     long long steps = 0;
+    // per-cell beat detector on Vm (cfg_monodomain_track_apd): sampled after
+    // every apd_every-th step
+    cfg::ApdTracker* d_apd = nullptr;
+    double *d_apd_ring_t = nullptr, *d_apd_ring_v = nullptr;
+    cfg::ApdParams apdp{};
+    int apd_every = 0;
+    long long apd_steps = 0;
     // time step a caller may leave to the context (cfg_monodomain_step with
     // dt = 0), and the explicit algorithm's Courant limit at maxCo = 1
     double delta_t = 0.0;

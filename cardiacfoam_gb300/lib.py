@@ -154,7 +154,8 @@ EXPORTS = [
     "cfg_monodomain_stream", "cfg_monodomain_destroy", "cfg_box_diffusion_solve_noalloc",
     "cfg_monodomain_set_persistent", "cfg_monodomain_suggest_explicit_delta_t",
     "cfg_monodomain_delta_t", "cfg_monodomain_set_delta_t", "cfg_monodomain_set_wait_limit",
-    "cfg_pseudo_ecg_set_wait_limit", "cfg_batch_create", "cfg_batch_run", "cfg_batch_results",
+    "cfg_pseudo_ecg_set_wait_limit", "cfg_monodomain_track_apd", "cfg_monodomain_apd_results",
+    "cfg_batch_create", "cfg_batch_run", "cfg_batch_results",
     "cfg_batch_trace", "cfg_batch_get_states", "cfg_batch_stats", "cfg_batch_stream",
     "cfg_batch_destroy", "cfg_adjoint_create", "cfg_adjoint_set_target", "cfg_adjoint_forward",
     "cfg_adjoint_backward", "cfg_adjoint_destroy", "cfg_ionic_autotune", "cfg_monodomain_autotune",
@@ -222,6 +223,8 @@ def load(path: Optional[os.PathLike] = None):
     L.cfg_monodomain_delta_t.argtypes = [C.c_void_p, _dp]
     L.cfg_monodomain_set_delta_t.argtypes = [C.c_void_p, C.c_double]
     L.cfg_monodomain_set_wait_limit.argtypes = [C.c_void_p, C.c_longlong]
+    L.cfg_monodomain_track_apd.argtypes = [C.c_void_p, C.c_int]
+    L.cfg_monodomain_apd_results.argtypes = [C.c_void_p, C.c_void_p, _dp, _dp]
     L.cfg_pseudo_ecg_set_wait_limit.argtypes = [C.c_void_p, C.c_longlong]
     L.cfg_batch_create.argtypes = [C.POINTER(BatchDesc), C.POINTER(C.c_void_p)]
     L.cfg_batch_run.argtypes = [C.c_void_p]

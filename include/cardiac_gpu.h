@@ -309,6 +309,21 @@ int cfg_monodomain_timings(const cfg_monodomain* md, double* ionic_ms, double* d
  * sums.  MonodomainSolver::solveDiffusionImplicit (monodomainSolver.C:112-150)
  * is what either form computes. */
 int cfg_monodomain_set_persistent(cfg_monodomain* md, int enable);
+/* Per-cell beat detection on the tissue's Vm: after every `every_steps`-th
+ * step (and once at the call, the field as it is) each cell's Vm [mV] and
+ * the time go through the reference's restitution post-processing as a
+ * streaming detector (postProcessing_restCurves.py:121-205: central dV/dt,
+ * upstroke at 5000 mV/s, baseline the minimum over the 2 ms before it, v90
+ * crossing after the peak).  No counterpart in the reference's tissue solver,
+ * whose traces are post-processed offline; it states the APD90 of a tissue
+ * run without copying its trace to the host.  every_steps <= 0 stops it.
+ * The sampling interval is every_steps times the context's time step, and
+ * the 2 ms baseline window may hold at most 4096 samples. */
+int cfg_monodomain_track_apd(cfg_monodomain* md, int every_steps);
+/* The tracked trace as it ends at the last sample: beats detected, the last
+ * beat's APD90 [ms] (NaN if it has not repolarised) and its upstroke time
+ * [s], per cell (host arrays of n_cells). */
+int cfg_monodomain_apd_results(cfg_monodomain* md, int* n_beats, double* apd90_ms, double* t_up);
 /* Bound on each grid-barrier wait of the persistent diffusion kernel, in
  * spins of at least 32 ns (default 2^25, about a second; a negative value
  * restores it).  A block that waits longer makes every block leave at its

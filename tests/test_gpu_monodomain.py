@@ -249,3 +249,37 @@ def test_explicit_delta_t_rule_on_the_niederer_slab(gpu_lib):
     assert m3.delta_t() == 5e-5
     for x in (m, m2, m3):
         x.close()
+
+
+@pytest.mark.gpu
+def test_tissue_apd_tracking_equals_trace_postprocessing(gpu_lib):
+    """Per-cell beat detection on the tissue's Vm (cfg_monodomain_track_apd)
+    over a full beat of a TNNP slab, sampled every 0.1 ms: the device's
+    beats, last-beat APD90 and upstroke times equal the restated
+    post-processing (oracle/apd.py) run on the same samples read back."""
+    from oracle import apd as oapd
+    dt, every, n_samples = 1e-5, 10, 4000
+    mesh = box_mesh(20, 7, 3, 0.02, 0.007, 0.003)
+    m = api.Monodomain(mesh, "TNNP", "epicardialCells", SIGMA, dt=dt, boxes=BOX,
+                       precision=lib.PRECISION_MIXED)
+    m.track_apd(every)
+    t = [m.time()]
+    trace = [m.vm() * 1000.0]
+    for _ in range(n_samples):
+        m.run(dt, every)
+        t.append(m.time())
+        trace.append(m.vm() * 1000.0)
+    t, trace = np.array(t), np.array(trace)
+    nb, apd, tup = m.apd_results()
+    for c in range(mesh.n_cells):
+        b, a, u, _ = oapd.last_beat(t, trace[:, c])
+        assert nb[c] == b, (c, nb[c], b)
+        if np.isnan(a):
+            assert np.isnan(apd[c])
+            continue
+        assert abs(a - apd[c]) <= 1e-9 * abs(a), (c, a, apd[c])
+        assert abs(u - tup[c]) <= 1e-12, (c, u, tup[c])
+    done = (nb >= 1) & ~np.isnan(apd)
+    assert done.sum() >= 8                          # at least the stimulated corner
+    assert 150.0 < np.min(apd[done]) and np.max(apd[done]) < 450.0
+    m.close()
