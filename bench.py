@@ -818,15 +818,16 @@ def full_run_arm(args):
 
 
 def tissue_apd_arm(args):
-    """APD90 of a tissue run in both forms: ORd myocyte on the slab at
-    h = 0.5 mm (40 x 14 x 6 = 3,360 cells), dt 5 us, corner stimulus, 400 ms
-    (one full beat and its repolarisation), per-cell beat detection on Vm
-    every 0.1 ms (cfg_monodomain_track_apd); mixed against FP64: APD90,
+    """APD90 of a tissue run in both forms: ORd myocyte on a 6 x 2 x 1 mm
+    piece of the slab at its own h = 0.1 mm (60 x 20 x 10 = 12,000 cells; at
+    h = 0.5 mm ORd does not propagate), dt 5 us, corner stimulus, 400 ms (one
+    full beat and its repolarisation), per-cell beat detection on Vm every
+    0.1 ms (cfg_monodomain_track_apd); mixed against FP64: APD90,
     activation times and Vm at the end."""
     from cardiacfoam_gb300 import build as gpu_build, lib, api
     from cardiacfoam_gb300.mesh import box_mesh
     gpu_build.build()
-    nx, ny, nz, h = 40, 14, 6, 5e-4
+    nx, ny, nz, h = 60, 20, 10, H
     mesh = box_mesh(nx, ny, nz, nx * h, ny * h, nz * h)
     steps, every = args.tissue_apd_steps, 20
     res = {}
@@ -843,7 +844,7 @@ def tissue_apd_arm(args):
     f, x = res["fp64"], res["mixed"]
     ok = ~np.isnan(f["apd"]) & ~np.isnan(x["apd"])
     both = (f["act"] > 0) & (x["act"] > 0)
-    return {"workload": (f"ORd myocyte slab 20x7x3 mm at h 0.5 mm ({mesh.n_cells} cells), dt 5 us, "
+    return {"workload": (f"ORd myocyte slab 6x2x1 mm at h 0.1 mm ({mesh.n_cells} cells), dt 5 us, "
                          f"{steps * DT * 1e3:g} ms, corner stimulus 5e4 A/m^3 x 2 ms; per-cell "
                          f"APD90 from Vm sampled every {every * DT * 1e3:g} ms"),
             "fp64_seconds": f["seconds"], "mixed_seconds": x["seconds"],

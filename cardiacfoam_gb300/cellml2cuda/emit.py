@@ -26,7 +26,7 @@ from __future__ import annotations
 import re
 from typing import Dict, List
 
-from .cexpr import Bin, Call, Cond, Node, Num, Ref, Unary, Var
+from .cexpr import Bin, Call, Cond, Node, Num, Ref, Unary, Var, walk
 from .model import Assign, Fatal, If, Model, iter_assigns, refs, use_before_def
 
 # states stored and accumulated in double precision in the mixed form: the
@@ -340,6 +340,39 @@ class _TissuePrinter(_CudaPrinter):
         self.invariant = set(invariant)
         self.needed = list(needed)
         self.hoisted_defined = set()
+        self.subtrees: Dict[Node, int] = {}   # expression -> its slot after `needed`
+
+    def _extractable(self, e: Node) -> bool:
+        """A subexpression of a statement that depends on the membrane
+        potential and constants alone and holds a special function: its
+        value is the same at every stage, so H keeps it too."""
+        if isinstance(e, (Num, Ref, Var)):
+            return False
+        special = False
+        for n in walk(e):
+            if isinstance(n, Var) and n.name not in ("tissueFlag", "dimension"):
+                return False
+            if isinstance(n, Call):
+                if n.fn == "computeIstim":
+                    return False
+                if n.fn in ("exp", "log", "sqrt", "tanh") or (
+                        n.fn == "pow" and _int_exponent(n.args[1]) is None):
+                    special = True
+            if isinstance(n, Ref):
+                if n.array == "STATES" and n.name != self.m.states[0]:
+                    return False
+                if n.array == "RATES":
+                    return False
+                if n.array == "ALGEBRAIC" and (n.name not in self.invariant or
+                                               n.name not in self.hoisted_defined):
+                    return False
+        return special
+
+    def __call__(self, e: Node) -> str:
+        if self._extractable(e):
+            k = self.subtrees.setdefault(e, len(self.subtrees))
+            return f"H({len(self.needed) + k})"
+        return super().__call__(e)
 
     def ref(self, r: Ref) -> str:
         if r.array == "ALGEBRAIC" and r.name in self.invariant:
@@ -373,6 +406,17 @@ def _cuda_body_tissue(m: Model, stmts, pr: _TissuePrinter, indent: str, out: Lis
             out.append(f"{indent}/* unsupported configuration in the reference */")
 
 
+def tissue_subtrees(m: Model) -> List[Node]:
+    """The special-function subexpressions rhs_tissue() reads from H."""
+    from .hoist import analyse
+    h = analyse(m, m.rates)
+    if not h.needed:
+        return []
+    pr = _TissuePrinter(m, use_before_def(m.rates), h.invariant, h.needed)
+    _cuda_body_tissue(m, m.rates, pr, "    ", [])
+    return [e for e, _ in sorted(pr.subtrees.items(), key=lambda kv: kv[1])]
+
+
 def _emit_tissue_rhs(m: Model, L: List[str]):
     """hoist() and rhs_tissue(): the right-hand side of tissue mode split into
     its membrane-potential-only part, evaluated once per cell and PDE step,
@@ -380,13 +424,35 @@ def _emit_tissue_rhs(m: Model, L: List[str]):
     from .hoist import analyse, invariant_statements
     h = analyse(m, m.rates)
     vm = m.states[0]
+    # the rest of the body first: it finds the subexpressions H also keeps
+    rest: List[str] = []
+    subtrees: Dict[Node, int] = {}
+    if h.needed:
+        pr = _TissuePrinter(m, use_before_def(m.rates), h.invariant, h.needed)
+        body = []
+        for name in _predeclare_conditional_algebraics(m, m.rates, body, "    "):
+            if name in h.invariant:
+                continue
+            body.append(f"    R a_{name} = R(0);")
+            pr.defined.add(name)
+        _cuda_body_tissue(m, m.rates, pr, "    ", body)
+        rest.extend(_state_loads(m, pr))
+        rest.extend(body)
+        if m.iion_name in h.invariant:
+            rest.append(f"    return H(H_{m.iion_name});")
+        else:
+            rest.append(f"    return a_{m.iion_name};")
+        subtrees = pr.subtrees
+    nh = len(h.needed) + len(subtrees)
     L.append("// Tissue mode (solveVmWithinODESolver false): the PDE owns the membrane")
     L.append("// potential, so state 0 is the same at every RKF45 stage of a PDE step and")
     L.append("// the algebraics computed from it and constants alone are too.  hoist()")
-    L.append("// evaluates the ones the rest of the body reads, once per cell and step,")
-    L.append("// into H[NH]; rhs_tissue() is the body without them, reading H(H_x) (the")
-    L.append("// same expressions in the same order: bitwise the values of rhs()).")
-    L.append(f"constexpr int NH = {len(h.needed)};")
+    L.append("// evaluates the ones the rest of the body reads, and the special-function")
+    L.append("// subexpressions of the rest that depend on state 0 and constants alone,")
+    L.append("// once per cell and step into H[NH]; rhs_tissue() is the body without them,")
+    L.append("// reading H (the same expressions in the same order: bitwise the values")
+    L.append("// of rhs() in FP64).")
+    L.append(f"constexpr int NH = {nh};")
     if h.needed:
         L.append("enum Hoisted { " + ", ".join(f"H_{a}" for a in h.needed) + " };")
     L.append("template <class R, class KS>")
@@ -396,16 +462,18 @@ def _emit_tissue_rhs(m: Model, L: List[str]):
     if h.needed:
         stmts = invariant_statements(m.rates, h.invariant)
         pr = _CudaPrinter(m, [], "rhs")
-        body: List[str] = []
+        body = []
         for name in _predeclare_conditional_algebraics(m, stmts, body, "    "):
             body.append(f"    R a_{name} = R(0);")
             pr.defined.add(name)
         _cuda_body(m, stmts, pr, "    ", body)
+        for a in h.needed:
+            body.append(f"    H[H_{a}] = a_{a};")
+        for e, k in sorted(subtrees.items(), key=lambda kv: kv[1]):
+            body.append(f"    H[{len(h.needed) + k}] = {pr(e)};")
         if set(pr.states_read) - {vm}:
             raise ValueError(f"{m.name}: hoisted statements read {pr.states_read}")
         L.extend(body)
-        for a in h.needed:
-            L.append(f"    H[H_{a}] = a_{a};")
     L.append("}")
     L.append("template <class R, class YS, class KS, class HS>")
     L.append("__device__ __forceinline__ R rhs_tissue(double t, const YS& Y, const KS& K, "
@@ -418,20 +486,7 @@ def _emit_tissue_rhs(m: Model, L: List[str]):
         return h
     L.append("    constexpr bool SOLVE_VM = false;")
     L.append("    (void)tissue; (void)stim; (void)t; (void)H;")
-    pr = _TissuePrinter(m, use_before_def(m.rates), h.invariant, h.needed)
-    body = []
-    for name in _predeclare_conditional_algebraics(m, m.rates, body, "    "):
-        if name in h.invariant:
-            continue
-        body.append(f"    R a_{name} = R(0);")
-        pr.defined.add(name)
-    _cuda_body_tissue(m, m.rates, pr, "    ", body)
-    L.extend(_state_loads(m, pr))
-    L.extend(body)
-    if m.iion_name in h.invariant:
-        L.append(f"    return H(H_{m.iion_name});")
-    else:
-        L.append(f"    return a_{m.iion_name};")
+    L.extend(rest)
     L.append("}")
     return h
 

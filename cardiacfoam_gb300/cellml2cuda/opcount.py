@@ -127,7 +127,9 @@ def count_rhs(m: Model, tissue: int) -> dict:
     elif m.vm_to_state == "bueno":
         volts = [(v + 84) / 85.7 for v in volts]
     from .hoist import analyse, invariant_statements
+    from .emit import tissue_subtrees
     inv_body = invariant_statements(m.rates, analyse(m, m.rates).invariant)
+    subtrees = tissue_subtrees(m)
     total, inv = Counter(), Counter()
     for v in volts:
         ev = _Eval(m, dict(consts), dict(states, **{v0: v}), tissue)
@@ -135,6 +137,8 @@ def count_rhs(m: Model, tissue: int) -> dict:
         total.update(ev.n)
         ev = _Eval(m, dict(consts), dict(states, **{v0: v}), tissue)
         ev.run(inv_body, "rates")
+        for e in subtrees:
+            ev.ev(e)
         inv.update(ev.n)
 
     def summary(c):

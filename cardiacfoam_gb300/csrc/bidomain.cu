@@ -186,7 +186,8 @@ __global__ void k_stimulus(long long n, const double* __restrict__ centres, Stim
 // (= -source), diag = sum of the coefficients; at the reference cell the
 // diagonal doubles and b gains the diagonal times the reference value
 __global__ void k_phie_system(BdOp op, const double* __restrict__ dv, long long ref,
-                              double ref_value, double* __restrict__ diag, double* __restrict__ b)
+                              double ref_value, double* __restrict__ diag,
+                              double* __restrict__ rdiag, double* __restrict__ b)
 {
     const long long c = (long long)blockIdx.x * kBlock + threadIdx.x;
     if (c >= op.n) return;
@@ -200,6 +201,7 @@ __global__ void k_phie_system(BdOp op, const double* __restrict__ dv, long long 
         d = d + d;
     }
     diag[c] = -d;
+    rdiag[c] = 1.0 / (-d);
     b[c] = bb;
 }
 
@@ -214,7 +216,8 @@ struct VmArgs {
 __global__ void k_vm_system(BdOp op, VmArgs a, const double* __restrict__ vm_old,
                             const double* __restrict__ vm_oldold, const double* __restrict__ iion,
                             const double* __restrict__ src, const double* __restrict__ dp,
-                            double* __restrict__ diag, double* __restrict__ b)
+                            double* __restrict__ diag, double* __restrict__ rdiag,
+                            double* __restrict__ b)
 {
     const long long c = (long long)blockIdx.x * kBlock + threadIdx.x;
     if (c >= op.n) return;
@@ -230,6 +233,7 @@ __global__ void k_vm_system(BdOp op, VmArgs a, const double* __restrict__ vm_old
     double lapdiag = 0.0;
     for (int e = 0; e < op.cnt[c]; ++e) lapdiag -= op.coef_i[(long long)e * op.n + c];
     diag[c] = a.chicm * ddt_diag - lapdiag;
+    rdiag[c] = 1.0 / diag[c];
     double bb = a.chicm * ddt_src;
     double su = -(a.chicm * iion[c]) * V;
     su = su + src[c] * V;
@@ -339,6 +343,7 @@ struct PcgArgs {
     BdOp op;
     const double* coef;
     const double* diag;
+    const double* rdiag;      // 1/diag: the diagonal preconditioner multiplies by it
     const double* b;
     double *x, *ax, *r, *z, *p, *ap, *partial;
     unsigned* ticket;
@@ -367,7 +372,7 @@ __global__ void k_pcg_norm(PcgArgs a)
     if (c < a.op.n) {
         const double pa = row_sum(a.op, a.coef, a.diag, c) * a.st->avg;
         v[0] = fabs(a.ax[c] - pa) + fabs(a.b[c] - pa);
-        const double zc = a.r[c] / a.diag[c];
+        const double zc = a.rdiag[c] * a.r[c];
         a.z[c] = zc;
         v[1] = zc * a.r[c];
     }
@@ -407,7 +412,7 @@ __global__ void k_pcg_update(PcgArgs a)
         a.x[c] = a.x[c] + al * a.p[c];
         const double rr = a.r[c] - al * a.ap[c];
         a.r[c] = rr;
-        const double zc = rr / a.diag[c];
+        const double zc = a.rdiag[c] * rr;
         a.z[c] = zc;
         v[0] = fabs(rr);
         v[1] = zc * rr;
@@ -508,7 +513,7 @@ __global__ void __launch_bounds__(kCoopBlock, 1) k_pcg_coop(CoopPcgArgs ca)
             const double pa = row_sum(op, a.coef, a.diag, c) * avg;
             s2[0] += fabs(a.ax[c] - pa) + fabs(a.b[c] - pa);
             const double rr = a.r[c];
-            const double zc = rr / a.diag[c];
+            const double zc = a.rdiag[c] * rr;
             __stcg(&a.z[c], zc);
             s2[1] += zc * rr;
         }
@@ -552,7 +557,7 @@ __global__ void __launch_bounds__(kCoopBlock, 1) k_pcg_coop(CoopPcgArgs ca)
                 a.x[c] = a.x[c] + alpha * __ldcg(&p_new[c]);
                 const double rr = a.r[c] - alpha * a.ap[c];
                 a.r[c] = rr;
-                const double zc = rr / a.diag[c];
+                const double zc = a.rdiag[c] * rr;
                 __stcg(&a.z[c], zc);
                 s4[0] += fabs(rr);
                 s4[1] += zc * rr;
@@ -621,7 +626,8 @@ struct cfg_bidomain {
            *d_src = nullptr, *d_act = nullptr, *d_phie = nullptr, *d_phii = nullptr;
     unsigned char* d_calc = nullptr;
     // work
-    double *d_grad = nullptr, *d_dv = nullptr, *d_diag = nullptr, *d_b = nullptr, *d_r = nullptr,
+    double *d_grad = nullptr, *d_dv = nullptr, *d_diag = nullptr, *d_rdiag = nullptr,
+           *d_b = nullptr, *d_r = nullptr,
            *d_z = nullptr, *d_p = nullptr, *d_ap = nullptr, *d_ax = nullptr, *d_partial = nullptr;
     PcgScalars* d_st = nullptr;
     PcgScalars* h_st = nullptr;     // pinned
@@ -661,6 +667,7 @@ PcgArgs pcg_args(cfg_bidomain* bd, const double* coef, double* x)
     a.op = bd->op;
     a.coef = coef;
     a.diag = bd->d_diag;
+    a.rdiag = bd->d_rdiag;
     a.b = bd->d_b;
     a.x = x;
     a.ax = bd->d_ax;
@@ -774,7 +781,8 @@ extern "C" int cfg_bidomain_destroy(cfg_bidomain* bd)
     for (double** p : {&bd->d_coef_i, &bd->d_coef_e, &bd->d_gw, &bd->d_sf, &bd->d_w, &bd->d_bw,
                        &bd->d_vol, &bd->d_centres, &bd->d_vm, &bd->d_vm_old, &bd->d_vm_oldold,
                        &bd->d_iion, &bd->d_src, &bd->d_act, &bd->d_phie, &bd->d_phii,
-                       &bd->d_grad, &bd->d_dv, &bd->d_diag, &bd->d_b, &bd->d_r, &bd->d_z,
+                       &bd->d_grad, &bd->d_dv, &bd->d_diag, &bd->d_rdiag, &bd->d_b, &bd->d_r,
+                       &bd->d_z,
                        &bd->d_p, &bd->d_ap, &bd->d_ax, &bd->d_partial, &bd->d_p_alt,
                        &bd->d_coop_partial})
         dfree(*p);
@@ -957,7 +965,8 @@ extern "C" int cfg_bidomain_create(const cfg_bidomain_desc* d, const cfg_mesh_de
     if (!e) e = up(&bd->d_vol, vol);
     if (!e) e = up(&bd->d_centres, cen);
     for (double** p : {&bd->d_vm, &bd->d_vm_old, &bd->d_vm_oldold, &bd->d_iion, &bd->d_src,
-                       &bd->d_act, &bd->d_phie, &bd->d_phii, &bd->d_dv, &bd->d_diag, &bd->d_b,
+                       &bd->d_act, &bd->d_phie, &bd->d_phii, &bd->d_dv, &bd->d_diag,
+                       &bd->d_rdiag, &bd->d_b,
                        &bd->d_r, &bd->d_z, &bd->d_p, &bd->d_ap, &bd->d_ax})
         if (!e) e = dmalloc(p, size_t(n));
     if (!e) e = dmalloc(&bd->d_grad, 3 * size_t(n));
@@ -1046,7 +1055,7 @@ extern "C" int cfg_bidomain_step(cfg_bidomain* bd, double dt)
         // BidomainSolver::solveDiffusionExplicit (bidomainSolver.C:183-213)
         div_gamma_grad(bd, bd->d_vm, bd->d_dv);
         k_phie_system<<<nb, kBlock, 0, s>>>(bd->op, bd->d_dv, bd->ref, bd->ref_value, bd->d_diag,
-                                            bd->d_b);
+                                            bd->d_rdiag, bd->d_b);
         if (int rc = pcg_solve(bd, 0, bd->e_tol, bd->e_rel, bd->e_max, bd->e_stats))
             return rc;
         double cft = 1.0, cft0 = 1.0, cft00 = 0.0;
@@ -1086,7 +1095,7 @@ extern "C" int cfg_bidomain_step(cfg_bidomain* bd, double dt)
         // phiE
         div_gamma_grad(bd, bd->d_vm, bd->d_dv);
         k_phie_system<<<nb, kBlock, 0, s>>>(bd->op, bd->d_dv, bd->ref, bd->ref_value, bd->d_diag,
-                                            bd->d_b);
+                                            bd->d_rdiag, bd->d_b);
         if (int rc = pcg_solve(bd, 0, bd->e_tol, bd->e_rel, bd->e_max, bd->e_stats))
             return rc;
         // Vm: fvm::ddt creates the old-time levels on first access
@@ -1108,7 +1117,8 @@ extern "C" int cfg_bidomain_step(cfg_bidomain* bd, double dt)
         div_gamma_grad(bd, bd->d_phie, bd->d_dv);
         VmArgs va{bd->chicm, 1.0 / dt, cft, cft0, cft00, bd->backward ? 1 : 0};
         k_vm_system<<<nb, kBlock, 0, s>>>(bd->op, va, bd->d_vm_old, bd->d_vm_oldold, bd->d_iion,
-                                          bd->d_src, bd->d_dv, bd->d_diag, bd->d_b);
+                                          bd->d_src, bd->d_dv, bd->d_diag, bd->d_rdiag,
+                                          bd->d_b);
         if (int rc = pcg_solve(bd, 1, bd->vm_tol, bd->vm_rel, bd->vm_max, bd->vm_stats))
             return rc;
         k_phii<<<nb, kBlock, 0, s>>>(n, bd->d_vm, bd->d_phie, bd->d_phii);

@@ -111,9 +111,11 @@ __device__ __forceinline__ R rhs(double t, const YS& Y, const KS& K, R* dydt, in
 // Tissue mode (solveVmWithinODESolver false): the PDE owns the membrane
 // potential, so state 0 is the same at every RKF45 stage of a PDE step and
 // the algebraics computed from it and constants alone are too.  hoist()
-// evaluates the ones the rest of the body reads, once per cell and step,
-// into H[NH]; rhs_tissue() is the body without them, reading H(H_x) (the
-// same expressions in the same order: bitwise the values of rhs()).
+// evaluates the ones the rest of the body reads, and the special-function
+// subexpressions of the rest that depend on state 0 and constants alone,
+// once per cell and step into H[NH]; rhs_tissue() is the body without them,
+// reading H (the same expressions in the same order: bitwise the values
+// of rhs() in FP64).
 constexpr int NH = 0;
 template <class R, class KS>
 __device__ __forceinline__ void hoist(R y_u, const KS& K, int tissue, R* H)

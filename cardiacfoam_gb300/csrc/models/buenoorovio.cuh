@@ -234,10 +234,12 @@ __device__ __forceinline__ R rhs(double t, const YS& Y, const KS& K, R* dydt, in
 // Tissue mode (solveVmWithinODESolver false): the PDE owns the membrane
 // potential, so state 0 is the same at every RKF45 stage of a PDE step and
 // the algebraics computed from it and constants alone are too.  hoist()
-// evaluates the ones the rest of the body reads, once per cell and step,
-// into H[NH]; rhs_tissue() is the body without them, reading H(H_x) (the
-// same expressions in the same order: bitwise the values of rhs()).
-constexpr int NH = 6;
+// evaluates the ones the rest of the body reads, and the special-function
+// subexpressions of the rest that depend on state 0 and constants alone,
+// once per cell and step into H[NH]; rhs_tissue() is the body without them,
+// reading H (the same expressions in the same order: bitwise the values
+// of rhs() in FP64).
+constexpr int NH = 7;
 enum Hoisted { H_Jso, H_vInfty, H_tauVMinus, H_wInfty, H_tauWMinus, H_tauS };
 template <class R, class KS>
 __device__ __forceinline__ void hoist(R y_u, const KS& K, int tissue, R* H)
@@ -257,6 +259,7 @@ __device__ __forceinline__ void hoist(R y_u, const KS& K, int tissue, R* H)
     H[H_wInfty] = a_wInfty;
     H[H_tauWMinus] = a_tauWMinus;
     H[H_tauS] = a_tauS;
+    H[6] = ((R(1.0) + cfg_tanh((K(C_kS) * (y_u - K(C_uS))))) / R(2.0));
 }
 template <class R, class YS, class KS, class HS>
 __device__ __forceinline__ R rhs_tissue(double t, const YS& Y, const KS& K, const HS& H, R* dydt, int tissue, const CfgStimulus& stim)
@@ -272,7 +275,7 @@ __device__ __forceinline__ R rhs_tissue(double t, const YS& Y, const KS& K, cons
     R a_Jion = ((a_Jfi + H(H_Jso)) + a_Jsi);
     dydt[S_v] = ((((R(1.0) - (((y_u - K(C_thetaV))) > R(0) ? 1 : 0)) * (H(H_vInfty) - y_v)) / H(H_tauVMinus)) - (((((y_u - K(C_thetaV))) > R(0) ? 1 : 0) * y_v) / K(C_tauVPlus)));
     dydt[S_w] = ((((R(1.0) - (((y_u - K(C_thetaW))) > R(0) ? 1 : 0)) * (H(H_wInfty) - y_w)) / H(H_tauWMinus)) - (((((y_u - K(C_thetaW))) > R(0) ? 1 : 0) * y_w) / K(C_tauWPlus)));
-    dydt[S_s] = ((((R(1.0) + cfg_tanh((K(C_kS) * (y_u - K(C_uS))))) / R(2.0)) - y_s) / H(H_tauS));
+    dydt[S_s] = ((H(6) - y_s) / H(H_tauS));
     R a_Istim = (SOLVE_VM ? R(cfg_stimulus_current<double>(t, stim)) : R(0));
     if (SOLVE_VM) {
         dydt[S_u] = ((-a_Jion) - a_Istim);

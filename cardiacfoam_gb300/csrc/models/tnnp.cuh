@@ -406,10 +406,12 @@ __device__ __forceinline__ R rhs(double t, const YS& Y, const KS& K, R* dydt, in
 // Tissue mode (solveVmWithinODESolver false): the PDE owns the membrane
 // potential, so state 0 is the same at every RKF45 stage of a PDE step and
 // the algebraics computed from it and constants alone are too.  hoist()
-// evaluates the ones the rest of the body reads, once per cell and step,
-// into H[NH]; rhs_tissue() is the body without them, reading H(H_x) (the
-// same expressions in the same order: bitwise the values of rhs()).
-constexpr int NH = 20;
+// evaluates the ones the rest of the body reads, and the special-function
+// subexpressions of the rest that depend on state 0 and constants alone,
+// once per cell and step into H[NH]; rhs_tissue() is the body without them,
+// reading H (the same expressions in the same order: bitwise the values
+// of rhs() in FP64).
+constexpr int NH = 29;
 enum Hoisted { H_m_inf, H_tau_m, H_h_inf, H_tau_h, H_j_inf, H_tau_j, H_d_inf, H_tau_d, H_f_inf, H_tau_f, H_s_inf, H_tau_s, H_r_inf, H_tau_r, H_xr1_inf, H_tau_xr1, H_xr2_inf, H_tau_xr2, H_xs_inf, H_tau_xs };
 template <class R, class KS>
 __device__ __forceinline__ void hoist(R y_V, const KS& K, int tissue, R* H)
@@ -470,6 +472,15 @@ __device__ __forceinline__ void hoist(R y_V, const KS& K, int tissue, R* H)
     H[H_tau_xr2] = a_tau_xr2;
     H[H_xs_inf] = a_xs_inf;
     H[H_tau_xs] = a_tau_xs;
+    H[20] = ((R(1.00000) + (R(0.124500) * cfg_exp(((((-R(0.100000)) * y_V) * K(C_F)) / (K(C_R) * K(C_T)))))) + (R(0.0353000) * cfg_exp((((-y_V) * K(C_F)) / (K(C_R) * K(C_T))))));
+    H[21] = cfg_exp((((K(C_gamma_NCX) * y_V) * K(C_F)) / (K(C_R) * K(C_T))));
+    H[22] = (cfg_exp(((((K(C_gamma_NCX) - R(1.00000)) * y_V) * K(C_F)) / (K(C_R) * K(C_T)))) * cfg_ipow<3>(K(C_Na_o)));
+    H[23] = (((cfg_ipow<3>(K(C_Km_Nai)) + cfg_ipow<3>(K(C_Na_o))) * (K(C_Km_Ca) + K(C_Ca_o))) * (R(1.00000) + (K(C_K_sat) * cfg_exp(((((K(C_gamma_NCX) - R(1.00000)) * y_V) * K(C_F)) / (K(C_R) * K(C_T)))))));
+    H[24] = cfg_sqrt((K(C_K_o) / R(5.40000)));
+    H[25] = (K(C_g_Kr) * cfg_sqrt((K(C_K_o) / R(5.40000))));
+    H[26] = cfg_exp((((R(2.00000) * y_V) * K(C_F)) / (K(C_R) * K(C_T))));
+    H[27] = cfg_expm1((((R(2.00000) * y_V) * K(C_F)) / (K(C_R) * K(C_T))));
+    H[28] = (R(1.00000) + cfg_exp(((R(25.0000) - y_V) / R(5.98000))));
 }
 template <class R, class YS, class KS, class HS>
 __device__ __forceinline__ R rhs_tissue(double t, const YS& Y, const KS& K, const HS& H, R* dydt, int tissue, const CfgStimulus& stim)
@@ -512,25 +523,25 @@ __device__ __forceinline__ R rhs_tissue(double t, const YS& Y, const KS& K, cons
     R a_g_inf = ((y_Ca_i < R(0.000350000)) ? (R(1.00000) / (R(1.00000) + cfg_ipow<6>((y_Ca_i / R(0.000350000))))) : (R(1.00000) / (R(1.00000) + cfg_ipow<16>((y_Ca_i / R(0.000350000))))));
     R a_d_g = ((a_g_inf - y_g) / K(C_tau_g));
     dydt[S_g] = (((a_g_inf > y_g) && (y_V > (-R(60.0000)))) ? R(0.00000) : a_d_g);
-    R a_i_NaK = (((((K(C_P_NaK) * K(C_K_o)) / (K(C_K_o) + K(C_K_mk))) * y_Na_i) / (y_Na_i + K(C_K_mNa))) / ((R(1.00000) + (R(0.124500) * cfg_exp(((((-R(0.100000)) * y_V) * K(C_F)) / (K(C_R) * K(C_T)))))) + (R(0.0353000) * cfg_exp((((-y_V) * K(C_F)) / (K(C_R) * K(C_T)))))));
+    R a_i_NaK = (((((K(C_P_NaK) * K(C_K_o)) / (K(C_K_o) + K(C_K_mk))) * y_Na_i) / (y_Na_i + K(C_K_mNa))) / H(20));
     R a_E_Na = (((K(C_R) * K(C_T)) / K(C_F)) * cfg_log((K(C_Na_o) / y_Na_i)));
     R a_i_Na = ((((K(C_g_Na) * cfg_ipow<3>(y_m)) * y_h) * y_j) * (y_V - a_E_Na));
     R a_i_b_Na = (K(C_g_bNa) * (y_V - a_E_Na));
-    R a_i_NaCa = ((K(C_K_NaCa) * (((cfg_exp((((K(C_gamma_NCX) * y_V) * K(C_F)) / (K(C_R) * K(C_T)))) * cfg_ipow<3>(y_Na_i)) * K(C_Ca_o)) - (((cfg_exp(((((K(C_gamma_NCX) - R(1.00000)) * y_V) * K(C_F)) / (K(C_R) * K(C_T)))) * cfg_ipow<3>(K(C_Na_o))) * y_Ca_i) * K(C_alpha_NCX)))) / (((cfg_ipow<3>(K(C_Km_Nai)) + cfg_ipow<3>(K(C_Na_o))) * (K(C_Km_Ca) + K(C_Ca_o))) * (R(1.00000) + (K(C_K_sat) * cfg_exp(((((K(C_gamma_NCX) - R(1.00000)) * y_V) * K(C_F)) / (K(C_R) * K(C_T))))))));
+    R a_i_NaCa = ((K(C_K_NaCa) * (((H(21) * cfg_ipow<3>(y_Na_i)) * K(C_Ca_o)) - ((H(22) * y_Ca_i) * K(C_alpha_NCX)))) / H(23));
     dydt[S_Na_i] = (((-(((a_i_Na + a_i_b_Na) + (R(3.00000) * a_i_NaK)) + (R(3.00000) * a_i_NaCa))) * K(C_Cm)) / (K(C_V_c) * K(C_F)));
     R a_E_K = (((K(C_R) * K(C_T)) / K(C_F)) * cfg_log((K(C_K_o) / y_K_i)));
     R a_alpha_K1 = (R(0.100000) / (R(1.00000) + cfg_exp((R(0.0600000) * ((y_V - a_E_K) - R(200.000))))));
     R a_beta_K1 = (((R(3.00000) * cfg_exp((R(0.000200000) * ((y_V - a_E_K) + R(100.000))))) + (R(1.00000) * cfg_exp((R(0.100000) * ((y_V - a_E_K) - R(10.0000)))))) / (R(1.00000) + cfg_exp(((-R(0.500000)) * (y_V - a_E_K)))));
     R a_xK1_inf = (a_alpha_K1 / (a_alpha_K1 + a_beta_K1));
-    R a_i_K1 = (((K(C_g_K1) * a_xK1_inf) * cfg_sqrt((K(C_K_o) / R(5.40000)))) * (y_V - a_E_K));
+    R a_i_K1 = (((K(C_g_K1) * a_xK1_inf) * H(24)) * (y_V - a_E_K));
     R a_i_to = (((K(C_g_to) * y_r) * y_s) * (y_V - a_E_K));
-    R a_i_Kr = ((((K(C_g_Kr) * cfg_sqrt((K(C_K_o) / R(5.40000)))) * y_Xr1) * y_Xr2) * (y_V - a_E_K));
+    R a_i_Kr = (((H(25) * y_Xr1) * y_Xr2) * (y_V - a_E_K));
     R a_E_Ks = (((K(C_R) * K(C_T)) / K(C_F)) * cfg_log(((K(C_K_o) + (K(C_P_kna) * K(C_Na_o))) / (y_K_i + (K(C_P_kna) * y_Na_i)))));
     R a_i_Ks = ((K(C_g_Ks) * cfg_ipow<2>(y_Xs)) * (y_V - a_E_Ks));
-    R a_i_CaL = (((((((((K(C_g_CaL) * y_d) * y_f) * y_fCa) * R(4.00000)) * y_V) * cfg_ipow<2>(K(C_F))) / (K(C_R) * K(C_T))) * ((y_Ca_i * cfg_exp((((R(2.00000) * y_V) * K(C_F)) / (K(C_R) * K(C_T))))) - (R(0.341000) * K(C_Ca_o)))) / cfg_expm1((((R(2.00000) * y_V) * K(C_F)) / (K(C_R) * K(C_T)))));
+    R a_i_CaL = (((((((((K(C_g_CaL) * y_d) * y_f) * y_fCa) * R(4.00000)) * y_V) * cfg_ipow<2>(K(C_F))) / (K(C_R) * K(C_T))) * ((y_Ca_i * H(26)) - (R(0.341000) * K(C_Ca_o)))) / H(27));
     R a_E_Ca = ((((R(0.500000) * K(C_R)) * K(C_T)) / K(C_F)) * cfg_log((K(C_Ca_o) / y_Ca_i)));
     R a_i_b_Ca = (K(C_g_bCa) * (y_V - a_E_Ca));
-    R a_i_p_K = ((K(C_g_pK) * (y_V - a_E_K)) / (R(1.00000) + cfg_exp(((R(25.0000) - y_V) / R(5.98000)))));
+    R a_i_p_K = ((K(C_g_pK) * (y_V - a_E_K)) / H(28));
     R a_i_p_Ca = ((K(C_g_pCa) * y_Ca_i) / (y_Ca_i + K(C_K_pCa)));
     R a_Iion_cm = (((((((((((a_i_K1 + a_i_to) + a_i_Kr) + a_i_Ks) + a_i_CaL) + a_i_NaK) + a_i_Na) + a_i_b_Na) + a_i_NaCa) + a_i_b_Ca) + a_i_p_K) + a_i_p_Ca);
     R a_Istim = (SOLVE_VM ? R(cfg_stimulus_current<double>(t, stim)) : R(0));
