@@ -750,6 +750,83 @@ class PseudoECG:
     __del__ = close
 
 
+class Purkinje:
+    """ConductionSystemDomain with Monodomain1DSolver on the GPU
+    (cfg_purkinje_*, monodomain1DSolver.C:36-190): a tree of conduction
+    edges (nodeA, nodeB, length [m], conductance [S/m]) rooted at node 0, an
+    ionic model on its nodes, a root stimulus (node, start [s], duration [s],
+    intensity) and PVJ terminals (nodes and locations)."""
+
+    def __init__(self, edges, model="BuenoOrovio", tissue="epicardialCells", dt=1e-5,
+                 precision=_L.PRECISION_FP64, chi=140000.0, cm=0.01, root_stimulus=None,
+                 pvj_nodes=(), pvj_locations=(), ode=None, max_steps=10 ** 6):
+        self._lib = _L.load()
+        e = np.asarray(edges, dtype=np.float64).reshape(-1, 4)
+        self._a = np.ascontiguousarray(e[:, 0], dtype=np.int32)
+        self._b = np.ascontiguousarray(e[:, 1], dtype=np.int32)
+        self._len = np.ascontiguousarray(e[:, 2])
+        self._cond = np.ascontiguousarray(e[:, 3])
+        self.n = int(max(self._a.max(), self._b.max())) + 1
+        self._tn = np.ascontiguousarray(pvj_nodes, dtype=np.int32).reshape(-1)
+        self._tl = np.ascontiguousarray(pvj_locations, dtype=np.float64).reshape(-1, 3)
+        self.n_pvj = int(self._tn.size)
+        keep: list = []
+        d = _L.PurkinjeDesc()
+        d.ionic = ionic_desc(model, tissue, self.n, dt, False, precision,
+                             ode if ode is not None else ode_desc(max_steps=max_steps),
+                             None, None, None, keep)
+        d.n_edges = len(e)
+        d.edge_a, d.edge_b = _L.iptr(self._a), _L.iptr(self._b)
+        d.edge_length, d.edge_conductance = _L.dptr(self._len), _L.dptr(self._cond)
+        d.chi, d.cm = chi, cm
+        node, start, dur, inten = root_stimulus if root_stimulus else (0, 1e300, 0.0, 0.0)
+        d.root_node, d.root_start, d.root_duration, d.root_intensity = node, start, dur, inten
+        d.n_pvj = self.n_pvj
+        if self.n_pvj:
+            d.pvj_nodes = _L.iptr(self._tn)
+            d.pvj_locations = _L.dptr(self._tl)
+        h = C.c_void_p()
+        _L.check(self._lib.cfg_purkinje_create(C.byref(d), C.byref(h)))
+        self.h = h
+
+    def step(self, dt: float):
+        _L.check(self._lib.cfg_purkinje_step(self.h, dt))
+
+    def couple(self, tissue: "Monodomain", r_pvj: float, pvj_radius: float,
+               bidirectional=False):
+        """reactionDiffusionPvjCoupler with a monodomain context: from now on
+        the context's steps advance the network too."""
+        md, self._mesh_keep = mesh_desc(tissue.mesh, structured=False)
+        _L.check(self._lib.cfg_purkinje_couple(self.h, tissue.h, C.byref(md), r_pvj, pvj_radius,
+                                               int(bidirectional)))
+        self._tissue = tissue
+
+    def vm(self) -> np.ndarray:
+        a = np.zeros(self.n)
+        _L.check(self._lib.cfg_purkinje_get_field(self.h, _L.FIELD_VM, _L.dptr(a)))
+        return a
+
+    def iion(self) -> np.ndarray:
+        a = np.zeros(self.n)
+        _L.check(self._lib.cfg_purkinje_get_field(self.h, _L.FIELD_IION, _L.dptr(a)))
+        return a
+
+    def terminal_current(self) -> np.ndarray:
+        a = np.zeros(max(self.n_pvj, 1))
+        _L.check(self._lib.cfg_purkinje_terminal_current(self.h, _L.dptr(a)))
+        return a[:self.n_pvj]
+
+    def time(self) -> float:
+        return self._lib.cfg_purkinje_time(self.h)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self._lib.cfg_purkinje_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+
 class AdjointProblem:
     """Probe-voltage misfit of the differentiable monodomain step and its
     gradient (cfg_adjoint_*): per-cell log-scales of TNNP g_Na and g_K1 and

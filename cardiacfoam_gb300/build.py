@@ -75,6 +75,7 @@ def _units():
                  if os.environ.get(k)]
     units.append(("ecg", CSRC / "ecg.cu", ecg_extra))
     units.append(("bidomain", CSRC / "bidomain.cu", []))
+    units.append(("purkinje", CSRC / "purkinje.cu", []))
     units.append(("adjoint", CSRC / "adjoint.cu", ["--use_fast_math"]))
     return units
 

@@ -267,9 +267,14 @@ __global__ void __launch_bounds__(kCoopBlock, 1) k_implicit_coop(DiffusionArgs a
                 double g3[1];
                 grid_sums<1>(a.partial, set, g3);
                 set ^= 1;
-                const double wApA = g3[0];
-                if (fabs(wApA) / normf < 1e-300) break;   // checkSingularity
-                const double alpha = wArA / wApA;
+                // checkSingularity and alpha, once per block
+                double q3[2];
+                gsync::block_scalars<2>(q3, [&](double* v) {
+                    v[0] = fabs(g3[0]) / normf < 1e-300 ? 1.0 : 0.0;
+                    v[1] = wArA / g3[0];
+                });
+                if (q3[0] != 0.0) break;
+                const double alpha = q3[1];
                 // --- update pass: x, r, z; |r| and z.r
                 double s4[2] = {0.0, 0.0};
                 for (unsigned c = first; c < n; c += 2 * stride) {
@@ -297,7 +302,13 @@ __global__ void __launch_bounds__(kCoopBlock, 1) k_implicit_coop(DiffusionArgs a
                 double g4[2];
                 grid_sums<2>(a.partial, set, g4);
                 set ^= 1;
-                res = g4[0] / normf;
+                // the residual and beta, once per block
+                double q4[2];
+                gsync::block_scalars<2>(q4, [&](double* v) {
+                    v[0] = g4[0] / normf;
+                    v[1] = g4[1] / wArA;
+                });
+                res = q4[0];
                 ++iter;
                 ++step_iters;
                 if (conv(res) || iter >= max_iter) {
@@ -310,9 +321,8 @@ __global__ void __launch_bounds__(kCoopBlock, 1) k_implicit_coop(DiffusionArgs a
                     aborted = true;
                     break;
                 }
-                const double wArAold = wArA;
                 wArA = g4[1];
-                beta = wArA / wArAold;
+                beta = q4[1];
             }
         }
         if (lead && n_solves < kMaxSolves) {

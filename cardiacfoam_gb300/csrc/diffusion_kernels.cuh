@@ -107,6 +107,10 @@ struct DiffusionArgs {
     cudaGraphConditionalHandle h_outer, h_inner;
     long long iter_cap;        // PCG iterations per step before the step is aborted
     long long spin_limit;      // spins a block waits at a grid barrier before it aborts
+    // per-cell source density of the step when a conduction network is
+    // coupled (box stimulus plus the PVJ deposits, set before the step);
+    // null: the box stimulus alone
+    const double* src_total;
     // step constants
     double dt, chicm;
     int ddt_backward;
@@ -308,6 +312,7 @@ __device__ __forceinline__ int ddt_variant(const DiffusionArgs& a, int n_old)
 // MyocardiumDomain::updateExternalStimulusCurrent for one cell
 __device__ __forceinline__ double box_source(const DiffusionArgs& a, long long c, double t0)
 {
+    if (a.src_total) return a.src_total[c];
     double s = 0.0;
     if (!a.box_mask) return s;
     const unsigned m = a.box_mask[c];

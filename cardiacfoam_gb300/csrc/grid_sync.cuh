@@ -106,5 +106,21 @@ __device__ __forceinline__ void grid_sums(const double* partial, int set, double
     __syncthreads();
 }
 
+// K scalars derived from reduction results (ratios of sums), computed by
+// thread 0 and read by every thread of the block.  Every thread holds the
+// same sums, so every block gets the same values; doing the arithmetic once
+// per block instead of once per thread matters because an FP64 division is a
+// few tens of instructions on GB300's FP64 pipe, which the row work shares.
+template <int K, class F>
+__device__ __forceinline__ void block_scalars(double (&out)[K], F f)
+{
+    __shared__ double v[K];
+    if (threadIdx.x == 0) f(v);
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < K; ++k) out[k] = v[k];
+    __syncthreads();   // v is written again by the next call
+}
+
 }  // namespace gsync
 }  // namespace cfg

@@ -306,6 +306,7 @@ static void fill_args(cfg_monodomain* md, double dt)
     a.use_graph = 0;
     a.iter_cap = md->iter_cap;
     a.spin_limit = md->spin_limit;
+    a.src_total = md->d_src_total;
     // ddt coefficients (EulerDdtScheme; backwardDdtScheme with deltaT0 =
     // GREAT while fewer than two old-time levels exist, then deltaT0 = dt)
     a.rdt = 1.0 / dt;
@@ -589,6 +590,66 @@ __global__ void k_apd_results(long long n, const ApdTracker* apd, ApdParams P, i
     t_up[c] = a.last_t_up;
 }
 
+namespace cfg {
+
+// The tissue's source density of a coupled step: the box stimulus
+// (MyocardiumDomain::updateExternalStimulusCurrent) then each deposit of the
+// PVJ coupling in terminal order (PVJMapper::depositCoupling).
+struct BoxSrc {
+    const unsigned char* mask;
+    int n_boxes;
+    double start[8], end[8], intensity[8];
+};
+
+__global__ void k_src_total(long long n, BoxSrc b, double t0, const int* dep_off,
+                            const int* dep_term, const double* dep_value, double* src)
+{
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    double s = 0.0;
+    if (b.mask) {
+        const unsigned m = b.mask[c];
+        for (int k = 0; k < b.n_boxes; ++k) {
+            if (t0 < b.start[k] || t0 > b.end[k]) continue;
+            if (m & (1u << k)) s += b.intensity[k];
+        }
+    }
+    for (int k = dep_off[c]; k < dep_off[c + 1]; ++k) s += dep_value[dep_term[k]];
+    src[c] = s;
+}
+
+int monodomain_source_total(cfg_monodomain* md, double t0, const int* dep_off,
+                            const int* dep_term, const double* dep_value, double* src_total)
+{
+    BoxSrc b{};
+    b.mask = md->d_box;
+    b.n_boxes = md->n_boxes;
+    for (int k = 0; k < md->n_boxes; ++k) {
+        b.start[k] = md->box_start[k];
+        b.end[k] = md->box_start[k] + md->box_duration[k];
+        b.intensity[k] = md->box_intensity[k];
+    }
+    k_src_total<<<unsigned((md->n + 255) / 256), 256, 0, md->stream>>>(md->n, b, t0, dep_off,
+                                                                      dep_term, dep_value,
+                                                                      src_total);
+    CFG_CUDA_TRY(cudaGetLastError());
+    return CFG_OK;
+}
+
+int monodomain_attach_network(cfg_monodomain* md, cfg_purkinje* pk, double* src_total)
+{
+    if (md->graph_exec) {   // the source pointer is an argument of the captured kernels
+        cudaGraphExecDestroy(md->graph_exec);
+        md->graph_exec = nullptr;
+    }
+    md->pk = pk;
+    md->d_src_total = src_total;
+    md->prepared_dt = 0.0;  // refill the launch arguments at the next step
+    return CFG_OK;
+}
+
+}  // namespace cfg
+
 static int apd_after_step(cfg_monodomain* md)
 {
     if (md->apd_every <= 0) return CFG_OK;
@@ -709,12 +770,15 @@ int cfg_monodomain_step(cfg_monodomain* md, double dt)
     if (!md) return fail(CFG_ERR_INVALID, "null context");
     if (dt == 0.0) dt = md->delta_t;   // the context's own time step
     if (!(dt > 0)) return fail(CFG_ERR_INVALID, "deltaT must be positive");
+    if (md->pk)
+        if (int rc = purkinje_prepare_coupled_step(md->pk, md, md->t_host, dt)) return rc;
     int rc = md->use_graph ? enqueue_graph_step(md, dt) : enqueue_step(md, dt, true);
     if (rc) return rc;
     md->t_host = md->t_host + dt;
     md->steps++;
     if ((rc = apd_after_step(md))) return rc;
     rc = check_step(md);
+    if (!rc && md->pk) rc = purkinje_check(md->pk);
     if (!rc && md->use_graph && md->timing) md->timed_launches += graph_step_launches(md);
     return rc;
 }
@@ -732,13 +796,18 @@ int cfg_monodomain_run(cfg_monodomain* md, double dt, long long n_steps)
         return CFG_OK;
     }
     for (long long i = 0; i < n_steps; ++i) {
+        if (md->pk)
+            if (int rc = purkinje_prepare_coupled_step(md->pk, md, md->t_host, dt)) return rc;
         int rc = enqueue_graph_step(md, dt);
         if (rc) return rc;
         md->t_host = md->t_host + dt;
         md->steps++;
         if ((rc = apd_after_step(md))) return rc;
     }
-    return n_steps > 0 ? check_step(md) : CFG_OK;
+    if (n_steps <= 0) return CFG_OK;
+    int rc = check_step(md);
+    if (!rc && md->pk) rc = purkinje_check(md->pk);
+    return rc;
 }
 
 int cfg_monodomain_set_graph(cfg_monodomain* md, int enable)
@@ -913,6 +982,7 @@ int cfg_monodomain_destroy(cfg_monodomain* md)
 {
     if (md) {
         cudaStreamSynchronize(md->stream);
+        if (md->pk) purkinje_detach(md->pk);   // the network may outlive the context
         md_free(md);
     }
     return CFG_OK;

@@ -8,6 +8,8 @@
 #include "grid_sync.cuh"
 #include "host_common.h"
 
+struct cfg_purkinje;
+
 struct cfg_monodomain {
     cfg_ionic* ion = nullptr;
     long long n = 0;
@@ -79,6 +81,11 @@ struct cfg_monodomain {
     // dt = 0), and the explicit algorithm's Courant limit at maxCo = 1
     double delta_t = 0.0;
     double explicit_dt_unit = -1.0;
+    // a coupled conduction network (cfg_purkinje_couple): its step runs
+    // before the myocardium's, and the tissue's source of the step is
+    // d_src_total (the network's buffer)
+    cfg_purkinje* pk = nullptr;
+    double* d_src_total = nullptr;
     // phase timing
     bool timing = false;
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
@@ -95,4 +102,11 @@ int build_step_graph(cfg_monodomain* md, double dt);
 void fill_args_public(cfg_monodomain* md, double dt);
 int coop_grid_blocks(long long n);
 cudaError_t launch_implicit_coop(const DiffusionArgs& a, int blocks, cudaStream_t s);
+// coupling of a conduction network (csrc/purkinje.cu)
+int monodomain_attach_network(cfg_monodomain* md, cfg_purkinje* pk, double* src_total);
+int monodomain_source_total(cfg_monodomain* md, double t0, const int* dep_off,
+                            const int* dep_term, const double* dep_value, double* src_total);
+int purkinje_prepare_coupled_step(cfg_purkinje* pk, cfg_monodomain* md, double t0, double dt);
+int purkinje_check(cfg_purkinje* pk);
+void purkinje_detach(cfg_purkinje* pk);
 }  // namespace cfg

@@ -143,3 +143,79 @@ def write_pseudo_ecg(case_dir, names: Sequence[str], times: Sequence[float], val
         for t, row in zip(times, v):
             fh.write(ecg_row(float(t), row))
     return path
+
+
+def read_purkinje_graph(text: str) -> dict:
+    """The conduction graph file a purkinjeGraphModel names (graphFile, read by
+    conductionSystemDomain.C:100-165 and conductionGraph::readFromDict):
+    ``rootNode``, ``pvjNodes N(...)``, ``pvjLocations N((x y z) ...)`` and
+    ``conductionEdges N(4(a b length conductance) ...)`` in OpenFOAM list
+    syntax (the size prefixes are optional).  Returns edges [n][4], root,
+    pvj_nodes and pvj_locations [n][3]."""
+    import re
+    body = re.sub(r"/\*.*?\*/", " ", text, flags=re.S)
+    body = re.sub(r"//[^\n]*", " ", body)
+    body = re.sub(r"FoamFile\s*\{[^}]*\}", " ", body)
+
+    def entry(key):
+        m = re.search(r"\b" + key + r"\b\s*(.*?);", body, flags=re.S)
+        if not m:
+            raise ValueError(f"keyword {key} is undefined")
+        return m.group(1)
+
+    def numbers(s):
+        # drop OpenFOAM list-size prefixes: an integer directly before "("
+        s = re.sub(r"\b\d+\s*\(", "(", s)
+        return [float(v) for v in re.findall(r"[-+]?(?:\d+\.?\d*|\.\d+)(?:[eE][-+]?\d+)?", s)]
+
+    out = {"root": int(numbers(entry("rootNode"))[0]) if re.search(r"\brootNode\b", body) else 0}
+    e = numbers(entry("conductionEdges"))
+    if len(e) % 4:
+        raise ValueError("each entry in 'conductionEdges' must have 4 values: "
+                         "(nodeA nodeB length conductance)")
+    out["edges"] = np.array(e, dtype=np.float64).reshape(-1, 4)
+    if re.search(r"\bpvjNodes\b", body):
+        out["pvj_nodes"] = np.array(numbers(entry("pvjNodes")), dtype=np.int64)
+        loc = numbers(entry("pvjLocations"))
+        out["pvj_locations"] = np.array(loc, dtype=np.float64).reshape(-1, 3)
+        if len(out["pvj_locations"]) != len(out["pvj_nodes"]):
+            raise ValueError("pvjNodes and pvjLocations differ in length")
+    else:
+        out["pvj_nodes"] = np.zeros(0, dtype=np.int64)
+        out["pvj_locations"] = np.zeros((0, 3))
+    return out
+
+
+def synthetic_purkinje_tree(depth: int, segment: int, h: float, origin=(0.0, 0.0, 0.0),
+                            spread=(1.0, 0.0, 0.0), conductance: float = 1.0, seed: int = 0):
+    """A binary branching network for tests and benchmarks: a trunk of
+    `segment` edges of length h from node 0, then at every branch point two
+    branches of `segment` edges, `depth` generations deep; branches turn by a
+    seeded angle in the x-y plane.  Returns (edges [n][4], node positions
+    [n][3], leaf nodes)."""
+    rng = np.random.default_rng(seed)
+    pos = [np.array(origin, dtype=np.float64)]
+    edges = []
+    d0 = np.array(spread, dtype=np.float64)
+    d0 /= np.linalg.norm(d0)
+
+    def grow(start, direction, k):
+        prev = start
+        for _ in range(k):
+            pos.append(pos[prev] + h * direction)
+            edges.append((prev, len(pos) - 1, h, conductance))
+            prev = len(pos) - 1
+        return prev
+
+    tips = [(grow(0, d0, segment), d0)]
+    for _ in range(depth):
+        nxt = []
+        for node, d in tips:
+            for sgn in (-1.0, 1.0):
+                a = sgn * rng.uniform(0.3, 0.8)
+                rot = np.array([[np.cos(a), -np.sin(a), 0.0], [np.sin(a), np.cos(a), 0.0],
+                                [0.0, 0.0, 1.0]])
+                nd = rot @ d
+                nxt.append((grow(node, nd, segment), nd))
+        tips = nxt
+    return np.array(edges, dtype=np.float64), np.array(pos), np.array([t for t, _ in tips])

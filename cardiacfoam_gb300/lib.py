@@ -137,6 +137,14 @@ class BidomainDesc(C.Structure):
                 ("explicit_algorithm", C.c_int)]
 
 
+class PurkinjeDesc(C.Structure):
+    _fields_ = [("ionic", IonicDesc), ("n_edges", C.c_longlong), ("edge_a", _ip), ("edge_b", _ip),
+                ("edge_length", _dp), ("edge_conductance", _dp), ("chi", C.c_double),
+                ("cm", C.c_double), ("root_node", C.c_int), ("root_start", C.c_double),
+                ("root_duration", C.c_double), ("root_intensity", C.c_double),
+                ("n_pvj", C.c_int), ("pvj_nodes", _ip), ("pvj_locations", _dp)]
+
+
 class PseudoEcgDesc(C.Structure):
     _fields_ = [("conductivity", C.c_double * 6), ("conductivity_per_cell", _dp),
                 ("grad_scheme", C.c_int), ("n_electrodes", C.c_int), ("electrodes", _dp),
@@ -155,6 +163,9 @@ EXPORTS = [
     "cfg_monodomain_set_persistent", "cfg_monodomain_suggest_explicit_delta_t",
     "cfg_monodomain_delta_t", "cfg_monodomain_set_delta_t", "cfg_monodomain_set_wait_limit",
     "cfg_pseudo_ecg_set_wait_limit", "cfg_monodomain_track_apd", "cfg_monodomain_apd_results",
+    "cfg_purkinje_create", "cfg_purkinje_step", "cfg_purkinje_couple", "cfg_purkinje_get_field",
+    "cfg_purkinje_terminal_current", "cfg_purkinje_nodes", "cfg_purkinje_time",
+    "cfg_purkinje_destroy",
     "cfg_batch_create", "cfg_batch_run", "cfg_batch_results",
     "cfg_batch_trace", "cfg_batch_get_states", "cfg_batch_stats", "cfg_batch_stream",
     "cfg_batch_destroy", "cfg_adjoint_create", "cfg_adjoint_set_target", "cfg_adjoint_forward",
@@ -224,6 +235,17 @@ def load(path: Optional[os.PathLike] = None):
     L.cfg_monodomain_set_delta_t.argtypes = [C.c_void_p, C.c_double]
     L.cfg_monodomain_set_wait_limit.argtypes = [C.c_void_p, C.c_longlong]
     L.cfg_monodomain_track_apd.argtypes = [C.c_void_p, C.c_int]
+    L.cfg_purkinje_create.argtypes = [C.POINTER(PurkinjeDesc), C.POINTER(C.c_void_p)]
+    L.cfg_purkinje_step.argtypes = [C.c_void_p, C.c_double]
+    L.cfg_purkinje_couple.argtypes = [C.c_void_p, C.c_void_p, C.POINTER(MeshDesc), C.c_double,
+                                      C.c_double, C.c_int]
+    L.cfg_purkinje_get_field.argtypes = [C.c_void_p, C.c_int, _dp]
+    L.cfg_purkinje_terminal_current.argtypes = [C.c_void_p, _dp]
+    L.cfg_purkinje_nodes.argtypes = [C.c_void_p]
+    L.cfg_purkinje_nodes.restype = C.c_longlong
+    L.cfg_purkinje_time.argtypes = [C.c_void_p]
+    L.cfg_purkinje_time.restype = C.c_double
+    L.cfg_purkinje_destroy.argtypes = [C.c_void_p]
     L.cfg_monodomain_apd_results.argtypes = [C.c_void_p, C.c_void_p, _dp, _dp]
     L.cfg_pseudo_ecg_set_wait_limit.argtypes = [C.c_void_p, C.c_longlong]
     L.cfg_batch_create.argtypes = [C.POINTER(BatchDesc), C.POINTER(C.c_void_p)]

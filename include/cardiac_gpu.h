@@ -579,6 +579,65 @@ int cfg_pseudo_ecg_electrodes_from_dict(const char* electro_properties, const ch
                                         char* names, size_t len, double* positions, int max,
                                         int* n_electrodes);
 
+/* ------------------------------------------------- Purkinje network
+ * ConductionSystemDomain with the Monodomain1DSolver
+ * (src/electroModels/conductionSystemModels/monodomain1DSolver/
+ * monodomain1DSolver.C:36-190; conductionSystemDomain.C, conductionGraph.H):
+ * a tree of nodes joined by edges of given length and conductance
+ * (conductionEdges (nodeA nodeB length conductance) of the graph file), node 0
+ * the root, Strang-split steps (ionic model over dt/2, the implicit cable step
+ * solved exactly by Hines elimination, ionic model over dt/2), a root
+ * stimulus (rootStimulus: node, startTime, duration, intensity; applied while
+ * startTime <= t0 <= startTime + duration) and terminals (pvjNodes,
+ * pvjLocations) where the network meets the tissue.  The ionic description's
+ * n_cells is the node count (largest node index + 1) and its
+ * solve_vm_within_ode 0; nodes start at the model's resting Vm
+ * (ionicModel::vmRest). */
+typedef struct cfg_purkinje_desc {
+    cfg_ionic_desc ionic;
+    long long n_edges;                 /* the nodes - 1 of a tree */
+    const int* edge_a;                 /* [n_edges] */
+    const int* edge_b;
+    const double* edge_length;         /* [m] */
+    const double* edge_conductance;    /* [S/m] */
+    double chi, cm;
+    int root_node;
+    double root_start, root_duration, root_intensity;   /* start 1e300: no stimulus */
+    int n_pvj;
+    const int* pvj_nodes;              /* [n_pvj] */
+    const double* pvj_locations;       /* [n_pvj][3] */
+} cfg_purkinje_desc;
+
+typedef struct cfg_purkinje cfg_purkinje;
+
+int cfg_purkinje_create(const cfg_purkinje_desc* desc, cfg_purkinje** out);
+/* One step of the network alone, Monodomain1DSolver::advance(t, dt), t then
+ * advanced by dt (CFG_ERR_INVALID once the network is coupled). */
+int cfg_purkinje_step(cfg_purkinje* pk, double dt);
+/* ReactionDiffusionPvjCoupler between the network and a monodomain context
+ * (reactionDiffusionPvjCoupler.C:36-164, pvjMapper.C): rPvj, pvjRadius and
+ * couplingMode (bidirectional 1, unidirectional 0).  Each terminal maps to
+ * the cell holding it (here the nearest cell centre, the first on ties) and
+ * to the cells whose centres lie within pvjRadius (or that cell alone);
+ * pvjRadius below the cube root of that cell's volume is rejected.  From
+ * then on every cfg_monodomain_step / _run of the context runs the
+ * staggered scheme's coupled step: the terminals' currents (Vnet -
+ * Vtissue)/rPvj, the network's step with them as negative applied currents
+ * (zero in unidirectional mode), the currents again from the new network
+ * Vm, deposited as current/sphere volume into the tissue's source on top of
+ * the box stimulus, then the myocardium's step.  `mesh` is the context's
+ * mesh (centres and volumes are read). */
+int cfg_purkinje_couple(cfg_purkinje* pk, cfg_monodomain* md, const cfg_mesh_desc* mesh,
+                        double r_pvj, double pvj_radius, int bidirectional);
+/* CFG_FIELD_VM [V] or CFG_FIELD_IION of the nodes (host, n nodes). */
+int cfg_purkinje_get_field(cfg_purkinje* pk, int field, double* host);
+/* The terminals' coupling currents of the last evaluation (host, n_pvj). */
+int cfg_purkinje_terminal_current(cfg_purkinje* pk, double* host);
+long long cfg_purkinje_nodes(const cfg_purkinje* pk);
+double cfg_purkinje_time(const cfg_purkinje* pk);
+/* Detaches from the coupled context, then frees the network. */
+int cfg_purkinje_destroy(cfg_purkinje* pk);
+
 /* ------------------------------------ diffusion solve without allocation
  * No counterpart in the reference.  For callers that cannot call cudaMalloc
  * when they need a solve (a host application that owns all device memory

@@ -587,6 +587,13 @@ struct oracle_tissue {
     /* general mesh: gaussLaplacianScheme with corrected snGrad */
     int corrected_mesh; /* face centres given: explicit corrections are on */
     const double* extra_src;  /* bidomain: V fvc::div(Gi & grad(phiE)) added to the source */
+    /* PVJ coupling (reactionDiffusionPvjCoupler): per step, source densities
+     * deposited after the box stimulus, pair k adding dep_value[dep_term[k]]
+     * to cell dep_cell[k], in pair order */
+    long n_dep;
+    const long* dep_cell;
+    const long* dep_term;
+    const double* dep_value;
     double *w, *dcoef, *corrv, *sfgsn, *sfgcorr, *bsfgcorr, *bn, *lsp, *lsn, *grad, *fflux;
     /* PCG work */
     double *diag, *upper, *b, *rA, *wA, *pA, *rD, *tmp;
@@ -1044,6 +1051,9 @@ static void update_stimulus(oracle_tissue* T, double t0)
                 T->src[c] += T->d.box_intensity[b];
         }
     }
+    /* PVJMapper::depositCoupling (pvjMapper.C) on top of the box stimulus */
+    if (T->dep_value)
+        for (long k = 0; k < T->n_dep; k++) T->src[T->dep_cell[k]] += T->dep_value[T->dep_term[k]];
 }
 
 /* ddt coefficients (EulerDdtScheme / backwardDdtScheme); backward uses
@@ -1606,4 +1616,306 @@ long oracle_single_cell_traces(int model, int tissue, double dt, long n_steps,
     if (final_states) memcpy(final_states, io->y, sizeof(double) * (size_t)m->ns);
     oracle_ionic_free(io);
     return total;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Purkinje network                                                          */
+
+/* ConductionSystemDomain with Monodomain1DSolver
+ * (src/electroModels/electroDomains/conductionSystemDomain/conductionSystemDomain.C,
+ * conductionGraph.H; src/electroModels/conductionSystemModels/monodomain1DSolver/
+ * monodomain1DSolver.C:36-190) and the reaction-diffusion PVJ coupling
+ * (electroCouplers/pvjCoupler/reactionDiffusion/reactionDiffusionPvjCoupler.C:36-164,
+ * pvjMapper.C), restated.  The graph is a tree rooted at node 0: BFS order
+ * over adjacency lists built in edge order, parent links, reverse BFS order
+ * for the elimination. */
+struct oracle_purkinje {
+    long n, ne;
+    int *ea, *eb;
+    double *elen, *econd;
+    int *parent, *order, *rev;
+    double chi, cm;
+    oracle_ionic* ionic;
+    double *vm, *iion, *app;
+    double *diag, *rhs, *pc, *cc, *clen;
+    int root;
+    double root_start, root_dur, root_int;
+    long n_term;
+    int* term_node;
+    double* term_loc;
+    double* term_current;     /* setTerminalCoupling's current [(V)/R] */
+    /* coupling */
+    int coupled, mode;        /* mode 0: unidirectional, 1: bidirectional */
+    double r_pvj, radius;
+    long* term_cell;
+    long n_dep;
+    long *dep_cell, *dep_term;
+    double *sphere_vol, *dep_value, *tissue_vm_buf, *net_vm_buf;
+};
+
+oracle_purkinje* oracle_purkinje_new(long n_edges, const int* ea, const int* eb, const double* len,
+                                     const double* cond, int model, int tissue,
+                                     const oracle_ode_settings* ode, double initial_dt,
+                                     double chi, double cm, int root, double root_start,
+                                     double root_dur, double root_int, long n_term,
+                                     const int* term_node, const double* term_loc)
+{
+    int maxn = 0;
+    for (long e = 0; e < n_edges; e++) {
+        if (ea[e] < 0 || eb[e] < 0) return NULL;
+        if (ea[e] > maxn) maxn = ea[e];
+        if (eb[e] > maxn) maxn = eb[e];
+    }
+    const long n = (long)maxn + 1;
+    if (n < 1 || n_edges != n - 1) return NULL;   /* a tree: N - 1 edges */
+    oracle_purkinje* P = (oracle_purkinje*)calloc(1, sizeof(oracle_purkinje));
+    P->n = n;
+    P->ne = n_edges;
+    P->ea = (int*)malloc(sizeof(int) * (size_t)n_edges);
+    P->eb = (int*)malloc(sizeof(int) * (size_t)n_edges);
+    P->elen = (double*)malloc(sizeof(double) * (size_t)n_edges);
+    P->econd = (double*)malloc(sizeof(double) * (size_t)n_edges);
+    memcpy(P->ea, ea, sizeof(int) * (size_t)n_edges);
+    memcpy(P->eb, eb, sizeof(int) * (size_t)n_edges);
+    memcpy(P->elen, len, sizeof(double) * (size_t)n_edges);
+    memcpy(P->econd, cond, sizeof(double) * (size_t)n_edges);
+    /* adjacency in edge order (conductionGraph::buildTreeTopology) */
+    int* deg = (int*)calloc((size_t)n + 1, sizeof(int));
+    for (long e = 0; e < n_edges; e++) { deg[ea[e] + 1]++; deg[eb[e] + 1]++; }
+    for (long i = 0; i < n; i++) deg[i + 1] += deg[i];
+    int* adj = (int*)malloc(sizeof(int) * (size_t)(2 * n_edges + 1));
+    int* fill = (int*)calloc((size_t)n_edges + 1, sizeof(int));
+    for (long e = 0; e < n_edges; e++) {
+        adj[deg[ea[e]] + fill[ea[e]]++] = eb[e];
+        adj[deg[eb[e]] + fill[eb[e]]++] = ea[e];
+    }
+    P->parent = (int*)malloc(sizeof(int) * (size_t)n);
+    P->order = (int*)malloc(sizeof(int) * (size_t)n);
+    P->rev = (int*)malloc(sizeof(int) * (size_t)n);
+    unsigned char* seen = (unsigned char*)calloc((size_t)n, 1);
+    for (long i = 0; i < n; i++) P->parent[i] = -1;
+    long head = 0, tail = 0;
+    P->order[tail++] = 0;
+    seen[0] = 1;
+    while (head < tail) {
+        const int v = P->order[head++];
+        for (int k = deg[v]; k < deg[v + 1]; k++) {
+            const int w = adj[k];
+            if (!seen[w]) { seen[w] = 1; P->parent[w] = v; P->order[tail++] = w; }
+        }
+    }
+    free(deg); free(adj); free(fill); free(seen);
+    if (tail != n) { oracle_purkinje_free(P); return NULL; }   /* not connected */
+    for (long i = 0; i < n; i++) P->rev[i] = P->order[n - 1 - i];
+    P->chi = chi;
+    P->cm = cm;
+    P->ionic = oracle_ionic_new(model, n, tissue, initial_dt, 0, ode, NULL, NULL);
+    if (!P->ionic) { oracle_purkinje_free(P); return NULL; }
+    P->vm = (double*)malloc(sizeof(double) * (size_t)n);
+    P->iion = (double*)calloc((size_t)n, sizeof(double));
+    P->app = (double*)calloc((size_t)n, sizeof(double));
+    P->diag = (double*)malloc(sizeof(double) * (size_t)n);
+    P->rhs = (double*)malloc(sizeof(double) * (size_t)n);
+    P->pc = (double*)malloc(sizeof(double) * (size_t)n);
+    P->cc = (double*)malloc(sizeof(double) * (size_t)n);
+    P->clen = (double*)malloc(sizeof(double) * (size_t)n);
+    /* ionicModel::vmRest: the model's state 0 in V */
+    {
+        const double u = P->ionic->y[0];
+        const int map = P->ionic->m->vm_map;
+        const double mv = map == 1 ? u * 100 - 80 : map == 2 ? u * 85.7 - 84.0 : u;
+        const double v = map == 3 ? u : mv * 1e-3;
+        for (long i = 0; i < n; i++) P->vm[i] = v;
+    }
+    P->root = root;
+    P->root_start = root_start;
+    P->root_dur = root_dur;
+    P->root_int = root_int;
+    P->n_term = n_term;
+    P->term_node = (int*)malloc(sizeof(int) * (size_t)(n_term + 1));
+    P->term_loc = (double*)malloc(sizeof(double) * 3 * (size_t)(n_term + 1));
+    P->term_current = (double*)calloc((size_t)n_term + 1, sizeof(double));
+    if (n_term) {
+        memcpy(P->term_node, term_node, sizeof(int) * (size_t)n_term);
+        memcpy(P->term_loc, term_loc, sizeof(double) * 3 * (size_t)n_term);
+    }
+    return P;
+}
+
+void oracle_purkinje_free(oracle_purkinje* P)
+{
+    if (!P) return;
+    free(P->ea); free(P->eb); free(P->elen); free(P->econd);
+    free(P->parent); free(P->order); free(P->rev);
+    if (P->ionic) oracle_ionic_free(P->ionic);
+    free(P->vm); free(P->iion); free(P->app);
+    free(P->diag); free(P->rhs); free(P->pc); free(P->cc); free(P->clen);
+    free(P->term_node); free(P->term_loc); free(P->term_current);
+    free(P->term_cell); free(P->dep_cell); free(P->dep_term); free(P->sphere_vol);
+    free(P->dep_value); free(P->tissue_vm_buf); free(P->net_vm_buf);
+    free(P);
+}
+
+double* oracle_purkinje_vm(oracle_purkinje* P) { return P->vm; }
+double* oracle_purkinje_iion(oracle_purkinje* P) { return P->iion; }
+double* oracle_purkinje_terminal_current(oracle_purkinje* P) { return P->term_current; }
+long oracle_purkinje_nodes(oracle_purkinje* P) { return P->n; }
+const int* oracle_purkinje_order(oracle_purkinje* P) { return P->order; }
+const int* oracle_purkinje_parent(oracle_purkinje* P) { return P->parent; }
+
+/* Monodomain1DSolver::advance (monodomain1DSolver.C:36-190): half ionic step,
+ * the applied current, the implicit cable step by Hines elimination over the
+ * tree, the second half ionic step. */
+int oracle_purkinje_advance(oracle_purkinje* P, double t0, double dt, int nthreads)
+{
+    const long n = P->n;
+    if (oracle_ionic_solve(P->ionic, t0, dt / 2.0, P->vm, P->iion, nthreads) < 0) return -1;
+    /* ConductionSystemDomain::assembleAppliedCurrent */
+    for (long i = 0; i < n; i++) P->app[i] = 0.0;
+    if (t0 >= P->root_start && t0 <= (P->root_start + P->root_dur)) P->app[P->root] += P->root_int;
+    for (long i = 0; i < P->n_term; i++) P->app[P->term_node[i]] -= P->term_current[i];
+    const double chiCm = P->chi * P->cm;
+    for (long i = 0; i < n; i++) {
+        P->diag[i] = 1.0;
+        P->rhs[i] = 0.0;
+        P->pc[i] = 0.0;
+        P->cc[i] = 0.0;
+        P->clen[i] = 0.0;
+    }
+    for (long e = 0; e < P->ne; e++) {
+        P->clen[P->ea[e]] += 0.5 * P->elen[e];
+        P->clen[P->eb[e]] += 0.5 * P->elen[e];
+    }
+    for (long i = 0; i < n; i++)
+        if (P->clen[i] <= 1e-15) return -2;       /* zero control length */
+    for (long e = 0; e < P->ne; e++) {
+        const int a = P->ea[e], b = P->eb[e];
+        const double edgeCoeff = P->econd[e] / P->elen[e];
+        const double coeffA = dt * edgeCoeff / (chiCm * P->clen[a]);
+        const double coeffB = dt * edgeCoeff / (chiCm * P->clen[b]);
+        P->diag[a] += coeffA;
+        P->diag[b] += coeffB;
+        if (P->parent[a] == b) { P->pc[a] = -coeffA; P->cc[a] = -coeffB; }
+        else if (P->parent[b] == a) { P->pc[b] = -coeffB; P->cc[b] = -coeffA; }
+        else return -3;
+    }
+    for (long i = 0; i < n; i++)
+        P->rhs[i] = P->vm[i] - dt * P->iion[i] + dt * P->app[i] / chiCm;
+    for (long i = 0; i < n - 1; i++) {
+        const int c = P->rev[i], p = P->parent[c];
+        const double factor = P->cc[c] / P->diag[c];
+        P->diag[p] -= factor * P->pc[c];
+        P->rhs[p] -= factor * P->rhs[c];
+    }
+    const int root = P->order[0];
+    P->vm[root] = P->rhs[root] / P->diag[root];
+    for (long i = 1; i < n; i++) {
+        const int c = P->order[i], p = P->parent[c];
+        P->vm[c] = (P->rhs[c] - P->pc[c] * P->vm[p]) / P->diag[c];
+    }
+    if (oracle_ionic_solve(P->ionic, t0 + (dt / 2.0), dt / 2.0, P->vm, P->iion, nthreads) < 0)
+        return -1;
+    return 0;
+}
+
+/* PVJMapper (pvjMapper.C) on the tissue mesh: per terminal the cell holding
+ * the location (the nearest centre here; the first on ties), the cells whose
+ * centres lie within pvjRadius and their volume. */
+int oracle_purkinje_couple(oracle_purkinje* P, const oracle_mesh* M, double r_pvj, double radius,
+                           int mode)
+{
+    const long nt = P->n_term;
+    P->coupled = 1;
+    P->mode = mode;
+    P->r_pvj = r_pvj;
+    P->radius = radius;
+    P->term_cell = (long*)malloc(sizeof(long) * (size_t)(nt + 1));
+    P->sphere_vol = (double*)calloc((size_t)nt + 1, sizeof(double));
+    P->dep_value = (double*)calloc((size_t)nt + 1, sizeof(double));
+    P->tissue_vm_buf = (double*)calloc((size_t)nt + 1, sizeof(double));
+    P->net_vm_buf = (double*)calloc((size_t)nt + 1, sizeof(double));
+    long cap = 16, nd = 0;
+    P->dep_cell = (long*)malloc(sizeof(long) * (size_t)cap);
+    P->dep_term = (long*)malloc(sizeof(long) * (size_t)cap);
+    for (long i = 0; i < nt; i++) {
+        const double* x = P->term_loc + 3 * i;
+        long best = -1;
+        double bd = 1e300;
+        for (long c = 0; c < M->n; c++) {
+            const double* C = M->centres + 3 * c;
+            const double d[3] = {C[0] - x[0], C[1] - x[1], C[2] - x[2]};
+            const double dist = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+            if (dist < bd) { bd = dist; best = c; }
+        }
+        if (best < 0) return -1;
+        if (radius < cbrt(M->vol[best])) return -2;    /* pvjRadius below the cell size */
+        P->term_cell[i] = best;
+        for (long c = 0; c < M->n; c++) {
+            const double* C = M->centres + 3 * c;
+            const double d[3] = {C[0] - x[0], C[1] - x[1], C[2] - x[2]};
+            if (sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]) <= radius) {
+                if (nd == cap) {
+                    cap *= 2;
+                    P->dep_cell = (long*)realloc(P->dep_cell, sizeof(long) * (size_t)cap);
+                    P->dep_term = (long*)realloc(P->dep_term, sizeof(long) * (size_t)cap);
+                }
+                P->dep_cell[nd] = c;
+                P->dep_term[nd] = i;
+                nd++;
+                P->sphere_vol[i] += M->vol[c];
+            }
+        }
+        if (P->sphere_vol[i] <= 1e-15) {
+            /* no centre within the radius: the nearest cell alone */
+            if (nd == cap) {
+                cap *= 2;
+                P->dep_cell = (long*)realloc(P->dep_cell, sizeof(long) * (size_t)cap);
+                P->dep_term = (long*)realloc(P->dep_term, sizeof(long) * (size_t)cap);
+            }
+            P->dep_cell[nd] = best;
+            P->dep_term[nd] = i;
+            nd++;
+            P->sphere_vol[i] = M->vol[best];
+        }
+    }
+    P->n_dep = nd;
+    return 0;
+}
+
+/* ReactionDiffusionPvjCoupler::evaluateCoupling: I = (Vnet - Vtissue)/R_pvj
+ * per terminal, and its volumetric source I/sphereVolume. */
+static void pvj_evaluate(oracle_purkinje* P, const double* tissue_vm)
+{
+    for (long i = 0; i < P->n_term; i++) {
+        P->tissue_vm_buf[i] = tissue_vm[P->term_cell[i]];
+        P->net_vm_buf[i] = P->vm[P->term_node[i]];
+        const double I = (P->net_vm_buf[i] - P->tissue_vm_buf[i]) / P->r_pvj;
+        P->term_current[i] = I;
+        P->dep_value[i] = I / P->sphere_vol[i];
+    }
+}
+
+/* staggeredElectrophysicsAdvanceScheme::advance with one conduction network
+ * coupled to the myocardium: prepareTimeStep (box stimulus, inside the tissue
+ * step), prepareSecondaryCoupling, the network's advance,
+ * preparePrimaryCoupling (deposit into the source), the myocardium's advance. */
+int oracle_purkinje_coupled_step(oracle_purkinje* P, oracle_tissue* T, double dt, int nthreads)
+{
+    if (oracle_tissue_init_ionic(T, dt)) return -1;
+    const double t0 = T->t;
+    /* prepareSecondaryCoupling */
+    pvj_evaluate(P, T->vm);
+    if (P->mode == 0)
+        for (long i = 0; i < P->n_term; i++) P->term_current[i] = 0.0;
+    if (oracle_purkinje_advance(P, t0, dt, nthreads) < 0) return -1;
+    /* preparePrimaryCoupling: the new network Vm, deposited with the tissue's
+     * stimulus; the network keeps these currents */
+    pvj_evaluate(P, T->vm);
+    T->n_dep = P->n_dep;
+    T->dep_cell = P->dep_cell;
+    T->dep_term = P->dep_term;
+    T->dep_value = P->dep_value;
+    const int rc = oracle_tissue_step(T, dt, nthreads);
+    T->dep_value = NULL;
+    return rc;
 }

@@ -167,6 +167,27 @@ long oracle_single_cell_traces(int model, int tissue, double dt, long n_steps,
                                const double* scales, double* vm_trace, int state_b,
                                double* b_trace, double* final_states);
 
+/* --- Purkinje network (ConductionSystemDomain + Monodomain1DSolver) and
+ * the reaction-diffusion PVJ coupling ------------------------------------ */
+typedef struct oracle_purkinje oracle_purkinje;
+oracle_purkinje* oracle_purkinje_new(long n_edges, const int* ea, const int* eb, const double* len,
+                                     const double* cond, int model, int tissue,
+                                     const oracle_ode_settings* ode, double initial_dt,
+                                     double chi, double cm, int root, double root_start,
+                                     double root_dur, double root_int, long n_term,
+                                     const int* term_node, const double* term_loc);
+void oracle_purkinje_free(oracle_purkinje*);
+int oracle_purkinje_advance(oracle_purkinje*, double t0, double dt, int nthreads);
+int oracle_purkinje_couple(oracle_purkinje*, const oracle_mesh* M, double r_pvj, double radius,
+                           int mode);
+int oracle_purkinje_coupled_step(oracle_purkinje*, oracle_tissue* T, double dt, int nthreads);
+double* oracle_purkinje_vm(oracle_purkinje*);
+double* oracle_purkinje_iion(oracle_purkinje*);
+double* oracle_purkinje_terminal_current(oracle_purkinje*);
+long oracle_purkinje_nodes(oracle_purkinje*);
+const int* oracle_purkinje_order(oracle_purkinje*);
+const int* oracle_purkinje_parent(oracle_purkinje*);
+
 #ifdef __cplusplus
 }
 #endif

@@ -129,6 +129,21 @@ def lib():
                                                 C.POINTER(OdeSettings), C.POINTER(Stimulus),
                                                 _dp, _dp, C.c_int, _dp, _dp]
         L.oracle_single_cell_traces.restype = C.c_long
+        L.oracle_purkinje_new.argtypes = [C.c_long, _ip, _ip, _dp, _dp, C.c_int, C.c_int,
+                                          C.POINTER(OdeSettings), C.c_double, C.c_double,
+                                          C.c_double, C.c_int, C.c_double, C.c_double,
+                                          C.c_double, C.c_long, _ip, _dp]
+        L.oracle_purkinje_new.restype = C.c_void_p
+        L.oracle_purkinje_free.argtypes = [C.c_void_p]
+        L.oracle_purkinje_advance.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_int]
+        L.oracle_purkinje_couple.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.c_double,
+                                             C.c_int]
+        L.oracle_purkinje_coupled_step.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.c_int]
+        for f in ("vm", "iion", "terminal_current"):
+            getattr(L, f"oracle_purkinje_{f}").argtypes = [C.c_void_p]
+            getattr(L, f"oracle_purkinje_{f}").restype = _dp
+        L.oracle_purkinje_nodes.argtypes = [C.c_void_p]
+        L.oracle_purkinje_nodes.restype = C.c_long
         _lib = L
     return _lib
 
@@ -510,4 +525,66 @@ class Bidomain:
     def __del__(self):
         if getattr(self, "h", None):
             lib().oracle_bidomain_free(self.h)
+            self.h = None
+
+
+class Purkinje:
+    """A conduction network (ConductionSystemDomain with Monodomain1DSolver)
+    and, after ``couple``, its reaction-diffusion PVJ coupling to a Tissue."""
+
+    def __init__(self, edges, model: str, tissue: int, initial_dt: float, chi=140000.0,
+                 cm=0.01, root=0, root_stimulus=(1e300, 0.0, 0.0), pvj_nodes=(),
+                 pvj_locations=(), ode: Optional[OdeSettings] = None):
+        e = np.asarray(edges, dtype=np.float64).reshape(-1, 4)
+        self._a = np.ascontiguousarray(e[:, 0], dtype=np.int32)
+        self._b = np.ascontiguousarray(e[:, 1], dtype=np.int32)
+        self._len = np.ascontiguousarray(e[:, 2])
+        self._cond = np.ascontiguousarray(e[:, 3])
+        self._tn = np.ascontiguousarray(pvj_nodes, dtype=np.int32).reshape(-1)
+        self._tl = np.ascontiguousarray(pvj_locations, dtype=np.float64).reshape(-1, 3)
+        start, dur, inten = root_stimulus
+        self.h = lib().oracle_purkinje_new(
+            len(e), iptr(self._a), iptr(self._b), ptr(self._len), ptr(self._cond), MODELS[model],
+            tissue, C.byref(ode if ode is not None else ode_settings(max_steps=10 ** 6)),
+            initial_dt, chi, cm, root, start, dur, inten, self._tn.size,
+            iptr(self._tn) if self._tn.size else None,
+            ptr(np.ascontiguousarray(self._tl)) if self._tn.size else None)
+        if not self.h:
+            raise ValueError("oracle_purkinje_new failed (not a connected tree?)")
+        self.n = lib().oracle_purkinje_nodes(self.h)
+        self.t = 0.0
+
+    def _arr(self, name, n):
+        p = getattr(lib(), f"oracle_purkinje_{name}")(self.h)
+        return np.ctypeslib.as_array(p, shape=(n,)).copy()
+
+    def vm(self):
+        return self._arr("vm", self.n)
+
+    def iion(self):
+        return self._arr("iion", self.n)
+
+    def terminal_current(self):
+        return self._arr("terminal_current", max(self._tn.size, 1))[:self._tn.size]
+
+    def advance(self, dt, nthreads=1):
+        """The network alone: Monodomain1DSolver::advance(t, dt), then t += dt."""
+        if lib().oracle_purkinje_advance(self.h, self.t, dt, nthreads) < 0:
+            raise RuntimeError("oracle Purkinje advance failed")
+        self.t = self.t + dt
+
+    def couple(self, mesh: "Mesh", r_pvj: float, radius: float, bidirectional=False):
+        if lib().oracle_purkinje_couple(self.h, mesh.h, r_pvj, radius, int(bidirectional)) < 0:
+            raise ValueError("PVJ mapping failed (pvjRadius below the cell size?)")
+        self._mesh = mesh
+
+    def coupled_step(self, tissue: "Tissue", dt, nthreads=1):
+        """One staggered step of the network coupled to the tissue."""
+        if lib().oracle_purkinje_coupled_step(self.h, tissue.h, dt, nthreads) < 0:
+            raise RuntimeError("oracle coupled step failed")
+        self.t = tissue.time()
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().oracle_purkinje_free(self.h)
             self.h = None
