@@ -185,7 +185,38 @@ __global__ void k_stimulus(long long n, const double* __restrict__ centres, Stim
 // phiE right-hand side and diagonal of the negated system: b = V div(Gi grad Vm)
 // (= -source), diag = sum of the coefficients; at the reference cell the
 // diagonal doubles and b gains the diagonal times the reference value
-__global__ void k_phie_system(BdOp op, const double* __restrict__ dv, long long ref,
+// V fvc::div of the Laplacian's explicit correction fluxes (Gauss linear
+// corrected on a non-orthogonal mesh, or a conductivity not aligned with the
+// faces) at row c, from the cell gradient g of the field: each face's flux
+// k.(w (g_P - g_N) + g_N) with the row's sign, in slot order, then the wall
+// term bk.g_c (gaussLaplacianScheme's faceFluxCorrection, restated)
+__global__ void k_correction(BdOp op, const double* __restrict__ kv,
+                             const double* __restrict__ bk, const double* __restrict__ g,
+                             double* __restrict__ out)
+{
+    const long long c = (long long)blockIdx.x * kBlock + threadIdx.x;
+    if (c >= op.n) return;
+    const long long n = op.n, wn = (long long)op.width * n;
+    const double g0 = g[c], g1 = g[n + c], g2 = g[2 * n + c];
+    double s = 0.0;
+    for (int e = 0; e < op.cnt[c]; ++e) {
+        const long long i = (long long)e * n + c;
+        const long long nb = op.col[i];
+        const double om = op.own[i] ? op.w[i] : 1.0 - op.w[i];
+        const double n0 = g[nb], n1 = g[n + nb], n2 = g[2 * n + nb];
+        const double f0 = om * (g0 - n0) + n0;
+        const double f1 = om * (g1 - n1) + n1;
+        const double f2 = om * (g2 - n2) + n2;
+        s += kv[i] * f0 + kv[wn + i] * f1 + kv[2 * wn + i] * f2;
+    }
+    s += bk[c] * g0 + bk[n + c] * g1 + bk[2 * n + c] * g2;
+    out[c] = s;
+}
+
+// phiE system; cv (may be null) is the Laplacian's explicit correction of
+// the current phiE, which fvm::laplacian takes off the source
+__global__ void k_phie_system(BdOp op, const double* __restrict__ dv,
+                              const double* __restrict__ cv, long long ref,
                               double ref_value, double* __restrict__ diag,
                               double* __restrict__ rdiag, double* __restrict__ b)
 {
@@ -195,14 +226,15 @@ __global__ void k_phie_system(BdOp op, const double* __restrict__ dv, long long 
     for (int e = 0; e < op.cnt[c]; ++e) d -= op.coef_e[(long long)e * op.n + c];
     // the reference form's diagonal is d (negative); setReference: source +=
     // d * value, d += d; negated here
-    double bb = -(-dv[c]);
+    double src = -dv[c];
+    if (cv) src = src - cv[c];
     if (c == ref) {
-        bb = -((-dv[c]) + d * ref_value);
+        src = src + d * ref_value;
         d = d + d;
     }
     diag[c] = -d;
     rdiag[c] = 1.0 / (-d);
-    b[c] = bb;
+    b[c] = -src;
 }
 
 struct VmArgs {
@@ -216,8 +248,8 @@ struct VmArgs {
 __global__ void k_vm_system(BdOp op, VmArgs a, const double* __restrict__ vm_old,
                             const double* __restrict__ vm_oldold, const double* __restrict__ iion,
                             const double* __restrict__ src, const double* __restrict__ dp,
-                            double* __restrict__ diag, double* __restrict__ rdiag,
-                            double* __restrict__ b)
+                            const double* __restrict__ cv, double* __restrict__ diag,
+                            double* __restrict__ rdiag, double* __restrict__ b)
 {
     const long long c = (long long)blockIdx.x * kBlock + threadIdx.x;
     if (c >= op.n) return;
@@ -238,6 +270,7 @@ __global__ void k_vm_system(BdOp op, VmArgs a, const double* __restrict__ vm_old
     double su = -(a.chicm * iion[c]) * V;
     su = su + src[c] * V;
     bb = bb + su;
+    if (cv) bb = bb + cv[c];   // the Laplacian's explicit correction of the current Vm
     b[c] = bb + dp[c];
 }
 
@@ -637,6 +670,11 @@ struct cfg_bidomain {
            *d_src = nullptr, *d_act = nullptr, *d_phie = nullptr, *d_phii = nullptr;
     unsigned char* d_calc = nullptr;
     // work
+    // explicit Laplacian corrections (non-orthogonal meshes): per slot the
+    // signed correction vectors of Gi and of Gi + Ge [3][slot], per cell the
+    // wall factors [3][cell]; null where no correction is needed
+    double *d_ki = nullptr, *d_ke = nullptr, *d_bki = nullptr, *d_bke = nullptr,
+           *d_cv = nullptr;
     double *d_grad = nullptr, *d_dv = nullptr, *d_diag = nullptr, *d_rdiag = nullptr,
            *d_b = nullptr, *d_r = nullptr,
            *d_z = nullptr, *d_p = nullptr, *d_ap = nullptr, *d_ax = nullptr, *d_partial = nullptr;
@@ -777,6 +815,16 @@ int pcg_solve(cfg_bidomain* bd, int kind, double tol, double rel, int max_iter,
     return CFG_OK;
 }
 
+// V fvc::div of the explicit correction of laplacian(G, x) into bd->d_cv
+// (G: kv/bk of Gi or of Gi + Ge); null where the mesh needs none
+const double* correction(cfg_bidomain* bd, const double* kv, const double* bk, const double* x)
+{
+    if (!kv) return nullptr;
+    k_gradient<<<bd->blocks, kBlock, 0, bd->stream>>>(bd->op, x, bd->d_grad);
+    k_correction<<<bd->blocks, kBlock, 0, bd->stream>>>(bd->op, kv, bk, bd->d_grad, bd->d_cv);
+    return bd->d_cv;
+}
+
 void div_gamma_grad(cfg_bidomain* bd, const double* x, double* out)
 {
     k_gradient<<<bd->blocks, kBlock, 0, bd->stream>>>(bd->op, x, bd->d_grad);
@@ -795,7 +843,8 @@ extern "C" int cfg_bidomain_destroy(cfg_bidomain* bd)
                        &bd->d_grad, &bd->d_dv, &bd->d_diag, &bd->d_rdiag, &bd->d_b, &bd->d_r,
                        &bd->d_z,
                        &bd->d_p, &bd->d_ap, &bd->d_ax, &bd->d_partial, &bd->d_p_alt,
-                       &bd->d_coop_partial})
+                       &bd->d_coop_partial, &bd->d_ki, &bd->d_ke, &bd->d_bki, &bd->d_bke,
+                       &bd->d_cv})
         dfree(*p);
     dfree(bd->d_bar);
     dfree(bd->d_abort);
@@ -838,31 +887,26 @@ extern "C" int cfg_bidomain_create(const cfg_bidomain_desc* d, const cfg_mesh_de
     CorrectedOperator oi, oe;
     if (int rc = assemble_corrected(m, d->conductivity_i, nullptr, d->grad_scheme, 0, oi)) return rc;
     if (int rc = assemble_corrected(m, ge, nullptr, d->grad_scheme, 0, oe)) return rc;
-    // no explicit Laplacian correction may be needed: the non-orthogonal and
-    // tangential parts (k per face, the wall factor per cell) must vanish
     double gmax = 0.0;
     for (int k = 0; k < 6; ++k) gmax = std::max(gmax, std::fabs(ge[k]));
     if (!(gmax > 0.0))
         return fail(CFG_ERR_INVALID, "the bulk conductivity Gi + Ge is zero (phiE is undefined)");
-    for (long long f = 0; f < nf; ++f) {
+    // the explicit correction is needed where a face is non-orthogonal or a
+    // conductivity is not aligned with it (k per face), or at a wall (bk)
+    bool corrected = false;
+    for (long long f = 0; f < nf && !corrected; ++f) {
         const double* S = m->face_sf + 3 * f;
         const double scale = gmax * std::sqrt(S[0] * S[0] + S[1] * S[1] + S[2] * S[2]);
         for (const CorrectedOperator* o : {&oi, &oe})
             for (int k = 0; k < 3; ++k)
-                if (std::fabs(o->k[size_t(3 * f + k)]) > 1e-12 * scale)
-                    return fail(CFG_ERR_UNSUPPORTED,
-                                "face %lld needs an explicit Laplacian correction (non-orthogonal "
-                                "face or a conductivity not aligned with it): not built for the "
-                                "bidomain step", f);
+                if (std::fabs(o->k[size_t(3 * f + k)]) > 1e-12 * scale) corrected = true;
     }
-    for (long long c = 0; c < n; ++c)
+    for (long long c = 0; c < n && !corrected; ++c)
         for (const CorrectedOperator* o : {&oi, &oe})
             for (int k = 0; k < 3; ++k)
                 if (std::fabs(o->bk[size_t(3 * c + k)]) > 1e-12 * gmax * std::cbrt(m->volumes[c]) *
                                                                std::cbrt(m->volumes[c]))
-                    return fail(CFG_ERR_UNSUPPORTED,
-                                "cell %lld needs a wall correction of the Laplacian: not built for "
-                                "the bidomain step", c);
+                    corrected = true;
     // ELL rows: (column, face, own) sorted by column
     struct Entry {
         int col;
@@ -886,6 +930,14 @@ extern "C" int cfg_bidomain_create(const cfg_bidomain_desc* d, const cfg_mesh_de
     std::vector<unsigned char> cnt(static_cast<size_t>(n)), own(slots, 0);
     std::vector<double> ci(slots, 0.0), ce(slots, 0.0), gw(3 * slots, 0.0), sf(3 * slots, 0.0),
         wv(slots, 0.0), bw(3 * size_t(n), 0.0);
+    std::vector<double> kiv(corrected ? 3 * slots : 0, 0.0), kev(corrected ? 3 * slots : 0, 0.0),
+        bki(corrected ? 3 * size_t(n) : 0, 0.0), bke(corrected ? 3 * size_t(n) : 0, 0.0);
+    if (corrected)
+        for (long long c = 0; c < n; ++c)
+            for (int k = 0; k < 3; ++k) {
+                bki[size_t(k) * size_t(n) + size_t(c)] = oi.bk[size_t(3 * c + k)];
+                bke[size_t(k) * size_t(n) + size_t(c)] = oe.bk[size_t(3 * c + k)];
+            }
     for (long long c = 0; c < n; ++c) {
         const auto& r = rows[size_t(c)];
         cnt[size_t(c)] = (unsigned char)r.size();
@@ -898,9 +950,14 @@ extern "C" int cfg_bidomain_create(const cfg_bidomain_desc* d, const cfg_mesh_de
             ce[i] = oe.coeff[size_t(f)];
             wv[i] = oi.w[size_t(f)];
             const double* g = r[q].own ? oi.g_own.data() : oi.g_nei.data();
+            const double sg = r[q].own ? 1.0 : -1.0;
             for (int k = 0; k < 3; ++k) {
                 gw[size_t(k) * slots + i] = g[3 * f + k];
                 sf[size_t(k) * slots + i] = m->face_sf[3 * f + k];
+                if (corrected) {
+                    kiv[size_t(k) * slots + i] = sg * oi.k[size_t(3 * f + k)];
+                    kev[size_t(k) * slots + i] = sg * oe.k[size_t(3 * f + k)];
+                }
             }
         }
     }
@@ -975,6 +1032,11 @@ extern "C" int cfg_bidomain_create(const cfg_bidomain_desc* d, const cfg_mesh_de
     if (!e) e = up(&bd->d_bw, bw);
     if (!e) e = up(&bd->d_vol, vol);
     if (!e) e = up(&bd->d_centres, cen);
+    if (!e && corrected) e = up(&bd->d_ki, kiv);
+    if (!e && corrected) e = up(&bd->d_ke, kev);
+    if (!e && corrected) e = up(&bd->d_bki, bki);
+    if (!e && corrected) e = up(&bd->d_bke, bke);
+    if (!e && corrected) e = dmalloc(&bd->d_cv, size_t(n));
     for (double** p : {&bd->d_vm, &bd->d_vm_old, &bd->d_vm_oldold, &bd->d_iion, &bd->d_src,
                        &bd->d_act, &bd->d_phie, &bd->d_phii, &bd->d_dv, &bd->d_diag,
                        &bd->d_rdiag, &bd->d_b,
@@ -1064,9 +1126,10 @@ extern "C" int cfg_bidomain_step(cfg_bidomain* bd, double dt)
     bd->e_stats = cfg_step_stats{};
     if (bd->explicit_alg) {
         // BidomainSolver::solveDiffusionExplicit (bidomainSolver.C:183-213)
+        const double* cve = correction(bd, bd->d_ke, bd->d_bke, bd->d_phie);
         div_gamma_grad(bd, bd->d_vm, bd->d_dv);
-        k_phie_system<<<nb, kBlock, 0, s>>>(bd->op, bd->d_dv, bd->ref, bd->ref_value, bd->d_diag,
-                                            bd->d_rdiag, bd->d_b);
+        k_phie_system<<<nb, kBlock, 0, s>>>(bd->op, bd->d_dv, cve, bd->ref, bd->ref_value,
+                                            bd->d_diag, bd->d_rdiag, bd->d_b);
         if (int rc = pcg_solve(bd, 0, bd->e_tol, bd->e_rel, bd->e_max, bd->e_stats))
             return rc;
         double cft = 1.0, cft0 = 1.0, cft00 = 0.0;
@@ -1104,9 +1167,10 @@ extern "C" int cfg_bidomain_step(cfg_bidomain* bd, double dt)
                 bd->outer_tol)
             converged = true;
         // phiE
+        const double* cve = correction(bd, bd->d_ke, bd->d_bke, bd->d_phie);
         div_gamma_grad(bd, bd->d_vm, bd->d_dv);
-        k_phie_system<<<nb, kBlock, 0, s>>>(bd->op, bd->d_dv, bd->ref, bd->ref_value, bd->d_diag,
-                                            bd->d_rdiag, bd->d_b);
+        k_phie_system<<<nb, kBlock, 0, s>>>(bd->op, bd->d_dv, cve, bd->ref, bd->ref_value,
+                                            bd->d_diag, bd->d_rdiag, bd->d_b);
         if (int rc = pcg_solve(bd, 0, bd->e_tol, bd->e_rel, bd->e_max, bd->e_stats))
             return rc;
         // Vm: fvm::ddt creates the old-time levels on first access
@@ -1127,8 +1191,11 @@ extern "C" int cfg_bidomain_step(cfg_bidomain* bd, double dt)
         }
         div_gamma_grad(bd, bd->d_phie, bd->d_dv);
         VmArgs va{bd->chicm, 1.0 / dt, cft, cft0, cft00, bd->backward ? 1 : 0};
+        // the correction of laplacian(Gi, Vm) at the current Vm; its gradient
+        // work array is free again once the divergence above is formed
+        const double* cvi = correction(bd, bd->d_ki, bd->d_bki, bd->d_vm);
         k_vm_system<<<nb, kBlock, 0, s>>>(bd->op, va, bd->d_vm_old, bd->d_vm_oldold, bd->d_iion,
-                                          bd->d_src, bd->d_dv, bd->d_diag, bd->d_rdiag,
+                                          bd->d_src, bd->d_dv, cvi, bd->d_diag, bd->d_rdiag,
                                           bd->d_b);
         if (int rc = pcg_solve(bd, 1, bd->vm_tol, bd->vm_rel, bd->vm_max, bd->vm_stats))
             return rc;

@@ -165,7 +165,3 @@ def test_create_rejects_bad_arguments(gpu_lib):
     assert create(geo, n_outer=0) == lib.CFG_ERR_INVALID
     assert create(geo, boxes=9) == lib.CFG_ERR_INVALID
     assert create(geo, zero_sigma=True) == lib.CFG_ERR_INVALID
-    # tetrahedra need the explicit Laplacian corrections: not built
-    from cardiacfoam_gb300 import lv
-    assert create(lv.left_ventricle(3, 6, 8).mesh) == lib.CFG_ERR_UNSUPPORTED
-    assert "correction" in lib.load().cfg_last_error().decode()

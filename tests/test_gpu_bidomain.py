@@ -1,7 +1,8 @@
 """The bidomain step on the GPU (cfg_bidomain_*) against the oracle's
 restatement of BidomainSolver: the manufactured case (FP64, both
 preconditioners of the oracle), a propagating TNNP slab, second-order
-convergence of the manufactured run, and the meshes it rejects."""
+convergence of the manufactured run, a tetrahedral left ventricle with the
+Laplacians' explicit corrections, and the explicit algorithm."""
 import numpy as np
 import pytest
 
@@ -111,37 +112,37 @@ def test_manufactured_convergence(gpu_lib):
 
 
 @pytest.mark.gpu
-def test_rejects_meshes_that_need_corrections(gpu_lib):
+def test_tetrahedral_lv_matches_oracle(gpu_lib, oracle):
+    """A tetrahedral left ventricle (4,104 tets): non-orthogonal faces, so
+    both Laplacians carry their explicit corrections (Gauss linear corrected,
+    leastSquares gradient) in the phiE and the Vm solve.  Vm, phiE and the
+    activation times against the oracle, PCG iteration counts within one."""
     L = lv.left_ventricle(3, 6, 8)
-    with pytest.raises(lib.CfgError) as e:
-        api.Bidomain(L.mesh, "TNNP", "epicardialCells")
-    assert e.value.code == lib.CFG_ERR_UNSUPPORTED
+    lo, hi = L.apex_box(8e-3)
+    box = [(lo, hi, 0.0, 1e-3, 1e5)]
+    gi, ge = (0.17, 0.0, 0.0, 0.019, 0.0, 0.019), (0.62, 0.0, 0.0, 0.24, 0.0, 0.24)
+    dt = 2e-5
+    bd = api.Bidomain(L.mesh, "TNNP", "epicardialCells", sigma_i=gi, sigma_e=ge, dt=dt,
+                      pcg_tol=1e-10, phie_tol=1e-10, n_outer=2, ref_point=(0.0, 0.0, 0.0),
+                      boxes=box)
+    d = oracle.tissue_desc("TNNP", 1, gi, implicit=True, precond_dic=False, pcg_tol=1e-10,
+                           pcg_rel_tol=0.0, n_outer=2, outer_tol=0.0, boxes=box)
+    B = oracle.Bidomain(d, ge, oracle.Mesh.general(L.mesh), (0.0, 0.0, 0.0), 0.0, 1e-10, 0.0,
+                        1000)
+    for _ in range(150):
+        bd.step(dt)
+        B.step(dt)
+        (_, _, it_v), (_, _, it_e) = bd.stats()
+        assert np.max(np.abs(it_v - B.tissue.solves()[2])) <= 1
+        assert np.max(np.abs(it_e - B.phie_solves()[2])) <= 1
+    assert _close(bd.vm(), B.tissue.vm(), 1e-9)
+    assert _close(bd.phie(), B.phie(), 1e-9)
+    ag, ao = bd.activation(), B.tissue.activation()
+    assert np.array_equal(ag > 0, ao > 0) and (ag > 0).sum() >= 10
+    assert np.max(np.abs(ag - ao)) < 1e-9
+    bd.close()
     with pytest.raises(ValueError):
         api.Bidomain(box_mesh(4, 4, 4, 1e-3, 1e-3, 1e-3), "TNNP", "epicardialCells")
-
-
-ELECTRO_PROPERTIES = """
-myocardiumSolver  bidomainSolver;
-bidomainSolverCoeffs
-{
-    conductivityIntracellular [-1 -3 3 0 0 2 0] (0.17 0 0 0.019 0 0.019);
-    conductivityExtracellular [-1 -3 3 0 0 2 0] (0.62 0 0 0.24 0 0.24);
-    chi  [0 -1 0 0 0 0 0] 140000;
-    cm   [-1 -4 4 0 0 2 0] 0.01;
-    ionicModel TNNP;
-    tissue epicardialCells;
-    solutionAlgorithm implicit;
-    maxSteps 1000000;
-    phiERefPoint (0 0 0);
-    externalStimulus
-    {
-        stimulusLocationMin (0 0 0);
-        stimulusLocationMax (1e-3 4e-3 5e-4);
-        stimulusDuration [0 0 1 0 0 0 0] 1e-3;
-        stimulusIntensity [0 -3 0 0 0 1 0] 1e5;
-    }
-}
-"""
 
 
 @pytest.mark.gpu
