@@ -298,9 +298,10 @@ def bidomain_arm(args):
     """The bidomain tutorial's manufactured case (bidomainSolver,
     bidomainFDAManufactured, 3D unit cube at 40 cells per direction, dt of the
     tutorial's sweep, two PIMPLE correctors, PCG tolerance 1e-12 for Vm and
-    phiE): GPU steps timed with CUDA events after warm-up, the oracle (DIC, one
-    thread) on a bounded sample of the same steps, and the two compared
-    after that sample."""
+    phiE): GPU steps timed with CUDA events after warm-up, with the PCG of both
+    systems in float pairs (the headline) and in FP64, the oracle (DIC, one
+    thread) on a bounded sample of the same steps, and each GPU form
+    compared with it after that sample."""
     import torch
     from cardiacfoam_gb300 import api, lib
     from cardiacfoam_gb300 import verification as V
@@ -309,37 +310,46 @@ def bidomain_arm(args):
     dt = V.SWEEP.get(n, 0.2 / (10 * n * n / 4))
     mesh = V.geometry_mesh_for(dim, n)
 
-    def gpu():
+    def gpu(arithmetic):
         bd = api.Bidomain(mesh, model="bidomainFDAManufactured", tissue=f"{dim}D",
                           sigma_i=V.BIDOMAIN_SIGMA_I, sigma_e=V.BIDOMAIN_SIGMA_E, chi=V.CHI,
                           cm=V.CM, dt=dt, pcg_tol=1e-12, phie_tol=1e-12, phie_max_iter=4000,
                           n_outer=2, ref_point=V.BIDOMAIN_REF_POINT,
                           grad_scheme=lib.GRAD_GAUSS_LINEAR)
+        bd.set_pcg_arithmetic(arithmetic)
         vm, pe, _, u1, u2, u3 = V.bidomain_fields(mesh.centres, 0.0, dim)
         bd.set_field(lib.FIELD_VM, vm)
         bd.set_field(lib.FIELD_PHIE, pe)
         bd.set_states(np.stack([vm, u1, u2, u3]))
         return bd
 
-    bd = gpu()
     ks = args.bidomain_sample
-    bd.run(dt, ks)
-    g_vm, g_pe = bd.vm(), bd.phie()
-    bd.run(dt, 3)
-    s = torch.cuda.ExternalStream(bd.stream())
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    its_v, its_e = [], []
-    torch.cuda.synchronize()
-    e0.record(s)
-    for _ in range(args.bidomain_steps):
-        bd.step(dt)
-        (_, _, iv), (_, _, ie) = bd.stats()
-        its_v.append(int(iv.sum()))
-        its_e.append(int(ie.sum()))
-    e1.record(s)
-    e1.synchronize()
-    ms = e0.elapsed_time(e1) / args.bidomain_steps
-    bd.close()
+
+    def timed(arithmetic):
+        """ks sample steps (kept for the oracle comparison), 3 warm-up
+        steps, then the timed steps"""
+        bd = gpu(arithmetic)
+        bd.run(dt, ks)
+        sample = (bd.vm(), bd.phie())
+        bd.run(dt, 3)
+        s = torch.cuda.ExternalStream(bd.stream())
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        its_v, its_e = [], []
+        torch.cuda.synchronize()
+        e0.record(s)
+        for _ in range(args.bidomain_steps):
+            bd.step(dt)
+            (_, _, iv), (_, _, ie) = bd.stats()
+            its_v.append(int(iv.sum()))
+            its_e.append(int(ie.sum()))
+        e1.record(s)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1) / args.bidomain_steps
+        bd.close()
+        return ms, its_v, its_e, sample
+
+    runs = {name: timed(a) for name, a in (("float_pairs", lib.PCG_FLOAT_PAIRS),
+                                           ("fp64", lib.PCG_FP64))}
     # oracle sample: the same first steps from the same state
     d = pyoracle.tissue_desc("bidomainFDAManufactured", 10 + dim, V.BIDOMAIN_SIGMA_I, chi=V.CHI,
                              cm=V.CM, implicit=True, precond_dic=True, pcg_tol=1e-12,
@@ -356,18 +366,30 @@ def bidomain_arm(args):
         B.step(dt)
     t_cpu = time.perf_counter() - t0
     cells = mesh.n_cells
+
+    def vs_oracle(sample):
+        g_vm, g_pe = sample
+        return {"vm_max_rel": float(np.max(np.abs(g_vm - B.tissue.vm())) /
+                                    np.max(np.abs(B.tissue.vm()))),
+                "phie_max_rel": float(np.max(np.abs(g_pe - B.phie())) / np.max(np.abs(B.phie())))}
+
+    ms, its_v, its_e, sample = runs["float_pairs"]
+    ms64, its_v64, its_e64, sample64 = runs["fp64"]
     return {"workload": (f"bidomain tutorial manufactured case, 3D unit cube {n}^3 = {cells} "
                          f"cells, dt {dt} s, Gi/Ge of the tutorial, backward ddt, 2 PIMPLE "
-                         f"correctors, PCG 1e-12 (Vm, phiE), Gauss linear gradients"),
+                         f"correctors, PCG 1e-12 (Vm, phiE), Gauss linear gradients, FP64 "
+                         f"ionic update"),
+            "pcg_arithmetic": "float pairs (about 48 significant bits, FP32 pipe)",
             "value": cells / (ms * 1e-3), "unit": "cell-steps/s", "ms_per_step": ms,
             "steps": args.bidomain_steps,
             "pcg_iterations_per_step": {"vm": its_v, "phie": its_e},
+            "us_per_phie_iteration": ms * 1e3 / max(1, np.mean(its_e)),
+            "gpu_vs_oracle_after_sample": vs_oracle(sample),
+            "fp64_pcg": {"value": cells / (ms64 * 1e-3), "ms_per_step": ms64,
+                         "pcg_iterations_per_step": {"vm": its_v64, "phie": its_e64},
+                         "gpu_vs_oracle_after_sample": vs_oracle(sample64)},
             "cpu_oracle": {"value": cells * ks / t_cpu, "unit": "cell-steps/s", "cores": 1,
-                           "kind": "port", "sample": f"the first {ks} steps, DIC preconditioner"},
-            "gpu_vs_oracle_after_sample": {
-                "vm_max_rel": float(np.max(np.abs(g_vm - B.tissue.vm())) /
-                                    np.max(np.abs(B.tissue.vm()))),
-                "phie_max_rel": float(np.max(np.abs(g_pe - B.phie())) / np.max(np.abs(B.phie())))}}
+                           "kind": "port", "sample": f"the first {ks} steps, DIC preconditioner"}}
 
 
 def ecg_timing(L, source, launches: int = 50):
@@ -1044,6 +1066,7 @@ def main():
         "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64 (mixed)",
         "data": "synthetic (seeded geometry/stimulus of the ORd slab configuration)",
         "config": {"workload": WORKLOAD, "cells": n, "dt_s": DT, "precision": "mixed",
+                   "pcg": "float pairs (FP32 pipe, about 48 significant bits); FP64 source",
                    "l2": "flushed (256 MB write) between timed steps",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "fp64": {"value": fp64_value, "unit": "cell-steps/s", "steps": r["k64"],

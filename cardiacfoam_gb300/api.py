@@ -331,6 +331,11 @@ class Monodomain:
         sequence per PCG iteration."""
         _L.check(self._lib.cfg_monodomain_set_persistent(self.h, int(enable)))
 
+    def set_pcg_arithmetic(self, arithmetic: int):
+        """PCG of the persistent solve in FP64 (lib.PCG_FP64) or float pairs
+        (lib.PCG_FLOAT_PAIRS, the mixed form's default)."""
+        _L.check(self._lib.cfg_monodomain_set_pcg_arithmetic(self.h, int(arithmetic)))
+
     def set_timing(self, enable: bool = True):
         _L.check(self._lib.cfg_monodomain_set_timing(self.h, int(enable)))
 
@@ -530,6 +535,11 @@ class Bidomain:
 
     def step(self, dt: float):
         _L.check(self._lib.cfg_bidomain_step(self.h, dt))
+
+    def set_pcg_arithmetic(self, arithmetic: int):
+        """PCG of both systems in FP64 (lib.PCG_FP64) or float pairs
+        (lib.PCG_FLOAT_PAIRS, the mixed form's default)."""
+        _L.check(self._lib.cfg_bidomain_set_pcg_arithmetic(self.h, int(arithmetic)))
 
     def run(self, dt: float, n_steps: int):
         _L.check(self._lib.cfg_bidomain_run(self.h, dt, n_steps))

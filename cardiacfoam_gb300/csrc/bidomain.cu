@@ -39,6 +39,8 @@
 #include "host_common.h"
 #include "ionic_host.h"
 
+namespace fp = cfg::fp;
+
 namespace {
 
 constexpr int kBlock = 256;
@@ -633,6 +635,207 @@ __global__ void __launch_bounds__(kCoopBlock, 1) k_pcg_coop(CoopPcgArgs ca)
     }
 }
 
+// ---------------------------------------------------------------- float pairs
+// The same solve with the PCG in float pairs (the mixed form's default): the
+// system scaled by 2^shift (a power of two, so the solution and the residual
+// ratios are those of the unscaled system), its coefficients as (hi, lo)
+// pairs, the diagonal, source and iterate split from their FP64 values at the
+// start, every vector and sum of the iteration in pairs on the FP32 pipe.
+// The scalars are formed by every thread from the same block-order sums.
+struct PairPcgArgs {
+    const float2* pcoef;   // [slot][cell] scaled coefficients of the system
+    int shift;
+    float2 *px, *pdiag, *prdiag;   // [cell]
+};
+
+template <int W, class F>
+__device__ __forceinline__ fp::P offdiag_pair(const BdOp& op, const float2* pcoef, long long c,
+                                             F f, fp::Acc& acc)
+{
+    if constexpr (W > 0) {
+        fp::P v[W], k[W];
+#pragma unroll
+        for (int e = 0; e < W; ++e) {
+            const long long i = (long long)e * op.n + c;
+            k[e] = pcoef[i];
+            v[e] = f(op.col[i]);
+        }
+#pragma unroll
+        for (int e = 0; e < W; ++e) acc.sub_prod(k[e], v[e]);
+    } else {
+        const int k = op.cnt[c];
+        for (int e = 0; e < k; ++e) {
+            const long long i = (long long)e * op.n + c;
+            acc.sub_prod(pcoef[i], f(op.col[i]));
+        }
+    }
+    return acc.value();
+}
+
+__device__ __forceinline__ fp::P direction_pair(const fp::P* z, const fp::P* p_old, fp::P beta,
+                                                bool first, long long q)
+{
+    const fp::P zq = __ldcg(&z[q]);
+    return first ? zq : fp::madd(beta, __ldcg(&p_old[q]), zq);
+}
+
+template <int W>
+__global__ void __launch_bounds__(kCoopBlock, 1) k_pcg_pair(CoopPcgArgs ca, PairPcgArgs q)
+{
+    using namespace cfg::gsync;
+    using fp::P;
+    const PcgArgs& a = ca.a;
+    const BdOp& op = a.op;
+    PcgScalars* st = a.st;
+    const long long n = op.n;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const long long first = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const P tol = fp::split(st->tol), rel = fp::split(st->rel);
+    const bool use_rel = st->rel > 1e-20;
+    const int max_iter = st->max_iter;
+    const int sh = q.shift;
+    const P small = fp::split(1e-20, sh), count = fp::split(double(n));
+    P* ax = reinterpret_cast<P*>(a.ax);
+    P* r = reinterpret_cast<P*>(a.r);
+    P* z = reinterpret_cast<P*>(a.z);
+    P* ap = reinterpret_cast<P*>(a.ap);
+    float2* partial = reinterpret_cast<float2*>(ca.partial);
+    unsigned epoch = 0;
+    int set = 0;
+    bool aborted = false, started = false;
+    P init_res = fp::make(0.0f), res = fp::make(0.0f);
+    int iter = 0, status = 0;
+    do {
+        // --- A x, r = b - A x; sums of x and |r|
+        P s1[2] = {fp::make(0.0f), fp::make(0.0f)};
+        const double* xx = a.x;
+        for (long long c = first; c < n; c += stride) {
+            const P d = fp::split(a.diag[c], sh);
+            q.pdiag[c] = d;
+            q.prdiag[c] = fp::split(a.rdiag[c], -sh);
+            const P xc = fp::split(xx[c]);
+            q.px[c] = xc;
+            fp::Acc acc;
+            acc.add_prod(d, xc);
+            const P axc = offdiag_pair<W>(op, q.pcoef, c, [xx](long long k) {
+                return fp::split(xx[k]);
+            }, acc);
+            const P rc = fp::sub(fp::split(a.b[c], sh), axc);
+            ax[c] = axc;
+            r[c] = rc;
+            s1[0] = fp::add(s1[0], xc);
+            s1[1] = fp::add(s1[1], fp::abs(rc));
+        }
+        started = true;
+        block_sums_pair<kCoopBlock, 2>(partial, set, s1);
+        if (!grid_barrier(ca.bar_count, ca.bar_abort, epoch, ca.spin_limit)) { aborted = true; break; }
+        P g1[2];
+        grid_sums_pair<2>(partial, set, g1);
+        set ^= 1;
+        const P avg = fp::div(g1[0], count);
+        // --- normFactor; z = D^-1 r (published), z.r
+        P s2[2] = {fp::make(0.0f), fp::make(0.0f)};
+        for (long long c = first; c < n; c += stride) {
+            fp::Acc rs;
+            rs.add_prod(q.pdiag[c], fp::make(1.0f));
+            const P pa = fp::mul(offdiag_pair<W>(op, q.pcoef, c, [](long long) {
+                return fp::make(1.0f);
+            }, rs), avg);
+            const P bc = fp::split(a.b[c], sh);
+            s2[0] = fp::add(s2[0], fp::add(fp::abs(fp::sub(ax[c], pa)), fp::abs(fp::sub(bc, pa))));
+            const P rc = r[c];
+            const P zc = fp::mul(q.prdiag[c], rc);
+            __stcg(&z[c], zc);
+            s2[1] = fp::madd(zc, rc, s2[1]);
+        }
+        block_sums_pair<kCoopBlock, 2>(partial, set, s2);
+        if (!grid_barrier(ca.bar_count, ca.bar_abort, epoch, ca.spin_limit)) { aborted = true; break; }
+        P g2[2];
+        grid_sums_pair<2>(partial, set, g2);
+        set ^= 1;
+        const P normf = fp::add(g2[0], small);
+        init_res = fp::div(g1[1], normf);
+        const P rel_init = fp::mul(rel, init_res);
+        const auto conv = [&](P rr) {
+            return fp::less(rr, tol) || (use_rel && fp::less(rr, rel_init));
+        };
+        res = init_res;
+        P wArA = g2[1], beta = fp::make(0.0f);
+        P* p_old = reinterpret_cast<P*>(a.p);
+        P* p_new = reinterpret_cast<P*>(ca.p_alt);
+        while (!conv(res)) {
+            // --- direction pass: p = z + beta p_old, A p, sum p.A p
+            const bool first_it = iter == 0;
+            P s3[1] = {fp::make(0.0f)};
+            for (long long c = first; c < n; c += stride) {
+                const P pc = direction_pair(z, p_old, beta, first_it, c);
+                const P* zz = z;
+                const P* po = p_old;
+                fp::Acc acc;
+                acc.add_prod(q.pdiag[c], pc);
+                const P apc = offdiag_pair<W>(op, q.pcoef, c, [zz, po, beta, first_it](long long k) {
+                    return direction_pair(zz, po, beta, first_it, k);
+                }, acc);
+                __stcg(&p_new[c], pc);
+                ap[c] = apc;
+                s3[0] = fp::madd(apc, pc, s3[0]);
+            }
+            block_sums_pair<kCoopBlock, 1>(partial, set, s3);
+            if (!grid_barrier(ca.bar_count, ca.bar_abort, epoch, ca.spin_limit)) { aborted = true; break; }
+            P g3[1];
+            grid_sums_pair<1>(partial, set, g3);
+            set ^= 1;
+            if (g3[0].x == 0.0f) break;   // checkSingularity
+            const P alpha = fp::div(wArA, g3[0]);
+            const P nalpha = fp::neg(alpha);
+            // --- update pass: x, r, z; |r| and z.r
+            P s4[2] = {fp::make(0.0f), fp::make(0.0f)};
+            for (long long c = first; c < n; c += stride) {
+                q.px[c] = fp::madd(alpha, __ldcg(&p_new[c]), q.px[c]);
+                const P rc = fp::madd(nalpha, ap[c], r[c]);
+                r[c] = rc;
+                const P zc = fp::mul(q.prdiag[c], rc);
+                __stcg(&z[c], zc);
+                s4[0] = fp::add(s4[0], fp::abs(rc));
+                s4[1] = fp::madd(zc, rc, s4[1]);
+            }
+            block_sums_pair<kCoopBlock, 2>(partial, set, s4);
+            if (!grid_barrier(ca.bar_count, ca.bar_abort, epoch, ca.spin_limit)) { aborted = true; break; }
+            P g4[2];
+            grid_sums_pair<2>(partial, set, g4);
+            set ^= 1;
+            res = fp::div(g4[0], normf);
+            ++iter;
+            if (conv(res) || iter >= max_iter) {
+                if (!conv(res)) status = 1;
+                break;
+            }
+            beta = fp::div(g4[1], wArA);
+            wArA = g4[1];
+            P* t = p_old;
+            p_old = p_new;
+            p_new = t;
+        }
+    } while (false);
+    // the iterate back into the FP64 field (own rows)
+    if (started && !aborted)
+        for (long long c = first; c < n; c += stride) a.x[c] = fp::join(q.px[c]);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        st->iter = iter;
+        st->init_res = fp::join(init_res);
+        st->res = fp::join(res);
+        st->status = aborted ? 2 : status;
+        st->done = 1;
+    }
+}
+
+// scaled float-pair copy of a coefficient array
+__global__ void k_pair_coef(long long m, const double* coef, int shift, float2* out)
+{
+    const long long i = (long long)blockIdx.x * kBlock + threadIdx.x;
+    if (i < m) out[i] = fp::split(coef[i], shift);
+}
+
 __global__ void k_phii(long long n, const double* vm, const double* phie, double* phii)
 {
     const long long c = (long long)blockIdx.x * kBlock + threadIdx.x;
@@ -685,6 +888,17 @@ struct cfg_bidomain {
     // its reduction partials and grid barrier
     int coop_blocks = 0;
     double *d_p_alt = nullptr, *d_coop_partial = nullptr;
+    // float-pair PCG of the persistent solve (CFG_PCG_FLOAT_PAIRS, the mixed
+    // form's default): per system [0] phiE, [1] Vm the scaled coefficients
+    // and their scale, the iterate and the scaled diagonal as pairs; the
+    // scale follows from bounds of the largest diagonal
+    bool pair = false;
+    float2* d_pcoef[2] = {nullptr, nullptr};
+    int pcoef_shift[2] = {0, 0};
+    bool pcoef_ready[2] = {false, false};
+    float2 *d_px = nullptr, *d_pdiag = nullptr, *d_prdiag = nullptr;
+    double max_vol = 0.0, max_row_i = 0.0, max_row_e = 0.0;
+    double step_dt = 0.0;
     unsigned* d_bar = nullptr;
     int* d_abort = nullptr;
     long long spin_limit = cfg::gsync::kSpinLimit;
@@ -709,6 +923,18 @@ struct cfg_bidomain {
 using namespace cfg;
 
 namespace {
+
+cudaError_t alloc_pairs(cfg_bidomain* bd)
+{
+    if (bd->d_px) return cudaSuccess;
+    const size_t n = size_t(bd->n), m = size_t(bd->op.width > 0 ? bd->op.width : 1) * n;
+    cudaError_t e = dmalloc(&bd->d_pcoef[0], m);
+    if (!e) e = dmalloc(&bd->d_pcoef[1], m);
+    if (!e) e = dmalloc(&bd->d_px, n);
+    if (!e) e = dmalloc(&bd->d_pdiag, n);
+    if (!e) e = dmalloc(&bd->d_prdiag, n);
+    return e;
+}
 
 PcgArgs pcg_args(cfg_bidomain* bd, const double* coef, double* x)
 {
@@ -750,12 +976,37 @@ int pcg_solve(cfg_bidomain* bd, int kind, double tol, double rel, int max_iter,
         CFG_CUDA_TRY(cudaMemsetAsync(bd->d_abort, 0, sizeof(int), s));
         CoopPcgArgs ca{a, bd->d_p_alt, bd->d_coop_partial, bd->d_bar, bd->d_abort,
                        bd->spin_limit};
-        void* params[] = {&ca};
-        const void* fn = bd->op.width == 6 ? (const void*)k_pcg_coop<6>
-                       : bd->op.width == 4 ? (const void*)k_pcg_coop<4>
-                                           : (const void*)k_pcg_coop<0>;
-        CFG_CUDA_TRY(cudaLaunchCooperativeKernel(fn, dim3(bd->coop_blocks), dim3(kCoopBlock),
-                                                 params, 0, s));
+        if (bd->pair) {
+            // the largest diagonal is at most 2 x the largest row sum of the
+            // phiE system (setReference doubles one), chi Cm 2 V / dt + the
+            // largest row sum of the Vm system
+            const double dmax = kind == 0 ? 2.0 * bd->max_row_e
+                                          : bd->chicm * 2.0 * bd->max_vol / bd->step_dt +
+                                                bd->max_row_i;
+            const int shift = dmax > 0 ? -std::ilogb(dmax) : 0;
+            if (!bd->pcoef_ready[kind] || bd->pcoef_shift[kind] != shift) {
+                const long long m = (long long)bd->op.width * bd->n;
+                k_pair_coef<<<unsigned((m + kBlock - 1) / kBlock), kBlock, 0, s>>>(
+                    m, kind == 0 ? bd->op.coef_e : bd->op.coef_i, shift, bd->d_pcoef[kind]);
+                CFG_CUDA_TRY(cudaGetLastError());
+                bd->pcoef_shift[kind] = shift;
+                bd->pcoef_ready[kind] = true;
+            }
+            PairPcgArgs pa{bd->d_pcoef[kind], shift, bd->d_px, bd->d_pdiag, bd->d_prdiag};
+            void* params[] = {&ca, &pa};
+            const void* fn = bd->op.width == 6 ? (const void*)k_pcg_pair<6>
+                           : bd->op.width == 4 ? (const void*)k_pcg_pair<4>
+                                               : (const void*)k_pcg_pair<0>;
+            CFG_CUDA_TRY(cudaLaunchCooperativeKernel(fn, dim3(bd->coop_blocks), dim3(kCoopBlock),
+                                                     params, 0, s));
+        } else {
+            void* params[] = {&ca};
+            const void* fn = bd->op.width == 6 ? (const void*)k_pcg_coop<6>
+                           : bd->op.width == 4 ? (const void*)k_pcg_coop<4>
+                                               : (const void*)k_pcg_coop<0>;
+            CFG_CUDA_TRY(cudaLaunchCooperativeKernel(fn, dim3(bd->coop_blocks), dim3(kCoopBlock),
+                                                     params, 0, s));
+        }
         CFG_CUDA_TRY(cudaMemcpyAsync(bd->h_st, bd->d_st, sizeof(PcgScalars),
                                      cudaMemcpyDeviceToHost, s));
         CFG_CUDA_TRY(cudaStreamSynchronize(s));
@@ -848,6 +1099,11 @@ extern "C" int cfg_bidomain_destroy(cfg_bidomain* bd)
         dfree(*p);
     dfree(bd->d_bar);
     dfree(bd->d_abort);
+    dfree(bd->d_pcoef[0]);
+    dfree(bd->d_pcoef[1]);
+    dfree(bd->d_px);
+    dfree(bd->d_pdiag);
+    dfree(bd->d_prdiag);
     dfree(bd->d_col);
     dfree(bd->d_cnt);
     dfree(bd->d_own);
@@ -1021,6 +1277,16 @@ extern "C" int cfg_bidomain_create(const cfg_bidomain_desc* d, const cfg_mesh_de
         return err;
     };
     std::vector<double> vol(m->volumes, m->volumes + n), cen(m->centres, m->centres + 3 * n);
+    for (long long c = 0; c < n; ++c) {
+        double si = 0.0, se = 0.0;
+        for (int q = 0; q < width; ++q) {
+            si += std::fabs(ci[size_t(q) * size_t(n) + size_t(c)]);
+            se += std::fabs(ce[size_t(q) * size_t(n) + size_t(c)]);
+        }
+        bd->max_row_i = std::max(bd->max_row_i, si);
+        bd->max_row_e = std::max(bd->max_row_e, se);
+        bd->max_vol = std::max(bd->max_vol, vol[size_t(c)]);
+    }
     if (!e) e = up(&bd->d_col, col);
     if (!e) e = up(&bd->d_cnt, cnt);
     if (!e) e = up(&bd->d_own, own);
@@ -1060,7 +1326,9 @@ extern "C" int cfg_bidomain_create(const cfg_bidomain_desc* d, const cfg_mesh_de
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pcg_coop<0>, kCoopBlock, 0) ==
                 cudaSuccess &&
             per_sm > 0) {
-            for (const void* f : {(const void*)k_pcg_coop<4>, (const void*)k_pcg_coop<6>}) {
+            for (const void* f : {(const void*)k_pcg_coop<4>, (const void*)k_pcg_coop<6>,
+                                  (const void*)k_pcg_pair<0>, (const void*)k_pcg_pair<4>,
+                                  (const void*)k_pcg_pair<6>}) {
                 int k = 0;
                 if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&k, f, kCoopBlock, 0) ==
                     cudaSuccess)
@@ -1100,7 +1368,29 @@ extern "C" int cfg_bidomain_create(const cfg_bidomain_desc* d, const cfg_mesh_de
     op.bw = bd->d_bw;
     op.vol = bd->d_vol;
     for (int k = 0; k < 6; ++k) op.G[k] = d->conductivity_i[k];
+    if (bd->coop_blocks > 0 && d->ionic.precision == CFG_PRECISION_MIXED) {
+        if ((e = alloc_pairs(bd)))
+            return bail(fail(CFG_ERR_CUDA, "bidomain allocation: %s", cudaGetErrorString(e)));
+        bd->pair = true;
+    }
     *out = bd;
+    return CFG_OK;
+}
+
+extern "C" int cfg_bidomain_set_pcg_arithmetic(cfg_bidomain* bd, int arithmetic)
+{
+    if (!bd) return fail(CFG_ERR_INVALID, "null context");
+    if (arithmetic != CFG_PCG_FP64 && arithmetic != CFG_PCG_FLOAT_PAIRS)
+        return fail(CFG_ERR_INVALID, "unknown PCG arithmetic %d", arithmetic);
+    if (arithmetic == CFG_PCG_FP64) {
+        bd->pair = false;
+        return CFG_OK;
+    }
+    if (bd->coop_blocks <= 0)
+        return fail(CFG_ERR_UNSUPPORTED, "float pairs need the cooperative solve");
+    const cudaError_t e = alloc_pairs(bd);
+    if (e) return fail(CFG_ERR_CUDA, "device allocation failed: %s", cudaGetErrorString(e));
+    bd->pair = true;
     return CFG_OK;
 }
 
@@ -1112,6 +1402,7 @@ extern "C" int cfg_bidomain_step(cfg_bidomain* bd, double dt)
     const long long n = bd->n;
     const size_t bytes = size_t(n) * sizeof(double);
     const int nb = bd->blocks;
+    bd->step_dt = dt;
     // Time::operator++ and the old-time levels of Vm
     bd->t = bd->t + dt;
     if (bd->n_old >= 1) {

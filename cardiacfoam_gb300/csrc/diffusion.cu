@@ -46,7 +46,17 @@ __global__ void k_prepare(DiffusionArgs a)
         a.diag2[v * a.n + c] = d;
         a.rdiag2[v * a.n + c] = 1.0 / d;
         a.sumA2[v * a.n + c] = row_sum(a, c, d);
+        if (a.pair) {
+            a.pdiag2[v * a.n + c] = fp::split(d, a.pair_shift);
+            a.prdiag2[v * a.n + c] = fp::split(1.0 / d, -a.pair_shift);
+            a.psumA2[v * a.n + c] = fp::split(a.sumA2[v * a.n + c], a.pair_shift);
+        }
     }
+    if (a.pair && !a.sx)
+        for (int e = 0; e < a.width; ++e) {
+            const long long i = (long long)e * a.n + c;
+            a.pcoef[i] = fp::split(a.ell_coef[i], a.pair_shift);
+        }
 }
 
 // Start of one PIMPLE corrector: the source of

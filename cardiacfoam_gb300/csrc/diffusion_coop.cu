@@ -360,6 +360,268 @@ __global__ void __launch_bounds__(kCoopBlock, 1) k_implicit_coop(DiffusionArgs a
     if (status && threadIdx.x == 0) atomicOr(&st->status, status);
 }
 
+// ---------------------------------------------------------------- float pairs
+// The same solve with the PCG in float pairs (the mixed form): the operator,
+// the source and every vector of the iteration as (hi, lo) pairs on the FP32
+// pipe, the system scaled by 2^pair_shift so that its quantities sit well
+// inside the float range.  The corrector's source is formed in FP64 as above
+// (once per corrector) and split; the iterate x is published as a pair (px)
+// for the neighbours and written back to Vm in FP64 after each solve.  The
+// scalars (alpha, beta, the residuals) are formed by every thread from the
+// same block-order sums, so every block takes the same decisions without a
+// shared-memory broadcast.
+
+template <int W, class F>
+__device__ __forceinline__ fp::P amul_pair(const DiffusionArgs& a, const CoopArgs& ca, unsigned c,
+                                           fp::P d, F q)
+{
+    fp::Acc acc;
+    acc.add_prod(d, q(c));
+    if (a.sx) {
+        const unsigned nx = unsigned(a.sx), nxy = nx * unsigned(a.sy);
+        const unsigned line = fdiv(c, ca.div_nx), i = c - line * nx;
+        const unsigned k = fdiv(line, ca.div_ny), j = line - k * unsigned(a.sy);
+        if (k > 0) acc.sub_prod(a.pcz, q(c - nxy));
+        if (j > 0) acc.sub_prod(a.pcy, q(c - nx));
+        if (i > 0) acc.sub_prod(a.pcx, q(c - 1));
+        if (i + 1 < nx) acc.sub_prod(a.pcx, q(c + 1));
+        if (j + 1 < unsigned(a.sy)) acc.sub_prod(a.pcy, q(c + nx));
+        if (k + 1 < unsigned(a.sz)) acc.sub_prod(a.pcz, q(c + nxy));
+    } else if constexpr (W > 0) {
+#pragma unroll
+        for (int e = 0; e < W; ++e)
+            acc.sub_prod(ld_stream(&a.pcoef[(long long)e * a.n + c]),
+                         q(unsigned(ld_stream(&a.ell_col[(long long)e * a.n + c]))));
+    } else {
+        const int cnt = a.ell_cnt[c];
+        for (int e = 0; e < cnt; ++e)
+            acc.sub_prod(a.pcoef[(long long)e * a.n + c],
+                         q(unsigned(a.ell_col[(long long)e * a.n + c])));
+    }
+    return acc.value();
+}
+
+template <class CR, int W>
+__global__ void __launch_bounds__(kCoopBlock, 1) k_implicit_pair(DiffusionArgs a, CoopArgs ca)
+{
+    using fp::P;
+    PcgState* st = a.st;
+    const unsigned n = unsigned(a.n);
+    const unsigned stride = gridDim.x * blockDim.x;
+    const unsigned first = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool lead = blockIdx.x == 0 && threadIdx.x == 0;
+    int n_old = st->n_old;
+    const double t_step = st->t, t0 = st->t0;
+    const bool use_rel = st->rel_tol > 1e-20;
+    const P tol = fp::split(st->tol), outer_tol = fp::split(st->outer_tol);
+    const P rel = fp::split(st->rel_tol);
+    const int max_iter = st->max_iter, n_outer = st->n_outer;
+    const int sh = a.pair_shift;
+    // the ratio sum|r| / normFactor is scale free when the small number
+    // lduMatrix adds to normFactor is scaled with the system
+    const P small = fp::split(1e-20, sh);
+    const P count = fp::split(double(n));
+    double* __restrict__ x = a.vm;
+    P* __restrict__ px = a.px;                          // published
+    P* __restrict__ b = reinterpret_cast<P*>(a.b);
+    P* __restrict__ ax = reinterpret_cast<P*>(a.ax);
+    P* __restrict__ r = reinterpret_cast<P*>(a.r);
+    P* __restrict__ z = reinterpret_cast<P*>(a.z);      // published
+    P* __restrict__ p = reinterpret_cast<P*>(a.pA);
+    P* __restrict__ ap = reinterpret_cast<P*>(a.ap);
+    float2* partial = reinterpret_cast<float2*>(a.partial);
+    unsigned epoch = 0;
+    int set = 0;
+    int n_solves = 0, status = 0;
+    bool converged_outer = false, abort_step = false;
+    long long step_iters = 0;
+    P last_init = fp::make(0.0f), last_res = fp::make(0.0f);
+    int last_iter = 0, last_v = 0;
+    int bsrc_variant = -1;
+
+    for (int corr = 1;; ++corr) {
+        const int v = ddt_variant(a, n_old);
+        const P* __restrict__ diag = a.pdiag2 + size_t(v) * n;
+        const P* __restrict__ rdiag = a.prdiag2 + size_t(v) * n;
+        const P* __restrict__ sumA = a.psumA2 + size_t(v) * n;
+        const double cft0 = a.cft0[v], cft00 = a.cft00[v];
+        // the iterate of the neighbours: Vm itself in the first corrector,
+        // the published pair afterwards
+        const bool from_vm = corr == 1;
+        const auto xq = [x, px, from_vm](unsigned q) {
+            return from_vm ? fp::split(__ldcg(&x[q])) : __ldcg(&px[q]);
+        };
+        CR* __restrict__ grad = static_cast<CR*>(a.grad);
+        if (a.nc_gw) {
+            for (unsigned c = first; c < n; c += stride) {
+                CR g[3];
+                nc_gradient<CR, W>(a, c, [&xq](long long q) { return fp::join(xq(unsigned(q))); },
+                                   g);
+                __stcg(&grad[c], g[0]);
+                __stcg(&grad[size_t(n) + c], g[1]);
+                __stcg(&grad[2 * size_t(n) + c], g[2]);
+            }
+            if (!grid_barrier(st, epoch, a.spin_limit)) { abort_step = true; break; }
+        }
+        // --- source (FP64, split), A.x, r = b - A.x; sums of x and |r|
+        P s1[2] = {fp::make(0.0f), fp::make(0.0f)};
+        const bool fresh = corr == 1 || v != bsrc_variant;
+        bsrc_variant = v;
+        for (unsigned c = first; c < n; c += stride) {
+            double rhs;
+            if (fresh) {
+                const double V = a.vol[c];
+                double ddt_src;
+                if (a.ddt_backward)
+                    ddt_src = a.rdt * V * (cft0 * a.vm_old[c] - cft00 * a.vm_oldold[c]);
+                else
+                    ddt_src = a.rdt * a.vm_old[c] * V;
+                double bb = a.chicm * ddt_src;
+                double su = -(a.chicm * a.iion[c]) * V;
+                su = su + box_source(a, c, t0) * V;
+                rhs = bb + su;
+                a.bsrc[c] = rhs;
+            } else {
+                rhs = a.bsrc[c];
+            }
+            if (a.nc_gw)
+                rhs = rhs + nc_correction<CR, W>(a, c, [grad, n](long long q, int k) {
+                          return __ldcg(&grad[size_t(k) * n + size_t(q)]);
+                      });
+            const P bc = fp::split(rhs, sh);
+            const P xc = xq(c);
+            const P axc = amul_pair<W>(a, ca, c, diag[c], xq);
+            const P rc = fp::sub(bc, axc);
+            b[c] = bc; ax[c] = axc; r[c] = rc;
+            if (from_vm) __stcg(&px[c], xc);
+            s1[0] = fp::add(s1[0], xc);
+            s1[1] = fp::add(s1[1], fp::abs(rc));
+        }
+        gsync::block_sums_pair<kCoopBlock, 2>(partial, set, s1);
+        if (!grid_barrier(st, epoch, a.spin_limit)) { abort_step = true; break; }
+        P g1[2];
+        gsync::grid_sums_pair<2>(partial, set, g1);
+        set ^= 1;
+        const P avg = fp::div(g1[0], count);
+        if (n_old < 1) n_old = 1;
+        if (a.ddt_backward && n_old < 2) n_old = 2;
+        // --- normFactor, z = D^-1 r (published), z.r
+        P s2[2] = {fp::make(0.0f), fp::make(0.0f)};
+        for (unsigned c = first; c < n; c += stride) {
+            const P pa = fp::mul(sumA[c], avg);
+            s2[0] = fp::add(s2[0], fp::add(fp::abs(fp::sub(ax[c], pa)), fp::abs(fp::sub(b[c], pa))));
+            const P rc = r[c];
+            const P zc = fp::mul(rdiag[c], rc);
+            __stcg(&z[c], zc);
+            s2[1] = fp::madd(zc, rc, s2[1]);
+        }
+        gsync::block_sums_pair<kCoopBlock, 2>(partial, set, s2);
+        if (!grid_barrier(st, epoch, a.spin_limit)) { abort_step = true; break; }
+        P g2[2];
+        gsync::grid_sums_pair<2>(partial, set, g2);
+        set ^= 1;
+        const P normf = fp::add(g2[0], small);
+        const P init_res = fp::div(g1[1], normf);
+        const P rel_init = fp::mul(rel, init_res);
+        P res = init_res;
+        P wArA = g2[1], beta = fp::make(0.0f);
+        int iter = 0;
+        bool aborted = false;
+        const auto conv = [&](P rr) {
+            return fp::less(rr, tol) || (use_rel && fp::less(rr, rel_init));
+        };
+        if (!conv(res)) {
+            for (;;) {
+                // --- halo pass: w = A.z, p = z + beta p, A.p = w + beta A.p
+                P s3[1] = {fp::make(0.0f)};
+                const bool first_it = iter == 0;
+                for (unsigned c = first; c < n; c += stride) {
+                    const P w = amul_pair<W>(a, ca, c, diag[c],
+                                             [z](unsigned q) { return __ldcg(&z[q]); });
+                    const P zc = __ldcg(&z[c]);
+                    P pc, qc;
+                    if (first_it) {
+                        pc = zc; qc = w;
+                    } else {
+                        pc = fp::madd(beta, p[c], zc);
+                        qc = fp::madd(beta, ap[c], w);
+                    }
+                    p[c] = pc; ap[c] = qc;
+                    s3[0] = fp::madd(qc, pc, s3[0]);
+                }
+                gsync::block_sums_pair<kCoopBlock, 1>(partial, set, s3);
+                if (!grid_barrier(st, epoch, a.spin_limit)) { aborted = true; break; }
+                P g3[1];
+                gsync::grid_sums_pair<1>(partial, set, g3);
+                set ^= 1;
+                if (g3[0].x == 0.0f) break;   // checkSingularity
+                const P alpha = fp::div(wArA, g3[0]);
+                const P nalpha = fp::neg(alpha);
+                // --- update pass: x, r, z; |r| and z.r
+                P s4[2] = {fp::make(0.0f), fp::make(0.0f)};
+                for (unsigned c = first; c < n; c += stride) {
+                    __stcg(&px[c], fp::madd(alpha, p[c], __ldcg(&px[c])));
+                    const P rc = fp::madd(nalpha, ap[c], r[c]);
+                    r[c] = rc;
+                    const P zc = fp::mul(rdiag[c], rc);
+                    __stcg(&z[c], zc);
+                    s4[0] = fp::add(s4[0], fp::abs(rc));
+                    s4[1] = fp::madd(zc, rc, s4[1]);
+                }
+                gsync::block_sums_pair<kCoopBlock, 2>(partial, set, s4);
+                if (!grid_barrier(st, epoch, a.spin_limit)) { aborted = true; break; }
+                P g4[2];
+                gsync::grid_sums_pair<2>(partial, set, g4);
+                set ^= 1;
+                res = fp::div(g4[0], normf);
+                ++iter;
+                ++step_iters;
+                if (conv(res) || iter >= max_iter) {
+                    if (!conv(res)) status |= CFG_ERR_PCG;
+                    break;
+                }
+                if (step_iters >= a.iter_cap) {
+                    status |= CFG_ERR_PCG;
+                    aborted = true;
+                    break;
+                }
+                beta = fp::div(g4[1], wArA);
+                wArA = g4[1];
+            }
+        }
+        // the solve's iterate back into Vm (own rows; the neighbours read px)
+        for (unsigned c = first; c < n; c += stride) x[c] = fp::join(__ldcg(&px[c]));
+        if (lead && n_solves < kMaxSolves) {
+            st->iters[n_solves] = iter;
+            st->init_r[n_solves] = fp::join(init_res);
+            st->final_r[n_solves] = fp::join(res);
+        }
+        ++n_solves;
+        last_init = init_res; last_res = res; last_iter = iter; last_v = v;
+        if (aborted) { abort_step = true; break; }
+        if (converged_outer || corr + 1 > n_outer) break;
+        if (fp::less(init_res, outer_tol)) converged_outer = true;
+    }
+    if (abort_step) status |= CFG_ERR_PCG;
+    else
+        for (unsigned c = first; c < n; c += stride)
+            activation(a, c, x[c], a.vm_old[c], t_step - a.dt);
+    if (lead) {
+        st->n_old = n_old;
+        st->n_solves = n_solves;
+        st->iter = last_iter;
+        st->init_res = fp::join(last_init);
+        st->res = fp::join(last_res);
+        st->variant = last_v;
+        st->step_iters = step_iters;
+        st->corr = n_solves + 1;
+        st->solve_active = 0;
+        st->outer_active = 0;
+        st->converged_outer = converged_outer ? 1 : 0;
+    }
+    if (status && threadIdx.x == 0) atomicOr(&st->status, status);
+}
+
 // Host helpers: fast-division constants and the cooperative launch.
 static FastDiv make_fastdiv(unsigned d)
 {
@@ -377,7 +639,9 @@ int coop_grid_blocks(long long n)
     per_sm = 1 << 30;
     const void* fns[] = {(const void*)k_implicit_coop<double, 0>, (const void*)k_implicit_coop<float, 0>,
                          (const void*)k_implicit_coop<double, 4>, (const void*)k_implicit_coop<float, 4>,
-                         (const void*)k_implicit_coop<double, 6>, (const void*)k_implicit_coop<float, 6>};
+                         (const void*)k_implicit_coop<double, 6>, (const void*)k_implicit_coop<float, 6>,
+                         (const void*)k_implicit_pair<float, 0>, (const void*)k_implicit_pair<float, 4>,
+                         (const void*)k_implicit_pair<float, 6>};
     for (const void* f : fns) {
         int k = 0;
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&k, f, kCoopBlock, 0) != cudaSuccess)
@@ -402,7 +666,10 @@ cudaError_t launch_implicit_coop(const DiffusionArgs& a, int blocks, cudaStream_
     // (tetrahedra) or 6 (hexahedra)
     const int w = (!a.sx && (a.width == 4 || a.width == 6)) ? a.width : 0;
     void* fn = nullptr;
-    if (a.nc_fp32)
+    if (a.pair)
+        fn = w == 4 ? (void*)k_implicit_pair<float, 4> : w == 6 ? (void*)k_implicit_pair<float, 6>
+                                                               : (void*)k_implicit_pair<float, 0>;
+    else if (a.nc_fp32)
         fn = w == 4 ? (void*)k_implicit_coop<float, 4> : w == 6 ? (void*)k_implicit_coop<float, 6>
                                                                 : (void*)k_implicit_coop<float, 0>;
     else

@@ -19,6 +19,7 @@
 #include <cuda_runtime.h>
 
 #include "../../include/cardiac_gpu.h"
+#include "float_pair.cuh"
 
 namespace cfg {
 
@@ -114,6 +115,18 @@ struct DiffusionArgs {
     // step constants
     double dt, chicm;
     int ddt_backward;
+    // float-pair form of the persistent solve (pair != 0): the matrix and
+    // the source scaled by 2^pair_shift (a power of two, so the scaled system
+    // has exactly the same solution and residual ratios) and held as (hi,
+    // lo) float pairs; b, r, z, A.x, p and A.p then hold pairs in their
+    // 8-byte slots, px the iterate
+    int pair, pair_shift;
+    float2* pdiag2;            // [2][n]
+    float2* prdiag2;           // [2][n] reciprocal of the scaled diagonal
+    float2* psumA2;            // [2][n]
+    float2* pcoef;             // [width][n]
+    float2 pcx, pcy, pcz;      // stencil form
+    float2* px;                // [n]
 };
 
 // ------------------------------------------------------------------ helpers

@@ -8,6 +8,8 @@
 
 #include <cuda_runtime.h>
 
+#include "float_pair.cuh"
+
 namespace cfg {
 namespace gsync {
 
@@ -120,6 +122,48 @@ __device__ __forceinline__ void block_scalars(double (&out)[K], F f)
 #pragma unroll
     for (int k = 0; k < K; ++k) out[k] = v[k];
     __syncthreads();   // v is written again by the next call
+}
+
+// Float-pair forms of block_sums / grid_sums (partial slots of 8 bytes hold
+// one pair).  Warp k adds the block's warp sums of value k in a fixed tree;
+// every block then adds the block sums in the same fixed order, so all
+// blocks hold bitwise the same totals.
+template <int kBlock, int K>
+__device__ __forceinline__ void block_sums_pair(float2* partial, int set, fp::P (&v)[K])
+{
+    constexpr int kWarps = kBlock / 32;
+    static_assert(kWarps <= 32 && K <= kWarps, "one warp per value");
+    __shared__ float2 sh[K][kWarps];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        const fp::P s = fp::warp_sum(v[k]);
+        if (lane == 0) sh[k][w] = s;
+    }
+    __syncthreads();
+    if (w < K) {
+        fp::P s = lane < kWarps ? sh[w][lane] : fp::make(0.0f);
+        s = fp::warp_sum(s);
+        if (lane == 0) __stcg(&partial[(size_t(set) * 2 + w) * gridDim.x + blockIdx.x], s);
+    }
+}
+
+template <int K>
+__device__ __forceinline__ void grid_sums_pair(const float2* partial, int set, fp::P (&out)[K])
+{
+    __shared__ float2 sh[K];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (w < K) {
+        const float2* src = partial + (size_t(set) * 2 + w) * gridDim.x;
+        fp::P s = fp::make(0.0f);
+        for (unsigned i = lane; i < gridDim.x; i += 32) s = fp::add(s, __ldcg(&src[i]));
+        s = fp::warp_sum(s);
+        if (lane == 0) sh[w] = s;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < K; ++k) out[k] = sh[k];
+    __syncthreads();
 }
 
 }  // namespace gsync

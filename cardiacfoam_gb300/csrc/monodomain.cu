@@ -28,10 +28,12 @@ __global__ void k_grad_start(DiffusionArgs a);
 
 static void md_free(cfg_monodomain* md)
 {
+    if (!md) return;
     dfree(md->d_apd);
     dfree(md->d_apd_ring_t);
     dfree(md->d_apd_ring_v);
-    if (!md) return;
+    dfree(md->d_pdiag2); dfree(md->d_prdiag2); dfree(md->d_psumA2); dfree(md->d_pcoef);
+    dfree(md->d_px);
     if (md->graph_exec) cudaGraphExecDestroy(md->graph_exec);
     for (cudaEvent_t& e : md->ev)
         if (e) cudaEventDestroy(e);
@@ -219,6 +221,7 @@ static int build_operator(cfg_monodomain* md, const cfg_mesh_desc* m, const cfg_
     CFG_CUDA_TRY(dmalloc(&md->d_col, col.size()));
     CFG_CUDA_TRY(dmalloc(&md->d_coef, coef.size()));
     CFG_CUDA_TRY(dmalloc(&md->d_cnt, cnt.size()));
+    for (double v : lapdiag) md->max_neglap = std::max(md->max_neglap, -v);
     CFG_CUDA_TRY(dmalloc(&md->d_lapdiag, lapdiag.size()));
     CFG_CUDA_TRY(cudaMemcpy(md->d_col, col.data(), col.size() * sizeof(int), cudaMemcpyHostToDevice));
     CFG_CUDA_TRY(cudaMemcpy(md->d_coef, coef.data(), coef.size() * sizeof(double),
@@ -257,6 +260,18 @@ static int build_operator(cfg_monodomain* md, const cfg_mesh_desc* m, const cfg_
         md->ell_bytes += (gw.size() + kc.size() + om.size()) * esz;
     }
     return CFG_OK;
+}
+
+static cudaError_t alloc_pairs(cfg_monodomain* md)
+{
+    if (md->d_px) return cudaSuccess;
+    const size_t n = size_t(md->n);
+    cudaError_t e = dmalloc(&md->d_pdiag2, 2 * n);
+    if (!e) e = dmalloc(&md->d_prdiag2, 2 * n);
+    if (!e) e = dmalloc(&md->d_psumA2, 2 * n);
+    if (!e) e = dmalloc(&md->d_pcoef, size_t(md->width > 0 ? md->width : 1) * n);
+    if (!e) e = dmalloc(&md->d_px, n);
+    return e;
 }
 
 static void fill_args(cfg_monodomain* md, double dt)
@@ -307,6 +322,21 @@ static void fill_args(cfg_monodomain* md, double dt)
     a.iter_cap = md->iter_cap;
     a.spin_limit = md->spin_limit;
     a.src_total = md->d_src_total;
+    // float pairs: the system scaled by the power of two that brings its
+    // largest diagonal near one
+    a.pair = (md->pair && md->persistent && md->implicit) ? 1 : 0;
+    if (a.pair) {
+        const double dmax = md->chicm * 2.0 * md->max_vol / dt + md->max_neglap;
+        a.pair_shift = dmax > 0 ? -std::ilogb(dmax) : 0;
+        a.pdiag2 = md->d_pdiag2; a.prdiag2 = md->d_prdiag2; a.psumA2 = md->d_psumA2;
+        a.pcoef = md->d_pcoef; a.px = md->d_px;
+        const auto hsplit = [&](double v) {
+            const double w = std::ldexp(v, a.pair_shift);
+            const float h = float(w);
+            return make_float2(h, float(w - double(h)));
+        };
+        a.pcx = hsplit(md->cx); a.pcy = hsplit(md->cy); a.pcz = hsplit(md->cz);
+    }
     // ddt coefficients (EulerDdtScheme; backwardDdtScheme with deltaT0 =
     // GREAT while fewer than two old-time levels exist, then deltaT0 = dt)
     a.rdt = 1.0 / dt;
@@ -384,6 +414,11 @@ int monodomain_create(const cfg_monodomain_desc* d, const cfg_mesh_desc* m, cfg_
     if (!e) e = dmalloc(&md->d_partial, size_t(4) * nblocks);
     if (!e) e = dmalloc(&md->d_act_flag, n);
     if (!e) e = dmalloc(&md->d_st, 1);
+    for (size_t c = 0; c < n; ++c) md->max_vol = std::max(md->max_vol, m->volumes[c]);
+    if (!e && d->ionic.precision == CFG_PRECISION_MIXED) {
+        e = alloc_pairs(md);
+        md->pair = !e;
+    }
     if (!e) e = cudaMallocHost(reinterpret_cast<void**>(&md->h_st), sizeof(PcgState));
     if (e) return bail(fail(CFG_ERR_CUDA, "device allocation failed: %s", cudaGetErrorString(e)));
     // box membership (boundBox::contains is inclusive)
@@ -852,7 +887,30 @@ int cfg_monodomain_set_persistent(cfg_monodomain* md, int enable)
     if (!md) return fail(CFG_ERR_INVALID, "null context");
     if (enable && md->coop_blocks <= 0)
         return fail(CFG_ERR_UNSUPPORTED, "cooperative launch is not available on this device");
+    if (md->persistent != (enable != 0))
+        md->prepared_dt = 0.0;   // the pair operator follows the persistent kernel
     md->persistent = enable != 0;
+    return CFG_OK;
+}
+
+int cfg_monodomain_set_pcg_arithmetic(cfg_monodomain* md, int arithmetic)
+{
+    if (!md) return fail(CFG_ERR_INVALID, "null context");
+    if (arithmetic != CFG_PCG_FP64 && arithmetic != CFG_PCG_FLOAT_PAIRS)
+        return fail(CFG_ERR_INVALID, "unknown PCG arithmetic %d", arithmetic);
+    const bool pair = arithmetic == CFG_PCG_FLOAT_PAIRS;
+    if (pair) {
+        const cudaError_t e = alloc_pairs(md);
+        if (e) return fail(CFG_ERR_CUDA, "device allocation failed: %s", cudaGetErrorString(e));
+    }
+    if (pair != md->pair) {
+        md->pair = pair;
+        md->prepared_dt = 0.0;   // the pair operator is prepared with the next step
+        if (md->graph_exec) {
+            cudaGraphExecDestroy(md->graph_exec);
+            md->graph_exec = nullptr;
+        }
+    }
     return CFG_OK;
 }
 

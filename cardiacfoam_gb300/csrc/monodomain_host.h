@@ -48,6 +48,14 @@ struct cfg_monodomain {
     double *d_b = nullptr, *d_r = nullptr, *d_z = nullptr, *d_ax = nullptr, *d_pA = nullptr,
            *d_pB = nullptr, *d_ap = nullptr;
     double* d_partial = nullptr;
+    // float-pair PCG of the persistent solve (CFG_PCG_FLOAT_PAIRS, the mixed
+    // form's default): the scaled operator as pairs and the published
+    // iterate; the scale follows from the largest diagonal, bounded by
+    // chi Cm 2 V_max / dt + max(-lapdiag)
+    bool pair = false;
+    float2 *d_pdiag2 = nullptr, *d_prdiag2 = nullptr, *d_psumA2 = nullptr, *d_pcoef = nullptr,
+           *d_px = nullptr;
+    double max_vol = 0.0, max_neglap = 0.0;
     cfg::PcgState* d_st = nullptr;
     cfg::PcgState* h_st = nullptr;   // pinned mirror
     cfg::DiffusionArgs args{};

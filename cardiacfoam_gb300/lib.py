@@ -60,6 +60,7 @@ class IonicDesc(C.Structure):
 
 GRAD_LEAST_SQUARES, GRAD_GAUSS_LINEAR = 0, 1
 ECG_FP64, ECG_FLOAT_PAIRS = 0, 1
+PCG_FP64, PCG_FLOAT_PAIRS = 0, 1
 
 
 class MeshDesc(C.Structure):
@@ -161,6 +162,7 @@ EXPORTS = [
     "cfg_monodomain_last_stats", "cfg_monodomain_set_timing", "cfg_monodomain_timings",
     "cfg_monodomain_stream", "cfg_monodomain_destroy", "cfg_box_diffusion_solve_noalloc",
     "cfg_monodomain_set_persistent", "cfg_monodomain_suggest_explicit_delta_t",
+    "cfg_monodomain_set_pcg_arithmetic", "cfg_bidomain_set_pcg_arithmetic",
     "cfg_monodomain_delta_t", "cfg_monodomain_set_delta_t", "cfg_monodomain_set_wait_limit",
     "cfg_pseudo_ecg_set_wait_limit", "cfg_monodomain_track_apd", "cfg_monodomain_apd_results",
     "cfg_purkinje_create", "cfg_purkinje_step", "cfg_purkinje_couple", "cfg_purkinje_get_field",
@@ -230,6 +232,8 @@ def load(path: Optional[os.PathLike] = None):
     L.cfg_monodomain_stream.restype = C.c_void_p
     L.cfg_monodomain_destroy.argtypes = [C.c_void_p]
     L.cfg_monodomain_set_persistent.argtypes = [C.c_void_p, C.c_int]
+    L.cfg_monodomain_set_pcg_arithmetic.argtypes = [C.c_void_p, C.c_int]
+    L.cfg_bidomain_set_pcg_arithmetic.argtypes = [C.c_void_p, C.c_int]
     L.cfg_monodomain_suggest_explicit_delta_t.argtypes = [C.c_void_p, C.c_double, _dp]
     L.cfg_monodomain_delta_t.argtypes = [C.c_void_p, _dp]
     L.cfg_monodomain_set_delta_t.argtypes = [C.c_void_p, C.c_double]

@@ -309,6 +309,18 @@ int cfg_monodomain_timings(const cfg_monodomain* md, double* ionic_ms, double* d
  * sums.  MonodomainSolver::solveDiffusionImplicit (monodomainSolver.C:112-150)
  * is what either form computes. */
 int cfg_monodomain_set_persistent(cfg_monodomain* md, int enable);
+#define CFG_PCG_FP64 0          /* operator, vectors and sums in FP64 */
+#define CFG_PCG_FLOAT_PAIRS 1   /* (hi, lo) float pairs, about 48 significant bits,
+                                   on the FP32 pipe; the system scaled by a power
+                                   of two */
+/* Arithmetic of the persistent implicit solve: the PCG of
+ * MonodomainSolver::solveDiffusionImplicit (monodomainSolver.C:112-150,
+ * lduMatrix PCG with its normFactor and convergence test) in FP64, or in
+ * float pairs, the default of CFG_PRECISION_MIXED contexts (GB300 issues
+ * FP64 at 1/64 of the FP32 rate).  The source of each corrector is formed in
+ * FP64 either way.  The kernel sequence (cfg_monodomain_set_persistent(md,
+ * 0)) always runs FP64. */
+int cfg_monodomain_set_pcg_arithmetic(cfg_monodomain* md, int arithmetic);
 /* Per-cell beat detection on the tissue's Vm: after every `every_steps`-th
  * step (and once at the call, the field as it is) each cell's Vm [mV] and
  * the time go through the reference's restitution post-processing as a
@@ -494,6 +506,13 @@ int cfg_bidomain_create(const cfg_bidomain_desc* desc, const cfg_mesh_desc* mesh
  * gradScheme). */
 int cfg_bidomain_create_from_dict(const char* electro_properties, const cfg_mesh_desc* mesh,
                                   double delta_t, int precision, cfg_bidomain** out);
+/* Arithmetic of the cooperative PCG solves of both bidomain systems (the
+ * phiE and Vm solves of BidomainSolver, bidomainSolver.C:201-245, lduMatrix
+ * PCG): CFG_PCG_FP64, or CFG_PCG_FLOAT_PAIRS, the default of
+ * CFG_PRECISION_MIXED contexts.  The systems are assembled in FP64 either
+ * way; float pairs need the cooperative solve (CFG_ERR_UNSUPPORTED where
+ * the device has none). */
+int cfg_bidomain_set_pcg_arithmetic(cfg_bidomain* bd, int arithmetic);
 /* One time step (runTime++ then the staggered advance, as
  * cfg_monodomain_step). */
 int cfg_bidomain_step(cfg_bidomain* bd, double dt);

@@ -2,7 +2,8 @@
 restatement of BidomainSolver: the manufactured case (FP64, both
 preconditioners of the oracle), a propagating TNNP slab, second-order
 convergence of the manufactured run, a tetrahedral left ventricle with the
-Laplacians' explicit corrections, and the explicit algorithm."""
+Laplacians' explicit corrections, and the explicit algorithm; the PCG of
+both systems in FP64 and in float pairs."""
 import numpy as np
 import pytest
 
@@ -42,13 +43,17 @@ def _close(a, b, tol):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("dic", [False, True], ids=["diagonal", "dic"])
-def test_manufactured_matches_oracle(gpu_lib, oracle, dic):
+@pytest.mark.parametrize("dic,arithmetic", [(False, lib.PCG_FP64), (False, lib.PCG_FLOAT_PAIRS),
+                                            (True, lib.PCG_FP64)],
+                         ids=["diagonal", "diagonal-float-pairs", "dic"])
+def test_manufactured_matches_oracle(gpu_lib, oracle, dic, arithmetic):
     """8^3 cube, 20 steps: with the same (diagonal) preconditioner Vm, phiE and
-    phiI within 1e-9 and PCG iteration counts within one; against the
-    reference's DIC preconditioner within the solver tolerance's reach."""
+    phiI within 1e-9 and PCG iteration counts within one, with the GPU's PCG
+    in FP64 or in float pairs; against the reference's DIC preconditioner
+    within the solver tolerance's reach."""
     dt = 2e-3
     mesh, bd = _gpu_mms(3, 8, dt)
+    bd.set_pcg_arithmetic(arithmetic)
     B = _oracle_mms(oracle, mesh, 3, dt, dic)
     assert bd.reference_cell() == B.ref_cell()
     tol = 1e-9 if not dic else 1e-7
@@ -112,7 +117,9 @@ def test_manufactured_convergence(gpu_lib):
 
 
 @pytest.mark.gpu
-def test_tetrahedral_lv_matches_oracle(gpu_lib, oracle):
+@pytest.mark.parametrize("arithmetic", [lib.PCG_FP64, lib.PCG_FLOAT_PAIRS],
+                         ids=["fp64", "float-pairs"])
+def test_tetrahedral_lv_matches_oracle(gpu_lib, oracle, arithmetic):
     """A tetrahedral left ventricle (4,104 tets): non-orthogonal faces, so
     both Laplacians carry their explicit corrections (Gauss linear corrected,
     leastSquares gradient) in the phiE and the Vm solve.  Vm, phiE and the
@@ -125,6 +132,7 @@ def test_tetrahedral_lv_matches_oracle(gpu_lib, oracle):
     bd = api.Bidomain(L.mesh, "TNNP", "epicardialCells", sigma_i=gi, sigma_e=ge, dt=dt,
                       pcg_tol=1e-10, phie_tol=1e-10, n_outer=2, ref_point=(0.0, 0.0, 0.0),
                       boxes=box)
+    bd.set_pcg_arithmetic(arithmetic)
     d = oracle.tissue_desc("TNNP", 1, gi, implicit=True, precond_dic=False, pcg_tol=1e-10,
                            pcg_rel_tol=0.0, n_outer=2, outer_tol=0.0, boxes=box)
     B = oracle.Bidomain(d, ge, oracle.Mesh.general(L.mesh), (0.0, 0.0, 0.0), 0.0, 1e-10, 0.0,
@@ -197,3 +205,29 @@ def test_explicit_algorithm_matches_oracle(gpu_lib, oracle):
     assert np.array_equal(ag > 0, ao > 0) and (ag > 0).sum() > 20
     assert np.max(np.abs(ag - ao)) < 1e-9
     bd.close()
+
+
+@pytest.mark.gpu
+def test_mixed_form_float_pairs_against_fp64_pcg(gpu_lib):
+    """Mixed ionic form on the propagating TNNP slab: the default float-pair
+    PCG against the FP64 PCG of the same context type (Vm and phiE within
+    1e-9 of their scale, the same activated cells within 1e-8 s)."""
+    h, dt = 2.5e-4, 2e-5
+    mesh = with_box_geometry(box_mesh(24, 8, 2, 24 * h, 8 * h, 2 * h), 24 * h, 8 * h, 2 * h)
+    box = [((0.0, 0.0, 0.0), (1.0e-3, 2 * h * 8, 2 * h), 0.0, 1e-3, 1e5)]
+    gi, ge = (0.17, 0.0, 0.0, 0.019, 0.0, 0.019), (0.62, 0.0, 0.0, 0.24, 0.0, 0.24)
+    runs = []
+    for arithmetic in (lib.PCG_FP64, lib.PCG_FLOAT_PAIRS):
+        bd = api.Bidomain(mesh, "TNNP", "epicardialCells", sigma_i=gi, sigma_e=ge, dt=dt,
+                          pcg_tol=1e-10, phie_tol=1e-10, n_outer=2, ref_point=(0.0, 0.0, 0.0),
+                          boxes=box, precision=lib.PRECISION_MIXED)
+        bd.set_pcg_arithmetic(arithmetic)
+        for _ in range(200):
+            bd.step(dt)
+        runs.append((bd.vm(), bd.phie(), bd.activation()))
+        bd.close()
+    (va, pa, aa), (vb, pb, ab) = runs
+    assert _close(vb, va, 1e-9)
+    assert _close(pb, pa, 1e-9)
+    assert np.array_equal(aa > 0, ab > 0) and (aa > 0).sum() > 20
+    assert np.max(np.abs(aa - ab)) < 1e-8
