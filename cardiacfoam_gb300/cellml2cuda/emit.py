@@ -335,12 +335,26 @@ class _TissuePrinter(_CudaPrinter):
     algebraics read from the per-cell values H (see hoist.py); a read before
     such an algebraic's assignment is the zeroed scratch, as in the body."""
 
-    def __init__(self, m: Model, early: List[str], invariant, needed):
+    def __init__(self, m: Model, early: List[str], invariant, needed, recip=frozenset()):
         super().__init__(m, early, "rhs")
         self.invariant = set(invariant)
         self.needed = list(needed)
         self.hoisted_defined = set()
         self.subtrees: Dict[Node, int] = {}   # expression -> its slot after `needed`
+        # slots read only as divisors hold their reciprocal (cfg_hrcp) and
+        # are read through cfg_hdiv; the first pass counts the uses
+        self.recip = set(recip)
+        self.div_uses: Dict[str, int] = {}
+        self.other_uses: Dict[str, int] = {}
+
+    def _slot(self, e: Node):
+        """The H slot an expression reads, or None."""
+        if isinstance(e, Ref) and e.array == "ALGEBRAIC" and e.name in self.invariant:
+            return f"H_{e.name}" if e.name in self.hoisted_defined else None
+        if self._extractable(e):
+            k = self.subtrees.setdefault(e, len(self.subtrees))
+            return str(len(self.needed) + k)
+        return None
 
     def _extractable(self, e: Node) -> bool:
         """A subexpression of a statement that depends on the membrane
@@ -369,16 +383,26 @@ class _TissuePrinter(_CudaPrinter):
         return special
 
     def __call__(self, e: Node) -> str:
-        if self._extractable(e):
-            k = self.subtrees.setdefault(e, len(self.subtrees))
-            return f"H({len(self.needed) + k})"
+        if isinstance(e, Bin) and e.op == "/":
+            slot = self._slot(e.r)
+            if slot is not None:
+                self.div_uses[slot] = self.div_uses.get(slot, 0) + 1
+                if slot in self.recip:
+                    return f"cfg_hdiv({self(e.l)}, H({slot}))"
+                return f"({self(e.l)} / H({slot}))"
+        slot = self._slot(e) if not isinstance(e, Ref) else None
+        if slot is not None:
+            self.other_uses[slot] = self.other_uses.get(slot, 0) + 1
+            return f"H({slot})"
         return super().__call__(e)
 
     def ref(self, r: Ref) -> str:
         if r.array == "ALGEBRAIC" and r.name in self.invariant:
             if r.name not in self.hoisted_defined:
                 return "R(0)"
-            return f"H(H_{r.name})"
+            slot = f"H_{r.name}"
+            self.other_uses[slot] = self.other_uses.get(slot, 0) + 1
+            return f"H({slot})"
         return super().ref(r)
 
 
@@ -427,8 +451,10 @@ def _emit_tissue_rhs(m: Model, L: List[str]):
     # the rest of the body first: it finds the subexpressions H also keeps
     rest: List[str] = []
     subtrees: Dict[Node, int] = {}
-    if h.needed:
-        pr = _TissuePrinter(m, use_before_def(m.rates), h.invariant, h.needed)
+    recip: set = set()
+
+    def print_rest(recip_slots):
+        pr = _TissuePrinter(m, use_before_def(m.rates), h.invariant, h.needed, recip_slots)
         body = []
         for name in _predeclare_conditional_algebraics(m, m.rates, body, "    "):
             if name in h.invariant:
@@ -436,6 +462,14 @@ def _emit_tissue_rhs(m: Model, L: List[str]):
             body.append(f"    R a_{name} = R(0);")
             pr.defined.add(name)
         _cuda_body_tissue(m, m.rates, pr, "    ", body)
+        return pr, body
+
+    if h.needed:
+        # pass 1 finds the slots read only as divisors, pass 2 prints
+        pr, _ = print_rest(frozenset())
+        recip = {k for k in pr.div_uses if k not in pr.other_uses}
+        recip.discard(f"H_{m.iion_name}")
+        pr, body = print_rest(frozenset(recip))
         rest.extend(_state_loads(m, pr))
         rest.extend(body)
         if m.iion_name in h.invariant:
@@ -468,9 +502,12 @@ def _emit_tissue_rhs(m: Model, L: List[str]):
             pr.defined.add(name)
         _cuda_body(m, stmts, pr, "    ", body)
         for a in h.needed:
-            body.append(f"    H[H_{a}] = a_{a};")
+            v = f"cfg_hrcp(a_{a})" if f"H_{a}" in recip else f"a_{a}"
+            body.append(f"    H[H_{a}] = {v};")
         for e, k in sorted(subtrees.items(), key=lambda kv: kv[1]):
-            body.append(f"    H[{len(h.needed) + k}] = {pr(e)};")
+            slot = str(len(h.needed) + k)
+            v = f"cfg_hrcp({pr(e)})" if slot in recip else pr(e)
+            body.append(f"    H[{slot}] = {v};")
         if set(pr.states_read) - {vm}:
             raise ValueError(f"{m.name}: hoisted statements read {pr.states_read}")
         L.extend(body)

@@ -50,6 +50,17 @@ CFG_HD __forceinline__ double cfg_expm1(double x) { return exp(x) - 1.0; }
 CFG_HD __forceinline__ float cfg_expm1(float x) { return expm1f(x); }
 CFG_HD __forceinline__ float cfg_pow(float x, float y) { return powf(x, y); }
 
+// Division by a value the tissue form keeps per cell and step (a rate
+// constant or time constant of the membrane potential alone): the hoisted
+// slot holds cfg_hrcp(v) and each stage evaluates cfg_hdiv(a, slot).  In
+// double that is exactly a / v; in float (the mixed form, where a division
+// is already a reciprocal and a product) the reciprocal is formed once per
+// step instead of at every stage.
+CFG_HD __forceinline__ double cfg_hrcp(double v) { return v; }
+CFG_HD __forceinline__ float cfg_hrcp(float v) { return 1.0f / v; }
+CFG_HD __forceinline__ double cfg_hdiv(double a, double h) { return a / h; }
+CFG_HD __forceinline__ float cfg_hdiv(float a, float h) { return a * h; }
+
 template <int N, class R>
 CFG_HD __forceinline__ R cfg_ipow(R x)
 {

@@ -255,10 +255,10 @@ __device__ __forceinline__ void hoist(R y_u, const KS& K, int tissue, R* H)
     R a_wInfty = (((R(1.0) - (((y_u - K(C_thetaO))) > R(0) ? 1 : 0)) * (R(1.0) - (y_u / K(C_tauWInfty)))) + ((((y_u - K(C_thetaO))) > R(0) ? 1 : 0) * K(C_wInftyStar)));
     H[H_Jso] = a_Jso;
     H[H_vInfty] = a_vInfty;
-    H[H_tauVMinus] = a_tauVMinus;
+    H[H_tauVMinus] = cfg_hrcp(a_tauVMinus);
     H[H_wInfty] = a_wInfty;
-    H[H_tauWMinus] = a_tauWMinus;
-    H[H_tauS] = a_tauS;
+    H[H_tauWMinus] = cfg_hrcp(a_tauWMinus);
+    H[H_tauS] = cfg_hrcp(a_tauS);
     H[6] = ((R(1.0) + cfg_tanh((K(C_kS) * (y_u - K(C_uS))))) / R(2.0));
 }
 template <class R, class YS, class KS, class HS>
@@ -273,9 +273,9 @@ __device__ __forceinline__ R rhs_tissue(double t, const YS& Y, const KS& K, cons
     R a_Jfi = (((((-y_v) * (((y_u - K(C_thetaV))) > R(0) ? 1 : 0)) * (y_u - K(C_thetaV))) * (K(C_uU) - y_u)) / K(C_tauFi));
     R a_Jsi = ((((-(((y_u - K(C_thetaW))) > R(0) ? 1 : 0)) * y_w) * y_s) / K(C_tauSi));
     R a_Jion = ((a_Jfi + H(H_Jso)) + a_Jsi);
-    dydt[S_v] = ((((R(1.0) - (((y_u - K(C_thetaV))) > R(0) ? 1 : 0)) * (H(H_vInfty) - y_v)) / H(H_tauVMinus)) - (((((y_u - K(C_thetaV))) > R(0) ? 1 : 0) * y_v) / K(C_tauVPlus)));
-    dydt[S_w] = ((((R(1.0) - (((y_u - K(C_thetaW))) > R(0) ? 1 : 0)) * (H(H_wInfty) - y_w)) / H(H_tauWMinus)) - (((((y_u - K(C_thetaW))) > R(0) ? 1 : 0) * y_w) / K(C_tauWPlus)));
-    dydt[S_s] = ((H(6) - y_s) / H(H_tauS));
+    dydt[S_v] = (cfg_hdiv(((R(1.0) - (((y_u - K(C_thetaV))) > R(0) ? 1 : 0)) * (H(H_vInfty) - y_v)), H(H_tauVMinus)) - (((((y_u - K(C_thetaV))) > R(0) ? 1 : 0) * y_v) / K(C_tauVPlus)));
+    dydt[S_w] = (cfg_hdiv(((R(1.0) - (((y_u - K(C_thetaW))) > R(0) ? 1 : 0)) * (H(H_wInfty) - y_w)), H(H_tauWMinus)) - (((((y_u - K(C_thetaW))) > R(0) ? 1 : 0) * y_w) / K(C_tauWPlus)));
+    dydt[S_s] = cfg_hdiv((H(6) - y_s), H(H_tauS));
     R a_Istim = (SOLVE_VM ? R(cfg_stimulus_current<double>(t, stim)) : R(0));
     if (SOLVE_VM) {
         dydt[S_u] = ((-a_Jion) - a_Istim);

@@ -453,34 +453,34 @@ __device__ __forceinline__ void hoist(R y_V, const KS& K, int tissue, R* H)
     R a_beta_xs = (R(1.00000) / (R(1.00000) + cfg_exp(((y_V - R(60.0000)) / R(20.0000)))));
     R a_tau_xs = ((R(1.00000) * a_alpha_xs) * a_beta_xs);
     H[H_m_inf] = a_m_inf;
-    H[H_tau_m] = a_tau_m;
+    H[H_tau_m] = cfg_hrcp(a_tau_m);
     H[H_h_inf] = a_h_inf;
-    H[H_tau_h] = a_tau_h;
+    H[H_tau_h] = cfg_hrcp(a_tau_h);
     H[H_j_inf] = a_j_inf;
-    H[H_tau_j] = a_tau_j;
+    H[H_tau_j] = cfg_hrcp(a_tau_j);
     H[H_d_inf] = a_d_inf;
-    H[H_tau_d] = a_tau_d;
+    H[H_tau_d] = cfg_hrcp(a_tau_d);
     H[H_f_inf] = a_f_inf;
-    H[H_tau_f] = a_tau_f;
+    H[H_tau_f] = cfg_hrcp(a_tau_f);
     H[H_s_inf] = a_s_inf;
-    H[H_tau_s] = a_tau_s;
+    H[H_tau_s] = cfg_hrcp(a_tau_s);
     H[H_r_inf] = a_r_inf;
-    H[H_tau_r] = a_tau_r;
+    H[H_tau_r] = cfg_hrcp(a_tau_r);
     H[H_xr1_inf] = a_xr1_inf;
-    H[H_tau_xr1] = a_tau_xr1;
+    H[H_tau_xr1] = cfg_hrcp(a_tau_xr1);
     H[H_xr2_inf] = a_xr2_inf;
-    H[H_tau_xr2] = a_tau_xr2;
+    H[H_tau_xr2] = cfg_hrcp(a_tau_xr2);
     H[H_xs_inf] = a_xs_inf;
-    H[H_tau_xs] = a_tau_xs;
-    H[20] = ((R(1.00000) + (R(0.124500) * cfg_exp(((((-R(0.100000)) * y_V) * K(C_F)) / (K(C_R) * K(C_T)))))) + (R(0.0353000) * cfg_exp((((-y_V) * K(C_F)) / (K(C_R) * K(C_T))))));
-    H[21] = cfg_exp((((K(C_gamma_NCX) * y_V) * K(C_F)) / (K(C_R) * K(C_T))));
-    H[22] = (cfg_exp(((((K(C_gamma_NCX) - R(1.00000)) * y_V) * K(C_F)) / (K(C_R) * K(C_T)))) * cfg_ipow<3>(K(C_Na_o)));
-    H[23] = (((cfg_ipow<3>(K(C_Km_Nai)) + cfg_ipow<3>(K(C_Na_o))) * (K(C_Km_Ca) + K(C_Ca_o))) * (R(1.00000) + (K(C_K_sat) * cfg_exp(((((K(C_gamma_NCX) - R(1.00000)) * y_V) * K(C_F)) / (K(C_R) * K(C_T)))))));
+    H[H_tau_xs] = cfg_hrcp(a_tau_xs);
+    H[20] = cfg_hrcp(((R(1.00000) + (R(0.124500) * cfg_exp(((((-R(0.100000)) * y_V) * K(C_F)) / (K(C_R) * K(C_T)))))) + (R(0.0353000) * cfg_exp((((-y_V) * K(C_F)) / (K(C_R) * K(C_T)))))));
+    H[21] = cfg_hrcp((((cfg_ipow<3>(K(C_Km_Nai)) + cfg_ipow<3>(K(C_Na_o))) * (K(C_Km_Ca) + K(C_Ca_o))) * (R(1.00000) + (K(C_K_sat) * cfg_exp(((((K(C_gamma_NCX) - R(1.00000)) * y_V) * K(C_F)) / (K(C_R) * K(C_T))))))));
+    H[22] = cfg_exp((((K(C_gamma_NCX) * y_V) * K(C_F)) / (K(C_R) * K(C_T))));
+    H[23] = (cfg_exp(((((K(C_gamma_NCX) - R(1.00000)) * y_V) * K(C_F)) / (K(C_R) * K(C_T)))) * cfg_ipow<3>(K(C_Na_o)));
     H[24] = cfg_sqrt((K(C_K_o) / R(5.40000)));
     H[25] = (K(C_g_Kr) * cfg_sqrt((K(C_K_o) / R(5.40000))));
-    H[26] = cfg_exp((((R(2.00000) * y_V) * K(C_F)) / (K(C_R) * K(C_T))));
-    H[27] = cfg_expm1((((R(2.00000) * y_V) * K(C_F)) / (K(C_R) * K(C_T))));
-    H[28] = (R(1.00000) + cfg_exp(((R(25.0000) - y_V) / R(5.98000))));
+    H[26] = cfg_hrcp(cfg_expm1((((R(2.00000) * y_V) * K(C_F)) / (K(C_R) * K(C_T)))));
+    H[27] = cfg_exp((((R(2.00000) * y_V) * K(C_F)) / (K(C_R) * K(C_T))));
+    H[28] = cfg_hrcp((R(1.00000) + cfg_exp(((R(25.0000) - y_V) / R(5.98000)))));
 }
 template <class R, class YS, class KS, class HS>
 __device__ __forceinline__ R rhs_tissue(double t, const YS& Y, const KS& K, const HS& H, R* dydt, int tissue, const CfgStimulus& stim)
@@ -504,30 +504,30 @@ __device__ __forceinline__ R rhs_tissue(double t, const YS& Y, const KS& K, cons
     const R y_r = Y(S_r);
     const R y_Ca_SR = Y(S_Ca_SR);
     const R y_g = Y(S_g);
-    dydt[S_m] = ((H(H_m_inf) - y_m) / H(H_tau_m));
-    dydt[S_h] = ((H(H_h_inf) - y_h) / H(H_tau_h));
-    dydt[S_j] = ((H(H_j_inf) - y_j) / H(H_tau_j));
-    dydt[S_d] = ((H(H_d_inf) - y_d) / H(H_tau_d));
-    dydt[S_f] = ((H(H_f_inf) - y_f) / H(H_tau_f));
+    dydt[S_m] = cfg_hdiv((H(H_m_inf) - y_m), H(H_tau_m));
+    dydt[S_h] = cfg_hdiv((H(H_h_inf) - y_h), H(H_tau_h));
+    dydt[S_j] = cfg_hdiv((H(H_j_inf) - y_j), H(H_tau_j));
+    dydt[S_d] = cfg_hdiv((H(H_d_inf) - y_d), H(H_tau_d));
+    dydt[S_f] = cfg_hdiv((H(H_f_inf) - y_f), H(H_tau_f));
     R a_alpha_fCa = (R(1.00000) / (R(1.00000) + cfg_ipow<8>((y_Ca_i / R(0.000325000)))));
     R a_beta_fCa = (R(0.100000) / (R(1.00000) + cfg_exp(((y_Ca_i - R(0.000500000)) / R(0.000100000)))));
     R a_beta_d = (R(0.200000) / (R(1.00000) + cfg_exp(((y_Ca_i - R(0.000750000)) / R(0.000800000)))));
     R a_fCa_inf = ((((a_alpha_fCa + a_beta_fCa) + a_beta_d) + R(0.230000)) / R(1.46000));
     R a_d_fCa = ((a_fCa_inf - y_fCa) / K(C_tau_fCa));
     dydt[S_fCa] = (((a_fCa_inf > y_fCa) && (y_V > (-R(60.0000)))) ? R(0.00000) : a_d_fCa);
-    dydt[S_s] = ((H(H_s_inf) - y_s) / H(H_tau_s));
-    dydt[S_r] = ((H(H_r_inf) - y_r) / H(H_tau_r));
-    dydt[S_Xr1] = ((H(H_xr1_inf) - y_Xr1) / H(H_tau_xr1));
-    dydt[S_Xr2] = ((H(H_xr2_inf) - y_Xr2) / H(H_tau_xr2));
-    dydt[S_Xs] = ((H(H_xs_inf) - y_Xs) / H(H_tau_xs));
+    dydt[S_s] = cfg_hdiv((H(H_s_inf) - y_s), H(H_tau_s));
+    dydt[S_r] = cfg_hdiv((H(H_r_inf) - y_r), H(H_tau_r));
+    dydt[S_Xr1] = cfg_hdiv((H(H_xr1_inf) - y_Xr1), H(H_tau_xr1));
+    dydt[S_Xr2] = cfg_hdiv((H(H_xr2_inf) - y_Xr2), H(H_tau_xr2));
+    dydt[S_Xs] = cfg_hdiv((H(H_xs_inf) - y_Xs), H(H_tau_xs));
     R a_g_inf = ((y_Ca_i < R(0.000350000)) ? (R(1.00000) / (R(1.00000) + cfg_ipow<6>((y_Ca_i / R(0.000350000))))) : (R(1.00000) / (R(1.00000) + cfg_ipow<16>((y_Ca_i / R(0.000350000))))));
     R a_d_g = ((a_g_inf - y_g) / K(C_tau_g));
     dydt[S_g] = (((a_g_inf > y_g) && (y_V > (-R(60.0000)))) ? R(0.00000) : a_d_g);
-    R a_i_NaK = (((((K(C_P_NaK) * K(C_K_o)) / (K(C_K_o) + K(C_K_mk))) * y_Na_i) / (y_Na_i + K(C_K_mNa))) / H(20));
+    R a_i_NaK = cfg_hdiv(((((K(C_P_NaK) * K(C_K_o)) / (K(C_K_o) + K(C_K_mk))) * y_Na_i) / (y_Na_i + K(C_K_mNa))), H(20));
     R a_E_Na = (((K(C_R) * K(C_T)) / K(C_F)) * cfg_log((K(C_Na_o) / y_Na_i)));
     R a_i_Na = ((((K(C_g_Na) * cfg_ipow<3>(y_m)) * y_h) * y_j) * (y_V - a_E_Na));
     R a_i_b_Na = (K(C_g_bNa) * (y_V - a_E_Na));
-    R a_i_NaCa = ((K(C_K_NaCa) * (((H(21) * cfg_ipow<3>(y_Na_i)) * K(C_Ca_o)) - ((H(22) * y_Ca_i) * K(C_alpha_NCX)))) / H(23));
+    R a_i_NaCa = cfg_hdiv((K(C_K_NaCa) * (((H(22) * cfg_ipow<3>(y_Na_i)) * K(C_Ca_o)) - ((H(23) * y_Ca_i) * K(C_alpha_NCX)))), H(21));
     dydt[S_Na_i] = (((-(((a_i_Na + a_i_b_Na) + (R(3.00000) * a_i_NaK)) + (R(3.00000) * a_i_NaCa))) * K(C_Cm)) / (K(C_V_c) * K(C_F)));
     R a_E_K = (((K(C_R) * K(C_T)) / K(C_F)) * cfg_log((K(C_K_o) / y_K_i)));
     R a_alpha_K1 = (R(0.100000) / (R(1.00000) + cfg_exp((R(0.0600000) * ((y_V - a_E_K) - R(200.000))))));
@@ -538,10 +538,10 @@ __device__ __forceinline__ R rhs_tissue(double t, const YS& Y, const KS& K, cons
     R a_i_Kr = (((H(25) * y_Xr1) * y_Xr2) * (y_V - a_E_K));
     R a_E_Ks = (((K(C_R) * K(C_T)) / K(C_F)) * cfg_log(((K(C_K_o) + (K(C_P_kna) * K(C_Na_o))) / (y_K_i + (K(C_P_kna) * y_Na_i)))));
     R a_i_Ks = ((K(C_g_Ks) * cfg_ipow<2>(y_Xs)) * (y_V - a_E_Ks));
-    R a_i_CaL = (((((((((K(C_g_CaL) * y_d) * y_f) * y_fCa) * R(4.00000)) * y_V) * cfg_ipow<2>(K(C_F))) / (K(C_R) * K(C_T))) * ((y_Ca_i * H(26)) - (R(0.341000) * K(C_Ca_o)))) / H(27));
+    R a_i_CaL = cfg_hdiv(((((((((K(C_g_CaL) * y_d) * y_f) * y_fCa) * R(4.00000)) * y_V) * cfg_ipow<2>(K(C_F))) / (K(C_R) * K(C_T))) * ((y_Ca_i * H(27)) - (R(0.341000) * K(C_Ca_o)))), H(26));
     R a_E_Ca = ((((R(0.500000) * K(C_R)) * K(C_T)) / K(C_F)) * cfg_log((K(C_Ca_o) / y_Ca_i)));
     R a_i_b_Ca = (K(C_g_bCa) * (y_V - a_E_Ca));
-    R a_i_p_K = ((K(C_g_pK) * (y_V - a_E_K)) / H(28));
+    R a_i_p_K = cfg_hdiv((K(C_g_pK) * (y_V - a_E_K)), H(28));
     R a_i_p_Ca = ((K(C_g_pCa) * y_Ca_i) / (y_Ca_i + K(C_K_pCa)));
     R a_Iion_cm = (((((((((((a_i_K1 + a_i_to) + a_i_Kr) + a_i_Ks) + a_i_CaL) + a_i_NaK) + a_i_Na) + a_i_b_Na) + a_i_NaCa) + a_i_b_Ca) + a_i_p_K) + a_i_p_Ca);
     R a_Istim = (SOLVE_VM ? R(cfg_stimulus_current<double>(t, stim)) : R(0));
