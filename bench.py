@@ -843,6 +843,16 @@ def full_run_arm(args):
         "activation_error_ms_p99": float(np.percentile(np.abs(a64[both] - amx[both]), 99) * 1e3),
         "latest_activation_ms": float(np.max(a64) * 1e3),
         "vm_linf_error_V": float(np.max(np.abs(v64 - vmx)))}
+    err = np.where(both, np.abs(a64 - amx), 0.0)
+    worst = int(np.argmax(err))
+    out["accuracy"].update({
+        "cells_over_0.01_ms": int((err > 1e-5).sum()), "cells_over_0.05_ms": int((err > 5e-5).sum()),
+        "worst_cell": {"centre_mm": [float(x) * 1e3 for x in c[worst]],
+                       "activation_fp64_ms": float(a64[worst] * 1e3),
+                       "activation_mixed_ms": float(amx[worst] * 1e3)}})
+    if args.full_run_save:
+        np.savez_compressed(args.full_run_save, activation_fp64=a64, activation_mixed=amx,
+                            vm_fp64=v64, vm_mixed=vmx, centres=c)
     out["speedup_mixed_vs_fp64"] = out["fp64"]["seconds"] / out["mixed"]["seconds"]
     return out
 
@@ -998,6 +1008,8 @@ def main():
     ap.add_argument("--full-run", action="store_true",
                     help="only the whole 100 ms run of both forms and their comparison")
     ap.add_argument("--full-run-steps", type=int, default=20000)
+    ap.add_argument("--full-run-save", default=None,
+                    help="write both forms' activation times and Vm (npz) to this path")
     ap.add_argument("--tissue-apd", action="store_true",
                     help="only the tissue APD90 comparison of both forms (reduced ORd slab)")
     ap.add_argument("--tissue-apd-steps", type=int, default=80000)

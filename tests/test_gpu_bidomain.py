@@ -153,6 +153,30 @@ def test_tetrahedral_lv_matches_oracle(gpu_lib, oracle, arithmetic):
         api.Bidomain(box_mesh(4, 4, 4, 1e-3, 1e-3, 1e-3), "TNNP", "epicardialCells")
 
 
+ELECTRO_PROPERTIES = """
+myocardiumSolver  bidomainSolver;
+bidomainSolverCoeffs
+{
+    conductivityIntracellular [-1 -3 3 0 0 2 0] (0.17 0 0 0.019 0 0.019);
+    conductivityExtracellular [-1 -3 3 0 0 2 0] (0.62 0 0 0.24 0 0.24);
+    chi  [0 -1 0 0 0 0 0] 140000;
+    cm   [-1 -4 4 0 0 2 0] 0.01;
+    ionicModel TNNP;
+    tissue epicardialCells;
+    solutionAlgorithm implicit;
+    maxSteps 1000000;
+    phiERefPoint (0 0 0);
+    externalStimulus
+    {
+        stimulusLocationMin (0 0 0);
+        stimulusLocationMax (1e-3 4e-3 5e-4);
+        stimulusDuration [0 0 1 0 0 0 0] 1e-3;
+        stimulusIntensity [0 -3 0 0 0 1 0] 1e5;
+    }
+}
+"""
+
+
 @pytest.mark.gpu
 def test_from_dict_equals_the_description(gpu_lib):
     """cfg_bidomain_create_from_dict builds the same context as the
