@@ -455,8 +455,7 @@ __global__ void __launch_bounds__(kCoopBlock, 1) k_implicit_pair(DiffusionArgs a
         if (a.nc_gw) {
             for (unsigned c = first; c < n; c += stride) {
                 CR g[3];
-                nc_gradient<CR, W>(a, c, [&xq](long long q) { return fp::join(xq(unsigned(q))); },
-                                   g);
+                nc_gradient<CR, W>(a, c, [&xq](long long q) { return xq(unsigned(q)); }, g);
                 __stcg(&grad[c], g[0]);
                 __stcg(&grad[size_t(n) + c], g[1]);
                 __stcg(&grad[2 * size_t(n) + c], g[2]);

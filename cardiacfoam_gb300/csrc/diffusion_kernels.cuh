@@ -232,18 +232,29 @@ __device__ __forceinline__ T ld_stream(const T* p)
 // W > 0: every row is visited over W slots (the ELL width); padded slots
 // hold zero weights and coefficients, so they add exact zeros, and the
 // fixed trip count lets all of a row's loads be issued together.
+// x_nb - x_c in the gradient's type: from FP64 values, or from float pairs
+// (the float-pair solve's iterate) without the FP64 pipe
+template <class R>
+__device__ __forceinline__ R value_diff(double u, double v) { return R(u - v); }
+template <class R>
+__device__ __forceinline__ R value_diff(fp::P u, fp::P v)
+{
+    const fp::P d = fp::sub(u, v);
+    return R(d.x) + R(d.y);
+}
+
 template <class R, int W = 0, class F>
 __device__ __forceinline__ void nc_gradient(const DiffusionArgs& a, long long c, F x, R (&g)[3])
 {
     const R* gw = static_cast<const R*>(a.nc_gw);
     const long long n = a.n, wn = (long long)a.width * n;
-    const double xc = x(c);
+    const auto xc = x(c);
     g[0] = g[1] = g[2] = R(0);
     const int cnt = W > 0 ? W : a.ell_cnt[c];
 #pragma unroll
     for (int e = 0; e < (W > 0 ? W : cnt); ++e) {
         const long long i = (long long)e * n + c;
-        const R dv = R(x(ld_stream(&a.ell_col[i])) - xc);
+        const R dv = value_diff<R>(x(ld_stream(&a.ell_col[i])), xc);
         g[0] += ld_stream(&gw[i]) * dv;
         g[1] += ld_stream(&gw[wn + i]) * dv;
         g[2] += ld_stream(&gw[2 * wn + i]) * dv;

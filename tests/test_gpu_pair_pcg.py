@@ -68,7 +68,7 @@ def test_float_pairs_against_fp64_pcg_on_a_propagating_slab(gpu_lib):
     assert np.max(np.abs(va - vb)) <= 1e-9 * np.max(np.abs(va))
     aa, ab = a.activation(), b.activation()
     assert np.array_equal(aa > 0, ab > 0)
-    assert (aa > 0).sum() > 200
+    assert (aa > 0).sum() > 60            # the stimulus box holds 27 cells
     assert np.max(np.abs(aa - ab)) <= 1e-8
     assert abs(ia - ib) <= max(2, ia // 100)
     # back to FP64 and to pairs again: the context keeps stepping
