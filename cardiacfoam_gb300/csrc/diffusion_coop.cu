@@ -466,7 +466,7 @@ __global__ void __launch_bounds__(kCoopBlock, 1) k_implicit_pair(DiffusionArgs a
         P s1[2] = {fp::make(0.0f), fp::make(0.0f)};
         const bool fresh = corr == 1 || v != bsrc_variant;
         bsrc_variant = v;
-        for (unsigned c = first; c < n; c += stride) {
+        const auto row_rhs = [&](unsigned c) {
             double rhs;
             if (fresh) {
                 const double V = a.vol[c];
@@ -487,14 +487,25 @@ __global__ void __launch_bounds__(kCoopBlock, 1) k_implicit_pair(DiffusionArgs a
                 rhs = rhs + nc_correction<CR, W>(a, c, [grad, n](long long q, int k) {
                           return __ldcg(&grad[size_t(k) * n + size_t(q)]);
                       });
-            const P bc = fp::split(rhs, sh);
+            return fp::split(rhs, sh);
+        };
+        const auto row_res = [&](unsigned c, P bc, P axc) {
             const P xc = xq(c);
-            const P axc = amul_pair<W>(a, ca, c, diag[c], xq);
             const P rc = fp::sub(bc, axc);
             b[c] = bc; ax[c] = axc; r[c] = rc;
             if (from_vm) __stcg(&px[c], xc);
             s1[0] = fp::add(s1[0], xc);
             s1[1] = fp::add(s1[1], fp::abs(rc));
+        };
+        for (unsigned c = first; c < n; c += 2 * stride) {
+            const unsigned c2 = c + stride;
+            const bool two = c2 < n;
+            const P b0 = row_rhs(c);
+            const P b1 = two ? row_rhs(c2) : fp::make(0.0f);
+            const P a0 = amul_pair<W>(a, ca, c, diag[c], xq);
+            const P a1 = two ? amul_pair<W>(a, ca, c2, diag[c2], xq) : fp::make(0.0f);
+            row_res(c, b0, a0);
+            if (two) row_res(c2, b1, a1);
         }
         gsync::block_sums_pair<kCoopBlock, 2>(partial, set, s1);
         if (!grid_barrier(st, epoch, a.spin_limit)) { abort_step = true; break; }
@@ -534,19 +545,25 @@ __global__ void __launch_bounds__(kCoopBlock, 1) k_implicit_pair(DiffusionArgs a
                 // --- halo pass: w = A.z, p = z + beta p, A.p = w + beta A.p
                 P s3[1] = {fp::make(0.0f)};
                 const bool first_it = iter == 0;
-                for (unsigned c = first; c < n; c += stride) {
-                    const P w = amul_pair<W>(a, ca, c, diag[c],
-                                             [z](unsigned q) { return __ldcg(&z[q]); });
+                const auto zq = [z](unsigned q) { return __ldcg(&z[q]); };
+                const auto dir = [&](unsigned c, P w) {
                     const P zc = __ldcg(&z[c]);
-                    P pc, qc;
-                    if (first_it) {
-                        pc = zc; qc = w;
-                    } else {
+                    P pc = zc, qc = w;
+                    if (!first_it) {
                         pc = fp::madd(beta, p[c], zc);
                         qc = fp::madd(beta, ap[c], w);
                     }
                     p[c] = pc; ap[c] = qc;
                     s3[0] = fp::madd(qc, pc, s3[0]);
+                };
+                // two rows per trip: both products' loads are in flight together
+                for (unsigned c = first; c < n; c += 2 * stride) {
+                    const unsigned c2 = c + stride;
+                    const bool two = c2 < n;
+                    const P w0 = amul_pair<W>(a, ca, c, diag[c], zq);
+                    const P w1 = two ? amul_pair<W>(a, ca, c2, diag[c2], zq) : fp::make(0.0f);
+                    dir(c, w0);
+                    if (two) dir(c2, w1);
                 }
                 gsync::block_sums_pair<kCoopBlock, 1>(partial, set, s3);
                 if (!grid_barrier(st, epoch, a.spin_limit)) { aborted = true; break; }

@@ -29,10 +29,20 @@ __device__ __forceinline__ int ld_relaxed_int(const int* p)
     return v;
 }
 
+// count += 1 with release semantics at GPU scope: the block's writes, made
+// visible to thread 0 by the block barrier before it, are visible to any
+// thread whose acquire load reads this arrival or a later one
+__device__ __forceinline__ void red_release_add(unsigned* p, unsigned v)
+{
+    asm volatile("red.release.gpu.global.add.u32 [%0], %1;" :: "l"(p), "r"(v) : "memory");
+}
+
 // Each block adds one arrival and waits until all gridDim.x arrivals of this
-// barrier are in; `epoch` counts the arrivals expected so far.  Returns false
-// when the launch was aborted (some block waited more than `spin_limit`
-// spins).
+// barrier are in; `epoch` counts the arrivals expected so far.  The arrival
+// is a release and the wait an acquire on the same counter, which orders the
+// blocks' writes before the barrier against their reads after it without a
+// full fence.  Returns false when the launch was aborted (some block waited
+// more than `spin_limit` spins).
 __device__ __forceinline__ bool grid_barrier(unsigned* count, int* abort, unsigned& epoch,
                                              long long spin_limit = kSpinLimit)
 {
@@ -40,8 +50,7 @@ __device__ __forceinline__ bool grid_barrier(unsigned* count, int* abort, unsign
     epoch += gridDim.x;
     __syncthreads();
     if (threadIdx.x == 0) {
-        __threadfence();
-        atomicAdd(count, 1u);
+        red_release_add(count, 1u);
         int good = 1;
         long long spins = 0;
         while (ld_acquire(count) < epoch) {
@@ -56,7 +65,6 @@ __device__ __forceinline__ bool grid_barrier(unsigned* count, int* abort, unsign
             if (spins > 4096) __nanosleep(64);
         }
         if (ld_relaxed_int(abort)) good = 0;
-        __threadfence();
         ok = good;
     }
     __syncthreads();
