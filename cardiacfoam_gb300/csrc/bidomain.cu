@@ -636,16 +636,25 @@ __global__ void __launch_bounds__(kCoopBlock, 1) k_pcg_coop(CoopPcgArgs ca)
 }
 
 // ---------------------------------------------------------------- float pairs
-// The same solve with the PCG in float pairs (the mixed form's default): the
-// system scaled by 2^shift (a power of two, so the solution and the residual
-// ratios are those of the unscaled system), its coefficients as (hi, lo)
-// pairs, the diagonal, source and iterate split from their FP64 values at the
-// start, every vector and sum of the iteration in pairs on the FP32 pipe.
-// The scalars are formed by every thread from the same block-order sums.
+// The mixed form's solve: the system scaled by 2^shift (a power of two, so
+// the solution and the residual ratios are those of the unscaled system),
+// its coefficients as (hi, lo) float pairs, the diagonal, source and iterate
+// split from their FP64 values at the start, every vector and sum of the
+// iteration in pairs on the FP32 pipe, and CG in its single-reduction form
+// (Chronopoulos and Gear, 1989): with u = M r and w = A u, the three sums of
+// an iteration, (u, r), (w, u) and |r|, are formed in one pass, so an
+// iteration has one grid barrier instead of two.  In exact arithmetic the
+// iterates are lduMatrix PCG's (same x, r, p and the same convergence test on
+// the L1 residual after each update); rounding differs.  A row's new u needs
+// the neighbours' new u, which each thread forms itself from the
+// neighbours' previous r, s = A p and w (double-buffered) with the same
+// operations as their owners, so no halo exchange is needed inside an
+// iteration.  The scalars are formed by every thread from the same
+// block-order sums.
 struct PairPcgArgs {
     const float2* pcoef;   // [slot][cell] scaled coefficients of the system
     int shift;
-    float2 *px, *pdiag, *prdiag;   // [cell]
+    float2 *px, *pdiag, *prdiag, *pw;   // [cell]
 };
 
 template <int W, class F>
@@ -672,12 +681,21 @@ __device__ __forceinline__ fp::P offdiag_pair(const BdOp& op, const float2* pcoe
     return acc.value();
 }
 
-__device__ __forceinline__ fp::P direction_pair(const fp::P* z, const fp::P* p_old, fp::P beta,
-                                                bool first, long long q)
-{
-    const fp::P zq = __ldcg(&z[q]);
-    return first ? zq : fp::madd(beta, __ldcg(&p_old[q]), zq);
-}
+// One row's update of an iteration, from the previous r, s, w of that row:
+// s' = w + beta s (A p'), r' = r - alpha s', u' = M r'.  Owners and
+// neighbours evaluate it the same way, so both see the same bits.
+struct PairStep {
+    fp::P alpha, nalpha, beta;
+    bool first;
+    __device__ __forceinline__ fp::P s_next(fp::P w, fp::P s_old) const
+    {
+        return first ? w : fp::madd(beta, s_old, w);
+    }
+    __device__ __forceinline__ fp::P r_next(fp::P r, fp::P s_new) const
+    {
+        return fp::madd(nalpha, s_new, r);
+    }
+};
 
 template <int W>
 __global__ void __launch_bounds__(kCoopBlock, 1) k_pcg_pair(CoopPcgArgs ca, PairPcgArgs q)
@@ -695,10 +713,16 @@ __global__ void __launch_bounds__(kCoopBlock, 1) k_pcg_pair(CoopPcgArgs ca, Pair
     const int max_iter = st->max_iter;
     const int sh = q.shift;
     const P small = fp::split(1e-20, sh), count = fp::split(double(n));
+    // r, s and w double-buffered: [k] holds the previous iteration's values
+    // (read at the neighbours), [k ^ 1] receives this iteration's
+    P* r_cur = reinterpret_cast<P*>(a.r);
+    P* r_new = reinterpret_cast<P*>(a.ax);
+    P* s_cur = reinterpret_cast<P*>(a.ap);
+    P* s_new = reinterpret_cast<P*>(ca.p_alt);
+    P* w_cur = reinterpret_cast<P*>(a.z);
+    P* w_new = q.pw;
+    P* p = reinterpret_cast<P*>(a.p);
     P* ax = reinterpret_cast<P*>(a.ax);
-    P* r = reinterpret_cast<P*>(a.r);
-    P* z = reinterpret_cast<P*>(a.z);
-    P* ap = reinterpret_cast<P*>(a.ap);
     float2* partial = reinterpret_cast<float2*>(ca.partial);
     unsigned epoch = 0;
     int set = 0;
@@ -722,18 +746,18 @@ __global__ void __launch_bounds__(kCoopBlock, 1) k_pcg_pair(CoopPcgArgs ca, Pair
             }, acc);
             const P rc = fp::sub(fp::split(a.b[c], sh), axc);
             ax[c] = axc;
-            r[c] = rc;
+            r_cur[c] = rc;
             s1[0] = fp::add(s1[0], xc);
             s1[1] = fp::add(s1[1], fp::abs(rc));
         }
         started = true;
-        block_sums_pair<kCoopBlock, 2>(partial, set, s1);
+        block_sums_pair<kCoopBlock, 2, 3>(partial, set, s1);
         if (!grid_barrier(ca.bar_count, ca.bar_abort, epoch, ca.spin_limit)) { aborted = true; break; }
         P g1[2];
-        grid_sums_pair<2>(partial, set, g1);
+        grid_sums_pair<2, 3>(partial, set, g1);
         set ^= 1;
         const P avg = fp::div(g1[0], count);
-        // --- normFactor; z = D^-1 r (published), z.r
+        // --- normFactor; u = M r (published in w[1] until w = A u is formed)
         P s2[2] = {fp::make(0.0f), fp::make(0.0f)};
         for (long long c = first; c < n; c += stride) {
             fp::Acc rs;
@@ -743,15 +767,15 @@ __global__ void __launch_bounds__(kCoopBlock, 1) k_pcg_pair(CoopPcgArgs ca, Pair
             }, rs), avg);
             const P bc = fp::split(a.b[c], sh);
             s2[0] = fp::add(s2[0], fp::add(fp::abs(fp::sub(ax[c], pa)), fp::abs(fp::sub(bc, pa))));
-            const P rc = r[c];
-            const P zc = fp::mul(q.prdiag[c], rc);
-            __stcg(&z[c], zc);
-            s2[1] = fp::madd(zc, rc, s2[1]);
+            const P rc = r_cur[c];
+            const P uc = fp::mul(q.prdiag[c], rc);
+            __stcg(&w_new[c], uc);
+            s2[1] = fp::madd(uc, rc, s2[1]);
         }
-        block_sums_pair<kCoopBlock, 2>(partial, set, s2);
+        block_sums_pair<kCoopBlock, 2, 3>(partial, set, s2);
         if (!grid_barrier(ca.bar_count, ca.bar_abort, epoch, ca.spin_limit)) { aborted = true; break; }
         P g2[2];
-        grid_sums_pair<2>(partial, set, g2);
+        grid_sums_pair<2, 3>(partial, set, g2);
         set ^= 1;
         const P normf = fp::add(g2[0], small);
         init_res = fp::div(g1[1], normf);
@@ -760,61 +784,86 @@ __global__ void __launch_bounds__(kCoopBlock, 1) k_pcg_pair(CoopPcgArgs ca, Pair
             return fp::less(rr, tol) || (use_rel && fp::less(rr, rel_init));
         };
         res = init_res;
-        P wArA = g2[1], beta = fp::make(0.0f);
-        P* p_old = reinterpret_cast<P*>(a.p);
-        P* p_new = reinterpret_cast<P*>(ca.p_alt);
-        while (!conv(res)) {
-            // --- direction pass: p = z + beta p_old, A p, sum p.A p
-            const bool first_it = iter == 0;
-            P s3[1] = {fp::make(0.0f)};
+        if (conv(res)) break;
+        // --- w = A u; (w, u)
+        P s3[1] = {fp::make(0.0f)};
+        for (long long c = first; c < n; c += stride) {
+            const P* u0 = w_new;
+            fp::Acc acc;
+            acc.add_prod(q.pdiag[c], __ldcg(&u0[c]));
+            const P wc = offdiag_pair<W>(op, q.pcoef, c, [u0](long long k) {
+                return __ldcg(&u0[k]);
+            }, acc);
+            w_cur[c] = wc;
+            s3[0] = fp::madd(wc, __ldcg(&u0[c]), s3[0]);
+        }
+        block_sums_pair<kCoopBlock, 1, 3>(partial, set, s3);
+        if (!grid_barrier(ca.bar_count, ca.bar_abort, epoch, ca.spin_limit)) { aborted = true; break; }
+        P g3[1];
+        grid_sums_pair<1, 3>(partial, set, g3);
+        set ^= 1;
+        P gamma = g2[1], delta = g3[0], gamma_old = fp::make(0.0f), alpha_old = fp::make(1.0f);
+        for (;;) {
+            // the scalars of this iteration; (p, A p) = delta - beta gamma / alpha_old
+            PairStep ps;
+            ps.first = iter == 0;
+            ps.beta = ps.first ? fp::make(0.0f) : fp::div(gamma, gamma_old);
+            const P pap = ps.first ? delta
+                                   : fp::sub(delta, fp::div(fp::mul(ps.beta, gamma), alpha_old));
+            if (pap.x == 0.0f) break;   // checkSingularity
+            ps.alpha = fp::div(gamma, pap);
+            ps.nalpha = fp::neg(ps.alpha);
+            const P* r0 = r_cur;
+            const P* s0 = s_cur;
+            const P* w0 = w_cur;
+            P* r1 = r_new;
+            P* s1n = s_new;
+            P* w1 = w_new;
+            // u' of row j from its previous r, s, w
+            const auto u_next = [&](long long j) {
+                const P sj = ps.s_next(__ldcg(&w0[j]), __ldcg(&s0[j]));
+                return fp::mul(__ldcg(&q.prdiag[j]), ps.r_next(__ldcg(&r0[j]), sj));
+            };
+            P s4[3] = {fp::make(0.0f), fp::make(0.0f), fp::make(0.0f)};
             for (long long c = first; c < n; c += stride) {
-                const P pc = direction_pair(z, p_old, beta, first_it, c);
-                const P* zz = z;
-                const P* po = p_old;
+                const P rc = __ldcg(&r0[c]);
+                const P sc = ps.s_next(__ldcg(&w0[c]), __ldcg(&s0[c]));
+                const P uc_old = fp::mul(q.prdiag[c], rc);
+                const P pc = ps.first ? uc_old : fp::madd(ps.beta, p[c], uc_old);
+                p[c] = pc;
+                q.px[c] = fp::madd(ps.alpha, pc, q.px[c]);
+                const P rn = ps.r_next(rc, sc);
+                const P un = fp::mul(q.prdiag[c], rn);
                 fp::Acc acc;
-                acc.add_prod(q.pdiag[c], pc);
-                const P apc = offdiag_pair<W>(op, q.pcoef, c, [zz, po, beta, first_it](long long k) {
-                    return direction_pair(zz, po, beta, first_it, k);
-                }, acc);
-                __stcg(&p_new[c], pc);
-                ap[c] = apc;
-                s3[0] = fp::madd(apc, pc, s3[0]);
+                acc.add_prod(q.pdiag[c], un);
+                const P wn = offdiag_pair<W>(op, q.pcoef, c, u_next, acc);
+                __stcg(&r1[c], rn);
+                __stcg(&s1n[c], sc);
+                __stcg(&w1[c], wn);
+                s4[0] = fp::madd(un, rn, s4[0]);
+                s4[1] = fp::madd(wn, un, s4[1]);
+                s4[2] = fp::add(s4[2], fp::abs(rn));
             }
-            block_sums_pair<kCoopBlock, 1>(partial, set, s3);
+            // the three sums in one set of three slots; sets alternate, so a
+            // set is written again only after every block has read it
+            block_sums_pair<kCoopBlock, 3, 3>(partial, set, s4);
             if (!grid_barrier(ca.bar_count, ca.bar_abort, epoch, ca.spin_limit)) { aborted = true; break; }
-            P g3[1];
-            grid_sums_pair<1>(partial, set, g3);
+            P g4[3];
+            grid_sums_pair<3, 3>(partial, set, g4);
             set ^= 1;
-            if (g3[0].x == 0.0f) break;   // checkSingularity
-            const P alpha = fp::div(wArA, g3[0]);
-            const P nalpha = fp::neg(alpha);
-            // --- update pass: x, r, z; |r| and z.r
-            P s4[2] = {fp::make(0.0f), fp::make(0.0f)};
-            for (long long c = first; c < n; c += stride) {
-                q.px[c] = fp::madd(alpha, __ldcg(&p_new[c]), q.px[c]);
-                const P rc = fp::madd(nalpha, ap[c], r[c]);
-                r[c] = rc;
-                const P zc = fp::mul(q.prdiag[c], rc);
-                __stcg(&z[c], zc);
-                s4[0] = fp::add(s4[0], fp::abs(rc));
-                s4[1] = fp::madd(zc, rc, s4[1]);
-            }
-            block_sums_pair<kCoopBlock, 2>(partial, set, s4);
-            if (!grid_barrier(ca.bar_count, ca.bar_abort, epoch, ca.spin_limit)) { aborted = true; break; }
-            P g4[2];
-            grid_sums_pair<2>(partial, set, g4);
-            set ^= 1;
-            res = fp::div(g4[0], normf);
+            res = fp::div(g4[2], normf);
             ++iter;
+            P* t = r_cur; r_cur = r_new; r_new = t;
+            t = s_cur; s_cur = s_new; s_new = t;
+            t = w_cur; w_cur = w_new; w_new = t;
             if (conv(res) || iter >= max_iter) {
                 if (!conv(res)) status = 1;
                 break;
             }
-            beta = fp::div(g4[1], wArA);
-            wArA = g4[1];
-            P* t = p_old;
-            p_old = p_new;
-            p_new = t;
+            gamma_old = gamma;
+            alpha_old = ps.alpha;
+            gamma = g4[0];
+            delta = g4[1];
         }
     } while (false);
     // the iterate back into the FP64 field (own rows)
@@ -896,7 +945,7 @@ struct cfg_bidomain {
     float2* d_pcoef[2] = {nullptr, nullptr};
     int pcoef_shift[2] = {0, 0};
     bool pcoef_ready[2] = {false, false};
-    float2 *d_px = nullptr, *d_pdiag = nullptr, *d_prdiag = nullptr;
+    float2 *d_px = nullptr, *d_pdiag = nullptr, *d_prdiag = nullptr, *d_pw = nullptr;
     double max_vol = 0.0, max_row_i = 0.0, max_row_e = 0.0;
     double step_dt = 0.0;
     unsigned* d_bar = nullptr;
@@ -933,6 +982,7 @@ cudaError_t alloc_pairs(cfg_bidomain* bd)
     if (!e) e = dmalloc(&bd->d_px, n);
     if (!e) e = dmalloc(&bd->d_pdiag, n);
     if (!e) e = dmalloc(&bd->d_prdiag, n);
+    if (!e) e = dmalloc(&bd->d_pw, n);
     return e;
 }
 
@@ -992,7 +1042,8 @@ int pcg_solve(cfg_bidomain* bd, int kind, double tol, double rel, int max_iter,
                 bd->pcoef_shift[kind] = shift;
                 bd->pcoef_ready[kind] = true;
             }
-            PairPcgArgs pa{bd->d_pcoef[kind], shift, bd->d_px, bd->d_pdiag, bd->d_prdiag};
+            PairPcgArgs pa{bd->d_pcoef[kind], shift, bd->d_px, bd->d_pdiag, bd->d_prdiag,
+                           bd->d_pw};
             void* params[] = {&ca, &pa};
             const void* fn = bd->op.width == 6 ? (const void*)k_pcg_pair<6>
                            : bd->op.width == 4 ? (const void*)k_pcg_pair<4>
@@ -1104,6 +1155,7 @@ extern "C" int cfg_bidomain_destroy(cfg_bidomain* bd)
     dfree(bd->d_px);
     dfree(bd->d_pdiag);
     dfree(bd->d_prdiag);
+    dfree(bd->d_pw);
     dfree(bd->d_col);
     dfree(bd->d_cnt);
     dfree(bd->d_own);
@@ -1343,7 +1395,8 @@ extern "C" int cfg_bidomain_create(const cfg_bidomain_desc* d, const cfg_mesh_de
     if (!e && bd->coop_blocks > 0) {
         e = dmalloc(&bd->d_p_alt, size_t(n));
         if (!e) e = cudaMemset(bd->d_p_alt, 0, size_t(n) * sizeof(double));
-        if (!e) e = dmalloc(&bd->d_coop_partial, 4 * size_t(bd->coop_blocks));
+        // two sets of up to three sums per block
+        if (!e) e = dmalloc(&bd->d_coop_partial, 6 * size_t(bd->coop_blocks));
         if (!e) e = dmalloc(&bd->d_bar, 1);
         if (!e) e = dmalloc(&bd->d_abort, 1);
     }

@@ -133,14 +133,16 @@ __device__ __forceinline__ void block_scalars(double (&out)[K], F f)
 }
 
 // Float-pair forms of block_sums / grid_sums (partial slots of 8 bytes hold
-// one pair).  Warp k adds the block's warp sums of value k in a fixed tree;
-// every block then adds the block sums in the same fixed order, so all
-// blocks hold bitwise the same totals.
-template <int kBlock, int K>
+// one pair; a set has S slots of gridDim.x, so a kernel whose reductions
+// alternate between two sets needs 2 S gridDim.x pairs).  Warp k adds the
+// block's warp sums of value k in a fixed tree; every block then adds the
+// block sums in the same fixed order, so all blocks hold bitwise the same
+// totals.
+template <int kBlock, int K, int S = 2>
 __device__ __forceinline__ void block_sums_pair(float2* partial, int set, fp::P (&v)[K])
 {
     constexpr int kWarps = kBlock / 32;
-    static_assert(kWarps <= 32 && K <= kWarps, "one warp per value");
+    static_assert(kWarps <= 32 && K <= kWarps && K <= S, "one warp per value");
     __shared__ float2 sh[K][kWarps];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
@@ -152,17 +154,17 @@ __device__ __forceinline__ void block_sums_pair(float2* partial, int set, fp::P 
     if (w < K) {
         fp::P s = lane < kWarps ? sh[w][lane] : fp::make(0.0f);
         s = fp::warp_sum(s);
-        if (lane == 0) __stcg(&partial[(size_t(set) * 2 + w) * gridDim.x + blockIdx.x], s);
+        if (lane == 0) __stcg(&partial[(size_t(set) * S + w) * gridDim.x + blockIdx.x], s);
     }
 }
 
-template <int K>
+template <int K, int S = 2>
 __device__ __forceinline__ void grid_sums_pair(const float2* partial, int set, fp::P (&out)[K])
 {
     __shared__ float2 sh[K];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     if (w < K) {
-        const float2* src = partial + (size_t(set) * 2 + w) * gridDim.x;
+        const float2* src = partial + (size_t(set) * S + w) * gridDim.x;
         fp::P s = fp::make(0.0f);
         for (unsigned i = lane; i < gridDim.x; i += 32) s = fp::add(s, __ldcg(&src[i]));
         s = fp::warp_sum(s);
