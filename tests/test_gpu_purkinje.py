@@ -92,3 +92,50 @@ def test_network_argument_checks(gpu_lib):
     assert "pvjRadius" in str(err.value)
     pk.close()
     md.close()
+
+
+@pytest.mark.gpu
+def test_niederer_purkinje_tutorial_matches_oracle(gpu_lib, oracle):
+    """The reference's Purkinje tutorial (tutorials/Niederer/
+    NiedererEtAl2011MonodomainPurkinje): its 193-node graph (fixture from
+    its purkinjeGraph), BuenoOrovio epicardial nodes, root stimulus 5e5 at
+    10-12 ms, unidirectional reactionDiffusionPvjCoupler (rPvj 1e4,
+    pvjRadius 0.3 mm) into the Niederer slab (100 x 15 x 35 cells of 0.2 mm,
+    explicit algorithm at the maxCo 0.1 time step, no box stimulus).  Over
+    24 ms the network fires, its eight terminals excite the tissue, and the
+    tissue's Vm and activation times, the network's Vm and the terminal
+    currents equal the oracle's coupled step."""
+    import os
+    from pathlib import Path
+    g = np.load(Path(__file__).parent / "golden" / "niederer_purkinje_graph.npz")
+    nx, ny, nz, lx, ly, lz = 100, 15, 35, 0.02, 0.003, 0.007
+    chicm = 140000 * 0.01
+    dt = 0.1 * (lx / nx) ** 2 / (SIGMA[0] / chicm)
+    mesh = box_mesh(nx, ny, nz, lx, ly, lz)
+    md = api.Monodomain(mesh, "BuenoOrovio", "epicardialCells", SIGMA, dt=dt, implicit=False)
+    root = (int(g["root"]), 0.01, 2e-3, 5e5)
+    pk = api.Purkinje(g["edges"], "BuenoOrovio", "epicardialCells", dt=dt, chi=140000.0,
+                      cm=0.01, root_stimulus=root, pvj_nodes=g["pvj_nodes"],
+                      pvj_locations=g["pvj_locations"])
+    pk.couple(md, 1e4, 3e-4)
+    om = oracle.Mesh(nx, ny, nz, lx, ly, lz)
+    T = oracle.Tissue(oracle.tissue_desc("BuenoOrovio", 1, SIGMA, implicit=False), om)
+    P = oracle.Purkinje(g["edges"], "BuenoOrovio", 1, dt, root_stimulus=root[1:],
+                        pvj_nodes=g["pvj_nodes"], pvj_locations=g["pvj_locations"])
+    P.couple(om, 1e4, 3e-4)
+    threads = os.cpu_count() or 1
+    for _ in range(int(0.024 / dt)):
+        md.step(dt)
+        P.coupled_step(T, dt, threads)
+    assert np.all(P.vm()[g["pvj_nodes"]] > -0.084)       # the terminals fired
+    vg, vo = md.vm(), T.vm()
+    assert np.max(np.abs(vg - vo)) <= 1e-9 * np.max(np.abs(vo))
+    ag, ao = md.activation(), T.activation()
+    assert np.array_equal(ag > 0, ao > 0) and np.sum(ao > 0) > 50
+    assert np.max(np.abs(ag - ao)) < 1e-9
+    pv, po = pk.vm(), P.vm()
+    assert np.max(np.abs(pv - po)) <= 1e-9 * np.max(np.abs(po))
+    ig, io_ = pk.terminal_current(), P.terminal_current()
+    assert np.max(np.abs(ig - io_)) <= 1e-9 * max(np.max(np.abs(io_)), 1e-300)
+    pk.close()
+    md.close()

@@ -37,6 +37,29 @@ def test_graph_reader():
         io.read_purkinje_graph(GRAPH.replace("4(0 1 0.001 1)", "3(0 1 0.001)"))
 
 
+def test_tutorial_graph_fixture():
+    """The reference Purkinje tutorial's graph (fixture made from its
+    purkinjeGraph by tests/golden/make_purkinje_fixture.py): 192 edges of a
+    193-node tree rooted at node 0, eight PVJs inside the Niederer slab; the
+    reader gives the same arrays from the file itself where the reference
+    is at hand."""
+    from pathlib import Path
+    from oracle.build import reference_dir
+    g = np.load(Path(__file__).parent / "golden" / "niederer_purkinje_graph.npz")
+    e = g["edges"]
+    assert e.shape == (192, 4) and int(g["root"]) == 0
+    nodes = np.unique(e[:, :2].astype(int))
+    assert nodes.size == 193 and nodes[0] == 0 and nodes[-1] == 192
+    assert list(g["pvj_nodes"]) == list(range(8, 16))
+    assert np.all((g["pvj_locations"] > 0) & (g["pvj_locations"] < [0.02, 0.003, 0.007]))
+    ref = reference_dir()
+    if ref is not None:
+        f = Path(ref) / "tutorials/Niederer/NiedererEtAl2011MonodomainPurkinje/constant/purkinjeGraph"
+        r = io.read_purkinje_graph(f.read_text())
+        assert np.array_equal(r["edges"], e)
+        assert np.array_equal(r["pvj_locations"], g["pvj_locations"])
+
+
 def test_synthetic_tree_is_a_tree():
     e, pos, leaves = io.synthetic_purkinje_tree(3, 4, 2.5e-4)
     n = len(pos)
