@@ -517,13 +517,21 @@ __global__ void __launch_bounds__(kCoopBlock, 1) k_implicit_pair(DiffusionArgs a
         if (a.ddt_backward && n_old < 2) n_old = 2;
         // --- normFactor, z = D^-1 r (published), z.r
         P s2[2] = {fp::make(0.0f), fp::make(0.0f)};
-        for (unsigned c = first; c < n; c += stride) {
-            const P pa = fp::mul(sumA[c], avg);
-            s2[0] = fp::add(s2[0], fp::add(fp::abs(fp::sub(ax[c], pa)), fp::abs(fp::sub(b[c], pa))));
-            const P rc = r[c];
-            const P zc = fp::mul(rdiag[c], rc);
+        const auto norm_row = [&](unsigned c, P sa, P axc, P bc, P rc, P m) {
+            const P pa = fp::mul(sa, avg);
+            s2[0] = fp::add(s2[0], fp::add(fp::abs(fp::sub(axc, pa)), fp::abs(fp::sub(bc, pa))));
+            const P zc = fp::mul(m, rc);
             __stcg(&z[c], zc);
             s2[1] = fp::madd(zc, rc, s2[1]);
+        };
+        for (unsigned c = first; c < n; c += 2 * stride) {
+            const unsigned c2 = c + stride;
+            const bool two = c2 < n;
+            const unsigned d = two ? c2 : c;
+            const P sa0 = sumA[c], sa1 = sumA[d], a0 = ax[c], a1 = ax[d], b0 = b[c], b1 = b[d];
+            const P r0 = r[c], r1 = r[d], m0 = rdiag[c], m1 = rdiag[d];
+            norm_row(c, sa0, a0, b0, r0, m0);
+            if (two) norm_row(c2, sa1, a1, b1, r1, m1);
         }
         gsync::block_sums_pair<kCoopBlock, 2>(partial, set, s2);
         if (!grid_barrier(st, epoch, a.spin_limit)) { abort_step = true; break; }
@@ -575,14 +583,31 @@ __global__ void __launch_bounds__(kCoopBlock, 1) k_implicit_pair(DiffusionArgs a
                 const P nalpha = fp::neg(alpha);
                 // --- update pass: x, r, z; |r| and z.r
                 P s4[2] = {fp::make(0.0f), fp::make(0.0f)};
-                for (unsigned c = first; c < n; c += stride) {
-                    __stcg(&px[c], fp::madd(alpha, p[c], __ldcg(&px[c])));
-                    const P rc = fp::madd(nalpha, ap[c], r[c]);
+                // two rows per trip, all of their loads issued first (the
+                // pass streams from HBM when the vectors exceed L2)
+                for (unsigned c = first; c < n; c += 2 * stride) {
+                    const unsigned c2 = c + stride;
+                    const bool two = c2 < n;
+                    const unsigned d = two ? c2 : c;
+                    const P p0 = p[c], p1 = p[d], q0 = ap[c], q1 = ap[d];
+                    const P r0 = r[c], r1 = r[d], x0 = __ldcg(&px[c]), x1 = __ldcg(&px[d]);
+                    const P m0 = rdiag[c], m1 = rdiag[d];
+                    __stcg(&px[c], fp::madd(alpha, p0, x0));
+                    const P rc = fp::madd(nalpha, q0, r0);
                     r[c] = rc;
-                    const P zc = fp::mul(rdiag[c], rc);
+                    const P zc = fp::mul(m0, rc);
                     __stcg(&z[c], zc);
                     s4[0] = fp::add(s4[0], fp::abs(rc));
                     s4[1] = fp::madd(zc, rc, s4[1]);
+                    if (two) {
+                        __stcg(&px[c2], fp::madd(alpha, p1, x1));
+                        const P rd = fp::madd(nalpha, q1, r1);
+                        r[c2] = rd;
+                        const P zd = fp::mul(m1, rd);
+                        __stcg(&z[c2], zd);
+                        s4[0] = fp::add(s4[0], fp::abs(rd));
+                        s4[1] = fp::madd(zd, rd, s4[1]);
+                    }
                 }
                 gsync::block_sums_pair<kCoopBlock, 2>(partial, set, s4);
                 if (!grid_barrier(st, epoch, a.spin_limit)) { aborted = true; break; }
@@ -606,7 +631,15 @@ __global__ void __launch_bounds__(kCoopBlock, 1) k_implicit_pair(DiffusionArgs a
             }
         }
         // the solve's iterate back into Vm (own rows; the neighbours read px)
-        for (unsigned c = first; c < n; c += stride) x[c] = fp::join(__ldcg(&px[c]));
+        for (unsigned c = first; c < n; c += 2 * stride) {
+            const unsigned c2 = c + stride;
+            const P x0 = __ldcg(&px[c]);
+            if (c2 < n) {
+                const P x1 = __ldcg(&px[c2]);
+                x[c2] = fp::join(x1);
+            }
+            x[c] = fp::join(x0);
+        }
         if (lead && n_solves < kMaxSolves) {
             st->iters[n_solves] = iter;
             st->init_r[n_solves] = fp::join(init_res);
