@@ -630,16 +630,6 @@ __global__ void __launch_bounds__(kCoopBlock, 1) k_implicit_pair(DiffusionArgs a
                 wArA = g4[1];
             }
         }
-        // the solve's iterate back into Vm (own rows; the neighbours read px)
-        for (unsigned c = first; c < n; c += 2 * stride) {
-            const unsigned c2 = c + stride;
-            const P x0 = __ldcg(&px[c]);
-            if (c2 < n) {
-                const P x1 = __ldcg(&px[c2]);
-                x[c2] = fp::join(x1);
-            }
-            x[c] = fp::join(x0);
-        }
         if (lead && n_solves < kMaxSolves) {
             st->iters[n_solves] = iter;
             st->init_r[n_solves] = fp::join(init_res);
@@ -653,8 +643,13 @@ __global__ void __launch_bounds__(kCoopBlock, 1) k_implicit_pair(DiffusionArgs a
     }
     if (abort_step) status |= CFG_ERR_PCG;
     else
-        for (unsigned c = first; c < n; c += stride)
-            activation(a, c, x[c], a.vm_old[c], t_step - a.dt);
+        // the step's iterate back into Vm (own rows: between correctors the
+        // neighbours read px, so Vm is written once), and the activation time
+        for (unsigned c = first; c < n; c += stride) {
+            const double xc = fp::join(__ldcg(&px[c]));
+            x[c] = xc;
+            activation(a, c, xc, a.vm_old[c], t_step - a.dt);
+        }
     if (lead) {
         st->n_old = n_old;
         st->n_solves = n_solves;
