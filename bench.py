@@ -526,7 +526,8 @@ def lv_arm(args, flush):
                      f"{n} tetrahedra; fibres +60 (endo) to -60 deg (epi), sigma_l 0.1334, "
                      f"sigma_t 0.0176 S/m per cell; apical 2 mm cube stimulus 5e4 A/m^3 x 2 ms; "
                      f"dt 1e-5 s; implicit backward ddt, Gauss linear corrected Laplacian "
-                     f"(leastSquares gradient), PIMPLE residualControl 1e-6, PCG tol 1e-8"),
+                     f"(leastSquares gradient), PIMPLE residualControl 1e-6, PCG tol 1e-8 "
+                     f"(FP64 PCG: the mixed form's default on corrected meshes)"),
         "cells": n, "faces": L.mesh.n_faces, "wall_faces": L.mesh.n_boundary_faces,
         "autotune": None if tune is None else {"block": tune[0], "cells_per_thread": tune[1],
                                                "ionic_ms": tune[2]},

@@ -415,7 +415,10 @@ int monodomain_create(const cfg_monodomain_desc* d, const cfg_mesh_desc* m, cfg_
     if (!e) e = dmalloc(&md->d_act_flag, n);
     if (!e) e = dmalloc(&md->d_st, 1);
     for (size_t c = 0; c < n; ++c) md->max_vol = std::max(md->max_vol, m->volumes[c]);
-    if (!e && d->ionic.precision == CFG_PRECISION_MIXED) {
+    // float pairs by default in the mixed form on meshes without explicit
+    // corrections; on corrected (tetrahedral) meshes the solve streams from
+    // HBM and the FP64 PCG measured faster
+    if (!e && d->ionic.precision == CFG_PRECISION_MIXED && !md->corrected) {
         e = alloc_pairs(md);
         md->pair = !e;
     }
