@@ -256,7 +256,6 @@ def gpu_arm(args, rank, world):
     for _ in range(ke2e):
         mixed.set_field(lib.FIELD_VM, vm_host)
         mixed.step(DT)
-        vm_out[:] = 0.0
         lib.check(mixed._lib.cfg_monodomain_get_field(mixed.h, lib.FIELD_VM, lib.dptr(vm_out)))
         vm_host, vm_out = vm_out, vm_host
     t_e2e = time.perf_counter() - t0
