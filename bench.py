@@ -148,20 +148,24 @@ def make_model(mesh, precision):
 
 
 def timed_steps(md, k, flush, dt=DT):
-    """Run k steps, timing each with CUDA events on the context's stream;
-    L2 is flushed (256 MB write on another stream) between steps."""
+    """Run k steps, timing each with CUDA events on the context's stream.
+    Before each step L2 is flushed (a 256 MB write) on that stream, ahead of
+    the start event: the host submits the step while the flush runs, so the
+    events bracket the step's device work and not the host's launch
+    latency (the end-to-end figure keeps that)."""
     import torch
     stream = torch.cuda.ExternalStream(md.stream())
     total = 0.0
     for _ in range(k):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            flush.zero_()
         e0.record(stream)
         md.step(dt)
         e1.record(stream)
         e1.synchronize()
         total += e0.elapsed_time(e1)
-        flush.zero_()
-        torch.cuda.synchronize()
+    torch.cuda.synchronize()
     return total / 1e3
 
 
