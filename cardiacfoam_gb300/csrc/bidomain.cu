@@ -1,5 +1,5 @@
 // Bidomain step (BidomainSolver, bidomainSolver.C:36-263, in
-// MyocardiumDomain's staggered advance) on the GPU, FP64 diffusion.
+// MyocardiumDomain's staggered advance) on the GPU.
 //
 // Per step: box stimulus, the ionic update (cfg_ionic, either form), then per
 // PIMPLE corrector
@@ -13,8 +13,10 @@
 // Gi & grad(x) is Gauss linear over the faces with gaussGrad's zeroGradient
 // wall values.  Operators are per-row ELL slots (column, the two Laplacian
 // coefficients, gradient weights, face area vector and interpolation
-// weight).  Meshes whose Laplacians need explicit non-orthogonal or
-// tangential corrections are rejected (CFG_ERR_UNSUPPORTED).
+// weight).  On meshes whose Laplacians need explicit non-orthogonal or
+// tangential corrections (tetrahedra, rotated fibres) both systems carry
+// them in their sources, evaluated from the current phiE or Vm before each
+// solve; solutionAlgorithm explicit runs solveDiffusionExplicit.
 //
 // Each PCG solve is one persistent cooperative launch (every block resident,
 // rows strided over the grid) with two grid barriers per iteration: the
@@ -27,7 +29,9 @@
 // results reproducible bit for bit.  Barrier waits are bounded (the step then
 // reports CFG_ERR_PCG).  Where cooperative launch is not available the same
 // iteration runs as a kernel sequence with its scalars on the device, two
-// launches per iteration, replayed in chunks from a CUDA graph.
+// launches per iteration, replayed in chunks from a CUDA graph.  That is the
+// FP64 solve; the mixed form's default is the float-pair, single-reduction
+// solve (k_pcg_pair, one grid barrier per iteration).
 #include <cuda_runtime.h>
 
 #include <algorithm>

@@ -22,6 +22,9 @@
 // iterate (one more barrier) for the explicit correction of the Laplacian
 // in the source.
 //
+// k_implicit_pair is the same solve with the PCG in float pairs (the mixed
+// form's default on meshes without explicit corrections).
+//
 // Grid barriers are cooperative-launch safe (all blocks co-resident) and
 // bounded: a block that waits longer than the context's spin limit (~1 s by
 // default) sets an abort flag, every block leaves at its next barrier, and
