@@ -66,35 +66,6 @@ __device__ __forceinline__ double warp_sum(double v)
     return v;
 }
 
-// v = hi + lo with |v - hi - lo| <= 2^-48 |v|: hi takes the leading 24
-// significant bits of the double (truncated), lo the remaining 29 rounded to
-// 24, both assembled from the bit pattern with integer operations (the FP64
-// pipe is not used).  |v| below 2^-126 reads as zero, beyond the float range
-// as the rounded float.
-__device__ __forceinline__ void split_fp64(double v, float& hi, float& lo)
-{
-    const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(v));
-    const unsigned hw = unsigned(b >> 32), lw = unsigned(b);
-    const unsigned sign = hw & 0x80000000u;
-    const int e = int((hw >> 20) & 0x7ffu);
-    const int ef = e - 896;                // biased float exponent of 2^(e - 1023)
-    if (ef <= 0) {
-        hi = lo = 0.0f;
-        return;
-    }
-    if (ef >= 255) {
-        hi = __double2float_rn(v);
-        lo = 0.0f;
-        return;
-    }
-    hi = __uint_as_float(sign | (unsigned(ef) << 23) | ((hw & 0xfffffu) << 3) | (lw >> 29));
-    const int es = e - 948;                // biased float exponent of 2^(e - 1075)
-    const float rem = es > 0 ? __fmul_rn(__uint2float_rn(lw & 0x1fffffffu),
-                                         __uint_as_float(unsigned(es) << 23))
-                             : 0.0f;
-    lo = __uint_as_float(__float_as_uint(rem) | sign);
-}
-
 // Accumulators: FP64 multiply-add, or a float pair (ch + cl) fed by the
 // error-free product of two float pairs (Dekker's product with fmaf for the
 // rounding error, the low-order cross terms added into it) and Knuth's
@@ -195,10 +166,10 @@ __device__ __forceinline__ void cell_terms(Acc<PAIR> (&acc)[NE], const Entry* le
     constexpr int T = tile_of(NE);
     const Entry* e = lead + (c / T) * NE * T + c % T;
     if constexpr (PAIR) {
-        float vh, vl;
-        split_fp64(v, vh, vl);
+        // Vm as a float pair from its bit pattern (no FP64 operation)
+        const float2 vp = cfg::fp::split(v);
 #pragma unroll
-        for (int j = 0; j < NE; ++j) acc[j].add(e[j * T], vh, vl);
+        for (int j = 0; j < NE; ++j) acc[j].add(e[j * T], vp.x, vp.y);
     } else {
 #pragma unroll
         for (int j = 0; j < NE; ++j) acc[j].add(e[j * T], v);
