@@ -480,10 +480,13 @@ def lv_arm(args, flush):
     boxes = [(lo, hi, 0.0, 2e-3, LV_INTENSITY)]
 
     def make(precision):
-        return api.Monodomain(L.mesh, "TNNP", "epicardialCells", dt=LV_DT, precision=precision,
-                              boxes=boxes, tissue_per_cell=L.tissue,
-                              conductivity_per_cell=L.conductivity, stencil=False,
-                              max_steps=10 ** 6)
+        m = api.Monodomain(L.mesh, "TNNP", "epicardialCells", dt=LV_DT, precision=precision,
+                           boxes=boxes, tissue_per_cell=L.tissue,
+                           conductivity_per_cell=L.conductivity, stencil=False,
+                           max_steps=10 ** 6)
+        if precision == lib.PRECISION_MIXED and args.lv_pcg != "default":
+            m.set_pcg_arithmetic(lib.PCG_FLOAT_PAIRS if args.lv_pcg == "pairs" else lib.PCG_FP64)
+        return m
 
     t0 = time.perf_counter()
     mixed = make(lib.PRECISION_MIXED)
@@ -1005,6 +1008,8 @@ def main():
     ap.add_argument("--lv-dims", default="",
                     help="nt,m,nr of the LV mesh (default: the 4.0 M-tet configuration)")
     ap.add_argument("--lv-steps", type=int, default=20)
+    ap.add_argument("--lv-pcg", default="default", choices=["default", "fp64", "pairs"],
+                    help="PCG arithmetic of the LV's mixed form (default: the library's)")
     ap.add_argument("--lv-fp64-steps", type=int, default=3)
     ap.add_argument("--lv-accuracy-steps", type=int, default=250)
     ap.add_argument("--batch-cells", type=int, default=65536)
