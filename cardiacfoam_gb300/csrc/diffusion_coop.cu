@@ -112,7 +112,8 @@ __device__ __forceinline__ double amul_cg(const DiffusionArgs& a, const CoopArgs
 //   update pass: x += alpha p, r -= alpha A.p, z = D^-1 r (published for
 //                the next halo pass), sums |r| and z.r           | barrier
 template <class CR, int W>
-__global__ void __launch_bounds__(kCoopBlock, 1) k_implicit_coop(DiffusionArgs a, CoopArgs ca)
+__global__ void __launch_bounds__(kCoopBlock, W == 4 ? 2 : 1)
+    k_implicit_coop(DiffusionArgs a, CoopArgs ca)
 {
     PcgState* st = a.st;
     const unsigned n = unsigned(a.n);
@@ -405,7 +406,7 @@ __device__ __forceinline__ fp::P amul_pair(const DiffusionArgs& a, const CoopArg
 }
 
 template <class CR, int W>
-__global__ void __launch_bounds__(kCoopBlock, 1) k_implicit_pair(DiffusionArgs a, CoopArgs ca)
+__global__ void __launch_bounds__(kCoopBlock, 2) k_implicit_pair(DiffusionArgs a, CoopArgs ca)
 {
     using fp::P;
     PcgState* st = a.st;
@@ -722,6 +723,19 @@ cudaError_t launch_implicit_coop(const DiffusionArgs& a, int blocks, cudaStream_
     else
         fn = w == 4 ? (void*)k_implicit_coop<double, 4> : w == 6 ? (void*)k_implicit_coop<double, 6>
                                                                  : (void*)k_implicit_coop<double, 0>;
+    {
+        // as many co-resident blocks as the chosen kernel fits: two per SM
+        // for the float-pair solve and for tetrahedral rows, whose kernels
+        // are built for 64 registers a thread, one for the others
+        int dev = 0, sms = 0, per = 0;
+        if (cudaGetDevice(&dev) == cudaSuccess &&
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess &&
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, kCoopBlock, 0) == cudaSuccess) {
+            const long long want = (a.n + kCoopBlock - 1) / kCoopBlock;
+            const long long cap = (long long)sms * per;
+            blocks = int(want < cap ? want : cap);
+        }
+    }
     return cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(kCoopBlock), params, 0, s);
 }
 
