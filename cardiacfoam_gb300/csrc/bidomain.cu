@@ -701,8 +701,8 @@ struct PairStep {
     }
 };
 
-template <int W>
-__global__ void __launch_bounds__(kCoopBlock, 1) k_pcg_pair(CoopPcgArgs ca, PairPcgArgs q)
+template <int W, int B = kCoopBlock>
+__global__ void __launch_bounds__(B, 1) k_pcg_pair(CoopPcgArgs ca, PairPcgArgs q)
 {
     using namespace cfg::gsync;
     using fp::P;
@@ -755,7 +755,7 @@ __global__ void __launch_bounds__(kCoopBlock, 1) k_pcg_pair(CoopPcgArgs ca, Pair
             s1[1] = fp::add(s1[1], fp::abs(rc));
         }
         started = true;
-        block_sums_pair<kCoopBlock, 2, 3>(partial, set, s1);
+        block_sums_pair<B, 2, 3>(partial, set, s1);
         if (!grid_barrier(ca.bar_count, ca.bar_abort, epoch, ca.spin_limit)) { aborted = true; break; }
         P g1[2];
         grid_sums_pair<2, 3>(partial, set, g1);
@@ -776,7 +776,7 @@ __global__ void __launch_bounds__(kCoopBlock, 1) k_pcg_pair(CoopPcgArgs ca, Pair
             __stcg(&w_new[c], uc);
             s2[1] = fp::madd(uc, rc, s2[1]);
         }
-        block_sums_pair<kCoopBlock, 2, 3>(partial, set, s2);
+        block_sums_pair<B, 2, 3>(partial, set, s2);
         if (!grid_barrier(ca.bar_count, ca.bar_abort, epoch, ca.spin_limit)) { aborted = true; break; }
         P g2[2];
         grid_sums_pair<2, 3>(partial, set, g2);
@@ -801,7 +801,7 @@ __global__ void __launch_bounds__(kCoopBlock, 1) k_pcg_pair(CoopPcgArgs ca, Pair
             w_cur[c] = wc;
             s3[0] = fp::madd(wc, __ldcg(&u0[c]), s3[0]);
         }
-        block_sums_pair<kCoopBlock, 1, 3>(partial, set, s3);
+        block_sums_pair<B, 1, 3>(partial, set, s3);
         if (!grid_barrier(ca.bar_count, ca.bar_abort, epoch, ca.spin_limit)) { aborted = true; break; }
         P g3[1];
         grid_sums_pair<1, 3>(partial, set, g3);
@@ -850,7 +850,7 @@ __global__ void __launch_bounds__(kCoopBlock, 1) k_pcg_pair(CoopPcgArgs ca, Pair
             }
             // the three sums in one set of three slots; sets alternate, so a
             // set is written again only after every block has read it
-            block_sums_pair<kCoopBlock, 3, 3>(partial, set, s4);
+            block_sums_pair<B, 3, 3>(partial, set, s4);
             if (!grid_barrier(ca.bar_count, ca.bar_abort, epoch, ca.spin_limit)) { aborted = true; break; }
             P g4[3];
             grid_sums_pair<3, 3>(partial, set, g4);
@@ -946,6 +946,7 @@ struct cfg_bidomain {
     // and their scale, the iterate and the scaled diagonal as pairs; the
     // scale follows from bounds of the largest diagonal
     bool pair = false;
+    int pair_block = 512, pair_blocks = 0;   // launch shape of the float-pair solve
     float2* d_pcoef[2] = {nullptr, nullptr};
     int pcoef_shift[2] = {0, 0};
     bool pcoef_ready[2] = {false, false};
@@ -1010,6 +1011,19 @@ PcgArgs pcg_args(cfg_bidomain* bd, const double* coef, double* x)
     return a;
 }
 
+// The float-pair solve's kernel for an ELL width and block size
+const void* pair_kernel(int width, int block)
+{
+    if (block == 448)
+        return width == 6 ? (const void*)k_pcg_pair<6, 448>
+             : width == 4 ? (const void*)k_pcg_pair<4, 448> : (const void*)k_pcg_pair<0, 448>;
+    if (block == 384)
+        return width == 6 ? (const void*)k_pcg_pair<6, 384>
+             : width == 4 ? (const void*)k_pcg_pair<4, 384> : (const void*)k_pcg_pair<0, 384>;
+    return width == 6 ? (const void*)k_pcg_pair<6> : width == 4 ? (const void*)k_pcg_pair<4>
+                                                                : (const void*)k_pcg_pair<0>;
+}
+
 // kind 0: phiE (coef_e, phiE), 1: Vm (coef_i, Vm)
 int pcg_solve(cfg_bidomain* bd, int kind, double tol, double rel, int max_iter,
               cfg_step_stats& stats)
@@ -1049,10 +1063,8 @@ int pcg_solve(cfg_bidomain* bd, int kind, double tol, double rel, int max_iter,
             PairPcgArgs pa{bd->d_pcoef[kind], shift, bd->d_px, bd->d_pdiag, bd->d_prdiag,
                            bd->d_pw};
             void* params[] = {&ca, &pa};
-            const void* fn = bd->op.width == 6 ? (const void*)k_pcg_pair<6>
-                           : bd->op.width == 4 ? (const void*)k_pcg_pair<4>
-                                               : (const void*)k_pcg_pair<0>;
-            CFG_CUDA_TRY(cudaLaunchCooperativeKernel(fn, dim3(bd->coop_blocks), dim3(kCoopBlock),
+            CFG_CUDA_TRY(cudaLaunchCooperativeKernel(pair_kernel(bd->op.width, bd->pair_block),
+                                                     dim3(bd->pair_blocks), dim3(bd->pair_block),
                                                      params, 0, s));
         } else {
             void* params[] = {&ca};
@@ -1393,6 +1405,22 @@ extern "C" int cfg_bidomain_create(const cfg_bidomain_desc* d, const cfg_mesh_de
             const long long want = (n + kCoopBlock - 1) / kCoopBlock;
             const long long cap = (long long)sms * per_sm;
             bd->coop_blocks = int(want < cap ? want : cap);
+            // the float-pair solve: the smallest block of 384, 448 or 512
+            // threads whose grid, one row per thread, fits one block per SM,
+            // so that every SM takes part in a small system
+            bd->pair_block = 512;
+            bd->pair_blocks = bd->coop_blocks;
+            for (int b : {384, 448}) {
+                const long long nb = (n + b - 1) / b;
+                int k = 0;
+                if (nb <= sms &&
+                    cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                        &k, pair_kernel(width, b), b, 0) == cudaSuccess && k >= 1) {
+                    bd->pair_block = b;
+                    bd->pair_blocks = int(nb);
+                    break;
+                }
+            }
         }
         cudaGetLastError();
     }
@@ -1400,7 +1428,8 @@ extern "C" int cfg_bidomain_create(const cfg_bidomain_desc* d, const cfg_mesh_de
         e = dmalloc(&bd->d_p_alt, size_t(n));
         if (!e) e = cudaMemset(bd->d_p_alt, 0, size_t(n) * sizeof(double));
         // two sets of up to three sums per block
-        if (!e) e = dmalloc(&bd->d_coop_partial, 6 * size_t(bd->coop_blocks));
+        if (!e) e = dmalloc(&bd->d_coop_partial,
+                            6 * size_t(std::max(bd->coop_blocks, bd->pair_blocks)));
         if (!e) e = dmalloc(&bd->d_bar, 1);
         if (!e) e = dmalloc(&bd->d_abort, 1);
     }
