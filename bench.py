@@ -10,13 +10,16 @@ dataset for this path).  A step is one runTime++/evolve over all cells.
 
 The headline `value` is the mixed-precision form's device-resident
 throughput in cell-steps/s over K steps of the wavefront window (from
-t = 10 ms, step 2000: the front inside the slab, cells in the upstroke taking
-many RKF45 substeps); the rest-state window right after the warm-up is
-reported beside it.  The FP64 plain form is timed in the same window and
-both forms are compared at its end (activation times, Vm).  `e2e` repeats the mixed run through the C ABI with Vm copied in
-from and out to pinned host memory every step.  Under torchrun every rank
-runs an independent replica on its own GPU (the step has no cross-rank
-exchange at one GPU per replica).
+t = 10 ms, step 2000: the front inside the slab, about 21,600 cells
+activated); the rest-state window right after the warm-up is reported
+beside it, with the RHS evaluations per cell-step of each window.  The FP64
+plain form is timed in the same window and both forms are compared at its
+end (activation times, Vm).  `e2e` repeats the mixed run through the C ABI
+with Vm copied in from and out to pinned host memory every step.  Under
+torchrun every rank runs an independent replica on its own GPU (the step
+has no cross-rank exchange at one GPU per replica).  `--impl reference`
+times the CPU oracle (the reference's ionic code and restated OpenFOAM
+numerics) on a bounded corner piece of the slab at the same window.
 """
 from __future__ import annotations
 
