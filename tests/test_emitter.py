@@ -57,3 +57,29 @@ def test_supplement_covers_exactly_the_unassigned_constants():
         sup = supplement_for(m)          # raises on any mismatch
         assert [c for c, _ in sup] == [c for c, _ in SUPPLEMENT.get(name, [])]
         assert (len(unassigned_constants(m)) > 0) == (name == "ORd")
+
+
+def test_reciprocal_slots_are_read_only_as_divisors():
+    """The tissue form stores cfg_hrcp(v) in the per-step slots that the
+    stage body reads only as divisors, and reads exactly those through
+    cfg_hdiv: every slot that holds a reciprocal is read nowhere else, so
+    the FP64 form (where cfg_hrcp is the identity and cfg_hdiv a division)
+    is unchanged and the mixed form multiplies by the reciprocal."""
+    import re
+    n_recip = 0
+    for name in WRAPPERS:
+        text = (ROOT / "cardiacfoam_gb300" / "csrc" / "models" / f"{name.lower()}.cuh").read_text()
+        if "rhs_tissue" not in text or "constexpr int NH = 0;" in text:
+            continue
+        hoist = text[text.index("void hoist("):text.index("R rhs_tissue(")]
+        body = text[text.index("R rhs_tissue("):]
+        body = body[:body.index("\n}\n")]
+        stored = set(re.findall(r"H\[([^\]]+)\] = cfg_hrcp\(", hoist))
+        divisors = set(re.findall(r"cfg_hdiv\([^;]*?, H\(([^)]+)\)\)", body))
+        assert stored == divisors, name
+        reads = re.findall(r"H\(([^)]+)\)", body)
+        div_reads = len(re.findall(r"cfg_hdiv\(", body))
+        other = [r for r in reads if r in stored]
+        assert len(other) == div_reads, name     # every read of such a slot is a divisor
+        n_recip += len(stored)
+    assert n_recip > 0
