@@ -269,7 +269,8 @@ static cudaError_t alloc_pairs(cfg_monodomain* md)
     cudaError_t e = dmalloc(&md->d_pdiag2, 2 * n);
     if (!e) e = dmalloc(&md->d_prdiag2, 2 * n);
     if (!e) e = dmalloc(&md->d_psumA2, 2 * n);
-    if (!e) e = dmalloc(&md->d_pcoef, size_t(md->width > 0 ? md->width : 1) * n);
+    // the stencil form keeps its three coefficients in the launch arguments
+    if (!e && !md->use_stencil) e = dmalloc(&md->d_pcoef, size_t(md->width > 0 ? md->width : 1) * n);
     if (!e) e = dmalloc(&md->d_px, n);
     return e;
 }
