@@ -51,7 +51,7 @@ DT = 5e-6
 # from an ncu capture of the current kernel (dram__bytes_read.sum +
 # dram__bytes_write.sum); ncu cannot run inside the timed region, so the
 # figure is carried here and refreshed with each capture.
-IONIC_TRAFFIC_BYTES = 120.3e6
+IONIC_TRAFFIC_BYTES = 120.6e6
 IONIC_TRAFFIC_SOURCE = "profiles/ionic_mixed_kernel_ord_420k.md"
 # states read and written (31 FP32 + 10 FP32 hi/lo pairs = 204 B) + Vm in + Iion out
 IONIC_STATE_BYTES = 2 * 204 + 16
