@@ -562,6 +562,224 @@ void oracle_mesh_centres(const oracle_mesh* m, double* c)
 }
 
 /* ------------------------------------------------------------------------ */
+/* Cell centres of one uniformly graded blockMesh block with every rounding  */
+/* of OpenFOAM's own geometry (v2312 published algorithms, restated):        */
+/*  - blockMesh's block point interpolation (block::createPoints): each      */
+/*    point is a third of the sum over the 12 straight edges of edge point x  */
+/*    edge weight, the 4 weights per direction normalised by their sum;      */
+/*    lineDivide's uniform lambdas i/n; the scale applied at the end;        */
+/*  - primitiveMeshTools::makeFaceCentresAndAreas: the triangle fan about    */
+/*    the face's point average;                                             */
+/*  - primitiveMeshTools::makeCellCentresAndVols: face-pyramid centroids     */
+/*    weighted by 3 x pyramid volume, about the average of the face centres; */
+/*  - polyMesh from cell shapes: internal faces upper-triangular (per owner  */
+/*    +x, +y, +z, as the owner's hex faces (1 2 6 5), (3 7 6 2), (4 5 6 7)),  */
+/*    then the boundary faces in the patch's block-face order.              */
+/* The sums over a cell's faces run in face order: its owned faces, then the */
+/* faces it neighbours.  A cell centre that lies exactly on a plane of the   */
+/* grid comes out a few units in the last place either side of it, and an    */
+/* inclusive box test (stimulus boxes) on such a plane takes part of the     */
+/* layer.  `contract` selects which expressions a compiler fuses into fma    */
+/* (clang's -ffp-contract=on on an FMA target): bit 1 the blockMesh weights, */
+/* bit 2 cross products, bit 4 dot products, bit 8 squared magnitudes.       */
+/* extent = the block's far vertex before scaling (the near one is 0);       */
+/* patch_order = the 6 block faces (0 x-min, 1 x-max, 2 y-min, 3 y-max,      */
+/* 4 z-min, 5 z-max) in the order the boundary patch lists them.  Centres    */
+/* out: 3 per cell, x fastest. Test infrastructure.                          */
+
+typedef struct { double x, y, z; } bm_v;
+
+static bm_v bm_add(bm_v a, bm_v b) { bm_v r = {a.x + b.x, a.y + b.y, a.z + b.z}; return r; }
+static bm_v bm_sub(bm_v a, bm_v b) { bm_v r = {a.x - b.x, a.y - b.y, a.z - b.z}; return r; }
+static bm_v bm_scale(double s, bm_v a) { bm_v r = {s * a.x, s * a.y, s * a.z}; return r; }
+static bm_v bm_div(bm_v a, double s) { bm_v r = {a.x / s, a.y / s, a.z / s}; return r; }
+
+/* a*b - c*d as one expression */
+static double bm_msub(double a, double b, double c, double d, int fuse)
+{
+    return fuse ? fma(a, b, -(c * d)) : a * b - c * d;
+}
+
+static double bm_dot(bm_v a, bm_v b, int fuse)
+{
+    return fuse ? fma(a.z, b.z, fma(a.x, b.x, a.y * b.y)) : a.x * b.x + a.y * b.y + a.z * b.z;
+}
+
+static bm_v bm_cross(bm_v a, bm_v b, int fuse)
+{
+    bm_v r = {bm_msub(a.y, b.z, a.z, b.y, fuse), bm_msub(a.z, b.x, a.x, b.z, fuse),
+              bm_msub(a.x, b.y, a.y, b.x, fuse)};
+    return r;
+}
+
+/* edge weight (1-a)(1-b)(1-c) + a(1-d)(1-e) style: p*q*r + s*t*u */
+static double bm_w(double p, double q, double r, double s, double t, double u, int fuse)
+{
+    return fuse ? fma(p * q, r, s * t * u) : p * q * r + s * t * u;
+}
+
+static void bm_face(const bm_v* q, int contract, bm_v* centre, bm_v* area)
+{
+    bm_v avg = q[0];
+    for (int t = 1; t < 4; t++) avg = bm_add(avg, q[t]);
+    avg = bm_div(avg, 4.0);
+    bm_v sum_n = {0, 0, 0}, sum_ac = {0, 0, 0};
+    double sum_a = 0.0;
+    for (int t = 0; t < 4; t++) {
+        const bm_v a = q[t], b = q[(t + 1) % 4];
+        const bm_v c = bm_add(bm_add(a, b), avg);
+        const bm_v n = bm_cross(bm_sub(b, a), bm_sub(avg, a), contract & 2);
+        const double mag = sqrt(bm_dot(n, n, contract & 8));
+        sum_n = bm_add(sum_n, n);
+        sum_a += mag;
+        sum_ac = bm_add(sum_ac, bm_scale(mag, c));
+    }
+    *centre = bm_div(bm_scale(1.0 / 3.0, sum_ac), sum_a);
+    *area = bm_scale(0.5, sum_n);
+}
+
+int oracle_blockmesh_centres(int ni, int nj, int nk, const double* extent, double scale,
+                             const int* patch_order, int contract, double* centres)
+{
+    if (ni < 1 || nj < 1 || nk < 1) return -1;
+    for (int r = 0; r < 6; r++)
+        if (patch_order[r] < 0 || patch_order[r] > 5) return -1;
+    const long pi_ = ni + 1, pj_ = nj + 1;
+    const long np = pi_ * pj_ * (nk + 1);
+    bm_v* pts = (bm_v*)malloc(sizeof(bm_v) * (size_t)np);
+    if (!pts) return -1;
+    const double X = extent[0], Y = extent[1], Z = extent[2];
+    /* block vertices in hex order; edges x1..x4, y1..y4, z1..z4 */
+    const bm_v v000 = {0, 0, 0}, v100 = {X, 0, 0}, v110 = {X, Y, 0}, v010 = {0, Y, 0};
+    const bm_v v001 = {0, 0, Z}, v101 = {X, 0, Z}, v111 = {X, Y, Z}, v011 = {0, Y, Z};
+    const int fw = contract & 1;
+    for (int k = 0; k <= nk; k++)
+        for (int j = 0; j <= nj; j++)
+            for (int i = 0; i <= ni; i++) {
+                bm_v p;
+                if ((i == 0 || i == ni) && (j == 0 || j == nj) && (k == 0 || k == nk)) {
+                    p.x = i ? X : 0.0; p.y = j ? Y : 0.0; p.z = k ? Z : 0.0;
+                } else {
+                    const double a = 0.0 + 1.0 * (double)i / ni;
+                    const double b = 0.0 + 1.0 * (double)j / nj;
+                    const double c = 0.0 + 1.0 * (double)k / nk;
+                    double wx[4] = {bm_w(1 - a, 1 - b, 1 - c, a, 1 - b, 1 - c, fw),
+                                    bm_w(1 - a, b, 1 - c, a, b, 1 - c, fw),
+                                    bm_w(1 - a, b, c, a, b, c, fw),
+                                    bm_w(1 - a, 1 - b, c, a, 1 - b, c, fw)};
+                    double wy[4] = {bm_w(1 - b, 1 - a, 1 - c, b, 1 - a, 1 - c, fw),
+                                    bm_w(1 - b, a, 1 - c, b, a, 1 - c, fw),
+                                    bm_w(1 - b, a, c, b, a, c, fw),
+                                    bm_w(1 - b, 1 - a, c, b, 1 - a, c, fw)};
+                    double wz[4] = {bm_w(1 - c, 1 - a, 1 - b, c, 1 - a, 1 - b, fw),
+                                    bm_w(1 - c, a, 1 - b, c, a, 1 - b, fw),
+                                    bm_w(1 - c, a, b, c, a, b, fw),
+                                    bm_w(1 - c, 1 - a, b, c, 1 - a, b, fw)};
+                    double* ws[3] = {wx, wy, wz};
+                    for (int d = 0; d < 3; d++) {
+                        const double s = ws[d][0] + ws[d][1] + ws[d][2] + ws[d][3];
+                        for (int e = 0; e < 4; e++) ws[d][e] /= s;
+                    }
+                    const bm_v e[12] = {
+                        bm_add(v000, bm_scale(a, bm_sub(v100, v000))),
+                        bm_add(v010, bm_scale(a, bm_sub(v110, v010))),
+                        bm_add(v011, bm_scale(a, bm_sub(v111, v011))),
+                        bm_add(v001, bm_scale(a, bm_sub(v101, v001))),
+                        bm_add(v000, bm_scale(b, bm_sub(v010, v000))),
+                        bm_add(v100, bm_scale(b, bm_sub(v110, v100))),
+                        bm_add(v101, bm_scale(b, bm_sub(v111, v101))),
+                        bm_add(v001, bm_scale(b, bm_sub(v011, v001))),
+                        bm_add(v000, bm_scale(c, bm_sub(v001, v000))),
+                        bm_add(v100, bm_scale(c, bm_sub(v101, v100))),
+                        bm_add(v110, bm_scale(c, bm_sub(v111, v110))),
+                        bm_add(v010, bm_scale(c, bm_sub(v011, v010)))};
+                    bm_v s = bm_scale(wx[0], e[0]);
+                    for (int m = 1; m < 12; m++) s = bm_add(s, bm_scale(ws[m / 4][m % 4], e[m]));
+                    p = bm_div(s, 3.0);
+                }
+                pts[i + pi_ * (j + pj_ * (long)k)] = bm_scale(scale, p);
+            }
+#define BM_P(i, j, k) pts[(i) + pi_ * ((j) + pj_ * (long)(k))]
+    for (int k = 0; k < nk; k++)
+        for (int j = 0; j < nj; j++)
+            for (int i = 0; i < ni; i++) {
+                /* the cell's 6 faces in face order, with the side they are
+                 * owned from: owned internal (+x +y +z), boundary (patch
+                 * order), then neighboured internal (-z -y -x) */
+                bm_v q[6][4];
+                int owned[6], nfc = 0;
+#define BM_FACE(own_, a0, a1, a2, a3)                                      \
+    do {                                                                   \
+        q[nfc][0] = a0; q[nfc][1] = a1; q[nfc][2] = a2; q[nfc][3] = a3;    \
+        owned[nfc++] = own_;                                               \
+    } while (0)
+                if (i + 1 < ni)
+                    BM_FACE(1, BM_P(i + 1, j, k), BM_P(i + 1, j + 1, k), BM_P(i + 1, j + 1, k + 1),
+                            BM_P(i + 1, j, k + 1));
+                if (j + 1 < nj)
+                    BM_FACE(1, BM_P(i, j + 1, k), BM_P(i, j + 1, k + 1), BM_P(i + 1, j + 1, k + 1),
+                            BM_P(i + 1, j + 1, k));
+                if (k + 1 < nk)
+                    BM_FACE(1, BM_P(i, j, k + 1), BM_P(i + 1, j, k + 1), BM_P(i + 1, j + 1, k + 1),
+                            BM_P(i, j + 1, k + 1));
+                for (int r = 0; r < 6; r++) {
+                    const int bf = patch_order[r];
+                    if (bf == 0 && i == 0)
+                        BM_FACE(1, BM_P(0, j, k), BM_P(0, j, k + 1), BM_P(0, j + 1, k + 1),
+                                BM_P(0, j + 1, k));
+                    if (bf == 1 && i == ni - 1)
+                        BM_FACE(1, BM_P(ni, j, k), BM_P(ni, j + 1, k), BM_P(ni, j + 1, k + 1),
+                                BM_P(ni, j, k + 1));
+                    if (bf == 2 && j == 0)
+                        BM_FACE(1, BM_P(i, 0, k), BM_P(i + 1, 0, k), BM_P(i + 1, 0, k + 1),
+                                BM_P(i, 0, k + 1));
+                    if (bf == 3 && j == nj - 1)
+                        BM_FACE(1, BM_P(i, nj, k), BM_P(i, nj, k + 1), BM_P(i + 1, nj, k + 1),
+                                BM_P(i + 1, nj, k));
+                    if (bf == 4 && k == 0)
+                        BM_FACE(1, BM_P(i, j, 0), BM_P(i, j + 1, 0), BM_P(i + 1, j + 1, 0),
+                                BM_P(i + 1, j, 0));
+                    if (bf == 5 && k == nk - 1)
+                        BM_FACE(1, BM_P(i, j, nk), BM_P(i + 1, j, nk), BM_P(i + 1, j + 1, nk),
+                                BM_P(i, j + 1, nk));
+                }
+                /* internal faces the cell neighbours, as their owners hold them */
+                if (k > 0)
+                    BM_FACE(0, BM_P(i, j, k), BM_P(i + 1, j, k), BM_P(i + 1, j + 1, k),
+                            BM_P(i, j + 1, k));
+                if (j > 0)
+                    BM_FACE(0, BM_P(i, j, k), BM_P(i, j, k + 1), BM_P(i + 1, j, k + 1),
+                            BM_P(i + 1, j, k));
+                if (i > 0)
+                    BM_FACE(0, BM_P(i, j, k), BM_P(i, j + 1, k), BM_P(i, j + 1, k + 1),
+                            BM_P(i, j, k + 1));
+#undef BM_FACE
+                bm_v fc[6], fa[6];
+                bm_v est = {0, 0, 0};
+                for (int f = 0; f < nfc; f++) {
+                    bm_face(q[f], contract, &fc[f], &fa[f]);
+                    est = bm_add(est, fc[f]);
+                }
+                est = bm_div(est, (double)nfc);
+                bm_v sum_c = {0, 0, 0};
+                double sum_v = 0.0;
+                for (int f = 0; f < nfc; f++) {
+                    const double pv = owned[f] ? bm_dot(fa[f], bm_sub(fc[f], est), contract & 4)
+                                               : bm_dot(fa[f], bm_sub(est, fc[f]), contract & 4);
+                    const bm_v pc = bm_add(bm_scale(3.0 / 4.0, fc[f]), bm_scale(1.0 / 4.0, est));
+                    sum_c = bm_add(sum_c, bm_scale(pv, pc));
+                    sum_v += pv;
+                }
+                const bm_v cc = bm_div(sum_c, sum_v);
+                double* out = centres + 3 * ((size_t)i + (size_t)ni * ((size_t)j + (size_t)nj * k));
+                out[0] = cc.x; out[1] = cc.y; out[2] = cc.z;
+            }
+#undef BM_P
+    free(pts);
+    return 0;
+}
+
+/* ------------------------------------------------------------------------ */
 /* monodomain tissue                                                        */
 
 #define MAX_SOLVES 64

@@ -85,6 +85,14 @@ long oracle_mesh_ncells(const oracle_mesh*);
 long oracle_mesh_nfaces(const oracle_mesh*);
 void oracle_mesh_addressing(const oracle_mesh*, int* owner, int* neighbour);
 void oracle_mesh_centres(const oracle_mesh*, double* c);
+/* Cell centres of one uniformly graded blockMesh block as OpenFOAM's
+ * geometry code rounds them (block point interpolation, face and cell
+ * centres in polyMesh face order); contract: fma fusion bits (1 blockMesh
+ * weights, 2 cross, 4 dot, 8 magSqr); extent: far block vertex before
+ * `scale`; patch_order: block faces 0..5 (x-min x-max y-min y-max z-min
+ * z-max) in the boundary patch's order.  0 on success. */
+int oracle_blockmesh_centres(int ni, int nj, int nk, const double* extent, double scale,
+                             const int* patch_order, int contract, double* centres);
 /* --- general mesh: lduAddressing plus the geometry of fvMesh ----------- */
 oracle_mesh* oracle_mesh_general(long n, long nf, const int* owner, const int* neigh,
                                  const double* centres, const double* vol,

@@ -90,6 +90,8 @@ def lib():
         L.oracle_mesh_general.argtypes = [C.c_long, C.c_long, _ip, _ip, _dp, _dp, _dp, _dp,
                                           C.c_long, _ip, _dp, _dp]
         L.oracle_mesh_general.restype = C.c_void_p
+        L.oracle_blockmesh_centres.argtypes = [C.c_int, C.c_int, C.c_int, _dp, C.c_double, _ip,
+                                               C.c_int, _dp]
         L.oracle_tissue_set_conductivity.argtypes = [C.c_void_p, _dp]
         L.oracle_tissue_set_cell_tissue.argtypes = [C.c_void_p, C.POINTER(C.c_ubyte)]
         L.oracle_tissue_laplacian.argtypes = [C.c_void_p, _dp, _dp]
@@ -245,6 +247,28 @@ class Ionic:
         if getattr(self, "h", None):
             lib().oracle_ionic_free(self.h)
             self.h = None
+
+
+BLOCK_FACES = ("x-min", "x-max", "y-min", "y-max", "z-min", "z-max")
+
+
+def blockmesh_centres(ni, nj, nk, extent, scale, patch_order, contract=0) -> np.ndarray:
+    """Cell centres [ni*nj*nk, 3] (x fastest) of one uniformly graded
+    blockMesh block, rounded as OpenFOAM's geometry code rounds them.
+    extent: the far block vertex before `scale` (the near one is the origin);
+    patch_order: the block faces (names of BLOCK_FACES) in the order the
+    boundary patch lists them; contract: which expressions are fused into fma
+    (bits 1 blockMesh weights, 2 cross products, 4 dot products, 8 squared
+    magnitudes), as a compiler that contracts within expressions builds it."""
+    out = np.zeros((ni * nj * nk, 3))
+    ext = np.ascontiguousarray(extent, dtype=np.float64)
+    order = np.array([BLOCK_FACES.index(f) for f in patch_order], dtype=np.int32)
+    if sorted(order.tolist()) != list(range(6)):
+        raise ValueError("patch_order must name each block face once")
+    if lib().oracle_blockmesh_centres(ni, nj, nk, ptr(ext), scale, iptr(order), contract,
+                                      ptr(out)) != 0:
+        raise ValueError("invalid block")
+    return out
 
 
 class Mesh:

@@ -253,6 +253,34 @@ def test_explicit_delta_t_rule_on_the_niederer_slab(gpu_lib):
 
 
 @pytest.mark.gpu
+def test_niederer_regression_probes_on_openfoam_centres(gpu_lib, oracle):
+    """The reference's NiedererEtAl2012 regression case through the
+    dictionary front end, on the cell centres OpenFOAM computes for its
+    blockMesh (which decide the stimulated set: the box's inner faces pass
+    through cell centres): the six probes within the reference's own
+    tolerances (NiedererEtAl2012.reference:8-13), and every activation time
+    within 1e-9 s of the oracle on the same mesh and time step."""
+    import niederer_case as nc
+    mesh = nc.openfoam_mesh(oracle, 0)
+    m = api.Monodomain.from_dict(NIEDERER_DICT, mesh, 5e-5)
+    dt = m.delta_t()
+    assert abs(dt - nc.explicit_dt()) <= 1e-12 * dt
+    d = oracle.tissue_desc("BuenoOrovio", 1, nc.SIGMA, implicit=False, ddt_backward=True,
+                           boxes=[(*nc.BOX, *nc.STIMULUS)])
+    o = oracle.Tissue(d, oracle.Mesh.general(mesh))
+    while m.time() < nc.END_TIME - 1e-12:
+        m.step(0.0)
+        o.step(dt, 8)
+    ag, ao = m.activation(), o.activation()
+    assert np.array_equal(ag > 0, ao > 0)
+    assert np.max(np.abs(ag - ao)) < 1e-9
+    for probe, expect, tol in nc.pins():
+        got = ag[nc.probe_cell(nc.PROBES[probe])]
+        assert abs(got - expect) <= tol, (probe, got, expect)
+    m.close()
+
+
+@pytest.mark.gpu
 def test_tissue_apd_tracking_equals_trace_postprocessing(gpu_lib):
     """Per-cell beat detection on the tissue's Vm (cfg_monodomain_track_apd)
     over a full beat of a TNNP slab, sampled every 0.1 ms: the device's
