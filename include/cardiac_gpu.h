@@ -318,9 +318,10 @@ int cfg_monodomain_set_persistent(cfg_monodomain* md, int enable);
  * lduMatrix PCG with its normFactor and convergence test) in FP64, or in
  * float pairs, the default of CFG_PRECISION_MIXED contexts on meshes whose
  * Laplacian needs no explicit correction (GB300 issues FP64 at 1/64 of the
- * FP32 rate; on corrected meshes the solve streams from HBM and keeps FP64).  The source of each corrector is formed in
- * FP64 either way.  The kernel sequence (cfg_monodomain_set_persistent(md,
- * 0)) always runs FP64. */
+ * FP32 rate; on corrected meshes the solve streams from HBM and keeps
+ * FP64).  The source of each corrector is formed in FP64 either way.  The
+ * kernel sequence (cfg_monodomain_set_persistent(md, 0)) always runs FP64;
+ * the explicit algorithm has no solve. */
 int cfg_monodomain_set_pcg_arithmetic(cfg_monodomain* md, int arithmetic);
 /* Per-cell beat detection on the tissue's Vm: after every `every_steps`-th
  * step (and once at the call, the field as it is) each cell's Vm [mV] and
