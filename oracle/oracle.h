@@ -19,7 +19,10 @@
  * Parity status: the ionic right-hand sides are pinned bit-for-bit against
  * the reference's own generated headers (golden vectors under tests/golden);
  * RKF45 is pinned by the reference's single-cell regression values; the
- * implicit PCG path has no reference test and is "parity unpinned"; so is
+ * explicit tissue step by the NiedererEtAl2012 regression probes (all six
+ * within the reference's tolerances on OpenFOAM's rounding of the case's
+ * cell centres, oracle_blockmesh_centres); the implicit PCG path has no
+ * reference test and is "parity unpinned"; so is
  * the corrected Laplacian on general meshes, restated from OpenFOAM v2312's
  * finiteVolume library (absent from the reference tree).
  */
